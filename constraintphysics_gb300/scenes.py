@@ -1,0 +1,202 @@
+"""Seeded synthetic scenes for the contact-path workloads.
+
+The reference ships no benchmark scenes beyond its profiling demo
+(Demo/src/Demos/PerformanceProfilingScenes.h:218-262: a fixed 500x2x500 base
+plate, sleeping disabled, dt 1/60, bodies created through createRigidBody).
+These generators build the same kind of scenes with seeded numpy RNGs; a scene
+is a list of operations that `apply()` replays on any World (device path or
+oracle), so every backend receives bit-identical inputs.
+
+Workloads:
+  hull_drop      1,000 convex hulls (8-32 random points on the unit sphere,
+                 scale U[0.5,1.5] m, density 1000) on a 10x10x10 grid with 0.1 m
+                 jitter and random orientations, dropped on the static plate;
+                 friction 0.5, restitution 0, dt 1/60, 10 PGS iterations, one
+                 substep.
+  batched_world  one world of the 4,096-world batch: floor(exp(U[ln 8, ln 512]))
+                 bodies, either a box pyramid (base 4-16) or a hull pile built as
+                 in hull_drop, each world with its own plate.
+"""
+import math
+
+import numpy as np
+
+DYNAMIC, FIXED, KINEMATIC = 0, 1, 2
+
+PILE_MATERIAL = {"density": 1000.0, "restitution": 0.0, "kinetic_friction": 0.5, "static_friction": 0.5}
+
+# engine settings shared by the hull_drop and batched workloads
+DROP_PARAMS = dict(step_time=1.0 / 60.0, substeps=1, pgs=(10, 1, 1), sleeping=False)
+
+
+def unit_sphere_points(rng, n):
+    g = rng.normal(size=(n, 3))
+    return g / np.linalg.norm(g, axis=1, keepdims=True)
+
+
+def convex_hull(points):
+    """Vertices and triangular faces of the convex hull of `points`."""
+    from scipy.spatial import ConvexHull
+    h = ConvexHull(points)
+    verts = np.asarray(h.vertices)
+    remap = -np.ones(len(points), dtype=np.int64)
+    remap[verts] = np.arange(len(verts))
+    faces = [[int(remap[i]) for i in s] for s in h.simplices]
+    return np.ascontiguousarray(points[verts]), faces
+
+
+def random_quat(rng):
+    q = rng.normal(size=4)
+    return q / np.linalg.norm(q)
+
+
+def random_hull(rng, nmin=8, nmax=32):
+    n = int(rng.integers(nmin, nmax + 1))
+    pts = unit_sphere_points(rng, n) * rng.uniform(0.5, 1.5)
+    return convex_hull(pts)
+
+
+class Scene:
+    """Replayable list of world-building operations."""
+
+    def __init__(self, name, params):
+        self.name = name
+        self.params = dict(params)
+        self.ops = []
+        self.n_bodies = 0
+
+    def _body(self, op):
+        self.ops.append(op)
+        self.n_bodies += 1
+        return self.n_bodies  # ids start at 1
+
+    def hull(self, points, faces, material, movement, pos):
+        return self._body(("hull", points, faces, material, movement, tuple(pos)))
+
+    def box(self, corner, dx, dy, dz, material, movement, pos=(0, 0, 0)):
+        return self._body(("box", tuple(corner), dx, dy, dz, material, movement, tuple(pos)))
+
+    def sphere(self, center, r, material, movement, pos=(0, 0, 0)):
+        return self._body(("sphere", tuple(center), r, material, movement, tuple(pos)))
+
+    def cylinder(self, base, r, h, material, movement, pos=(0, 0, 0)):
+        return self._body(("cylinder", tuple(base), r, h, material, movement, tuple(pos)))
+
+    def orient(self, bid, q):
+        self.ops.append(("orient", bid, tuple(q)))
+
+    def velocity(self, bid, v):
+        self.ops.append(("vel", bid, tuple(v)))
+
+
+def apply(scene, world):
+    """Replay `scene` on a World; returns the list of created body ids."""
+    world.set_params(**scene.params)
+    ids = []
+    for op in scene.ops:
+        kind = op[0]
+        if kind == "hull":
+            ids.append(world.add_hull(op[1], op[2], op[3], op[4], op[5]))
+        elif kind == "box":
+            ids.append(world.add_box(op[1], op[2], op[3], op[4], op[5], op[6], op[7]))
+        elif kind == "sphere":
+            ids.append(world.add_sphere(op[1], op[2], op[3], op[4], op[5]))
+        elif kind == "cylinder":
+            ids.append(world.add_cylinder(op[1], op[2], op[3], op[4], op[5], op[6]))
+        elif kind == "orient":
+            world.set_orientation(op[1], op[2])
+        elif kind == "vel":
+            world.set_velocity(op[1], op[2])
+        else:
+            raise ValueError(kind)
+    return ids
+
+
+def _plate(scene, material=PILE_MATERIAL):
+    # PerformanceProfilingScenes.h:233-237: box((-s/2, -2, -s/2), s, 2, s), FIXED
+    s = 500.0
+    return scene.box((-s / 2, -2.0, -s / 2), s, 2.0, s, material, FIXED)
+
+
+def hull_drop(seed=0, n_side=10, spacing=3.2, jitter=0.1, base_y=2.0):
+    """1,000 random hulls (n_side^3) dropped on the static plate."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(f"hull_drop_{n_side}^3_seed{seed}", DROP_PARAMS)
+    _plate(sc)
+    off = (n_side - 1) * spacing / 2.0
+    for i in range(n_side):
+        for j in range(n_side):
+            for k in range(n_side):
+                pts, faces = random_hull(rng)
+                pos = np.array([i * spacing - off, base_y + j * spacing, k * spacing - off])
+                pos += rng.uniform(-jitter, jitter, size=3)
+                bid = sc.hull(pts, faces, PILE_MATERIAL, DYNAMIC, pos)
+                sc.orient(bid, random_quat(rng))
+    return sc
+
+
+class HullPool:
+    """A pool of unit-scale random hulls reused (with a per-body scale) by the
+    batched workload, so that generating 10^5 hulls does not need 10^5 Qhull
+    runs."""
+
+    def __init__(self, seed, size=512, nmin=8, nmax=32):
+        rng = np.random.default_rng(seed + 7919)
+        self.shapes = []
+        for _ in range(size):
+            n = int(rng.integers(nmin, nmax + 1))
+            self.shapes.append(convex_hull(unit_sphere_points(rng, n)))
+
+    def draw(self, rng):
+        pts, faces = self.shapes[int(rng.integers(len(self.shapes)))]
+        return pts * rng.uniform(0.5, 1.5), faces
+
+
+def batched_world(rng, pool, nmin=8, nmax=512, gap=0.05):
+    """One world of the batched workload (log-uniform body count)."""
+    n = int(math.floor(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+    kind = "pyramid" if rng.random() < 0.5 else "pile"
+    sc = Scene(f"{kind}_{n}", DROP_PARAMS)
+    _plate(sc)
+    if kind == "pyramid":
+        base = int(rng.integers(4, 17))
+        pitch = 1.0 + gap
+        placed, pyr = 0, 0
+        while placed < n:  # extra pyramids go beside the first when n exceeds one
+            shift = pyr * (base * pitch + 4.0)
+            for layer in range(base):
+                side = base - layer
+                off = (side - 1) * pitch / 2.0
+                for x in range(side):
+                    for z in range(side):
+                        if placed >= n:
+                            break
+                        corner = (x * pitch - off + shift, layer * 1.01 + 0.005, z * pitch - off)
+                        sc.box((0.0, 0.0, 0.0), 1.0, 1.0, 1.0, PILE_MATERIAL, DYNAMIC, corner)
+                        placed += 1
+            pyr += 1
+    else:
+        side = max(1, int(math.ceil(n ** (1.0 / 3.0))))
+        spacing = 3.2
+        off = (side - 1) * spacing / 2.0
+        placed = 0
+        j = 0
+        while placed < n:
+            for i in range(side):
+                for k in range(side):
+                    if placed >= n:
+                        break
+                    pts, faces = pool.draw(rng)
+                    pos = np.array([i * spacing - off, 2.0 + j * spacing, k * spacing - off])
+                    pos += rng.uniform(-0.1, 0.1, size=3)
+                    bid = sc.hull(pts, faces, PILE_MATERIAL, DYNAMIC, pos)
+                    sc.orient(bid, random_quat(rng))
+                    placed += 1
+            j += 1
+    return sc
+
+
+def batched_worlds(seed=0, n_worlds=4096, nmin=8, nmax=512):
+    rng = np.random.default_rng(seed)
+    pool = HullPool(seed)
+    return [batched_world(rng, pool, nmin, nmax) for _ in range(n_worlds)]

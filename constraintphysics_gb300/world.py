@@ -1,0 +1,241 @@
+"""Python handle over one world of any library exporting the cpgpu C ABI.
+
+The product library (libcpgpu.so) and the oracle libraries export the same
+function set (include/cpgpu.h), so this one class drives all of them; tests use
+it to run identical scenes through the device path and the oracles.
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._abi import Contact, Material
+
+
+class CPGPUError(RuntimeError):
+    pass
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f64(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+class World:
+    """One PhysicsEngine instance behind a cpgpu-style C ABI."""
+
+    def __init__(self, abi):
+        self.abi = abi
+        h = C.c_void_p()
+        self._check(abi.world_create(C.byref(h)))
+        self.h = h
+        self.n_bodies = 0
+
+    # -- error handling ----------------------------------------------------
+    def _check(self, rc):
+        if rc != 0:
+            msg = self.abi.last_error() if hasattr(self.abi, "last_error") else b""
+            raise CPGPUError(f"status {rc}: {msg.decode(errors='replace') if msg else ''}")
+        return rc
+
+    def close(self):
+        if self.h is not None and self.h.value:
+            self.abi.world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- parameters (PhysicsEngine setters) -----------------------------------
+    def set_params(self, step_time=None, gravity=None, substeps=None, pgs=None,
+                   sleeping=None, warm_start_disabled=None, cfm=None,
+                   angle_vel_ticks=None, gyro_disabled=None):
+        a, h = self.abi, self.h
+        if step_time is not None:
+            self._check(a.set_step_time(h, float(step_time)))
+        if gravity is not None:
+            self._check(a.set_gravity(h, *map(float, gravity)))
+        if substeps is not None:
+            self._check(a.set_substep_count(h, int(substeps)))
+        if pgs is not None:
+            self._check(a.set_pgs_iterations(h, *map(int, pgs)))
+        if sleeping is not None:
+            self._check(a.set_sleeping_enabled(h, int(bool(sleeping))))
+        if warm_start_disabled is not None:
+            self._check(a.set_warm_start_disabled(h, int(bool(warm_start_disabled))))
+        if cfm is not None:
+            self._check(a.set_global_cfm(h, float(cfm)))
+        if angle_vel_ticks is not None:
+            self._check(a.set_angle_vel_update_tick_count(h, int(angle_vel_ticks)))
+        if gyro_disabled is not None:
+            self._check(a.set_internal_gyro_forces_disabled(h, int(bool(gyro_disabled))))
+
+    # -- bodies -----------------------------------------------------------------
+    @staticmethod
+    def _mat(m):
+        m = m or {}
+        return Material(m.get("density", 1.0), m.get("restitution", 0.3),
+                        m.get("kinetic_friction", 0.6), m.get("static_friction", 1.1))
+
+    def _new_id(self, rc, out):
+        self._check(rc)
+        self.n_bodies += 1
+        return out.value
+
+    def add_hull(self, points, faces, material=None, movement=0, pos=(0, 0, 0)):
+        pts = _f64(points)
+        offs = np.zeros(len(faces) + 1, dtype=np.int32)
+        offs[1:] = np.cumsum([len(f) for f in faces])
+        idx = np.ascontiguousarray(np.concatenate([np.asarray(f, dtype=np.int32) for f in faces]))
+        pos = _f64(pos, 3)
+        mat = self._mat(material)
+        out = C.c_uint32()
+        rc = self.abi.body_hull(self.h, _ptr(pts), pts.size // 3, _ptr(offs), _ptr(idx), len(faces),
+                                C.addressof(mat), int(movement), _ptr(pos), C.addressof(out))
+        return self._new_id(rc, out)
+
+    def add_box(self, corner, dx, dy, dz, material=None, movement=0, pos=(0, 0, 0)):
+        corner = _f64(corner, 3)
+        pos = _f64(pos, 3)
+        mat = self._mat(material)
+        out = C.c_uint32()
+        rc = self.abi.body_box(self.h, _ptr(corner), float(dx), float(dy), float(dz),
+                               C.addressof(mat), int(movement), _ptr(pos), C.addressof(out))
+        return self._new_id(rc, out)
+
+    def add_sphere(self, center, radius, material=None, movement=0, pos=(0, 0, 0)):
+        center = _f64(center, 3)
+        pos = _f64(pos, 3)
+        mat = self._mat(material)
+        out = C.c_uint32()
+        rc = self.abi.body_sphere(self.h, _ptr(center), float(radius), C.addressof(mat), int(movement),
+                                  _ptr(pos), C.addressof(out))
+        return self._new_id(rc, out)
+
+    def add_cylinder(self, base, radius, height, material=None, movement=0, pos=(0, 0, 0)):
+        base = _f64(base, 3)
+        pos = _f64(pos, 3)
+        mat = self._mat(material)
+        out = C.c_uint32()
+        rc = self.abi.body_cylinder(self.h, _ptr(base), float(radius), float(height), C.addressof(mat),
+                                    int(movement), _ptr(pos), C.addressof(out))
+        return self._new_id(rc, out)
+
+    def add_mesh(self, points, tris, material=None, fixed=True):
+        pts = _f64(points)
+        tr = np.ascontiguousarray(tris, dtype=np.int32)
+        mat = self._mat(material)
+        out = C.c_uint32()
+        rc = self.abi.body_mesh(self.h, _ptr(pts), pts.size // 3, _ptr(tr), tr.size // 3,
+                                C.addressof(mat), int(bool(fixed)), C.addressof(out))
+        return self._new_id(rc, out)
+
+    def set_velocity(self, bid, v):
+        v = _f64(v, 3)
+        self._check(self.abi.body_set_velocity(self.h, int(bid), _ptr(v)))
+
+    def set_ang_velocity(self, bid, v):
+        v = _f64(v, 3)
+        self._check(self.abi.body_set_ang_velocity(self.h, int(bid), _ptr(v)))
+
+    def set_orientation(self, bid, q):
+        q = _f64(q, 4)
+        self._check(self.abi.body_set_orientation(self.h, int(bid), _ptr(q)))
+
+    def set_position(self, bid, p):
+        p = _f64(p, 3)
+        self._check(self.abi.body_set_position(self.h, int(bid), _ptr(p)))
+
+    def set_mass(self, bid, m):
+        self._check(self.abi.body_set_mass(self.h, int(bid), float(m)))
+
+    def add_ball_socket(self, b1, b2, a1, a2, strength=15000.0):
+        a1, a2 = _f64(a1, 3), _f64(a2, 3)
+        out = C.c_uint32()
+        self._check(self.abi.add_ball_socket(self.h, int(b1), int(b2), _ptr(a1), _ptr(a2),
+                                             float(strength), C.addressof(out)))
+        return out.value
+
+    def add_hinge(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
+        a1, a2, ax1, ax2 = (_f64(x, 3) for x in (a1, a2, ax1, ax2))
+        out = C.c_uint32()
+        self._check(self.abi.add_hinge(self.h, int(b1), int(b2), _ptr(a1), _ptr(a2), _ptr(ax1), _ptr(ax2),
+                                       float(pos_strength), float(rot_strength), C.addressof(out)))
+        return out.value
+
+    # -- stepping and state -------------------------------------------------------
+    def step(self, n=1):
+        self._check(self.abi.step(self.h, int(n)))
+
+    def state(self):
+        n = C.c_int()
+        self._check(self.abi.num_bodies(self.h, C.addressof(n)))
+        n = n.value
+        com = np.zeros((n, 3)); quat = np.zeros((n, 4)); vel = np.zeros((n, 3)); ang = np.zeros((n, 3))
+        self._check(self.abi.get_body_state(self.h, _ptr(com), _ptr(quat), _ptr(vel), _ptr(ang)))
+        return {"com": com, "quat": quat, "vel": vel, "ang_vel": ang}
+
+    def set_state(self, com=None, quat=None, vel=None, ang_vel=None):
+        arrs = [None if a is None else _f64(a) for a in (com, quat, vel, ang_vel)]
+        self._check(self.abi.set_body_state(self.h, *[_ptr(a) for a in arrs]))
+
+    def aabbs(self):
+        out = np.zeros((self.n_bodies, 6))
+        self._check(self.abi.get_aabbs(self.h, _ptr(out)))
+        return out
+
+    def pairs(self):
+        n = C.c_int()
+        self._check(self.abi.get_pairs(self.h, None, 0, C.addressof(n)))
+        out = np.zeros((max(n.value, 1), 2), dtype=np.uint32)
+        self._check(self.abi.get_pairs(self.h, _ptr(out), n.value, C.addressof(n)))
+        return out[: n.value]
+
+    def contacts(self):
+        n = C.c_int()
+        self._check(self.abi.get_contacts(self.h, None, 0, C.addressof(n)))
+        arr = (Contact * max(n.value, 1))()
+        self._check(self.abi.get_contacts(self.h, C.addressof(arr), n.value, C.addressof(n)))
+        return contacts_to_numpy(arr, n.value)
+
+    def set_contacts(self, cts):
+        arr = numpy_to_contacts(cts)
+        self._check(self.abi.set_contacts(self.h, C.addressof(arr), len(cts["b1"])))
+
+
+_CONTACT_FIELDS = [f[0] for f in Contact._fields_ if f[0] != "pad_"]
+
+
+def contacts_to_numpy(arr, n):
+    out = {}
+    for name in _CONTACT_FIELDS:
+        vals = [getattr(arr[i], name) for i in range(n)]
+        if vals and isinstance(vals[0], C.Array):
+            out[name] = np.array([list(v) for v in vals], dtype=np.float64).reshape(n, -1)
+        else:
+            out[name] = np.array(vals)
+    return out
+
+
+def numpy_to_contacts(cts):
+    n = len(cts["b1"])
+    arr = (Contact * max(n, 1))()
+    for i in range(n):
+        c = arr[i]
+        for name in _CONTACT_FIELDS:
+            v = cts[name][i]
+            f = getattr(c, name)
+            if isinstance(f, C.Array):
+                for k in range(len(f)):
+                    f[k] = float(v[k])
+            else:
+                setattr(c, name, type(f)(v) if not isinstance(f, float) else float(v))
+    return arr

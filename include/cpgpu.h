@@ -1,0 +1,201 @@
+/*
+ * cpgpu.h — C ABI of the GB300 per-step contact path of the ConstraintPhysics
+ * rigid-body engine.
+ *
+ * The reference engine has no FFI: its operator API is the C++ class
+ * phyz::PhysicsEngine (ConstraintPhysics/src/PhysicsEngine.h:60-161).  Every
+ * entry point below replaces one member of that class (or one RigidBody
+ * setter) and is cited beside its declaration.  Conventions:
+ *   - every function returns an int status (CPGPU_OK == 0, negative on error);
+ *     no C++ exception crosses this boundary (the reference uses assert only);
+ *   - all arguments are plain pointers, sizes and doubles (the reference is
+ *     FP64 at its API; the device path computes in FP32);
+ *   - body ids start at 1 and increase by one per created body, exactly like
+ *     PhysicsEngine::next_id (PhysicsEngine.h:172, PhysicsEngine.cpp:487);
+ *   - vectors are xyz triples, quaternions are (r, i, j, k) as in
+ *     mthz::Quaternion (Math/src/Quaternion.h:8).
+ *
+ * The same function set (with prefix cpref_ for the reference engine itself
+ * and cport_ for the CPU restatement) is exported by the oracle libraries under
+ * oracle/, so one test harness drives all three.
+ */
+#ifndef CPGPU_H
+#define CPGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define CPGPU_OK                 0
+#define CPGPU_ERR_INVALID_ARG   -1  /* bad handle, id, size or value            */
+#define CPGPU_ERR_CUDA          -2  /* a CUDA runtime call failed                */
+#define CPGPU_ERR_CAPACITY      -3  /* a device buffer (pairs, contacts...) overflowed */
+#define CPGPU_ERR_NAN           -4  /* a body state became NaN/Inf on the device */
+#define CPGPU_ERR_UNSUPPORTED   -5  /* feature outside the implemented path      */
+#define CPGPU_ERR_OUT_OF_BUDGET -6  /* serving: request exceeds the HBM budget   */
+#define CPGPU_ERR_TIMEOUT       -7  /* a bounded device wait gave up             */
+#define CPGPU_ERR_NO_DEVICE     -8  /* no CUDA device / extension not usable     */
+
+/* movement types: RigidBody::MovementType (RigidBody.h:22) */
+#define CPGPU_DYNAMIC   0
+#define CPGPU_FIXED     1
+#define CPGPU_KINEMATIC 2
+
+typedef struct cpgpu_world  cpgpu_world;   /* one PhysicsEngine              */
+typedef struct cpgpu_batch  cpgpu_batch;   /* many independent worlds        */
+typedef struct cpgpu_server cpgpu_server;  /* continuous-batching rollouts   */
+
+/* Material (ConvexPrimitive.h:17-34).  cfm is always the global one. */
+typedef struct cpgpu_material {
+    double density;
+    double restitution;
+    double kinetic_friction;
+    double static_friction;
+} cpgpu_material;
+
+/* One persistent contact point (PersistentConstraint.h:51-86), as stored in the
+ * contact graph after a step.  Used for diagnostics, checkpoints and parity. */
+typedef struct cpgpu_contact {
+    uint32_t b1, b2;            /* body ids, b1 < b2 (OrderedBodyPair)      */
+    uint32_t live;              /* is_live_contact                          */
+    int32_t  memory_life;       /* memory_life                              */
+    uint64_t magic_c, magic_b;  /* MagicID {cID, bID} (CollisionDetect.h:29) */
+    double   p_local_b1[3];     /* contact_pos_local_b1                     */
+    double   p_local_b2[3];     /* contact_pos_local_b2                     */
+    double   n_local_b1[3];     /* normal_local_b1                          */
+    double   pen_depth;
+    double   bounce;
+    double   friction_coeff;
+    double   normal_impulse;    /* contact.impulse                          */
+    double   friction_impulse[2];
+    double   friction_u[3];     /* friction.u / friction.w of the last row  */
+    double   friction_w[3];
+    uint32_t static_ready;      /* friction.getStaticReady()                */
+    uint32_t pad_;
+} cpgpu_contact;
+
+/* ---- world lifetime and parameters ------------------------------------- */
+/* PhysicsEngine::PhysicsEngine() with the defaults of PhysicsEngine.h:170-227 */
+int cpgpu_world_create(cpgpu_world** out);
+/* PhysicsEngine::~PhysicsEngine (PhysicsEngine.cpp:31-37) */
+int cpgpu_world_destroy(cpgpu_world* w);
+/* PhysicsEngine::setStep_time (PhysicsEngine.cpp:1214-1217) */
+int cpgpu_set_step_time(cpgpu_world* w, double dt);
+/* PhysicsEngine::setGravity (PhysicsEngine.cpp:1142-1145) */
+int cpgpu_set_gravity(cpgpu_world* w, double gx, double gy, double gz);
+/* PhysicsEngine::setSubstepCount (PhysicsEngine.h:91) */
+int cpgpu_set_substep_count(cpgpu_world* w, int substeps);
+/* PhysicsEngine::setPGSIterations (PhysicsEngine.h:90) */
+int cpgpu_set_pgs_iterations(cpgpu_world* w, int n_vel, int n_pos, int n_holonomic);
+/* PhysicsEngine::setSleepingEnabled (PhysicsEngine.cpp:1138-1140); the device
+ * path implements sleeping disabled only and rejects enabling it. */
+int cpgpu_set_sleeping_enabled(cpgpu_world* w, int enabled);
+/* PhysicsEngine::setWarmStartDisabled (PhysicsEngine.cpp:1182-1184) */
+int cpgpu_set_warm_start_disabled(cpgpu_world* w, int disabled);
+/* PhysicsEngine::setGlobalConstraintForceMixing (PhysicsEngine.cpp:1193-1195) */
+int cpgpu_set_global_cfm(cpgpu_world* w, double cfm);
+/* PhysicsEngine::setAngleVelUpdateTickCount (PhysicsEngine.cpp:1173-1176) */
+int cpgpu_set_angle_vel_update_tick_count(cpgpu_world* w, int n);
+/* PhysicsEngine::setInternalGyroscopicForcesDisabled (PhysicsEngine.cpp:1178-1180) */
+int cpgpu_set_internal_gyro_forces_disabled(cpgpu_world* w, int disabled);
+
+/* ---- bodies ------------------------------------------------------------- */
+/* createRigidBody(ConvexUnionGeometry(Polyhedron(points, faces), material),
+ * movement, position) (PhysicsEngine.cpp:486-496, ConvexPrimitive.h:212).
+ * points: n_points xyz; faces: CSR (face_offsets has n_faces+1 entries). */
+int cpgpu_body_hull(cpgpu_world* w, const double* points, int n_points,
+                    const int* face_offsets, const int* face_indices, int n_faces,
+                    const cpgpu_material* mat, int movement, const double pos[3],
+                    uint32_t* out_id);
+/* createRigidBody(ConvexUnionGeometry::box(corner, dx, dy, dz, material), ...)
+ * (Geometry.cpp:14-37) */
+int cpgpu_body_box(cpgpu_world* w, const double corner[3], double dx, double dy, double dz,
+                   const cpgpu_material* mat, int movement, const double pos[3],
+                   uint32_t* out_id);
+/* createRigidBody(ConvexUnionGeometry::sphere(center, radius, material), ...)
+ * (Geometry.cpp:39-41) */
+int cpgpu_body_sphere(cpgpu_world* w, const double center[3], double radius,
+                      const cpgpu_material* mat, int movement, const double pos[3],
+                      uint32_t* out_id);
+/* createRigidBody(ConvexUnionGeometry::cylinder(base, radius, height, material), ...)
+ * (Geometry.cpp:47-49) */
+int cpgpu_body_cylinder(cpgpu_world* w, const double base[3], double radius, double height,
+                        const cpgpu_material* mat, int movement, const double pos[3],
+                        uint32_t* out_id);
+/* createRigidBody(StaticMeshGeometry(MeshInput{tris, points}), fixed)
+ * (PhysicsEngine.cpp:498-512, Geometry.h:52-55) */
+int cpgpu_body_mesh(cpgpu_world* w, const double* points, int n_points,
+                    const int* tris, int n_tris, const cpgpu_material* mat,
+                    int fixed, uint32_t* out_id);
+
+/* RigidBody::setVel / setAngVel / setOrientation / setToPosition / setMass
+ * (RigidBody.cpp:69-118) */
+int cpgpu_body_set_velocity(cpgpu_world* w, uint32_t id, const double v[3]);
+int cpgpu_body_set_ang_velocity(cpgpu_world* w, uint32_t id, const double v[3]);
+int cpgpu_body_set_orientation(cpgpu_world* w, uint32_t id, const double q[4]);
+int cpgpu_body_set_position(cpgpu_world* w, uint32_t id, const double p[3]);
+int cpgpu_body_set_mass(cpgpu_world* w, uint32_t id, double mass);
+
+/* ---- holonomic constraints --------------------------------------------- */
+/* PhysicsEngine::addBallSocketConstraint (PhysicsEngine.cpp:664-687) */
+int cpgpu_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2,
+                          const double b1_attach_local[3], const double b2_attach_local[3],
+                          double pos_correct_strength, uint32_t* out_id);
+/* PhysicsEngine::addHingeConstraint (PhysicsEngine.cpp:693-723) */
+int cpgpu_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2,
+                    const double b1_attach_local[3], const double b2_attach_local[3],
+                    const double b1_axis_local[3], const double b2_axis_local[3],
+                    double pos_correct_strength, double rot_correct_strength,
+                    uint32_t* out_id);
+
+/* ---- stepping and state ------------------------------------------------- */
+/* n_steps x PhysicsEngine::timeStep (PhysicsEngine.cpp:50-471) */
+int cpgpu_step(cpgpu_world* w, int n_steps);
+/* PhysicsEngine::getNumBodies (PhysicsEngine.h:86) */
+int cpgpu_num_bodies(cpgpu_world* w, int* n);
+/* RigidBody::getCOM/getOrientation/getVel/getAngVel for every body in id order;
+ * any output pointer may be NULL.  com/vel/ang_vel: 3 doubles per body,
+ * quat: 4 doubles (r,i,j,k) per body. */
+int cpgpu_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel, double* ang_vel);
+/* Overwrite the dynamic state of every body (a checkpoint restore); any input
+ * pointer may be NULL.  The world geometry follows the new poses. */
+int cpgpu_set_body_state(cpgpu_world* w, const double* com, const double* quat,
+                         const double* vel, const double* ang_vel);
+/* RigidBody::getAABB for every body, 6 doubles (min xyz, max xyz) per body */
+int cpgpu_get_aabbs(cpgpu_world* w, double* aabbs);
+/* Candidate pairs of the last broadphase (AABBTree::getAllCollisionCandidates,
+ * AABB_Tree.h:153-224) as (lower id, higher id), sorted; *n receives the count,
+ * at most cap pairs are written. */
+int cpgpu_get_pairs(cpgpu_world* w, uint32_t* pairs, int cap, int* n);
+/* Every persistent contact of the contact graph, sorted by (b1, b2) and in the
+ * per-edge order of SharedConstraintsEdge::constraints (PhysicsEngine.h:248). */
+int cpgpu_get_contacts(cpgpu_world* w, cpgpu_contact* out, int cap, int* n);
+/* Replace the whole contact graph (a checkpoint restore).  Same layout and
+ * order as cpgpu_get_contacts. */
+int cpgpu_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n);
+
+/* ---- batched worlds ----------------------------------------------------- */
+/* Pack independent worlds into one device batch (segmented arrays) that one
+ * launch sequence per step advances.  The worlds keep their own state; the
+ * batch starts from their current state and the substep count must agree. */
+int cpgpu_batch_create(cpgpu_world* const* worlds, int n_worlds, cpgpu_batch** out);
+int cpgpu_batch_destroy(cpgpu_batch* b);
+int cpgpu_batch_step(cpgpu_batch* b, int n_steps);
+/* Body state of world `world_index` of the batch (same layout as above). */
+int cpgpu_batch_get_body_state(cpgpu_batch* b, int world_index, double* com, double* quat,
+                               double* vel, double* ang_vel);
+/* Total bodies, worlds and live contact points of the batch. */
+int cpgpu_batch_info(cpgpu_batch* b, int64_t* n_bodies, int64_t* n_worlds, int64_t* n_contacts);
+
+/* ---- diagnostics -------------------------------------------------------- */
+/* Last error message of this thread (static storage, never NULL). */
+const char* cpgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPGPU_H */

@@ -1,0 +1,439 @@
+// geometry.cpp — hull preparation, mass properties, SAT narrowphase and
+// contact clipping of the CPU restatement (test infrastructure; see cport.h).
+#include "cport.h"
+
+namespace cport {
+
+static const double EPS_GAUSS = 0.0000000001;  // ConvexPrimitive.cpp:10
+
+V3 Hull::faceNormal(int f) const {
+    const std::vector<int>& s = faces[f];
+    V3 p1 = pts[s[0]], p2 = pts[s[1]], p3 = pts[s[face_nci[f]]];
+    return (p2 - p1).cross(p3 - p2).normalize() * (double)face_dir[f];
+}
+
+// Surface::findNormalCalcInfo (ConvexPrimitive.cpp:797-815): the third point of
+// the normal is the first one not (nearly) collinear with the first edge, and
+// the sign makes the normal point away from the interior point.
+static void normalCalcInfo(Hull& h, int f, const V3& normalish) {
+    const std::vector<int>& s = h.faces[f];
+    V3 p0 = h.pts[s[0]], p1 = h.pts[s[1]];
+    int nci = 2;
+    V3 v1 = (p1 - p0).normalize();
+    V3 v2 = (h.pts[s[nci]] - p0).normalize();
+    while (std::abs(v1.dot(v2)) > 0.99 && nci + 1 < (int)s.size()) v2 = (h.pts[s[++nci]] - p0).normalize();
+    h.face_nci[f] = nci;
+    h.face_dir[f] = 1;
+    if (normalish.dot(h.faceNormal(f)) < 0) h.face_dir[f] = -1;
+}
+
+// Surface::setWindingAntiClockwise (ConvexPrimitive.cpp:834-859)
+static void windAntiClockwise(Hull& h, int f, const V3& n) {
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    std::vector<int>& s = h.faces[f];
+    int np = (int)s.size();
+    double area = 0;
+    for (int i = 0; i < np; i++) {
+        V3 p1 = h.pts[s[i]], p2 = h.pts[s[(i + 1 == np) ? 0 : i + 1]];
+        double p1u = p1.dot(u), p1w = p1.dot(w), p2u = p2.dot(u), p2w = p2.dot(w);
+        area += (p2w - p1w) * (p2u + p1u) / 2.0;
+    }
+    if (area < 0) {
+        std::reverse(s.begin(), s.end());
+        normalCalcInfo(h, f, n);
+    }
+}
+
+Extrema findExtrema(const Hull& h, const V3& axis) {
+    // CollisionDetect.cpp:627-644 (strict comparisons: the first index wins ties)
+    Extrema e;
+    for (int i = 0; i < (int)h.pts.size(); i++) {
+        double v = h.pts[i].dot(axis);
+        if (v < e.min_v) { e.min_id = i; e.min_v = v; }
+        if (v > e.max_v) { e.max_id = i; e.max_v = v; }
+    }
+    return e;
+}
+
+void Hull::build(const std::vector<V3>& points, const std::vector<std::vector<int>>& face_idx) {
+    // Polyhedron::Polyhedron (ConvexPrimitive.cpp:582-658)
+    pts = points;
+    interior = V3();
+    for (const V3& p : pts) interior += p;
+    interior /= (double)pts.size();
+    int nf = (int)face_idx.size();
+    faces = face_idx;
+    face_nci.assign(nf, 2);
+    face_dir.assign(nf, 1);
+    face_id.resize(nf);
+    vert_faces.assign(pts.size(), {});
+    vert_edges.assign(pts.size(), {});
+    for (int f = 0; f < nf; f++) {
+        for (int j : faces[f]) vert_faces[j].push_back(f);
+        face_id[f] = (int)pts.size() + f;
+        normalCalcInfo(*this, f, pts[faces[f][0]] - interior);
+        windAntiClockwise(*this, f, faceNormal(f));
+    }
+    edges.clear();
+    for (int f = 0; f < nf; f++) {
+        int n = (int)faces[f].size();
+        for (int i = 0; i < n; i++) {
+            int a = faces[f][i], b = faces[f][(i + 1) % n];
+            bool seen = false;
+            for (auto& e : edges) if ((e.first == a && e.second == b) || (e.first == b && e.second == a)) { seen = true; break; }
+            if (!seen) edges.push_back({a, b});
+        }
+    }
+    for (int i = 0; i < (int)edges.size(); i++) {
+        vert_edges[edges[i].first].push_back(i);
+        vert_edges[edges[i].second].push_back(i);
+    }
+    // Polyhedron::computeGaussMap (ConvexPrimitive.cpp:861-896)
+    gv.clear(); g_redundant.clear(); g_cache.clear(); g_ref_idx.clear(); g_ref_val.clear(); arcs.clear();
+    for (int i = 0; i < nf; i++) {
+        V3 n = faceNormal(i);
+        bool red = false;
+        for (const V3& g : gv) if (n.dot(g) < -1 + EPS_GAUSS) { red = true; break; }
+        int ref = faces[i][0];
+        gv.push_back(n);
+        g_redundant.push_back(red);
+        g_cache.push_back(findExtrema(*this, n));
+        g_ref_idx.push_back(ref);
+        g_ref_val.push_back(n.dot(pts[ref]));
+        for (int j = i + 1; j < nf; j++) {
+            const std::vector<int>& s1 = faces[i];
+            const std::vector<int>& s2 = faces[j];
+            for (size_t k = 0; k < s1.size(); k++) {
+                for (size_t w = 0; w < s2.size(); w++) {
+                    int a1 = s1[k], a2 = s1[(k + 1) % s1.size()], b1 = s2[w], b2 = s2[(w + 1) % s2.size()];
+                    if ((a1 == b1 && a2 == b2) || (a1 == b2 && a2 == b1)) { arcs.push_back({i, j}); break; }
+                }
+            }
+        }
+    }
+}
+
+// Volume, first and second moments of a convex polyhedron by decomposition
+// into tetrahedra (interior point, face fan).  Same quantities as Mirtich's
+// surface-integral method used by the reference (RigidBody.cpp:427-640),
+// computed differently, so results agree to rounding.
+void massProperties(const Hull& h, double density, V3* com, M3* tensor, double* mass) {
+    double vol = 0;
+    V3 first;
+    double c[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // integral of x_i x_j dV
+    V3 o = h.interior;
+    for (int f = 0; f < (int)h.faces.size(); f++) {
+        const std::vector<int>& s = h.faces[f];
+        for (size_t t = 1; t + 1 < s.size(); t++) {
+            V3 p[4] = {o, h.pts[s[0]], h.pts[s[t]], h.pts[s[t + 1]]};
+            double v6 = (p[1] - p[0]).dot((p[2] - p[0]).cross(p[3] - p[0]));  // 6 * signed volume
+            double v = v6 / 6.0;
+            V3 sum = p[0] + p[1] + p[2] + p[3];
+            vol += v;
+            first += sum * (v / 4.0);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) {
+                    double acc = sum[i] * sum[j];
+                    for (int k = 0; k < 4; k++) acc += p[k][i] * p[k][j];
+                    c[i][j] += v / 20.0 * acc;
+                }
+        }
+    }
+    *mass = density * vol;
+    *com = first * density / *mass;
+    M3 t;
+    double tr = c[0][0] + c[1][1] + c[2][2];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) t.m[i][j] = density * ((i == j ? tr : 0.0) - c[i][j]);
+    // about the centre of mass (parallel axis; RigidBody.cpp:400-420)
+    V3 cm = *com;
+    double m = *mass;
+    double cc[3] = {cm.x, cm.y, cm.z};
+    double c2 = cm.mag2();
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) t.m[i][j] -= m * ((i == j ? c2 : 0.0) - cc[i] * cc[j]);
+    *tensor = t;
+}
+
+// ---------------------------------------------------------------- SAT ----
+struct NormResult { int a_id, b_id; V3 n; double pen; };
+
+// sat_checknorm (CollisionDetect.cpp:705-715)
+static NormResult checkNorm(const Extrema& a, const Extrema& b, const V3& n) {
+    double fwd = a.max_v - b.min_v;
+    double rev = b.max_v - a.min_v;
+    if (fwd < rev) return {a.max_id, b.min_id, n, fwd};
+    return {a.min_id, b.max_id, -n, rev};
+}
+
+static Extrema recenter(const Extrema& e, double old_ref, double new_ref) {
+    double d = new_ref - old_ref;
+    Extrema o = e;
+    o.min_v = e.min_v + d;
+    o.max_v = e.max_v + d;
+    return o;
+}
+
+struct P2 { double x = 0, y = 0; };
+static P2 p2(double a, double b) { P2 p; p.x = a; p.y = b; return p; }
+static P2 sub(P2 a, P2 b) { return p2(a.x - b.x, a.y - b.y); }
+static P2 add(P2 a, P2 b) { return p2(a.x + b.x, a.y + b.y); }
+static P2 mul(P2 a, double d) { return p2(a.x * d, a.y * d); }
+static double dot2(P2 a, P2 b) { double s = 0; s += a.x * b.x; s += a.y * b.y; return s; }
+static P2 norm2(P2 a) { return mul(a, 1.0 / std::sqrt(dot2(a, a))); }
+// getInDirOfEdge (CollisionDetect.cpp:394-397): inward normal of a CCW edge
+static P2 inDir(P2 a, P2 b) { return norm2(p2(a.y - b.y, b.x - a.x)); }
+
+enum Origin { FACE, EDGE, VERTEX };
+struct Area { std::vector<P2> ps; std::vector<int> ids; int surface; Origin origin; };
+
+// findContactArea (CollisionDetect.cpp:237-280)
+static Area contactArea(const Hull& c, const V3& n, const V3& p, int pid, const V3& u, const V3& w) {
+    int best_f = -1;
+    double best_ft = 1.0;
+    for (int f : c.vert_faces[pid]) {
+        double ca = c.faceNormal(f).dot(n);
+        if (1 - ca < best_ft) { best_ft = 1 - ca; best_f = f; }
+    }
+    if (best_ft <= cosTol()) {
+        Area a;
+        for (int id : c.faces[best_f]) { V3 v = c.pts[id]; a.ps.push_back(p2(v.dot(u), v.dot(w))); a.ids.push_back(id); }
+        a.surface = c.face_id[best_f];
+        a.origin = FACE;
+        return a;
+    }
+    int best_e = -1;
+    double best_et = 1.0;
+    for (int e : c.vert_edges[pid]) {
+        V3 d = c.pts[c.edges[e].second] - c.pts[c.edges[e].first];
+        double sa = std::abs(d.normalize().dot(n));
+        if (sa < best_et) { best_et = sa; best_e = e; }
+    }
+    if (best_et <= sinTol()) {
+        Area a;
+        V3 e1 = c.pts[c.edges[best_e].first], e2 = c.pts[c.edges[best_e].second];
+        a.ps = {p2(e1.dot(u), e1.dot(w)), p2(e2.dot(u), e2.dot(w))};
+        a.ids = {c.edges[best_e].first, c.edges[best_e].second};
+        a.surface = -1;
+        a.origin = EDGE;
+        return a;
+    }
+    Area a;
+    a.ps = {p2(p.dot(u), p.dot(w))};
+    a.ids = {pid};
+    a.surface = -1;
+    a.origin = VERTEX;
+    return a;
+}
+
+// getEdgeID (CollisionDetect.cpp:9-21): ids are truncated to 16 bits
+static uint32_t edgeId(int a, int b) {
+    uint16_t p1 = (uint16_t)a, p2v = (uint16_t)b;
+    int mn, mx;
+    if (p1 < p2v) { mn = p1; mx = p2v; } else { mn = p2v; mx = p1; }
+    return (0x0000FFFFu & (uint32_t)mn) + (0xFFFF0000u & ((uint32_t)mx << 16));
+}
+
+struct ClipP { P2 pos; int32_t src; uint64_t magic; bool skip; };
+
+static uint64_t packMagic(uint64_t lo, uint64_t hi) {
+    return (0x00000000FFFFFFFFull & lo) | (0xFFFFFFFF00000000ull & (hi << 32));
+}
+
+static bool windingCCW(const Area& c) {
+    P2 in = inDir(c.ps[0], c.ps[1]);
+    for (size_t i = 2; i < c.ps.size(); i++) {
+        double d = dot2(sub(c.ps[i], c.ps[0]), in);
+        if (d > 0.0000000001) return true;
+        if (d < -0.0000000001) return false;
+    }
+    return false;
+}
+
+// createClipEvaluationPoly (CollisionDetect.cpp:441-460)
+static std::vector<ClipP> clipPoly(const Area& c, uint32_t other_surface, bool flip) {
+    std::vector<ClipP> out;
+    for (size_t i = 0; i < c.ps.size(); i++) {
+        uint64_t id = (uint64_t)(int64_t)c.ids[i];
+        uint64_t m = flip ? packMagic(other_surface, id) : packMagic(id, other_surface);
+        out.push_back({c.ps[i], c.ids[i], m, false});
+    }
+    if (c.ps.size() > 2 && !windingCCW(c)) std::reverse(out.begin(), out.end());
+    return out;
+}
+
+// getEdgeIntersectionWithClippingEdge (CollisionDetect.cpp:462-487)
+static ClipP intersect(const ClipP& e1, const ClipP& e2, P2 nrm, P2 sample, int32_t clip_edge, bool flip) {
+    P2 d = sub(e2.pos, e1.pos);
+    P2 pos = add(e1.pos, mul(d, dot2(nrm, sub(sample, e1.pos)) / dot2(nrm, d)));
+    bool e2_kept = dot2(d, nrm) > 0;
+    int32_t src = e2_kept ? e1.src : e2.src;
+    uint64_t eid = edgeId(e1.src, e2.src);
+    uint64_t ce = (uint64_t)(int64_t)clip_edge;
+    uint64_t m = flip ? packMagic(ce, eid) : packMagic(eid, ce);
+    return {pos, src, m, !e2_kept};
+}
+
+enum ClipRes { BOTH, P1_ON_P2_CLIPPED, P2_ON_P1_CLIPPED, NEITHER, ONLY_P1, ONLY_P2 };
+static ClipRes checkSegment(double a, double b, double c) {
+    if (a >= c && b >= c) return NEITHER;
+    if (a == c && b < c) return P1_ON_P2_CLIPPED;
+    if (a < c && b == c) return P2_ON_P1_CLIPPED;
+    if (a < c && b >= c) return ONLY_P1;
+    if (a >= c && b < c) return ONLY_P2;
+    return BOTH;
+}
+
+// getClipEvaluatinPolyAfterClippingByEdge (CollisionDetect.cpp:500-576)
+static std::vector<ClipP> clipByEdge(const std::vector<ClipP>& c, P2 side, P2 sample, int32_t eid, bool flip) {
+    std::vector<ClipP> out;
+    double cv = dot2(sample, side);
+    if (c.size() >= 3) {
+        double v1 = 0, v2 = 0;
+        ClipP q1, q2;
+        for (size_t i = 0; i < c.size(); i++) {
+            if (i > 0) { v1 = v2; q1 = q2; }
+            else { q1 = c[0]; v1 = dot2(q1.pos, side); }
+            q2 = c[(i + 1) % c.size()];
+            v2 = dot2(q2.pos, side);
+            ClipRes r = checkSegment(v1, v2, cv);
+            if (r == NEITHER || r == P1_ON_P2_CLIPPED) out.push_back(q1);
+            else if (r == ONLY_P2) { out.push_back(q1); out.push_back(intersect(q1, q2, side, sample, eid, flip)); }
+            else if (r == ONLY_P1) out.push_back(intersect(q1, q2, side, sample, eid, flip));
+        }
+        return out;
+    }
+    if (c.size() == 2) {
+        double v1 = dot2(c[0].pos, side), v2 = dot2(c[1].pos, side);
+        ClipRes r = checkSegment(v1, v2, cv);
+        if (r == NEITHER) return c;
+        if (r == P1_ON_P2_CLIPPED) return {c[0]};
+        if (r == P2_ON_P1_CLIPPED) return {c[1]};
+        if (r == ONLY_P1) return {intersect(c[0], c[1], side, sample, eid, flip), c[1]};
+        if (r == ONLY_P2) return {c[0], intersect(c[0], c[1], side, sample, eid, flip)};
+        return out;
+    }
+    if (dot2(c[0].pos, side) >= cv) return c;
+    return out;
+}
+
+static std::vector<ClipP> clipByAll(std::vector<ClipP> c1, const std::vector<ClipP>& c2, bool flip) {
+    for (size_t i = 0; i < c2.size(); i++) {
+        const ClipP& e1 = c2[i];
+        if (e1.skip) continue;
+        const ClipP& e2 = c2[(i + 1) % c2.size()];
+        c1 = clipByEdge(c1, inDir(e1.pos, e2.pos), e1.pos, (int32_t)edgeId(e1.src, e2.src), flip);
+        if (c1.empty()) return c1;
+    }
+    return c1;
+}
+
+// clipContacts (CollisionDetect.cpp:578-620)
+static std::vector<ClipP> clipContacts(const Area& c1, const Area& c2) {
+    std::vector<ClipP> p1 = clipPoly(c1, (uint32_t)c2.surface, false);
+    std::vector<ClipP> p2v = clipPoly(c2, (uint32_t)c1.surface, true);
+    if (p1.size() == 1) return p1;
+    if (p2v.size() == 1) return p2v;
+    if (p1.size() == 2 && p2v.size() == 2) {
+        P2 nrm = inDir(p2v[0].pos, p2v[1].pos);
+        return {intersect(p1[0], p1[1], nrm, p2v[0].pos, (int32_t)edgeId(p2v[0].src, p2v[1].src), false)};
+    }
+    if (p1.size() == 2) return clipByAll(p1, p2v, false);
+    if (p2v.size() == 2) return clipByAll(p2v, p1, true);
+    p1 = clipByAll(p1, p2v, false);
+    return clipByAll(p2v, p1, true);
+}
+
+// SAT_PolyPoly (CollisionDetect.cpp:717-835)
+Manifold satPolyPoly(const Hull& a, uint32_t a_id, const Material& am, const Hull& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    out.max_pen = -1;
+    NormResult best = {-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    for (size_t f = 0; f < a.gv.size(); f++) {
+        if (a.g_redundant[f]) continue;
+        Extrema ea = recenter(a.g_cache[f], a.g_ref_val[f], a.gv[f].dot(a.pts[a.g_ref_idx[f]]));
+        NormResult x = checkNorm(ea, findExtrema(b, a.gv[f]), a.gv[f]);
+        if (x.pen < 0) { out.max_pen = -1; return out; }
+        if (x.pen < best.pen) best = x;
+    }
+    for (size_t f = 0; f < b.gv.size(); f++) {
+        if (b.g_redundant[f]) continue;
+        Extrema eb = recenter(b.g_cache[f], b.g_ref_val[f], b.gv[f].dot(b.pts[b.g_ref_idx[f]]));
+        NormResult x = checkNorm(findExtrema(a, b.gv[f]), eb, b.gv[f]);
+        if (x.pen < 0) { out.max_pen = -1; return out; }
+        if (x.pen < best.pen) best = x;
+    }
+    for (auto& arc1 : a.arcs) {
+        for (auto& arc2 : b.arcs) {
+            V3 a1 = a.gv[arc1.first], a2 = a.gv[arc1.second];
+            V3 b1 = -b.gv[arc2.first], b2 = -b.gv[arc2.second];
+            V3 avg = a1 + a2;
+            if (avg.dot(b1) + avg.dot(b2) <= 0) continue;
+            V3 ap = a1.cross(a2), bp = b1.cross(b2);
+            if (ap.dot(b1) * ap.dot(b2) > 0 || bp.dot(a1) * bp.dot(a2) > 0) continue;
+            V3 n = ap.cross(bp);
+            if (n.mag2() == 0) continue;
+            n = n.normalize();
+            if (avg.dot(n) < 0) n *= -1;
+            NormResult x = checkNorm(findExtrema(a, n), findExtrema(b, n), n);
+            if (x.pen < 0) { out.max_pen = -1; return out; }
+            if (x.pen < best.pen) best = x;
+        }
+    }
+    out.normal = best.n;
+    V3 n = best.n;
+    V3 amax = a.pts[best.a_id], bmax = b.pts[best.b_id];
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    Area ac = contactArea(a, n, amax, best.a_id, u, w);
+    Area bc = contactArea(b, (-1) * n, bmax, best.b_id, u, w);
+    std::vector<ClipP> pool = clipContacts(ac, bc);
+    double a_dot = amax.dot(n);
+    V3 off = n * a_dot;
+    uint64_t cid = (0x00000000FFFFFFFFull & (uint64_t)a_id) | (0xFFFFFFFF00000000ull & ((uint64_t)b_id << 32));
+    for (const ClipP& p : pool) {
+        ManifoldPoint mp;
+        mp.pos = u * p.pos.x + w * p.pos.y + off;
+        mp.pen = mp.pos.dot(n) - a_dot + best.pen;
+        mp.restitution = std::max(am.restitution, bm.restitution);
+        mp.kinetic = (am.kinetic + bm.kinetic) / 2.0;
+        mp.stat = (am.stat + bm.stat) / 2.0;
+        mp.magic_c = cid;
+        mp.magic_b = p.magic;
+        out.pts.push_back(mp);
+    }
+    out.max_pen = best.pen;
+    return out;
+}
+
+// cull_manifold (CollisionDetect.cpp:2795-2830): keep the extreme points in 4
+// directions of the contact plane
+Manifold cullManifold(const Manifold& m, int n) {
+    if (n >= (int)m.pts.size()) return m;
+    Manifold out;
+    out.normal = m.normal;
+    out.max_pen = 0;
+    out.pts.resize(n);
+    std::vector<bool> avail(m.pts.size(), true);
+    V3 u, w;
+    m.normal.perpBasis(&u, &w);
+    for (int i = 0; i < n; i++) {
+        double vu = std::cos(2 * PI_FULL * i / n);
+        double vw = std::sin(2 * PI_FULL * i / n);
+        V3 dir = u * vu + w * vw;
+        int best = -1;
+        double bv = -std::numeric_limits<double>::infinity();
+        for (size_t j = 0; j < m.pts.size(); j++) {
+            if (!avail[j]) continue;
+            double v = m.pts[j].pos.dot(dir);
+            if (v > bv) { bv = v; best = (int)j; }
+        }
+        out.pts[i] = m.pts[best];
+        out.max_pen = std::max(out.max_pen, m.pts[best].pen);
+        avail[best] = false;
+    }
+    return out;
+}
+
+}  // namespace cport

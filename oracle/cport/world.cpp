@@ -1,0 +1,675 @@
+// world.cpp — per-step pipeline of the CPU restatement (test infrastructure;
+// see cport.h): broadphase, narrowphase, contact persistence, islands, row
+// rebuild, PGS and integration, plus the cport_ C ABI.
+#include "cport.h"
+
+#include <set>
+#include <string>
+
+extern "C" {
+#include "cpgpu.h"
+}
+
+namespace cport {
+
+// ------------------------------------------------------------ bodies ----
+static AABB genAABB(const Hull& h) {
+    const double inf = std::numeric_limits<double>::infinity();
+    AABB a{V3(inf, inf, inf), V3(-inf, -inf, -inf)};
+    for (const V3& p : h.pts) {
+        a.mn.x = std::min<double>(a.mn.x, p.x); a.mn.y = std::min<double>(a.mn.y, p.y); a.mn.z = std::min<double>(a.mn.z, p.z);
+        a.mx.x = std::max<double>(a.mx.x, p.x); a.mx.y = std::max<double>(a.mx.y, p.y); a.mx.z = std::max<double>(a.mx.z, p.z);
+    }
+    return a;
+}
+
+// RigidBody::updateGeometry (RigidBody.cpp:281-312) for a single polyhedron
+void Body::updateGeometry() {
+    q = q.normalize();
+    M3 rot = q.rotMatrix();
+    for (size_t i = 0; i < shape.pts.size(); i++) shape.pts[i] = com + rot * ref_shape.pts[i];
+    shape.interior = com + rot * ref_shape.interior;
+    for (size_t i = 0; i < shape.gv.size(); i++) shape.gv[i] = rot * ref_shape.gv[i];
+    aabb = genAABB(shape);
+}
+
+// RigidBody::updateInertiaTensor (RigidBody.cpp:270-279)
+void Body::updateInertiaTensor() {
+    q = q.normalize();
+    M3 rot = q.rotMatrix();
+    M3 rc = q.conj().rotMatrix();
+    tensor = rot * ref_tensor * rc;
+    inv_tensor = rot * ref_inv_tensor * rc;
+}
+
+// RigidBody::rotateWhileApplyingGyroAccel (RigidBody.cpp:207-255): implicit
+// gyroscopic update, n_itr sub-steps of two Newton iterations each
+void Body::rotateWithGyro(double dt, int n_itr, bool gyro_disabled) {
+    const double CUT = 0.00000000001;
+    if (ang_vel.mag2() == 0) return;
+    if (gyro_disabled) {
+        Q rot = Q::axisAngle(ang_vel.mag() * dt, ang_vel.normalize());
+        q = rot * q;
+        return;
+    }
+    M3 it = tensor;
+    Q iq = q;
+    V3 iw = ang_vel;
+    for (int i = 0; i < n_itr; i++) {
+        V3 w = iw;
+        double ts = dt / n_itr;
+        for (int k = 0; k < 2; k++) {
+            V3 f = ts * w.cross(it * w) - it * (iw - w);
+            M3 jac = it + ts * (M3::crossMat(w) * it - M3::crossMat(it * w));
+            if (std::abs(jac.det()) > CUT) w -= jac.inverse() * f;
+        }
+        iw = w;
+        iq = Q::axisAngle(ts * iw.mag(), iw) * iq;
+        if (i + 1 < n_itr) {
+            M3 rot = iq.rotMatrix();
+            M3 rc = iq.conj().rotMatrix();
+            it = rot * ref_tensor * rc;
+        }
+    }
+    q = iq;
+    ang_vel = iw;
+}
+
+// RigidBody::RigidBody + PhysicsEngine::createRigidBody (RigidBody.cpp:13-39,
+// PhysicsEngine.cpp:486-496)
+Body* World::addHull(const std::vector<V3>& pts, const std::vector<std::vector<int>>& faces, const Material& m,
+                     int movement, V3 pos) {
+    auto b = std::make_unique<Body>();
+    b->id = (uint32_t)bodies.size() + 1;
+    b->movement = movement;
+    b->mat = m;
+    b->src_shape.build(pts, faces);
+    b->create_pos = pos;
+    double mass;
+    V3 com;
+    M3 tensor;
+    massProperties(b->src_shape, m.density, &com, &tensor, &mass);
+    Body* raw = b.get();
+    bodies.push_back(std::move(b));
+    placeBody(raw, mass, com, tensor);
+    nodes[raw->id] = raw;
+    adj[raw];
+    return raw;
+}
+
+// The part of the RigidBody constructor that follows the mass properties
+// (RigidBody.cpp:19-36): recentre the reference geometry on the COM, track the
+// geometry origin and move it to the creation position.
+void World::placeBody(Body* b, double mass, const V3& com_geom, const M3& tensor) {
+    b->mass = mass;
+    b->com = com_geom;
+    b->ref_tensor = tensor;
+    b->ref_inv_tensor = b->ref_tensor.inverse();
+    b->tensor = b->ref_tensor;
+    b->inv_tensor = b->ref_inv_tensor;
+    b->q = Q();
+    b->ref_shape = b->src_shape;
+    M3 I = M3::iden();
+    V3 mc = -b->com;
+    for (V3& p : b->ref_shape.pts) p = mc + I * p;
+    b->ref_shape.interior = mc + I * b->ref_shape.interior;
+    for (V3& g : b->ref_shape.gv) g = I * g;
+    b->shape = b->src_shape;
+    b->aabb = genAABB(b->shape);
+    b->local_origin = -b->com;
+    b->track_p.assign(1, b->local_origin + V3(0, 0, 0));
+    V3 t = b->create_pos - b->trackedP(0);
+    b->com += t;
+    b->updateGeometry();
+}
+
+// --------------------------------------------------------- constraint graph ----
+Edge* World::edgeBetween(Body* a, Body* b) {
+    for (Edge* e : adj[a]) if (e->other(a) == b) return e;
+    return nullptr;
+}
+
+// ConstraintGraphNode::getOrCreateEdgeTo / insertNewEdge
+// (PhysicsEngine.cpp:1958-1995): node edge lists stay sorted by other id
+Edge* World::getOrCreateEdge(Body* a, Body* b) {
+    if (Edge* e = edgeBetween(a, b)) return e;
+    auto e = std::make_unique<Edge>();
+    e->n1 = a;
+    e->n2 = b;
+    Edge* raw = e.get();
+    edges.push_back(std::move(e));
+    for (Body* n : {a, b}) {
+        std::vector<Edge*>& l = adj[n];
+        uint32_t oid = raw->other(n)->id;
+        size_t i = 0;
+        while (i < l.size() && !(oid < l[i]->other(n)->id)) i++;
+        l.insert(l.begin() + i, raw);
+    }
+    return raw;
+}
+
+void World::deleteEdge(Edge* e) {
+    for (Body* n : {e->n1, e->n2}) {
+        std::vector<Edge*>& l = adj[n];
+        l.erase(std::remove(l.begin(), l.end(), e), l.end());
+    }
+    for (size_t i = 0; i < edges.size(); i++)
+        if (edges[i].get() == e) { edges.erase(edges.begin() + i); break; }
+}
+
+// PhysicsEngine::addContact (PhysicsEngine.cpp:1062-1111): warm-start match by
+// MagicID, otherwise append a new contact
+void World::addContact(Body* b1, Body* b2, const ManifoldPoint& mp, const V3& n) {
+    Edge* e = getOrCreateEdge(b1, b2);
+    M3 i1 = b1->q.conj().rotMatrix();
+    M3 i2 = b2->q.conj().rotMatrix();
+    V3 nl = i1 * n;
+    V3 p1 = i1 * (mp.pos - b1->com);
+    V3 p2 = i2 * (mp.pos - b2->com);
+    for (auto& c : e->contacts) {
+        if (c->magic_b == mp.magic_b && c->magic_c == mp.magic_c) {
+            c->friction_coeff = c->static_ready ? mp.stat : mp.kinetic;
+            c->pen = mp.pen;
+            c->n_local = nl;
+            c->p1_local = p1;
+            c->p2_local = p2;
+            c->life = p.contact_life;
+            c->live = true;
+            return;
+        }
+    }
+    auto c = std::make_unique<Contact>();
+    c->b1 = b1; c->b2 = b2;
+    c->p1_local = p1; c->p2_local = p2; c->n_local = nl;
+    c->pen = mp.pen;
+    c->bounce = mp.restitution;
+    c->hardness = p.hardness;
+    c->friction_coeff = mp.kinetic;
+    c->cutoff = p.cutoff_vel;
+    c->magic_c = mp.magic_c;
+    c->magic_b = mp.magic_b;
+    c->life = p.contact_life;
+    c->live = true;
+    e->contacts.push_back(std::move(c));
+}
+
+// ------------------------------------------------------------- rows ----
+static Mat<6, 6> invMassMat(const Body* b) {
+    Mat<6, 6> o;
+    double im = b->invMass();
+    M3 it = b->invTensor();
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) { o.v[i][j] = (i == j ? 1.0 : 0.0) * im; o.v[3 + i][3 + j] = it.m[i][j]; }
+    return o;
+}
+
+template <int N>
+static Mat<N, N> withCFM(Mat<N, N> m, double cfm) {
+    for (int i = 0; i < N; i++) m.v[i][i] *= (1 + cfm);
+    return m;
+}
+
+// Contact::updateSolverConstraints (PersistentConstraint.cpp:201-215) with the
+// ContactConstraint and FrictionConstraint constructors
+// (ConstraintSolver.cpp:240-261, 277-329)
+static void rebuildContact(Contact* c, const Params& p, double dt) {
+    Body* a = c->b1;
+    Body* b = c->b2;
+    V3 pa = a->q.rotate(c->p1_local) + a->com;
+    V3 pb = b->q.rotate(c->p2_local) + b->com;
+    V3 n = a->q.rotate(c->n_local);
+    double depth = (pb - pa).dot(n) + c->pen;
+    Vec<1> wn = p.warm_start_disabled ? Vec<1>() : scale(1.0, c->normal.impulse);
+    Vec<2> wf = p.warm_start_disabled ? Vec<2>() : scale(1.0, c->friction.impulse);
+    double pcc = std::min<double>(c->hardness * dt, 1.0 / dt);
+    V3 rA = pa - a->com, rB = pa - b->com;
+    Mat<6, 6> ma = invMassMat(a), mb = invMassMat(b);
+
+    Row<1>& r = c->normal;
+    r = Row<1>();
+    r.a = a; r.b = b;
+    Mat<1, 3> nd; nd.v[0][0] = n.x; nd.v[0][1] = n.y; nd.v[0][2] = n.z;
+    put(r.ja, -nd, 0, 0);
+    put(r.ja, nd * skew(rA), 0, 3);
+    put(r.jb, nd, 0, 0);
+    put(r.jb, (-nd) * skew(rB), 0, 3);
+    r.ita = ma * r.ja.T();
+    r.itb = mb * r.jb.T();
+    Mat<1, 1> itv = r.ja * r.ita + r.jb * r.itb;
+    r.minv = inverse(withCFM(itv, p.cfm));
+    r.ptarget.v[0] = std::max<double>(0.0, depth - 0.05) * pcc;
+    r.impulse = wn;
+
+    Row<2>& f = c->friction;
+    V3 su = c->fu, sw = c->fw;
+    f = Row<2>();
+    f.a = a; f.b = b;
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    f.impulse.v[0] = u.dot(su) * wf.v[0] + u.dot(sw) * wf.v[1];
+    f.impulse.v[1] = w.dot(su) * wf.v[0] + w.dot(sw) * wf.v[1];
+    Mat<1, 3> ud, wd;
+    ud.v[0][0] = u.x; ud.v[0][1] = u.y; ud.v[0][2] = u.z;
+    wd.v[0][0] = w.x; wd.v[0][1] = w.y; wd.v[0][2] = w.z;
+    put(f.ja, ud, 0, 0);
+    put(f.ja, (-ud) * skew(rA), 0, 3);
+    put(f.jb, -ud, 0, 0);
+    put(f.jb, ud * skew(rB), 0, 3);
+    put(f.ja, wd, 1, 0);
+    put(f.ja, (-wd) * skew(rA), 1, 3);
+    put(f.jb, -wd, 1, 0);
+    put(f.jb, wd * skew(rB), 1, 3);
+    f.ita = ma * f.ja.T();
+    f.itb = mb * f.jb.T();
+    Mat<2, 2> fv = f.ja * f.ita + f.jb * f.itb;
+    f.minv = inverse(withCFM(fv, p.cfm));
+    c->fu = u;
+    c->fw = w;
+    c->static_ready = false;
+    c->friction_built = true;
+}
+
+static Vec<6> velAng(const V3& v, const V3& w) { Vec<6> o; o.v[0] = v.x; o.v[1] = v.y; o.v[2] = v.z; o.v[3] = w.x; o.v[4] = w.y; o.v[5] = w.z; return o; }
+
+// PGSConstraintStep (ConstraintSolver.cpp:12-40): Gauss-Seidel update with the
+// projection applied to the accumulated impulse
+template <int N, class Proj>
+static void pgsStep(Row<N>& r, bool pseudo, Proj proj) {
+    Vec<6>* va = pseudo ? &r.da->pv : &r.da->v;
+    Vec<6>* vb = pseudo ? &r.db->pv : &r.db->v;
+    Vec<N>* acc = pseudo ? &r.pimpulse : &r.impulse;
+    Vec<N> target = pseudo ? r.ptarget : r.target;
+    Vec<N> cur = r.value(*va, *vb);
+    Vec<N> delta = target - cur;
+    Vec<N> nw = *acc + mul(r.minv, delta);
+    Vec<N> diff = proj(nw) - *acc;
+    if (!diff.isZero()) {
+        r.applyImpulse(diff, va, vb);
+        *acc += diff;
+    }
+}
+
+// PGS_solve (ConstraintSolver.cpp:80-213) for the contact rows of one island
+static void pgsSolve(std::vector<RowRef>& rows, int n_vel, int n_pos) {
+    std::unordered_map<Body*, std::unique_ptr<DV>> dv;
+    auto slot = [&](Body* b) { auto& s = dv[b]; if (!s) s = std::make_unique<DV>(); return s.get(); };
+    for (RowRef& rr : rows) {
+        if (rr.kind == 0) { rr.c->normal.da = slot(rr.c->b1); rr.c->normal.db = slot(rr.c->b2); }
+        else { rr.c->friction.da = slot(rr.c->b1); rr.c->friction.db = slot(rr.c->b2); }
+    }
+    for (RowRef& rr : rows) {
+        Contact* c = rr.c;
+        if (rr.kind == 0) {
+            Row<1>& r = c->normal;
+            double cur = r.value(velAng(r.a->getVel(), r.a->getAngVel()), velAng(r.b->getVel(), r.b->getAngVel())).v[0];
+            r.target.v[0] = (cur < -c->cutoff) ? -(1 + c->bounce) * cur : -cur;
+        } else {
+            Row<2>& r = c->friction;
+            r.target = -r.value(velAng(r.a->getVel(), r.a->getAngVel()), velAng(r.b->getVel(), r.b->getAngVel()));
+        }
+    }
+    for (RowRef& rr : rows) {
+        if (rr.kind == 0) { Row<1>& r = rr.c->normal; if (!r.impulse.isZero()) r.applyImpulse(r.impulse, &r.da->v, &r.db->v); }
+        else { Row<2>& r = rr.c->friction; if (!r.impulse.isZero()) r.applyImpulse(r.impulse, &r.da->v, &r.db->v); }
+    }
+    auto projN = [](const Vec<1>& x) { Vec<1> o; o.v[0] = std::max<double>(x.v[0], 0); return o; };
+    for (int it = 0; it < n_vel; it++) {
+        for (RowRef& rr : rows) {
+            Contact* c = rr.c;
+            if (rr.kind == 0) pgsStep(c->normal, false, projN);
+            else {
+                pgsStep(c->friction, false, [c](const Vec<2>& x) {
+                    double mx = c->friction_coeff * std::min<double>(std::numeric_limits<double>::infinity(), c->normal.impulse.v[0]);
+                    double mag = std::sqrt(x.v[0] * x.v[0] + x.v[1] * x.v[1]);
+                    if (mag > mx) {
+                        c->static_ready = false;
+                        double r = mx / mag;
+                        Vec<2> o; o.v[0] = x.v[0] * r; o.v[1] = x.v[1] * r;
+                        return o;
+                    }
+                    c->static_ready = true;
+                    return x;
+                });
+            }
+        }
+    }
+    for (int it = 0; it < n_pos; it++)
+        for (RowRef& rr : rows)
+            if (rr.kind == 0) pgsStep(rr.c->normal, true, projN);
+    // PhysicsEngine::applyVelocityChange (PhysicsEngine.cpp:1113-1136)
+    for (auto& kv : dv) {
+        Body* b = kv.first;
+        if (b->movement != DYNAMIC) continue;
+        const DV& d = *kv.second;
+        b->vel += V3(d.v.v[0], d.v.v[1], d.v.v[2]);
+        b->ang_vel += V3(d.v.v[3], d.v.v[4], d.v.v[5]);
+        b->pvel += V3(d.pv.v[0], d.pv.v[1], d.pv.v[2]);
+        b->pang_vel += V3(d.pv.v[3], d.pv.v[4], d.pv.v[5]);
+    }
+}
+
+// -------------------------------------------------------------- step ----
+void World::step() {
+    // gravity once per step (PhysicsEngine.cpp:65-87)
+    for (auto& b : bodies)
+        if (b->movement == DYNAMIC) b->vel += p.g * p.dt;
+
+    // broadphase: every pair whose true AABBs overlap (AABB_Tree.h:153-224)
+    last_pairs.clear();
+    for (size_t i = 0; i < bodies.size(); i++)
+        for (size_t j = i + 1; j < bodies.size(); j++)
+            if (AABB::overlap(bodies[i]->aabb, bodies[j]->aabb)) last_pairs.push_back({bodies[i]->id, bodies[j]->id});
+
+    // narrowphase + contact persistence (PhysicsEngine.cpp:167-326)
+    for (auto& pr : last_pairs) {
+        Body* b1 = bodies[pr.first - 1].get();
+        Body* b2 = bodies[pr.second - 1].get();
+        if (!(b1->movement == DYNAMIC || b2->movement == DYNAMIC)) continue;
+        Manifold man = satPolyPoly(b1->shape, b1->id, b1->mat, b2->shape, b2->id, b2->mat);
+        if (!(man.max_pen > 0)) continue;
+        Manifold m = cullManifold(man, 4);
+        getOrCreateEdge(b1, b2);
+        for (const ManifoldPoint& mp : m.pts) addContact(b1, b2, mp, m.normal);
+    }
+
+    // islands in constraint_graph_nodes iteration order (PhysicsEngine.cpp:1536-1613)
+    std::vector<std::vector<RowRef>> islands;
+    std::set<Body*> visited;
+    for (auto& kv : nodes) {
+        Body* n = kv.second;
+        if (n->movement != DYNAMIC || visited.count(n)) continue;
+        std::vector<RowRef> rows;
+        std::vector<Body*> stack{n};
+        while (!stack.empty()) {
+            Body* cur = stack.back();
+            stack.pop_back();
+            if (!visited.insert(cur).second) continue;
+            if (cur->movement == DYNAMIC) {
+                for (Edge* e : adj[cur]) {
+                    Body* o = e->other(cur);
+                    if (visited.count(o)) continue;
+                    for (auto& c : e->contacts)
+                        if (c->live) { rows.push_back({0, c.get()}); rows.push_back({1, c.get()}); }
+                }
+            }
+            for (Edge* e : adj[cur]) {
+                Body* o = e->other(cur);
+                if (o->movement == DYNAMIC && !visited.count(o)) stack.push_back(o);
+            }
+        }
+        if (!rows.empty()) islands.push_back(std::move(rows));
+    }
+
+    // substeps (PhysicsEngine.cpp:368-420)
+    double dts = p.dt / p.substeps;
+    for (int s = 0; s < p.substeps; s++) {
+        bool first = s == 0, last = s == p.substeps - 1;
+        std::vector<Edge*> dead;
+        for (auto& e : edges) {
+            for (auto& c : e->contacts) {
+                bool skip = !c->live;
+                if (last) { c->life--; c->live = false; }
+                if (skip) continue;
+                rebuildContact(c.get(), p, dts);
+            }
+            if (first) {
+                auto& v = e->contacts;
+                v.erase(std::remove_if(v.begin(), v.end(), [](const std::unique_ptr<Contact>& c) { return c->life < 0; }), v.end());
+                if (v.empty()) dead.push_back(e.get());
+            }
+        }
+        for (Edge* e : dead) deleteEdge(e);
+        for (auto& rows : islands) pgsSolve(rows, p.pgs_vel, p.pgs_pos);
+        for (auto& bp : bodies) {
+            Body* b = bp.get();
+            if (b->movement == FIXED) continue;
+            b->prev_com = b->com;
+            b->prev_q = b->q;
+            b->com += (b->vel + b->pvel) * dts;
+            if (b->ang_vel.mag2() != 0) {
+                bool no_gyro = p.gyro_disabled || b->movement == KINEMATIC;
+                b->rotateWithGyro(dts, p.angle_ticks, no_gyro);
+                V3 pr = b->pang_vel;
+                b->q = Q::axisAngle(dts * pr.mag(), pr) * b->q;
+            }
+            b->pvel = V3();
+            b->pang_vel = V3();
+            b->updateInertiaTensor();
+        }
+    }
+    for (auto& bp : bodies) {
+        Body* b = bp.get();
+        if (b->movement == FIXED) continue;
+        if (b->com != b->prev_com || b->q != b->prev_q) b->updateGeometry();
+    }
+}
+
+}  // namespace cport
+
+// ================================================================ C ABI ====
+using namespace cport;
+
+namespace {
+thread_local std::string g_err;
+int fail(const char* m, int code = CPGPU_ERR_INVALID_ARG) { g_err = m; return code; }
+World* W(cpgpu_world* w) { return reinterpret_cast<World*>(w); }
+Body* B(cpgpu_world* w, uint32_t id) {
+    World* x = W(w);
+    if (id == 0 || id > x->bodies.size()) return nullptr;
+    return x->bodies[id - 1].get();
+}
+Material mat(const cpgpu_material* m) {
+    Material o;
+    if (m) { o.density = m->density; o.restitution = m->restitution; o.kinetic = m->kinetic_friction; o.stat = m->static_friction; }
+    return o;
+}
+V3 v3(const double* p) { return p ? V3(p[0], p[1], p[2]) : V3(); }
+void cutoff(World* w) { w->p.cutoff_vel = 2 * w->p.g.mag() * w->p.dt; }  // PhysicsEngine.h:203
+}  // namespace
+
+extern "C" {
+
+const char* cport_last_error(void) { return g_err.c_str(); }
+int cport_world_create(cpgpu_world** out) {
+    World* w = new World();
+    w->p.sleeping = false;  // the restatement implements the sleeping-disabled path
+    *out = reinterpret_cast<cpgpu_world*>(w);
+    return CPGPU_OK;
+}
+int cport_world_destroy(cpgpu_world* w) { delete W(w); return CPGPU_OK; }
+int cport_set_step_time(cpgpu_world* w, double dt) { W(w)->p.dt = dt; cutoff(W(w)); return CPGPU_OK; }
+int cport_set_gravity(cpgpu_world* w, double x, double y, double z) { W(w)->p.g = V3(x, y, z); cutoff(W(w)); return CPGPU_OK; }
+int cport_set_substep_count(cpgpu_world* w, int s) { if (s < 1) return fail("substeps < 1"); W(w)->p.substeps = s; return CPGPU_OK; }
+int cport_set_pgs_iterations(cpgpu_world* w, int v, int p, int h) { W(w)->p.pgs_vel = v; W(w)->p.pgs_pos = p; W(w)->p.pgs_holo = h; return CPGPU_OK; }
+int cport_set_sleeping_enabled(cpgpu_world* w, int e) {
+    if (e) return fail("sleeping is not implemented", CPGPU_ERR_UNSUPPORTED);
+    W(w)->p.sleeping = false;
+    return CPGPU_OK;
+}
+int cport_set_warm_start_disabled(cpgpu_world* w, int d) { W(w)->p.warm_start_disabled = d != 0; return CPGPU_OK; }
+int cport_set_global_cfm(cpgpu_world* w, double c) { W(w)->p.cfm = c; return CPGPU_OK; }
+int cport_set_angle_vel_update_tick_count(cpgpu_world* w, int n) { W(w)->p.angle_ticks = n; return CPGPU_OK; }
+int cport_set_internal_gyro_forces_disabled(cpgpu_world* w, int d) { W(w)->p.gyro_disabled = d != 0; return CPGPU_OK; }
+
+int cport_body_hull(cpgpu_world* w, const double* points, int n_points, const int* face_offsets, const int* face_indices,
+                    int n_faces, const cpgpu_material* m, int movement, const double pos[3], uint32_t* out_id) {
+    if (n_points < 4 || n_faces < 4) return fail("hull needs >= 4 points and faces");
+    std::vector<V3> pts(n_points);
+    for (int i = 0; i < n_points; i++) pts[i] = V3(points[3 * i], points[3 * i + 1], points[3 * i + 2]);
+    std::vector<std::vector<int>> faces(n_faces);
+    for (int f = 0; f < n_faces; f++)
+        for (int k = face_offsets[f]; k < face_offsets[f + 1]; k++) faces[f].push_back(face_indices[k]);
+    Body* b = W(w)->addHull(pts, faces, mat(m), movement, v3(pos));
+    if (out_id) *out_id = b->id;
+    return CPGPU_OK;
+}
+// ConvexUnionGeometry::box (Geometry.cpp:14-37)
+int cport_body_box(cpgpu_world* w, const double c[3], double dx, double dy, double dz, const cpgpu_material* m,
+                   int movement, const double pos[3], uint32_t* out_id) {
+    V3 p = v3(c);
+    std::vector<V3> pts = {V3(p.x, p.y, p.z), V3(p.x + dx, p.y, p.z), V3(p.x + dx, p.y + dy, p.z), V3(p.x, p.y + dy, p.z),
+                           V3(p.x, p.y, p.z + dz), V3(p.x + dx, p.y, p.z + dz), V3(p.x + dx, p.y + dy, p.z + dz), V3(p.x, p.y + dy, p.z + dz)};
+    std::vector<std::vector<int>> faces = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+    Body* b = W(w)->addHull(pts, faces, mat(m), movement, v3(pos));
+    if (out_id) *out_id = b->id;
+    return CPGPU_OK;
+}
+int cport_body_sphere(cpgpu_world*, const double*, double, const cpgpu_material*, int, const double*, uint32_t*) {
+    return fail("spheres are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+}
+int cport_body_cylinder(cpgpu_world*, const double*, double, double, const cpgpu_material*, int, const double*, uint32_t*) {
+    return fail("cylinders are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+}
+int cport_body_mesh(cpgpu_world*, const double*, int, const int*, int, const cpgpu_material*, int, uint32_t*) {
+    return fail("static meshes are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+}
+int cport_body_set_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {
+    Body* b = B(w, id); if (!b) return fail("bad id"); b->vel = v3(v); return CPGPU_OK;
+}
+int cport_body_set_ang_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {
+    Body* b = B(w, id); if (!b) return fail("bad id"); b->ang_vel = v3(v); return CPGPU_OK;
+}
+// RigidBody::setOrientation (RigidBody.cpp:103-107): the world inertia tensor is
+// left as it was until the next integration
+int cport_body_set_orientation(cpgpu_world* w, uint32_t id, const double q[4]) {
+    Body* b = B(w, id); if (!b) return fail("bad id");
+    b->q = Q(q[0], q[1], q[2], q[3]);
+    b->updateGeometry();
+    return CPGPU_OK;
+}
+int cport_body_set_position(cpgpu_world* w, uint32_t id, const double p[3]) {
+    Body* b = B(w, id); if (!b) return fail("bad id");
+    b->com += v3(p) - b->trackedP(0);
+    b->updateGeometry();
+    return CPGPU_OK;
+}
+// RigidBody::setMass (RigidBody.cpp:80-89)
+int cport_body_set_mass(cpgpu_world* w, uint32_t id, double m) {
+    Body* b = B(w, id); if (!b) return fail("bad id");
+    double r = m / b->mass;
+    b->ref_tensor *= r; b->ref_inv_tensor /= r; b->tensor *= r; b->inv_tensor /= r;
+    b->mass = m;
+    return CPGPU_OK;
+}
+int cport_add_ball_socket(cpgpu_world*, uint32_t, uint32_t, const double*, const double*, double, uint32_t*) {
+    return fail("joints are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+}
+int cport_add_hinge(cpgpu_world*, uint32_t, uint32_t, const double*, const double*, const double*, const double*, double, double, uint32_t*) {
+    return fail("joints are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+}
+// Test hook: replace the mass properties computed at creation by given ones
+// (the reference's, so that both engines start from bit-identical bodies).
+// Valid right after the body was created.
+int cport_body_set_mass_properties(cpgpu_world* w, uint32_t id, double mass, const double* com_geom, const double* tensor) {
+    Body* b = B(w, id); if (!b) return fail("bad id");
+    M3 t;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) t.m[i][j] = tensor[3 * i + j];
+    W(w)->placeBody(b, mass, v3(com_geom), t);
+    return CPGPU_OK;
+}
+int cport_step(cpgpu_world* w, int n) { for (int i = 0; i < n; i++) W(w)->step(); return CPGPU_OK; }
+int cport_num_bodies(cpgpu_world* w, int* n) { *n = (int)W(w)->bodies.size(); return CPGPU_OK; }
+int cport_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel, double* ang) {
+    World* x = W(w);
+    for (size_t i = 0; i < x->bodies.size(); i++) {
+        const Body* b = x->bodies[i].get();
+        V3 v = b->getVel(), a = b->getAngVel();
+        if (com) { com[3 * i] = b->com.x; com[3 * i + 1] = b->com.y; com[3 * i + 2] = b->com.z; }
+        if (quat) { quat[4 * i] = b->q.r; quat[4 * i + 1] = b->q.i; quat[4 * i + 2] = b->q.j; quat[4 * i + 3] = b->q.k; }
+        if (vel) { vel[3 * i] = v.x; vel[3 * i + 1] = v.y; vel[3 * i + 2] = v.z; }
+        if (ang) { ang[3 * i] = a.x; ang[3 * i + 1] = a.y; ang[3 * i + 2] = a.z; }
+    }
+    return CPGPU_OK;
+}
+// State import: poses and velocities, then the derived tensors and geometry
+// are recomputed from the new poses.
+int cport_set_body_state(cpgpu_world* w, const double* com, const double* quat, const double* vel, const double* ang) {
+    World* x = W(w);
+    for (size_t i = 0; i < x->bodies.size(); i++) {
+        Body* b = x->bodies[i].get();
+        if (com) b->com = V3(com[3 * i], com[3 * i + 1], com[3 * i + 2]);
+        if (quat) b->q = Q(quat[4 * i], quat[4 * i + 1], quat[4 * i + 2], quat[4 * i + 3]);
+        if (vel) b->vel = V3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+        if (ang) b->ang_vel = V3(ang[3 * i], ang[3 * i + 1], ang[3 * i + 2]);
+        if (b->movement != FIXED) b->updateInertiaTensor();
+        b->updateGeometry();
+    }
+    return CPGPU_OK;
+}
+int cport_get_aabbs(cpgpu_world* w, double* out) {
+    World* x = W(w);
+    for (size_t i = 0; i < x->bodies.size(); i++) {
+        const AABB& a = x->bodies[i]->aabb;
+        double* o = out + 6 * i;
+        o[0] = a.mn.x; o[1] = a.mn.y; o[2] = a.mn.z; o[3] = a.mx.x; o[4] = a.mx.y; o[5] = a.mx.z;
+    }
+    return CPGPU_OK;
+}
+int cport_get_pairs(cpgpu_world* w, uint32_t* pairs, int cap, int* n) {
+    World* x = W(w);
+    *n = (int)x->last_pairs.size();
+    for (int i = 0; i < *n && i < cap; i++) { pairs[2 * i] = x->last_pairs[i].first; pairs[2 * i + 1] = x->last_pairs[i].second; }
+    return CPGPU_OK;
+}
+int cport_get_contacts(cpgpu_world* w, cpgpu_contact* out, int cap, int* n) {
+    World* x = W(w);
+    std::vector<std::pair<std::pair<uint32_t, uint32_t>, Edge*>> es;
+    for (auto& e : x->edges) {
+        uint32_t a = e->n1->id, b = e->n2->id;
+        es.push_back({{std::min(a, b), std::max(a, b)}, e.get()});
+    }
+    std::sort(es.begin(), es.end(), [](const auto& p, const auto& q) { return p.first < q.first; });
+    int k = 0;
+    for (auto& pe : es) {
+        for (auto& c : pe.second->contacts) {
+            if (out && k < cap) {
+                cpgpu_contact& o = out[k];
+                std::memset(&o, 0, sizeof(o));
+                o.b1 = c->b1->id; o.b2 = c->b2->id;
+                o.live = c->live; o.memory_life = c->life;
+                o.magic_c = c->magic_c; o.magic_b = c->magic_b;
+                const V3* vs[3] = {&c->p1_local, &c->p2_local, &c->n_local};
+                double* ds[3] = {o.p_local_b1, o.p_local_b2, o.n_local_b1};
+                for (int t = 0; t < 3; t++) { ds[t][0] = vs[t]->x; ds[t][1] = vs[t]->y; ds[t][2] = vs[t]->z; }
+                o.pen_depth = c->pen; o.bounce = c->bounce; o.friction_coeff = c->friction_coeff;
+                o.normal_impulse = c->normal.impulse.v[0];
+                o.friction_impulse[0] = c->friction.impulse.v[0]; o.friction_impulse[1] = c->friction.impulse.v[1];
+                o.friction_u[0] = c->fu.x; o.friction_u[1] = c->fu.y; o.friction_u[2] = c->fu.z;
+                o.friction_w[0] = c->fw.x; o.friction_w[1] = c->fw.y; o.friction_w[2] = c->fw.z;
+                o.static_ready = c->static_ready;
+            }
+            k++;
+        }
+    }
+    *n = k;
+    return CPGPU_OK;
+}
+// State import of the persistent contact graph (same layout and order as
+// cport_get_contacts); edges without contacts are dropped.
+int cport_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n) {
+    World* x = W(w);
+    std::vector<Edge*> all;
+    for (auto& e : x->edges) all.push_back(e.get());
+    for (Edge* e : all) x->deleteEdge(e);
+    for (int k = 0; k < n; k++) {
+        const cpgpu_contact& r = in[k];
+        Body* b1 = B(w, r.b1);
+        Body* b2 = B(w, r.b2);
+        if (!b1 || !b2 || r.b1 >= r.b2) return fail("bad contact body ids");
+        Edge* e = x->getOrCreateEdge(b1, b2);
+        auto c = std::make_unique<Contact>();
+        c->b1 = b1; c->b2 = b2;
+        c->p1_local = v3(r.p_local_b1); c->p2_local = v3(r.p_local_b2); c->n_local = v3(r.n_local_b1);
+        c->pen = r.pen_depth; c->bounce = r.bounce; c->hardness = x->p.hardness; c->friction_coeff = r.friction_coeff;
+        c->cutoff = x->p.cutoff_vel;
+        c->magic_c = r.magic_c; c->magic_b = r.magic_b;
+        c->life = r.memory_life; c->live = r.live != 0;
+        c->normal.impulse.v[0] = r.normal_impulse;
+        c->friction.impulse.v[0] = r.friction_impulse[0]; c->friction.impulse.v[1] = r.friction_impulse[1];
+        c->fu = v3(r.friction_u); c->fw = v3(r.friction_w);
+        c->static_ready = r.static_ready != 0;
+        e->contacts.push_back(std::move(c));
+    }
+    return CPGPU_OK;
+}
+
+}  // extern "C"
