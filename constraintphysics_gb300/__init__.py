@@ -1,0 +1,91 @@
+"""GB300 per-step contact path of the ConstraintPhysics rigid-body engine.
+
+The compute lives in libcpgpu.so (hand-written sm_103a CUDA behind the C ABI
+of include/cpgpu.h, built in-tree by constraintphysics_gb300.build).  This
+package only loads that library and wraps it for Python callers:
+
+  world()            a new PhysicsEngine-like world (constraintphysics_gb300.world.World)
+  Batch(worlds)      independent worlds packed into one device batch
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+present, the calls raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from ._abi import bind
+from .world import CPGPUError, World
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcpgpu.so")
+_ABI = None
+
+
+def lib():
+    """The bound product library (raises if it was not built)."""
+    global _ABI
+    if _ABI is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is not built: run constraintphysics_gb300.build.build()")
+        handle = ctypes.CDLL(LIB_PATH)
+        abi = bind(handle, "cpgpu_")
+        fn = handle.cpgpu_batch_step_timed
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        abi.batch_step_timed = fn
+        abi._lib = handle
+        _ABI = abi
+    return _ABI
+
+
+def world():
+    return World(lib())
+
+
+class Batch:
+    """Independent worlds advanced together by one launch sequence per step."""
+
+    def __init__(self, worlds):
+        self.abi = lib()
+        arr = (ctypes.c_void_p * len(worlds))(*[w.h.value for w in worlds])
+        h = ctypes.c_void_p()
+        self._check(self.abi.batch_create(arr, len(worlds), ctypes.byref(h)))
+        self.h = h
+        self.sizes = [w.n_bodies for w in worlds]
+
+    def _check(self, rc):
+        if rc != 0:
+            raise CPGPUError(f"status {rc}: {self.abi.last_error().decode(errors='replace')}")
+
+    def step(self, n=1):
+        self._check(self.abi.batch_step(self.h, int(n)))
+
+    def step_timed(self, n=1):
+        ms = ctypes.c_double()
+        self._check(self.abi.batch_step_timed(self.h, int(n), ctypes.addressof(ms)))
+        return ms.value
+
+    def state(self, wi):
+        n = self.sizes[wi]
+        com = np.zeros((n, 3)); quat = np.zeros((n, 4)); vel = np.zeros((n, 3)); ang = np.zeros((n, 3))
+        self._check(self.abi.batch_get_body_state(self.h, int(wi), com.ctypes.data, quat.ctypes.data,
+                                                  vel.ctypes.data, ang.ctypes.data))
+        return {"com": com, "quat": quat, "vel": vel, "ang_vel": ang}
+
+    def info(self):
+        nb, nw, nc = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.abi.batch_info(self.h, ctypes.addressof(nb), ctypes.addressof(nw), ctypes.addressof(nc)))
+        return {"bodies": nb.value, "worlds": nw.value, "contacts": nc.value}
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.abi.batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,175 @@
+// broadphase.cu — gravity, candidate pairs, geometry/AABB update and the
+// device-counted exclusive scan used by the graph kernels.
+//
+// Pair generation returns exactly the set the reference's AABB tree returns:
+// every pair of bodies of the same world whose true AABBs overlap under the
+// inclusive test of AABB::intersects (ConstraintPhysics/src/AABB.h:10-14; the
+// tree query AABB_Tree.h:153-224 visits every overlapping leaf pair once).
+// Pairs are emitted as (lower id, higher id) sorted by (a, b): one thread per
+// body counts its overlaps with the later bodies of its world, an exclusive
+// scan gives each body its output offset, and a second pass writes.
+#include "kernels.cuh"
+#include "devmath.cuh"
+
+namespace cpgpu {
+
+namespace {
+constexpr int kScanBlock = 1024;
+
+__device__ __forceinline__ bool overlap(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+    return !(ahi.x < blo.x || alo.x > bhi.x || ahi.y < blo.y || alo.y > bhi.y || ahi.z < blo.z || alo.z > bhi.z);
+}
+
+// inclusive block scan of one value per thread (blockDim.x == kScanBlock)
+__device__ int block_scan_incl(int v, int* warp_sums) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) warp_sums[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        int s = (lane < (blockDim.x >> 5)) ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += t;
+        }
+        warp_sums[lane] = s;
+    }
+    __syncthreads();
+    if (wid > 0) v += warp_sums[wid - 1];
+    __syncthreads();
+    return v;
+}
+
+__global__ void k_scan_chunks(const int* in, int* out, const int* n_dev, int n_host, int* chunk_sums) {
+    __shared__ int ws[32];
+    const int n = n_dev ? *n_dev : n_host;
+    const int nchunks = (n + kScanBlock - 1) / kScanBlock;
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        int i = c * kScanBlock + threadIdx.x;
+        int v = (i < n) ? in[i] : 0;
+        int inc = block_scan_incl(v, ws);
+        if (i < n) out[i] = inc - v;
+        if (threadIdx.x == kScanBlock - 1) chunk_sums[c] = inc;
+    }
+}
+
+__global__ void k_scan_top(int* chunk_sums, const int* n_dev, int n_host, int* total) {
+    __shared__ int ws[32];
+    __shared__ int carry;
+    const int n = n_dev ? *n_dev : n_host;
+    const int nchunks = (n + kScanBlock - 1) / kScanBlock;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nchunks; base += kScanBlock) {
+        int i = base + threadIdx.x;
+        int v = (i < nchunks) ? chunk_sums[i] : 0;
+        int inc = block_scan_incl(v, ws);
+        int c0 = carry;
+        if (i < nchunks) chunk_sums[i] = c0 + inc - v;
+        __syncthreads();
+        if (threadIdx.x == kScanBlock - 1) carry = c0 + inc;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(int* out, const int* n_dev, int n_host, const int* chunk_sums) {
+    const int n = n_dev ? *n_dev : n_host;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] += chunk_sums[i / kScanBlock];
+}
+
+__global__ void k_gravity(Dev d) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
+        if (d.movement[i] != 0) continue;
+        const WorldParams& p = d.wparams[d.world[i]];
+        float4 v = d.vel[i];
+        // vel += gravity * step_time (PhysicsEngine.cpp:85)
+        v.x += p.gx * p.dt; v.y += p.gy * p.dt; v.z += p.gz * p.dt;
+        d.vel[i] = v;
+    }
+}
+
+__global__ void k_pairs(Dev d, int write) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
+        const int end = d.world_start[d.world[i] + 1];
+        const float4 lo = d.aabb_lo[i], hi = d.aabb_hi[i];
+        if (!write) {
+            int c = 0;
+            for (int j = i + 1; j < end; j++) c += overlap(lo, hi, d.aabb_lo[j], d.aabb_hi[j]);
+            d.pair_count[i] = c;
+        } else {
+            int o = d.pair_count[i];
+            for (int j = i + 1; j < end; j++) {
+                if (overlap(lo, hi, d.aabb_lo[j], d.aabb_hi[j])) {
+                    if (o < d.cap_pairs) { d.pair_a[o] = i; d.pair_b[o] = j; }
+                    o++;
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_clamp_pairs(Dev d) {
+    if (*d.n_pairs > d.cap_pairs) { atomicOr(d.status, ST_PAIR_OVERFLOW); *d.n_pairs = d.cap_pairs; }
+}
+
+// RigidBody::updateGeometry (RigidBody.cpp:281-312) for moved bodies: the
+// orientation is renormalised and the AABB recomputed from the world vertices
+// (Polyhedron::gen_AABB, ConvexPrimitive.cpp:660-676).
+__global__ void k_geometry(Dev d, int force_all) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
+        if (!force_all && (d.movement[i] == 1 || !d.moved[i])) continue;
+        float4 q = d.rot[i];
+        q = qnormalize(q);
+        d.rot[i] = q;
+        M33 R = quatRot(q);
+        f3 c = mk(d.pos[i]);
+        const uint8_t* blob = d.shapes + d.shape[i];
+        const HullHeader* H = reinterpret_cast<const HullHeader*>(blob);
+        const float4* v = reinterpret_cast<const float4*>(blob + sizeof(HullHeader));
+        f3 mn = mk(INFINITY, INFINITY, INFINITY), mx = mk(-INFINITY, -INFINITY, -INFINITY);
+        for (int k = 0; k < H->nv; k++) {
+            f3 p = c + mul(R, mk(v[k]));
+            mn.x = fminf(mn.x, p.x); mn.y = fminf(mn.y, p.y); mn.z = fminf(mn.z, p.z);
+            mx.x = fmaxf(mx.x, p.x); mx.y = fmaxf(mx.y, p.y); mx.z = fmaxf(mx.z, p.z);
+        }
+        d.aabb_lo[i] = make_float4(mn.x, mn.y, mn.z, 0.f);
+        d.aabb_hi[i] = make_float4(mx.x, mx.y, mx.z, 0.f);
+    }
+}
+}  // namespace
+
+void scan_exclusive(const int* in, int* out, const int* n_dev, int n_host, int cap, int* total, int* tmp, const Launch& L) {
+    int max_chunks = (cap + kScanBlock - 1) / kScanBlock;
+    int g = max_chunks < L.n_sms * 2 ? (max_chunks > 0 ? max_chunks : 1) : L.n_sms * 2;
+    k_scan_chunks<<<g, kScanBlock, 0, L.st>>>(in, out, n_dev, n_host, tmp);
+    k_scan_top<<<1, kScanBlock, 0, L.st>>>(tmp, n_dev, n_host, total);
+    k_scan_add<<<L.n_sms * 4, 256, 0, L.st>>>(out, n_dev, n_host, tmp);
+}
+
+static int grid_for(int n, int per_block, int n_sms) {
+    int g = (n + per_block - 1) / per_block;
+    int cap = n_sms * 8;
+    return g < 1 ? 1 : (g > cap ? cap : g);
+}
+
+void launch_gravity(const Dev& d, const Launch& L) {
+    k_gravity<<<grid_for(d.n_bodies, 256, L.n_sms), 256, 0, L.st>>>(d);
+}
+
+void launch_pairs(const Dev& d, const Launch& L) {
+    int g = grid_for(d.n_bodies, 128, L.n_sms);
+    k_pairs<<<g, 128, 0, L.st>>>(d, 0);
+    scan_exclusive(d.pair_count, d.pair_count, nullptr, d.n_bodies, d.n_bodies, d.n_pairs, d.scan_tmp, L);
+    k_pairs<<<g, 128, 0, L.st>>>(d, 1);
+    k_clamp_pairs<<<1, 1, 0, L.st>>>(d);
+}
+
+void launch_geometry(const Dev& d, int force_all, const Launch& L) {
+    k_geometry<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d, force_all);
+}
+
+}  // namespace cpgpu

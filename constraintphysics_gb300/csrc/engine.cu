@@ -1,0 +1,1033 @@
+// engine.cu — host side of the device path: worlds, batches, upload/download,
+// the per-step launch sequence (captured in CUDA graphs) and the C ABI of
+// include/cpgpu.h.
+//
+// A cpgpu_world mirrors one phyz::PhysicsEngine (PhysicsEngine.h:60-161): the
+// host keeps its bodies, shapes and parameters; the dynamic state lives on the
+// device once the world has stepped.  Mutations between steps pull the state
+// back, change the host mirror and re-upload on the next step.  A batch packs
+// many worlds into one set of segmented device arrays.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "hull.hpp"
+#include "kernels.cuh"
+
+extern "C" {
+#include "../../include/cpgpu.h"
+}
+
+namespace cpgpu {
+
+thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                            \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) throw CudaFail(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct CudaFail {
+    std::string msg;
+    explicit CudaFail(std::string m) : msg(std::move(m)) {}
+};
+struct ApiFail {
+    int code;
+    std::string msg;
+};
+
+// ---------------------------------------------------------------- host mirror ----
+struct Quat { double r = 1, i = 0, j = 0, k = 0; };
+
+static D3 qrot(const Quat& q, const D3& v) {
+    double r = q.r, i = q.i, j = q.j, k = q.k;
+    return D3(v.x * (r * r + i * i - j * j - k * k) + v.y * (2 * i * j - 2 * r * k) + v.z * (2 * i * k + 2 * r * j),
+              v.x * (2 * i * j + 2 * r * k) + v.y * (r * r - i * i + j * j - k * k) + v.z * (2 * j * k - 2 * r * i),
+              v.x * (2 * i * k - 2 * r * j) + v.y * (2 * j * k + 2 * r * i) + v.z * (r * r - i * i - j * j + k * k));
+}
+static Quat qnorm(const Quat& q) {
+    double m = std::sqrt(q.r * q.r + q.i * q.i + q.j * q.j + q.k * q.k);
+    return Quat{q.r / m, q.i / m, q.j / m, q.k / m};
+}
+
+static void inv3(const double a[9], double o[9]) {
+    double A = a[0], B = a[1], C = a[2], D = a[3], E = a[4], F = a[5], G = a[6], H = a[7], I = a[8];
+    double dt = A * (E * I - F * H) - B * (D * I - F * G) + C * (D * H - E * G);
+    o[0] = (E * I - F * H) / dt; o[1] = (C * H - B * I) / dt; o[2] = (B * F - C * E) / dt;
+    o[3] = (F * G - D * I) / dt; o[4] = (A * I - C * G) / dt; o[5] = (C * D - A * F) / dt;
+    o[6] = (D * H - E * G) / dt; o[7] = (B * G - A * H) / dt; o[8] = (A * E - B * D) / dt;
+}
+
+struct Shape {
+    std::vector<uint8_t> blob;   // 16-byte multiple
+    int hot = 0;                 // bytes staged to shared memory
+};
+
+struct Body {
+    int shape = 0;
+    int movement = CPGPU_DYNAMIC;
+    double mass = 0;
+    D3 com, vel, angv;
+    Quat q;
+    double iref[9], iinv_ref[9], iw[9], iinv[9];
+    D3 local_origin;             // tracked geometry origin (RigidBody.cpp:32-33)
+    double rest = 0.3, kin = 0.6, sta = 1.1;
+};
+
+struct Params {
+    double dt = 1.0 / 90;
+    D3 g = D3(0, -6, 0);
+    int substeps = 8, pgs_vel = 4, pgs_pos = 1, pgs_holo = 1;
+    double cfm = 0.0000025;
+    int contact_life = 6;
+    double hardness = 1000;
+    int angle_ticks = 4;
+    bool gyro_disabled = false, warm_disabled = false;
+    double cutoff = 0;           // 2|g|dt, set by setStep_time / setGravity
+};
+
+struct Batch;
+
+struct World {
+    Params p;
+    std::vector<Shape> shapes;
+    std::vector<Body> bodies;
+    std::unordered_map<unsigned int, int> nodes;   // same insert sequence as constraint_graph_nodes
+    std::vector<cpgpu_contact> contacts;           // host copy of the contact graph
+    std::vector<uint32_t> last_pairs;
+    std::unique_ptr<Batch> dev;
+    bool dev_valid = false;
+};
+
+// ---------------------------------------------------------------- shape packing ----
+static void put16(std::vector<uint8_t>& b) { while (b.size() % 16) b.push_back(0); }
+template <class T>
+static void put(std::vector<uint8_t>& b, const T& v) {
+    size_t o = b.size();
+    b.resize(o + sizeof(T));
+    std::memcpy(b.data() + o, &v, sizeof(T));
+}
+
+// Packs a prepared hull (reference frame = centred on `com`) into the blob the
+// kernels read.  Hot sections first (header, vertices, normals, cache, arcs).
+static Shape pack_hull(const HullPrep& h, const D3& com) {
+    if ((int)h.pts.size() > kMaxHullVerts || (int)h.faces.size() > kMaxHullFaces || (int)h.edges.size() > kMaxHullEdges ||
+        (int)h.arcs.size() > kMaxHullEdges)
+        throw ApiFail{CPGPU_ERR_UNSUPPORTED, "hull too large (limit 255 vertices / faces / edges)"};
+    HullHeader H;
+    std::memset(&H, 0, sizeof(H));
+    H.nv = (uint16_t)h.pts.size();
+    H.nf = (uint16_t)h.faces.size();
+    H.ne = (uint16_t)h.edges.size();
+    H.na = (uint16_t)h.arcs.size();
+    std::vector<uint8_t> b(sizeof(HullHeader));
+    double rad = 0;
+    for (const D3& p : h.pts) {
+        D3 q = p - com;
+        rad = std::max(rad, q.mag());
+        put(b, make_float4((float)q.x, (float)q.y, (float)q.z, 0.f));
+    }
+    H.off_norm = (uint16_t)b.size();
+    for (size_t f = 0; f < h.faces.size(); f++)
+        put(b, make_float4((float)h.gn[f].x, (float)h.gn[f].y, (float)h.gn[f].z, h.redundant[f] ? 1.f : 0.f));
+    H.off_cache = (uint16_t)b.size();
+    for (size_t f = 0; f < h.faces.size(); f++) {
+        // recentred extrema (CollisionDetect.cpp:622-625): shift by the change of
+        // the reference point's projection between construction frame and COM frame
+        const D3& n = h.gn[f];
+        double shift = n.dot(h.pts[h.ref_idx[f]] - com) - h.ref_val[f];
+        float4 c;
+        c.x = (float)(h.cmax[f] + shift);
+        c.y = (float)(h.cmin[f] + shift);
+        int mx = h.cmax_id[f], mn = h.cmin_id[f];
+        std::memcpy(&c.z, &mx, 4);
+        std::memcpy(&c.w, &mn, 4);
+        put(b, c);
+    }
+    H.off_arc = (uint16_t)b.size();
+    for (auto& a : h.arcs) { b.push_back((uint8_t)a.first); b.push_back((uint8_t)a.second); }
+    put16(b);
+    H.off_fofs = (uint16_t)b.size();  // end of the hot part
+    {
+        uint16_t o = 0;
+        for (auto& f : h.faces) { put(b, o); o = (uint16_t)(o + f.size()); }
+        put(b, o);
+        H.nfi = o;
+        put16(b);
+        H.off_fidx = (uint16_t)b.size();
+        for (auto& f : h.faces) for (int v : f) b.push_back((uint8_t)v);
+        put16(b);
+    }
+    H.off_edge = (uint16_t)b.size();
+    for (auto& e : h.edges) { b.push_back((uint8_t)e.first); b.push_back((uint8_t)e.second); }
+    put16(b);
+    auto csr = [&](const std::vector<std::vector<int>>& lists, uint16_t* off_ofs, uint16_t* off_idx) {
+        *off_ofs = (uint16_t)b.size();
+        uint16_t o = 0;
+        for (auto& l : lists) { put(b, o); o = (uint16_t)(o + l.size()); }
+        put(b, o);
+        put16(b);
+        *off_idx = (uint16_t)b.size();
+        for (auto& l : lists) for (int x : l) b.push_back((uint8_t)x);
+        put16(b);
+    };
+    csr(h.vfaces, &H.off_vfofs, &H.off_vfidx);
+    csr(h.vedges, &H.off_veofs, &H.off_veidx);
+    if (b.size() > (size_t)kMaxHullBlob) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "hull blob too large"};
+    H.size16 = (uint16_t)(b.size() / 16);
+    H.kind = 0;
+    H.radius = (float)rad;
+    std::memcpy(b.data(), &H, sizeof(H));
+    Shape s;
+    s.blob = std::move(b);
+    s.hot = H.off_fofs;
+    return s;
+}
+
+// ---------------------------------------------------------------- device batch ----
+struct Arena {
+    uint8_t* base = nullptr;
+    size_t size = 0, used = 0;
+    template <class T>
+    T* take(size_t n) {
+        used = (used + 255) & ~size_t(255);
+        T* p = reinterpret_cast<T*>(base + used);
+        used += sizeof(T) * std::max<size_t>(n, 1);
+        return p;
+    }
+};
+
+struct Batch {
+    int n_worlds = 0, n_bodies = 0;
+    int substeps = 1;
+    int n_sms = 0;
+    int slot_bytes = 0;
+    cudaStream_t st = nullptr;
+    uint8_t* mem = nullptr;
+    Dev d[2];                  // d[p]: old = buffer p, new = buffer 1-p
+    int parity = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    std::vector<int> world_start;
+    std::vector<uint8_t> movement;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    ~Batch() {
+        for (auto& g : graph) if (g) cudaGraphExecDestroy(g);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (mem) cudaFree(mem);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    const Dev& cur() const { return d[parity]; }      // old buffers hold the current graph
+
+    void launch_step(const Dev& x) {
+        Launch L{n_sms, st};
+        launch_gravity(x, L);
+        launch_pairs(x, L);
+        launch_narrowphase(x, slot_bytes, n_sms, st);
+        launch_merge(x, L);
+        launch_islands(x, L);
+        for (int s = 0; s < substeps; s++) {
+            launch_rows(x, s == 0, s == substeps - 1, L);
+            launch_pgs(x, L);
+            launch_integrate(x, s == substeps - 1, L);
+        }
+        launch_geometry(x, 0, L);
+    }
+
+    void build_graphs() {
+        for (int p = 0; p < 2; p++) {
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            launch_step(d[p]);
+            CK(cudaStreamEndCapture(st, &g));
+            CK(cudaGraphInstantiate(&graph[p], g, 0));
+            cudaGraphDestroy(g);
+        }
+    }
+
+    void step(int n, bool use_graph = true) {
+        for (int i = 0; i < n; i++) {
+            if (use_graph) CK(cudaGraphLaunch(graph[parity], st));
+            else launch_step(d[parity]);
+            parity ^= 1;
+        }
+    }
+
+    int check_status() {
+        int s = 0;
+        CK(cudaMemcpyAsync(&s, d[0].status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (s == 0) return CPGPU_OK;
+        std::string m = "device status";
+        if (s & ST_PAIR_OVERFLOW) m += " pair-capacity-overflow";
+        if (s & ST_EDGE_OVERFLOW) m += " edge-capacity-overflow";
+        if (s & ST_CONTACT_OVERFLOW) m += " contact-capacity-overflow";
+        if (s & ST_CLIP_OVERFLOW) m += " clip-overflow";
+        if (s & ST_STACK_OVERFLOW) m += " island-stack-overflow";
+        if (s & ST_NAN) m += " non-finite-state";
+        if (s & ST_TIMEOUT) m += " bounded-wait-timeout";
+        int code = (s & ST_NAN) ? CPGPU_ERR_NAN : (s & ST_TIMEOUT) ? CPGPU_ERR_TIMEOUT : CPGPU_ERR_CAPACITY;
+        throw ApiFail{code, m};
+    }
+};
+
+static int env_int(const char* name, int dflt) {
+    const char* v = std::getenv(name);
+    return v ? std::atoi(v) : dflt;
+}
+
+static std::vector<int> map_iteration_order(const World& w) {
+    // constraint_graph_nodes iteration order (PhysicsEngine.h:230); ids are 1-based
+    std::vector<int> order;
+    order.reserve(w.nodes.size());
+    for (const auto& kv : w.nodes) order.push_back(kv.second);
+    return order;
+}
+
+static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
+    auto B = std::make_unique<Batch>();
+    B->n_worlds = (int)worlds.size();
+    B->substeps = worlds.empty() ? 1 : worlds[0]->p.substeps;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&B->n_sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&B->ev0));
+    CK(cudaEventCreate(&B->ev1));
+
+    // ---- host packing
+    std::vector<int> wstart{0};
+    int N = 0, n_contacts = 0;
+    for (World* w : worlds) {
+        if (w->p.substeps != B->substeps) throw ApiFail{CPGPU_ERR_INVALID_ARG, "worlds of a batch must use the same substep count"};
+        N += (int)w->bodies.size();
+        wstart.push_back(N);
+        n_contacts += (int)w->contacts.size();
+    }
+    B->n_bodies = N;
+    B->world_start = wstart;
+    std::vector<uint8_t> pool;
+    std::map<std::string, int> dedupe;
+    std::vector<int> shape_off(N);
+    std::vector<float4> pos(N), rot(N), vel(N), angv(N), zero4(N, make_float4(0.f, 0.f, 0.f, 0.f)), mat(N);
+    std::vector<float> iref(9 * (size_t)N), iinv_ref(9 * (size_t)N), iw(9 * (size_t)N), iinv(9 * (size_t)N);
+    std::vector<int> world_of(N), map_order(N);
+    std::vector<uint8_t> movement(N);
+    std::vector<WorldParams> wp(worlds.size());
+    int max_hot = 16;
+    for (size_t wi = 0; wi < worlds.size(); wi++) {
+        World& w = *worlds[wi];
+        std::vector<int> shape_pool_off(w.shapes.size());
+        for (size_t s = 0; s < w.shapes.size(); s++) {
+            const Shape& sh = w.shapes[s];
+            std::string key(reinterpret_cast<const char*>(sh.blob.data()), sh.blob.size());
+            auto it = dedupe.find(key);
+            if (it == dedupe.end()) {
+                int off = (int)pool.size();
+                pool.insert(pool.end(), sh.blob.begin(), sh.blob.end());
+                dedupe.emplace(std::move(key), off);
+                shape_pool_off[s] = off;
+            } else {
+                shape_pool_off[s] = it->second;
+            }
+            max_hot = std::max(max_hot, (sh.hot + 15) & ~15);
+        }
+        const int base = wstart[wi];
+        for (size_t i = 0; i < w.bodies.size(); i++) {
+            const Body& b = w.bodies[i];
+            int g = base + (int)i;
+            shape_off[g] = shape_pool_off[b.shape];
+            bool dyn = b.movement == CPGPU_DYNAMIC;
+            pos[g] = make_float4((float)b.com.x, (float)b.com.y, (float)b.com.z, dyn ? (float)(1.0 / b.mass) : 0.f);
+            rot[g] = make_float4((float)b.q.r, (float)b.q.i, (float)b.q.j, (float)b.q.k);
+            vel[g] = b.movement == CPGPU_FIXED ? zero4[0] : make_float4((float)b.vel.x, (float)b.vel.y, (float)b.vel.z, 0.f);
+            angv[g] = b.movement == CPGPU_FIXED ? zero4[0] : make_float4((float)b.angv.x, (float)b.angv.y, (float)b.angv.z, 0.f);
+            mat[g] = make_float4((float)b.rest, (float)b.kin, (float)b.sta, 0.f);
+            for (int k = 0; k < 9; k++) {
+                iref[9 * (size_t)g + k] = (float)b.iref[k];
+                iinv_ref[9 * (size_t)g + k] = (float)b.iinv_ref[k];
+                iw[9 * (size_t)g + k] = (float)b.iw[k];
+                iinv[9 * (size_t)g + k] = dyn ? (float)b.iinv[k] : 0.f;
+            }
+            world_of[g] = (int)wi;
+            movement[g] = (uint8_t)b.movement;
+        }
+        std::vector<int> order = map_iteration_order(w);
+        for (size_t k = 0; k < order.size(); k++) map_order[base + k] = base + order[k];
+        WorldParams& P = wp[wi];
+        std::memset(&P, 0, sizeof(P));
+        P.dt = (float)w.p.dt;
+        P.dt_sub = (float)(w.p.dt / w.p.substeps);
+        P.gx = (float)w.p.g.x; P.gy = (float)w.p.g.y; P.gz = (float)w.p.g.z;
+        P.cfm = (float)w.p.cfm;
+        P.cutoff_vel = (float)w.p.cutoff;
+        P.hardness = (float)w.p.hardness;
+        P.contact_life = w.p.contact_life;
+        P.angle_ticks = w.p.angle_ticks;
+        P.gyro_disabled = w.p.gyro_disabled;
+        P.warm_disabled = w.p.warm_disabled;
+        P.pgs_vel = w.p.pgs_vel;
+        P.pgs_pos = w.p.pgs_pos;
+    }
+    B->movement = movement;
+    B->slot_bytes = 2 * max_hot;
+    if (pool.empty()) pool.resize(16);
+
+    // ---- contacts of the worlds (sorted by (b1, b2) within each world)
+    std::vector<uint64_t> ekey;
+    std::vector<int> ecstart, eccount;
+    std::vector<uint64_t> cmag;
+    std::vector<float4> cp1, cp2, cn, cimp, cfu, cfw;
+    std::vector<int> cstate, cedge;
+    for (size_t wi = 0; wi < worlds.size(); wi++) {
+        const int base = wstart[wi];
+        for (const cpgpu_contact& c : worlds[wi]->contacts) {
+            uint64_t key = ((uint64_t)(base + c.b1 - 1) << 32) | (uint32_t)(base + c.b2 - 1);
+            if (ekey.empty() || ekey.back() != key) {
+                ekey.push_back(key);
+                ecstart.push_back((int)cmag.size());
+                eccount.push_back(0);
+            }
+            eccount.back()++;
+            cmag.push_back(c.magic_b);
+            cp1.push_back(make_float4((float)c.p_local_b1[0], (float)c.p_local_b1[1], (float)c.p_local_b1[2], (float)c.pen_depth));
+            cp2.push_back(make_float4((float)c.p_local_b2[0], (float)c.p_local_b2[1], (float)c.p_local_b2[2], (float)c.bounce));
+            cn.push_back(make_float4((float)c.n_local_b1[0], (float)c.n_local_b1[1], (float)c.n_local_b1[2], (float)c.friction_coeff));
+            cimp.push_back(make_float4((float)c.normal_impulse, (float)c.friction_impulse[0], (float)c.friction_impulse[1], 0.f));
+            cfu.push_back(make_float4((float)c.friction_u[0], (float)c.friction_u[1], (float)c.friction_u[2], 0.f));
+            cfw.push_back(make_float4((float)c.friction_w[0], (float)c.friction_w[1], (float)c.friction_w[2], 0.f));
+            cstate.push_back(cs_make(c.memory_life, c.live != 0, c.static_ready != 0, false));
+            cedge.push_back((int)ekey.size() - 1);
+        }
+    }
+
+    // ---- capacities and device allocation
+    const int cap_pairs = std::max(1 << 14, env_int("CPGPU_PAIRS_PER_BODY", 24) * N);
+    const int cap_edges = cap_pairs;
+    const int cap_contacts = std::max(std::max(1 << 15, 2 * (int)cmag.size()), env_int("CPGPU_CONTACTS_PER_BODY", 24) * N);
+    const int scan_tmp = std::max(cap_pairs, cap_contacts) / 1024 + 64;
+    Dev x;
+    EdgeStore es[2];
+    ContactStore cs[2];
+    int* counts = nullptr;
+    WorldParams* d_wp = nullptr;
+    int *d_wstart = nullptr, *d_map = nullptr, *d_shape = nullptr, *d_world = nullptr;
+    float *d_iref = nullptr, *d_iinv_ref = nullptr;
+    uint8_t *d_mov = nullptr, *d_pool = nullptr;
+    float4* d_mat = nullptr;
+    // the same carving runs twice: once to measure, once on the allocation
+    auto carve = [&](Arena& A) {
+        std::memset(&x, 0, sizeof(x));
+        x.n_worlds = (int)worlds.size();
+        x.n_bodies = N;
+        x.cap_pairs = cap_pairs; x.cap_edges = cap_edges; x.cap_contacts = cap_contacts;
+        d_wp = A.take<WorldParams>(worlds.size());
+        d_wstart = A.take<int>(wstart.size());
+        d_map = A.take<int>(N);
+        x.wparams = d_wp; x.world_start = d_wstart; x.map_order = d_map;
+        x.pos = A.take<float4>(N); x.rot = A.take<float4>(N); x.vel = A.take<float4>(N); x.angv = A.take<float4>(N);
+        x.pvel = A.take<float4>(N); x.pangv = A.take<float4>(N);
+        x.iinv = A.take<float>(9 * (size_t)N); x.iw = A.take<float>(9 * (size_t)N);
+        d_iref = A.take<float>(9 * (size_t)N);
+        d_iinv_ref = A.take<float>(9 * (size_t)N);
+        x.iref = d_iref; x.iinv_ref = d_iinv_ref;
+        d_shape = A.take<int>(N); d_world = A.take<int>(N);
+        d_mov = A.take<uint8_t>(N);
+        d_mat = A.take<float4>(N);
+        x.shape = d_shape; x.world = d_world; x.movement = d_mov; x.material = d_mat;
+        x.aabb_lo = A.take<float4>(N); x.aabb_hi = A.take<float4>(N);
+        x.moved = A.take<int>(N);
+        d_pool = A.take<uint8_t>(pool.size());
+        x.shapes = d_pool;
+        x.pair_count = A.take<int>(N);
+        x.pair_a = A.take<int>(cap_pairs); x.pair_b = A.take<int>(cap_pairs);
+        x.mf_n = A.take<float4>(cap_pairs); x.mf_cnt = A.take<int>(cap_pairs);
+        x.mf_pt = A.take<float4>(4 * (size_t)cap_pairs); x.mf_magic = A.take<uint64_t>(4 * (size_t)cap_pairs);
+        for (int k = 0; k < 2; k++) {
+            es[k].key = A.take<uint64_t>(cap_edges); es[k].cstart = A.take<int>(cap_edges); es[k].ccount = A.take<int>(cap_edges);
+            cs[k].magic = A.take<uint64_t>(cap_contacts);
+            cs[k].p1 = A.take<float4>(cap_contacts); cs[k].p2 = A.take<float4>(cap_contacts); cs[k].n = A.take<float4>(cap_contacts);
+            cs[k].imp = A.take<float4>(cap_contacts); cs[k].fu = A.take<float4>(cap_contacts); cs[k].fw = A.take<float4>(cap_contacts);
+            cs[k].state = A.take<int>(cap_contacts); cs[k].edge = A.take<int>(cap_contacts);
+        }
+        counts = A.take<int>(64);   // n_pairs, n_edges[2], n_contacts[2], n_islands, status, .., cnt[16..]
+        x.n_pairs = counts + 0;
+        x.surv = A.take<int>(cap_edges); x.surv_scan = A.take<int>(cap_edges);
+        x.unm = A.take<int>(cap_pairs); x.unm_scan = A.take<int>(cap_pairs); x.pair_edge = A.take<int>(cap_pairs);
+        x.edge_src = A.take<int>(cap_edges); x.edge_pair = A.take<int>(cap_edges); x.edge_cnt = A.take<int>(cap_edges);
+        x.scan_tmp = A.take<int>(scan_tmp);
+        x.adj_ofs = A.take<int>(N); x.adj_cursor = A.take<int>(N);
+        x.adj_list = A.take<int>(2 * (2 * (size_t)cap_edges + N));
+        x.visited = A.take<int>(N);
+        x.stack = A.take<int>(2 * (size_t)cap_edges + N);
+        x.isl_count_w = A.take<int>(worlds.size()); x.isl_scan = A.take<int>(worlds.size());
+        x.isl_row_start = A.take<int>(N); x.isl_row_count = A.take<int>(N); x.isl_body_start = A.take<int>(N);
+        x.isl_body_count = A.take<int>(N); x.isl_world = A.take<int>(N);
+        x.g_isl_row_start = A.take<int>(N); x.g_isl_row_count = A.take<int>(N); x.g_isl_body_start = A.take<int>(N);
+        x.g_isl_body_count = A.take<int>(N); x.g_isl_world = A.take<int>(N);
+        x.n_islands = counts + 5;
+        x.isl_bodies = A.take<int>(N);
+        x.row_contact = A.take<int>(cap_contacts); x.row_of_contact = A.take<int>(cap_contacts);
+        x.rows = A.take<RowBlock>(cap_contacts);
+        x.dv = A.take<float4>(4 * (size_t)N);
+        x.status = counts + 6;
+        x.cnt = counts + 16;
+    };
+    Arena measure{nullptr, 0, 0};
+    carve(measure);
+    const size_t bytes = measure.used + 256;
+    CK(cudaMalloc(&B->mem, bytes));
+    Arena A{B->mem, bytes, 0};
+    carve(A);
+
+    // ---- upload
+    auto up = [&](void* dst, const void* src, size_t n) { if (n) CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, B->st)); };
+    CK(cudaMemsetAsync(counts, 0, 64 * sizeof(int), B->st));
+    up(d_wp, wp.data(), wp.size() * sizeof(WorldParams));
+    up(d_wstart, wstart.data(), wstart.size() * sizeof(int));
+    up(d_map, map_order.data(), N * sizeof(int));
+    up(x.pos, pos.data(), N * sizeof(float4)); up(x.rot, rot.data(), N * sizeof(float4));
+    up(x.vel, vel.data(), N * sizeof(float4)); up(x.angv, angv.data(), N * sizeof(float4));
+    up(x.pvel, zero4.data(), N * sizeof(float4)); up(x.pangv, zero4.data(), N * sizeof(float4));
+    up(x.iinv, iinv.data(), iinv.size() * 4); up(x.iw, iw.data(), iw.size() * 4);
+    up(d_iref, iref.data(), iref.size() * 4); up(d_iinv_ref, iinv_ref.data(), iinv_ref.size() * 4);
+    up(d_shape, shape_off.data(), N * 4); up(d_world, world_of.data(), N * 4);
+    up(d_mov, movement.data(), N); up(d_mat, mat.data(), N * sizeof(float4));
+    up(d_pool, pool.data(), pool.size());
+    CK(cudaMemsetAsync(x.moved, 0, N * sizeof(int), B->st));
+    const int ne = (int)ekey.size(), nc = (int)cmag.size();
+    up(es[0].key, ekey.data(), ne * 8); up(es[0].cstart, ecstart.data(), ne * 4); up(es[0].ccount, eccount.data(), ne * 4);
+    up(cs[0].magic, cmag.data(), nc * 8);
+    up(cs[0].p1, cp1.data(), nc * 16); up(cs[0].p2, cp2.data(), nc * 16); up(cs[0].n, cn.data(), nc * 16);
+    up(cs[0].imp, cimp.data(), nc * 16); up(cs[0].fu, cfu.data(), nc * 16); up(cs[0].fw, cfw.data(), nc * 16);
+    up(cs[0].state, cstate.data(), nc * 4); up(cs[0].edge, cedge.data(), nc * 4);
+    int host_counts[5] = {0, ne, 0, nc, 0};   // n_pairs, n_edges[0], n_edges[1], n_contacts[0], n_contacts[1]
+    up(counts, host_counts, sizeof(host_counts));
+    for (int p = 0; p < 2; p++) {
+        Dev y = x;
+        y.e_old = es[p]; y.e_new = es[1 - p];
+        y.c_old = cs[p]; y.c_new = cs[1 - p];
+        y.n_edges_old = counts + 1 + p; y.n_edges_new = counts + 1 + (1 - p);
+        y.n_contacts_old = counts + 3 + p; y.n_contacts_new = counts + 3 + (1 - p);
+        B->d[p] = y;
+    }
+    B->parity = 0;
+    Launch L{B->n_sms, B->st};
+    launch_geometry(B->d[0], 1, L);
+    prepare_kernels();
+    CK(cudaStreamSynchronize(B->st));
+    CK(cudaGetLastError());
+    B->build_graphs();
+    return B;
+}
+
+// ---------------------------------------------------------------- world helpers ----
+static void download_state(World& w) {
+    if (!w.dev || !w.dev_valid) return;
+    Batch& B = *w.dev;
+    const Dev& x = B.cur();
+    int N = B.n_bodies;
+    std::vector<float4> pos(N), rot(N), vel(N), angv(N);
+    std::vector<float> iw(9 * (size_t)N), iinv(9 * (size_t)N);
+    CK(cudaMemcpyAsync(pos.data(), x.pos, N * 16, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(rot.data(), x.rot, N * 16, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(vel.data(), x.vel, N * 16, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(angv.data(), x.angv, N * 16, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(iw.data(), x.iw, iw.size() * 4, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(iinv.data(), x.iinv, iinv.size() * 4, cudaMemcpyDeviceToHost, B.st));
+    int counts[6];
+    CK(cudaMemcpyAsync(counts, x.n_pairs, sizeof(counts), cudaMemcpyDeviceToHost, B.st));
+    CK(cudaStreamSynchronize(B.st));
+    for (int i = 0; i < N; i++) {
+        Body& b = w.bodies[i];
+        b.com = D3(pos[i].x, pos[i].y, pos[i].z);
+        b.q = Quat{rot[i].x, rot[i].y, rot[i].z, rot[i].w};
+        if (b.movement != CPGPU_FIXED) {
+            b.vel = D3(vel[i].x, vel[i].y, vel[i].z);
+            b.angv = D3(angv[i].x, angv[i].y, angv[i].z);
+        }
+        if (b.movement == CPGPU_DYNAMIC)
+            for (int k = 0; k < 9; k++) { b.iw[k] = iw[9 * (size_t)i + k]; b.iinv[k] = iinv[9 * (size_t)i + k]; }
+    }
+    // contact graph (current = the old buffers of the next step)
+    const int ne = *(&counts[1] + B.parity), nc = *(&counts[3] + B.parity);
+    std::vector<uint64_t> key(ne), mag(nc);
+    std::vector<int> cstart(ne), ccount(ne), state(nc);
+    std::vector<float4> p1(nc), p2(nc), n(nc), imp(nc), fu(nc), fw(nc);
+    const EdgeStore& E = x.e_old;
+    const ContactStore& C = x.c_old;
+    if (ne) {
+        CK(cudaMemcpyAsync(key.data(), E.key, ne * 8, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(cstart.data(), E.cstart, ne * 4, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(ccount.data(), E.ccount, ne * 4, cudaMemcpyDeviceToHost, B.st));
+    }
+    if (nc) {
+        CK(cudaMemcpyAsync(mag.data(), C.magic, nc * 8, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(p1.data(), C.p1, nc * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(p2.data(), C.p2, nc * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(n.data(), C.n, nc * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(imp.data(), C.imp, nc * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(fu.data(), C.fu, nc * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(fw.data(), C.fw, nc * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(state.data(), C.state, nc * 4, cudaMemcpyDeviceToHost, B.st));
+    }
+    int np = counts[0];
+    std::vector<int> pa(np), pb(np);
+    if (np) {
+        CK(cudaMemcpyAsync(pa.data(), x.pair_a, np * 4, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(pb.data(), x.pair_b, np * 4, cudaMemcpyDeviceToHost, B.st));
+    }
+    CK(cudaStreamSynchronize(B.st));
+    w.contacts.clear();
+    for (int e = 0; e < ne; e++) {
+        uint32_t b1 = (uint32_t)(key[e] >> 32) + 1, b2 = (uint32_t)(key[e] & 0xffffffffu) + 1;
+        for (int k = cstart[e]; k < cstart[e] + ccount[e]; k++) {
+            if (cs_dead(state[k])) continue;
+            cpgpu_contact c;
+            std::memset(&c, 0, sizeof(c));
+            c.b1 = b1; c.b2 = b2;
+            c.live = cs_live(state[k]);
+            c.memory_life = cs_life(state[k]);
+            c.magic_c = ((uint64_t)b2 << 32) | b1;
+            c.magic_b = mag[k];
+            c.p_local_b1[0] = p1[k].x; c.p_local_b1[1] = p1[k].y; c.p_local_b1[2] = p1[k].z;
+            c.p_local_b2[0] = p2[k].x; c.p_local_b2[1] = p2[k].y; c.p_local_b2[2] = p2[k].z;
+            c.n_local_b1[0] = n[k].x; c.n_local_b1[1] = n[k].y; c.n_local_b1[2] = n[k].z;
+            c.pen_depth = p1[k].w; c.bounce = p2[k].w; c.friction_coeff = n[k].w;
+            c.normal_impulse = imp[k].x; c.friction_impulse[0] = imp[k].y; c.friction_impulse[1] = imp[k].z;
+            c.friction_u[0] = fu[k].x; c.friction_u[1] = fu[k].y; c.friction_u[2] = fu[k].z;
+            c.friction_w[0] = fw[k].x; c.friction_w[1] = fw[k].y; c.friction_w[2] = fw[k].z;
+            c.static_ready = cs_static(state[k]);
+            w.contacts.push_back(c);
+        }
+    }
+    w.last_pairs.clear();
+    for (int i = 0; i < np; i++) { w.last_pairs.push_back((uint32_t)pa[i] + 1); w.last_pairs.push_back((uint32_t)pb[i] + 1); }
+}
+
+// Pull device state into the host mirror and mark the device copy stale, so the
+// next step re-uploads the (mutated) world.
+static void begin_mutation(World& w) {
+    if (w.dev && w.dev_valid) download_state(w);
+    w.dev_valid = false;
+}
+
+static void update_cutoff(World& w) { w.p.cutoff = 2 * w.p.g.mag() * w.p.dt; }
+
+static Body& body_ref(World& w, uint32_t id) {
+    if (id == 0 || id > w.bodies.size()) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad body id"};
+    return w.bodies[id - 1];
+}
+
+static uint32_t add_hull(World& w, const std::vector<D3>& pts, const std::vector<std::vector<int>>& faces,
+                         const cpgpu_material* m, int movement, const double* pos) {
+    if (movement < 0 || movement > 2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad movement type"};
+    if (movement == CPGPU_KINEMATIC) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "kinematic bodies are not implemented on the device path"};
+    HullPrep h;
+    if (pts.size() < 4 || faces.size() < 4 || !h.build(pts, faces)) throw ApiFail{CPGPU_ERR_INVALID_ARG, "invalid hull"};
+    Body b;
+    double density = m ? m->density : 1.0;
+    double t[3][3];
+    hullMassProperties(h, density, &b.com, t, &b.mass);
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) b.iref[3 * i + j] = t[i][j];
+    inv3(b.iref, b.iinv_ref);
+    std::memcpy(b.iw, b.iref, sizeof(b.iw));
+    std::memcpy(b.iinv, b.iinv_ref, sizeof(b.iinv));
+    Shape s = pack_hull(h, b.com);
+    b.local_origin = -b.com;
+    // setToPosition: translate so the geometry origin lands on pos
+    D3 p = pos ? D3(pos[0], pos[1], pos[2]) : D3();
+    D3 tracked = b.com + qrot(b.q, b.local_origin);
+    b.com = b.com + (p - tracked);
+    b.movement = movement;
+    if (m) { b.rest = m->restitution; b.kin = m->kinetic_friction; b.sta = m->static_friction; }
+    begin_mutation(w);
+    b.shape = (int)w.shapes.size();
+    w.shapes.push_back(std::move(s));
+    w.bodies.push_back(b);
+    uint32_t id = (uint32_t)w.bodies.size();
+    w.nodes[id] = (int)id - 1;
+    return id;
+}
+
+static void ensure_device(World& w) {
+    if (w.dev && w.dev_valid) return;
+    w.dev.reset();
+    std::vector<World*> one{&w};
+    w.dev = build_batch(one);
+    w.dev_valid = true;
+}
+
+}  // namespace cpgpu
+
+// ================================================================== C ABI ====
+using namespace cpgpu;
+
+struct cpgpu_world { World w; };
+struct cpgpu_batch {
+    std::unique_ptr<Batch> b;
+    std::vector<int> sizes;
+};
+
+template <class F>
+static int guarded(F&& f) {
+    try {
+        return f();
+    } catch (const ApiFail& e) {
+        return fail(e.code, e.msg);
+    } catch (const CudaFail& e) {
+        return fail(CPGPU_ERR_CUDA, e.msg);
+    } catch (const std::bad_alloc&) {
+        return fail(CPGPU_ERR_CUDA, "host allocation failed");
+    } catch (...) {
+        return fail(CPGPU_ERR_INVALID_ARG, "unexpected error");
+    }
+}
+
+#define W_OR_FAIL(w) if (!(w)) return fail(CPGPU_ERR_INVALID_ARG, "null world")
+
+extern "C" {
+
+const char* cpgpu_last_error(void) { return g_err.c_str(); }
+
+int cpgpu_world_create(cpgpu_world** out) {
+    return guarded([&] {
+        if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null out"};
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw ApiFail{CPGPU_ERR_NO_DEVICE, "no CUDA device"};
+        *out = new cpgpu_world();
+        return CPGPU_OK;
+    });
+}
+int cpgpu_world_destroy(cpgpu_world* w) { delete w; return CPGPU_OK; }
+
+#define SETTER(name, ...)                                                           \
+    int name {                                                                      \
+        W_OR_FAIL(w);                                                               \
+        return guarded([&] { begin_mutation(w->w); __VA_ARGS__; return CPGPU_OK; }); \
+    }
+SETTER(cpgpu_set_step_time(cpgpu_world* w, double dt), {
+    if (!(dt > 0)) throw ApiFail{CPGPU_ERR_INVALID_ARG, "step time must be positive"};
+    w->w.p.dt = dt; update_cutoff(w->w); })
+SETTER(cpgpu_set_gravity(cpgpu_world* w, double x, double y, double z), { w->w.p.g = D3(x, y, z); update_cutoff(w->w); })
+SETTER(cpgpu_set_substep_count(cpgpu_world* w, int s), {
+    if (s < 1) throw ApiFail{CPGPU_ERR_INVALID_ARG, "substeps < 1"};
+    w->w.p.substeps = s; })
+SETTER(cpgpu_set_pgs_iterations(cpgpu_world* w, int v, int p, int h), {
+    if (v < 0 || p < 0 || h < 0) throw ApiFail{CPGPU_ERR_INVALID_ARG, "negative iteration count"};
+    w->w.p.pgs_vel = v; w->w.p.pgs_pos = p; w->w.p.pgs_holo = h; })
+SETTER(cpgpu_set_sleeping_enabled(cpgpu_world* w, int e), {
+    if (e) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "sleeping is not implemented on the device path"}; })
+SETTER(cpgpu_set_warm_start_disabled(cpgpu_world* w, int d), { w->w.p.warm_disabled = d != 0; })
+SETTER(cpgpu_set_global_cfm(cpgpu_world* w, double c), { w->w.p.cfm = c; })
+SETTER(cpgpu_set_angle_vel_update_tick_count(cpgpu_world* w, int n), {
+    if (n < 0) throw ApiFail{CPGPU_ERR_INVALID_ARG, "negative tick count"};
+    w->w.p.angle_ticks = n; })
+SETTER(cpgpu_set_internal_gyro_forces_disabled(cpgpu_world* w, int d), { w->w.p.gyro_disabled = d != 0; })
+
+int cpgpu_body_hull(cpgpu_world* w, const double* points, int n_points, const int* face_offsets, const int* face_indices,
+                    int n_faces, const cpgpu_material* m, int movement, const double pos[3], uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!points || !face_offsets || !face_indices || n_points < 4 || n_faces < 4)
+            throw ApiFail{CPGPU_ERR_INVALID_ARG, "hull needs >= 4 points and faces"};
+        std::vector<D3> pts(n_points);
+        for (int i = 0; i < n_points; i++) pts[i] = D3(points[3 * i], points[3 * i + 1], points[3 * i + 2]);
+        std::vector<std::vector<int>> faces(n_faces);
+        for (int f = 0; f < n_faces; f++)
+            for (int k = face_offsets[f]; k < face_offsets[f + 1]; k++) faces[f].push_back(face_indices[k]);
+        uint32_t id = add_hull(w->w, pts, faces, m, movement, pos);
+        if (out_id) *out_id = id;
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_body_box(cpgpu_world* w, const double c[3], double dx, double dy, double dz, const cpgpu_material* m,
+                   int movement, const double pos[3], uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!c) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null corner"};
+        // ConvexUnionGeometry::box (Geometry.cpp:14-37): same points and faces
+        D3 p(c[0], c[1], c[2]);
+        std::vector<D3> pts = {D3(p.x, p.y, p.z), D3(p.x + dx, p.y, p.z), D3(p.x + dx, p.y + dy, p.z), D3(p.x, p.y + dy, p.z),
+                               D3(p.x, p.y, p.z + dz), D3(p.x + dx, p.y, p.z + dz), D3(p.x + dx, p.y + dy, p.z + dz), D3(p.x, p.y + dy, p.z + dz)};
+        std::vector<std::vector<int>> faces = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+        uint32_t id = add_hull(w->w, pts, faces, m, movement, pos);
+        if (out_id) *out_id = id;
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_body_sphere(cpgpu_world*, const double*, double, const cpgpu_material*, int, const double*, uint32_t*) {
+    return fail(CPGPU_ERR_UNSUPPORTED, "spheres are not implemented on the device path yet");
+}
+int cpgpu_body_cylinder(cpgpu_world*, const double*, double, double, const cpgpu_material*, int, const double*, uint32_t*) {
+    return fail(CPGPU_ERR_UNSUPPORTED, "cylinders are not implemented on the device path yet");
+}
+int cpgpu_body_mesh(cpgpu_world*, const double*, int, const int*, int, const cpgpu_material*, int, uint32_t*) {
+    return fail(CPGPU_ERR_UNSUPPORTED, "static meshes are not implemented on the device path yet");
+}
+
+int cpgpu_body_set_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {
+    W_OR_FAIL(w);
+    return guarded([&] { begin_mutation(w->w); body_ref(w->w, id).vel = D3(v[0], v[1], v[2]); return CPGPU_OK; });
+}
+int cpgpu_body_set_ang_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {
+    W_OR_FAIL(w);
+    return guarded([&] { begin_mutation(w->w); body_ref(w->w, id).angv = D3(v[0], v[1], v[2]); return CPGPU_OK; });
+}
+// RigidBody::setOrientation (RigidBody.cpp:103-107): the orientation is set and
+// normalised by updateGeometry; the world inertia tensor keeps its value until
+// the next integration updates it.
+int cpgpu_body_set_orientation(cpgpu_world* w, uint32_t id, const double q[4]) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        begin_mutation(w->w);
+        Body& b = body_ref(w->w, id);
+        b.q = qnorm(Quat{q[0], q[1], q[2], q[3]});
+        return CPGPU_OK;
+    });
+}
+int cpgpu_body_set_position(cpgpu_world* w, uint32_t id, const double p[3]) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        begin_mutation(w->w);
+        Body& b = body_ref(w->w, id);
+        D3 tracked = b.com + qrot(b.q, b.local_origin);
+        b.com = b.com + (D3(p[0], p[1], p[2]) - tracked);
+        b.q = qnorm(b.q);
+        return CPGPU_OK;
+    });
+}
+int cpgpu_body_set_mass(cpgpu_world* w, uint32_t id, double mass) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!(mass > 0)) throw ApiFail{CPGPU_ERR_INVALID_ARG, "mass must be positive"};
+        begin_mutation(w->w);
+        Body& b = body_ref(w->w, id);
+        double r = mass / b.mass;
+        for (int k = 0; k < 9; k++) { b.iref[k] *= r; b.iinv_ref[k] /= r; b.iw[k] *= r; b.iinv[k] /= r; }
+        b.mass = mass;
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_add_ball_socket(cpgpu_world*, uint32_t, uint32_t, const double*, const double*, double, uint32_t*) {
+    return fail(CPGPU_ERR_UNSUPPORTED, "joints are not implemented on the device path yet");
+}
+int cpgpu_add_hinge(cpgpu_world*, uint32_t, uint32_t, const double*, const double*, const double*, const double*, double, double,
+                    uint32_t*) {
+    return fail(CPGPU_ERR_UNSUPPORTED, "joints are not implemented on the device path yet");
+}
+
+int cpgpu_step(cpgpu_world* w, int n_steps) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (n_steps < 0) throw ApiFail{CPGPU_ERR_INVALID_ARG, "negative step count"};
+        if (w->w.bodies.empty()) return CPGPU_OK;
+        ensure_device(w->w);
+        w->w.dev->step(n_steps);
+        return w->w.dev->check_status();
+    });
+}
+
+int cpgpu_num_bodies(cpgpu_world* w, int* n) {
+    W_OR_FAIL(w);
+    *n = (int)w->w.bodies.size();
+    return CPGPU_OK;
+}
+
+int cpgpu_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel, double* ang) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (w->w.dev && w->w.dev_valid) download_state(w->w);
+        for (size_t i = 0; i < w->w.bodies.size(); i++) {
+            const Body& b = w->w.bodies[i];
+            D3 v = b.movement == CPGPU_FIXED ? D3() : b.vel, a = b.movement == CPGPU_FIXED ? D3() : b.angv;
+            if (com) { com[3 * i] = b.com.x; com[3 * i + 1] = b.com.y; com[3 * i + 2] = b.com.z; }
+            if (quat) { quat[4 * i] = b.q.r; quat[4 * i + 1] = b.q.i; quat[4 * i + 2] = b.q.j; quat[4 * i + 3] = b.q.k; }
+            if (vel) { vel[3 * i] = v.x; vel[3 * i + 1] = v.y; vel[3 * i + 2] = v.z; }
+            if (ang) { ang[3 * i] = a.x; ang[3 * i + 1] = a.y; ang[3 * i + 2] = a.z; }
+        }
+        return CPGPU_OK;
+    });
+}
+
+// Checkpoint restore of the dynamic state: poses and velocities are replaced
+// and the world inertia tensors recomputed from the new orientations.
+int cpgpu_set_body_state(cpgpu_world* w, const double* com, const double* quat, const double* vel, const double* ang) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        begin_mutation(w->w);
+        for (size_t i = 0; i < w->w.bodies.size(); i++) {
+            Body& b = w->w.bodies[i];
+            if (com) b.com = D3(com[3 * i], com[3 * i + 1], com[3 * i + 2]);
+            if (quat) b.q = qnorm(Quat{quat[4 * i], quat[4 * i + 1], quat[4 * i + 2], quat[4 * i + 3]});
+            if (vel) b.vel = D3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+            if (ang) b.angv = D3(ang[3 * i], ang[3 * i + 1], ang[3 * i + 2]);
+            if (b.movement == CPGPU_DYNAMIC) {
+                // I_world = R I_ref R^T (RigidBody::updateInertiaTensor)
+                double R[9];
+                const Quat& q = b.q;
+                double r = q.r, ii = q.i, j = q.j, k = q.k;
+                R[0] = r * r + ii * ii - j * j - k * k; R[1] = 2 * ii * j - 2 * r * k; R[2] = 2 * ii * k + 2 * r * j;
+                R[3] = 2 * ii * j + 2 * r * k; R[4] = r * r - ii * ii + j * j - k * k; R[5] = 2 * j * k - 2 * r * ii;
+                R[6] = 2 * ii * k - 2 * r * j; R[7] = 2 * j * k + 2 * r * ii; R[8] = r * r - ii * ii - j * j + k * k;
+                for (int which = 0; which < 2; which++) {
+                    const double* I = which ? b.iinv_ref : b.iref;
+                    double* out = which ? b.iinv : b.iw;
+                    double T[9];
+                    for (int a = 0; a < 3; a++) for (int c = 0; c < 3; c++) { double s = 0; for (int m = 0; m < 3; m++) s += R[3 * a + m] * I[3 * m + c]; T[3 * a + c] = s; }
+                    for (int a = 0; a < 3; a++) for (int c = 0; c < 3; c++) { double s = 0; for (int m = 0; m < 3; m++) s += T[3 * a + m] * R[3 * c + m]; out[3 * a + c] = s; }
+                }
+            }
+        }
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_get_aabbs(cpgpu_world* w, double* out) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        ensure_device(w->w);
+        Batch& B = *w->w.dev;
+        int N = B.n_bodies;
+        std::vector<float4> lo(N), hi(N);
+        CK(cudaMemcpyAsync(lo.data(), B.cur().aabb_lo, N * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(hi.data(), B.cur().aabb_hi, N * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaStreamSynchronize(B.st));
+        for (int i = 0; i < N; i++) {
+            double* o = out + 6 * i;
+            o[0] = lo[i].x; o[1] = lo[i].y; o[2] = lo[i].z; o[3] = hi[i].x; o[4] = hi[i].y; o[5] = hi[i].z;
+        }
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_get_pairs(cpgpu_world* w, uint32_t* pairs, int cap, int* n) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (w->w.dev && w->w.dev_valid) download_state(w->w);
+        int np = (int)(w->w.last_pairs.size() / 2);
+        *n = np;
+        for (int i = 0; i < np && i < cap; i++) { pairs[2 * i] = w->w.last_pairs[2 * i]; pairs[2 * i + 1] = w->w.last_pairs[2 * i + 1]; }
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_get_contacts(cpgpu_world* w, cpgpu_contact* out, int cap, int* n) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (w->w.dev && w->w.dev_valid) download_state(w->w);
+        *n = (int)w->w.contacts.size();
+        if (out) for (int i = 0; i < *n && i < cap; i++) out[i] = w->w.contacts[i];
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        begin_mutation(w->w);
+        std::vector<cpgpu_contact> cs(in, in + n);
+        for (const cpgpu_contact& c : cs)
+            if (c.b1 == 0 || c.b2 == 0 || c.b1 >= c.b2 || c.b2 > w->w.bodies.size())
+                throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad contact body ids"};
+        std::stable_sort(cs.begin(), cs.end(), [](const cpgpu_contact& a, const cpgpu_contact& b) {
+            return a.b1 != b.b1 ? a.b1 < b.b1 : a.b2 < b.b2;
+        });
+        w->w.contacts = cs;
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_batch_create(cpgpu_world* const* worlds, int n, cpgpu_batch** out) {
+    return guarded([&] {
+        if (!worlds || n <= 0 || !out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "empty batch"};
+        std::vector<World*> ws;
+        for (int i = 0; i < n; i++) {
+            if (!worlds[i]) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null world"};
+            if (worlds[i]->w.dev && worlds[i]->w.dev_valid) download_state(worlds[i]->w);
+            ws.push_back(&worlds[i]->w);
+        }
+        auto b = std::make_unique<cpgpu_batch>();
+        b->b = build_batch(ws);
+        for (World* x : ws) b->sizes.push_back((int)x->bodies.size());
+        *out = b.release();
+        return CPGPU_OK;
+    });
+}
+int cpgpu_batch_destroy(cpgpu_batch* b) { delete b; return CPGPU_OK; }
+int cpgpu_batch_step(cpgpu_batch* b, int n) {
+    if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
+    return guarded([&] { b->b->step(n); return b->b->check_status(); });
+}
+int cpgpu_batch_get_body_state(cpgpu_batch* b, int wi, double* com, double* quat, double* vel, double* ang) {
+    if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
+    return guarded([&] {
+        Batch& B = *b->b;
+        if (wi < 0 || wi >= B.n_worlds) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad world index"};
+        int s = B.world_start[wi], n = B.world_start[wi + 1] - s;
+        std::vector<float4> pos(n), rot(n), vel4(n), ang4(n);
+        const Dev& x = B.cur();
+        CK(cudaMemcpyAsync(pos.data(), x.pos + s, n * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(rot.data(), x.rot + s, n * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(vel4.data(), x.vel + s, n * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(ang4.data(), x.angv + s, n * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaStreamSynchronize(B.st));
+        for (int i = 0; i < n; i++) {
+            bool fixed = B.movement[s + i] == CPGPU_FIXED;
+            if (com) { com[3 * i] = pos[i].x; com[3 * i + 1] = pos[i].y; com[3 * i + 2] = pos[i].z; }
+            if (quat) { quat[4 * i] = rot[i].x; quat[4 * i + 1] = rot[i].y; quat[4 * i + 2] = rot[i].z; quat[4 * i + 3] = rot[i].w; }
+            if (vel) { vel[3 * i] = fixed ? 0 : vel4[i].x; vel[3 * i + 1] = fixed ? 0 : vel4[i].y; vel[3 * i + 2] = fixed ? 0 : vel4[i].z; }
+            if (ang) { ang[3 * i] = fixed ? 0 : ang4[i].x; ang[3 * i + 1] = fixed ? 0 : ang4[i].y; ang[3 * i + 2] = fixed ? 0 : ang4[i].z; }
+        }
+        return CPGPU_OK;
+    });
+}
+int cpgpu_batch_info(cpgpu_batch* b, int64_t* n_bodies, int64_t* n_worlds, int64_t* n_contacts) {
+    if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
+    return guarded([&] {
+        Batch& B = *b->b;
+        int counts[6];
+        CK(cudaMemcpyAsync(counts, B.cur().n_pairs, sizeof(counts), cudaMemcpyDeviceToHost, B.st));
+        CK(cudaStreamSynchronize(B.st));
+        if (n_bodies) *n_bodies = B.n_bodies;
+        if (n_worlds) *n_worlds = B.n_worlds;
+        if (n_contacts) *n_contacts = counts[3 + B.parity];
+        return CPGPU_OK;
+    });
+}
+
+// Device time of n steps of the batch, measured with CUDA events recorded on
+// the batch's own stream around the graph launches.
+int cpgpu_batch_step_timed(cpgpu_batch* b, int n, double* device_ms) {
+    if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
+    return guarded([&] {
+        Batch& B = *b->b;
+        CK(cudaEventRecord(B.ev0, B.st));
+        B.step(n);
+        CK(cudaEventRecord(B.ev1, B.st));
+        CK(cudaEventSynchronize(B.ev1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, B.ev0, B.ev1));
+        if (device_ms) *device_ms = ms;
+        return B.check_status();
+    });
+}
+
+}  // extern "C"

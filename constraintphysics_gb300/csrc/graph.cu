@@ -1,0 +1,347 @@
+// graph.cu — persistent contact graph and islands on the device.
+//
+// Contact persistence (PhysicsEngine::addContact, PhysicsEngine.cpp:1062-1111;
+// expiry :1434-1446): the edge list of the previous step (sorted by the pair
+// key) loses its expired contacts and empty edges, and is merged with this
+// step's manifolds.  Both lists are sorted, so every element finds its output
+// position by a binary search in the other list plus an exclusive scan; no sort
+// is needed.  Within an edge, surviving contacts keep their order, manifold
+// points update the first contact with the same MagicID or are appended.
+//
+// Islands and row order (PhysicsEngine::sleepOrSolveIslands / bfsVisitAll,
+// PhysicsEngine.cpp:1260-1283, 1536-1613): one block per world builds the
+// adjacency of dynamic bodies sorted by the other body id
+// (ConstraintGraphNode::insertNewEdge, :1984-1995), then a depth-first search
+// (LIFO stack) starts from every unvisited dynamic body in constraint-graph
+// node-map iteration order (supplied by the host) and emits each live contact
+// of each edge to a not-yet-visited neighbour, in per-edge order.  That is the
+// reference's exact row order.
+#include "kernels.cuh"
+#include "devmath.cuh"
+
+namespace cpgpu {
+
+namespace {
+
+constexpr int kMaxEdgeContacts = 64;
+
+__device__ __forceinline__ int lower_bound_u64(const uint64_t* keys, int n, uint64_t k) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int m = (lo + hi) >> 1;
+        if (keys[m] < k) lo = m + 1; else hi = m;
+    }
+    return lo;
+}
+__device__ __forceinline__ uint64_t pair_key(const Dev& d, int p) {
+    return ((uint64_t)(uint32_t)d.pair_a[p] << 32) | (uint32_t)d.pair_b[p];
+}
+__device__ __forceinline__ int lower_bound_pairs(const Dev& d, int n, uint64_t k) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int m = (lo + hi) >> 1;
+        if (pair_key(d, m) < k) lo = m + 1; else hi = m;
+    }
+    return lo;
+}
+
+__global__ void k_surv(Dev d) {
+    const int n = *d.n_edges_old;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        int s = d.e_old.cstart[e], c = d.e_old.ccount[e], alive = 0;
+        for (int k = s; k < s + c; k++) alive += !cs_dead(d.c_old.state[k]);
+        d.surv[e] = alive > 0;
+    }
+}
+
+__global__ void k_pair_match(Dev d) {
+    const int np = *d.n_pairs, ne = *d.n_edges_old;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        bool hasm = d.mf_n[p].w > 0.f;
+        uint64_t key = pair_key(d, p);
+        int e = lower_bound_u64(d.e_old.key, ne, key);
+        bool matched = e < ne && d.e_old.key[e] == key && d.surv[e];
+        d.pair_edge[p] = matched ? e : -1;
+        d.unm[p] = hasm && !matched;
+    }
+}
+
+// cnt[0] = surviving old edges, cnt[1] = unmatched manifolds (both from scans)
+__global__ void k_place(Dev d, const int* cnt) {
+    const int ne = *d.n_edges_old, np = *d.n_pairs;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    for (int e = tid; e < ne; e += stride) {
+        if (!d.surv[e]) continue;
+        uint64_t key = d.e_old.key[e];
+        int r = lower_bound_pairs(d, np, key);
+        int ub = (r < np) ? d.unm_scan[r] : cnt[1];
+        int pos = d.surv_scan[e] + ub;
+        if (pos < d.cap_edges) {
+            d.e_new.key[pos] = key;
+            d.edge_src[pos] = e;
+            d.edge_pair[pos] = (r < np && pair_key(d, r) == key && d.mf_n[r].w > 0.f) ? r : -1;
+        }
+    }
+    for (int p = tid; p < np; p += stride) {
+        if (!d.unm[p]) continue;
+        uint64_t key = pair_key(d, p);
+        int r = lower_bound_u64(d.e_old.key, ne, key);
+        int sb = (r < ne) ? d.surv_scan[r] : cnt[0];
+        int pos = d.unm_scan[p] + sb;
+        if (pos < d.cap_edges) {
+            d.e_new.key[pos] = key;
+            d.edge_src[pos] = -1;
+            d.edge_pair[pos] = p;
+        }
+    }
+}
+
+__global__ void k_edge_total(Dev d, const int* cnt) {
+    int n = cnt[0] + cnt[1];
+    if (n > d.cap_edges) { atomicOr(d.status, ST_EDGE_OVERFLOW); n = d.cap_edges; }
+    *d.n_edges_new = n;
+}
+
+__global__ void k_contact_total(Dev d) {
+    if (*d.n_contacts_new > d.cap_contacts) { atomicOr(d.status, ST_CONTACT_OVERFLOW); *d.n_contacts_new = d.cap_contacts; }
+}
+
+// per new edge: surviving old contacts (in order), then this step's manifold
+// points matched by MagicID or appended
+__global__ void k_contacts(Dev d, int write) {
+    const int ne = *d.n_edges_new;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
+        int ids[kMaxEdgeContacts];
+        signed char upd[kMaxEdgeContacts];
+        uint64_t mags[kMaxEdgeContacts];
+        int n = 0;
+        const int src = d.edge_src[e], p = d.edge_pair[e];
+        if (src >= 0) {
+            int s = d.e_old.cstart[src], c = d.e_old.ccount[src];
+            for (int k = s; k < s + c; k++) {
+                if (cs_dead(d.c_old.state[k])) continue;
+                if (n < kMaxEdgeContacts) { ids[n] = k; mags[n] = d.c_old.magic[k]; upd[n] = -1; n++; }
+                else atomicOr(d.status, ST_CONTACT_OVERFLOW);
+            }
+        }
+        int np = (p >= 0) ? d.mf_cnt[p] : 0;
+        for (int k = 0; k < np; k++) {
+            uint64_t m = d.mf_magic[4 * p + k];
+            int j = 0;
+            while (j < n && mags[j] != m) j++;
+            if (j < n) upd[j] = (signed char)k;
+            else if (n < kMaxEdgeContacts) { ids[n] = -1; mags[n] = m; upd[n] = (signed char)k; n++; }
+            else atomicOr(d.status, ST_CONTACT_OVERFLOW);
+        }
+        if (!write) { d.edge_cnt[e] = n; continue; }
+        const int base = d.e_new.cstart[e];
+        if (base + n > d.cap_contacts) n = base < d.cap_contacts ? d.cap_contacts - base : 0;
+        d.e_new.ccount[e] = n;
+        const uint64_t key = d.e_new.key[e];
+        const int b1 = (int)(key >> 32), b2 = (int)(key & 0xffffffffu);
+        M33 i1 = quatRot(qconj(d.rot[b1])), i2 = quatRot(qconj(d.rot[b2]));
+        f3 c1 = mk(d.pos[b1]), c2 = mk(d.pos[b2]);
+        float4 m1 = d.material[b1], m2 = d.material[b2];
+        float rest = fmaxf(m1.x, m2.x), kin = (m1.y + m2.y) / 2.0f, sta = (m1.z + m2.z) / 2.0f;
+        const WorldParams& wp = d.wparams[d.world[b1]];
+        for (int j = 0; j < n; j++) {
+            int dst = base + j;
+            const ContactStore& O = d.c_old;
+            const ContactStore& N = d.c_new;
+            float4 p1, p2, nn, imp, fu, fw;
+            int st;
+            if (ids[j] >= 0) {
+                int o = ids[j];
+                p1 = O.p1[o]; p2 = O.p2[o]; nn = O.n[o]; imp = O.imp[o]; fu = O.fu[o]; fw = O.fw[o]; st = O.state[o];
+            } else {
+                p2.w = rest;
+                nn.w = kin;
+                imp = make_float4(0.f, 0.f, 0.f, 0.f);
+                fu = fw = make_float4(0.f, 0.f, 0.f, 0.f);
+                st = cs_make(0, false, false, false);
+            }
+            if (upd[j] >= 0) {
+                float4 pt = d.mf_pt[4 * p + upd[j]];
+                f3 pos = mk(pt);
+                f3 nw = mk(d.mf_n[p]);
+                f3 nl = mul(i1, nw), l1 = mul(i1, pos - c1), l2 = mul(i2, pos - c2);
+                float fc = (ids[j] >= 0) ? (cs_static(st) ? sta : kin) : kin;
+                p1 = make_float4(l1.x, l1.y, l1.z, pt.w);
+                p2 = make_float4(l2.x, l2.y, l2.z, p2.w);
+                nn = make_float4(nl.x, nl.y, nl.z, fc);
+                st = cs_make(wp.contact_life, true, cs_static(st), false);
+            }
+            N.magic[dst] = mags[j];
+            N.p1[dst] = p1; N.p2[dst] = p2; N.n[dst] = nn; N.imp[dst] = imp; N.fu[dst] = fu; N.fw[dst] = fw;
+            N.state[dst] = st;
+            N.edge[dst] = e;
+        }
+    }
+}
+
+// ---- islands: one block per world ---------------------------------------------------
+__global__ void __launch_bounds__(256) k_islands(Dev d) {
+    __shared__ int sh_carry, sh_rows_end;
+    __shared__ int warp_sums[8];
+    const int w = blockIdx.x;
+    const int s = d.world_start[w], e = d.world_start[w + 1];
+    const int ne = *d.n_edges_new, ncon = *d.n_contacts_new;
+    const int e0 = lower_bound_u64(d.e_new.key, ne, (uint64_t)s << 32);
+    const int e1 = lower_bound_u64(d.e_new.key, ne, (uint64_t)e << 32);
+    const int c0 = (e0 < ne) ? d.e_new.cstart[e0] : ncon;
+    const int c1 = (e1 < ne) ? d.e_new.cstart[e1] : ncon;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int i = s + tid; i < e; i += nt) { d.adj_cursor[i] = 0; d.visited[i] = -1; }
+    for (int c = c0 + tid; c < c1; c += nt) d.row_of_contact[c] = -1;
+    __syncthreads();
+    for (int k = e0 + tid; k < e1; k += nt) {
+        uint64_t key = d.e_new.key[k];
+        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+        if (d.movement[a] == 0) atomicAdd(&d.adj_cursor[a], 1);
+        if (d.movement[b] == 0) atomicAdd(&d.adj_cursor[b], 1);
+    }
+    __syncthreads();
+    // exclusive scan of the degrees into adjacency offsets (region starts at 2 * e0)
+    if (tid == 0) sh_carry = 2 * e0;
+    __syncthreads();
+    for (int base = s; base < e; base += nt) {
+        int i = base + tid;
+        int v = (i < e) ? d.adj_cursor[i] : 0;
+        int x = v;
+        const int lane = tid & 31, wid = tid >> 5;
+        for (int o = 1; o < 32; o <<= 1) { int t = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += t; }
+        if (lane == 31) warp_sums[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            int y = (lane < (nt >> 5)) ? warp_sums[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) { int t = __shfl_up_sync(0xffffffffu, y, o); if (lane >= o) y += t; }
+            if (lane < 8) warp_sums[lane] = y;
+        }
+        __syncthreads();
+        int incl = x + (wid > 0 ? warp_sums[wid - 1] : 0);
+        int carry = sh_carry;
+        if (i < e) { d.adj_ofs[i] = carry + incl - v; d.adj_cursor[i] = carry + incl - v; }
+        __syncthreads();
+        if (tid == nt - 1) sh_carry = carry + incl;
+        __syncthreads();
+    }
+    for (int k = e0 + tid; k < e1; k += nt) {
+        uint64_t key = d.e_new.key[k];
+        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+        if (d.movement[a] == 0) { int slot = atomicAdd(&d.adj_cursor[a], 1); d.adj_list[2 * slot] = b; d.adj_list[2 * slot + 1] = k; }
+        if (d.movement[b] == 0) { int slot = atomicAdd(&d.adj_cursor[b], 1); d.adj_list[2 * slot] = a; d.adj_list[2 * slot + 1] = k; }
+    }
+    __syncthreads();
+    // each dynamic node's edges sorted by the other body's id (insertion sort)
+    for (int i = s + tid; i < e; i += nt) {
+        if (d.movement[i] != 0) continue;
+        int lo = d.adj_ofs[i], hi = d.adj_cursor[i];
+        for (int x = lo + 1; x < hi; x++) {
+            int ko = d.adj_list[2 * x], kk = d.adj_list[2 * x + 1];
+            int y = x - 1;
+            while (y >= lo && d.adj_list[2 * y] > ko) { d.adj_list[2 * (y + 1)] = d.adj_list[2 * y]; d.adj_list[2 * (y + 1) + 1] = d.adj_list[2 * y + 1]; y--; }
+            d.adj_list[2 * (y + 1)] = ko;
+            d.adj_list[2 * (y + 1) + 1] = kk;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int* stack = d.stack + 2 * e0 + s;
+        const int stack_cap = 2 * (e1 - e0) + (e - s);
+        int rc = c0, bc = s, ni = 0;
+        for (int t = s; t < e; t++) {
+            int node = d.map_order[t];
+            if (d.movement[node] != 0 || d.visited[node] >= 0) continue;
+            int rs = rc, bs = bc, sp = 0;
+            stack[sp++] = node;
+            while (sp > 0) {
+                int cur = stack[--sp];
+                if (d.visited[cur] >= 0) continue;
+                d.visited[cur] = bc - bs;
+                d.isl_bodies[bc++] = cur;
+                int lo = d.adj_ofs[cur], hi = d.adj_cursor[cur];
+                for (int j = lo; j < hi; j++) {
+                    int o = d.adj_list[2 * j], k = d.adj_list[2 * j + 1];
+                    if (d.visited[o] >= 0) continue;
+                    int cs = d.e_new.cstart[k], cn = d.e_new.ccount[k];
+                    for (int c = cs; c < cs + cn; c++)
+                        if (cs_live(d.c_new.state[c])) d.row_contact[rc++] = c;
+                }
+                for (int j = lo; j < hi; j++) {
+                    int o = d.adj_list[2 * j];
+                    if (d.movement[o] == 0 && d.visited[o] < 0) {
+                        if (sp < stack_cap) stack[sp++] = o;
+                        else atomicOr(d.status, ST_STACK_OVERFLOW);
+                    }
+                }
+            }
+            if (rc > rs) {
+                d.isl_row_start[s + ni] = rs;
+                d.isl_row_count[s + ni] = rc - rs;
+                d.isl_body_start[s + ni] = bs;
+                d.isl_body_count[s + ni] = bc - bs;
+                d.isl_world[s + ni] = w;
+                ni++;
+            } else {
+                bc = bs;
+            }
+        }
+        d.isl_count_w[w] = ni;
+        sh_rows_end = rc;
+    }
+    __syncthreads();
+    const int rows_end = sh_rows_end;
+    for (int r = c0 + tid; r < rows_end; r += nt) {
+        int c = d.row_contact[r];
+        d.row_of_contact[c] = r;
+        uint64_t key = d.e_new.key[d.c_new.edge[c]];
+        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+        d.rows[r].sa = (d.movement[a] == 0) ? d.visited[a] : -1;
+        d.rows[r].sb = (d.movement[b] == 0) ? d.visited[b] : -1;
+        d.rows[r].contact = c;
+    }
+}
+
+__global__ void k_island_copy(Dev d) {
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < d.n_worlds; w += gridDim.x * blockDim.x) {
+        int s = d.world_start[w], n = d.isl_count_w[w], o = d.isl_scan[w];
+        for (int k = 0; k < n; k++) {
+            d.g_isl_row_start[o + k] = d.isl_row_start[s + k];
+            d.g_isl_row_count[o + k] = d.isl_row_count[s + k];
+            d.g_isl_body_start[o + k] = d.isl_body_start[s + k];
+            d.g_isl_body_count[o + k] = d.isl_body_count[s + k];
+            d.g_isl_world[o + k] = d.isl_world[s + k];
+        }
+    }
+}
+
+int grid_for(int n, int per_block, int n_sms) {
+    int g = (n + per_block - 1) / per_block;
+    int cap = n_sms * 8;
+    return g < 1 ? 1 : (g > cap ? cap : g);
+}
+
+}  // namespace
+
+void launch_merge(const Dev& d, const Launch& L) {
+    const int gb = L.n_sms * 4, bs = 256;
+    int* cnt = d.cnt;
+    k_surv<<<gb, bs, 0, L.st>>>(d);
+    scan_exclusive(d.surv, d.surv_scan, d.n_edges_old, 0, d.cap_edges, cnt + 0, d.scan_tmp, L);
+    k_pair_match<<<gb, bs, 0, L.st>>>(d);
+    scan_exclusive(d.unm, d.unm_scan, d.n_pairs, 0, d.cap_pairs, cnt + 1, d.scan_tmp, L);
+    k_place<<<gb, bs, 0, L.st>>>(d, cnt);
+    k_edge_total<<<1, 1, 0, L.st>>>(d, cnt);
+    k_contacts<<<gb, 128, 0, L.st>>>(d, 0);
+    scan_exclusive(d.edge_cnt, d.e_new.cstart, d.n_edges_new, 0, d.cap_edges, d.n_contacts_new, d.scan_tmp, L);
+    k_contact_total<<<1, 1, 0, L.st>>>(d);
+    k_contacts<<<gb, 128, 0, L.st>>>(d, 1);
+}
+
+void launch_islands(const Dev& d, const Launch& L) {
+    k_islands<<<d.n_worlds, 256, 0, L.st>>>(d);
+    scan_exclusive(d.isl_count_w, d.isl_scan, nullptr, d.n_worlds, d.n_worlds, d.n_islands, d.scan_tmp, L);
+    k_island_copy<<<grid_for(d.n_worlds, 128, L.n_sms), 128, 0, L.st>>>(d);
+}
+
+}  // namespace cpgpu

@@ -1,0 +1,29 @@
+// kernels.cuh — launch wrappers of the contact-path kernels.  All kernels take
+// the batch's device-pointer table (Dev) by value and read per-step sizes from
+// device counters, so one step's launch sequence can be captured in a graph.
+#pragma once
+#include "layout.h"
+
+namespace cpgpu {
+
+struct Launch {
+    int n_sms;
+    cudaStream_t st;
+};
+
+// device-counted exclusive scan: out[i] = sum(in[0..i)), *total = sum(in[0..n))
+// where n = *n_dev (or n_host when n_dev is null); tmp needs 2 + cap/1024 ints.
+void scan_exclusive(const int* in, int* out, const int* n_dev, int n_host, int cap, int* total, int* tmp, const Launch& L);
+
+void prepare_kernels();   // one-time function attributes (outside graph capture)
+void launch_gravity(const Dev& d, const Launch& L);
+void launch_pairs(const Dev& d, const Launch& L);
+void launch_geometry(const Dev& d, int force_all, const Launch& L);
+void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, cudaStream_t st);
+void launch_merge(const Dev& d, const Launch& L);
+void launch_islands(const Dev& d, const Launch& L);
+void launch_rows(const Dev& d, int first, int last, const Launch& L);
+void launch_pgs(const Dev& d, const Launch& L);
+void launch_integrate(const Dev& d, int last, const Launch& L);
+
+}  // namespace cpgpu

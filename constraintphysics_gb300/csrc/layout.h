@@ -1,0 +1,164 @@
+// layout.h — device data layout of the GB300 contact path (shared by the host
+// engine and the kernels).
+//
+// One "batch" holds any number of independent worlds in segmented
+// structure-of-arrays buffers: bodies of world w occupy the contiguous global
+// index range [world_body_start[w], world_body_start[w+1]); a single world is a
+// batch of one.  Everything a step touches lives in HBM; per-step sizes (pairs,
+// edges, contacts, islands) are device-side counters so the whole step can be
+// captured once in a CUDA graph and replayed.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cpgpu {
+
+// ---- packed convex-hull blob -------------------------------------------------
+// 16-byte aligned, size a multiple of 16 B, copied into shared memory with one
+// bulk copy.  All geometry is in the body's reference frame (centred on the
+// centre of mass), FP32.  Section offsets are in bytes from the blob start.
+struct alignas(16) HullHeader {
+    uint16_t nv, nf, ne, na;       // vertices, faces, edges, Gauss arcs
+    uint16_t nfi, size16;          // face-index count, blob size in 16 B units
+    uint16_t off_norm, off_cache;  // float4 sections
+    uint16_t off_fofs, off_fidx;   // face CSR (uint16 offsets, uint8 vertex ids)
+    uint16_t off_edge, off_arc;    // uint8 pairs
+    uint16_t off_vfofs, off_vfidx; // vertex -> adjacent faces CSR
+    uint16_t off_veofs, off_veidx; // vertex -> adjacent edges CSR
+    uint32_t kind;                 // 0 = hull
+    float radius;                  // bound on |vertex| (reference frame)
+    uint32_t pad[2];
+};
+static_assert(sizeof(HullHeader) == 48, "hull header size");
+// verts follow the header: float4 {x, y, z, 0} x nv
+// norm:  float4 {nx, ny, nz, redundant ? 1 : 0} x nf  (Gauss-map vertices)
+// cache: float4 {max, min, bits(max_id), bits(min_id)} x nf: extrema of the hull
+//        along its own face normal, in the reference frame; the world value adds
+//        dot(R n, com) (the recentring of CollisionDetect.cpp:622-625)
+constexpr int kMaxHullVerts = 255;   // uint8 vertex ids
+constexpr int kMaxHullFaces = 255;
+constexpr int kMaxHullEdges = 255;
+constexpr int kMaxHullBlob = 16384; // bytes; bigger hulls are rejected
+
+// ---- per-world parameters (PhysicsEngine.h:170-227) ---------------------------
+struct WorldParams {
+    float dt, dt_sub;
+    float gx, gy, gz;
+    float cfm;
+    float cutoff_vel;            // 2 |g| dt (PhysicsEngine.h:203)
+    float hardness;              // contact_pos_correct_hardness
+    int contact_life;
+    int angle_ticks;
+    int gyro_disabled;
+    int warm_disabled;
+    int pgs_vel, pgs_pos;
+    int pad[2];
+};
+
+// ---- status word bits ----------------------------------------------------------
+enum StatusBits : int {
+    ST_PAIR_OVERFLOW = 1, ST_EDGE_OVERFLOW = 2, ST_CONTACT_OVERFLOW = 4,
+    ST_NAN = 8, ST_TIMEOUT = 16, ST_CLIP_OVERFLOW = 32, ST_STACK_OVERFLOW = 64,
+};
+
+// contact state word: bits 0-7 life (int8), bit 8 live, bit 9 static_ready, bit 10 dead
+__host__ __device__ inline int cs_life(int s) { return (int)(int8_t)(s & 0xff); }
+__host__ __device__ inline bool cs_live(int s) { return (s >> 8) & 1; }
+__host__ __device__ inline bool cs_static(int s) { return (s >> 9) & 1; }
+__host__ __device__ inline bool cs_dead(int s) { return (s >> 10) & 1; }
+__host__ __device__ inline int cs_make(int life, bool live, bool st, bool dead) {
+    return (life & 0xff) | ((int)live << 8) | ((int)st << 9) | ((int)dead << 10);
+}
+
+// One persistent contact point (PersistentConstraint.h:51-86), SoA over the
+// contact store.  p1/p2/n are local to body 1 / body 2 / body 1.
+struct ContactStore {
+    uint64_t* magic;     // bID of the MagicID (cID is implied by the edge)
+    float4* p1;          // xyz p1_local, w pen_depth
+    float4* p2;          // xyz p2_local, w bounce
+    float4* n;           // xyz n_local_b1, w friction_coeff
+    float4* imp;         // normal impulse, friction impulse u, w, unused
+    float4* fu;          // friction basis u of the last rebuild
+    float4* fw;          // friction basis w
+    int* state;          // cs_* bits
+    int* edge;           // owning edge (index in the edge list)
+};
+
+struct EdgeStore {
+    uint64_t* key;       // (global body a) << 32 | global body b, a < b
+    int* cstart;         // first contact
+    int* ccount;         // contacts of the edge
+};
+
+// Solver row block of one contact (normal row + 2-dof friction row), built each
+// substep in island order (ConstraintSolver.cpp:240-343).
+struct alignas(16) RowBlock {
+    int sa, sb;          // island body slots (-1 = body with infinite mass)
+    int contact;         // contact index
+    int ga, gb;          // global body indices
+    float bounce;
+    float tgt_n, tgt_f0, tgt_f1;   // velocity targets set at the start of PGS
+    float nja[6], njb[6], nita[6], nitb[6];
+    float nminv, nptarget, cutoff, fcoeff;
+    float fja[12], fjb[12], fita[12], fitb[12];   // row-major [2][6] / [6][2]
+    float fminv[4];
+    float imp_n, pimp_n, imp_f0, imp_f1;
+};
+
+struct Batch;  // host object, engine.cu
+
+// All device pointers of a batch, passed by value to kernels.
+struct Dev {
+    int n_worlds, n_bodies;
+    int cap_pairs, cap_edges, cap_contacts;
+    const WorldParams* wparams;
+    const int* world_start;        // [n_worlds + 1]
+    const int* map_order;          // bodies of each world in node-map iteration order
+    // bodies
+    float4 *pos, *rot, *vel, *angv, *pvel, *pangv;   // pos.w = inverse mass
+    float *iinv, *iw;              // world inverse inertia / inertia, 9 floats each
+    const float *iref, *iinv_ref;  // reference-frame tensors, 9 floats each
+    const int* shape;              // byte offset of the body's hull blob
+    const int* world;              // world index of the body
+    const uint8_t* movement;
+    const float4* material;        // restitution, kinetic, static, unused
+    float4 *aabb_lo, *aabb_hi;
+    int* moved;
+    const uint8_t* shapes;         // hull blob pool
+    // broadphase
+    int* pair_count;               // per body, then exclusive scan
+    int* pair_a; int* pair_b;
+    int* n_pairs;
+    // narrowphase output per pair
+    float4* mf_n;                  // normal xyz, w max_pen (<= 0: no manifold)
+    int* mf_cnt;
+    float4* mf_pt;                 // [4] per pair: pos xyz, w pen
+    uint64_t* mf_magic;            // [4] per pair
+    // persistent graph (double-buffered by the host)
+    EdgeStore e_old, e_new;
+    ContactStore c_old, c_new;
+    int *n_edges_old, *n_edges_new, *n_contacts_old, *n_contacts_new;
+    // merge scratch
+    int *surv, *surv_scan, *unm, *unm_scan, *pair_edge, *edge_src, *edge_pair, *edge_cnt;
+    int *scan_tmp;
+    // islands
+    int* adj_ofs;                  // per body CSR offsets (scratch)
+    int* adj_list;                 // other endpoint | edge index (scratch, 2 ints per entry)
+    int* adj_cursor;
+    int* visited;                  // per body: island-local slot (-1 = not visited)
+    int* stack;                    // per world DFS stack (scratch)
+    int* isl_count_w;              // islands per world
+    int* isl_row_start; int* isl_row_count; int* isl_body_start; int* isl_body_count; int* isl_world;
+    int* isl_scan;
+    int* g_isl_row_start; int* g_isl_row_count; int* g_isl_body_start; int* g_isl_body_count; int* g_isl_world;
+    int* n_islands;
+    int* isl_bodies;               // island body lists (global body index), per-world region
+    int* row_contact;              // row slot -> contact
+    int* row_of_contact;           // contact -> row slot
+    RowBlock* rows;
+    float4* dv;                    // 4 float4 per island body slot: dv lin, dv ang, dpv lin, dpv ang
+    int* cnt;                      // small device counters (merge totals)
+    int* status;
+};
+
+}  // namespace cpgpu

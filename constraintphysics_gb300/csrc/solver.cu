@@ -1,0 +1,371 @@
+// solver.cu — per-substep row rebuild, projected Gauss-Seidel and integration.
+//
+// Rows (Contact::updateSolverConstraints, PersistentConstraint.cpp:201-215;
+// ContactConstraint / FrictionConstraint constructors, ConstraintSolver.cpp:
+// 240-343): one thread per live contact rebuilds its normal row and 2-dof
+// friction row from the current poses and writes them, with the warm-start
+// impulses (the friction impulse re-projected onto the new tangent basis), to
+// the contact's slot in island order.  The same pass advances the contact's
+// lifetime (PhysicsEngine.cpp:1378-1399) and marks expired contacts.
+//
+// PGS (PGS_solve, ConstraintSolver.cpp:80-213): one thread per island walks
+// its rows in the reference's order: targets from the bodies' velocities,
+// warm start, n_vel velocity sweeps of block Gauss-Seidel with the projection
+// on the accumulated impulse, n_pos pseudo-velocity sweeps of the normal rows,
+// then the velocity deltas are applied to the island's bodies.  A serial chain
+// per island is the latency-optimal form of Gauss-Seidel (each row depends on
+// the previous one); throughput comes from running thousands of islands at
+// once.
+//
+// Integration (PhysicsEngine.cpp:390-419, RigidBody.cpp:207-279): one thread
+// per body.
+#include "kernels.cuh"
+#include "devmath.cuh"
+
+namespace cpgpu {
+
+namespace {
+
+constexpr float kZero = 0.00000001f;  // NVec::isZero cutoff (Math/src/NVec.h:4)
+
+__device__ __forceinline__ f3 qrotate(float4 q, f3 v) {  // Quaternion::applyRotation
+    float r = q.x, i = q.y, j = q.z, k = q.w;
+    return mk(v.x * (r * r + i * i - j * j - k * k) + v.y * (2 * i * j - 2 * r * k) + v.z * (2 * i * k + 2 * r * j),
+              v.x * (2 * i * j + 2 * r * k) + v.y * (r * r - i * i + j * j - k * k) + v.z * (2 * j * k - 2 * r * i),
+              v.x * (2 * i * k - 2 * r * j) + v.y * (2 * j * k + 2 * r * i) + v.z * (r * r - i * i - j * j + k * k));
+}
+
+// J angular part n^T [r]x (ConstraintSolver.cpp:247-252)
+__device__ __forceinline__ f3 nskew(f3 n, f3 r) {
+    return mk(n.y * r.z - n.z * r.y, n.z * r.x - n.x * r.z, n.x * r.y - n.y * r.x);
+}
+
+__device__ __forceinline__ void it_of(float im, const M33& I, const float* j, float* out) {
+    out[0] = im * j[0]; out[1] = im * j[1]; out[2] = im * j[2];
+    f3 a = mul(I, mk(j[3], j[4], j[5]));
+    out[3] = a.x; out[4] = a.y; out[5] = a.z;
+}
+
+__device__ __forceinline__ float dot6(const float* a, const float* b) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) s += a[k] * b[k];
+    return s;
+}
+
+__global__ void k_rows(Dev d, int first, int last) {
+    const int nc = *d.n_contacts_new;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        int st = d.c_new.state[c];
+        const bool live = cs_live(st);
+        const int r = live ? d.row_of_contact[c] : -1;
+        if (live && r >= 0) {
+            const uint64_t key = d.e_new.key[d.c_new.edge[c]];
+            const int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+            const WorldParams& P = d.wparams[d.world[a]];
+            const float dt = P.dt_sub;
+            const float4 qa = d.rot[a], qb = d.rot[b];
+            const f3 ca = mk(d.pos[a]), cb = mk(d.pos[b]);
+            const float ima = d.pos[a].w, imb = d.pos[b].w;
+            const M33 Ia = load9(d.iinv + 9 * a), Ib = load9(d.iinv + 9 * b);
+            const float4 p1 = d.c_new.p1[c], p2 = d.c_new.p2[c], nl = d.c_new.n[c], imp = d.c_new.imp[c];
+            const f3 pa = qrotate(qa, mk(p1)) + ca;
+            const f3 pb = qrotate(qb, mk(p2)) + cb;
+            const f3 n = qrotate(qa, mk(nl));
+            const float depth = dot(pb - pa, n) + p1.w;
+            const float wn = P.warm_disabled ? 0.f : imp.x;
+            const float wf0 = P.warm_disabled ? 0.f : imp.y, wf1 = P.warm_disabled ? 0.f : imp.z;
+            const float pcc = fminf(P.hardness * dt, 1.0f / dt);
+            const f3 rA = pa - ca, rB = pa - cb;
+            RowBlock& R = d.rows[r];
+            R.ga = a; R.gb = b;
+            R.bounce = p2.w;
+            R.cutoff = P.cutoff_vel;
+            R.fcoeff = nl.w;
+            // normal row
+            float ja[6], jb[6], ia[6], ib[6];
+            f3 t = nskew(n, rA), t2 = nskew(-n, rB);
+            ja[0] = -n.x; ja[1] = -n.y; ja[2] = -n.z; ja[3] = t.x; ja[4] = t.y; ja[5] = t.z;
+            jb[0] = n.x; jb[1] = n.y; jb[2] = n.z; jb[3] = t2.x; jb[4] = t2.y; jb[5] = t2.z;
+            it_of(ima, Ia, ja, ia);
+            it_of(imb, Ib, jb, ib);
+            float itv = dot6(ja, ia) + dot6(jb, ib);
+            for (int k = 0; k < 6; k++) { R.nja[k] = ja[k]; R.njb[k] = jb[k]; R.nita[k] = ia[k]; R.nitb[k] = ib[k]; }
+            R.nminv = 1.0f / (itv * (1.0f + P.cfm));
+            R.nptarget = fmaxf(0.0f, depth - 0.05f) * pcc;
+            R.imp_n = wn;
+            R.pimp_n = 0.f;
+            // friction rows in the tangent basis of n, warm impulse re-projected
+            f3 u, w;
+            basis(n, &u, &w);
+            const f3 su = mk(d.c_new.fu[c]), sw = mk(d.c_new.fw[c]);
+            R.imp_f0 = dot(u, su) * wf0 + dot(u, sw) * wf1;
+            R.imp_f1 = dot(w, su) * wf0 + dot(w, sw) * wf1;
+            float fja[12], fjb[12], fia[12], fib[12];
+            f3 ta = nskew(-u, rA), tb = nskew(u, rB), wa = nskew(-w, rA), wb = nskew(w, rB);
+            fja[0] = u.x; fja[1] = u.y; fja[2] = u.z; fja[3] = ta.x; fja[4] = ta.y; fja[5] = ta.z;
+            fja[6] = w.x; fja[7] = w.y; fja[8] = w.z; fja[9] = wa.x; fja[10] = wa.y; fja[11] = wa.z;
+            fjb[0] = -u.x; fjb[1] = -u.y; fjb[2] = -u.z; fjb[3] = tb.x; fjb[4] = tb.y; fjb[5] = tb.z;
+            fjb[6] = -w.x; fjb[7] = -w.y; fjb[8] = -w.z; fjb[9] = wb.x; fjb[10] = wb.y; fjb[11] = wb.z;
+            float tmp[6];
+            for (int row = 0; row < 2; row++) {
+                it_of(ima, Ia, fja + 6 * row, tmp);
+                for (int k = 0; k < 6; k++) fia[2 * k + row] = tmp[k];
+                it_of(imb, Ib, fjb + 6 * row, tmp);
+                for (int k = 0; k < 6; k++) fib[2 * k + row] = tmp[k];
+            }
+            float fv[4];
+            for (int i = 0; i < 2; i++)
+                for (int j = 0; j < 2; j++) {
+                    float sa = 0.f, sb = 0.f;
+                    for (int k = 0; k < 6; k++) { sa += fja[6 * i + k] * fia[2 * k + j]; sb += fjb[6 * i + k] * fib[2 * k + j]; }
+                    fv[2 * i + j] = sa + sb;
+                }
+            fv[0] *= (1.0f + P.cfm);
+            fv[3] *= (1.0f + P.cfm);
+            float di = 1.0f / (fv[0] * fv[3] - fv[1] * fv[2]);
+            R.fminv[0] = fv[3] * di; R.fminv[1] = -fv[1] * di; R.fminv[2] = -fv[2] * di; R.fminv[3] = fv[0] * di;
+            for (int k = 0; k < 12; k++) { R.fja[k] = fja[k]; R.fjb[k] = fjb[k]; R.fita[k] = fia[k]; R.fitb[k] = fib[k]; }
+            d.c_new.fu[c] = make_float4(u.x, u.y, u.z, 0.f);
+            d.c_new.fw[c] = make_float4(w.x, w.y, w.z, 0.f);
+        }
+        // lifetime (PhysicsEngine.cpp:1378-1399, expiry :1434-1446)
+        int life = cs_life(st);
+        bool lv = live;
+        if (last) { life -= 1; lv = false; }
+        bool dead = cs_dead(st) || (first && life < 0);
+        // a rebuilt FrictionConstraint starts with static_ready = false
+        d.c_new.state[c] = cs_make(life, lv, live ? false : cs_static(st), dead);
+    }
+}
+
+struct DV6 { float v[6]; };
+
+__device__ __forceinline__ void load_dv(const float4* dv, int slot, int which, float* out) {
+    if (slot < 0) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
+    float4 l = dv[4 * slot + 2 * which], a = dv[4 * slot + 2 * which + 1];
+    out[0] = l.x; out[1] = l.y; out[2] = l.z; out[3] = a.x; out[4] = a.y; out[5] = a.z;
+}
+__device__ __forceinline__ void store_dv(float4* dv, int slot, int which, const float* v) {
+    if (slot < 0) return;
+    dv[4 * slot + 2 * which] = make_float4(v[0], v[1], v[2], 0.f);
+    dv[4 * slot + 2 * which + 1] = make_float4(v[3], v[4], v[5], 0.f);
+}
+__device__ __forceinline__ void body_vel(const Dev& d, int g, float* out) {
+    if (d.movement[g] == 1) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
+    float4 v = d.vel[g], w = d.angv[g];
+    out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = w.x; out[4] = w.y; out[5] = w.z;
+}
+
+__global__ void k_pgs(Dev d) {
+    const int ni = *d.n_islands;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
+        const int rs = d.g_isl_row_start[i], rc = d.g_isl_row_count[i];
+        const int bs = d.g_isl_body_start[i], bc = d.g_isl_body_count[i];
+        const WorldParams& P = d.wparams[d.g_isl_world[i]];
+        float4* dv = d.dv + 4 * (size_t)bs;
+        for (int k = 0; k < 4 * bc; k++) dv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        // targets (ContactConstraint::findTargetConstraintValue, ConstraintSolver.cpp:264-268)
+        for (int r = rs; r < rs + rc; r++) {
+            RowBlock& R = d.rows[r];
+            float va[6], vb[6];
+            body_vel(d, R.ga, va);
+            body_vel(d, R.gb, vb);
+            float cur = dot6(R.nja, va) + dot6(R.njb, vb);
+            R.tgt_n = (cur < -R.cutoff) ? -(1.0f + R.bounce) * cur : -cur;
+            R.tgt_f0 = -(dot6(R.fja, va) + dot6(R.fjb, vb));
+            R.tgt_f1 = -(dot6(R.fja + 6, va) + dot6(R.fjb + 6, vb));
+        }
+        // warm start
+        for (int r = rs; r < rs + rc; r++) {
+            const RowBlock& R = d.rows[r];
+            float va[6], vb[6];
+            load_dv(dv, R.sa, 0, va);
+            load_dv(dv, R.sb, 0, vb);
+            if (fabsf(R.imp_n) > kZero) {
+                for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * R.imp_n; vb[k] += R.nitb[k] * R.imp_n; }
+            }
+            if (fabsf(R.imp_f0) > kZero || fabsf(R.imp_f1) > kZero) {
+                for (int k = 0; k < 6; k++) {
+                    va[k] += R.imp_f0 * R.fita[2 * k] + R.imp_f1 * R.fita[2 * k + 1];
+                    vb[k] += R.imp_f0 * R.fitb[2 * k] + R.imp_f1 * R.fitb[2 * k + 1];
+                }
+            }
+            store_dv(dv, R.sa, 0, va);
+            store_dv(dv, R.sb, 0, vb);
+        }
+        // velocity sweeps (PGSConstraintStep, ConstraintSolver.cpp:12-40)
+        for (int it = 0; it < P.pgs_vel; it++) {
+            for (int r = rs; r < rs + rc; r++) {
+                RowBlock& R = d.rows[r];
+                float va[6], vb[6];
+                load_dv(dv, R.sa, 0, va);
+                load_dv(dv, R.sb, 0, vb);
+                {   // normal row, impulse clamped at zero
+                    float cur = dot6(R.nja, va) + dot6(R.njb, vb);
+                    float nw = R.imp_n + R.nminv * (R.tgt_n - cur);
+                    float diff = fmaxf(nw, 0.0f) - R.imp_n;
+                    if (fabsf(diff) > kZero) {
+                        for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * diff; vb[k] += R.nitb[k] * diff; }
+                        R.imp_n += diff;
+                    }
+                }
+                {   // friction rows, impulse projected on the friction disc
+                    float c0 = dot6(R.fja, va) + dot6(R.fjb, vb);
+                    float c1 = dot6(R.fja + 6, va) + dot6(R.fjb + 6, vb);
+                    float d0 = R.tgt_f0 - c0, d1 = R.tgt_f1 - c1;
+                    float n0 = R.imp_f0 + (d0 * R.fminv[0] + d1 * R.fminv[1]);
+                    float n1 = R.imp_f1 + (d0 * R.fminv[2] + d1 * R.fminv[3]);
+                    float mx = R.fcoeff * R.imp_n;
+                    float mg = sqrtf(n0 * n0 + n1 * n1);
+                    int sr;
+                    if (mg > mx) { float s = mx / mg; n0 *= s; n1 *= s; sr = 0; }
+                    else sr = 1;
+                    int cst = d.c_new.state[R.contact];
+                    d.c_new.state[R.contact] = sr ? (cst | (1 << 9)) : (cst & ~(1 << 9));
+                    float e0 = n0 - R.imp_f0, e1 = n1 - R.imp_f1;
+                    if (fabsf(e0) > kZero || fabsf(e1) > kZero) {
+                        for (int k = 0; k < 6; k++) {
+                            va[k] += e0 * R.fita[2 * k] + e1 * R.fita[2 * k + 1];
+                            vb[k] += e0 * R.fitb[2 * k] + e1 * R.fitb[2 * k + 1];
+                        }
+                        R.imp_f0 += e0;
+                        R.imp_f1 += e1;
+                    }
+                }
+                store_dv(dv, R.sa, 0, va);
+                store_dv(dv, R.sb, 0, vb);
+            }
+        }
+        // pseudo-velocity sweeps of the normal rows (position correction)
+        for (int it = 0; it < P.pgs_pos; it++) {
+            for (int r = rs; r < rs + rc; r++) {
+                RowBlock& R = d.rows[r];
+                float va[6], vb[6];
+                load_dv(dv, R.sa, 1, va);
+                load_dv(dv, R.sb, 1, vb);
+                float cur = dot6(R.nja, va) + dot6(R.njb, vb);
+                float nw = R.pimp_n + R.nminv * (R.nptarget - cur);
+                float diff = fmaxf(nw, 0.0f) - R.pimp_n;
+                if (fabsf(diff) > kZero) {
+                    for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * diff; vb[k] += R.nitb[k] * diff; }
+                    R.pimp_n += diff;
+                    store_dv(dv, R.sa, 1, va);
+                    store_dv(dv, R.sb, 1, vb);
+                }
+            }
+        }
+        // impulses back to the contacts (warm start of the next rebuild)
+        for (int r = rs; r < rs + rc; r++) {
+            const RowBlock& R = d.rows[r];
+            d.c_new.imp[R.contact] = make_float4(R.imp_n, R.imp_f0, R.imp_f1, 0.f);
+        }
+        // PhysicsEngine::applyVelocityChange (PhysicsEngine.cpp:1113-1136)
+        for (int k = 0; k < bc; k++) {
+            int g = d.isl_bodies[bs + k];
+            if (d.movement[g] != 0) continue;
+            float4 a = dv[4 * k], b = dv[4 * k + 1], c = dv[4 * k + 2], e = dv[4 * k + 3];
+            float4 v = d.vel[g], w = d.angv[g], pv = d.pvel[g], pw = d.pangv[g];
+            d.vel[g] = make_float4(v.x + a.x, v.y + a.y, v.z + a.z, 0.f);
+            d.angv[g] = make_float4(w.x + b.x, w.y + b.y, w.z + b.z, 0.f);
+            d.pvel[g] = make_float4(pv.x + c.x, pv.y + c.y, pv.z + c.z, 0.f);
+            d.pangv[g] = make_float4(pw.x + e.x, pw.y + e.y, pw.z + e.z, 0.f);
+        }
+    }
+}
+
+__device__ M33 crossm(f3 v) {
+    M33 o;
+    o.m[0] = 0.f;  o.m[1] = -v.z; o.m[2] = v.y;
+    o.m[3] = v.z;  o.m[4] = 0.f;  o.m[5] = -v.x;
+    o.m[6] = -v.y; o.m[7] = v.x;  o.m[8] = 0.f;
+    return o;
+}
+
+__global__ void k_integrate(Dev d, int last) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
+        const int mv = d.movement[i];
+        if (mv == 1) continue;
+        const WorldParams& P = d.wparams[d.world[i]];
+        const float dt = P.dt_sub;
+        float4 pos = d.pos[i], q = d.rot[i];
+        const float4 pos0 = pos, q0 = q;
+        f3 v = mk(d.vel[i]), w = mk(d.angv[i]), pv = mk(d.pvel[i]), pw = mk(d.pangv[i]);
+        f3 c = mk(pos) + (v + pv) * dt;
+        pos.x = c.x; pos.y = c.y; pos.z = c.z;
+        if (mag2(w) != 0.f) {
+            const bool no_gyro = P.gyro_disabled || mv == 2;
+            if (no_gyro) {
+                q = qmul(qaxis(mag(w) * dt, normalize(w)), q);
+            } else {
+                // RigidBody::rotateWhileApplyingGyroAccel: implicit Euler on the
+                // gyroscopic term, angle_ticks sub-steps of two Newton iterations
+                const M33 Iref = load9(d.iref + 9 * i);
+                M33 it = load9(d.iw + 9 * i);
+                float4 iq = q;
+                f3 iw = w;
+                const int n_itr = P.angle_ticks;
+                for (int s = 0; s < n_itr; s++) {
+                    f3 wv = iw;
+                    float ts = dt / n_itr;
+                    for (int k = 0; k < 2; k++) {
+                        f3 Iw = mul(it, wv);
+                        f3 f = ts * cross(wv, Iw) - mul(it, iw - wv);
+                        M33 cw = mul(crossm(wv), it), ci = crossm(Iw);
+                        M33 jac;
+                        for (int m = 0; m < 9; m++) jac.m[m] = it.m[m] + ts * (cw.m[m] - ci.m[m]);
+                        if (fabsf(det(jac)) > 0.00000000001f) wv = wv - mul(inverse(jac), f);
+                    }
+                    iw = wv;
+                    iq = qmul(qaxis(ts * mag(iw), iw), iq);
+                    if (s + 1 < n_itr) {
+                        M33 R = quatRot(iq), Rc = quatRot(qconj(iq));
+                        it = mul(mul(R, Iref), Rc);
+                    }
+                }
+                q = iq;
+                w = iw;
+            }
+            q = qmul(qaxis(dt * mag(pw), pw), q);
+        }
+        // RigidBody::updateInertiaTensor (RigidBody.cpp:270-279)
+        q = qnormalize(q);
+        if (mv == 0) {
+            M33 R = quatRot(q), Rc = quatRot(qconj(q));
+            store9(d.iw + 9 * i, mul(mul(R, load9(d.iref + 9 * i)), Rc));
+            store9(d.iinv + 9 * i, mul(mul(R, load9(d.iinv_ref + 9 * i)), Rc));
+        }
+        if (!(isfinite(c.x) && isfinite(c.y) && isfinite(c.z) && isfinite(q.x))) atomicOr(d.status, ST_NAN);
+        d.pos[i] = pos;
+        d.rot[i] = q;
+        d.angv[i] = make_float4(w.x, w.y, w.z, 0.f);
+        d.pvel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        d.pangv[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (last) {
+            bool moved = pos.x != pos0.x || pos.y != pos0.y || pos.z != pos0.z || q.x != q0.x || q.y != q0.y || q.z != q0.z || q.w != q0.w;
+            d.moved[i] = moved;
+        }
+    }
+}
+
+int grid_for(int n, int per_block, int n_sms) {
+    int g = (n + per_block - 1) / per_block;
+    int cap = n_sms * 8;
+    return g < 1 ? 1 : (g > cap ? cap : g);
+}
+
+}  // namespace
+
+void launch_rows(const Dev& d, int first, int last, const Launch& L) {
+    k_rows<<<L.n_sms * 8, 128, 0, L.st>>>(d, first, last);
+}
+
+void launch_pgs(const Dev& d, const Launch& L) {
+    k_pgs<<<L.n_sms * 4, 64, 0, L.st>>>(d);
+}
+
+void launch_integrate(const Dev& d, int last, const Launch& L) {
+    k_integrate<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d, last);
+}
+
+}  // namespace cpgpu

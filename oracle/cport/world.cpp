@@ -566,6 +566,14 @@ int cport_body_set_mass_properties(cpgpu_world* w, uint32_t id, double mass, con
     W(w)->placeBody(b, mass, v3(com_geom), t);
     return CPGPU_OK;
 }
+// Mass properties computed by the restatement (same layout as cpref_get_mass_properties).
+int cport_get_mass_properties(cpgpu_world* w, uint32_t id, double* mass, double* com_geom, double* tensor) {
+    Body* b = B(w, id); if (!b) return fail("bad id");
+    *mass = b->mass;
+    com_geom[0] = -b->local_origin.x; com_geom[1] = -b->local_origin.y; com_geom[2] = -b->local_origin.z;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) tensor[3 * i + j] = b->ref_tensor.m[i][j];
+    return CPGPU_OK;
+}
 int cport_step(cpgpu_world* w, int n) { for (int i = 0; i < n; i++) W(w)->step(); return CPGPU_OK; }
 int cport_num_bodies(cpgpu_world* w, int* n) { *n = (int)W(w)->bodies.size(); return CPGPU_OK; }
 int cport_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel, double* ang) {
