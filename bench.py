@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Batched contact-path throughput on GB300.
+
+Workload (one GPU): 4,096 independent worlds with body counts log-uniform in
+[8, 512] (box pyramids with base 4-16 and random-hull piles as in the 1,000-hull
+drop), each with its own static plate; dt 1/60, one substep, 10 PGS velocity
+iterations + 1 position iteration, warm start on, sleeping off.  A step advances
+every world by one timeStep.
+
+Reported (one JSON line on rank 0):
+  value      batched body-steps/s with the state resident in HBM, device time
+             (CUDA events on the library's stream) of exactly --steps graph-
+             launched steps after --warmup untimed ones
+  e2e        the same through the C ABI with host buffers: every step writes
+             the full body state from pinned host memory, steps, and reads the
+             full state back
+  plain      body-steps/s of the plain path (each world as its own
+             single-world device batch) on an evenly spaced sample of worlds;
+             vs_plain = value / plain
+  roofline   dominant kernel: algorithmic bytes / its measured time against the
+             measured HBM copy bandwidth (MEASURED_PEAKS.json)
+  cpu_baseline  the reference engine (compiled from its own sources) on the
+             box's host cores, one engine per thread, on a bounded sample of
+             the same worlds and steps
+
+--impl reference times only the reference engine on that sample and prints
+its line.  Under torchrun each rank takes its own 4,096 worlds (weak scaling,
+no collective on the data path); rank 0 prints the max-time line.
+"""
+import argparse
+import concurrent.futures
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+from constraintphysics_gb300 import scenes  # noqa: E402
+
+METRIC = "batched body-steps/s vs plain GPU path @ <=1e-3 m drift; p50/p99 step latency"
+UNIT = "body-steps/s"
+WORKLOAD = "batched_4096_worlds"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=60)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--worlds", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--cpu-budget-s", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="build the batch, run warmup + steps, no extras")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def build_worlds(ws_scenes, make_world):
+    worlds = []
+    for sc in ws_scenes:
+        w = make_world()
+        scenes.apply(sc, w)
+        worlds.append(w)
+    return worlds
+
+
+def dynamic_bodies(ws_scenes):
+    return sum(sc.n_bodies - 1 for sc in ws_scenes)   # every world has one fixed plate
+
+
+def hull_sizes(ws_scenes):
+    """Mean vertices / faces / edges over the scenes' hulls (boxes: 8/6/12)."""
+    v = f = e = n = 0
+    for sc in ws_scenes:
+        for op in sc.ops:
+            if op[0] == "hull":
+                nv, nf = len(op[1]), len(op[2])
+                v, f, e, n = v + nv, f + nf, e + nv + nf - 2, n + 1
+            elif op[0] == "box":
+                v, f, e, n = v + 8, f + 6, e + 12, n + 1
+    return v / n, f / n, e / n
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.gpu = gpu_index
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if len(r) > 8]
+        mx = [float(r[2]) for r in rows if len(r) > 8]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) > 8:
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(stage, counts, nbodies, vfe, params):
+    """Algorithmic bytes of one launch of a stage (each datum read/written once)."""
+    V, F, E = vfe
+    npairs, ncont = counts["pairs"], counts["contacts"]
+    iv, ip = params["pgs_vel"], params["pgs_pos"]
+    if stage == "narrowphase":
+        # both poses + both hulls (vertices, face planes, arcs) + manifold out
+        return npairs * (2 * (32 + 16 * V + 16 * F + 4 * E) + 112)
+    if stage == "pgs":
+        # per contact: each velocity sweep reads 3 rows (48 B each) and
+        # read-modify-writes 2 bodies' velocity deltas; each position sweep 1 row + 2 deltas
+        return ncont * (iv * (3 * 48 + 2 * 48) + ip * (48 + 2 * 48))
+    if stage == "rows":
+        return ncont * (64 + 3 * 48)
+    if stage == "integrate":
+        return nbodies * (92 + 52)
+    if stage == "pairs":
+        return nbodies * 32 + npairs * 8
+    return None
+
+
+def run_reference_sample(ws_scenes, warmup, steps, budget_s, threads):
+    """The reference engine on an evenly spaced sample of worlds: one engine per
+    worker thread (ctypes releases the GIL), `warmup` untimed then `steps` timed
+    steps per world.  Returns (body_steps_per_s, sample description, cores)."""
+    import oracle
+    if not oracle.ref_available():
+        oracle.build()
+    abi = oracle.ref_abi()
+    step_untraced = abi._lib.cpref_step_untraced
+    import ctypes
+    step_untraced.restype = ctypes.c_int
+    step_untraced.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    # probe one world to size the sample
+    idx = list(range(0, len(ws_scenes), max(1, len(ws_scenes) // 512)))
+    probe = oracle.ref_world()
+    scenes.apply(ws_scenes[idx[0]], probe)
+    step_untraced(probe.h, warmup)
+    t = time.perf_counter()
+    step_untraced(probe.h, steps)
+    per_body_step = (time.perf_counter() - t) / max(1, steps * (ws_scenes[idx[0]].n_bodies - 1))
+    est_total = per_body_step * steps * sum(ws_scenes[i].n_bodies - 1 for i in idx) / threads
+    keep = max(threads, int(len(idx) * min(1.0, budget_s / max(est_total, 1e-9))))
+    idx = idx[:: max(1, len(idx) // keep)][:keep]
+    worlds = []
+    for i in idx:
+        w = oracle.ref_world()
+        scenes.apply(ws_scenes[i], w)
+        worlds.append((w, ws_scenes[i].n_bodies - 1))
+
+    def warm(item):
+        step_untraced(item[0].h, warmup)
+
+    def timed(item):
+        t0 = time.perf_counter()
+        step_untraced(item[0].h, steps)
+        return time.perf_counter() - t0
+
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(warm, worlds))
+        t0 = time.perf_counter()
+        list(ex.map(timed, worlds))
+        wall = time.perf_counter() - t0
+    body_steps = sum(n for _, n in worlds) * steps
+    sample = (f"{len(worlds)} of {len(ws_scenes)} worlds (every {len(ws_scenes) // max(1, len(idx))}th), "
+              f"{sum(n for _, n in worlds)} dynamic bodies, {warmup} untimed + {steps} timed steps each, "
+              f"one single-threaded reference engine per thread")
+    return body_steps / wall, sample, wall
+
+
+def main():
+    a = parse()
+    rank, world_size, local_rank = dist_env()
+    t_setup = time.perf_counter()
+    ws_scenes = scenes.batched_worlds(seed=a.seed + 1000 * rank, n_worlds=a.worlds)
+    params = {"pgs_vel": 10, "pgs_pos": 1, "substeps": 1}
+    n_dyn = dynamic_bodies(ws_scenes)
+    config = {"workload": WORKLOAD, "worlds": a.worlds, "bodies_per_world": "log-uniform [8, 512]",
+              "dynamic_bodies": n_dyn, "dt": 1 / 60, "substeps": 1, "pgs": [10, 1, 1],
+              "scenes": "box pyramids (base 4-16) and random-hull piles (8-32 vertices), own plate per world",
+              "seed": a.seed, "parallelism": f"world-sharded x{world_size}" if world_size > 1 else "single GPU"}
+    threads = max(1, os.cpu_count() or 1)
+
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        bsps, sample, wall = run_reference_sample(ws_scenes, a.warmup, a.steps, a.cpu_budget_s, threads)
+        line = {"impl": "reference", "metric": METRIC, "value": bsps, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": config,
+                "cpu_baseline": {"value": bsps, "unit": UNIT, "cores": threads, "kind": "reference", "sample": sample},
+                "e2e": {"value": bsps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import constraintphysics_gb300 as cg
+    if world_size > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    worlds = build_worlds(ws_scenes, cg.world)
+    batch = cg.Batch(worlds)
+    setup_s = time.perf_counter() - t_setup
+
+    def barrier():
+        if world_size > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    batch.step(a.warmup)
+    if a.profile_only:
+        batch.step(a.steps)
+        print(json.dumps({"profile_only": True, "steps": a.steps, "warmup": a.warmup}), flush=True)
+        return
+    sampler = ClockSampler(local_rank)
+    barrier()
+    dev_ms = batch.step_timed(a.steps)
+    barrier()
+    # per-step latency distribution over another `steps` steps
+    lat = [batch.step_timed(1) for _ in range(a.steps)]
+    clocks = sampler.stop()
+    if world_size > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    value = n_dyn * a.steps * world_size / (dev_ms / 1e3)
+    info = batch.info()
+
+    # end to end through the C ABI with pinned host buffers
+    try:
+        import torch
+        host = torch.empty((batch.n_bodies, 16), dtype=torch.float32, pin_memory=True)
+        host_desc = "pinned"
+    except Exception:
+        host = np.empty((batch.n_bodies, 16), dtype=np.float32)
+        host_desc = "pageable"
+    batch.read_state(host)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        batch.write_state(host)
+        batch.step(1)
+        batch.read_state(host)
+    e2e_s = time.perf_counter() - t0
+    state_bytes = batch.n_bodies * 64
+    e2e = {"value": n_dyn * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
+           "d2h_bytes_per_step": state_bytes, "host_buffers": host_desc,
+           "call": "cpgpu_batch_write_state + cpgpu_batch_step + cpgpu_batch_read_state per step"}
+
+    # per-stage profile (stage by stage, no graph) for the roofline
+    stage_ms, counts = batch.profile(3)
+    stage_ms = {k: v / 3 for k, v in stage_ms.items()}
+    dominant = max(stage_ms, key=stage_ms.get)
+    vfe = hull_sizes(ws_scenes)
+    peak, peak_kind = measured_peaks()
+    roof = None
+    for stage in [dominant] + [s for s in ("pgs", "narrowphase") if s != dominant]:
+        b = algorithmic_bytes(stage, counts, batch.n_bodies, vfe, params)
+        if b is not None:
+            achieved = b / (stage_ms[stage] / 1e3) / 1e9
+            roof = {"bound": "hbm", "kernel": stage, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                    "algorithmic_bytes_per_launch": b, "launch_ms": stage_ms[stage],
+                    "note": "dominant stage" if stage == dominant else f"dominant stage {dominant} has no byte model"}
+            break
+
+    # plain single-world path on an evenly spaced sample of the same worlds
+    plain = None
+    if a.plain_sample > 0:
+        step = max(1, a.worlds // a.plain_sample)
+        pw = build_worlds([ws_scenes[i] for i in range(0, a.worlds, step)][: a.plain_sample], cg.world)
+        total_bs, total_ms = 0, 0.0
+        for w, i in zip(pw, range(0, a.worlds, step)):
+            b1 = cg.Batch([w])
+            b1.step(a.warmup)
+            total_ms += b1.step_timed(a.steps)
+            total_bs += (ws_scenes[i].n_bodies - 1) * a.steps
+            b1.close()
+        plain = total_bs / (total_ms / 1e3)
+
+    cpu = None
+    if not a.no_cpu and rank == 0:
+        bsps, sample, wall = run_reference_sample(ws_scenes, a.warmup, a.steps, a.cpu_budget_s, threads)
+        cpu = {"value": bsps, "unit": UNIT, "cores": threads, "kind": "reference", "sample": sample}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": dev_ms / a.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
+                "config": dict(config, l2="state larger than L2 (%.0f MB resident)" % (batch.n_bodies * 600 / 1e6),
+                               contacts=info["contacts"]),
+                "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                "plain": {"value": plain, "unit": UNIT, "sample_worlds": a.plain_sample,
+                          "vs_plain": (value / world_size / plain) if plain else None},
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+                "gpu_launches": batch.launches_per_step() * a.steps,
+                "stage_ms": stage_ms, "counts": counts, "setup_s": setup_s}
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -31,10 +31,18 @@ def lib():
             raise RuntimeError(f"{LIB_PATH} is not built: run constraintphysics_gb300.build.build()")
         handle = ctypes.CDLL(LIB_PATH)
         abi = bind(handle, "cpgpu_")
-        fn = handle.cpgpu_batch_step_timed
-        fn.restype = ctypes.c_int
-        fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
-        abi.batch_step_timed = fn
+        extra = {
+            "batch_step_timed": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p],
+            "batch_read_state": [ctypes.c_void_p, ctypes.c_void_p],
+            "batch_write_state": [ctypes.c_void_p, ctypes.c_void_p],
+            "batch_profile": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
+            "batch_launches_per_step": [ctypes.c_void_p, ctypes.c_void_p],
+        }
+        for short, args in extra.items():
+            fn = getattr(handle, "cpgpu_" + short)
+            fn.restype = ctypes.c_int
+            fn.argtypes = args
+            setattr(abi, short, fn)
         abi._lib = handle
         _ABI = abi
     return _ABI
@@ -42,6 +50,12 @@ def lib():
 
 def world():
     return World(lib())
+
+
+def _addr(buf):
+    if hasattr(buf, "data_ptr"):          # torch tensor (e.g. pinned host memory)
+        return buf.data_ptr()
+    return buf.ctypes.data
 
 
 class Batch:
@@ -73,6 +87,36 @@ class Batch:
         self._check(self.abi.batch_get_body_state(self.h, int(wi), com.ctypes.data, quat.ctypes.data,
                                                   vel.ctypes.data, ang.ctypes.data))
         return {"com": com, "quat": quat, "vel": vel, "ang_vel": ang}
+
+    STAGES = ("gravity", "pairs", "narrowphase", "merge", "islands", "rows", "pgs", "integrate", "geometry")
+
+    @property
+    def n_bodies(self):
+        return int(sum(self.sizes))
+
+    def read_state(self, out=None):
+        """All bodies' state, 16 floats per body (see cpgpu_batch_read_state).
+        `out` may be any writable float32 buffer with 16 * n_bodies entries
+        (e.g. pinned host memory); its address is passed to the library."""
+        if out is None:
+            out = np.empty((self.n_bodies, 16), dtype=np.float32)
+        self._check(self.abi.batch_read_state(self.h, _addr(out)))
+        return out
+
+    def write_state(self, buf):
+        self._check(self.abi.batch_write_state(self.h, _addr(buf)))
+
+    def profile(self, n=1):
+        ms = np.zeros(len(self.STAGES))
+        counts = np.zeros(3, dtype=np.int64)
+        self._check(self.abi.batch_profile(self.h, int(n), ms.ctypes.data, counts.ctypes.data))
+        return dict(zip(self.STAGES, ms.tolist())), {"pairs": int(counts[0]), "contacts": int(counts[1]),
+                                                      "islands": int(counts[2])}
+
+    def launches_per_step(self):
+        n = ctypes.c_int()
+        self._check(self.abi.batch_launches_per_step(self.h, ctypes.addressof(n)))
+        return n.value
 
     def info(self):
         nb, nw, nc = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

@@ -233,20 +233,29 @@ struct Batch {
 
     const Dev& cur() const { return d[parity]; }      // old buffers hold the current graph
 
+    // stage markers: when `marks` is set an event is recorded after each stage
+    std::vector<cudaEvent_t>* marks = nullptr;
+    void mark(int stage) {
+        if (marks) CK(cudaEventRecord((*marks)[stage], st));
+    }
     void launch_step(const Dev& x) {
         Launch L{n_sms, st};
-        launch_gravity(x, L);
-        launch_pairs(x, L);
-        launch_narrowphase(x, slot_bytes, n_sms, st);
-        launch_merge(x, L);
-        launch_islands(x, L);
+        mark(0);
+        launch_gravity(x, L);      mark(1);
+        launch_pairs(x, L);        mark(2);
+        launch_narrowphase(x, slot_bytes, n_sms, st); mark(3);
+        launch_merge(x, L);        mark(4);
+        launch_islands(x, L);      mark(5);
         for (int s = 0; s < substeps; s++) {
-            launch_rows(x, s == 0, s == substeps - 1, L);
-            launch_pgs(x, L);
-            launch_integrate(x, s == substeps - 1, L);
+            launch_rows(x, s == 0, s == substeps - 1, L);  mark(6 + 3 * s);
+            launch_pgs(x, L);                              mark(7 + 3 * s);
+            launch_integrate(x, s == substeps - 1, L);     mark(8 + 3 * s);
         }
-        launch_geometry(x, 0, L);
+        launch_geometry(x, 0, L);  mark(6 + 3 * substeps);
     }
+    // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 1,
+    // merge 6 + 3 scans, islands 2 + scan 3, 3 per substep, geometry 1
+    int launches_per_step() const { return 1 + 6 + 1 + (6 + 9) + (2 + 3) + 3 * substeps + 1; }
 
     void build_graphs() {
         for (int p = 0; p < 2; p++) {
@@ -416,9 +425,11 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     }
 
     // ---- capacities and device allocation
-    const int cap_pairs = std::max(1 << 14, env_int("CPGPU_PAIRS_PER_BODY", 24) * N);
+    // capacities per body, with floors; both can be overridden by the environment
+    const int floor_ = env_int("CPGPU_CAPACITY_FLOOR", 1 << 14);
+    const int cap_pairs = std::max(floor_, env_int("CPGPU_PAIRS_PER_BODY", 24) * N);
     const int cap_edges = cap_pairs;
-    const int cap_contacts = std::max(std::max(1 << 15, 2 * (int)cmag.size()), env_int("CPGPU_CONTACTS_PER_BODY", 24) * N);
+    const int cap_contacts = std::max(std::max(2 * floor_, 2 * (int)cmag.size()), env_int("CPGPU_CONTACTS_PER_BODY", 24) * N);
     const int scan_tmp = std::max(cap_pairs, cap_contacts) / 1024 + 64;
     Dev x;
     EdgeStore es[2];
@@ -1010,6 +1021,78 @@ int cpgpu_batch_info(cpgpu_batch* b, int64_t* n_bodies, int64_t* n_worlds, int64
         if (n_worlds) *n_worlds = B.n_worlds;
         if (n_contacts) *n_contacts = counts[3 + B.parity];
         return CPGPU_OK;
+    });
+}
+
+int cpgpu_batch_launches_per_step(cpgpu_batch* b, int* n) {
+    if (!b || !n) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
+    *n = b->b->launches_per_step();
+    return CPGPU_OK;
+}
+
+int cpgpu_batch_read_state(cpgpu_batch* b, float* out) {
+    if (!b || !out) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
+    return guarded([&] {
+        Batch& B = *b->b;
+        const Dev& x = B.cur();
+        const size_t N = B.n_bodies;
+        // four strided copies into the 16-float-per-body host layout
+        const float4* src[4] = {x.pos, x.rot, x.vel, x.angv};
+        for (int k = 0; k < 4; k++)
+            CK(cudaMemcpy2DAsync(out + 4 * k, 64, src[k], 16, 16, N, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaStreamSynchronize(B.st));
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_batch_write_state(cpgpu_batch* b, const float* in) {
+    if (!b || !in) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
+    return guarded([&] {
+        Batch& B = *b->b;
+        const Dev& x = B.cur();
+        const size_t N = B.n_bodies;
+        float4* dst[4] = {x.pos, x.rot, x.vel, x.angv};
+        for (int k = 0; k < 4; k++)
+            CK(cudaMemcpy2DAsync(dst[k], 16, in + 4 * k, 64, 16, N, cudaMemcpyHostToDevice, B.st));
+        launch_refresh(x, Launch{B.n_sms, B.st});
+        CK(cudaStreamSynchronize(B.st));
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* counts) {
+    if (!b || !stage_ms) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
+    return guarded([&] {
+        Batch& B = *b->b;
+        const int n_marks = 7 + 3 * B.substeps;
+        std::vector<cudaEvent_t> ev(n_marks);
+        for (auto& e : ev) CK(cudaEventCreate(&e));
+        for (int k = 0; k < CPGPU_N_STAGES; k++) stage_ms[k] = 0;
+        B.marks = &ev;
+        for (int i = 0; i < n_steps; i++) {
+            B.launch_step(B.d[B.parity]);
+            B.parity ^= 1;
+            CK(cudaEventSynchronize(ev[n_marks - 1]));
+            auto span = [&](int a, int c) { float ms = 0; CK(cudaEventElapsedTime(&ms, ev[a], ev[c])); return (double)ms; };
+            for (int k = 0; k < 5; k++) stage_ms[k] += span(k, k + 1);
+            for (int s = 0; s < B.substeps; s++) {
+                stage_ms[5] += span(5 + 3 * s, 6 + 3 * s);
+                stage_ms[6] += span(6 + 3 * s, 7 + 3 * s);
+                stage_ms[7] += span(7 + 3 * s, 8 + 3 * s);
+            }
+            stage_ms[8] += span(5 + 3 * B.substeps, 6 + 3 * B.substeps);
+        }
+        B.marks = nullptr;
+        for (auto& e : ev) cudaEventDestroy(e);
+        if (counts) {
+            int c[6];
+            CK(cudaMemcpyAsync(c, B.cur().n_pairs, sizeof(c), cudaMemcpyDeviceToHost, B.st));
+            CK(cudaStreamSynchronize(B.st));
+            counts[0] = c[0];
+            counts[1] = c[3 + B.parity];
+            counts[2] = c[5];
+        }
+        return B.check_status();
     });
 }
 

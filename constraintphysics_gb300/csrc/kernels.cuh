@@ -25,5 +25,7 @@ void launch_islands(const Dev& d, const Launch& L);
 void launch_rows(const Dev& d, int first, int last, const Launch& L);
 void launch_pgs(const Dev& d, const Launch& L);
 void launch_integrate(const Dev& d, int last, const Launch& L);
+// after an external state write: world inertia tensors and AABBs from the poses
+void launch_refresh(const Dev& d, const Launch& L);
 
 }  // namespace cpgpu

@@ -348,6 +348,17 @@ __global__ void k_integrate(Dev d, int last) {
     }
 }
 
+__global__ void k_refresh_tensors(Dev d) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
+        if (d.movement[i] != 0) continue;
+        float4 q = qnormalize(d.rot[i]);
+        d.rot[i] = q;
+        M33 R = quatRot(q), Rc = quatRot(qconj(q));
+        store9(d.iw + 9 * i, mul(mul(R, load9(d.iref + 9 * i)), Rc));
+        store9(d.iinv + 9 * i, mul(mul(R, load9(d.iinv_ref + 9 * i)), Rc));
+    }
+}
+
 int grid_for(int n, int per_block, int n_sms) {
     int g = (n + per_block - 1) / per_block;
     int cap = n_sms * 8;
@@ -366,6 +377,11 @@ void launch_pgs(const Dev& d, const Launch& L) {
 
 void launch_integrate(const Dev& d, int last, const Launch& L) {
     k_integrate<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d, last);
+}
+
+void launch_refresh(const Dev& d, const Launch& L) {
+    k_refresh_tensors<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d);
+    launch_geometry(d, 1, L);
 }
 
 }  // namespace cpgpu

@@ -190,6 +190,23 @@ int cpgpu_batch_get_body_state(cpgpu_batch* b, int world_index, double* com, dou
 /* Total bodies, worlds and live contact points of the batch. */
 int cpgpu_batch_info(cpgpu_batch* b, int64_t* n_bodies, int64_t* n_worlds, int64_t* n_contacts);
 
+/* Device time of n_steps of the batch (CUDA events on the batch's stream). */
+int cpgpu_batch_step_timed(cpgpu_batch* b, int n_steps, double* device_ms);
+/* Whole-batch state transfer in the device layout: 16 floats per body
+ * (com xyz, inverse mass, quaternion r i j k, velocity xyz + pad, angular
+ * velocity xyz + pad), bodies in batch order.  Writing recomputes the world
+ * inertia tensors and AABBs from the new poses; the contact graph is kept. */
+int cpgpu_batch_read_state(cpgpu_batch* b, float* out);
+int cpgpu_batch_write_state(cpgpu_batch* b, const float* in);
+/* Per-stage device time of n_steps run stage by stage (no graph), for the
+ * roofline: stage_ms receives CPGPU_N_STAGES totals in the order gravity,
+ * pairs, narrowphase, merge, islands, rows, pgs, integrate, geometry; counts
+ * (may be NULL) receives the last step's pairs, contacts and islands. */
+#define CPGPU_N_STAGES 9
+int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* counts);
+/* Number of kernel launches one step of the batch issues. */
+int cpgpu_batch_launches_per_step(cpgpu_batch* b, int* n);
+
 /* ---- diagnostics -------------------------------------------------------- */
 /* Last error message of this thread (static storage, never NULL). */
 const char* cpgpu_last_error(void);

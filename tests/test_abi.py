@@ -35,7 +35,7 @@ def test_device_library_exports_every_declared_symbol():
 def test_oracle_libraries_export_the_world_api(oracle_mod, which):
     abi = oracle_mod.ref_abi() if which == "ref" else oracle_mod.port_abi()
     prefix = "cpref_" if which == "ref" else "cport_"
-    batch_only = {"batch_create", "batch_destroy", "batch_step", "batch_get_body_state", "batch_info"}
+    batch_only = {n[len("cpgpu_"):] for n in declared() if n.startswith("cpgpu_batch_")}
     state_import = {"set_body_state", "set_contacts"}
     for n in declared():
         short = n[len("cpgpu_"):]

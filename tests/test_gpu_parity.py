@@ -1,0 +1,175 @@
+"""Device path against the oracle, on a GB300.
+
+Per-step parity: the device state (bodies and the persistent contact graph)
+after k steps is imported into the CPU restatement, both advance one step from
+that identical input, and the results are compared.  Tolerances are FP32-vs-FP64
+ones, written at each assertion; at exact ties of the separating-axis choice
+(face-on-face stacking) the two sides may pick different but equivalent
+features, so contact-id equality is asserted only where no such tie exists.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import constraintphysics_gb300 as cg
+from constraintphysics_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _step_both(sc, k, oracle_mod):
+    g = cg.world()
+    scenes.apply(sc, g)
+    g.step(k)
+    p = oracle_mod.port_world()
+    scenes.apply(sc, p)
+    p.set_state(**g.state())
+    p.set_contacts(g.contacts())
+    aabb = g.aabbs()
+    g.step(1)
+    p.step(1)
+    return g, p, aabb
+
+
+def _fresh(c):
+    m = c["memory_life"] == 5   # detected in the last step
+    return set(zip(c["b1"][m].tolist(), c["b2"][m].tolist(), c["magic_b"][m].tolist()))
+
+
+def test_smoke():
+    import __graft_entry__
+    __graft_entry__.smoke()
+
+
+@pytest.mark.parametrize("k", [40, 80, 120])
+def test_single_step_parity_hull_pile(oracle_mod, k):
+    g, p, aabb = _step_both(scenes.hull_drop(seed=1, n_side=3), k, oracle_mod)
+    # pair set: bit-exact, and exactly the overlaps of the device's own AABBs
+    assert np.array_equal(g.pairs(), p.pairs())
+    lo, hi = aabb[:, :3], aabb[:, 3:]
+    ov = ~((hi[:, None, :] < lo[None, :, :]) | (lo[:, None, :] > hi[None, :, :])).any(axis=2)
+    i, j = np.nonzero(np.triu(ov, 1))
+    assert np.array_equal(np.stack([i + 1, j + 1], 1).astype(np.uint32), g.pairs())
+    # contact features (MagicIDs) identical
+    assert _fresh(g.contacts()) == _fresh(p.contacts())
+    sg, sp = g.state(), p.state()
+    assert np.abs(sg["vel"] - sp["vel"]).max() <= 1e-4          # m/s, FP32 vs FP64
+    assert np.abs(sg["ang_vel"] - sp["ang_vel"]).max() <= 1e-4  # rad/s
+    assert np.abs(sg["com"] - sp["com"]).max() <= 1e-5          # m
+
+
+def test_single_step_parity_1000_hulls(oracle_mod):
+    g, p, _ = _step_both(scenes.hull_drop(seed=0, n_side=10), 60, oracle_mod)
+    assert np.array_equal(g.pairs(), p.pairs())
+    fg, fp = _fresh(g.contacts()), _fresh(p.contacts())
+    assert len(fg ^ fp) <= 0.05 * len(fp)
+    sg, sp = g.state(), p.state()
+    dv = np.linalg.norm(sg["vel"] - sp["vel"], axis=1)
+    vm = np.linalg.norm(sp["vel"], axis=1)
+    assert np.mean(dv <= 1e-4 + 1e-3 * vm) >= 0.99
+    assert np.median(dv) <= 1e-5
+
+
+def test_single_step_parity_pyramid(oracle_mod):
+    rng = np.random.default_rng(7)
+    pool = scenes.HullPool(0, size=8)
+    sc = None
+    while sc is None or not sc.name.startswith("pyramid"):
+        sc = scenes.batched_world(rng, pool, 30, 120)
+    g, p, _ = _step_both(sc, 60, oracle_mod)
+    assert np.array_equal(g.pairs(), p.pairs())
+    sg, sp = g.state(), p.state()
+    assert np.abs(sg["vel"] - sp["vel"]).max() <= 1e-4
+    assert np.abs(sg["com"] - sp["com"]).max() <= 1e-5
+
+
+def test_box_vs_ground_device():
+    """CollisionTests.h:77-165 (Box vs Ground) with sleeping disabled."""
+    w = cg.world()
+    w.set_params(step_time=1.0 / 60.0, sleeping=False)
+    w.add_box((-50.0, -0.5, -50.0), 100.0, 0.5, 100.0, None, scenes.FIXED)
+    box = w.add_box((0.0, 5.0, 0.0), 1.0, 1.0, 1.0, None, scenes.DYNAMIC)
+    w.step(300)
+    st, c = w.state(), w.contacts()
+    fresh = c["memory_life"] == 5
+    assert fresh.any() and (np.abs(c["n_local_b1"][fresh][:, 1]) >= 0.9999).all()
+    assert np.linalg.norm(st["vel"][box - 1]) < 1e-3
+    assert abs(st["com"][box - 1, 1] - 0.5) < 0.1
+
+
+def test_trajectory_drift_box_drop(oracle_mod):
+    """A tilted box dropped on the plate, 300 steps, device vs reference engine:
+    positions agree to 1e-3 m until the box comes to rest; at rest both settle
+    inside the 0.05 m penetration slop, so the final heights agree to 1e-2 m."""
+    sc = scenes.Scene("box", dict(step_time=1 / 60, sleeping=False))
+    sc.box((-50, -2, -50), 100, 2, 100, None, scenes.FIXED)
+    b = sc.box((-0.5, 3, -0.5), 1, 1, 1, None, scenes.DYNAMIC)
+    sc.orient(b, scenes.random_quat(np.random.default_rng(3)))
+    g = cg.world()
+    scenes.apply(sc, g)
+    r = oracle_mod.ref_world()
+    scenes.apply(sc, r)
+    for s in range(300):
+        g.step(1)
+        r.step(1)
+        if s == 100:
+            assert np.abs(g.state()["com"] - r.state()["com"]).max() <= 1e-3
+    assert np.abs(g.state()["com"] - r.state()["com"]).max() <= 1e-2
+
+
+def test_batch_equals_single_worlds():
+    rng = np.random.default_rng(5)
+    pool = scenes.HullPool(1, size=8)
+    scs = [scenes.batched_world(rng, pool, 8, 60) for _ in range(3)]
+    singles = []
+    for sc in scs:
+        w = cg.world()
+        scenes.apply(sc, w)
+        w.step(50)
+        singles.append(w.state())
+    ws = []
+    for sc in scs:
+        w = cg.world()
+        scenes.apply(sc, w)
+        ws.append(w)
+    b = cg.Batch(ws)
+    b.step(50)
+    for i, st in enumerate(singles):
+        bs = b.state(i)
+        for k in ("com", "quat", "vel", "ang_vel"):
+            assert np.array_equal(bs[k], st[k]), (i, k)
+
+
+def test_batch_state_roundtrip_is_exact():
+    rng = np.random.default_rng(9)
+    pool = scenes.HullPool(2, size=8)
+    scs = [scenes.batched_world(rng, pool, 8, 60) for _ in range(2)]
+    outs = []
+    for roundtrip in (False, True):
+        ws = []
+        for sc in scs:
+            w = cg.world()
+            scenes.apply(sc, w)
+            ws.append(w)
+        b = cg.Batch(ws)
+        for _ in range(40):
+            if roundtrip:
+                b.write_state(b.read_state())
+            b.step(1)
+        outs.append([b.state(i) for i in range(len(scs))])
+    for a, c in zip(*outs):
+        for k in a:
+            assert np.array_equal(a[k], c[k]), k
+
+
+def test_capacity_overflow_is_reported(monkeypatch):
+    """A pair buffer that is too small makes step() return CPGPU_ERR_CAPACITY
+    (the kernels clamp their writes); the world stays usable for queries."""
+    monkeypatch.setenv("CPGPU_CAPACITY_FLOOR", "16")
+    monkeypatch.setenv("CPGPU_PAIRS_PER_BODY", "0")
+    w = cg.world()
+    scenes.apply(scenes.hull_drop(seed=1, n_side=3), w)
+    with pytest.raises(cg.CPGPUError, match="status -3"):
+        w.step(120)
+    assert np.isfinite(w.state()["com"]).all()
