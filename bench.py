@@ -256,6 +256,9 @@ def main():
             dist.barrier()
 
     batch.step(a.warmup)
+    # per-stage profile (stage by stage, no graph) for the roofline, taken on
+    # the steps right after the warm-up (the same phase as the timed steps)
+    stage_ms, counts = (None, None) if a.profile_only else batch.profile(3)
     if a.profile_only:
         batch.step(a.steps)
         print(json.dumps({"profile_only": True, "steps": a.steps, "warmup": a.warmup}), flush=True)
@@ -296,8 +299,6 @@ def main():
            "d2h_bytes_per_step": state_bytes, "host_buffers": host_desc,
            "call": "cpgpu_batch_write_state + cpgpu_batch_step + cpgpu_batch_read_state per step"}
 
-    # per-stage profile (stage by stage, no graph) for the roofline
-    stage_ms, counts = batch.profile(3)
     stage_ms = {k: v / 3 for k, v in stage_ms.items()}
     dominant = max(stage_ms, key=stage_ms.get)
     vfe = hull_sizes(ws_scenes)

@@ -215,6 +215,9 @@ struct Batch {
     int n_sms = 0;
     int slot_bytes = 0;
     cudaStream_t st = nullptr;
+    cudaStream_t side = nullptr;       // concurrent branch (small-island PGS)
+    cudaEvent_t fork = nullptr, join = nullptr;
+    int dv_cap = 64;                   // island bodies whose Δv fits in shared memory
     uint8_t* mem = nullptr;
     Dev d[2];                  // d[p]: old = buffer p, new = buffer 1-p
     int parity = 0;
@@ -228,6 +231,9 @@ struct Batch {
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (mem) cudaFree(mem);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -245,17 +251,19 @@ struct Batch {
         launch_pairs(x, L);        mark(2);
         launch_narrowphase(x, slot_bytes, n_sms, st); mark(3);
         launch_merge(x, L);        mark(4);
-        launch_islands(x, L);      mark(5);
+        launch_islands(x, L);
+        launch_pgs_schedule(x, L); mark(5);
         for (int s = 0; s < substeps; s++) {
             launch_rows(x, s == 0, s == substeps - 1, L);  mark(6 + 3 * s);
-            launch_pgs(x, L);                              mark(7 + 3 * s);
+            launch_pgs(x, dv_cap, side, fork, join, L);    mark(7 + 3 * s);
             launch_integrate(x, s == substeps - 1, L);     mark(8 + 3 * s);
         }
         launch_geometry(x, 0, L);  mark(6 + 3 * substeps);
     }
     // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 1,
-    // merge 6 + 3 scans, islands 2 + scan 3, 3 per substep, geometry 1
-    int launches_per_step() const { return 1 + 6 + 1 + (6 + 9) + (2 + 3) + 3 * substeps + 1; }
+    // merge 6 + 3 scans, islands 2 + scan 3, schedule 3, 4 per substep
+    // (rows, small + large PGS, integrate), geometry 1
+    int launches_per_step() const { return 1 + 6 + 1 + (6 + 9) + (2 + 3) + 3 + 4 * substeps + 1; }
 
     void build_graphs() {
         for (int p = 0; p < 2; p++) {
@@ -315,6 +323,9 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&B->n_sms, cudaDevAttrMultiProcessorCount, dev));
     CK(cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&B->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&B->join, cudaEventDisableTiming));
     CK(cudaEventCreate(&B->ev0));
     CK(cudaEventCreate(&B->ev1));
 
@@ -329,6 +340,11 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     }
     B->n_bodies = N;
     B->world_start = wstart;
+    {
+        int max_world = 0;
+        for (size_t k = 0; k + 1 < wstart.size(); k++) max_world = std::max(max_world, wstart[k + 1] - wstart[k]);
+        B->dv_cap = std::min(1536, std::max(64, max_world));
+    }
     std::vector<uint8_t> pool;
     std::map<std::string, int> dedupe;
     std::vector<int> shape_off(N);
@@ -495,6 +511,10 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         x.row_contact = A.take<int>(cap_contacts); x.row_of_contact = A.take<int>(cap_contacts);
         x.rows = A.take<RowBlock>(cap_contacts);
         x.dv = A.take<float4>(4 * (size_t)N);
+        x.stage = A.take<float4>(4 * (size_t)N);
+        x.big_list = A.take<int>(N);
+        x.small_list = A.take<int>(N);
+        x.sched = A.take<int>(96);
         x.status = counts + 6;
         x.cnt = counts + 16;
     };
@@ -540,6 +560,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     Launch L{B->n_sms, B->st};
     launch_geometry(B->d[0], 1, L);
     prepare_kernels();
+    prepare_pgs(B->dv_cap);
     CK(cudaStreamSynchronize(B->st));
     CK(cudaGetLastError());
     B->build_graphs();
@@ -1051,10 +1072,8 @@ int cpgpu_batch_write_state(cpgpu_batch* b, const float* in) {
         Batch& B = *b->b;
         const Dev& x = B.cur();
         const size_t N = B.n_bodies;
-        float4* dst[4] = {x.pos, x.rot, x.vel, x.angv};
-        for (int k = 0; k < 4; k++)
-            CK(cudaMemcpy2DAsync(dst[k], 16, in + 4 * k, 64, 16, N, cudaMemcpyHostToDevice, B.st));
-        launch_refresh(x, Launch{B.n_sms, B.st});
+        CK(cudaMemcpyAsync(x.stage, in, N * 64, cudaMemcpyHostToDevice, B.st));
+        launch_apply_state(x, Launch{B.n_sms, B.st});
         CK(cudaStreamSynchronize(B.st));
         return CPGPU_OK;
     });

@@ -23,9 +23,16 @@ void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, cudaStream_t st
 void launch_merge(const Dev& d, const Launch& L);
 void launch_islands(const Dev& d, const Launch& L);
 void launch_rows(const Dev& d, int first, int last, const Launch& L);
-void launch_pgs(const Dev& d, const Launch& L);
+// PGS: islands are split by size after the island pass (largest first); large
+// islands run one warp each with rows streamed through shared memory, small
+// ones one thread each on the `side` stream, concurrently.
+void launch_pgs_schedule(const Dev& d, const Launch& L);
+void prepare_pgs(int dv_cap);
+int pgs_big_smem_bytes(int dv_cap);
+void launch_pgs(const Dev& d, int dv_cap, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, const Launch& L);
 void launch_integrate(const Dev& d, int last, const Launch& L);
-// after an external state write: world inertia tensors and AABBs from the poses
-void launch_refresh(const Dev& d, const Launch& L);
+// external state write: apply the staged state (d.stage); bodies whose pose
+// changed get their world inertia tensors and AABBs recomputed
+void launch_apply_state(const Dev& d, const Launch& L);
 
 }  // namespace cpgpu

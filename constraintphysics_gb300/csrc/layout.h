@@ -91,19 +91,23 @@ struct EdgeStore {
 };
 
 // Solver row block of one contact (normal row + 2-dof friction row), built each
-// substep in island order (ConstraintSolver.cpp:240-343).
+// substep in island order (ConstraintSolver.cpp:240-343).  384 bytes, 16-byte
+// aligned, so contiguous runs of rows can be bulk-copied to shared memory.
 struct alignas(16) RowBlock {
+    float4 imp;          // accumulated impulses: normal, pseudo normal, friction u, w
     int sa, sb;          // island body slots (-1 = body with infinite mass)
     int contact;         // contact index
+    int stat;            // friction static_ready of the last projection
     int ga, gb;          // global body indices
-    float bounce;
-    float tgt_n, tgt_f0, tgt_f1;   // velocity targets set at the start of PGS
+    float bounce, cutoff;
+    float tgt_n, tgt_f0, tgt_f1;   // velocity targets (findTargetConstraintValue)
+    float fcoeff;
+    float nminv, nptarget, pad0, pad1;
     float nja[6], njb[6], nita[6], nitb[6];
-    float nminv, nptarget, cutoff, fcoeff;
     float fja[12], fjb[12], fita[12], fitb[12];   // row-major [2][6] / [6][2]
     float fminv[4];
-    float imp_n, pimp_n, imp_f0, imp_f1;
 };
+static_assert(sizeof(RowBlock) == 384, "row block size");
 
 struct Batch;  // host object, engine.cu
 
@@ -157,6 +161,9 @@ struct Dev {
     int* row_of_contact;           // contact -> row slot
     RowBlock* rows;
     float4* dv;                    // 4 float4 per island body slot: dv lin, dv ang, dpv lin, dpv ang
+    float4* stage;                 // 4 float4 per body: staging of external state writes
+    int* big_list; int* small_list;  // island indices split by row count (PGS scheduling)
+    int* sched;                    // [0] n_big, [1] n_small, [2] big queue head, [32..63] bucket counts, [64..95] cursors
     int* cnt;                      // small device counters (merge totals)
     int* status;
 };

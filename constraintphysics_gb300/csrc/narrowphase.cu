@@ -26,6 +26,8 @@ namespace {
 constexpr float kCosTol = (float)1.5230484360873042e-4;  // 1 - cos(1 deg), CollisionDetect.h:21-23
 constexpr float kSinTol = (float)0.017452406437283512;   // sin(1 deg)
 constexpr int kMaxClip = 40;
+constexpr int kQueue = 64;                       // queued edge-edge axes per warp
+constexpr int kQueueBytes = kQueue * (16 + 4);
 constexpr long long kSpinLimit = 1LL << 24;  // bounded mbarrier wait
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -96,7 +98,9 @@ __device__ __forceinline__ void check(const Ext& a, const Ext& b, f3 n, int idx,
     if (fwd < rev) x = Axis{fwd, idx, a.mx_id, b.mn_id, n};
     else x = Axis{rev, idx, a.mn_id, b.mx_id, -n};
     if (x.pen < 0.f) *sep = true;
-    else if (x.pen < best->pen) *best = x;
+    // strict minimum over the reference's axis order: ties go to the axis that
+    // comes first (axes reach a lane out of order, so compare the index too)
+    else if (x.pen < best->pen || (x.pen == best->pen && idx < best->idx)) *best = x;
 }
 
 // ---- 2-D clipping (lane 0) --------------------------------------------------------
@@ -322,7 +326,8 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
     const int wib = threadIdx.x >> 5;
     const int warps_per_block = blockDim.x >> 5;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
-    uint8_t* slot = smem + 16 * warps_per_block + (size_t)wib * slot_bytes;
+    uint8_t* qslot = smem + 16 * warps_per_block + (size_t)wib * (slot_bytes + kQueueBytes);
+    uint8_t* slot = qslot + kQueueBytes;
     if (lane == 0) mbar_init(&bars[wib]);
     __syncthreads();
     uint32_t parity = 0;
@@ -390,11 +395,20 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
             if (lane == 0) { d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f); d.mf_cnt[p] = 0; }
             continue;
         }
-        // edge-edge axes from intersecting Gauss arcs
+        // edge-edge axes from intersecting Gauss arcs.  The arc-pair tests are
+        // cheap and uniform; the axes that pass need two support queries each,
+        // so they are queued (ballot + prefix count) and then evaluated with
+        // every lane taking one queued axis, instead of one lane at a time.
         const int naa = A.h->na, nab = B.h->na;
         const int total = naa * nab;
+        float4* qn = reinterpret_cast<float4*>(qslot);
+        int* qi = reinterpret_cast<int*>(qslot + kQueue * sizeof(float4));
+        int qcount = 0;
+        const unsigned lt_mask = (1u << lane) - 1u;
         for (int base = 0; base < total; base += 32) {
             int t = base + lane;
+            bool pass = false;
+            f3 n = mk(0.f, 0.f, 0.f);
             if (t < total) {
                 int ia = t / nab, ib = t - ia * nab;
                 f3 a1 = mk(A.n[A.arc[2 * ia]]), a2 = mk(A.n[A.arc[2 * ia + 1]]);
@@ -403,16 +417,33 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
                 if (dot(avg, b1) + dot(avg, b2) > 0.f) {
                     f3 ap = cross(a1, a2), bp = cross(b1, b2);
                     if (!(dot(ap, b1) * dot(ap, b2) > 0.f || dot(bp, a1) * dot(bp, a2) > 0.f)) {
-                        f3 n = cross(ap, bp);
+                        n = cross(ap, bp);
                         if (mag2(n) != 0.f) {
                             n = normalize(n);
                             if (dot(avg, n) < 0.f) n = n * -1.f;
-                            check(extrema(A.v, nva, n), extrema(B.v, nvb, n), n, nfa + nfb + t, &best, &sep);
+                            pass = true;
                         }
                     }
                 }
             }
-            if (__any_sync(0xffffffffu, sep)) break;
+            const unsigned m = __ballot_sync(0xffffffffu, pass);
+            if (pass) {
+                int at = qcount + __popc(m & lt_mask);
+                qn[at] = make_float4(n.x, n.y, n.z, 0.f);
+                qi[at] = nfa + nfb + t;
+            }
+            qcount += __popc(m);
+            const bool last = base + 32 >= total;
+            if (qcount > kQueue - 32 || last) {
+                __syncwarp();
+                for (int k = lane; k < qcount; k += 32) {
+                    f3 ax = mk(qn[k]);
+                    check(extrema(A.v, nva, ax), extrema(B.v, nvb, ax), ax, qi[k], &best, &sep);
+                }
+                qcount = 0;
+                __syncwarp();
+                if (__any_sync(0xffffffffu, sep)) break;
+            }
         }
         if (__any_sync(0xffffffffu, sep)) {
             if (lane == 0) { d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f); d.mf_cnt[p] = 0; }
@@ -495,7 +526,7 @@ void prepare_kernels() {
 
 void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, cudaStream_t st) {
     const int warps = 8;
-    size_t smem = 16 * warps + (size_t)warps * slot_bytes;
+    size_t smem = 16 * warps + (size_t)warps * (slot_bytes + kQueueBytes);
     k_narrowphase<<<n_sms * 4, warps * 32, smem, st>>>(d, slot_bytes);
 }
 

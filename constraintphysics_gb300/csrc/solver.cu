@@ -53,6 +53,12 @@ __device__ __forceinline__ float dot6(const float* a, const float* b) {
     return s;
 }
 
+__device__ __forceinline__ void body_vel(const Dev& d, int g, float* out) {
+    if (d.movement[g] == 1) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
+    float4 v = d.vel[g], w = d.angv[g];
+    out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = w.x; out[4] = w.y; out[5] = w.z;
+}
+
 __global__ void k_rows(Dev d, int first, int last) {
     const int nc = *d.n_contacts_new;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
@@ -82,6 +88,7 @@ __global__ void k_rows(Dev d, int first, int last) {
             R.bounce = p2.w;
             R.cutoff = P.cutoff_vel;
             R.fcoeff = nl.w;
+            R.stat = 0;
             // normal row
             float ja[6], jb[6], ia[6], ib[6];
             f3 t = nskew(n, rA), t2 = nskew(-n, rB);
@@ -93,14 +100,11 @@ __global__ void k_rows(Dev d, int first, int last) {
             for (int k = 0; k < 6; k++) { R.nja[k] = ja[k]; R.njb[k] = jb[k]; R.nita[k] = ia[k]; R.nitb[k] = ib[k]; }
             R.nminv = 1.0f / (itv * (1.0f + P.cfm));
             R.nptarget = fmaxf(0.0f, depth - 0.05f) * pcc;
-            R.imp_n = wn;
-            R.pimp_n = 0.f;
             // friction rows in the tangent basis of n, warm impulse re-projected
             f3 u, w;
             basis(n, &u, &w);
             const f3 su = mk(d.c_new.fu[c]), sw = mk(d.c_new.fw[c]);
-            R.imp_f0 = dot(u, su) * wf0 + dot(u, sw) * wf1;
-            R.imp_f1 = dot(w, su) * wf0 + dot(w, sw) * wf1;
+            R.imp = make_float4(wn, 0.f, dot(u, su) * wf0 + dot(u, sw) * wf1, dot(w, su) * wf0 + dot(w, sw) * wf1);
             float fja[12], fjb[12], fia[12], fib[12];
             f3 ta = nskew(-u, rA), tb = nskew(u, rB), wa = nskew(-w, rA), wb = nskew(w, rB);
             fja[0] = u.x; fja[1] = u.y; fja[2] = u.z; fja[3] = ta.x; fja[4] = ta.y; fja[5] = ta.z;
@@ -126,6 +130,18 @@ __global__ void k_rows(Dev d, int first, int last) {
             float di = 1.0f / (fv[0] * fv[3] - fv[1] * fv[2]);
             R.fminv[0] = fv[3] * di; R.fminv[1] = -fv[1] * di; R.fminv[2] = -fv[2] * di; R.fminv[3] = fv[0] * di;
             for (int k = 0; k < 12; k++) { R.fja[k] = fja[k]; R.fjb[k] = fjb[k]; R.fita[k] = fia[k]; R.fitb[k] = fib[k]; }
+            // velocity targets from the bodies' velocities at the start of the
+            // solve (ContactConstraint::findTargetConstraintValue,
+            // ConstraintSolver.cpp:264-268; DegreedConstraint default, ConstraintSolver.h:78)
+            {
+                float va[6], vb[6];
+                body_vel(d, a, va);
+                body_vel(d, b, vb);
+                float cur = dot6(ja, va) + dot6(jb, vb);
+                R.tgt_n = (cur < -P.cutoff_vel) ? -(1.0f + p2.w) * cur : -cur;
+                R.tgt_f0 = -(dot6(fja, va) + dot6(fjb, vb));
+                R.tgt_f1 = -(dot6(fja + 6, va) + dot6(fjb + 6, vb));
+            }
             d.c_new.fu[c] = make_float4(u.x, u.y, u.z, 0.f);
             d.c_new.fw[c] = make_float4(w.x, w.y, w.z, 0.f);
         }
@@ -139,8 +155,6 @@ __global__ void k_rows(Dev d, int first, int last) {
     }
 }
 
-struct DV6 { float v[6]; };
-
 __device__ __forceinline__ void load_dv(const float4* dv, int slot, int which, float* out) {
     if (slot < 0) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
     float4 l = dv[4 * slot + 2 * which], a = dv[4 * slot + 2 * which + 1];
@@ -151,126 +165,289 @@ __device__ __forceinline__ void store_dv(float4* dv, int slot, int which, const 
     dv[4 * slot + 2 * which] = make_float4(v[0], v[1], v[2], 0.f);
     dv[4 * slot + 2 * which + 1] = make_float4(v[3], v[4], v[5], 0.f);
 }
-__device__ __forceinline__ void body_vel(const Dev& d, int g, float* out) {
-    if (d.movement[g] == 1) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
-    float4 v = d.vel[g], w = d.angv[g];
-    out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = w.x; out[4] = w.y; out[5] = w.z;
+
+// ---- one row of each PGS pass (PGS_solve, ConstraintSolver.cpp:120-161) ----------
+// warm start: apply the stored impulses when they are non-zero
+// (DegreedConstraint::constraintWarmStarted / applyWarmStartVelocityChange)
+__device__ __forceinline__ void row_warm(const RowBlock& R, const float4 imp, float4* dv) {
+    const bool wn = fabsf(imp.x) > kZero, wf = fabsf(imp.z) > kZero || fabsf(imp.w) > kZero;
+    if (!wn && !wf) return;
+    float va[6], vb[6];
+    load_dv(dv, R.sa, 0, va);
+    load_dv(dv, R.sb, 0, vb);
+    if (wn)
+        for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * imp.x; vb[k] += R.nitb[k] * imp.x; }
+    if (wf)
+        for (int k = 0; k < 6; k++) {
+            va[k] += imp.z * R.fita[2 * k] + imp.w * R.fita[2 * k + 1];
+            vb[k] += imp.z * R.fitb[2 * k] + imp.w * R.fitb[2 * k + 1];
+        }
+    store_dv(dv, R.sa, 0, va);
+    store_dv(dv, R.sb, 0, vb);
 }
 
-__global__ void k_pgs(Dev d) {
+// velocity pass: normal row clamped at zero, then the friction rows projected on
+// the friction disc of the current normal impulse (PGSConstraintStep,
+// ConstraintSolver.cpp:12-40; projections :270-272, :331-343)
+__device__ __forceinline__ void row_vel(const RowBlock& R, float4& imp, int& stat, float4* dv) {
+    float va[6], vb[6];
+    load_dv(dv, R.sa, 0, va);
+    load_dv(dv, R.sb, 0, vb);
+    {
+        float cur = dot6(R.nja, va) + dot6(R.njb, vb);
+        float nw = imp.x + R.nminv * (R.tgt_n - cur);
+        float diff = fmaxf(nw, 0.0f) - imp.x;
+        if (fabsf(diff) > kZero) {
+            for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * diff; vb[k] += R.nitb[k] * diff; }
+            imp.x += diff;
+        }
+    }
+    {
+        float c0 = dot6(R.fja, va) + dot6(R.fjb, vb);
+        float c1 = dot6(R.fja + 6, va) + dot6(R.fjb + 6, vb);
+        float d0 = R.tgt_f0 - c0, d1 = R.tgt_f1 - c1;
+        float n0 = imp.z + (d0 * R.fminv[0] + d1 * R.fminv[1]);
+        float n1 = imp.w + (d0 * R.fminv[2] + d1 * R.fminv[3]);
+        float mx = R.fcoeff * imp.x;
+        float mg = sqrtf(n0 * n0 + n1 * n1);
+        if (mg > mx) { float sc = mx / mg; n0 *= sc; n1 *= sc; stat = 0; }
+        else stat = 1;
+        float e0 = n0 - imp.z, e1 = n1 - imp.w;
+        if (fabsf(e0) > kZero || fabsf(e1) > kZero) {
+            for (int k = 0; k < 6; k++) {
+                va[k] += e0 * R.fita[2 * k] + e1 * R.fita[2 * k + 1];
+                vb[k] += e0 * R.fitb[2 * k] + e1 * R.fitb[2 * k + 1];
+            }
+            imp.z += e0;
+            imp.w += e1;
+        }
+    }
+    store_dv(dv, R.sa, 0, va);
+    store_dv(dv, R.sb, 0, vb);
+}
+
+// pseudo-velocity (position correction) pass of the normal row
+__device__ __forceinline__ void row_pos(const RowBlock& R, float4& imp, float4* dv) {
+    float va[6], vb[6];
+    load_dv(dv, R.sa, 1, va);
+    load_dv(dv, R.sb, 1, vb);
+    float cur = dot6(R.nja, va) + dot6(R.njb, vb);
+    float nw = imp.y + R.nminv * (R.nptarget - cur);
+    float diff = fmaxf(nw, 0.0f) - imp.y;
+    if (fabsf(diff) > kZero) {
+        for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * diff; vb[k] += R.nitb[k] * diff; }
+        imp.y += diff;
+        store_dv(dv, R.sa, 1, va);
+        store_dv(dv, R.sb, 1, vb);
+    }
+}
+
+// island epilogue: impulses to the contacts (warm start of the next rebuild)
+// and velocity deltas to the bodies (PhysicsEngine::applyVelocityChange,
+// PhysicsEngine.cpp:1113-1136); `t`/`nt` stride over the island
+__device__ void island_finish(const Dev& d, int rs, int rc, int bs, int bc, const float4* dv, int t, int nt) {
+    for (int r = rs + t; r < rs + rc; r += nt) {
+        const RowBlock& R = d.rows[r];
+        float4 imp = R.imp;
+        d.c_new.imp[R.contact] = make_float4(imp.x, imp.z, imp.w, 0.f);
+        int cst = d.c_new.state[R.contact];
+        d.c_new.state[R.contact] = R.stat ? (cst | (1 << 9)) : (cst & ~(1 << 9));
+    }
+    for (int k = t; k < bc; k += nt) {
+        int g = d.isl_bodies[bs + k];
+        if (d.movement[g] != 0) continue;
+        float4 a = dv[4 * k], b = dv[4 * k + 1], c = dv[4 * k + 2], e = dv[4 * k + 3];
+        float4 v = d.vel[g], w = d.angv[g], pv = d.pvel[g], pw = d.pangv[g];
+        d.vel[g] = make_float4(v.x + a.x, v.y + a.y, v.z + a.z, 0.f);
+        d.angv[g] = make_float4(w.x + b.x, w.y + b.y, w.z + b.z, 0.f);
+        d.pvel[g] = make_float4(pv.x + c.x, pv.y + c.y, pv.z + c.z, 0.f);
+        d.pangv[g] = make_float4(pw.x + e.x, pw.y + e.y, pw.z + e.z, 0.f);
+    }
+}
+
+// ---- scheduling: islands with at least kBigRows rows get a warp each, largest first
+constexpr int kBigRows = 48;
+
+__global__ void k_sched_reset(Dev d) {
+    if (threadIdx.x < 96) d.sched[threadIdx.x] = 0;
+}
+
+__device__ __forceinline__ int size_bucket(int rows) { return 31 - __clz(rows); }
+
+__global__ void k_sched_count(Dev d) {
     const int ni = *d.n_islands;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
+        int rc = d.g_isl_row_count[i];
+        if (rc >= kBigRows) atomicAdd(&d.sched[32 + size_bucket(rc)], 1);
+        else d.small_list[atomicAdd(&d.sched[1], 1)] = i;
+    }
+}
+
+__global__ void k_sched_place(Dev d) {
+    const int ni = *d.n_islands;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
+        int rc = d.g_isl_row_count[i];
+        if (rc < kBigRows) continue;
+        int b = size_bucket(rc), off = 0;
+        for (int k = 31; k > b; k--) off += d.sched[32 + k];   // larger buckets first
+        d.big_list[off + atomicAdd(&d.sched[64 + b], 1)] = i;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int n = 0;
+        for (int k = 0; k < 32; k++) n += d.sched[32 + k];
+        d.sched[0] = n;
+    }
+}
+
+// small islands: one thread walks the island's rows in global memory
+__global__ void k_pgs_small(Dev d) {
+    const int n = d.sched[1];
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int i = d.small_list[q];
         const int rs = d.g_isl_row_start[i], rc = d.g_isl_row_count[i];
         const int bs = d.g_isl_body_start[i], bc = d.g_isl_body_count[i];
         const WorldParams& P = d.wparams[d.g_isl_world[i]];
         float4* dv = d.dv + 4 * (size_t)bs;
         for (int k = 0; k < 4 * bc; k++) dv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        // targets (ContactConstraint::findTargetConstraintValue, ConstraintSolver.cpp:264-268)
-        for (int r = rs; r < rs + rc; r++) {
-            RowBlock& R = d.rows[r];
-            float va[6], vb[6];
-            body_vel(d, R.ga, va);
-            body_vel(d, R.gb, vb);
-            float cur = dot6(R.nja, va) + dot6(R.njb, vb);
-            R.tgt_n = (cur < -R.cutoff) ? -(1.0f + R.bounce) * cur : -cur;
-            R.tgt_f0 = -(dot6(R.fja, va) + dot6(R.fjb, vb));
-            R.tgt_f1 = -(dot6(R.fja + 6, va) + dot6(R.fjb + 6, vb));
-        }
-        // warm start
-        for (int r = rs; r < rs + rc; r++) {
-            const RowBlock& R = d.rows[r];
-            float va[6], vb[6];
-            load_dv(dv, R.sa, 0, va);
-            load_dv(dv, R.sb, 0, vb);
-            if (fabsf(R.imp_n) > kZero) {
-                for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * R.imp_n; vb[k] += R.nitb[k] * R.imp_n; }
-            }
-            if (fabsf(R.imp_f0) > kZero || fabsf(R.imp_f1) > kZero) {
-                for (int k = 0; k < 6; k++) {
-                    va[k] += R.imp_f0 * R.fita[2 * k] + R.imp_f1 * R.fita[2 * k + 1];
-                    vb[k] += R.imp_f0 * R.fitb[2 * k] + R.imp_f1 * R.fitb[2 * k + 1];
-                }
-            }
-            store_dv(dv, R.sa, 0, va);
-            store_dv(dv, R.sb, 0, vb);
-        }
-        // velocity sweeps (PGSConstraintStep, ConstraintSolver.cpp:12-40)
-        for (int it = 0; it < P.pgs_vel; it++) {
+        for (int r = rs; r < rs + rc; r++) row_warm(d.rows[r], d.rows[r].imp, dv);
+        for (int it = 0; it < P.pgs_vel; it++)
             for (int r = rs; r < rs + rc; r++) {
                 RowBlock& R = d.rows[r];
-                float va[6], vb[6];
-                load_dv(dv, R.sa, 0, va);
-                load_dv(dv, R.sb, 0, vb);
-                {   // normal row, impulse clamped at zero
-                    float cur = dot6(R.nja, va) + dot6(R.njb, vb);
-                    float nw = R.imp_n + R.nminv * (R.tgt_n - cur);
-                    float diff = fmaxf(nw, 0.0f) - R.imp_n;
-                    if (fabsf(diff) > kZero) {
-                        for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * diff; vb[k] += R.nitb[k] * diff; }
-                        R.imp_n += diff;
-                    }
-                }
-                {   // friction rows, impulse projected on the friction disc
-                    float c0 = dot6(R.fja, va) + dot6(R.fjb, vb);
-                    float c1 = dot6(R.fja + 6, va) + dot6(R.fjb + 6, vb);
-                    float d0 = R.tgt_f0 - c0, d1 = R.tgt_f1 - c1;
-                    float n0 = R.imp_f0 + (d0 * R.fminv[0] + d1 * R.fminv[1]);
-                    float n1 = R.imp_f1 + (d0 * R.fminv[2] + d1 * R.fminv[3]);
-                    float mx = R.fcoeff * R.imp_n;
-                    float mg = sqrtf(n0 * n0 + n1 * n1);
-                    int sr;
-                    if (mg > mx) { float s = mx / mg; n0 *= s; n1 *= s; sr = 0; }
-                    else sr = 1;
-                    int cst = d.c_new.state[R.contact];
-                    d.c_new.state[R.contact] = sr ? (cst | (1 << 9)) : (cst & ~(1 << 9));
-                    float e0 = n0 - R.imp_f0, e1 = n1 - R.imp_f1;
-                    if (fabsf(e0) > kZero || fabsf(e1) > kZero) {
-                        for (int k = 0; k < 6; k++) {
-                            va[k] += e0 * R.fita[2 * k] + e1 * R.fita[2 * k + 1];
-                            vb[k] += e0 * R.fitb[2 * k] + e1 * R.fitb[2 * k + 1];
-                        }
-                        R.imp_f0 += e0;
-                        R.imp_f1 += e1;
-                    }
-                }
-                store_dv(dv, R.sa, 0, va);
-                store_dv(dv, R.sb, 0, vb);
+                float4 imp = R.imp;
+                int st = R.stat;
+                row_vel(R, imp, st, dv);
+                R.imp = imp;
+                R.stat = st;
             }
-        }
-        // pseudo-velocity sweeps of the normal rows (position correction)
-        for (int it = 0; it < P.pgs_pos; it++) {
+        for (int it = 0; it < P.pgs_pos; it++)
             for (int r = rs; r < rs + rc; r++) {
                 RowBlock& R = d.rows[r];
-                float va[6], vb[6];
-                load_dv(dv, R.sa, 1, va);
-                load_dv(dv, R.sb, 1, vb);
-                float cur = dot6(R.nja, va) + dot6(R.njb, vb);
-                float nw = R.pimp_n + R.nminv * (R.nptarget - cur);
-                float diff = fmaxf(nw, 0.0f) - R.pimp_n;
-                if (fabsf(diff) > kZero) {
-                    for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * diff; vb[k] += R.nitb[k] * diff; }
-                    R.pimp_n += diff;
-                    store_dv(dv, R.sa, 1, va);
-                    store_dv(dv, R.sb, 1, vb);
-                }
+                float4 imp = R.imp;
+                row_pos(R, imp, dv);
+                R.imp = imp;
+            }
+        island_finish(d, rs, rc, bs, bc, dv, 0, 1);
+    }
+}
+
+// ---- large islands: one warp per island, rows streamed through shared memory
+constexpr int kRingSlots = 4;
+constexpr int kChunkRows = 16;
+constexpr long long kWaitLimit = 1LL << 24;
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void ring_load(RowBlock* dst, const RowBlock* src, int rows, uint64_t* bar) {
+    uint32_t bytes = (uint32_t)(rows * sizeof(RowBlock));
+    // this thread wrote impulses to `src` with generic stores, and read `dst`
+    // before: order both against the async-proxy copy
+    asm volatile("fence.proxy.async;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool ring_wait(uint64_t* bar, uint32_t parity) {
+    for (long long it = 0; it < kWaitLimit; it++) {
+        uint32_t done;
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done) : "r"(saddr(bar)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// The serial Gauss-Seidel chain of one island on one thread: 1 warm-start pass,
+// pgs_vel velocity passes and pgs_pos position passes over the island's rows,
+// in order.  Rows stream through the shared ring (look-ahead up to one pass,
+// since a pass must see the impulses the previous pass wrote back); each row
+// is copied to registers with 16-byte loads before it is used.
+__device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t* bars, uint32_t& phase, float4* dv, int rs,
+                                       int rc, const WorldParams& P) {
+    const int nch = (rc + kChunkRows - 1) / kChunkRows;
+    const int passes = 1 + P.pgs_vel + P.pgs_pos;
+    const int total = passes * nch;
+    const int ahead = nch < kRingSlots ? nch : kRingSlots;
+    auto issue = [&](int t) {
+        int c = t % nch, slot = t % kRingSlots;
+        int n = min(kChunkRows, rc - c * kChunkRows);
+        ring_load(ring + slot * kChunkRows, d.rows + rs + c * kChunkRows, n, &bars[slot]);
+    };
+    for (int t = 0; t < ahead && t < total; t++) issue(t);
+    for (int t = 0; t < total; t++) {
+        const int slot = t % kRingSlots, pass = t / nch, c = t % nch;
+        if (!ring_wait(&bars[slot], (phase >> slot) & 1u)) return false;
+        phase ^= 1u << slot;
+        const int n = min(kChunkRows, rc - c * kChunkRows);
+        const float4* rb = reinterpret_cast<const float4*>(ring + slot * kChunkRows);
+        RowBlock* g = d.rows + rs + c * kChunkRows;
+        for (int j = 0; j < n; j++) {
+            RowBlock R;
+            float4* dst = reinterpret_cast<float4*>(&R);
+#pragma unroll
+            for (int k = 0; k < (int)(sizeof(RowBlock) / 16); k++) dst[k] = rb[j * (sizeof(RowBlock) / 16) + k];
+            float4 imp = R.imp;
+            if (pass == 0) {
+                row_warm(R, imp, dv);
+            } else if (pass <= P.pgs_vel) {
+                int st = R.stat;
+                row_vel(R, imp, st, dv);
+                g[j].imp = imp;
+                g[j].stat = st;
+            } else {
+                row_pos(R, imp, dv);
+                g[j].imp = imp;
             }
         }
-        // impulses back to the contacts (warm start of the next rebuild)
-        for (int r = rs; r < rs + rc; r++) {
-            const RowBlock& R = d.rows[r];
-            d.c_new.imp[R.contact] = make_float4(R.imp_n, R.imp_f0, R.imp_f1, 0.f);
+        if (t + ahead < total) issue(t + ahead);
+    }
+    return true;
+}
+
+// blockDim.x == 32; `dv_cap` island bodies fit in the shared Δv area
+__global__ void __launch_bounds__(32) k_pgs_big(Dev d, int dv_cap) {
+    extern __shared__ __align__(16) uint8_t sm[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm);
+    RowBlock* ring = reinterpret_cast<RowBlock*>(sm + 64);
+    float4* sdv = reinterpret_cast<float4*>(sm + 64 + kRingSlots * kChunkRows * sizeof(RowBlock));
+    __shared__ int sh_island;
+    const int lane = threadIdx.x;
+    if (lane == 0)
+        for (int k = 0; k < kRingSlots; k++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(&bars[k])), "r"(1) : "memory");
         }
-        // PhysicsEngine::applyVelocityChange (PhysicsEngine.cpp:1113-1136)
-        for (int k = 0; k < bc; k++) {
-            int g = d.isl_bodies[bs + k];
-            if (d.movement[g] != 0) continue;
-            float4 a = dv[4 * k], b = dv[4 * k + 1], c = dv[4 * k + 2], e = dv[4 * k + 3];
-            float4 v = d.vel[g], w = d.angv[g], pv = d.pvel[g], pw = d.pangv[g];
-            d.vel[g] = make_float4(v.x + a.x, v.y + a.y, v.z + a.z, 0.f);
-            d.angv[g] = make_float4(w.x + b.x, w.y + b.y, w.z + b.z, 0.f);
-            d.pvel[g] = make_float4(pv.x + c.x, pv.y + c.y, pv.z + c.z, 0.f);
-            d.pangv[g] = make_float4(pw.x + e.x, pw.y + e.y, pw.z + e.z, 0.f);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+    uint32_t phase = 0;   // bit k: parity of slot k
+    const int n_big = d.sched[0];
+    while (true) {
+        if (lane == 0) sh_island = atomicAdd(&d.sched[2], 1);
+        __syncwarp();
+        const int q = sh_island;
+        __syncwarp();
+        if (q >= n_big) break;
+        const int i = d.big_list[q];
+        const int rs = d.g_isl_row_start[i], rc = d.g_isl_row_count[i];
+        const int bs = d.g_isl_body_start[i], bc = d.g_isl_body_count[i];
+        const WorldParams& P = d.wparams[d.g_isl_world[i]];
+        float4* dv = (bc <= dv_cap) ? sdv : d.dv + 4 * (size_t)bs;
+        for (int k = lane; k < 4 * bc; k += 32) dv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncwarp();
+        bool ok = true;
+        if (lane == 0) {
+            ok = (bc <= dv_cap) ? big_chain(d, ring, bars, phase, sdv, rs, rc, P)
+                                : big_chain(d, ring, bars, phase, d.dv + 4 * (size_t)bs, rs, rc, P);
+            if (!ok) {
+                atomicOr(d.status, ST_TIMEOUT);
+                for (int k = 0; k < kRingSlots; k++) ring_wait(&bars[k], (phase >> k) & 1u);
+            }
         }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) return;
+        __syncwarp();
+        island_finish(d, rs, rc, bs, bc, dv, lane, 32);
+        __syncwarp();
     }
 }
 
@@ -348,14 +525,36 @@ __global__ void k_integrate(Dev d, int last) {
     }
 }
 
-__global__ void k_refresh_tensors(Dev d) {
+// External state write (cpgpu_batch_write_state): velocities are taken as
+// given; a body whose pose changed gets its world inertia tensors and AABB
+// recomputed from the new pose, an unchanged body keeps them bit for bit.
+__global__ void k_apply_state(Dev d) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
-        if (d.movement[i] != 0) continue;
-        float4 q = qnormalize(d.rot[i]);
+        const float4 p = d.stage[4 * i], q = d.stage[4 * i + 1], v = d.stage[4 * i + 2], w = d.stage[4 * i + 3];
+        if (d.movement[i] != 1) {
+            d.vel[i] = make_float4(v.x, v.y, v.z, 0.f);
+            d.angv[i] = make_float4(w.x, w.y, w.z, 0.f);
+        }
+        const float4 p0 = d.pos[i], q0 = d.rot[i];
+        if (p.x == p0.x && p.y == p0.y && p.z == p0.z && q.x == q0.x && q.y == q0.y && q.z == q0.z && q.w == q0.w) continue;
+        d.pos[i] = make_float4(p.x, p.y, p.z, p0.w);
         d.rot[i] = q;
         M33 R = quatRot(q), Rc = quatRot(qconj(q));
-        store9(d.iw + 9 * i, mul(mul(R, load9(d.iref + 9 * i)), Rc));
-        store9(d.iinv + 9 * i, mul(mul(R, load9(d.iinv_ref + 9 * i)), Rc));
+        if (d.movement[i] == 0) {
+            store9(d.iw + 9 * i, mul(mul(R, load9(d.iref + 9 * i)), Rc));
+            store9(d.iinv + 9 * i, mul(mul(R, load9(d.iinv_ref + 9 * i)), Rc));
+        }
+        const uint8_t* blob = d.shapes + d.shape[i];
+        const HullHeader* H = reinterpret_cast<const HullHeader*>(blob);
+        const float4* vv = reinterpret_cast<const float4*>(blob + sizeof(HullHeader));
+        f3 c = mk(p), mn = mk(INFINITY, INFINITY, INFINITY), mx = mk(-INFINITY, -INFINITY, -INFINITY);
+        for (int k = 0; k < H->nv; k++) {
+            f3 x = c + mul(R, mk(vv[k]));
+            mn.x = fminf(mn.x, x.x); mn.y = fminf(mn.y, x.y); mn.z = fminf(mn.z, x.z);
+            mx.x = fmaxf(mx.x, x.x); mx.y = fmaxf(mx.y, x.y); mx.z = fmaxf(mx.z, x.z);
+        }
+        d.aabb_lo[i] = make_float4(mn.x, mn.y, mn.z, 0.f);
+        d.aabb_hi[i] = make_float4(mx.x, mx.y, mx.z, 0.f);
     }
 }
 
@@ -371,17 +570,37 @@ void launch_rows(const Dev& d, int first, int last, const Launch& L) {
     k_rows<<<L.n_sms * 8, 128, 0, L.st>>>(d, first, last);
 }
 
-void launch_pgs(const Dev& d, const Launch& L) {
-    k_pgs<<<L.n_sms * 4, 64, 0, L.st>>>(d);
+int pgs_big_smem_bytes(int dv_cap) {
+    return 64 + kRingSlots * kChunkRows * (int)sizeof(RowBlock) + dv_cap * 64;
+}
+
+void prepare_pgs(int dv_cap) {
+    cudaFuncSetAttribute(k_pgs_big, cudaFuncAttributeMaxDynamicSharedMemorySize, pgs_big_smem_bytes(dv_cap));
+}
+
+void launch_pgs_schedule(const Dev& d, const Launch& L) {
+    k_sched_reset<<<1, 96, 0, L.st>>>(d);
+    k_sched_count<<<L.n_sms * 2, 256, 0, L.st>>>(d);
+    k_sched_place<<<L.n_sms * 2, 256, 0, L.st>>>(d);
+}
+
+void launch_pgs(const Dev& d, int dv_cap, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, const Launch& L) {
+    // large islands on the main stream, small ones concurrently on a side branch
+    cudaMemsetAsync(d.sched + 2, 0, sizeof(int), L.st);
+    cudaEventRecord(fork, L.st);
+    cudaStreamWaitEvent(side, fork, 0);
+    k_pgs_small<<<L.n_sms * 4, 64, 0, side>>>(d);
+    cudaEventRecord(join, side);
+    k_pgs_big<<<L.n_sms * 3, 32, pgs_big_smem_bytes(dv_cap), L.st>>>(d, dv_cap);
+    cudaStreamWaitEvent(L.st, join, 0);
 }
 
 void launch_integrate(const Dev& d, int last, const Launch& L) {
     k_integrate<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d, last);
 }
 
-void launch_refresh(const Dev& d, const Launch& L) {
-    k_refresh_tensors<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d);
-    launch_geometry(d, 1, L);
+void launch_apply_state(const Dev& d, const Launch& L) {
+    k_apply_state<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d);
 }
 
 }  // namespace cpgpu

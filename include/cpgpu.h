@@ -194,8 +194,11 @@ int cpgpu_batch_info(cpgpu_batch* b, int64_t* n_bodies, int64_t* n_worlds, int64
 int cpgpu_batch_step_timed(cpgpu_batch* b, int n_steps, double* device_ms);
 /* Whole-batch state transfer in the device layout: 16 floats per body
  * (com xyz, inverse mass, quaternion r i j k, velocity xyz + pad, angular
- * velocity xyz + pad), bodies in batch order.  Writing recomputes the world
- * inertia tensors and AABBs from the new poses; the contact graph is kept. */
+ * velocity xyz + pad), bodies in batch order.  Writing takes the velocities
+ * as given; bodies whose pose changed get their world inertia tensors and
+ * AABBs recomputed (unchanged bodies keep them exactly, so a read/write round
+ * trip does not perturb the simulation); the inverse mass slot is ignored on
+ * write and the contact graph is kept. */
 int cpgpu_batch_read_state(cpgpu_batch* b, float* out);
 int cpgpu_batch_write_state(cpgpu_batch* b, const float* in);
 /* Per-stage device time of n_steps run stage by stage (no graph), for the

@@ -1,0 +1,181 @@
+// cpgpu_engine.hpp — header-only C++ facade over the cpgpu C ABI with the
+// method names of the reference's phyz::PhysicsEngine
+// (ConstraintPhysics/src/PhysicsEngine.h:60-161), so scene code written for
+// the reference compiles against the device path with a namespace change.
+//
+// Differences a caller sees:
+//   * bodies are addressed by id (RigidBody handles wrap the id);
+//   * errors that the reference reports with assert() throw cpgpu::Error;
+//   * only the contact path is on the device: convex hulls and boxes, ball
+//     sockets and hinges are the supported shapes/joints (others throw
+//     cpgpu::Error with CPGPU_ERR_UNSUPPORTED), sleeping stays disabled.
+#pragma once
+#include <array>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cpgpu.h"
+
+namespace cpgpu {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(int rc) {
+    if (rc != CPGPU_OK) throw Error(rc, std::string("cpgpu: ") + cpgpu_last_error());
+}
+
+struct Vec3 {
+    double x = 0, y = 0, z = 0;
+    Vec3() {}
+    Vec3(double a, double b, double c) : x(a), y(b), z(c) {}
+    const double* data() const { return &x; }
+};
+struct Quaternion {
+    double r = 1, i = 0, j = 0, k = 0;
+    Quaternion() {}
+    Quaternion(double a, double b, double c, double d) : r(a), i(b), j(c), k(d) {}
+};
+
+enum MovementType { DYNAMIC = CPGPU_DYNAMIC, FIXED = CPGPU_FIXED, KINEMATIC = CPGPU_KINEMATIC };
+
+// Material (ConvexPrimitive.h:17-34)
+struct Material {
+    double density = 1.0, restitution = 0.3, kinetic_friction_coeff = 0.6, static_friction_coeff = 1.1;
+    static Material default_material() { return Material(); }
+    static Material modified_density(double d) { Material m; m.density = d; return m; }
+    cpgpu_material c() const { return cpgpu_material{density, restitution, kinetic_friction_coeff, static_friction_coeff}; }
+};
+
+// ConvexUnionGeometry restricted to one convex primitive (Geometry.h:9-47)
+struct ConvexUnionGeometry {
+    enum Kind { HULL, BOX } kind = HULL;
+    std::vector<Vec3> points;
+    std::vector<std::vector<int>> faces;
+    Vec3 corner;
+    double dx = 0, dy = 0, dz = 0;
+    Material material;
+    static ConvexUnionGeometry box(Vec3 pos, double dx, double dy, double dz, Material m = Material::default_material()) {
+        ConvexUnionGeometry g;
+        g.kind = BOX; g.corner = pos; g.dx = dx; g.dy = dy; g.dz = dz; g.material = m;
+        return g;
+    }
+    static ConvexUnionGeometry polyhedron(const std::vector<Vec3>& pts, const std::vector<std::vector<int>>& faces,
+                                          Material m = Material::default_material()) {
+        ConvexUnionGeometry g;
+        g.kind = HULL; g.points = pts; g.faces = faces; g.material = m;
+        return g;
+    }
+};
+
+class PhysicsEngine;
+
+// Handle with the RigidBody getters/setters used by scene code (RigidBody.h:25-68)
+class RigidBody {
+public:
+    RigidBody(PhysicsEngine* e, uint32_t id) : e_(e), id_(id) {}
+    uint32_t getID() const { return id_; }
+    Vec3 getCOM() const;
+    Quaternion getOrientation() const;
+    Vec3 getVel() const;
+    Vec3 getAngVel() const;
+    void setVel(Vec3 v);
+    void setAngVel(Vec3 w);
+    void setOrientation(Quaternion q);
+    void setToPosition(const Vec3& p);
+    void setMass(double m);
+private:
+    PhysicsEngine* e_;
+    uint32_t id_;
+};
+
+struct ConstraintID { uint32_t id; };
+
+class PhysicsEngine {
+public:
+    PhysicsEngine() { check(cpgpu_world_create(&w_)); }
+    ~PhysicsEngine() { if (w_) cpgpu_world_destroy(w_); for (RigidBody* b : owned_) delete b; }
+    PhysicsEngine(const PhysicsEngine&) = delete;
+    PhysicsEngine& operator=(const PhysicsEngine&) = delete;
+
+    void timeStep() { check(cpgpu_step(w_, 1)); }
+    void timeSteps(int n) { check(cpgpu_step(w_, n)); }
+
+    RigidBody* createRigidBody(const ConvexUnionGeometry& g, MovementType movement = DYNAMIC, Vec3 position = Vec3()) {
+        uint32_t id = 0;
+        cpgpu_material m = g.material.c();
+        if (g.kind == ConvexUnionGeometry::BOX) {
+            check(cpgpu_body_box(w_, g.corner.data(), g.dx, g.dy, g.dz, &m, movement, position.data(), &id));
+        } else {
+            std::vector<double> pts;
+            for (const Vec3& p : g.points) { pts.push_back(p.x); pts.push_back(p.y); pts.push_back(p.z); }
+            std::vector<int> offs{0}, idx;
+            for (const auto& f : g.faces) { idx.insert(idx.end(), f.begin(), f.end()); offs.push_back((int)idx.size()); }
+            check(cpgpu_body_hull(w_, pts.data(), (int)g.points.size(), offs.data(), idx.data(), (int)g.faces.size(), &m,
+                                  movement, position.data(), &id));
+        }
+        RigidBody* b = new RigidBody(this, id);
+        owned_.push_back(b);
+        return b;
+    }
+
+    ConstraintID addBallSocketConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, double strength = 15000) {
+        uint32_t id = 0;
+        check(cpgpu_add_ball_socket(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), strength, &id));
+        return ConstraintID{id};
+    }
+    ConstraintID addHingeConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, Vec3 a1, Vec3 a2,
+                                    double pos_strength = 15000, double rot_strength = 15000) {
+        uint32_t id = 0;
+        check(cpgpu_add_hinge(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), a1.data(), a2.data(), pos_strength,
+                              rot_strength, &id));
+        return ConstraintID{id};
+    }
+
+    void setStep_time(double d) { check(cpgpu_set_step_time(w_, d)); }
+    void setGravity(const Vec3& g) { check(cpgpu_set_gravity(w_, g.x, g.y, g.z)); }
+    void setSubstepCount(int c) { check(cpgpu_set_substep_count(w_, c)); }
+    void setPGSIterations(int v, int p, int h = 1) { check(cpgpu_set_pgs_iterations(w_, v, p, h)); }
+    void setSleepingEnabled(bool s) { check(cpgpu_set_sleeping_enabled(w_, s ? 1 : 0)); }
+    void setWarmStartDisabled(bool b) { check(cpgpu_set_warm_start_disabled(w_, b ? 1 : 0)); }
+    void setGlobalConstraintForceMixing(double c) { check(cpgpu_set_global_cfm(w_, c)); }
+    void setAngleVelUpdateTickCount(int n) { check(cpgpu_set_angle_vel_update_tick_count(w_, n)); }
+    void setInternalGyroscopicForcesDisabled(bool b) { check(cpgpu_set_internal_gyro_forces_disabled(w_, b ? 1 : 0)); }
+    uint32_t getNumBodies() { int n = 0; check(cpgpu_num_bodies(w_, &n)); return (uint32_t)n; }
+
+    cpgpu_world* handle() { return w_; }
+
+    // per-body state of body `id` (all bodies are fetched; cache when iterating)
+    void bodyState(uint32_t id, double* com, double* quat, double* vel, double* ang) {
+        int n = (int)getNumBodies();
+        std::vector<double> c(3 * n), q(4 * n), v(3 * n), a(3 * n);
+        check(cpgpu_get_body_state(w_, c.data(), q.data(), v.data(), a.data()));
+        size_t i = id - 1;
+        if (com) for (int k = 0; k < 3; k++) com[k] = c[3 * i + k];
+        if (quat) for (int k = 0; k < 4; k++) quat[k] = q[4 * i + k];
+        if (vel) for (int k = 0; k < 3; k++) vel[k] = v[3 * i + k];
+        if (ang) for (int k = 0; k < 3; k++) ang[k] = a[3 * i + k];
+    }
+
+private:
+    cpgpu_world* w_ = nullptr;
+    std::vector<RigidBody*> owned_;
+};
+
+inline Vec3 RigidBody::getCOM() const { double c[3]; e_->bodyState(id_, c, nullptr, nullptr, nullptr); return Vec3(c[0], c[1], c[2]); }
+inline Quaternion RigidBody::getOrientation() const {
+    double q[4]; e_->bodyState(id_, nullptr, q, nullptr, nullptr); return Quaternion(q[0], q[1], q[2], q[3]);
+}
+inline Vec3 RigidBody::getVel() const { double v[3]; e_->bodyState(id_, nullptr, nullptr, v, nullptr); return Vec3(v[0], v[1], v[2]); }
+inline Vec3 RigidBody::getAngVel() const { double a[3]; e_->bodyState(id_, nullptr, nullptr, nullptr, a); return Vec3(a[0], a[1], a[2]); }
+inline void RigidBody::setVel(Vec3 v) { check(cpgpu_body_set_velocity(e_->handle(), id_, v.data())); }
+inline void RigidBody::setAngVel(Vec3 w) { check(cpgpu_body_set_ang_velocity(e_->handle(), id_, w.data())); }
+inline void RigidBody::setOrientation(Quaternion q) { double d[4] = {q.r, q.i, q.j, q.k}; check(cpgpu_body_set_orientation(e_->handle(), id_, d)); }
+inline void RigidBody::setToPosition(const Vec3& p) { check(cpgpu_body_set_position(e_->handle(), id_, p.data())); }
+inline void RigidBody::setMass(double m) { check(cpgpu_body_set_mass(e_->handle(), id_, m)); }
+
+}  // namespace cpgpu

@@ -1,0 +1,36 @@
+"""The C++ facade (include/cpgpu_engine.hpp) compiles against the C ABI and
+links with the device library; the reference scenario written against it runs
+(on a GPU) or fails loudly with CPGPU_ERR_NO_DEVICE (without one)."""
+import os
+import subprocess
+
+import pytest
+
+import constraintphysics_gb300 as cg
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+
+
+def _build(tmp_path):
+    exe = str(tmp_path / "facade_box_drop")
+    lib_dir = os.path.dirname(cg.LIB_PATH)
+    cmd = ["g++", "-std=c++17", "-O1", "-I" + os.path.join(REPO, "include"), os.path.join(HERE, "cxx", "facade_box_drop.cpp"),
+           "-L" + lib_dir, "-lcpgpu", "-Wl,-rpath," + lib_dir, "-o", exe]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return exe
+
+
+def test_facade_compiles_and_fails_loudly_without_gpu(tmp_path):
+    exe = _build(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode in (0, 2), r.stdout + r.stderr
+    if r.returncode == 2:
+        assert "no CUDA device" in r.stdout
+
+
+@pytest.mark.gpu
+def test_facade_box_drop_on_device(tmp_path):
+    exe = _build(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
