@@ -33,6 +33,8 @@ static int fail(int code, const std::string& msg) {
     return code;
 }
 
+void set_last_error(const char* msg) { g_err = msg; }
+
 #define CK(call)                                                                            \
     do {                                                                                    \
         cudaError_t e_ = (call);                                                            \

@@ -16,6 +16,7 @@ struct Launch {
 void scan_exclusive(const int* in, int* out, const int* n_dev, int n_host, int cap, int* total, int* tmp, const Launch& L);
 
 void prepare_kernels();   // one-time function attributes (outside graph capture)
+void set_last_error(const char* msg);   // message returned by cpgpu_last_error
 void launch_gravity(const Dev& d, const Launch& L);
 void launch_pairs(const Dev& d, const Launch& L);
 void launch_geometry(const Dev& d, int force_all, const Launch& L);

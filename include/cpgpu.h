@@ -210,6 +210,30 @@ int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* 
 /* Number of kernel launches one step of the batch issues. */
 int cpgpu_batch_launches_per_step(cpgpu_batch* b, int* n);
 
+/* ---- allocation-free pair generation ------------------------------------ */
+/* No counterpart in the reference (its broadphase is the AABB tree inside
+ * PhysicsEngine::timeStep).  For callers that cannot allocate device memory
+ * when they need the broadphase -- code living inside another framework's
+ * memory pool, real-time loops that must not enter the driver's allocator,
+ * plugins handed only pre-allocated buffers -- this computes the same
+ * candidate pairs as the device path's pair generation for one set of AABBs
+ * and allocates nothing: every buffer is the caller's device memory, and the
+ * only scratch is a fixed file-scope device array (about 260 KB, held by
+ * every GPU that loads the library until the process exits).
+ *   aabbs   device, n_bodies x 6 floats (min xyz, max xyz)
+ *   pairs   device, cap x 2 uint32: (i, j) with 1-based ids, i < j, sorted
+ *   count   device int: number of overlapping pairs (may exceed cap; only
+ *           the first cap are written)
+ *   stream  cudaStream_t (NULL: the default stream)
+ * n_bodies may be at most 65536; larger sizes return CPGPU_ERR_INVALID_ARG
+ * with a message.  The first call on a device looks up the scratch array's
+ * device address (with that device current), so make that first call before
+ * any stream capture.  Every call on a device shares the scratch array, so
+ * calls whose executions overlap on the GPU (different streams without
+ * ordering) race; calls ordered on one stream are safe.  Each call rewrites
+ * all the scratch it reads. */
+int cpgpu_pairs_noalloc(const float* aabbs, int n_bodies, uint32_t* pairs, int cap, int* count, void* stream);
+
 /* ---- diagnostics -------------------------------------------------------- */
 /* Last error message of this thread (static storage, never NULL). */
 const char* cpgpu_last_error(void);

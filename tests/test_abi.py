@@ -35,7 +35,8 @@ def test_device_library_exports_every_declared_symbol():
 def test_oracle_libraries_export_the_world_api(oracle_mod, which):
     abi = oracle_mod.ref_abi() if which == "ref" else oracle_mod.port_abi()
     prefix = "cpref_" if which == "ref" else "cport_"
-    batch_only = {n[len("cpgpu_"):] for n in declared() if n.startswith("cpgpu_batch_")}
+    # batches and the allocation-free pair entry point exist on the device path only
+    batch_only = {n[len("cpgpu_"):] for n in declared() if n.startswith("cpgpu_batch_")} | {"pairs_noalloc"}
     state_import = {"set_body_state", "set_contacts"}
     for n in declared():
         short = n[len("cpgpu_"):]
