@@ -10,6 +10,7 @@
 // scan gives each body its output offset, and a second pass writes.
 #include "kernels.cuh"
 #include "devmath.cuh"
+#include "shapes.cuh"
 
 namespace cpgpu {
 
@@ -117,8 +118,8 @@ __global__ void k_clamp_pairs(Dev d) {
 }
 
 // RigidBody::updateGeometry (RigidBody.cpp:281-312) for moved bodies: the
-// orientation is renormalised and the AABB recomputed from the world vertices
-// (Polyhedron::gen_AABB, ConvexPrimitive.cpp:660-676).
+// orientation is renormalised and the AABB recomputed from the world geometry
+// (gen_AABB of the body's primitive).
 __global__ void k_geometry(Dev d, int force_all) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
         if (!force_all && (d.movement[i] == 1 || !d.moved[i])) continue;
@@ -127,15 +128,8 @@ __global__ void k_geometry(Dev d, int force_all) {
         d.rot[i] = q;
         M33 R = quatRot(q);
         f3 c = mk(d.pos[i]);
-        const uint8_t* blob = d.shapes + d.shape[i];
-        const HullHeader* H = reinterpret_cast<const HullHeader*>(blob);
-        const float4* v = reinterpret_cast<const float4*>(blob + sizeof(HullHeader));
-        f3 mn = mk(INFINITY, INFINITY, INFINITY), mx = mk(-INFINITY, -INFINITY, -INFINITY);
-        for (int k = 0; k < H->nv; k++) {
-            f3 p = c + mul(R, mk(v[k]));
-            mn.x = fminf(mn.x, p.x); mn.y = fminf(mn.y, p.y); mn.z = fminf(mn.z, p.z);
-            mx.x = fmaxf(mx.x, p.x); mx.y = fmaxf(mx.y, p.y); mx.z = fmaxf(mx.z, p.z);
-        }
+        f3 mn, mx;
+        shape_aabb(d.shapes + d.shape[i], c, R, &mn, &mx);
         d.aabb_lo[i] = make_float4(mn.x, mn.y, mn.z, 0.f);
         d.aabb_hi[i] = make_float4(mx.x, mx.y, mx.z, 0.f);
     }

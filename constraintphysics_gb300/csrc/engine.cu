@@ -198,6 +198,55 @@ static Shape pack_hull(const HullPrep& h, const D3& com) {
     return s;
 }
 
+// Sphere / cylinder blobs (layout.h), geometry given in the reference frame.
+static Shape pack_prim(uint32_t kind, const std::vector<float4>& body, float bound) {
+    HullHeader H;
+    std::memset(&H, 0, sizeof(H));
+    std::vector<uint8_t> b(sizeof(HullHeader));
+    for (const float4& v : body) put(b, v);
+    H.size16 = (uint16_t)(b.size() / 16);
+    H.off_fofs = (uint16_t)b.size();   // the whole blob is staged
+    H.kind = kind;
+    H.radius = bound;
+    std::memcpy(b.data(), &H, sizeof(H));
+    Shape s;
+    s.blob = std::move(b);
+    s.hot = H.off_fofs;
+    return s;
+}
+
+static float4 f4(const D3& v, double w) { return make_float4((float)v.x, (float)v.y, (float)v.z, (float)w); }
+
+// Sphere at `cref` (reference frame) of radius r
+static Shape pack_sphere(const D3& cref, double r) {
+    return pack_prim(SHAPE_SPHERE, {f4(cref, r)}, (float)(cref.mag() + r));
+}
+
+// Cylinder (ConvexPrimitive.cpp:222-256, default height axis (0,1,0)) centred at
+// `cref` in the reference frame: Gauss vertices of the two caps and the
+// 12-vertex ring, and the 8-gon cap approximations of radius r / cos(pi/8).
+// PI is the reference's truncated 3.1415926535 (Math/src/Quaternion.h:4).
+static Shape pack_cylinder(const D3& cref, double r, double h) {
+    const double pi = 3.1415926535;
+    std::vector<float4> v;
+    v.push_back(f4(cref, r));
+    v.push_back(make_float4(0.f, 1.f, 0.f, (float)h));
+    v.push_back(make_float4(0.f, 1.f, 0.f, 0.f));
+    v.push_back(make_float4(0.f, -1.f, 0.f, 0.f));
+    for (int i = 0; i < kCylRing; i++) {
+        double th = i * (2 * pi / kCylRing);
+        v.push_back(make_float4((float)std::sin(th), 0.f, (float)std::cos(th), 0.f));
+    }
+    double er = r / std::cos(pi / kCylCap);
+    for (int side = 0; side < 2; side++)
+        for (int i = 0; i < kCylCap; i++) {
+            double th = i * (2 * pi / kCylCap);
+            double y = side == 0 ? h / 2.0 : -h / 2.0;
+            v.push_back(f4(cref + D3(er * std::sin(th), y, er * std::cos(th)), 0));
+        }
+    return pack_prim(SHAPE_CYLINDER, v, (float)(cref.mag() + std::sqrt(er * er + h * h / 4)));
+}
+
 // ---------------------------------------------------------------- device batch ----
 struct Arena {
     uint8_t* base = nullptr;
@@ -216,6 +265,7 @@ struct Batch {
     int substeps = 1;
     int n_sms = 0;
     int slot_bytes = 0;
+    bool prims = false;                // the batch holds spheres or cylinders
     cudaStream_t st = nullptr;
     cudaStream_t side = nullptr;       // concurrent branch (small-island PGS)
     cudaEvent_t fork = nullptr, join = nullptr;
@@ -251,7 +301,7 @@ struct Batch {
         mark(0);
         launch_gravity(x, L);      mark(1);
         launch_pairs(x, L);        mark(2);
-        launch_narrowphase(x, slot_bytes, n_sms, st); mark(3);
+        launch_narrowphase(x, slot_bytes, n_sms, prims, st); mark(3);
         launch_merge(x, L);        mark(4);
         launch_islands(x, L);
         launch_pgs_schedule(x, L); mark(5);
@@ -262,10 +312,10 @@ struct Batch {
         }
         launch_geometry(x, 0, L);  mark(6 + 3 * substeps);
     }
-    // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 1,
-    // merge 6 + 3 scans, islands 2 + scan 3, schedule 3, 4 per substep
-    // (rows, small + large PGS, integrate), geometry 1
-    int launches_per_step() const { return 1 + 6 + 1 + (6 + 9) + (2 + 3) + 3 + 4 * substeps + 1; }
+    // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 1
+    // (+1 with spheres / cylinders), merge 6 + 3 scans, islands 2 + scan 3,
+    // schedule 3, 4 per substep (rows, small + large PGS, integrate), geometry 1
+    int launches_per_step() const { return 1 + 6 + 1 + (prims ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 4 * substeps + 1; }
 
     void build_graphs() {
         for (int p = 0; p < 2; p++) {
@@ -372,6 +422,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
                 shape_pool_off[s] = it->second;
             }
             max_hot = std::max(max_hot, (sh.hot + 15) & ~15);
+            if (reinterpret_cast<const HullHeader*>(sh.blob.data())->kind != SHAPE_HULL) B->prims = true;
         }
         const int base = wstart[wi];
         for (size_t i = 0; i < w.bodies.size(); i++) {
@@ -698,6 +749,54 @@ static uint32_t add_hull(World& w, const std::vector<D3>& pts, const std::vector
     return id;
 }
 
+// calculateMassProperties (RigidBody.cpp:427-640), SPHERE and CYLINDER cases
+// for a one-primitive body with the default height axis: mass, centre of mass
+// and the inertia tensor about it.
+static void prim_mass(bool sphere, const D3& c, double r, double h, double density, double* mass, double t[9]) {
+    const double pi = 3.1415926535;
+    double m, d0, d1;
+    if (sphere) {
+        m = (4.0 / 3.0) * pi * r * r * r * density;
+        d0 = d1 = 2.0 / 5.0 * m * r * r;
+    } else {
+        m = pi * r * r * h * density;
+        d0 = m * (h * h / 12 + r * r / 4);
+        d1 = m * r * r / 2;
+    }
+    (void)c;   // one primitive: its centre is the centre of mass, the parallel-axis terms cancel
+    *mass = m;
+    for (int k = 0; k < 9; k++) t[k] = 0;
+    t[0] = d0; t[4] = d1; t[8] = d0;
+}
+
+static uint32_t add_prim(World& w, bool sphere, const D3& center, double r, double h, const cpgpu_material* m,
+                         int movement, const double* pos) {
+    if (movement < 0 || movement > 2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad movement type"};
+    if (movement == CPGPU_KINEMATIC) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "kinematic bodies are not implemented on the device path"};
+    if (!(r > 0) || (!sphere && !(h > 0))) throw ApiFail{CPGPU_ERR_INVALID_ARG, "radius and height must be > 0"};
+    Body b;
+    double density = m ? m->density : 1.0;
+    prim_mass(sphere, center, r, h, density, &b.mass, b.iref);
+    b.com = center;
+    inv3(b.iref, b.iinv_ref);
+    std::memcpy(b.iw, b.iref, sizeof(b.iw));
+    std::memcpy(b.iinv, b.iinv_ref, sizeof(b.iinv));
+    Shape s = sphere ? pack_sphere(D3(), r) : pack_cylinder(D3(), r, h);
+    b.local_origin = -b.com;
+    D3 p = pos ? D3(pos[0], pos[1], pos[2]) : D3();
+    D3 tracked = b.com + qrot(b.q, b.local_origin);
+    b.com = b.com + (p - tracked);
+    b.movement = movement;
+    if (m) { b.rest = m->restitution; b.kin = m->kinetic_friction; b.sta = m->static_friction; }
+    begin_mutation(w);
+    b.shape = (int)w.shapes.size();
+    w.shapes.push_back(std::move(s));
+    w.bodies.push_back(b);
+    uint32_t id = (uint32_t)w.bodies.size();
+    w.nodes[id] = (int)id - 1;
+    return id;
+}
+
 static void ensure_device(World& w) {
     if (w.dev && w.dev_valid) return;
     w.dev.reset();
@@ -806,11 +905,28 @@ int cpgpu_body_box(cpgpu_world* w, const double c[3], double dx, double dy, doub
     });
 }
 
-int cpgpu_body_sphere(cpgpu_world*, const double*, double, const cpgpu_material*, int, const double*, uint32_t*) {
-    return fail(CPGPU_ERR_UNSUPPORTED, "spheres are not implemented on the device path yet");
+int cpgpu_body_sphere(cpgpu_world* w, const double center[3], double radius, const cpgpu_material* m, int movement,
+                      const double pos[3], uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!center) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null center"};
+        uint32_t id = add_prim(w->w, true, D3(center[0], center[1], center[2]), radius, 0, m, movement, pos);
+        if (out_id) *out_id = id;
+        return CPGPU_OK;
+    });
 }
-int cpgpu_body_cylinder(cpgpu_world*, const double*, double, double, const cpgpu_material*, int, const double*, uint32_t*) {
-    return fail(CPGPU_ERR_UNSUPPORTED, "cylinders are not implemented on the device path yet");
+// ConvexUnionGeometry::cylinder (Geometry.cpp:47-49): `base` is the centre of
+// the bottom cap, the height axis is +y
+int cpgpu_body_cylinder(cpgpu_world* w, const double base[3], double radius, double height, const cpgpu_material* m,
+                        int movement, const double pos[3], uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!base) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null base"};
+        D3 c(base[0], base[1] + height / 2.0, base[2]);
+        uint32_t id = add_prim(w->w, false, c, radius, height, m, movement, pos);
+        if (out_id) *out_id = id;
+        return CPGPU_OK;
+    });
 }
 int cpgpu_body_mesh(cpgpu_world*, const double*, int, const int*, int, const cpgpu_material*, int, uint32_t*) {
     return fail(CPGPU_ERR_UNSUPPORTED, "static meshes are not implemented on the device path yet");

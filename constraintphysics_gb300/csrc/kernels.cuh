@@ -20,7 +20,9 @@ void set_last_error(const char* msg);   // message returned by cpgpu_last_error
 void launch_gravity(const Dev& d, const Launch& L);
 void launch_pairs(const Dev& d, const Launch& L);
 void launch_geometry(const Dev& d, int force_all, const Launch& L);
-void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, cudaStream_t st);
+// hull-hull pairs, then (when the batch holds spheres or cylinders) the pairs
+// that involve one
+void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st);
 void launch_merge(const Dev& d, const Launch& L);
 void launch_islands(const Dev& d, const Launch& L);
 void launch_rows(const Dev& d, int first, int last, const Launch& L);

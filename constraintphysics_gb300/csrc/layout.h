@@ -25,7 +25,7 @@ struct alignas(16) HullHeader {
     uint16_t off_edge, off_arc;    // uint8 pairs
     uint16_t off_vfofs, off_vfidx; // vertex -> adjacent faces CSR
     uint16_t off_veofs, off_veidx; // vertex -> adjacent edges CSR
-    uint32_t kind;                 // 0 = hull
+    uint32_t kind;                 // ShapeKind
     float radius;                  // bound on |vertex| (reference frame)
     uint32_t pad[2];
 };
@@ -35,6 +35,21 @@ static_assert(sizeof(HullHeader) == 48, "hull header size");
 // cache: float4 {max, min, bits(max_id), bits(min_id)} x nf: extrema of the hull
 //        along its own face normal, in the reference frame; the world value adds
 //        dot(R n, com) (the recentring of CollisionDetect.cpp:622-625)
+// ---- sphere and cylinder blobs ------------------------------------------------
+// Same header (kind 1 = sphere, 2 = cylinder; nv = nf = ne = na = 0; the whole
+// blob is the hot part, off_fofs = its size), then, in the reference frame:
+//   float4 c      {centre xyz, radius}
+// cylinders only (Cylinder, ConvexPrimitive.h:160-210; 12 Gauss ring vertices,
+// 8-gon cap approximations):
+//   float4 axis   {height axis xyz, height}
+//   float4 gv[14] Gauss vertices: caps (+axis, -axis), then the ring
+//   float4 top[8] top-cap 8-gon
+//   float4 bot[8] bottom-cap 8-gon
+enum ShapeKind : uint32_t { SHAPE_HULL = 0, SHAPE_SPHERE = 1, SHAPE_CYLINDER = 2 };
+constexpr int kCylRing = 12, kCylCap = 8;
+constexpr int kCylOffAxis = 64, kCylOffGv = 80, kCylOffTop = 80 + 16 * 14, kCylOffBot = 80 + 16 * 22;
+constexpr int kSphereBlob = 64, kCylBlob = 80 + 16 * 30;
+
 constexpr int kMaxHullVerts = 255;   // uint8 vertex ids
 constexpr int kMaxHullFaces = 255;
 constexpr int kMaxHullEdges = 255;

@@ -317,6 +317,519 @@ __device__ __forceinline__ void stage_hull(const uint8_t* g, uint8_t* s, const f
     hv->com = com;
 }
 
+// cull_manifold (CollisionDetect.cpp:2795-2830) to at most 4 points and write
+// the pair's manifold
+__device__ void emit_manifold(const Dev& d, int p, f3 n, float maxpen, const float4* pts, const unsigned long long* magic, int m) {
+    int out_n = m;
+    int pick[4] = {0, 1, 2, 3};
+    if (m > 4) {
+        out_n = 4;
+        unsigned long long avail = (m >= 64) ? ~0ull : ((1ull << m) - 1ull);
+        f3 cu, cw;
+        basis(n, &cu, &cw);
+        const float cs[4] = {1.0f, 6.123233995736766e-17f, -1.0f, -1.8369701987210297e-16f};
+        const float sn[4] = {0.0f, 1.0f, 1.2246467991473532e-16f, -1.0f};
+        for (int i = 0; i < 4; i++) {
+            f3 dir = cu * cs[i] + cw * sn[i];
+            int bi2 = -1;
+            float bv = -INFINITY;
+            for (int j = 0; j < m; j++) {
+                if (!((avail >> j) & 1ull)) continue;
+                float v = dot(mk(pts[j]), dir);
+                if (v > bv) { bv = v; bi2 = j; }
+            }
+            if (bi2 < 0) { out_n = i; break; }
+            pick[i] = bi2;
+            avail &= ~(1ull << bi2);
+        }
+    }
+    for (int i = 0; i < out_n; i++) {
+        d.mf_pt[4 * p + i] = pts[pick[i]];
+        d.mf_magic[4 * p + i] = magic[pick[i]];
+    }
+    d.mf_n[p] = make_float4(n.x, n.y, n.z, maxpen);
+    d.mf_cnt[p] = out_n;
+}
+
+__device__ __forceinline__ void no_manifold(const Dev& d, int p) {
+    d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f);
+    d.mf_cnt[p] = 0;
+}
+
+// warp argmin over (pen, axis order); every lane gets the winner
+__device__ __forceinline__ Axis warp_best(const Axis& best) {
+    float bp = best.pen;
+    int bi = best.idx;
+    for (int o = 16; o > 0; o >>= 1) {
+        float op = __shfl_xor_sync(0xffffffffu, bp, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (op < bp || (op == bp && oi < bi)) { bp = op; bi = oi; }
+    }
+    unsigned owner_mask = __ballot_sync(0xffffffffu, best.idx == bi && best.pen == bp);
+    int owner = owner_mask ? __ffs(owner_mask) - 1 : 0;
+    Axis w;
+    w.pen = bp;
+    w.idx = bi;
+    w.n = mk(__shfl_sync(0xffffffffu, best.n.x, owner), __shfl_sync(0xffffffffu, best.n.y, owner),
+             __shfl_sync(0xffffffffu, best.n.z, owner));
+    w.aid = __shfl_sync(0xffffffffu, best.aid, owner);
+    w.bid = __shfl_sync(0xffffffffu, best.bid, owner);
+    return w;
+}
+
+// ---- spheres and cylinders ------------------------------------------------------
+// Sphere (ConvexPrimitive.h:79-109) and Cylinder (:160-210) in world space.
+struct PrimView {
+    uint32_t kind;
+    f3 c, axis;
+    float r, h;
+    const float4 *gv, *top, *bot;   // cylinder: Gauss vertices, cap 8-gons
+};
+
+// world pose of a staged sphere / cylinder blob; the cylinder's Gauss vertices
+// and caps are transformed in place (Cylinder::recomputeFromReference,
+// ConvexPrimitive.cpp:272-287: the bottom cap is top - height * axis)
+__device__ void stage_prim(uint8_t* s, float4 pos, float4 rot, PrimView* pv, int lane) {
+    const HullHeader* H = reinterpret_cast<const HullHeader*>(s);
+    M33 R = quatRot(qnormalize(rot));
+    f3 com = mk(pos);
+    float4 cref = *reinterpret_cast<const float4*>(s + sizeof(HullHeader));
+    pv->kind = H->kind;
+    pv->r = cref.w;
+    pv->c = mul(R, mk(cref)) + com;
+    pv->axis = mk(0.f, 0.f, 0.f);
+    pv->h = 0.f;
+    if (H->kind != SHAPE_CYLINDER) return;
+    float4 ax = *reinterpret_cast<const float4*>(s + kCylOffAxis);
+    pv->axis = mul(R, mk(ax));
+    pv->h = ax.w;
+    float4* gv = reinterpret_cast<float4*>(s + kCylOffGv);
+    float4* top = reinterpret_cast<float4*>(s + kCylOffTop);
+    float4* bot = reinterpret_cast<float4*>(s + kCylOffBot);
+    if (lane < 2 + kCylRing) {
+        f3 g = mul(R, mk(gv[lane]));
+        gv[lane] = make_float4(g.x, g.y, g.z, 0.f);
+    }
+    if (lane < kCylCap) {
+        f3 t = mul(R, mk(top[lane])) + com;
+        f3 b = t - pv->h * pv->axis;
+        top[lane] = make_float4(t.x, t.y, t.z, 0.f);
+        bot[lane] = make_float4(b.x, b.y, b.z, 0.f);
+    }
+    pv->gv = gv;
+    pv->top = top;
+    pv->bot = bot;
+}
+
+// getSphereExtrema (CollisionDetect.cpp:646-655)
+__device__ __forceinline__ Ext sphereExt(const PrimView& s, f3 d) {
+    float cv = dot(d, s.c);
+    return Ext{cv - s.r, cv + s.r, -1, -1};
+}
+
+// Cylinder::getExtremaOfDisk (ConvexPrimitive.cpp:319-355): the point of the
+// disk rim furthest along `target`.  Two FP32 restatements keep the reference's
+// FP64 behaviour: its parallel test |n.t| > 1 - 1e-8 is below FP32 resolution
+// near 1, so it is applied as the equivalent sin(angle) < sqrt(2e-8) on the
+// cross product; and the rim height dw = sqrt(r^2 - r^2 / (1 + g^2)) cancels
+// catastrophically for nearly parallel directions in FP32, so it is evaluated
+// as the equal r g / sqrt(1 + g^2).  (A tilt of 4e-4 rad otherwise moves the
+// extremum's projection by r * 4e-4.)
+__device__ f3 diskExtremum(f3 center, f3 normal, float r, f3 target) {
+    if (mag(cross(normal, target)) < 1.41421356e-4f) return center;
+    float nd = fabsf(dot(normal, target));
+    if (nd < 1e-8f) return center + target * r;
+    f3 u, v;
+    basis(target, &u, &v);
+    f3 w = target;
+    float nu = dot(normal, u), nv = dot(normal, v), nw = dot(normal, w);
+    float dwdu = -nu / nw, dwdv = -nv / nw;
+    float gm = sqrtf(dwdu * dwdu + dwdv * dwdv);
+    float gu = dwdu / gm, gv = dwdv / gm;
+    float root = sqrtf(1.f + gm * gm);
+    float su = r / root;            // sqrt(uv_mag_sqrd)
+    float dw = r * gm / root;       // sqrt(r^2 - uv_mag_sqrd)
+    return center + u * (gu * su) + v * (gv * su) + w * dw;
+}
+
+__device__ __forceinline__ f3 topCenter(const PrimView& c) { return c.c + (0.5f * c.h) * c.axis; }
+__device__ __forceinline__ f3 botCenter(const PrimView& c) { return c.c - (0.5f * c.h) * c.axis; }
+
+// getCylinderExtrema (CollisionDetect.cpp:657-683): extremes of the two caps by
+// symmetry about the centre
+__device__ Ext cylExt(const PrimView& c, f3 d) {
+    f3 tc = topCenter(c);
+    f3 tmax = diskExtremum(tc, c.axis, c.r, d);
+    f3 tmin = 2.f * tc - tmax;
+    f3 bmax = 2.f * c.c - tmin;
+    f3 bmin = 2.f * c.c - tmax;
+    return Ext{fminf(dot(d, tmin), dot(d, bmin)), fmaxf(dot(d, tmax), dot(d, bmax)), -1, -1};
+}
+
+// findCylinderContactArea (CollisionDetect.cpp:354-374).  Returns 0 for a cap
+// face (8-gon, point ids offset + i, surface 16 / 17), 1 for the barrel line
+// (ids 18, 19) and 2 for a single rim point.
+__device__ int cylArea(const PrimView& c, f3 n, f3 u, f3 w, Area* a) {
+    float ad = dot(c.axis, n);
+    if (1.f - fabsf(ad) <= kCosTol) {
+        bool top = dot(n, c.axis) > 0.f;
+        const float4* ring = top ? c.top : c.bot;
+        for (int i = 0; i < kCylCap; i++) {
+            f3 q = mk(ring[i]);
+            a->ps[i] = P2{dot(q, u), dot(q, w)};
+            a->ids[i] = i + (top ? 0 : kCylCap);
+        }
+        a->n = kCylCap;
+        a->surface = top ? 2 * kCylCap : 2 * kCylCap + 1;
+        return 0;
+    }
+    if (fabsf(ad) <= kSinTol) {
+        // cylinderLengthwiseLineInDirection (CollisionDetect.cpp:346-351)
+        f3 barrel = normalize(n - c.axis * dot(c.axis, n));
+        f3 p1 = c.c + barrel * c.r + (0.5f * c.h) * c.axis;
+        f3 p2 = p1 - c.h * c.axis;
+        a->ps[0] = P2{dot(p1, u), dot(p1, w)};
+        a->ps[1] = P2{dot(p2, u), dot(p2, w)};
+        a->ids[0] = 2 * kCylCap + 2;
+        a->ids[1] = 2 * kCylCap + 3;
+        a->n = 2;
+        a->surface = -1;
+        return 1;
+    }
+    bool top = dot(n, c.axis) > 0.f;
+    f3 q = diskExtremum(top ? topCenter(c) : botCenter(c), c.axis, c.r, n);
+    a->ps[0] = P2{dot(q, u), dot(q, w)};
+    a->ids[0] = top ? 2 * kCylCap + 2 : 2 * kCylCap + 3;
+    a->n = 1;
+    a->surface = -1;
+    return 2;
+}
+
+// The FP64 reference skips an axis cross(edge, axis) when its length is below
+// 1e-11, i.e. only for exactly parallel directions; FP32 rounding leaves ~1e-7
+// of noise there, so the skip is relative: sin(angle) below 1e-6.
+__device__ __forceinline__ bool edgeAxis(f3 edge, f3 axis, f3* n) {
+    f3 dir = cross(edge, axis);
+    float m = mag(dir);
+    if (m < 1e-6f * mag(edge) || m == 0.f) return false;
+    *n = dir * (1.f / m);
+    return true;
+}
+
+// Gauss-arc pair test shared by the hull-cylinder and cylinder-cylinder
+// edge axes (same steps as SAT_PolyPoly's)
+__device__ __forceinline__ bool arcAxis(f3 a1, f3 a2, f3 b1, f3 b2, f3* n) {
+    f3 avg = a1 + a2;
+    if (!(dot(avg, b1) + dot(avg, b2) > 0.f)) return false;
+    f3 ap = cross(a1, a2), bp = cross(b1, b2);
+    if (dot(ap, b1) * dot(ap, b2) > 0.f || dot(bp, a1) * dot(bp, a2) > 0.f) return false;
+    f3 x = cross(ap, bp);
+    if (mag2(x) == 0.f) return false;
+    x = normalize(x);
+    if (dot(avg, x) < 0.f) x = x * -1.f;
+    *n = x;
+    return true;
+}
+
+// cylinder Gauss arcs as the constructor builds them (ConvexPrimitive.cpp:
+// 243-244): arc 2i joins Gauss vertex 0 to vertex i, arc 2i+1 vertex 1 to i
+__device__ __forceinline__ void cylArc(const PrimView& c, int k, f3* g1, f3* g2) {
+    *g1 = mk(c.gv[k & 1]);
+    *g2 = mk(c.gv[k >> 1]);
+}
+
+// ManifoldPoint list of one detector call (before the cull)
+struct PrimOut {
+    int m;
+    f3 n;
+    float pen;
+    float4 pts[kMaxClip];
+    unsigned long long magic[kMaxClip];
+};
+
+__device__ void points_from_pool(const CP* pool, int m, f3 u, f3 w, f3 n, float a_dot, float pen, PrimOut* o) {
+    f3 off = n * a_dot;
+    for (int i = 0; i < m; i++) {
+        f3 q = u * pool[i].p.x + w * pool[i].p.y + off;
+        o->pts[i] = make_float4(q.x, q.y, q.z, dot(q, n) - a_dot + pen);
+        o->magic[i] = pool[i].magic;
+    }
+    o->m = m;
+}
+
+// SAT_PolySphere (CollisionDetect.cpp:1336-1411): face, vertex and edge axes of
+// the hull; the contact is the sphere's deepest point, its feature id the
+// winning axis' face (n_points + f), vertex or edge id.
+__device__ bool polySphere(const HullView& A, const PrimView& S, int lane, PrimOut* o) {
+    const HullHeader& H = *A.h;
+    const int nf = H.nf, nv = H.nv, ne = H.ne;
+    const uint8_t* edges = A.g + H.off_edge;
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)};
+    bool sep = false;
+    for (int t = lane; t < nf + nv + ne; t += 32) {
+        Ext ea;
+        f3 n;
+        if (t < nf) {
+            float4 g = A.n[t];
+            if (g.w != 0.f) continue;
+            n = mk(g);
+            float4 c = A.cache[t];
+            float shift = dot(n, A.com);
+            ea = Ext{c.y + shift, c.x + shift, __float_as_int(c.w), __float_as_int(c.z)};
+        } else if (t < nf + nv) {
+            n = normalize(mk(A.v[t - nf]) - S.c);
+            ea = extrema(A.v, nv, n);
+        } else {
+            int e = t - nf - nv;
+            f3 p1 = mk(A.v[edges[2 * e]]), p2 = mk(A.v[edges[2 * e + 1]]);
+            f3 dir = normalize(p2 - p1);
+            f3 sample = p1 - S.c;
+            n = normalize(sample - dir * dot(dir, sample));
+            ea = extrema(A.v, nv, n);
+        }
+        check(ea, sphereExt(S, n), n, t, &best, &sep);
+    }
+    if (__any_sync(0xffffffffu, sep)) return false;
+    Axis b = warp_best(best);
+    if (!(b.pen < INFINITY)) return false;
+    if (lane == 0) {
+        uint32_t feature;
+        if (b.idx < nf) feature = (uint32_t)(nv + b.idx);
+        else if (b.idx < nf + nv) feature = (uint32_t)(b.idx - nf);
+        else {
+            int e = b.idx - nf - nv;
+            feature = edgeId(edges[2 * e], edges[2 * e + 1]);
+        }
+        f3 q = S.c - b.n * S.r;
+        o->n = b.n;
+        o->pen = b.pen;
+        o->pts[0] = make_float4(q.x, q.y, q.z, b.pen);
+        o->magic[0] = feature;
+        o->m = 1;
+    }
+    return true;
+}
+
+// SAT_PolyCylinder (CollisionDetect.cpp:1563-1709): hull faces, the cylinder
+// axis, hull edges x axis, hull vertices radially, Gauss-arc pairs; contact by
+// clipping the hull's feature against the cylinder's cap / barrel line, or the
+// single rim point.
+__device__ bool polyCylinder(const HullView& A, const PrimView& C, int lane, Scratch& scratch, CP* clipped,
+                             int* status, PrimOut* o) {
+    const HullHeader& H = *A.h;
+    const int nf = H.nf, nv = H.nv, ne = H.ne, na = H.na;
+    const uint8_t* edges = A.g + H.off_edge;
+    const int e0 = nf + 1, v0 = e0 + ne, a0 = v0 + nv, total = a0 + na * 2 * kCylRing;
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)};
+    bool sep = false;
+    for (int t = lane; t < total; t += 32) {
+        Ext ea;
+        f3 n;
+        if (t < nf) {
+            float4 g = A.n[t];
+            if (g.w != 0.f) continue;
+            n = mk(g);
+            float4 c = A.cache[t];
+            float shift = dot(n, A.com);
+            ea = Ext{c.y + shift, c.x + shift, __float_as_int(c.w), __float_as_int(c.z)};
+        } else {
+            if (t == nf) n = C.axis;
+            else if (t < v0) {
+                int e = t - e0;
+                if (!edgeAxis(mk(A.v[edges[2 * e + 1]]) - mk(A.v[edges[2 * e]]), C.axis, &n)) continue;
+            } else if (t < a0) {
+                f3 diff = mk(A.v[t - v0]) - C.c;
+                n = normalize(diff - C.axis * dot(C.axis, diff));
+            } else {
+                int k = t - a0, ia = k / (2 * kCylRing), ib = k - ia * (2 * kCylRing);
+                f3 g1, g2;
+                cylArc(C, ib, &g1, &g2);
+                if (!arcAxis(mk(A.n[A.arc[2 * ia]]), mk(A.n[A.arc[2 * ia + 1]]), -g1, -g2, &n)) continue;
+            }
+            ea = extrema(A.v, nv, n);
+        }
+        check(ea, cylExt(C, n), n, t, &best, &sep);
+    }
+    if (__any_sync(0xffffffffu, sep)) return false;
+    Axis b = warp_best(best);
+    if (!(b.pen < INFINITY) || b.aid < 0) return false;
+    if (lane == 0) {
+        f3 n = b.n, u, w;
+        basis(n, &u, &w);
+        Area ac, bc;
+        contactArea(A, n, b.aid, u, w, &ac);
+        int m;
+        if (cylArea(C, -1.f * n, u, w, &bc) == 2) {
+            clipped[0] = CP{bc.ps[0], 0, 0ull, 0};
+            m = 1;
+        } else {
+            m = clipContacts(ac, bc, scratch, clipped, status);
+        }
+        points_from_pool(clipped, m, u, w, n, dot(mk(A.v[b.aid]), n), b.pen, o);
+        o->n = n;
+        o->pen = b.pen;
+    }
+    return true;
+}
+
+// detectSphereSphere (CollisionDetect.cpp:837-866)
+__device__ bool sphereSphere(const PrimView& A, const PrimView& B, PrimOut* o) {
+    f3 diff = B.c - A.c;
+    float pen = A.r + B.r - mag(diff);
+    if (pen < 0.f) return false;
+    f3 n = normalize(diff);
+    f3 q = A.c + n * A.r;
+    o->n = n;
+    o->pen = pen;
+    o->pts[0] = make_float4(q.x, q.y, q.z, pen);
+    o->magic[0] = 0ull;
+    o->m = 1;
+    return true;
+}
+
+// detectSphereCylinder (CollisionDetect.cpp:1712-1792): the cylinder axis, the
+// radial direction and two rim directions.  The reference computes both rim
+// points from the top cap (its "bottom" centre also adds half the height,
+// :1756); that is kept.
+__device__ bool sphereCylinder(const PrimView& S, const PrimView& C, PrimOut* o) {
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)};
+    bool sep = false;
+    f3 ax = C.axis;
+    check(sphereExt(S, ax), cylExt(C, ax), ax, 0, &best, &sep);
+    if (sep) return false;
+    f3 diff = C.c - S.c;
+    f3 barrel = normalize(diff - ax * dot(ax, diff));
+    check(sphereExt(S, barrel), cylExt(C, barrel), barrel, 1, &best, &sep);
+    if (sep) return false;
+    f3 rim_c = C.c + ax * 0.5f * C.h;
+    f3 rim = diskExtremum(rim_c, ax, C.r, -normalize(diff));
+    f3 e = normalize(rim - S.c);
+    check(sphereExt(S, e), cylExt(C, e), e, 2, &best, &sep);
+    if (sep) return false;
+    check(sphereExt(S, e), cylExt(C, e), e, 3, &best, &sep);
+    if (sep || !(best.pen < INFINITY)) return false;
+    f3 q = S.c + best.n * S.r;
+    o->n = best.n;
+    o->pen = best.pen;
+    o->pts[0] = make_float4(q.x, q.y, q.z, best.pen);
+    o->magic[0] = 0ull;
+    o->m = 1;
+    return true;
+}
+
+// checkCylinderEdgeApproxVsBarrel (CollisionDetect.cpp:938-956), one ring edge
+__device__ __forceinline__ bool ringAxis(const float4* ring, int i, f3 barrel_axis, f3* n) {
+    return edgeAxis(mk(ring[(i + 1) % kCylCap]) - mk(ring[i]), barrel_axis, n);
+}
+
+// detectCylinderCylinder (CollisionDetect.cpp:958-1137): both axes, the four cap
+// 8-gons' edges against the other barrel, the barrel-barrel axis, Gauss-arc
+// pairs; then the contact cases (rim point, parallel barrels, clipping).
+__device__ bool cylinderCylinder(const PrimView& A, const PrimView& B, int lane, Scratch& scratch, CP* clipped,
+                                 int* status, PrimOut* o) {
+    const int r0 = 2, bb = r0 + 4 * kCylCap, a0 = bb + 1, total = a0 + 4 * kCylRing * kCylRing;
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)};
+    bool sep = false;
+    for (int t = lane; t < total; t += 32) {
+        f3 n;
+        if (t == 0) n = A.axis;
+        else if (t == 1) n = B.axis;
+        else if (t < bb) {
+            int k = t - r0, ring = k / kCylCap, i = k - ring * kCylCap;
+            const float4* pts = ring == 0 ? A.top : ring == 1 ? A.bot : ring == 2 ? B.top : B.bot;
+            if (!ringAxis(pts, i, ring < 2 ? B.axis : A.axis, &n)) continue;
+        } else if (t == bb) {
+            f3 x = cross(A.axis, B.axis);
+            if (!(mag2(x) > 0.00000001f)) continue;
+            n = normalize(x);
+        } else {
+            int k = t - a0, ia = k / (2 * kCylRing), ib = k - ia * (2 * kCylRing);
+            f3 a1, a2, b1, b2;
+            cylArc(A, ia, &a1, &a2);
+            cylArc(B, ib, &b1, &b2);
+            if (!arcAxis(a1, a2, -b1, -b2, &n)) continue;
+        }
+        check(cylExt(A, n), cylExt(B, n), n, t, &best, &sep);
+    }
+    if (__any_sync(0xffffffffu, sep)) return false;
+    Axis b = warp_best(best);
+    if (!(b.pen < INFINITY)) return false;
+    if (lane == 0) {
+        f3 n = b.n, u, w;
+        basis(n, &u, &w);
+        Area ac, bc;
+        int ka = cylArea(A, n, u, w, &ac);
+        int kb = cylArea(B, -1.f * n, u, w, &bc);
+        int m;
+        if (ka == 2) { clipped[0] = CP{ac.ps[0], 0, 0ull, 0}; m = 1; }
+        else if (kb == 2) { clipped[0] = CP{bc.ps[0], 0, 0ull, 0}; m = 1; }
+        else if (ka == 1 && kb == 1 && fabsf(dot(A.axis, B.axis)) > 0.995f) {
+            // parallel barrels: overlap of the two lines along A's axis
+            f3 ba = normalize(n - A.axis * dot(A.axis, n));
+            f3 a1 = A.c + ba * A.r + (0.5f * A.h) * A.axis, a2 = a1 - A.h * A.axis;
+            f3 bbv = normalize(-1.f * n - B.axis * dot(B.axis, -1.f * n));
+            f3 b1 = B.c + bbv * B.r + (0.5f * B.h) * B.axis, b2 = b1 - B.h * B.axis;
+            if (dot(B.axis, A.axis) < 0.f) { f3 t = b1; b1 = b2; b2 = t; }
+            float amx = dot(a1, A.axis), amn = dot(a2, A.axis), bmx = dot(b1, A.axis), bmn = dot(b2, A.axis);
+            f3 imx = (amx > bmx) ? b1 : a1;
+            f3 imn = (amn > bmn) ? a2 : b2;
+            clipped[0] = CP{P2{dot(u, imx), dot(w, imx)}, 0, 0ull, 0};
+            clipped[1] = CP{P2{dot(u, imn), dot(w, imn)}, 0, 1ull, 0};
+            m = 2;
+        } else {
+            m = clipContacts(ac, bc, scratch, clipped, status);
+        }
+        f3 amax = diskExtremum(dot(A.axis, n) > 0.f ? topCenter(A) : botCenter(A), A.axis, A.r, n);
+        points_from_pool(clipped, m, u, w, n, dot(amax, n), b.pen, o);
+        o->n = n;
+        o->pen = b.pen;
+    }
+    return true;
+}
+
+// detectCollision's primitive dispatch (CollisionDetect.cpp:57-150) for every
+// pair involving a sphere or cylinder.  Pairs the detectors take the other way
+// round are flipped back: normal negated, both MagicID halves swapped.
+__device__ __forceinline__ void narrow_prim(const Dev& d, int p, int a, int b, uint8_t* sa, uint8_t* sb, const uint8_t* ga,
+                                         const uint8_t* gb, uint32_t ka, uint32_t kb, int lane, Scratch& scratch,
+                                         CP* clipped) {
+    HullView hv;
+    PrimView pa, pb;
+    if (ka == SHAPE_HULL) stage_hull(ga, sa, d.pos[a], d.rot[a], &hv, lane);
+    else stage_prim(sa, d.pos[a], d.rot[a], &pa, lane);
+    if (kb == SHAPE_HULL) stage_hull(gb, sb, d.pos[b], d.rot[b], &hv, lane);
+    else stage_prim(sb, d.pos[b], d.rot[b], &pb, lane);
+    __syncwarp();
+    PrimOut o;
+    o.m = 0;
+    bool hit, flip = false;
+    if (ka == SHAPE_HULL) {
+        hit = kb == SHAPE_SPHERE ? polySphere(hv, pb, lane, &o) : polyCylinder(hv, pb, lane, scratch, clipped, d.status, &o);
+    } else if (kb == SHAPE_HULL) {
+        flip = true;
+        hit = ka == SHAPE_SPHERE ? polySphere(hv, pa, lane, &o) : polyCylinder(hv, pa, lane, scratch, clipped, d.status, &o);
+    } else if (ka == SHAPE_SPHERE && kb == SHAPE_SPHERE) {
+        hit = sphereSphere(pa, pb, &o);
+    } else if (ka == SHAPE_SPHERE) {
+        hit = sphereCylinder(pa, pb, &o);
+    } else if (kb == SHAPE_SPHERE) {
+        flip = true;
+        hit = sphereCylinder(pb, pa, &o);
+    } else {
+        hit = cylinderCylinder(pa, pb, lane, scratch, clipped, d.status, &o);
+    }
+    if (lane != 0) return;
+    if (!hit || !(o.pen > 0.f) || o.m == 0) { no_manifold(d, p); return; }
+    if (flip) {
+        o.n = -1.f * o.n;
+        for (int i = 0; i < o.m; i++) {
+            unsigned long long x = o.magic[i];
+            o.magic[i] = (x >> 32) | (x << 32);
+        }
+    }
+    emit_manifold(d, p, o.n, o.pen, o.pts, o.magic, o.m);
+}
+
 }  // namespace
 
 // One warp per candidate pair; `slot_bytes` of shared memory per warp.
@@ -336,13 +849,15 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
     const int n_pairs = *d.n_pairs;
     for (int p = blockIdx.x * warps_per_block + wib; p < n_pairs; p += gridDim.x * warps_per_block) {
         const int a = d.pair_a[p], b = d.pair_b[p];
+        const uint8_t* ga = d.shapes + d.shape[a];
+        const uint8_t* gb = d.shapes + d.shape[b];
+        // pairs with a sphere or cylinder belong to k_narrow_prim
+        if ((reinterpret_cast<const HullHeader*>(ga)->kind | reinterpret_cast<const HullHeader*>(gb)->kind) != SHAPE_HULL) continue;
         // collision filter of PhysicsEngine.cpp:174 (at least one dynamic body)
         if (!(d.movement[a] == 0 || d.movement[b] == 0)) {
             if (lane == 0) { d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f); d.mf_cnt[p] = 0; }
             continue;
         }
-        const uint8_t* ga = d.shapes + d.shape[a];
-        const uint8_t* gb = d.shapes + d.shape[b];
         const uint32_t hot_a = reinterpret_cast<const HullHeader*>(ga)->off_fofs;
         const uint32_t hot_b = reinterpret_cast<const HullHeader*>(gb)->off_fofs;
         uint8_t* sa = slot;
@@ -520,14 +1035,64 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
     }
 }
 
-void prepare_kernels() {
-    cudaFuncSetAttribute(k_narrowphase, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+// One warp per candidate pair that involves a sphere or a cylinder (the other
+// pairs are k_narrowphase's).  Same staging as k_narrowphase.
+__global__ void __launch_bounds__(256) k_narrow_prim(Dev d, int slot_bytes) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int warps_per_block = blockDim.x >> 5;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+    uint8_t* slot = smem + 16 * warps_per_block + (size_t)wib * slot_bytes;
+    if (lane == 0) mbar_init(&bars[wib]);
+    __syncthreads();
+    uint32_t parity = 0;
+    Scratch scratch;
+    CP clipped[kMaxClip];
+    const int n_pairs = *d.n_pairs;
+    for (int p = blockIdx.x * warps_per_block + wib; p < n_pairs; p += gridDim.x * warps_per_block) {
+        const int a = d.pair_a[p], b = d.pair_b[p];
+        const uint8_t* ga = d.shapes + d.shape[a];
+        const uint8_t* gb = d.shapes + d.shape[b];
+        const HullHeader* Ha = reinterpret_cast<const HullHeader*>(ga);
+        const HullHeader* Hb = reinterpret_cast<const HullHeader*>(gb);
+        const uint32_t ka = Ha->kind, kb = Hb->kind;
+        if ((ka | kb) == SHAPE_HULL) continue;
+        if (!(d.movement[a] == 0 || d.movement[b] == 0)) {
+            if (lane == 0) no_manifold(d, p);
+            continue;
+        }
+        const uint32_t hot_a = Ha->off_fofs, hot_b = Hb->off_fofs;
+        uint8_t* sa = slot;
+        uint8_t* sb = slot + ((hot_a + 15u) & ~15u);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) {
+            mbar_expect(&bars[wib], hot_a + hot_b);
+            bulk_load(sa, ga, hot_a, &bars[wib]);
+            bulk_load(sb, gb, hot_b, &bars[wib]);
+        }
+        bool ok = mbar_wait(&bars[wib], parity);
+        parity ^= 1u;
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) { atomicOr(d.status, ST_TIMEOUT); no_manifold(d, p); }
+            mbar_wait(&bars[wib], parity ^ 1u);
+            return;
+        }
+        narrow_prim(d, p, a, b, sa, sb, ga, gb, ka, kb, lane, scratch, clipped);
+    }
 }
 
-void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, cudaStream_t st) {
+void prepare_kernels() {
+    cudaFuncSetAttribute(k_narrowphase, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_narrow_prim, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st) {
     const int warps = 8;
     size_t smem = 16 * warps + (size_t)warps * (slot_bytes + kQueueBytes);
     k_narrowphase<<<n_sms * 4, warps * 32, smem, st>>>(d, slot_bytes);
+    if (prims) k_narrow_prim<<<n_sms * 4, warps * 32, 16 * warps + (size_t)warps * slot_bytes, st>>>(d, slot_bytes);
 }
 
 }  // namespace cpgpu

@@ -21,6 +21,7 @@
 // per body.
 #include "kernels.cuh"
 #include "devmath.cuh"
+#include "shapes.cuh"
 
 namespace cpgpu {
 
@@ -544,15 +545,8 @@ __global__ void k_apply_state(Dev d) {
             store9(d.iw + 9 * i, mul(mul(R, load9(d.iref + 9 * i)), Rc));
             store9(d.iinv + 9 * i, mul(mul(R, load9(d.iinv_ref + 9 * i)), Rc));
         }
-        const uint8_t* blob = d.shapes + d.shape[i];
-        const HullHeader* H = reinterpret_cast<const HullHeader*>(blob);
-        const float4* vv = reinterpret_cast<const float4*>(blob + sizeof(HullHeader));
-        f3 c = mk(p), mn = mk(INFINITY, INFINITY, INFINITY), mx = mk(-INFINITY, -INFINITY, -INFINITY);
-        for (int k = 0; k < H->nv; k++) {
-            f3 x = c + mul(R, mk(vv[k]));
-            mn.x = fminf(mn.x, x.x); mn.y = fminf(mn.y, x.y); mn.z = fminf(mn.z, x.z);
-            mx.x = fmaxf(mx.x, x.x); mx.y = fmaxf(mx.y, x.y); mx.z = fmaxf(mx.z, x.z);
-        }
+        f3 mn, mx;
+        shape_aabb(d.shapes + d.shape[i], mk(p), R, &mn, &mx);
         d.aabb_lo[i] = make_float4(mn.x, mn.y, mn.z, 0.f);
         d.aabb_hi[i] = make_float4(mx.x, mx.y, mx.z, 0.f);
     }

@@ -13,6 +13,10 @@ Workloads:
                  jitter and random orientations, dropped on the static plate;
                  friction 0.5, restitution 0, dt 1/60, 10 PGS iterations, one
                  substep.
+  mixed_drop     mixed bodies (40% boxes with sides U[0.5,1.5] m, 20% spheres
+                 r U[0.3,0.8], 20% cylinders r U[0.3,0.6] h U[0.5,1.5], 20%
+                 random hulls of 12-32 points) on a jittered grid with random
+                 orientations, dropped on the static plate; 20 PGS iterations.
   batched_world  one world of the 4,096-world batch: floor(exp(U[ln 8, ln 512]))
                  bodies, either a box pyramid (base 4-16) or a hull pile built as
                  in hull_drop, each world with its own plate.
@@ -131,6 +135,38 @@ def hull_drop(seed=0, n_side=10, spacing=3.2, jitter=0.1, base_y=2.0):
                 pos = np.array([i * spacing - off, base_y + j * spacing, k * spacing - off])
                 pos += rng.uniform(-jitter, jitter, size=3)
                 bid = sc.hull(pts, faces, PILE_MATERIAL, DYNAMIC, pos)
+                sc.orient(bid, random_quat(rng))
+    return sc
+
+
+MIXED_PARAMS = dict(step_time=1.0 / 60.0, substeps=1, pgs=(20, 1, 1), sleeping=False)
+
+
+def mixed_drop(seed=0, n_side=6, spacing=3.2, jitter=0.1, base_y=2.0, n_layers=None):
+    """Mixed boxes, spheres, cylinders and hulls (n_side^2 x n_layers) dropped
+    on the static plate."""
+    rng = np.random.default_rng(seed)
+    n_layers = n_side if n_layers is None else n_layers
+    sc = Scene(f"mixed_drop_{n_side}x{n_side}x{n_layers}_seed{seed}", MIXED_PARAMS)
+    _plate(sc)
+    off = (n_side - 1) * spacing / 2.0
+    for j in range(n_layers):
+        for i in range(n_side):
+            for k in range(n_side):
+                pos = np.array([i * spacing - off, base_y + j * spacing, k * spacing - off])
+                pos += rng.uniform(-jitter, jitter, size=3)
+                u = rng.random()
+                if u < 0.4:
+                    d = rng.uniform(0.5, 1.5, size=3)
+                    bid = sc.box((-d[0] / 2, -d[1] / 2, -d[2] / 2), d[0], d[1], d[2], PILE_MATERIAL, DYNAMIC, pos)
+                elif u < 0.6:
+                    bid = sc.sphere((0.0, 0.0, 0.0), rng.uniform(0.3, 0.8), PILE_MATERIAL, DYNAMIC, pos)
+                elif u < 0.8:
+                    r, h = rng.uniform(0.3, 0.6), rng.uniform(0.5, 1.5)
+                    bid = sc.cylinder((0.0, -h / 2, 0.0), r, h, PILE_MATERIAL, DYNAMIC, pos)
+                else:
+                    pts, faces = random_hull(rng, 12, 32)
+                    bid = sc.hull(pts, faces, PILE_MATERIAL, DYNAMIC, pos)
                 sc.orient(bid, random_quat(rng))
     return sc
 

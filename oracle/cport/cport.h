@@ -245,6 +245,20 @@ struct Hull {
 };
 Extrema findExtrema(const Hull& h, const V3& axis);
 
+// Sphere (ConvexPrimitive.h:79-109) and cylinder (:160-210) primitives
+struct SphereG { V3 c; double r = 0; };
+struct CylG {
+    V3 c, axis;
+    double r = 0, h = 0;
+    std::vector<V3> gv;                       // Gauss vertices (2 caps + 12 around)
+    std::vector<std::pair<int, int>> arcs;    // 24 arcs, as the constructor builds them
+    std::vector<V3> top, bot;                 // 8-gon approximations of the caps
+    V3 topCenter() const { return c + 0.5 * h * axis; }
+    V3 botCenter() const { return c - 0.5 * h * axis; }
+};
+enum Kind { K_HULL = 0, K_SPHERE = 1, K_CYLINDER = 2 };
+CylG makeCylinder(V3 center, double radius, double height);
+
 // --------------------------------------------------------------- world ----
 enum Movement { DYNAMIC = 0, FIXED = 1, KINEMATIC = 2 };
 
@@ -252,8 +266,11 @@ struct Body {
     uint32_t id = 0;
     int movement = DYNAMIC;
     Material mat;
+    int kind = K_HULL;
     Hull ref_shape;       // COM-centred reference geometry
     Hull shape;           // world geometry (points and Gauss normals follow the pose)
+    SphereG sph_src, sph_ref, sph;
+    CylG cyl_src, cyl_ref, cyl;
     AABB aabb;
     V3 com, vel, ang_vel, pvel, pang_vel, prev_com;
     Q q, prev_q;
@@ -336,6 +353,9 @@ struct World {
     std::vector<std::pair<uint32_t, uint32_t>> last_pairs;
 
     Body* addHull(const std::vector<V3>& pts, const std::vector<std::vector<int>>& faces, const Material& m, int movement, V3 pos);
+    Body* addSphere(V3 center, double r, const Material& m, int movement, V3 pos);
+    Body* addCylinder(V3 base, double r, double h, const Material& m, int movement, V3 pos);
+    Body* finishBody(std::unique_ptr<Body> b, double mass, const V3& com, const M3& tensor);
     void placeBody(Body* b, double mass, const V3& com_geom, const M3& tensor);
     Edge* edgeBetween(Body* a, Body* b);
     Edge* getOrCreateEdge(Body* a, Body* b);
@@ -345,6 +365,12 @@ struct World {
 };
 
 Manifold satPolyPoly(const Hull& a, uint32_t a_id, const Material& am, const Hull& b, uint32_t b_id, const Material& bm);
+Manifold satPolySphere(const Hull& a, uint32_t a_id, const Material& am, const SphereG& b, uint32_t b_id, const Material& bm);
+Manifold satPolyCylinder(const Hull& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm);
+Manifold sphereSphere(const SphereG& a, uint32_t a_id, const Material& am, const SphereG& b, uint32_t b_id, const Material& bm);
+Manifold sphereCylinder(const SphereG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm);
+Manifold cylinderCylinder(const CylG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm);
+Manifold flipped(Manifold m);   // normal negated, MagicID halves swapped (CollisionDetect.cpp:29-40)
 Manifold cullManifold(const Manifold& m, int n);
 void massProperties(const Hull& h, double density, V3* com, M3* tensor, double* mass);
 

@@ -2,6 +2,8 @@
 // contact clipping of the CPU restatement (test infrastructure; see cport.h).
 #include "cport.h"
 
+#include <functional>
+
 namespace cport {
 
 static const double EPS_GAUSS = 0.0000000001;  // ConvexPrimitive.cpp:10
@@ -403,6 +405,354 @@ Manifold satPolyPoly(const Hull& a, uint32_t a_id, const Material& am, const Hul
         mp.magic_b = p.magic;
         out.pts.push_back(mp);
     }
+    out.max_pen = best.pen;
+    return out;
+}
+
+// ---------------------------------------------- spheres and cylinders ----
+// Cylinder::Cylinder (ConvexPrimitive.cpp:222-256) for the default axis (0,1,0),
+// 12 Gauss ring vertices and 8-gon cap approximations.  The arcs are built as
+// the constructor builds them: {0, i} and {1, i} for i in [0, 12).
+CylG makeCylinder(V3 center, double radius, double height) {
+    CylG c;
+    c.c = center; c.axis = V3(0, 1, 0); c.r = radius; c.h = height;
+    M3 rot = M3::iden();
+    c.gv.resize(14);
+    c.gv[0] = rot * V3(0, 1, 0);
+    c.gv[1] = rot * V3(0, -1, 0);
+    double dth = 2 * PI_TRUNC / 12;
+    for (int i = 0; i < 12; i++) {
+        double th = i * dth;
+        c.gv[i + 2] = rot * V3(std::sin(th), 0, std::cos(th));
+    }
+    c.arcs.resize(24);
+    for (int i = 0; i < 12; i++) { c.arcs[2 * i] = {0, i}; c.arcs[2 * i + 1] = {1, i}; }
+    double fth = 2 * PI_TRUNC / 8;
+    double er = radius / std::cos(PI_TRUNC / 8);
+    c.top.resize(8); c.bot.resize(8);
+    for (int i = 0; i < 8; i++) {
+        double th = i * fth;
+        c.top[i] = center + rot * V3(er * std::sin(th), height / 2.0, er * std::cos(th));
+        c.bot[i] = center + rot * V3(er * std::sin(th), -height / 2.0, er * std::cos(th));
+    }
+    return c;
+}
+
+static Extrema sphereExtrema(const SphereG& s, const V3& d) {   // getSphereExtrema (CollisionDetect.cpp:646-655)
+    Extrema e;
+    double cv = d.dot(s.c);
+    e.max_v = cv + s.r;
+    e.min_v = cv - s.r;
+    e.min_id = e.max_id = -1;
+    return e;
+}
+
+// Cylinder::getExtremaOfDisk (ConvexPrimitive.cpp:319-355)
+static V3 diskExtremum(V3 center, V3 normal, double r, V3 target) {
+    if (std::abs(normal.dot(target)) > 0.99999999) return center;
+    if (std::abs(normal.dot(target)) < 0.00000001) return center + target * r;
+    V3 u, v, w;
+    w = target;
+    target.perpBasis(&u, &v);
+    V3 uvw_n(normal.dot(u), normal.dot(v), normal.dot(w));
+    double dwdu = -uvw_n.x / uvw_n.z;
+    double dwdv = -uvw_n.y / uvw_n.z;
+    double gm = std::sqrt(dwdu * dwdu + dwdv * dwdv);
+    double gu = dwdu / gm, gv = dwdv / gm;
+    double uv2 = r * r / (1 + gm * gm);
+    double dw = std::sqrt(r * r - uv2);
+    double du = gu * std::sqrt(uv2), dv = gv * std::sqrt(uv2);
+    return center + u * du + v * dv + w * dw;
+}
+
+static Extrema cylinderExtrema(const CylG& c, const V3& d) {   // getCylinderExtrema (CollisionDetect.cpp:657-683)
+    V3 tc = c.topCenter();
+    V3 tmax = diskExtremum(tc, c.axis, c.r, d);
+    V3 tmin = 2 * tc - tmax;
+    V3 bmax = 2 * c.c - tmin;
+    V3 bmin = 2 * c.c - tmax;
+    double a = d.dot(tmax), b = d.dot(tmin), e = d.dot(bmax), f = d.dot(bmin);
+    Extrema x;
+    x.max_v = std::max<double>(a, e);
+    x.min_v = std::min<double>(b, f);
+    x.min_id = x.max_id = -1;
+    return x;
+}
+
+// apply one candidate axis: returns true when it separates
+static bool axisTest(const Extrema& a, const Extrema& b, const V3& n, NormResult* best) {
+    NormResult x = checkNorm(a, b, n);
+    if (x.pen < 0) return true;
+    if (x.pen < best->pen) *best = x;
+    return false;
+}
+
+static ManifoldPoint mkPoint(const V3& pos, double pen, const Material& am, const Material& bm, uint64_t cid, uint64_t bid) {
+    ManifoldPoint mp;
+    mp.pos = pos;
+    mp.pen = pen;
+    mp.restitution = std::max(am.restitution, bm.restitution);
+    mp.kinetic = (am.kinetic + bm.kinetic) / 2.0;
+    mp.stat = (am.stat + bm.stat) / 2.0;
+    mp.magic_c = cid;
+    mp.magic_b = bid;
+    return mp;
+}
+
+static uint64_t cidOf(uint32_t a, uint32_t b) {
+    return (0x00000000FFFFFFFFull & (uint64_t)a) | (0xFFFFFFFF00000000ull & ((uint64_t)b << 32));
+}
+
+Manifold flipped(Manifold m) {
+    m.normal = -m.normal;
+    for (ManifoldPoint& p : m.pts) {
+        uint64_t c1 = p.magic_c & 0xFFFFFFFFull, c2 = p.magic_c >> 32, b1 = p.magic_b & 0xFFFFFFFFull, b2 = p.magic_b >> 32;
+        p.magic_c = c2 | (c1 << 32);
+        p.magic_b = b2 | (b1 << 32);
+    }
+    return m;
+}
+
+// detectSphereSphere (CollisionDetect.cpp:837-866)
+Manifold sphereSphere(const SphereG& a, uint32_t a_id, const Material& am, const SphereG& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    V3 diff = b.c - a.c;
+    double dist = diff.mag();
+    out.max_pen = a.r + b.r - dist;
+    if (out.max_pen < 0) return out;
+    out.normal = diff.normalize();
+    out.pts.push_back(mkPoint(a.c + out.normal * a.r, out.max_pen, am, bm, cidOf(a_id, b_id), 0));
+    return out;
+}
+
+// SAT_PolySphere (CollisionDetect.cpp:1336-1411): face, vertex and edge axes
+Manifold satPolySphere(const Hull& a, uint32_t a_id, const Material& am, const SphereG& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    out.max_pen = -1;
+    NormResult best = {-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    uint32_t feature = 0;
+    uint32_t surf = (uint32_t)a.pts.size();
+    for (size_t f = 0; f < a.gv.size(); f++, surf++) {
+        if (a.g_redundant[f]) continue;
+        Extrema ea = recenter(a.g_cache[f], a.g_ref_val[f], a.gv[f].dot(a.pts[a.g_ref_idx[f]]));
+        double before = best.pen;
+        if (axisTest(ea, sphereExtrema(b, a.gv[f]), a.gv[f], &best)) { out.max_pen = -1; return out; }
+        if (best.pen < before) feature = surf;
+    }
+    for (int p = 0; p < (int)a.pts.size(); p++) {
+        V3 n = (a.pts[p] - b.c).normalize();
+        double before = best.pen;
+        if (axisTest(findExtrema(a, n), sphereExtrema(b, n), n, &best)) { out.max_pen = -1; return out; }
+        if (best.pen < before) feature = (uint32_t)p;
+    }
+    for (auto& e : a.edges) {
+        V3 dir = (a.pts[e.second] - a.pts[e.first]).normalize();
+        V3 sample = a.pts[e.first] - b.c;
+        V3 n = (sample - dir * dir.dot(sample)).normalize();
+        double before = best.pen;
+        if (axisTest(findExtrema(a, n), sphereExtrema(b, n), n, &best)) { out.max_pen = -1; return out; }
+        if (best.pen < before) feature = edgeId(e.first, e.second);
+    }
+    out.normal = best.n;
+    out.pts.push_back(mkPoint(b.c - out.normal * b.r, best.pen, am, bm, cidOf(a_id, b_id), feature));
+    out.max_pen = best.pen;
+    return out;
+}
+
+// findCylinderContactArea (CollisionDetect.cpp:354-374) and the barrel line
+// of cylinderLengthwiseLineInDirection (:346-351)
+static void lengthwiseLine(const CylG& c, V3 n, V3* p1, V3* p2) {
+    V3 barrel = (n - c.axis * c.axis.dot(n)).normalize();
+    *p1 = c.c + barrel * c.r + 0.5 * c.h * c.axis;
+    *p2 = *p1 - c.h * c.axis;
+}
+enum CylArea { CA_FACE, CA_EDGE, CA_BARREL };
+static Area cylinderArea(const CylG& c, V3 n, V3 u, V3 w, CylArea* kind) {
+    Area a;
+    double ad = c.axis.dot(n);
+    if (1 - std::abs(ad) <= cosTol() && n.dot(c.axis) > 0) {
+        for (int i = 0; i < 8; i++) { a.ps.push_back(p2(c.top[i].dot(u), c.top[i].dot(w))); a.ids.push_back(i); }
+        a.surface = 16; a.origin = FACE; *kind = CA_FACE;
+        return a;
+    }
+    if (1 - std::abs(ad) <= cosTol()) {
+        for (int i = 0; i < 8; i++) { a.ps.push_back(p2(c.bot[i].dot(u), c.bot[i].dot(w))); a.ids.push_back(i + 8); }
+        a.surface = 17; a.origin = FACE; *kind = CA_FACE;
+        return a;
+    }
+    if (std::abs(ad) <= sinTol()) {
+        V3 l1, l2;
+        lengthwiseLine(c, n, &l1, &l2);
+        a.ps = {p2(l1.dot(u), l1.dot(w)), p2(l2.dot(u), l2.dot(w))};
+        a.ids = {18, 19};
+        a.surface = -1; a.origin = EDGE; *kind = CA_BARREL;
+        return a;
+    }
+    V3 p = n.dot(c.axis) > 0 ? diskExtremum(c.topCenter(), c.axis, c.r, n) : diskExtremum(c.botCenter(), c.axis, c.r, n);
+    a.ps = {p2(p.dot(u), p.dot(w))};
+    a.ids = {n.dot(c.axis) > 0 ? 18 : 19};
+    a.surface = -1; a.origin = EDGE; *kind = CA_EDGE;
+    return a;
+}
+
+static bool arcAxes(const std::vector<V3>& ag, const std::vector<std::pair<int, int>>& aarcs, const std::vector<V3>& bg,
+                    const std::vector<std::pair<int, int>>& barcs, const std::function<Extrema(const V3&)>& ea,
+                    const std::function<Extrema(const V3&)>& eb, NormResult* best) {
+    for (auto& arc1 : aarcs) {
+        for (auto& arc2 : barcs) {
+            V3 a1 = ag[arc1.first], a2 = ag[arc1.second];
+            V3 b1 = -bg[arc2.first], b2 = -bg[arc2.second];
+            V3 avg = a1 + a2;
+            if (avg.dot(b1) + avg.dot(b2) <= 0) continue;
+            V3 ap = a1.cross(a2), bp = b1.cross(b2);
+            if (ap.dot(b1) * ap.dot(b2) > 0 || bp.dot(a1) * bp.dot(a2) > 0) continue;
+            V3 n = ap.cross(bp);
+            if (n.mag2() == 0) continue;
+            n = n.normalize();
+            if (avg.dot(n) < 0) n *= -1;
+            if (axisTest(ea(n), eb(n), n, best)) return true;
+        }
+    }
+    return false;
+}
+
+static Manifold pointsFromPool(const std::vector<ClipP>& pool, V3 u, V3 w, V3 n, double a_dot, double a_pen,
+                               const Material& am, const Material& bm, uint64_t cid) {
+    Manifold out;
+    V3 off = n * a_dot;
+    for (const ClipP& p : pool) {
+        V3 pos = u * p.pos.x + w * p.pos.y + off;
+        out.pts.push_back(mkPoint(pos, pos.dot(n) - a_dot + a_pen, am, bm, cid, p.magic));
+    }
+    return out;
+}
+
+// SAT_PolyCylinder (CollisionDetect.cpp:1563-1709)
+Manifold satPolyCylinder(const Hull& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    out.max_pen = -1;
+    NormResult best = {-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    for (size_t f = 0; f < a.gv.size(); f++) {
+        if (a.g_redundant[f]) continue;
+        Extrema ea = recenter(a.g_cache[f], a.g_ref_val[f], a.gv[f].dot(a.pts[a.g_ref_idx[f]]));
+        if (axisTest(ea, cylinderExtrema(b, a.gv[f]), a.gv[f], &best)) return out;
+    }
+    V3 ax = b.axis;
+    if (axisTest(findExtrema(a, ax), cylinderExtrema(b, ax), ax, &best)) return out;
+    for (auto& e : a.edges) {
+        V3 ed = a.pts[e.second] - a.pts[e.first];
+        V3 dir = ed.cross(ax);
+        if (dir.mag() < 0.00000000001) continue;
+        V3 dn = dir.normalize();
+        if (axisTest(findExtrema(a, dn), cylinderExtrema(b, dn), dn, &best)) return out;
+    }
+    for (const V3& p : a.pts) {
+        V3 diff = p - b.c;
+        V3 n = (diff - ax * ax.dot(diff)).normalize();
+        if (axisTest(findExtrema(a, n), cylinderExtrema(b, n), n, &best)) return out;
+    }
+    if (arcAxes(a.gv, a.arcs, b.gv, b.arcs, [&](const V3& n) { return findExtrema(a, n); },
+                [&](const V3& n) { return cylinderExtrema(b, n); }, &best))
+        return out;
+    V3 n = best.n;
+    V3 amax = a.pts[best.a_id];
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    Area ac = contactArea(a, n, amax, best.a_id, u, w);
+    CylArea bk;
+    Area bc = cylinderArea(b, -n, u, w, &bk);
+    std::vector<ClipP> pool;
+    if (bk == CA_EDGE) pool = {ClipP{bc.ps[0], 0, 0x0, false}};
+    else pool = clipContacts(ac, bc);
+    out = pointsFromPool(pool, u, w, n, amax.dot(n), best.pen, am, bm, cidOf(a_id, b_id));
+    out.normal = n;
+    out.max_pen = best.pen;
+    return out;
+}
+
+// detectSphereCylinder (CollisionDetect.cpp:1712-1792).  The fourth axis uses
+// the same disk as the third: the reference computes its "bottom" disk centre
+// with +0.5 h along the axis (:1756), and that is reproduced here.
+Manifold sphereCylinder(const SphereG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    out.max_pen = -1;
+    NormResult best = {-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    V3 ax = b.axis;
+    if (axisTest(sphereExtrema(a, ax), cylinderExtrema(b, ax), ax, &best)) return out;
+    V3 diff = b.c - a.c;
+    V3 barrel = (diff - ax * ax.dot(diff)).normalize();
+    if (axisTest(sphereExtrema(a, barrel), cylinderExtrema(b, barrel), barrel, &best)) return out;
+    V3 top = b.c + ax * 0.5 * b.h;
+    V3 tp = diskExtremum(top, ax, b.r, -diff.normalize());
+    V3 e1 = (tp - a.c).normalize();
+    if (axisTest(sphereExtrema(a, e1), cylinderExtrema(b, e1), e1, &best)) return out;
+    V3 bot = b.c + ax * 0.5 * b.h;
+    V3 bp = diskExtremum(bot, ax, b.r, -diff.normalize());
+    V3 e2 = (bp - a.c).normalize();
+    if (axisTest(sphereExtrema(a, e2), cylinderExtrema(b, e2), e2, &best)) return out;
+    out.normal = best.n;
+    out.pts.push_back(mkPoint(a.c + out.normal * a.r, best.pen, am, bm, cidOf(a_id, b_id), 0));
+    out.max_pen = best.pen;
+    return out;
+}
+
+// checkCylinderEdgeApproxVsBarrel (CollisionDetect.cpp:938-956)
+static bool edgeApproxVsBarrel(const CylG& a, const CylG& b, V3 barrel_axis, const std::vector<V3>& ring, NormResult* best) {
+    int n = (int)ring.size();
+    for (int i = 0; i < n; i++) {
+        V3 ed = ring[(i + 1) % n] - ring[i];
+        V3 dir = ed.cross(barrel_axis);
+        if (dir.mag() < 0.00000000001) continue;
+        V3 dn = dir.normalize();
+        if (axisTest(cylinderExtrema(a, dn), cylinderExtrema(b, dn), dn, best)) return true;
+    }
+    return false;
+}
+
+// detectCylinderCylinder (CollisionDetect.cpp:958-1137)
+Manifold cylinderCylinder(const CylG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    out.max_pen = -1;
+    NormResult best = {-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    V3 aa = a.axis, ba = b.axis;
+    if (axisTest(cylinderExtrema(a, aa), cylinderExtrema(b, aa), aa, &best)) return out;
+    if (axisTest(cylinderExtrema(a, ba), cylinderExtrema(b, ba), ba, &best)) return out;
+    if (edgeApproxVsBarrel(a, b, ba, a.top, &best)) return out;
+    if (edgeApproxVsBarrel(a, b, ba, a.bot, &best)) return out;
+    if (edgeApproxVsBarrel(a, b, aa, b.top, &best)) return out;
+    if (edgeApproxVsBarrel(a, b, aa, b.bot, &best)) return out;
+    V3 bb = aa.cross(ba);
+    if (bb.mag2() > 0.00000001) {
+        bb = bb.normalize();
+        if (axisTest(cylinderExtrema(a, bb), cylinderExtrema(b, bb), bb, &best)) return out;
+    }
+    if (arcAxes(a.gv, a.arcs, b.gv, b.arcs, [&](const V3& n) { return cylinderExtrema(a, n); },
+                [&](const V3& n) { return cylinderExtrema(b, n); }, &best))
+        return out;
+    V3 n = best.n;
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    CylArea ak, bk;
+    Area ac = cylinderArea(a, n, u, w, &ak);
+    Area bc = cylinderArea(b, -n, u, w, &bk);
+    std::vector<ClipP> pool;
+    if (ak == CA_EDGE) pool = {ClipP{ac.ps[0], 0, 0x0, false}};
+    else if (bk == CA_EDGE) pool = {ClipP{bc.ps[0], 0, 0x0, false}};
+    else if (ak == CA_BARREL && bk == CA_BARREL && std::abs(aa.dot(ba)) > 0.995) {
+        V3 a1, a2, b1, b2;
+        lengthwiseLine(a, n, &a1, &a2);
+        lengthwiseLine(b, -n, &b1, &b2);
+        if (ba.dot(aa) < 0) std::swap(b1, b2);
+        double amx = a1.dot(aa), amn = a2.dot(aa), bmx = b1.dot(aa), bmn = b2.dot(aa);
+        V3 imx = (amx > bmx) ? b1 : a1;
+        V3 imn = (amn > bmn) ? a2 : b2;
+        pool = {ClipP{p2(u.dot(imx), w.dot(imx)), 0, 0x0, false}, ClipP{p2(u.dot(imn), w.dot(imn)), 0, 0x1, false}};
+    } else {
+        pool = clipContacts(ac, bc);
+    }
+    V3 amax = aa.dot(n) > 0 ? diskExtremum(a.topCenter(), aa, a.r, n) : diskExtremum(a.botCenter(), aa, a.r, n);
+    out = pointsFromPool(pool, u, w, n, amax.dot(n), best.pen, am, bm, cidOf(a_id, b_id));
+    out.normal = n;
     out.max_pen = best.pen;
     return out;
 }

@@ -23,10 +23,51 @@ static AABB genAABB(const Hull& h) {
     return a;
 }
 
-// RigidBody::updateGeometry (RigidBody.cpp:281-312) for a single polyhedron
+// Sphere::gen_AABB (ConvexPrimitive.cpp:439-443)
+static AABB genAABB(const SphereG& s) {
+    return AABB{s.c - V3(s.r, s.r, s.r), s.c + V3(s.r, s.r, s.r)};
+}
+
+// Cylinder::gen_AABB (ConvexPrimitive.cpp:289-298): the two cap 8-gons,
+// interleaved top/bottom as the reference collects them
+static AABB genAABB(const CylG& c) {
+    const double inf = std::numeric_limits<double>::infinity();
+    AABB a{V3(inf, inf, inf), V3(-inf, -inf, -inf)};
+    for (size_t i = 0; i < c.top.size(); i++) {
+        for (const V3& p : {c.top[i], c.bot[i]}) {
+            a.mn.x = std::min<double>(a.mn.x, p.x); a.mn.y = std::min<double>(a.mn.y, p.y); a.mn.z = std::min<double>(a.mn.z, p.z);
+            a.mx.x = std::max<double>(a.mx.x, p.x); a.mx.y = std::max<double>(a.mx.y, p.y); a.mx.z = std::max<double>(a.mx.z, p.z);
+        }
+    }
+    return a;
+}
+
+// Cylinder::recomputeFromReference (ConvexPrimitive.cpp:272-287): the bottom
+// cap is re-derived from the top one
+static void cylFromReference(CylG& out, const CylG& ref, const M3& rot, const V3& trans) {
+    out.c = rot * ref.c + trans;
+    out.axis = rot * ref.axis;
+    for (size_t i = 0; i < out.gv.size(); i++) out.gv[i] = rot * ref.gv[i];
+    for (size_t i = 0; i < out.top.size(); i++) {
+        out.top[i] = rot * ref.top[i] + trans;
+        out.bot[i] = out.top[i] - out.h * out.axis;
+    }
+}
+
+// RigidBody::updateGeometry (RigidBody.cpp:281-312) for a single primitive
 void Body::updateGeometry() {
     q = q.normalize();
     M3 rot = q.rotMatrix();
+    if (kind == K_SPHERE) {
+        sph.c = com + rot * sph_ref.c;            // Sphere::recomputeFromReference (ConvexPrimitive.cpp:433-437)
+        aabb = genAABB(sph);
+        return;
+    }
+    if (kind == K_CYLINDER) {
+        cylFromReference(cyl, cyl_ref, rot, com);
+        aabb = genAABB(cyl);
+        return;
+    }
     for (size_t i = 0; i < shape.pts.size(); i++) shape.pts[i] = com + rot * ref_shape.pts[i];
     shape.interior = com + rot * ref_shape.interior;
     for (size_t i = 0; i < shape.gv.size(); i++) shape.gv[i] = rot * ref_shape.gv[i];
@@ -97,6 +138,89 @@ Body* World::addHull(const std::vector<V3>& pts, const std::vector<std::vector<i
     return raw;
 }
 
+// recenterTensor (RigidBody.cpp:406-425): parallel-axis shift of an inertia
+// tensor to a new centre of rotation
+static M3 recenterTensor(double mass, const M3& t, V3 new_c, V3 old_origin, V3 true_com) {
+    M3 o = t;
+    V3 d = new_c - old_origin;
+    V3 c = true_com - old_origin;
+    o.m[0][0] += mass * (d.y * d.y + d.z * d.z - 2 * d.y * c.y - 2 * d.z * c.z);
+    o.m[0][1] += mass * (d.x * c.y + d.y * c.x - d.x * d.y);
+    o.m[0][2] += mass * (d.x * c.z + d.z * c.x - d.x * d.z);
+    o.m[1][1] += mass * (d.x * d.x + d.z * d.z - 2 * d.x * c.x - 2 * d.z * c.z);
+    o.m[1][2] += mass * (d.y * c.z + d.z * c.y - d.y * d.z);
+    o.m[2][2] += mass * (d.x * d.x + d.y * d.y - 2 * d.x * c.x - 2 * d.y * c.y);
+    o.m[1][0] = o.m[0][1];
+    o.m[2][0] = o.m[0][2];
+    o.m[2][1] = o.m[1][2];
+    return o;
+}
+
+// calculateMassProperties (RigidBody.cpp:427-640), SPHERE and CYLINDER cases
+// for a body of one primitive with the default height axis
+static void primitiveMass(const Body& b, double* mass, V3* com, M3* tensor) {
+    double m;
+    V3 c;
+    M3 local;
+    if (b.kind == K_SPHERE) {
+        double r = b.sph_src.r;
+        m = (4.0 / 3.0) * PI_TRUNC * r * r * r * b.mat.density;
+        c = b.sph_src.c;
+        double k = 2.0 / 5.0 * m * r * r;
+        local = k * M3::iden();
+    } else {
+        double h = b.cyl_src.h, r = b.cyl_src.r;
+        m = PI_TRUNC * r * r * h * b.mat.density;
+        c = b.cyl_src.c;
+        local.m[0][0] = m * (h * h / 12 + r * r / 4);
+        local.m[1][1] = m * r * r / 2;
+        local.m[2][2] = local.m[0][0];
+    }
+    M3 t = M3() + recenterTensor(m, local, V3(0, 0, 0), c, c);
+    V3 csum = V3(0, 0, 0) + m * c;
+    double msum = 0 + m;
+    *com = csum / msum;
+    *mass = msum;
+    *tensor = recenterTensor(msum, t, *com, V3(0, 0, 0), *com);
+}
+
+Body* World::addSphere(V3 center, double r, const Material& m, int movement, V3 pos) {
+    auto b = std::make_unique<Body>();
+    b->kind = K_SPHERE;
+    b->movement = movement;
+    b->mat = m;
+    b->sph_src.c = center;
+    b->sph_src.r = r;
+    b->create_pos = pos;
+    double mass; V3 com; M3 tensor;
+    primitiveMass(*b, &mass, &com, &tensor);
+    return finishBody(std::move(b), mass, com, tensor);
+}
+
+// ConvexUnionGeometry::cylinder (Geometry.cpp:47-49): the base point is the
+// centre of the bottom cap
+Body* World::addCylinder(V3 base, double r, double h, const Material& m, int movement, V3 pos) {
+    auto b = std::make_unique<Body>();
+    b->kind = K_CYLINDER;
+    b->movement = movement;
+    b->mat = m;
+    b->cyl_src = makeCylinder(base + V3(0, h / 2.0, 0), r, h);
+    b->create_pos = pos;
+    double mass; V3 com; M3 tensor;
+    primitiveMass(*b, &mass, &com, &tensor);
+    return finishBody(std::move(b), mass, com, tensor);
+}
+
+Body* World::finishBody(std::unique_ptr<Body> b, double mass, const V3& com, const M3& tensor) {
+    b->id = (uint32_t)bodies.size() + 1;
+    Body* raw = b.get();
+    bodies.push_back(std::move(b));
+    placeBody(raw, mass, com, tensor);
+    nodes[raw->id] = raw;
+    adj[raw];
+    return raw;
+}
+
 // The part of the RigidBody constructor that follows the mass properties
 // (RigidBody.cpp:19-36): recentre the reference geometry on the COM, track the
 // geometry origin and move it to the creation position.
@@ -108,14 +232,26 @@ void World::placeBody(Body* b, double mass, const V3& com_geom, const M3& tensor
     b->tensor = b->ref_tensor;
     b->inv_tensor = b->ref_inv_tensor;
     b->q = Q();
-    b->ref_shape = b->src_shape;
     M3 I = M3::iden();
     V3 mc = -b->com;
-    for (V3& p : b->ref_shape.pts) p = mc + I * p;
-    b->ref_shape.interior = mc + I * b->ref_shape.interior;
-    for (V3& g : b->ref_shape.gv) g = I * g;
-    b->shape = b->src_shape;
-    b->aabb = genAABB(b->shape);
+    if (b->kind == K_SPHERE) {
+        b->sph_ref = b->sph_src;
+        b->sph_ref.c = mc + I * b->sph_src.c;
+        b->sph = b->sph_src;
+        b->aabb = genAABB(b->sph);
+    } else if (b->kind == K_CYLINDER) {
+        b->cyl_ref = b->cyl_src;
+        cylFromReference(b->cyl_ref, b->cyl_src, I, mc);
+        b->cyl = b->cyl_src;
+        b->aabb = genAABB(b->cyl);
+    } else {
+        b->ref_shape = b->src_shape;
+        for (V3& p : b->ref_shape.pts) p = mc + I * p;
+        b->ref_shape.interior = mc + I * b->ref_shape.interior;
+        for (V3& g : b->ref_shape.gv) g = I * g;
+        b->shape = b->src_shape;
+        b->aabb = genAABB(b->shape);
+    }
     b->local_origin = -b->com;
     b->track_p.assign(1, b->local_origin + V3(0, 0, 0));
     V3 t = b->create_pos - b->trackedP(0);
@@ -347,6 +483,28 @@ static void pgsSolve(std::vector<RowRef>& rows, int n_vel, int n_pos) {
     }
 }
 
+// detectCollision (CollisionDetect.cpp:57-150): primitive-type dispatch; the
+// pairs the detectors take the other way round are flipped back so that the
+// normal points away from b1
+static Manifold collide(const Body* b1, const Body* b2) {
+    int k1 = b1->kind, k2 = b2->kind;
+    uint32_t i1 = b1->id, i2 = b2->id;
+    const Material &m1 = b1->mat, &m2 = b2->mat;
+    if (k1 == K_HULL) {
+        if (k2 == K_HULL) return satPolyPoly(b1->shape, i1, m1, b2->shape, i2, m2);
+        if (k2 == K_SPHERE) return satPolySphere(b1->shape, i1, m1, b2->sph, i2, m2);
+        return satPolyCylinder(b1->shape, i1, m1, b2->cyl, i2, m2);
+    }
+    if (k1 == K_SPHERE) {
+        if (k2 == K_HULL) return flipped(satPolySphere(b2->shape, i2, m2, b1->sph, i1, m1));
+        if (k2 == K_SPHERE) return sphereSphere(b1->sph, i1, m1, b2->sph, i2, m2);
+        return sphereCylinder(b1->sph, i1, m1, b2->cyl, i2, m2);
+    }
+    if (k2 == K_HULL) return flipped(satPolyCylinder(b2->shape, i2, m2, b1->cyl, i1, m1));
+    if (k2 == K_SPHERE) return flipped(sphereCylinder(b2->sph, i2, m2, b1->cyl, i1, m1));
+    return cylinderCylinder(b1->cyl, i1, m1, b2->cyl, i2, m2);
+}
+
 // -------------------------------------------------------------- step ----
 void World::step() {
     // gravity once per step (PhysicsEngine.cpp:65-87)
@@ -364,7 +522,7 @@ void World::step() {
         Body* b1 = bodies[pr.first - 1].get();
         Body* b2 = bodies[pr.second - 1].get();
         if (!(b1->movement == DYNAMIC || b2->movement == DYNAMIC)) continue;
-        Manifold man = satPolyPoly(b1->shape, b1->id, b1->mat, b2->shape, b2->id, b2->mat);
+        Manifold man = collide(b1, b2);
         if (!(man.max_pen > 0)) continue;
         Manifold m = cullManifold(man, 4);
         getOrCreateEdge(b1, b2);
@@ -513,11 +671,21 @@ int cport_body_box(cpgpu_world* w, const double c[3], double dx, double dy, doub
     if (out_id) *out_id = b->id;
     return CPGPU_OK;
 }
-int cport_body_sphere(cpgpu_world*, const double*, double, const cpgpu_material*, int, const double*, uint32_t*) {
-    return fail("spheres are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+// ConvexUnionGeometry::sphere (Geometry.cpp:39-41)
+int cport_body_sphere(cpgpu_world* w, const double center[3], double radius, const cpgpu_material* m, int movement,
+                      const double pos[3], uint32_t* out_id) {
+    if (!(radius > 0)) return fail("sphere radius must be > 0");
+    Body* b = W(w)->addSphere(v3(center), radius, mat(m), movement, v3(pos));
+    if (out_id) *out_id = b->id;
+    return CPGPU_OK;
 }
-int cport_body_cylinder(cpgpu_world*, const double*, double, double, const cpgpu_material*, int, const double*, uint32_t*) {
-    return fail("cylinders are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+// ConvexUnionGeometry::cylinder (Geometry.cpp:47-49)
+int cport_body_cylinder(cpgpu_world* w, const double base[3], double radius, double height, const cpgpu_material* m,
+                        int movement, const double pos[3], uint32_t* out_id) {
+    if (!(radius > 0) || !(height > 0)) return fail("cylinder radius and height must be > 0");
+    Body* b = W(w)->addCylinder(v3(base), radius, height, mat(m), movement, v3(pos));
+    if (out_id) *out_id = b->id;
+    return CPGPU_OK;
 }
 int cport_body_mesh(cpgpu_world*, const double*, int, const int*, int, const cpgpu_material*, int, uint32_t*) {
     return fail("static meshes are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);

@@ -16,7 +16,43 @@ import oracle  # noqa: E402
 from constraintphysics_gb300 import scenes  # noqa: E402
 
 
+def mass_properties(world, n):
+    """The reference's mass, centre of mass (geometry frame) and inertia tensor
+    of bodies 1..n."""
+    import ctypes
+    g = oracle.ref_abi()._lib.cpref_get_mass_properties
+    g.restype = ctypes.c_int
+    g.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    mass, com, tensor = np.zeros(n), np.zeros((n, 3)), np.zeros((n, 9))
+    for i in range(n):
+        m = np.zeros(1)
+        c = np.zeros(3)
+        t = np.zeros(9)
+        assert g(world.h, i + 1, m.ctypes.data, c.ctypes.data, t.ctypes.data) == 0
+        mass[i], com[i], tensor[i] = m[0], c, t
+    return mass, com, tensor
+
+
+def mixed():
+    """Boxes, spheres, cylinders and hulls (scenes.mixed_drop, 4x4x2, seed 1)
+    after 150 reference steps, with the reference's mass properties so the
+    restatement can start from the same bodies without the reference."""
+    steps = 150
+    sc = scenes.mixed_drop(seed=1, n_side=4, n_layers=2)
+    w = oracle.ref_world()
+    scenes.apply(sc, w)
+    mass, com, tensor = mass_properties(w, sc.n_bodies)
+    w.step(steps)
+    st = w.state()
+    c = w.contacts()
+    np.savez_compressed(os.path.join(HERE, "mixed_drop_4x4x2_seed1.npz"), steps=steps, mass=mass, com_geom=com,
+                        tensor=tensor, com=st["com"], quat=st["quat"], vel=st["vel"], ang_vel=st["ang_vel"],
+                        magic_b=c["magic_b"], b1=c["b1"], b2=c["b2"], normal_impulse=c["normal_impulse"],
+                        pen_depth=c["pen_depth"])
+
+
 def main():
+    mixed()
     steps = 120
     w = oracle.ref_world()
     scenes.apply(scenes.hull_drop(seed=1, n_side=3), w)

@@ -40,6 +40,28 @@ def test_restatement_bitwise_on_batched_worlds(oracle_mod):
         assert len(r.contacts()["b1"]) == len(p.contacts()["b1"])
 
 
+def test_restatement_bitwise_on_mixed_drop(oracle_mod):
+    # boxes, spheres, cylinders and hulls: every primitive pair kind occurs
+    sc = scenes.mixed_drop(seed=2, n_side=4, n_layers=3)
+    kinds = [op[0] for op in sc.ops if op[0] in ("hull", "box", "sphere", "cylinder")]
+    r, p = oracle_mod.twin_worlds(sc)
+    seen = set()
+    for s in range(200):
+        r.step(1)
+        p.step(1)
+        c = r.contacts()
+        for a, b in zip(c["b1"].tolist(), c["b2"].tolist()):
+            seen.add(tuple(sorted((kinds[a - 1].replace("box", "hull"), kinds[b - 1].replace("box", "hull")))))
+        if s % 25 == 24:
+            assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
+            assert np.array_equal(r.pairs(), p.pairs()), f"pair set differs at step {s}"
+    cr, cp = r.contacts(), p.contacts()
+    for k in ("b1", "b2", "magic_b", "live", "memory_life", "normal_impulse", "friction_impulse", "pen_depth"):
+        assert np.array_equal(cr[k], cp[k]), k
+    assert {("cylinder", "hull"), ("hull", "sphere"), ("cylinder", "cylinder"), ("cylinder", "sphere"),
+            ("sphere", "sphere")} <= seen, seen
+
+
 def test_mass_properties_agree(oracle_mod):
     sc = scenes.hull_drop(seed=4, n_side=2)
     r, p = oracle_mod.ref_world(), oracle_mod.port_world()
@@ -135,3 +157,34 @@ def test_golden_fixture(oracle_mod):
     c = p.contacts()
     assert np.array_equal(c["magic_b"], g["magic_b"])
     assert np.allclose(c["normal_impulse"], g["normal_impulse"], rtol=0, atol=1e-9)
+
+
+def test_golden_fixture_mixed(oracle_mod):
+    """Spheres, cylinders, boxes and hulls: the restatement, started from the
+    reference's mass properties stored in the fixture, reproduces the
+    reference's state and contacts after 150 steps (no reference library
+    needed)."""
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "mixed_drop_4x4x2_seed1.npz")
+    g = np.load(path)
+    sc = scenes.mixed_drop(seed=1, n_side=4, n_layers=2)
+    p = oracle_mod.port_world()
+    scenes.apply(sc, p)
+    put = oracle_mod.port_abi()._lib.cport_body_set_mass_properties
+    put.restype = ctypes.c_int
+    put.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+    for i in range(sc.n_bodies):
+        c = np.ascontiguousarray(g["com_geom"][i])
+        t = np.ascontiguousarray(g["tensor"][i])
+        assert put(p.h, i + 1, float(g["mass"][i]), c.ctypes.data, t.ctypes.data) == 0
+    # orientations set by the scene after creation: replay them on the moved bodies
+    for op in sc.ops:
+        if op[0] == "orient":
+            p.set_orientation(op[1], op[2])
+    p.step(int(g["steps"]))
+    st = p.state()
+    for k in ("com", "quat", "vel", "ang_vel"):
+        assert np.array_equal(st[k], g[k]), k
+    c = p.contacts()
+    assert np.array_equal(c["magic_b"], g["magic_b"])
+    assert np.array_equal(c["normal_impulse"], g["normal_impulse"])
