@@ -17,6 +17,12 @@ Workloads:
                  r U[0.3,0.8], 20% cylinders r U[0.3,0.6] h U[0.5,1.5], 20%
                  random hulls of 12-32 points) on a jittered grid with random
                  orientations, dropped on the static plate; 20 PGS iterations.
+  chain_world    one articulated chain: L unit boxes (L in [lmin, lmax]) with
+                 link masses log-uniform in [0.1, 100] kg, pinned to a fixed box
+                 by a ball-socket and joined alternately by ball-sockets and
+                 hinges with random axes, starting horizontal and swinging
+                 through fixed spheres (r U[0.5,1.5]) placed in its swing
+                 volume; engine defaults (8 substeps, PGS (4,1,1)).
   batched_world  one world of the 4,096-world batch: floor(exp(U[ln 8, ln 512]))
                  bodies, either a box pyramid (base 4-16) or a hull pile built as
                  in hull_drop, each world with its own plate.
@@ -86,6 +92,16 @@ class Scene:
     def cylinder(self, base, r, h, material, movement, pos=(0, 0, 0)):
         return self._body(("cylinder", tuple(base), r, h, material, movement, tuple(pos)))
 
+    def mass(self, bid, m):
+        self.ops.append(("mass", bid, float(m)))
+
+    def ball_socket(self, b1, b2, a1, a2, strength=15000.0):
+        self.ops.append(("ball", b1, b2, tuple(a1), tuple(a2), float(strength)))
+
+    def hinge(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
+        self.ops.append(("hinge", b1, b2, tuple(a1), tuple(a2), tuple(ax1), tuple(ax2), float(pos_strength),
+                         float(rot_strength)))
+
     def orient(self, bid, q):
         self.ops.append(("orient", bid, tuple(q)))
 
@@ -111,6 +127,12 @@ def apply(scene, world):
             world.set_orientation(op[1], op[2])
         elif kind == "vel":
             world.set_velocity(op[1], op[2])
+        elif kind == "mass":
+            world.set_mass(op[1], op[2])
+        elif kind == "ball":
+            world.add_ball_socket(op[1], op[2], op[3], op[4], op[5])
+        elif kind == "hinge":
+            world.add_hinge(op[1], op[2], op[3], op[4], op[5], op[6], op[7], op[8])
         else:
             raise ValueError(kind)
     return ids
@@ -168,6 +190,70 @@ def mixed_drop(seed=0, n_side=6, spacing=3.2, jitter=0.1, base_y=2.0, n_layers=N
                     pts, faces = random_hull(rng, 12, 32)
                     bid = sc.hull(pts, faces, PILE_MATERIAL, DYNAMIC, pos)
                 sc.orient(bid, random_quat(rng))
+    return sc
+
+
+CHAIN_PARAMS = dict(step_time=1.0 / 60.0, substeps=8, pgs=(4, 1, 1), sleeping=False)
+
+
+def chain_world(rng, lmin=16, lmax=64, n_spheres=50, pitch=1.1):
+    """One articulated chain (see the module docstring)."""
+    n = int(rng.integers(lmin, lmax + 1))
+    sc = Scene(f"chain_{n}", CHAIN_PARAMS)
+    anchor = sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, PILE_MATERIAL, FIXED)
+    links = []
+    for i in range(n):
+        b = sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, PILE_MATERIAL, DYNAMIC, ((i + 1) * pitch, 0.0, 0.0))
+        sc.mass(b, float(math.exp(rng.uniform(math.log(0.1), math.log(100.0)))))
+        links.append(b)
+    prev = anchor
+    for i, b in enumerate(links):
+        # the joint sits halfway between the two bodies' centres; anchors are
+        # given in each body's own model coordinates
+        x = (i + 0.5) * pitch
+        a_prev = (x - (i * pitch if i > 0 else 0.0), 0.0, 0.0)
+        a_this = (x - (i + 1) * pitch, 0.0, 0.0)
+        if i % 2 == 0:
+            sc.ball_socket(prev, b, a_prev, a_this)
+        else:
+            axis = unit_sphere_points(rng, 1)[0]
+            sc.hinge(prev, b, a_prev, a_this, tuple(axis), tuple(axis))
+        prev = b
+    reach = (n + 1) * pitch
+    placed = 0
+    while placed < n_spheres:
+        r = rng.uniform(0.5, 1.5)
+        c = np.array([rng.uniform(-reach, reach), rng.uniform(-reach, -1.0), rng.uniform(-2.0, 2.0)])
+        if c[1] + r > -0.8:   # clear of the chain's starting line
+            continue
+        sc.sphere(tuple(c), r, PILE_MATERIAL, FIXED)
+        placed += 1
+    return sc
+
+
+def heavy_chain():
+    """The reference's "High mass Ratio Chain" scenario
+    (Demo/src/Demos/Tests/HolonomicBlockSolvingTests.h:8-91): 35 links of
+    0.31 x 1 x 0.31 (density 2) hanging from a fixed box by ball-sockets, a
+    radius-7 ball (density 2) on the end moving at 25 m/s; 24 substeps, PGS
+    (1, 1, 1).  The reference requires the ball to stay within 65 m of the
+    fixture for 30 s.  Sleeping is disabled here (the reference scenario leaves
+    it on; a swinging chain does not sleep)."""
+    sc = Scene("heavy_chain", dict(step_time=1.0 / 60.0, substeps=24, pgs=(1, 1, 1), sleeping=False))
+    default = {"density": 1.0, "restitution": 0.3, "kinetic_friction": 0.6, "static_friction": 1.1}
+    heavy = dict(default, density=2.0)
+    w, h = 0.31, 1.0
+    anchor = sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, default, FIXED)
+    prev = anchor
+    for i in range(35):
+        pos = (0.0, -i * h, 0.0)
+        link = sc.box((-w / 2.0, -i * h, -w / 2.0), w, -h, w, heavy, DYNAMIC)
+        sc.ball_socket(prev, link, pos, pos)
+        prev = link
+    final = (0.0, -35 * h, 0.0)
+    ball = sc.sphere((0.0, -35 * h - 7.0, 0.0), 7.0, heavy, DYNAMIC)
+    sc.velocity(ball, (25.0, 0.0, 0.0))
+    sc.ball_socket(ball, prev, final, final)
     return sc
 
 

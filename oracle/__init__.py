@@ -105,7 +105,7 @@ def twin_worlds(scene):
             def both(*a, **k):
                 out = fr(*a, **k)
                 fp(*a, **k)
-                if name.startswith("add_"):
+                if name in ("add_hull", "add_box", "add_sphere", "add_cylinder"):
                     m = np.zeros(1); c = np.zeros(3); t = np.zeros(9)
                     assert get(r.h, out, m.ctypes.data, c.ctypes.data, t.ctypes.data) == 0
                     assert put(p.h, out, float(m[0]), c.ctypes.data, t.ctypes.data) == 0
@@ -117,3 +117,62 @@ def twin_worlds(scene):
 
     sc_mod.apply(scene, _Twin())
     return r, p
+
+
+_CREATE = ("add_hull", "add_box", "add_sphere", "add_cylinder")
+
+
+class _Hooked:
+    """Forwards world calls; runs `after(body_id)` right after each body is
+    created (before any later operation of the scene touches it)."""
+
+    def __init__(self, world, after):
+        self._w, self._after = world, after
+
+    def __getattr__(self, name):
+        f = getattr(self._w, name)
+
+        def call(*a, **k):
+            out = f(*a, **k)
+            if name in _CREATE:
+                self._after(out)
+            return out
+        return call
+
+
+def capture_mass_properties(scene):
+    """The reference's mass properties of every body of `scene`, read right
+    after the body is created (mass, centre of mass in the geometry frame,
+    3x3 tensor), with the reference world the scene was applied to."""
+    import numpy as np
+    from constraintphysics_gb300 import scenes as sc_mod
+    get, _ = _mass_hooks()
+    r = ref_world()
+    r.set_params(**scene.params)
+    rows = []
+
+    def after(bid):
+        m, c, t = np.zeros(1), np.zeros(3), np.zeros(9)
+        assert get(r.h, bid, m.ctypes.data, c.ctypes.data, t.ctypes.data) == 0
+        rows.append((m[0], c, t))
+    sc_mod.apply(scene, _Hooked(r, after))
+    mass = np.array([x[0] for x in rows])
+    return mass, np.array([x[1] for x in rows]), np.array([x[2] for x in rows]), r
+
+
+def port_world_with_mass(scene, mass, com, tensor):
+    """The restatement built from `scene`, each body's mass properties replaced
+    by the given ones right after it is created."""
+    import numpy as np
+    from constraintphysics_gb300 import scenes as sc_mod
+    _, put = _mass_hooks()
+    p = port_world()
+    p.set_params(**scene.params)
+
+    def after(bid):
+        i = bid - 1
+        c = np.ascontiguousarray(com[i], dtype=np.float64)
+        t = np.ascontiguousarray(tensor[i], dtype=np.float64)
+        assert put(p.h, bid, float(mass[i]), c.ctypes.data, t.ctypes.data) == 0
+    sc_mod.apply(scene, _Hooked(p, after))
+    return p

@@ -20,6 +20,8 @@
 #include <vector>
 #include <memory>
 #include <unordered_map>
+#include <set>
+#include <functional>
 
 namespace cport {
 
@@ -277,6 +279,7 @@ struct Body {
     double mass = 0;
     M3 tensor, inv_tensor, ref_tensor, ref_inv_tensor;
     std::vector<V3> track_p;
+    std::set<const Body*> no_collide;   // no_collision_set (RigidBody.h), filled by joints
     V3 local_origin;
     Hull src_shape;       // geometry as given at creation (geometry frame)
     V3 create_pos;
@@ -290,7 +293,59 @@ struct Body {
     void rotateWithGyro(double dt, int n_itr, bool gyro_disabled);
 };
 
-struct DV { Vec<6> v, pv; };
+struct DV { Vec<6> v, pv, lin_err; };   // VelPair (ConstraintSolver.cpp:83-89)
+
+// A joint row: DegreedConstraint<n> (ConstraintSolver.h:60-144) for n = 3
+// (BallSocketConstraint) or 5 (HingeConstraint), stored at the largest size
+// with every loop bounded by n, in the reference's accumulation order.
+constexpr int kMaxDof = 5;
+struct JRow {
+    int n = 3;
+    Body* a = nullptr; Body* b = nullptr;
+    DV* da = nullptr; DV* db = nullptr;
+    bool in_holo = false;
+    double impulse[kMaxDof] = {}, pimpulse[kMaxDof] = {}, holo[kMaxDof] = {};
+    double target[kMaxDof] = {}, ptarget[kMaxDof] = {};
+    double ja[kMaxDof][6] = {}, jb[kMaxDof][6] = {};
+    double ita[6][kMaxDof] = {}, itb[6][kMaxDof] = {};
+    double itv[kMaxDof][kMaxDof] = {}, minv[kMaxDof][kMaxDof] = {};
+};
+
+struct Edge;
+struct Params;
+// BallSocket / Hinge (PersistentConstraint.h:118-313)
+struct Joint {
+    int n = 3;                    // 3 ball-socket, 5 hinge
+    Body* b1 = nullptr; Body* b2 = nullptr;
+    int k1 = 0, k2 = 0;           // tracked point keys
+    V3 ax1, ax2;                  // hinge axes in body space (normalised)
+    double pos_hard = 15000, rot_hard = 15000;
+    JRow row;
+    V3 u, w;                      // HingeConstraint::u / w of the last rebuild
+    Edge* edge = nullptr;
+    void rebuild(const Params& p, double dt_sub, bool in_holo);
+};
+
+// HolonomicSystem (HolonomicBlockSolver.cpp:11-132): constraint order chosen
+// by minimum fill, block-sparse LDL^T of J M^-1 J^T
+struct HoloSys {
+    std::vector<Edge*> member_edges;
+    bool changed = false;
+    std::vector<JRow*> cons;      // elimination order
+    int degree = 0;
+    std::vector<int> table;       // block_location_table
+    std::vector<int> vpos;        // vector_location_lookup
+    std::vector<double> buf;      // blocks, then the diagonal-element scratch
+    int cap = 0, dcap = 0;
+    void build(const std::vector<JRow*>& og);
+    int loc(int row, int col) const;
+    int firstBelow(int col) const;
+    int dloc(int row, int col) const;
+    void computeInverse(double cfm);
+    void solve(std::vector<double>& v) const;
+    void computeAndApply(bool pseudo, double lin_err_threshold);
+    double inverseError(double cfm) const;
+};
 
 // one solver row of the reference's DegreedConstraint<n> (ConstraintSolver.h:60-144)
 template <int N>
@@ -321,11 +376,17 @@ struct Contact {
 
 struct Edge {
     Body* n1; Body* n2;                       // n1 = node the edge was created from
+    // SharedConstraintsEdge::constraints: joints are listed before contacts
+    // (a joint forbids contacts between its bodies from then on)
+    std::vector<Joint*> joints;
     std::vector<std::unique_ptr<Contact>> contacts;
+    HoloSys* h = nullptr;                     // holonomic system of the edge
+    bool scan_needed = false;                 // holonomic_system_scan_needed
     Body* other(Body* x) const { return x == n1 ? n2 : n1; }
 };
 
-struct RowRef { int kind; Contact* c; };    // kind 0 = normal row, 1 = friction row
+// kind 0 = normal row, 1 = friction row (of contact c), 2 = joint row (j)
+struct RowRef { int kind; Contact* c; Joint* j = nullptr; };
 
 struct Params {
     double dt = 1.0 / 90;
@@ -338,6 +399,7 @@ struct Params {
     bool gyro_disabled = false;
     bool warm_start_disabled = false;
     bool sleeping = true;
+    double lin_err_threshold = 15;   // excessive_linear_error_torque_threshold (PhysicsEngine.h:217)
     double cutoff_vel = 0;   // set by setStep_time / setGravity (PhysicsEngine.cpp:1142-1145,1214-1217)
 };
 
@@ -351,6 +413,8 @@ struct World {
     std::unordered_map<Body*, std::vector<Edge*>> adj;        // node -> edges sorted by other id
     std::vector<std::unique_ptr<Edge>> edges;
     std::vector<std::pair<uint32_t, uint32_t>> last_pairs;
+    std::vector<std::unique_ptr<Joint>> joints;
+    std::vector<std::unique_ptr<HoloSys>> systems;
 
     Body* addHull(const std::vector<V3>& pts, const std::vector<std::vector<int>>& faces, const Material& m, int movement, V3 pos);
     Body* addSphere(V3 center, double r, const Material& m, int movement, V3 pos);
@@ -361,8 +425,17 @@ struct World {
     Edge* getOrCreateEdge(Body* a, Body* b);
     void deleteEdge(Edge* e);
     void addContact(Body* b1, Body* b2, const ManifoldPoint& mp, const V3& n);
+    Joint* addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, double pos_hard, double rot_hard);
+    void maintainHolonomicSystems();
+    void holonomicScan(Edge* e);
+    void updateHolonomicInverses();
     void step();
 };
+
+void jrowTarget(JRow& r);
+void jrowWarm(JRow& r);
+void jrowStep(JRow& r, bool pseudo);
+void jrowApply(const JRow& r, const double* imp, Vec<6>* va, Vec<6>* vb);
 
 Manifold satPolyPoly(const Hull& a, uint32_t a_id, const Material& am, const Hull& b, uint32_t b_id, const Material& bm);
 Manifold satPolySphere(const Hull& a, uint32_t a_id, const Material& am, const SphereG& b, uint32_t b_id, const Material& bm);

@@ -1,0 +1,595 @@
+// joints.cpp — ball-socket and hinge rows and the holonomic block solver of the
+// CPU restatement (test infrastructure; see cport.h).
+#include "cport.h"
+
+namespace cport {
+
+// ------------------------------------------------------------- rows ----
+// rowMajorOrderInverse<n> for n >= 4 (Math/src/NMat.h:124-149): Gauss-Jordan
+// elimination without pivoting
+static void gaussJordan(int n, const double* src, double* dst) {
+    double c[kMaxDof * kMaxDof * 2];
+    for (int i = 0; i < n * n; i++) c[i] = src[i];
+    for (int i = 0; i < n * n; i++) dst[i] = 0;
+    for (int i = 0; i < n; i++) dst[i * (n + 1)] = 1.0;
+    for (int piv = 0; piv < n; piv++)
+        for (int r = 0; r < n; r++) {
+            if (piv == r) continue;
+            double ratio = c[n * r + piv] / c[n * piv + piv];
+            for (int k = 0; k < n; k++) {
+                c[n * r + k] -= ratio * c[n * piv + k];
+                dst[n * r + k] -= ratio * dst[n * piv + k];
+            }
+        }
+    for (int piv = 0; piv < n; piv++)
+        for (int k = 0; k < n; k++) dst[n * piv + k] /= c[n * piv + piv];
+}
+
+// rowMajorOrderInverse<n> (NMat.cpp:5-34 for n <= 3), in place allowed
+static void invertBlock(int n, double* m) {
+    double out[kMaxDof * kMaxDof];
+    if (n == 1) { out[0] = 1.0 / m[0]; }
+    else if (n == 2) {
+        double a = m[0], b = m[1], c = m[2], d = m[3];
+        double di = 1.0 / (a * d - b * c);
+        out[0] = d * di; out[1] = -b * di; out[2] = -c * di; out[3] = a * di;
+    } else if (n == 3) {
+        double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5], g = m[6], h = m[7], i = m[8];
+        double di = 1.0 / (a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g));
+        out[0] = (e * i - f * h) * di; out[1] = (c * h - b * i) * di; out[2] = (b * f - c * e) * di;
+        out[3] = (f * g - d * i) * di; out[4] = (a * i - c * g) * di; out[5] = (c * d - a * f) * di;
+        out[6] = (d * h - e * g) * di; out[7] = (b * g - a * h) * di; out[8] = (a * e - b * d) * di;
+    } else {
+        gaussJordan(n, m, out);
+    }
+    for (int k = 0; k < n * n; k++) m[k] = out[k];
+}
+
+static void crossMatInto(const V3& v, double m[3][3]) {   // crossMat (NMat.cpp:59-67)
+    m[0][0] = 0; m[0][1] = -v.z; m[0][2] = v.y;
+    m[1][0] = v.z; m[1][1] = 0; m[1][2] = -v.x;
+    m[2][0] = -v.y; m[2][1] = v.x; m[2][2] = 0;
+}
+
+// impulse_to_{a,b}_velocity = invMass(body) * J^T, impulse_to_value and its
+// CFM-regularised inverse (ConstraintSolver.cpp:255-258 pattern)
+static void finishRow(JRow& r, double cfm) {
+    const int n = r.n;
+    for (int side = 0; side < 2; side++) {
+        const Body* body = side == 0 ? r.a : r.b;
+        double (*j)[6] = side == 0 ? r.ja : r.jb;
+        double (*it)[kMaxDof] = side == 0 ? r.ita : r.itb;
+        double im[6][6] = {};
+        double m = body->invMass();
+        M3 t = body->invTensor();
+        for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) { im[i][k] = (i == k ? 1.0 : 0.0) * m; im[3 + i][3 + k] = t.m[i][k]; }
+        for (int i = 0; i < 6; i++)
+            for (int c = 0; c < n; c++) {
+                it[i][c] = 0;
+                for (int k = 0; k < 6; k++) it[i][c] += im[i][k] * j[c][k];
+            }
+    }
+    for (int i = 0; i < n; i++)
+        for (int c = 0; c < n; c++) {
+            double pa = 0, pb = 0;
+            for (int k = 0; k < 6; k++) pa += r.ja[i][k] * r.ita[k][c];
+            for (int k = 0; k < 6; k++) pb += r.jb[i][k] * r.itb[k][c];
+            r.itv[i][c] = pa + pb;
+        }
+    double m[kMaxDof * kMaxDof];
+    for (int i = 0; i < n; i++) for (int c = 0; c < n; c++) m[i * n + c] = r.itv[i][c];
+    for (int i = 0; i < n; i++) m[i * n + i] *= (1 + cfm);   // applyCFM (ConstraintSolver.cpp:919-926)
+    invertBlock(n, m);
+    for (int i = 0; i < n; i++) for (int c = 0; c < n; c++) r.minv[i][c] = m[i * n + c];
+}
+
+// BallSocket::updateSolverConstraints (PersistentConstraint.cpp:225-231) with
+// the BallSocketConstraint constructor (ConstraintSolver.cpp:382-405), and
+// Hinge::updateSolverConstraints (:274-285) with HingeConstraint
+// (ConstraintSolver.cpp:468-550).  The hinge's rB is taken from body 1's
+// anchor point, as the reference's constructor does.
+void Joint::rebuild(const Params& p, double dts, bool in_holo) {
+    V3 pa = b1->trackedP(k1), pb = b2->trackedP(k2);
+    double warm[kMaxDof] = {};
+    for (int i = 0; i < n; i++) warm[i] = p.warm_start_disabled ? 0.0 : 1.0 * row.impulse[i];
+    double pos_c = std::min<double>(pos_hard * dts, 1.0 / dts);
+    JRow r;
+    r.n = n; r.a = b1; r.b = b2; r.in_holo = in_holo;
+    for (int i = 0; i < n; i++) r.impulse[i] = warm[i];
+    V3 rA = pa - b1->com;
+    double sa[3][3], sb[3][3];
+    crossMatInto(rA, sa);
+    if (n == 3) {
+        V3 rB = pb - b2->com;
+        crossMatInto(rB, sb);
+        for (int i = 0; i < 3; i++) {
+            for (int k = 0; k < 3; k++) {
+                r.ja[i][k] = (i == k) ? 1.0 : 0.0;
+                r.ja[i][3 + k] = -sa[i][k];
+                r.jb[i][k] = -((i == k) ? 1.0 : 0.0);
+                r.jb[i][3 + k] = sb[i][k];
+            }
+        }
+        V3 err = pb - pa;
+        r.ptarget[0] = pos_c * err.x; r.ptarget[1] = pos_c * err.y; r.ptarget[2] = pos_c * err.z;
+    } else {
+        V3 rB = pa - b2->com;
+        crossMatInto(rB, sb);
+        V3 h1 = b1->q.rotate(ax1), h2 = b2->q.rotate(ax2);
+        double rot_c = std::min<double>(rot_hard * dts, 1.0 / dts);
+        V3 uu, ww;
+        h1.perpBasis(&uu, &ww);
+        V3 nn = h2;
+        r.impulse[3] = uu.dot(u) * warm[3] + uu.dot(w) * warm[4];
+        r.impulse[4] = ww.dot(u) * warm[3] + ww.dot(w) * warm[4];
+        for (int i = 0; i < 3; i++) {
+            for (int k = 0; k < 3; k++) {
+                r.ja[i][k] = (i == k) ? 1.0 : 0.0;
+                r.ja[i][3 + k] = -sa[i][k];
+                r.jb[i][k] = -((i == k) ? 1.0 : 0.0);
+                r.jb[i][3 + k] = sb[i][k];
+            }
+        }
+        double us[3][3], ws[3][3], ns[3][3];
+        crossMatInto(uu, us); crossMatInto(ww, ws); crossMatInto(nn, ns);
+        const double ud[3] = {uu.x, uu.y, uu.z}, wd[3] = {ww.x, ww.y, ww.z}, nd[3] = {nn.x, nn.y, nn.z};
+        for (int k = 0; k < 3; k++) {
+            double a3 = 0, b3 = 0, a4 = 0, b4 = 0;
+            for (int q = 0; q < 3; q++) {
+                a3 += nd[q] * us[q][k];
+                b3 += ud[q] * ns[q][k];
+                a4 += nd[q] * ws[q][k];
+                b4 += wd[q] * ns[q][k];
+            }
+            r.ja[3][k] = 0; r.jb[3][k] = 0; r.ja[4][k] = 0; r.jb[4][k] = 0;
+            r.ja[3][3 + k] = a3; r.jb[3][3 + k] = b3;
+            r.ja[4][3 + k] = a4; r.jb[4][3 + k] = b4;
+        }
+        V3 pc = (pb - pa) * pos_c;
+        r.ptarget[0] = pc.x; r.ptarget[1] = pc.y; r.ptarget[2] = pc.z;
+        r.ptarget[3] = uu.dot(nn) * rot_c;
+        r.ptarget[4] = ww.dot(nn) * rot_c;
+        u = uu;
+        w = ww;
+    }
+    finishRow(r, p.cfm);
+    row = r;
+}
+
+// J_a v_a + J_b v_b (NMat * NVec, then NVec + NVec)
+static void jrowValue(const JRow& r, const Vec<6>& va, const Vec<6>& vb, double* out) {
+    for (int i = 0; i < r.n; i++) {
+        double x = 0, y = 0;
+        for (int k = 0; k < 6; k++) x += va.v[k] * r.ja[i][k];
+        for (int k = 0; k < 6; k++) y += vb.v[k] * r.jb[i][k];
+        out[i] = x + y;
+    }
+}
+
+// computeAndApplyVelocityChange (ConstraintSolver.h:72-75)
+void jrowApply(const JRow& r, const double* imp, Vec<6>* va, Vec<6>* vb) {
+    for (int k = 0; k < 6; k++) {
+        double x = 0;
+        for (int i = 0; i < r.n; i++) x += imp[i] * r.ita[k][i];
+        va->v[k] += x;
+    }
+    for (int k = 0; k < 6; k++) {
+        double x = 0;
+        for (int i = 0; i < r.n; i++) x += imp[i] * r.itb[k][i];
+        vb->v[k] += x;
+    }
+}
+
+static bool isZero(const double* x, int n) {
+    for (int i = 0; i < n; i++) if (std::abs(x[i]) > 0.00000001) return false;
+    return true;
+}
+
+// DegreedConstraint::findTargetConstraintValue (ConstraintSolver.h:79)
+void jrowTarget(JRow& r) {
+    Vec<6> va, vb;
+    V3 v = r.a->getVel(), w = r.a->getAngVel();
+    va.v[0] = v.x; va.v[1] = v.y; va.v[2] = v.z; va.v[3] = w.x; va.v[4] = w.y; va.v[5] = w.z;
+    v = r.b->getVel(); w = r.b->getAngVel();
+    vb.v[0] = v.x; vb.v[1] = v.y; vb.v[2] = v.z; vb.v[3] = w.x; vb.v[4] = w.y; vb.v[5] = w.z;
+    double cur[kMaxDof];
+    jrowValue(r, va, vb, cur);
+    for (int i = 0; i < r.n; i++) r.target[i] = -cur[i];
+}
+
+void jrowWarm(JRow& r) {
+    if (!isZero(r.impulse, r.n)) jrowApply(r, r.impulse, &r.da->v, &r.db->v);
+}
+
+// PGSConstraintStep<n> (ConstraintSolver.cpp:12-40) for an equality row
+void jrowStep(JRow& r, bool pseudo) {
+    Vec<6>* va = pseudo ? &r.da->pv : &r.da->v;
+    Vec<6>* vb = pseudo ? &r.db->pv : &r.db->v;
+    double* acc = pseudo ? r.pimpulse : r.impulse;
+    const double* tgt = pseudo ? r.ptarget : r.target;
+    double cur[kMaxDof], delta[kMaxDof], diff[kMaxDof];
+    jrowValue(r, *va, *vb, cur);
+    for (int i = 0; i < r.n; i++) delta[i] = tgt[i] - cur[i];
+    for (int i = 0; i < r.n; i++) {
+        double x = 0;
+        for (int k = 0; k < r.n; k++) x += delta[k] * r.minv[i][k];
+        diff[i] = (acc[i] + x) - acc[i];
+    }
+    if (!isZero(diff, r.n)) {
+        jrowApply(r, diff, va, vb);
+        for (int i = 0; i < r.n; i++) acc[i] += diff[i];
+    }
+}
+
+// ------------------------------------------------- holonomic system ----
+static const int kEmpty = -1;
+
+void HoloSys::build(const std::vector<JRow*>& og) {
+    cons.clear(); table.clear(); vpos.clear(); buf.clear();
+    degree = 0; cap = 0;
+    const int n = (int)og.size();
+    if (n == 0) return;
+    std::vector<char> edge((size_t)n * n, 0), empty((size_t)n * n, 1);
+    auto E = [&](int i, int j) -> char& { return edge[(size_t)i + (size_t)j * n]; };
+    auto shares = [](const JRow* x, const JRow* y) { return x->a == y->a || x->a == y->b || x->b == y->a || x->b == y->b; };
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) {
+            if (shares(og[i], og[j])) {
+                empty[(size_t)i * n + j] = 0; empty[(size_t)j * n + i] = 0;
+                E(i, j) = 1; E(j, i) = 1;
+            }
+        }
+    std::vector<int> remaining(n);
+    for (int i = 0; i < n; i++) remaining[i] = i;
+    std::vector<int> order;
+    while (!remaining.empty()) {
+        int best_i = -1, best_count = std::numeric_limits<int>::max();
+        std::vector<int> best_nb;
+        for (int i = 0; i < (int)remaining.size(); i++) {
+            std::vector<int> nb;
+            for (int j = 0; j < n; j++)
+                if (j != remaining[i] && E(remaining[i], j)) nb.push_back(j);
+            int unconnected = 0;
+            for (size_t a = 0; a < nb.size(); a++)
+                for (size_t b = a + 1; b < nb.size(); b++)
+                    if (!E(nb[a], nb[b])) unconnected++;
+            if (unconnected < best_count) {
+                best_count = unconnected;
+                best_i = i;
+                best_nb = nb;
+                if (unconnected == 0) break;
+            }
+        }
+        int x = remaining[best_i];
+        order.push_back(x);
+        remaining.erase(remaining.begin() + best_i);
+        for (int j = 0; j < n; j++) { E(x, j) = 0; E(j, x) = 0; }
+        for (size_t a = 0; a < best_nb.size(); a++)
+            for (size_t b = a + 1; b < best_nb.size(); b++) {
+                int p = best_nb[a], q = best_nb[b];
+                empty[(size_t)p * n + q] = 0; empty[(size_t)q * n + p] = 0;
+                E(p, q) = 1; E(q, p) = 1;
+            }
+    }
+    for (int x : order) cons.push_back(og[x]);
+    for (int col = 0; col < n; col++) {
+        vpos.push_back(degree);
+        degree += cons[col]->n;
+        for (int row = col; row < n; row++) {
+            if (empty[(size_t)order[row] * n + order[col]]) table.push_back(kEmpty);
+            else { table.push_back(cap); cap += cons[row]->n * cons[col]->n; }
+        }
+    }
+    dcap = 6 * degree;
+    buf.assign((size_t)cap + dcap, 0.0);
+}
+
+int HoloSys::loc(int row, int col) const {   // getBlockBufferLocation (:584-595)
+    int n = (int)cons.size();
+    return table[row - col + ((2 * n + 1) * col - col * col) / 2];
+}
+int HoloSys::firstBelow(int col) const {
+    for (int r = col + 1; r < (int)cons.size(); r++) { int l = loc(r, col); if (l != kEmpty) return l; }
+    return kEmpty;
+}
+int HoloSys::dloc(int row, int col) const {
+    int l = loc(row, col);
+    if (l == kEmpty) return kEmpty;
+    return l - firstBelow(col);
+}
+
+static double dotN(int n, const double* a, const double* b) {
+    double o = 0;
+    for (int i = 0; i < n; i++) o += a[i] * b[i];
+    return o;
+}
+
+// computeBlockInitialValue (HolonomicBlockSolver.cpp:731-760): the diagonal
+// block is impulse_to_value with CFM; an off-diagonal block couples through
+// the first shared body in the order (a,a), (a,b), (b,a), (b,b)
+static void initialBlock(double* t, const JRow* c1, const JRow* c2, double cfm) {
+    if (c1 == c2) {
+        int n = c1->n;
+        for (int i = 0; i < n; i++) for (int j = 0; j < n; j++) t[i * n + j] = c1->itv[i][j];
+        for (int i = 0; i < n; i++) t[i + n * i] *= (1 + cfm);
+        return;
+    }
+    const double (*j)[6] = nullptr;
+    const double (*it)[kMaxDof] = nullptr;
+    if (c1->a == c2->a) { j = c1->ja; it = c2->ita; }
+    else if (c1->a == c2->b) { j = c1->ja; it = c2->itb; }
+    else if (c1->b == c2->a) { j = c1->jb; it = c2->ita; }
+    else if (c1->b == c2->b) { j = c1->jb; it = c2->itb; }
+    for (int i = 0; i < c1->n * c2->n; i++) {
+        int r = i / c2->n, c = i % c2->n;
+        t[i] = 0;
+        if (j) for (int k = 0; k < 6; k++) t[i] += j[r][k] * it[k][c];
+    }
+}
+
+// HolonomicSystem::computeInverse (HolonomicBlockSolver.cpp:427-543): block
+// LDL^T with the diagonal blocks inverted in place and L = A D^-1
+void HoloSys::computeInverse(double cfm) {
+    const int n = (int)cons.size();
+    double* B = buf.data();
+    double* Dg = buf.data() + cap;
+    for (int col = 0; col < n; col++)
+        for (int row = col; row < n; row++) {
+            int l = loc(row, col);
+            if (l == kEmpty) continue;
+            initialBlock(B + l, cons[row], cons[col], cfm);
+        }
+    for (int col = 0; col < n; col++) {
+        double* diag = B + loc(col, col);
+        const int w = cons[col]->n;
+        invertBlock(w, diag);
+        if (col + 1 == n) continue;
+        for (int row = col + 1; row < n; row++) {
+            int l = loc(row, col);
+            if (l == kEmpty) continue;
+            double* tgt = Dg + dloc(row, col);
+            const int h = cons[row]->n;
+            const double* src = B + l;
+            for (int r = 0; r < h; r++)
+                for (int c = 0; c < w; c++) tgt[c + w * r] = dotN(w, src + w * r, diag + w * c);
+        }
+        for (int lc = col + 1; lc < n; lc++)
+            for (int lr = lc; lr < n; lr++) {
+                int l = loc(lr, col);
+                if (l == kEmpty || loc(lc, col) == kEmpty) continue;
+                const double* a_src = B + l;
+                const double* l_src = Dg + dloc(lc, col);
+                double* tgt = B + loc(lr, lc);
+                const int bw = cons[lc]->n, bh = cons[lr]->n;
+                for (int r = 0; r < bh; r++)
+                    for (int c = 0; c < bw; c++) tgt[r * bw + c] -= dotN(w, a_src + r * w, l_src + c * w);
+            }
+        int first = firstBelow(col);
+        if (first == kEmpty) continue;
+        int total = loc(col + 1, col + 1) - first;
+        std::memcpy(B + first, Dg, sizeof(double) * (size_t)total);
+    }
+}
+
+// multInverseWithVector (HolonomicBlockSolver.cpp:251-317): v <- L^-T D^-1 L^-1 v
+void HoloSys::solve(std::vector<double>& v) const {
+    const int n = (int)cons.size();
+    const double* B = buf.data();
+    std::vector<double> eff(degree);
+    for (int col = 0; col + 1 < n; col++) {
+        eff.assign(degree, 0.0);
+        for (int row = col + 1; row < n; row++) {
+            int l = loc(row, col);
+            if (l == kEmpty) continue;
+            const int bw = cons[col]->n, bh = cons[row]->n;
+            for (int i = 0; i < bh; i++) eff[vpos[row] + i] = dotN(bw, B + l + i * bw, v.data() + vpos[col]);
+        }
+        for (int i = 0; i < degree; i++) v[i] -= eff[i];
+    }
+    std::vector<double> d(degree);
+    for (int col = 0; col < n; col++) {
+        const int w = cons[col]->n;
+        const double* blk = B + loc(col, col);
+        for (int i = 0; i < w; i++) d[vpos[col] + i] = dotN(w, blk + i * w, v.data() + vpos[col]);
+    }
+    v = d;
+    std::vector<double> e6(6);
+    for (int col = n - 2; col >= 0; col--) {
+        e6.assign(6, 0.0);
+        for (int row = col + 1; row < n; row++) {
+            int l = loc(row, col);
+            if (l == kEmpty) continue;
+            const int bw = cons[col]->n, bh = cons[row]->n;
+            for (int i = 0; i < bw; i++) {
+                double dp = 0;
+                for (int j = 0; j < bh; j++) dp += v[vpos[row] + j] * B[l + i + bw * j];
+                e6[i] += dp;
+            }
+        }
+        for (int i = 0; i < cons[col]->n; i++) v[vpos[col] + i] -= e6[i];
+    }
+}
+
+// HolonomicSystem::computeAndApplyImpulses (HolonomicBlockSolver.cpp:319-378):
+// solve A d = t - J dv for the whole system; with a threshold, a pseudo
+// solution whose angular velocity change exceeds it anywhere is discarded
+void HoloSys::computeAndApply(bool pseudo, double thr) {
+    std::vector<double> delta(degree);
+    for (size_t i = 0; i < cons.size(); i++) {
+        JRow& r = *cons[i];
+        double cur[kMaxDof];
+        if (pseudo) jrowValue(r, r.da->pv, r.db->pv, cur);
+        else jrowValue(r, r.da->v, r.db->v, cur);
+        const double* tgt = pseudo ? r.ptarget : r.target;
+        for (int k = 0; k < r.n; k++) delta[vpos[i] + k] = tgt[k] - cur[k];
+    }
+    solve(delta);
+    if (thr > 0) {
+        for (size_t i = 0; i < cons.size(); i++) {
+            JRow& r = *cons[i];
+            if (isZero(&delta[vpos[i]], r.n)) continue;
+            jrowApply(r, &delta[vpos[i]], &r.da->lin_err, &r.db->lin_err);
+        }
+        for (size_t i = 0; i < cons.size(); i++) {
+            const JRow& r = *cons[i];
+            double r2 = 0;
+            for (int k = 3; k < 6; k++) r2 += r.da->lin_err.v[k] * r.da->lin_err.v[k] + r.db->lin_err.v[k] * r.db->lin_err.v[k];
+            if (r2 > thr * thr) return;
+        }
+    }
+    for (size_t i = 0; i < cons.size(); i++) {
+        JRow& r = *cons[i];
+        const double* ic = &delta[vpos[i]];
+        if (isZero(ic, r.n)) continue;
+        if (pseudo) jrowApply(r, ic, &r.da->pv, &r.db->pv);
+        else jrowApply(r, ic, &r.da->v, &r.db->v);
+        double* acc = pseudo ? r.pimpulse : r.holo;
+        for (int k = 0; k < r.n; k++) acc[k] += ic[k];
+    }
+}
+
+// HolonomicSystem::verifyInverse (HolonomicBlockSolver.cpp:545-583): the
+// factorisation applied to every column of A gives the identity; returns the
+// Frobenius norm of the difference (the reference accepts < 1e-5)
+double HoloSys::inverseError(double cfm) const {
+    const int n = (int)cons.size();
+    std::vector<double> A((size_t)degree * degree);
+    int ro = 0;
+    for (int r = 0; r < n; r++) {
+        int co = 0;
+        for (int c = 0; c < n; c++) {
+            const int bw = cons[c]->n, bh = cons[r]->n;
+            double blk[kMaxDof * kMaxDof];
+            initialBlock(blk, cons[r], cons[c], cfm);
+            for (int i = 0; i < bh; i++)
+                for (int j = 0; j < bw; j++) A[(size_t)(j + co) + (size_t)(i + ro) * degree] = blk[j + i * bw];
+            co += bw;
+        }
+        ro += cons[r]->n;
+    }
+    double diff = 0;
+    for (int i = 0; i < degree; i++) {
+        std::vector<double> col(degree);
+        for (int j = 0; j < degree; j++) col[j] = A[(size_t)i + (size_t)degree * j];
+        solve(col);
+        for (int j = 0; j < degree; j++) {
+            double d = (j == i ? 1.0 : 0.0) - col[j];
+            diff += d * d;
+        }
+    }
+    return std::sqrt(diff);
+}
+
+// ------------------------------------------------------ world side ----
+// PhysicsEngine::addBallSocketConstraint / addHingeConstraint
+// (PhysicsEngine.cpp:664-723): collisions between the two bodies are
+// disallowed, the anchors become tracked points, the edge is flagged for a
+// holonomic-system scan
+Joint* World::addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, double pos_hard, double rot_hard) {
+    b1->no_collide.insert(b2);
+    b2->no_collide.insert(b1);
+    auto j = std::make_unique<Joint>();
+    j->n = n;
+    j->b1 = b1; j->b2 = b2;
+    b1->track_p.push_back(b1->local_origin + p1);
+    j->k1 = (int)b1->track_p.size() - 1;
+    b2->track_p.push_back(b2->local_origin + p2);
+    j->k2 = (int)b2->track_p.size() - 1;
+    if (n == 5) { j->ax1 = ax1.normalize(); j->ax2 = ax2.normalize(); }
+    j->pos_hard = pos_hard;
+    j->rot_hard = rot_hard;
+    j->row.n = n; j->row.a = b1; j->row.b = b2;
+    Edge* e = getOrCreateEdge(b1, b2);
+    if (e->h) e->h->changed = true;
+    else e->scan_needed = true;
+    j->edge = e;
+    e->joints.push_back(j.get());
+    joints.push_back(std::move(j));
+    return joints.back().get();
+}
+
+// getAllEdgesConnectedHolonomically (PhysicsEngine.cpp:1745-1777)
+static std::vector<Edge*> connectedHolonomically(World& w, Edge* e) {
+    std::set<Edge*> visited;
+    std::vector<Edge*> to_visit{e}, out;
+    while (!to_visit.empty()) {
+        Edge* v = to_visit.back();
+        to_visit.pop_back();
+        if (visited.count(v)) continue;
+        visited.insert(v);
+        out.push_back(v);
+        std::vector<Edge*> nb;
+        if (v->n1->movement == DYNAMIC) nb.insert(nb.end(), w.adj[v->n1].begin(), w.adj[v->n1].end());
+        if (v->n2->movement == DYNAMIC) nb.insert(nb.end(), w.adj[v->n2].begin(), w.adj[v->n2].end());
+        for (Edge* x : nb) {
+            if (visited.count(x)) continue;
+            if (!x->joints.empty()) to_visit.push_back(x);
+        }
+    }
+    return out;
+}
+
+// maintainAllHolonomicSystemStuffRelatedToThisEdge (PhysicsEngine.cpp:1466-1532)
+void World::holonomicScan(Edge* e) {
+    if (e->scan_needed) {
+        e->scan_needed = false;
+        std::vector<Edge*> conn = connectedHolonomically(*this, e);
+        if (conn.size() <= 1) return;
+        std::set<HoloSys*> seen;
+        for (Edge* x : conn) seen.insert(x->h);
+        if (seen.size() == 1 && *seen.begin() != nullptr) {
+        } else if (seen.size() == 1) {
+            auto h = std::make_unique<HoloSys>();
+            h->member_edges = conn;
+            h->changed = true;
+            for (Edge* x : conn) { x->h = h.get(); x->scan_needed = false; }
+            systems.push_back(std::move(h));
+        } else {
+            auto it = seen.begin();
+            HoloSys* keep = (*it == nullptr) ? *std::next(it) : *it;
+            for (Edge* x : conn) {
+                if (x->h != keep) { keep->member_edges.push_back(x); x->h = keep; }
+                x->scan_needed = false;
+            }
+            keep->changed = true;
+            for (HoloSys* s : seen)
+                if (s != nullptr && s != keep)
+                    for (size_t i = 0; i < systems.size(); i++)
+                        if (systems[i].get() == s) { systems.erase(systems.begin() + i); break; }
+        }
+    }
+    if (e->h != nullptr && e->h->changed) {
+        e->h->changed = false;
+        std::vector<JRow*> rows;   // HolonomicSystemNodes::revaluateSystem (:1789-1802)
+        for (Edge* x : e->h->member_edges)
+            for (Joint* j : x->joints) rows.push_back(&j->row);
+        e->h->build(rows);
+        for (Edge* x : e->h->member_edges)
+            for (Joint* j : x->joints) j->rebuild(p, p.dt / p.substeps, true);
+        e->h->computeInverse(p.cfm);
+    }
+}
+
+// PhysicsEngine::maintainHolonomicSystems (PhysicsEngine.cpp:1292-1306)
+void World::maintainHolonomicSystems() {
+    for (auto& kv : nodes)
+        for (Edge* e : adj[kv.second]) holonomicScan(e);
+}
+
+// calculateHolonomicSystemInversesAsync (PhysicsEngine.cpp:1617-1649): at the
+// end of a step the system rows are rebuilt from the new poses and the
+// factorisations recomputed for the next step's first substep
+void World::updateHolonomicInverses() {
+    std::set<HoloSys*> seen;
+    std::set<Edge*> seen_edges;
+    for (auto& kv : nodes)
+        for (Edge* e : adj[kv.second]) {
+            if (e->h == nullptr || seen_edges.count(e)) continue;
+            for (Joint* j : e->joints) j->rebuild(p, p.dt / p.substeps, true);
+            seen_edges.insert(e);
+            seen.insert(e->h);
+        }
+    for (HoloSys* h : seen) h->computeInverse(p.cfm);
+}
+
+}  // namespace cport

@@ -425,16 +425,20 @@ static void pgsStep(Row<N>& r, bool pseudo, Proj proj) {
 }
 
 // PGS_solve (ConstraintSolver.cpp:80-213) for the contact rows of one island
-static void pgsSolve(std::vector<RowRef>& rows, int n_vel, int n_pos) {
+static void pgsSolve(std::vector<RowRef>& rows, int n_vel, int n_pos, const std::vector<HoloSys*>& blocks, int n_holo,
+                     double lin_err_threshold) {
     std::unordered_map<Body*, std::unique_ptr<DV>> dv;
     auto slot = [&](Body* b) { auto& s = dv[b]; if (!s) s = std::make_unique<DV>(); return s.get(); };
     for (RowRef& rr : rows) {
         if (rr.kind == 0) { rr.c->normal.da = slot(rr.c->b1); rr.c->normal.db = slot(rr.c->b2); }
-        else { rr.c->friction.da = slot(rr.c->b1); rr.c->friction.db = slot(rr.c->b2); }
+        else if (rr.kind == 1) { rr.c->friction.da = slot(rr.c->b1); rr.c->friction.db = slot(rr.c->b2); }
+        else { rr.j->row.da = slot(rr.j->b1); rr.j->row.db = slot(rr.j->b2); }
     }
     for (RowRef& rr : rows) {
         Contact* c = rr.c;
-        if (rr.kind == 0) {
+        if (rr.kind == 2) {
+            jrowTarget(rr.j->row);
+        } else if (rr.kind == 0) {
             Row<1>& r = c->normal;
             double cur = r.value(velAng(r.a->getVel(), r.a->getAngVel()), velAng(r.b->getVel(), r.b->getAngVel())).v[0];
             r.target.v[0] = (cur < -c->cutoff) ? -(1 + c->bounce) * cur : -cur;
@@ -445,13 +449,15 @@ static void pgsSolve(std::vector<RowRef>& rows, int n_vel, int n_pos) {
     }
     for (RowRef& rr : rows) {
         if (rr.kind == 0) { Row<1>& r = rr.c->normal; if (!r.impulse.isZero()) r.applyImpulse(r.impulse, &r.da->v, &r.db->v); }
-        else { Row<2>& r = rr.c->friction; if (!r.impulse.isZero()) r.applyImpulse(r.impulse, &r.da->v, &r.db->v); }
+        else if (rr.kind == 1) { Row<2>& r = rr.c->friction; if (!r.impulse.isZero()) r.applyImpulse(r.impulse, &r.da->v, &r.db->v); }
+        else jrowWarm(rr.j->row);
     }
     auto projN = [](const Vec<1>& x) { Vec<1> o; o.v[0] = std::max<double>(x.v[0], 0); return o; };
     for (int it = 0; it < n_vel; it++) {
         for (RowRef& rr : rows) {
             Contact* c = rr.c;
-            if (rr.kind == 0) pgsStep(c->normal, false, projN);
+            if (rr.kind == 2) jrowStep(rr.j->row, false);
+            else if (rr.kind == 0) pgsStep(c->normal, false, projN);
             else {
                 pgsStep(c->friction, false, [c](const Vec<2>& x) {
                     double mx = c->friction_coeff * std::min<double>(std::numeric_limits<double>::infinity(), c->normal.impulse.v[0]);
@@ -469,8 +475,26 @@ static void pgsSolve(std::vector<RowRef>& rows, int n_vel, int n_pos) {
         }
     }
     for (int it = 0; it < n_pos; it++)
-        for (RowRef& rr : rows)
+        for (RowRef& rr : rows) {
             if (rr.kind == 0) pgsStep(rr.c->normal, true, projN);
+            else if (rr.kind == 2) jrowStep(rr.j->row, true);
+        }
+    // direct solve of the holonomic systems after the sweeps
+    // (ConstraintSolver.cpp:160-190); the holonomic impulse is carried into the
+    // next warm start scaled by 0
+    if (n_holo > 0 && !blocks.empty()) {
+        for (int it = 0; it < n_holo; it++)
+            for (HoloSys* h : blocks) {
+                h->computeAndApply(false, -1.0);
+                h->computeAndApply(true, lin_err_threshold);
+            }
+        const float scale = 0.0f;
+        for (RowRef& rr : rows) {
+            if (rr.kind != 2 || !rr.j->row.in_holo) continue;
+            JRow& r = rr.j->row;
+            for (int i = 0; i < r.n; i++) r.impulse[i] += scale * r.holo[i];
+        }
+    }
     // PhysicsEngine::applyVelocityChange (PhysicsEngine.cpp:1113-1136)
     for (auto& kv : dv) {
         Body* b = kv.first;
@@ -522,6 +546,7 @@ void World::step() {
         Body* b1 = bodies[pr.first - 1].get();
         Body* b2 = bodies[pr.second - 1].get();
         if (!(b1->movement == DYNAMIC || b2->movement == DYNAMIC)) continue;
+        if (b1->no_collide.count(b2)) continue;   // collisionAllowed (PhysicsEngine.cpp:570-572)
         Manifold man = collide(b1, b2);
         if (!(man.max_pen > 0)) continue;
         Manifold m = cullManifold(man, 4);
@@ -529,13 +554,19 @@ void World::step() {
         for (const ManifoldPoint& mp : m.pts) addContact(b1, b2, mp, m.normal);
     }
 
+    // holonomic systems of new joints (PhysicsEngine.cpp:360-362)
+    const bool holo = p.pgs_holo > 0;
+    if (holo) maintainHolonomicSystems();
+
     // islands in constraint_graph_nodes iteration order (PhysicsEngine.cpp:1536-1613)
     std::vector<std::vector<RowRef>> islands;
+    std::vector<std::vector<HoloSys*>> island_blocks;
     std::set<Body*> visited;
     for (auto& kv : nodes) {
         Body* n = kv.second;
         if (n->movement != DYNAMIC || visited.count(n)) continue;
         std::vector<RowRef> rows;
+        std::vector<HoloSys*> blocks;
         std::vector<Body*> stack{n};
         while (!stack.empty()) {
             Body* cur = stack.back();
@@ -545,6 +576,8 @@ void World::step() {
                 for (Edge* e : adj[cur]) {
                     Body* o = e->other(cur);
                     if (visited.count(o)) continue;
+                    if (holo && e->h && std::find(blocks.begin(), blocks.end(), e->h) == blocks.end()) blocks.push_back(e->h);
+                    for (Joint* j : e->joints) rows.push_back({2, nullptr, j});
                     for (auto& c : e->contacts)
                         if (c->live) { rows.push_back({0, c.get()}); rows.push_back({1, c.get()}); }
                 }
@@ -554,7 +587,7 @@ void World::step() {
                 if (o->movement == DYNAMIC && !visited.count(o)) stack.push_back(o);
             }
         }
-        if (!rows.empty()) islands.push_back(std::move(rows));
+        if (!rows.empty()) { islands.push_back(std::move(rows)); island_blocks.push_back(std::move(blocks)); }
     }
 
     // substeps (PhysicsEngine.cpp:368-420)
@@ -563,6 +596,11 @@ void World::step() {
         bool first = s == 0, last = s == p.substeps - 1;
         std::vector<Edge*> dead;
         for (auto& e : edges) {
+            // holonomic rows were rebuilt (and factorised) at the end of the
+            // previous step for the first substep (PhysicsEngine.cpp:1397-1404)
+            const bool in_holo = e->h != nullptr;
+            for (Joint* j : e->joints)
+                if (!(first && in_holo && holo)) j->rebuild(p, dts, in_holo);
             for (auto& c : e->contacts) {
                 bool skip = !c->live;
                 if (last) { c->life--; c->live = false; }
@@ -572,11 +610,12 @@ void World::step() {
             if (first) {
                 auto& v = e->contacts;
                 v.erase(std::remove_if(v.begin(), v.end(), [](const std::unique_ptr<Contact>& c) { return c->life < 0; }), v.end());
-                if (v.empty()) dead.push_back(e.get());
+                if (v.empty() && e->joints.empty()) dead.push_back(e.get());
             }
         }
         for (Edge* e : dead) deleteEdge(e);
-        for (auto& rows : islands) pgsSolve(rows, p.pgs_vel, p.pgs_pos);
+        for (size_t k = 0; k < islands.size(); k++)
+            pgsSolve(islands[k], p.pgs_vel, p.pgs_pos, island_blocks[k], first ? p.pgs_holo : 0, p.lin_err_threshold);
         for (auto& bp : bodies) {
             Body* b = bp.get();
             if (b->movement == FIXED) continue;
@@ -599,6 +638,7 @@ void World::step() {
         if (b->movement == FIXED) continue;
         if (b->com != b->prev_com || b->q != b->prev_q) b->updateGeometry();
     }
+    if (holo) updateHolonomicInverses();
 }
 
 }  // namespace cport
@@ -718,11 +758,23 @@ int cport_body_set_mass(cpgpu_world* w, uint32_t id, double m) {
     b->mass = m;
     return CPGPU_OK;
 }
-int cport_add_ball_socket(cpgpu_world*, uint32_t, uint32_t, const double*, const double*, double, uint32_t*) {
-    return fail("joints are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+// PhysicsEngine::addBallSocketConstraint (PhysicsEngine.cpp:664-687)
+int cport_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], double strength,
+                          uint32_t* out_id) {
+    Body* x = B(w, b1); Body* y = B(w, b2);
+    if (!x || !y || x == y) return fail("bad body id");
+    W(w)->addJoint(3, x, y, v3(a1), v3(a2), V3(), V3(), strength, 0);
+    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    return CPGPU_OK;
 }
-int cport_add_hinge(cpgpu_world*, uint32_t, uint32_t, const double*, const double*, const double*, const double*, double, double, uint32_t*) {
-    return fail("joints are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+// PhysicsEngine::addHingeConstraint (PhysicsEngine.cpp:693-723)
+int cport_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], const double ax1[3],
+                    const double ax2[3], double ps, double rs, uint32_t* out_id) {
+    Body* x = B(w, b1); Body* y = B(w, b2);
+    if (!x || !y || x == y) return fail("bad body id");
+    W(w)->addJoint(5, x, y, v3(a1), v3(a2), v3(ax1), v3(ax2), ps, rs);
+    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    return CPGPU_OK;
 }
 // Test hook: replace the mass properties computed at creation by given ones
 // (the reference's, so that both engines start from bit-identical bodies).
@@ -740,6 +792,19 @@ int cport_get_mass_properties(cpgpu_world* w, uint32_t id, double* mass, double*
     *mass = b->mass;
     com_geom[0] = -b->local_origin.x; com_geom[1] = -b->local_origin.y; com_geom[2] = -b->local_origin.z;
     for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) tensor[3 * i + j] = b->ref_tensor.m[i][j];
+    return CPGPU_OK;
+}
+// Test hook: number of holonomic systems and the largest verifyInverse error
+// over them (factorisations as left by the last step).
+int cport_holonomic_check(cpgpu_world* w, int* n_systems, int* max_degree, double* max_err) {
+    World* x = W(w);
+    *n_systems = (int)x->systems.size();
+    *max_degree = 0;
+    *max_err = 0;
+    for (auto& h : x->systems) {
+        *max_degree = std::max(*max_degree, h->degree);
+        *max_err = std::max(*max_err, h->inverseError(x->p.cfm));
+    }
     return CPGPU_OK;
 }
 int cport_step(cpgpu_world* w, int n) { for (int i = 0; i < n; i++) W(w)->step(); return CPGPU_OK; }

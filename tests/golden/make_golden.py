@@ -51,7 +51,21 @@ def mixed():
                         pen_depth=c["pen_depth"])
 
 
+def chain():
+    """One articulated chain (scenes.chain_world, rng seed 5, 10-14 links, 20
+    spheres) after 200 reference steps, with the reference's mass properties
+    as created (before the scene's setMass calls)."""
+    steps = 200
+    sc = scenes.chain_world(np.random.default_rng(5), 10, 14, n_spheres=20)
+    mass, com, tensor, w = oracle.capture_mass_properties(sc)
+    w.step(steps)
+    st = w.state()
+    np.savez_compressed(os.path.join(HERE, "chain_seed5.npz"), steps=steps, mass=mass, com_geom=com, tensor=tensor,
+                        com=st["com"], quat=st["quat"], vel=st["vel"], ang_vel=st["ang_vel"])
+
+
 def main():
+    chain()
     mixed()
     steps = 120
     w = oracle.ref_world()
