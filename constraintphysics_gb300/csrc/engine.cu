@@ -102,10 +102,22 @@ struct Params {
 
 struct Batch;
 
+// BallSocket / Hinge (PersistentConstraint.h:118-313) in the host mirror
+struct HJoint {
+    int b1 = 0, b2 = 0;          // body indices (0-based) in the world
+    int n = 3;                   // 3 ball-socket, 5 hinge
+    D3 p1, p2;                   // anchors: tracked points relative to the COM, body frame
+    D3 ax1, ax2;                 // normalised hinge axes, body space
+    double ph = 15000, rh = 15000;
+    float impulse[kJMax] = {};   // warm-start impulse carried between uploads
+    float u[3] = {}, w[3] = {};  // hinge basis of the last rebuild
+};
+
 struct World {
     Params p;
     std::vector<Shape> shapes;
     std::vector<Body> bodies;
+    std::vector<HJoint> joints;
     std::unordered_map<unsigned int, int> nodes;   // same insert sequence as constraint_graph_nodes
     std::vector<cpgpu_contact> contacts;           // host copy of the contact graph
     std::vector<uint32_t> last_pairs;
@@ -266,6 +278,8 @@ struct Batch {
     int n_sms = 0;
     int slot_bytes = 0;
     bool prims = false;                // the batch holds spheres or cylinders
+    bool joints = false;               // the batch holds joints
+    bool systems = false;              // ... and holonomic systems
     cudaStream_t st = nullptr;
     cudaStream_t side = nullptr;       // concurrent branch (small-island PGS)
     cudaEvent_t fork = nullptr, join = nullptr;
@@ -306,8 +320,10 @@ struct Batch {
         launch_islands(x, L);
         launch_pgs_schedule(x, L); mark(5);
         for (int s = 0; s < substeps; s++) {
-            launch_rows(x, s == 0, s == substeps - 1, L);  mark(6 + 3 * s);
-            launch_pgs(x, dv_cap, side, fork, join, L);    mark(7 + 3 * s);
+            launch_rows(x, s == 0, s == substeps - 1, L);
+            launch_joint_rows(x, s == 0, L);               mark(6 + 3 * s);
+            launch_pgs(x, dv_cap, side, fork, join, L);
+            launch_pgs_joint(x, s == 0, L);                mark(7 + 3 * s);
             launch_integrate(x, s == substeps - 1, L);     mark(8 + 3 * s);
         }
         launch_geometry(x, 0, L);  mark(6 + 3 * substeps);
@@ -315,7 +331,11 @@ struct Batch {
     // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 1
     // (+1 with spheres / cylinders), merge 6 + 3 scans, islands 2 + scan 3,
     // schedule 3, 4 per substep (rows, small + large PGS, integrate), geometry 1
-    int launches_per_step() const { return 1 + 6 + 1 + (prims ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 4 * substeps + 1; }
+    // (+2 per substep and 1 factorisation with joints)
+    int launches_per_step() const {
+        return 1 + 6 + 1 + (prims ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 4 * substeps + 1 + (joints ? 2 * substeps : 0) +
+               (systems ? 1 : 0);
+    }
 
     void build_graphs() {
         for (int p = 0; p < 2; p++) {
@@ -365,6 +385,141 @@ static std::vector<int> map_iteration_order(const World& w) {
     order.reserve(w.nodes.size());
     for (const auto& kv : w.nodes) order.push_back(kv.second);
     return order;
+}
+
+// ---------------------------------------------------------------- holonomic systems ----
+// A world's joint edges (one per jointed body pair, joints in insertion order)
+// and its holonomic systems, found as PhysicsEngine::maintainHolonomicSystems
+// (PhysicsEngine.cpp:1292-1306, 1466-1532, 1745-1777) finds them on the first
+// step: nodes in node-map order, each node's joint edges by the other body's
+// id, a scan from every edge not yet in a system collecting the edges
+// connected through dynamic bodies.
+struct HSystem {
+    std::vector<int> cons;       // joint indices (world-local) in elimination order
+    std::vector<int> vpos, table;
+    int degree = 0, cap = 0;
+    bool fp64 = false;
+};
+
+struct JointGraph {
+    std::vector<std::pair<int, int>> edge_pair;       // (lower body, higher body)
+    std::vector<std::vector<int>> edge_joints;
+    std::vector<int> edge_sys;
+    std::vector<HSystem> systems;
+};
+
+// HolonomicSystem::HolonomicSystem (HolonomicBlockSolver.cpp:11-132): greedy
+// minimum-fill elimination order over constraints that share a body, and the
+// lower-triangle block table of the factor
+static HSystem order_system(const World& w, const std::vector<int>& og) {
+    HSystem H;
+    const int n = (int)og.size();
+    std::vector<char> edge((size_t)n * n, 0), empty((size_t)n * n, 1);
+    auto E = [&](int i, int j) -> char& { return edge[(size_t)i + (size_t)j * n]; };
+    auto shares = [&](int x, int y) {
+        const HJoint &a = w.joints[og[x]], &b = w.joints[og[y]];
+        return a.b1 == b.b1 || a.b1 == b.b2 || a.b2 == b.b1 || a.b2 == b.b2;
+    };
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++)
+            if (shares(i, j)) { empty[(size_t)i * n + j] = empty[(size_t)j * n + i] = 0; E(i, j) = E(j, i) = 1; }
+    std::vector<int> remaining(n), order;
+    for (int i = 0; i < n; i++) remaining[i] = i;
+    while (!remaining.empty()) {
+        int best_i = -1, best = INT32_MAX;
+        std::vector<int> best_nb;
+        for (int i = 0; i < (int)remaining.size(); i++) {
+            std::vector<int> nb;
+            for (int j = 0; j < n; j++)
+                if (j != remaining[i] && E(remaining[i], j)) nb.push_back(j);
+            int un = 0;
+            for (size_t a = 0; a < nb.size(); a++)
+                for (size_t b = a + 1; b < nb.size(); b++) un += !E(nb[a], nb[b]);
+            if (un < best) { best = un; best_i = i; best_nb = nb; if (un == 0) break; }
+        }
+        const int x = remaining[best_i];
+        order.push_back(x);
+        remaining.erase(remaining.begin() + best_i);
+        for (int j = 0; j < n; j++) E(x, j) = E(j, x) = 0;
+        for (size_t a = 0; a < best_nb.size(); a++)
+            for (size_t b = a + 1; b < best_nb.size(); b++) {
+                const int p = best_nb[a], q = best_nb[b];
+                empty[(size_t)p * n + q] = empty[(size_t)q * n + p] = 0;
+                E(p, q) = E(q, p) = 1;
+            }
+    }
+    for (int xi : order) H.cons.push_back(og[xi]);
+    for (int col = 0; col < n; col++) {
+        H.vpos.push_back(H.degree);
+        H.degree += w.joints[H.cons[col]].n;
+        for (int row = col; row < n; row++) {
+            if (empty[(size_t)order[row] * n + order[col]]) H.table.push_back(-1);
+            else { H.table.push_back(H.cap); H.cap += w.joints[H.cons[row]].n * w.joints[H.cons[col]].n; }
+        }
+    }
+    double mmin = 1e300, mmax = 0;
+    for (int j : H.cons)
+        for (int b : {w.joints[j].b1, w.joints[j].b2})
+            if (w.bodies[b].movement == CPGPU_DYNAMIC) { mmin = std::min(mmin, w.bodies[b].mass); mmax = std::max(mmax, w.bodies[b].mass); }
+    H.fp64 = mmax > 100.0 * mmin;   // FP64 factorisation for mass ratios above 100
+    return H;
+}
+
+static JointGraph joint_graph(const World& w, const std::vector<int>& map_order) {
+    JointGraph G;
+    std::map<std::pair<int, int>, int> idx;
+    for (int j = 0; j < (int)w.joints.size(); j++) {
+        std::pair<int, int> k(std::min(w.joints[j].b1, w.joints[j].b2), std::max(w.joints[j].b1, w.joints[j].b2));
+        auto it = idx.find(k);
+        if (it == idx.end()) {
+            it = idx.emplace(k, (int)G.edge_pair.size()).first;
+            G.edge_pair.push_back(k);
+            G.edge_joints.emplace_back();
+        }
+        G.edge_joints[it->second].push_back(j);
+    }
+    const int ne = (int)G.edge_pair.size();
+    G.edge_sys.assign(ne, -1);
+    if (ne == 0 || w.p.pgs_holo <= 0) return G;
+    const int nb = (int)w.bodies.size();
+    std::vector<std::vector<int>> adj(nb);
+    for (int e = 0; e < ne; e++) { adj[G.edge_pair[e].first].push_back(e); adj[G.edge_pair[e].second].push_back(e); }
+    for (int b = 0; b < nb; b++)
+        std::sort(adj[b].begin(), adj[b].end(), [&](int x, int y) {
+            auto other = [&](int e) { return G.edge_pair[e].first == b ? G.edge_pair[e].second : G.edge_pair[e].first; };
+            return other(x) < other(y);
+        });
+    std::vector<char> scanned(ne, 0);
+    for (int node : map_order)
+        for (int e0 : adj[node]) {
+            if (scanned[e0]) continue;
+            scanned[e0] = 1;
+            // getAllEdgesConnectedHolonomically: DFS with a LIFO stack
+            std::vector<char> vis(ne, 0);
+            std::vector<int> stack{e0}, conn;
+            while (!stack.empty()) {
+                int v = stack.back();
+                stack.pop_back();
+                if (vis[v]) continue;
+                vis[v] = 1;
+                conn.push_back(v);
+                // the first body's edges, then the second's (n1 is the body
+                // the edge was created from: the first joint's b1)
+                std::vector<int> nbr;
+                const HJoint& j0 = w.joints[G.edge_joints[v][0]];
+                for (int end : {j0.b1, j0.b2})
+                    if (w.bodies[end].movement == CPGPU_DYNAMIC) nbr.insert(nbr.end(), adj[end].begin(), adj[end].end());
+                for (int x : nbr) if (!vis[x]) stack.push_back(x);
+            }
+            for (int x : conn) scanned[x] = 1;
+            if (conn.size() <= 1) continue;
+            std::vector<int> og;
+            for (int x : conn) for (int j : G.edge_joints[x]) og.push_back(j);
+            const int sid = (int)G.systems.size();
+            for (int x : conn) G.edge_sys[x] = sid;
+            G.systems.push_back(order_system(w, og));
+        }
+    return G;
 }
 
 static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
@@ -460,6 +615,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         P.warm_disabled = w.p.warm_disabled;
         P.pgs_vel = w.p.pgs_vel;
         P.pgs_pos = w.p.pgs_pos;
+        P.pgs_holo = w.p.pgs_holo;
     }
     B->movement = movement;
     B->slot_bytes = 2 * max_hot;
@@ -492,6 +648,71 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
             cedge.push_back((int)ekey.size() - 1);
         }
     }
+
+    // ---- joints, joint edges and holonomic systems of the worlds
+    std::vector<int> j_b1, j_b2, j_n;
+    std::vector<float4> j_p1, j_p2, j_ax1, j_ax2, j_u, j_w;
+    std::vector<float2> j_hard;
+    std::vector<float> j_imp;
+    std::vector<uint64_t> je_key;
+    std::vector<int> je_jstart, je_jcount, je_sys, je_wstart{0}, je_wjstart{0}, hs_wstart{0};
+    std::vector<int> hs_cstart{0}, hs_cons, hs_vpos, hs_degree, hs_tstart{0}, hs_table, hs_bstart, hs_cap, hs_fp64, hs_wk;
+    size_t pool32_n = 0, pool64_n = 0, work_n = 0;
+    for (size_t wi = 0; wi < worlds.size(); wi++) {
+        const World& w = *worlds[wi];
+        const int base = wstart[wi], jbase = (int)j_b1.size();
+        for (const HJoint& j : w.joints) {
+            j_b1.push_back(base + j.b1); j_b2.push_back(base + j.b2); j_n.push_back(j.n);
+            j_p1.push_back(make_float4((float)j.p1.x, (float)j.p1.y, (float)j.p1.z, 0.f));
+            j_p2.push_back(make_float4((float)j.p2.x, (float)j.p2.y, (float)j.p2.z, 0.f));
+            j_ax1.push_back(make_float4((float)j.ax1.x, (float)j.ax1.y, (float)j.ax1.z, 0.f));
+            j_ax2.push_back(make_float4((float)j.ax2.x, (float)j.ax2.y, (float)j.ax2.z, 0.f));
+            j_u.push_back(make_float4(j.u[0], j.u[1], j.u[2], 0.f));
+            j_w.push_back(make_float4(j.w[0], j.w[1], j.w[2], 0.f));
+            j_hard.push_back(make_float2((float)j.ph, (float)j.rh));
+            for (int k = 0; k < kJMax; k++) j_imp.push_back(j.impulse[k]);
+        }
+        if (!w.joints.empty()) {
+            std::vector<int> order = map_iteration_order(w);
+            JointGraph G = joint_graph(w, order);
+            std::vector<int> eorder(G.edge_pair.size());
+            for (size_t e = 0; e < eorder.size(); e++) eorder[e] = (int)e;
+            std::sort(eorder.begin(), eorder.end(), [&](int x, int y) { return G.edge_pair[x] < G.edge_pair[y]; });
+            const int sbase = (int)hs_degree.size();
+            for (int e : eorder) {
+                je_key.push_back(((uint64_t)(base + G.edge_pair[e].first) << 32) | (uint32_t)(base + G.edge_pair[e].second));
+                je_jstart.push_back(jbase + G.edge_joints[e][0]);
+                je_jcount.push_back((int)G.edge_joints[e].size());
+                je_sys.push_back(G.edge_sys[e] >= 0 ? sbase + G.edge_sys[e] : -1);
+            }
+            // joints of an edge must be contiguous for the device's (start, count)
+            for (int e : eorder)
+                for (size_t k = 1; k < G.edge_joints[e].size(); k++)
+                    if (G.edge_joints[e][k] != G.edge_joints[e][0] + (int)k)
+                        throw ApiFail{CPGPU_ERR_UNSUPPORTED, "joints between one body pair must be added consecutively"};
+            for (const HSystem& H : G.systems) {
+                for (int j : H.cons) hs_cons.push_back(jbase + j);
+                hs_vpos.insert(hs_vpos.end(), H.vpos.begin(), H.vpos.end());
+                hs_cstart.push_back((int)hs_cons.size());
+                hs_degree.push_back(H.degree);
+                hs_table.insert(hs_table.end(), H.table.begin(), H.table.end());
+                hs_tstart.push_back((int)hs_table.size());
+                hs_cap.push_back(H.cap);
+                hs_fp64.push_back(H.fp64 ? 1 : 0);
+                const size_t need = (size_t)H.cap + 6 * (size_t)H.degree;
+                if (H.fp64) { hs_bstart.push_back((int)pool64_n); pool64_n += need; }
+                else { hs_bstart.push_back((int)pool32_n); pool32_n += (need + 3) & ~size_t(3); }
+                hs_wk.push_back((int)work_n);
+                work_n += 2 * (size_t)H.degree;
+            }
+        }
+        je_wstart.push_back((int)je_key.size());
+        je_wjstart.push_back((int)j_b1.size());
+        hs_wstart.push_back((int)hs_degree.size());
+    }
+    const int n_joints = (int)j_b1.size(), n_je = (int)je_key.size(), n_sys = (int)hs_degree.size();
+    B->joints = n_joints > 0;
+    B->systems = n_sys > 0;
 
     // ---- capacities and device allocation
     // capacities per body, with floors; both can be overridden by the environment
@@ -551,9 +772,9 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         x.edge_src = A.take<int>(cap_edges); x.edge_pair = A.take<int>(cap_edges); x.edge_cnt = A.take<int>(cap_edges);
         x.scan_tmp = A.take<int>(scan_tmp);
         x.adj_ofs = A.take<int>(N); x.adj_cursor = A.take<int>(N);
-        x.adj_list = A.take<int>(2 * (2 * (size_t)cap_edges + N));
+        x.adj_list = A.take<int>(2 * (2 * ((size_t)cap_edges + n_je) + N));
         x.visited = A.take<int>(N);
-        x.stack = A.take<int>(2 * (size_t)cap_edges + N);
+        x.stack = A.take<int>(2 * ((size_t)cap_edges + n_je) + N);
         x.isl_count_w = A.take<int>(worlds.size()); x.isl_scan = A.take<int>(worlds.size());
         x.isl_row_start = A.take<int>(N); x.isl_row_count = A.take<int>(N); x.isl_body_start = A.take<int>(N);
         x.isl_body_count = A.take<int>(N); x.isl_world = A.take<int>(N);
@@ -561,8 +782,8 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         x.g_isl_body_count = A.take<int>(N); x.g_isl_world = A.take<int>(N);
         x.n_islands = counts + 5;
         x.isl_bodies = A.take<int>(N);
-        x.row_contact = A.take<int>(cap_contacts); x.row_of_contact = A.take<int>(cap_contacts);
-        x.rows = A.take<RowBlock>(cap_contacts);
+        x.row_contact = A.take<int>((size_t)cap_contacts + n_joints); x.row_of_contact = A.take<int>(cap_contacts);
+        x.rows = A.take<RowBlock>((size_t)cap_contacts + n_joints);
         x.dv = A.take<float4>(4 * (size_t)N);
         x.stage = A.take<float4>(4 * (size_t)N);
         x.big_list = A.take<int>(N);
@@ -570,6 +791,39 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         x.sched = A.take<int>(96);
         x.status = counts + 6;
         x.cnt = counts + 16;
+        x.n_joints = n_joints;
+        x.n_joint_edges = n_je;
+        x.lin_err_threshold = 15.0f;   // excessive_linear_error_torque_threshold (PhysicsEngine.h:217)
+        if (n_joints > 0) {
+            JointStore& J = x.jt;
+            int* ib1 = A.take<int>(n_joints); int* ib2 = A.take<int>(n_joints); int* in = A.take<int>(n_joints);
+            J.b1 = ib1; J.b2 = ib2; J.n = in;
+            J.p1 = A.take<float4>(n_joints); J.p2 = A.take<float4>(n_joints);
+            J.ax1 = A.take<float4>(n_joints); J.ax2 = A.take<float4>(n_joints);
+            J.hard = A.take<float2>(n_joints);
+            J.impulse = A.take<float>(kJMax * (size_t)n_joints);
+            J.u = A.take<float4>(n_joints); J.w = A.take<float4>(n_joints);
+            J.rows = A.take<JointRow>(n_joints);
+            JointEdgeStore& E = x.je;
+            E.key = A.take<uint64_t>(n_je); E.jstart = A.take<int>(n_je); E.jcount = A.take<int>(n_je);
+            E.sys = A.take<int>(n_je);
+            E.world_start = A.take<int>(worlds.size() + 1); E.world_jstart = A.take<int>(worlds.size() + 1);
+            HoloStore& H = x.hs;
+            H.n = n_sys;
+            H.cstart = A.take<int>(n_sys + 1); H.cons = A.take<int>(hs_cons.size()); H.vpos = A.take<int>(hs_vpos.size());
+            H.degree = A.take<int>(n_sys); H.tstart = A.take<int>(n_sys + 1); H.table = A.take<int>(hs_table.size());
+            H.bstart = A.take<int>(n_sys); H.cap = A.take<int>(n_sys); H.fp64 = A.take<int>(n_sys);
+            H.wstart = A.take<int>(n_sys);
+            H.pool32 = A.take<float>(pool32_n); H.pool64 = A.take<double>(pool64_n); H.work = A.take<double>(work_n);
+            H.isl = nullptr;
+            x.hs_world_start = A.take<int>(worlds.size() + 1);
+            x.isl_flags = A.take<int>(N); x.g_isl_flags = A.take<int>(N);
+            x.isl_sys_start = A.take<int>(N); x.isl_sys_count = A.take<int>(N);
+            x.g_isl_sys_start = A.take<int>(N); x.g_isl_sys_count = A.take<int>(N);
+            x.isl_sys = A.take<int>(n_sys);
+            x.joint_list = A.take<int>(N);
+            x.dv_err = A.take<float4>(4 * (size_t)N);
+        }
     };
     Arena measure{nullptr, 0, 0};
     carve(measure);
@@ -601,6 +855,28 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     up(cs[0].state, cstate.data(), nc * 4); up(cs[0].edge, cedge.data(), nc * 4);
     int host_counts[5] = {0, ne, 0, nc, 0};   // n_pairs, n_edges[0], n_edges[1], n_contacts[0], n_contacts[1]
     up(counts, host_counts, sizeof(host_counts));
+    if (n_joints > 0) {
+        const JointStore& J = x.jt;
+        up((void*)J.b1, j_b1.data(), n_joints * 4); up((void*)J.b2, j_b2.data(), n_joints * 4); up((void*)J.n, j_n.data(), n_joints * 4);
+        up((void*)J.p1, j_p1.data(), n_joints * 16); up((void*)J.p2, j_p2.data(), n_joints * 16);
+        up((void*)J.ax1, j_ax1.data(), n_joints * 16); up((void*)J.ax2, j_ax2.data(), n_joints * 16);
+        up((void*)J.hard, j_hard.data(), n_joints * 8);
+        up(J.impulse, j_imp.data(), j_imp.size() * 4);
+        up(J.u, j_u.data(), n_joints * 16); up(J.w, j_w.data(), n_joints * 16);
+        CK(cudaMemsetAsync(J.rows, 0, sizeof(JointRow) * (size_t)n_joints, B->st));
+        const JointEdgeStore& E = x.je;
+        up((void*)E.key, je_key.data(), n_je * 8); up((void*)E.jstart, je_jstart.data(), n_je * 4);
+        up((void*)E.jcount, je_jcount.data(), n_je * 4); up((void*)E.sys, je_sys.data(), n_je * 4);
+        up((void*)E.world_start, je_wstart.data(), je_wstart.size() * 4);
+        up((void*)E.world_jstart, je_wjstart.data(), je_wjstart.size() * 4);
+        const HoloStore& H = x.hs;
+        up((void*)H.cstart, hs_cstart.data(), hs_cstart.size() * 4); up((void*)H.cons, hs_cons.data(), hs_cons.size() * 4);
+        up((void*)H.vpos, hs_vpos.data(), hs_vpos.size() * 4); up((void*)H.degree, hs_degree.data(), hs_degree.size() * 4);
+        up((void*)H.tstart, hs_tstart.data(), hs_tstart.size() * 4); up((void*)H.table, hs_table.data(), hs_table.size() * 4);
+        up((void*)H.bstart, hs_bstart.data(), hs_bstart.size() * 4); up((void*)H.cap, hs_cap.data(), hs_cap.size() * 4);
+        up((void*)H.fp64, hs_fp64.data(), hs_fp64.size() * 4); up((void*)H.wstart, hs_wk.data(), hs_wk.size() * 4);
+        up((void*)x.hs_world_start, hs_wstart.data(), hs_wstart.size() * 4);
+    }
     for (int p = 0; p < 2; p++) {
         Dev y = x;
         y.e_old = es[p]; y.e_new = es[1 - p];
@@ -647,6 +923,21 @@ static void download_state(World& w) {
         }
         if (b.movement == CPGPU_DYNAMIC)
             for (int k = 0; k < 9; k++) { b.iw[k] = iw[9 * (size_t)i + k]; b.iinv[k] = iinv[9 * (size_t)i + k]; }
+    }
+    // joints' warm-start impulses and hinge bases
+    if (!w.joints.empty() && x.n_joints > 0) {
+        const int nj = x.n_joints;
+        std::vector<float> imp((size_t)kJMax * nj);
+        std::vector<float4> u(nj), wv(nj);
+        CK(cudaMemcpyAsync(imp.data(), x.jt.impulse, imp.size() * 4, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(u.data(), x.jt.u, nj * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(wv.data(), x.jt.w, nj * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaStreamSynchronize(B.st));
+        for (int j = 0; j < nj && j < (int)w.joints.size(); j++) {
+            for (int k = 0; k < kJMax; k++) w.joints[j].impulse[k] = imp[(size_t)kJMax * j + k];
+            w.joints[j].u[0] = u[j].x; w.joints[j].u[1] = u[j].y; w.joints[j].u[2] = u[j].z;
+            w.joints[j].w[0] = wv[j].x; w.joints[j].w[1] = wv[j].y; w.joints[j].w[2] = wv[j].z;
+        }
     }
     // contact graph (current = the old buffers of the next step)
     const int ne = *(&counts[1] + B.parity), nc = *(&counts[3] + B.parity);
@@ -976,12 +1267,44 @@ int cpgpu_body_set_mass(cpgpu_world* w, uint32_t id, double mass) {
     });
 }
 
-int cpgpu_add_ball_socket(cpgpu_world*, uint32_t, uint32_t, const double*, const double*, double, uint32_t*) {
-    return fail(CPGPU_ERR_UNSUPPORTED, "joints are not implemented on the device path yet");
+// PhysicsEngine::addBallSocketConstraint / addHingeConstraint
+// (PhysicsEngine.cpp:664-723): anchors in each body's model coordinates become
+// tracked points (RigidBody::trackPoint, RigidBody.cpp:134-137); hinge axes
+// are normalised; the two bodies stop colliding with each other.
+static uint32_t add_joint(World& w, int n, uint32_t b1, uint32_t b2, const double* a1, const double* a2, const double* ax1,
+                          const double* ax2, double ph, double rh) {
+    if (!a1 || !a2 || (n == 5 && (!ax1 || !ax2))) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null anchor or axis"};
+    if (b1 == b2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "a joint needs two different bodies"};
+    Body& x = body_ref(w, b1);
+    Body& y = body_ref(w, b2);
+    begin_mutation(w);
+    HJoint j;
+    j.b1 = (int)b1 - 1; j.b2 = (int)b2 - 1; j.n = n;
+    j.p1 = x.local_origin + D3(a1[0], a1[1], a1[2]);
+    j.p2 = y.local_origin + D3(a2[0], a2[1], a2[2]);
+    if (n == 5) { j.ax1 = D3(ax1[0], ax1[1], ax1[2]).normalize(); j.ax2 = D3(ax2[0], ax2[1], ax2[2]).normalize(); }
+    j.ph = ph; j.rh = rh;
+    w.joints.push_back(j);
+    return (uint32_t)w.joints.size();
 }
-int cpgpu_add_hinge(cpgpu_world*, uint32_t, uint32_t, const double*, const double*, const double*, const double*, double, double,
-                    uint32_t*) {
-    return fail(CPGPU_ERR_UNSUPPORTED, "joints are not implemented on the device path yet");
+
+int cpgpu_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], double strength,
+                          uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        uint32_t id = add_joint(w->w, 3, b1, b2, a1, a2, nullptr, nullptr, strength, 0);
+        if (out_id) *out_id = id;
+        return CPGPU_OK;
+    });
+}
+int cpgpu_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], const double ax1[3],
+                    const double ax2[3], double ps, double rs, uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        uint32_t id = add_joint(w->w, 5, b1, b2, a1, a2, ax1, ax2, ps, rs);
+        if (out_id) *out_id = id;
+        return CPGPU_OK;
+    });
 }
 
 int cpgpu_step(cpgpu_world* w, int n_steps) {
@@ -1101,6 +1424,35 @@ int cpgpu_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n) {
             return a.b1 != b.b1 ? a.b1 < b.b1 : a.b2 < b.b2;
         });
         w->w.contacts = cs;
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv, int* n) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!n) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null count"};
+        if (w->w.dev && w->w.dev_valid) download_state(w->w);
+        *n = (int)w->w.joints.size();
+        for (size_t j = 0; j < w->w.joints.size(); j++) {
+            const HJoint& x = w->w.joints[j];
+            for (int k = 0; k < kJMax; k++) if (impulse) impulse[kJMax * j + k] = x.impulse[k];
+            for (int k = 0; k < 3; k++) { if (u) u[3 * j + k] = x.u[k]; if (wv) wv[3 * j + k] = x.w[k]; }
+        }
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u, const double* wv, int n) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (n != (int)w->w.joints.size()) throw ApiFail{CPGPU_ERR_INVALID_ARG, "joint count mismatch"};
+        begin_mutation(w->w);
+        for (int j = 0; j < n; j++) {
+            HJoint& x = w->w.joints[j];
+            for (int k = 0; k < kJMax; k++) if (impulse) x.impulse[k] = (float)impulse[kJMax * j + k];
+            for (int k = 0; k < 3; k++) { if (u) x.u[k] = (float)u[3 * j + k]; if (wv) x.w[k] = (float)wv[3 * j + k]; }
+        }
         return CPGPU_OK;
     });
 }

@@ -190,6 +190,12 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
     const int e1 = lower_bound_u64(d.e_new.key, ne, (uint64_t)e << 32);
     const int c0 = (e0 < ne) ? d.e_new.cstart[e0] : ncon;
     const int c1 = (e1 < ne) ? d.e_new.cstart[e1] : ncon;
+    // joint edges and joints of this world (row slots of the world start after
+    // the joints of the worlds before it)
+    const bool joints = d.n_joints > 0;
+    const int je0 = joints ? d.je.world_start[w] : 0, je1 = joints ? d.je.world_start[w + 1] : 0;
+    const int jj0 = joints ? d.je.world_jstart[w] : 0;
+    const int sys0 = joints ? d.hs_world_start[w] : 0;
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int i = s + tid; i < e; i += nt) { d.adj_cursor[i] = 0; d.visited[i] = -1; }
     for (int c = c0 + tid; c < c1; c += nt) d.row_of_contact[c] = -1;
@@ -200,9 +206,16 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
         if (d.movement[a] == 0) atomicAdd(&d.adj_cursor[a], 1);
         if (d.movement[b] == 0) atomicAdd(&d.adj_cursor[b], 1);
     }
+    for (int k = je0 + tid; k < je1; k += nt) {
+        uint64_t key = d.je.key[k];
+        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+        if (d.movement[a] == 0) atomicAdd(&d.adj_cursor[a], 1);
+        if (d.movement[b] == 0) atomicAdd(&d.adj_cursor[b], 1);
+    }
     __syncthreads();
-    // exclusive scan of the degrees into adjacency offsets (region starts at 2 * e0)
-    if (tid == 0) sh_carry = 2 * e0;
+    // exclusive scan of the degrees into adjacency offsets (region starts at
+    // 2 * (e0 + je0): two entries per contact or joint edge before this world)
+    if (tid == 0) sh_carry = 2 * (e0 + je0);
     __syncthreads();
     for (int base = s; base < e; base += nt) {
         int i = base + tid;
@@ -232,6 +245,15 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
         if (d.movement[b] == 0) { int slot = atomicAdd(&d.adj_cursor[b], 1); d.adj_list[2 * slot] = a; d.adj_list[2 * slot + 1] = k; }
     }
     __syncthreads();
+    // joint edges after the contact edges, marked -(index + 1); the sort below
+    // is stable, so a pair holding both kinds lists its contacts first
+    for (int k = je0 + tid; k < je1; k += nt) {
+        uint64_t key = d.je.key[k];
+        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+        if (d.movement[a] == 0) { int slot = atomicAdd(&d.adj_cursor[a], 1); d.adj_list[2 * slot] = b; d.adj_list[2 * slot + 1] = -(k + 1); }
+        if (d.movement[b] == 0) { int slot = atomicAdd(&d.adj_cursor[b], 1); d.adj_list[2 * slot] = a; d.adj_list[2 * slot + 1] = -(k + 1); }
+    }
+    __syncthreads();
     // each dynamic node's edges sorted by the other body's id (insertion sort)
     for (int i = s + tid; i < e; i += nt) {
         if (d.movement[i] != 0) continue;
@@ -246,13 +268,14 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
     }
     __syncthreads();
     if (tid == 0) {
-        int* stack = d.stack + 2 * e0 + s;
-        const int stack_cap = 2 * (e1 - e0) + (e - s);
-        int rc = c0, bc = s, ni = 0;
+        int* stack = d.stack + 2 * (e0 + je0) + s;
+        const int stack_cap = 2 * (e1 - e0 + je1 - je0) + (e - s);
+        int rc = c0 + jj0, bc = s, ni = 0, sc = sys0;
         for (int t = s; t < e; t++) {
             int node = d.map_order[t];
             if (d.movement[node] != 0 || d.visited[node] >= 0) continue;
-            int rs = rc, bs = bc, sp = 0;
+            int rs = rc, bs = bc, sp = 0, ss = sc;
+            bool has_joint = false;
             stack[sp++] = node;
             while (sp > 0) {
                 int cur = stack[--sp];
@@ -263,6 +286,19 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
                 for (int j = lo; j < hi; j++) {
                     int o = d.adj_list[2 * j], k = d.adj_list[2 * j + 1];
                     if (d.visited[o] >= 0) continue;
+                    if (k < 0) {
+                        // joint edge: its holonomic system joins the island's
+                        // list at first sight, then its joints' rows
+                        const int je = -k - 1, sy = d.je.sys[je];
+                        if (sy >= 0) {
+                            bool seen = false;
+                            for (int q = ss; q < sc; q++) seen |= d.isl_sys[q] == sy;
+                            if (!seen) d.isl_sys[sc++] = sy;
+                        }
+                        for (int q = d.je.jstart[je]; q < d.je.jstart[je] + d.je.jcount[je]; q++) d.row_contact[rc++] = -(q + 1);
+                        has_joint = true;
+                        continue;
+                    }
                     int cs = d.e_new.cstart[k], cn = d.e_new.ccount[k];
                     for (int c = cs; c < cs + cn; c++)
                         if (cs_live(d.c_new.state[c])) d.row_contact[rc++] = c;
@@ -281,9 +317,15 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
                 d.isl_body_start[s + ni] = bs;
                 d.isl_body_count[s + ni] = bc - bs;
                 d.isl_world[s + ni] = w;
+                if (joints) {
+                    d.isl_flags[s + ni] = has_joint ? 1 : 0;
+                    d.isl_sys_start[s + ni] = ss;
+                    d.isl_sys_count[s + ni] = sc - ss;
+                }
                 ni++;
             } else {
                 bc = bs;
+                sc = ss;
             }
         }
         d.isl_count_w[w] = ni;
@@ -291,8 +333,15 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
     }
     __syncthreads();
     const int rows_end = sh_rows_end;
-    for (int r = c0 + tid; r < rows_end; r += nt) {
+    for (int r = c0 + jj0 + tid; r < rows_end; r += nt) {
         int c = d.row_contact[r];
+        if (c < 0) {
+            const int j = -c - 1, a = d.jt.b1[j], b = d.jt.b2[j];
+            d.jt.rows[j].sa = (d.movement[a] == 0) ? d.visited[a] : -1;
+            d.jt.rows[j].sb = (d.movement[b] == 0) ? d.visited[b] : -1;
+            d.rows[r].contact = c;
+            continue;
+        }
         d.row_of_contact[c] = r;
         uint64_t key = d.e_new.key[d.c_new.edge[c]];
         int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
@@ -311,6 +360,11 @@ __global__ void k_island_copy(Dev d) {
             d.g_isl_body_start[o + k] = d.isl_body_start[s + k];
             d.g_isl_body_count[o + k] = d.isl_body_count[s + k];
             d.g_isl_world[o + k] = d.isl_world[s + k];
+            if (d.n_joints > 0) {
+                d.g_isl_flags[o + k] = d.isl_flags[s + k];
+                d.g_isl_sys_start[o + k] = d.isl_sys_start[s + k];
+                d.g_isl_sys_count[o + k] = d.isl_sys_count[s + k];
+            }
         }
     }
 }

@@ -1,0 +1,141 @@
+// joints.cuh — device helpers for joint rows (ball-socket, hinge) and the
+// holonomic block solve, shared by the row-building kernels (joints.cu) and
+// the joint-island PGS kernel (solver.cu).
+#pragma once
+#include "devmath.cuh"
+#include "layout.h"
+
+namespace cpgpu {
+
+constexpr float kJZero = 0.00000001f;   // NVec::isZero cutoff (Math/src/NVec.h:4)
+
+__device__ __forceinline__ bool jzero(const float* x, int n) {
+    for (int i = 0; i < n; i++)
+        if (fabsf(x[i]) > kJZero) return false;
+    return true;
+}
+
+// Δv slots of one island: 4 float4 per island body (v lin, v ang, pv lin, pv ang)
+__device__ __forceinline__ void jload(const float4* dv, int slot, int which, float* out) {
+    if (slot < 0) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
+    float4 l = dv[4 * slot + 2 * which], a = dv[4 * slot + 2 * which + 1];
+    out[0] = l.x; out[1] = l.y; out[2] = l.z; out[3] = a.x; out[4] = a.y; out[5] = a.z;
+}
+__device__ __forceinline__ void jadd(float4* dv, int slot, int which, const float* x) {
+    if (slot < 0) return;
+    float4& l = dv[4 * slot + 2 * which];
+    float4& a = dv[4 * slot + 2 * which + 1];
+    l.x += x[0]; l.y += x[1]; l.z += x[2];
+    a.x += x[3]; a.y += x[4]; a.z += x[5];
+}
+
+// J_a v_a + J_b v_b
+__device__ __forceinline__ void jvalue(const JointRow& R, const float* va, const float* vb, float* out) {
+    for (int i = 0; i < R.n; i++) {
+        float x = 0.f, y = 0.f;
+        for (int k = 0; k < 6; k++) x += va[k] * R.ja[6 * i + k];
+        for (int k = 0; k < 6; k++) y += vb[k] * R.jb[6 * i + k];
+        out[i] = x + y;
+    }
+}
+
+// impulse_to_velocity * imp added to both bodies' slots (`which` 0 = velocity,
+// 1 = pseudo velocity)
+__device__ __forceinline__ void japply(const JointRow& R, const float* imp, float4* dv, int which) {
+    float xa[6], xb[6];
+    for (int k = 0; k < 6; k++) {
+        float x = 0.f, y = 0.f;
+        for (int i = 0; i < R.n; i++) { x += imp[i] * R.ita[kJMax * k + i]; y += imp[i] * R.itb[kJMax * k + i]; }
+        xa[k] = x;
+        xb[k] = y;
+    }
+    jadd(dv, R.sa, which, xa);
+    jadd(dv, R.sb, which, xb);
+}
+
+// warm start (DegreedConstraint::applyWarmStartVelocityChange)
+__device__ __forceinline__ void jwarm(const JointRow& R, float4* dv) {
+    if (!jzero(R.impulse, R.n)) japply(R, R.impulse, dv, 0);
+}
+
+// PGSConstraintStep<n> (ConstraintSolver.cpp:12-40) of an equality row
+__device__ __forceinline__ void jstep(JointRow& R, float4* dv, bool pseudo) {
+    const int which = pseudo ? 1 : 0;
+    float va[6], vb[6], cur[kJMax], delta[kJMax], diff[kJMax];
+    jload(dv, R.sa, which, va);
+    jload(dv, R.sb, which, vb);
+    jvalue(R, va, vb, cur);
+    float* acc = pseudo ? R.pimpulse : R.impulse;
+    const float* tgt = pseudo ? R.ptarget : R.target;
+    for (int i = 0; i < R.n; i++) delta[i] = tgt[i] - cur[i];
+    for (int i = 0; i < R.n; i++) {
+        float x = 0.f;
+        for (int k = 0; k < R.n; k++) x += delta[k] * R.minv[kJMax * i + k];
+        diff[i] = (acc[i] + x) - acc[i];
+    }
+    if (!jzero(diff, R.n)) {
+        japply(R, diff, dv, which);
+        for (int i = 0; i < R.n; i++) acc[i] += diff[i];
+    }
+}
+
+// ---- holonomic systems (HolonomicBlockSolver.cpp) ------------------------------
+__device__ __forceinline__ int holo_loc(const int* table, int n, int row, int col) {
+    return table[row - col + ((2 * n + 1) * col - col * col) / 2];
+}
+
+// multInverseWithVector (HolonomicBlockSolver.cpp:251-317): v <- L^-T D^-1 L^-1 v.
+// `eff` holds `degree` scratch values.
+template <class T>
+__device__ void holo_solve(const HoloStore& hs, int s, const JointRow* rows, const T* B, T* v, T* eff) {
+    const int c0 = hs.cstart[s], n = hs.cstart[s + 1] - c0, deg = hs.degree[s];
+    const int* cons = hs.cons + c0;
+    const int* vp = hs.vpos + c0;
+    const int* table = hs.table + hs.tstart[s];
+    for (int col = 0; col + 1 < n; col++) {
+        const int bw = rows[cons[col]].n;
+        for (int row = col + 1; row < n; row++) {
+            const int l = holo_loc(table, n, row, col);
+            if (l < 0) continue;
+            const int bh = rows[cons[row]].n;
+            for (int i = 0; i < bh; i++) {
+                T x = 0;
+                for (int k = 0; k < bw; k++) x += B[l + i * bw + k] * v[vp[col] + k];
+                eff[vp[row] + i] = x;
+            }
+        }
+        // only rows below `col` were written this pass: subtract and clear them
+        for (int row = col + 1; row < n; row++) {
+            if (holo_loc(table, n, row, col) < 0) continue;
+            for (int i = 0; i < rows[cons[row]].n; i++) { v[vp[row] + i] -= eff[vp[row] + i]; eff[vp[row] + i] = 0; }
+        }
+    }
+    for (int col = 0; col < n; col++) {
+        const int w = rows[cons[col]].n, l = holo_loc(table, n, col, col);
+        T tmp[kJMax];
+        for (int i = 0; i < w; i++) {
+            T x = 0;
+            for (int k = 0; k < w; k++) x += B[l + i * w + k] * v[vp[col] + k];
+            tmp[i] = x;
+        }
+        for (int i = 0; i < w; i++) v[vp[col] + i] = tmp[i];
+    }
+    for (int col = n - 2; col >= 0; col--) {
+        const int bw = rows[cons[col]].n;
+        T e6[kJMax] = {0, 0, 0, 0, 0};
+        for (int row = col + 1; row < n; row++) {
+            const int l = holo_loc(table, n, row, col);
+            if (l < 0) continue;
+            const int bh = rows[cons[row]].n;
+            for (int i = 0; i < bw; i++) {
+                T dp = 0;
+                for (int j = 0; j < bh; j++) dp += v[vp[row] + j] * B[l + i + bw * j];
+                e6[i] += dp;
+            }
+        }
+        for (int i = 0; i < bw; i++) v[vp[col] + i] -= e6[i];
+    }
+    (void)deg;
+}
+
+}  // namespace cpgpu

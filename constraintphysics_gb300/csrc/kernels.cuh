@@ -34,6 +34,10 @@ void prepare_pgs(int dv_cap);
 int pgs_big_smem_bytes(int dv_cap);
 void launch_pgs(const Dev& d, int dv_cap, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, const Launch& L);
 void launch_integrate(const Dev& d, int last, const Launch& L);
+// joints: rows every substep, the holonomic systems' factorisation on the
+// first; islands with joint rows solved by their own kernel
+void launch_joint_rows(const Dev& d, bool first, const Launch& L);
+void launch_pgs_joint(const Dev& d, bool first, const Launch& L);
 // external state write: apply the staged state (d.stage); bodies whose pose
 // changed get their world inertia tensors and AABBs recomputed
 void launch_apply_state(const Dev& d, const Launch& L);

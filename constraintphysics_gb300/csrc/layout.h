@@ -67,7 +67,8 @@ struct WorldParams {
     int gyro_disabled;
     int warm_disabled;
     int pgs_vel, pgs_pos;
-    int pad[2];
+    int pgs_holo;                // holonomic block-solve iterations (first substep)
+    int pad;
 };
 
 // ---- status word bits ----------------------------------------------------------
@@ -123,6 +124,70 @@ struct alignas(16) RowBlock {
     float fminv[4];
 };
 static_assert(sizeof(RowBlock) == 384, "row block size");
+
+// One joint row per substep: DegreedConstraint<n> of a BallSocketConstraint
+// (n = 3) or HingeConstraint (n = 5) (ConstraintSolver.h:60-144), row-major,
+// sized for n = 5.
+constexpr int kJMax = 5;
+struct alignas(16) JointRow {
+    float ja[kJMax * 6], jb[kJMax * 6];     // [n][6]
+    float ita[6 * kJMax], itb[6 * kJMax];   // [6][n]
+    float itv[kJMax * kJMax], minv[kJMax * kJMax];
+    float target[kJMax], ptarget[kJMax];
+    float impulse[kJMax], pimpulse[kJMax], holo[kJMax];
+    int n, sa, sb;                          // island body slots (-1: infinite mass)
+    int pad;
+};
+
+// Static joint description (PhysicsEngine::addBallSocketConstraint /
+// addHingeConstraint): anchors are the tracked points relative to each body's
+// centre of mass in its body frame; hinge axes in body space.
+struct JointStore {
+    const int* b1;          // global body indices
+    const int* b2;
+    const int* n;           // 3 or 5
+    const float4* p1;       // xyz anchor on body 1
+    const float4* p2;
+    const float4* ax1;      // hinge axis (body 1 space)
+    const float4* ax2;
+    const float2* hard;     // pos / rot correction strength
+    float* impulse;         // [5] per joint: persistent warm-start impulse
+    float4* u;              // hinge basis of the last rebuild (HingeConstraint::u / w)
+    float4* w;
+    JointRow* rows;
+};
+
+// Joint edges (SharedConstraintsEdge with joints) sorted by key, per world;
+// their joints in insertion order; the holonomic system of the edge (or -1).
+struct JointEdgeStore {
+    const uint64_t* key;    // (global a) << 32 | global b, a < b
+    const int* jstart;
+    const int* jcount;
+    const int* sys;
+    const int* world_start; // [n_worlds + 1] joint-edge ranges
+    const int* world_jstart;// [n_worlds + 1] joint ranges (row-slot offsets)
+};
+
+// Holonomic systems (HolonomicSystem, HolonomicBlockSolver.cpp): constraint
+// order, block table and vector offsets built on the host; factor storage in
+// FP64 when the system's link-mass ratio exceeds 100, FP32 otherwise.
+struct HoloStore {
+    int n;                  // systems
+    const int* cstart;      // [n + 1] into cons / vpos
+    const int* cons;        // joint indices in elimination order
+    const int* vpos;        // vector offset of each constraint
+    const int* degree;
+    const int* tstart;      // [n + 1] into table
+    const int* table;       // block_location_table (-1 empty)
+    const int* bstart;      // offset into the FP32 or FP64 pool
+    const int* cap;         // block storage (the diagonal scratch follows)
+    const int* fp64;
+    const int* wstart;      // offset into the solve workspace (degree doubles)
+    float* pool32;
+    double* pool64;
+    double* work;
+    int* isl;               // island of the system in this step (-1 none)
+};
 
 struct Batch;  // host object, engine.cu
 
@@ -181,6 +246,20 @@ struct Dev {
     int* sched;                    // [0] n_big, [1] n_small, [2] big queue head, [32..63] bucket counts, [64..95] cursors
     int* cnt;                      // small device counters (merge totals)
     int* status;
+    // joints and holonomic systems (n_joints == 0: none in the batch)
+    int n_joints, n_joint_edges;
+    JointStore jt;
+    JointEdgeStore je;
+    HoloStore hs;
+    int* isl_flags;                // per world-region island: 1 = has joint rows
+    int* g_isl_flags;
+    int* isl_sys_start; int* isl_sys_count;        // per world-region island
+    int* g_isl_sys_start; int* g_isl_sys_count;
+    int* isl_sys;                  // system ids in discovery order (per-world region)
+    int* joint_list;               // joint islands (PGS scheduling), count in sched[3]
+    const int* hs_world_start;     // [n_worlds + 1] holonomic system ranges (island lists)
+    float lin_err_threshold;       // excessive_linear_error_torque_threshold
+    float4* dv_err;                // 4 float4 per island body: linearisation-error probe
 };
 
 }  // namespace cpgpu

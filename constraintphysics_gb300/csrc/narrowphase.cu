@@ -317,6 +317,19 @@ __device__ __forceinline__ void stage_hull(const uint8_t* g, uint8_t* s, const f
     hv->com = com;
 }
 
+// collisionAllowed (PhysicsEngine.cpp:570-572): bodies joined by a joint do
+// not collide; the joint-edge keys are sorted, so one binary search decides
+__device__ __forceinline__ bool jointed(const Dev& d, int a, int b) {
+    if (d.n_joint_edges == 0) return false;
+    const uint64_t k = ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
+    int lo = 0, hi = d.n_joint_edges;
+    while (lo < hi) {
+        int m = (lo + hi) >> 1;
+        if (d.je.key[m] < k) lo = m + 1; else hi = m;
+    }
+    return lo < d.n_joint_edges && d.je.key[lo] == k;
+}
+
 // cull_manifold (CollisionDetect.cpp:2795-2830) to at most 4 points and write
 // the pair's manifold
 __device__ void emit_manifold(const Dev& d, int p, f3 n, float maxpen, const float4* pts, const unsigned long long* magic, int m) {
@@ -854,7 +867,8 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
         // pairs with a sphere or cylinder belong to k_narrow_prim
         if ((reinterpret_cast<const HullHeader*>(ga)->kind | reinterpret_cast<const HullHeader*>(gb)->kind) != SHAPE_HULL) continue;
         // collision filter of PhysicsEngine.cpp:174 (at least one dynamic body)
-        if (!(d.movement[a] == 0 || d.movement[b] == 0)) {
+        // and collisionAllowed
+        if (!(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
             if (lane == 0) { d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f); d.mf_cnt[p] = 0; }
             continue;
         }
@@ -1058,7 +1072,7 @@ __global__ void __launch_bounds__(256) k_narrow_prim(Dev d, int slot_bytes) {
         const HullHeader* Hb = reinterpret_cast<const HullHeader*>(gb);
         const uint32_t ka = Ha->kind, kb = Hb->kind;
         if ((ka | kb) == SHAPE_HULL) continue;
-        if (!(d.movement[a] == 0 || d.movement[b] == 0)) {
+        if (!(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
             if (lane == 0) no_manifold(d, p);
             continue;
         }

@@ -22,6 +22,7 @@
 #include "kernels.cuh"
 #include "devmath.cuh"
 #include "shapes.cuh"
+#include "joints.cuh"
 
 namespace cpgpu {
 
@@ -249,6 +250,7 @@ __device__ __forceinline__ void row_pos(const RowBlock& R, float4& imp, float4* 
 __device__ void island_finish(const Dev& d, int rs, int rc, int bs, int bc, const float4* dv, int t, int nt) {
     for (int r = rs + t; r < rs + rc; r += nt) {
         const RowBlock& R = d.rows[r];
+        if (R.contact < 0) continue;   // joint row (k_pgs_joint writes those back)
         float4 imp = R.imp;
         d.c_new.imp[R.contact] = make_float4(imp.x, imp.z, imp.w, 0.f);
         int cst = d.c_new.state[R.contact];
@@ -278,6 +280,7 @@ __device__ __forceinline__ int size_bucket(int rows) { return 31 - __clz(rows); 
 __global__ void k_sched_count(Dev d) {
     const int ni = *d.n_islands;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
+        if (d.n_joints > 0 && d.g_isl_flags[i]) { d.joint_list[atomicAdd(&d.sched[3], 1)] = i; continue; }
         int rc = d.g_isl_row_count[i];
         if (rc >= kBigRows) atomicAdd(&d.sched[32 + size_bucket(rc)], 1);
         else d.small_list[atomicAdd(&d.sched[1], 1)] = i;
@@ -287,6 +290,7 @@ __global__ void k_sched_count(Dev d) {
 __global__ void k_sched_place(Dev d) {
     const int ni = *d.n_islands;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
+        if (d.n_joints > 0 && d.g_isl_flags[i]) continue;
         int rc = d.g_isl_row_count[i];
         if (rc < kBigRows) continue;
         int b = size_bucket(rc), off = 0;
@@ -452,6 +456,127 @@ __global__ void __launch_bounds__(32) k_pgs_big(Dev d, int dv_cap) {
     }
 }
 
+// HolonomicSystem::computeAndApplyImpulses (HolonomicBlockSolver.cpp:319-378)
+// for system s: solve A d = t - J dv with the factorisation, then (with a
+// threshold) discard a pseudo solution whose angular velocity change exceeds
+// it anywhere, else apply d.  Runs on one thread.
+template <class T>
+__device__ void holo_apply(const Dev& d, int s, float4* dv, float4* err, bool pseudo, float thr) {
+    const HoloStore& hs = d.hs;
+    const int c0 = hs.cstart[s], n = hs.cstart[s + 1] - c0, deg = hs.degree[s];
+    const int* cons = hs.cons + c0;
+    const int* vp = hs.vpos + c0;
+    const T* B = reinterpret_cast<const T*>(hs.fp64[s] ? (const void*)(hs.pool64 + hs.bstart[s])
+                                                       : (const void*)(hs.pool32 + hs.bstart[s]));
+    T* v = reinterpret_cast<T*>(hs.work + hs.wstart[s]);
+    T* eff = v + deg;
+    const int which = pseudo ? 1 : 0;
+    for (int i = 0; i < n; i++) {
+        const JointRow& R = d.jt.rows[cons[i]];
+        float va[6], vb[6], cur[kJMax];
+        jload(dv, R.sa, which, va);
+        jload(dv, R.sb, which, vb);
+        jvalue(R, va, vb, cur);
+        const float* tgt = pseudo ? R.ptarget : R.target;
+        for (int k = 0; k < R.n; k++) { v[vp[i] + k] = (T)tgt[k] - (T)cur[k]; eff[vp[i] + k] = 0; }
+    }
+    holo_solve<T>(hs, s, d.jt.rows, B, v, eff);
+    if (thr > 0.f) {
+        for (int i = 0; i < n; i++) {
+            const JointRow& R = d.jt.rows[cons[i]];
+            float ic[kJMax];
+            for (int k = 0; k < R.n; k++) ic[k] = (float)v[vp[i] + k];
+            if (!jzero(ic, R.n)) japply(R, ic, err, 0);
+        }
+        for (int i = 0; i < n; i++) {
+            const JointRow& R = d.jt.rows[cons[i]];
+            float ea[6], eb[6];
+            jload(err, R.sa, 0, ea);
+            jload(err, R.sb, 0, eb);
+            float r2 = 0.f;
+            for (int k = 3; k < 6; k++) r2 += ea[k] * ea[k] + eb[k] * eb[k];
+            if (r2 > thr * thr) return;
+        }
+    }
+    for (int i = 0; i < n; i++) {
+        JointRow& R = d.jt.rows[cons[i]];
+        float ic[kJMax];
+        for (int k = 0; k < R.n; k++) ic[k] = (float)v[vp[i] + k];
+        if (jzero(ic, R.n)) continue;
+        japply(R, ic, dv, which);
+        float* acc = pseudo ? R.pimpulse : R.holo;
+        for (int k = 0; k < R.n; k++) acc[k] += ic[k];
+    }
+}
+
+// islands with joint rows: one warp per island, the serial chain on lane 0
+// over contact rows and joint rows in island order, then the island's
+// holonomic systems (first substep); Δv and the linearisation probe in global
+// memory
+__global__ void __launch_bounds__(32) k_pgs_joint(Dev d, int first) {
+    const int lane = threadIdx.x;
+    const int nj = d.sched[3];
+    for (int q = blockIdx.x; q < nj; q += gridDim.x) {
+        const int i = d.joint_list[q];
+        const int rs = d.g_isl_row_start[i], rc = d.g_isl_row_count[i];
+        const int bs = d.g_isl_body_start[i], bc = d.g_isl_body_count[i];
+        const WorldParams& P = d.wparams[d.g_isl_world[i]];
+        float4* dv = d.dv + 4 * (size_t)bs;
+        float4* err = d.dv_err + 4 * (size_t)bs;
+        for (int k = lane; k < 4 * bc; k += 32) { dv[k] = make_float4(0.f, 0.f, 0.f, 0.f); err[k] = dv[k]; }
+        __syncwarp();
+        if (lane == 0) {
+            for (int r = rs; r < rs + rc; r++) {
+                const int c = d.rows[r].contact;
+                if (c >= 0) row_warm(d.rows[r], d.rows[r].imp, dv);
+                else jwarm(d.jt.rows[-c - 1], dv);
+            }
+            for (int it = 0; it < P.pgs_vel; it++)
+                for (int r = rs; r < rs + rc; r++) {
+                    RowBlock& R = d.rows[r];
+                    if (R.contact < 0) { jstep(d.jt.rows[-R.contact - 1], dv, false); continue; }
+                    float4 imp = R.imp;
+                    int st = R.stat;
+                    row_vel(R, imp, st, dv);
+                    R.imp = imp;
+                    R.stat = st;
+                }
+            for (int it = 0; it < P.pgs_pos; it++)
+                for (int r = rs; r < rs + rc; r++) {
+                    RowBlock& R = d.rows[r];
+                    if (R.contact < 0) { jstep(d.jt.rows[-R.contact - 1], dv, true); continue; }
+                    float4 imp = R.imp;
+                    row_pos(R, imp, dv);
+                    R.imp = imp;
+                }
+            if (first && P.pgs_holo > 0) {
+                const int ss = d.g_isl_sys_start[i], sn = d.g_isl_sys_count[i];
+                for (int it = 0; it < P.pgs_holo; it++)
+                    for (int k = 0; k < sn; k++) {
+                        const int s = d.isl_sys[ss + k];
+                        if (d.hs.fp64[s]) {
+                            holo_apply<double>(d, s, dv, err, false, -1.f);
+                            holo_apply<double>(d, s, dv, err, true, d.lin_err_threshold);
+                        } else {
+                            holo_apply<float>(d, s, dv, err, false, -1.f);
+                            holo_apply<float>(d, s, dv, err, true, d.lin_err_threshold);
+                        }
+                    }
+            }
+        }
+        __syncwarp();
+        for (int r = rs + lane; r < rs + rc; r += 32) {
+            const int c = d.rows[r].contact;
+            if (c >= 0) continue;
+            const int j = -c - 1;
+            const JointRow& R = d.jt.rows[j];
+            for (int k = 0; k < R.n; k++) d.jt.impulse[kJMax * j + k] = R.impulse[k];
+        }
+        island_finish(d, rs, rc, bs, bc, dv, lane, 32);
+        __syncwarp();
+    }
+}
+
 __device__ M33 crossm(f3 v) {
     M33 o;
     o.m[0] = 0.f;  o.m[1] = -v.z; o.m[2] = v.y;
@@ -576,6 +701,11 @@ void launch_pgs_schedule(const Dev& d, const Launch& L) {
     k_sched_reset<<<1, 96, 0, L.st>>>(d);
     k_sched_count<<<L.n_sms * 2, 256, 0, L.st>>>(d);
     k_sched_place<<<L.n_sms * 2, 256, 0, L.st>>>(d);
+}
+
+void launch_pgs_joint(const Dev& d, bool first, const Launch& L) {
+    if (d.n_joints == 0) return;
+    k_pgs_joint<<<L.n_sms * 8, 32, 0, L.st>>>(d, first ? 1 : 0);
 }
 
 void launch_pgs(const Dev& d, int dv_cap, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, const Launch& L) {

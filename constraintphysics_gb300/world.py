@@ -206,6 +206,21 @@ class World:
         self._check(self.abi.get_contacts(self.h, C.addressof(arr), n.value, C.addressof(n)))
         return contacts_to_numpy(arr, n.value)
 
+    def joint_state(self):
+        """Warm-start impulses (n x 5) and hinge bases u, w (n x 3) of the
+        joints in creation order."""
+        n = C.c_int()
+        self._check(self.abi.get_joint_state(self.h, None, None, None, C.addressof(n)))
+        imp, u, w = np.zeros((n.value, 5)), np.zeros((n.value, 3)), np.zeros((n.value, 3))
+        self._check(self.abi.get_joint_state(self.h, _ptr(imp), _ptr(u), _ptr(w), C.addressof(n)))
+        return {"impulse": imp, "u": u, "w": w}
+
+    def set_joint_state(self, st):
+        imp = np.ascontiguousarray(st["impulse"], dtype=np.float64)
+        u = np.ascontiguousarray(st["u"], dtype=np.float64)
+        w = np.ascontiguousarray(st["w"], dtype=np.float64)
+        self._check(self.abi.set_joint_state(self.h, _ptr(imp), _ptr(u), _ptr(w), int(imp.shape[0])))
+
     def set_contacts(self, cts):
         arr = numpy_to_contacts(cts)
         self._check(self.abi.set_contacts(self.h, C.addressof(arr), len(cts["b1"])))

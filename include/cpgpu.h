@@ -176,6 +176,14 @@ int cpgpu_get_contacts(cpgpu_world* w, cpgpu_contact* out, int cap, int* n);
 /* Replace the whole contact graph (a checkpoint restore).  Same layout and
  * order as cpgpu_get_contacts. */
 int cpgpu_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n);
+/* Warm-start state of the joints in creation order (the impulse of each
+ * BallSocketConstraint / HingeConstraint, PersistentConstraint.h:118-313, and
+ * a hinge's tangent basis u, w of its last rebuild): impulse 5 doubles per
+ * joint (3 used by a ball-socket), u and w 3 doubles each.  With the body
+ * state and the contacts this completes a checkpoint; no counterpart in the
+ * reference, which keeps these inside its constraint objects. */
+int cpgpu_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv, int* n);
+int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u, const double* wv, int n);
 
 /* ---- batched worlds ----------------------------------------------------- */
 /* Pack independent worlds into one device batch (segmented arrays) that one

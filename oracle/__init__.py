@@ -47,7 +47,8 @@ def _load(name, prefix):
         if not os.path.exists(path):
             raise FileNotFoundError(f"{path} is not built (run oracle.build())")
         lib = ctypes.CDLL(path)
-        _LIBS[name] = bind(lib, prefix, optional=("set_body_state", "set_contacts", "batch_create",
+        _LIBS[name] = bind(lib, prefix, optional=("set_body_state", "set_contacts", "get_joint_state",
+                                                  "set_joint_state", "batch_create",
                                                   "batch_destroy", "batch_step", "batch_get_body_state",
                                                   "batch_info"))
         _LIBS[name]._lib = lib

@@ -794,6 +794,34 @@ int cport_get_mass_properties(cpgpu_world* w, uint32_t id, double* mass, double*
     for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) tensor[3 * i + j] = b->ref_tensor.m[i][j];
     return CPGPU_OK;
 }
+// Joint warm-start state (same layout as cpgpu_get/set_joint_state)
+int cport_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv, int* n) {
+    World* x = W(w);
+    *n = (int)x->joints.size();
+    for (size_t j = 0; j < x->joints.size(); j++) {
+        const Joint& J = *x->joints[j];
+        for (int k = 0; k < kMaxDof; k++) if (impulse) impulse[kMaxDof * j + k] = k < J.n ? J.row.impulse[k] : 0.0;
+        if (u) { u[3 * j] = J.u.x; u[3 * j + 1] = J.u.y; u[3 * j + 2] = J.u.z; }
+        if (wv) { wv[3 * j] = J.w.x; wv[3 * j + 1] = J.w.y; wv[3 * j + 2] = J.w.z; }
+    }
+    return CPGPU_OK;
+}
+// Import: the impulses become the warm start of every joint's next rebuild
+// (the rebuild of the first substep for rows inside a holonomic system, which
+// the restatement otherwise takes from the end of the previous step, is
+// redone here from the current poses with the imported impulses).
+int cport_set_joint_state(cpgpu_world* w, const double* impulse, const double* u, const double* wv, int n) {
+    World* x = W(w);
+    if (n != (int)x->joints.size()) return fail("joint count mismatch");
+    for (int j = 0; j < n; j++) {
+        Joint& J = *x->joints[j];
+        for (int k = 0; k < J.n; k++) if (impulse) J.row.impulse[k] = impulse[kMaxDof * j + k];
+        if (u) J.u = V3(u[3 * j], u[3 * j + 1], u[3 * j + 2]);
+        if (wv) J.w = V3(wv[3 * j], wv[3 * j + 1], wv[3 * j + 2]);
+    }
+    if (x->p.pgs_holo > 0) x->updateHolonomicInverses();
+    return CPGPU_OK;
+}
 // Test hook: number of holonomic systems and the largest verifyInverse error
 // over them (factorisations as left by the last step).
 int cport_holonomic_check(cpgpu_world* w, int* n_systems, int* max_degree, double* max_err) {
@@ -888,8 +916,12 @@ int cport_get_contacts(cpgpu_world* w, cpgpu_contact* out, int cap, int* n) {
 // cport_get_contacts); edges without contacts are dropped.
 int cport_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n) {
     World* x = W(w);
+    // contacts are replaced; edges that carry joints stay (with their joints)
     std::vector<Edge*> all;
-    for (auto& e : x->edges) all.push_back(e.get());
+    for (auto& e : x->edges) {
+        e->contacts.clear();
+        if (e->joints.empty()) all.push_back(e.get());
+    }
     for (Edge* e : all) x->deleteEdge(e);
     for (int k = 0; k < n; k++) {
         const cpgpu_contact& r = in[k];

@@ -37,7 +37,7 @@ def test_oracle_libraries_export_the_world_api(oracle_mod, which):
     prefix = "cpref_" if which == "ref" else "cport_"
     # batches and the allocation-free pair entry point exist on the device path only
     batch_only = {n[len("cpgpu_"):] for n in declared() if n.startswith("cpgpu_batch_")} | {"pairs_noalloc"}
-    state_import = {"set_body_state", "set_contacts"}
+    state_import = {"set_body_state", "set_contacts", "get_joint_state", "set_joint_state"}
     for n in declared():
         short = n[len("cpgpu_"):]
         if short in batch_only or (which == "ref" and short in state_import):
