@@ -6,6 +6,8 @@ package only loads that library and wraps it for Python callers:
 
   world()            a new PhysicsEngine-like world (constraintphysics_gb300.world.World)
   Batch(worlds)      independent worlds packed into one device batch
+  Server(budget)     continuous-batching rollout server (requests = world + K steps)
+  clone(world)       a copy of a world that steps exactly as the original
 
 There is no CPU fallback: if the library is missing or no CUDA device is
 present, the calls raise.
@@ -37,6 +39,14 @@ def lib():
             "batch_write_state": [ctypes.c_void_p, ctypes.c_void_p],
             "batch_profile": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
             "batch_launches_per_step": [ctypes.c_void_p, ctypes.c_void_p],
+            "world_clone": [ctypes.c_void_p, ctypes.c_void_p],
+            "server_create": [ctypes.c_int64, ctypes.c_int, ctypes.c_void_p],
+            "server_destroy": [ctypes.c_void_p],
+            "server_submit": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p],
+            "server_advance": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
+            "server_poll": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p],
+            "server_stats": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                             ctypes.c_void_p],
         }
         for short, args in extra.items():
             fn = getattr(handle, "cpgpu_" + short)
@@ -126,6 +136,80 @@ class Batch:
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
             self.abi.batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def clone(w):
+    """A copy of world `w` (cpgpu_world_clone)."""
+    abi = lib()
+    h = ctypes.c_void_p()
+    rc = abi.world_clone(w.h, ctypes.addressof(h))
+    if rc != 0:
+        raise CPGPUError(f"status {rc}: {abi.last_error().decode(errors='replace')}")
+    c = World.__new__(World)
+    c.abi = abi
+    c.h = h
+    c.n_bodies = getattr(w, "n_bodies", 0)
+    return c
+
+
+class Server:
+    """Continuous-batching rollout server (cpgpu_server_*): submit(world, K)
+    returns a token; advance(n) runs up to n batch steps, admitting waiting
+    requests under the device-memory budget and re-forming the batch as
+    requests complete; poll() returns the tokens completed since the last
+    call, whose worlds then hold their final state."""
+
+    def __init__(self, budget_bytes, epoch_steps=10):
+        self.abi = lib()
+        self.h = ctypes.c_void_p()
+        self._check(self.abi.server_create(int(budget_bytes), int(epoch_steps), ctypes.addressof(self.h)))
+        self._worlds = {}
+
+    def _check(self, rc):
+        if rc != 0:
+            raise CPGPUError(f"status {rc}: {self.abi.last_error().decode(errors='replace')}")
+
+    def submit(self, w, steps):
+        tok = ctypes.c_uint64()
+        self._check(self.abi.server_submit(self.h, w.h, int(steps), ctypes.addressof(tok)))
+        self._worlds[tok.value] = w   # keep the world alive while it is served
+        return tok.value
+
+    def advance(self, max_steps):
+        r, q = ctypes.c_int(), ctypes.c_int()
+        self._check(self.abi.server_advance(self.h, int(max_steps), ctypes.addressof(r), ctypes.addressof(q)))
+        return r.value, q.value
+
+    def poll(self):
+        out = []
+        buf = (ctypes.c_uint64 * 4096)()
+        n = ctypes.c_int()
+        while True:
+            self._check(self.abi.server_poll(self.h, ctypes.addressof(buf), 4096, ctypes.addressof(n)))
+            out.extend(buf[i] for i in range(n.value))
+            if n.value < 4096:
+                break
+        for t in out:
+            self._worlds.pop(t, None)
+        return out
+
+    def stats(self):
+        bs, rf, ms, db, rb = (ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64())
+        self._check(self.abi.server_stats(self.h, ctypes.addressof(bs), ctypes.addressof(rf), ctypes.addressof(ms),
+                                          ctypes.addressof(db), ctypes.addressof(rb)))
+        return {"body_steps": bs.value, "reforms": rf.value, "reform_ms": ms.value, "device_bytes": db.value,
+                "running_bodies": rb.value}
+
+    def close(self):
+        if self.h:
+            self.abi.server_destroy(self.h)
             self.h = None
 
     def __del__(self):

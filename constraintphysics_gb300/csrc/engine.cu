@@ -8,6 +8,8 @@
 // back, change the host mirror and re-upload on the next step.  A batch packs
 // many worlds into one set of segmented device arrays.
 #include <algorithm>
+#include <chrono>
+#include <deque>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -285,10 +287,12 @@ struct Batch {
     cudaEvent_t fork = nullptr, join = nullptr;
     int dv_cap = 64;                   // island bodies whose Δv fits in shared memory
     uint8_t* mem = nullptr;
+    size_t bytes = 0;                  // device arena size
     Dev d[2];                  // d[p]: old = buffer p, new = buffer 1-p
     int parity = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     std::vector<int> world_start;
+    std::vector<int> world_jstart;     // joint ranges of the worlds
     std::vector<uint8_t> movement;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -711,6 +715,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         hs_wstart.push_back((int)hs_degree.size());
     }
     const int n_joints = (int)j_b1.size(), n_je = (int)je_key.size(), n_sys = (int)hs_degree.size();
+    B->world_jstart = je_wjstart;
     B->joints = n_joints > 0;
     B->systems = n_sys > 0;
 
@@ -828,6 +833,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     Arena measure{nullptr, 0, 0};
     carve(measure);
     const size_t bytes = measure.used + 256;
+    B->bytes = bytes;
     CK(cudaMalloc(&B->mem, bytes));
     Arena A{B->mem, bytes, 0};
     carve(A);
@@ -897,11 +903,13 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
 }
 
 // ---------------------------------------------------------------- world helpers ----
-static void download_state(World& w) {
-    if (!w.dev || !w.dev_valid) return;
-    Batch& B = *w.dev;
+// Pull the device state of the batch's worlds into their host mirrors: poses,
+// velocities, world inertia tensors, joint warm starts, the persistent contact
+// graph (dead contacts dropped, as the next merge would) and the last pair
+// list.  All arrays are read once and split per world.
+static void download_worlds(Batch& B, const std::vector<World*>& ws) {
     const Dev& x = B.cur();
-    int N = B.n_bodies;
+    const int N = B.n_bodies;
     std::vector<float4> pos(N), rot(N), vel(N), angv(N);
     std::vector<float> iw(9 * (size_t)N), iinv(9 * (size_t)N);
     CK(cudaMemcpyAsync(pos.data(), x.pos, N * 16, cudaMemcpyDeviceToHost, B.st));
@@ -912,33 +920,15 @@ static void download_state(World& w) {
     CK(cudaMemcpyAsync(iinv.data(), x.iinv, iinv.size() * 4, cudaMemcpyDeviceToHost, B.st));
     int counts[6];
     CK(cudaMemcpyAsync(counts, x.n_pairs, sizeof(counts), cudaMemcpyDeviceToHost, B.st));
+    const int nj = x.n_joints;
+    std::vector<float> jimp((size_t)kJMax * nj);
+    std::vector<float4> ju(nj), jw(nj);
+    if (nj > 0) {
+        CK(cudaMemcpyAsync(jimp.data(), x.jt.impulse, jimp.size() * 4, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(ju.data(), x.jt.u, nj * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(jw.data(), x.jt.w, nj * 16, cudaMemcpyDeviceToHost, B.st));
+    }
     CK(cudaStreamSynchronize(B.st));
-    for (int i = 0; i < N; i++) {
-        Body& b = w.bodies[i];
-        b.com = D3(pos[i].x, pos[i].y, pos[i].z);
-        b.q = Quat{rot[i].x, rot[i].y, rot[i].z, rot[i].w};
-        if (b.movement != CPGPU_FIXED) {
-            b.vel = D3(vel[i].x, vel[i].y, vel[i].z);
-            b.angv = D3(angv[i].x, angv[i].y, angv[i].z);
-        }
-        if (b.movement == CPGPU_DYNAMIC)
-            for (int k = 0; k < 9; k++) { b.iw[k] = iw[9 * (size_t)i + k]; b.iinv[k] = iinv[9 * (size_t)i + k]; }
-    }
-    // joints' warm-start impulses and hinge bases
-    if (!w.joints.empty() && x.n_joints > 0) {
-        const int nj = x.n_joints;
-        std::vector<float> imp((size_t)kJMax * nj);
-        std::vector<float4> u(nj), wv(nj);
-        CK(cudaMemcpyAsync(imp.data(), x.jt.impulse, imp.size() * 4, cudaMemcpyDeviceToHost, B.st));
-        CK(cudaMemcpyAsync(u.data(), x.jt.u, nj * 16, cudaMemcpyDeviceToHost, B.st));
-        CK(cudaMemcpyAsync(wv.data(), x.jt.w, nj * 16, cudaMemcpyDeviceToHost, B.st));
-        CK(cudaStreamSynchronize(B.st));
-        for (int j = 0; j < nj && j < (int)w.joints.size(); j++) {
-            for (int k = 0; k < kJMax; k++) w.joints[j].impulse[k] = imp[(size_t)kJMax * j + k];
-            w.joints[j].u[0] = u[j].x; w.joints[j].u[1] = u[j].y; w.joints[j].u[2] = u[j].z;
-            w.joints[j].w[0] = wv[j].x; w.joints[j].w[1] = wv[j].y; w.joints[j].w[2] = wv[j].z;
-        }
-    }
     // contact graph (current = the old buffers of the next step)
     const int ne = *(&counts[1] + B.parity), nc = *(&counts[3] + B.parity);
     std::vector<uint64_t> key(ne), mag(nc);
@@ -968,31 +958,66 @@ static void download_state(World& w) {
         CK(cudaMemcpyAsync(pb.data(), x.pair_b, np * 4, cudaMemcpyDeviceToHost, B.st));
     }
     CK(cudaStreamSynchronize(B.st));
-    w.contacts.clear();
-    for (int e = 0; e < ne; e++) {
-        uint32_t b1 = (uint32_t)(key[e] >> 32) + 1, b2 = (uint32_t)(key[e] & 0xffffffffu) + 1;
-        for (int k = cstart[e]; k < cstart[e] + ccount[e]; k++) {
-            if (cs_dead(state[k])) continue;
-            cpgpu_contact c;
-            std::memset(&c, 0, sizeof(c));
-            c.b1 = b1; c.b2 = b2;
-            c.live = cs_live(state[k]);
-            c.memory_life = cs_life(state[k]);
-            c.magic_c = ((uint64_t)b2 << 32) | b1;
-            c.magic_b = mag[k];
-            c.p_local_b1[0] = p1[k].x; c.p_local_b1[1] = p1[k].y; c.p_local_b1[2] = p1[k].z;
-            c.p_local_b2[0] = p2[k].x; c.p_local_b2[1] = p2[k].y; c.p_local_b2[2] = p2[k].z;
-            c.n_local_b1[0] = n[k].x; c.n_local_b1[1] = n[k].y; c.n_local_b1[2] = n[k].z;
-            c.pen_depth = p1[k].w; c.bounce = p2[k].w; c.friction_coeff = n[k].w;
-            c.normal_impulse = imp[k].x; c.friction_impulse[0] = imp[k].y; c.friction_impulse[1] = imp[k].z;
-            c.friction_u[0] = fu[k].x; c.friction_u[1] = fu[k].y; c.friction_u[2] = fu[k].z;
-            c.friction_w[0] = fw[k].x; c.friction_w[1] = fw[k].y; c.friction_w[2] = fw[k].z;
-            c.static_ready = cs_static(state[k]);
-            w.contacts.push_back(c);
+    int e_cursor = 0, p_cursor = 0;
+    for (size_t wi = 0; wi < ws.size(); wi++) {
+        World& w = *ws[wi];
+        const int s0 = B.world_start[wi], s1 = B.world_start[wi + 1];
+        for (int i = s0; i < s1; i++) {
+            Body& b = w.bodies[i - s0];
+            b.com = D3(pos[i].x, pos[i].y, pos[i].z);
+            b.q = Quat{rot[i].x, rot[i].y, rot[i].z, rot[i].w};
+            if (b.movement != CPGPU_FIXED) {
+                b.vel = D3(vel[i].x, vel[i].y, vel[i].z);
+                b.angv = D3(angv[i].x, angv[i].y, angv[i].z);
+            }
+            if (b.movement == CPGPU_DYNAMIC)
+                for (int k = 0; k < 9; k++) { b.iw[k] = iw[9 * (size_t)i + k]; b.iinv[k] = iinv[9 * (size_t)i + k]; }
+        }
+        if (nj > 0) {
+            const int j0 = B.world_jstart[wi];
+            for (size_t j = 0; j < w.joints.size(); j++) {
+                const size_t g = (size_t)j0 + j;
+                for (int k = 0; k < kJMax; k++) w.joints[j].impulse[k] = jimp[kJMax * g + k];
+                w.joints[j].u[0] = ju[g].x; w.joints[j].u[1] = ju[g].y; w.joints[j].u[2] = ju[g].z;
+                w.joints[j].w[0] = jw[g].x; w.joints[j].w[1] = jw[g].y; w.joints[j].w[2] = jw[g].z;
+            }
+        }
+        w.contacts.clear();
+        for (; e_cursor < ne && (int)(key[e_cursor] >> 32) < s1; e_cursor++) {
+            const int e = e_cursor;
+            uint32_t b1 = (uint32_t)((key[e] >> 32) - s0) + 1, b2 = (uint32_t)((key[e] & 0xffffffffu) - s0) + 1;
+            for (int k = cstart[e]; k < cstart[e] + ccount[e]; k++) {
+                if (cs_dead(state[k])) continue;
+                cpgpu_contact c;
+                std::memset(&c, 0, sizeof(c));
+                c.b1 = b1; c.b2 = b2;
+                c.live = cs_live(state[k]);
+                c.memory_life = cs_life(state[k]);
+                c.magic_c = ((uint64_t)b2 << 32) | b1;
+                c.magic_b = mag[k];
+                c.p_local_b1[0] = p1[k].x; c.p_local_b1[1] = p1[k].y; c.p_local_b1[2] = p1[k].z;
+                c.p_local_b2[0] = p2[k].x; c.p_local_b2[1] = p2[k].y; c.p_local_b2[2] = p2[k].z;
+                c.n_local_b1[0] = n[k].x; c.n_local_b1[1] = n[k].y; c.n_local_b1[2] = n[k].z;
+                c.pen_depth = p1[k].w; c.bounce = p2[k].w; c.friction_coeff = n[k].w;
+                c.normal_impulse = imp[k].x; c.friction_impulse[0] = imp[k].y; c.friction_impulse[1] = imp[k].z;
+                c.friction_u[0] = fu[k].x; c.friction_u[1] = fu[k].y; c.friction_u[2] = fu[k].z;
+                c.friction_w[0] = fw[k].x; c.friction_w[1] = fw[k].y; c.friction_w[2] = fw[k].z;
+                c.static_ready = cs_static(state[k]);
+                w.contacts.push_back(c);
+            }
+        }
+        w.last_pairs.clear();
+        for (; p_cursor < np && pa[p_cursor] < s1; p_cursor++) {
+            w.last_pairs.push_back((uint32_t)(pa[p_cursor] - s0) + 1);
+            w.last_pairs.push_back((uint32_t)(pb[p_cursor] - s0) + 1);
         }
     }
-    w.last_pairs.clear();
-    for (int i = 0; i < np; i++) { w.last_pairs.push_back((uint32_t)pa[i] + 1); w.last_pairs.push_back((uint32_t)pb[i] + 1); }
+}
+
+static void download_state(World& w) {
+    if (!w.dev || !w.dev_valid) return;
+    std::vector<World*> one{&w};
+    download_worlds(*w.dev, one);
 }
 
 // Pull device state into the host mirror and mark the device copy stale, so the
@@ -1600,6 +1625,191 @@ int cpgpu_batch_step_timed(cpgpu_batch* b, int n, double* device_ms) {
         if (device_ms) *device_ms = ms;
         return B.check_status();
     });
+}
+
+// ------------------------------------------------------------------ serving ----
+int cpgpu_world_clone(cpgpu_world* src, cpgpu_world** out) {
+    W_OR_FAIL(src);
+    return guarded([&] {
+        if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null out"};
+        if (src->w.dev && src->w.dev_valid) download_state(src->w);
+        auto c = std::make_unique<cpgpu_world>();
+        c->w.p = src->w.p;
+        c->w.shapes = src->w.shapes;
+        c->w.bodies = src->w.bodies;
+        c->w.joints = src->w.joints;
+        c->w.contacts = src->w.contacts;
+        c->w.last_pairs = src->w.last_pairs;
+        // same insert sequence, so the same iteration order
+        for (size_t i = 0; i < src->w.bodies.size(); i++) c->w.nodes[(unsigned)(i + 1)] = (int)i;
+        *out = c.release();
+        return CPGPU_OK;
+    });
+}
+
+}  // extern "C"
+
+namespace cpgpu {
+
+struct ServerRequest {
+    World* w = nullptr;
+    int remaining = 0;
+    uint64_t token = 0;
+    int64_t bodies = 0;
+    size_t bytes = 0;   // estimated device bytes
+};
+
+struct Server {
+    int64_t budget = 0;
+    int epoch_steps = 10;
+    double bytes_per_body = 2048;     // updated from every batch built
+    std::deque<ServerRequest> waiting;
+    std::vector<ServerRequest> running;   // in batch order
+    std::unique_ptr<Batch> batch;
+    std::vector<uint64_t> done;
+    int since_reform = 0;
+    uint64_t next_token = 1;
+    int64_t body_steps = 0, reforms = 0;
+    double reform_ms = 0;
+
+    size_t estimate(const World& w) const { return (size_t)(bytes_per_body * (double)w.bodies.size()) + (1u << 20); }
+
+    void reform() {
+        auto t0 = std::chrono::steady_clock::now();
+        if (batch) {
+            std::vector<World*> ws;
+            for (auto& r : running) ws.push_back(r.w);
+            download_worlds(*batch, ws);
+            batch.reset();
+        }
+        std::vector<ServerRequest> keep;
+        for (auto& r : running) {
+            if (r.remaining <= 0) done.push_back(r.token);
+            else keep.push_back(r);
+        }
+        running.swap(keep);
+        size_t used = 0;
+        for (auto& r : running) used += r.bytes;
+        while (!waiting.empty()) {
+            ServerRequest& r = waiting.front();
+            r.bytes = estimate(*r.w);
+            if (!running.empty() && used + r.bytes > (size_t)budget) break;
+            used += r.bytes;
+            running.push_back(r);
+            waiting.pop_front();
+        }
+        if (!running.empty()) {
+            std::vector<World*> ws;
+            for (auto& r : running) ws.push_back(r.w);
+            batch = build_batch(ws);
+            int64_t nb = 0;
+            for (auto& r : running) nb += r.bodies;
+            if (nb > 0) bytes_per_body = (double)batch->bytes / (double)nb;
+            for (auto& r : running) r.bytes = estimate(*r.w);
+        }
+        since_reform = 0;
+        reforms++;
+        reform_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+
+    int advance(int max_steps) {
+        int stepped = 0;
+        while (stepped < max_steps) {
+            bool finished = false;
+            for (auto& r : running) finished |= r.remaining <= 0;
+            const bool want = !waiting.empty() && (running.empty() || since_reform >= epoch_steps);
+            if (finished || want || (!batch && !running.empty())) reform();
+            if (running.empty()) break;
+            int n = max_steps - stepped;
+            for (auto& r : running) n = std::min(n, r.remaining);
+            if (!waiting.empty()) n = std::min(n, std::max(1, epoch_steps - since_reform));
+            batch->step(n);
+            int code = batch->check_status();
+            (void)code;
+            for (auto& r : running) { r.remaining -= n; body_steps += (int64_t)n * r.bodies; }
+            stepped += n;
+            since_reform += n;
+        }
+        // hand back requests that completed in the last stretch
+        bool finished = false;
+        for (auto& r : running) finished |= r.remaining <= 0;
+        if (finished) reform();
+        return stepped;
+    }
+};
+
+}  // namespace cpgpu
+
+struct cpgpu_server { cpgpu::Server s; };
+
+extern "C" {
+
+int cpgpu_server_create(int64_t hbm_budget_bytes, int epoch_steps, cpgpu_server** out) {
+    return guarded([&] {
+        if (!out || hbm_budget_bytes <= 0 || epoch_steps < 1) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad server arguments"};
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw ApiFail{CPGPU_ERR_NO_DEVICE, "no CUDA device"};
+        auto s = std::make_unique<cpgpu_server>();
+        s->s.budget = hbm_budget_bytes;
+        s->s.epoch_steps = epoch_steps;
+        *out = s.release();
+        return CPGPU_OK;
+    });
+}
+int cpgpu_server_destroy(cpgpu_server* s) { delete s; return CPGPU_OK; }
+
+int cpgpu_server_submit(cpgpu_server* s, cpgpu_world* w, int steps, uint64_t* token) {
+    if (!s || !w) return fail(CPGPU_ERR_INVALID_ARG, "null server or world");
+    return guarded([&] {
+        if (steps < 0) throw ApiFail{CPGPU_ERR_INVALID_ARG, "negative step count"};
+        if (w->w.bodies.empty()) throw ApiFail{CPGPU_ERR_INVALID_ARG, "empty world"};
+        if (w->w.dev && w->w.dev_valid) download_state(w->w);
+        w->w.dev_valid = false;
+        cpgpu::ServerRequest r;
+        r.w = &w->w;
+        r.remaining = steps;
+        r.token = s->s.next_token++;
+        r.bodies = 0;
+        for (const auto& b : w->w.bodies) r.bodies += b.movement == CPGPU_DYNAMIC;
+        s->s.waiting.push_back(r);
+        if (token) *token = r.token;
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_server_advance(cpgpu_server* s, int max_steps, int* n_running, int* n_waiting) {
+    if (!s) return fail(CPGPU_ERR_INVALID_ARG, "null server");
+    return guarded([&] {
+        s->s.advance(max_steps);
+        if (n_running) *n_running = (int)s->s.running.size();
+        if (n_waiting) *n_waiting = (int)s->s.waiting.size();
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_server_poll(cpgpu_server* s, uint64_t* tokens, int cap, int* n) {
+    if (!s || !n) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
+    auto& d = s->s.done;
+    int k = std::min((int)d.size(), cap);
+    for (int i = 0; i < k; i++) if (tokens) tokens[i] = d[i];
+    d.erase(d.begin(), d.begin() + k);
+    *n = k;
+    return CPGPU_OK;
+}
+
+int cpgpu_server_stats(cpgpu_server* s, int64_t* body_steps, int64_t* reforms, double* reform_ms, int64_t* device_bytes,
+                       int64_t* running_bodies) {
+    if (!s) return fail(CPGPU_ERR_INVALID_ARG, "null server");
+    if (body_steps) *body_steps = s->s.body_steps;
+    if (reforms) *reforms = s->s.reforms;
+    if (reform_ms) *reform_ms = s->s.reform_ms;
+    if (device_bytes) *device_bytes = s->s.batch ? (int64_t)s->s.batch->bytes : 0;
+    if (running_bodies) {
+        int64_t nb = 0;
+        for (auto& r : s->s.running) nb += r.bodies;
+        *running_bodies = nb;
+    }
+    return CPGPU_OK;
 }
 
 }  // extern "C"

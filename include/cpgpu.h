@@ -242,6 +242,37 @@ int cpgpu_batch_launches_per_step(cpgpu_batch* b, int* n);
  * all the scratch it reads. */
 int cpgpu_pairs_noalloc(const float* aabbs, int n_bodies, uint32_t* pairs, int cap, int* count, void* stream);
 
+/* ---- serving ------------------------------------------------------------- */
+/* A copy of a world (bodies, shapes, joints, parameters, contact graph, the
+ * same node-map order); the copy steps exactly as the original would.  For
+ * rollout services that instantiate many requests from a few templates.  No
+ * counterpart in the reference. */
+int cpgpu_world_clone(cpgpu_world* src, cpgpu_world** out);
+
+/* Continuous-batching rollout server (no counterpart in the reference).  A
+ * request is a world plus a number of steps.  Requests wait in arrival order
+ * until their estimated device memory fits the budget next to the running
+ * ones; the running requests are stepped together as one batch (one launch
+ * sequence per step), their state resident on the device between admission
+ * points.  The batch is re-formed when a request completes, or when requests
+ * are waiting and `epoch_steps` steps have passed since the last re-form; a
+ * completed request's final state is written back into its world, which the
+ * caller then reads as usual.  Each request's result equals stepping its
+ * world alone.  The caller must not touch a submitted world until its token
+ * is returned by cpgpu_server_poll. */
+typedef struct cpgpu_server cpgpu_server;
+int cpgpu_server_create(int64_t hbm_budget_bytes, int epoch_steps, cpgpu_server** out);
+int cpgpu_server_destroy(cpgpu_server* s);
+int cpgpu_server_submit(cpgpu_server* s, cpgpu_world* w, int steps, uint64_t* token);
+/* Run up to max_steps batch steps (fewer when nothing is running). */
+int cpgpu_server_advance(cpgpu_server* s, int max_steps, int* n_running, int* n_waiting);
+/* Tokens of requests completed since the last poll. */
+int cpgpu_server_poll(cpgpu_server* s, uint64_t* tokens, int cap, int* n);
+/* Totals: body-steps advanced, batch re-forms and their host time (ms),
+ * device bytes of the current batch, bodies running. */
+int cpgpu_server_stats(cpgpu_server* s, int64_t* body_steps, int64_t* reforms, double* reform_ms,
+                       int64_t* device_bytes, int64_t* running_bodies);
+
 /* ---- diagnostics -------------------------------------------------------- */
 /* Last error message of this thread (static storage, never NULL). */
 const char* cpgpu_last_error(void);

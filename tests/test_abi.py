@@ -36,7 +36,8 @@ def test_oracle_libraries_export_the_world_api(oracle_mod, which):
     abi = oracle_mod.ref_abi() if which == "ref" else oracle_mod.port_abi()
     prefix = "cpref_" if which == "ref" else "cport_"
     # batches and the allocation-free pair entry point exist on the device path only
-    batch_only = {n[len("cpgpu_"):] for n in declared() if n.startswith("cpgpu_batch_")} | {"pairs_noalloc"}
+    batch_only = {n[len("cpgpu_"):] for n in declared()
+                  if n.startswith(("cpgpu_batch_", "cpgpu_server_"))} | {"pairs_noalloc", "world_clone"}
     state_import = {"set_body_state", "set_contacts", "get_joint_state", "set_joint_state"}
     for n in declared():
         short = n[len("cpgpu_"):]
