@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="build the batch, run warmup + steps, no extras")
+    ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of each serving run (0: none)")
+    ap.add_argument("--serve-rates", default="2000,20", help="Poisson request rates (requests/s) of the serving runs")
     return ap.parse_args()
 
 
@@ -164,6 +166,58 @@ def algorithmic_bytes(stage, counts, nbodies, vfe, params):
     if stage == "pairs":
         return nbodies * 32 + npairs * 8
     return None
+
+
+def run_serving(cg, rates, duration, seed, budget_bytes=150 << 30, epoch_steps=10, n_templates=48):
+    """Serving workload: Poisson arrivals; each request is a world of
+    floor(exp(U[ln 16, ln 2048])) bodies (pile or pyramid, generated as the
+    batched workload) advanced K ~ U{30..300} steps, admitted under the
+    device-memory budget into the continuously re-formed batch.  Requests are
+    cloned from a pool of seeded template worlds.  Latency = completion minus
+    arrival (wall clock)."""
+    rng = np.random.default_rng(seed + 4242)
+    pool = scenes.HullPool(seed + 5, size=128)
+    temps = []
+    for _ in range(n_templates):
+        w = cg.world()
+        scenes.apply(scenes.batched_world(rng, pool, 16, 2048), w)
+        temps.append(w)
+    out = []
+    for rate in rates:
+        srv = cg.Server(budget_bytes, epoch_steps)
+        arr, t = [], 0.0
+        while True:
+            t += rng.exponential(1.0 / rate)
+            if t > duration:
+                break
+            arr.append(t)
+        meta, lat, offered, i = {}, [], 0, 0
+        start = time.perf_counter()
+        while True:
+            now = time.perf_counter() - start
+            while i < len(arr) and arr[i] <= now:
+                tmp = temps[int(rng.integers(len(temps)))]
+                k = int(rng.integers(30, 301))
+                meta[srv.submit(cg.clone(tmp), k)] = arr[i]
+                offered += k * (tmp.n_bodies - 1)
+                i += 1
+            if now > duration:
+                break
+            srv.advance(5)
+            tn = time.perf_counter() - start
+            for tok in srv.poll():
+                lat.append(tn - meta.pop(tok))
+        wall = time.perf_counter() - start
+        st = srv.stats()
+        srv.close()
+        lat = np.array(lat) if lat else np.zeros(1)
+        out.append({"rate_per_s": rate, "duration_s": duration, "arrived": len(arr), "completed": int(len(lat)),
+                    "offered_body_steps_per_s": offered / duration, "served_body_steps_per_s": st["body_steps"] / wall,
+                    "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                    "reforms": st["reforms"], "reform_s": st["reform_ms"] / 1e3,
+                    "device_gb": st["device_bytes"] / 1e9, "running_bodies_at_end": st["running_bodies"],
+                    "budget_gb": budget_bytes / 1e9})
+    return out
 
 
 def run_reference_sample(ws_scenes, warmup, steps, budget_s, threads):
@@ -328,6 +382,13 @@ def main():
             b1.close()
         plain = total_bs / (total_ms / 1e3)
 
+    serving = None
+    launches = batch.launches_per_step() * a.steps
+    batch_bodies = batch.n_bodies
+    if a.serve_seconds > 0 and rank == 0:
+        batch.close()
+        serving = run_serving(cg, [float(r) for r in a.serve_rates.split(",") if r], a.serve_seconds, a.seed)
+
     cpu = None
     if not a.no_cpu and rank == 0:
         bsps, sample, wall = run_reference_sample(ws_scenes, a.warmup, a.steps, a.cpu_budget_s, threads)
@@ -337,14 +398,14 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": dev_ms / a.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
-                "config": dict(config, l2="state larger than L2 (%.0f MB resident)" % (batch.n_bodies * 600 / 1e6),
+                "config": dict(config, l2="state larger than L2 (%.0f MB resident)" % (batch_bodies * 600 / 1e6),
                                contacts=info["contacts"]),
                 "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
                 "plain": {"value": plain, "unit": UNIT, "sample_worlds": a.plain_sample,
                           "vs_plain": (value / world_size / plain) if plain else None},
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-                "gpu_launches": batch.launches_per_step() * a.steps,
-                "stage_ms": stage_ms, "counts": counts, "setup_s": setup_s}
+                "gpu_launches": launches,
+                "stage_ms": stage_ms, "counts": counts, "setup_s": setup_s, "serving": serving}
         print(json.dumps(line), flush=True)
 
 

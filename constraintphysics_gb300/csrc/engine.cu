@@ -1014,6 +1014,109 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
     }
 }
 
+// The state of some of the batch's worlds (indices `widx`) into their host
+// mirrors, reading only their ranges: bodies, joints, and their contacts via
+// the per-world edge / contact ranges of the current graph.
+static void download_subset(Batch& B, const std::vector<int>& widx, const std::vector<World*>& ws) {
+    const Dev& x = B.cur();
+    const int n = (int)widx.size();
+    if (n == 0) return;
+    int* dwi = nullptr;
+    CK(cudaMallocAsync((void**)&dwi, sizeof(int) * 5 * (size_t)n, B.st));
+    int* dout = dwi + n;
+    CK(cudaMemcpyAsync(dwi, widx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, B.st));
+    launch_world_ranges(x, dwi, n, dout, B.st);
+    std::vector<int> rg(4 * (size_t)n);
+    CK(cudaMemcpyAsync(rg.data(), dout, sizeof(int) * 4 * (size_t)n, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaFreeAsync(dwi, B.st));
+    CK(cudaStreamSynchronize(B.st));
+    struct Buf {
+        std::vector<float4> pos, rot, vel, angv;
+        std::vector<float> iw, iinv, jimp;
+        std::vector<float4> ju, jw;
+        std::vector<uint64_t> key, mag;
+        std::vector<int> cstart, ccount, state;
+        std::vector<float4> p1, p2, nrm, imp, fu, fw;
+    };
+    std::vector<Buf> bufs(n);
+    auto get = [&](void* dst, const void* src, size_t bytes) {
+        if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, B.st));
+    };
+    for (int i = 0; i < n; i++) {
+        const int w = widx[i], s0 = B.world_start[w], nb = B.world_start[w + 1] - s0;
+        Buf& b = bufs[i];
+        b.pos.resize(nb); b.rot.resize(nb); b.vel.resize(nb); b.angv.resize(nb);
+        b.iw.resize(9 * (size_t)nb); b.iinv.resize(9 * (size_t)nb);
+        get(b.pos.data(), x.pos + s0, nb * 16); get(b.rot.data(), x.rot + s0, nb * 16);
+        get(b.vel.data(), x.vel + s0, nb * 16); get(b.angv.data(), x.angv + s0, nb * 16);
+        get(b.iw.data(), x.iw + 9 * (size_t)s0, 36 * (size_t)nb); get(b.iinv.data(), x.iinv + 9 * (size_t)s0, 36 * (size_t)nb);
+        if (x.n_joints > 0) {
+            const int j0 = B.world_jstart[w], nj = B.world_jstart[w + 1] - j0;
+            b.jimp.resize((size_t)kJMax * nj); b.ju.resize(nj); b.jw.resize(nj);
+            get(b.jimp.data(), x.jt.impulse + (size_t)kJMax * j0, (size_t)kJMax * nj * 4);
+            get(b.ju.data(), x.jt.u + j0, nj * 16); get(b.jw.data(), x.jt.w + j0, nj * 16);
+        }
+        const int e0 = rg[4 * i], e1 = rg[4 * i + 1], c0 = rg[4 * i + 2], c1 = rg[4 * i + 3];
+        const int ne = e1 - e0, nc = c1 - c0;
+        b.key.resize(ne); b.cstart.resize(ne); b.ccount.resize(ne);
+        get(b.key.data(), x.e_old.key + e0, ne * 8); get(b.cstart.data(), x.e_old.cstart + e0, ne * 4);
+        get(b.ccount.data(), x.e_old.ccount + e0, ne * 4);
+        b.mag.resize(nc); b.state.resize(nc);
+        b.p1.resize(nc); b.p2.resize(nc); b.nrm.resize(nc); b.imp.resize(nc); b.fu.resize(nc); b.fw.resize(nc);
+        get(b.mag.data(), x.c_old.magic + c0, nc * 8); get(b.state.data(), x.c_old.state + c0, nc * 4);
+        get(b.p1.data(), x.c_old.p1 + c0, nc * 16); get(b.p2.data(), x.c_old.p2 + c0, nc * 16);
+        get(b.nrm.data(), x.c_old.n + c0, nc * 16); get(b.imp.data(), x.c_old.imp + c0, nc * 16);
+        get(b.fu.data(), x.c_old.fu + c0, nc * 16); get(b.fw.data(), x.c_old.fw + c0, nc * 16);
+        for (int& c : b.cstart) c -= c0;
+    }
+    CK(cudaStreamSynchronize(B.st));
+    for (int i = 0; i < n; i++) {
+        World& w = *ws[i];
+        const Buf& b = bufs[i];
+        const int s0 = B.world_start[widx[i]];
+        for (size_t k = 0; k < w.bodies.size(); k++) {
+            Body& bd = w.bodies[k];
+            bd.com = D3(b.pos[k].x, b.pos[k].y, b.pos[k].z);
+            bd.q = Quat{b.rot[k].x, b.rot[k].y, b.rot[k].z, b.rot[k].w};
+            if (bd.movement != CPGPU_FIXED) {
+                bd.vel = D3(b.vel[k].x, b.vel[k].y, b.vel[k].z);
+                bd.angv = D3(b.angv[k].x, b.angv[k].y, b.angv[k].z);
+            }
+            if (bd.movement == CPGPU_DYNAMIC)
+                for (int q = 0; q < 9; q++) { bd.iw[q] = b.iw[9 * k + q]; bd.iinv[q] = b.iinv[9 * k + q]; }
+        }
+        for (size_t j = 0; j < b.ju.size() && j < w.joints.size(); j++) {
+            for (int k = 0; k < kJMax; k++) w.joints[j].impulse[k] = b.jimp[kJMax * j + k];
+            w.joints[j].u[0] = b.ju[j].x; w.joints[j].u[1] = b.ju[j].y; w.joints[j].u[2] = b.ju[j].z;
+            w.joints[j].w[0] = b.jw[j].x; w.joints[j].w[1] = b.jw[j].y; w.joints[j].w[2] = b.jw[j].z;
+        }
+        w.contacts.clear();
+        for (size_t e = 0; e < b.key.size(); e++) {
+            uint32_t b1 = (uint32_t)((b.key[e] >> 32) - s0) + 1, b2 = (uint32_t)((b.key[e] & 0xffffffffu) - s0) + 1;
+            for (int k = b.cstart[e]; k < b.cstart[e] + b.ccount[e]; k++) {
+                if (cs_dead(b.state[k])) continue;
+                cpgpu_contact c;
+                std::memset(&c, 0, sizeof(c));
+                c.b1 = b1; c.b2 = b2;
+                c.live = cs_live(b.state[k]);
+                c.memory_life = cs_life(b.state[k]);
+                c.magic_c = ((uint64_t)b2 << 32) | b1;
+                c.magic_b = b.mag[k];
+                c.p_local_b1[0] = b.p1[k].x; c.p_local_b1[1] = b.p1[k].y; c.p_local_b1[2] = b.p1[k].z;
+                c.p_local_b2[0] = b.p2[k].x; c.p_local_b2[1] = b.p2[k].y; c.p_local_b2[2] = b.p2[k].z;
+                c.n_local_b1[0] = b.nrm[k].x; c.n_local_b1[1] = b.nrm[k].y; c.n_local_b1[2] = b.nrm[k].z;
+                c.pen_depth = b.p1[k].w; c.bounce = b.p2[k].w; c.friction_coeff = b.nrm[k].w;
+                c.normal_impulse = b.imp[k].x; c.friction_impulse[0] = b.imp[k].y; c.friction_impulse[1] = b.imp[k].z;
+                c.friction_u[0] = b.fu[k].x; c.friction_u[1] = b.fu[k].y; c.friction_u[2] = b.fu[k].z;
+                c.friction_w[0] = b.fw[k].x; c.friction_w[1] = b.fw[k].y; c.friction_w[2] = b.fw[k].z;
+                c.static_ready = cs_static(b.state[k]);
+                w.contacts.push_back(c);
+            }
+        }
+        w.last_pairs.clear();
+    }
+}
+
 static void download_state(World& w) {
     if (!w.dev || !w.dev_valid) return;
     std::vector<World*> one{&w};
@@ -1657,6 +1760,7 @@ struct ServerRequest {
     uint64_t token = 0;
     int64_t bodies = 0;
     size_t bytes = 0;   // estimated device bytes
+    bool finished = false;   // result captured; still in the batch until the next re-form
 };
 
 struct Server {
@@ -1674,19 +1778,28 @@ struct Server {
 
     size_t estimate(const World& w) const { return (size_t)(bytes_per_body * (double)w.bodies.size()) + (1u << 20); }
 
+    // capture the exact state of requests that reached their step count,
+    // without stopping the batch (they keep stepping as dead weight until the
+    // next re-form)
+    void capture_finished() {
+        std::vector<int> idx;
+        std::vector<World*> ws;
+        for (size_t i = 0; i < running.size(); i++)
+            if (!running[i].finished && running[i].remaining <= 0) { idx.push_back((int)i); ws.push_back(running[i].w); }
+        if (idx.empty()) return;
+        download_subset(*batch, idx, ws);
+        for (int i : idx) { running[i].finished = true; done.push_back(running[i].token); }
+    }
+
     void reform() {
         auto t0 = std::chrono::steady_clock::now();
-        if (batch) {
-            std::vector<World*> ws;
-            for (auto& r : running) ws.push_back(r.w);
-            download_worlds(*batch, ws);
-            batch.reset();
-        }
         std::vector<ServerRequest> keep;
-        for (auto& r : running) {
-            if (r.remaining <= 0) done.push_back(r.token);
-            else keep.push_back(r);
-        }
+        std::vector<int> idx;
+        std::vector<World*> ws;
+        for (size_t i = 0; i < running.size(); i++)
+            if (!running[i].finished) { keep.push_back(running[i]); idx.push_back((int)i); ws.push_back(running[i].w); }
+        if (batch) download_subset(*batch, idx, ws);
+        batch.reset();
         running.swap(keep);
         size_t used = 0;
         for (auto& r : running) used += r.bytes;
@@ -1712,28 +1825,31 @@ struct Server {
         reform_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
 
+    // Re-form when requests wait and an epoch has passed since the last
+    // re-form, or when finished requests hold a quarter of the batch's bodies.
     int advance(int max_steps) {
         int stepped = 0;
         while (stepped < max_steps) {
-            bool finished = false;
-            for (auto& r : running) finished |= r.remaining <= 0;
-            const bool want = !waiting.empty() && (running.empty() || since_reform >= epoch_steps);
-            if (finished || want || (!batch && !running.empty())) reform();
-            if (running.empty()) break;
+            int64_t live = 0, dead = 0;
+            for (auto& r : running) (r.finished ? dead : live) += r.bodies;
+            const bool want = !waiting.empty() && (live == 0 || since_reform >= epoch_steps);
+            const bool reclaim = dead > 0 && (live == 0 || 4 * dead >= live + dead);
+            if (want || reclaim) reform();
+            if (!batch) break;
             int n = max_steps - stepped;
-            for (auto& r : running) n = std::min(n, r.remaining);
+            for (auto& r : running) if (!r.finished) n = std::min(n, r.remaining);
             if (!waiting.empty()) n = std::min(n, std::max(1, epoch_steps - since_reform));
             batch->step(n);
-            int code = batch->check_status();
-            (void)code;
-            for (auto& r : running) { r.remaining -= n; body_steps += (int64_t)n * r.bodies; }
+            batch->check_status();
+            for (auto& r : running) {
+                if (r.finished) continue;
+                r.remaining -= n;
+                body_steps += (int64_t)n * r.bodies;
+            }
             stepped += n;
             since_reform += n;
+            capture_finished();
         }
-        // hand back requests that completed in the last stretch
-        bool finished = false;
-        for (auto& r : running) finished |= r.remaining <= 0;
-        if (finished) reform();
         return stepped;
     }
 };

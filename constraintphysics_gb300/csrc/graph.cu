@@ -392,6 +392,28 @@ void launch_merge(const Dev& d, const Launch& L) {
     k_contacts<<<gb, 128, 0, L.st>>>(d, 1);
 }
 
+// Edge and contact index ranges of the given worlds in the current contact
+// graph (edges sorted by key, contacts stored in edge order): out[4 w] =
+// (first edge, end edge, first contact, end contact).
+__global__ void k_world_ranges(const uint64_t* keys, const int* cstart, const int* n_edges, const int* n_contacts,
+                               const int* world_start, const int* worlds, int n, int* out) {
+    const int ne = *n_edges, nc = *n_contacts;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int w = worlds[i];
+        const int e0 = lower_bound_u64(keys, ne, (uint64_t)world_start[w] << 32);
+        const int e1 = lower_bound_u64(keys, ne, (uint64_t)world_start[w + 1] << 32);
+        out[4 * i] = e0;
+        out[4 * i + 1] = e1;
+        out[4 * i + 2] = e0 < ne ? cstart[e0] : nc;
+        out[4 * i + 3] = e1 < ne ? cstart[e1] : nc;
+    }
+}
+
+void launch_world_ranges(const Dev& d, const int* worlds, int n, int* out, cudaStream_t st) {
+    k_world_ranges<<<(n + 127) / 128, 128, 0, st>>>(d.e_old.key, d.e_old.cstart, d.n_edges_old, d.n_contacts_old, d.world_start,
+                                                      worlds, n, out);
+}
+
 void launch_islands(const Dev& d, const Launch& L) {
     k_islands<<<d.n_worlds, 256, 0, L.st>>>(d);
     scan_exclusive(d.isl_count_w, d.isl_scan, nullptr, d.n_worlds, d.n_worlds, d.n_islands, d.scan_tmp, L);

@@ -25,6 +25,8 @@ void launch_geometry(const Dev& d, int force_all, const Launch& L);
 void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st);
 void launch_merge(const Dev& d, const Launch& L);
 void launch_islands(const Dev& d, const Launch& L);
+// per-world edge / contact ranges of the current graph (4 ints per world)
+void launch_world_ranges(const Dev& d, const int* worlds, int n, int* out, cudaStream_t st);
 void launch_rows(const Dev& d, int first, int last, const Launch& L);
 // PGS: islands are split by size after the island pass (largest first); large
 // islands run one warp each with rows streamed through shared memory, small
