@@ -23,6 +23,11 @@ Workloads:
                  hinges with random axes, starting horizontal and swinging
                  through fixed spheres (r U[0.5,1.5]) placed in its swing
                  volume; engine defaults (8 substeps, PGS (4,1,1)).
+  terrain_drop   mixed bodies as in mixed_drop falling onto a fixed triangle-
+                 mesh terrain: an n x n heightfield at 1 m spacing triangulated
+                 as generateGridMeshInput does (Geometry.cpp:589-611), heights
+                 summed from 4 octaves of seeded value noise (periods 32, 16, 8,
+                 4 m, amplitudes halving) scaled to 8 m; 20 PGS iterations.
   batched_world  one world of the 4,096-world batch: floor(exp(U[ln 8, ln 512]))
                  bodies, either a box pyramid (base 4-16) or a hull pile built as
                  in hull_drop, each world with its own plate.
@@ -92,6 +97,9 @@ class Scene:
     def cylinder(self, base, r, h, material, movement, pos=(0, 0, 0)):
         return self._body(("cylinder", tuple(base), r, h, material, movement, tuple(pos)))
 
+    def mesh(self, points, tris, material):
+        return self._body(("mesh", np.asarray(points, dtype=np.float64), np.asarray(tris, dtype=np.int32), material))
+
     def mass(self, bid, m):
         self.ops.append(("mass", bid, float(m)))
 
@@ -123,6 +131,8 @@ def apply(scene, world):
             ids.append(world.add_sphere(op[1], op[2], op[3], op[4], op[5]))
         elif kind == "cylinder":
             ids.append(world.add_cylinder(op[1], op[2], op[3], op[4], op[5], op[6]))
+        elif kind == "mesh":
+            ids.append(world.add_mesh(op[1], op[2], op[3], True))
         elif kind == "orient":
             world.set_orientation(op[1], op[2])
         elif kind == "vel":
@@ -254,6 +264,80 @@ def heavy_chain():
     ball = sc.sphere((0.0, -35 * h - 7.0, 0.0), 7.0, heavy, DYNAMIC)
     sc.velocity(ball, (25.0, 0.0, 0.0))
     sc.ball_socket(ball, prev, final, final)
+    return sc
+
+
+def value_noise(rng, n, periods=(32, 16, 8, 4), amplitude=8.0):
+    """(n+1) x (n+1) heights: octaves of lattice value noise (uniform lattice
+    values, smoothstep interpolation), weights halving per octave, the sum
+    scaled so its largest magnitude is `amplitude`."""
+    xs = np.arange(n + 1, dtype=np.float64)
+    total = np.zeros((n + 1, n + 1))
+    for k, per in enumerate(periods):
+        m = int(np.ceil(n / per)) + 2
+        lat = rng.uniform(-1.0, 1.0, size=(m, m))
+        f = xs / per
+        i0 = np.floor(f).astype(int)
+        t = f - i0
+        t = t * t * (3 - 2 * t)
+        a = lat[i0][:, i0]
+        b = lat[i0 + 1][:, i0]
+        c = lat[i0][:, i0 + 1]
+        d = lat[i0 + 1][:, i0 + 1]
+        ti, tj = t[:, None], t[None, :]
+        total += 0.5 ** k * (a * (1 - ti) * (1 - tj) + b * ti * (1 - tj) + c * (1 - ti) * tj + d * ti * tj)
+    return total * (amplitude / max(np.abs(total).max(), 1e-12))
+
+
+def grid_mesh(heights, spacing=1.0, origin=(0.0, 0.0, 0.0)):
+    """Points and triangles of an n x n grid, indexed and wound as
+    generateGridMeshInput (Geometry.cpp:589-611) does; point (i, j) sits at
+    origin + (spacing i, height, spacing j)."""
+    n = heights.shape[0] - 1
+    pts = np.zeros(((n + 1) * (n + 1), 3))
+    for j in range(n + 1):
+        for i in range(n + 1):
+            pts[i + (n + 1) * j] = (origin[0] + spacing * i, origin[1] + heights[i, j], origin[2] + spacing * j)
+    tris = np.zeros((2 * n * n, 3), dtype=np.int64)
+    for j in range(1, n + 1):
+        for i in range(1, n + 1):
+            tile = i - 1 + n * (j - 1)
+            i1 = i - 1 + (n + 1) * (j - 1)
+            i2 = i + (n + 1) * (j - 1)
+            i3 = i + (n + 1) * j
+            i4 = i - 1 + (n + 1) * j
+            tris[2 * tile] = (i3, i2, i1)
+            tris[2 * tile + 1] = (i4, i3, i1)
+    return pts, tris
+
+
+def terrain_drop(seed=0, n_grid=32, n_side=6, n_layers=2, spacing=3.2, clearance=3.0):
+    """Mixed bodies (see mixed_drop) dropped on a value-noise terrain mesh."""
+    rng = np.random.default_rng(seed)
+    h = value_noise(rng, n_grid)
+    pts, tris = grid_mesh(h, 1.0, (-n_grid / 2.0, 0.0, -n_grid / 2.0))
+    sc = Scene(f"terrain_drop_{n_grid}_{n_side}x{n_side}x{n_layers}_seed{seed}", MIXED_PARAMS)
+    sc.mesh(pts, tris, PILE_MATERIAL)
+    top = float(h.max()) + clearance
+    off = (n_side - 1) * spacing / 2.0
+    for j in range(n_layers):
+        for i in range(n_side):
+            for k in range(n_side):
+                pos = np.array([i * spacing - off, top + j * spacing, k * spacing - off])
+                pos += rng.uniform(-0.1, 0.1, size=3)
+                u = rng.random()
+                if u < 0.4:
+                    d = rng.uniform(0.5, 1.5, size=3)
+                    bid = sc.box((-d[0] / 2, -d[1] / 2, -d[2] / 2), d[0], d[1], d[2], PILE_MATERIAL, DYNAMIC, pos)
+                elif u < 0.6:
+                    bid = sc.sphere((0.0, 0.0, 0.0), rng.uniform(0.3, 0.8), PILE_MATERIAL, DYNAMIC, pos)
+                elif u < 0.8:
+                    r, hh = rng.uniform(0.3, 0.6), rng.uniform(0.5, 1.5)
+                    bid = sc.cylinder((0.0, -hh / 2, 0.0), r, hh, PILE_MATERIAL, DYNAMIC, pos)
+                else:
+                    p_, f_ = random_hull(rng, 12, 32)
+                    bid = sc.hull(p_, f_, PILE_MATERIAL, DYNAMIC, pos)
+                sc.orient(bid, random_quat(rng))
     return sc
 
 

@@ -120,12 +120,12 @@ def twin_worlds(scene):
     return r, p
 
 
-_CREATE = ("add_hull", "add_box", "add_sphere", "add_cylinder")
+_CREATE = ("add_hull", "add_box", "add_sphere", "add_cylinder", "add_mesh")
 
 
 class _Hooked:
-    """Forwards world calls; runs `after(body_id)` right after each body is
-    created (before any later operation of the scene touches it)."""
+    """Forwards world calls; runs `after(body_id, kind)` right after each body
+    is created (before any later operation of the scene touches it)."""
 
     def __init__(self, world, after):
         self._w, self._after = world, after
@@ -136,7 +136,7 @@ class _Hooked:
         def call(*a, **k):
             out = f(*a, **k)
             if name in _CREATE:
-                self._after(out)
+                self._after(out, name)
             return out
         return call
 
@@ -152,9 +152,10 @@ def capture_mass_properties(scene):
     r.set_params(**scene.params)
     rows = []
 
-    def after(bid):
+    def after(bid, kind):
         m, c, t = np.zeros(1), np.zeros(3), np.zeros(9)
-        assert get(r.h, bid, m.ctypes.data, c.ctypes.data, t.ctypes.data) == 0
+        if kind != "add_mesh":   # meshes have no mass properties
+            assert get(r.h, bid, m.ctypes.data, c.ctypes.data, t.ctypes.data) == 0
         rows.append((m[0], c, t))
     sc_mod.apply(scene, _Hooked(r, after))
     mass = np.array([x[0] for x in rows])
@@ -170,7 +171,9 @@ def port_world_with_mass(scene, mass, com, tensor):
     p = port_world()
     p.set_params(**scene.params)
 
-    def after(bid):
+    def after(bid, kind):
+        if kind == "add_mesh":
+            return
         i = bid - 1
         c = np.ascontiguousarray(com[i], dtype=np.float64)
         t = np.ascontiguousarray(tensor[i], dtype=np.float64)

@@ -22,6 +22,7 @@
 #include <unordered_map>
 #include <set>
 #include <functional>
+#include <array>
 
 namespace cport {
 
@@ -258,7 +259,32 @@ struct CylG {
     V3 topCenter() const { return c + 0.5 * h * axis; }
     V3 botCenter() const { return c - 0.5 * h * axis; }
 };
-enum Kind { K_HULL = 0, K_SPHERE = 1, K_CYLINDER = 2 };
+enum Kind { K_HULL = 0, K_SPHERE = 1, K_CYLINDER = 2, K_MESH = 3 };
+
+// StaticMeshFace (Geometry.h:74-86) as built by StaticMeshGeometry's
+// constructor (Geometry.cpp:675-820)
+struct MeshTri {
+    V3 normal;
+    V3 v[3];
+    int vid[3] = {0, 0, 0};
+    V3 ep1[3], ep2[3], out[3];   // edges (p1, p2) and outward directions in the face plane
+    int eid[3] = {0, 0, 0};
+    std::vector<V3> gauss;       // gauss_region
+    int concave = 0;             // concave_neighbor_count
+    int id = 0;
+    AABB aabb;
+};
+
+// AABBTree<unsigned int> (AABB_Tree.h) with margin 0 and the surface-area
+// cost, filled by add() in triangle order as the mesh copy constructor does
+// (Geometry.cpp:660-666); candidates() is getCollisionCandidatesWith.
+struct MeshTree {
+    struct Node { int parent = -1, left = -1, right = -1; bool leaf = false; int obj = -1; AABB box, true_box; double cost = 0; };
+    std::vector<Node> nodes;
+    int root = -1;
+    void add(int obj, const AABB& b);
+    std::vector<int> candidates(const AABB& target) const;
+};
 CylG makeCylinder(V3 center, double radius, double height);
 
 // --------------------------------------------------------------- world ----
@@ -273,6 +299,8 @@ struct Body {
     Hull shape;           // world geometry (points and Gauss normals follow the pose)
     SphereG sph_src, sph_ref, sph;
     CylG cyl_src, cyl_ref, cyl;
+    std::vector<MeshTri> tris;    // static mesh (world coordinates)
+    MeshTree tree;
     AABB aabb;
     V3 com, vel, ang_vel, pvel, pang_vel, prev_com;
     Q q, prev_q;
@@ -420,6 +448,7 @@ struct World {
     Body* addSphere(V3 center, double r, const Material& m, int movement, V3 pos);
     Body* addCylinder(V3 base, double r, double h, const Material& m, int movement, V3 pos);
     Body* finishBody(std::unique_ptr<Body> b, double mass, const V3& com, const M3& tensor);
+    Body* addMesh(const std::vector<V3>& points, const std::vector<std::array<int, 3>>& tris, const Material& m);
     void placeBody(Body* b, double mass, const V3& com_geom, const M3& tensor);
     Edge* edgeBetween(Body* a, Body* b);
     Edge* getOrCreateEdge(Body* a, Body* b);
@@ -443,7 +472,9 @@ Manifold satPolyCylinder(const Hull& a, uint32_t a_id, const Material& am, const
 Manifold sphereSphere(const SphereG& a, uint32_t a_id, const Material& am, const SphereG& b, uint32_t b_id, const Material& bm);
 Manifold sphereCylinder(const SphereG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm);
 Manifold cylinderCylinder(const CylG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm);
-Manifold flipped(Manifold m);   // normal negated, MagicID halves swapped (CollisionDetect.cpp:29-40)
+Manifold flipped(Manifold m);
+std::vector<Manifold> meshCollide(const Body* convex, const Body* mesh);   // SAT_*Mesh (CollisionDetect.cpp:2648-2778)
+Manifold mergeManifold(const Manifold& a, const Manifold& b);              // merge_manifold (:2780-2793)   // normal negated, MagicID halves swapped (CollisionDetect.cpp:29-40)
 Manifold cullManifold(const Manifold& m, int n);
 void massProperties(const Hull& h, double density, V3* com, M3* tensor, double* mass);
 

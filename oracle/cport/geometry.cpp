@@ -757,6 +757,250 @@ Manifold cylinderCylinder(const CylG& a, uint32_t a_id, const Material& am, cons
     return out;
 }
 
+// ------------------------------------------------------ mesh triangles ----
+// findTriangleExtrema (CollisionDetect.cpp:2004-2021)
+static Extrema triExtrema(const MeshTri& t, const V3& d) {
+    Extrema e;
+    for (int i = 0; i < 3; i++) {
+        double v = t.v[i].dot(d);
+        if (v < e.min_v) { e.min_id = i; e.min_v = v; }
+        if (v > e.max_v) { e.max_id = i; e.max_v = v; }
+    }
+    return e;
+}
+
+// normalDirectionValid (CollisionDetect.cpp:2024-2060): the normal must lie in
+// the face's Gauss region (triangle of 3 directions, arc of 2, or the normal)
+static bool normalValid(const MeshTri& s, const V3& n) {
+    const double EPS = 0.0001;
+    const std::vector<V3>& g = s.gauss;
+    switch (s.concave) {
+    case 0:
+    case 1:
+        for (size_t i = 0; i < g.size(); i++) {
+            V3 inner = g[i].cross(g[(i + 1) % g.size()]);
+            if (n.dot(inner) < -EPS) return false;
+        }
+        break;
+    case 2: {
+        V3 arc = g[0].cross(g[1]);
+        if (std::abs(n.dot(arc)) > EPS) return false;
+        V3 up = arc.cross(g[0]);
+        if (n.dot(up) < -EPS) return false;
+        V3 down = g[1].cross(arc);
+        if (n.dot(down) < -EPS) return false;
+        break;
+    }
+    case 3:
+        if (n.dot(s.normal) < 1 - EPS) return false;
+        break;
+    }
+    return true;
+}
+
+// findTriangleContactArea (CollisionDetect.cpp:303-329) with projectTriangleFace
+// / projectTriangleEdge (:282-300): face points carry ids 0..2, edge points the
+// edge id
+static Area triangleArea(const MeshTri& t, const V3& n, const V3& p, int pid, const V3& u, const V3& w) {
+    Area a;
+    if (1 - t.normal.dot(n) <= cosTol()) {
+        for (int i = 0; i < 3; i++) { a.ps.push_back(p2(t.v[i].dot(u), t.v[i].dot(w))); a.ids.push_back(i); }
+        a.surface = t.id;
+        a.origin = FACE;
+        return a;
+    }
+    for (int i = 0; i < 3; i++) {
+        if (i != pid && (i + 1) % 3 != pid) continue;
+        double sn = std::abs((t.ep2[i] - t.ep1[i]).normalize().dot(n));
+        if (sn <= sinTol()) {
+            a.ps = {p2(t.ep1[i].dot(u), t.ep1[i].dot(w)), p2(t.ep2[i].dot(u), t.ep2[i].dot(w))};
+            a.ids = {t.eid[i], t.eid[i]};
+            a.surface = -1;
+            a.origin = EDGE;
+            return a;
+        }
+    }
+    a.ps = {p2(p.dot(u), p.dot(w))};
+    a.ids = {pid};
+    a.surface = -1;
+    a.origin = VERTEX;
+    return a;
+}
+
+// the six Gauss arcs of a triangle (normal to each edge's outward direction,
+// and on to the reversed normal)
+static void triArcs(const MeshTri& t, V3 g1[6], V3 g2[6]) {
+    for (int i = 0; i < 3; i++) {
+        g1[2 * i] = t.normal; g2[2 * i] = t.out[i];
+        g1[2 * i + 1] = t.out[i]; g2[2 * i + 1] = -t.normal;
+    }
+}
+
+struct TriSat {
+    NormResult min_pen{-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    NormResult min_valid{-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    bool sep = false;
+    // one axis: false when it separates
+    bool take(const MeshTri& t, const Extrema& ea, const Extrema& eb, const V3& n, bool* improved = nullptr) {
+        NormResult x = checkNorm(ea, eb, n);
+        if (x.pen < 0) { sep = true; return false; }
+        if (improved) *improved = false;
+        if (x.pen < min_pen.pen) { min_pen = x; if (improved) *improved = true; }
+        if (x.pen < min_valid.pen && normalValid(t, -x.n)) min_valid = x;
+        return true;
+    }
+    // the penalised choice; returns the unpenalised minimum as well
+    NormResult choose(double penalty, NormResult* nongauss) const {
+        *nongauss = min_pen;
+        return (min_valid.pen < min_pen.pen + penalty) ? min_valid : min_pen;
+    }
+};
+
+static bool triArcAxes(TriSat& S, const MeshTri& t, const std::vector<V3>& ag, const std::vector<std::pair<int, int>>& aarcs,
+                       const std::function<Extrema(const V3&)>& ea) {
+    V3 g1[6], g2[6];
+    triArcs(t, g1, g2);
+    for (auto& arc1 : aarcs)
+        for (int k = 0; k < 6; k++) {
+            V3 a1 = ag[arc1.first], a2 = ag[arc1.second];
+            V3 b1 = -g1[k], b2 = -g2[k];
+            V3 avg = a1 + a2;
+            if (avg.dot(b1) + avg.dot(b2) <= 0) continue;
+            V3 ap = a1.cross(a2), bp = b1.cross(b2);
+            if (ap.dot(b1) * ap.dot(b2) > 0 || bp.dot(a1) * bp.dot(a2) > 0) continue;
+            V3 n = ap.cross(bp);
+            if (n.mag2() == 0) continue;
+            n = n.normalize();
+            if (avg.dot(n) < 0) n *= -1;
+            if (!S.take(t, ea(n), triExtrema(t, n), n)) return false;
+        }
+    return true;
+}
+
+// SAT_PolyTriangle (CollisionDetect.cpp:2062-2194)
+static Manifold satPolyTriangle(const Hull& a, uint32_t a_id, const Material& am, const MeshTri& b, const Material& bm, double penalty) {
+    Manifold out;
+    TriSat S;
+    if (!S.take(b, findExtrema(a, b.normal), triExtrema(b, b.normal), b.normal)) return out;
+    for (size_t f = 0; f < a.gv.size(); f++) {
+        if (a.g_redundant[f]) continue;
+        Extrema ea = recenter(a.g_cache[f], a.g_ref_val[f], a.gv[f].dot(a.pts[a.g_ref_idx[f]]));
+        if (!S.take(b, ea, triExtrema(b, a.gv[f]), a.gv[f])) return out;
+    }
+    if (!triArcAxes(S, b, a.gv, a.arcs, [&](const V3& n) { return findExtrema(a, n); })) return out;
+    NormResult ng;
+    NormResult mp = S.choose(penalty, &ng);
+    V3 n = mp.n;
+    V3 amax = a.pts[ng.a_id], bmax = b.v[ng.b_id];
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    Area ac = contactArea(a, ng.n, amax, ng.a_id, u, w);
+    Area bc = triangleArea(b, (-1) * ng.n, bmax, ng.b_id, u, w);
+    std::vector<ClipP> pool = clipContacts(ac, bc);
+    out = pointsFromPool(pool, u, w, n, amax.dot(n), mp.pen, am, bm, cidOf(a_id, (uint32_t)b.id));
+    out.normal = n;
+    out.max_pen = mp.pen;
+    return out;
+}
+
+// SAT_SphereTriangle (CollisionDetect.cpp:2196-2276)
+static Manifold satSphereTriangle(const SphereG& a, uint32_t a_id, const Material& am, const MeshTri& b, const Material& bm, double penalty) {
+    Manifold out;
+    TriSat S;
+    uint32_t feature = (uint32_t)-1;
+    if (!S.take(b, sphereExtrema(a, b.normal), triExtrema(b, b.normal), b.normal)) return out;
+    for (int i = 0; i < 3; i++) {
+        V3 n = (b.v[i] - a.c).normalize();
+        bool imp;
+        if (!S.take(b, sphereExtrema(a, n), triExtrema(b, n), n, &imp)) return out;
+        if (imp) feature = (uint32_t)i;
+    }
+    for (int i = 0; i < 3; i++) {
+        V3 dir = (b.ep2[i] - b.ep1[i]).normalize();
+        V3 sample = b.ep1[i] - a.c;
+        V3 n = (sample - dir * dir.dot(sample)).normalize();
+        bool imp;
+        if (!S.take(b, sphereExtrema(a, n), triExtrema(b, n), n, &imp)) return out;
+        if (imp) feature = (uint32_t)b.eid[i];
+    }
+    NormResult ng;
+    NormResult mp = S.choose(penalty, &ng);
+    out.normal = mp.n;
+    out.pts.push_back(mkPoint(a.c + mp.n * a.r, mp.pen, am, bm, cidOf(a_id, (uint32_t)b.id), feature));
+    out.max_pen = mp.pen;
+    return out;
+}
+
+// SAT_CylinderTriangle (CollisionDetect.cpp:2466-2646)
+static Manifold satCylinderTriangle(const CylG& a, uint32_t a_id, const Material& am, const MeshTri& b, const Material& bm, double penalty) {
+    Manifold out;
+    TriSat S;
+    V3 ax = a.axis;
+    if (!S.take(b, cylinderExtrema(a, ax), triExtrema(b, ax), ax)) return out;
+    if (!S.take(b, cylinderExtrema(a, b.normal), triExtrema(b, b.normal), b.normal)) return out;
+    for (int i = 0; i < 3; i++) {
+        V3 dir = (b.ep2[i] - b.ep1[i]).cross(ax);
+        if (dir.mag() < 0.00000000001) continue;
+        V3 dn = dir.normalize();
+        if (!S.take(b, cylinderExtrema(a, dn), triExtrema(b, dn), dn)) return out;
+    }
+    for (int i = 0; i < 3; i++) {
+        V3 diff = b.v[i] - a.c;
+        V3 n = (diff - ax * ax.dot(diff)).normalize();
+        if (!S.take(b, cylinderExtrema(a, n), triExtrema(b, n), n)) return out;
+    }
+    if (!triArcAxes(S, b, a.gv, a.arcs, [&](const V3& n) { return cylinderExtrema(a, n); })) return out;
+    NormResult ng;
+    NormResult mp = S.choose(penalty, &ng);
+    V3 n = mp.n;
+    V3 amax = ax.dot(n) > 0 ? diskExtremum(a.topCenter(), ax, a.r, n) : diskExtremum(a.botCenter(), ax, a.r, n);
+    V3 bmax = b.v[ng.b_id];
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    CylArea ak;
+    Area ac = cylinderArea(a, ng.n, u, w, &ak);
+    Area bc = triangleArea(b, -ng.n, bmax, ng.b_id, u, w);
+    std::vector<ClipP> pool;
+    if (ak == CA_EDGE) pool = {ClipP{ac.ps[0], 0, 0x0, false}};
+    else pool = clipContacts(ac, bc);
+    out = pointsFromPool(pool, u, w, n, amax.dot(n), mp.pen, am, bm, cidOf(a_id, (uint32_t)b.id));
+    out.normal = n;
+    out.max_pen = mp.pen;
+    return out;
+}
+
+static double longest(const AABB& b) {
+    return std::max<double>(b.mx.x - b.mn.x, std::max<double>(b.mx.y - b.mn.y, b.mx.z - b.mn.z));
+}
+
+// SAT_PolyMesh / SAT_SphereMesh / SAT_CylinderMesh (CollisionDetect.cpp:
+// 2648-2778) for a fixed mesh in world coordinates: candidate triangles from
+// the mesh tree in its traversal order, penalty 0 for polyhedra and
+// 0.15 min(longest AABB sides) otherwise
+std::vector<Manifold> meshCollide(const Body* c, const Body* m) {
+    std::vector<Manifold> out;
+    const Material& mm = m->mat;
+    for (int ti : m->tree.candidates(c->aabb)) {
+        const MeshTri& t = m->tris[ti];
+        Manifold r;
+        if (c->kind == K_HULL) r = satPolyTriangle(c->shape, c->id, c->mat, t, mm, 0 * std::min<double>(longest(c->aabb), longest(t.aabb)));
+        else if (c->kind == K_SPHERE) r = satSphereTriangle(c->sph, c->id, c->mat, t, mm, 0.15 * std::min<double>(longest(c->aabb), longest(t.aabb)));
+        else r = satCylinderTriangle(c->cyl, c->id, c->mat, t, mm, 0.15 * std::min<double>(longest(c->aabb), longest(t.aabb)));
+        if (r.max_pen > 0 && !r.pts.empty()) out.push_back(r);
+    }
+    return out;
+}
+
+// merge_manifold (CollisionDetect.cpp:2780-2793)
+Manifold mergeManifold(const Manifold& a, const Manifold& b) {
+    Manifold o;
+    o.pts = a.pts;
+    o.pts.insert(o.pts.end(), b.pts.begin(), b.pts.end());
+    o.normal = (a.normal + b.normal).normalize();
+    o.max_pen = std::max<double>(a.max_pen, b.max_pen);
+    return o;
+}
+
 // cull_manifold (CollisionDetect.cpp:2795-2830): keep the extreme points in 4
 // directions of the contact plane
 Manifold cullManifold(const Manifold& m, int n) {

@@ -56,6 +56,7 @@ static void cylFromReference(CylG& out, const CylG& ref, const M3& rot, const V3
 
 // RigidBody::updateGeometry (RigidBody.cpp:281-312) for a single primitive
 void Body::updateGeometry() {
+    if (kind == K_MESH) return;   // fixed meshes stay in world coordinates
     q = q.normalize();
     M3 rot = q.rotMatrix();
     if (kind == K_SPHERE) {
@@ -257,6 +258,225 @@ void World::placeBody(Body* b, double mass, const V3& com_geom, const M3& tensor
     V3 t = b->create_pos - b->trackedP(0);
     b->com += t;
     b->updateGeometry();
+}
+
+// ------------------------------------------------------------ meshes ----
+static AABB boxUnion(const AABB& a, const AABB& b) {   // AABB::combine
+    AABB o;
+    o.mn.x = std::min<double>(a.mn.x, b.mn.x); o.mn.y = std::min<double>(a.mn.y, b.mn.y); o.mn.z = std::min<double>(a.mn.z, b.mn.z);
+    o.mx.x = std::max<double>(a.mx.x, b.mx.x); o.mx.y = std::max<double>(a.mx.y, b.mx.y); o.mx.z = std::max<double>(a.mx.z, b.mx.z);
+    return o;
+}
+// AABB::surfaceArea (AABB.h:112-118), as written there: 2 dx dy + dy dz + dz dx
+static double boxCost(const AABB& a) {
+    double dx = a.mx.x - a.mn.x, dy = a.mx.y - a.mn.y, dz = a.mx.z - a.mn.z;
+    return 2 * (dx * dy) + (dy * dz) + (dz * dx);
+}
+
+// AABBTree::add (AABB_Tree.h:39-105): best sibling by branch-and-bound on the
+// inherited cost, new parent, ancestors refitted and rebalanced by rotations
+void MeshTree::add(int obj, const AABB& b) {
+    Node leaf;
+    leaf.leaf = true; leaf.obj = obj; leaf.true_box = b; leaf.box = b; leaf.cost = boxCost(b);
+    const int nl = (int)nodes.size();
+    nodes.push_back(leaf);
+    if (root < 0) { root = nl; return; }
+    int best = -1;
+    double best_cost = std::numeric_limits<double>::infinity();
+    std::vector<std::pair<int, double>> cand{{root, 0.0}};
+    while (!cand.empty()) {
+        auto c = cand.back();
+        cand.pop_back();
+        if (c.second >= best_cost) continue;
+        AABB cb = boxUnion(nodes[nl].box, nodes[c.first].box);
+        double direct = boxCost(cb);
+        double cost = c.second + direct;
+        if (cost < best_cost) { best = c.first; best_cost = cost; }
+        if (!nodes[c.first].leaf) {
+            double inherited = c.second + direct - nodes[c.first].cost;
+            cand.push_back({nodes[c.first].left, inherited});
+            cand.push_back({nodes[c.first].right, inherited});
+        }
+    }
+    Node par;
+    const int np = (int)nodes.size();
+    nodes.push_back(par);
+    if (best == root) root = np;
+    else {
+        int op = nodes[best].parent;
+        if (nodes[op].left == best) nodes[op].left = np; else nodes[op].right = np;
+        nodes[np].parent = op;
+    }
+    nodes[np].left = best; nodes[best].parent = np;
+    nodes[np].right = nl; nodes[nl].parent = np;
+    // haveAncestorsRecalculateAABB
+    for (int cur = nodes[nl].parent; cur >= 0; cur = nodes[cur].parent) {
+        nodes[cur].box = boxUnion(nodes[nodes[cur].left].box, nodes[nodes[cur].right].box);
+        nodes[cur].cost = boxCost(nodes[cur].box);
+    }
+    // rebalanceAncestors (AABB_Tree.h:373-421)
+    auto swapNodes = [&](int n1, int n2) {
+        int p1 = nodes[n1].parent, p2n = nodes[n2].parent;
+        if (nodes[p1].left == n1) nodes[p1].left = n2; else nodes[p1].right = n2;
+        if (nodes[p2n].left == n2) nodes[p2n].left = n1; else nodes[p2n].right = n1;
+        nodes[n1].parent = p2n;
+        nodes[n2].parent = p1;
+    };
+    int cur = nodes[nl].parent;
+    while (cur >= 0 && nodes[cur].parent >= 0) {
+        int pp = nodes[cur].parent;
+        int sib = nodes[pp].left == cur ? nodes[pp].right : nodes[pp].left;
+        if (sib >= 0) {
+            AABB sl_box = boxUnion(nodes[nodes[cur].right].box, nodes[sib].box);
+            AABB sr_box = boxUnion(nodes[nodes[cur].left].box, nodes[sib].box);
+            double sl = boxCost(sl_box), sr = boxCost(sr_box), cl, cr;
+            AABB cl_box, cr_box;
+            if (nodes[sib].leaf) {
+                cl = std::numeric_limits<double>::infinity();
+                cr = std::numeric_limits<double>::infinity();
+            } else {
+                cl_box = boxUnion(nodes[nodes[sib].right].box, nodes[cur].box);
+                cr_box = boxUnion(nodes[nodes[sib].left].box, nodes[cur].box);
+                cl = boxCost(cl_box);
+                cr = boxCost(cr_box);
+            }
+            double clc = cl - nodes[sib].cost, crc = cr - nodes[sib].cost;
+            double slc = sl - nodes[cur].cost, src = sr - nodes[cur].cost;
+            double mn = std::min<double>(clc, std::min<double>(crc, std::min<double>(slc, src)));
+            if (mn >= 0) {
+            } else if (mn == clc) {
+                swapNodes(cur, nodes[sib].left);
+                nodes[sib].box = cl_box; nodes[sib].cost = cl;
+            } else if (mn == crc) {
+                swapNodes(cur, nodes[sib].right);
+                nodes[sib].box = cr_box; nodes[sib].cost = cr;
+            } else if (mn == slc) {
+                swapNodes(sib, nodes[cur].left);
+                nodes[cur].box = sl_box; nodes[cur].cost = sl;
+            } else {
+                swapNodes(sib, nodes[cur].right);
+                nodes[cur].box = sr_box; nodes[cur].cost = sr;
+            }
+        }
+        cur = nodes[cur].parent;
+    }
+}
+
+// getCollisionCandidatesWith (AABB_Tree.h:226-246): LIFO traversal, leaves
+// tested on their true boxes
+std::vector<int> MeshTree::candidates(const AABB& target) const {
+    std::vector<int> out;
+    if (root < 0) return out;
+    std::vector<int> st{root};
+    while (!st.empty()) {
+        int n = st.back();
+        st.pop_back();
+        const Node& x = nodes[n];
+        if (x.leaf) {
+            if (AABB::overlap(x.true_box, target)) out.push_back(x.obj);
+        } else if (AABB::overlap(x.box, target)) {
+            st.push_back(x.left);
+            st.push_back(x.right);
+        }
+    }
+    return out;
+}
+
+// StaticMeshGeometry::StaticMeshGeometry (Geometry.cpp:675-820): face normals,
+// neighbours across shared edges, ids (faces 0.., vertices n_faces + i, edges
+// after), outward edge directions, Gauss regions with concave-neighbour count;
+// then RigidBody(StaticMeshGeometry) (RigidBody.cpp:41-58) as a fixed body
+Body* World::addMesh(const std::vector<V3>& pts, const std::vector<std::array<int, 3>>& tri_idx, const Material& m) {
+    struct E { int p1, p2, opp, id = -1; uint64_t key; };
+    struct TN { int p[3]; int nb[3]; E e[3]; V3 normal; };
+    auto mkE = [](int a, int b, int o) {
+        E e; e.p1 = a; e.p2 = b; e.opp = o;
+        unsigned mx = (unsigned)std::max(a, b), mn = (unsigned)std::min(a, b);
+        e.key = (((uint64_t)mx << 32) & 0xFFFFFFFF00000000ull) + mn;
+        return e;
+    };
+    std::vector<TN> g;
+    for (auto& t : tri_idx) {
+        V3 v1 = pts[t[1]] - pts[t[0]], v2 = pts[t[2]] - pts[t[0]];
+        TN n;
+        n.p[0] = t[0]; n.p[1] = t[1]; n.p[2] = t[2];
+        n.nb[0] = n.nb[1] = n.nb[2] = -1;
+        n.e[0] = mkE(t[0], t[1], t[2]); n.e[1] = mkE(t[1], t[2], t[0]); n.e[2] = mkE(t[2], t[0], t[1]);
+        n.normal = v1.cross(v2).normalize();
+        g.push_back(n);
+    }
+    std::unordered_map<uint64_t, unsigned> efm;
+    for (int i = 0; i < (int)g.size(); i++)
+        for (int j = 0; j < 3; j++) {
+            const E& e = g[i].e[j];
+            auto q = efm.find(e.key);
+            if (q != efm.end()) {
+                g[i].nb[j] = (int)q->second;
+                for (int k = 0; k < 3; k++)
+                    if (g[q->second].e[k].key == e.key) g[q->second].nb[k] = i;
+                efm.erase(q);
+            } else {
+                efm[e.key] = (unsigned)i;
+            }
+        }
+    auto b = std::make_unique<Body>();
+    b->kind = K_MESH;
+    b->movement = FIXED;
+    b->mat = m;
+    int next_tri = 0, voff = (int)tri_idx.size(), next_edge = (int)(tri_idx.size() + pts.size());
+    for (TN& t : g) {
+        MeshTri tri;
+        tri.concave = 0;
+        tri.normal = t.normal;
+        for (int i = 0; i < 3; i++) { tri.v[i] = pts[t.p[i]]; tri.vid[i] = t.p[i] + voff; }
+        tri.id = next_tri++;
+        for (int i = 0; i < 3; i++) {
+            tri.ep1[i] = tri.v[i];
+            tri.ep2[i] = tri.v[(i + 1) % 3];
+            tri.out[i] = (tri.ep2[i] - tri.ep1[i]).cross(tri.normal).normalize();
+            if (t.e[i].id == -1) t.e[i].id = next_edge++;
+            tri.eid[i] = t.e[i].id;
+            if (t.nb[i] == -1) {
+                tri.gauss.push_back(tri.out[i]);
+            } else {
+                E comp{};
+                for (int j = 0; j < 3; j++) {
+                    const E& ne = g[t.nb[i]].e[j];
+                    if (t.e[i].p1 == ne.p2 && t.e[i].p2 == ne.p1) comp = ne;
+                }
+                V3 tip = pts[t.e[i].opp], ntip = pts[comp.opp];
+                const double EPS = 0.00001;
+                bool concave = (ntip - tip).normalize().dot(t.normal) >= -EPS;
+                if (concave) {
+                    tri.concave++;
+                    if (tri.concave <= 1) tri.gauss.push_back(tri.normal);
+                } else {
+                    tri.gauss.push_back(g[t.nb[i]].normal);
+                }
+            }
+        }
+        AABB a;
+        a.mn = V3(std::numeric_limits<double>::infinity(), std::numeric_limits<double>::infinity(), std::numeric_limits<double>::infinity());
+        a.mx = V3(-std::numeric_limits<double>::infinity(), -std::numeric_limits<double>::infinity(), -std::numeric_limits<double>::infinity());
+        for (int i = 0; i < 3; i++) {
+            a.mn.x = std::min<double>(a.mn.x, tri.v[i].x); a.mn.y = std::min<double>(a.mn.y, tri.v[i].y); a.mn.z = std::min<double>(a.mn.z, tri.v[i].z);
+            a.mx.x = std::max<double>(a.mx.x, tri.v[i].x); a.mx.y = std::max<double>(a.mx.y, tri.v[i].y); a.mx.z = std::max<double>(a.mx.z, tri.v[i].z);
+        }
+        tri.aabb = a;
+        b->tris.push_back(tri);
+    }
+    for (int i = 0; i < (int)b->tris.size(); i++) b->tree.add(i, b->tris[i].aabb);
+    AABB box = b->tris[0].aabb;
+    for (size_t i = 1; i < b->tris.size(); i++) box = boxUnion(box, b->tris[i].aabb);
+    b->aabb = box;
+    b->mass = std::numeric_limits<double>::quiet_NaN();
+    b->track_p.assign(1, V3());
+    b->id = (uint32_t)bodies.size() + 1;
+    Body* raw = b.get();
+    bodies.push_back(std::move(b));
+    nodes[raw->id] = raw;
+    adj[raw];
+    return raw;
 }
 
 // --------------------------------------------------------- constraint graph ----
@@ -547,11 +767,29 @@ void World::step() {
         Body* b2 = bodies[pr.second - 1].get();
         if (!(b1->movement == DYNAMIC || b2->movement == DYNAMIC)) continue;
         if (b1->no_collide.count(b2)) continue;   // collisionAllowed (PhysicsEngine.cpp:570-572)
-        Manifold man = collide(b1, b2);
-        if (!(man.max_pen > 0)) continue;
-        Manifold m = cullManifold(man, 4);
-        getOrCreateEdge(b1, b2);
-        for (const ManifoldPoint& mp : m.pts) addContact(b1, b2, mp, m.normal);
+        if (b1->kind == K_MESH && b2->kind == K_MESH) continue;
+        std::vector<Manifold> mans;
+        if (b2->kind == K_MESH) {
+            mans = meshCollide(b1, b2);
+        } else if (b1->kind == K_MESH) {
+            for (Manifold& x : meshCollide(b2, b1)) mans.push_back(flipped(x));
+        } else {
+            Manifold man = collide(b1, b2);
+            if (man.max_pen > 0) mans.push_back(man);
+        }
+        // manifolds with normals within 1 degree merge (PhysicsEngine.cpp:257-295)
+        std::vector<char> merged(mans.size(), 0);
+        for (size_t i = 0; i < mans.size(); i++) {
+            if (merged[i]) continue;
+            for (size_t j = i + 1; j < mans.size(); j++) {
+                if (merged[j]) continue;
+                double v = mans[i].normal.dot(mans[j].normal);
+                if (1 - v < cosTol()) { mans[i] = mergeManifold(mans[i], mans[j]); merged[j] = 1; }
+            }
+            Manifold m = cullManifold(mans[i], 4);
+            getOrCreateEdge(b1, b2);
+            for (const ManifoldPoint& mp : m.pts) addContact(b1, b2, mp, m.normal);
+        }
     }
 
     // holonomic systems of new joints (PhysicsEngine.cpp:360-362)
@@ -727,8 +965,24 @@ int cport_body_cylinder(cpgpu_world* w, const double base[3], double radius, dou
     if (out_id) *out_id = b->id;
     return CPGPU_OK;
 }
-int cport_body_mesh(cpgpu_world*, const double*, int, const int*, int, const cpgpu_material*, int, uint32_t*) {
-    return fail("static meshes are not implemented in the restatement yet", CPGPU_ERR_UNSUPPORTED);
+// createRigidBody(StaticMeshGeometry(MeshInput), fixed) (PhysicsEngine.cpp:498-512)
+int cport_body_mesh(cpgpu_world* w, const double* points, int n_points, const int* tris, int n_tris, const cpgpu_material* m,
+                    int fixed, uint32_t* out_id) {
+    if (!fixed) return fail("kinematic meshes are not implemented in the restatement", CPGPU_ERR_UNSUPPORTED);
+    if (n_points < 3 || n_tris < 1) return fail("mesh needs >= 3 points and >= 1 triangle");
+    std::vector<V3> pts(n_points);
+    for (int i = 0; i < n_points; i++) pts[i] = V3(points[3 * i], points[3 * i + 1], points[3 * i + 2]);
+    std::vector<std::array<int, 3>> t(n_tris);
+    for (int i = 0; i < n_tris; i++) {
+        for (int k = 0; k < 3; k++) {
+            int x = tris[3 * i + k];
+            if (x < 0 || x >= n_points) return fail("mesh index out of range");
+            t[i][k] = x;
+        }
+    }
+    Body* b = W(w)->addMesh(pts, t, mat(m));
+    if (out_id) *out_id = b->id;
+    return CPGPU_OK;
 }
 int cport_body_set_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {
     Body* b = B(w, id); if (!b) return fail("bad id"); b->vel = v3(v); return CPGPU_OK;

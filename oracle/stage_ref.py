@@ -4,7 +4,7 @@ Test infrastructure only.  Copies the reference engine's C++ sources
 (ConstraintPhysics/src and Math/src) from the read-only reference checkout into
 baseline/_ref/src (git-ignored: never committed, but it travels with the
 working tree so a machine without the checkout can rebuild the oracle), writes
-the Linux build shim, and applies one documented fix:
+the Linux build shim, and applies documented fixes:
 
   * the narrowphase reads a constraint-graph node's edge list without holding
     the node mutexes (ConstraintPhysics/src/PhysicsEngine.cpp:197-210) while
@@ -18,6 +18,15 @@ the Linux build shim, and applies one documented fix:
     RigidBody.cpp:13-39,41-58 leave unset), so whether a body collides at all
     depends on heap contents.  The staged copy gives both the value the API
     implies (false: setNoCollision / setSleepDisabled turn them on).
+
+  * the static-mesh constructor (RigidBody.cpp:41-58) never sets `com_type`
+    (RigidBody.h:80; the convex constructor sets PHYSICALLY_BASED), so
+    getCOM() of a mesh body returns either its com or the (-1, -1, -1) of an
+    invalid tracked point, depending on heap contents.  The dynamics do not
+    depend on it (a mesh body is fixed: the offset cancels between a
+    contact's stored local point and its rebuild, and every Jacobian term of a
+    body with zero inverse mass vanishes); the reported state does.  The
+    staged copy initialises it to PHYSICALLY_BASED.
 
 The shim makes the MSVC-only code compile with g++:
   * a forced-include header that pulls in the C headers MSVC includes
@@ -96,6 +105,10 @@ def stage(ref_root):
         if text.count(member) != 1:
             raise SystemExit(f"anchor {member!r} not found exactly once in RigidBody.h")
         text = text.replace(member, member[:-1] + " = false;")
+    member = "CenterOfMassType com_type;"
+    if text.count(member) != 1:
+        raise SystemExit(f"anchor {member!r} not found exactly once in RigidBody.h")
+    text = text.replace(member, "CenterOfMassType com_type = PHYSICALLY_BASED;")
     open(rb, "w", encoding="utf-8", errors="surrogateescape").write(text)
     shim = os.path.join(DEST, "shim")
     os.makedirs(shim, exist_ok=True)

@@ -64,7 +64,22 @@ def chain():
                         com=st["com"], quat=st["quat"], vel=st["vel"], ang_vel=st["ang_vel"])
 
 
+def terrain():
+    """Mixed bodies on a 16 x 16 value-noise terrain mesh (scenes.terrain_drop,
+    seed 2) after 150 reference steps, with creation-time mass properties."""
+    steps = 150
+    sc = scenes.terrain_drop(seed=2, n_grid=16, n_side=3, n_layers=2)
+    mass, com, tensor, w = oracle.capture_mass_properties(sc)
+    w.step(steps)
+    st = w.state()
+    c = w.contacts()
+    np.savez_compressed(os.path.join(HERE, "terrain_drop_seed2.npz"), steps=steps, mass=mass, com_geom=com, tensor=tensor,
+                        com=st["com"], quat=st["quat"], vel=st["vel"], ang_vel=st["ang_vel"], magic_c=c["magic_c"],
+                        magic_b=c["magic_b"])
+
+
 def main():
+    terrain()
     chain()
     mixed()
     steps = 120
