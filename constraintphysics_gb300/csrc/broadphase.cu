@@ -115,6 +115,7 @@ __global__ void k_pairs(Dev d, int write) {
 
 __global__ void k_clamp_pairs(Dev d) {
     if (*d.n_pairs > d.cap_pairs) { atomicOr(d.status, ST_PAIR_OVERFLOW); *d.n_pairs = d.cap_pairs; }
+    if (d.has_mesh) *d.mm_count = 0;   // mesh store of this step's narrowphase
 }
 
 // RigidBody::updateGeometry (RigidBody.cpp:281-312) for moved bodies: the

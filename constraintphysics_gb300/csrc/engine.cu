@@ -8,6 +8,8 @@
 // back, change the host mirror and re-upload on the next step.  A batch packs
 // many worlds into one set of segmented device arrays.
 #include <algorithm>
+#include <array>
+#include <cmath>
 #include <chrono>
 #include <deque>
 #include <cstdio>
@@ -261,6 +263,217 @@ static Shape pack_cylinder(const D3& cref, double r, double h) {
     return pack_prim(SHAPE_CYLINDER, v, (float)(cref.mag() + std::sqrt(er * er + h * h / 4)));
 }
 
+// ---------------------------------------------------------------- static meshes ----
+// StaticMeshGeometry (Geometry.cpp:675-820) prepared on the host: face normals,
+// neighbours across shared edges, ids (faces from 0, edges after the
+// vertices), outward edge directions, Gauss regions with the concave-neighbour
+// count; and the AABB tree the reference's copy constructor builds
+// (Geometry.cpp:660-666: AABBTree::add per face in order, surface-area cost,
+// no margin, AABB_Tree.h:39-105, 373-421), whose traversal order decides the
+// order of a body's triangle candidates and so its contacts.
+struct MBox { D3 lo, hi; };
+static MBox mbox_union(const MBox& a, const MBox& b) {
+    return MBox{D3(std::min(a.lo.x, b.lo.x), std::min(a.lo.y, b.lo.y), std::min(a.lo.z, b.lo.z)),
+                D3(std::max(a.hi.x, b.hi.x), std::max(a.hi.y, b.hi.y), std::max(a.hi.z, b.hi.z))};
+}
+// AABB::surfaceArea as written in AABB.h:112-118 (2 dx dy + dy dz + dz dx)
+static double mbox_cost(const MBox& a) {
+    double dx = a.hi.x - a.lo.x, dy = a.hi.y - a.lo.y, dz = a.hi.z - a.lo.z;
+    return 2 * (dx * dy) + (dy * dz) + (dz * dx);
+}
+
+struct MTree {
+    struct Node { int parent = -1, left = -1, right = -1, obj = -1; bool leaf = false; MBox box; double cost = 0; };
+    std::vector<Node> n;
+    int root = -1;
+    void add(int obj, const MBox& b) {
+        Node leaf;
+        leaf.leaf = true; leaf.obj = obj; leaf.box = b; leaf.cost = mbox_cost(b);
+        const int nl = (int)n.size();
+        n.push_back(leaf);
+        if (root < 0) { root = nl; return; }
+        int best = -1;
+        double best_cost = std::numeric_limits<double>::infinity();
+        std::vector<std::pair<int, double>> cand{{root, 0.0}};
+        while (!cand.empty()) {
+            auto c = cand.back();
+            cand.pop_back();
+            if (c.second >= best_cost) continue;
+            double direct = mbox_cost(mbox_union(n[nl].box, n[c.first].box));
+            double cost = c.second + direct;
+            if (cost < best_cost) { best = c.first; best_cost = cost; }
+            if (!n[c.first].leaf) {
+                double inh = c.second + direct - n[c.first].cost;
+                cand.push_back({n[c.first].left, inh});
+                cand.push_back({n[c.first].right, inh});
+            }
+        }
+        const int np = (int)n.size();
+        n.push_back(Node());
+        if (best == root) root = np;
+        else {
+            int op = n[best].parent;
+            if (n[op].left == best) n[op].left = np; else n[op].right = np;
+            n[np].parent = op;
+        }
+        n[np].left = best; n[best].parent = np;
+        n[np].right = nl; n[nl].parent = np;
+        for (int cur = n[nl].parent; cur >= 0; cur = n[cur].parent) {
+            n[cur].box = mbox_union(n[n[cur].left].box, n[n[cur].right].box);
+            n[cur].cost = mbox_cost(n[cur].box);
+        }
+        auto swp = [&](int a, int b) {
+            int pa = n[a].parent, pb = n[b].parent;
+            if (n[pa].left == a) n[pa].left = b; else n[pa].right = b;
+            if (n[pb].left == b) n[pb].left = a; else n[pb].right = a;
+            n[a].parent = pb;
+            n[b].parent = pa;
+        };
+        for (int cur = n[nl].parent; cur >= 0 && n[cur].parent >= 0; cur = n[cur].parent) {
+            const int pp = n[cur].parent;
+            const int sib = n[pp].left == cur ? n[pp].right : n[pp].left;
+            MBox slb = mbox_union(n[n[cur].right].box, n[sib].box), srb = mbox_union(n[n[cur].left].box, n[sib].box), clb, crb;
+            double sl = mbox_cost(slb), sr = mbox_cost(srb), cl, cr;
+            if (n[sib].leaf) { cl = cr = std::numeric_limits<double>::infinity(); }
+            else {
+                clb = mbox_union(n[n[sib].right].box, n[cur].box);
+                crb = mbox_union(n[n[sib].left].box, n[cur].box);
+                cl = mbox_cost(clb);
+                cr = mbox_cost(crb);
+            }
+            double clc = cl - n[sib].cost, crc = cr - n[sib].cost, slc = sl - n[cur].cost, src = sr - n[cur].cost;
+            double mn = std::min(clc, std::min(crc, std::min(slc, src)));
+            if (mn >= 0) continue;
+            if (mn == clc) { swp(cur, n[sib].left); n[sib].box = clb; n[sib].cost = cl; }
+            else if (mn == crc) { swp(cur, n[sib].right); n[sib].box = crb; n[sib].cost = cr; }
+            else if (mn == slc) { swp(sib, n[cur].left); n[cur].box = slb; n[cur].cost = sl; }
+            else { swp(sib, n[cur].right); n[cur].box = srb; n[cur].cost = sr; }
+        }
+    }
+};
+
+static float4 f4b(const D3& v, int bits) {
+    float4 o = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+    std::memcpy(&o.w, &bits, 4);
+    return o;
+}
+
+static Shape pack_mesh(const std::vector<D3>& pts, const std::vector<std::array<int, 3>>& tris, D3* lo_out, D3* hi_out) {
+    struct E { int p1, p2, opp, id = -1; uint64_t key; };
+    struct TN { int p[3]; int nb[3]; E e[3]; D3 normal; };
+    auto mkE = [](int a, int b, int o) {
+        E e; e.p1 = a; e.p2 = b; e.opp = o;
+        uint64_t mx = (uint32_t)std::max(a, b), mn = (uint32_t)std::min(a, b);
+        e.key = ((mx << 32) & 0xFFFFFFFF00000000ull) + mn;
+        return e;
+    };
+    std::vector<TN> g(tris.size());
+    for (size_t i = 0; i < tris.size(); i++) {
+        const auto& t = tris[i];
+        TN& x = g[i];
+        for (int k = 0; k < 3; k++) { x.p[k] = t[k]; x.nb[k] = -1; }
+        x.e[0] = mkE(t[0], t[1], t[2]); x.e[1] = mkE(t[1], t[2], t[0]); x.e[2] = mkE(t[2], t[0], t[1]);
+        x.normal = (pts[t[1]] - pts[t[0]]).cross(pts[t[2]] - pts[t[0]]).normalize();
+    }
+    std::unordered_map<uint64_t, unsigned> efm;
+    for (size_t i = 0; i < g.size(); i++)
+        for (int j = 0; j < 3; j++) {
+            auto q = efm.find(g[i].e[j].key);
+            if (q != efm.end()) {
+                g[i].nb[j] = (int)q->second;
+                for (int k = 0; k < 3; k++)
+                    if (g[q->second].e[k].key == g[i].e[j].key) g[q->second].nb[k] = (int)i;
+                efm.erase(q);
+            } else {
+                efm[g[i].e[j].key] = (unsigned)i;
+            }
+        }
+    std::vector<float4> tri_data;
+    std::vector<MBox> boxes;
+    int next_edge = (int)(tris.size() + pts.size());
+    for (size_t ti = 0; ti < g.size(); ti++) {
+        TN& t = g[ti];
+        D3 v[3] = {pts[t.p[0]], pts[t.p[1]], pts[t.p[2]]};
+        D3 out[3];
+        int eid[3];
+        std::vector<D3> gauss;
+        int concave = 0;
+        for (int i = 0; i < 3; i++) {
+            out[i] = (v[(i + 1) % 3] - v[i]).cross(t.normal).normalize();
+            if (t.e[i].id == -1) t.e[i].id = next_edge++;
+            eid[i] = t.e[i].id;
+            if (t.nb[i] == -1) { gauss.push_back(out[i]); continue; }
+            E comp{};
+            for (int j = 0; j < 3; j++) {
+                const E& ne = g[t.nb[i]].e[j];
+                if (t.e[i].p1 == ne.p2 && t.e[i].p2 == ne.p1) comp = ne;
+            }
+            bool conc = (pts[comp.opp] - pts[t.e[i].opp]).normalize().dot(t.normal) >= -0.00001;
+            if (conc) { concave++; if (concave <= 1) gauss.push_back(t.normal); }
+            else gauss.push_back(g[t.nb[i]].normal);
+        }
+        MBox b{D3(std::min(v[0].x, std::min(v[1].x, v[2].x)), std::min(v[0].y, std::min(v[1].y, v[2].y)), std::min(v[0].z, std::min(v[1].z, v[2].z))),
+               D3(std::max(v[0].x, std::max(v[1].x, v[2].x)), std::max(v[0].y, std::max(v[1].y, v[2].y)), std::max(v[0].z, std::max(v[1].z, v[2].z)))};
+        boxes.push_back(b);
+        tri_data.push_back(f4b(t.normal, concave));
+        for (int i = 0; i < 3; i++) tri_data.push_back(f4b(v[i], 0));
+        for (int i = 0; i < 3; i++) tri_data.push_back(f4b(out[i], 0));
+        for (int i = 0; i < 3; i++) tri_data.push_back(f4b(i < (int)gauss.size() ? gauss[i] : D3(), i == 0 ? (int)gauss.size() : 0));
+        float4 ids;
+        int idv[4] = {eid[0], eid[1], eid[2], (int)ti};
+        std::memcpy(&ids, idv, 16);
+        tri_data.push_back(ids);
+        tri_data.push_back(f4b(b.lo, 0));
+        tri_data.push_back(f4b(b.hi, 0));
+    }
+    MTree tree;
+    for (int i = 0; i < (int)boxes.size(); i++) tree.add(i, boxes[i]);
+    // flatten with the root first (indices remapped)
+    std::vector<int> order, remap(tree.n.size(), -1);
+    std::vector<int> st{tree.root};
+    while (!st.empty()) {
+        int x = st.back();
+        st.pop_back();
+        remap[x] = (int)order.size();
+        order.push_back(x);
+        if (!tree.n[x].leaf) { st.push_back(tree.n[x].right); st.push_back(tree.n[x].left); }
+    }
+    HullHeader H;
+    std::memset(&H, 0, sizeof(H));
+    H.kind = SHAPE_MESH;
+    H.pad[0] = (uint32_t)tris.size();
+    H.pad[1] = (uint32_t)order.size();
+    std::vector<uint8_t> blob(sizeof(HullHeader));
+    MBox all = boxes[0];
+    for (size_t i = 1; i < boxes.size(); i++) all = mbox_union(all, boxes[i]);
+    put(blob, f4b(all.lo, 0));
+    put(blob, f4b(all.hi, 0));
+    for (int x : order) {
+        const MTree::Node& nd = tree.n[x];
+        // node boxes rounded outwards so FP32 traversal never drops a candidate
+        // the FP64 test keeps; leaves carry the triangle's own box (in the
+        // triangle record) for the final test
+        auto down = [](double v) { float f = (float)v; return (double)f > v ? std::nextafter(f, -INFINITY) : f; };
+        auto up = [](double v) { float f = (float)v; return (double)f < v ? std::nextafter(f, INFINITY) : f; };
+        float4 lo = make_float4(down(nd.box.lo.x), down(nd.box.lo.y), down(nd.box.lo.z), 0.f);
+        float4 hi = make_float4(up(nd.box.hi.x), up(nd.box.hi.y), up(nd.box.hi.z), 0.f);
+        int l = nd.leaf ? -1 : remap[nd.left];
+        int r = nd.leaf ? nd.obj : remap[nd.right];
+        std::memcpy(&lo.w, &l, 4);
+        std::memcpy(&hi.w, &r, 4);
+        put(blob, lo);
+        put(blob, hi);
+    }
+    for (const float4& f : tri_data) put(blob, f);
+    std::memcpy(blob.data(), &H, sizeof(H));
+    *lo_out = all.lo;
+    *hi_out = all.hi;
+    Shape sh;
+    sh.blob = std::move(blob);
+    sh.hot = 0;   // read from global memory, never staged
+    return sh;
+}
+
 // ---------------------------------------------------------------- device batch ----
 struct Arena {
     uint8_t* base = nullptr;
@@ -280,6 +493,7 @@ struct Batch {
     int n_sms = 0;
     int slot_bytes = 0;
     bool prims = false;                // the batch holds spheres or cylinders
+    bool meshes = false;               // the batch holds static triangle meshes
     bool joints = false;               // the batch holds joints
     bool systems = false;              // ... and holonomic systems
     cudaStream_t st = nullptr;
@@ -319,7 +533,7 @@ struct Batch {
         mark(0);
         launch_gravity(x, L);      mark(1);
         launch_pairs(x, L);        mark(2);
-        launch_narrowphase(x, slot_bytes, n_sms, prims, st); mark(3);
+        launch_narrowphase(x, slot_bytes, n_sms, prims, st); mark(3);   // + mesh pairs
         launch_merge(x, L);        mark(4);
         launch_islands(x, L);
         launch_pgs_schedule(x, L); mark(5);
@@ -333,11 +547,11 @@ struct Batch {
         launch_geometry(x, 0, L);  mark(6 + 3 * substeps);
     }
     // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 1
-    // (+1 with spheres / cylinders), merge 6 + 3 scans, islands 2 + scan 3,
+    // (+1 with spheres / cylinders, +1 with meshes), merge 6 + 3 scans, islands 2 + scan 3,
     // schedule 3, 4 per substep (rows, small + large PGS, integrate), geometry 1
     // (+2 per substep and 1 factorisation with joints)
     int launches_per_step() const {
-        return 1 + 6 + 1 + (prims ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 4 * substeps + 1 + (joints ? 2 * substeps : 0) +
+        return 1 + 6 + 1 + (prims ? 1 : 0) + (meshes ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 4 * substeps + 1 + (joints ? 2 * substeps : 0) +
                (systems ? 1 : 0);
     }
 
@@ -371,6 +585,7 @@ struct Batch {
         if (s & ST_CONTACT_OVERFLOW) m += " contact-capacity-overflow";
         if (s & ST_CLIP_OVERFLOW) m += " clip-overflow";
         if (s & ST_STACK_OVERFLOW) m += " island-stack-overflow";
+        if (s & ST_MESH_OVERFLOW) m += " mesh-pair-overflow";
         if (s & ST_NAN) m += " non-finite-state";
         if (s & ST_TIMEOUT) m += " bounded-wait-timeout";
         int code = (s & ST_NAN) ? CPGPU_ERR_NAN : (s & ST_TIMEOUT) ? CPGPU_ERR_TIMEOUT : CPGPU_ERR_CAPACITY;
@@ -526,6 +741,25 @@ static JointGraph joint_graph(const World& w, const std::vector<int>& map_order)
     return G;
 }
 
+static bool is_mesh(const World& w, uint32_t id) {
+    const Shape& sh = w.shapes[w.bodies[id - 1].shape];
+    return reinterpret_cast<const HullHeader*>(sh.blob.data())->kind == SHAPE_MESH;
+}
+
+// The cID of a contact's MagicID (CollisionDetect.cpp: the primitives' ids,
+// first body low): body ids for convex pairs; for a mesh pair the convex body's
+// id and the triangle id, which is the only part the device keeps.
+static uint64_t contact_cid(const World& w, uint32_t b1, uint32_t b2, int tri) {
+    if (is_mesh(w, b1)) return (uint32_t)tri | ((uint64_t)b2 << 32);
+    if (is_mesh(w, b2)) return b1 | ((uint64_t)(uint32_t)tri << 32);
+    return ((uint64_t)b2 << 32) | b1;
+}
+static int contact_tri(const World& w, uint32_t b1, uint32_t b2, uint64_t cid) {
+    if (is_mesh(w, b1)) return (int)(uint32_t)(cid & 0xffffffffu);
+    if (is_mesh(w, b2)) return (int)(uint32_t)(cid >> 32);
+    return 0;
+}
+
 static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     auto B = std::make_unique<Batch>();
     B->n_worlds = (int)worlds.size();
@@ -581,7 +815,9 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
                 shape_pool_off[s] = it->second;
             }
             max_hot = std::max(max_hot, (sh.hot + 15) & ~15);
-            if (reinterpret_cast<const HullHeader*>(sh.blob.data())->kind != SHAPE_HULL) B->prims = true;
+            const uint32_t kind = reinterpret_cast<const HullHeader*>(sh.blob.data())->kind;
+            if (kind == SHAPE_SPHERE || kind == SHAPE_CYLINDER) B->prims = true;
+            if (kind == SHAPE_MESH) B->meshes = true;
         }
         const int base = wstart[wi];
         for (size_t i = 0; i < w.bodies.size(); i++) {
@@ -630,10 +866,11 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     std::vector<int> ecstart, eccount;
     std::vector<uint64_t> cmag;
     std::vector<float4> cp1, cp2, cn, cimp, cfu, cfw;
-    std::vector<int> cstate, cedge;
+    std::vector<int> cstate, cedge, ctri;
     for (size_t wi = 0; wi < worlds.size(); wi++) {
         const int base = wstart[wi];
         for (const cpgpu_contact& c : worlds[wi]->contacts) {
+            ctri.push_back(contact_tri(*worlds[wi], c.b1, c.b2, c.magic_c));
             uint64_t key = ((uint64_t)(base + c.b1 - 1) << 32) | (uint32_t)(base + c.b2 - 1);
             if (ekey.empty() || ekey.back() != key) {
                 ekey.push_back(key);
@@ -725,6 +962,8 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     const int cap_pairs = std::max(floor_, env_int("CPGPU_PAIRS_PER_BODY", 24) * N);
     const int cap_edges = cap_pairs;
     const int cap_contacts = std::max(std::max(2 * floor_, 2 * (int)cmag.size()), env_int("CPGPU_CONTACTS_PER_BODY", 24) * N);
+    const int cap_mesh = B->meshes ? std::max(4096, env_int("CPGPU_MESH_POINTS_PER_BODY", 32) * N) : 0;
+    const int mesh_warps = B->meshes ? mesh_scratch_warps(B->n_sms) : 0;
     const int scan_tmp = std::max(cap_pairs, cap_contacts) / 1024 + 64;
     Dev x;
     EdgeStore es[2];
@@ -769,6 +1008,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
             cs[k].p1 = A.take<float4>(cap_contacts); cs[k].p2 = A.take<float4>(cap_contacts); cs[k].n = A.take<float4>(cap_contacts);
             cs[k].imp = A.take<float4>(cap_contacts); cs[k].fu = A.take<float4>(cap_contacts); cs[k].fw = A.take<float4>(cap_contacts);
             cs[k].state = A.take<int>(cap_contacts); cs[k].edge = A.take<int>(cap_contacts);
+            cs[k].tri = A.take<int>(cap_contacts);
         }
         counts = A.take<int>(64);   // n_pairs, n_edges[2], n_contacts[2], n_islands, status, .., cnt[16..]
         x.n_pairs = counts + 0;
@@ -796,6 +1036,16 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         x.sched = A.take<int>(96);
         x.status = counts + 6;
         x.cnt = counts + 16;
+        if (B->meshes) {
+            x.has_mesh = 1;
+            x.cap_mesh_pts = cap_mesh;
+            x.mesh_warps = mesh_warps;
+            x.mf_ofs = A.take<int>(cap_pairs);
+            x.mm_pt = A.take<float4>(cap_mesh); x.mm_n = A.take<float4>(cap_mesh);
+            x.mm_magic = A.take<uint64_t>(cap_mesh); x.mm_tri = A.take<int>(cap_mesh);
+            x.mm_count = counts + 8;
+            x.msc = A.take<MeshScratch>(mesh_warps);
+        }
         x.n_joints = n_joints;
         x.n_joint_edges = n_je;
         x.lin_err_threshold = 15.0f;   // excessive_linear_error_torque_threshold (PhysicsEngine.h:217)
@@ -859,6 +1109,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     up(cs[0].p1, cp1.data(), nc * 16); up(cs[0].p2, cp2.data(), nc * 16); up(cs[0].n, cn.data(), nc * 16);
     up(cs[0].imp, cimp.data(), nc * 16); up(cs[0].fu, cfu.data(), nc * 16); up(cs[0].fw, cfw.data(), nc * 16);
     up(cs[0].state, cstate.data(), nc * 4); up(cs[0].edge, cedge.data(), nc * 4);
+    up(cs[0].tri, ctri.data(), nc * 4);
     int host_counts[5] = {0, ne, 0, nc, 0};   // n_pairs, n_edges[0], n_edges[1], n_contacts[0], n_contacts[1]
     up(counts, host_counts, sizeof(host_counts));
     if (n_joints > 0) {
@@ -932,7 +1183,7 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
     // contact graph (current = the old buffers of the next step)
     const int ne = *(&counts[1] + B.parity), nc = *(&counts[3] + B.parity);
     std::vector<uint64_t> key(ne), mag(nc);
-    std::vector<int> cstart(ne), ccount(ne), state(nc);
+    std::vector<int> cstart(ne), ccount(ne), state(nc), tri(nc);
     std::vector<float4> p1(nc), p2(nc), n(nc), imp(nc), fu(nc), fw(nc);
     const EdgeStore& E = x.e_old;
     const ContactStore& C = x.c_old;
@@ -950,6 +1201,7 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
         CK(cudaMemcpyAsync(fu.data(), C.fu, nc * 16, cudaMemcpyDeviceToHost, B.st));
         CK(cudaMemcpyAsync(fw.data(), C.fw, nc * 16, cudaMemcpyDeviceToHost, B.st));
         CK(cudaMemcpyAsync(state.data(), C.state, nc * 4, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(tri.data(), C.tri, nc * 4, cudaMemcpyDeviceToHost, B.st));
     }
     int np = counts[0];
     std::vector<int> pa(np), pb(np);
@@ -993,7 +1245,7 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
                 c.b1 = b1; c.b2 = b2;
                 c.live = cs_live(state[k]);
                 c.memory_life = cs_life(state[k]);
-                c.magic_c = ((uint64_t)b2 << 32) | b1;
+                c.magic_c = contact_cid(w, b1, b2, tri[k]);
                 c.magic_b = mag[k];
                 c.p_local_b1[0] = p1[k].x; c.p_local_b1[1] = p1[k].y; c.p_local_b1[2] = p1[k].z;
                 c.p_local_b2[0] = p2[k].x; c.p_local_b2[1] = p2[k].y; c.p_local_b2[2] = p2[k].z;
@@ -1035,7 +1287,7 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
         std::vector<float> iw, iinv, jimp;
         std::vector<float4> ju, jw;
         std::vector<uint64_t> key, mag;
-        std::vector<int> cstart, ccount, state;
+        std::vector<int> cstart, ccount, state, tri;
         std::vector<float4> p1, p2, nrm, imp, fu, fw;
     };
     std::vector<Buf> bufs(n);
@@ -1061,7 +1313,8 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
         b.key.resize(ne); b.cstart.resize(ne); b.ccount.resize(ne);
         get(b.key.data(), x.e_old.key + e0, ne * 8); get(b.cstart.data(), x.e_old.cstart + e0, ne * 4);
         get(b.ccount.data(), x.e_old.ccount + e0, ne * 4);
-        b.mag.resize(nc); b.state.resize(nc);
+        b.mag.resize(nc); b.state.resize(nc); b.tri.resize(nc);
+        get(b.tri.data(), x.c_old.tri + c0, nc * 4);
         b.p1.resize(nc); b.p2.resize(nc); b.nrm.resize(nc); b.imp.resize(nc); b.fu.resize(nc); b.fw.resize(nc);
         get(b.mag.data(), x.c_old.magic + c0, nc * 8); get(b.state.data(), x.c_old.state + c0, nc * 4);
         get(b.p1.data(), x.c_old.p1 + c0, nc * 16); get(b.p2.data(), x.c_old.p2 + c0, nc * 16);
@@ -1100,7 +1353,7 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
                 c.b1 = b1; c.b2 = b2;
                 c.live = cs_live(b.state[k]);
                 c.memory_life = cs_life(b.state[k]);
-                c.magic_c = ((uint64_t)b2 << 32) | b1;
+                c.magic_c = contact_cid(w, b1, b2, b.tri[k]);
                 c.magic_b = b.mag[k];
                 c.p_local_b1[0] = b.p1[k].x; c.p_local_b1[1] = b.p1[k].y; c.p_local_b1[2] = b.p1[k].z;
                 c.p_local_b2[0] = b.p2[k].x; c.p_local_b2[1] = b.p2[k].y; c.p_local_b2[2] = b.p2[k].z;
@@ -1347,8 +1600,41 @@ int cpgpu_body_cylinder(cpgpu_world* w, const double base[3], double radius, dou
         return CPGPU_OK;
     });
 }
-int cpgpu_body_mesh(cpgpu_world*, const double*, int, const int*, int, const cpgpu_material*, int, uint32_t*) {
-    return fail(CPGPU_ERR_UNSUPPORTED, "static meshes are not implemented on the device path yet");
+// createRigidBody(StaticMeshGeometry(MeshInput{tris, points}), fixed)
+// (PhysicsEngine.cpp:498-512, RigidBody.cpp:41-58): a fixed body at the
+// origin whose triangles are in world coordinates
+int cpgpu_body_mesh(cpgpu_world* w, const double* points, int n_points, const int* tris, int n_tris, const cpgpu_material* m,
+                    int fixed, uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!fixed) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "kinematic meshes are not implemented on the device path"};
+        if (!points || !tris || n_points < 3 || n_tris < 1) throw ApiFail{CPGPU_ERR_INVALID_ARG, "mesh needs >= 3 points and >= 1 triangle"};
+        std::vector<D3> pts(n_points);
+        for (int i = 0; i < n_points; i++) pts[i] = D3(points[3 * i], points[3 * i + 1], points[3 * i + 2]);
+        std::vector<std::array<int, 3>> t(n_tris);
+        for (int i = 0; i < n_tris; i++)
+            for (int k = 0; k < 3; k++) {
+                int x = tris[3 * i + k];
+                if (x < 0 || x >= n_points) throw ApiFail{CPGPU_ERR_INVALID_ARG, "mesh index out of range"};
+                t[i][k] = x;
+            }
+        D3 lo, hi;
+        Shape sh = pack_mesh(pts, t, &lo, &hi);
+        Body b;
+        b.movement = CPGPU_FIXED;
+        b.mass = std::numeric_limits<double>::quiet_NaN();
+        for (int k = 0; k < 9; k++) { b.iref[k] = 0; b.iinv_ref[k] = 0; b.iw[k] = 0; b.iinv[k] = 0; }
+        b.local_origin = D3();
+        if (m) { b.rest = m->restitution; b.kin = m->kinetic_friction; b.sta = m->static_friction; }
+        begin_mutation(w->w);
+        b.shape = (int)w->w.shapes.size();
+        w->w.shapes.push_back(std::move(sh));
+        w->w.bodies.push_back(b);
+        uint32_t id = (uint32_t)w->w.bodies.size();
+        w->w.nodes[id] = (int)id - 1;
+        if (out_id) *out_id = id;
+        return CPGPU_OK;
+    });
 }
 
 int cpgpu_body_set_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {

@@ -114,23 +114,28 @@ __global__ void k_contacts(Dev d, int write) {
         int ids[kMaxEdgeContacts];
         signed char upd[kMaxEdgeContacts];
         uint64_t mags[kMaxEdgeContacts];
+        int tris[kMaxEdgeContacts];
         int n = 0;
         const int src = d.edge_src[e], p = d.edge_pair[e];
         if (src >= 0) {
             int s = d.e_old.cstart[src], c = d.e_old.ccount[src];
             for (int k = s; k < s + c; k++) {
                 if (cs_dead(d.c_old.state[k])) continue;
-                if (n < kMaxEdgeContacts) { ids[n] = k; mags[n] = d.c_old.magic[k]; upd[n] = -1; n++; }
+                if (n < kMaxEdgeContacts) { ids[n] = k; mags[n] = d.c_old.magic[k]; tris[n] = d.c_old.tri[k]; upd[n] = -1; n++; }
                 else atomicOr(d.status, ST_CONTACT_OVERFLOW);
             }
         }
+        // a mesh pair's points (each with its merged manifold's normal) are in
+        // the mesh store; the MagicID's cID then carries the triangle id
+        const int mofs = (p >= 0 && d.has_mesh) ? d.mf_ofs[p] : -1;
         int np = (p >= 0) ? d.mf_cnt[p] : 0;
         for (int k = 0; k < np; k++) {
-            uint64_t m = d.mf_magic[4 * p + k];
+            uint64_t m = mofs >= 0 ? d.mm_magic[mofs + k] : d.mf_magic[4 * p + k];
+            int t = mofs >= 0 ? d.mm_tri[mofs + k] : 0;
             int j = 0;
-            while (j < n && mags[j] != m) j++;
+            while (j < n && (mags[j] != m || tris[j] != t)) j++;
             if (j < n) upd[j] = (signed char)k;
-            else if (n < kMaxEdgeContacts) { ids[n] = -1; mags[n] = m; upd[n] = (signed char)k; n++; }
+            else if (n < kMaxEdgeContacts) { ids[n] = -1; mags[n] = m; tris[n] = t; upd[n] = (signed char)k; n++; }
             else atomicOr(d.status, ST_CONTACT_OVERFLOW);
         }
         if (!write) { d.edge_cnt[e] = n; continue; }
@@ -161,9 +166,9 @@ __global__ void k_contacts(Dev d, int write) {
                 st = cs_make(0, false, false, false);
             }
             if (upd[j] >= 0) {
-                float4 pt = d.mf_pt[4 * p + upd[j]];
+                float4 pt = mofs >= 0 ? d.mm_pt[mofs + upd[j]] : d.mf_pt[4 * p + upd[j]];
                 f3 pos = mk(pt);
-                f3 nw = mk(d.mf_n[p]);
+                f3 nw = mk(mofs >= 0 ? d.mm_n[mofs + upd[j]] : d.mf_n[p]);
                 f3 nl = mul(i1, nw), l1 = mul(i1, pos - c1), l2 = mul(i2, pos - c2);
                 float fc = (ids[j] >= 0) ? (cs_static(st) ? sta : kin) : kin;
                 p1 = make_float4(l1.x, l1.y, l1.z, pt.w);
@@ -175,6 +180,7 @@ __global__ void k_contacts(Dev d, int write) {
             N.p1[dst] = p1; N.p2[dst] = p2; N.n[dst] = nn; N.imp[dst] = imp; N.fu[dst] = fu; N.fw[dst] = fw;
             N.state[dst] = st;
             N.edge[dst] = e;
+            N.tri[dst] = tris[j];
         }
     }
 }

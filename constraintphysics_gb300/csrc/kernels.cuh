@@ -23,6 +23,7 @@ void launch_geometry(const Dev& d, int force_all, const Launch& L);
 // hull-hull pairs, then (when the batch holds spheres or cylinders) the pairs
 // that involve one
 void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st);
+int mesh_scratch_warps(int n_sms);   // per-warp scratch entries the mesh narrowphase uses
 void launch_merge(const Dev& d, const Launch& L);
 void launch_islands(const Dev& d, const Launch& L);
 // per-world edge / contact ranges of the current graph (4 ints per world)

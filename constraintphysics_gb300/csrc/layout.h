@@ -45,10 +45,40 @@ static_assert(sizeof(HullHeader) == 48, "hull header size");
 //   float4 gv[14] Gauss vertices: caps (+axis, -axis), then the ring
 //   float4 top[8] top-cap 8-gon
 //   float4 bot[8] bottom-cap 8-gon
-enum ShapeKind : uint32_t { SHAPE_HULL = 0, SHAPE_SPHERE = 1, SHAPE_CYLINDER = 2 };
+enum ShapeKind : uint32_t { SHAPE_HULL = 0, SHAPE_SPHERE = 1, SHAPE_CYLINDER = 2, SHAPE_MESH = 3 };
 constexpr int kCylRing = 12, kCylCap = 8;
 constexpr int kCylOffAxis = 64, kCylOffGv = 80, kCylOffTop = 80 + 16 * 14, kCylOffBot = 80 + 16 * 22;
 constexpr int kSphereBlob = 64, kCylBlob = 80 + 16 * 30;
+
+// ---- static triangle mesh blob (kind 3; world coordinates; read from global,
+// never staged).  Header pad[0] = triangles, pad[1] = tree nodes (root first):
+//   float4 lo, hi                  mesh AABB
+//   nodes: float4 lo (w: left child, bits; -1 = leaf), float4 hi (w: right
+//          child or, for a leaf, the triangle index, bits)
+//   triangles, kMeshTriF4 float4 each: normal (w: concave-neighbour count,
+//          bits), v0, v1, v2 (w: unused), out0..2 (outward edge directions),
+//          g0..2 (Gauss region; g0.w: its size, bits), ids (edge ids 0..2,
+//          triangle id, bits), aabb lo, hi
+constexpr int kMeshTriF4 = 13;
+constexpr int kMeshOffNodes = 80;
+// per-pair limits of the mesh narrowphase (exceeding one sets ST_MESH_OVERFLOW)
+constexpr int kMeshCand = 128;   // candidate triangles
+constexpr int kMeshMans = 64;    // triangle manifolds
+constexpr int kMeshRaw = 256;    // their points before the merge and cull
+constexpr int kMeshOut = 64;     // contact points after it
+constexpr int kMeshStack = 64;   // tree traversal depth
+
+// per-warp scratch of the mesh narrowphase (global memory, one per resident warp)
+struct alignas(16) MeshScratch {
+    float4 pt[kMeshRaw];               // raw points: xyz, w pen
+    float4 man_n[kMeshMans];           // triangle manifold normal, w its pen
+    float4 out_n[kMeshOut];            // normal of each kept point's merged manifold
+    unsigned long long magic[kMeshRaw];
+    int tri[kMeshRaw];                 // triangle id of each raw point
+    int man_first[kMeshMans], man_cnt[kMeshMans];
+    int cand[kMeshCand];
+    int out[kMeshOut];                 // kept raw points
+};
 
 constexpr int kMaxHullVerts = 255;   // uint8 vertex ids
 constexpr int kMaxHullFaces = 255;
@@ -74,7 +104,7 @@ struct WorldParams {
 // ---- status word bits ----------------------------------------------------------
 enum StatusBits : int {
     ST_PAIR_OVERFLOW = 1, ST_EDGE_OVERFLOW = 2, ST_CONTACT_OVERFLOW = 4,
-    ST_NAN = 8, ST_TIMEOUT = 16, ST_CLIP_OVERFLOW = 32, ST_STACK_OVERFLOW = 64,
+    ST_NAN = 8, ST_TIMEOUT = 16, ST_CLIP_OVERFLOW = 32, ST_STACK_OVERFLOW = 64, ST_MESH_OVERFLOW = 128,
 };
 
 // contact state word: bits 0-7 life (int8), bit 8 live, bit 9 static_ready, bit 10 dead
@@ -98,6 +128,7 @@ struct ContactStore {
     float4* fw;          // friction basis w
     int* state;          // cs_* bits
     int* edge;           // owning edge (index in the edge list)
+    int* tri;            // mesh triangle id of the cID (0 for convex pairs)
 };
 
 struct EdgeStore {
@@ -218,6 +249,16 @@ struct Dev {
     int* mf_cnt;
     float4* mf_pt;                 // [4] per pair: pos xyz, w pen
     uint64_t* mf_magic;            // [4] per pair
+    // static meshes (has_mesh == 0: none in the batch).  A mesh pair's points
+    // are in the mesh store at mf_ofs[p] (-1: not a mesh pair), mf_cnt[p] of
+    // them, each with its merged manifold's normal; mf_n[p].w is their max pen
+    int has_mesh, cap_mesh_pts, mesh_warps;
+    int* mf_ofs;
+    float4 *mm_pt, *mm_n;
+    uint64_t* mm_magic;
+    int* mm_tri;
+    int* mm_count;
+    MeshScratch* msc;
     // persistent graph (double-buffered by the host)
     EdgeStore e_old, e_new;
     ContactStore c_old, c_new;

@@ -29,6 +29,7 @@ constexpr int kMaxClip = 40;
 constexpr int kQueue = 64;                       // queued edge-edge axes per warp
 constexpr int kQueueBytes = kQueue * (16 + 4);
 constexpr long long kSpinLimit = 1LL << 24;  // bounded mbarrier wait
+constexpr int kMeshBlocksPerSm = 2;          // mesh-pair kernel grid (its scratch is per warp)
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -843,6 +844,329 @@ __device__ __forceinline__ void narrow_prim(const Dev& d, int p, int a, int b, u
     emit_manifold(d, p, o.n, o.pen, o.pts, o.magic, o.m);
 }
 
+// ---- static triangle meshes --------------------------------------------------------
+// One face of a StaticMeshGeometry (Geometry.h:120-175) read from the mesh blob.
+struct TriView {
+    f3 n;            // face normal
+    int concave;     // concave neighbours (normalDirectionValid's case)
+    f3 v[3], out[3]; // vertices; outward edge directions (edge i: v[i] -> v[i+1])
+    f3 g[3];         // Gauss region
+    int ng;
+    int eid[3], id;
+    f3 lo, hi;
+};
+
+__device__ __forceinline__ void load_tri(const float4* t, TriView* T) {
+    float4 x = __ldg(t);
+    T->n = mk(x);
+    T->concave = __float_as_int(x.w);
+    for (int i = 0; i < 3; i++) T->v[i] = mk(__ldg(t + 1 + i));
+    for (int i = 0; i < 3; i++) T->out[i] = mk(__ldg(t + 4 + i));
+    float4 g0 = __ldg(t + 7);
+    T->g[0] = mk(g0);
+    T->ng = __float_as_int(g0.w);
+    T->g[1] = mk(__ldg(t + 8));
+    T->g[2] = mk(__ldg(t + 9));
+    int4 ids = __ldg(reinterpret_cast<const int4*>(t + 10));
+    T->eid[0] = ids.x; T->eid[1] = ids.y; T->eid[2] = ids.z; T->id = ids.w;
+    T->lo = mk(__ldg(t + 11));
+    T->hi = mk(__ldg(t + 12));
+}
+
+// findTriangleExtrema (CollisionDetect.cpp:2004-2021)
+__device__ __forceinline__ Ext triExt(const TriView& T, f3 d) {
+    Ext e{INFINITY, -INFINITY, -1, -1};
+    for (int i = 0; i < 3; i++) {
+        float x = dot(T.v[i], d);
+        if (x < e.mn) { e.mn = x; e.mn_id = i; }
+        if (x > e.mx) { e.mx = x; e.mx_id = i; }
+    }
+    return e;
+}
+
+// normalDirectionValid (CollisionDetect.cpp:2024-2060): the direction lies in
+// the face's Gauss region (a spherical triangle, an arc, or the normal alone)
+__device__ bool triNormalValid(const TriView& T, f3 n) {
+    const float eps = 0.0001f;
+    if (T.concave <= 1) {
+        for (int i = 0; i < T.ng; i++)
+            if (dot(n, cross(T.g[i], T.g[(i + 1) % T.ng])) < -eps) return false;
+        return true;
+    }
+    if (T.concave == 2) {
+        f3 arc = cross(T.g[0], T.g[1]);
+        if (fabsf(dot(n, arc)) > eps) return false;
+        if (dot(n, cross(arc, T.g[0])) < -eps) return false;
+        return !(dot(n, cross(T.g[1], arc)) < -eps);
+    }
+    return !(dot(n, T.n) < 1.f - eps);
+}
+
+// one axis of a triangle SAT: the plain minimum and the minimum whose contact
+// normal (pointing into the triangle) lies in the face's Gauss region, both
+// first-in-order on ties
+__device__ __forceinline__ void triCheck(const Ext& a, const Ext& b, f3 n, int idx, const TriView& T, Axis* best,
+                                         Axis* valid, bool* sep) {
+    float fwd = a.mx - b.mn, rev = b.mx - a.mn;
+    Axis x;
+    if (fwd < rev) x = Axis{fwd, idx, a.mx_id, b.mn_id, n};
+    else x = Axis{rev, idx, a.mn_id, b.mx_id, -n};
+    if (x.pen < 0.f) { *sep = true; return; }
+    if (x.pen < best->pen || (x.pen == best->pen && idx < best->idx)) *best = x;
+    if ((x.pen < valid->pen || (x.pen == valid->pen && idx < valid->idx)) && triNormalValid(T, -1.f * x.n)) *valid = x;
+}
+
+// the six Gauss arcs of a face, negated as the other side of an arc pair:
+// normal -> out[i], out[i] -> -normal
+__device__ __forceinline__ void triArc(const TriView& T, int k, f3* b1, f3* b2) {
+    const int i = k >> 1;
+    if ((k & 1) == 0) { *b1 = -1.f * T.n; *b2 = -1.f * T.out[i]; }
+    else { *b1 = -1.f * T.out[i]; *b2 = T.n; }
+}
+
+// findTriangleContactArea (CollisionDetect.cpp:303-329): the face (ids 0..2,
+// surface = face id), an edge next to vertex pid (both ids the edge id), or
+// the vertex
+__device__ void triArea(const TriView& T, f3 n, f3 p, int pid, f3 u, f3 w, Area* a) {
+    if (1.f - dot(T.n, n) <= kCosTol) {
+        for (int i = 0; i < 3; i++) { a->ps[i] = P2{dot(T.v[i], u), dot(T.v[i], w)}; a->ids[i] = i; }
+        a->n = 3;
+        a->surface = T.id;
+        return;
+    }
+    for (int i = 0; i < 3; i++) {
+        if (i != pid && (i + 1) % 3 != pid) continue;
+        f3 e1 = T.v[i], e2 = T.v[(i + 1) % 3];
+        if (fabsf(dot(normalize(e2 - e1), n)) <= kSinTol) {
+            a->ps[0] = P2{dot(e1, u), dot(e1, w)};
+            a->ps[1] = P2{dot(e2, u), dot(e2, w)};
+            a->ids[0] = a->ids[1] = T.eid[i];
+            a->n = 2;
+            a->surface = -1;
+            return;
+        }
+    }
+    a->ps[0] = P2{dot(p, u), dot(p, w)};
+    a->ids[0] = pid;
+    a->n = 1;
+    a->surface = -1;
+}
+
+// penalised choice of a triangle SAT: the Gauss-valid minimum when it is
+// within `penalty` of the plain one
+__device__ __forceinline__ bool triChoose(const Axis& best, const Axis& valid, float penalty, bool sep, Axis* ng, Axis* mp) {
+    if (__any_sync(0xffffffffu, sep)) return false;
+    *ng = warp_best(best);
+    Axis v = warp_best(valid);
+    *mp = (v.pen < ng->pen + penalty) ? v : *ng;
+    return mp->pen < INFINITY;
+}
+
+// SAT_PolyTriangle (CollisionDetect.cpp:2062-2194): the face normal, the hull's
+// faces, hull-arc x face-arc pairs; features and clipping from the plain
+// minimum, the manifold normal and depth from the penalised choice
+__device__ bool polyTri(const HullView& A, const TriView& T, float penalty, int lane, Scratch& scratch, CP* clipped,
+                        int* status, PrimOut* o) {
+    const HullHeader& H = *A.h;
+    const int nf = H.nf, nv = H.nv, na = H.na, total = 1 + nf + 6 * na;
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)}, valid = best;
+    bool sep = false;
+    for (int t = lane; t < total; t += 32) {
+        Ext ea;
+        f3 n;
+        if (t == 0) {
+            n = T.n;
+            ea = extrema(A.v, nv, n);
+        } else if (t <= nf) {
+            float4 g = A.n[t - 1];
+            if (g.w != 0.f) continue;
+            n = mk(g);
+            float4 c = A.cache[t - 1];
+            float shift = dot(n, A.com);
+            ea = Ext{c.y + shift, c.x + shift, __float_as_int(c.w), __float_as_int(c.z)};
+        } else {
+            int k = t - 1 - nf, ia = k / 6;
+            f3 b1, b2;
+            triArc(T, k - 6 * ia, &b1, &b2);
+            if (!arcAxis(mk(A.n[A.arc[2 * ia]]), mk(A.n[A.arc[2 * ia + 1]]), b1, b2, &n)) continue;
+            ea = extrema(A.v, nv, n);
+        }
+        triCheck(ea, triExt(T, n), n, t, T, &best, &valid, &sep);
+    }
+    Axis ng, mp;
+    if (!triChoose(best, valid, penalty, sep, &ng, &mp) || ng.aid < 0 || ng.bid < 0) return false;
+    if (lane == 0) {
+        f3 n = mp.n, u, w;
+        basis(n, &u, &w);
+        Area ac, bc;
+        contactArea(A, ng.n, ng.aid, u, w, &ac);
+        triArea(T, -1.f * ng.n, T.v[ng.bid], ng.bid, u, w, &bc);
+        int m = clipContacts(ac, bc, scratch, clipped, status);
+        points_from_pool(clipped, m, u, w, n, dot(mk(A.v[ng.aid]), n), mp.pen, o);
+        o->n = n;
+        o->pen = mp.pen;
+    }
+    return true;
+}
+
+// SAT_SphereTriangle (CollisionDetect.cpp:2196-2276): the face normal, the
+// vertices and the edges; the point is the sphere's deepest one along the
+// chosen normal, its feature id the vertex (0..2) or edge id of the plain
+// minimum (none, 0xFFFFFFFF, when the face normal is the minimum)
+__device__ bool sphereTri(const PrimView& S, const TriView& T, float penalty, int lane, PrimOut* o) {
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)}, valid = best;
+    bool sep = false;
+    if (lane < 7) {
+        f3 n;
+        if (lane == 0) n = T.n;
+        else if (lane < 4) n = normalize(T.v[lane - 1] - S.c);
+        else {
+            int i = lane - 4;
+            f3 dir = normalize(T.v[(i + 1) % 3] - T.v[i]);
+            f3 sample = T.v[i] - S.c;
+            n = normalize(sample - dir * dot(dir, sample));
+        }
+        triCheck(sphereExt(S, n), triExt(T, n), n, lane, T, &best, &valid, &sep);
+    }
+    Axis ng, mp;
+    if (!triChoose(best, valid, penalty, sep, &ng, &mp)) return false;
+    if (lane == 0) {
+        uint32_t feature = 0xFFFFFFFFu;
+        if (ng.idx >= 1 && ng.idx < 4) feature = (uint32_t)(ng.idx - 1);
+        else if (ng.idx >= 4) feature = (uint32_t)T.eid[ng.idx - 4];
+        f3 q = S.c + mp.n * S.r;
+        o->n = mp.n;
+        o->pen = mp.pen;
+        o->pts[0] = make_float4(q.x, q.y, q.z, mp.pen);
+        o->magic[0] = feature;
+        o->m = 1;
+    }
+    return true;
+}
+
+// SAT_CylinderTriangle (CollisionDetect.cpp:2466-2646): the cylinder axis, the
+// face normal, face edges x axis, the vertices radially, cylinder-arc x
+// face-arc pairs; the rim point or the clipped cap / barrel line
+__device__ bool cylTri(const PrimView& C, const TriView& T, float penalty, int lane, Scratch& scratch, CP* clipped,
+                       int* status, PrimOut* o) {
+    const int a0 = 8, total = a0 + 2 * kCylRing * 6;
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)}, valid = best;
+    bool sep = false;
+    for (int t = lane; t < total; t += 32) {
+        f3 n;
+        if (t == 0) n = C.axis;
+        else if (t == 1) n = T.n;
+        else if (t < 5) {
+            int i = t - 2;
+            if (!edgeAxis(T.v[(i + 1) % 3] - T.v[i], C.axis, &n)) continue;
+        } else if (t < a0) {
+            f3 diff = T.v[t - 5] - C.c;
+            n = normalize(diff - C.axis * dot(C.axis, diff));
+        } else {
+            int k = t - a0, ia = k / 6;
+            f3 g1, g2, b1, b2;
+            cylArc(C, ia, &g1, &g2);
+            triArc(T, k - 6 * ia, &b1, &b2);
+            if (!arcAxis(g1, g2, b1, b2, &n)) continue;
+        }
+        triCheck(cylExt(C, n), triExt(T, n), n, t, T, &best, &valid, &sep);
+    }
+    Axis ng, mp;
+    if (!triChoose(best, valid, penalty, sep, &ng, &mp) || ng.bid < 0) return false;
+    if (lane == 0) {
+        f3 n = mp.n, u, w;
+        basis(n, &u, &w);
+        f3 amax = diskExtremum(dot(C.axis, n) > 0.f ? topCenter(C) : botCenter(C), C.axis, C.r, n);
+        Area ac, bc;
+        int ak = cylArea(C, ng.n, u, w, &ac);
+        triArea(T, -1.f * ng.n, T.v[ng.bid], ng.bid, u, w, &bc);
+        int m;
+        if (ak == 2) { clipped[0] = CP{ac.ps[0], 0, 0ull, 0}; m = 1; }
+        else m = clipContacts(ac, bc, scratch, clipped, status);
+        points_from_pool(clipped, m, u, w, n, dot(amax, n), mp.pen, o);
+        o->n = n;
+        o->pen = mp.pen;
+    }
+    return true;
+}
+
+__device__ __forceinline__ bool box_overlap(f3 alo, f3 ahi, f3 blo, f3 bhi) {
+    return !(ahi.x < blo.x || alo.x > bhi.x || ahi.y < blo.y || alo.y > bhi.y || ahi.z < blo.z || alo.z > bhi.z);
+}
+
+__device__ __forceinline__ float longest(f3 lo, f3 hi) {
+    return fmaxf(hi.x - lo.x, fmaxf(hi.y - lo.y, hi.z - lo.z));
+}
+
+// The manifolds of one (convex, mesh) pair after the per-triangle tests:
+// PhysicsEngine.cpp:257-295 merges, in manifold order, every later manifold
+// whose normal is within 1 degree of the current one (normal = normalised
+// sum, points appended), culls each merged manifold to 4 points
+// (cull_manifold) and adds its points with its normal.  Lane 0; returns the
+// kept point count (their raw indices in S.out, normals in S.out_n).
+__device__ int mesh_merge(MeshScratch& S, int nman, float* maxpen, int* status) {
+    const float cs[4] = {1.0f, 6.123233995736766e-17f, -1.0f, -1.8369701987210297e-16f};
+    const float sn[4] = {0.0f, 1.0f, 1.2246467991473532e-16f, -1.0f};
+    unsigned long long merged = 0ull;
+    int nout = 0;
+    *maxpen = -1.f;
+    for (int i = 0; i < nman; i++) {
+        if ((merged >> i) & 1ull) continue;
+        float4 mi = S.man_n[i];
+        f3 gn = mk(mi);
+        float gpen = mi.w;
+        unsigned long long mem = 1ull << i;
+        for (int j = i + 1; j < nman; j++) {
+            if ((merged >> j) & 1ull) continue;
+            float4 mj = S.man_n[j];
+            if (1.f - dot(gn, mk(mj)) < kCosTol) {
+                gn = normalize(gn + mk(mj));
+                gpen = fmaxf(gpen, mj.w);
+                merged |= 1ull << j;
+                mem |= 1ull << j;
+            }
+        }
+        *maxpen = fmaxf(*maxpen, gpen);
+        int total = 0;
+        for (unsigned long long b = mem; b; b &= b - 1) total += S.man_cnt[__ffsll((long long)b) - 1];
+        int pick[4], np = 0;
+        if (total <= 4) {
+            for (unsigned long long b = mem; b; b &= b - 1) {
+                const int m = __ffsll((long long)b) - 1;
+                for (int k = 0; k < S.man_cnt[m]; k++) pick[np++] = S.man_first[m] + k;
+            }
+        } else {
+            f3 cu, cw;
+            basis(gn, &cu, &cw);
+            for (int q = 0; q < 4; q++) {
+                f3 dir = cu * cs[q] + cw * sn[q];
+                int bi = -1;
+                float bv = -INFINITY;
+                for (unsigned long long b = mem; b; b &= b - 1) {
+                    const int m = __ffsll((long long)b) - 1;
+                    for (int k = 0; k < S.man_cnt[m]; k++) {
+                        const int idx = S.man_first[m] + k;
+                        bool used = false;
+                        for (int r = 0; r < np; r++) used |= pick[r] == idx;
+                        if (used) continue;
+                        float v = dot(mk(S.pt[idx]), dir);
+                        if (v > bv) { bv = v; bi = idx; }
+                    }
+                }
+                if (bi < 0) break;
+                pick[np++] = bi;
+            }
+        }
+        for (int r = 0; r < np; r++) {
+            if (nout >= kMeshOut) { atomicOr(status, ST_MESH_OVERFLOW); return nout; }
+            S.out[nout] = pick[r];
+            S.out_n[nout] = make_float4(gn.x, gn.y, gn.z, 0.f);
+            nout++;
+        }
+    }
+    return nout;
+}
+
 }  // namespace
 
 // One warp per candidate pair; `slot_bytes` of shared memory per warp.
@@ -1071,7 +1395,7 @@ __global__ void __launch_bounds__(256) k_narrow_prim(Dev d, int slot_bytes) {
         const HullHeader* Ha = reinterpret_cast<const HullHeader*>(ga);
         const HullHeader* Hb = reinterpret_cast<const HullHeader*>(gb);
         const uint32_t ka = Ha->kind, kb = Hb->kind;
-        if ((ka | kb) == SHAPE_HULL) continue;
+        if ((ka | kb) == SHAPE_HULL || ka == SHAPE_MESH || kb == SHAPE_MESH) continue;
         if (!(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
             if (lane == 0) no_manifold(d, p);
             continue;
@@ -1097,16 +1421,164 @@ __global__ void __launch_bounds__(256) k_narrow_prim(Dev d, int slot_bytes) {
     }
 }
 
+// One warp per candidate pair with a static mesh (the other pairs are
+// k_narrowphase's and k_narrow_prim's): SAT_PolyMesh / SAT_SphereMesh /
+// SAT_CylinderMesh (CollisionDetect.cpp:2648-2778) for a fixed mesh in world
+// coordinates.  The convex body is staged as in k_narrow_prim; lane 0 walks
+// the mesh's AABB tree (LIFO, right child first, as AABBTree::getAllOverlapping
+// does) into the candidate list; each candidate triangle is tested by the
+// whole warp, its manifold (flipped when the mesh is the pair's first body)
+// appended to the warp's scratch; lane 0 then merges, culls and writes the
+// pair's points to the mesh store.
+__global__ void __launch_bounds__(256) k_narrow_mesh(Dev d, int slot_bytes) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int warps_per_block = blockDim.x >> 5;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+    uint8_t* slot = smem + 16 * warps_per_block + (size_t)wib * slot_bytes;
+    if (lane == 0) mbar_init(&bars[wib]);
+    __syncthreads();
+    const int gw = blockIdx.x * warps_per_block + wib;
+    if (gw >= d.mesh_warps) return;
+    MeshScratch& S = d.msc[gw];
+    uint32_t parity = 0;
+    Scratch scratch;
+    CP clipped[kMaxClip];
+    const int n_pairs = *d.n_pairs;
+    for (int p = gw; p < n_pairs; p += d.mesh_warps) {
+        const int a = d.pair_a[p], b = d.pair_b[p];
+        const uint8_t* ga = d.shapes + d.shape[a];
+        const uint8_t* gb = d.shapes + d.shape[b];
+        const uint32_t ka = reinterpret_cast<const HullHeader*>(ga)->kind, kb = reinterpret_cast<const HullHeader*>(gb)->kind;
+        if (lane == 0) d.mf_ofs[p] = -1;
+        if (ka != SHAPE_MESH && kb != SHAPE_MESH) continue;
+        if ((ka == SHAPE_MESH && kb == SHAPE_MESH) || !(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
+            if (lane == 0) no_manifold(d, p);
+            continue;
+        }
+        const bool flip = ka == SHAPE_MESH;
+        const int c = flip ? b : a;
+        const uint8_t* gc = flip ? gb : ga;
+        const uint8_t* gm = flip ? ga : gb;
+        const uint32_t kc = flip ? kb : ka;
+        const uint32_t hot = reinterpret_cast<const HullHeader*>(gc)->off_fofs;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) {
+            mbar_expect(&bars[wib], hot);
+            bulk_load(slot, gc, hot, &bars[wib]);
+        }
+        bool ok = mbar_wait(&bars[wib], parity);
+        parity ^= 1u;
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) { atomicOr(d.status, ST_TIMEOUT); no_manifold(d, p); }
+            mbar_wait(&bars[wib], parity ^ 1u);
+            return;
+        }
+        HullView hv;
+        PrimView pv;
+        if (kc == SHAPE_HULL) stage_hull(gc, slot, d.pos[c], d.rot[c], &hv, lane);
+        else stage_prim(slot, d.pos[c], d.rot[c], &pv, lane);
+        const f3 blo = mk(d.aabb_lo[c]), bhi = mk(d.aabb_hi[c]);
+        const HullHeader* Hm = reinterpret_cast<const HullHeader*>(gm);
+        const float4* nodes = reinterpret_cast<const float4*>(gm + kMeshOffNodes);
+        const float4* tris = nodes + 2 * (size_t)Hm->pad[1];
+        int ncand = 0;
+        if (lane == 0) {
+            int stack[kMeshStack];
+            int sp = 0;
+            stack[sp++] = 0;
+            while (sp > 0) {
+                const int x = stack[--sp];
+                const float4 lo = __ldg(nodes + 2 * x), hi = __ldg(nodes + 2 * x + 1);
+                const int l = __float_as_int(lo.w), r = __float_as_int(hi.w);
+                if (l < 0) {
+                    const float4* t = tris + (size_t)kMeshTriF4 * r;
+                    if (box_overlap(mk(__ldg(t + 11)), mk(__ldg(t + 12)), blo, bhi)) {
+                        if (ncand < kMeshCand) S.cand[ncand++] = r;
+                        else { atomicOr(d.status, ST_MESH_OVERFLOW); break; }
+                    }
+                } else if (box_overlap(mk(lo), mk(hi), blo, bhi)) {
+                    if (sp + 2 > kMeshStack) { atomicOr(d.status, ST_MESH_OVERFLOW); break; }
+                    stack[sp++] = l;
+                    stack[sp++] = r;
+                }
+            }
+        }
+        ncand = __shfl_sync(0xffffffffu, ncand, 0);
+        __syncwarp();
+        const float pen_scale = kc == SHAPE_HULL ? 0.f : 0.15f;
+        const float body_long = longest(blo, bhi);
+        int nman = 0, npts = 0;   // lane 0's counts
+        for (int ci = 0; ci < ncand; ci++) {
+            TriView T;
+            load_tri(tris + (size_t)kMeshTriF4 * S.cand[ci], &T);
+            const float penalty = pen_scale * fminf(body_long, longest(T.lo, T.hi));
+            PrimOut o;
+            o.m = 0;
+            bool hit;
+            if (kc == SHAPE_HULL) hit = polyTri(hv, T, penalty, lane, scratch, clipped, d.status, &o);
+            else if (kc == SHAPE_SPHERE) hit = sphereTri(pv, T, penalty, lane, &o);
+            else hit = cylTri(pv, T, penalty, lane, scratch, clipped, d.status, &o);
+            if (lane == 0 && hit && o.pen > 0.f && o.m > 0) {
+                if (nman >= kMeshMans || npts + o.m > kMeshRaw) {
+                    atomicOr(d.status, ST_MESH_OVERFLOW);
+                    continue;
+                }
+                f3 n = flip ? -1.f * o.n : o.n;
+                S.man_n[nman] = make_float4(n.x, n.y, n.z, o.pen);
+                S.man_first[nman] = npts;
+                S.man_cnt[nman] = o.m;
+                for (int i = 0; i < o.m; i++) {
+                    unsigned long long x = o.magic[i];
+                    S.pt[npts + i] = o.pts[i];
+                    S.magic[npts + i] = flip ? ((x >> 32) | (x << 32)) : x;
+                    S.tri[npts + i] = T.id;
+                }
+                npts += o.m;
+                nman++;
+            }
+        }
+        if (lane == 0) {
+            float maxpen;
+            const int nout = mesh_merge(S, nman, &maxpen, d.status);
+            int ofs = nout > 0 ? atomicAdd(d.mm_count, nout) : 0;
+            if (nout > 0 && ofs + nout > d.cap_mesh_pts) { atomicOr(d.status, ST_MESH_OVERFLOW); ofs = -1; }
+            if (nout == 0 || ofs < 0) {
+                no_manifold(d, p);
+            } else {
+                for (int i = 0; i < nout; i++) {
+                    const int r = S.out[i];
+                    d.mm_pt[ofs + i] = S.pt[r];
+                    d.mm_n[ofs + i] = S.out_n[i];
+                    d.mm_magic[ofs + i] = S.magic[r];
+                    d.mm_tri[ofs + i] = S.tri[r];
+                }
+                d.mf_ofs[p] = ofs;
+                d.mf_cnt[p] = nout;
+                d.mf_n[p] = make_float4(0.f, 0.f, 0.f, maxpen);
+            }
+        }
+        __syncwarp();
+    }
+}
+
 void prepare_kernels() {
     cudaFuncSetAttribute(k_narrowphase, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_narrow_prim, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_narrow_mesh, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
+
+int mesh_scratch_warps(int n_sms) { return n_sms * kMeshBlocksPerSm * 8; }
 
 void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st) {
     const int warps = 8;
     size_t smem = 16 * warps + (size_t)warps * (slot_bytes + kQueueBytes);
     k_narrowphase<<<n_sms * 4, warps * 32, smem, st>>>(d, slot_bytes);
     if (prims) k_narrow_prim<<<n_sms * 4, warps * 32, 16 * warps + (size_t)warps * slot_bytes, st>>>(d, slot_bytes);
+    if (d.has_mesh)
+        k_narrow_mesh<<<n_sms * kMeshBlocksPerSm, warps * 32, 16 * warps + (size_t)warps * slot_bytes, st>>>(d, slot_bytes);
 }
 
 }  // namespace cpgpu

@@ -1,5 +1,5 @@
-// shapes.cuh — device-side world-frame geometry of the three primitive kinds
-// (convex hull, sphere, cylinder) shared by the pose/AABB kernels.
+// shapes.cuh — device-side world-frame geometry of the body kinds (convex
+// hull, sphere, cylinder, static triangle mesh) shared by the pose/AABB kernels.
 #pragma once
 #include "devmath.cuh"
 #include "layout.h"
@@ -18,6 +18,11 @@ __device__ __forceinline__ void aabb_add(f3 p, f3* mn, f3* mx) {
 // (Cylinder::recomputeFromReference, :272-287).
 __device__ __forceinline__ void shape_aabb(const uint8_t* blob, f3 c, const M33& R, f3* mn, f3* mx) {
     const HullHeader* H = reinterpret_cast<const HullHeader*>(blob);
+    if (H->kind == SHAPE_MESH) {   // StaticMeshGeometry: world-space triangles
+        *mn = mk(*reinterpret_cast<const float4*>(blob + sizeof(HullHeader)));
+        *mx = mk(*reinterpret_cast<const float4*>(blob + sizeof(HullHeader) + 16));
+        return;
+    }
     *mn = mk(INFINITY, INFINITY, INFINITY);
     *mx = mk(-INFINITY, -INFINITY, -INFINITY);
     if (H->kind == SHAPE_SPHERE) {
