@@ -500,6 +500,7 @@ struct Batch {
     cudaStream_t side = nullptr;       // concurrent branch (small-island PGS)
     cudaEvent_t fork = nullptr, join = nullptr;
     int dv_cap = 64;                   // island bodies whose Δv fits in shared memory
+    int pgs_blocks = 0;                // k_pgs_big grid: one resident chain per block
     uint8_t* mem = nullptr;
     size_t bytes = 0;                  // device arena size
     Dev d[2];                  // d[p]: old = buffer p, new = buffer 1-p
@@ -540,7 +541,7 @@ struct Batch {
         for (int s = 0; s < substeps; s++) {
             launch_rows(x, s == 0, s == substeps - 1, L);
             launch_joint_rows(x, s == 0, L);               mark(6 + 3 * s);
-            launch_pgs(x, dv_cap, side, fork, join, L);
+            launch_pgs(x, dv_cap, pgs_blocks, side, fork, join, L);
             launch_pgs_joint(x, s == 0, L);                mark(7 + 3 * s);
             launch_integrate(x, s == substeps - 1, L);     mark(8 + 3 * s);
         }
@@ -548,10 +549,10 @@ struct Batch {
     }
     // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 1
     // (+1 with spheres / cylinders, +1 with meshes), merge 6 + 3 scans, islands 2 + scan 3,
-    // schedule 3, 4 per substep (rows, small + large PGS, integrate), geometry 1
+    // schedule 3, 5 per substep (rows, small + grouped + large PGS, integrate), geometry 1
     // (+2 per substep and 1 factorisation with joints)
     int launches_per_step() const {
-        return 1 + 6 + 1 + (prims ? 1 : 0) + (meshes ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 4 * substeps + 1 + (joints ? 2 * substeps : 0) +
+        return 1 + 6 + 1 + (prims ? 1 : 0) + (meshes ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 5 * substeps + 1 + (joints ? 2 * substeps : 0) +
                (systems ? 1 : 0);
     }
 
@@ -1033,7 +1034,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         x.stage = A.take<float4>(4 * (size_t)N);
         x.big_list = A.take<int>(N);
         x.small_list = A.take<int>(N);
-        x.sched = A.take<int>(96);
+        x.sched = A.take<int>(kSchedInts);
         x.status = counts + 6;
         x.cnt = counts + 16;
         if (B->meshes) {
@@ -1147,6 +1148,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     launch_geometry(B->d[0], 1, L);
     prepare_kernels();
     prepare_pgs(B->dv_cap);
+    B->pgs_blocks = B->n_sms * pgs_big_blocks_per_sm(B->dv_cap);
     CK(cudaStreamSynchronize(B->st));
     CK(cudaGetLastError());
     B->build_graphs();
@@ -1483,9 +1485,43 @@ static void ensure_device(World& w) {
 using namespace cpgpu;
 
 struct cpgpu_world { World w; };
+// A batch of worlds, split by world size into parts that step concurrently,
+// each on its own streams with its own graphs.  A step is bounded by the
+// longest serial Gauss-Seidel chain of its largest island; with the largest
+// worlds in a part of their own, the other parts' narrowphase and solves run
+// beside that chain instead of after it.  Worlds never interact, so every
+// world steps exactly as it does alone, whatever its part.
 struct cpgpu_batch {
-    std::unique_ptr<Batch> b;
-    std::vector<int> sizes;
+    std::vector<std::unique_ptr<Batch>> parts;
+    std::vector<int> part_of, local_of;   // per world: its part and index within it
+    std::vector<int> row0;                // per world: first row in the batch's body order
+    int64_t n_bodies = 0;
+    float4* stage = nullptr;              // host-layout rows of all bodies (4 float4 each)
+    std::vector<int*> rows;               // per part: batch row of each of its bodies
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr;
+    std::vector<cudaEvent_t> done;        // per part
+    ~cpgpu_batch() {
+        for (int* r : rows) if (r) cudaFree(r);
+        if (stage) cudaFree(stage);
+        for (cudaEvent_t e : done) cudaEventDestroy(e);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (fork) cudaEventDestroy(fork);
+    }
+    Batch& part(int p) { return *parts[p]; }
+    cudaStream_t st0() { return parts[0]->st; }
+    // every part's stream waits for what part 0's stream has issued so far
+    void fan_out() {
+        CK(cudaEventRecord(fork, st0()));
+        for (size_t p = 1; p < parts.size(); p++) CK(cudaStreamWaitEvent(parts[p]->st, fork, 0));
+    }
+    // part 0's stream waits for what every part has issued so far
+    void fan_in() {
+        for (size_t p = 1; p < parts.size(); p++) {
+            CK(cudaEventRecord(done[p], parts[p]->st));
+            CK(cudaStreamWaitEvent(st0(), done[p], 0));
+        }
+    }
 };
 
 template <class F>
@@ -1871,6 +1907,41 @@ int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
     });
 }
 
+// Parts of a batch: worlds sorted by body count (largest first) and cut into
+// runs of about equal total bodies.  CPGPU_BATCH_PARTS sets the count (default
+// 1): parts pay off when one world's serial solve chain is longer than the rest
+// of the step (a few very large worlds among many small ones); when the step is
+// throughput-bound, concurrent parts only contend for the same SMs.
+static std::vector<std::vector<int>> batch_partition(const std::vector<World*>& ws) {
+    const int n = (int)ws.size();
+    int P = env_int("CPGPU_BATCH_PARTS", 1);
+    P = std::max(1, std::min(P, n));
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ws[a]->bodies.size() > ws[b]->bodies.size(); });
+    int64_t total = 0;
+    for (World* w : ws) total += (int64_t)w->bodies.size();
+    std::vector<std::vector<int>> parts(P);
+    if (env_int("CPGPU_BATCH_MIX", 0)) {
+        // every part the same mix of sizes: worlds dealt round-robin by size
+        for (int k = 0; k < n; k++) parts[k % P].push_back(order[k]);
+        for (auto& q : parts) std::sort(q.begin(), q.end());
+        return parts;
+    }
+    int64_t acc = 0;
+    int p = 0;
+    for (int k = 0; k < n; k++) {
+        const int left = n - k;
+        // move on once this part holds its share, keeping one world for each later part
+        if (p + 1 < P && !parts[p].empty() && (acc >= (total * (p + 1)) / P || left <= P - 1 - p)) p++;
+        parts[p].push_back(order[k]);
+        acc += (int64_t)ws[order[k]]->bodies.size();
+    }
+    for (auto& q : parts) std::sort(q.begin(), q.end());   // batch order within a part
+    parts.erase(std::remove_if(parts.begin(), parts.end(), [](const std::vector<int>& q) { return q.empty(); }), parts.end());
+    return parts;
+}
+
 int cpgpu_batch_create(cpgpu_world* const* worlds, int n, cpgpu_batch** out) {
     return guarded([&] {
         if (!worlds || n <= 0 || !out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "empty batch"};
@@ -1881,23 +1952,61 @@ int cpgpu_batch_create(cpgpu_world* const* worlds, int n, cpgpu_batch** out) {
             ws.push_back(&worlds[i]->w);
         }
         auto b = std::make_unique<cpgpu_batch>();
-        b->b = build_batch(ws);
-        for (World* x : ws) b->sizes.push_back((int)x->bodies.size());
+        b->part_of.resize(n);
+        b->local_of.resize(n);
+        b->row0.resize(n);
+        for (int i = 0; i < n; i++) {
+            b->row0[i] = (int)b->n_bodies;
+            b->n_bodies += (int64_t)ws[i]->bodies.size();
+        }
+        const auto parts = batch_partition(ws);
+        for (size_t p = 0; p < parts.size(); p++) {
+            std::vector<World*> sub;
+            std::vector<int> rows;
+            for (size_t k = 0; k < parts[p].size(); k++) {
+                const int wi = parts[p][k];
+                b->part_of[wi] = (int)p;
+                b->local_of[wi] = (int)k;
+                sub.push_back(ws[wi]);
+                for (size_t j = 0; j < ws[wi]->bodies.size(); j++) rows.push_back(b->row0[wi] + (int)j);
+            }
+            b->parts.push_back(build_batch(sub));
+            int* d_rows = nullptr;
+            CK(cudaMalloc(&d_rows, sizeof(int) * std::max<size_t>(rows.size(), 1)));
+            CK(cudaMemcpy(d_rows, rows.data(), sizeof(int) * rows.size(), cudaMemcpyHostToDevice));
+            b->rows.push_back(d_rows);
+        }
+        CK(cudaMalloc(&b->stage, sizeof(float4) * 4 * std::max<int64_t>(b->n_bodies, 1)));
+        CK(cudaEventCreate(&b->ev0));
+        CK(cudaEventCreate(&b->ev1));
+        CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        b->done.resize(b->parts.size());
+        for (auto& e : b->done) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         *out = b.release();
         return CPGPU_OK;
     });
 }
 int cpgpu_batch_destroy(cpgpu_batch* b) { delete b; return CPGPU_OK; }
+
+static int batch_check(cpgpu_batch* b) {
+    for (auto& p : b->parts) p->check_status();
+    return CPGPU_OK;
+}
+
 int cpgpu_batch_step(cpgpu_batch* b, int n) {
     if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
-    return guarded([&] { b->b->step(n); return b->b->check_status(); });
+    return guarded([&] {
+        for (auto& p : b->parts) p->step(n);   // graph launches only: the parts run concurrently
+        return batch_check(b);
+    });
 }
 int cpgpu_batch_get_body_state(cpgpu_batch* b, int wi, double* com, double* quat, double* vel, double* ang) {
     if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
     return guarded([&] {
-        Batch& B = *b->b;
-        if (wi < 0 || wi >= B.n_worlds) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad world index"};
-        int s = B.world_start[wi], n = B.world_start[wi + 1] - s;
+        if (wi < 0 || wi >= (int)b->part_of.size()) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad world index"};
+        Batch& B = b->part(b->part_of[wi]);
+        const int lw = b->local_of[wi];
+        int s = B.world_start[lw], n = B.world_start[lw + 1] - s;
         std::vector<float4> pos(n), rot(n), vel4(n), ang4(n);
         const Dev& x = B.cur();
         CK(cudaMemcpyAsync(pos.data(), x.pos + s, n * 16, cudaMemcpyDeviceToHost, B.st));
@@ -1918,34 +2027,41 @@ int cpgpu_batch_get_body_state(cpgpu_batch* b, int wi, double* com, double* quat
 int cpgpu_batch_info(cpgpu_batch* b, int64_t* n_bodies, int64_t* n_worlds, int64_t* n_contacts) {
     if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
     return guarded([&] {
-        Batch& B = *b->b;
-        int counts[6];
-        CK(cudaMemcpyAsync(counts, B.cur().n_pairs, sizeof(counts), cudaMemcpyDeviceToHost, B.st));
-        CK(cudaStreamSynchronize(B.st));
-        if (n_bodies) *n_bodies = B.n_bodies;
-        if (n_worlds) *n_worlds = B.n_worlds;
-        if (n_contacts) *n_contacts = counts[3 + B.parity];
+        int64_t contacts = 0;
+        for (auto& p : b->parts) {
+            Batch& B = *p;
+            int counts[6];
+            CK(cudaMemcpyAsync(counts, B.cur().n_pairs, sizeof(counts), cudaMemcpyDeviceToHost, B.st));
+            CK(cudaStreamSynchronize(B.st));
+            contacts += counts[3 + B.parity];
+        }
+        if (n_bodies) *n_bodies = b->n_bodies;
+        if (n_worlds) *n_worlds = (int64_t)b->part_of.size();
+        if (n_contacts) *n_contacts = contacts;
         return CPGPU_OK;
     });
 }
 
 int cpgpu_batch_launches_per_step(cpgpu_batch* b, int* n) {
     if (!b || !n) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
-    *n = b->b->launches_per_step();
+    int t = 0;
+    for (auto& p : b->parts) t += p->launches_per_step();
+    *n = t;
     return CPGPU_OK;
 }
 
+// host layout: 16 floats per body in batch order (pos with inverse mass, rot,
+// vel, ang vel); one copy each way, each part gathering / scattering its rows
 int cpgpu_batch_read_state(cpgpu_batch* b, float* out) {
     if (!b || !out) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
     return guarded([&] {
-        Batch& B = *b->b;
-        const Dev& x = B.cur();
-        const size_t N = B.n_bodies;
-        // four strided copies into the 16-float-per-body host layout
-        const float4* src[4] = {x.pos, x.rot, x.vel, x.angv};
-        for (int k = 0; k < 4; k++)
-            CK(cudaMemcpy2DAsync(out + 4 * k, 64, src[k], 16, 16, N, cudaMemcpyDeviceToHost, B.st));
-        CK(cudaStreamSynchronize(B.st));
+        for (size_t p = 0; p < b->parts.size(); p++) {
+            Batch& B = b->part((int)p);
+            launch_scatter_state(B.cur(), b->rows[p], b->stage, Launch{B.n_sms, B.st});
+        }
+        b->fan_in();
+        CK(cudaMemcpyAsync(out, b->stage, (size_t)b->n_bodies * 64, cudaMemcpyDeviceToHost, b->st0()));
+        CK(cudaStreamSynchronize(b->st0()));
         return CPGPU_OK;
     });
 }
@@ -1953,66 +2069,78 @@ int cpgpu_batch_read_state(cpgpu_batch* b, float* out) {
 int cpgpu_batch_write_state(cpgpu_batch* b, const float* in) {
     if (!b || !in) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
     return guarded([&] {
-        Batch& B = *b->b;
-        const Dev& x = B.cur();
-        const size_t N = B.n_bodies;
-        CK(cudaMemcpyAsync(x.stage, in, N * 64, cudaMemcpyHostToDevice, B.st));
-        launch_apply_state(x, Launch{B.n_sms, B.st});
-        CK(cudaStreamSynchronize(B.st));
+        CK(cudaMemcpyAsync(b->stage, in, (size_t)b->n_bodies * 64, cudaMemcpyHostToDevice, b->st0()));
+        b->fan_out();
+        for (size_t p = 0; p < b->parts.size(); p++) {
+            Batch& B = b->part((int)p);
+            const Launch L{B.n_sms, B.st};
+            launch_gather_state(B.cur(), b->stage, b->rows[p], L);
+            launch_apply_state(B.cur(), L);
+        }
+        // the staging buffer is reused by the next read: order it after these gathers
+        b->fan_in();
+        CK(cudaStreamSynchronize(b->st0()));
         return CPGPU_OK;
     });
 }
 
+// Stage times of n steps, part by part (each part's stages timed alone and
+// summed over the parts: the work of each stage, not the overlapped step)
 int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* counts) {
     if (!b || !stage_ms) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
     return guarded([&] {
-        Batch& B = *b->b;
-        const int n_marks = 7 + 3 * B.substeps;
-        std::vector<cudaEvent_t> ev(n_marks);
-        for (auto& e : ev) CK(cudaEventCreate(&e));
         for (int k = 0; k < CPGPU_N_STAGES; k++) stage_ms[k] = 0;
-        B.marks = &ev;
-        for (int i = 0; i < n_steps; i++) {
-            B.launch_step(B.d[B.parity]);
-            B.parity ^= 1;
-            CK(cudaEventSynchronize(ev[n_marks - 1]));
-            auto span = [&](int a, int c) { float ms = 0; CK(cudaEventElapsedTime(&ms, ev[a], ev[c])); return (double)ms; };
-            for (int k = 0; k < 5; k++) stage_ms[k] += span(k, k + 1);
-            for (int s = 0; s < B.substeps; s++) {
-                stage_ms[5] += span(5 + 3 * s, 6 + 3 * s);
-                stage_ms[6] += span(6 + 3 * s, 7 + 3 * s);
-                stage_ms[7] += span(7 + 3 * s, 8 + 3 * s);
+        if (counts) counts[0] = counts[1] = counts[2] = 0;
+        for (auto& part : b->parts) {
+            Batch& B = *part;
+            const int n_marks = 7 + 3 * B.substeps;
+            std::vector<cudaEvent_t> ev(n_marks);
+            for (auto& e : ev) CK(cudaEventCreate(&e));
+            B.marks = &ev;
+            for (int i = 0; i < n_steps; i++) {
+                B.launch_step(B.d[B.parity]);
+                B.parity ^= 1;
+                CK(cudaEventSynchronize(ev[n_marks - 1]));
+                auto span = [&](int a, int c) { float ms = 0; CK(cudaEventElapsedTime(&ms, ev[a], ev[c])); return (double)ms; };
+                for (int k = 0; k < 5; k++) stage_ms[k] += span(k, k + 1);
+                for (int s = 0; s < B.substeps; s++) {
+                    stage_ms[5] += span(5 + 3 * s, 6 + 3 * s);
+                    stage_ms[6] += span(6 + 3 * s, 7 + 3 * s);
+                    stage_ms[7] += span(7 + 3 * s, 8 + 3 * s);
+                }
+                stage_ms[8] += span(5 + 3 * B.substeps, 6 + 3 * B.substeps);
             }
-            stage_ms[8] += span(5 + 3 * B.substeps, 6 + 3 * B.substeps);
+            B.marks = nullptr;
+            for (auto& e : ev) cudaEventDestroy(e);
+            if (counts) {
+                int c[6];
+                CK(cudaMemcpyAsync(c, B.cur().n_pairs, sizeof(c), cudaMemcpyDeviceToHost, B.st));
+                CK(cudaStreamSynchronize(B.st));
+                counts[0] += c[0];
+                counts[1] += c[3 + B.parity];
+                counts[2] += c[5];
+            }
+            B.check_status();
         }
-        B.marks = nullptr;
-        for (auto& e : ev) cudaEventDestroy(e);
-        if (counts) {
-            int c[6];
-            CK(cudaMemcpyAsync(c, B.cur().n_pairs, sizeof(c), cudaMemcpyDeviceToHost, B.st));
-            CK(cudaStreamSynchronize(B.st));
-            counts[0] = c[0];
-            counts[1] = c[3 + B.parity];
-            counts[2] = c[5];
-        }
-        return B.check_status();
+        return CPGPU_OK;
     });
 }
 
-// Device time of n steps of the batch, measured with CUDA events recorded on
-// the batch's own stream around the graph launches.
+// Device time of n steps of the batch: CUDA events on part 0's stream, which
+// the other parts' streams join before the start and after the last step.
 int cpgpu_batch_step_timed(cpgpu_batch* b, int n, double* device_ms) {
     if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
     return guarded([&] {
-        Batch& B = *b->b;
-        CK(cudaEventRecord(B.ev0, B.st));
-        B.step(n);
-        CK(cudaEventRecord(B.ev1, B.st));
-        CK(cudaEventSynchronize(B.ev1));
+        CK(cudaEventRecord(b->ev0, b->st0()));
+        b->fan_out();
+        for (auto& p : b->parts) p->step(n);
+        b->fan_in();
+        CK(cudaEventRecord(b->ev1, b->st0()));
+        CK(cudaEventSynchronize(b->ev1));
         float ms = 0;
-        CK(cudaEventElapsedTime(&ms, B.ev0, B.ev1));
+        CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
         if (device_ms) *device_ms = ms;
-        return B.check_status();
+        return batch_check(b);
     });
 }
 

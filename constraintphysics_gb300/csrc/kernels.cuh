@@ -35,7 +35,8 @@ void launch_rows(const Dev& d, int first, int last, const Launch& L);
 void launch_pgs_schedule(const Dev& d, const Launch& L);
 void prepare_pgs(int dv_cap);
 int pgs_big_smem_bytes(int dv_cap);
-void launch_pgs(const Dev& d, int dv_cap, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, const Launch& L);
+int pgs_big_blocks_per_sm(int dv_cap);
+void launch_pgs(const Dev& d, int dv_cap, int big_blocks, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, const Launch& L);
 void launch_integrate(const Dev& d, int last, const Launch& L);
 // joints: rows every substep, the holonomic systems' factorisation on the
 // first; islands with joint rows solved by their own kernel
@@ -44,5 +45,8 @@ void launch_pgs_joint(const Dev& d, bool first, const Launch& L);
 // external state write: apply the staged state (d.stage); bodies whose pose
 // changed get their world inertia tensors and AABBs recomputed
 void launch_apply_state(const Dev& d, const Launch& L);
+// host-layout rows (pos, rot, vel, ang vel: 4 float4 per body) of a split batch
+void launch_gather_state(const Dev& d, const float4* all, const int* rows, const Launch& L);   // all -> d.stage
+void launch_scatter_state(const Dev& d, const int* rows, float4* all, const Launch& L);       // d -> all
 
 }  // namespace cpgpu

@@ -139,7 +139,14 @@ struct EdgeStore {
 
 // Solver row block of one contact (normal row + 2-dof friction row), built each
 // substep in island order (ConstraintSolver.cpp:240-343).  384 bytes, 16-byte
-// aligned, so contiguous runs of rows can be bulk-copied to shared memory.
+// aligned.  The Jacobian entries are split by component triple (h[0] linear,
+// h[1] angular, each for both bodies), so that a solver lane owning one triple
+// reads one contiguous half.
+struct RowHalf {
+    float nja[3], njb[3], nita[3], nitb[3];          // normal row J and M^-1 J^T
+    float fja0[3], fja1[3], fjb0[3], fjb1[3];        // friction rows (u, w)
+    float fita0[3], fita1[3], fitb0[3], fitb1[3];    // friction M^-1 J^T columns (u, w)
+};
 struct alignas(16) RowBlock {
     float4 imp;          // accumulated impulses: normal, pseudo normal, friction u, w
     int sa, sb;          // island body slots (-1 = body with infinite mass)
@@ -149,12 +156,13 @@ struct alignas(16) RowBlock {
     float bounce, cutoff;
     float tgt_n, tgt_f0, tgt_f1;   // velocity targets (findTargetConstraintValue)
     float fcoeff;
-    float nminv, nptarget, pad0, pad1;
-    float nja[6], njb[6], nita[6], nitb[6];
-    float fja[12], fjb[12], fita[12], fitb[12];   // row-major [2][6] / [6][2]
+    float nminv, nptarget;
+    float kf0, kf1;      // J_f M^-1 J_n^T of friction rows u, w: their velocity change per unit normal impulse
     float fminv[4];
+    RowHalf h[2];
 };
 static_assert(sizeof(RowBlock) == 384, "row block size");
+static_assert(sizeof(RowHalf) == 144, "row half size");
 
 // One joint row per substep: DegreedConstraint<n> of a BallSocketConstraint
 // (n = 3) or HingeConstraint (n = 5) (ConstraintSolver.h:60-144), row-major,
@@ -220,6 +228,8 @@ struct HoloStore {
     int* isl;               // island of the system in this step (-1 none)
 };
 
+constexpr int kSchedInts = 1024;
+
 struct Batch;  // host object, engine.cu
 
 // All device pointers of a batch, passed by value to kernels.
@@ -284,7 +294,7 @@ struct Dev {
     float4* dv;                    // 4 float4 per island body slot: dv lin, dv ang, dpv lin, dpv ang
     float4* stage;                 // 4 float4 per body: staging of external state writes
     int* big_list; int* small_list;  // island indices split by row count (PGS scheduling)
-    int* sched;                    // [0] n_big, [1] n_small, [2] big queue head, [32..63] bucket counts, [64..95] cursors
+    int* sched;                    // schedule counters and tables (kSchedInts ints, layout in solver.cu)
     int* cnt;                      // small device counters (merge totals)
     int* status;
     // joints and holonomic systems (n_joints == 0: none in the batch)

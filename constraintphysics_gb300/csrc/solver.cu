@@ -55,6 +55,40 @@ __device__ __forceinline__ float dot6(const float* a, const float* b) {
     return s;
 }
 
+// row entries by component k (0..5: linear xyz, angular xyz) and friction
+// direction i (0: u, 1: w), over the split RowBlock layout
+__device__ __forceinline__ float& r_nja(RowBlock& R, int k) { return R.h[k / 3].nja[k % 3]; }
+__device__ __forceinline__ float& r_njb(RowBlock& R, int k) { return R.h[k / 3].njb[k % 3]; }
+__device__ __forceinline__ float& r_nita(RowBlock& R, int k) { return R.h[k / 3].nita[k % 3]; }
+__device__ __forceinline__ float& r_nitb(RowBlock& R, int k) { return R.h[k / 3].nitb[k % 3]; }
+__device__ __forceinline__ float& r_fja(RowBlock& R, int i, int k) { return i ? R.h[k / 3].fja1[k % 3] : R.h[k / 3].fja0[k % 3]; }
+__device__ __forceinline__ float& r_fjb(RowBlock& R, int i, int k) { return i ? R.h[k / 3].fjb1[k % 3] : R.h[k / 3].fjb0[k % 3]; }
+__device__ __forceinline__ float& r_fita(RowBlock& R, int i, int k) { return i ? R.h[k / 3].fita1[k % 3] : R.h[k / 3].fita0[k % 3]; }
+__device__ __forceinline__ float& r_fitb(RowBlock& R, int i, int k) { return i ? R.h[k / 3].fitb1[k % 3] : R.h[k / 3].fitb0[k % 3]; }
+__device__ __forceinline__ float c_nita(const RowBlock& R, int k) { return R.h[k / 3].nita[k % 3]; }
+__device__ __forceinline__ float c_nitb(const RowBlock& R, int k) { return R.h[k / 3].nitb[k % 3]; }
+__device__ __forceinline__ float c_fita(const RowBlock& R, int i, int k) { return i ? R.h[k / 3].fita1[k % 3] : R.h[k / 3].fita0[k % 3]; }
+__device__ __forceinline__ float c_fitb(const RowBlock& R, int i, int k) { return i ? R.h[k / 3].fitb1[k % 3] : R.h[k / 3].fitb0[k % 3]; }
+// six-term dot product as a tree of pairs (three levels of dependent
+// operations instead of six: the solver's serial chain runs through these)
+__device__ __forceinline__ float tdot6(float a0, float a1, float a2, float a3, float a4, float a5, const float* v) {
+    return (a0 * v[0] + a1 * v[1]) + (a2 * v[2] + a3 * v[3]) + (a4 * v[4] + a5 * v[5]);
+}
+// J_a v_a + J_b v_b of the normal row / friction row i
+__device__ __forceinline__ float jn_dot(const RowBlock& R, const float* va, const float* vb) {
+    const RowHalf &l = R.h[0], &w = R.h[1];
+    return tdot6(l.nja[0], l.nja[1], l.nja[2], w.nja[0], w.nja[1], w.nja[2], va) +
+           tdot6(l.njb[0], l.njb[1], l.njb[2], w.njb[0], w.njb[1], w.njb[2], vb);
+}
+__device__ __forceinline__ float jf_dot(const RowBlock& R, int i, const float* va, const float* vb) {
+    const RowHalf &l = R.h[0], &w = R.h[1];
+    if (i == 0)
+        return tdot6(l.fja0[0], l.fja0[1], l.fja0[2], w.fja0[0], w.fja0[1], w.fja0[2], va) +
+               tdot6(l.fjb0[0], l.fjb0[1], l.fjb0[2], w.fjb0[0], w.fjb0[1], w.fjb0[2], vb);
+    return tdot6(l.fja1[0], l.fja1[1], l.fja1[2], w.fja1[0], w.fja1[1], w.fja1[2], va) +
+           tdot6(l.fjb1[0], l.fjb1[1], l.fjb1[2], w.fjb1[0], w.fjb1[1], w.fjb1[2], vb);
+}
+
 __device__ __forceinline__ void body_vel(const Dev& d, int g, float* out) {
     if (d.movement[g] == 1) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
     float4 v = d.vel[g], w = d.angv[g];
@@ -99,7 +133,7 @@ __global__ void k_rows(Dev d, int first, int last) {
             it_of(ima, Ia, ja, ia);
             it_of(imb, Ib, jb, ib);
             float itv = dot6(ja, ia) + dot6(jb, ib);
-            for (int k = 0; k < 6; k++) { R.nja[k] = ja[k]; R.njb[k] = jb[k]; R.nita[k] = ia[k]; R.nitb[k] = ib[k]; }
+            for (int k = 0; k < 6; k++) { r_nja(R, k) = ja[k]; r_njb(R, k) = jb[k]; r_nita(R, k) = ia[k]; r_nitb(R, k) = ib[k]; }
             R.nminv = 1.0f / (itv * (1.0f + P.cfm));
             R.nptarget = fmaxf(0.0f, depth - 0.05f) * pcc;
             // friction rows in the tangent basis of n, warm impulse re-projected
@@ -131,7 +165,14 @@ __global__ void k_rows(Dev d, int first, int last) {
             fv[3] *= (1.0f + P.cfm);
             float di = 1.0f / (fv[0] * fv[3] - fv[1] * fv[2]);
             R.fminv[0] = fv[3] * di; R.fminv[1] = -fv[1] * di; R.fminv[2] = -fv[2] * di; R.fminv[3] = fv[0] * di;
-            for (int k = 0; k < 12; k++) { R.fja[k] = fja[k]; R.fjb[k] = fjb[k]; R.fita[k] = fia[k]; R.fitb[k] = fib[k]; }
+            R.kf0 = tdot6(fja[0], fja[1], fja[2], fja[3], fja[4], fja[5], ia) + tdot6(fjb[0], fjb[1], fjb[2], fjb[3], fjb[4], fjb[5], ib);
+            R.kf1 = tdot6(fja[6], fja[7], fja[8], fja[9], fja[10], fja[11], ia) +
+                    tdot6(fjb[6], fjb[7], fjb[8], fjb[9], fjb[10], fjb[11], ib);
+            for (int i = 0; i < 2; i++)
+                for (int k = 0; k < 6; k++) {
+                    r_fja(R, i, k) = fja[6 * i + k]; r_fjb(R, i, k) = fjb[6 * i + k];
+                    r_fita(R, i, k) = fia[2 * k + i]; r_fitb(R, i, k) = fib[2 * k + i];
+                }
             // velocity targets from the bodies' velocities at the start of the
             // solve (ContactConstraint::findTargetConstraintValue,
             // ConstraintSolver.cpp:264-268; DegreedConstraint default, ConstraintSolver.h:78)
@@ -178,11 +219,11 @@ __device__ __forceinline__ void row_warm(const RowBlock& R, const float4 imp, fl
     load_dv(dv, R.sa, 0, va);
     load_dv(dv, R.sb, 0, vb);
     if (wn)
-        for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * imp.x; vb[k] += R.nitb[k] * imp.x; }
+        for (int k = 0; k < 6; k++) { va[k] += c_nita(R, k) * imp.x; vb[k] += c_nitb(R, k) * imp.x; }
     if (wf)
         for (int k = 0; k < 6; k++) {
-            va[k] += imp.z * R.fita[2 * k] + imp.w * R.fita[2 * k + 1];
-            vb[k] += imp.z * R.fitb[2 * k] + imp.w * R.fitb[2 * k + 1];
+            va[k] += imp.z * c_fita(R, 0, k) + imp.w * c_fita(R, 1, k);
+            vb[k] += imp.z * c_fitb(R, 0, k) + imp.w * c_fitb(R, 1, k);
         }
     store_dv(dv, R.sa, 0, va);
     store_dv(dv, R.sb, 0, vb);
@@ -190,42 +231,44 @@ __device__ __forceinline__ void row_warm(const RowBlock& R, const float4 imp, fl
 
 // velocity pass: normal row clamped at zero, then the friction rows projected on
 // the friction disc of the current normal impulse (PGSConstraintStep,
-// ConstraintSolver.cpp:12-40; projections :270-272, :331-343)
+// ConstraintSolver.cpp:12-40; projections :270-272, :331-343).  The friction
+// rows see the velocities after the normal change; that is evaluated as the
+// friction values of the incoming velocities plus the normal change times the
+// row's coupling constants kf0/kf1 (the same quantity, associated
+// differently), so that both dot products run alongside the normal one instead
+// of after it.  The disc projection compares squared magnitudes and scales by
+// rsqrt.
 __device__ __forceinline__ void row_vel(const RowBlock& R, float4& imp, int& stat, float4* dv) {
     float va[6], vb[6];
     load_dv(dv, R.sa, 0, va);
     load_dv(dv, R.sb, 0, vb);
-    {
-        float cur = dot6(R.nja, va) + dot6(R.njb, vb);
-        float nw = imp.x + R.nminv * (R.tgt_n - cur);
-        float diff = fmaxf(nw, 0.0f) - imp.x;
-        if (fabsf(diff) > kZero) {
-            for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * diff; vb[k] += R.nitb[k] * diff; }
-            imp.x += diff;
+    const float cur = jn_dot(R, va, vb);
+    const float b0 = jf_dot(R, 0, va, vb), b1 = jf_dot(R, 1, va, vb);
+    const float nw = imp.x + R.nminv * (R.tgt_n - cur);
+    float diff = fmaxf(nw, 0.0f) - imp.x;
+    if (!(fabsf(diff) > kZero)) diff = 0.f;
+    const float ix = imp.x + diff;
+    const float c0 = fmaf(diff, R.kf0, b0), c1 = fmaf(diff, R.kf1, b1);
+    const float d0 = R.tgt_f0 - c0, d1 = R.tgt_f1 - c1;
+    float n0 = imp.z + (d0 * R.fminv[0] + d1 * R.fminv[1]);
+    float n1 = imp.w + (d0 * R.fminv[2] + d1 * R.fminv[3]);
+    const float mx = R.fcoeff * ix;
+    const float s2 = n0 * n0 + n1 * n1;
+    if (s2 > mx * mx) { const float sc = mx * rsqrtf(s2); n0 *= sc; n1 *= sc; stat = 0; }
+    else stat = 1;
+    float e0 = n0 - imp.z, e1 = n1 - imp.w;
+    if (!(fabsf(e0) > kZero || fabsf(e1) > kZero)) { e0 = 0.f; e1 = 0.f; }
+    if (diff != 0.f || e0 != 0.f || e1 != 0.f) {
+        for (int k = 0; k < 6; k++) {
+            va[k] += c_nita(R, k) * diff + (c_fita(R, 0, k) * e0 + c_fita(R, 1, k) * e1);
+            vb[k] += c_nitb(R, k) * diff + (c_fitb(R, 0, k) * e0 + c_fitb(R, 1, k) * e1);
         }
+        store_dv(dv, R.sa, 0, va);
+        store_dv(dv, R.sb, 0, vb);
     }
-    {
-        float c0 = dot6(R.fja, va) + dot6(R.fjb, vb);
-        float c1 = dot6(R.fja + 6, va) + dot6(R.fjb + 6, vb);
-        float d0 = R.tgt_f0 - c0, d1 = R.tgt_f1 - c1;
-        float n0 = imp.z + (d0 * R.fminv[0] + d1 * R.fminv[1]);
-        float n1 = imp.w + (d0 * R.fminv[2] + d1 * R.fminv[3]);
-        float mx = R.fcoeff * imp.x;
-        float mg = sqrtf(n0 * n0 + n1 * n1);
-        if (mg > mx) { float sc = mx / mg; n0 *= sc; n1 *= sc; stat = 0; }
-        else stat = 1;
-        float e0 = n0 - imp.z, e1 = n1 - imp.w;
-        if (fabsf(e0) > kZero || fabsf(e1) > kZero) {
-            for (int k = 0; k < 6; k++) {
-                va[k] += e0 * R.fita[2 * k] + e1 * R.fita[2 * k + 1];
-                vb[k] += e0 * R.fitb[2 * k] + e1 * R.fitb[2 * k + 1];
-            }
-            imp.z += e0;
-            imp.w += e1;
-        }
-    }
-    store_dv(dv, R.sa, 0, va);
-    store_dv(dv, R.sb, 0, vb);
+    imp.x = ix;
+    imp.z += e0;
+    imp.w += e1;
 }
 
 // pseudo-velocity (position correction) pass of the normal row
@@ -233,11 +276,11 @@ __device__ __forceinline__ void row_pos(const RowBlock& R, float4& imp, float4* 
     float va[6], vb[6];
     load_dv(dv, R.sa, 1, va);
     load_dv(dv, R.sb, 1, vb);
-    float cur = dot6(R.nja, va) + dot6(R.njb, vb);
+    float cur = jn_dot(R, va, vb);
     float nw = imp.y + R.nminv * (R.nptarget - cur);
     float diff = fmaxf(nw, 0.0f) - imp.y;
     if (fabsf(diff) > kZero) {
-        for (int k = 0; k < 6; k++) { va[k] += R.nita[k] * diff; vb[k] += R.nitb[k] * diff; }
+        for (int k = 0; k < 6; k++) { va[k] += c_nita(R, k) * diff; vb[k] += c_nitb(R, k) * diff; }
         imp.y += diff;
         store_dv(dv, R.sa, 1, va);
         store_dv(dv, R.sb, 1, vb);
@@ -371,7 +414,8 @@ __device__ __forceinline__ bool ring_wait(uint64_t* bar, uint32_t parity) {
 __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t* bars, uint32_t& phase, float4* dv, int rs,
                                        int rc, const WorldParams& P) {
     const int nch = (rc + kChunkRows - 1) / kChunkRows;
-    const int passes = 1 + P.pgs_vel + P.pgs_pos;
+    const int n_vel = P.pgs_vel;   // read once: the row stores below could alias P for the compiler
+    const int passes = 1 + n_vel + P.pgs_pos;
     const int total = passes * nch;
     const int ahead = nch < kRingSlots ? nch : kRingSlots;
     auto issue = [&](int t) {
@@ -395,7 +439,7 @@ __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t
             float4 imp = R.imp;
             if (pass == 0) {
                 row_warm(R, imp, dv);
-            } else if (pass <= P.pgs_vel) {
+            } else if (pass <= n_vel) {
                 int st = R.stat;
                 row_vel(R, imp, st, dv);
                 g[j].imp = imp;
@@ -677,6 +721,21 @@ __global__ void k_apply_state(Dev d) {
     }
 }
 
+// host-layout state rows (pos, rot, vel, ang vel per body) of a batch split
+// into parts: each part gathers / scatters its bodies' rows by index
+__global__ void k_gather_state(const float4* __restrict__ all, const int* __restrict__ rows, int n, float4* __restrict__ stage) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int r = rows[i];
+        for (int k = 0; k < 4; k++) stage[4 * i + k] = all[4 * (size_t)r + k];
+    }
+}
+__global__ void k_scatter_state(Dev d, const int* __restrict__ rows, float4* __restrict__ all) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
+        float4* o = all + 4 * (size_t)rows[i];
+        o[0] = d.pos[i]; o[1] = d.rot[i]; o[2] = d.vel[i]; o[3] = d.angv[i];
+    }
+}
+
 int grid_for(int n, int per_block, int n_sms) {
     int g = (n + per_block - 1) / per_block;
     int cap = n_sms * 8;
@@ -691,6 +750,13 @@ void launch_rows(const Dev& d, int first, int last, const Launch& L) {
 
 int pgs_big_smem_bytes(int dv_cap) {
     return 64 + kRingSlots * kChunkRows * (int)sizeof(RowBlock) + dv_cap * 64;
+}
+
+// blocks of k_pgs_big resident per SM for this Δv capacity (one chain each)
+int pgs_big_blocks_per_sm(int dv_cap) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pgs_big, 32, pgs_big_smem_bytes(dv_cap)) != cudaSuccess || n < 1) n = 1;
+    return n;
 }
 
 void prepare_pgs(int dv_cap) {
@@ -708,14 +774,14 @@ void launch_pgs_joint(const Dev& d, bool first, const Launch& L) {
     k_pgs_joint<<<L.n_sms * 8, 32, 0, L.st>>>(d, first ? 1 : 0);
 }
 
-void launch_pgs(const Dev& d, int dv_cap, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, const Launch& L) {
+void launch_pgs(const Dev& d, int dv_cap, int big_blocks, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, const Launch& L) {
     // large islands on the main stream, small ones concurrently on a side branch
     cudaMemsetAsync(d.sched + 2, 0, sizeof(int), L.st);
     cudaEventRecord(fork, L.st);
     cudaStreamWaitEvent(side, fork, 0);
     k_pgs_small<<<L.n_sms * 4, 64, 0, side>>>(d);
     cudaEventRecord(join, side);
-    k_pgs_big<<<L.n_sms * 3, 32, pgs_big_smem_bytes(dv_cap), L.st>>>(d, dv_cap);
+    k_pgs_big<<<big_blocks, 32, pgs_big_smem_bytes(dv_cap), L.st>>>(d, dv_cap);
     cudaStreamWaitEvent(L.st, join, 0);
 }
 
@@ -725,6 +791,14 @@ void launch_integrate(const Dev& d, int last, const Launch& L) {
 
 void launch_apply_state(const Dev& d, const Launch& L) {
     k_apply_state<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d);
+}
+
+void launch_gather_state(const Dev& d, const float4* all, const int* rows, const Launch& L) {
+    k_gather_state<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(all, rows, d.n_bodies, d.stage);
+}
+
+void launch_scatter_state(const Dev& d, const int* rows, float4* all, const Launch& L) {
+    k_scatter_state<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d, rows, all);
 }
 
 }  // namespace cpgpu
