@@ -547,12 +547,12 @@ struct Batch {
         }
         launch_geometry(x, 0, L);  mark(6 + 3 * substeps);
     }
-    // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 1
+    // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 2
     // (+1 with spheres / cylinders, +1 with meshes), merge 6 + 3 scans, islands 2 + scan 3,
     // schedule 3, 5 per substep (rows, small + grouped + large PGS, integrate), geometry 1
     // (+2 per substep and 1 factorisation with joints)
     int launches_per_step() const {
-        return 1 + 6 + 1 + (prims ? 1 : 0) + (meshes ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 5 * substeps + 1 + (joints ? 2 * substeps : 0) +
+        return 1 + 6 + 2 + (prims ? 1 : 0) + (meshes ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 5 * substeps + 1 + (joints ? 2 * substeps : 0) +
                (systems ? 1 : 0);
     }
 
@@ -1003,6 +1003,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         x.pair_a = A.take<int>(cap_pairs); x.pair_b = A.take<int>(cap_pairs);
         x.mf_n = A.take<float4>(cap_pairs); x.mf_cnt = A.take<int>(cap_pairs);
         x.mf_pt = A.take<float4>(4 * (size_t)cap_pairs); x.mf_magic = A.take<uint64_t>(4 * (size_t)cap_pairs);
+        x.mf_feat = A.take<int2>(cap_pairs);
         for (int k = 0; k < 2; k++) {
             es[k].key = A.take<uint64_t>(cap_edges); es[k].cstart = A.take<int>(cap_edges); es[k].ccount = A.take<int>(cap_edges);
             cs[k].magic = A.take<uint64_t>(cap_contacts);

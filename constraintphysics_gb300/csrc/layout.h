@@ -259,6 +259,7 @@ struct Dev {
     int* mf_cnt;
     float4* mf_pt;                 // [4] per pair: pos xyz, w pen
     uint64_t* mf_magic;            // [4] per pair
+    int2* mf_feat;                 // hull pairs: features of the minimum axis (vertex of A, of B) for k_clip
     // static meshes (has_mesh == 0: none in the batch).  A mesh pair's points
     // are in the mesh store at mf_ofs[p] (-1: not a mesh pair), mf_cnt[p] of
     // them, each with its merged manifold's normal; mf_n[p].w is their max pen

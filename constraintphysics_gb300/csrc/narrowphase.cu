@@ -72,6 +72,30 @@ struct HullView {
     const uint8_t* arc;  // staged arc pairs
     const uint8_t* g;    // global blob (cold sections)
     f3 com;
+    __device__ __forceinline__ f3 vert(int i) const { return mk(v[i]); }
+    __device__ __forceinline__ f3 norm(int f) const { return mk(n[f]); }
+};
+
+// The same hull read from its global blob by one thread, each vertex and
+// normal put in world space when it is used (the arithmetic of stage_hull, so
+// both views give identical values)
+struct HullG {
+    const HullHeader* h;
+    const float4* vref;
+    const float4* nref;
+    const uint8_t* g;
+    f3 com;
+    M33 R;
+    __device__ __forceinline__ HullG(const uint8_t* blob, float4 pos, float4 rot) {
+        h = reinterpret_cast<const HullHeader*>(blob);
+        vref = reinterpret_cast<const float4*>(blob + sizeof(HullHeader));
+        nref = reinterpret_cast<const float4*>(blob + h->off_norm);
+        g = blob;
+        com = mk(pos);
+        R = quatRot(qnormalize(rot));
+    }
+    __device__ __forceinline__ f3 vert(int i) const { return com + mul(R, mk(__ldg(vref + i))); }
+    __device__ __forceinline__ f3 norm(int f) const { return mul(R, mk(__ldg(nref + f))); }
 };
 
 __device__ __forceinline__ const uint16_t* u16(const uint8_t* base, int off) { return reinterpret_cast<const uint16_t*>(base + off); }
@@ -213,7 +237,8 @@ __device__ int toClipPoly(const Area& a, uint32_t other_surface, bool flip, CP* 
 }
 
 // findContactArea (CollisionDetect.cpp:237-280)
-__device__ void contactArea(const HullView& h, f3 n, int pid, f3 u, f3 w, Area* a) {
+template <class HV>
+__device__ void contactArea(const HV& h, f3 n, int pid, f3 u, f3 w, Area* a) {
     const HullHeader& H = *h.h;
     const uint16_t* vfofs = u16(h.g, H.off_vfofs);
     const uint8_t* vfidx = h.g + H.off_vfidx;
@@ -221,7 +246,7 @@ __device__ void contactArea(const HullView& h, f3 n, int pid, f3 u, f3 w, Area* 
     float best_ft = 1.0f;
     for (int k = vfofs[pid]; k < vfofs[pid + 1]; k++) {
         int f = vfidx[k];
-        float ca = dot(mk(h.n[f]), n);
+        float ca = dot(h.norm(f), n);
         if (1.f - ca < best_ft) { best_ft = 1.f - ca; best_f = f; }
     }
     if (best_ft <= kCosTol) {
@@ -230,7 +255,7 @@ __device__ void contactArea(const HullView& h, f3 n, int pid, f3 u, f3 w, Area* 
         a->n = 0;
         for (int k = fofs[best_f]; k < fofs[best_f + 1] && a->n < kMaxClip; k++) {
             int id = fidx[k];
-            f3 v = mk(h.v[id]);
+            f3 v = h.vert(id);
             a->ps[a->n] = P2{dot(v, u), dot(v, w)};
             a->ids[a->n++] = id;
         }
@@ -244,13 +269,13 @@ __device__ void contactArea(const HullView& h, f3 n, int pid, f3 u, f3 w, Area* 
     float best_et = 1.0f;
     for (int k = veofs[pid]; k < veofs[pid + 1]; k++) {
         int e = veidx[k];
-        f3 d = mk(h.v[edges[2 * e + 1]]) - mk(h.v[edges[2 * e]]);
+        f3 d = h.vert(edges[2 * e + 1]) - h.vert(edges[2 * e]);
         float sa = fabsf(dot(normalize(d), n));
         if (sa < best_et) { best_et = sa; best_e = e; }
     }
     if (best_et <= kSinTol) {
         int p1 = edges[2 * best_e], p2 = edges[2 * best_e + 1];
-        f3 e1 = mk(h.v[p1]), e2 = mk(h.v[p2]);
+        f3 e1 = h.vert(p1), e2 = h.vert(p2);
         a->ps[0] = P2{dot(e1, u), dot(e1, w)};
         a->ps[1] = P2{dot(e2, u), dot(e2, w)};
         a->ids[0] = p1; a->ids[1] = p2;
@@ -258,7 +283,7 @@ __device__ void contactArea(const HullView& h, f3 n, int pid, f3 u, f3 w, Area* 
         a->surface = -1;
         return;
     }
-    f3 p = mk(h.v[pid]);
+    f3 p = h.vert(pid);
     a->ps[0] = P2{dot(p, u), dot(p, w)};
     a->ids[0] = pid;
     a->n = 1;
@@ -1181,8 +1206,6 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
     if (lane == 0) mbar_init(&bars[wib]);
     __syncthreads();
     uint32_t parity = 0;
-    Scratch scratch;
-    CP clipped[kMaxClip];
     const int n_pairs = *d.n_pairs;
     for (int p = blockIdx.x * warps_per_block + wib; p < n_pairs; p += gridDim.x * warps_per_block) {
         const int a = d.pair_a[p], b = d.pair_b[p];
@@ -1317,59 +1340,55 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
         float nz = __shfl_sync(0xffffffffu, best.n.z, owner);
         int aid = __shfl_sync(0xffffffffu, best.aid, owner);
         int bid = __shfl_sync(0xffffffffu, best.bid, owner);
+        // the axis and the two features; k_clip turns them into the manifold
         if (lane == 0) {
-            f3 n = mk(nx, ny, nz);
             if (!(bp < INFINITY) || aid < 0 || bid < 0) {
                 d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f);
-                d.mf_cnt[p] = 0;
             } else {
-                f3 u, w;
-                basis(n, &u, &w);
-                Area ac, bc;
-                contactArea(A, n, aid, u, w, &ac);
-                contactArea(B, -1.f * n, bid, u, w, &bc);
-                int m = clipContacts(ac, bc, scratch, clipped, d.status);
-                f3 amax = mk(A.v[aid]);
-                float a_dot = dot(amax, n);
-                f3 off = n * a_dot;
-                float4 pts[kMaxClip];
-                for (int i = 0; i < m; i++) {
-                    f3 q = u * clipped[i].p.x + w * clipped[i].p.y + off;
-                    pts[i] = make_float4(q.x, q.y, q.z, dot(q, n) - a_dot + bp);
-                }
-                // cull_manifold to 4 points (CollisionDetect.cpp:2795-2830)
-                int out_n = m;
-                int pick[4] = {0, 1, 2, 3};
-                if (m > 4) {
-                    out_n = 4;
-                    unsigned long long avail = (m >= 64) ? ~0ull : ((1ull << m) - 1ull);
-                    f3 cu, cw;
-                    basis(n, &cu, &cw);
-                    const float cs[4] = {1.0f, 6.123233995736766e-17f, -1.0f, -1.8369701987210297e-16f};
-                    const float sn[4] = {0.0f, 1.0f, 1.2246467991473532e-16f, -1.0f};
-                    for (int i = 0; i < 4; i++) {
-                        f3 dir = cu * cs[i] + cw * sn[i];
-                        int bi2 = -1;
-                        float bv = -INFINITY;
-                        for (int j = 0; j < m; j++) {
-                            if (!((avail >> j) & 1ull)) continue;
-                            float v = dot(mk(pts[j]), dir);
-                            if (v > bv) { bv = v; bi2 = j; }
-                        }
-                        if (bi2 < 0) { out_n = i; break; }
-                        pick[i] = bi2;
-                        avail &= ~(1ull << bi2);
-                    }
-                }
-                float maxpen = bp;
-                for (int i = 0; i < out_n; i++) {
-                    d.mf_pt[4 * p + i] = pts[pick[i]];
-                    d.mf_magic[4 * p + i] = clipped[pick[i]].magic;
-                }
-                d.mf_n[p] = make_float4(n.x, n.y, n.z, maxpen);
-                d.mf_cnt[p] = out_n;
+                d.mf_n[p] = make_float4(nx, ny, nz, bp);
+                d.mf_feat[p] = make_int2(aid, bid);
             }
+            d.mf_cnt[p] = 0;
         }
+    }
+}
+
+// Contact generation of the convex-hull pairs k_narrowphase found
+// overlapping, one thread per pair: contact features (findContactArea,
+// CollisionDetect.cpp:237-280), clipping (:394-620) and the 4-direction cull
+// (:2795-2830).  The clip is serial per pair; a thread each keeps all lanes of
+// a warp busy on 32 pairs, where a warp per pair would idle 31.
+__global__ void __launch_bounds__(128) k_clip(Dev d) {
+    const int n_pairs = *d.n_pairs;
+    Scratch scratch;
+    CP clipped[kMaxClip];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_pairs; p += gridDim.x * blockDim.x) {
+        const float4 nn = d.mf_n[p];
+        if (!(nn.w > 0.f)) continue;
+        const int a = d.pair_a[p], b = d.pair_b[p];
+        const uint8_t* ga = d.shapes + d.shape[a];
+        const uint8_t* gb = d.shapes + d.shape[b];
+        if ((reinterpret_cast<const HullHeader*>(ga)->kind | reinterpret_cast<const HullHeader*>(gb)->kind) != SHAPE_HULL) continue;
+        const HullG A(ga, d.pos[a], d.rot[a]), B(gb, d.pos[b], d.rot[b]);
+        const int2 feat = d.mf_feat[p];
+        const f3 n = mk(nn);
+        const float bp = nn.w;
+        f3 u, w;
+        basis(n, &u, &w);
+        Area ac, bc;
+        contactArea(A, n, feat.x, u, w, &ac);
+        contactArea(B, -1.f * n, feat.y, u, w, &bc);
+        const int m = clipContacts(ac, bc, scratch, clipped, d.status);
+        const float a_dot = dot(A.vert(feat.x), n);
+        const f3 off = n * a_dot;
+        float4 pts[kMaxClip];
+        unsigned long long mag[kMaxClip];
+        for (int i = 0; i < m; i++) {
+            f3 q = u * clipped[i].p.x + w * clipped[i].p.y + off;
+            pts[i] = make_float4(q.x, q.y, q.z, dot(q, n) - a_dot + bp);
+            mag[i] = clipped[i].magic;
+        }
+        emit_manifold(d, p, n, bp, pts, mag, m);
     }
 }
 
@@ -1576,6 +1595,7 @@ void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cud
     const int warps = 8;
     size_t smem = 16 * warps + (size_t)warps * (slot_bytes + kQueueBytes);
     k_narrowphase<<<n_sms * 4, warps * 32, smem, st>>>(d, slot_bytes);
+    k_clip<<<n_sms * 16, 128, 0, st>>>(d);
     if (prims) k_narrow_prim<<<n_sms * 4, warps * 32, 16 * warps + (size_t)warps * slot_bytes, st>>>(d, slot_bytes);
     if (d.has_mesh)
         k_narrow_mesh<<<n_sms * kMeshBlocksPerSm, warps * 32, 16 * warps + (size_t)warps * slot_bytes, st>>>(d, slot_bytes);
