@@ -385,11 +385,13 @@ constexpr long long kWaitLimit = 1LL << 24;
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 
-__device__ __forceinline__ void ring_load(RowBlock* dst, const RowBlock* src, int rows, uint64_t* bar) {
+// `fence`: this thread wrote impulses to `src` with generic stores since its
+// last proxy fence; those writes must be ordered before the async-proxy copy
+// reads them.  (Its earlier reads of `dst` have completed: their values were
+// used before this copy is issued.)
+__device__ __forceinline__ void ring_load(RowBlock* dst, const RowBlock* src, int rows, uint64_t* bar, bool fence) {
     uint32_t bytes = (uint32_t)(rows * sizeof(RowBlock));
-    // this thread wrote impulses to `src` with generic stores, and read `dst`
-    // before: order both against the async-proxy copy
-    asm volatile("fence.proxy.async;" ::: "memory");
+    if (fence) asm volatile("fence.proxy.async;" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(saddr(dst)),
                  "l"(src), "r"(bytes), "r"(saddr(bar))
@@ -418,12 +420,21 @@ __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t
     const int passes = 1 + n_vel + P.pgs_pos;
     const int total = passes * nch;
     const int ahead = nch < kRingSlots ? nch : kRingSlots;
-    auto issue = [&](int t) {
+    // A proxy fence covers every impulse write issued before it.  Chunk c of
+    // sequence t was last written at sequence t - nch (by a velocity or
+    // position pass, i.e. t - nch >= nch); a fence is needed only if none was
+    // issued since: about once per pass on a large island, every chunk on a
+    // small one.
+    int fenced = -1;
+    auto issue = [&](int t, int now) {
         int c = t % nch, slot = t % kRingSlots;
         int n = min(kChunkRows, rc - c * kChunkRows);
-        ring_load(ring + slot * kChunkRows, d.rows + rs + c * kChunkRows, n, &bars[slot]);
+        const int tw = t - nch;
+        const bool fence = tw >= nch && tw > fenced;
+        if (fence) fenced = now;
+        ring_load(ring + slot * kChunkRows, d.rows + rs + c * kChunkRows, n, &bars[slot], fence);
     };
-    for (int t = 0; t < ahead && t < total; t++) issue(t);
+    for (int t = 0; t < ahead && t < total; t++) issue(t, -1);
     for (int t = 0; t < total; t++) {
         const int slot = t % kRingSlots, pass = t / nch, c = t % nch;
         if (!ring_wait(&bars[slot], (phase >> slot) & 1u)) return false;
@@ -449,7 +460,7 @@ __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t
                 g[j].imp = imp;
             }
         }
-        if (t + ahead < total) issue(t + ahead);
+        if (t + ahead < total) issue(t + ahead, t);
     }
     return true;
 }
