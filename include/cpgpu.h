@@ -126,7 +126,9 @@ int cpgpu_body_cylinder(cpgpu_world* w, const double base[3], double radius, dou
                         const cpgpu_material* mat, int movement, const double pos[3],
                         uint32_t* out_id);
 /* createRigidBody(StaticMeshGeometry(MeshInput{tris, points}), fixed)
- * (PhysicsEngine.cpp:498-512, Geometry.h:52-55) */
+ * (PhysicsEngine.cpp:498-512, Geometry.h:52-55): points (xyz) and triangles
+ * (three point indices each) in world coordinates; `fixed` must be nonzero
+ * (kinematic meshes: CPGPU_ERR_UNSUPPORTED).  Mesh-mesh pairs never collide. */
 int cpgpu_body_mesh(cpgpu_world* w, const double* points, int n_points,
                     const int* tris, int n_tris, const cpgpu_material* mat,
                     int fixed, uint32_t* out_id);
