@@ -147,6 +147,21 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_traffic(stage, worlds):
+    """DRAM bytes per launch of the stage's kernels from the committed ncu
+    summary (profiles/roofline_traffic.txt), for this workload size only."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "roofline_traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 3 and not line.startswith("#") and parts[0] == stage and int(parts[2]) == worlds:
+                    return int(parts[1])
+    except OSError:
+        pass
+    return None
+
+
 def algorithmic_bytes(stage, counts, nbodies, vfe, params):
     """Algorithmic bytes of one launch of a stage (each datum read/written once)."""
     V, F, E = vfe
@@ -363,7 +378,7 @@ def main():
         if b is not None:
             achieved = b / (stage_ms[stage] / 1e3) / 1e9
             roof = {"bound": "hbm", "kernel": stage, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": measured_traffic(stage, a.worlds),
                     "algorithmic_bytes_per_launch": b, "launch_ms": stage_ms[stage],
                     "note": "dominant stage" if stage == dominant else f"dominant stage {dominant} has no byte model"}
             break
