@@ -1017,6 +1017,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         x.surv = A.take<int>(cap_edges); x.surv_scan = A.take<int>(cap_edges);
         x.unm = A.take<int>(cap_pairs); x.unm_scan = A.take<int>(cap_pairs); x.pair_edge = A.take<int>(cap_pairs);
         x.edge_src = A.take<int>(cap_edges); x.edge_pair = A.take<int>(cap_edges); x.edge_cnt = A.take<int>(cap_edges);
+        x.edge_live = A.take<int>(cap_edges); x.edge_row = A.take<int>(cap_edges);
         x.scan_tmp = A.take<int>(scan_tmp);
         x.adj_ofs = A.take<int>(N); x.adj_cursor = A.take<int>(N);
         x.adj_list = A.take<int>(2 * (2 * ((size_t)cap_edges + n_je) + N));

@@ -205,6 +205,15 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int i = s + tid; i < e; i += nt) { d.adj_cursor[i] = 0; d.visited[i] = -1; }
     for (int c = c0 + tid; c < c1; c += nt) d.row_of_contact[c] = -1;
+    // live contacts per edge, so that the serial DFS below advances its row
+    // cursor by one load per edge instead of one per contact
+    for (int k = e0 + tid; k < e1; k += nt) {
+        const int cs = d.e_new.cstart[k], cn = d.e_new.ccount[k];
+        int live = 0;
+        for (int c = cs; c < cs + cn; c++) live += cs_live(d.c_new.state[c]);
+        d.edge_live[k] = live;
+        d.edge_row[k] = -1;
+    }
     __syncthreads();
     for (int k = e0 + tid; k < e1; k += nt) {
         uint64_t key = d.e_new.key[k];
@@ -305,9 +314,9 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
                         has_joint = true;
                         continue;
                     }
-                    int cs = d.e_new.cstart[k], cn = d.e_new.ccount[k];
-                    for (int c = cs; c < cs + cn; c++)
-                        if (cs_live(d.c_new.state[c])) d.row_contact[rc++] = c;
+                    // the edge's live contacts take the next rows (written below)
+                    const int nl = d.edge_live[k];
+                    if (nl > 0) { d.edge_row[k] = rc; rc += nl; }
                 }
                 for (int j = lo; j < hi; j++) {
                     int o = d.adj_list[2 * j];
@@ -336,6 +345,15 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
         }
         d.isl_count_w[w] = ni;
         sh_rows_end = rc;
+    }
+    __syncthreads();
+    // each emitted edge's live contacts into its rows, in contact order
+    for (int k = e0 + tid; k < e1; k += nt) {
+        int r = d.edge_row[k];
+        if (r < 0) continue;
+        const int cs = d.e_new.cstart[k], cn = d.e_new.ccount[k];
+        for (int c = cs; c < cs + cn; c++)
+            if (cs_live(d.c_new.state[c])) d.row_contact[r++] = c;
     }
     __syncthreads();
     const int rows_end = sh_rows_end;

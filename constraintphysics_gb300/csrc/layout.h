@@ -276,6 +276,7 @@ struct Dev {
     int *n_edges_old, *n_edges_new, *n_contacts_old, *n_contacts_new;
     // merge scratch
     int *surv, *surv_scan, *unm, *unm_scan, *pair_edge, *edge_src, *edge_pair, *edge_cnt;
+    int *edge_live, *edge_row;     // islands: live contacts per edge, first row of an emitted edge
     int *scan_tmp;
     // islands
     int* adj_ofs;                  // per body CSR offsets (scratch)

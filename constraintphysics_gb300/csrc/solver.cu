@@ -119,7 +119,13 @@ __global__ void k_rows(Dev d, int first, int last) {
             const float wf0 = P.warm_disabled ? 0.f : imp.y, wf1 = P.warm_disabled ? 0.f : imp.z;
             const float pcc = fminf(P.hardness * dt, 1.0f / dt);
             const f3 rA = pa - ca, rB = pa - cb;
-            RowBlock& R = d.rows[r];
+            // the row is assembled in registers and written with 16-byte stores
+            // (a thread per contact writing 384 scattered bytes field by field
+            // would issue 96 partial-sector stores)
+            RowBlock R;
+            R.sa = (d.movement[a] == 0) ? d.visited[a] : -1;
+            R.sb = (d.movement[b] == 0) ? d.visited[b] : -1;
+            R.contact = c;
             R.ga = a; R.gb = b;
             R.bounce = p2.w;
             R.cutoff = P.cutoff_vel;
@@ -184,6 +190,12 @@ __global__ void k_rows(Dev d, int first, int last) {
                 R.tgt_n = (cur < -P.cutoff_vel) ? -(1.0f + p2.w) * cur : -cur;
                 R.tgt_f0 = -(dot6(fja, va) + dot6(fjb, vb));
                 R.tgt_f1 = -(dot6(fja + 6, va) + dot6(fjb + 6, vb));
+            }
+            {
+                float4* dst = reinterpret_cast<float4*>(d.rows + r);
+                const float4* src = reinterpret_cast<const float4*>(&R);
+#pragma unroll
+                for (int k = 0; k < (int)(sizeof(RowBlock) / 16); k++) dst[k] = src[k];
             }
             d.c_new.fu[c] = make_float4(u.x, u.y, u.z, 0.f);
             d.c_new.fw[c] = make_float4(w.x, w.y, w.z, 0.f);
