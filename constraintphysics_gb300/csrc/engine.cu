@@ -899,6 +899,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     std::vector<uint64_t> je_key;
     std::vector<int> je_jstart, je_jcount, je_sys, je_wstart{0}, je_wjstart{0}, hs_wstart{0};
     std::vector<int> hs_cstart{0}, hs_cons, hs_vpos, hs_degree, hs_tstart{0}, hs_table, hs_bstart, hs_cap, hs_fp64, hs_wk;
+    std::vector<int> hs_lbase, hs_lstart, hs_lrow, hs_lloc;   // per-column lists of the nonzero blocks below the diagonal
     size_t pool32_n = 0, pool64_n = 0, work_n = 0;
     for (size_t wi = 0; wi < worlds.size(); wi++) {
         const World& w = *worlds[wi];
@@ -939,6 +940,19 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
                 hs_degree.push_back(H.degree);
                 hs_table.insert(hs_table.end(), H.table.begin(), H.table.end());
                 hs_tstart.push_back((int)hs_table.size());
+                {
+                    const int nc = (int)H.cons.size();
+                    hs_lbase.push_back((int)hs_lstart.size());
+                    for (int col = 0; col < nc; col++) {
+                        hs_lstart.push_back((int)hs_lrow.size());
+                        const int base = col * nc - (col * (col - 1)) / 2;   // column col starts at its diagonal
+                        for (int row = col + 1; row < nc; row++) {
+                            const int l = H.table[base + (row - col)];
+                            if (l >= 0) { hs_lrow.push_back(row); hs_lloc.push_back(l); }
+                        }
+                    }
+                    hs_lstart.push_back((int)hs_lrow.size());
+                }
                 hs_cap.push_back(H.cap);
                 hs_fp64.push_back(H.fp64 ? 1 : 0);
                 const size_t need = (size_t)H.cap + 6 * (size_t)H.degree;
@@ -1070,6 +1084,8 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
             H.n = n_sys;
             H.cstart = A.take<int>(n_sys + 1); H.cons = A.take<int>(hs_cons.size()); H.vpos = A.take<int>(hs_vpos.size());
             H.degree = A.take<int>(n_sys); H.tstart = A.take<int>(n_sys + 1); H.table = A.take<int>(hs_table.size());
+            H.lbase = A.take<int>(n_sys); H.lstart = A.take<int>(hs_lstart.size());
+            H.lrow = A.take<int>(hs_lrow.size()); H.lloc = A.take<int>(hs_lloc.size());
             H.bstart = A.take<int>(n_sys); H.cap = A.take<int>(n_sys); H.fp64 = A.take<int>(n_sys);
             H.wstart = A.take<int>(n_sys);
             H.pool32 = A.take<float>(pool32_n); H.pool64 = A.take<double>(pool64_n); H.work = A.take<double>(work_n);
@@ -1133,6 +1149,8 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
         up((void*)H.cstart, hs_cstart.data(), hs_cstart.size() * 4); up((void*)H.cons, hs_cons.data(), hs_cons.size() * 4);
         up((void*)H.vpos, hs_vpos.data(), hs_vpos.size() * 4); up((void*)H.degree, hs_degree.data(), hs_degree.size() * 4);
         up((void*)H.tstart, hs_tstart.data(), hs_tstart.size() * 4); up((void*)H.table, hs_table.data(), hs_table.size() * 4);
+        up((void*)H.lbase, hs_lbase.data(), hs_lbase.size() * 4); up((void*)H.lstart, hs_lstart.data(), hs_lstart.size() * 4);
+        up((void*)H.lrow, hs_lrow.data(), hs_lrow.size() * 4); up((void*)H.lloc, hs_lloc.data(), hs_lloc.size() * 4);
         up((void*)H.bstart, hs_bstart.data(), hs_bstart.size() * 4); up((void*)H.cap, hs_cap.data(), hs_cap.size() * 4);
         up((void*)H.fp64, hs_fp64.data(), hs_fp64.size() * 4); up((void*)H.wstart, hs_wk.data(), hs_wk.size() * 4);
         up((void*)x.hs_world_start, hs_wstart.data(), hs_wstart.size() * 4);

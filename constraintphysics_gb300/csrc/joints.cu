@@ -62,17 +62,23 @@ __device__ void invert_block(int n, T* m) {
         T c[kJMax * kJMax];
         for (int k = 0; k < n * n; k++) { c[k] = m[k]; out[k] = 0; }
         for (int k = 0; k < n; k++) out[k * (n + 1)] = 1;
-        for (int piv = 0; piv < n; piv++)
+        // one reciprocal per pivot (FP64 division is a long instruction
+        // sequence; the ratios and the final scaling multiply by it)
+        for (int piv = 0; piv < n; piv++) {
+            const T rp = T(1) / c[n * piv + piv];
             for (int r = 0; r < n; r++) {
                 if (r == piv) continue;
-                T ratio = c[n * r + piv] / c[n * piv + piv];
+                T ratio = c[n * r + piv] * rp;
                 for (int k = 0; k < n; k++) {
                     c[n * r + k] -= ratio * c[n * piv + k];
                     out[n * r + k] -= ratio * out[n * piv + k];
                 }
             }
-        for (int piv = 0; piv < n; piv++)
-            for (int k = 0; k < n; k++) out[n * piv + k] /= c[n * piv + piv];
+        }
+        for (int piv = 0; piv < n; piv++) {
+            const T rp = T(1) / c[n * piv + piv];
+            for (int k = 0; k < n; k++) out[n * piv + k] *= rp;
+        }
     }
     for (int k = 0; k < n * n; k++) m[k] = out[k];
 }
@@ -201,25 +207,21 @@ __device__ void factorise(const Dev& d, int s, T* B, float cfm) {
     const int c0 = hs.cstart[s], n = hs.cstart[s + 1] - c0;
     const int* cons = hs.cons + c0;
     const int* table = hs.table + hs.tstart[s];
+    const int* ls = hs.lstart + hs.lbase[s];   // column col's blocks below the diagonal: [ls[col], ls[col + 1])
     T* Dg = B + hs.cap[s];
-    auto first_below = [&](int col) {
-        for (int r = col + 1; r < n; r++) { int l = holo_loc(table, n, r, col); if (l >= 0) return l; }
-        return -1;
-    };
-    for (int col = 0; col < n; col++)
-        for (int row = col; row < n; row++) {
-            const int l = holo_loc(table, n, row, col);
-            if (l >= 0) initial_block<T>(d, cons[row], cons[col], B + l, cfm);
-        }
+    for (int col = 0; col < n; col++) {
+        initial_block<T>(d, cons[col], cons[col], B + holo_loc(table, n, col, col), cfm);
+        for (int q = ls[col]; q < ls[col + 1]; q++) initial_block<T>(d, cons[hs.lrow[q]], cons[col], B + hs.lloc[q], cfm);
+    }
     for (int col = 0; col < n; col++) {
         const int w = d.jt.rows[cons[col]].n;
         T* diag = B + holo_loc(table, n, col, col);
         invert_block<T>(w, diag);
         if (col + 1 == n) continue;
-        const int fb = first_below(col);
-        for (int row = col + 1; row < n; row++) {
-            const int l = holo_loc(table, n, row, col);
-            if (l < 0) continue;
+        const int q0 = ls[col], q1 = ls[col + 1];
+        const int fb = q0 < q1 ? hs.lloc[q0] : -1;
+        for (int q = q0; q < q1; q++) {
+            const int row = hs.lrow[q], l = hs.lloc[q];
             const int h = d.jt.rows[cons[row]].n;
             T* tgt = Dg + (l - fb);
             for (int r = 0; r < h; r++)
@@ -229,13 +231,11 @@ __device__ void factorise(const Dev& d, int s, T* B, float cfm) {
                     tgt[c + w * r] = x;
                 }
         }
-        for (int lc = col + 1; lc < n; lc++) {
-            const int llc = holo_loc(table, n, lc, col);
-            if (llc < 0) continue;
+        for (int qa = q0; qa < q1; qa++) {
+            const int lc = hs.lrow[qa], llc = hs.lloc[qa];
             const int bw = d.jt.rows[cons[lc]].n;
-            for (int lr = lc; lr < n; lr++) {
-                const int l = holo_loc(table, n, lr, col);
-                if (l < 0) continue;
+            for (int qb = qa; qb < q1; qb++) {
+                const int lr = hs.lrow[qb], l = hs.lloc[qb];
                 const int bh = d.jt.rows[cons[lr]].n;
                 T* tgt = B + holo_loc(table, n, lr, lc);
                 const T* lsrc = Dg + (llc - fb);
@@ -270,9 +270,11 @@ void launch_joint_rows(const Dev& d, bool first, const Launch& L) {
     g = g > L.n_sms * 8 ? L.n_sms * 8 : g;
     k_joint_rows<<<g, 128, 0, L.st>>>(d);
     if (first && d.hs.n > 0) {
-        int gs = (d.hs.n + 63) / 64;
-        gs = gs > L.n_sms * 8 ? L.n_sms * 8 : gs;
-        k_holo_factor<<<gs, 64, 0, L.st>>>(d);
+        // a system per thread, few threads per block: the FP64 work spreads
+        // over every SM instead of packing into a handful
+        int gs = (d.hs.n + 7) / 8;
+        gs = gs > L.n_sms * 32 ? L.n_sms * 32 : gs;
+        k_holo_factor<<<gs, 8, 0, L.st>>>(d);
     }
 }
 

@@ -53,30 +53,69 @@ __device__ __forceinline__ void japply(const JointRow& R, const float* imp, floa
     jadd(dv, R.sb, which, xb);
 }
 
+// The same steps for a row of N dofs known at compile time (3: ball-socket,
+// 5: hinge): every loop unrolls, so the row's entries are loaded once into
+// registers instead of through loops over a run-time count (identical sums)
+template <int N>
+__device__ __forceinline__ void japply_n(const JointRow& R, const float* imp, float4* dv, int which) {
+    float xa[6], xb[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        float x = 0.f, y = 0.f;
+#pragma unroll
+        for (int i = 0; i < N; i++) { x += imp[i] * R.ita[kJMax * k + i]; y += imp[i] * R.itb[kJMax * k + i]; }
+        xa[k] = x;
+        xb[k] = y;
+    }
+    jadd(dv, R.sa, which, xa);
+    jadd(dv, R.sb, which, xb);
+}
+
+template <int N>
+__device__ __forceinline__ void jstep_n(JointRow& R, float4* dv, bool pseudo) {
+    const int which = pseudo ? 1 : 0;
+    float va[6], vb[6], delta[N], diff[N], acc[N];
+    jload(dv, R.sa, which, va);
+    jload(dv, R.sb, which, vb);
+    float* accp = pseudo ? R.pimpulse : R.impulse;
+    const float* tgt = pseudo ? R.ptarget : R.target;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        float x = 0.f, y = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; k++) x += va[k] * R.ja[6 * i + k];
+#pragma unroll
+        for (int k = 0; k < 6; k++) y += vb[k] * R.jb[6 * i + k];
+        delta[i] = tgt[i] - (x + y);
+        acc[i] = accp[i];
+    }
+    bool zero = true;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        float x = 0.f;
+#pragma unroll
+        for (int k = 0; k < N; k++) x += delta[k] * R.minv[kJMax * i + k];
+        diff[i] = (acc[i] + x) - acc[i];
+        zero = zero && !(fabsf(diff[i]) > kJZero);
+    }
+    if (!zero) {
+        japply_n<N>(R, diff, dv, which);
+#pragma unroll
+        for (int i = 0; i < N; i++) accp[i] = acc[i] + diff[i];
+    }
+}
+
 // warm start (DegreedConstraint::applyWarmStartVelocityChange)
 __device__ __forceinline__ void jwarm(const JointRow& R, float4* dv) {
-    if (!jzero(R.impulse, R.n)) japply(R, R.impulse, dv, 0);
+    if (jzero(R.impulse, R.n)) return;
+    if (R.n == 3) japply_n<3>(R, R.impulse, dv, 0);
+    else japply_n<5>(R, R.impulse, dv, 0);
 }
 
 // PGSConstraintStep<n> (ConstraintSolver.cpp:12-40) of an equality row
 __device__ __forceinline__ void jstep(JointRow& R, float4* dv, bool pseudo) {
-    const int which = pseudo ? 1 : 0;
-    float va[6], vb[6], cur[kJMax], delta[kJMax], diff[kJMax];
-    jload(dv, R.sa, which, va);
-    jload(dv, R.sb, which, vb);
-    jvalue(R, va, vb, cur);
-    float* acc = pseudo ? R.pimpulse : R.impulse;
-    const float* tgt = pseudo ? R.ptarget : R.target;
-    for (int i = 0; i < R.n; i++) delta[i] = tgt[i] - cur[i];
-    for (int i = 0; i < R.n; i++) {
-        float x = 0.f;
-        for (int k = 0; k < R.n; k++) x += delta[k] * R.minv[kJMax * i + k];
-        diff[i] = (acc[i] + x) - acc[i];
-    }
-    if (!jzero(diff, R.n)) {
-        japply(R, diff, dv, which);
-        for (int i = 0; i < R.n; i++) acc[i] += diff[i];
-    }
+    if (R.n == 3) jstep_n<3>(R, dv, pseudo);
+    else jstep_n<5>(R, dv, pseudo);
 }
 
 // ---- holonomic systems (HolonomicBlockSolver.cpp) ------------------------------
@@ -88,15 +127,15 @@ __device__ __forceinline__ int holo_loc(const int* table, int n, int row, int co
 // `eff` holds `degree` scratch values.
 template <class T>
 __device__ void holo_solve(const HoloStore& hs, int s, const JointRow* rows, const T* B, T* v, T* eff) {
-    const int c0 = hs.cstart[s], n = hs.cstart[s + 1] - c0, deg = hs.degree[s];
+    const int c0 = hs.cstart[s], n = hs.cstart[s + 1] - c0;
     const int* cons = hs.cons + c0;
     const int* vp = hs.vpos + c0;
     const int* table = hs.table + hs.tstart[s];
+    const int* ls = hs.lstart + hs.lbase[s];   // column col's blocks below the diagonal
     for (int col = 0; col + 1 < n; col++) {
         const int bw = rows[cons[col]].n;
-        for (int row = col + 1; row < n; row++) {
-            const int l = holo_loc(table, n, row, col);
-            if (l < 0) continue;
+        for (int q = ls[col]; q < ls[col + 1]; q++) {
+            const int row = hs.lrow[q], l = hs.lloc[q];
             const int bh = rows[cons[row]].n;
             for (int i = 0; i < bh; i++) {
                 T x = 0;
@@ -105,8 +144,8 @@ __device__ void holo_solve(const HoloStore& hs, int s, const JointRow* rows, con
             }
         }
         // only rows below `col` were written this pass: subtract and clear them
-        for (int row = col + 1; row < n; row++) {
-            if (holo_loc(table, n, row, col) < 0) continue;
+        for (int q = ls[col]; q < ls[col + 1]; q++) {
+            const int row = hs.lrow[q];
             for (int i = 0; i < rows[cons[row]].n; i++) { v[vp[row] + i] -= eff[vp[row] + i]; eff[vp[row] + i] = 0; }
         }
     }
@@ -123,9 +162,8 @@ __device__ void holo_solve(const HoloStore& hs, int s, const JointRow* rows, con
     for (int col = n - 2; col >= 0; col--) {
         const int bw = rows[cons[col]].n;
         T e6[kJMax] = {0, 0, 0, 0, 0};
-        for (int row = col + 1; row < n; row++) {
-            const int l = holo_loc(table, n, row, col);
-            if (l < 0) continue;
+        for (int q = ls[col]; q < ls[col + 1]; q++) {
+            const int row = hs.lrow[q], l = hs.lloc[q];
             const int bh = rows[cons[row]].n;
             for (int i = 0; i < bw; i++) {
                 T dp = 0;
@@ -135,7 +173,6 @@ __device__ void holo_solve(const HoloStore& hs, int s, const JointRow* rows, con
         }
         for (int i = 0; i < bw; i++) v[vp[col] + i] -= e6[i];
     }
-    (void)deg;
 }
 
 }  // namespace cpgpu

@@ -218,6 +218,10 @@ struct HoloStore {
     const int* degree;
     const int* tstart;      // [n + 1] into table
     const int* table;       // block_location_table (-1 empty)
+    const int* lbase;       // per system: first entry in lstart (n + 1 entries each)
+    const int* lstart;      // per column: its nonzero blocks below the diagonal in lrow / lloc
+    const int* lrow;        //   their rows (ascending)
+    const int* lloc;        //   their block offsets
     const int* bstart;      // offset into the FP32 or FP64 pool
     const int* cap;         // block storage (the diagonal scratch follows)
     const int* fp64;

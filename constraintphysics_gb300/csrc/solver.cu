@@ -598,7 +598,8 @@ __global__ void __launch_bounds__(32) k_pgs_joint(Dev d, int first) {
                 if (c >= 0) row_warm(d.rows[r], d.rows[r].imp, dv);
                 else jwarm(d.jt.rows[-c - 1], dv);
             }
-            for (int it = 0; it < P.pgs_vel; it++)
+            const int n_vel = P.pgs_vel, n_pos = P.pgs_pos;   // read once: the row stores could alias P
+            for (int it = 0; it < n_vel; it++)
                 for (int r = rs; r < rs + rc; r++) {
                     RowBlock& R = d.rows[r];
                     if (R.contact < 0) { jstep(d.jt.rows[-R.contact - 1], dv, false); continue; }
@@ -608,7 +609,7 @@ __global__ void __launch_bounds__(32) k_pgs_joint(Dev d, int first) {
                     R.imp = imp;
                     R.stat = st;
                 }
-            for (int it = 0; it < P.pgs_pos; it++)
+            for (int it = 0; it < n_pos; it++)
                 for (int r = rs; r < rs + rc; r++) {
                     RowBlock& R = d.rows[r];
                     if (R.contact < 0) { jstep(d.jt.rows[-R.contact - 1], dv, true); continue; }
