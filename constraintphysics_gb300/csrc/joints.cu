@@ -201,36 +201,44 @@ __device__ void initial_block(const Dev& d, int j1, int j2, T* t, float cfm) {
     }
 }
 
+// One warp per system: the column loop stays in order (each column needs the
+// previous columns' updates); within a column the diagonal block is inverted
+// by lane 0 and the entries of the L blocks and of the trailing updates are
+// spread over the lanes, each entry summed in the same order as a serial
+// loop would.
 template <class T>
-__device__ void factorise(const Dev& d, int s, T* B, float cfm) {
+__device__ void factorise(const Dev& d, int s, T* B, float cfm, int lane) {
     const HoloStore& hs = d.hs;
     const int c0 = hs.cstart[s], n = hs.cstart[s + 1] - c0;
     const int* cons = hs.cons + c0;
     const int* table = hs.table + hs.tstart[s];
     const int* ls = hs.lstart + hs.lbase[s];   // column col's blocks below the diagonal: [ls[col], ls[col + 1])
     T* Dg = B + hs.cap[s];
-    for (int col = 0; col < n; col++) {
+    for (int col = lane; col < n; col += 32) {
         initial_block<T>(d, cons[col], cons[col], B + holo_loc(table, n, col, col), cfm);
         for (int q = ls[col]; q < ls[col + 1]; q++) initial_block<T>(d, cons[hs.lrow[q]], cons[col], B + hs.lloc[q], cfm);
     }
+    __syncwarp();
     for (int col = 0; col < n; col++) {
         const int w = d.jt.rows[cons[col]].n;
         T* diag = B + holo_loc(table, n, col, col);
-        invert_block<T>(w, diag);
-        if (col + 1 == n) continue;
+        if (lane == 0) invert_block<T>(w, diag);
+        __syncwarp();
+        if (col + 1 == n) break;
         const int q0 = ls[col], q1 = ls[col + 1];
         const int fb = q0 < q1 ? hs.lloc[q0] : -1;
         for (int q = q0; q < q1; q++) {
             const int row = hs.lrow[q], l = hs.lloc[q];
             const int h = d.jt.rows[cons[row]].n;
             T* tgt = Dg + (l - fb);
-            for (int r = 0; r < h; r++)
-                for (int c = 0; c < w; c++) {
-                    T x = 0;
-                    for (int k = 0; k < w; k++) x += B[l + w * r + k] * diag[w * c + k];
-                    tgt[c + w * r] = x;
-                }
+            for (int e = lane; e < h * w; e += 32) {
+                const int r = e / w, c = e - r * w;
+                T x = 0;
+                for (int k = 0; k < w; k++) x += B[l + w * r + k] * diag[w * c + k];
+                tgt[c + w * r] = x;
+            }
         }
+        __syncwarp();
         for (int qa = q0; qa < q1; qa++) {
             const int lc = hs.lrow[qa], llc = hs.lloc[qa];
             const int bw = d.jt.rows[cons[lc]].n;
@@ -239,26 +247,30 @@ __device__ void factorise(const Dev& d, int s, T* B, float cfm) {
                 const int bh = d.jt.rows[cons[lr]].n;
                 T* tgt = B + holo_loc(table, n, lr, lc);
                 const T* lsrc = Dg + (llc - fb);
-                for (int r = 0; r < bh; r++)
-                    for (int c = 0; c < bw; c++) {
-                        T x = 0;
-                        for (int k = 0; k < w; k++) x += B[l + r * w + k] * lsrc[c * w + k];
-                        tgt[r * bw + c] -= x;
-                    }
+                for (int e = lane; e < bh * bw; e += 32) {
+                    const int r = e / bw, c = e - r * bw;
+                    T x = 0;
+                    for (int k = 0; k < w; k++) x += B[l + r * w + k] * lsrc[c * w + k];
+                    tgt[r * bw + c] -= x;
+                }
             }
         }
-        if (fb < 0) continue;
-        const int total = holo_loc(table, n, col + 1, col + 1) - fb;
-        for (int k = 0; k < total; k++) B[fb + k] = Dg[k];
+        __syncwarp();
+        if (fb >= 0) {
+            const int total = holo_loc(table, n, col + 1, col + 1) - fb;
+            for (int k = lane; k < total; k += 32) B[fb + k] = Dg[k];
+        }
+        __syncwarp();
     }
 }
 
-__global__ void k_holo_factor(Dev d) {
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < d.hs.n; s += gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(32) k_holo_factor(Dev d) {
+    const int lane = threadIdx.x;
+    for (int s = blockIdx.x; s < d.hs.n; s += gridDim.x) {
         const int j0 = d.hs.cons[d.hs.cstart[s]];
         const float cfm = d.wparams[d.world[d.jt.b1[j0]]].cfm;
-        if (d.hs.fp64[s]) factorise<double>(d, s, d.hs.pool64 + d.hs.bstart[s], cfm);
-        else factorise<float>(d, s, d.hs.pool32 + d.hs.bstart[s], cfm);
+        if (d.hs.fp64[s]) factorise<double>(d, s, d.hs.pool64 + d.hs.bstart[s], cfm, lane);
+        else factorise<float>(d, s, d.hs.pool32 + d.hs.bstart[s], cfm, lane);
     }
 }
 
@@ -270,11 +282,10 @@ void launch_joint_rows(const Dev& d, bool first, const Launch& L) {
     g = g > L.n_sms * 8 ? L.n_sms * 8 : g;
     k_joint_rows<<<g, 128, 0, L.st>>>(d);
     if (first && d.hs.n > 0) {
-        // a system per thread, few threads per block: the FP64 work spreads
-        // over every SM instead of packing into a handful
-        int gs = (d.hs.n + 7) / 8;
+        // a warp per system
+        int gs = d.hs.n;
         gs = gs > L.n_sms * 32 ? L.n_sms * 32 : gs;
-        k_holo_factor<<<gs, 8, 0, L.st>>>(d);
+        k_holo_factor<<<gs, 32, 0, L.st>>>(d);
     }
 }
 
