@@ -422,27 +422,33 @@ __device__ __forceinline__ bool ring_wait(uint64_t* bar, uint32_t parity) {
 
 // The serial Gauss-Seidel chain of one island on one thread: 1 warm-start pass,
 // pgs_vel velocity passes and pgs_pos position passes over the island's rows,
-// in order.  Rows stream through the shared ring (look-ahead up to one pass,
+// in order.  The first position pass is fused into the warm-start pass: the
+// position rows read and write only the pseudo velocities and the pseudo
+// impulse, which no other pass touches and which start at zero, so running
+// position row j right after warm-start row j gives the same result as a
+// separate pass, one pass sooner (the two rows' arithmetic interleaves).  Rows stream through the shared ring (look-ahead up to one pass,
 // since a pass must see the impulses the previous pass wrote back); each row
 // is copied to registers with 16-byte loads before it is used.
 __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t* bars, uint32_t& phase, float4* dv, int rs,
                                        int rc, const WorldParams& P) {
     const int nch = (rc + kChunkRows - 1) / kChunkRows;
     const int n_vel = P.pgs_vel;   // read once: the row stores below could alias P for the compiler
-    const int passes = 1 + n_vel + P.pgs_pos;
+    const int n_pos = P.pgs_pos;
+    const bool fused = n_pos > 0;
+    const int passes = 1 + n_vel + (fused ? n_pos - 1 : 0);
     const int total = passes * nch;
     const int ahead = nch < kRingSlots ? nch : kRingSlots;
     // A proxy fence covers every impulse write issued before it.  Chunk c of
-    // sequence t was last written at sequence t - nch (by a velocity or
-    // position pass, i.e. t - nch >= nch); a fence is needed only if none was
-    // issued since: about once per pass on a large island, every chunk on a
-    // small one.
+    // sequence t was last written at sequence t - nch (every pass writes when
+    // the position rows are fused into the warm-start pass, the others from
+    // the first velocity pass on); a fence is needed only if none was issued
+    // since: about once per pass on a large island, every chunk on a small one.
     int fenced = -1;
     auto issue = [&](int t, int now) {
         int c = t % nch, slot = t % kRingSlots;
         int n = min(kChunkRows, rc - c * kChunkRows);
         const int tw = t - nch;
-        const bool fence = tw >= nch && tw > fenced;
+        const bool fence = tw >= (fused ? 0 : nch) && tw > fenced;
         if (fence) fenced = now;
         ring_load(ring + slot * kChunkRows, d.rows + rs + c * kChunkRows, n, &bars[slot], fence);
     };
@@ -462,6 +468,10 @@ __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t
             float4 imp = R.imp;
             if (pass == 0) {
                 row_warm(R, imp, dv);
+                if (fused) {
+                    row_pos(R, imp, dv);
+                    g[j].imp = imp;
+                }
             } else if (pass <= n_vel) {
                 int st = R.stat;
                 row_vel(R, imp, st, dv);
