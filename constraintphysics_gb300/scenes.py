@@ -116,6 +116,11 @@ class Scene:
     def velocity(self, bid, v):
         self.ops.append(("vel", bid, tuple(v)))
 
+    def movements(self):
+        """Movement type of each body, in id order."""
+        slot = {"hull": 4, "box": 6, "sphere": 4, "cylinder": 5}
+        return [FIXED if op[0] == "mesh" else op[slot[op[0]]] for op in self.ops if op[0] in slot or op[0] == "mesh"]
+
 
 def apply(scene, world):
     """Replay `scene` on a World; returns the list of created body ids."""
