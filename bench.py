@@ -291,7 +291,7 @@ def measure_drift(cg, ws_scenes, n_worlds=8, steps=300):
     body the distance between the two centres of mass."""
     import oracle
     idx = list(range(0, len(ws_scenes), max(1, len(ws_scenes) // n_worlds)))[:n_worlds]
-    d = []
+    d, c = [], []
     for i in idx:
         g = cg.world()
         scenes.apply(ws_scenes[i], g)
@@ -299,16 +299,25 @@ def measure_drift(cg, ws_scenes, n_worlds=8, steps=300):
         r = oracle.ref_world()
         scenes.apply(ws_scenes[i], r)
         r.step(steps)
+        # control: the FP64 restatement, whose mass properties differ from the
+        # reference's by ~1e-12 relative, against the reference
+        p = oracle.port_world()
+        scenes.apply(ws_scenes[i], p)
+        p.step(steps)
         dyn = np.array([m == scenes.DYNAMIC for m in ws_scenes[i].movements()])
-        diff = np.linalg.norm(g.state()["com"] - r.state()["com"], axis=1)[dyn]
-        d.append(diff)
-        g.close() if hasattr(g, "close") else None
-    d = np.concatenate(d) if d else np.zeros(0)
-    return {"worlds": len(idx), "steps": steps, "bodies": int(d.size), "median_m": float(np.median(d)),
-            "p95_m": float(np.percentile(d, 95)), "max_m": float(d.max()),
-            "frac_within_1e-3_m": float(np.mean(d <= 1e-3)),
-            "note": "device FP32 vs the reference engine FP64 from the same scene; piles are chaotic "
-                    "(the reference itself diverges for 5e-14 mass-property changes), resting pyramids are not"}
+        rc = r.state()["com"]
+        d.append(np.linalg.norm(g.state()["com"] - rc, axis=1)[dyn])
+        c.append(np.linalg.norm(p.state()["com"] - rc, axis=1)[dyn])
+
+    def stats(x):
+        x = np.concatenate(x) if x else np.zeros(1)
+        return {"median_m": float(np.median(x)), "p95_m": float(np.percentile(x, 95)), "max_m": float(x.max()),
+                "frac_within_1e-3_m": float(np.mean(x <= 1e-3))}
+    return dict(stats(d), worlds=len(idx), steps=steps, bodies=int(sum(x.size for x in d)),
+                fp64_control=stats(c),
+                note="device FP32 vs the reference engine FP64 from the same scene; fp64_control: the FP64 "
+                     "restatement (mass properties within 1e-12 of the reference's) vs the reference, the "
+                     "drift these scenes show for rounding-level differences alone")
 
 
 def main():
