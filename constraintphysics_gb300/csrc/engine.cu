@@ -8,6 +8,7 @@
 // back, change the host mirror and re-upload on the next step.  A batch packs
 // many worlds into one set of segmented device arrays.
 #include <algorithm>
+#include <thread>
 #include <array>
 #include <cmath>
 #include <chrono>
@@ -2197,94 +2198,182 @@ struct ServerRequest {
     bool finished = false;   // result captured; still in the batch until the next re-form
 };
 
+// One lane of the server: the requests of one world-size class, stepped as a
+// batch on the lane's own stream.
+struct ServerLane {
+    std::deque<ServerRequest> waiting;
+    std::vector<ServerRequest> running;   // in batch order
+    std::unique_ptr<Batch> batch;
+    int since_reform = 0;
+    int inflight = 0;                     // steps launched and not yet accounted
+    cudaEvent_t ev = nullptr;             // recorded after the in-flight steps
+    ~ServerLane() { if (ev) cudaEventDestroy(ev); }
+};
+
+// Requests are worlds with a step count.  They are sorted by size into lanes
+// (fewer than 128 dynamic bodies, fewer than 512, the rest): a step of a batch
+// lasts as long as its largest island's serial solve, so a small world batched
+// with large ones would advance at the large ones' pace.  Each lane steps on
+// its own stream in chunks: advance() launches the next chunk on every idle
+// lane and returns once one lane's chunk has completed, so small requests take
+// more steps per second than large ones.  Admission is in arrival order per
+// lane under one device-memory budget for all lanes.
 struct Server {
     int64_t budget = 0;
     int epoch_steps = 10;
     double bytes_per_body = 2048;     // updated from every batch built
-    std::deque<ServerRequest> waiting;
-    std::vector<ServerRequest> running;   // in batch order
-    std::unique_ptr<Batch> batch;
+    std::vector<std::unique_ptr<ServerLane>> lanes;
+    std::vector<int64_t> bounds{128, 512};
     std::vector<uint64_t> done;
-    int since_reform = 0;
     uint64_t next_token = 1;
     int64_t body_steps = 0, reforms = 0;
     double reform_ms = 0;
 
+    Server() {
+        for (size_t k = 0; k <= bounds.size(); k++) lanes.push_back(std::make_unique<ServerLane>());
+    }
+
+    int lane_of(int64_t bodies) const {
+        int k = 0;
+        while (k < (int)bounds.size() && bodies >= bounds[k]) k++;
+        return k;
+    }
     size_t estimate(const World& w) const { return (size_t)(bytes_per_body * (double)w.bodies.size()) + (1u << 20); }
+    size_t used_bytes() const {
+        size_t u = 0;
+        for (auto& L : lanes)
+            for (auto& r : L->running) u += r.bytes;
+        return u;
+    }
+    int64_t running_count() const {
+        int64_t n = 0;
+        for (auto& L : lanes) n += (int64_t)L->running.size();
+        return n;
+    }
+    int64_t waiting_count() const {
+        int64_t n = 0;
+        for (auto& L : lanes) n += (int64_t)L->waiting.size();
+        return n;
+    }
+
+    void submit(const ServerRequest& r) { lanes[lane_of(r.bodies)]->waiting.push_back(r); }
 
     // capture the exact state of requests that reached their step count,
     // without stopping the batch (they keep stepping as dead weight until the
     // next re-form)
-    void capture_finished() {
+    void capture_finished(ServerLane& L) {
         std::vector<int> idx;
         std::vector<World*> ws;
-        for (size_t i = 0; i < running.size(); i++)
-            if (!running[i].finished && running[i].remaining <= 0) { idx.push_back((int)i); ws.push_back(running[i].w); }
+        for (size_t i = 0; i < L.running.size(); i++)
+            if (!L.running[i].finished && L.running[i].remaining <= 0) { idx.push_back((int)i); ws.push_back(L.running[i].w); }
         if (idx.empty()) return;
-        download_subset(*batch, idx, ws);
-        for (int i : idx) { running[i].finished = true; done.push_back(running[i].token); }
+        download_subset(*L.batch, idx, ws);
+        for (int i : idx) { L.running[i].finished = true; done.push_back(L.running[i].token); }
     }
 
-    void reform() {
+    void reform(ServerLane& L) {
         auto t0 = std::chrono::steady_clock::now();
         std::vector<ServerRequest> keep;
         std::vector<int> idx;
         std::vector<World*> ws;
-        for (size_t i = 0; i < running.size(); i++)
-            if (!running[i].finished) { keep.push_back(running[i]); idx.push_back((int)i); ws.push_back(running[i].w); }
-        if (batch) download_subset(*batch, idx, ws);
-        batch.reset();
-        running.swap(keep);
-        size_t used = 0;
-        for (auto& r : running) used += r.bytes;
-        while (!waiting.empty()) {
-            ServerRequest& r = waiting.front();
+        for (size_t i = 0; i < L.running.size(); i++)
+            if (!L.running[i].finished) { keep.push_back(L.running[i]); idx.push_back((int)i); ws.push_back(L.running[i].w); }
+        if (L.batch) download_subset(*L.batch, idx, ws);
+        L.batch.reset();
+        L.running.swap(keep);
+        size_t used = used_bytes();
+        while (!L.waiting.empty()) {
+            ServerRequest& r = L.waiting.front();
             r.bytes = estimate(*r.w);
-            if (!running.empty() && used + r.bytes > (size_t)budget) break;
+            if (running_count() > 0 && used + r.bytes > (size_t)budget) break;
             used += r.bytes;
-            running.push_back(r);
-            waiting.pop_front();
+            L.running.push_back(r);
+            L.waiting.pop_front();
         }
-        if (!running.empty()) {
-            std::vector<World*> ws;
-            for (auto& r : running) ws.push_back(r.w);
-            batch = build_batch(ws);
+        if (!L.running.empty()) {
+            std::vector<World*> ws2;
+            for (auto& r : L.running) ws2.push_back(r.w);
+            L.batch = build_batch(ws2);
             int64_t nb = 0;
-            for (auto& r : running) nb += r.bodies;
-            if (nb > 0) bytes_per_body = (double)batch->bytes / (double)nb;
-            for (auto& r : running) r.bytes = estimate(*r.w);
+            for (auto& r : L.running) nb += r.bodies;
+            if (nb > 0) bytes_per_body = (double)L.batch->bytes / (double)nb;
+            for (auto& r : L.running) r.bytes = estimate(*r.w);
+            if (!L.ev) CK(cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming));
         }
-        since_reform = 0;
+        L.since_reform = 0;
         reforms++;
         reform_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
 
-    // Re-form when requests wait and an epoch has passed since the last
-    // re-form, or when finished requests hold a quarter of the batch's bodies.
-    int advance(int max_steps) {
-        int stepped = 0;
-        while (stepped < max_steps) {
-            int64_t live = 0, dead = 0;
-            for (auto& r : running) (r.finished ? dead : live) += r.bodies;
-            const bool want = !waiting.empty() && (live == 0 || since_reform >= epoch_steps);
-            const bool reclaim = dead > 0 && (live == 0 || 4 * dead >= live + dead);
-            if (want || reclaim) reform();
-            if (!batch) break;
-            int n = max_steps - stepped;
-            for (auto& r : running) if (!r.finished) n = std::min(n, r.remaining);
-            if (!waiting.empty()) n = std::min(n, std::max(1, epoch_steps - since_reform));
-            batch->step(n);
-            batch->check_status();
-            for (auto& r : running) {
-                if (r.finished) continue;
-                r.remaining -= n;
-                body_steps += (int64_t)n * r.bodies;
-            }
-            stepped += n;
-            since_reform += n;
-            capture_finished();
+    // account for a lane's completed chunk
+    void complete(ServerLane& L) {
+        if (L.inflight == 0) return;
+        L.batch->check_status();
+        for (auto& r : L.running) {
+            if (r.finished) continue;
+            r.remaining -= L.inflight;
+            body_steps += (int64_t)L.inflight * r.bodies;
         }
-        return stepped;
+        L.since_reform += L.inflight;
+        L.inflight = 0;
+        capture_finished(L);
+    }
+
+    // Launch a lane's next chunk (no wait).  Re-form when requests wait and an
+    // epoch has passed since the last re-form, or when finished requests hold
+    // a quarter of the lane's bodies.  A chunk never passes a running
+    // request's remaining count or the end of the epoch.
+    bool launch(ServerLane& L, int max_steps) {
+        int64_t live = 0, dead = 0;
+        for (auto& r : L.running) (r.finished ? dead : live) += r.bodies;
+        const bool want = !L.waiting.empty() && (live == 0 || L.since_reform >= epoch_steps);
+        const bool reclaim = dead > 0 && (live == 0 || 4 * dead >= live + dead);
+        if (want || reclaim) reform(L);
+        if (!L.batch) return false;
+        live = 0;
+        for (auto& r : L.running) if (!r.finished) live += r.bodies;
+        if (live == 0) return false;
+        int n = max_steps;
+        for (auto& r : L.running) if (!r.finished) n = std::min(n, r.remaining);
+        if (!L.waiting.empty()) n = std::min(n, std::max(1, epoch_steps - L.since_reform));
+        if (n <= 0) { capture_finished(L); return false; }
+        L.batch->step(n);
+        CK(cudaEventRecord(L.ev, L.batch->st));
+        L.inflight = n;
+        return true;
+    }
+
+    // Launch on every idle lane, then wait (bounded) until one lane's chunk
+    // completes and account for it.  Returns the steps that lane completed.
+    int advance(int max_steps) {
+        for (auto& L : lanes)
+            if (L->inflight == 0) launch(*L, max_steps);
+        const auto t0 = std::chrono::steady_clock::now();
+        while (true) {
+            int stepped = 0;
+            bool any = false;
+            for (auto& L : lanes) {
+                if (L->inflight == 0) continue;
+                any = true;
+                const cudaError_t q = cudaEventQuery(L->ev);
+                if (q == cudaSuccess) {
+                    stepped = std::max(stepped, L->inflight);
+                    complete(*L);
+                } else if (q != cudaErrorNotReady) {
+                    CK(q);
+                }
+            }
+            if (!any || stepped > 0) return stepped;
+            if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(600))
+                throw ApiFail{CPGPU_ERR_TIMEOUT, "server chunk did not complete within 600 s"};
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+    }
+
+    // wait for every lane's chunk in flight
+    void drain() {
+        for (auto& L : lanes)
+            if (L->inflight) { CK(cudaEventSynchronize(L->ev)); complete(*L); }
     }
 };
 
@@ -2306,7 +2395,13 @@ int cpgpu_server_create(int64_t hbm_budget_bytes, int epoch_steps, cpgpu_server*
         return CPGPU_OK;
     });
 }
-int cpgpu_server_destroy(cpgpu_server* s) { delete s; return CPGPU_OK; }
+int cpgpu_server_destroy(cpgpu_server* s) {
+    if (s) {
+        try { s->s.drain(); } catch (...) {}
+    }
+    delete s;
+    return CPGPU_OK;
+}
 
 int cpgpu_server_submit(cpgpu_server* s, cpgpu_world* w, int steps, uint64_t* token) {
     if (!s || !w) return fail(CPGPU_ERR_INVALID_ARG, "null server or world");
@@ -2321,7 +2416,7 @@ int cpgpu_server_submit(cpgpu_server* s, cpgpu_world* w, int steps, uint64_t* to
         r.token = s->s.next_token++;
         r.bodies = 0;
         for (const auto& b : w->w.bodies) r.bodies += b.movement == CPGPU_DYNAMIC;
-        s->s.waiting.push_back(r);
+        s->s.submit(r);
         if (token) *token = r.token;
         return CPGPU_OK;
     });
@@ -2331,8 +2426,8 @@ int cpgpu_server_advance(cpgpu_server* s, int max_steps, int* n_running, int* n_
     if (!s) return fail(CPGPU_ERR_INVALID_ARG, "null server");
     return guarded([&] {
         s->s.advance(max_steps);
-        if (n_running) *n_running = (int)s->s.running.size();
-        if (n_waiting) *n_waiting = (int)s->s.waiting.size();
+        if (n_running) *n_running = (int)s->s.running_count();
+        if (n_waiting) *n_waiting = (int)s->s.waiting_count();
         return CPGPU_OK;
     });
 }
@@ -2353,12 +2448,13 @@ int cpgpu_server_stats(cpgpu_server* s, int64_t* body_steps, int64_t* reforms, d
     if (body_steps) *body_steps = s->s.body_steps;
     if (reforms) *reforms = s->s.reforms;
     if (reform_ms) *reform_ms = s->s.reform_ms;
-    if (device_bytes) *device_bytes = s->s.batch ? (int64_t)s->s.batch->bytes : 0;
-    if (running_bodies) {
-        int64_t nb = 0;
-        for (auto& r : s->s.running) nb += r.bodies;
-        *running_bodies = nb;
+    int64_t bytes = 0, nb = 0;
+    for (auto& L : s->s.lanes) {
+        if (L->batch) bytes += (int64_t)L->batch->bytes;
+        for (auto& r : L->running) nb += r.bodies;
     }
+    if (device_bytes) *device_bytes = bytes;
+    if (running_bodies) *running_bodies = nb;
     return CPGPU_OK;
 }
 

@@ -97,3 +97,42 @@ def test_budget_admission_queues_requests():
         s = r.state()
         for k in KEYS:
             assert np.array_equal(s[k], a[k]), (i, k)
+
+
+def test_size_lanes_exact_and_small_first():
+    """Requests of three world sizes (one per server lane: < 128, < 512 and
+    >= 512 dynamic bodies) submitted together with the same step count: each
+    result equals its stand-alone run bit for bit, and the small request is
+    done no later than the large one (its lane steps at its own pace)."""
+    rng = np.random.default_rng(31)
+    pool = scenes.HullPool(5, size=8)
+    sizes = [(30, 60), (200, 300), (560, 700)]
+    temps = []
+    for lo, hi in sizes:
+        sc = None
+        while sc is None or not sc.name.startswith("pyramid"):
+            sc = scenes.batched_world(rng, pool, lo, hi)
+        w = cg.world()
+        scenes.apply(sc, w)
+        temps.append(w)
+    k = 40
+    alone = []
+    for t in temps:
+        w = cg.clone(t)
+        w.step(k)
+        alone.append(w.state())
+    srv = cg.Server(budget_bytes=8 << 30, epoch_steps=4)
+    reqs = [cg.clone(t) for t in temps]
+    toks = [srv.submit(r, k) for r in reqs]
+    order = []
+    for _ in range(1000):
+        running, waiting = srv.advance(5)
+        order += srv.poll()
+        if running == 0 and waiting == 0:
+            break
+    assert sorted(order) == sorted(toks)
+    assert order.index(toks[0]) <= order.index(toks[2])
+    for i, (r, a) in enumerate(zip(reqs, alone)):
+        s = r.state()
+        for key in KEYS:
+            assert np.array_equal(s[key], a[key]), (i, key)
