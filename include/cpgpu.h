@@ -252,12 +252,14 @@ int cpgpu_pairs_noalloc(const float* aabbs, int n_bodies, uint32_t* pairs, int c
 int cpgpu_world_clone(cpgpu_world* src, cpgpu_world** out);
 
 /* Continuous-batching rollout server (no counterpart in the reference).  A
- * request is a world plus a number of steps.  Requests wait in arrival order
- * until their estimated device memory fits the budget next to the running
- * ones; the running requests are stepped together as one batch (one launch
- * sequence per step), their state resident on the device between admission
- * points.  The batch is re-formed when a request completes, or when requests
- * are waiting and `epoch_steps` steps have passed since the last re-form; a
+ * request is a world plus a number of steps.  Requests are sorted by size
+ * into lanes (fewer than 128 dynamic bodies, fewer than 512, the rest); in
+ * each lane they wait in arrival order until their estimated device memory
+ * fits the one budget next to all running requests, and a lane's running
+ * requests are stepped together as one batch on the lane's own stream, their
+ * state resident on the device between admission points.  A lane's batch is
+ * re-formed when its finished requests hold a quarter of its bodies, or when
+ * requests wait and `epoch_steps` steps have passed since its last re-form; a
  * completed request's final state is written back into its world, which the
  * caller then reads as usual.  Each request's result equals stepping its
  * world alone.  The caller must not touch a submitted world until its token
@@ -266,12 +268,14 @@ typedef struct cpgpu_server cpgpu_server;
 int cpgpu_server_create(int64_t hbm_budget_bytes, int epoch_steps, cpgpu_server** out);
 int cpgpu_server_destroy(cpgpu_server* s);
 int cpgpu_server_submit(cpgpu_server* s, cpgpu_world* w, int steps, uint64_t* token);
-/* Run up to max_steps batch steps (fewer when nothing is running). */
+/* Launch up to max_steps steps on every idle lane (never past a running
+ * request's remaining count) and return once one lane's launched steps have
+ * completed, or at once when nothing runs; lanes progress at their own pace. */
 int cpgpu_server_advance(cpgpu_server* s, int max_steps, int* n_running, int* n_waiting);
 /* Tokens of requests completed since the last poll. */
 int cpgpu_server_poll(cpgpu_server* s, uint64_t* tokens, int cap, int* n);
 /* Totals: body-steps advanced, batch re-forms and their host time (ms),
- * device bytes of the current batch, bodies running. */
+ * device bytes of the lanes' current batches, bodies running. */
 int cpgpu_server_stats(cpgpu_server* s, int64_t* body_steps, int64_t* reforms, double* reform_ms,
                        int64_t* device_bytes, int64_t* running_bodies);
 
