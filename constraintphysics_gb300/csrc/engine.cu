@@ -1943,12 +1943,6 @@ static std::vector<std::vector<int>> batch_partition(const std::vector<World*>& 
     int64_t total = 0;
     for (World* w : ws) total += (int64_t)w->bodies.size();
     std::vector<std::vector<int>> parts(P);
-    if (env_int("CPGPU_BATCH_MIX", 0)) {
-        // every part the same mix of sizes: worlds dealt round-robin by size
-        for (int k = 0; k < n; k++) parts[k % P].push_back(order[k]);
-        for (auto& q : parts) std::sort(q.begin(), q.end());
-        return parts;
-    }
     int64_t acc = 0;
     int p = 0;
     for (int k = 0; k < n; k++) {
