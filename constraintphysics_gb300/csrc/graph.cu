@@ -186,7 +186,20 @@ __global__ void k_contacts(Dev d, int write) {
 }
 
 // ---- islands: one block per world ---------------------------------------------------
-__global__ void __launch_bounds__(256) k_islands(Dev d) {
+// The world's graph (body flags, adjacency, DFS stack, live-contact counts) is
+// built in dynamic shared memory when it fits the launch's budget: the serial
+// DFS below is a chain of dependent loads, about 30 cycles each from shared
+// memory instead of several hundred from L2.  A world that does not fit runs
+// the same code over its slices of the global scratch arrays.  All indices
+// here are world-local: body i - s, contact edge k - e0 (joint edges keep
+// their global index, stored as -(k + 1)).
+__device__ __forceinline__ long long islands_need(int nb, int ne_w, int nj) {
+    const long long E = (long long)ne_w + nj;
+    return 4LL * (4LL * nb + 4 * E + ne_w + 2 * E + nb) + nb;   // ints, then the body flags (bytes)
+}
+
+__global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
+    extern __shared__ int sm_isl[];
     __shared__ int sh_carry, sh_rows_end;
     __shared__ int warp_sums[8];
     const int w = blockIdx.x;
@@ -202,39 +215,60 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
     const int je0 = joints ? d.je.world_start[w] : 0, je1 = joints ? d.je.world_start[w + 1] : 0;
     const int jj0 = joints ? d.je.world_jstart[w] : 0;
     const int sys0 = joints ? d.hs_world_start[w] : 0;
+    const int nb = e - s, ne_w = e1 - e0, nj = je1 - je0, E = ne_w + nj;
+    const int stack_cap = 2 * E + nb;
+    const bool fast = islands_need(nb, ne_w, nj) <= smem_bytes;
+    int *vis, *a_ofs, *a_cur, *adj, *live, *stk;
+    const uint8_t* mov;
+    uint8_t* mov_s = nullptr;
+    if (fast) {
+        vis = sm_isl; a_ofs = vis + nb; a_cur = a_ofs + nb; adj = a_cur + nb;
+        live = adj + 4 * E; stk = live + ne_w;
+        mov_s = reinterpret_cast<uint8_t*>(stk + stack_cap);
+        mov = mov_s;
+    } else {
+        vis = d.visited + s; a_ofs = d.adj_ofs + s; a_cur = d.adj_cursor + s;
+        adj = d.adj_list + 4 * (size_t)(e0 + je0);   // entries from 2 (e0 + je0), two ints each
+        live = d.edge_live + e0;
+        stk = d.stack + 2 * (e0 + je0) + s;
+        mov = d.movement + s;
+    }
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (int i = s + tid; i < e; i += nt) { d.adj_cursor[i] = 0; d.visited[i] = -1; }
+    for (int i = tid; i < nb; i += nt) {
+        a_cur[i] = 0;
+        vis[i] = -1;
+        if (fast) mov_s[i] = d.movement[s + i];
+    }
     for (int c = c0 + tid; c < c1; c += nt) d.row_of_contact[c] = -1;
     // live contacts per edge, so that the serial DFS below advances its row
     // cursor by one load per edge instead of one per contact
-    for (int k = e0 + tid; k < e1; k += nt) {
-        const int cs = d.e_new.cstart[k], cn = d.e_new.ccount[k];
-        int live = 0;
-        for (int c = cs; c < cs + cn; c++) live += cs_live(d.c_new.state[c]);
-        d.edge_live[k] = live;
-        d.edge_row[k] = -1;
+    for (int k = tid; k < ne_w; k += nt) {
+        const int cs = d.e_new.cstart[e0 + k], cn = d.e_new.ccount[e0 + k];
+        int l = 0;
+        for (int c = cs; c < cs + cn; c++) l += cs_live(d.c_new.state[c]);
+        live[k] = l;
+        d.edge_row[e0 + k] = -1;
     }
     __syncthreads();
-    for (int k = e0 + tid; k < e1; k += nt) {
-        uint64_t key = d.e_new.key[k];
-        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
-        if (d.movement[a] == 0) atomicAdd(&d.adj_cursor[a], 1);
-        if (d.movement[b] == 0) atomicAdd(&d.adj_cursor[b], 1);
+    for (int k = tid; k < ne_w; k += nt) {
+        const uint64_t key = d.e_new.key[e0 + k];
+        const int a = (int)(key >> 32) - s, b = (int)(key & 0xffffffffu) - s;
+        if (mov[a] == 0) atomicAdd(&a_cur[a], 1);
+        if (mov[b] == 0) atomicAdd(&a_cur[b], 1);
     }
-    for (int k = je0 + tid; k < je1; k += nt) {
-        uint64_t key = d.je.key[k];
-        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
-        if (d.movement[a] == 0) atomicAdd(&d.adj_cursor[a], 1);
-        if (d.movement[b] == 0) atomicAdd(&d.adj_cursor[b], 1);
+    for (int k = tid; k < nj; k += nt) {
+        const uint64_t key = d.je.key[je0 + k];
+        const int a = (int)(key >> 32) - s, b = (int)(key & 0xffffffffu) - s;
+        if (mov[a] == 0) atomicAdd(&a_cur[a], 1);
+        if (mov[b] == 0) atomicAdd(&a_cur[b], 1);
     }
     __syncthreads();
-    // exclusive scan of the degrees into adjacency offsets (region starts at
-    // 2 * (e0 + je0): two entries per contact or joint edge before this world)
-    if (tid == 0) sh_carry = 2 * (e0 + je0);
+    // exclusive scan of the degrees into adjacency offsets
+    if (tid == 0) sh_carry = 0;
     __syncthreads();
-    for (int base = s; base < e; base += nt) {
-        int i = base + tid;
-        int v = (i < e) ? d.adj_cursor[i] : 0;
+    for (int base = 0; base < nb; base += nt) {
+        const int i = base + tid;
+        const int v = (i < nb) ? a_cur[i] : 0;
         int x = v;
         const int lane = tid & 31, wid = tid >> 5;
         for (int o = 1; o < 32; o <<= 1) { int t = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += t; }
@@ -246,61 +280,60 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
             if (lane < 8) warp_sums[lane] = y;
         }
         __syncthreads();
-        int incl = x + (wid > 0 ? warp_sums[wid - 1] : 0);
-        int carry = sh_carry;
-        if (i < e) { d.adj_ofs[i] = carry + incl - v; d.adj_cursor[i] = carry + incl - v; }
+        const int incl = x + (wid > 0 ? warp_sums[wid - 1] : 0);
+        const int carry = sh_carry;
+        if (i < nb) { a_ofs[i] = carry + incl - v; a_cur[i] = carry + incl - v; }
         __syncthreads();
         if (tid == nt - 1) sh_carry = carry + incl;
         __syncthreads();
     }
-    for (int k = e0 + tid; k < e1; k += nt) {
-        uint64_t key = d.e_new.key[k];
-        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
-        if (d.movement[a] == 0) { int slot = atomicAdd(&d.adj_cursor[a], 1); d.adj_list[2 * slot] = b; d.adj_list[2 * slot + 1] = k; }
-        if (d.movement[b] == 0) { int slot = atomicAdd(&d.adj_cursor[b], 1); d.adj_list[2 * slot] = a; d.adj_list[2 * slot + 1] = k; }
+    for (int k = tid; k < ne_w; k += nt) {
+        const uint64_t key = d.e_new.key[e0 + k];
+        const int a = (int)(key >> 32) - s, b = (int)(key & 0xffffffffu) - s;
+        if (mov[a] == 0) { int slot = atomicAdd(&a_cur[a], 1); adj[2 * slot] = b; adj[2 * slot + 1] = k; }
+        if (mov[b] == 0) { int slot = atomicAdd(&a_cur[b], 1); adj[2 * slot] = a; adj[2 * slot + 1] = k; }
     }
     __syncthreads();
     // joint edges after the contact edges, marked -(index + 1); the sort below
     // is stable, so a pair holding both kinds lists its contacts first
-    for (int k = je0 + tid; k < je1; k += nt) {
-        uint64_t key = d.je.key[k];
-        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
-        if (d.movement[a] == 0) { int slot = atomicAdd(&d.adj_cursor[a], 1); d.adj_list[2 * slot] = b; d.adj_list[2 * slot + 1] = -(k + 1); }
-        if (d.movement[b] == 0) { int slot = atomicAdd(&d.adj_cursor[b], 1); d.adj_list[2 * slot] = a; d.adj_list[2 * slot + 1] = -(k + 1); }
+    for (int k = tid; k < nj; k += nt) {
+        const uint64_t key = d.je.key[je0 + k];
+        const int a = (int)(key >> 32) - s, b = (int)(key & 0xffffffffu) - s;
+        if (mov[a] == 0) { int slot = atomicAdd(&a_cur[a], 1); adj[2 * slot] = b; adj[2 * slot + 1] = -(je0 + k + 1); }
+        if (mov[b] == 0) { int slot = atomicAdd(&a_cur[b], 1); adj[2 * slot] = a; adj[2 * slot + 1] = -(je0 + k + 1); }
     }
     __syncthreads();
     // each dynamic node's edges sorted by the other body's id (insertion sort)
-    for (int i = s + tid; i < e; i += nt) {
-        if (d.movement[i] != 0) continue;
-        int lo = d.adj_ofs[i], hi = d.adj_cursor[i];
+    for (int i = tid; i < nb; i += nt) {
+        if (mov[i] != 0) continue;
+        const int lo = a_ofs[i], hi = a_cur[i];
         for (int x = lo + 1; x < hi; x++) {
-            int ko = d.adj_list[2 * x], kk = d.adj_list[2 * x + 1];
+            const int ko = adj[2 * x], kk = adj[2 * x + 1];
             int y = x - 1;
-            while (y >= lo && d.adj_list[2 * y] > ko) { d.adj_list[2 * (y + 1)] = d.adj_list[2 * y]; d.adj_list[2 * (y + 1) + 1] = d.adj_list[2 * y + 1]; y--; }
-            d.adj_list[2 * (y + 1)] = ko;
-            d.adj_list[2 * (y + 1) + 1] = kk;
+            while (y >= lo && adj[2 * y] > ko) { adj[2 * (y + 1)] = adj[2 * y]; adj[2 * (y + 1) + 1] = adj[2 * y + 1]; y--; }
+            adj[2 * (y + 1)] = ko;
+            adj[2 * (y + 1) + 1] = kk;
         }
     }
     __syncthreads();
     if (tid == 0) {
-        int* stack = d.stack + 2 * (e0 + je0) + s;
-        const int stack_cap = 2 * (e1 - e0 + je1 - je0) + (e - s);
         int rc = c0 + jj0, bc = s, ni = 0, sc = sys0;
         for (int t = s; t < e; t++) {
-            int node = d.map_order[t];
-            if (d.movement[node] != 0 || d.visited[node] >= 0) continue;
-            int rs = rc, bs = bc, sp = 0, ss = sc;
+            const int node = d.map_order[t] - s;
+            if (mov[node] != 0 || vis[node] >= 0) continue;
+            const int rs = rc, bs = bc, ss = sc;
+            int sp = 0;
             bool has_joint = false;
-            stack[sp++] = node;
+            stk[sp++] = node;
             while (sp > 0) {
-                int cur = stack[--sp];
-                if (d.visited[cur] >= 0) continue;
-                d.visited[cur] = bc - bs;
-                d.isl_bodies[bc++] = cur;
-                int lo = d.adj_ofs[cur], hi = d.adj_cursor[cur];
+                const int cur = stk[--sp];
+                if (vis[cur] >= 0) continue;
+                vis[cur] = bc - bs;
+                d.isl_bodies[bc++] = cur + s;
+                const int lo = a_ofs[cur], hi = a_cur[cur];
                 for (int j = lo; j < hi; j++) {
-                    int o = d.adj_list[2 * j], k = d.adj_list[2 * j + 1];
-                    if (d.visited[o] >= 0) continue;
+                    const int o = adj[2 * j], k = adj[2 * j + 1];
+                    if (vis[o] >= 0) continue;
                     if (k < 0) {
                         // joint edge: its holonomic system joins the island's
                         // list at first sight, then its joints' rows
@@ -315,13 +348,13 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
                         continue;
                     }
                     // the edge's live contacts take the next rows (written below)
-                    const int nl = d.edge_live[k];
-                    if (nl > 0) { d.edge_row[k] = rc; rc += nl; }
+                    const int nl = live[k];
+                    if (nl > 0) { d.edge_row[e0 + k] = rc; rc += nl; }
                 }
                 for (int j = lo; j < hi; j++) {
-                    int o = d.adj_list[2 * j];
-                    if (d.movement[o] == 0 && d.visited[o] < 0) {
-                        if (sp < stack_cap) stack[sp++] = o;
+                    const int o = adj[2 * j];
+                    if (mov[o] == 0 && vis[o] < 0) {
+                        if (sp < stack_cap) stk[sp++] = o;
                         else atomicOr(d.status, ST_STACK_OVERFLOW);
                     }
                 }
@@ -347,6 +380,8 @@ __global__ void __launch_bounds__(256) k_islands(Dev d) {
         sh_rows_end = rc;
     }
     __syncthreads();
+    if (fast)
+        for (int i = tid; i < nb; i += nt) d.visited[s + i] = vis[i];
     // each emitted edge's live contacts into its rows, in contact order
     for (int k = e0 + tid; k < e1; k += nt) {
         int r = d.edge_row[k];
@@ -438,8 +473,16 @@ void launch_world_ranges(const Dev& d, const int* worlds, int n, int* out, cudaS
                                                       worlds, n, out);
 }
 
-void launch_islands(const Dev& d, const Launch& L) {
-    k_islands<<<d.n_worlds, 256, 0, L.st>>>(d);
+int islands_smem_bytes(int max_bodies) {
+    // about four constraint edges per body, at most 160 KB
+    const long long want = 4LL * (5LL * max_bodies + 7LL * 4 * max_bodies) + max_bodies + 64;
+    const int bytes = (int)std::min<long long>(want, 160 * 1024);
+    cudaFuncSetAttribute(k_islands, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return bytes;
+}
+
+void launch_islands(const Dev& d, int smem_bytes, const Launch& L) {
+    k_islands<<<d.n_worlds, 256, smem_bytes, L.st>>>(d, smem_bytes);
     scan_exclusive(d.isl_count_w, d.isl_scan, nullptr, d.n_worlds, d.n_worlds, d.n_islands, d.scan_tmp, L);
     k_island_copy<<<grid_for(d.n_worlds, 128, L.n_sms), 128, 0, L.st>>>(d);
 }

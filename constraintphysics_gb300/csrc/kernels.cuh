@@ -25,7 +25,10 @@ void launch_geometry(const Dev& d, int force_all, const Launch& L);
 void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st);
 int mesh_scratch_warps(int n_sms);   // per-warp scratch entries the mesh narrowphase uses
 void launch_merge(const Dev& d, const Launch& L);
-void launch_islands(const Dev& d, const Launch& L);
+// k_islands' dynamic shared memory for worlds of up to `max_bodies` bodies
+// (sets the kernel's limit); worlds that need more run from global memory
+int islands_smem_bytes(int max_bodies);
+void launch_islands(const Dev& d, int smem_bytes, const Launch& L);
 // per-world edge / contact ranges of the current graph (4 ints per world)
 void launch_world_ranges(const Dev& d, const int* worlds, int n, int* out, cudaStream_t st);
 void launch_rows(const Dev& d, int first, int last, const Launch& L);
