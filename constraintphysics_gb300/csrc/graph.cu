@@ -195,7 +195,7 @@ __global__ void k_contacts(Dev d, int write) {
 // their global index, stored as -(k + 1)).
 __device__ __forceinline__ long long islands_need(int nb, int ne_w, int nj) {
     const long long E = (long long)ne_w + nj;
-    return 4LL * (4LL * nb + 4 * E + ne_w + 2 * E + nb) + nb;   // ints, then the body flags (bytes)
+    return 4LL * (5LL * nb + 4 * E + ne_w + 2 * E + nb) + nb;   // ints, then the body flags (bytes)
 }
 
 __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
@@ -218,13 +218,13 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
     const int nb = e - s, ne_w = e1 - e0, nj = je1 - je0, E = ne_w + nj;
     const int stack_cap = 2 * E + nb;
     const bool fast = islands_need(nb, ne_w, nj) <= smem_bytes;
-    int *vis, *a_ofs, *a_cur, *adj, *live, *stk;
+    int *vis, *a_ofs, *a_cur, *adj, *live, *stk, *order = nullptr;
     const uint8_t* mov;
     uint8_t* mov_s = nullptr;
     if (fast) {
         vis = sm_isl; a_ofs = vis + nb; a_cur = a_ofs + nb; adj = a_cur + nb;
-        live = adj + 4 * E; stk = live + ne_w;
-        mov_s = reinterpret_cast<uint8_t*>(stk + stack_cap);
+        live = adj + 4 * E; stk = live + ne_w; order = stk + stack_cap;
+        mov_s = reinterpret_cast<uint8_t*>(order + nb);
         mov = mov_s;
     } else {
         vis = d.visited + s; a_ofs = d.adj_ofs + s; a_cur = d.adj_cursor + s;
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
     for (int i = tid; i < nb; i += nt) {
         a_cur[i] = 0;
         vis[i] = -1;
-        if (fast) mov_s[i] = d.movement[s + i];
+        if (fast) { mov_s[i] = d.movement[s + i]; order[i] = d.map_order[s + i] - s; }
     }
     for (int c = c0 + tid; c < c1; c += nt) d.row_of_contact[c] = -1;
     // live contacts per edge, so that the serial DFS below advances its row
@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
     if (tid == 0) {
         int rc = c0 + jj0, bc = s, ni = 0, sc = sys0;
         for (int t = s; t < e; t++) {
-            const int node = d.map_order[t] - s;
+            const int node = fast ? order[t - s] : d.map_order[t] - s;
             if (mov[node] != 0 || vis[node] >= 0) continue;
             const int rs = rc, bs = bc, ss = sc;
             int sp = 0;
@@ -331,6 +331,10 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
                 vis[cur] = bc - bs;
                 d.isl_bodies[bc++] = cur + s;
                 const int lo = a_ofs[cur], hi = a_cur[cur];
+                // each edge to a not-yet-visited neighbour emits its rows, then
+                // the neighbour (if dynamic) is pushed; visits happen only at
+                // pops, so one pass over the edges gives the rows in edge order
+                // and the pushes in edge order
                 for (int j = lo; j < hi; j++) {
                     const int o = adj[2 * j], k = adj[2 * j + 1];
                     if (vis[o] >= 0) continue;
@@ -345,15 +349,12 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
                         }
                         for (int q = d.je.jstart[je]; q < d.je.jstart[je] + d.je.jcount[je]; q++) d.row_contact[rc++] = -(q + 1);
                         has_joint = true;
-                        continue;
+                    } else {
+                        // the edge's live contacts take the next rows (written below)
+                        const int nl = live[k];
+                        if (nl > 0) { d.edge_row[e0 + k] = rc; rc += nl; }
                     }
-                    // the edge's live contacts take the next rows (written below)
-                    const int nl = live[k];
-                    if (nl > 0) { d.edge_row[e0 + k] = rc; rc += nl; }
-                }
-                for (int j = lo; j < hi; j++) {
-                    const int o = adj[2 * j];
-                    if (mov[o] == 0 && vis[o] < 0) {
+                    if (mov[o] == 0) {
                         if (sp < stack_cap) stk[sp++] = o;
                         else atomicOr(d.status, ST_STACK_OVERFLOW);
                     }
@@ -475,7 +476,7 @@ void launch_world_ranges(const Dev& d, const int* worlds, int n, int* out, cudaS
 
 int islands_smem_bytes(int max_bodies) {
     // about four constraint edges per body, at most 160 KB
-    const long long want = 4LL * (5LL * max_bodies + 7LL * 4 * max_bodies) + max_bodies + 64;
+    const long long want = 4LL * (6LL * max_bodies + 7LL * 4 * max_bodies) + max_bodies + 64;
     const int bytes = (int)std::min<long long>(want, 160 * 1024);
     cudaFuncSetAttribute(k_islands, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return bytes;
