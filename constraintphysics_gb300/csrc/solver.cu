@@ -460,24 +460,41 @@ __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t
         const int n = min(kChunkRows, rc - c * kChunkRows);
         const float4* rb = reinterpret_cast<const float4*>(ring + slot * kChunkRows);
         RowBlock* g = d.rows + rs + c * kChunkRows;
-        for (int j = 0; j < n; j++) {
-            RowBlock R;
+        auto load = [&](int j, RowBlock& R) {
             float4* dst = reinterpret_cast<float4*>(&R);
 #pragma unroll
             for (int k = 0; k < (int)(sizeof(RowBlock) / 16); k++) dst[k] = rb[j * (sizeof(RowBlock) / 16) + k];
-            float4 imp = R.imp;
-            if (pass == 0) {
+        };
+        // one loop per pass kind (the pass is fixed within a chunk); the
+        // friction state is read only after the last velocity pass, so only
+        // that pass stores it
+        if (pass == 0) {
+            for (int j = 0; j < n; j++) {
+                RowBlock R;
+                load(j, R);
+                float4 imp = R.imp;
                 row_warm(R, imp, dv);
                 if (fused) {
                     row_pos(R, imp, dv);
                     g[j].imp = imp;
                 }
-            } else if (pass <= n_vel) {
+            }
+        } else if (pass <= n_vel) {
+            const bool last_vel = pass == n_vel;
+            for (int j = 0; j < n; j++) {
+                RowBlock R;
+                load(j, R);
+                float4 imp = R.imp;
                 int st = R.stat;
                 row_vel(R, imp, st, dv);
                 g[j].imp = imp;
-                g[j].stat = st;
-            } else {
+                if (last_vel) g[j].stat = st;
+            }
+        } else {
+            for (int j = 0; j < n; j++) {
+                RowBlock R;
+                load(j, R);
+                float4 imp = R.imp;
                 row_pos(R, imp, dv);
                 g[j].imp = imp;
             }
