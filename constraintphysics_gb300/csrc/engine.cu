@@ -791,7 +791,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
     {
         int max_world = 0;
         for (size_t k = 0; k + 1 < wstart.size(); k++) max_world = std::max(max_world, wstart[k + 1] - wstart[k]);
-        B->dv_cap = std::min(1536, std::max(64, max_world));
+        B->dv_cap = std::min(kPgsDvCapMax, std::max(64, max_world));
         B->isl_smem = islands_smem_bytes(max_world);
     }
     std::vector<uint8_t> pool;
@@ -2130,6 +2130,7 @@ int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* 
             B.marks = &ev;
             for (int i = 0; i < n_steps; i++) {
                 B.launch_step(B.d[B.parity]);
+                CK(cudaGetLastError());   // a launch refused here would leave its stage untimed
                 B.parity ^= 1;
                 CK(cudaEventSynchronize(ev[n_marks - 1]));
                 auto span = [&](int a, int c) { float ms = 0; CK(cudaEventElapsedTime(&ms, ev[a], ev[c])); return (double)ms; };

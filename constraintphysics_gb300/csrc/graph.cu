@@ -475,11 +475,11 @@ void launch_world_ranges(const Dev& d, const int* worlds, int n, int* out, cudaS
 }
 
 int islands_smem_bytes(int max_bodies) {
-    // about four constraint edges per body, at most 160 KB
+    // about four constraint edges per body, at most kIslandsSmemMax; the
+    // kernel's limit (shared by every batch of the process) is that maximum
     const long long want = 4LL * (6LL * max_bodies + 7LL * 4 * max_bodies) + max_bodies + 64;
-    const int bytes = (int)std::min<long long>(want, 160 * 1024);
-    cudaFuncSetAttribute(k_islands, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    return bytes;
+    cudaFuncSetAttribute(k_islands, cudaFuncAttributeMaxDynamicSharedMemorySize, kIslandsSmemMax);
+    return (int)std::min<long long>(want, kIslandsSmemMax);
 }
 
 void launch_islands(const Dev& d, int smem_bytes, const Launch& L) {

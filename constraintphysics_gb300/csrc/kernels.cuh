@@ -25,6 +25,11 @@ void launch_geometry(const Dev& d, int force_all, const Launch& L);
 void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st);
 int mesh_scratch_warps(int n_sms);   // per-warp scratch entries the mesh narrowphase uses
 void launch_merge(const Dev& d, const Launch& L);
+// largest k_pgs_big shared Δv area (island bodies) and k_islands shared
+// memory any batch uses: the kernels' dynamic shared memory limits are set to
+// these once for all batches
+constexpr int kPgsDvCapMax = 1536;
+constexpr int kIslandsSmemMax = 160 * 1024;
 // k_islands' dynamic shared memory for worlds of up to `max_bodies` bodies
 // (sets the kernel's limit); worlds that need more run from global memory
 int islands_smem_bytes(int max_bodies);

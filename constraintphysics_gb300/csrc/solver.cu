@@ -810,8 +810,12 @@ int pgs_big_blocks_per_sm(int dv_cap) {
     return n;
 }
 
+// The attribute is the kernel's, shared by every batch of the process: it is
+// set for the largest Δv area any batch uses, so that a batch built later with
+// a smaller one does not lower the limit under an earlier batch's launches
 void prepare_pgs(int dv_cap) {
-    cudaFuncSetAttribute(k_pgs_big, cudaFuncAttributeMaxDynamicSharedMemorySize, pgs_big_smem_bytes(dv_cap));
+    (void)dv_cap;
+    cudaFuncSetAttribute(k_pgs_big, cudaFuncAttributeMaxDynamicSharedMemorySize, pgs_big_smem_bytes(kPgsDvCapMax));
 }
 
 void launch_pgs_schedule(const Dev& d, const Launch& L) {

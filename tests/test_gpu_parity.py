@@ -284,3 +284,27 @@ def test_capacity_overflow_is_reported(monkeypatch):
     with pytest.raises(cg.CPGPUError, match="status -3"):
         w.step(120)
     assert np.isfinite(w.state()["com"]).all()
+
+
+def test_default_partition_of_large_worlds_equals_single(monkeypatch):
+    """512 worlds, four of 500 bodies and the rest of 8-16: the default
+    partition puts the large worlds in a part of their own, whose kernels use
+    more dynamic shared memory (island graph, solver Δv) than the part built
+    after it.  Every world still steps exactly as it does alone."""
+    monkeypatch.delenv("CPGPU_BATCH_PARTS", raising=False)
+    monkeypatch.delenv("CPGPU_BATCH_FIRST_SHARE", raising=False)
+    rng = np.random.default_rng(33)
+    pool = scenes.HullPool(4, size=8)
+    scs = [scenes.batched_world(rng, pool, 500, 501) for _ in range(4)]
+    scs += [scenes.batched_world(rng, pool, 8, 16) for _ in range(508)]
+    order = rng.permutation(len(scs))
+    scs = [scs[i] for i in order]
+    check = [int(np.where(order == k)[0][0]) for k in range(4)] + [0, 1, 2, 511]
+    b = cg.Batch(_worlds(scs))
+    b.step(20)
+    for i in check:
+        w = _worlds([scs[i]])[0]
+        w.step(20)
+        st, bs = w.state(), b.state(i)
+        for k in ("com", "quat", "vel", "ang_vel"):
+            assert np.array_equal(bs[k], st[k]), (i, k)
