@@ -30,6 +30,7 @@ SIGNATURES = {
     "body_box": (I, [P, P, D, D, D, P, I, P, P]),
     "body_sphere": (I, [P, P, D, P, I, P, P]),
     "body_cylinder": (I, [P, P, D, D, P, I, P, P]),
+    "body_capsule": (I, [P, P, D, D, P, I, P, P]),
     "body_mesh": (I, [P, P, I, P, I, P, I, P]),
     "body_set_velocity": (I, [P, U32, P]),
     "body_set_ang_velocity": (I, [P, U32, P]),

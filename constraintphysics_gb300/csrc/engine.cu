@@ -264,6 +264,12 @@ static Shape pack_cylinder(const D3& cref, double r, double h) {
     return pack_prim(SHAPE_CYLINDER, v, (float)(cref.mag() + std::sqrt(er * er + h * h / 4)));
 }
 
+// Capsule (ConvexPrimitive.cpp:357-360, height axis (0,1,0)) centred at `cref`
+// in the reference frame: radius r, drum height h
+static Shape pack_capsule(const D3& cref, double r, double h) {
+    return pack_prim(SHAPE_CAPSULE, {f4(cref, r), make_float4(0.f, 1.f, 0.f, (float)h)}, (float)(cref.mag() + h / 2 + r));
+}
+
 // ---------------------------------------------------------------- static meshes ----
 // StaticMeshGeometry (Geometry.cpp:675-820) prepared on the host: face normals,
 // neighbours across shared edges, ids (faces from 0, edges after the
@@ -820,7 +826,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds) {
             }
             max_hot = std::max(max_hot, (sh.hot + 15) & ~15);
             const uint32_t kind = reinterpret_cast<const HullHeader*>(sh.blob.data())->kind;
-            if (kind == SHAPE_SPHERE || kind == SHAPE_CYLINDER) B->prims = true;
+            if (kind == SHAPE_SPHERE || kind == SHAPE_CYLINDER || kind == SHAPE_CAPSULE) B->prims = true;
             if (kind == SHAPE_MESH) B->meshes = true;
         }
         const int base = wstart[wi];
@@ -1446,15 +1452,22 @@ static uint32_t add_hull(World& w, const std::vector<D3>& pts, const std::vector
     return id;
 }
 
-// calculateMassProperties (RigidBody.cpp:427-640), SPHERE and CYLINDER cases
-// for a one-primitive body with the default height axis: mass, centre of mass
-// and the inertia tensor about it.
-static void prim_mass(bool sphere, const D3& c, double r, double h, double density, double* mass, double t[9]) {
+// calculateMassProperties (RigidBody.cpp:427-640), SPHERE, CYLINDER and
+// CAPSULE cases for a one-primitive body with the default height axis: mass,
+// centre of mass and the inertia tensor about it.  For a capsule the
+// reference's mass is the volume (the density scales only the tensor,
+// RigidBody.cpp:577-585); kept.
+static void prim_mass(uint32_t kind, const D3& c, double r, double h, double density, double* mass, double t[9]) {
     const double pi = 3.1415926535;
     double m, d0, d1;
-    if (sphere) {
+    if (kind == SHAPE_SPHERE) {
         m = (4.0 / 3.0) * pi * r * r * r * density;
         d0 = d1 = 2.0 / 5.0 * m * r * r;
+    } else if (kind == SHAPE_CAPSULE) {
+        const double r3 = r * r * r, r4 = r3 * r, r5 = r4 * r;
+        m = (4.0 / 3.0) * pi * r * r * r + pi * r * r * h;
+        d0 = density * pi * ((8.0 / 15.0) * r5 + (1.0 / 3.0) * r3 * h * h + 0.75 * r4 * h + (1.0 / 12.0) * r * r * h * h * h);
+        d1 = density * pi * ((8.0 / 15.0) * r5 + 0.5 * h * r4);
     } else {
         m = pi * r * r * h * density;
         d0 = m * (h * h / 12 + r * r / 4);
@@ -1466,19 +1479,20 @@ static void prim_mass(bool sphere, const D3& c, double r, double h, double densi
     t[0] = d0; t[4] = d1; t[8] = d0;
 }
 
-static uint32_t add_prim(World& w, bool sphere, const D3& center, double r, double h, const cpgpu_material* m,
+static uint32_t add_prim(World& w, uint32_t kind, const D3& center, double r, double h, const cpgpu_material* m,
                          int movement, const double* pos) {
     if (movement < 0 || movement > 2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad movement type"};
     if (movement == CPGPU_KINEMATIC) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "kinematic bodies are not implemented on the device path"};
-    if (!(r > 0) || (!sphere && !(h > 0))) throw ApiFail{CPGPU_ERR_INVALID_ARG, "radius and height must be > 0"};
+    if (!(r > 0) || (kind == SHAPE_CYLINDER && !(h > 0)) || (kind == SHAPE_CAPSULE && !(h >= 0)))
+        throw ApiFail{CPGPU_ERR_INVALID_ARG, "radius must be > 0, cylinder height > 0, capsule drum height >= 0"};
     Body b;
     double density = m ? m->density : 1.0;
-    prim_mass(sphere, center, r, h, density, &b.mass, b.iref);
+    prim_mass(kind, center, r, h, density, &b.mass, b.iref);
     b.com = center;
     inv3(b.iref, b.iinv_ref);
     std::memcpy(b.iw, b.iref, sizeof(b.iw));
     std::memcpy(b.iinv, b.iinv_ref, sizeof(b.iinv));
-    Shape s = sphere ? pack_sphere(D3(), r) : pack_cylinder(D3(), r, h);
+    Shape s = kind == SHAPE_SPHERE ? pack_sphere(D3(), r) : kind == SHAPE_CAPSULE ? pack_capsule(D3(), r, h) : pack_cylinder(D3(), r, h);
     b.local_origin = -b.com;
     D3 p = pos ? D3(pos[0], pos[1], pos[2]) : D3();
     D3 tracked = b.com + qrot(b.q, b.local_origin);
@@ -1641,7 +1655,7 @@ int cpgpu_body_sphere(cpgpu_world* w, const double center[3], double radius, con
     W_OR_FAIL(w);
     return guarded([&] {
         if (!center) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null center"};
-        uint32_t id = add_prim(w->w, true, D3(center[0], center[1], center[2]), radius, 0, m, movement, pos);
+        uint32_t id = add_prim(w->w, SHAPE_SPHERE, D3(center[0], center[1], center[2]), radius, 0, m, movement, pos);
         if (out_id) *out_id = id;
         return CPGPU_OK;
     });
@@ -1654,7 +1668,20 @@ int cpgpu_body_cylinder(cpgpu_world* w, const double base[3], double radius, dou
     return guarded([&] {
         if (!base) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null base"};
         D3 c(base[0], base[1] + height / 2.0, base[2]);
-        uint32_t id = add_prim(w->w, false, c, radius, height, m, movement, pos);
+        uint32_t id = add_prim(w->w, SHAPE_CYLINDER, c, radius, height, m, movement, pos);
+        if (out_id) *out_id = id;
+        return CPGPU_OK;
+    });
+}
+// ConvexUnionGeometry::capsule (Geometry.cpp:43-45): `bot` is the centre of the
+// bottom cap sphere, the height axis is +y
+int cpgpu_body_capsule(cpgpu_world* w, const double bot[3], double radius, double drum_height, const cpgpu_material* m,
+                       int movement, const double pos[3], uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!bot) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null bot"};
+        D3 c(bot[0], bot[1] + drum_height / 2.0, bot[2]);
+        uint32_t id = add_prim(w->w, SHAPE_CAPSULE, c, radius, drum_height, m, movement, pos);
         if (out_id) *out_id = id;
         return CPGPU_OK;
     });

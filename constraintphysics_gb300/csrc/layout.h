@@ -36,7 +36,7 @@ static_assert(sizeof(HullHeader) == 48, "hull header size");
 //        along its own face normal, in the reference frame; the world value adds
 //        dot(R n, com) (the recentring of CollisionDetect.cpp:622-625)
 // ---- sphere and cylinder blobs ------------------------------------------------
-// Same header (kind 1 = sphere, 2 = cylinder; nv = nf = ne = na = 0; the whole
+// Same header (kind 1 = sphere, 2 = cylinder, 4 = capsule; nv = nf = ne = na = 0; the whole
 // blob is the hot part, off_fofs = its size), then, in the reference frame:
 //   float4 c      {centre xyz, radius}
 // cylinders only (Cylinder, ConvexPrimitive.h:160-210; 12 Gauss ring vertices,
@@ -45,10 +45,13 @@ static_assert(sizeof(HullHeader) == 48, "hull header size");
 //   float4 gv[14] Gauss vertices: caps (+axis, -axis), then the ring
 //   float4 top[8] top-cap 8-gon
 //   float4 bot[8] bottom-cap 8-gon
-enum ShapeKind : uint32_t { SHAPE_HULL = 0, SHAPE_SPHERE = 1, SHAPE_CYLINDER = 2, SHAPE_MESH = 3 };
+// capsules only (Capsule, ConvexPrimitive.h:107-141; kind 4):
+//   float4 c      {centre xyz, radius}
+//   float4 axis   {height axis xyz, drum height (distance of the cap-sphere centres)}
+enum ShapeKind : uint32_t { SHAPE_HULL = 0, SHAPE_SPHERE = 1, SHAPE_CYLINDER = 2, SHAPE_MESH = 3, SHAPE_CAPSULE = 4 };
 constexpr int kCylRing = 12, kCylCap = 8;
 constexpr int kCylOffAxis = 64, kCylOffGv = 80, kCylOffTop = 80 + 16 * 14, kCylOffBot = 80 + 16 * 22;
-constexpr int kSphereBlob = 64, kCylBlob = 80 + 16 * 30;
+constexpr int kSphereBlob = 64, kCylBlob = 80 + 16 * 30, kCapBlob = 80;
 
 // ---- static triangle mesh blob (kind 3; world coordinates; read from global,
 // never staged).  Header pad[0] = triangles, pad[1] = tree nodes (root first):

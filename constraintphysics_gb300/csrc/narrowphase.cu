@@ -416,8 +416,9 @@ __device__ __forceinline__ Axis warp_best(const Axis& best) {
     return w;
 }
 
-// ---- spheres and cylinders ------------------------------------------------------
-// Sphere (ConvexPrimitive.h:79-109) and Cylinder (:160-210) in world space.
+// ---- spheres, cylinders and capsules ------------------------------------------------
+// Sphere (ConvexPrimitive.h:79-109), Cylinder (:160-210) and Capsule (:107-141;
+// `h` is its drum height) in world space.
 struct PrimView {
     uint32_t kind;
     f3 c, axis;
@@ -438,6 +439,12 @@ __device__ void stage_prim(uint8_t* s, float4 pos, float4 rot, PrimView* pv, int
     pv->c = mul(R, mk(cref)) + com;
     pv->axis = mk(0.f, 0.f, 0.f);
     pv->h = 0.f;
+    if (H->kind == SHAPE_CAPSULE) {   // Capsule::recomputeFromReference (ConvexPrimitive.cpp:383-388)
+        float4 ax = *reinterpret_cast<const float4*>(s + kCylOffAxis);
+        pv->axis = mul(R, mk(ax));
+        pv->h = ax.w;
+        return;
+    }
     if (H->kind != SHAPE_CYLINDER) return;
     float4 ax = *reinterpret_cast<const float4*>(s + kCylOffAxis);
     pv->axis = mul(R, mk(ax));
@@ -826,8 +833,250 @@ __device__ bool cylinderCylinder(const PrimView& A, const PrimView& B, int lane,
     return true;
 }
 
+// ---- capsules ----------------------------------------------------------------------
+__device__ __forceinline__ f3 capTop(const PrimView& c) { return c.c + c.axis * (0.5f * c.h); }
+__device__ __forceinline__ f3 capBot(const PrimView& c) { return c.c - c.axis * (0.5f * c.h); }
+
+// getCapsuleExtrema (CollisionDetect.cpp:685-703): the two cap spheres
+__device__ __forceinline__ Ext capExt(const PrimView& c, f3 d) {
+    float v1 = dot(d, capTop(c)), v2 = dot(d, capBot(c));
+    return Ext{fminf(v1 - c.r, v2 - c.r), fmaxf(v1 + c.r, v2 + c.r), -1, -1};
+}
+
+// findCapsuleContactArea (CollisionDetect.cpp:376-390): 1 for the barrel line
+// (ids 0 = top cap, 1 = bottom cap), 2 for the single cap point
+__device__ int capArea(const PrimView& c, f3 n, f3 u, f3 w, Area* a) {
+    if (fabsf(dot(c.axis, n)) <= kSinTol) {
+        f3 barrel = normalize(n - c.axis * dot(c.axis, n));
+        f3 p1 = c.c + barrel * c.r + (0.5f * c.h) * c.axis;
+        f3 p2 = p1 - c.h * c.axis;
+        a->ps[0] = P2{dot(p1, u), dot(p1, w)};
+        a->ps[1] = P2{dot(p2, u), dot(p2, w)};
+        a->ids[0] = 0;
+        a->ids[1] = 1;
+        a->n = 2;
+        a->surface = -1;
+        return 1;
+    }
+    const bool top = dot(n, c.axis) > 0.f;
+    f3 q = top ? n * c.r + c.c + c.axis * (0.5f * c.h) : n * c.r + c.c - c.axis * (0.5f * c.h);
+    a->ps[0] = P2{dot(q, u), dot(q, w)};
+    a->ids[0] = top ? 0 : 1;
+    a->n = 1;
+    a->surface = -1;
+    return 2;
+}
+
+// two parallel barrel lines (A's along n, B's along -n) clipped to their
+// overlap along A's axis, as detectCapsuleCapsule / detectCapsuleCylinder build
+// the contact (CollisionDetect.cpp:1277-1297, 1947-1966)
+__device__ int parallelBarrels(const PrimView& A, const PrimView& B, f3 n, f3 u, f3 w, CP* out) {
+    f3 ba = normalize(n - A.axis * dot(A.axis, n));
+    f3 a1 = A.c + ba * A.r + (0.5f * A.h) * A.axis, a2 = a1 - A.h * A.axis;
+    f3 bbv = normalize(-1.f * n - B.axis * dot(B.axis, -1.f * n));
+    f3 b1 = B.c + bbv * B.r + (0.5f * B.h) * B.axis, b2 = b1 - B.h * B.axis;
+    if (dot(B.axis, A.axis) < 0.f) { f3 t = b1; b1 = b2; b2 = t; }
+    float amx = dot(a1, A.axis), amn = dot(a2, A.axis), bmx = dot(b1, A.axis), bmn = dot(b2, A.axis);
+    f3 imx = (amx > bmx) ? b1 : a1;
+    f3 imn = (amn > bmn) ? a2 : b2;
+    out[0] = CP{P2{dot(u, imx), dot(w, imx)}, 0, 0ull, 0};
+    out[1] = CP{P2{dot(u, imn), dot(w, imn)}, 0, 1ull, 0};
+    return 2;
+}
+
+// detectSphereCapsule (CollisionDetect.cpp:868-935): the radial direction to
+// the capsule axis, then the directions to both cap centres
+__device__ bool sphereCapsule(const PrimView& S, const PrimView& C, PrimOut* o) {
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)};
+    bool sep = false;
+    f3 ax = C.axis;
+    f3 diff = C.c - S.c;
+    f3 barrel = normalize(diff - ax * dot(ax, diff));
+    check(sphereExt(S, barrel), capExt(C, barrel), barrel, 0, &best, &sep);
+    if (sep) return false;
+    f3 e1 = normalize(capTop(C) - S.c);
+    check(sphereExt(S, e1), capExt(C, e1), e1, 1, &best, &sep);
+    if (sep) return false;
+    f3 e2 = normalize(capBot(C) - S.c);
+    check(sphereExt(S, e2), capExt(C, e2), e2, 2, &best, &sep);
+    if (sep || !(best.pen < INFINITY)) return false;
+    f3 q = S.c + best.n * S.r;
+    o->n = best.n;
+    o->pen = best.pen;
+    o->pts[0] = make_float4(q.x, q.y, q.z, best.pen);
+    o->magic[0] = 0ull;
+    o->m = 1;
+    return true;
+}
+
+// detectCapsuleCapsule (CollisionDetect.cpp:1139-1334): the reference's eight
+// axes in its order (cap-centre pairs top-top, b top - a bottom,
+// bottom-bottom; a's caps against b's barrel; b's caps against a's barrel,
+// taken from b's centre; barrel x barrel), one lane each; then the parallel-
+// barrel case or clipping
+__device__ bool capsuleCapsule(const PrimView& A, const PrimView& B, int lane, Scratch& scratch, CP* clipped,
+                               int* status, PrimOut* o) {
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)};
+    bool sep = false;
+    const f3 at = capTop(A), ab = capBot(A), bt = capTop(B), bb = capBot(B);
+    if (lane < 8) {
+        f3 n;
+        bool use = true;
+        switch (lane) {
+        case 0: n = normalize(bt - at); break;
+        case 1: n = normalize(bt - ab); break;
+        case 2: n = normalize(bb - ab); break;
+        case 3: { f3 d = B.c - at; n = normalize(d - B.axis * dot(B.axis, d)); } break;
+        case 4: { f3 d = B.c - ab; n = normalize(d - B.axis * dot(B.axis, d)); } break;
+        case 5: { f3 d = B.c - bt; n = normalize(d - A.axis * dot(A.axis, d)); } break;
+        case 6: { f3 d = B.c - bb; n = normalize(d - A.axis * dot(A.axis, d)); } break;
+        default: {
+            f3 x = cross(A.axis, B.axis);
+            use = mag2(x) > 0.00000001f;
+            n = use ? normalize(x) : x;
+        }
+        }
+        if (use) check(capExt(A, n), capExt(B, n), n, lane, &best, &sep);
+    }
+    if (__any_sync(0xffffffffu, sep)) return false;
+    Axis b = warp_best(best);
+    if (!(b.pen < INFINITY)) return false;
+    if (lane == 0) {
+        f3 n = b.n, u, w;
+        basis(n, &u, &w);
+        Area ac, bc;
+        int ka = capArea(A, n, u, w, &ac);
+        int kb = capArea(B, -1.f * n, u, w, &bc);
+        int m;
+        if (ka == 1 && kb == 1 && fabsf(dot(A.axis, B.axis)) > 0.995f) m = parallelBarrels(A, B, n, u, w, clipped);
+        else m = clipContacts(ac, bc, scratch, clipped, status);
+        f3 amax = dot(A.axis, n) > 0.f ? at + n * A.r : ab + n * A.r;
+        points_from_pool(clipped, m, u, w, n, dot(amax, n), b.pen, o);
+        o->n = n;
+        o->pen = b.pen;
+    }
+    return true;
+}
+
+// SAT_PolyCapsule (CollisionDetect.cpp:1413-1561): the hull's faces, its
+// vertices (radially to the drum, or to the nearer cap centre), and per edge
+// the cap axis, again the cap axis (the reference's "bottom cap" test samples
+// the top cap, :1486-1488) and edge x height axis; the reference places the
+// cap centres a full drum height from the centre in this function
+// (:1436-1437).  Contact by clipping the hull feature against the capsule's.
+__device__ bool polyCapsule(const HullView& A, const PrimView& C, int lane, Scratch& scratch, CP* clipped,
+                            int* status, PrimOut* o) {
+    const HullHeader& H = *A.h;
+    const int nf = H.nf, nv = H.nv, ne = H.ne;
+    const uint8_t* edges = A.g + H.off_edge;
+    const int v0 = nf, e0 = nf + nv, total = e0 + 3 * ne;
+    const f3 ax = C.axis;
+    const f3 tcc = C.c + ax * C.h, bcc = C.c - ax * C.h;
+    const float tv = dot(tcc, ax), bv = dot(bcc, ax);
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)};
+    bool sep = false;
+    for (int t = lane; t < total; t += 32) {
+        Ext ea;
+        f3 n;
+        if (t < nf) {
+            float4 g = A.n[t];
+            if (g.w != 0.f) continue;
+            n = mk(g);
+            float4 c = A.cache[t];
+            float shift = dot(n, A.com);
+            ea = Ext{c.y + shift, c.x + shift, __float_as_int(c.w), __float_as_int(c.z)};
+        } else {
+            if (t < e0) {
+                f3 p = mk(A.v[t - v0]);
+                float v = dot(p, ax);
+                if (bv <= v && v <= tv) n = normalize((p - C.c) - ax * dot(ax, p - C.c));
+                else if (v > tv) n = normalize(p - tcc);
+                else n = normalize(p - bcc);
+            } else {
+                int k = t - e0, e = k / 3, which = k - 3 * e;
+                f3 p1 = mk(A.v[edges[2 * e]]), p2 = mk(A.v[edges[2 * e + 1]]);
+                f3 dir = normalize(p2 - p1);
+                if (which < 2) {
+                    f3 sample = p1 - tcc;
+                    n = normalize(sample - dir * dot(dir, sample));
+                } else if (!edgeAxis(dir, ax, &n)) {
+                    continue;
+                }
+            }
+            ea = extrema(A.v, nv, n);
+        }
+        check(ea, capExt(C, n), n, t, &best, &sep);
+    }
+    if (__any_sync(0xffffffffu, sep)) return false;
+    Axis b = warp_best(best);
+    if (!(b.pen < INFINITY) || b.aid < 0) return false;
+    if (lane == 0) {
+        f3 n = b.n, u, w;
+        basis(n, &u, &w);
+        Area ac, bc;
+        contactArea(A, n, b.aid, u, w, &ac);
+        capArea(C, -1.f * n, u, w, &bc);
+        int m = clipContacts(ac, bc, scratch, clipped, status);
+        points_from_pool(clipped, m, u, w, n, dot(mk(A.v[b.aid]), n), b.pen, o);
+        o->n = n;
+        o->pen = b.pen;
+    }
+    return true;
+}
+
+// detectCapsuleCylinder (CollisionDetect.cpp:1794-2002): the cylinder axis, its
+// top 8-gon's edges x the capsule axis, both rim points (towards each cap
+// centre) of both cylinder caps, each cap centre radially to the cylinder,
+// barrel x barrel; then the rim point, parallel barrels or clipping
+__device__ bool capsuleCylinder(const PrimView& A, const PrimView& B, int lane, Scratch& scratch, CP* clipped,
+                                int* status, PrimOut* o) {
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)};
+    bool sep = false;
+    const f3 at = capTop(A), ab = capBot(A);
+    if (lane < 16) {
+        f3 n;
+        bool use = true;
+        if (lane == 0) n = B.axis;
+        else if (lane <= kCylCap) use = ringAxis(B.top, lane - 1, A.axis, &n);
+        else if (lane <= kCylCap + 4) {
+            const int k = lane - kCylCap - 1;
+            const f3 disk = k < 2 ? topCenter(B) : botCenter(B);
+            const f3 cap = (k & 1) ? ab : at;
+            f3 cp = diskExtremum(disk, B.axis, B.r, normalize(cap - B.c));
+            n = normalize(cp - cap);
+        } else if (lane <= kCylCap + 6) {
+            f3 d = B.c - (lane == kCylCap + 5 ? at : ab);
+            n = normalize(d - B.axis * dot(B.axis, d));
+        } else {
+            f3 x = cross(A.axis, B.axis);
+            use = mag2(x) > 0.00000001f;
+            n = use ? normalize(x) : x;
+        }
+        if (use) check(capExt(A, n), cylExt(B, n), n, lane, &best, &sep);
+    }
+    if (__any_sync(0xffffffffu, sep)) return false;
+    Axis b = warp_best(best);
+    if (!(b.pen < INFINITY)) return false;
+    if (lane == 0) {
+        f3 n = b.n, u, w;
+        basis(n, &u, &w);
+        Area ac, bc;
+        int ka = capArea(A, n, u, w, &ac);
+        int kb = cylArea(B, -1.f * n, u, w, &bc);
+        int m;
+        if (kb == 2) { clipped[0] = CP{bc.ps[0], 0, 0ull, 0}; m = 1; }
+        else if (ka == 1 && kb == 1 && fabsf(dot(A.axis, B.axis)) > 0.995f) m = parallelBarrels(A, B, n, u, w, clipped);
+        else m = clipContacts(ac, bc, scratch, clipped, status);
+        f3 amax = dot(A.axis, n) > 0.f ? at + n * A.r : ab + n * A.r;
+        points_from_pool(clipped, m, u, w, n, dot(amax, n), b.pen, o);
+        o->n = n;
+        o->pen = b.pen;
+    }
+    return true;
+}
+
 // detectCollision's primitive dispatch (CollisionDetect.cpp:57-150) for every
-// pair involving a sphere or cylinder.  Pairs the detectors take the other way
+// pair involving a sphere, cylinder or capsule.  Pairs the detectors take the other way
 // round are flipped back: normal negated, both MagicID halves swapped.
 __device__ __forceinline__ void narrow_prim(const Dev& d, int p, int a, int b, uint8_t* sa, uint8_t* sb, const uint8_t* ga,
                                          const uint8_t* gb, uint32_t ka, uint32_t kb, int lane, Scratch& scratch,
@@ -842,18 +1091,26 @@ __device__ __forceinline__ void narrow_prim(const Dev& d, int p, int a, int b, u
     PrimOut o;
     o.m = 0;
     bool hit, flip = false;
-    if (ka == SHAPE_HULL) {
-        hit = kb == SHAPE_SPHERE ? polySphere(hv, pb, lane, &o) : polyCylinder(hv, pb, lane, scratch, clipped, d.status, &o);
-    } else if (kb == SHAPE_HULL) {
-        flip = true;
-        hit = ka == SHAPE_SPHERE ? polySphere(hv, pa, lane, &o) : polyCylinder(hv, pa, lane, scratch, clipped, d.status, &o);
+    if (ka == SHAPE_HULL || kb == SHAPE_HULL) {
+        flip = kb == SHAPE_HULL;
+        const PrimView& q = flip ? pa : pb;
+        const uint32_t kq = flip ? ka : kb;
+        if (kq == SHAPE_SPHERE) hit = polySphere(hv, q, lane, &o);
+        else if (kq == SHAPE_CAPSULE) hit = polyCapsule(hv, q, lane, scratch, clipped, d.status, &o);
+        else hit = polyCylinder(hv, q, lane, scratch, clipped, d.status, &o);
     } else if (ka == SHAPE_SPHERE && kb == SHAPE_SPHERE) {
         hit = sphereSphere(pa, pb, &o);
-    } else if (ka == SHAPE_SPHERE) {
-        hit = sphereCylinder(pa, pb, &o);
-    } else if (kb == SHAPE_SPHERE) {
-        flip = true;
-        hit = sphereCylinder(pb, pa, &o);
+    } else if (ka == SHAPE_SPHERE || kb == SHAPE_SPHERE) {
+        flip = kb == SHAPE_SPHERE;
+        const PrimView& s = flip ? pb : pa;
+        const PrimView& q = flip ? pa : pb;
+        hit = (flip ? ka : kb) == SHAPE_CAPSULE ? sphereCapsule(s, q, &o) : sphereCylinder(s, q, &o);
+    } else if (ka == SHAPE_CAPSULE && kb == SHAPE_CAPSULE) {
+        hit = capsuleCapsule(pa, pb, lane, scratch, clipped, d.status, &o);
+    } else if (ka == SHAPE_CAPSULE || kb == SHAPE_CAPSULE) {
+        flip = kb == SHAPE_CAPSULE;
+        hit = flip ? capsuleCylinder(pb, pa, lane, scratch, clipped, d.status, &o)
+                   : capsuleCylinder(pa, pb, lane, scratch, clipped, d.status, &o);
     } else {
         hit = cylinderCylinder(pa, pb, lane, scratch, clipped, d.status, &o);
     }
@@ -1104,6 +1361,54 @@ __device__ bool cylTri(const PrimView& C, const TriView& T, float penalty, int l
         f3 amax = diskExtremum(dot(C.axis, n) > 0.f ? topCenter(C) : botCenter(C), C.axis, C.r, n);
         Area ac, bc;
         int ak = cylArea(C, ng.n, u, w, &ac);
+        triArea(T, -1.f * ng.n, T.v[ng.bid], ng.bid, u, w, &bc);
+        int m;
+        if (ak == 2) { clipped[0] = CP{ac.ps[0], 0, 0ull, 0}; m = 1; }
+        else m = clipContacts(ac, bc, scratch, clipped, status);
+        points_from_pool(clipped, m, u, w, n, dot(amax, n), mp.pen, o);
+        o->n = n;
+        o->pen = mp.pen;
+    }
+    return true;
+}
+
+// SAT_CapsuleTriangle (CollisionDetect.cpp:2278-2464): the face normal, face
+// edges x capsule axis, the vertices radially, the vertices and the edges
+// against the cap centres; the reference computes its "bottom" cap centre
+// with +h/2 too (:2285-2286), so both sets of cap axes use the top cap (and
+// the deepest point is always on the top cap); kept.  One lane per axis.
+__device__ bool capTri(const PrimView& C, const TriView& T, float penalty, int lane, Scratch& scratch, CP* clipped,
+                       int* status, PrimOut* o) {
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)}, valid = best;
+    bool sep = false;
+    const f3 ax = C.axis;
+    const f3 at = capTop(C), ab = capTop(C);
+    if (lane < 19) {
+        f3 n;
+        bool use = true;
+        if (lane == 0) n = T.n;
+        else if (lane < 4) use = edgeAxis(T.v[lane % 3] - T.v[lane - 1], ax, &n);
+        else if (lane < 7) {
+            f3 diff = T.v[lane - 4] - C.c;
+            n = normalize(diff - ax * dot(ax, diff));
+        } else if (lane < 13) {
+            n = normalize(T.v[(lane - 7) % 3] - (lane < 10 ? at : ab));
+        } else {
+            const int i = (lane - 13) % 3;
+            f3 dir = normalize(T.v[(i + 1) % 3] - T.v[i]);
+            f3 sample = T.v[i] - (lane < 16 ? at : ab);
+            n = normalize(sample - dir * dot(dir, sample));
+        }
+        if (use) triCheck(capExt(C, n), triExt(T, n), n, lane, T, &best, &valid, &sep);
+    }
+    Axis ng, mp;
+    if (!triChoose(best, valid, penalty, sep, &ng, &mp) || ng.bid < 0) return false;
+    if (lane == 0) {
+        f3 n = mp.n, u, w;
+        basis(n, &u, &w);
+        f3 amax = dot(ax, n) > 0.f ? at + n * C.r : ab + n * C.r;
+        Area ac, bc;
+        int ak = capArea(C, ng.n, u, w, &ac);
         triArea(T, -1.f * ng.n, T.v[ng.bid], ng.bid, u, w, &bc);
         int m;
         if (ak == 2) { clipped[0] = CP{ac.ps[0], 0, 0ull, 0}; m = 1; }
@@ -1394,7 +1699,7 @@ __global__ void __launch_bounds__(128) k_clip(Dev d) {
 
 // One warp per candidate pair that involves a sphere or a cylinder (the other
 // pairs are k_narrowphase's).  Same staging as k_narrowphase.
-__global__ void __launch_bounds__(256) k_narrow_prim(Dev d, int slot_bytes) {
+__global__ void __launch_bounds__(256, 1) k_narrow_prim(Dev d, int slot_bytes) {
     extern __shared__ __align__(16) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -1539,6 +1844,7 @@ __global__ void __launch_bounds__(256) k_narrow_mesh(Dev d, int slot_bytes) {
             bool hit;
             if (kc == SHAPE_HULL) hit = polyTri(hv, T, penalty, lane, scratch, clipped, d.status, &o);
             else if (kc == SHAPE_SPHERE) hit = sphereTri(pv, T, penalty, lane, &o);
+            else if (kc == SHAPE_CAPSULE) hit = capTri(pv, T, penalty, lane, scratch, clipped, d.status, &o);
             else hit = cylTri(pv, T, penalty, lane, scratch, clipped, d.status, &o);
             if (lane == 0 && hit && o.pen > 0.f && o.m > 0) {
                 if (nman >= kMeshMans || npts + o.m > kMeshRaw) {

@@ -1,5 +1,6 @@
 // shapes.cuh — device-side world-frame geometry of the body kinds (convex
-// hull, sphere, cylinder, static triangle mesh) shared by the pose/AABB kernels.
+// hull, sphere, cylinder, capsule, static triangle mesh) shared by the
+// pose/AABB kernels.
 #pragma once
 #include "devmath.cuh"
 #include "layout.h"
@@ -30,6 +31,17 @@ __device__ __forceinline__ void shape_aabb(const uint8_t* blob, f3 c, const M33&
         f3 w = c + mul(R, mk(s));
         *mn = w - mk(s.w, s.w, s.w);
         *mx = w + mk(s.w, s.w, s.w);
+        return;
+    }
+    if (H->kind == SHAPE_CAPSULE) {
+        // Capsule::gen_AABB (ConvexPrimitive.cpp:390-401): centre +- (|axis h/2| + r)
+        float4 s = *reinterpret_cast<const float4*>(blob + sizeof(HullHeader));
+        float4 ax = *reinterpret_cast<const float4*>(blob + kCylOffAxis);
+        f3 w = c + mul(R, mk(s));
+        f3 v = mul(R, mk(ax)) * (0.5f * ax.w);
+        f3 e = mk(fabsf(v.x) + s.w, fabsf(v.y) + s.w, fabsf(v.z) + s.w);
+        *mn = w - e;
+        *mx = w + e;
         return;
     }
     if (H->kind == SHAPE_CYLINDER) {

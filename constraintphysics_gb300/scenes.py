@@ -97,6 +97,9 @@ class Scene:
     def cylinder(self, base, r, h, material, movement, pos=(0, 0, 0)):
         return self._body(("cylinder", tuple(base), r, h, material, movement, tuple(pos)))
 
+    def capsule(self, bot, r, h, material, movement, pos=(0, 0, 0)):
+        return self._body(("capsule", tuple(bot), r, h, material, movement, tuple(pos)))
+
     def mesh(self, points, tris, material):
         return self._body(("mesh", np.asarray(points, dtype=np.float64), np.asarray(tris, dtype=np.int32), material))
 
@@ -118,7 +121,7 @@ class Scene:
 
     def movements(self):
         """Movement type of each body, in id order."""
-        slot = {"hull": 4, "box": 6, "sphere": 4, "cylinder": 5}
+        slot = {"hull": 4, "box": 6, "sphere": 4, "cylinder": 5, "capsule": 5}
         return [FIXED if op[0] == "mesh" else op[slot[op[0]]] for op in self.ops if op[0] in slot or op[0] == "mesh"]
 
 
@@ -136,6 +139,8 @@ def apply(scene, world):
             ids.append(world.add_sphere(op[1], op[2], op[3], op[4], op[5]))
         elif kind == "cylinder":
             ids.append(world.add_cylinder(op[1], op[2], op[3], op[4], op[5], op[6]))
+        elif kind == "capsule":
+            ids.append(world.add_capsule(op[1], op[2], op[3], op[4], op[5], op[6]))
         elif kind == "mesh":
             ids.append(world.add_mesh(op[1], op[2], op[3], True))
         elif kind == "orient":
@@ -337,6 +342,45 @@ def terrain_drop(seed=0, n_grid=32, n_side=6, n_layers=2, spacing=3.2, clearance
                 elif u < 0.6:
                     bid = sc.sphere((0.0, 0.0, 0.0), rng.uniform(0.3, 0.8), PILE_MATERIAL, DYNAMIC, pos)
                 elif u < 0.8:
+                    r, hh = rng.uniform(0.3, 0.6), rng.uniform(0.5, 1.5)
+                    bid = sc.cylinder((0.0, -hh / 2, 0.0), r, hh, PILE_MATERIAL, DYNAMIC, pos)
+                else:
+                    p_, f_ = random_hull(rng, 12, 32)
+                    bid = sc.hull(p_, f_, PILE_MATERIAL, DYNAMIC, pos)
+                sc.orient(bid, random_quat(rng))
+    return sc
+
+
+def capsule_drop(seed=0, n_side=4, n_layers=2, terrain=False, n_grid=16, spacing=3.2):
+    """Capsules (about half the bodies, r U[0.25,0.5], drum height
+    U[0.3,1.2]) mixed with boxes, spheres, cylinders and hulls, dropped on the
+    plate or on a value-noise terrain mesh: every capsule pair kind occurs."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(f"capsule_drop_{'terrain' if terrain else 'plate'}_{n_side}x{n_side}x{n_layers}_seed{seed}", MIXED_PARAMS)
+    if terrain:
+        hts = value_noise(rng, n_grid)
+        pts, tris = grid_mesh(hts, 1.0, (-n_grid / 2.0, 0.0, -n_grid / 2.0))
+        sc.mesh(pts, tris, PILE_MATERIAL)
+        base = float(hts.max()) + 3.0
+    else:
+        _plate(sc)
+        base = 2.0
+    off = (n_side - 1) * spacing / 2.0
+    for j in range(n_layers):
+        for i in range(n_side):
+            for k in range(n_side):
+                pos = np.array([i * spacing - off, base + j * spacing, k * spacing - off])
+                pos += rng.uniform(-0.1, 0.1, size=3)
+                u = rng.random()
+                if u < 0.5:
+                    r, hh = rng.uniform(0.25, 0.5), rng.uniform(0.3, 1.2)
+                    bid = sc.capsule((0.0, -hh / 2, 0.0), r, hh, PILE_MATERIAL, DYNAMIC, pos)
+                elif u < 0.625:
+                    d = rng.uniform(0.5, 1.5, size=3)
+                    bid = sc.box((-d[0] / 2, -d[1] / 2, -d[2] / 2), d[0], d[1], d[2], PILE_MATERIAL, DYNAMIC, pos)
+                elif u < 0.75:
+                    bid = sc.sphere((0.0, 0.0, 0.0), rng.uniform(0.3, 0.8), PILE_MATERIAL, DYNAMIC, pos)
+                elif u < 0.875:
                     r, hh = rng.uniform(0.3, 0.6), rng.uniform(0.5, 1.5)
                     bid = sc.cylinder((0.0, -hh / 2, 0.0), r, hh, PILE_MATERIAL, DYNAMIC, pos)
                 else:

@@ -129,6 +129,17 @@ class World:
                                     int(movement), _ptr(pos), C.addressof(out))
         return self._new_id(rc, out)
 
+    def add_capsule(self, bot, radius, drum_height, material=None, movement=0, pos=(0, 0, 0)):
+        """ConvexUnionGeometry::capsule: `bot` is the centre of the bottom cap
+        sphere, `drum_height` the distance between the cap-sphere centres."""
+        bot = _f64(bot, 3)
+        pos = _f64(pos, 3)
+        mat = self._mat(material)
+        out = C.c_uint32()
+        rc = self.abi.body_capsule(self.h, _ptr(bot), float(radius), float(drum_height), C.addressof(mat),
+                                   int(movement), _ptr(pos), C.addressof(out))
+        return self._new_id(rc, out)
+
     def add_mesh(self, points, tris, material=None, fixed=True):
         pts = _f64(points)
         tr = np.ascontiguousarray(tris, dtype=np.int32)

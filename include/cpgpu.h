@@ -125,6 +125,15 @@ int cpgpu_body_sphere(cpgpu_world* w, const double center[3], double radius,
 int cpgpu_body_cylinder(cpgpu_world* w, const double base[3], double radius, double height,
                         const cpgpu_material* mat, int movement, const double pos[3],
                         uint32_t* out_id);
+/* createRigidBody(ConvexUnionGeometry::capsule(bot_sphere_center, radius,
+ * drum_height, material), ...) (Geometry.cpp:43-45): `bot` is the centre of
+ * the bottom cap sphere, `drum_height` the distance between the two cap-sphere
+ * centres, the height axis +y.  Pairs: SAT_PolyCapsule, detectSphereCapsule,
+ * detectCapsuleCapsule, detectCapsuleCylinder, SAT_CapsuleTriangle
+ * (CollisionDetect.cpp:1413-1561, 868-935, 1139-1334, 1794-2002, 2278-2464). */
+int cpgpu_body_capsule(cpgpu_world* w, const double bot[3], double radius, double drum_height,
+                       const cpgpu_material* mat, int movement, const double pos[3],
+                       uint32_t* out_id);
 /* createRigidBody(StaticMeshGeometry(MeshInput{tris, points}), fixed)
  * (PhysicsEngine.cpp:498-512, Geometry.h:52-55): points (xyz) and triangles
  * (three point indices each) in world coordinates; `fixed` must be nonzero

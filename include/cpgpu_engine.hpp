@@ -6,9 +6,10 @@
 // Differences a caller sees:
 //   * bodies are addressed by id (RigidBody handles wrap the id);
 //   * errors that the reference reports with assert() throw cpgpu::Error;
-//   * only the contact path is on the device: convex hulls and boxes, ball
-//     sockets and hinges are the supported shapes/joints (others throw
-//     cpgpu::Error with CPGPU_ERR_UNSUPPORTED), sleeping stays disabled.
+//   * only the contact path is on the device: convex hulls, boxes, spheres,
+//     cylinders, capsules and fixed static triangle meshes, ball sockets and
+//     hinges are the supported shapes/joints (others throw cpgpu::Error with
+//     CPGPU_ERR_UNSUPPORTED), one primitive per body, sleeping stays disabled.
 #pragma once
 #include <array>
 #include <cstdint>
@@ -53,12 +54,29 @@ struct Material {
 
 // ConvexUnionGeometry restricted to one convex primitive (Geometry.h:9-47)
 struct ConvexUnionGeometry {
-    enum Kind { HULL, BOX } kind = HULL;
+    enum Kind { HULL, BOX, SPHERE, CYLINDER, CAPSULE } kind = HULL;
     std::vector<Vec3> points;
     std::vector<std::vector<int>> faces;
-    Vec3 corner;
+    Vec3 corner;                 // box corner, sphere centre, cylinder base, capsule bottom-sphere centre
     double dx = 0, dy = 0, dz = 0;
+    double radius = 0, height = 0;   // sphere / cylinder / capsule (capsule: drum height)
     Material material;
+    static ConvexUnionGeometry sphere(Vec3 center, double radius, Material m = Material::default_material()) {
+        ConvexUnionGeometry g;
+        g.kind = SPHERE; g.corner = center; g.radius = radius; g.material = m;
+        return g;
+    }
+    static ConvexUnionGeometry cylinder(Vec3 pos, double radius, double height, Material m = Material::default_material()) {
+        ConvexUnionGeometry g;
+        g.kind = CYLINDER; g.corner = pos; g.radius = radius; g.height = height; g.material = m;
+        return g;
+    }
+    static ConvexUnionGeometry capsule(Vec3 bot_sphere_center, double radius, double drum_height,
+                                       Material m = Material::default_material()) {
+        ConvexUnionGeometry g;
+        g.kind = CAPSULE; g.corner = bot_sphere_center; g.radius = radius; g.height = drum_height; g.material = m;
+        return g;
+    }
     static ConvexUnionGeometry box(Vec3 pos, double dx, double dy, double dz, Material m = Material::default_material()) {
         ConvexUnionGeometry g;
         g.kind = BOX; g.corner = pos; g.dx = dx; g.dy = dy; g.dz = dz; g.material = m;
@@ -110,6 +128,12 @@ public:
         cpgpu_material m = g.material.c();
         if (g.kind == ConvexUnionGeometry::BOX) {
             check(cpgpu_body_box(w_, g.corner.data(), g.dx, g.dy, g.dz, &m, movement, position.data(), &id));
+        } else if (g.kind == ConvexUnionGeometry::SPHERE) {
+            check(cpgpu_body_sphere(w_, g.corner.data(), g.radius, &m, movement, position.data(), &id));
+        } else if (g.kind == ConvexUnionGeometry::CYLINDER) {
+            check(cpgpu_body_cylinder(w_, g.corner.data(), g.radius, g.height, &m, movement, position.data(), &id));
+        } else if (g.kind == ConvexUnionGeometry::CAPSULE) {
+            check(cpgpu_body_capsule(w_, g.corner.data(), g.radius, g.height, &m, movement, position.data(), &id));
         } else {
             std::vector<double> pts;
             for (const Vec3& p : g.points) { pts.push_back(p.x); pts.push_back(p.y); pts.push_back(p.z); }
@@ -118,6 +142,22 @@ public:
             check(cpgpu_body_hull(w_, pts.data(), (int)g.points.size(), offs.data(), idx.data(), (int)g.faces.size(), &m,
                                   movement, position.data(), &id));
         }
+        RigidBody* b = new RigidBody(this, id);
+        owned_.push_back(b);
+        return b;
+    }
+
+    // createRigidBody(StaticMeshGeometry(MeshInput{triangle_indices, points}), FIXED)
+    // (PhysicsEngine.cpp:498-512): triangles (three point indices each) in world coordinates
+    RigidBody* createStaticMesh(const std::vector<Vec3>& points, const std::vector<std::array<int, 3>>& tris,
+                                Material mat = Material::default_material()) {
+        std::vector<double> pts;
+        for (const Vec3& p : points) { pts.push_back(p.x); pts.push_back(p.y); pts.push_back(p.z); }
+        std::vector<int> idx;
+        for (const auto& t : tris) idx.insert(idx.end(), t.begin(), t.end());
+        cpgpu_material m = mat.c();
+        uint32_t id = 0;
+        check(cpgpu_body_mesh(w_, pts.data(), (int)points.size(), idx.data(), (int)tris.size(), &m, 1, &id));
         RigidBody* b = new RigidBody(this, id);
         owned_.push_back(b);
         return b;

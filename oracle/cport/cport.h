@@ -259,7 +259,10 @@ struct CylG {
     V3 topCenter() const { return c + 0.5 * h * axis; }
     V3 botCenter() const { return c - 0.5 * h * axis; }
 };
-enum Kind { K_HULL = 0, K_SPHERE = 1, K_CYLINDER = 2, K_MESH = 3 };
+// Capsule (ConvexPrimitive.h:107-141): centre, radius, drum height (the
+// distance between the two cap-sphere centres) and height axis
+struct CapG { V3 c, axis; double r = 0, h = 0; };
+enum Kind { K_HULL = 0, K_SPHERE = 1, K_CYLINDER = 2, K_MESH = 3, K_CAPSULE = 4 };
 
 // StaticMeshFace (Geometry.h:74-86) as built by StaticMeshGeometry's
 // constructor (Geometry.cpp:675-820)
@@ -299,6 +302,7 @@ struct Body {
     Hull shape;           // world geometry (points and Gauss normals follow the pose)
     SphereG sph_src, sph_ref, sph;
     CylG cyl_src, cyl_ref, cyl;
+    CapG cap_src, cap_ref, cap;
     std::vector<MeshTri> tris;    // static mesh (world coordinates)
     MeshTree tree;
     AABB aabb;
@@ -447,6 +451,7 @@ struct World {
     Body* addHull(const std::vector<V3>& pts, const std::vector<std::vector<int>>& faces, const Material& m, int movement, V3 pos);
     Body* addSphere(V3 center, double r, const Material& m, int movement, V3 pos);
     Body* addCylinder(V3 base, double r, double h, const Material& m, int movement, V3 pos);
+    Body* addCapsule(V3 bot, double r, double h, const Material& m, int movement, V3 pos);
     Body* finishBody(std::unique_ptr<Body> b, double mass, const V3& com, const M3& tensor);
     Body* addMesh(const std::vector<V3>& points, const std::vector<std::array<int, 3>>& tris, const Material& m);
     void placeBody(Body* b, double mass, const V3& com_geom, const M3& tensor);
@@ -472,6 +477,10 @@ Manifold satPolyCylinder(const Hull& a, uint32_t a_id, const Material& am, const
 Manifold sphereSphere(const SphereG& a, uint32_t a_id, const Material& am, const SphereG& b, uint32_t b_id, const Material& bm);
 Manifold sphereCylinder(const SphereG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm);
 Manifold cylinderCylinder(const CylG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm);
+Manifold sphereCapsule(const SphereG& a, uint32_t a_id, const Material& am, const CapG& b, uint32_t b_id, const Material& bm);
+Manifold capsuleCapsule(const CapG& a, uint32_t a_id, const Material& am, const CapG& b, uint32_t b_id, const Material& bm);
+Manifold satPolyCapsule(const Hull& a, uint32_t a_id, const Material& am, const CapG& b, uint32_t b_id, const Material& bm);
+Manifold capsuleCylinder(const CapG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm);
 Manifold flipped(Manifold m);
 std::vector<Manifold> meshCollide(const Body* convex, const Body* mesh);   // SAT_*Mesh (CollisionDetect.cpp:2648-2778)
 Manifold mergeManifold(const Manifold& a, const Manifold& b);              // merge_manifold (:2780-2793)   // normal negated, MagicID halves swapped (CollisionDetect.cpp:29-40)

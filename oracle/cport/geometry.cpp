@@ -757,6 +757,267 @@ Manifold cylinderCylinder(const CylG& a, uint32_t a_id, const Material& am, cons
     return out;
 }
 
+// --------------------------------------------------------------- capsules ----
+// getCapsuleExtrema (CollisionDetect.cpp:685-703): the two cap spheres
+static Extrema capsuleExtrema(const CapG& c, const V3& d) {
+    V3 off = c.axis * c.h / 2.0;
+    double v1 = d.dot(c.c + off);
+    double mn1 = v1 - c.r, mx1 = v1 + c.r;
+    double v2 = d.dot(c.c - off);
+    double mn2 = v2 - c.r, mx2 = v2 + c.r;
+    Extrema e;
+    e.max_v = std::max<double>(mx1, mx2);
+    e.min_v = std::min<double>(mn1, mn2);
+    e.min_id = e.max_id = -1;
+    return e;
+}
+
+// cylinderLengthwiseLineInDirection (CollisionDetect.cpp:346-351) for any
+// centre / axis / radius / height
+static void lineAlong(const V3& c, const V3& axis, double r, double h, const V3& n, V3* p1, V3* p2) {
+    V3 barrel = (n - axis * axis.dot(n)).normalize();
+    *p1 = c + barrel * r + 0.5 * h * axis;
+    *p2 = *p1 - h * axis;
+}
+
+// findCapsuleContactArea (CollisionDetect.cpp:376-390): the barrel line (ids
+// 0 = top cap, 1 = bottom cap) or the one cap point
+enum CapArea { CAP_BARREL, CAP_EDGE };
+static Area capsuleArea(const CapG& c, V3 n, V3 u, V3 w, CapArea* kind) {
+    Area a;
+    if (std::abs(c.axis.dot(n)) <= sinTol()) {
+        V3 l1, l2;
+        lineAlong(c.c, c.axis, c.r, c.h, n, &l1, &l2);
+        a.ps = {p2(l1.dot(u), l1.dot(w)), p2(l2.dot(u), l2.dot(w))};
+        a.ids = {0, 1};
+        a.surface = -1; a.origin = EDGE; *kind = CAP_BARREL;
+        return a;
+    }
+    if (n.dot(c.axis) > 0) {
+        V3 p = n * c.r + c.c + c.axis * c.h / 2.0;
+        a.ps = {p2(p.dot(u), p.dot(w))};
+        a.ids = {0};
+    } else {
+        V3 p = n * c.r + c.c - c.axis * c.h / 2.0;
+        a.ps = {p2(p.dot(u), p.dot(w))};
+        a.ids = {1};
+    }
+    a.surface = -1; a.origin = EDGE; *kind = CAP_EDGE;
+    return a;
+}
+
+// the contact of two parallel barrels (lengthwise lines clipped along a's
+// axis), as detectCapsuleCapsule / detectCapsuleCylinder /
+// detectCylinderCylinder build it
+static std::vector<ClipP> parallelBarrels(V3 a1, V3 a2, V3 b1, V3 b2, const V3& aa, const V3& ba, const V3& u, const V3& w) {
+    if (ba.dot(aa) < 0) std::swap(b1, b2);
+    double amx = a1.dot(aa), amn = a2.dot(aa), bmx = b1.dot(aa), bmn = b2.dot(aa);
+    V3 imx = (amx > bmx) ? b1 : a1;
+    V3 imn = (amn > bmn) ? a2 : b2;
+    return {ClipP{p2(u.dot(imx), w.dot(imx)), 0, 0x0, false}, ClipP{p2(u.dot(imn), w.dot(imn)), 0, 0x1, false}};
+}
+
+// detectSphereCapsule (CollisionDetect.cpp:868-935)
+Manifold sphereCapsule(const SphereG& a, uint32_t a_id, const Material& am, const CapG& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    out.max_pen = -1;
+    NormResult best = {-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    V3 ax = b.axis;
+    V3 diff = b.c - a.c;
+    V3 barrel = (diff - ax * ax.dot(diff)).normalize();
+    if (axisTest(sphereExtrema(a, barrel), capsuleExtrema(b, barrel), barrel, &best)) return out;
+    V3 cap1 = b.c + ax * b.h / 2.0;
+    V3 e1 = (cap1 - a.c).normalize();
+    if (axisTest(sphereExtrema(a, e1), capsuleExtrema(b, e1), e1, &best)) return out;
+    V3 cap2 = b.c - ax * b.h / 2.0;
+    V3 e2 = (cap2 - a.c).normalize();
+    if (axisTest(sphereExtrema(a, e2), capsuleExtrema(b, e2), e2, &best)) return out;
+    out.normal = best.n;
+    out.pts.push_back(mkPoint(a.c + out.normal * a.r, best.pen, am, bm, cidOf(a_id, b_id), 0));
+    out.max_pen = best.pen;
+    return out;
+}
+
+// detectCapsuleCapsule (CollisionDetect.cpp:1139-1334).  The axes are those
+// the reference tests, in its order: cap-centre pairs (top-top, bottom-top as
+// b top minus a bottom, bottom-bottom), each of a's caps against b's barrel,
+// b's caps against a's barrel (taken from b's centre), barrel-barrel.
+Manifold capsuleCapsule(const CapG& a, uint32_t a_id, const Material& am, const CapG& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    out.max_pen = -1;
+    NormResult best = {-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    V3 at = a.c + a.axis * a.h / 2.0, ab = a.c - a.axis * a.h / 2.0;
+    V3 bt = b.c + b.axis * b.h / 2.0, bb = b.c - b.axis * b.h / 2.0;
+    auto test = [&](const V3& n) { return axisTest(capsuleExtrema(a, n), capsuleExtrema(b, n), n, &best); };
+    if (test((bt - at).normalize())) return out;
+    if (test((bt - ab).normalize())) return out;
+    if (test((bb - ab).normalize())) return out;
+    {
+        V3 d = b.c - at;
+        if (test((d - b.axis * b.axis.dot(d)).normalize())) return out;
+    }
+    {
+        V3 d = b.c - ab;
+        if (test((d - b.axis * b.axis.dot(d)).normalize())) return out;
+    }
+    {
+        V3 d = b.c - bt;
+        if (test((d - a.axis * a.axis.dot(d)).normalize())) return out;
+    }
+    {
+        V3 d = b.c - bb;
+        if (test((d - a.axis * a.axis.dot(d)).normalize())) return out;
+    }
+    V3 bx = a.axis.cross(b.axis);
+    if (bx.mag2() > 0.00000001) {
+        bx = bx.normalize();
+        if (test(bx)) return out;
+    }
+    V3 n = best.n;
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    CapArea ak, bk;
+    Area ac = capsuleArea(a, n, u, w, &ak);
+    Area bc = capsuleArea(b, -n, u, w, &bk);
+    std::vector<ClipP> pool;
+    if (ak == CAP_BARREL && bk == CAP_BARREL && std::abs(a.axis.dot(b.axis)) > 0.995) {
+        V3 a1, a2, b1, b2;
+        lineAlong(a.c, a.axis, a.r, a.h, n, &a1, &a2);
+        lineAlong(b.c, b.axis, b.r, b.h, -n, &b1, &b2);
+        pool = parallelBarrels(a1, a2, b1, b2, a.axis, b.axis, u, w);
+    } else {
+        pool = clipContacts(ac, bc);
+    }
+    V3 amax = a.axis.dot(n) > 0 ? at + n * a.r : ab + n * a.r;
+    out = pointsFromPool(pool, u, w, n, amax.dot(n), best.pen, am, bm, cidOf(a_id, b_id));
+    out.normal = n;
+    out.max_pen = best.pen;
+    return out;
+}
+
+// SAT_PolyCapsule (CollisionDetect.cpp:1413-1561).  The reference places the
+// caps a full drum height from the centre here (:1436-1437) and tests each
+// edge's "bottom cap" axis against the top cap again (:1486-1488); both are
+// reproduced.
+Manifold satPolyCapsule(const Hull& a, uint32_t a_id, const Material& am, const CapG& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    out.max_pen = -1;
+    NormResult best = {-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    for (size_t f = 0; f < a.gv.size(); f++) {
+        if (a.g_redundant[f]) continue;
+        Extrema ea = recenter(a.g_cache[f], a.g_ref_val[f], a.gv[f].dot(a.pts[a.g_ref_idx[f]]));
+        if (axisTest(ea, capsuleExtrema(b, a.gv[f]), a.gv[f], &best)) return out;
+    }
+    V3 ax = b.axis;
+    V3 tcc = b.c + ax * b.h;
+    V3 bcc = b.c - ax * b.h;
+    double tv = tcc.dot(ax), bv = bcc.dot(ax);
+    for (const V3& p : a.pts) {
+        double v = p.dot(ax);
+        V3 n;
+        if (bv <= v && v <= tv) n = ((p - b.c) - ax * ax.dot(p - b.c)).normalize();
+        else if (v > tv) n = (p - tcc).normalize();
+        else n = (p - bcc).normalize();
+        if (axisTest(findExtrema(a, n), capsuleExtrema(b, n), n, &best)) return out;
+    }
+    for (auto& e : a.edges) {
+        V3 dir = (a.pts[e.second] - a.pts[e.first]).normalize();
+        for (int k = 0; k < 2; k++) {
+            V3 sample = a.pts[e.first] - tcc;
+            V3 n = (sample - dir * dir.dot(sample)).normalize();
+            if (axisTest(findExtrema(a, n), capsuleExtrema(b, n), n, &best)) return out;
+        }
+        V3 d = dir.cross(ax);
+        if (d.mag() < 0.00000000001) continue;
+        V3 n = d.normalize();
+        if (axisTest(findExtrema(a, n), capsuleExtrema(b, n), n, &best)) return out;
+    }
+    V3 n = best.n;
+    V3 amax = a.pts[best.a_id];
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    Area ac = contactArea(a, n, amax, best.a_id, u, w);
+    CapArea bk;
+    Area bc = capsuleArea(b, -n, u, w, &bk);
+    std::vector<ClipP> pool = clipContacts(ac, bc);
+    out = pointsFromPool(pool, u, w, n, amax.dot(n), best.pen, am, bm, cidOf(a_id, b_id));
+    out.normal = n;
+    out.max_pen = best.pen;
+    return out;
+}
+
+// detectCapsuleCylinder (CollisionDetect.cpp:1794-2002)
+Manifold capsuleCylinder(const CapG& a, uint32_t a_id, const Material& am, const CylG& b, uint32_t b_id, const Material& bm) {
+    Manifold out;
+    out.max_pen = -1;
+    NormResult best = {-1, -1, V3(), std::numeric_limits<double>::infinity()};
+    V3 aa = a.axis, ba = b.axis;
+    auto test = [&](const V3& n) { return axisTest(capsuleExtrema(a, n), cylinderExtrema(b, n), n, &best); };
+    if (test(ba)) return out;
+    const int nr = (int)b.top.size();
+    for (int i = 0; i < nr; i++) {
+        V3 ed = b.top[(i + 1) % nr] - b.top[i];
+        V3 dir = ed.cross(aa);
+        if (dir.mag() < 0.00000000001) continue;
+        if (test(dir.normalize())) return out;
+    }
+    V3 at = a.c + a.axis * a.h / 2.0, ab = a.c - a.axis * a.h / 2.0;
+    V3 tdc = b.c + ba * 0.5 * b.h;
+    {
+        V3 cp = diskExtremum(tdc, ba, b.r, (at - b.c).normalize());
+        if (test((cp - at).normalize())) return out;
+    }
+    {
+        V3 cp = diskExtremum(tdc, ba, b.r, (ab - b.c).normalize());
+        if (test((cp - ab).normalize())) return out;
+    }
+    V3 bdc = b.c - ba * 0.5 * b.h;
+    {
+        V3 cp = diskExtremum(bdc, ba, b.r, (at - b.c).normalize());
+        if (test((cp - at).normalize())) return out;
+    }
+    {
+        V3 cp = diskExtremum(bdc, ba, b.r, (ab - b.c).normalize());
+        if (test((cp - ab).normalize())) return out;
+    }
+    {
+        V3 d = b.c - at;
+        if (test((d - ba * ba.dot(d)).normalize())) return out;
+    }
+    {
+        V3 d = b.c - ab;
+        if (test((d - ba * ba.dot(d)).normalize())) return out;
+    }
+    V3 bx = aa.cross(ba);
+    if (bx.mag2() > 0.00000001) {
+        bx = bx.normalize();
+        if (test(bx)) return out;
+    }
+    V3 n = best.n;
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    CapArea ak;
+    CylArea bk;
+    Area ac = capsuleArea(a, n, u, w, &ak);
+    Area bc = cylinderArea(b, -n, u, w, &bk);
+    std::vector<ClipP> pool;
+    if (bk == CA_EDGE) {
+        pool = {ClipP{bc.ps[0], 0, 0x0, false}};
+    } else if (ak == CAP_BARREL && bk == CA_BARREL && std::abs(aa.dot(ba)) > 0.995) {
+        V3 a1, a2, b1, b2;
+        lineAlong(a.c, a.axis, a.r, a.h, n, &a1, &a2);
+        lineAlong(b.c, b.axis, b.r, b.h, -n, &b1, &b2);
+        pool = parallelBarrels(a1, a2, b1, b2, aa, ba, u, w);
+    } else {
+        pool = clipContacts(ac, bc);
+    }
+    V3 amax = a.axis.dot(n) > 0 ? at + n * a.r : ab + n * a.r;
+    out = pointsFromPool(pool, u, w, n, amax.dot(n), best.pen, am, bm, cidOf(a_id, b_id));
+    out.normal = n;
+    out.max_pen = best.pen;
+    return out;
+}
+
 // ------------------------------------------------------ mesh triangles ----
 // findTriangleExtrema (CollisionDetect.cpp:2004-2021)
 static Extrema triExtrema(const MeshTri& t, const V3& d) {
@@ -969,11 +1230,63 @@ static Manifold satCylinderTriangle(const CylG& a, uint32_t a_id, const Material
     return out;
 }
 
+// SAT_CapsuleTriangle (CollisionDetect.cpp:2278-2464).  The reference sets
+// its "bottom" cap centre with +h/2 as well (:2286), so both cap tests use the
+// top cap; reproduced.
+static Manifold satCapsuleTriangle(const CapG& a, uint32_t a_id, const Material& am, const MeshTri& b, const Material& bm, double penalty) {
+    Manifold out;
+    TriSat S;
+    V3 ax = a.axis;
+    V3 at = a.c + ax * a.h / 2.0;
+    V3 ab = a.c + ax * a.h / 2.0;
+    if (!S.take(b, capsuleExtrema(a, b.normal), triExtrema(b, b.normal), b.normal)) return out;
+    for (int i = 0; i < 3; i++) {
+        V3 dir = (b.ep2[i] - b.ep1[i]).cross(ax);
+        if (dir.mag() < 0.00000000001) continue;
+        V3 dn = dir.normalize();
+        if (!S.take(b, capsuleExtrema(a, dn), triExtrema(b, dn), dn)) return out;
+    }
+    for (int i = 0; i < 3; i++) {
+        V3 diff = b.v[i] - a.c;
+        V3 n = (diff - ax * ax.dot(diff)).normalize();
+        if (!S.take(b, capsuleExtrema(a, n), triExtrema(b, n), n)) return out;
+    }
+    for (const V3* cc : {&at, &ab})
+        for (int i = 0; i < 3; i++) {
+            V3 n = (b.v[i] - *cc).normalize();
+            if (!S.take(b, capsuleExtrema(a, n), triExtrema(b, n), n)) return out;
+        }
+    for (const V3* cc : {&at, &ab})
+        for (int i = 0; i < 3; i++) {
+            V3 dir = (b.ep2[i] - b.ep1[i]).normalize();
+            V3 sample = b.ep1[i] - *cc;
+            V3 n = (sample - dir * dir.dot(sample)).normalize();
+            if (!S.take(b, capsuleExtrema(a, n), triExtrema(b, n), n)) return out;
+        }
+    NormResult ng;
+    NormResult mp = S.choose(penalty, &ng);
+    V3 n = mp.n;
+    V3 amax = ax.dot(n) > 0 ? at + n * a.r : ab + n * a.r;
+    V3 bmax = b.v[ng.b_id];
+    V3 u, w;
+    n.perpBasis(&u, &w);
+    CapArea ak;
+    Area ac = capsuleArea(a, ng.n, u, w, &ak);
+    Area bc = triangleArea(b, -ng.n, bmax, ng.b_id, u, w);
+    std::vector<ClipP> pool;
+    if (ak == CAP_EDGE) pool = {ClipP{ac.ps[0], 0, 0x0, false}};
+    else pool = clipContacts(ac, bc);
+    out = pointsFromPool(pool, u, w, n, amax.dot(n), mp.pen, am, bm, cidOf(a_id, (uint32_t)b.id));
+    out.normal = n;
+    out.max_pen = mp.pen;
+    return out;
+}
+
 static double longest(const AABB& b) {
     return std::max<double>(b.mx.x - b.mn.x, std::max<double>(b.mx.y - b.mn.y, b.mx.z - b.mn.z));
 }
 
-// SAT_PolyMesh / SAT_SphereMesh / SAT_CylinderMesh (CollisionDetect.cpp:
+// SAT_PolyMesh / SAT_SphereMesh / SAT_CapsuleMesh / SAT_CylinderMesh (CollisionDetect.cpp:
 // 2648-2778) for a fixed mesh in world coordinates: candidate triangles from
 // the mesh tree in its traversal order, penalty 0 for polyhedra and
 // 0.15 min(longest AABB sides) otherwise
@@ -985,6 +1298,7 @@ std::vector<Manifold> meshCollide(const Body* c, const Body* m) {
         Manifold r;
         if (c->kind == K_HULL) r = satPolyTriangle(c->shape, c->id, c->mat, t, mm, 0 * std::min<double>(longest(c->aabb), longest(t.aabb)));
         else if (c->kind == K_SPHERE) r = satSphereTriangle(c->sph, c->id, c->mat, t, mm, 0.15 * std::min<double>(longest(c->aabb), longest(t.aabb)));
+        else if (c->kind == K_CAPSULE) r = satCapsuleTriangle(c->cap, c->id, c->mat, t, mm, 0.15 * std::min<double>(longest(c->aabb), longest(t.aabb)));
         else r = satCylinderTriangle(c->cyl, c->id, c->mat, t, mm, 0.15 * std::min<double>(longest(c->aabb), longest(t.aabb)));
         if (r.max_pen > 0 && !r.pts.empty()) out.push_back(r);
     }

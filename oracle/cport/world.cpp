@@ -28,6 +28,13 @@ static AABB genAABB(const SphereG& s) {
     return AABB{s.c - V3(s.r, s.r, s.r), s.c + V3(s.r, s.r, s.r)};
 }
 
+// Capsule::gen_AABB (ConvexPrimitive.cpp:390-401)
+static AABB genAABB(const CapG& c) {
+    V3 v = c.axis * c.h / 2.0;
+    double dx = std::abs(v.x) + c.r, dy = std::abs(v.y) + c.r, dz = std::abs(v.z) + c.r;
+    return AABB{V3(c.c.x - dx, c.c.y - dy, c.c.z - dz), V3(c.c.x + dx, c.c.y + dy, c.c.z + dz)};
+}
+
 // Cylinder::gen_AABB (ConvexPrimitive.cpp:289-298): the two cap 8-gons,
 // interleaved top/bottom as the reference collects them
 static AABB genAABB(const CylG& c) {
@@ -67,6 +74,12 @@ void Body::updateGeometry() {
     if (kind == K_CYLINDER) {
         cylFromReference(cyl, cyl_ref, rot, com);
         aabb = genAABB(cyl);
+        return;
+    }
+    if (kind == K_CAPSULE) {
+        cap.c = com + rot * cap_ref.c;            // Capsule::recomputeFromReference (ConvexPrimitive.cpp:383-388)
+        cap.axis = rot * cap_ref.axis;
+        aabb = genAABB(cap);
         return;
     }
     for (size_t i = 0; i < shape.pts.size(); i++) shape.pts[i] = com + rot * ref_shape.pts[i];
@@ -169,6 +182,17 @@ static void primitiveMass(const Body& b, double* mass, V3* com, M3* tensor) {
         c = b.sph_src.c;
         double k = 2.0 / 5.0 * m * r * r;
         local = k * M3::iden();
+    } else if (b.kind == K_CAPSULE) {
+        // RigidBody.cpp:570-600 (the mass is the volume: the density scales
+        // only the tensor there); the height axis is +y, no rotation
+        double h = b.cap_src.h, r = b.cap_src.r;
+        double r3 = r * r * r, r4 = r3 * r, r5 = r4 * r;
+        double d = b.mat.density;
+        m = (4.0 / 3.0) * PI_TRUNC * r * r * r + PI_TRUNC * r * r * h;
+        c = b.cap_src.c;
+        local.m[0][0] = d * PI_TRUNC * ((8.0 / 15.0) * r5 + (1.0 / 3.0) * r3 * h * h + 0.75 * r4 * h + (1.0 / 12.0) * r * r * h * h * h);
+        local.m[1][1] = d * PI_TRUNC * ((8.0 / 15.0) * r5 + 0.5 * h * r4);
+        local.m[2][2] = local.m[0][0];
     } else {
         double h = b.cyl_src.h, r = b.cyl_src.r;
         m = PI_TRUNC * r * r * h * b.mat.density;
@@ -212,6 +236,23 @@ Body* World::addCylinder(V3 base, double r, double h, const Material& m, int mov
     return finishBody(std::move(b), mass, com, tensor);
 }
 
+// ConvexUnionGeometry::capsule (Geometry.cpp:43-45): `bot` is the centre of
+// the bottom cap sphere, the height axis +y
+Body* World::addCapsule(V3 bot, double r, double h, const Material& m, int movement, V3 pos) {
+    auto b = std::make_unique<Body>();
+    b->kind = K_CAPSULE;
+    b->movement = movement;
+    b->mat = m;
+    b->cap_src.c = bot + V3(0, h / 2.0, 0);
+    b->cap_src.axis = V3(0, 1, 0);
+    b->cap_src.r = r;
+    b->cap_src.h = h;
+    b->create_pos = pos;
+    double mass; V3 com; M3 tensor;
+    primitiveMass(*b, &mass, &com, &tensor);
+    return finishBody(std::move(b), mass, com, tensor);
+}
+
 Body* World::finishBody(std::unique_ptr<Body> b, double mass, const V3& com, const M3& tensor) {
     b->id = (uint32_t)bodies.size() + 1;
     Body* raw = b.get();
@@ -245,6 +286,12 @@ void World::placeBody(Body* b, double mass, const V3& com_geom, const M3& tensor
         cylFromReference(b->cyl_ref, b->cyl_src, I, mc);
         b->cyl = b->cyl_src;
         b->aabb = genAABB(b->cyl);
+    } else if (b->kind == K_CAPSULE) {
+        b->cap_ref = b->cap_src;
+        b->cap_ref.c = mc + I * b->cap_src.c;
+        b->cap_ref.axis = I * b->cap_src.axis;
+        b->cap = b->cap_src;
+        b->aabb = genAABB(b->cap);
     } else {
         b->ref_shape = b->src_shape;
         for (V3& p : b->ref_shape.pts) p = mc + I * p;
@@ -737,15 +784,24 @@ static Manifold collide(const Body* b1, const Body* b2) {
     if (k1 == K_HULL) {
         if (k2 == K_HULL) return satPolyPoly(b1->shape, i1, m1, b2->shape, i2, m2);
         if (k2 == K_SPHERE) return satPolySphere(b1->shape, i1, m1, b2->sph, i2, m2);
+        if (k2 == K_CAPSULE) return satPolyCapsule(b1->shape, i1, m1, b2->cap, i2, m2);
         return satPolyCylinder(b1->shape, i1, m1, b2->cyl, i2, m2);
     }
     if (k1 == K_SPHERE) {
         if (k2 == K_HULL) return flipped(satPolySphere(b2->shape, i2, m2, b1->sph, i1, m1));
         if (k2 == K_SPHERE) return sphereSphere(b1->sph, i1, m1, b2->sph, i2, m2);
+        if (k2 == K_CAPSULE) return sphereCapsule(b1->sph, i1, m1, b2->cap, i2, m2);
         return sphereCylinder(b1->sph, i1, m1, b2->cyl, i2, m2);
+    }
+    if (k1 == K_CAPSULE) {
+        if (k2 == K_HULL) return flipped(satPolyCapsule(b2->shape, i2, m2, b1->cap, i1, m1));
+        if (k2 == K_SPHERE) return flipped(sphereCapsule(b2->sph, i2, m2, b1->cap, i1, m1));
+        if (k2 == K_CAPSULE) return capsuleCapsule(b1->cap, i1, m1, b2->cap, i2, m2);
+        return capsuleCylinder(b1->cap, i1, m1, b2->cyl, i2, m2);
     }
     if (k2 == K_HULL) return flipped(satPolyCylinder(b2->shape, i2, m2, b1->cyl, i1, m1));
     if (k2 == K_SPHERE) return flipped(sphereCylinder(b2->sph, i2, m2, b1->cyl, i1, m1));
+    if (k2 == K_CAPSULE) return flipped(capsuleCylinder(b2->cap, i2, m2, b1->cyl, i1, m1));
     return cylinderCylinder(b1->cyl, i1, m1, b2->cyl, i2, m2);
 }
 
@@ -962,6 +1018,14 @@ int cport_body_cylinder(cpgpu_world* w, const double base[3], double radius, dou
                         int movement, const double pos[3], uint32_t* out_id) {
     if (!(radius > 0) || !(height > 0)) return fail("cylinder radius and height must be > 0");
     Body* b = W(w)->addCylinder(v3(base), radius, height, mat(m), movement, v3(pos));
+    if (out_id) *out_id = b->id;
+    return CPGPU_OK;
+}
+// ConvexUnionGeometry::capsule (Geometry.cpp:43-45)
+int cport_body_capsule(cpgpu_world* w, const double bot[3], double radius, double drum_height, const cpgpu_material* m,
+                       int movement, const double pos[3], uint32_t* out_id) {
+    if (!(radius > 0) || !(drum_height >= 0)) return fail("capsule radius must be > 0 and drum height >= 0");
+    Body* b = W(w)->addCapsule(v3(bot), radius, drum_height, mat(m), movement, v3(pos));
     if (out_id) *out_id = b->id;
     return CPGPU_OK;
 }

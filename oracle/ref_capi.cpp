@@ -217,6 +217,13 @@ int cpref_body_cylinder(cpgpu_world* w, const double base[3], double radius, dou
     return finish_body(RW, r, out_id);
 }
 
+int cpref_body_capsule(cpgpu_world* w, const double bot[3], double radius, double drum_height,
+                       const cpgpu_material* mat, int movement, const double pos[3], uint32_t* out_id) {
+    phyz::ConvexUnionGeometry g = phyz::ConvexUnionGeometry::capsule(v3(bot), radius, drum_height, to_mat(mat));
+    phyz::RigidBody* r = RW->engine.createRigidBody(g, (phyz::RigidBody::MovementType)movement, v3(pos));
+    return finish_body(RW, r, out_id);
+}
+
 int cpref_body_mesh(cpgpu_world* w, const double* points, int n_points, const int* tris, int n_tris,
                     const cpgpu_material* mat, int fixed, uint32_t* out_id) {
     phyz::MeshInput in;

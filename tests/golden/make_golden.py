@@ -2,7 +2,7 @@
 
 Runs the reference (oracle/_ref/libcpref.so, built from the reference's own
 sources) on seeded scenes and stores the resulting states and contacts.
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [fixture function ...]
 """
 import os
 import sys
@@ -78,7 +78,27 @@ def terrain():
                         magic_b=c["magic_b"])
 
 
-def main():
+def capsules():
+    """Capsules with boxes, spheres, cylinders and hulls on a 16 x 16
+    value-noise terrain (scenes.capsule_drop, seed 5, 3x3x2) after 150
+    reference steps, with creation-time mass properties."""
+    steps = 150
+    sc = scenes.capsule_drop(seed=5, n_side=3, n_layers=2, terrain=True, n_grid=16)
+    mass, com, tensor, w = oracle.capture_mass_properties(sc)
+    w.step(steps)
+    st = w.state()
+    c = w.contacts()
+    np.savez_compressed(os.path.join(HERE, "capsule_terrain_seed5.npz"), steps=steps, mass=mass, com_geom=com,
+                        tensor=tensor, com=st["com"], quat=st["quat"], vel=st["vel"], ang_vel=st["ang_vel"],
+                        magic_c=c["magic_c"], magic_b=c["magic_b"], b1=c["b1"], b2=c["b2"])
+
+
+def main(names=()):
+    if names:
+        for n in names:
+            globals()[n]()
+        return
+    capsules()
     terrain()
     chain()
     mixed()
@@ -94,4 +114,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

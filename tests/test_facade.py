@@ -12,17 +12,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 
 
-def _build(tmp_path):
-    exe = str(tmp_path / "facade_box_drop")
+def _build(tmp_path, name="facade_box_drop"):
+    exe = str(tmp_path / name)
     lib_dir = os.path.dirname(cg.LIB_PATH)
-    cmd = ["g++", "-std=c++17", "-O1", "-I" + os.path.join(REPO, "include"), os.path.join(HERE, "cxx", "facade_box_drop.cpp"),
+    cmd = ["g++", "-std=c++17", "-O1", "-I" + os.path.join(REPO, "include"), os.path.join(HERE, "cxx", name + ".cpp"),
            "-L" + lib_dir, "-lcpgpu", "-Wl,-rpath," + lib_dir, "-o", exe]
     subprocess.run(cmd, check=True, capture_output=True)
     return exe
 
 
-def test_facade_compiles_and_fails_loudly_without_gpu(tmp_path):
-    exe = _build(tmp_path)
+@pytest.mark.parametrize("name", ["facade_box_drop", "facade_primitives_drop"])
+def test_facade_compiles_and_fails_loudly_without_gpu(tmp_path, name):
+    exe = _build(tmp_path, name)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode in (0, 2), r.stdout + r.stderr
     if r.returncode == 2:
@@ -30,7 +31,8 @@ def test_facade_compiles_and_fails_loudly_without_gpu(tmp_path):
 
 
 @pytest.mark.gpu
-def test_facade_box_drop_on_device(tmp_path):
-    exe = _build(tmp_path)
+@pytest.mark.parametrize("name", ["facade_box_drop", "facade_primitives_drop"])
+def test_facade_box_drop_on_device(tmp_path, name):
+    exe = _build(tmp_path, name)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr

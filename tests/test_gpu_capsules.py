@@ -1,0 +1,242 @@
+"""Capsules on the device path against the oracle, on a GB300.
+
+Same method as test_gpu_primitives: the device state and contact graph after k
+steps are imported into the CPU restatement (itself pinned bit for bit to the
+reference on capsule scenes, tests/test_oracle.py), both advance one step, and
+the results are compared (FP32 device vs FP64 restatement; tolerances written
+at each assertion).  Single-pair scenes cover every capsule detector and both
+dispatch orders: SAT_PolyCapsule (barrel line and cap point on a face),
+detectSphereCapsule, detectCapsuleCapsule (crossed and parallel barrels),
+detectCapsuleCylinder, SAT_CapsuleTriangle on a terrain mesh.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import constraintphysics_gb300 as cg
+from constraintphysics_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+MAT = scenes.PILE_MATERIAL
+D, F = scenes.DYNAMIC, scenes.FIXED
+R, H = 0.3, 1.0   # capsule radius and drum height of the single-pair scenes
+
+
+def _quat(axis, deg):
+    a = np.asarray(axis, dtype=np.float64)
+    a = a / np.linalg.norm(a)
+    h = math.radians(deg) / 2
+    return (math.cos(h), *(a * math.sin(h)))
+
+
+def _scene(name):
+    sc = scenes.Scene(name, scenes.DROP_PARAMS)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, MAT, F)   # plate, top at y = 0
+    return sc
+
+
+def _capsule(sc, pos, q=None, r=R, h=H, movement=D):
+    b = sc.capsule((0.0, -h / 2, 0.0), r, h, MAT, movement, pos)
+    if q is not None:
+        sc.orient(b, q)
+    return b
+
+
+LYING_X = _quat((0, 0, 1), 90)   # height axis along x
+LYING_Z = _quat((1, 0, 0), 90)   # height axis along z
+
+
+def case_capsule_lying():
+    sc = _scene("capsule_lying")
+    _capsule(sc, (0.0, R - 0.01, 0.0), LYING_X)
+    return sc
+
+
+def case_capsule_standing():
+    sc = _scene("capsule_standing")
+    _capsule(sc, (0.0, H / 2 + R - 0.01, 0.0))
+    return sc
+
+
+def case_capsule_tilted():
+    sc = _scene("capsule_tilted")
+    _capsule(sc, (0.0, H / 2 * math.cos(math.radians(30)) + R - 0.01, 0.0), _quat((1, 0, 0), 30))
+    return sc
+
+
+def case_sphere_on_capsule():
+    sc = _scene("sphere_on_capsule")
+    _capsule(sc, (0.0, R - 0.01, 0.0), LYING_X)
+    sc.sphere((0.0, 0.0, 0.0), 0.4, MAT, D, (0.1, 2 * R + 0.4 - 0.02, 0.05))
+    return sc
+
+
+def case_capsule_on_sphere():
+    # the capsule has the lower id: the sphere-capsule detector runs flipped
+    sc = _scene("capsule_on_sphere")
+    _capsule(sc, (0.05, 0.49 + 0.5 + R - 0.01, 0.0), LYING_X)
+    sc.sphere((0.0, 0.0, 0.0), 0.5, MAT, D, (0.0, 0.49, 0.0))
+    return sc
+
+
+def case_capsules_crossed():
+    sc = _scene("capsules_crossed")
+    _capsule(sc, (0.0, R - 0.01, 0.0), LYING_X)
+    _capsule(sc, (0.05, 3 * R - 0.03, 0.02), LYING_Z)
+    return sc
+
+
+def case_capsules_parallel():
+    sc = _scene("capsules_parallel")
+    _capsule(sc, (0.0, R - 0.01, 0.0), LYING_X)
+    _capsule(sc, (0.4, 3 * R - 0.03, 0.01), LYING_X)
+    return sc
+
+
+def case_capsule_on_cylinder():
+    sc = _scene("capsule_on_cylinder")
+    _capsule(sc, (0.05, 0.49 + 0.5 + R - 0.01, 0.02), LYING_X)
+    sc.cylinder((0.0, -0.5, 0.0), 0.5, 1.0, MAT, D, (0.0, 0.49, 0.0))
+    return sc
+
+
+def case_cylinder_under_capsule_end():
+    # the cylinder has the lower id (flipped detector); the capsule's cap rests on its rim region
+    sc = _scene("cylinder_under_capsule_end")
+    sc.cylinder((0.0, -0.5, 0.0), 0.5, 1.0, MAT, D, (0.0, 0.49, 0.0))
+    # height axis (-sin 70, cos 70, 0); the bottom cap sphere sits on the top face near the rim
+    s70, c70 = math.sin(math.radians(70)), math.cos(math.radians(70))
+    bot = np.array([0.4, 0.99 + R - 0.01, 0.0])
+    _capsule(sc, tuple(bot + np.array([-s70, c70, 0.0]) * (H / 2)), _quat((0, 0, 1), 70))
+    return sc
+
+
+CASES = [case_capsule_lying, case_capsule_standing, case_capsule_tilted, case_sphere_on_capsule,
+         case_capsule_on_sphere, case_capsules_crossed, case_capsules_parallel, case_capsule_on_cylinder,
+         case_cylinder_under_capsule_end]
+
+
+def _step_both(sc, k, oracle_mod):
+    g = cg.world()
+    scenes.apply(sc, g)
+    g.step(k)
+    p = oracle_mod.port_world()
+    scenes.apply(sc, p)
+    if k > 0:
+        p.set_state(**g.state())
+        p.set_contacts(g.contacts())
+    g.step(1)
+    p.step(1)
+    return g, p
+
+
+def _fresh_points(c):
+    m = c["memory_life"] == 5   # detected in the last step
+    out = {}
+    for i in np.nonzero(m)[0]:
+        out[(int(c["b1"][i]), int(c["b2"][i]), int(c["magic_b"][i]))] = (c["p_local_b1"][i], c["n_local_b1"][i],
+                                                                           float(c["pen_depth"][i]))
+    return out
+
+
+def _match(cg_, cp_, tol=2e-4):
+    """Contacts detected in the last step on both sides, paired by MagicID or
+    else by position within `tol` (a clipping near-tie can give the same point
+    another id).  Returns (by id, count by position, unmatched restatement,
+    unmatched device)."""
+    G, P = _fresh_points(cg_), _fresh_points(cp_)
+    by_id = [k for k in P if k in G]
+    rest_g = [k for k in G if k not in P]
+    used, unmatched = set(), []
+    for k in (k for k in P if k not in G):
+        near = [j for j in rest_g if j[:2] == k[:2] and j not in used and np.abs(G[j][0] - P[k][0]).max() <= tol]
+        if near:
+            used.add(near[0])
+        else:
+            unmatched.append(k)
+    return by_id, len(used), unmatched, [j for j in rest_g if j not in used]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda f: f.__name__[5:])
+@pytest.mark.parametrize("k", [0, 20])
+def test_capsule_pair_parity(oracle_mod, case, k):
+    g, p = _step_both(case(), k, oracle_mod)
+    assert np.array_equal(g.pairs(), p.pairs())
+    cg_, cp_ = g.contacts(), p.contacts()
+    by_id, by_pos, miss_p, miss_g = _match(cg_, cp_)
+    assert len(by_id) + by_pos > 0
+    assert not miss_p and not miss_g, (miss_p, miss_g)
+    pg, pp = _fresh_points(cg_), _fresh_points(cp_)
+    for key in by_id:
+        assert np.abs(pg[key][0] - pp[key][0]).max() <= 2e-4, (key, pg[key][0], pp[key][0])   # m, local point
+        assert np.abs(pg[key][1] - pp[key][1]).max() <= 1e-4, (key, pg[key][1], pp[key][1])   # local normal
+        assert abs(pg[key][2] - pp[key][2]) <= 2e-4, key                                       # m, depth
+    sg, sp = g.state(), p.state()
+    dv_max, dw_max = (1e-4, 1e-3) if by_pos == 0 else (1e-2, 5e-2)
+    assert np.abs(sg["vel"] - sp["vel"]).max() <= dv_max        # m/s
+    assert np.abs(sg["ang_vel"] - sp["ang_vel"]).max() <= dw_max  # rad/s
+    assert np.abs(sg["com"] - sp["com"]).max() <= 2e-4           # m
+
+
+@pytest.mark.parametrize("terrain,k", [(False, 80), (False, 150), (True, 100), (True, 150)])
+def test_single_step_parity_capsule_drop(oracle_mod, terrain, k):
+    """Capsules among every other primitive, on the plate or a terrain mesh:
+    after k device steps, one step on both sides agrees contact for contact
+    (by id or by position) and in the velocities of the bodies."""
+    sc = scenes.capsule_drop(seed=3, n_side=4, n_layers=2, terrain=terrain)
+    g, p = _step_both(sc, k, oracle_mod)
+    assert np.array_equal(g.pairs(), p.pairs())
+    cg_, cp_ = g.contacts(), p.contacts()
+    by_id, by_pos, miss_p, miss_g = _match(cg_, cp_)
+    n = len(by_id) + by_pos + len(miss_p)
+    assert n > 10
+    assert len(miss_p) + len(miss_g) <= 0.05 * n, (len(by_id), by_pos, len(miss_p), len(miss_g))
+    sg, sp = g.state(), p.state()
+    dv = np.linalg.norm(sg["vel"] - sp["vel"], axis=1)
+    vm = np.linalg.norm(sp["vel"], axis=1)
+    stats = f"median {np.median(dv):.2e} max {dv.max():.2e} ties {by_pos}"
+    assert np.median(dv) <= 1e-5, stats                          # m/s
+    assert np.mean(dv <= 1e-4 + 1e-3 * vm) >= 0.9, stats
+    assert dv.max() <= 0.1, stats   # m/s, warm-start loss at a near-tie
+
+
+def test_trajectory_drift_capsules(oracle_mod):
+    """Separate capsules (standing, lying, tilted) dropped on the plate: after
+    300 steps the device and the restatement agree within 1e-3 m."""
+    sc = _scene("capsule_drops")
+    _capsule(sc, (-3.0, 2.0, 0.0))
+    _capsule(sc, (0.0, 2.0, 0.0), LYING_X)
+    _capsule(sc, (3.0, 2.0, 0.0), _quat((1, 0, 1), 35))
+    g = cg.world()
+    scenes.apply(sc, g)
+    p = oracle_mod.port_world()
+    scenes.apply(sc, p)
+    g.step(300)
+    p.step(300)
+    err = np.abs(g.state()["com"] - p.state()["com"]).max()
+    assert err <= 1e-3, err
+    assert g.state()["com"][1:, 1].max() < 1.5   # landed
+
+
+def test_capsule_batch_equals_single_worlds():
+    """Worlds with capsules batched together step exactly as they do alone."""
+    scs = [scenes.capsule_drop(seed=s, n_side=3, n_layers=2, terrain=(s == 1)) for s in range(3)]
+    singles = []
+    for sc in scs:
+        w = cg.world()
+        scenes.apply(sc, w)
+        w.step(60)
+        singles.append(w.state())
+    ws = []
+    for sc in scs:
+        w = cg.world()
+        scenes.apply(sc, w)
+        ws.append(w)
+    b = cg.Batch(ws)
+    b.step(60)
+    for i, st in enumerate(singles):
+        bs = b.state(i)
+        for key in ("com", "quat", "vel", "ang_vel"):
+            assert np.array_equal(bs[key], st[key]), (i, key)

@@ -287,3 +287,76 @@ def test_golden_fixture_terrain(oracle_mod):
     c = p.contacts()
     assert np.array_equal(_tri_ids(c), np.where(c["b1"] == 1, g["magic_c"] & 0xFFFFFFFF, 0))
     assert np.array_equal(c["magic_b"], g["magic_b"])
+
+
+@pytest.mark.parametrize("terrain", [False, True])
+def test_restatement_bitwise_on_capsules(oracle_mod, terrain):
+    """Capsules with every other primitive, on the plate or on a terrain
+    mesh (SAT_PolyCapsule, detectSphereCapsule, detectCapsuleCapsule,
+    detectCapsuleCylinder, SAT_CapsuleTriangle): bit-identical to the
+    reference, and every capsule pair kind occurs."""
+    sc = scenes.capsule_drop(seed=3, n_side=4, n_layers=2, terrain=terrain)
+    kinds = [op[0] for op in sc.ops if op[0] in ("hull", "box", "sphere", "cylinder", "capsule", "mesh")]
+    r, p = oracle_mod.twin_worlds(sc)
+    seen = set()
+    for s in range(150):
+        r.step(1)
+        p.step(1)
+        c = r.contacts()
+        for a, b in zip(c["b1"].tolist(), c["b2"].tolist()):
+            seen.add(tuple(sorted((kinds[a - 1].replace("box", "hull"), kinds[b - 1].replace("box", "hull")))))
+        if s % 25 == 24:
+            assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
+    cr, cp = r.contacts(), p.contacts()
+    for k in ("b1", "b2", "magic_b", "normal_impulse", "pen_depth"):
+        assert np.array_equal(cr[k], cp[k]), k
+    want = {("capsule", "capsule"), ("capsule", "hull"), ("capsule", "sphere"), ("capsule", "cylinder")}
+    if terrain:
+        want.add(("capsule", "mesh"))
+    else:
+        assert ("capsule", "hull") in seen   # the plate
+    assert want <= seen, seen
+
+
+def test_capsule_mass_properties_agree(oracle_mod):
+    """Capsule mass properties (RigidBody.cpp:570-600: the mass is the volume,
+    the density scales only the tensor) restated within rounding."""
+    sc = scenes.Scene("capsules", dict(step_time=1.0 / 60.0))
+    dense = dict(scenes.PILE_MATERIAL, density=2.5)
+    for i, (r_, h_) in enumerate(((0.3, 0.8), (0.5, 0.0), (0.25, 1.7))):
+        sc.capsule((float(i), -h_ / 2, 0.0), r_, h_, dense, scenes.DYNAMIC, (3.0 * i, 2.0, 0.0))
+    r, p = oracle_mod.ref_world(), oracle_mod.port_world()
+    scenes.apply(sc, r)
+    scenes.apply(sc, p)
+    get_r = oracle_mod.ref_abi()._lib.cpref_get_mass_properties
+    get_p = oracle_mod.port_abi()._lib.cport_get_mass_properties
+    for f in (get_r, get_p):
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    for bid in range(1, sc.n_bodies + 1):
+        out = []
+        for f, w in ((get_r, r), (get_p, p)):
+            m, c, t = np.zeros(1), np.zeros(3), np.zeros(9)
+            assert f(w.h, bid, m.ctypes.data, c.ctypes.data, t.ctypes.data) == 0
+            out.append((m, c, t))
+        (mr, cr, tr), (mp, cp, tp) = out
+        assert abs(mr[0] - mp[0]) <= 1e-12 * mr[0]
+        assert np.abs(cr - cp).max() <= 1e-12 * (1 + np.abs(cr).max())
+        assert np.abs(tr - tp).max() <= 1e-10 * np.abs(tr).max()
+
+
+def test_golden_fixture_capsules(oracle_mod):
+    """Capsules on the terrain against the committed reference outputs (no
+    reference library needed)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "capsule_terrain_seed5.npz"))
+    sc = scenes.capsule_drop(seed=5, n_side=3, n_layers=2, terrain=True, n_grid=16)
+    p = oracle_mod.port_world_with_mass(sc, g["mass"], g["com_geom"], g["tensor"])
+    p.step(int(g["steps"]))
+    st = p.state()
+    for k in ("com", "quat", "vel", "ang_vel"):
+        assert np.array_equal(st[k], g[k]), k
+    c = p.contacts()
+    assert np.array_equal(c["b1"], g["b1"]) and np.array_equal(c["b2"], g["b2"])
+    assert np.array_equal(_tri_ids(c), np.where(c["b1"] == 1, g["magic_c"] & 0xFFFFFFFF, 0))
+    assert np.array_equal(c["magic_b"], g["magic_b"])
