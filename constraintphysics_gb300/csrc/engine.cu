@@ -1424,7 +1424,6 @@ static Body& body_ref(World& w, uint32_t id) {
 static uint32_t add_hull(World& w, const std::vector<D3>& pts, const std::vector<std::vector<int>>& faces,
                          const cpgpu_material* m, int movement, const double* pos) {
     if (movement < 0 || movement > 2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad movement type"};
-    if (movement == CPGPU_KINEMATIC) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "kinematic bodies are not implemented on the device path"};
     HullPrep h;
     if (pts.size() < 4 || faces.size() < 4 || !h.build(pts, faces)) throw ApiFail{CPGPU_ERR_INVALID_ARG, "invalid hull"};
     Body b;
@@ -1482,7 +1481,6 @@ static void prim_mass(uint32_t kind, const D3& c, double r, double h, double den
 static uint32_t add_prim(World& w, uint32_t kind, const D3& center, double r, double h, const cpgpu_material* m,
                          int movement, const double* pos) {
     if (movement < 0 || movement > 2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad movement type"};
-    if (movement == CPGPU_KINEMATIC) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "kinematic bodies are not implemented on the device path"};
     if (!(r > 0) || (kind == SHAPE_CYLINDER && !(h > 0)) || (kind == SHAPE_CAPSULE && !(h >= 0)))
         throw ApiFail{CPGPU_ERR_INVALID_ARG, "radius must be > 0, cylinder height > 0, capsule drum height >= 0"};
     Body b;

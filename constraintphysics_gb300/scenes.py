@@ -119,6 +119,9 @@ class Scene:
     def velocity(self, bid, v):
         self.ops.append(("vel", bid, tuple(v)))
 
+    def ang_velocity(self, bid, w):
+        self.ops.append(("angvel", bid, tuple(w)))
+
     def movements(self):
         """Movement type of each body, in id order."""
         slot = {"hull": 4, "box": 6, "sphere": 4, "cylinder": 5, "capsule": 5}
@@ -147,6 +150,8 @@ def apply(scene, world):
             world.set_orientation(op[1], op[2])
         elif kind == "vel":
             world.set_velocity(op[1], op[2])
+        elif kind == "angvel":
+            world.set_ang_velocity(op[1], op[2])
         elif kind == "mass":
             world.set_mass(op[1], op[2])
         elif kind == "ball":
@@ -387,6 +392,26 @@ def capsule_drop(seed=0, n_side=4, n_layers=2, terrain=False, n_grid=16, spacing
                     p_, f_ = random_hull(rng, 12, 32)
                     bid = sc.hull(p_, f_, PILE_MATERIAL, DYNAMIC, pos)
                 sc.orient(bid, random_quat(rng))
+    return sc
+
+
+def kinematic_push(seed=0):
+    """Kinematic bodies (RigidBody::KINEMATIC: infinite mass, moved by their
+    own velocity) among dynamic ones: a long box sliding at 1 m/s into a row
+    of stacked boxes, and a wide cylinder spinning about +y at 1.5 rad/s
+    under a sphere and a capsule."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(f"kinematic_push_seed{seed}", DROP_PARAMS)
+    sc.box((-20.0, -1.0, -20.0), 40.0, 1.0, 40.0, PILE_MATERIAL, FIXED)
+    pusher = sc.box((-0.5, -0.5, -2.0), 1.0, 1.0, 4.0, PILE_MATERIAL, KINEMATIC, (-4.0, 0.5, 0.0))
+    sc.velocity(pusher, (1.0, 0.0, 0.0))
+    spin = sc.cylinder((0.0, -0.25, 0.0), 2.0, 0.5, PILE_MATERIAL, KINEMATIC, (5.0, 0.25, 0.0))
+    sc.ang_velocity(spin, (0.0, 1.5, 0.0))
+    for i in range(6):
+        pos = np.array([-1.0 + 0.9 * (i % 3), 0.4 + 0.85 * (i // 3), 0.3 * (i % 2)]) + rng.uniform(-0.02, 0.02, 3)
+        sc.box((-0.4, -0.4, -0.4), 0.8, 0.8, 0.8, PILE_MATERIAL, DYNAMIC, pos)
+    sc.sphere((0.0, 0.0, 0.0), 0.4, PILE_MATERIAL, DYNAMIC, (5.5, 1.0, 0.5))
+    sc.capsule((0.0, -0.4, 0.0), 0.25, 0.8, PILE_MATERIAL, DYNAMIC, (4.2, 1.2, -0.6))
     return sc
 
 
