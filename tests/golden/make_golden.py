@@ -93,11 +93,27 @@ def capsules():
                         magic_c=c["magic_c"], magic_b=c["magic_b"], b1=c["b1"], b2=c["b2"])
 
 
+def kinematic():
+    """A kinematic pusher and spinner among dynamic bodies
+    (scenes.kinematic_push, seed 1) after 240 reference steps, with
+    creation-time mass properties."""
+    steps = 240
+    sc = scenes.kinematic_push(seed=1)
+    mass, com, tensor, w = oracle.capture_mass_properties(sc)
+    w.step(steps)
+    st = w.state()
+    c = w.contacts()
+    np.savez_compressed(os.path.join(HERE, "kinematic_push_seed1.npz"), steps=steps, mass=mass, com_geom=com,
+                        tensor=tensor, com=st["com"], quat=st["quat"], vel=st["vel"], ang_vel=st["ang_vel"],
+                        magic_b=c["magic_b"], b1=c["b1"], b2=c["b2"], normal_impulse=c["normal_impulse"])
+
+
 def main(names=()):
     if names:
         for n in names:
             globals()[n]()
         return
+    kinematic()
     capsules()
     terrain()
     chain()

@@ -381,3 +381,19 @@ def test_restatement_bitwise_with_kinematic_bodies(oracle_mod):
     assert ((cr["b1"] == 2) | (cr["b2"] == 2)).any()            # the pusher touches the boxes
     for k in ("b1", "b2", "magic_b", "normal_impulse", "pen_depth"):
         assert np.array_equal(cr[k], cp[k]), k
+
+
+def test_golden_fixture_kinematic(oracle_mod):
+    """The kinematic scene against the committed reference outputs (no
+    reference library needed)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "kinematic_push_seed1.npz"))
+    sc = scenes.kinematic_push(seed=1)
+    p = oracle_mod.port_world_with_mass(sc, g["mass"], g["com_geom"], g["tensor"])
+    p.step(int(g["steps"]))
+    st = p.state()
+    for k in ("com", "quat", "vel", "ang_vel"):
+        assert np.array_equal(st[k], g[k]), k
+    c = p.contacts()
+    for k in ("b1", "b2", "magic_b", "normal_impulse"):
+        assert np.array_equal(c[k], g[k]), k
