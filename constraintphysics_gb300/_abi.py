@@ -31,6 +31,7 @@ SIGNATURES = {
     "body_sphere": (I, [P, P, D, P, I, P, P]),
     "body_cylinder": (I, [P, P, D, D, P, I, P, P]),
     "body_capsule": (I, [P, P, D, D, P, I, P, P]),
+    "raycast": (I, [P, P, P, I, P, I, P, P, P, P]),
     "body_mesh": (I, [P, P, I, P, I, P, I, P]),
     "body_set_velocity": (I, [P, U32, P]),
     "body_set_ang_velocity": (I, [P, U32, P]),

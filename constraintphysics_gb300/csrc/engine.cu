@@ -1816,6 +1816,55 @@ int cpgpu_step(cpgpu_world* w, int n_steps) {
     });
 }
 
+// PhysicsEngine::raycastFirstIntersection (PhysicsEngine.cpp:582-609), one
+// device thread per ray against the world's current geometry
+int cpgpu_raycast(cpgpu_world* w, const double* origins, const double* dirs, int n_rays, const uint32_t* ignore,
+                  int n_ignore, uint32_t* hit_body, double* hit_pos, double* hit_normal, double* hit_dist) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (n_rays < 0 || n_ignore < 0 || (n_rays > 0 && (!origins || !dirs)) || (n_ignore > 0 && !ignore))
+            throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad ray arguments"};
+        std::vector<float> out(8 * (size_t)n_rays, 0.f);
+        for (int k = 0; k < n_rays; k++) out[8 * (size_t)k + 7] = -1.f;
+        if (n_rays > 0 && !w->w.bodies.empty()) {
+            ensure_device(w->w);
+            Batch& B = *w->w.dev;
+            std::vector<float> rays(6 * (size_t)n_rays);
+            for (size_t i = 0; i < 3 * (size_t)n_rays; i++) {
+                const size_t k = i / 3, c = i % 3;
+                rays[6 * k + c] = (float)origins[i];
+                rays[6 * k + 3 + c] = (float)dirs[i];
+            }
+            float *d_rays = nullptr, *d_out = nullptr;
+            uint32_t* d_ig = nullptr;
+            CK(cudaMalloc(&d_rays, sizeof(float) * rays.size()));
+            CK(cudaMalloc(&d_out, sizeof(float) * out.size()));
+            CK(cudaMalloc(&d_ig, sizeof(uint32_t) * std::max(n_ignore, 1)));
+            CK(cudaMemcpyAsync(d_rays, rays.data(), sizeof(float) * rays.size(), cudaMemcpyHostToDevice, B.st));
+            if (n_ignore > 0) CK(cudaMemcpyAsync(d_ig, ignore, sizeof(uint32_t) * n_ignore, cudaMemcpyHostToDevice, B.st));
+            launch_raycast(B.cur(), 0, (int)w->w.bodies.size(), d_rays, n_rays, d_ig, n_ignore, d_out, B.st);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(out.data(), d_out, sizeof(float) * out.size(), cudaMemcpyDeviceToHost, B.st));
+            CK(cudaStreamSynchronize(B.st));
+            cudaFree(d_rays);
+            cudaFree(d_out);
+            cudaFree(d_ig);
+        }
+        for (int k = 0; k < n_rays; k++) {
+            const float* r = &out[8 * (size_t)k];
+            uint32_t id;
+            std::memcpy(&id, &r[0], 4);
+            if (hit_body) hit_body[k] = id;
+            for (int c = 0; c < 3; c++) {
+                if (hit_pos) hit_pos[3 * k + c] = r[1 + c];
+                if (hit_normal) hit_normal[3 * k + c] = r[4 + c];
+            }
+            if (hit_dist) hit_dist[k] = r[7];
+        }
+        return CPGPU_OK;
+    });
+}
+
 int cpgpu_num_bodies(cpgpu_world* w, int* n) {
     W_OR_FAIL(w);
     *n = (int)w->w.bodies.size();

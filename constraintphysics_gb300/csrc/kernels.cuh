@@ -24,6 +24,11 @@ void launch_geometry(const Dev& d, int force_all, const Launch& L);
 // that involve one
 void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st);
 int mesh_scratch_warps(int n_sms);   // per-warp scratch entries the mesh narrowphase uses
+// ray queries against the bodies [s, e): rays 6 floats each (origin, unit
+// direction), `out` 8 floats per ray (body id bits, 0 = no hit; point;
+// normal; distance, -1 = no hit)
+void launch_raycast(const Dev& d, int s, int e, const float* rays, int n, const uint32_t* ignore, int n_ignore, float* out,
+                    cudaStream_t st);
 void launch_merge(const Dev& d, const Launch& L);
 // largest k_pgs_big shared Δv area (island bodies) and k_islands shared
 // memory any batch uses: the kernels' dynamic shared memory limits are set to

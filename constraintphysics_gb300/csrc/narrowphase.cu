@@ -1897,6 +1897,175 @@ void prepare_kernels() {
 
 int mesh_scratch_warps(int n_sms) { return n_sms * kMeshBlocksPerSm * 8; }
 
+// ---- ray queries ------------------------------------------------------------------
+// PhysicsEngine::raycastFirstIntersection (PhysicsEngine.cpp:582-609) for one
+// ray per thread against the bodies [s, e) of one world: every body whose
+// current AABB the ray crosses is tested with its primitive's ray test, the
+// nearest hit wins (strictly nearer replaces, in body order).
+namespace {
+struct RayHitD { bool hit; f3 p, n; float t; };
+
+// AABB::rayIntersectsAABB (AABB.h:143-172)
+__device__ bool rayAABB(f3 lo, f3 hi, f3 o, f3 d) {
+    float t_min = -INFINITY, t_max = INFINITY;
+    const float los[3] = {lo.x, lo.y, lo.z}, his[3] = {hi.x, hi.y, hi.z}, os[3] = {o.x, o.y, o.z}, ds[3] = {d.x, d.y, d.z};
+    for (int i = 0; i < 3; i++) {
+        if (fabsf(ds[i]) < 1e-11f) {
+            if (os[i] < los[i] || os[i] > his[i]) return false;
+        } else {
+            float t0 = (los[i] - os[i]) / ds[i], t1 = (his[i] - os[i]) / ds[i];
+            if (t0 > t1) { float x = t0; t0 = t1; t1 = x; }
+            t_min = fmaxf(t0, t_min);
+            t_max = fminf(t1, t_max);
+            if (t_max < 0.f || t_max < t_min) return false;
+        }
+    }
+    return true;
+}
+
+// smaller non-negative root of a t^2 + b t + c (ConvexPrimitive.cpp:134-150, 179-195)
+__device__ bool rayRoot(float a, float b, float c, float* t) {
+    const float radical = b * b - 4.f * a * c;
+    if (radical < 0.f) return false;
+    if (radical == 0.f) { *t = -0.5f * b / a; return *t >= 0.f; }
+    const float sr = sqrtf(radical);
+    const float t1 = (-b + sr) / (2.f * a), t2 = (-b - sr) / (2.f * a);
+    if (t1 < 0.f && t2 < 0.f) return false;
+    *t = t1 < 0.f ? t2 : t2 < 0.f ? t1 : fminf(t1, t2);
+    return true;
+}
+
+// testRayAgainstSphere (ConvexPrimitive.cpp:170-202)
+__device__ RayHitD raySphere(f3 o, f3 d, f3 c, float r) {
+    f3 rel = o - c;
+    float t;
+    if (!rayRoot(mag2(d), 2.f * dot(rel, d), mag2(rel) - r * r, &t)) return RayHitD{false};
+    f3 hp = o + t * d;
+    return RayHitD{true, hp, normalize(hp - c), t};
+}
+
+// testRayAgainstCylinderSide (ConvexPrimitive.cpp:113-168)
+__device__ RayHitD rayCylSide(f3 o, f3 d, f3 c, float r, float h, f3 ax) {
+    f3 u = d - ax * dot(ax, d);
+    f3 w = o - c - ax * (dot(ax, o) - dot(ax, c));
+    float t;
+    if (!rayRoot(mag2(u), 2.f * dot(u, w), mag2(w) - r * r, &t)) return RayHitD{false};
+    f3 hp = o + t * d;
+    const float x = dot(hp - c, ax);
+    if (fabsf(x) > 0.5f * h) return RayHitD{false};
+    return RayHitD{true, hp, normalize((hp - c) - ax * x), t};
+}
+
+// checkDiskIntersection (ConvexPrimitive.cpp:300-306)
+__device__ RayHitD rayDisk(f3 o, f3 d, f3 c, f3 n, float r) {
+    const float t = dot(n, c - o) / dot(n, d);
+    f3 ip = o + t * d;
+    if (t < 0.f || mag2(ip - c) > r * r) return RayHitD{false};
+    return RayHitD{true, ip, n, t};
+}
+
+__device__ __forceinline__ void rayNearer(RayHitD* out, const RayHitD& h) {
+    if (h.hit && (!out->hit || h.t < out->t)) *out = h;
+}
+
+// Polyhedron::testRayIntersection (ConvexPrimitive.cpp:731-758): the first face
+// whose plane the ray enters from outside at a point inside the face
+__device__ RayHitD rayHull(const uint8_t* blob, float4 pos, float4 rot, f3 o, f3 d) {
+    HullG h(blob, pos, rot);
+    const HullHeader& H = *h.h;
+    const uint16_t* fofs = u16(blob, H.off_fofs);
+    const uint8_t* fidx = blob + H.off_fidx;
+    for (int f = 0; f < H.nf; f++) {
+        const int k0 = fofs[f], k1 = fofs[f + 1];
+        f3 sp = h.vert(fidx[k0]);
+        f3 n = h.norm(f);
+        if (dot(d, n) > -0.0001f || dot(o - sp, n) < 0.f) continue;
+        const float t = dot(n, sp - o) / dot(n, d);
+        f3 ip = o + t * d;
+        bool inside = true;
+        for (int k = k0; k < k1 && inside; k++) {
+            f3 e1 = h.vert(fidx[k]), e2 = h.vert(fidx[k + 1 == k1 ? k0 : k + 1]);
+            if (dot(cross(e2 - e1, n), ip - e1) > 0.f) inside = false;
+        }
+        if (inside) return RayHitD{true, ip, n, t};
+    }
+    return RayHitD{false};
+}
+
+// StaticMeshGeometry::testRayIntersection (Geometry.cpp:867-897)
+__device__ RayHitD rayMesh(const uint8_t* blob, f3 o, f3 d) {
+    const HullHeader* H = reinterpret_cast<const HullHeader*>(blob);
+    const float4* nodes = reinterpret_cast<const float4*>(blob + kMeshOffNodes);
+    const float4* tris = nodes + 2 * (size_t)H->pad[1];
+    RayHitD best{false};
+    for (uint32_t i = 0; i < H->pad[0]; i++) {
+        TriView T;
+        load_tri(tris + (size_t)kMeshTriF4 * i, &T);
+        if (!rayAABB(T.lo, T.hi, o, d)) continue;
+        if (fabsf(dot(T.n, d)) < 1e-10f) continue;
+        const float t = -dot(o - T.v[1], T.n) / dot(d, T.n);
+        if (t < 0.f || (best.hit && best.t < t)) continue;
+        f3 hp = o + t * d;
+        if (dot(hp - T.v[0], T.out[0]) > 0.f || dot(hp - T.v[1], T.out[1]) > 0.f || dot(hp - T.v[2], T.out[2]) > 0.f) continue;
+        best = RayHitD{true, hp, T.n, t};
+    }
+    return best;
+}
+
+__global__ void k_raycast(Dev d, int s, int e, const float* rays, int n, const uint32_t* ignore, int n_ignore, float* out) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const f3 o = mk(rays[6 * k], rays[6 * k + 1], rays[6 * k + 2]);
+        const f3 dir = mk(rays[6 * k + 3], rays[6 * k + 4], rays[6 * k + 5]);
+        RayHitD best{false};
+        int best_id = 0;
+        for (int g = s; g < e; g++) {
+            const uint32_t id = (uint32_t)(g - s + 1);
+            bool skip = false;
+            for (int q = 0; q < n_ignore; q++) skip |= ignore[q] == id;
+            if (skip || !rayAABB(mk(d.aabb_lo[g]), mk(d.aabb_hi[g]), o, dir)) continue;
+            const uint8_t* blob = d.shapes + d.shape[g];
+            const uint32_t kind = reinterpret_cast<const HullHeader*>(blob)->kind;
+            RayHitD h{false};
+            if (kind == SHAPE_MESH) {
+                h = rayMesh(blob, o, dir);
+            } else if (kind == SHAPE_HULL) {
+                h = rayHull(blob, d.pos[g], d.rot[g], o, dir);
+            } else {
+                const M33 R = quatRot(qnormalize(d.rot[g]));
+                const float4 cr = *reinterpret_cast<const float4*>(blob + sizeof(HullHeader));
+                const f3 c = mul(R, mk(cr)) + mk(d.pos[g]);
+                if (kind == SHAPE_SPHERE) {
+                    h = raySphere(o, dir, c, cr.w);
+                } else {
+                    const float4 ax4 = *reinterpret_cast<const float4*>(blob + kCylOffAxis);
+                    const f3 ax = mul(R, mk(ax4));
+                    h = rayCylSide(o, dir, c, cr.w, ax4.w, ax);
+                    if (kind == SHAPE_CYLINDER) {   // Cylinder::testRayIntersection (ConvexPrimitive.cpp:308-318)
+                        const float sgn = dot(ax, dir) < 0.f ? 1.f : -1.f;
+                        rayNearer(&h, rayDisk(o, dir, c + sgn * ax * (0.5f * ax4.w), ax, cr.w));
+                    } else {                        // Capsule::testRayIntersection (:403-411)
+                        rayNearer(&h, raySphere(o, dir, c + ax * (0.5f * ax4.w), cr.w));
+                        rayNearer(&h, raySphere(o, dir, c - ax * (0.5f * ax4.w), cr.w));
+                    }
+                }
+            }
+            if (h.hit && (!best.hit || h.t < best.t)) { best = h; best_id = (int)id; }
+        }
+        float* r = out + 8 * (size_t)k;
+        r[0] = __int_as_float(best_id);
+        r[1] = best.hit ? best.p.x : 0.f; r[2] = best.hit ? best.p.y : 0.f; r[3] = best.hit ? best.p.z : 0.f;
+        r[4] = best.hit ? best.n.x : 0.f; r[5] = best.hit ? best.n.y : 0.f; r[6] = best.hit ? best.n.z : 0.f;
+        r[7] = best.hit ? best.t : -1.f;
+    }
+}
+}  // namespace
+
+void launch_raycast(const Dev& d, int s, int e, const float* rays, int n, const uint32_t* ignore, int n_ignore, float* out,
+                    cudaStream_t st) {
+    if (n <= 0) return;
+    k_raycast<<<(n + 127) / 128, 128, 0, st>>>(d, s, e, rays, n, ignore, n_ignore, out);
+}
+
 void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st) {
     const int warps = 8;
     size_t smem = 16 * warps + (size_t)warps * (slot_bytes + kQueueBytes);

@@ -140,6 +140,19 @@ class World:
                                    int(movement), _ptr(pos), C.addressof(out))
         return self._new_id(rc, out)
 
+    def raycast(self, origins, dirs, ignore=()):
+        """raycastFirstIntersection for each row of `origins` / `dirs` (unit
+        directions): dict of body (0: no hit), pos, normal, dist (-1: no hit)."""
+        o = _f64(origins).reshape(-1, 3)
+        d = _f64(dirs).reshape(-1, 3)
+        n = len(o)
+        ig = np.ascontiguousarray(list(ignore) or [0], dtype=np.uint32)
+        body = np.zeros(n, dtype=np.uint32)
+        pos, nrm, dist = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
+        self._check(self.abi.raycast(self.h, _ptr(o), _ptr(d), n, ig.ctypes.data, len(list(ignore)), body.ctypes.data,
+                                     _ptr(pos), _ptr(nrm), _ptr(dist)))
+        return {"body": body, "pos": pos, "normal": nrm, "dist": dist}
+
     def add_mesh(self, points, tris, material=None, fixed=True):
         pts = _f64(points)
         tr = np.ascontiguousarray(tris, dtype=np.int32)

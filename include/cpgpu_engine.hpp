@@ -113,6 +113,14 @@ private:
 
 struct ConstraintID { uint32_t id; };
 
+// RayHitInfo (PhysicsEngine.h:40-46)
+struct RayHitInfo {
+    bool did_hit = false;
+    RigidBody* hit_object = nullptr;
+    Vec3 hit_position, surface_normal;
+    double hit_distance = -1;
+};
+
 class PhysicsEngine {
 public:
     PhysicsEngine() { check(cpgpu_world_create(&w_)); }
@@ -161,6 +169,23 @@ public:
         RigidBody* b = new RigidBody(this, id);
         owned_.push_back(b);
         return b;
+    }
+
+    // PhysicsEngine::raycastFirstIntersection (PhysicsEngine.cpp:582-609)
+    RayHitInfo raycastFirstIntersection(Vec3 ray_origin, Vec3 ray_dir, const std::vector<RigidBody*>& ignore_list = {}) const {
+        std::vector<uint32_t> ig;
+        for (RigidBody* b : ignore_list) ig.push_back(b->getID());
+        uint32_t id = 0;
+        double p[3], n[3], t = -1;
+        check(cpgpu_raycast(w_, ray_origin.data(), ray_dir.data(), 1, ig.data(), (int)ig.size(), &id, p, n, &t));
+        RayHitInfo h;
+        if (id == 0) return h;
+        h.did_hit = true;
+        h.hit_object = id <= owned_.size() ? owned_[id - 1] : nullptr;
+        h.hit_position = Vec3(p[0], p[1], p[2]);
+        h.surface_normal = Vec3(n[0], n[1], n[2]);
+        h.hit_distance = t;
+        return h;
     }
 
     ConstraintID addBallSocketConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, double strength = 15000) {

@@ -1155,6 +1155,178 @@ int cport_holonomic_check(cpgpu_world* w, int* n_systems, int* max_degree, doubl
 }
 int cport_step(cpgpu_world* w, int n) { for (int i = 0; i < n; i++) W(w)->step(); return CPGPU_OK; }
 int cport_num_bodies(cpgpu_world* w, int* n) { *n = (int)W(w)->bodies.size(); return CPGPU_OK; }
+// ---- ray queries (PhysicsEngine::raycastFirstIntersection,
+// PhysicsEngine.cpp:582-609) against the bodies' current geometry: every
+// body whose current AABB the ray crosses (the reference filters with its
+// broadphase tree, whose leaves hold the AABBs of the start of the last step)
+// is tested with its primitive's ray test; the nearest hit wins (strictly
+// nearer replaces, in body order).
+namespace {
+struct RayHit { bool hit = false; V3 p, n; double t = 0; };
+
+// AABB::rayIntersectsAABB (AABB.h:143-172)
+bool rayAABB(const AABB& b, const V3& o, const V3& d) {
+    double t_min = -std::numeric_limits<double>::infinity(), t_max = std::numeric_limits<double>::infinity();
+    const double eps = 0.00000000001;
+    for (int i = 0; i < 3; i++) {
+        const double oi = o[i], di = d[i], lo = b.mn[i], hi = b.mx[i];
+        if (std::abs(di) < eps) {
+            if (oi < lo || oi > hi) return false;
+        } else {
+            double t0 = (lo - oi) / di, t1 = (hi - oi) / di;
+            if (t0 > t1) std::swap(t0, t1);
+            t_min = std::max<double>(t0, t_min);
+            t_max = std::min<double>(t1, t_max);
+            if (t_max < 0 || t_max < t_min) return false;
+        }
+    }
+    return true;
+}
+
+// the smaller non-negative root of a t^2 + b t + c (both ray tests below).
+// As in the reference, a ray parallel to a cylinder axis (a = b = 0) passes
+// the double-root test with t = NaN and is reported as a hit at NaN.
+bool rayRoot(double a, double b, double c, double* t) {
+    double radical = b * b - 4 * a * c;
+    if (radical < 0) return false;
+    if (radical == 0) {
+        *t = -0.5 * b / a;
+        return !(*t < 0);
+    }
+    double t1 = (-b + std::sqrt(radical)) / (2 * a), t2 = (-b - std::sqrt(radical)) / (2 * a);
+    if (t1 < 0 && t2 < 0) return false;
+    *t = t1 < 0 ? t2 : t2 < 0 ? t1 : std::min<double>(t1, t2);
+    return true;
+}
+
+// testRayAgainstSphere (ConvexPrimitive.cpp:170-202)
+RayHit raySphere(const V3& o, const V3& d, const V3& c, double r) {
+    V3 rel = o - c;
+    double t;
+    if (!rayRoot(d.mag2(), 2 * rel.dot(d), rel.mag2() - r * r, &t)) return {};
+    V3 hp = o + t * d;
+    return RayHit{true, hp, (hp - c).normalize(), t};
+}
+
+// testRayAgainstCylinderSide (ConvexPrimitive.cpp:113-168)
+RayHit rayCylSide(const V3& o, const V3& d, const V3& c, double r, double h, const V3& ax) {
+    V3 u = d - ax * ax.dot(d);
+    V3 w = o - c - ax * (ax.dot(o) - ax.dot(c));
+    double a = u.x * u.x + u.y * u.y + u.z * u.z;
+    double b = 2 * (u.x * w.x + u.y * w.y + u.z * w.z);
+    double cc = w.x * w.x + w.y * w.y + w.z * w.z - r * r;
+    double t;
+    if (!rayRoot(a, b, cc, &t)) return {};
+    V3 hp = o + t * d;
+    double x = (hp - c).dot(ax);
+    if (std::abs(x) > h / 2.0) return {};
+    return RayHit{true, hp, ((hp - c) - ax * x).normalize(), t};
+}
+
+// checkDiskIntersection (ConvexPrimitive.cpp:300-306)
+RayHit rayDisk(const V3& o, const V3& d, const V3& c, const V3& n, double r) {
+    double t = n.dot(c - o) / n.dot(d);
+    V3 ip = o + t * d;
+    if (t < 0 || (ip - c).mag2() > r * r) return {};
+    return RayHit{true, ip, n, t};
+}
+
+void nearer(RayHit* out, const RayHit& h) {
+    if (h.hit && (!out->hit || h.t < out->t)) *out = h;
+}
+
+// Polyhedron::testRayIntersection (ConvexPrimitive.cpp:731-758): the first
+// face, in surface order, whose plane the ray enters from outside at a point
+// inside the face
+RayHit rayHull(const Hull& h, const V3& o, const V3& d) {
+    for (size_t f = 0; f < h.faces.size(); f++) {
+        const std::vector<int>& s = h.faces[f];
+        V3 sp = h.pts[s[0]];
+        V3 n = h.faceNormal((int)f);
+        const double eps = 0.0001;
+        if (d.dot(n) > -eps || (o - sp).dot(n) < 0) continue;
+        double t = n.dot(sp - o) / n.dot(d);
+        V3 ip = o + t * d;
+        bool inside = true;
+        for (size_t i = 0; i < s.size() && inside; i++) {
+            V3 e1 = h.pts[s[i]], e2 = h.pts[s[i + 1 == s.size() ? 0 : i + 1]];
+            if ((e2 - e1).cross(n).dot(ip - e1) > 0) inside = false;
+        }
+        if (inside) return RayHit{true, ip, n, t};
+    }
+    return {};
+}
+
+// StaticMeshGeometry::testRayIntersection (Geometry.cpp:867-897): triangles
+// whose AABB the ray crosses, nearest plane hit inside the triangle (a later
+// triangle at an equal distance replaces)
+RayHit rayMesh(const Body* m, const V3& o, const V3& d) {
+    RayHit best;
+    for (const MeshTri& tri : m->tris) {
+        if (!rayAABB(tri.aabb, o, d)) continue;
+        if (std::abs(tri.normal.dot(d)) < 0.0000000001) continue;
+        double t = -(o - tri.v[1]).dot(tri.normal) / d.dot(tri.normal);
+        if (t < 0 || (best.hit && best.t < t)) continue;
+        V3 hp = o + t * d;
+        if ((hp - tri.ep1[0]).dot(tri.out[0]) > 0 || (hp - tri.ep1[1]).dot(tri.out[1]) > 0 ||
+            (hp - tri.ep1[2]).dot(tri.out[2]) > 0)
+            continue;
+        best = RayHit{true, hp, tri.normal, t};
+    }
+    return best;
+}
+
+// RigidBody::checkRayIntersection (RigidBody.cpp:185-204) and the
+// primitives' testRayIntersection (ConvexPrimitive.cpp:205-212, 308-318,
+// 403-411, 445-447)
+RayHit rayBody(const Body* b, const V3& o, const V3& d) {
+    switch (b->kind) {
+    case K_MESH: return rayMesh(b, o, d);
+    case K_SPHERE: return raySphere(o, d, b->sph.c, b->sph.r);
+    case K_CYLINDER: {
+        const CylG& c = b->cyl;
+        RayHit out = rayCylSide(o, d, c.c, c.r, c.h, c.axis);
+        double sgn = c.axis.dot(d) < 0 ? 1.0 : -1.0;
+        nearer(&out, rayDisk(o, d, c.c + sgn * c.axis * (c.h / 2.0), c.axis, c.r));
+        return out;
+    }
+    case K_CAPSULE: {
+        const CapG& c = b->cap;
+        RayHit out = rayCylSide(o, d, c.c, c.r, c.h, c.axis);
+        nearer(&out, raySphere(o, d, c.c + c.axis * (c.h / 2.0), c.r));
+        nearer(&out, raySphere(o, d, c.c - c.axis * (c.h / 2.0), c.r));
+        return out;
+    }
+    default: return rayHull(b->shape, o, d);
+    }
+}
+}  // namespace
+
+int cport_raycast(cpgpu_world* w, const double* origins, const double* dirs, int n_rays, const uint32_t* ignore,
+                  int n_ignore, uint32_t* hit_body, double* hit_pos, double* hit_normal, double* hit_dist) {
+    if (n_rays < 0 || (n_rays > 0 && (!origins || !dirs)) || n_ignore < 0 || (n_ignore > 0 && !ignore))
+        return fail("bad ray arguments");
+    World* wd = W(w);
+    std::set<uint32_t> skip(ignore, ignore + n_ignore);
+    for (int k = 0; k < n_rays; k++) {
+        V3 o = v3(origins + 3 * k), d = v3(dirs + 3 * k);
+        RayHit best;
+        uint32_t id = 0;
+        for (const auto& b : wd->bodies) {
+            if (skip.count(b->id) || !rayAABB(b->aabb, o, d)) continue;
+            RayHit h = rayBody(b.get(), o, d);
+            if (h.hit && (!best.hit || h.t < best.t)) { best = h; id = b->id; }
+        }
+        if (hit_body) hit_body[k] = id;
+        for (int i = 0; i < 3; i++) {
+            if (hit_pos) hit_pos[3 * k + i] = best.hit ? best.p[i] : 0;
+            if (hit_normal) hit_normal[3 * k + i] = best.hit ? best.n[i] : 0;
+        }
+        if (hit_dist) hit_dist[k] = best.hit ? best.t : -1;
+    }
+    return CPGPU_OK;
+}
+
 int cport_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel, double* ang) {
     World* x = W(w);
     for (size_t i = 0; i < x->bodies.size(); i++) {

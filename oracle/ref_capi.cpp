@@ -290,6 +290,31 @@ int cpref_step_untraced(cpgpu_world* w, int n_steps) {
 
 int cpref_num_bodies(cpgpu_world* w, int* n) { *n = (int)RW->bodies.size(); return CPGPU_OK; }
 
+// raycastFirstIntersection per ray, after refreshing the broadphase tree's
+// leaves to the bodies' current AABBs (the same update timeStep makes first,
+// PhysicsEngine.cpp:103-105; without it the leaves hold the AABBs of the
+// start of the last step)
+int cpref_raycast(cpgpu_world* w, const double* origins, const double* dirs, int n_rays, const uint32_t* ignore,
+                  int n_ignore, uint32_t* hit_body, double* hit_pos, double* hit_normal, double* hit_dist) {
+    std::vector<uint32_t> tmp;
+    phyz::DebugDemo::candidate_pairs(RW->engine, tmp);
+    std::vector<phyz::RigidBody*> ig;
+    for (int k = 0; k < n_ignore; k++)
+        if (phyz::RigidBody* r = body(RW, ignore[k])) ig.push_back(r);
+    for (int k = 0; k < n_rays; k++) {
+        phyz::RayHitInfo h = RW->engine.raycastFirstIntersection(v3(origins + 3 * k), v3(dirs + 3 * k), ig);
+        if (hit_body) hit_body[k] = h.did_hit ? h.hit_object->getID() : 0;
+        const double p[3] = {h.hit_position.x, h.hit_position.y, h.hit_position.z};
+        const double n[3] = {h.surface_normal.x, h.surface_normal.y, h.surface_normal.z};
+        for (int i = 0; i < 3; i++) {
+            if (hit_pos) hit_pos[3 * k + i] = h.did_hit ? p[i] : 0;
+            if (hit_normal) hit_normal[3 * k + i] = h.did_hit ? n[i] : 0;
+        }
+        if (hit_dist) hit_dist[k] = h.did_hit ? h.hit_distance : -1;
+    }
+    return CPGPU_OK;
+}
+
 int cpref_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel, double* ang_vel) {
     for (size_t i = 0; i < RW->bodies.size(); i++) {
         phyz::RigidBody* r = RW->bodies[i];

@@ -18,8 +18,12 @@ int main() {
         for (int i = 0; i < 300; i++) p.timeStep();
         cpgpu::Vec3 c = box->getCOM(), v = box->getVel();
         double speed = std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
-        std::printf("box y=%.6f |v|=%.3g\n", c.y, speed);
-        return (std::fabs(c.y - 0.5) < 0.1 && speed < 5e-3) ? 0 : 1;  // FP32 residual motion at rest
+        // a ray straight down onto the resting box hits its top face (y = 1) first
+        cpgpu::RayHitInfo h = p.raycastFirstIntersection(cpgpu::Vec3(c.x, 10, c.z), cpgpu::Vec3(0, -1, 0));
+        std::printf("box y=%.6f |v|=%.3g ray hit %d at %.4f\n", c.y, speed, h.did_hit ? (int)h.hit_object->getID() : 0,
+                    h.hit_distance);
+        bool ray_ok = h.did_hit && h.hit_object == box && std::fabs(h.hit_distance - (10 - (c.y + 0.5))) < 1e-3;
+        return (std::fabs(c.y - 0.5) < 0.1 && speed < 5e-3 && ray_ok) ? 0 : 1;  // FP32 residual motion at rest
     } catch (const cpgpu::Error& e) {
         std::printf("%s\n", e.what());
         return e.code == CPGPU_ERR_NO_DEVICE ? 2 : 1;
