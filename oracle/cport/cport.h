@@ -312,6 +312,16 @@ struct Body {
     M3 tensor, inv_tensor, ref_tensor, ref_inv_tensor;
     std::vector<V3> track_p;
     std::set<const Body*> no_collide;   // no_collision_set (RigidBody.h), filled by joints
+    // sleeping (RigidBody.h: asleep, sleep_ready_counter, non_sleepy_tick_count,
+    // history, recievedWakingAction; RigidBody.cpp:318-352)
+    bool asleep = false, waking = false;
+    double sleep_ready = 0;
+    int non_sleepy = 0;
+    std::vector<std::pair<V3, V3>> history;   // (vel, ang_vel) of the last steps
+    bool getAsleep() const { return asleep && movement == DYNAMIC; }
+    void sleep() { if (movement != DYNAMIC) return; asleep = true; vel = V3(); ang_vel = V3(); }
+    void wake() { if (asleep) { asleep = false; sleep_ready = 0; non_sleepy = 0; history.clear(); } }
+    void alertWaking() { waking = true; sleep_ready = 0; non_sleepy = 0; history.clear(); }
     V3 local_origin;
     Hull src_shape;       // geometry as given at creation (geometry frame)
     V3 create_pos;
@@ -431,6 +441,10 @@ struct Params {
     bool gyro_disabled = false;
     bool warm_start_disabled = false;
     bool sleeping = true;
+    // sleep parameters (PhysicsEngine.h:219-224)
+    double sleep_delay = 0.5;
+    int non_sleepy_threshold = 3;
+    double vel_sleep_coeff = 0.1, ang_vel_eps = 0.1, accel_sleep_coeff = 0.044;
     double lin_err_threshold = 15;   // excessive_linear_error_torque_threshold (PhysicsEngine.h:217)
     double cutoff_vel = 0;   // set by setStep_time / setGravity (PhysicsEngine.cpp:1142-1145,1214-1217)
 };
@@ -464,6 +478,10 @@ struct World {
     void holonomicScan(Edge* e);
     void updateHolonomicInverses();
     void step();
+    bool bodySleepy(const Body* b) const;
+    bool readyToSleep(const Body* b) const;
+    void wakeupIsland(Body* foothold);
+    void applyVelocityChange(Body* b, const V3& dv, const V3& dw, const V3& dpv, const V3& dpw);
 };
 
 void jrowTarget(JRow& r);

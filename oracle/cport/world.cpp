@@ -692,8 +692,8 @@ static void pgsStep(Row<N>& r, bool pseudo, Proj proj) {
 }
 
 // PGS_solve (ConstraintSolver.cpp:80-213) for the contact rows of one island
-static void pgsSolve(std::vector<RowRef>& rows, int n_vel, int n_pos, const std::vector<HoloSys*>& blocks, int n_holo,
-                     double lin_err_threshold) {
+static void pgsSolve(World& world, std::vector<RowRef>& rows, int n_vel, int n_pos, const std::vector<HoloSys*>& blocks,
+                     int n_holo, double lin_err_threshold) {
     std::unordered_map<Body*, std::unique_ptr<DV>> dv;
     auto slot = [&](Body* b) { auto& s = dv[b]; if (!s) s = std::make_unique<DV>(); return s.get(); };
     for (RowRef& rr : rows) {
@@ -762,15 +762,73 @@ static void pgsSolve(std::vector<RowRef>& rows, int n_vel, int n_pos, const std:
             for (int i = 0; i < r.n; i++) r.impulse[i] += scale * r.holo[i];
         }
     }
-    // PhysicsEngine::applyVelocityChange (PhysicsEngine.cpp:1113-1136)
+    // the island's velocity changes (ConstraintSolver.cpp:201-211), in the
+    // velocity-change map's iteration order
     for (auto& kv : dv) {
-        Body* b = kv.first;
-        if (b->movement != DYNAMIC) continue;
         const DV& d = *kv.second;
-        b->vel += V3(d.v.v[0], d.v.v[1], d.v.v[2]);
-        b->ang_vel += V3(d.v.v[3], d.v.v[4], d.v.v[5]);
-        b->pvel += V3(d.pv.v[0], d.pv.v[1], d.pv.v[2]);
-        b->pang_vel += V3(d.pv.v[3], d.pv.v[4], d.pv.v[5]);
+        world.applyVelocityChange(kv.first, V3(d.v.v[0], d.v.v[1], d.v.v[2]), V3(d.v.v[3], d.v.v[4], d.v.v[5]),
+                                  V3(d.pv.v[0], d.pv.v[1], d.pv.v[2]), V3(d.pv.v[3], d.pv.v[4], d.pv.v[5]));
+    }
+}
+
+// PhysicsEngine::applyVelocityChange (PhysicsEngine.cpp:1113-1136): a sleeping
+// body whose new velocity exceeds a quarter of the sleep velocity wakes its
+// island, otherwise it stays at rest.  (The reference visits the island's
+// bodies in the order of an unordered_map keyed by body address, so when one
+// sleeping body of an island wakes it and another would have been zeroed,
+// the outcome depends on that order; this restatement's order is its own.)
+void World::applyVelocityChange(Body* b, const V3& dv, const V3& dw, const V3& dpv, const V3& dpw) {
+    if (b->movement == FIXED || b->movement == KINEMATIC) return;
+    b->vel += dv;
+    b->ang_vel += dw;
+    b->pvel += dpv;
+    b->pang_vel += dpw;
+    const double wake_vel = 0.25 * p.vel_sleep_coeff * p.g.mag();
+    if (b->getAsleep() && (b->vel.mag() > wake_vel || b->ang_vel.mag() > wake_vel)) {
+        wakeupIsland(b);
+    } else if (b->getAsleep()) {
+        b->vel = V3();
+        b->ang_vel = V3();
+    }
+}
+
+// PhysicsEngine::bodySleepy (PhysicsEngine.cpp:1221-1254): average velocity,
+// angular velocity and accelerations over the recorded history below the
+// thresholds (at least half the sleep delay recorded)
+bool World::bodySleepy(const Body* r) const {
+    const int n = (int)r->history.size();
+    if (n == 0 || 2 * n < (p.sleep_delay / p.dt)) return false;
+    V3 av, aw;
+    for (const auto& s : r->history) { av += s.first; aw += s.second; }
+    av /= n;
+    aw /= n;
+    V3 acc = (r->history.back().first - r->history.front().first) / (p.dt * (n - 1));
+    V3 aacc = (r->history.back().second - r->history.front().second) / (p.dt * (n - 1));
+    const double vel_eps = p.vel_sleep_coeff * p.g.mag();
+    const double accel_eps = p.accel_sleep_coeff * p.g.mag();
+    const double ang_accel_eps = p.accel_sleep_coeff * 2.5;
+    return av.mag() <= vel_eps && aw.mag() <= p.ang_vel_eps && acc.mag() <= accel_eps && aacc.mag() <= ang_accel_eps;
+}
+
+// PhysicsEngine::readyToSleep (PhysicsEngine.cpp:1256-1258)
+bool World::readyToSleep(const Body* b) const {
+    return b->movement != KINEMATIC && (b->sleep_ready >= p.sleep_delay || b->movement == FIXED);
+}
+
+// PhysicsEngine::wakeupIsland / bfsVisitAll (PhysicsEngine.cpp:1263-1290):
+// every dynamic body reachable through dynamic bodies wakes
+void World::wakeupIsland(Body* foothold) {
+    std::set<Body*> visited;
+    std::vector<Body*> stack{foothold};
+    while (!stack.empty()) {
+        Body* cur = stack.back();
+        stack.pop_back();
+        if (!visited.insert(cur).second) continue;
+        if (cur->movement == DYNAMIC) cur->wake();
+        for (Edge* e : adj[cur]) {
+            Body* o = e->other(cur);
+            if (o->movement == DYNAMIC && !visited.count(o)) stack.push_back(o);
+        }
     }
 }
 
@@ -807,9 +865,28 @@ static Manifold collide(const Body* b1, const Body* b2) {
 
 // -------------------------------------------------------------- step ----
 void World::step() {
-    // gravity once per step (PhysicsEngine.cpp:65-87)
-    for (auto& b : bodies)
-        if (b->movement == DYNAMIC) b->vel += p.g * p.dt;
+    // waking actions, sleep bookkeeping and gravity once per step
+    // (PhysicsEngine.cpp:65-87; RigidBody::recordMovementState, RigidBody.cpp:347-352)
+    for (auto& bp : bodies) {
+        Body* b = bp.get();
+        if (b->waking) wakeupIsland(b);
+        b->waking = false;
+        if (b->movement == DYNAMIC && !b->getAsleep()) {
+            const int len = static_cast<int>(p.sleep_delay / p.dt);
+            b->history.push_back({b->vel, b->ang_vel});
+            while ((int)b->history.size() > len) b->history.erase(b->history.begin());
+            if (bodySleepy(b)) {
+                b->sleep_ready += p.dt;
+            } else {
+                b->non_sleepy++;
+                if (b->non_sleepy >= p.non_sleepy_threshold) {
+                    b->sleep_ready = 0.0;
+                    b->non_sleepy = 0;
+                }
+            }
+            b->vel += p.g * p.dt;
+        }
+    }
 
     // broadphase: every pair whose true AABBs overlap (AABB_Tree.h:153-224)
     last_pairs.clear();
@@ -821,7 +898,8 @@ void World::step() {
     for (auto& pr : last_pairs) {
         Body* b1 = bodies[pr.first - 1].get();
         Body* b2 = bodies[pr.second - 1].get();
-        if (!(b1->movement == DYNAMIC || b2->movement == DYNAMIC)) continue;
+        // at least one dynamic and one awake body (PhysicsEngine.cpp:174)
+        if (!(b1->movement == DYNAMIC || b2->movement == DYNAMIC) || !(!b1->getAsleep() || !b2->getAsleep())) continue;
         if (b1->no_collide.count(b2)) continue;   // collisionAllowed (PhysicsEngine.cpp:570-572)
         if (b1->kind == K_MESH && b2->kind == K_MESH) continue;
         std::vector<Manifold> mans;
@@ -861,27 +939,40 @@ void World::step() {
         if (n->movement != DYNAMIC || visited.count(n)) continue;
         std::vector<RowRef> rows;
         std::vector<HoloSys*> blocks;
+        std::vector<Body*> island_bodies;
+        bool all_ready = true;
         std::vector<Body*> stack{n};
         while (!stack.empty()) {
             Body* cur = stack.back();
             stack.pop_back();
             if (!visited.insert(cur).second) continue;
             if (cur->movement == DYNAMIC) {
+                island_bodies.push_back(cur);
+                bool kinematic_contact = false;
                 for (Edge* e : adj[cur]) {
                     Body* o = e->other(cur);
-                    if (visited.count(o)) continue;
+                    if (o->movement == KINEMATIC) kinematic_contact = true;
+                    // a sleeping body's edges to sleeping or fixed bodies carry no rows
+                    if ((cur->getAsleep() && (o->getAsleep() || o->movement == FIXED)) || visited.count(o)) continue;
                     if (holo && e->h && std::find(blocks.begin(), blocks.end(), e->h) == blocks.end()) blocks.push_back(e->h);
                     for (Joint* j : e->joints) rows.push_back({2, nullptr, j});
                     for (auto& c : e->contacts)
                         if (c->live) { rows.push_back({0, c.get()}); rows.push_back({1, c.get()}); }
                 }
+                if (kinematic_contact || !readyToSleep(cur)) all_ready = false;
             }
             for (Edge* e : adj[cur]) {
                 Body* o = e->other(cur);
                 if (o->movement == DYNAMIC && !visited.count(o)) stack.push_back(o);
             }
         }
-        if (!rows.empty()) { islands.push_back(std::move(rows)); island_blocks.push_back(std::move(blocks)); }
+        // an island whose bodies are all ready sleeps instead of being solved
+        if (p.sleeping && all_ready) {
+            for (Body* b : island_bodies) b->sleep();
+        } else if (!rows.empty()) {
+            islands.push_back(std::move(rows));
+            island_blocks.push_back(std::move(blocks));
+        }
     }
 
     // substeps (PhysicsEngine.cpp:368-420)
@@ -903,16 +994,22 @@ void World::step() {
             }
             if (first) {
                 auto& v = e->contacts;
-                v.erase(std::remove_if(v.begin(), v.end(), [](const std::unique_ptr<Contact>& c) { return c->life < 0; }), v.end());
+                // Contact::isExpired (PersistentConstraint.h:74): a contact of a
+                // sleeping body does not expire
+                v.erase(std::remove_if(v.begin(), v.end(),
+                                       [](const std::unique_ptr<Contact>& c) {
+                                           return !c->b1->getAsleep() && !c->b2->getAsleep() && c->life < 0;
+                                       }),
+                        v.end());
                 if (v.empty() && e->joints.empty()) dead.push_back(e.get());
             }
         }
         for (Edge* e : dead) deleteEdge(e);
         for (size_t k = 0; k < islands.size(); k++)
-            pgsSolve(islands[k], p.pgs_vel, p.pgs_pos, island_blocks[k], first ? p.pgs_holo : 0, p.lin_err_threshold);
+            pgsSolve(*this, islands[k], p.pgs_vel, p.pgs_pos, island_blocks[k], first ? p.pgs_holo : 0, p.lin_err_threshold);
         for (auto& bp : bodies) {
             Body* b = bp.get();
-            if (b->movement == FIXED) continue;
+            if (b->movement == FIXED || b->getAsleep()) continue;
             b->prev_com = b->com;
             b->prev_q = b->q;
             b->com += (b->vel + b->pvel) * dts;
@@ -929,7 +1026,7 @@ void World::step() {
     }
     for (auto& bp : bodies) {
         Body* b = bp.get();
-        if (b->movement == FIXED) continue;
+        if (b->movement == FIXED || b->getAsleep()) continue;
         if (b->com != b->prev_com || b->q != b->prev_q) b->updateGeometry();
     }
     if (holo) updateHolonomicInverses();
@@ -963,7 +1060,7 @@ extern "C" {
 const char* cport_last_error(void) { return g_err.c_str(); }
 int cport_world_create(cpgpu_world** out) {
     World* w = new World();
-    w->p.sleeping = false;  // the restatement implements the sleeping-disabled path
+    w->p.sleeping = false;  // as the device path: sleeping off unless enabled
     *out = reinterpret_cast<cpgpu_world*>(w);
     return CPGPU_OK;
 }
@@ -973,8 +1070,7 @@ int cport_set_gravity(cpgpu_world* w, double x, double y, double z) { W(w)->p.g 
 int cport_set_substep_count(cpgpu_world* w, int s) { if (s < 1) return fail("substeps < 1"); W(w)->p.substeps = s; return CPGPU_OK; }
 int cport_set_pgs_iterations(cpgpu_world* w, int v, int p, int h) { W(w)->p.pgs_vel = v; W(w)->p.pgs_pos = p; W(w)->p.pgs_holo = h; return CPGPU_OK; }
 int cport_set_sleeping_enabled(cpgpu_world* w, int e) {
-    if (e) return fail("sleeping is not implemented", CPGPU_ERR_UNSUPPORTED);
-    W(w)->p.sleeping = false;
+    W(w)->p.sleeping = e != 0;
     return CPGPU_OK;
 }
 int cport_set_warm_start_disabled(cpgpu_world* w, int d) { W(w)->p.warm_start_disabled = d != 0; return CPGPU_OK; }
@@ -1049,10 +1145,10 @@ int cport_body_mesh(cpgpu_world* w, const double* points, int n_points, const in
     return CPGPU_OK;
 }
 int cport_body_set_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {
-    Body* b = B(w, id); if (!b) return fail("bad id"); b->vel = v3(v); return CPGPU_OK;
+    Body* b = B(w, id); if (!b) return fail("bad id"); b->vel = v3(v); b->alertWaking(); return CPGPU_OK;
 }
 int cport_body_set_ang_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {
-    Body* b = B(w, id); if (!b) return fail("bad id"); b->ang_vel = v3(v); return CPGPU_OK;
+    Body* b = B(w, id); if (!b) return fail("bad id"); b->ang_vel = v3(v); b->alertWaking(); return CPGPU_OK;
 }
 // RigidBody::setOrientation (RigidBody.cpp:103-107): the world inertia tensor is
 // left as it was until the next integration
@@ -1060,12 +1156,14 @@ int cport_body_set_orientation(cpgpu_world* w, uint32_t id, const double q[4]) {
     Body* b = B(w, id); if (!b) return fail("bad id");
     b->q = Q(q[0], q[1], q[2], q[3]);
     b->updateGeometry();
+    b->alertWaking();
     return CPGPU_OK;
 }
 int cport_body_set_position(cpgpu_world* w, uint32_t id, const double p[3]) {
     Body* b = B(w, id); if (!b) return fail("bad id");
     b->com += v3(p) - b->trackedP(0);
     b->updateGeometry();
+    b->alertWaking();
     return CPGPU_OK;
 }
 // RigidBody::setMass (RigidBody.cpp:80-89)

@@ -426,3 +426,47 @@ def test_raycast_restatement_matches_reference(oracle_mod):
     kinds = [op[0] for op in sc.ops if op[0] in ("hull", "box", "sphere", "cylinder", "capsule", "mesh")]
     hit = r.raycast(o, d)["body"]
     assert {kinds[b - 1] for b in hit[hit > 0]} >= {"box", "sphere", "cylinder", "capsule", "hull", "mesh"}
+
+
+def _sleep_scene(seed):
+    params = dict(step_time=1.0 / 60.0, substeps=1, pgs=(10, 1, 1), sleeping=True)
+    sc = scenes.Scene(f"sleepers_{seed}", params)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, scenes.PILE_MATERIAL, scenes.FIXED)
+    rng = np.random.default_rng(seed)
+    for i in range(3):
+        for j in range(3):
+            sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, scenes.PILE_MATERIAL, scenes.DYNAMIC,
+                   (3.0 * i - 3, 0.6 + 1.05 * j, 0.1 * rng.uniform()))
+    ball = sc.sphere((0, 0, 0), 0.5, scenes.PILE_MATERIAL, scenes.DYNAMIC, (8.0, 2.0, 0.0))
+    return sc, ball, 3.0 + 0.2 * rng.uniform()
+
+
+@pytest.mark.parametrize("seed", [0, 2])
+def test_restatement_bitwise_with_sleeping(oracle_mod, seed):
+    """Sleeping enabled (PhysicsEngine.cpp:65-87, 174, 1113-1136, 1221-1290,
+    1536-1613; Contact::isExpired): three box stacks and a ball settle and
+    fall asleep, a velocity set on a sleeping box wakes it, the ball is then
+    dropped onto a sleeping stack and wakes it, and the boxes fall asleep
+    again; bit-identical to the reference over 500 steps."""
+    sc, ball, x = _sleep_scene(seed)
+    r, p = oracle_mod.twin_worlds(sc)
+    saw_all_asleep = saw_wake = False
+    for s in range(500):
+        if s == 150:
+            for w in (r, p):
+                w.set_velocity(3, (0.5, 0.0, 0.0))
+        if s == 300:
+            for w in (r, p):
+                w.set_position(ball, (x, 4.5, 0.1))
+                w.set_velocity(ball, (0.0, -3.0, 0.0))
+        r.step(1)
+        p.step(1)
+        st = r.state()
+        assert _states_equal(st, p.state()), f"state differs at step {s}"
+        moving = np.linalg.norm(st["vel"], axis=1) > 0
+        if s == 149:
+            saw_all_asleep = not moving.any()               # asleep bodies have exactly zero velocity
+        if 300 < s < 330 and moving[:-1].sum() >= 2:
+            saw_wake = True                                  # the impact woke boxes of the stack
+    assert saw_all_asleep and saw_wake
+    assert (np.linalg.norm(r.state()["vel"], axis=1) == 0).sum() >= 5   # the plate and most boxes asleep again
