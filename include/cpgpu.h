@@ -110,20 +110,6 @@ int cpgpu_body_hull(cpgpu_world* w, const double* points, int n_points,
                     const int* face_offsets, const int* face_indices, int n_faces,
                     const cpgpu_material* mat, int movement, const double pos[3],
                     uint32_t* out_id);
-/* PhysicsEngine::raycastFirstIntersection (PhysicsEngine.cpp:582-609) for
- * n_rays rays at once.  Ray k starts at origins[3k..3k+2] with the unit
- * direction dirs[3k..3k+2]; the bodies whose ids are listed in `ignore`
- * (n_ignore of them) are skipped.  Every body whose current AABB the ray
- * crosses (AABB::rayIntersectsAABB, AABB.h:143-172) is tested with its
- * primitive's ray test (RigidBody::checkRayIntersection, RigidBody.cpp:185-204;
- * ConvexPrimitive.cpp:113-212, 300-318, 403-411, 445-447, 731-758;
- * Geometry.cpp:867-897) and the nearest hit wins.  The reference filters with
- * its broadphase tree, whose leaves hold the AABBs of the start of the last
- * step; this call uses the current ones.  Outputs per ray (any may be NULL):
- * hit_body (0: no hit), hit_pos (3), hit_normal (3), hit_dist (-1: no hit). */
-int cpgpu_raycast(cpgpu_world* w, const double* origins, const double* dirs, int n_rays,
-                  const uint32_t* ignore, int n_ignore, uint32_t* hit_body,
-                  double* hit_pos, double* hit_normal, double* hit_dist);
 /* createRigidBody(ConvexUnionGeometry::box(corner, dx, dy, dz, material), ...)
  * (Geometry.cpp:14-37) */
 int cpgpu_body_box(cpgpu_world* w, const double corner[3], double dx, double dy, double dz,
@@ -201,6 +187,20 @@ int cpgpu_get_contacts(cpgpu_world* w, cpgpu_contact* out, int cap, int* n);
 /* Replace the whole contact graph (a checkpoint restore).  Same layout and
  * order as cpgpu_get_contacts. */
 int cpgpu_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n);
+/* PhysicsEngine::raycastFirstIntersection (PhysicsEngine.cpp:582-609) for
+ * n_rays rays at once.  Ray k starts at origins[3k..3k+2] with the unit
+ * direction dirs[3k..3k+2]; the bodies whose ids are listed in `ignore`
+ * (n_ignore of them) are skipped.  Every body whose current AABB the ray
+ * crosses (AABB::rayIntersectsAABB, AABB.h:143-172) is tested with its
+ * primitive's ray test (RigidBody::checkRayIntersection, RigidBody.cpp:185-204;
+ * ConvexPrimitive.cpp:113-212, 300-318, 403-411, 445-447, 731-758;
+ * Geometry.cpp:867-897) and the nearest hit wins.  The reference filters with
+ * its broadphase tree, whose leaves hold the AABBs of the start of the last
+ * step; this call uses the current ones.  Outputs per ray (any may be NULL):
+ * hit_body (0: no hit), hit_pos (3), hit_normal (3), hit_dist (-1: no hit). */
+int cpgpu_raycast(cpgpu_world* w, const double* origins, const double* dirs, int n_rays,
+                  const uint32_t* ignore, int n_ignore, uint32_t* hit_body,
+                  double* hit_pos, double* hit_normal, double* hit_dist);
 /* Warm-start state of the joints in creation order (the impulse of each
  * BallSocketConstraint / HingeConstraint, PersistentConstraint.h:118-313, and
  * a hinge's tangent basis u, w of its last rebuild): impulse 5 doubles per
