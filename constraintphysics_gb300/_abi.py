@@ -32,6 +32,7 @@ SIGNATURES = {
     "body_cylinder": (I, [P, P, D, D, P, I, P, P]),
     "body_capsule": (I, [P, P, D, D, P, I, P, P]),
     "raycast": (I, [P, P, P, I, P, I, P, P, P, P]),
+    "body_union": (I, [P, P, I, I, P, P]),
     "body_mesh": (I, [P, P, I, P, I, P, I, P]),
     "body_set_velocity": (I, [P, U32, P]),
     "body_set_ang_velocity": (I, [P, U32, P]),
@@ -76,6 +77,16 @@ class Material(C.Structure):
     """Mirror of struct cpgpu_material (include/cpgpu.h)."""
     _fields_ = [("density", C.c_double), ("restitution", C.c_double),
                 ("kinetic_friction", C.c_double), ("static_friction", C.c_double)]
+
+
+class Primitive(C.Structure):
+    """Mirror of struct cpgpu_primitive (include/cpgpu.h)."""
+    _fields_ = [("kind", C.c_int), ("p", C.c_double * 3), ("a", C.c_double), ("b", C.c_double), ("c", C.c_double),
+                ("points", C.c_void_p), ("n_points", C.c_int), ("face_offsets", C.c_void_p),
+                ("face_indices", C.c_void_p), ("n_faces", C.c_int), ("mat", Material)]
+
+
+PRIM_KINDS = {"hull": 0, "box": 1, "sphere": 2, "cylinder": 3, "capsule": 4}
 
 
 def bind(lib, prefix, optional=()):

@@ -1684,6 +1684,24 @@ int cpgpu_body_capsule(cpgpu_world* w, const double bot[3], double radius, doubl
         return CPGPU_OK;
     });
 }
+// createRigidBody(ConvexUnionGeometry) of one primitive: the single-primitive
+// calls; several primitives per body are not on the device path
+int cpgpu_body_union(cpgpu_world* w, const cpgpu_primitive* prims, int n, int movement, const double pos[3],
+                     uint32_t* out_id) {
+    W_OR_FAIL(w);
+    if (!prims || n < 1) return fail(CPGPU_ERR_INVALID_ARG, "a union needs >= 1 primitive");
+    if (n > 1) return fail(CPGPU_ERR_UNSUPPORTED, "multi-primitive bodies are not implemented on the device path");
+    const cpgpu_primitive& q = prims[0];
+    switch (q.kind) {
+    case CPGPU_PRIM_HULL:
+        return cpgpu_body_hull(w, q.points, q.n_points, q.face_offsets, q.face_indices, q.n_faces, &q.mat, movement, pos, out_id);
+    case CPGPU_PRIM_BOX: return cpgpu_body_box(w, q.p, q.a, q.b, q.c, &q.mat, movement, pos, out_id);
+    case CPGPU_PRIM_SPHERE: return cpgpu_body_sphere(w, q.p, q.a, &q.mat, movement, pos, out_id);
+    case CPGPU_PRIM_CYLINDER: return cpgpu_body_cylinder(w, q.p, q.a, q.b, &q.mat, movement, pos, out_id);
+    case CPGPU_PRIM_CAPSULE: return cpgpu_body_capsule(w, q.p, q.a, q.b, &q.mat, movement, pos, out_id);
+    default: return fail(CPGPU_ERR_INVALID_ARG, "bad primitive kind");
+    }
+}
 // createRigidBody(StaticMeshGeometry(MeshInput{tris, points}), fixed)
 // (PhysicsEngine.cpp:498-512, RigidBody.cpp:41-58): a fixed body at the
 // origin whose triangles are in world coordinates

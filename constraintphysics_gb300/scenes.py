@@ -97,6 +97,10 @@ class Scene:
     def cylinder(self, base, r, h, material, movement, pos=(0, 0, 0)):
         return self._body(("cylinder", tuple(base), r, h, material, movement, tuple(pos)))
 
+    def union(self, prims, movement, pos=(0, 0, 0)):
+        """A multi-primitive body (see World.add_union for the primitive tuples)."""
+        return self._body(("union", tuple(prims), movement, tuple(pos)))
+
     def capsule(self, bot, r, h, material, movement, pos=(0, 0, 0)):
         return self._body(("capsule", tuple(bot), r, h, material, movement, tuple(pos)))
 
@@ -124,7 +128,7 @@ class Scene:
 
     def movements(self):
         """Movement type of each body, in id order."""
-        slot = {"hull": 4, "box": 6, "sphere": 4, "cylinder": 5, "capsule": 5}
+        slot = {"hull": 4, "box": 6, "sphere": 4, "cylinder": 5, "capsule": 5, "union": 2}
         return [FIXED if op[0] == "mesh" else op[slot[op[0]]] for op in self.ops if op[0] in slot or op[0] == "mesh"]
 
 
@@ -144,6 +148,8 @@ def apply(scene, world):
             ids.append(world.add_cylinder(op[1], op[2], op[3], op[4], op[5], op[6]))
         elif kind == "capsule":
             ids.append(world.add_capsule(op[1], op[2], op[3], op[4], op[5], op[6]))
+        elif kind == "union":
+            ids.append(world.add_union(list(op[1]), op[2], op[3]))
         elif kind == "mesh":
             ids.append(world.add_mesh(op[1], op[2], op[3], True))
         elif kind == "orient":
@@ -412,6 +418,44 @@ def kinematic_push(seed=0):
         sc.box((-0.4, -0.4, -0.4), 0.8, 0.8, 0.8, PILE_MATERIAL, DYNAMIC, pos)
     sc.sphere((0.0, 0.0, 0.0), 0.4, PILE_MATERIAL, DYNAMIC, (5.5, 1.0, 0.5))
     sc.capsule((0.0, -0.4, 0.0), 0.25, 0.8, PILE_MATERIAL, DYNAMIC, (4.2, 1.2, -0.6))
+    return sc
+
+
+def union_drop(seed=0, n=8, terrain=False):
+    """Multi-primitive bodies (ConvexUnionGeometry::merge): L-shapes of two
+    boxes, dumbbells (a capsule and two spheres), small tables (a box top on
+    four cylinder legs) and hull-sphere pairs, dropped with single boxes on
+    the plate or on a 16 x 16 value-noise terrain mesh."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(f"union_drop_{n}_{'terrain' if terrain else 'plate'}_seed{seed}", MIXED_PARAMS)
+    if terrain:
+        hts = value_noise(rng, 16)
+        pts, tris = grid_mesh(hts, 1.0, (-8.0, 0.0, -8.0))
+        sc.mesh(pts, tris, PILE_MATERIAL)
+    else:
+        _plate(sc)
+    lift = float(hts.max()) + 1.0 if terrain else 0.0
+    m = PILE_MATERIAL
+    for i in range(n):
+        pos = np.array([(i % 4) * 3.2 - 4.8, 2.0 + lift + 2.5 * (i // 4), (i % 3) * 1.5 - 1.5]) + rng.uniform(-0.1, 0.1, 3)
+        kind = i % 5
+        if kind == 0:
+            prims = [("box", (-0.5, -0.25, -0.25), 1.0, 0.5, 0.5, m), ("box", (0.25, 0.25, -0.25), 0.5, 1.0, 0.5, m)]
+        elif kind == 1:
+            prims = [("capsule", (0.0, -0.6, 0.0), 0.15, 1.2, m), ("sphere", (0.0, 0.75, 0.0), 0.35, m),
+                     ("sphere", (0.0, -0.75, 0.0), 0.35, m)]
+        elif kind == 2:
+            prims = [("box", (-0.8, 0.4, -0.6), 1.6, 0.2, 1.2, m)]
+            prims += [("cylinder", (x, -0.4, z), 0.1, 0.8, m) for x in (-0.65, 0.65) for z in (-0.45, 0.45)]
+        elif kind == 3:
+            pts, faces = random_hull(rng, 10, 20)
+            prims = [("hull", pts * 0.8, faces, m), ("sphere", (0.0, 0.9, 0.0), 0.4, m)]
+        else:
+            d = rng.uniform(0.6, 1.2, size=3)
+            sc.box((-d[0] / 2, -d[1] / 2, -d[2] / 2), d[0], d[1], d[2], m, DYNAMIC, pos)
+            continue
+        bid = sc.union(prims, DYNAMIC, pos)
+        sc.orient(bid, random_quat(rng))
     return sc
 
 

@@ -140,6 +140,37 @@ class World:
                                    int(movement), _ptr(pos), C.addressof(out))
         return self._new_id(rc, out)
 
+    def add_union(self, prims, movement=0, pos=(0, 0, 0)):
+        """ConvexUnionGeometry::merge of primitives, each a tuple:
+        ("box", corner, dx, dy, dz, material), ("sphere", centre, r, material),
+        ("cylinder", base, r, h, material), ("capsule", bot, r, h, material) or
+        ("hull", points, faces, material)."""
+        from ._abi import Primitive, PRIM_KINDS
+        arr = (Primitive * len(prims))()
+        keep = []
+        for q, pr in zip(arr, prims):
+            kind = pr[0]
+            q.kind = PRIM_KINDS[kind]
+            if kind == "hull":
+                pts = _f64(pr[1])
+                offs = np.zeros(len(pr[2]) + 1, dtype=np.int32)
+                for i, f in enumerate(pr[2]):
+                    offs[i + 1] = offs[i] + len(f)
+                idx = np.ascontiguousarray([v for f in pr[2] for v in f], dtype=np.int32)
+                keep += [pts, offs, idx]
+                q.points, q.n_points = pts.ctypes.data, pts.size // 3
+                q.face_offsets, q.face_indices, q.n_faces = offs.ctypes.data, idx.ctypes.data, len(pr[2])
+                q.mat = self._mat(pr[3])
+            else:
+                q.p[:] = [float(x) for x in pr[1]]
+                vals = [float(x) for x in pr[2:-1]] + [0.0] * 3
+                q.a, q.b, q.c = vals[:3]
+                q.mat = self._mat(pr[-1])
+        pos = _f64(pos, 3)
+        out = C.c_uint32()
+        rc = self.abi.body_union(self.h, C.addressof(arr), len(prims), int(movement), _ptr(pos), C.addressof(out))
+        return self._new_id(rc, out)
+
     def raycast(self, origins, dirs, ignore=()):
         """raycastFirstIntersection for each row of `origins` / `dirs` (unit
         directions): dict of body (0: no hit), pos, normal, dist (-1: no hit)."""

@@ -134,6 +134,31 @@ int cpgpu_body_cylinder(cpgpu_world* w, const double base[3], double radius, dou
 int cpgpu_body_capsule(cpgpu_world* w, const double bot[3], double radius, double drum_height,
                        const cpgpu_material* mat, int movement, const double pos[3],
                        uint32_t* out_id);
+/* One primitive of a multi-primitive body (ConvexUnionGeometry, Geometry.h:9-47). */
+#define CPGPU_PRIM_HULL 0
+#define CPGPU_PRIM_BOX 1
+#define CPGPU_PRIM_SPHERE 2
+#define CPGPU_PRIM_CYLINDER 3
+#define CPGPU_PRIM_CAPSULE 4
+typedef struct cpgpu_primitive {
+    int kind;               /* CPGPU_PRIM_* */
+    double p[3];            /* box corner, sphere centre, cylinder base, capsule bottom-sphere centre */
+    double a, b, c;         /* box dx dy dz; sphere radius; cylinder radius, height; capsule radius, drum height */
+    const double* points;   /* hull: points (xyz) and faces as for cpgpu_body_hull */
+    int n_points;
+    const int* face_offsets;
+    const int* face_indices;
+    int n_faces;
+    cpgpu_material mat;
+} cpgpu_primitive;
+/* createRigidBody(ConvexUnionGeometry::merge(...) of the n primitives in
+ * order, movement, pos) (Geometry.cpp:540-550, RigidBody.cpp:13-39): mass
+ * properties summed over the primitives, each primitive its own AABB and
+ * material, pairs of bodies tested primitive pair by primitive pair
+ * (PhysicsEngine.cpp:182-219).  The device path takes n = 1 (the same as the
+ * single-primitive calls); n > 1 returns CPGPU_ERR_UNSUPPORTED there. */
+int cpgpu_body_union(cpgpu_world* w, const cpgpu_primitive* prims, int n, int movement, const double pos[3],
+                     uint32_t* out_id);
 /* createRigidBody(StaticMeshGeometry(MeshInput{tris, points}), fixed)
  * (PhysicsEngine.cpp:498-512, Geometry.h:52-55): points (xyz) and triangles
  * (three point indices each) in world coordinates; `fixed` must be nonzero

@@ -106,7 +106,7 @@ def twin_worlds(scene):
             def both(*a, **k):
                 out = fr(*a, **k)
                 fp(*a, **k)
-                if name in ("add_hull", "add_box", "add_sphere", "add_cylinder", "add_capsule"):
+                if name in ("add_hull", "add_box", "add_sphere", "add_cylinder", "add_capsule", "add_union"):
                     m = np.zeros(1); c = np.zeros(3); t = np.zeros(9)
                     assert get(r.h, out, m.ctypes.data, c.ctypes.data, t.ctypes.data) == 0
                     assert put(p.h, out, float(m[0]), c.ctypes.data, t.ctypes.data) == 0
@@ -120,7 +120,7 @@ def twin_worlds(scene):
     return r, p
 
 
-_CREATE = ("add_hull", "add_box", "add_sphere", "add_cylinder", "add_capsule", "add_mesh")
+_CREATE = ("add_hull", "add_box", "add_sphere", "add_cylinder", "add_capsule", "add_union", "add_mesh")
 
 
 class _Hooked:

@@ -262,7 +262,7 @@ struct CylG {
 // Capsule (ConvexPrimitive.h:107-141): centre, radius, drum height (the
 // distance between the two cap-sphere centres) and height axis
 struct CapG { V3 c, axis; double r = 0, h = 0; };
-enum Kind { K_HULL = 0, K_SPHERE = 1, K_CYLINDER = 2, K_MESH = 3, K_CAPSULE = 4 };
+enum Kind { K_HULL = 0, K_SPHERE = 1, K_CYLINDER = 2, K_MESH = 3, K_CAPSULE = 4, K_UNION = 5 };
 
 // StaticMeshFace (Geometry.h:74-86) as built by StaticMeshGeometry's
 // constructor (Geometry.cpp:675-820)
@@ -303,6 +303,10 @@ struct Body {
     SphereG sph_src, sph_ref, sph;
     CylG cyl_src, cyl_ref, cyl;
     CapG cap_src, cap_ref, cap;
+    // several primitives (ConvexUnionGeometry): each part holds one primitive's
+    // kind, material, source / reference / world geometry and AABB; its id
+    // (body id << 8 | index) names it in contact ids
+    std::vector<std::unique_ptr<Body>> parts;
     std::vector<MeshTri> tris;    // static mesh (world coordinates)
     MeshTree tree;
     AABB aabb;
@@ -466,6 +470,7 @@ struct World {
     Body* addSphere(V3 center, double r, const Material& m, int movement, V3 pos);
     Body* addCylinder(V3 base, double r, double h, const Material& m, int movement, V3 pos);
     Body* addCapsule(V3 bot, double r, double h, const Material& m, int movement, V3 pos);
+    Body* addUnion(std::vector<std::unique_ptr<Body>> parts, int movement, V3 pos);
     Body* finishBody(std::unique_ptr<Body> b, double mass, const V3& com, const M3& tensor);
     Body* addMesh(const std::vector<V3>& points, const std::vector<std::array<int, 3>>& tris, const Material& m);
     void placeBody(Body* b, double mass, const V3& com_geom, const M3& tensor);

@@ -13,6 +13,7 @@ extern "C" {
 namespace cport {
 
 // ------------------------------------------------------------ bodies ----
+static AABB boxUnion(const AABB& a, const AABB& b);
 static AABB genAABB(const Hull& h) {
     const double inf = std::numeric_limits<double>::infinity();
     AABB a{V3(inf, inf, inf), V3(-inf, -inf, -inf)};
@@ -62,10 +63,39 @@ static void cylFromReference(CylG& out, const CylG& ref, const M3& rot, const V3
 }
 
 // RigidBody::updateGeometry (RigidBody.cpp:281-312) for a single primitive
+// one primitive's world geometry from its reference geometry at (rot, com)
+// (the primitives' recomputeFromReference, ConvexPrimitive.cpp:272-287,
+// 383-388, 433-437, 715-729) and its AABB
+static void partWorld(Body* g, const M3& rot, const V3& com) {
+    if (g->kind == K_SPHERE) {
+        g->sph.c = com + rot * g->sph_ref.c;
+        g->aabb = genAABB(g->sph);
+    } else if (g->kind == K_CYLINDER) {
+        cylFromReference(g->cyl, g->cyl_ref, rot, com);
+        g->aabb = genAABB(g->cyl);
+    } else if (g->kind == K_CAPSULE) {
+        g->cap.c = com + rot * g->cap_ref.c;
+        g->cap.axis = rot * g->cap_ref.axis;
+        g->aabb = genAABB(g->cap);
+    } else {
+        for (size_t i = 0; i < g->shape.pts.size(); i++) g->shape.pts[i] = com + rot * g->ref_shape.pts[i];
+        g->shape.interior = com + rot * g->ref_shape.interior;
+        for (size_t i = 0; i < g->shape.gv.size(); i++) g->shape.gv[i] = rot * g->ref_shape.gv[i];
+        g->aabb = genAABB(g->shape);
+    }
+}
+
 void Body::updateGeometry() {
     if (kind == K_MESH) return;   // fixed meshes stay in world coordinates
     q = q.normalize();
     M3 rot = q.rotMatrix();
+    if (kind == K_UNION) {   // every primitive, then AABB::combine of theirs
+        for (size_t i = 0; i < parts.size(); i++) {
+            partWorld(parts[i].get(), rot, com);
+            aabb = i == 0 ? parts[i]->aabb : boxUnion(aabb, parts[i]->aabb);
+        }
+        return;
+    }
     if (kind == K_SPHERE) {
         sph.c = com + rot * sph_ref.c;            // Sphere::recomputeFromReference (ConvexPrimitive.cpp:433-437)
         aabb = genAABB(sph);
@@ -253,6 +283,43 @@ Body* World::addCapsule(V3 bot, double r, double h, const Material& m, int movem
     return finishBody(std::move(b), mass, com, tensor);
 }
 
+// createRigidBody(ConvexUnionGeometry of several primitives) (RigidBody.cpp:
+// 13-39, 427-640): mass, centre of mass and tensor summed over the primitives
+// in order (hulls by the tetrahedral decomposition, to rounding)
+Body* World::addUnion(std::vector<std::unique_ptr<Body>> parts, int movement, V3 pos) {
+    auto b = std::make_unique<Body>();
+    b->kind = K_UNION;
+    b->movement = movement;
+    b->mat = parts.front()->mat;
+    b->create_pos = pos;
+    const uint32_t id = (uint32_t)bodies.size() + 1;
+    double msum = 0;
+    V3 csum;
+    M3 tsum;
+    for (size_t i = 0; i < parts.size(); i++) {
+        Body* g = parts[i].get();
+        g->id = (id << 8) | (uint32_t)i;
+        g->movement = movement;
+        double m;
+        V3 c;
+        M3 t;
+        if (g->kind == K_HULL) {
+            massProperties(g->src_shape, g->mat.density, &c, &t, &m);
+            t = recenterTensor(m, t, V3(0, 0, 0), c, c);
+        } else {
+            primitiveMass(*g, &m, &c, &t);
+            t = recenterTensor(m, t, V3(0, 0, 0), c, c);
+        }
+        tsum = tsum + t;
+        csum = csum + m * c;
+        msum = msum + m;
+    }
+    V3 com = csum / msum;
+    M3 tensor = recenterTensor(msum, tsum, com, V3(0, 0, 0), com);
+    b->parts = std::move(parts);
+    return finishBody(std::move(b), msum, com, tensor);
+}
+
 Body* World::finishBody(std::unique_ptr<Body> b, double mass, const V3& com, const M3& tensor) {
     b->id = (uint32_t)bodies.size() + 1;
     Body* raw = b.get();
@@ -276,7 +343,27 @@ void World::placeBody(Body* b, double mass, const V3& com_geom, const M3& tensor
     b->q = Q();
     M3 I = M3::iden();
     V3 mc = -b->com;
-    if (b->kind == K_SPHERE) {
+    if (b->kind == K_UNION) {
+        // each primitive's reference geometry recentred on the body's COM
+        // (RigidBody.cpp:23-25)
+        for (auto& g : b->parts) {
+            g->sph_ref = g->sph_src;
+            g->sph_ref.c = mc + I * g->sph_src.c;
+            g->cyl_ref = g->cyl_src;
+            if (g->kind == K_CYLINDER) cylFromReference(g->cyl_ref, g->cyl_src, I, mc);
+            g->cap_ref = g->cap_src;
+            g->cap_ref.c = mc + I * g->cap_src.c;
+            g->cap_ref.axis = I * g->cap_src.axis;
+            g->ref_shape = g->src_shape;
+            for (V3& pt : g->ref_shape.pts) pt = mc + I * pt;
+            g->ref_shape.interior = mc + I * g->ref_shape.interior;
+            for (V3& gv : g->ref_shape.gv) gv = I * gv;
+            g->sph = g->sph_src;
+            g->cyl = g->cyl_src;
+            g->cap = g->cap_src;
+            g->shape = g->src_shape;
+        }
+    } else if (b->kind == K_SPHERE) {
         b->sph_ref = b->sph_src;
         b->sph_ref.c = mc + I * b->sph_src.c;
         b->sph = b->sph_src;
@@ -903,13 +990,30 @@ void World::step() {
         if (b1->no_collide.count(b2)) continue;   // collisionAllowed (PhysicsEngine.cpp:570-572)
         if (b1->kind == K_MESH && b2->kind == K_MESH) continue;
         std::vector<Manifold> mans;
+        // a body's primitives: itself, or the parts of a union
+        auto prims = [](Body* b) {
+            std::vector<Body*> v;
+            if (b->kind == K_UNION) for (auto& g : b->parts) v.push_back(g.get());
+            else v.push_back(b);
+            return v;
+        };
         if (b2->kind == K_MESH) {
-            mans = meshCollide(b1, b2);
+            for (Body* g : prims(b1))
+                for (Manifold& x : meshCollide(g, b2)) mans.push_back(x);
         } else if (b1->kind == K_MESH) {
-            for (Manifold& x : meshCollide(b2, b1)) mans.push_back(flipped(x));
+            for (Body* g : prims(b2))
+                for (Manifold& x : meshCollide(g, b1)) mans.push_back(flipped(x));
         } else {
-            Manifold man = collide(b1, b2);
-            if (man.max_pen > 0) mans.push_back(man);
+            // primitive pairs, skipping those whose AABBs miss unless both
+            // bodies have one primitive (PhysicsEngine.cpp:182-219)
+            const std::vector<Body*> p1 = prims(b1), p2 = prims(b2);
+            const bool single = p1.size() == 1 && p2.size() == 1;
+            for (Body* g1 : p1)
+                for (Body* g2 : p2) {
+                    if (!single && !AABB::overlap(g1->aabb, g2->aabb)) continue;
+                    Manifold man = collide(g1, g2);
+                    if (man.max_pen > 0) mans.push_back(man);
+                }
         }
         // manifolds with normals within 1 degree merge (PhysicsEngine.cpp:257-295)
         std::vector<char> merged(mans.size(), 0);
@@ -1122,6 +1226,62 @@ int cport_body_capsule(cpgpu_world* w, const double bot[3], double radius, doubl
                        int movement, const double pos[3], uint32_t* out_id) {
     if (!(radius > 0) || !(drum_height >= 0)) return fail("capsule radius must be > 0 and drum height >= 0");
     Body* b = W(w)->addCapsule(v3(bot), radius, drum_height, mat(m), movement, v3(pos));
+    if (out_id) *out_id = b->id;
+    return CPGPU_OK;
+}
+// createRigidBody(ConvexUnionGeometry::merge of the primitives in order)
+int cport_body_union(cpgpu_world* w, const cpgpu_primitive* prims, int n, int movement, const double pos[3],
+                     uint32_t* out_id) {
+    if (!prims || n < 1 || n > 255) return fail("a union needs 1 to 255 primitives");
+    std::vector<std::unique_ptr<Body>> parts;
+    for (int i = 0; i < n; i++) {
+        const cpgpu_primitive& q = prims[i];
+        auto g = std::make_unique<Body>();
+        g->mat = mat(&q.mat);
+        switch (q.kind) {
+        case CPGPU_PRIM_HULL: {
+            if (q.n_points < 4 || q.n_faces < 4) return fail("hull needs >= 4 points and faces");
+            std::vector<V3> pts(q.n_points);
+            for (int k = 0; k < q.n_points; k++) pts[k] = V3(q.points[3 * k], q.points[3 * k + 1], q.points[3 * k + 2]);
+            std::vector<std::vector<int>> faces(q.n_faces);
+            for (int f = 0; f < q.n_faces; f++)
+                for (int k = q.face_offsets[f]; k < q.face_offsets[f + 1]; k++) faces[f].push_back(q.face_indices[k]);
+            g->kind = K_HULL;
+            g->src_shape.build(pts, faces);
+            break;
+        }
+        case CPGPU_PRIM_BOX: {
+            // ConvexUnionGeometry::box (Geometry.cpp:14-37)
+            const V3 c = v3(q.p);
+            const double dx = q.a, dy = q.b, dz = q.c;
+            std::vector<V3> pts = {c, c + V3(dx, 0, 0), c + V3(dx, dy, 0), c + V3(0, dy, 0),
+                                   c + V3(0, 0, dz), c + V3(dx, 0, dz), c + V3(dx, dy, dz), c + V3(0, dy, dz)};
+            std::vector<std::vector<int>> faces = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+            g->kind = K_HULL;
+            g->src_shape.build(pts, faces);
+            break;
+        }
+        case CPGPU_PRIM_SPHERE:
+            g->kind = K_SPHERE;
+            g->sph_src.c = v3(q.p);
+            g->sph_src.r = q.a;
+            break;
+        case CPGPU_PRIM_CYLINDER:
+            g->kind = K_CYLINDER;
+            g->cyl_src = makeCylinder(v3(q.p) + V3(0, q.b / 2.0, 0), q.a, q.b);
+            break;
+        case CPGPU_PRIM_CAPSULE:
+            g->kind = K_CAPSULE;
+            g->cap_src.c = v3(q.p) + V3(0, q.b / 2.0, 0);
+            g->cap_src.axis = V3(0, 1, 0);
+            g->cap_src.r = q.a;
+            g->cap_src.h = q.b;
+            break;
+        default: return fail("bad primitive kind");
+        }
+        parts.push_back(std::move(g));
+    }
+    Body* b = W(w)->addUnion(std::move(parts), movement, v3(pos));
     if (out_id) *out_id = b->id;
     return CPGPU_OK;
 }
@@ -1378,6 +1538,14 @@ RayHit rayMesh(const Body* m, const V3& o, const V3& d) {
 // primitives' testRayIntersection (ConvexPrimitive.cpp:205-212, 308-318,
 // 403-411, 445-447)
 RayHit rayBody(const Body* b, const V3& o, const V3& d) {
+    if (b->kind == K_UNION) {   // each primitive behind its own AABB (RigidBody.cpp:188-197)
+        RayHit out;
+        for (const auto& g : b->parts) {
+            if (b->parts.size() != 1 && !rayAABB(g->aabb, o, d)) continue;
+            nearer(&out, rayBody(g.get(), o, d));
+        }
+        return out;
+    }
     switch (b->kind) {
     case K_MESH: return rayMesh(b, o, d);
     case K_SPHERE: return raySphere(o, d, b->sph.c, b->sph.r);

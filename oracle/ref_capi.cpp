@@ -224,6 +224,38 @@ int cpref_body_capsule(cpgpu_world* w, const double bot[3], double radius, doubl
     return finish_body(RW, r, out_id);
 }
 
+// ConvexUnionGeometry::merge of the primitives in order (Geometry.cpp:540-550)
+int cpref_body_union(cpgpu_world* w, const cpgpu_primitive* prims, int n, int movement, const double pos[3],
+                     uint32_t* out_id) {
+    if (!prims || n < 1) return fail("a union needs >= 1 primitive");
+    phyz::ConvexUnionGeometry g;
+    for (int i = 0; i < n; i++) {
+        const cpgpu_primitive& q = prims[i];
+        phyz::Material m = to_mat(&q.mat);
+        phyz::ConvexUnionGeometry gi;
+        switch (q.kind) {
+        case CPGPU_PRIM_HULL: {
+            std::vector<mthz::Vec3> pts(q.n_points);
+            for (int k = 0; k < q.n_points; k++) pts[k] = mthz::Vec3(q.points[3 * k], q.points[3 * k + 1], q.points[3 * k + 2]);
+            std::vector<std::vector<uint32_t>> faces(q.n_faces);
+            for (int f = 0; f < q.n_faces; f++)
+                for (int k = q.face_offsets[f]; k < q.face_offsets[f + 1]; k++) faces[f].push_back((uint32_t)q.face_indices[k]);
+            phyz::Polyhedron poly(pts, faces);
+            gi = phyz::ConvexUnionGeometry(phyz::ConvexPrimitive((const phyz::ConvexGeometry&)poly, m));
+            break;
+        }
+        case CPGPU_PRIM_BOX: gi = phyz::ConvexUnionGeometry::box(v3(q.p), q.a, q.b, q.c, m); break;
+        case CPGPU_PRIM_SPHERE: gi = phyz::ConvexUnionGeometry::sphere(v3(q.p), q.a, m); break;
+        case CPGPU_PRIM_CYLINDER: gi = phyz::ConvexUnionGeometry::cylinder(v3(q.p), q.a, q.b, m); break;
+        case CPGPU_PRIM_CAPSULE: gi = phyz::ConvexUnionGeometry::capsule(v3(q.p), q.a, q.b, m); break;
+        default: return fail("bad primitive kind");
+        }
+        g = i == 0 ? gi : phyz::ConvexUnionGeometry::merge(g, gi);
+    }
+    phyz::RigidBody* r = RW->engine.createRigidBody(g, (phyz::RigidBody::MovementType)movement, v3(pos));
+    return finish_body(RW, r, out_id);
+}
+
 int cpref_body_mesh(cpgpu_world* w, const double* points, int n_points, const int* tris, int n_tris,
                     const cpgpu_material* mat, int fixed, uint32_t* out_id) {
     phyz::MeshInput in;
