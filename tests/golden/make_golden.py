@@ -108,11 +108,26 @@ def kinematic():
                         magic_b=c["magic_b"], b1=c["b1"], b2=c["b2"], normal_impulse=c["normal_impulse"])
 
 
+def unions():
+    """Multi-primitive bodies on a terrain (scenes.union_drop, seed 2, 10
+    bodies) after 240 reference steps, with creation-time mass properties."""
+    steps = 240
+    sc = scenes.union_drop(seed=2, n=10, terrain=True)
+    mass, com, tensor, w = oracle.capture_mass_properties(sc)
+    w.step(steps)
+    st = w.state()
+    c = w.contacts()
+    np.savez_compressed(os.path.join(HERE, "union_terrain_seed2.npz"), steps=steps, mass=mass, com_geom=com,
+                        tensor=tensor, com=st["com"], quat=st["quat"], vel=st["vel"], ang_vel=st["ang_vel"],
+                        magic_b=c["magic_b"], b1=c["b1"], b2=c["b2"], normal_impulse=c["normal_impulse"])
+
+
 def main(names=()):
     if names:
         for n in names:
             globals()[n]()
         return
+    unions()
     kinematic()
     capsules()
     terrain()

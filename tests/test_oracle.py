@@ -520,3 +520,19 @@ def test_union_mass_properties_agree(oracle_mod):
         assert abs(mr[0] - mp[0]) <= 1e-12 * mr[0], bid
         assert np.abs(cr - cp).max() <= 1e-12 * (1 + np.abs(cr).max()), bid
         assert np.abs(tr - tp).max() <= 1e-10 * np.abs(tr).max(), bid
+
+
+def test_golden_fixture_unions(oracle_mod):
+    """Multi-primitive bodies on the terrain against the committed reference
+    outputs (no reference library needed)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "union_terrain_seed2.npz"))
+    sc = scenes.union_drop(seed=2, n=10, terrain=True)
+    p = oracle_mod.port_world_with_mass(sc, g["mass"], g["com_geom"], g["tensor"])
+    p.step(int(g["steps"]))
+    st = p.state()
+    for k in ("com", "quat", "vel", "ang_vel"):
+        assert np.array_equal(st[k], g[k]), k
+    c = p.contacts()
+    for k in ("b1", "b2", "magic_b", "normal_impulse"):
+        assert np.array_equal(c[k], g[k]), k
