@@ -453,6 +453,7 @@ def main():
                 "config": dict(config, l2="state larger than L2 (%.0f MB resident)" % (batch_bodies * 600 / 1e6),
                                contacts=info["contacts"]),
                 "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                "contacts_per_s": info["contacts"] * world_size / (dev_ms / a.steps / 1e3),
                 "plain": {"value": plain, "unit": UNIT, "sample_worlds": a.plain_sample,
                           "vs_plain": (value / world_size / plain) if plain else None},
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
