@@ -113,6 +113,9 @@ class Scene:
     def ball_socket(self, b1, b2, a1, a2, strength=15000.0):
         self.ops.append(("ball", b1, b2, tuple(a1), tuple(a2), float(strength)))
 
+    def distance(self, b1, b2, a1, a2, target=-1.0, strength=15000.0):
+        self.ops.append(("distance", b1, b2, tuple(a1), tuple(a2), float(target), float(strength)))
+
     def hinge(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
         self.ops.append(("hinge", b1, b2, tuple(a1), tuple(a2), tuple(ax1), tuple(ax2), float(pos_strength),
                          float(rot_strength)))
@@ -160,6 +163,8 @@ def apply(scene, world):
             world.set_ang_velocity(op[1], op[2])
         elif kind == "mass":
             world.set_mass(op[1], op[2])
+        elif kind == "distance":
+            world.add_distance(op[1], op[2], op[3], op[4], op[5], op[6])
         elif kind == "ball":
             world.add_ball_socket(op[1], op[2], op[3], op[4], op[5])
         elif kind == "hinge":

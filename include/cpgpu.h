@@ -180,6 +180,13 @@ int cpgpu_body_set_mass(cpgpu_world* w, uint32_t id, double mass);
 int cpgpu_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2,
                           const double b1_attach_local[3], const double b2_attach_local[3],
                           double pos_correct_strength, uint32_t* out_id);
+/* PhysicsEngine::addDistanceConstraint (PhysicsEngine.cpp:623-660): the
+ * attachment points stay `target_distance` apart (-1: their distance at
+ * creation); DistanceConstraint rows (ConstraintSolver.cpp:348-377).  Not on
+ * the device path yet: returns CPGPU_ERR_UNSUPPORTED there. */
+int cpgpu_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2,
+                       const double b1_attach_local[3], const double b2_attach_local[3],
+                       double target_distance, double pos_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addHingeConstraint (PhysicsEngine.cpp:693-723) */
 int cpgpu_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2,
                     const double b1_attach_local[3], const double b2_attach_local[3],

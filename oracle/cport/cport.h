@@ -361,7 +361,8 @@ struct Edge;
 struct Params;
 // BallSocket / Hinge (PersistentConstraint.h:118-313)
 struct Joint {
-    int n = 3;                    // 3 ball-socket, 5 hinge
+    int n = 3;                    // 1 distance, 3 ball-socket, 5 hinge
+    double target = 0;            // distance: the attachment points' distance
     Body* b1 = nullptr; Body* b2 = nullptr;
     int k1 = 0, k2 = 0;           // tracked point keys
     V3 ax1, ax2;                  // hinge axes in body space (normalised)
@@ -478,7 +479,8 @@ struct World {
     Edge* getOrCreateEdge(Body* a, Body* b);
     void deleteEdge(Edge* e);
     void addContact(Body* b1, Body* b2, const ManifoldPoint& mp, const V3& n);
-    Joint* addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, double pos_hard, double rot_hard);
+    Joint* addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, double pos_hard, double rot_hard,
+                    double target = -1);
     void maintainHolonomicSystems();
     void holonomicScan(Edge* e);
     void updateHolonomicInverses();

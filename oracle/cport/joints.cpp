@@ -99,7 +99,26 @@ void Joint::rebuild(const Params& p, double dts, bool in_holo) {
     V3 rA = pa - b1->com;
     double sa[3][3], sb[3][3];
     crossMatInto(rA, sa);
-    if (n == 3) {
+    if (n == 1) {
+        // Distance::updateSolverConstraints (PersistentConstraint.cpp:217-223)
+        // with the DistanceConstraint constructor (ConstraintSolver.cpp:348-377):
+        // one row along the attachment direction, position error target - |d|
+        V3 rB = pb - b2->com;
+        crossMatInto(rB, sb);
+        V3 diff = pa - pb;
+        V3 dd = diff.normalize();
+        const double dv[3] = {dd.x, dd.y, dd.z};
+        for (int k = 0; k < 3; k++) {
+            double ta = 0, tb = 0;
+            for (int i = 0; i < 3; i++) { ta += (-dv[i]) * sa[i][k]; tb += dv[i] * sb[i][k]; }
+            r.ja[0][k] = dv[k];
+            r.ja[0][3 + k] = ta;
+            r.jb[0][k] = -dv[k];
+            r.jb[0][3 + k] = tb;
+        }
+        double error = diff.mag2() < 0.00001 ? target : target - diff.normalize().dot(diff);
+        r.ptarget[0] = pos_c * error;
+    } else if (n == 3) {
         V3 rB = pb - b2->com;
         crossMatInto(rB, sb);
         for (int i = 0; i < 3; i++) {
@@ -485,7 +504,8 @@ double HoloSys::inverseError(double cfm) const {
 // (PhysicsEngine.cpp:664-723): collisions between the two bodies are
 // disallowed, the anchors become tracked points, the edge is flagged for a
 // holonomic-system scan
-Joint* World::addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, double pos_hard, double rot_hard) {
+Joint* World::addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, double pos_hard, double rot_hard,
+                       double target) {
     b1->no_collide.insert(b2);
     b2->no_collide.insert(b1);
     auto j = std::make_unique<Joint>();
@@ -496,6 +516,9 @@ Joint* World::addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, 
     b2->track_p.push_back(b2->local_origin + p2);
     j->k2 = (int)b2->track_p.size() - 1;
     if (n == 5) { j->ax1 = ax1.normalize(); j->ax2 = ax2.normalize(); }
+    // PhysicsEngine::addDistanceConstraint (PhysicsEngine.cpp:630-635): -1
+    // means the attachment points' current distance
+    if (n == 1) j->target = target == -1 ? (b1->trackedP(j->k1) - b2->trackedP(j->k2)).mag() : target;
     j->pos_hard = pos_hard;
     j->rot_hard = rot_hard;
     j->row.n = n; j->row.a = b1; j->row.b = b2;

@@ -536,3 +536,32 @@ def test_golden_fixture_unions(oracle_mod):
     c = p.contacts()
     for k in ("b1", "b2", "magic_b", "normal_impulse"):
         assert np.array_equal(c[k], g[k]), k
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_restatement_bitwise_with_distance_joints(oracle_mod, mixed):
+    """Distance constraints (PhysicsEngine::addDistanceConstraint,
+    DistanceConstraint rows, ConstraintSolver.cpp:348-377): a hanging chain of
+    spheres linked by distance joints, or by alternating distance and
+    ball-socket joints (one holonomic system, solved by the block LDL), hit by
+    a box; bit-identical to the reference over 300 steps."""
+    M = scenes.PILE_MATERIAL
+    sc = scenes.Scene("distance_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 8.0, 0.0))
+    for i in range(6):
+        b = sc.sphere((0, 0, 0), 0.25, M, scenes.DYNAMIC, (0.9 * (i + 1), 8.0, 0.0))
+        if mixed and i % 2 == 1:
+            sc.ball_socket(prev, b, (0.45, 0, 0), (-0.45, 0, 0))
+        else:
+            sc.distance(prev, b, (0.25, 0, 0), (-0.25, 0, 0))
+        prev = b
+    sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, M, scenes.DYNAMIC, (2.0, 1.0, 0.3))
+    r, p = oracle_mod.twin_worlds(sc)
+    for s in range(300):
+        r.step(1)
+        p.step(1)
+        if s % 50 == 49:
+            assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
+    st = r.state()
+    assert st["com"][2:8, 1].min() < 7.0   # the chain swung down
