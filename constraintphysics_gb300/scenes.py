@@ -116,6 +116,9 @@ class Scene:
     def distance(self, b1, b2, a1, a2, target=-1.0, strength=15000.0):
         self.ops.append(("distance", b1, b2, tuple(a1), tuple(a2), float(target), float(strength)))
 
+    def weld(self, b1, b2, a1, a2, pos_strength=15000.0, rot_strength=15000.0):
+        self.ops.append(("weld", b1, b2, tuple(a1), tuple(a2), float(pos_strength), float(rot_strength)))
+
     def hinge(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
         self.ops.append(("hinge", b1, b2, tuple(a1), tuple(a2), tuple(ax1), tuple(ax2), float(pos_strength),
                          float(rot_strength)))
@@ -165,6 +168,8 @@ def apply(scene, world):
             world.set_mass(op[1], op[2])
         elif kind == "distance":
             world.add_distance(op[1], op[2], op[3], op[4], op[5], op[6])
+        elif kind == "weld":
+            world.add_weld(op[1], op[2], op[3], op[4], op[5], op[6])
         elif kind == "ball":
             world.add_ball_socket(op[1], op[2], op[3], op[4], op[5])
         elif kind == "hinge":

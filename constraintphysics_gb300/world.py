@@ -226,6 +226,13 @@ class World:
                                           float(strength), C.addressof(out)))
         return out.value
 
+    def add_weld(self, b1, b2, a1, a2, pos_strength=15000.0, rot_strength=15000.0):
+        a1, a2 = _f64(a1, 3), _f64(a2, 3)
+        out = C.c_uint32()
+        self._check(self.abi.add_weld(self.h, int(b1), int(b2), _ptr(a1), _ptr(a2), float(pos_strength),
+                                      float(rot_strength), C.addressof(out)))
+        return out.value
+
     def add_hinge(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
         a1, a2, ax1, ax2 = (_f64(x, 3) for x in (a1, a2, ax1, ax2))
         out = C.c_uint32()

@@ -187,6 +187,13 @@ int cpgpu_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2,
 int cpgpu_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2,
                        const double b1_attach_local[3], const double b2_attach_local[3],
                        double target_distance, double pos_correct_strength, uint32_t* out_id);
+/* PhysicsEngine::addWeldConstraint (PhysicsEngine.cpp:892-915): the two
+ * bodies move as one about the attachment points; WeldConstraint rows
+ * (ConstraintSolver.cpp:861-899).  Not on the device path yet: returns
+ * CPGPU_ERR_UNSUPPORTED there. */
+int cpgpu_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2,
+                   const double b1_attach_local[3], const double b2_attach_local[3],
+                   double pos_correct_strength, double rot_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addHingeConstraint (PhysicsEngine.cpp:693-723) */
 int cpgpu_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2,
                     const double b1_attach_local[3], const double b2_attach_local[3],

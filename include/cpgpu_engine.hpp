@@ -193,6 +193,20 @@ public:
         check(cpgpu_add_ball_socket(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), strength, &id));
         return ConstraintID{id};
     }
+    // addDistanceConstraint / addWeldConstraint: the device path reports
+    // CPGPU_ERR_UNSUPPORTED for these joint types for now
+    ConstraintID addDistanceConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, double target = -1,
+                                       double strength = 15000) {
+        uint32_t id = 0;
+        check(cpgpu_add_distance(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), target, strength, &id));
+        return ConstraintID{id};
+    }
+    ConstraintID addWeldConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, double pos_strength = 15000,
+                                   double rot_strength = 15000) {
+        uint32_t id = 0;
+        check(cpgpu_add_weld(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), pos_strength, rot_strength, &id));
+        return ConstraintID{id};
+    }
     ConstraintID addHingeConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, Vec3 a1, Vec3 a2,
                                     double pos_strength = 15000, double rot_strength = 15000) {
         uint32_t id = 0;

@@ -344,7 +344,7 @@ struct DV { Vec<6> v, pv, lin_err; };   // VelPair (ConstraintSolver.cpp:83-89)
 // A joint row: DegreedConstraint<n> (ConstraintSolver.h:60-144) for n = 3
 // (BallSocketConstraint) or 5 (HingeConstraint), stored at the largest size
 // with every loop bounded by n, in the reference's accumulation order.
-constexpr int kMaxDof = 5;
+constexpr int kMaxDof = 6;
 struct JRow {
     int n = 3;
     Body* a = nullptr; Body* b = nullptr;
@@ -361,7 +361,7 @@ struct Edge;
 struct Params;
 // BallSocket / Hinge (PersistentConstraint.h:118-313)
 struct Joint {
-    int n = 3;                    // 1 distance, 3 ball-socket, 5 hinge
+    int n = 3;                    // 1 distance, 3 ball-socket, 5 hinge, 6 weld
     double target = 0;            // distance: the attachment points' distance
     Body* b1 = nullptr; Body* b2 = nullptr;
     int k1 = 0, k2 = 0;           // tracked point keys

@@ -92,6 +92,10 @@ void Joint::rebuild(const Params& p, double dts, bool in_holo) {
     V3 pa = b1->trackedP(k1), pb = b2->trackedP(k2);
     double warm[kMaxDof] = {};
     for (int i = 0; i < n; i++) warm[i] = p.warm_start_disabled ? 0.0 : 1.0 * row.impulse[i];
+    // Weld::updateSolverConstraints (PersistentConstraint.cpp:344-353) hands
+    // the previous impulse to the constructor unscaled, whatever the
+    // warm-start switch says
+    if (n == 6) for (int i = 0; i < n; i++) warm[i] = row.impulse[i];
     double pos_c = std::min<double>(pos_hard * dts, 1.0 / dts);
     JRow r;
     r.n = n; r.a = b1; r.b = b2; r.in_holo = in_holo;
@@ -131,6 +135,41 @@ void Joint::rebuild(const Params& p, double dts, bool in_holo) {
         }
         V3 err = pb - pa;
         r.ptarget[0] = pos_c * err.x; r.ptarget[1] = pos_c * err.y; r.ptarget[2] = pos_c * err.z;
+    } else if (n == 6) {
+        // WeldConstraint (ConstraintSolver.cpp:861-899): the ball-socket rows
+        // plus three rows locking the relative angular velocity; position
+        // error (pb - pa), orientation error angle * axis of b * conj(a)
+        V3 rB = pb - b2->com;
+        crossMatInto(rB, sb);
+        for (int i = 0; i < 3; i++) {
+            for (int k = 0; k < 3; k++) {
+                double id = (i == k) ? 1.0 : 0.0;
+                r.ja[i][k] = id;
+                r.ja[i][3 + k] = -sa[i][k];
+                r.jb[i][k] = -id;
+                r.jb[i][3 + k] = sb[i][k];
+                r.ja[3 + i][k] = 0;
+                r.ja[3 + i][3 + k] = id;
+                r.jb[3 + i][k] = 0;
+                r.jb[3 + i][3 + k] = -id;
+            }
+        }
+        double rot_c = std::min<double>(rot_hard * dts, 1.0 / dts);
+        V3 pc = (pb - pa) * pos_c;
+        const Q& qa = b1->q;
+        const Q& qb = b2->q;
+        Q dq = qb * qa.conj();
+        // Quaternion::angleTo (Quaternion.h:35-39), getRotAxis (:41-49)
+        double dot = std::fabs(qa.r * qb.r + qa.i * qb.i + qa.j * qb.j + qa.k * qb.k);
+        double angle = dot > 0.99999999999 ? 0.0 : 2 * std::acos(std::fabs(qa.r * qb.r + qa.i * qb.i + qa.j * qb.j + qa.k * qb.k));
+        V3 axis;
+        if (angle != 0) {
+            V3 raw(dq.i, dq.j, dq.k);
+            axis = (dq.r < 0 ? -raw.normalize() : raw.normalize()) * rot_c;
+        }
+        V3 rc = angle * axis;
+        r.ptarget[0] = pc.x; r.ptarget[1] = pc.y; r.ptarget[2] = pc.z;
+        r.ptarget[3] = rc.x; r.ptarget[4] = rc.y; r.ptarget[5] = rc.z;
     } else {
         V3 rB = pa - b2->com;
         crossMatInto(rB, sb);

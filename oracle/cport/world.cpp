@@ -1352,6 +1352,15 @@ int cport_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1
     if (out_id) *out_id = (uint32_t)W(w)->joints.size();
     return CPGPU_OK;
 }
+// PhysicsEngine::addWeldConstraint (PhysicsEngine.cpp:896-915)
+int cport_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], double ps,
+                   double rs, uint32_t* out_id) {
+    Body* x = B(w, b1); Body* y = B(w, b2);
+    if (!x || !y || x == y) return fail("bad body id");
+    W(w)->addJoint(6, x, y, v3(a1), v3(a2), V3(), V3(), ps, rs);
+    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    return CPGPU_OK;
+}
 // PhysicsEngine::addHingeConstraint (PhysicsEngine.cpp:693-723)
 int cport_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], const double ax1[3],
                     const double ax2[3], double ps, double rs, uint32_t* out_id) {

@@ -565,3 +565,35 @@ def test_restatement_bitwise_with_distance_joints(oracle_mod, mixed):
             assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
     st = r.state()
     assert st["com"][2:8, 1].min() < 7.0   # the chain swung down
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_restatement_bitwise_with_weld_joints(oracle_mod, mixed):
+    """Weld constraints (PhysicsEngine::addWeldConstraint, WeldConstraint
+    rows, ConstraintSolver.cpp:861-899): a cantilever of boxes welded to a
+    fixed post, one link turned so the orientation correction acts, or with
+    every other weld a hinge (one holonomic system of 6- and 5-dof blocks),
+    hit by a falling box; bit-identical to the reference over 300 steps."""
+    M = scenes.PILE_MATERIAL
+    sc = scenes.Scene("weld_cantilever", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 4.0, 0.0))
+    for i in range(5):
+        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.DYNAMIC, (0.6 * (i + 1), 4.0, 0.0))
+        if i == 2:
+            sc.orient(b, (0.9961946980917455, 0.0, 0.0, 0.08715574274765817))   # 10 degrees about z
+        if mixed and i % 2 == 1:
+            sc.hinge(prev, b, (0.3, 0, 0), (-0.3, 0, 0), (0, 0, 1), (0, 0, 1))
+        else:
+            sc.weld(prev, b, (0.3, 0, 0), (-0.3, 0, 0))
+        prev = b
+    sc.box((-0.3, -0.3, -0.3), 0.6, 0.6, 0.6, M, scenes.DYNAMIC, (2.4, 6.0, 0.1))
+    r, p = oracle_mod.twin_worlds(sc)
+    for s in range(300):
+        r.step(1)
+        p.step(1)
+        if s % 50 == 49:
+            assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
+    st = r.state()
+    assert st["com"][7, 1] < 5.0   # the dropped box came down
+
