@@ -1821,6 +1821,16 @@ int cpgpu_add_weld(cpgpu_world* w, uint32_t, uint32_t, const double*, const doub
     W_OR_FAIL(w);
     return fail(CPGPU_ERR_UNSUPPORTED, "weld constraints are not implemented on the device path");
 }
+int cpgpu_add_slider(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, const double*, const double*,
+                     double, double, uint32_t*) {
+    W_OR_FAIL(w);
+    return fail(CPGPU_ERR_UNSUPPORTED, "slider constraints are not implemented on the device path");
+}
+int cpgpu_add_sliding_hinge(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, const double*,
+                            const double*, double, double, uint32_t*) {
+    W_OR_FAIL(w);
+    return fail(CPGPU_ERR_UNSUPPORTED, "sliding-hinge constraints are not implemented on the device path");
+}
 int cpgpu_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], const double ax1[3],
                     const double ax2[3], double ps, double rs, uint32_t* out_id) {
     W_OR_FAIL(w);

@@ -233,6 +233,19 @@ class World:
                                       float(rot_strength), C.addressof(out)))
         return out.value
 
+    def add_slider(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
+        return self._axis_joint(self.abi.add_slider, b1, b2, a1, a2, ax1, ax2, pos_strength, rot_strength)
+
+    def add_sliding_hinge(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
+        return self._axis_joint(self.abi.add_sliding_hinge, b1, b2, a1, a2, ax1, ax2, pos_strength, rot_strength)
+
+    def _axis_joint(self, fn, b1, b2, a1, a2, ax1, ax2, pos_strength, rot_strength):
+        a1, a2, ax1, ax2 = (_f64(x, 3) for x in (a1, a2, ax1, ax2))
+        out = C.c_uint32()
+        self._check(fn(self.h, int(b1), int(b2), _ptr(a1), _ptr(a2), _ptr(ax1), _ptr(ax2), float(pos_strength),
+                       float(rot_strength), C.addressof(out)))
+        return out.value
+
     def add_hinge(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
         a1, a2, ax1, ax2 = (_f64(x, 3) for x in (a1, a2, ax1, ax2))
         out = C.c_uint32()

@@ -194,6 +194,22 @@ int cpgpu_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2,
 int cpgpu_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2,
                    const double b1_attach_local[3], const double b2_attach_local[3],
                    double pos_correct_strength, double rot_correct_strength, uint32_t* out_id);
+/* PhysicsEngine::addSliderConstraint (PhysicsEngine.cpp:769-806): body 2
+ * slides along body 1's axis without turning; SliderConstraint rows
+ * (ConstraintSolver.cpp:611-696).  Not on the device path yet: returns
+ * CPGPU_ERR_UNSUPPORTED there. */
+int cpgpu_add_slider(cpgpu_world* w, uint32_t b1, uint32_t b2,
+                     const double b1_slider_pos_local[3], const double b2_slider_pos_local[3],
+                     const double b1_slider_axis_local[3], const double b2_slider_axis_local[3],
+                     double pos_correct_strength, double rot_correct_strength, uint32_t* out_id);
+/* PhysicsEngine::addSlidingHingeConstraint (PhysicsEngine.cpp:856-890): body
+ * 2 slides along and turns about the shared axis; SlidingHingeConstraint rows
+ * (ConstraintSolver.cpp:781-852).  Not on the device path yet: returns
+ * CPGPU_ERR_UNSUPPORTED there. */
+int cpgpu_add_sliding_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2,
+                            const double b1_slider_pos_local[3], const double b2_slider_pos_local[3],
+                            const double b1_slider_axis_local[3], const double b2_slider_axis_local[3],
+                            double pos_correct_strength, double rot_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addHingeConstraint (PhysicsEngine.cpp:693-723) */
 int cpgpu_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2,
                     const double b1_attach_local[3], const double b2_attach_local[3],

@@ -193,7 +193,8 @@ public:
         check(cpgpu_add_ball_socket(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), strength, &id));
         return ConstraintID{id};
     }
-    // addDistanceConstraint / addWeldConstraint: the device path reports
+    // addDistanceConstraint / addWeldConstraint / addSliderConstraint /
+    // addSlidingHingeConstraint: the device path reports
     // CPGPU_ERR_UNSUPPORTED for these joint types for now
     ConstraintID addDistanceConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, double target = -1,
                                        double strength = 15000) {
@@ -205,6 +206,20 @@ public:
                                    double rot_strength = 15000) {
         uint32_t id = 0;
         check(cpgpu_add_weld(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), pos_strength, rot_strength, &id));
+        return ConstraintID{id};
+    }
+    ConstraintID addSliderConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, Vec3 a1, Vec3 a2,
+                                     double pos_strength = 15000, double rot_strength = 15000) {
+        uint32_t id = 0;
+        check(cpgpu_add_slider(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), a1.data(), a2.data(), pos_strength,
+                               rot_strength, &id));
+        return ConstraintID{id};
+    }
+    ConstraintID addSlidingHingeConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, Vec3 a1, Vec3 a2,
+                                           double pos_strength = 15000, double rot_strength = 15000) {
+        uint32_t id = 0;
+        check(cpgpu_add_sliding_hinge(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), a1.data(), a2.data(),
+                                      pos_strength, rot_strength, &id));
         return ConstraintID{id};
     }
     ConstraintID addHingeConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, Vec3 a1, Vec3 a2,

@@ -361,7 +361,8 @@ struct Edge;
 struct Params;
 // BallSocket / Hinge (PersistentConstraint.h:118-313)
 struct Joint {
-    int n = 3;                    // 1 distance, 3 ball-socket, 5 hinge, 6 weld
+    int n = 3;                    // 1 distance, 3 ball-socket, 4 sliding hinge, 5 hinge or slider, 6 weld
+    bool slider = false;          // n == 5: SliderConstraint rows instead of HingeConstraint's
     double target = 0;            // distance: the attachment points' distance
     Body* b1 = nullptr; Body* b2 = nullptr;
     int k1 = 0, k2 = 0;           // tracked point keys

@@ -51,6 +51,30 @@ static void crossMatInto(const V3& v, double m[3][3]) {   // crossMat (NMat.cpp:
     m[2][0] = -v.y; m[2][1] = v.x; m[2][2] = 0;
 }
 
+// (1x3 row) * (3x3) as NMat<1,3> * NMat<3,3> accumulates it
+static void rowTimes(const double v[3], const double m[3][3], double out[3]) {
+    for (int k = 0; k < 3; k++) {
+        double x = 0;
+        for (int q = 0; q < 3; q++) x += v[q] * m[q][k];
+        out[k] = x;
+    }
+}
+
+// angle * axis of b * conj(a) (Quaternion::angleTo, Quaternion.h:35-39, and
+// getRotAxis, :41-49), the axis scaled by `c`; the orientation error of the
+// weld and slider rows
+static V3 orientationError(const Q& qa, const Q& qb, double c) {
+    Q dq = qb * qa.conj();
+    double dot = std::fabs(qa.r * qb.r + qa.i * qb.i + qa.j * qb.j + qa.k * qb.k);
+    double angle = dot > 0.99999999999 ? 0.0 : 2 * std::acos(std::fabs(qa.r * qb.r + qa.i * qb.i + qa.j * qb.j + qa.k * qb.k));
+    V3 axis;
+    if (angle != 0) {
+        V3 raw(dq.i, dq.j, dq.k);
+        axis = (dq.r < 0 ? -raw.normalize() : raw.normalize()) * c;
+    }
+    return angle * axis;
+}
+
 // impulse_to_{a,b}_velocity = invMass(body) * J^T, impulse_to_value and its
 // CFM-regularised inverse (ConstraintSolver.cpp:255-258 pattern)
 static void finishRow(JRow& r, double cfm) {
@@ -156,20 +180,85 @@ void Joint::rebuild(const Params& p, double dts, bool in_holo) {
         }
         double rot_c = std::min<double>(rot_hard * dts, 1.0 / dts);
         V3 pc = (pb - pa) * pos_c;
-        const Q& qa = b1->q;
-        const Q& qb = b2->q;
-        Q dq = qb * qa.conj();
-        // Quaternion::angleTo (Quaternion.h:35-39), getRotAxis (:41-49)
-        double dot = std::fabs(qa.r * qb.r + qa.i * qb.i + qa.j * qb.j + qa.k * qb.k);
-        double angle = dot > 0.99999999999 ? 0.0 : 2 * std::acos(std::fabs(qa.r * qb.r + qa.i * qb.i + qa.j * qb.j + qa.k * qb.k));
-        V3 axis;
-        if (angle != 0) {
-            V3 raw(dq.i, dq.j, dq.k);
-            axis = (dq.r < 0 ? -raw.normalize() : raw.normalize()) * rot_c;
-        }
-        V3 rc = angle * axis;
+        V3 rc = orientationError(b1->q, b2->q, rot_c);
         r.ptarget[0] = pc.x; r.ptarget[1] = pc.y; r.ptarget[2] = pc.z;
         r.ptarget[3] = rc.x; r.ptarget[4] = rc.y; r.ptarget[5] = rc.z;
+    } else if (n == 5 && slider) {
+        // Slider::updateSolverConstraints (PersistentConstraint.cpp:287-298)
+        // with SliderConstraint (ConstraintSolver.cpp:611-696): two rows
+        // across the slide axis (u, w of body 1's axis) and three locking the
+        // relative rotation.  The reference hands the position coefficient
+        // to the orientation rows as well.
+        V3 rB = pb - b2->com;
+        crossMatInto(rB, sb);
+        V3 ax = b1->q.rotate(ax1).normalize();
+        V3 uu, ww;
+        ax.perpBasis(&uu, &ww);
+        r.impulse[0] = uu.dot(u) * warm[0] + uu.dot(w) * warm[1];
+        r.impulse[1] = ww.dot(u) * warm[0] + ww.dot(w) * warm[1];
+        V3 pe = pa - pb;
+        double us[3][3], ws[3][3];
+        crossMatInto(uu, us); crossMatInto(ww, ws);
+        const double ud[3] = {uu.x, uu.y, uu.z}, wd[3] = {ww.x, ww.y, ww.z}, ped[3] = {pe.x, pe.y, pe.z};
+        const double nud[3] = {-uu.x, -uu.y, -uu.z}, nwd[3] = {-ww.x, -ww.y, -ww.z};
+        double t0[3], t1[3], t2[3], t3[3], t4[3], t5[3];
+        rowTimes(nud, sa, t0); rowTimes(ped, us, t1); rowTimes(ud, sb, t2);
+        rowTimes(nwd, sa, t3); rowTimes(ped, ws, t4); rowTimes(wd, sb, t5);
+        for (int k = 0; k < 3; k++) {
+            r.ja[0][k] = ud[k];  r.ja[0][3 + k] = t0[k] - t1[k];
+            r.jb[0][k] = -ud[k]; r.jb[0][3 + k] = t2[k];
+            r.ja[1][k] = wd[k];  r.ja[1][3 + k] = t3[k] - t4[k];
+            r.jb[1][k] = -wd[k]; r.jb[1][3 + k] = t5[k];
+            for (int i = 0; i < 3; i++) {
+                double id = (i == k) ? 1.0 : 0.0;
+                r.ja[2 + i][k] = 0; r.ja[2 + i][3 + k] = id;
+                r.jb[2 + i][k] = 0; r.jb[2 + i][3 + k] = -id;
+            }
+        }
+        V3 rc = orientationError(b1->q, b2->q, pos_c);
+        r.ptarget[0] = -pe.dot(uu) * pos_c;
+        r.ptarget[1] = -pe.dot(ww) * pos_c;
+        r.ptarget[2] = rc.x; r.ptarget[3] = rc.y; r.ptarget[4] = rc.z;
+        u = uu;
+        w = ww;
+    } else if (n == 4) {
+        // SlidingHinge::updateSolverConstraints (PersistentConstraint.cpp:331-342)
+        // with SlidingHingeConstraint (ConstraintSolver.cpp:781-852): two rows
+        // across body 2's axis and two keeping body 1's axis parallel to it
+        V3 rB = pb - b2->com;
+        crossMatInto(rB, sb);
+        V3 na = b1->q.rotate(ax1), nb = b2->q.rotate(ax2);
+        V3 uu, ww;
+        nb.perpBasis(&uu, &ww);
+        r.impulse[2] = uu.dot(u) * warm[2] + uu.dot(w) * warm[3];
+        r.impulse[3] = ww.dot(u) * warm[2] + ww.dot(w) * warm[3];
+        V3 pd = pa - pb;
+        double us[3][3], ws[3][3], ns[3][3];
+        crossMatInto(uu, us); crossMatInto(ww, ws); crossMatInto(na, ns);
+        const double ud[3] = {uu.x, uu.y, uu.z}, wd[3] = {ww.x, ww.y, ww.z}, pdd[3] = {pd.x, pd.y, pd.z};
+        const double nud[3] = {-uu.x, -uu.y, -uu.z}, nwd[3] = {-ww.x, -ww.y, -ww.z}, nnd[3] = {-na.x, -na.y, -na.z};
+        double a0[3], b0a[3], b0b[3], a1[3], b1a[3], b1b[3], a2[3], b2r[3], a3[3], b3r[3];
+        rowTimes(nud, sa, a0); rowTimes(ud, sb, b0a); rowTimes(pdd, us, b0b);
+        rowTimes(nwd, sa, a1); rowTimes(wd, sb, b1a); rowTimes(pdd, ws, b1b);
+        rowTimes(nud, ns, a2); rowTimes(nnd, us, b2r);
+        rowTimes(nwd, ns, a3); rowTimes(nnd, ws, b3r);
+        for (int k = 0; k < 3; k++) {
+            r.ja[0][k] = ud[k];  r.ja[0][3 + k] = a0[k];
+            r.jb[0][k] = -ud[k]; r.jb[0][3 + k] = b0a[k] - b0b[k];
+            r.ja[1][k] = wd[k];  r.ja[1][3 + k] = a1[k];
+            r.jb[1][k] = -wd[k]; r.jb[1][3 + k] = b1a[k] - b1b[k];
+            r.ja[2][k] = 0; r.ja[2][3 + k] = a2[k];
+            r.jb[2][k] = 0; r.jb[2][3 + k] = b2r[k];
+            r.ja[3][k] = 0; r.ja[3][3 + k] = a3[k];
+            r.jb[3][k] = 0; r.jb[3][3 + k] = b3r[k];
+        }
+        double rot_c = std::min<double>(rot_hard * dts, 1.0 / dts);
+        r.ptarget[0] = -uu.dot(pd) * pos_c;
+        r.ptarget[1] = -ww.dot(pd) * pos_c;
+        r.ptarget[2] = -uu.dot(na) * rot_c;
+        r.ptarget[3] = -ww.dot(na) * rot_c;
+        u = uu;
+        w = ww;
     } else {
         V3 rB = pa - b2->com;
         crossMatInto(rB, sb);
@@ -554,7 +643,7 @@ Joint* World::addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, 
     j->k1 = (int)b1->track_p.size() - 1;
     b2->track_p.push_back(b2->local_origin + p2);
     j->k2 = (int)b2->track_p.size() - 1;
-    if (n == 5) { j->ax1 = ax1.normalize(); j->ax2 = ax2.normalize(); }
+    if (n == 4 || n == 5) { j->ax1 = ax1.normalize(); j->ax2 = ax2.normalize(); }
     // PhysicsEngine::addDistanceConstraint (PhysicsEngine.cpp:630-635): -1
     // means the attachment points' current distance
     if (n == 1) j->target = target == -1 ? (b1->trackedP(j->k1) - b2->trackedP(j->k2)).mag() : target;

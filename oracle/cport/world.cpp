@@ -1361,6 +1361,24 @@ int cport_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3],
     if (out_id) *out_id = (uint32_t)W(w)->joints.size();
     return CPGPU_OK;
 }
+// PhysicsEngine::addSliderConstraint (PhysicsEngine.cpp:773-806)
+int cport_add_slider(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3],
+                     const double ax1[3], const double ax2[3], double ps, double rs, uint32_t* out_id) {
+    Body* x = B(w, b1); Body* y = B(w, b2);
+    if (!x || !y || x == y) return fail("bad body id");
+    W(w)->addJoint(5, x, y, v3(a1), v3(a2), v3(ax1), v3(ax2), ps, rs)->slider = true;
+    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    return CPGPU_OK;
+}
+// PhysicsEngine::addSlidingHingeConstraint (PhysicsEngine.cpp:860-890)
+int cport_add_sliding_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3],
+                            const double ax1[3], const double ax2[3], double ps, double rs, uint32_t* out_id) {
+    Body* x = B(w, b1); Body* y = B(w, b2);
+    if (!x || !y || x == y) return fail("bad body id");
+    W(w)->addJoint(4, x, y, v3(a1), v3(a2), v3(ax1), v3(ax2), ps, rs);
+    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    return CPGPU_OK;
+}
 // PhysicsEngine::addHingeConstraint (PhysicsEngine.cpp:693-723)
 int cport_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], const double ax1[3],
                     const double ax2[3], double ps, double rs, uint32_t* out_id) {

@@ -597,3 +597,35 @@ def test_restatement_bitwise_with_weld_joints(oracle_mod, mixed):
     st = r.state()
     assert st["com"][7, 1] < 5.0   # the dropped box came down
 
+
+@pytest.mark.parametrize("kinds", [("slider",) * 4, ("sliding_hinge",) * 4,
+                                   ("slider", "sliding_hinge", "hinge", "slider")])
+def test_restatement_bitwise_with_slider_joints(oracle_mod, kinds):
+    """Slider and sliding-hinge constraints (PhysicsEngine::addSliderConstraint
+    / addSlidingHingeConstraint; SliderConstraint, ConstraintSolver.cpp:611-696,
+    SlidingHingeConstraint, :781-852): a chain of boxes hung from a fixed post
+    on tilted slide axes, one link turned, alone or mixed with a hinge in one
+    holonomic system, hit by a falling box; bit-identical to the reference over
+    300 steps."""
+    M = scenes.PILE_MATERIAL
+    sc = scenes.Scene("slider_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 4.0, 0.0))
+    axes = [(1.0, -0.4, 0.2), (0.3, -1.0, 0.0), (1.0, 0.2, -0.5), (0.0, -1.0, 0.4)]
+    for i, kind in enumerate(kinds):
+        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.DYNAMIC, (0.6 * (i + 1), 4.0, 0.0))
+        if i == 1:
+            sc.orient(b, (0.9961946980917455, 0.0, 0.0, 0.08715574274765817))   # 10 degrees about z
+        getattr(sc, kind)(prev, b, (0.3, 0, 0), (-0.3, 0, 0), axes[i], axes[i])
+        prev = b
+    sc.box((-0.3, -0.3, -0.3), 0.6, 0.6, 0.6, M, scenes.DYNAMIC, (1.8, 6.0, 0.1))
+    r, p = oracle_mod.twin_worlds(sc)
+    start = r.state()["com"][2:6].copy()
+    for s in range(300):
+        r.step(1)
+        p.step(1)
+        if s % 50 == 49:
+            assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
+    moved = np.linalg.norm(r.state()["com"][2:6] - start, axis=1)
+    assert moved.max() > 0.3   # the links slid
+
