@@ -233,6 +233,13 @@ class World:
                                       float(rot_strength), C.addressof(out)))
         return out.value
 
+    def add_spring(self, b1, b2, a1, a2, damping, stiffness, resting_length=-1.0):
+        a1, a2 = _f64(a1, 3), _f64(a2, 3)
+        out = C.c_uint32()
+        self._check(self.abi.add_spring(self.h, int(b1), int(b2), _ptr(a1), _ptr(a2), float(damping),
+                                        float(stiffness), float(resting_length), C.addressof(out)))
+        return out.value
+
     def add_slider(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
         return self._axis_joint(self.abi.add_slider, b1, b2, a1, a2, ax1, ax2, pos_strength, rot_strength)
 

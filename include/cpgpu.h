@@ -194,6 +194,14 @@ int cpgpu_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2,
 int cpgpu_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2,
                    const double b1_attach_local[3], const double b2_attach_local[3],
                    double pos_correct_strength, double rot_correct_strength, uint32_t* out_id);
+/* PhysicsEngine::addSpring (PhysicsEngine.cpp:974-998): a damped spring
+ * between the attachment points (resting_length < 0: their distance at
+ * creation), applied as impulses at the start of every substep
+ * (PhysicsEngine.cpp:1313-1356).  Not on the device path yet: returns
+ * CPGPU_ERR_UNSUPPORTED there. */
+int cpgpu_add_spring(cpgpu_world* w, uint32_t b1, uint32_t b2,
+                     const double b1_attach_local[3], const double b2_attach_local[3],
+                     double damping, double stiffness, double resting_length, uint32_t* out_id);
 /* PhysicsEngine::addSliderConstraint (PhysicsEngine.cpp:769-806): body 2
  * slides along body 1's axis without turning; SliderConstraint rows
  * (ConstraintSolver.cpp:611-696).  Not on the device path yet: returns

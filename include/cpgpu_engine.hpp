@@ -194,7 +194,7 @@ public:
         return ConstraintID{id};
     }
     // addDistanceConstraint / addWeldConstraint / addSliderConstraint /
-    // addSlidingHingeConstraint: the device path reports
+    // addSlidingHingeConstraint / addSpring: the device path reports
     // CPGPU_ERR_UNSUPPORTED for these joint types for now
     ConstraintID addDistanceConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, double target = -1,
                                        double strength = 15000) {
@@ -206,6 +206,13 @@ public:
                                    double rot_strength = 15000) {
         uint32_t id = 0;
         check(cpgpu_add_weld(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), pos_strength, rot_strength, &id));
+        return ConstraintID{id};
+    }
+    ConstraintID addSpring(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, double damping, double stiffness,
+                           double resting_length = -1) {
+        uint32_t id = 0;
+        check(cpgpu_add_spring(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), damping, stiffness,
+                               resting_length, &id));
         return ConstraintID{id};
     }
     ConstraintID addSliderConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, Vec3 a1, Vec3 a2,

@@ -422,12 +422,21 @@ struct Contact {
     bool friction_built = false;
 };
 
+// Spring (PersistentConstraint.h:411-434): not a solver row; an impulse pair
+// applied at the start of every substep
+struct Spring {
+    Body* b1; Body* b2;
+    int k1, k2;                   // tracked point keys
+    double stiffness, damping, rest;
+};
+
 struct Edge {
     Body* n1; Body* n2;                       // n1 = node the edge was created from
     // SharedConstraintsEdge::constraints: joints are listed before contacts
     // (a joint forbids contacts between its bodies from then on)
     std::vector<Joint*> joints;
     std::vector<std::unique_ptr<Contact>> contacts;
+    std::vector<Spring*> springs;
     HoloSys* h = nullptr;                     // holonomic system of the edge
     bool scan_needed = false;                 // holonomic_system_scan_needed
     Body* other(Body* x) const { return x == n1 ? n2 : n1; }
@@ -466,6 +475,7 @@ struct World {
     std::vector<std::unique_ptr<Edge>> edges;
     std::vector<std::pair<uint32_t, uint32_t>> last_pairs;
     std::vector<std::unique_ptr<Joint>> joints;
+    std::vector<std::unique_ptr<Spring>> springs;
     std::vector<std::unique_ptr<HoloSys>> systems;
 
     Body* addHull(const std::vector<V3>& pts, const std::vector<std::vector<int>>& faces, const Material& m, int movement, V3 pos);
@@ -483,6 +493,8 @@ struct World {
     Joint* addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, double pos_hard, double rot_hard,
                     double target = -1);
     void maintainHolonomicSystems();
+    void applySprings(double dt_sub);
+    Spring* addSpring(Body* b1, Body* b2, V3 p1, V3 p2, double damping, double stiffness, double rest);
     void holonomicScan(Edge* e);
     void updateHolonomicInverses();
     void step();

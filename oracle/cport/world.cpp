@@ -951,6 +951,67 @@ static Manifold collide(const Body* b1, const Body* b2) {
 }
 
 // -------------------------------------------------------------- step ----
+// RigidBody::applyImpulse (RigidBody.cpp:60-67)
+static void applyImpulseAt(Body* b, V3 impulse, V3 pos) {
+    V3 torque = (pos - b->com).cross(impulse);
+    b->vel += b->invMass() * impulse;
+    b->ang_vel += b->invTensor() * torque;
+    b->alertWaking();
+}
+
+// The spring pass of maintainConstraintGraphApplyPoweredConstraints
+// (PhysicsEngine.cpp:1309-1356): every edge once, in node order then edge
+// order; a stiffness impulse along the attachment direction, then a damping
+// impulse capped so it does not reverse the relative velocity
+void World::applySprings(double dt) {
+    std::set<Edge*> seen;
+    for (auto& kv : nodes) {
+        for (Edge* e : adj[kv.second]) {
+            if (!seen.insert(e).second) continue;
+            for (Spring* sp : e->springs) {
+                Body* a = sp->b1; Body* b = sp->b2;
+                V3 pa = a->trackedP(sp->k1), pb = b->trackedP(sp->k2);
+                V3 diff = pb - pa;
+                double distance = diff.mag();
+                V3 dir = distance != 0 ? (pb - pa).normalize() : V3(0, -1, 0);
+                double expand = sp->stiffness * (distance - sp->rest);
+                applyImpulseAt(a, dir * expand * dt, pa);
+                applyImpulseAt(b, -dir * expand * dt, pb);
+                V3 rA = pa - a->com, rB = pb - b->com;
+                V3 rdA = a->invTensor() * dir.cross(rA);
+                V3 rdB = b->invTensor() * dir.cross(rB);
+                double sens = 1.0 / (a->invMass() + b->invMass() + rA.cross(rdA).dot(dir) + rB.cross(rdB).dot(dir));
+                // getVelOfPoint (RigidBody.cpp:153-155), with the reference's
+                // crossed attachment points
+                double velocity = (b->vel + b->ang_vel.cross(pa - b->com)).dot(dir) -
+                                  (a->vel + a->ang_vel.cross(pb - a->com)).dot(dir);
+                double dampen = sp->damping * velocity;
+                double max_dampen = velocity * sens / dt;
+                if (velocity > 0 && dampen > max_dampen) dampen = max_dampen;
+                else if (velocity < 0 && dampen < max_dampen) dampen = max_dampen;
+                applyImpulseAt(a, dir * dampen * dt, pa);
+                applyImpulseAt(b, -dir * dampen * dt, pb);
+            }
+        }
+    }
+}
+
+// PhysicsEngine::addSpring (PhysicsEngine.cpp:974-998): no collision filter,
+// rest length < 0 means the attachment points' current distance
+Spring* World::addSpring(Body* b1, Body* b2, V3 p1, V3 p2, double damping, double stiffness, double rest) {
+    auto sp = std::make_unique<Spring>();
+    sp->b1 = b1; sp->b2 = b2;
+    b1->track_p.push_back(b1->local_origin + p1);
+    sp->k1 = (int)b1->track_p.size() - 1;
+    b2->track_p.push_back(b2->local_origin + p2);
+    sp->k2 = (int)b2->track_p.size() - 1;
+    if (rest < 0) rest = (b1->trackedP(sp->k1) - b2->trackedP(sp->k2)).mag();
+    sp->stiffness = stiffness; sp->damping = damping; sp->rest = rest;
+    getOrCreateEdge(b1, b2)->springs.push_back(sp.get());
+    springs.push_back(std::move(sp));
+    return springs.back().get();
+}
+
 void World::step() {
     // waking actions, sleep bookkeeping and gravity once per step
     // (PhysicsEngine.cpp:65-87; RigidBody::recordMovementState, RigidBody.cpp:347-352)
@@ -1083,6 +1144,7 @@ void World::step() {
     double dts = p.dt / p.substeps;
     for (int s = 0; s < p.substeps; s++) {
         bool first = s == 0, last = s == p.substeps - 1;
+        if (!springs.empty()) applySprings(dts);
         std::vector<Edge*> dead;
         for (auto& e : edges) {
             // holonomic rows were rebuilt (and factorised) at the end of the
@@ -1105,7 +1167,7 @@ void World::step() {
                                            return !c->b1->getAsleep() && !c->b2->getAsleep() && c->life < 0;
                                        }),
                         v.end());
-                if (v.empty() && e->joints.empty()) dead.push_back(e.get());
+                if (v.empty() && e->joints.empty() && e->springs.empty()) dead.push_back(e.get());
             }
         }
         for (Edge* e : dead) deleteEdge(e);
@@ -1359,6 +1421,15 @@ int cport_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3],
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addJoint(6, x, y, v3(a1), v3(a2), V3(), V3(), ps, rs);
     if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    return CPGPU_OK;
+}
+// PhysicsEngine::addSpring (PhysicsEngine.cpp:974-998)
+int cport_add_spring(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], double damping,
+                     double stiffness, double rest, uint32_t* out_id) {
+    Body* x = B(w, b1); Body* y = B(w, b2);
+    if (!x || !y || x == y) return fail("bad body id");
+    W(w)->addSpring(x, y, v3(a1), v3(a2), damping, stiffness, rest);
+    if (out_id) *out_id = (uint32_t)(W(w)->joints.size() + W(w)->springs.size());
     return CPGPU_OK;
 }
 // PhysicsEngine::addSliderConstraint (PhysicsEngine.cpp:773-806)
@@ -1712,7 +1783,7 @@ int cport_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n) {
     std::vector<Edge*> all;
     for (auto& e : x->edges) {
         e->contacts.clear();
-        if (e->joints.empty()) all.push_back(e.get());
+        if (e->joints.empty() && e->springs.empty()) all.push_back(e.get());
     }
     for (Edge* e : all) x->deleteEdge(e);
     for (int k = 0; k < n; k++) {

@@ -314,6 +314,14 @@ int cpref_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3],
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
+int cpref_add_spring(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3],
+                     double damping, double stiffness, double rest, uint32_t* out_id) {
+    phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
+    if (!r1 || !r2) return fail("bad body id");
+    phyz::ConstraintID id = RW->engine.addSpring(r1, r2, v3(a1), v3(a2), damping, stiffness, rest);
+    if (out_id) *out_id = id.getID();
+    return CPGPU_OK;
+}
 int cpref_add_slider(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3],
                      const double ax1[3], const double ax2[3], double ps, double rs, uint32_t* out_id) {
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);

@@ -629,3 +629,33 @@ def test_restatement_bitwise_with_slider_joints(oracle_mod, kinds):
     moved = np.linalg.norm(r.state()["com"][2:6] - start, axis=1)
     assert moved.max() > 0.3   # the links slid
 
+
+@pytest.mark.parametrize("with_joints", [False, True])
+def test_restatement_bitwise_with_springs(oracle_mod, with_joints):
+    """Springs (PhysicsEngine::addSpring, the impulse pass of
+    PhysicsEngine.cpp:1313-1356): boxes hung from a fixed post on damped
+    springs (two sharing a body, one at its creation length), bouncing on the
+    ground and off each other, or sharing bodies with ball-socket joints;
+    bit-identical to the reference over 300 steps."""
+    M = scenes.PILE_MATERIAL
+    sc = scenes.Scene("spring_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
+    post = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 4.0, 0.0))
+    prev = post
+    for i in range(4):
+        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.DYNAMIC, (0.4 * (i + 1), 3.2 - 0.7 * i, 0.1 * i))
+        if with_joints and i == 2:
+            sc.ball_socket(prev, b, (0.2, -0.35, 0.05), (-0.2, 0.35, -0.05))
+        else:
+            sc.spring(prev, b, (0.1, -0.25, 0.0), (0.0, 0.25, 0.1), 2.0 + i, 300.0 + 100.0 * i, 0.6 if i % 2 else -1.0)
+        prev = b
+    sc.spring(post, prev, (0.25, 0.0, 0.0), (0.0, 0.0, 0.25), 5.0, 80.0, 1.0)
+    r, p = oracle_mod.twin_worlds(sc)
+    start = r.state()["com"][2:6].copy()
+    for s in range(300):
+        r.step(1)
+        p.step(1)
+        if s % 50 == 49:
+            assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
+    assert np.linalg.norm(r.state()["com"][2:6] - start, axis=1).max() > 0.2   # the springs moved the boxes
+
