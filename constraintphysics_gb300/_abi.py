@@ -44,6 +44,7 @@ SIGNATURES = {
     "add_weld": (I, [P, U32, U32, P, P, D, D, P]),
     "add_spring": (I, [P, U32, U32, P, P, D, D, D, P]),
     "add_cone_limit": (I, [P, U32, U32, P, P, D, D, P]),
+    "add_twist_limit": (I, [P, U32, U32, P, P, D, D, D, P]),
     "add_slider": (I, [P, U32, U32, P, P, P, P, D, D, P]),
     "add_sliding_hinge": (I, [P, U32, U32, P, P, P, P, D, D, P]),
     "add_hinge": (I, [P, U32, U32, P, P, P, P, D, D, P]),

@@ -1821,6 +1821,11 @@ int cpgpu_add_weld(cpgpu_world* w, uint32_t, uint32_t, const double*, const doub
     W_OR_FAIL(w);
     return fail(CPGPU_ERR_UNSUPPORTED, "weld constraints are not implemented on the device path");
 }
+int cpgpu_add_twist_limit(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, double, double, double,
+                          uint32_t*) {
+    W_OR_FAIL(w);
+    return fail(CPGPU_ERR_UNSUPPORTED, "twist limits are not implemented on the device path");
+}
 int cpgpu_add_cone_limit(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, double, double,
                          uint32_t*) {
     W_OR_FAIL(w);

@@ -119,6 +119,10 @@ class Scene:
     def weld(self, b1, b2, a1, a2, pos_strength=15000.0, rot_strength=15000.0):
         self.ops.append(("weld", b1, b2, tuple(a1), tuple(a2), float(pos_strength), float(rot_strength)))
 
+    def twist_limit(self, b1, b2, ax1, ax2, min_angle, max_angle, rot_strength=15000.0):
+        self.ops.append(("twist_limit", b1, b2, tuple(ax1), tuple(ax2), float(min_angle), float(max_angle),
+                         float(rot_strength)))
+
     def cone_limit(self, b1, b2, ax1, ax2, max_angle, rot_strength=15000.0):
         self.ops.append(("cone_limit", b1, b2, tuple(ax1), tuple(ax2), float(max_angle), float(rot_strength)))
 
@@ -183,7 +187,7 @@ def apply(scene, world):
             world.set_mass(op[1], op[2])
         elif kind == "distance":
             world.add_distance(op[1], op[2], op[3], op[4], op[5], op[6])
-        elif kind in ("slider", "sliding_hinge", "spring", "cone_limit"):
+        elif kind in ("slider", "sliding_hinge", "spring", "cone_limit", "twist_limit"):
             getattr(world, "add_" + kind)(*op[1:])
         elif kind == "weld":
             world.add_weld(op[1], op[2], op[3], op[4], op[5], op[6])

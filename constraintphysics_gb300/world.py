@@ -233,6 +233,13 @@ class World:
                                       float(rot_strength), C.addressof(out)))
         return out.value
 
+    def add_twist_limit(self, b1, b2, ax1, ax2, min_angle, max_angle, rot_strength=15000.0):
+        ax1, ax2 = _f64(ax1, 3), _f64(ax2, 3)
+        out = C.c_uint32()
+        self._check(self.abi.add_twist_limit(self.h, int(b1), int(b2), _ptr(ax1), _ptr(ax2), float(min_angle),
+                                             float(max_angle), float(rot_strength), C.addressof(out)))
+        return out.value
+
     def add_cone_limit(self, b1, b2, ax1, ax2, max_angle, rot_strength=15000.0):
         ax1, ax2 = _f64(ax1, 3), _f64(ax2, 3)
         out = C.c_uint32()

@@ -194,6 +194,13 @@ int cpgpu_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2,
 int cpgpu_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2,
                    const double b1_attach_local[3], const double b2_attach_local[3],
                    double pos_correct_strength, double rot_correct_strength, uint32_t* out_id);
+/* PhysicsEngine::addTwistLimitConstraint (PhysicsEngine.cpp:948-972): the
+ * twist of body 2 about the axes stays within [min_angle, max_angle];
+ * TwistLimitConstraint row (ConstraintSolver.cpp:439-466).  Not on the
+ * device path yet: returns CPGPU_ERR_UNSUPPORTED there. */
+int cpgpu_add_twist_limit(cpgpu_world* w, uint32_t b1, uint32_t b2,
+                          const double b1_twist_axis_local[3], const double b2_twist_axis_local[3],
+                          double min_angle, double max_angle, double rot_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addConeLimitConstraint (PhysicsEngine.cpp:922-946): the
  * angle between the bodies' direction vectors (body space) stays below
  * max_angle (< pi); ConeLimitConstraint row (ConstraintSolver.cpp:410-436).

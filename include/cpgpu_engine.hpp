@@ -194,7 +194,8 @@ public:
         return ConstraintID{id};
     }
     // addDistanceConstraint / addWeldConstraint / addSliderConstraint /
-    // addSlidingHingeConstraint / addConeLimitConstraint / addSpring: the
+    // addSlidingHingeConstraint / addConeLimitConstraint /
+    // addTwistLimitConstraint / addSpring: the
     // device path reports
     // CPGPU_ERR_UNSUPPORTED for these joint types for now
     ConstraintID addDistanceConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, double target = -1,
@@ -207,6 +208,13 @@ public:
                                    double rot_strength = 15000) {
         uint32_t id = 0;
         check(cpgpu_add_weld(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), pos_strength, rot_strength, &id));
+        return ConstraintID{id};
+    }
+    ConstraintID addTwistLimitConstraint(RigidBody* b1, RigidBody* b2, Vec3 d1, Vec3 d2, double min_angle,
+                                         double max_angle, double rot_strength = 15000) {
+        uint32_t id = 0;
+        check(cpgpu_add_twist_limit(w_, b1->getID(), b2->getID(), d1.data(), d2.data(), min_angle, max_angle,
+                                    rot_strength, &id));
         return ConstraintID{id};
     }
     ConstraintID addConeLimitConstraint(RigidBody* b1, RigidBody* b2, Vec3 d1, Vec3 d2, double max_angle,

@@ -350,7 +350,7 @@ struct JRow {
     Body* a = nullptr; Body* b = nullptr;
     DV* da = nullptr; DV* db = nullptr;
     bool in_holo = false;
-    int proj = 0;                 // 1: accumulated impulse kept >= 0 (projectValidImpulse)
+    int proj = 0;                 // 1 / 2: accumulated impulse kept >= 0 / <= 0 (projectValidImpulse)
     double impulse[kMaxDof] = {}, pimpulse[kMaxDof] = {}, holo[kMaxDof] = {};
     double target[kMaxDof] = {}, ptarget[kMaxDof] = {};
     double ja[kMaxDof][6] = {}, jb[kMaxDof][6] = {};
@@ -370,7 +370,12 @@ struct Joint {
     bool cone = false;
     double max_angle = 0;
     bool inactive = true;
-    bool holonomic() const { return !cone; }
+    // TwistLimit (PersistentConstraint.h:174-215): as the cone, for the twist
+    // angle about the axes, tracked across ticks in cur_angle
+    bool twist = false;
+    double min_angle = 0, cur_angle = 0;
+    V3 u_local, w_local;          // b1's perpendicular basis (w first, as the reference)
+    bool holonomic() const { return !cone && !twist; }
     double target = 0;            // distance: the attachment points' distance
     Body* b1 = nullptr; Body* b2 = nullptr;
     int k1 = 0, k2 = 0;           // tracked point keys
@@ -502,6 +507,7 @@ struct World {
                     double target = -1);
     void maintainHolonomicSystems();
     void applySprings(double dt_sub);
+    Joint* addTwist(Body* b1, Body* b2, V3 ax1, V3 ax2, double min_angle, double max_angle, double rot_hard);
     Joint* addCone(Body* b1, Body* b2, V3 ax1, V3 ax2, double max_angle, double rot_hard);
     Spring* addSpring(Body* b1, Body* b2, V3 p1, V3 p2, double damping, double stiffness, double rest);
     void holonomicScan(Edge* e);

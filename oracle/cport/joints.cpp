@@ -140,6 +140,38 @@ void Joint::rebuild(const Params& p, double dts, bool in_holo) {
         row = r;
         return;
     }
+    if (twist) {
+        // TwistLimit::updateSolverConstraints (PersistentConstraint.cpp:249-272),
+        // getCurrentAngle (:115-131: the angle of b1's w axis carried by body 2,
+        // measured in b1's (w, u) frame and unwrapped against the last
+        // value; the reference's alignment rotation there is unused) and
+        // TwistLimitConstraint (ConstraintSolver.cpp:439-466)
+        M3 r1 = b1->q.rotMatrix(), r2 = b2->q.rotMatrix();
+        V3 t1 = r1 * ax1, u1 = r1 * u_local, w1 = r1 * w_local;
+        V3 t2 = r2 * ax2, r2w = r2 * w_local;
+        double prev = cur_angle;
+        double a = std::atan2(r2w.dot(u1), r2w.dot(w1));
+        while (prev - a > PI_TRUNC) a += 2 * PI_TRUNC;
+        while (prev - a < -PI_TRUNC) a -= 2 * PI_TRUNC;
+        cur_angle = a;
+        inactive = min_angle <= a && a <= max_angle;
+        if (inactive) { row.impulse[0] = 0.0; return; }
+        const bool above = a > max_angle;
+        JRow r;
+        r.n = 1; r.a = b1; r.b = b2; r.proj = above ? 2 : 1;
+        r.impulse[0] = row.impulse[0];
+        const double ta[3] = {t1.x, t1.y, t1.z}, tb[3] = {t2.x, t2.y, t2.z};
+        for (int k = 0; k < 3; k++) {
+            r.ja[0][k] = 0; r.ja[0][3 + k] = -ta[k];
+            r.jb[0][k] = 0; r.jb[0][3 + k] = tb[k];
+        }
+        double f = above ? a - max_angle : min_angle - a;
+        double err = -f * f * f * f * f * f * f * f / 40320.0 + f * f * f * f * f * f / 720.0 - f * f * f * f / 24.0 + f * f / 2.0;
+        r.ptarget[0] = err * rot_hard;
+        finishRow(r, p.cfm);
+        row = r;
+        return;
+    }
     V3 pa = b1->trackedP(k1), pb = b2->trackedP(k2);
     double warm[kMaxDof] = {};
     for (int i = 0; i < n; i++) warm[i] = p.warm_start_disabled ? 0.0 : 1.0 * row.impulse[i];
@@ -388,7 +420,10 @@ void jrowStep(JRow& r, bool pseudo) {
         double x = 0;
         for (int k = 0; k < r.n; k++) x += delta[k] * r.minv[i][k];
         double nw = acc[i] + x;
-        if (r.proj == 1) nw = std::max<double>(nw, 0);   // ConeLimitConstraint::projectValidImpulse (:434-436)
+        // ConeLimitConstraint / TwistLimitConstraint::projectValidImpulse
+        // (ConstraintSolver.cpp:434-436, 463-465)
+        if (r.proj == 1) nw = std::max<double>(nw, 0);
+        else if (r.proj == 2) nw = std::min<double>(nw, 0);
         diff[i] = nw - acc[i];
     }
     if (!isZero(diff, r.n)) {
@@ -705,6 +740,18 @@ Joint* World::addCone(Body* b1, Body* b2, V3 ax1, V3 ax2, double max_angle, doub
     e->joints.push_back(j.get());
     joints.push_back(std::move(j));
     return joints.back().get();
+}
+
+// PhysicsEngine::addTwistLimitConstraint (PhysicsEngine.cpp:952-972) and the
+// TwistLimit constructor (PersistentConstraint.h:177-184)
+Joint* World::addTwist(Body* b1, Body* b2, V3 ax1, V3 ax2, double min_angle, double max_angle, double rot_hard) {
+    Joint* j = addCone(b1, b2, ax1, ax2, 0, rot_hard);
+    j->cone = false;
+    j->twist = true;
+    j->min_angle = min_angle;
+    j->max_angle = max_angle;
+    ax1.perpBasis(&j->w_local, &j->u_local);
+    return j;
 }
 
 // getAllEdgesConnectedHolonomically (PhysicsEngine.cpp:1745-1777)

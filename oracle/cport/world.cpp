@@ -1122,7 +1122,7 @@ void World::step() {
                     if (holo && e->h && std::find(blocks.begin(), blocks.end(), e->h) == blocks.end()) blocks.push_back(e->h);
                     // ConeRotationLimit::addSolverConstraints: only while active
                     for (Joint* j : e->joints)
-                        if (!(j->cone && j->inactive)) rows.push_back({2, nullptr, j});
+                        if (!((j->cone || j->twist) && j->inactive)) rows.push_back({2, nullptr, j});
                     for (auto& c : e->contacts)
                         if (c->live) { rows.push_back({0, c.get()}); rows.push_back({1, c.get()}); }
                 }
@@ -1422,6 +1422,15 @@ int cport_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3],
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addJoint(6, x, y, v3(a1), v3(a2), V3(), V3(), ps, rs);
+    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    return CPGPU_OK;
+}
+// PhysicsEngine::addTwistLimitConstraint (PhysicsEngine.cpp:952-972)
+int cport_add_twist_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double ax1[3], const double ax2[3],
+                          double min_angle, double max_angle, double rs, uint32_t* out_id) {
+    Body* x = B(w, b1); Body* y = B(w, b2);
+    if (!x || !y || x == y) return fail("bad body id");
+    W(w)->addTwist(x, y, v3(ax1), v3(ax2), min_angle, max_angle, rs);
     if (out_id) *out_id = (uint32_t)W(w)->joints.size();
     return CPGPU_OK;
 }

@@ -314,6 +314,14 @@ int cpref_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3],
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
+int cpref_add_twist_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double ax1[3], const double ax2[3],
+                          double min_angle, double max_angle, double rs, uint32_t* out_id) {
+    phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
+    if (!r1 || !r2) return fail("bad body id");
+    phyz::ConstraintID id = RW->engine.addTwistLimitConstraint(r1, r2, v3(ax1), v3(ax2), min_angle, max_angle, rs);
+    if (out_id) *out_id = id.getID();
+    return CPGPU_OK;
+}
 int cpref_add_cone_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double ax1[3], const double ax2[3],
                          double max_angle, double rs, uint32_t* out_id) {
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);

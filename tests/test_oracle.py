@@ -685,3 +685,29 @@ def test_restatement_bitwise_with_cone_limits(oracle_mod, holo):
         if s % 50 == 49:
             assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
 
+
+def test_restatement_bitwise_with_twist_limits(oracle_mod):
+    """Twist limits (PhysicsEngine::addTwistLimitConstraint; TwistLimit's
+    unwrapped angle, PersistentConstraint.cpp:115-131, and the one-sided
+    TwistLimitConstraint row, ConstraintSolver.cpp:439-466) beside cone limits
+    on a ball-socket chain spun about its axis; bit-identical to the
+    reference over 300 steps, and the twist limit does engage."""
+    M = scenes.PILE_MATERIAL
+    sc = scenes.Scene("twist_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 6.0, 0.0))
+    for i in range(3):
+        b = sc.box((-0.3, -0.4, -0.1), 0.6, 0.8, 0.2, M, scenes.DYNAMIC, (0.0, 5.2 - 1.0 * i, 0.0))
+        sc.ball_socket(prev, b, (0.0, -0.5 if i else -0.25, 0.0), (0.0, 0.5, 0.0))
+        sc.cone_limit(prev, b, (0.0, -1.0, 0.0), (0.0, -1.0, 0.0), 20.0 * np.pi / 180.0)
+        sc.twist_limit(prev, b, (0.0, -1.0, 0.0), (0.0, -1.0, 0.0), -0.3, 0.5)
+        prev = b
+    sc.ang_velocity(prev, (0.5, 9.0, 0.0))
+    sc.velocity(prev, (2.0, 0.0, 0.0))
+    r, p = oracle_mod.twin_worlds(sc)
+    for s in range(300):
+        r.step(1)
+        p.step(1)
+        if s % 50 == 49:
+            assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
+
