@@ -1503,7 +1503,7 @@ int cport_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv
     *n = (int)x->joints.size();
     for (size_t j = 0; j < x->joints.size(); j++) {
         const Joint& J = *x->joints[j];
-        for (int k = 0; k < kMaxDof; k++) if (impulse) impulse[kMaxDof * j + k] = k < J.n ? J.row.impulse[k] : 0.0;
+        for (int k = 0; k < kStateDof; k++) if (impulse) impulse[kStateDof * j + k] = k < J.n ? J.row.impulse[k] : 0.0;
         if (u) { u[3 * j] = J.u.x; u[3 * j + 1] = J.u.y; u[3 * j + 2] = J.u.z; }
         if (wv) { wv[3 * j] = J.w.x; wv[3 * j + 1] = J.w.y; wv[3 * j + 2] = J.w.z; }
     }
@@ -1518,7 +1518,7 @@ int cport_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
     if (n != (int)x->joints.size()) return fail("joint count mismatch");
     for (int j = 0; j < n; j++) {
         Joint& J = *x->joints[j];
-        for (int k = 0; k < J.n; k++) if (impulse) J.row.impulse[k] = impulse[kMaxDof * j + k];
+        for (int k = 0; k < std::min(J.n, kStateDof); k++) if (impulse) J.row.impulse[k] = impulse[kStateDof * j + k];
         if (u) J.u = V3(u[3 * j], u[3 * j + 1], u[3 * j + 2]);
         if (wv) J.w = V3(wv[3 * j], wv[3 * j + 1], wv[3 * j + 2]);
     }

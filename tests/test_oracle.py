@@ -711,3 +711,35 @@ def test_restatement_bitwise_with_twist_limits(oracle_mod):
         if s % 50 == 49:
             assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
 
+
+def test_restatement_joint_state_layout(oracle_mod):
+    """The restatement's joint-state export and import use the C ABI's layout
+    (5 impulses per joint, as the device's cpgpu_get/set_joint_state): a
+    round trip through a second world reproduces the state, for hinges, ball
+    sockets and a weld (whose sixth impulse the layout does not carry)."""
+    M = scenes.PILE_MATERIAL
+    sc = scenes.Scene("state_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 4.0, 0.0))
+    for i, kind in enumerate(("hinge", "ball", "weld", "hinge")):
+        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.DYNAMIC, (0.6 * (i + 1), 4.0, 0.0))
+        if kind == "hinge":
+            sc.hinge(prev, b, (0.3, 0, 0), (-0.3, 0, 0), (0, 0, 1), (0, 0, 1))
+        elif kind == "ball":
+            sc.ball_socket(prev, b, (0.3, 0, 0), (-0.3, 0, 0))
+        else:
+            sc.weld(prev, b, (0.3, 0, 0), (-0.3, 0, 0))
+        prev = b
+    a, b = oracle_mod.port_world(), oracle_mod.port_world()
+    scenes.apply(sc, a)
+    scenes.apply(sc, b)
+    a.step(20)
+    ja = a.joint_state()
+    assert ja["impulse"].shape == (4, 5)
+    assert np.abs(ja["impulse"][[0, 1, 3]]).max() > 0
+    assert np.all(ja["impulse"][1, 3:] == 0) and np.all(ja["impulse"][1, :3] != 0)   # the ball socket: 3 rows
+    b.set_joint_state(ja)
+    jb = b.joint_state()
+    for k in ja:
+        assert np.array_equal(ja[k], jb[k]), k
+
