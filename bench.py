@@ -62,8 +62,10 @@ def parse():
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="build the batch, run warmup + steps, no extras")
-    ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of each serving run (0: none)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="duration of each serving run (0: none)")
     ap.add_argument("--serve-rates", default="2000,20", help="Poisson request rates (requests/s) of the serving runs")
+    ap.add_argument("--tune-steps", type=int, default=3,
+                    help="trial steps per candidate schedule of the batch autotuner (0: the hand-set schedule)")
     return ap.parse_args()
 
 
@@ -148,9 +150,11 @@ def measured_peaks():
 
 
 def measured_traffic(stage, worlds):
-    """DRAM bytes per launch of the stage's kernels from the committed ncu
-    summary (profiles/roofline_traffic.txt), for this workload size only."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "roofline_traffic.txt")
+    """DRAM bytes per launch of the stage's dominant kernel, from the committed
+    summary of an ncu capture of the current build (profiles/pgs_traffic.txt:
+    lines `stage bytes worlds`, the bytes scaled to the workload's world count
+    from a smaller capture, as the file states), or None."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "pgs_traffic.txt")
     try:
         with open(path) as f:
             for line in f:
@@ -284,40 +288,57 @@ def run_reference_sample(ws_scenes, warmup, steps, budget_s, threads):
     return body_steps / wall, sample, wall
 
 
-def measure_drift(cg, ws_scenes, n_worlds=8, steps=300):
-    """Position drift of the device against the reference engine: an evenly
-    spaced sample of the same worlds stepped `steps` times on both (the device
-    in FP32, the reference in FP64, each from the scene itself); per dynamic
-    body the distance between the two centres of mass."""
+def _f32_state(st):
+    return {k: np.asarray(v, np.float32).astype(np.float64) for k, v in st.items()}
+
+
+def measure_drift(cg, ws_scenes, n_per_kind=4, steps=300, max_bodies=400):
+    """Position drift against the reference engine after `steps` steps, per
+    scene kind (box pyramids, hull piles), on an evenly spaced sample of the
+    worlds with at most `max_bodies` bodies, each side stepping the scene from
+    scratch; per dynamic body the distance between the two centres of mass.
+    Beside the device (FP32) two controls run on the CPU: the FP64
+    restatement (mass properties within 1e-12 of the reference's, nothing else
+    different) and the same restatement with its state rounded to FP32 after
+    every step (FP64 arithmetic, FP32 storage: the smallest perturbation any
+    FP32 implementation makes).  On chaotic scenes all three drift alike."""
     import oracle
-    idx = list(range(0, len(ws_scenes), max(1, len(ws_scenes) // n_worlds)))[:n_worlds]
-    d, c = [], []
-    for i in idx:
+    pick = []
+    for kind in ("pyramid", "pile"):
+        idx = [i for i, sc in enumerate(ws_scenes) if sc.name.startswith(kind) and sc.n_bodies <= max_bodies]
+        pick += [(kind, i) for i in idx[:: max(1, len(idx) // n_per_kind)][:n_per_kind]]
+    acc = {}
+    for kind, i in pick:
+        sc = ws_scenes[i]
         g = cg.world()
-        scenes.apply(ws_scenes[i], g)
+        scenes.apply(sc, g)
         g.step(steps)
         r = oracle.ref_world()
-        scenes.apply(ws_scenes[i], r)
+        scenes.apply(sc, r)
         r.step(steps)
-        # control: the FP64 restatement, whose mass properties differ from the
-        # reference's by ~1e-12 relative, against the reference
         p = oracle.port_world()
-        scenes.apply(ws_scenes[i], p)
+        scenes.apply(sc, p)
         p.step(steps)
-        dyn = np.array([m == scenes.DYNAMIC for m in ws_scenes[i].movements()])
-        rc = r.state()["com"]
-        d.append(np.linalg.norm(g.state()["com"] - rc, axis=1)[dyn])
-        c.append(np.linalg.norm(p.state()["com"] - rc, axis=1)[dyn])
+        q = oracle.port_world()
+        scenes.apply(sc, q)
+        for _ in range(steps):
+            q.set_state(**_f32_state(q.state()))
+            q.step(1)
+        dyn = np.array([m == scenes.DYNAMIC for m in sc.movements()])
+        rc = r.state()["com"][dyn]
+        for name, w in (("device", g), ("fp64_control", p), ("fp32_state_control", q)):
+            acc.setdefault(kind, {}).setdefault(name, []).append(np.linalg.norm(w.state()["com"][dyn] - rc, axis=1))
 
     def stats(x):
-        x = np.concatenate(x) if x else np.zeros(1)
+        x = np.concatenate(x)
         return {"median_m": float(np.median(x)), "p95_m": float(np.percentile(x, 95)), "max_m": float(x.max()),
-                "frac_within_1e-3_m": float(np.mean(x <= 1e-3))}
-    return dict(stats(d), worlds=len(idx), steps=steps, bodies=int(sum(x.size for x in d)),
-                fp64_control=stats(c),
-                note="device FP32 vs the reference engine FP64 from the same scene; fp64_control: the FP64 "
-                     "restatement (mass properties within 1e-12 of the reference's) vs the reference, the "
-                     "drift these scenes show for rounding-level differences alone")
+                "frac_within_1e-3_m": float(np.mean(x <= 1e-3)), "bodies": int(x.size)}
+    out = {kind: {name: stats(v) for name, v in m.items()} for kind, m in acc.items()}
+    out.update(worlds=len(pick), steps=steps,
+               note="per scene kind, every dynamic body; device FP32 vs the reference engine FP64 from the same "
+                    "scene; fp64_control = the FP64 restatement, fp32_state_control = the restatement with its "
+                    "state rounded to FP32 after every step; hull piles are chaotic at rounding level")
+    return out
 
 
 def main():
@@ -352,7 +373,9 @@ def main():
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
     worlds = build_worlds(ws_scenes, cg.world)
-    batch = cg.Batch(worlds)
+    t_tune = time.perf_counter()
+    batch = cg.Batch(worlds, tune_steps=a.tune_steps)
+    schedule = dict(batch.schedule(), batch_build_and_tune_s=time.perf_counter() - t_tune)
     setup_s = time.perf_counter() - t_setup
 
     def barrier():
@@ -361,9 +384,6 @@ def main():
             dist.barrier()
 
     batch.step(a.warmup)
-    # per-stage profile (stage by stage, no graph) for the roofline, taken on
-    # the steps right after the warm-up (the same phase as the timed steps)
-    stage_ms, counts = (None, None) if a.profile_only else batch.profile(3)
     if a.profile_only:
         batch.step(a.steps)
         print(json.dumps({"profile_only": True, "steps": a.steps, "warmup": a.warmup}), flush=True)
@@ -374,7 +394,24 @@ def main():
     barrier()
     # per-step latency distribution over another `steps` steps
     lat = [batch.step_timed(1) for _ in range(a.steps)]
+    # per-stage device times over another `steps` steps launched stage by
+    # stage with CUDA events on every part's stream (the parts concurrent as
+    # in the graph-launched steps): each stage's window inside the step
+    stage_ms, counts = batch.profile(a.steps)
     clocks = sampler.stop()
+    # FP64 momentum / energy audit: a few steps with the audit kernel at the
+    # end of each, its cost against the same steps without it
+    plain_ms = batch.step_timed(a.warmup)
+    batch.set_audit(True)
+    audit_ms = batch.step_timed(a.warmup)
+    av = batch.read_audit()
+    batch.set_audit(False)
+    audit = {"steps": int(av[0, 9]), "ms_per_step_added": (audit_ms - plain_ms) / a.warmup,
+             "total_kinetic_J": float(av[:, 6].sum()), "total_potential_J": float(av[:, 7].sum()),
+             "max_step_energy_gain_J": float(av[:, 8].max()),
+             "worlds_gaining_energy": int((av[:, 8] > 1e-6 * (np.abs(av[:, 6]) + np.abs(av[:, 7]) + 1.0)).sum()),
+             "note": "per world, FP64 sums over the FP32 state after every step (cpgpu_batch_set_audit); "
+                     "max_step_energy_gain_J is the largest one-step increase of kinetic + potential energy"}
     if world_size > 1:
         import torch
         import torch.distributed as dist
@@ -404,7 +441,7 @@ def main():
            "d2h_bytes_per_step": state_bytes, "host_buffers": host_desc,
            "call": "cpgpu_batch_write_state + cpgpu_batch_step + cpgpu_batch_read_state per step"}
 
-    stage_ms = {k: v / 3 for k, v in stage_ms.items()}
+    stage_ms = {k: v / a.steps for k, v in stage_ms.items()}
     dominant = max(stage_ms, key=stage_ms.get)
     vfe = hull_sizes(ws_scenes)
     peak, peak_kind = measured_peaks()
@@ -416,7 +453,9 @@ def main():
             roof = {"bound": "hbm", "kernel": stage, "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": measured_traffic(stage, a.worlds),
                     "algorithmic_bytes_per_launch": b, "launch_ms": stage_ms[stage],
-                    "note": "dominant stage" if stage == dominant else f"dominant stage {dominant} has no byte model"}
+                    "note": ("dominant stage (k_pgs_big with k_pgs_small beside it, both parts); launch_ms is its "
+                             "window inside the step, CUDA events on every part's stream over --steps steps")
+                    if stage == dominant else f"dominant stage {dominant} has no byte model"}
             break
 
     # plain single-world path on an evenly spaced sample of the same worlds
@@ -450,14 +489,15 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": dev_ms / a.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
-                "config": dict(config, l2="state larger than L2 (%.0f MB resident)" % (batch_bodies * 600 / 1e6),
-                               contacts=info["contacts"]),
+                "config": config,
+                "l2": "state larger than L2 (%.0f MB resident)" % (batch_bodies * 600 / 1e6),
+                "contacts": info["contacts"],
                 "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
                 "contacts_per_s": info["contacts"] * world_size / (dev_ms / a.steps / 1e3),
                 "plain": {"value": plain, "unit": UNIT, "sample_worlds": a.plain_sample,
                           "vs_plain": (value / world_size / plain) if plain else None},
-                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-                "gpu_launches": launches,
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "audit": audit,
+                "gpu_launches": launches, "schedule": schedule,
                 "stage_ms": stage_ms, "counts": counts, "setup_s": setup_s, "serving": serving}
         print(json.dumps(line), flush=True)
 

@@ -47,6 +47,12 @@ def lib():
             "server_poll": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p],
             "server_stats": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_void_p],
+            "batch_create_tuned": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
+            "batch_schedule": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+            "world_set_audit": [ctypes.c_void_p, ctypes.c_int],
+            "world_read_audit": [ctypes.c_void_p, ctypes.c_void_p],
+            "batch_set_audit": [ctypes.c_void_p, ctypes.c_int],
+            "batch_read_audit": [ctypes.c_void_p, ctypes.c_void_p],
         }
         for short, args in extra.items():
             fn = getattr(handle, "cpgpu_" + short)
@@ -62,6 +68,33 @@ def world():
     return World(lib())
 
 
+AUDIT_FIELDS = ("px", "py", "pz", "Lx", "Ly", "Lz", "kinetic", "potential", "max_step_gain", "steps")
+
+
+def _audit_dict(v):
+    return {"momentum": v[0:3].copy(), "angular_momentum": v[3:6].copy(), "kinetic": float(v[6]),
+            "potential": float(v[7]), "max_step_gain": float(v[8]), "steps": int(v[9])}
+
+
+def set_audit(w, enabled=True):
+    """Enable (or disable) the per-step FP64 momentum / energy audit of world
+    `w` (cpgpu_world_set_audit)."""
+    abi = lib()
+    rc = abi.world_set_audit(w.h, 1 if enabled else 0)
+    if rc != 0:
+        raise CPGPUError(f"status {rc}: {abi.last_error().decode(errors='replace')}")
+
+
+def read_audit(w):
+    """The audit values of world `w` after its last step (cpgpu_world_read_audit)."""
+    abi = lib()
+    v = np.zeros(len(AUDIT_FIELDS))
+    rc = abi.world_read_audit(w.h, v.ctypes.data)
+    if rc != 0:
+        raise CPGPUError(f"status {rc}: {abi.last_error().decode(errors='replace')}")
+    return _audit_dict(v)
+
+
 def _addr(buf):
     if hasattr(buf, "data_ptr"):          # torch tensor (e.g. pinned host memory)
         return buf.data_ptr()
@@ -71,13 +104,28 @@ def _addr(buf):
 class Batch:
     """Independent worlds advanced together by one launch sequence per step."""
 
-    def __init__(self, worlds):
+    def __init__(self, worlds, tune_steps=0):
+        """Pack `worlds`; with tune_steps > 0 the schedule is chosen by timing
+        that many trial steps per candidate (cpgpu_batch_create_tuned)."""
         self.abi = lib()
         arr = (ctypes.c_void_p * len(worlds))(*[w.h.value for w in worlds])
         h = ctypes.c_void_p()
-        self._check(self.abi.batch_create(arr, len(worlds), ctypes.byref(h)))
+        if tune_steps > 0:
+            self._check(self.abi.batch_create_tuned(arr, len(worlds), int(tune_steps), ctypes.byref(h)))
+        else:
+            self._check(self.abi.batch_create(arr, len(worlds), ctypes.byref(h)))
         self.h = h
         self.sizes = [w.n_bodies for w in worlds]
+
+    def schedule(self):
+        """The batch's schedule (cpgpu_batch_schedule)."""
+        sched = (ctypes.c_int * 5)()
+        times = (ctypes.c_double * 2)()
+        self._check(self.abi.batch_schedule(self.h, ctypes.addressof(sched), ctypes.addressof(times)))
+        return {"parts": sched[0], "first_share_pct": sched[1], "rest_chain_workers_per_sm": sched[2],
+                "big_island_rows": sched[3], "tuned": bool(sched[4]),
+                "tuned_ms_per_step": times[0] if times[0] >= 0 else None,
+                "default_ms_per_step": times[1] if times[1] >= 0 else None}
 
     def _check(self, rc):
         if rc != 0:
@@ -122,6 +170,16 @@ class Batch:
         self._check(self.abi.batch_profile(self.h, int(n), ms.ctypes.data, counts.ctypes.data))
         return dict(zip(self.STAGES, ms.tolist())), {"pairs": int(counts[0]), "contacts": int(counts[1]),
                                                       "islands": int(counts[2])}
+
+    def set_audit(self, enabled=True):
+        """Per-step FP64 momentum / energy audit of every world (cpgpu_batch_set_audit)."""
+        self._check(self.abi.batch_set_audit(self.h, 1 if enabled else 0))
+
+    def read_audit(self):
+        """Audit values per world, (n_worlds, 10) FP64 in batch order."""
+        v = np.zeros((len(self.sizes), len(AUDIT_FIELDS)))
+        self._check(self.abi.batch_read_audit(self.h, v.ctypes.data))
+        return v
 
     def launches_per_step(self):
         n = ctypes.c_int()

@@ -56,8 +56,8 @@ SIGNATURES = {
     "get_pairs": (I, [P, P, I, P]),
     "get_contacts": (I, [P, P, I, P]),
     "set_contacts": (I, [P, P, I]),
-    "get_joint_state": (I, [P, P, P, P, P]),
-    "set_joint_state": (I, [P, P, P, P, I]),
+    "get_joint_state": (I, [P, P, P, P, P, P]),
+    "set_joint_state": (I, [P, P, P, P, P, I]),
     "batch_create": (I, [P, I, P]),
     "batch_destroy": (I, [P]),
     "batch_step": (I, [P, I]),

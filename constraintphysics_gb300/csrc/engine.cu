@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <string>
 #include <unordered_map>
@@ -107,15 +108,30 @@ struct Params {
 
 struct Batch;
 
-// BallSocket / Hinge (PersistentConstraint.h:118-313) in the host mirror
+// A joint (PersistentConstraint.h:90-420) in the host mirror
 struct HJoint {
     int b1 = 0, b2 = 0;          // body indices (0-based) in the world
-    int n = 3;                   // 3 ball-socket, 5 hinge
+    int kind = JK_BALL;          // JointKind
+    int n = 3;                   // dofs of its row
+    int seq = 0;                 // creation order among the world's joints and springs
     D3 p1, p2;                   // anchors: tracked points relative to the COM, body frame
-    D3 ax1, ax2;                 // normalised hinge axes, body space
+    D3 ax1, ax2;                 // axes / directions, body space
     double ph = 15000, rh = 15000;
+    double target = 0;           // distance: the attachment points' distance
+    double min_angle = 0, max_angle = 0;   // limits
+    D3 ul, wl;                   // twist: body 1's u and w axes (body space)
     float impulse[kJMax] = {};   // warm-start impulse carried between uploads
-    float u[3] = {}, w[3] = {};  // hinge basis of the last rebuild
+    float u[3] = {}, w[3] = {};  // hinge / slider basis of the last rebuild
+    float angle = 0;             // twist: current angle (unwrapped)
+    int active = 0;              // limits: reached at the last rebuild
+};
+
+// A spring (PhysicsEngine::addSpring, PhysicsEngine.cpp:974-998)
+struct HSpring {
+    int b1 = 0, b2 = 0;
+    int seq = 0;
+    D3 p1, p2;                   // tracked points relative to the COM, body frame
+    double damping = 0, stiffness = 0, rest = 0;
 };
 
 struct World {
@@ -123,11 +139,14 @@ struct World {
     std::vector<Shape> shapes;
     std::vector<Body> bodies;
     std::vector<HJoint> joints;
+    std::vector<HSpring> springs;
+    int constraint_seq = 0;                        // joints and springs created so far
     std::unordered_map<unsigned int, int> nodes;   // same insert sequence as constraint_graph_nodes
     std::vector<cpgpu_contact> contacts;           // host copy of the contact graph
     std::vector<uint32_t> last_pairs;
     std::unique_ptr<Batch> dev;
     bool dev_valid = false;
+    bool audit = false;                            // FP64 audit requested (cpgpu_world_set_audit)
 };
 
 // ---------------------------------------------------------------- shape packing ----
@@ -501,7 +520,8 @@ struct Batch {
     int slot_bytes = 0;
     bool prims = false;                // the batch holds spheres or cylinders
     bool meshes = false;               // the batch holds static triangle meshes
-    bool joints = false;               // the batch holds joints
+    bool joints = false;               // the batch holds joints (or springs: joint edges)
+    bool springs = false;              // the batch holds springs
     bool systems = false;              // ... and holonomic systems
     cudaStream_t st = nullptr;
     cudaStream_t side = nullptr;       // concurrent branch (small-island PGS)
@@ -518,9 +538,12 @@ struct Batch {
     std::vector<int> world_jstart;     // joint ranges of the worlds
     std::vector<uint8_t> movement;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double* audit = nullptr;           // FP64 audit values (kAuditValues per world), null when disabled
 
     ~Batch() {
         for (auto& g : graph) if (g) cudaGraphExecDestroy(g);
+        if (audit) cudaFree(audit);
+        if (snap) cudaFree(snap);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (mem) cudaFree(mem);
@@ -547,6 +570,7 @@ struct Batch {
         launch_islands(x, isl_smem, L);
         launch_pgs_schedule(x, L); mark(5);
         for (int s = 0; s < substeps; s++) {
+            launch_springs(x, L);                          // impulses before the rows read the velocities
             launch_rows(x, s == 0, s == substeps - 1, L);
             launch_joint_rows(x, s == 0, L);               mark(6 + 3 * s);
             launch_pgs(x, dv_cap, pgs_blocks, side, fork, join, L);
@@ -554,6 +578,7 @@ struct Batch {
             launch_integrate(x, s == substeps - 1, L);     mark(8 + 3 * s);
         }
         launch_geometry(x, 0, L);  mark(6 + 3 * substeps);
+        launch_audit(x, L);
     }
     // kernels per step: gravity 1, pairs 2 + scan 3 + clamp 1, narrowphase 2
     // (+1 with spheres / cylinders, +1 with meshes), merge 6 + 3 scans, islands 2 + scan 3,
@@ -561,7 +586,58 @@ struct Batch {
     // (+2 per substep and 1 factorisation with joints)
     int launches_per_step() const {
         return 1 + 6 + 2 + (prims ? 1 : 0) + (meshes ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 5 * substeps + 1 + (joints ? 2 * substeps : 0) +
-               (systems ? 1 : 0);
+               (systems ? 1 : 0) + (audit ? 1 : 0) + (springs ? substeps : 0);
+    }
+
+    // solver schedule: chain workers per SM of k_pgs_big (0 = as many as fit)
+    // and the big-island row threshold; the step graphs are rebuilt
+    int pgs_per_sm = 0;
+    void set_schedule(int per_sm, int big_rows) {
+        CK(cudaStreamSynchronize(st));
+        pgs_per_sm = per_sm;
+        const int fit = pgs_big_blocks_per_sm(dv_cap);
+        pgs_blocks = n_sms * (per_sm > 0 ? std::min(per_sm, fit) : fit);
+        d[0].big_rows = d[1].big_rows = big_rows;
+        for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        build_graphs();
+    }
+    // whole device state (one arena) copied aside and back, so that trial
+    // steps leave no trace (the autotuner's timing runs)
+    uint8_t* snap = nullptr;
+    int snap_parity = 0;
+    void snapshot() {
+        if (!snap) CK(cudaMalloc(&snap, bytes));
+        CK(cudaMemcpyAsync(snap, mem, bytes, cudaMemcpyDeviceToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        snap_parity = parity;
+    }
+    void restore(bool release) {
+        CK(cudaMemcpyAsync(mem, snap, bytes, cudaMemcpyDeviceToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        parity = snap_parity;
+        if (release) { CK(cudaFree(snap)); snap = nullptr; }
+    }
+
+    // FP64 audit on or off: the values restart (zeroed) when it is enabled,
+    // and the step graphs are rebuilt with or without the audit kernel
+    void set_audit(bool on) {
+        if (on == (audit != nullptr)) return;
+        CK(cudaStreamSynchronize(st));
+        if (on) {
+            CK(cudaMalloc(&audit, sizeof(double) * kAuditValues * std::max(n_worlds, 1)));
+            CK(cudaMemset(audit, 0, sizeof(double) * kAuditValues * std::max(n_worlds, 1)));
+        } else {
+            CK(cudaFree(audit));
+            audit = nullptr;
+        }
+        d[0].audit = d[1].audit = audit;
+        for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        build_graphs();
+    }
+    void read_audit(double* out) {
+        if (!audit) throw ApiFail{CPGPU_ERR_INVALID_ARG, "the audit is not enabled"};
+        CK(cudaMemcpyAsync(out, audit, sizeof(double) * kAuditValues * n_worlds, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
     }
 
     void build_graphs() {
@@ -616,12 +692,15 @@ static std::vector<int> map_iteration_order(const World& w) {
 }
 
 // ---------------------------------------------------------------- holonomic systems ----
-// A world's joint edges (one per jointed body pair, joints in insertion order)
-// and its holonomic systems, found as PhysicsEngine::maintainHolonomicSystems
-// (PhysicsEngine.cpp:1292-1306, 1466-1532, 1745-1777) finds them on the first
-// step: nodes in node-map order, each node's joint edges by the other body's
-// id, a scan from every edge not yet in a system collecting the edges
-// connected through dynamic bodies.
+// A world's joint edges (one per body pair joined by joints or springs, the
+// joints in insertion order) and its holonomic systems, found as
+// PhysicsEngine::maintainHolonomicSystems (PhysicsEngine.cpp:1292-1306,
+// 1466-1532, 1745-1777) finds them on the first step: nodes in node-map order,
+// each node's edges by the other body's id, a scan from every edge holding a
+// holonomic joint and not yet in a system, collecting the edges with
+// holonomic joints connected to it through dynamic bodies.  Cone and twist
+// limits are not holonomic (PersistentConstraint.h:168, 208) and springs are
+// no constraint rows: their edges connect islands but join no system.
 struct HSystem {
     std::vector<int> cons;       // joint indices (world-local) in elimination order
     std::vector<int> vpos, table;
@@ -631,10 +710,13 @@ struct HSystem {
 
 struct JointGraph {
     std::vector<std::pair<int, int>> edge_pair;       // (lower body, higher body)
-    std::vector<std::vector<int>> edge_joints;
+    std::vector<std::vector<int>> edge_joints;        // world-local joint indices, creation order
+    std::vector<int> edge_first;                      // body the edge was created from (its first constraint's b1)
     std::vector<int> edge_sys;
     std::vector<HSystem> systems;
 };
+
+static bool holonomic_kind(int k) { return !jk_limit(k); }
 
 // HolonomicSystem::HolonomicSystem (HolonomicBlockSolver.cpp:11-132): greedy
 // minimum-fill elimination order over constraints that share a body, and the
@@ -696,19 +778,31 @@ static HSystem order_system(const World& w, const std::vector<int>& og) {
 static JointGraph joint_graph(const World& w, const std::vector<int>& map_order) {
     JointGraph G;
     std::map<std::pair<int, int>, int> idx;
-    for (int j = 0; j < (int)w.joints.size(); j++) {
-        std::pair<int, int> k(std::min(w.joints[j].b1, w.joints[j].b2), std::max(w.joints[j].b1, w.joints[j].b2));
+    // joints and springs in creation order: an edge is created by the first
+    // constraint between its bodies
+    std::vector<std::pair<int, int>> items;   // (seq, joint index or -(spring index + 1))
+    for (int j = 0; j < (int)w.joints.size(); j++) items.push_back({w.joints[j].seq, j});
+    for (int k = 0; k < (int)w.springs.size(); k++) items.push_back({w.springs[k].seq, -(k + 1)});
+    std::sort(items.begin(), items.end());
+    for (const auto& it0 : items) {
+        const int b1 = it0.second >= 0 ? w.joints[it0.second].b1 : w.springs[-it0.second - 1].b1;
+        const int b2 = it0.second >= 0 ? w.joints[it0.second].b2 : w.springs[-it0.second - 1].b2;
+        std::pair<int, int> k(std::min(b1, b2), std::max(b1, b2));
         auto it = idx.find(k);
         if (it == idx.end()) {
             it = idx.emplace(k, (int)G.edge_pair.size()).first;
             G.edge_pair.push_back(k);
             G.edge_joints.emplace_back();
+            G.edge_first.push_back(b1);
         }
-        G.edge_joints[it->second].push_back(j);
+        if (it0.second >= 0) G.edge_joints[it->second].push_back(it0.second);
     }
     const int ne = (int)G.edge_pair.size();
     G.edge_sys.assign(ne, -1);
     if (ne == 0 || w.p.pgs_holo <= 0) return G;
+    std::vector<char> holo(ne, 0);
+    for (int e = 0; e < ne; e++)
+        for (int j : G.edge_joints[e]) holo[e] |= holonomic_kind(w.joints[j].kind);
     const int nb = (int)w.bodies.size();
     std::vector<std::vector<int>> adj(nb);
     for (int e = 0; e < ne; e++) { adj[G.edge_pair[e].first].push_back(e); adj[G.edge_pair[e].second].push_back(e); }
@@ -720,7 +814,7 @@ static JointGraph joint_graph(const World& w, const std::vector<int>& map_order)
     std::vector<char> scanned(ne, 0);
     for (int node : map_order)
         for (int e0 : adj[node]) {
-            if (scanned[e0]) continue;
+            if (scanned[e0] || !holo[e0]) continue;
             scanned[e0] = 1;
             // getAllEdgesConnectedHolonomically: DFS with a LIFO stack
             std::vector<char> vis(ne, 0);
@@ -732,17 +826,20 @@ static JointGraph joint_graph(const World& w, const std::vector<int>& map_order)
                 vis[v] = 1;
                 conn.push_back(v);
                 // the first body's edges, then the second's (n1 is the body
-                // the edge was created from: the first joint's b1)
+                // the edge was created from)
                 std::vector<int> nbr;
-                const HJoint& j0 = w.joints[G.edge_joints[v][0]];
-                for (int end : {j0.b1, j0.b2})
+                const int first = G.edge_first[v];
+                const int second = first == G.edge_pair[v].first ? G.edge_pair[v].second : G.edge_pair[v].first;
+                for (int end : {first, second})
                     if (w.bodies[end].movement == CPGPU_DYNAMIC) nbr.insert(nbr.end(), adj[end].begin(), adj[end].end());
-                for (int x : nbr) if (!vis[x]) stack.push_back(x);
+                for (int x : nbr) if (!vis[x] && holo[x]) stack.push_back(x);
             }
             for (int x : conn) scanned[x] = 1;
             if (conn.size() <= 1) continue;
             std::vector<int> og;
-            for (int x : conn) for (int j : G.edge_joints[x]) og.push_back(j);
+            for (int x : conn)
+                for (int j : G.edge_joints[x])
+                    if (holonomic_kind(w.joints[j].kind)) og.push_back(j);
             const int sid = (int)G.systems.size();
             for (int x : conn) G.edge_sys[x] = sid;
             G.systems.push_back(order_system(w, og));
@@ -900,31 +997,37 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
         }
     }
 
-    // ---- joints, joint edges and holonomic systems of the worlds
-    std::vector<int> j_b1, j_b2, j_n;
-    std::vector<float4> j_p1, j_p2, j_ax1, j_ax2, j_u, j_w;
+    // ---- joints, joint edges, springs and holonomic systems of the worlds
+    std::vector<int> j_b1, j_b2, j_n, j_kind, j_active;
+    std::vector<float4> j_p1, j_p2, j_ax1, j_ax2, j_u, j_w, j_par, j_ul, j_wl;
     std::vector<float2> j_hard;
-    std::vector<float> j_imp;
+    std::vector<float> j_imp, j_angle;
     std::vector<uint64_t> je_key;
-    std::vector<int> je_jstart, je_jcount, je_sys, je_wstart{0}, je_wjstart{0}, hs_wstart{0};
+    std::vector<int> je_jstart, je_jcount, je_jlist, je_sys, je_wstart{0}, je_wjstart{0}, hs_wstart{0};
     std::vector<int> hs_cstart{0}, hs_cons, hs_vpos, hs_degree, hs_tstart{0}, hs_table, hs_bstart, hs_cap, hs_fp64, hs_wk;
     std::vector<int> hs_lbase, hs_lstart, hs_lrow, hs_lloc;   // per-column lists of the nonzero blocks below the diagonal
+    std::vector<int> sp_b1, sp_b2, sp_wstart{0};
+    std::vector<float4> sp_p1, sp_p2, sp_par;
     size_t pool32_n = 0, pool64_n = 0, work_n = 0;
+    auto f4d = [](const D3& v) { return make_float4((float)v.x, (float)v.y, (float)v.z, 0.f); };
     for (size_t wi = 0; wi < worlds.size(); wi++) {
         const World& w = *worlds[wi];
         const int base = wstart[wi], jbase = (int)j_b1.size();
         for (const HJoint& j : w.joints) {
-            j_b1.push_back(base + j.b1); j_b2.push_back(base + j.b2); j_n.push_back(j.n);
-            j_p1.push_back(make_float4((float)j.p1.x, (float)j.p1.y, (float)j.p1.z, 0.f));
-            j_p2.push_back(make_float4((float)j.p2.x, (float)j.p2.y, (float)j.p2.z, 0.f));
-            j_ax1.push_back(make_float4((float)j.ax1.x, (float)j.ax1.y, (float)j.ax1.z, 0.f));
-            j_ax2.push_back(make_float4((float)j.ax2.x, (float)j.ax2.y, (float)j.ax2.z, 0.f));
+            j_b1.push_back(base + j.b1); j_b2.push_back(base + j.b2); j_n.push_back(j.n); j_kind.push_back(j.kind);
+            j_p1.push_back(f4d(j.p1)); j_p2.push_back(f4d(j.p2));
+            j_ax1.push_back(f4d(j.ax1)); j_ax2.push_back(f4d(j.ax2));
             j_u.push_back(make_float4(j.u[0], j.u[1], j.u[2], 0.f));
             j_w.push_back(make_float4(j.w[0], j.w[1], j.w[2], 0.f));
             j_hard.push_back(make_float2((float)j.ph, (float)j.rh));
+            const double par_x = j.kind == JK_DISTANCE ? j.target : j.max_angle;
+            j_par.push_back(make_float4((float)par_x, (float)j.min_angle, 0.f, 0.f));
+            j_ul.push_back(f4d(j.ul)); j_wl.push_back(f4d(j.wl));
+            j_angle.push_back(j.angle);
+            j_active.push_back(j.active);
             for (int k = 0; k < kJMax; k++) j_imp.push_back(j.impulse[k]);
         }
-        if (!w.joints.empty()) {
+        if (!w.joints.empty() || !w.springs.empty()) {
             std::vector<int> order = map_iteration_order(w);
             JointGraph G = joint_graph(w, order);
             std::vector<int> eorder(G.edge_pair.size());
@@ -933,15 +1036,48 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
             const int sbase = (int)hs_degree.size();
             for (int e : eorder) {
                 je_key.push_back(((uint64_t)(base + G.edge_pair[e].first) << 32) | (uint32_t)(base + G.edge_pair[e].second));
-                je_jstart.push_back(jbase + G.edge_joints[e][0]);
+                // the edge's joints (creation order) through an index list; a
+                // spring-only edge has none: it connects islands without rows
+                // and does not stop the pair from colliding
+                je_jstart.push_back((int)je_jlist.size());
                 je_jcount.push_back((int)G.edge_joints[e].size());
+                for (int j : G.edge_joints[e]) je_jlist.push_back(jbase + j);
                 je_sys.push_back(G.edge_sys[e] >= 0 ? sbase + G.edge_sys[e] : -1);
             }
-            // joints of an edge must be contiguous for the device's (start, count)
-            for (int e : eorder)
-                for (size_t k = 1; k < G.edge_joints[e].size(); k++)
-                    if (G.edge_joints[e][k] != G.edge_joints[e][0] + (int)k)
-                        throw ApiFail{CPGPU_ERR_UNSUPPORTED, "joints between one body pair must be added consecutively"};
+            // springs in the order the reference applies them: nodes in
+            // node-map order, each node's edges by the other body's id, each
+            // edge once, an edge's springs in creation order
+            if (!w.springs.empty()) {
+                const int nb = (int)w.bodies.size();
+                std::vector<std::vector<int>> sadj(nb);
+                for (int e = 0; e < (int)G.edge_pair.size(); e++) {
+                    sadj[G.edge_pair[e].first].push_back(e);
+                    sadj[G.edge_pair[e].second].push_back(e);
+                }
+                std::map<std::pair<int, int>, std::vector<int>> by_pair;
+                for (int k = 0; k < (int)w.springs.size(); k++)
+                    by_pair[{std::min(w.springs[k].b1, w.springs[k].b2), std::max(w.springs[k].b1, w.springs[k].b2)}].push_back(k);
+                std::vector<char> seen(G.edge_pair.size(), 0);
+                for (int node : order) {
+                    std::vector<int> es = sadj[node];
+                    std::sort(es.begin(), es.end(), [&](int x, int y) {
+                        auto other = [&](int e) { return G.edge_pair[e].first == node ? G.edge_pair[e].second : G.edge_pair[e].first; };
+                        return other(x) < other(y);
+                    });
+                    for (int e : es) {
+                        if (seen[e]) continue;
+                        seen[e] = 1;
+                        auto it = by_pair.find(G.edge_pair[e]);
+                        if (it == by_pair.end()) continue;
+                        for (int k : it->second) {
+                            const HSpring& sp = w.springs[k];
+                            sp_b1.push_back(base + sp.b1); sp_b2.push_back(base + sp.b2);
+                            sp_p1.push_back(f4d(sp.p1)); sp_p2.push_back(f4d(sp.p2));
+                            sp_par.push_back(make_float4((float)sp.damping, (float)sp.stiffness, (float)sp.rest, 0.f));
+                        }
+                    }
+                }
+            }
             for (const HSystem& H : G.systems) {
                 for (int j : H.cons) hs_cons.push_back(jbase + j);
                 hs_vpos.insert(hs_vpos.end(), H.vpos.begin(), H.vpos.end());
@@ -974,15 +1110,21 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
         je_wstart.push_back((int)je_key.size());
         je_wjstart.push_back((int)j_b1.size());
         hs_wstart.push_back((int)hs_degree.size());
+        sp_wstart.push_back((int)sp_b1.size());
     }
     const int n_joints = (int)j_b1.size(), n_je = (int)je_key.size(), n_sys = (int)hs_degree.size();
+    const int n_springs = (int)sp_b1.size();
     B->world_jstart = je_wjstart;
-    B->joints = n_joints > 0;
+    B->joints = n_je > 0;
+    B->springs = n_springs > 0;
     B->systems = n_sys > 0;
 
     // ---- capacities and device allocation
     // capacities per body, with floors; both can be overridden by the environment
     const int floor_ = env_int("CPGPU_CAPACITY_FLOOR", 1 << 14);
+    // polls of each bounded device wait; lowering it makes the waits give up
+    // (ST_TIMEOUT, CPGPU_ERR_TIMEOUT) without any fault, for failure tests
+    const long long wait_limit = std::max(0, env_int("CPGPU_WAIT_LIMIT", (int)std::min<long long>(kDefaultWaitLimit, 1 << 30)));
     const int cap_pairs = std::max(floor_, env_int("CPGPU_PAIRS_PER_BODY", 24) * N);
     const int cap_edges = cap_pairs;
     const int cap_contacts = std::max(std::max(2 * floor_, 2 * (int)cmag.size()), env_int("CPGPU_CONTACTS_PER_BODY", 24) * N);
@@ -1075,18 +1217,33 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
         x.n_joints = n_joints;
         x.n_joint_edges = n_je;
         x.lin_err_threshold = 15.0f;   // excessive_linear_error_torque_threshold (PhysicsEngine.h:217)
-        if (n_joints > 0) {
+        x.wait_limit = wait_limit;
+        x.big_rows = kDefaultBigRows;
+        if (n_springs > 0) {
+            SpringStore& S = x.sp;
+            S.n = n_springs;
+            S.b1 = A.take<int>(n_springs); S.b2 = A.take<int>(n_springs);
+            S.p1 = A.take<float4>(n_springs); S.p2 = A.take<float4>(n_springs); S.par = A.take<float4>(n_springs);
+            S.world_start = A.take<int>(worlds.size() + 1);
+        }
+        if (n_je > 0) {
+            // joint edges (joints or springs): the joint store is allocated
+            // even when only springs are present
             JointStore& J = x.jt;
             int* ib1 = A.take<int>(n_joints); int* ib2 = A.take<int>(n_joints); int* in = A.take<int>(n_joints);
             J.b1 = ib1; J.b2 = ib2; J.n = in;
+            J.kind = A.take<int>(n_joints);
             J.p1 = A.take<float4>(n_joints); J.p2 = A.take<float4>(n_joints);
             J.ax1 = A.take<float4>(n_joints); J.ax2 = A.take<float4>(n_joints);
             J.hard = A.take<float2>(n_joints);
+            J.par = A.take<float4>(n_joints); J.ul = A.take<float4>(n_joints); J.wl = A.take<float4>(n_joints);
             J.impulse = A.take<float>(kJMax * (size_t)n_joints);
             J.u = A.take<float4>(n_joints); J.w = A.take<float4>(n_joints);
+            J.angle = A.take<float>(n_joints); J.active = A.take<int>(n_joints);
             J.rows = A.take<JointRow>(n_joints);
             JointEdgeStore& E = x.je;
             E.key = A.take<uint64_t>(n_je); E.jstart = A.take<int>(n_je); E.jcount = A.take<int>(n_je);
+            E.jlist = A.take<int>(je_jlist.size());
             E.sys = A.take<int>(n_je);
             E.world_start = A.take<int>(worlds.size() + 1); E.world_jstart = A.take<int>(worlds.size() + 1);
             HoloStore& H = x.hs;
@@ -1140,18 +1297,29 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     up(cs[0].tri, ctri.data(), nc * 4);
     int host_counts[5] = {0, ne, 0, nc, 0};   // n_pairs, n_edges[0], n_edges[1], n_contacts[0], n_contacts[1]
     up(counts, host_counts, sizeof(host_counts));
-    if (n_joints > 0) {
+    if (n_springs > 0) {
+        const SpringStore& S = x.sp;
+        up((void*)S.b1, sp_b1.data(), n_springs * 4); up((void*)S.b2, sp_b2.data(), n_springs * 4);
+        up((void*)S.p1, sp_p1.data(), n_springs * 16); up((void*)S.p2, sp_p2.data(), n_springs * 16);
+        up((void*)S.par, sp_par.data(), n_springs * 16);
+        up((void*)S.world_start, sp_wstart.data(), sp_wstart.size() * 4);
+    }
+    if (n_je > 0) {
         const JointStore& J = x.jt;
         up((void*)J.b1, j_b1.data(), n_joints * 4); up((void*)J.b2, j_b2.data(), n_joints * 4); up((void*)J.n, j_n.data(), n_joints * 4);
+        up((void*)J.kind, j_kind.data(), n_joints * 4);
         up((void*)J.p1, j_p1.data(), n_joints * 16); up((void*)J.p2, j_p2.data(), n_joints * 16);
         up((void*)J.ax1, j_ax1.data(), n_joints * 16); up((void*)J.ax2, j_ax2.data(), n_joints * 16);
         up((void*)J.hard, j_hard.data(), n_joints * 8);
+        up((void*)J.par, j_par.data(), n_joints * 16); up((void*)J.ul, j_ul.data(), n_joints * 16); up((void*)J.wl, j_wl.data(), n_joints * 16);
         up(J.impulse, j_imp.data(), j_imp.size() * 4);
         up(J.u, j_u.data(), n_joints * 16); up(J.w, j_w.data(), n_joints * 16);
-        CK(cudaMemsetAsync(J.rows, 0, sizeof(JointRow) * (size_t)n_joints, B->st));
+        up(J.angle, j_angle.data(), n_joints * 4); up(J.active, j_active.data(), n_joints * 4);
+        if (n_joints > 0) CK(cudaMemsetAsync(J.rows, 0, sizeof(JointRow) * (size_t)n_joints, B->st));
         const JointEdgeStore& E = x.je;
         up((void*)E.key, je_key.data(), n_je * 8); up((void*)E.jstart, je_jstart.data(), n_je * 4);
         up((void*)E.jcount, je_jcount.data(), n_je * 4); up((void*)E.sys, je_sys.data(), n_je * 4);
+        up((void*)E.jlist, je_jlist.data(), je_jlist.size() * 4);
         up((void*)E.world_start, je_wstart.data(), je_wstart.size() * 4);
         up((void*)E.world_jstart, je_wjstart.data(), je_wjstart.size() * 4);
         const HoloStore& H = x.hs;
@@ -1177,6 +1345,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     launch_geometry(B->d[0], 1, L);
     prepare_kernels();
     prepare_pgs(B->dv_cap);
+    B->pgs_per_sm = pgs_per_sm;
     B->pgs_blocks = B->n_sms * (pgs_per_sm > 0 ? std::min(pgs_per_sm, pgs_big_blocks_per_sm(B->dv_cap)) : pgs_big_blocks_per_sm(B->dv_cap));
     CK(cudaStreamSynchronize(B->st));
     CK(cudaGetLastError());
@@ -1203,12 +1372,15 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
     int counts[6];
     CK(cudaMemcpyAsync(counts, x.n_pairs, sizeof(counts), cudaMemcpyDeviceToHost, B.st));
     const int nj = x.n_joints;
-    std::vector<float> jimp((size_t)kJMax * nj);
+    std::vector<float> jimp((size_t)kJMax * nj), jang(nj);
     std::vector<float4> ju(nj), jw(nj);
+    std::vector<int> jact(nj);
     if (nj > 0) {
         CK(cudaMemcpyAsync(jimp.data(), x.jt.impulse, jimp.size() * 4, cudaMemcpyDeviceToHost, B.st));
         CK(cudaMemcpyAsync(ju.data(), x.jt.u, nj * 16, cudaMemcpyDeviceToHost, B.st));
         CK(cudaMemcpyAsync(jw.data(), x.jt.w, nj * 16, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(jang.data(), x.jt.angle, nj * 4, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(jact.data(), x.jt.active, nj * 4, cudaMemcpyDeviceToHost, B.st));
     }
     CK(cudaStreamSynchronize(B.st));
     // contact graph (current = the old buffers of the next step)
@@ -1261,6 +1433,8 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
             for (size_t j = 0; j < w.joints.size(); j++) {
                 const size_t g = (size_t)j0 + j;
                 for (int k = 0; k < kJMax; k++) w.joints[j].impulse[k] = jimp[kJMax * g + k];
+                w.joints[j].angle = jang[g];
+                w.joints[j].active = jact[g];
                 w.joints[j].u[0] = ju[g].x; w.joints[j].u[1] = ju[g].y; w.joints[j].u[2] = ju[g].z;
                 w.joints[j].w[0] = jw[g].x; w.joints[j].w[1] = jw[g].y; w.joints[j].w[2] = jw[g].z;
             }
@@ -1315,8 +1489,9 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
     CK(cudaStreamSynchronize(B.st));
     struct Buf {
         std::vector<float4> pos, rot, vel, angv;
-        std::vector<float> iw, iinv, jimp;
+        std::vector<float> iw, iinv, jimp, jang;
         std::vector<float4> ju, jw;
+        std::vector<int> jact;
         std::vector<uint64_t> key, mag;
         std::vector<int> cstart, ccount, state, tri;
         std::vector<float4> p1, p2, nrm, imp, fu, fw;
@@ -1335,9 +1510,10 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
         get(b.iw.data(), x.iw + 9 * (size_t)s0, 36 * (size_t)nb); get(b.iinv.data(), x.iinv + 9 * (size_t)s0, 36 * (size_t)nb);
         if (x.n_joints > 0) {
             const int j0 = B.world_jstart[w], nj = B.world_jstart[w + 1] - j0;
-            b.jimp.resize((size_t)kJMax * nj); b.ju.resize(nj); b.jw.resize(nj);
+            b.jimp.resize((size_t)kJMax * nj); b.ju.resize(nj); b.jw.resize(nj); b.jang.resize(nj); b.jact.resize(nj);
             get(b.jimp.data(), x.jt.impulse + (size_t)kJMax * j0, (size_t)kJMax * nj * 4);
             get(b.ju.data(), x.jt.u + j0, nj * 16); get(b.jw.data(), x.jt.w + j0, nj * 16);
+            get(b.jang.data(), x.jt.angle + j0, nj * 4); get(b.jact.data(), x.jt.active + j0, nj * 4);
         }
         const int e0 = rg[4 * i], e1 = rg[4 * i + 1], c0 = rg[4 * i + 2], c1 = rg[4 * i + 3];
         const int ne = e1 - e0, nc = c1 - c0;
@@ -1371,6 +1547,8 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
         }
         for (size_t j = 0; j < b.ju.size() && j < w.joints.size(); j++) {
             for (int k = 0; k < kJMax; k++) w.joints[j].impulse[k] = b.jimp[kJMax * j + k];
+            w.joints[j].angle = b.jang[j];
+            w.joints[j].active = b.jact[j];
             w.joints[j].u[0] = b.ju[j].x; w.joints[j].u[1] = b.ju[j].y; w.joints[j].u[2] = b.ju[j].z;
             w.joints[j].w[0] = b.jw[j].x; w.joints[j].w[1] = b.jw[j].y; w.joints[j].w[2] = b.jw[j].z;
         }
@@ -1519,6 +1697,21 @@ static void ensure_device(World& w) {
 // ================================================================== C ABI ====
 using namespace cpgpu;
 
+// A batch's schedule: how its worlds are cut into parts that step
+// concurrently (each on its own streams with its own graphs), how many solver
+// chains per SM the later parts may run, and the island size from which an
+// island takes the warp-per-island solver.  Every world steps exactly as it
+// does alone under any schedule (the parts never interact; both island
+// solvers give identical results), so the schedule only changes the time.
+namespace cpgpu {
+struct Schedule {
+    int parts = 1;          // batch parts
+    int first_share = 100;  // percent of the bodies in the first part (the largest worlds)
+    int rest_per_sm = 0;    // chain workers per SM of the later parts (0 = as many as fit)
+    int big_rows = kDefaultBigRows;
+};
+}  // namespace cpgpu
+
 struct cpgpu_world { World w; };
 // A batch of worlds, split by world size into parts that step concurrently,
 // each on its own streams with its own graphs.  A step is bounded by the
@@ -1535,6 +1728,9 @@ struct cpgpu_batch {
     std::vector<int*> rows;               // per part: batch row of each of its bodies
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr;
     std::vector<cudaEvent_t> done;        // per part
+    Schedule sched;                       // the schedule the batch was built for
+    bool tuned = false;                   // chosen by the autotuner (now or from its cache)
+    double tuned_ms = -1, default_ms = -1;   // per step, measured when tuned here
     ~cpgpu_batch() {
         for (int* r : rows) if (r) cudaFree(r);
         if (stage) cudaFree(stage);
@@ -1783,75 +1979,142 @@ int cpgpu_body_set_mass(cpgpu_world* w, uint32_t id, double mass) {
     });
 }
 
-// PhysicsEngine::addBallSocketConstraint / addHingeConstraint
-// (PhysicsEngine.cpp:664-723): anchors in each body's model coordinates become
-// tracked points (RigidBody::trackPoint, RigidBody.cpp:134-137); hinge axes
-// are normalised; the two bodies stop colliding with each other.
-static uint32_t add_joint(World& w, int n, uint32_t b1, uint32_t b2, const double* a1, const double* a2, const double* ax1,
-                          const double* ax2, double ph, double rh) {
-    if (!a1 || !a2 || (n == 5 && (!ax1 || !ax2))) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null anchor or axis"};
+// PhysicsEngine::add*Constraint (PhysicsEngine.cpp:623-972): anchors in each
+// body's model coordinates become tracked points (RigidBody::trackPoint,
+// RigidBody.cpp:134-137); hinge, slider and sliding-hinge axes are
+// normalised (cone and twist directions are taken as given); the two bodies
+// stop colliding with each other.
+static HJoint& add_joint(World& w, int kind, int n, uint32_t b1, uint32_t b2, const double* a1, const double* a2,
+                         const double* ax1, const double* ax2, double ph, double rh) {
+    const bool need_anchor = !jk_limit(kind);
+    const bool need_axis = kind == JK_HINGE || kind == JK_SLIDER || kind == JK_SLIDING_HINGE || jk_limit(kind);
+    if ((need_anchor && (!a1 || !a2)) || (need_axis && (!ax1 || !ax2))) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null anchor or axis"};
     if (b1 == b2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "a joint needs two different bodies"};
     Body& x = body_ref(w, b1);
     Body& y = body_ref(w, b2);
     begin_mutation(w);
     HJoint j;
-    j.b1 = (int)b1 - 1; j.b2 = (int)b2 - 1; j.n = n;
-    j.p1 = x.local_origin + D3(a1[0], a1[1], a1[2]);
-    j.p2 = y.local_origin + D3(a2[0], a2[1], a2[2]);
-    if (n == 5) { j.ax1 = D3(ax1[0], ax1[1], ax1[2]).normalize(); j.ax2 = D3(ax2[0], ax2[1], ax2[2]).normalize(); }
+    j.b1 = (int)b1 - 1; j.b2 = (int)b2 - 1; j.n = n; j.kind = kind;
+    j.seq = w.constraint_seq++;
+    if (need_anchor) {
+        j.p1 = x.local_origin + D3(a1[0], a1[1], a1[2]);
+        j.p2 = y.local_origin + D3(a2[0], a2[1], a2[2]);
+    }
+    if (need_axis) {
+        j.ax1 = D3(ax1[0], ax1[1], ax1[2]);
+        j.ax2 = D3(ax2[0], ax2[1], ax2[2]);
+        if (!jk_limit(kind)) { j.ax1 = j.ax1.normalize(); j.ax2 = j.ax2.normalize(); }
+    }
     j.ph = ph; j.rh = rh;
     w.joints.push_back(j);
-    return (uint32_t)w.joints.size();
+    return w.joints.back();
 }
+
+static uint32_t joint_id(const World& w) { return (uint32_t)w.constraint_seq; }
 
 int cpgpu_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], double strength,
                           uint32_t* out_id) {
     W_OR_FAIL(w);
     return guarded([&] {
-        uint32_t id = add_joint(w->w, 3, b1, b2, a1, a2, nullptr, nullptr, strength, 0);
-        if (out_id) *out_id = id;
+        add_joint(w->w, JK_BALL, 3, b1, b2, a1, a2, nullptr, nullptr, strength, 0);
+        if (out_id) *out_id = joint_id(w->w);
         return CPGPU_OK;
     });
 }
-int cpgpu_add_distance(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, double, double, uint32_t*) {
+int cpgpu_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], double target,
+                       double strength, uint32_t* out_id) {
     W_OR_FAIL(w);
-    return fail(CPGPU_ERR_UNSUPPORTED, "distance constraints are not implemented on the device path");
+    return guarded([&] {
+        HJoint& j = add_joint(w->w, JK_DISTANCE, 1, b1, b2, a1, a2, nullptr, nullptr, strength, 0);
+        // -1: the attachment points' distance now (PhysicsEngine.cpp:630-635)
+        if (target == -1) {
+            const Body &x = w->w.bodies[j.b1], &y = w->w.bodies[j.b2];
+            target = ((x.com + qrot(x.q, j.p1)) - (y.com + qrot(y.q, j.p2))).mag();
+        }
+        j.target = target;
+        if (out_id) *out_id = joint_id(w->w);
+        return CPGPU_OK;
+    });
 }
-int cpgpu_add_weld(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, double, double, uint32_t*) {
+int cpgpu_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], double ps, double rs,
+                   uint32_t* out_id) {
     W_OR_FAIL(w);
-    return fail(CPGPU_ERR_UNSUPPORTED, "weld constraints are not implemented on the device path");
+    return guarded([&] {
+        add_joint(w->w, JK_WELD, 6, b1, b2, a1, a2, nullptr, nullptr, ps, rs);
+        if (out_id) *out_id = joint_id(w->w);
+        return CPGPU_OK;
+    });
 }
-int cpgpu_add_twist_limit(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, double, double, double,
-                          uint32_t*) {
+int cpgpu_add_twist_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double ax1[3], const double ax2[3], double min_angle,
+                          double max_angle, double rs, uint32_t* out_id) {
     W_OR_FAIL(w);
-    return fail(CPGPU_ERR_UNSUPPORTED, "twist limits are not implemented on the device path");
+    return guarded([&] {
+        HJoint& j = add_joint(w->w, JK_TWIST, 1, b1, b2, nullptr, nullptr, ax1, ax2, 0, rs);
+        j.min_angle = min_angle;
+        j.max_angle = max_angle;
+        // TwistLimit constructor (PersistentConstraint.h:177-184): body 1's
+        // perpendicular basis of its twist axis, w first
+        j.ax1.basis(&j.wl, &j.ul);
+        if (out_id) *out_id = joint_id(w->w);
+        return CPGPU_OK;
+    });
 }
-int cpgpu_add_cone_limit(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, double, double,
-                         uint32_t*) {
+int cpgpu_add_cone_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double ax1[3], const double ax2[3], double max_angle,
+                         double rs, uint32_t* out_id) {
     W_OR_FAIL(w);
-    return fail(CPGPU_ERR_UNSUPPORTED, "cone limits are not implemented on the device path");
+    return guarded([&] {
+        HJoint& j = add_joint(w->w, JK_CONE, 1, b1, b2, nullptr, nullptr, ax1, ax2, 0, rs);
+        j.max_angle = max_angle;
+        if (out_id) *out_id = joint_id(w->w);
+        return CPGPU_OK;
+    });
 }
-int cpgpu_add_spring(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, double, double, double,
-                     uint32_t*) {
+int cpgpu_add_spring(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], double damping,
+                     double stiffness, double rest, uint32_t* out_id) {
     W_OR_FAIL(w);
-    return fail(CPGPU_ERR_UNSUPPORTED, "springs are not implemented on the device path");
+    return guarded([&] {
+        if (!a1 || !a2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null anchor"};
+        if (b1 == b2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "a spring needs two different bodies"};
+        Body& x = body_ref(w->w, b1);
+        Body& y = body_ref(w->w, b2);
+        begin_mutation(w->w);
+        HSpring sp;
+        sp.b1 = (int)b1 - 1; sp.b2 = (int)b2 - 1;
+        sp.seq = w->w.constraint_seq++;
+        sp.p1 = x.local_origin + D3(a1[0], a1[1], a1[2]);
+        sp.p2 = y.local_origin + D3(a2[0], a2[1], a2[2]);
+        // a negative resting length: the attachment points' distance now
+        if (rest < 0) rest = ((x.com + qrot(x.q, sp.p1)) - (y.com + qrot(y.q, sp.p2))).mag();
+        sp.damping = damping; sp.stiffness = stiffness; sp.rest = rest;
+        w->w.springs.push_back(sp);
+        if (out_id) *out_id = joint_id(w->w);
+        return CPGPU_OK;
+    });
 }
-int cpgpu_add_slider(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, const double*, const double*,
-                     double, double, uint32_t*) {
+int cpgpu_add_slider(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], const double ax1[3],
+                     const double ax2[3], double ps, double rs, uint32_t* out_id) {
     W_OR_FAIL(w);
-    return fail(CPGPU_ERR_UNSUPPORTED, "slider constraints are not implemented on the device path");
+    return guarded([&] {
+        add_joint(w->w, JK_SLIDER, 5, b1, b2, a1, a2, ax1, ax2, ps, rs);
+        if (out_id) *out_id = joint_id(w->w);
+        return CPGPU_OK;
+    });
 }
-int cpgpu_add_sliding_hinge(cpgpu_world* w, uint32_t, uint32_t, const double*, const double*, const double*,
-                            const double*, double, double, uint32_t*) {
+int cpgpu_add_sliding_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3],
+                            const double ax1[3], const double ax2[3], double ps, double rs, uint32_t* out_id) {
     W_OR_FAIL(w);
-    return fail(CPGPU_ERR_UNSUPPORTED, "sliding-hinge constraints are not implemented on the device path");
+    return guarded([&] {
+        add_joint(w->w, JK_SLIDING_HINGE, 4, b1, b2, a1, a2, ax1, ax2, ps, rs);
+        if (out_id) *out_id = joint_id(w->w);
+        return CPGPU_OK;
+    });
 }
 int cpgpu_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], const double ax1[3],
                     const double ax2[3], double ps, double rs, uint32_t* out_id) {
     W_OR_FAIL(w);
     return guarded([&] {
-        uint32_t id = add_joint(w->w, 5, b1, b2, a1, a2, ax1, ax2, ps, rs);
-        if (out_id) *out_id = id;
+        add_joint(w->w, JK_HINGE, 5, b1, b2, a1, a2, ax1, ax2, ps, rs);
+        if (out_id) *out_id = joint_id(w->w);
         return CPGPU_OK;
     });
 }
@@ -1862,8 +2125,34 @@ int cpgpu_step(cpgpu_world* w, int n_steps) {
         if (n_steps < 0) throw ApiFail{CPGPU_ERR_INVALID_ARG, "negative step count"};
         if (w->w.bodies.empty()) return CPGPU_OK;
         ensure_device(w->w);
+        w->w.dev->set_audit(w->w.audit);
         w->w.dev->step(n_steps);
         return w->w.dev->check_status();
+    });
+}
+
+int cpgpu_world_set_audit(cpgpu_world* w, int enabled) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        w->w.audit = enabled != 0;
+        if (w->w.dev && w->w.dev_valid) w->w.dev->set_audit(w->w.audit);
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_world_read_audit(cpgpu_world* w, double* out) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null output"};
+        if (!w->w.audit) throw ApiFail{CPGPU_ERR_INVALID_ARG, "the audit is not enabled"};
+        if (!(w->w.dev && w->w.dev_valid)) {
+            // not stepped since the audit was enabled (or since a rebuild)
+            for (int k = 0; k < kAuditValues; k++) out[k] = 0.0;
+            return CPGPU_OK;
+        }
+        w->w.dev->set_audit(true);
+        w->w.dev->read_audit(out);
+        return CPGPU_OK;
     });
 }
 
@@ -2026,7 +2315,7 @@ int cpgpu_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n) {
     });
 }
 
-int cpgpu_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv, int* n) {
+int cpgpu_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv, double* aux, int* n) {
     W_OR_FAIL(w);
     return guarded([&] {
         if (!n) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null count"};
@@ -2036,12 +2325,13 @@ int cpgpu_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv
             const HJoint& x = w->w.joints[j];
             for (int k = 0; k < kJMax; k++) if (impulse) impulse[kJMax * j + k] = x.impulse[k];
             for (int k = 0; k < 3; k++) { if (u) u[3 * j + k] = x.u[k]; if (wv) wv[3 * j + k] = x.w[k]; }
+            if (aux) { aux[2 * j] = x.angle; aux[2 * j + 1] = x.active; }
         }
         return CPGPU_OK;
     });
 }
 
-int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u, const double* wv, int n) {
+int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u, const double* wv, const double* aux, int n) {
     W_OR_FAIL(w);
     return guarded([&] {
         if (n != (int)w->w.joints.size()) throw ApiFail{CPGPU_ERR_INVALID_ARG, "joint count mismatch"};
@@ -2050,39 +2340,51 @@ int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
             HJoint& x = w->w.joints[j];
             for (int k = 0; k < kJMax; k++) if (impulse) x.impulse[k] = (float)impulse[kJMax * j + k];
             for (int k = 0; k < 3; k++) { if (u) x.u[k] = (float)u[3 * j + k]; if (wv) x.w[k] = (float)wv[3 * j + k]; }
+            if (aux) { x.angle = (float)aux[2 * j]; x.active = aux[2 * j + 1] != 0.0 ? 1 : 0; }
         }
         return CPGPU_OK;
     });
 }
 
-// Parts of a batch: worlds sorted by body count (largest first) and cut into
-// runs of about equal total bodies.  CPGPU_BATCH_PARTS sets the count (default
-// 1): parts pay off when one world's serial solve chain is longer than the rest
-// of the step (a few very large worlds among many small ones); when the step is
-// throughput-bound, concurrent parts only contend for the same SMs.
-// Worlds sorted by size and cut into parts, each stepped by its own graphs on
-// its own streams.  By default a large batch of very unequal worlds (at least
-// 512 worlds, the largest at least 4 times the median) gets two parts, the
-// largest worlds holding 20 % of the bodies and the rest: the long solver
-// chains of the largest worlds then overlap the other worlds' whole step
-// (measured on 4,096 worlds of 8-512 bodies: 23.7 -> 21.3 ms per step).
-// CPGPU_BATCH_PARTS and CPGPU_BATCH_FIRST_SHARE (percent of the bodies in the
-// first part) override it; CPGPU_PGS_REST_PER_SM sets the later parts' solver
-// chain workers per SM (default 2, 0 = as many as fit).
-static std::vector<std::vector<int>> batch_partition(const std::vector<World*>& ws) {
-    const int n = (int)ws.size();
-    std::vector<int> order(n);
-    for (int i = 0; i < n; i++) order[i] = i;
+// ---------------------------------------------------------------- batch schedule ----
+
+// The hand-set schedule: a large batch of very unequal worlds (at least 512
+// worlds, the largest at least 4 times the median) gets two parts, the
+// largest worlds holding 20 % of the bodies and the rest, the later part at
+// most 2 chain workers per SM (the parts' solver kernels share the SMs'
+// shared memory; measured on 4,096 worlds of 8-512 bodies: 23.7 -> 21.3 ms
+// per step with the parts, 21.5 -> 20.3 ms with the cap); otherwise one
+// part.  CPGPU_BATCH_PARTS, CPGPU_BATCH_FIRST_SHARE (percent) and
+// CPGPU_PGS_REST_PER_SM override it.
+static std::vector<int> size_order(const std::vector<World*>& ws) {
+    std::vector<int> order(ws.size());
+    for (size_t i = 0; i < ws.size(); i++) order[i] = (int)i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ws[a]->bodies.size() > ws[b]->bodies.size(); });
+    return order;
+}
+
+static Schedule default_schedule(const std::vector<World*>& ws) {
+    const int n = (int)ws.size();
+    const std::vector<int> order = size_order(ws);
     const bool skewed = n >= 512 && ws[order[0]]->bodies.size() >= 4 * ws[order[n / 2]]->bodies.size();
-    int P = env_int("CPGPU_BATCH_PARTS", skewed ? 2 : 1);
-    P = std::max(1, std::min(P, n));
+    Schedule S;
+    S.parts = std::max(1, std::min(env_int("CPGPU_BATCH_PARTS", skewed ? 2 : 1), n));
+    const int first_dflt = (skewed && S.parts == 2) ? 20 : 100 / S.parts;
+    S.first_share = S.parts > 1 ? std::max(1, std::min(99, env_int("CPGPU_BATCH_FIRST_SHARE", first_dflt))) : 100;
+    S.rest_per_sm = S.parts > 1 ? env_int("CPGPU_PGS_REST_PER_SM", 2) : 0;
+    return S;
+}
+
+// Worlds sorted by body count (largest first) and cut into S.parts runs:
+// the first holds S.first_share percent of the bodies, the others split the
+// rest evenly.
+static std::vector<std::vector<int>> batch_partition(const std::vector<World*>& ws, const Schedule& S) {
+    const int n = (int)ws.size();
+    const std::vector<int> order = size_order(ws);
+    const int P = std::max(1, std::min(S.parts, n));
     int64_t total = 0;
     for (World* w : ws) total += (int64_t)w->bodies.size();
-    // part 0 (the largest worlds) holds `first` percent of the bodies, the
-    // other parts split the rest evenly
-    const int first_dflt = (skewed && P == 2) ? 20 : 100 / P;
-    const int first = P > 1 ? std::max(1, std::min(99, env_int("CPGPU_BATCH_FIRST_SHARE", first_dflt))) : 100;
+    const int first = S.first_share;
     auto bound = [&](int q) { return P > 1 ? total * (first * (P - 1) + (100 - first) * q) / (100 * (P - 1)) : total; };
     std::vector<std::vector<int>> parts(P);
     int64_t acc = 0;
@@ -2099,54 +2401,223 @@ static std::vector<std::vector<int>> batch_partition(const std::vector<World*>& 
     return parts;
 }
 
+// Autotuner cache: schedules chosen by timing, keyed on the batch's
+// world-size histogram (log2 bins of the body counts, each bin's share of
+// the worlds in sixteenths, and log2 of the world count), kept for the
+// process and, when CPGPU_TUNE_FILE names one, in that file.
+static std::string histogram_key(const std::vector<World*>& ws) {
+    int bins[24] = {0};
+    for (World* w : ws) {
+        int b = 0;
+        for (size_t x = w->bodies.size(); x > 1 && b < 23; x >>= 1) b++;
+        bins[b]++;
+    }
+    int lw = 0;
+    for (size_t x = ws.size(); x > 1; x >>= 1) lw++;
+    std::string key = "w" + std::to_string(lw) + ":";
+    for (int b = 0; b < 24; b++) {
+        const int q = (int)((16LL * bins[b] + (int64_t)ws.size() / 2) / (int64_t)ws.size());
+        key += std::to_string(q) + (b + 1 < 24 ? "," : "");
+    }
+    return key;
+}
+
+static std::mutex g_tune_mutex;
+static std::map<std::string, Schedule> g_tuned;
+static bool g_tune_file_loaded = false;
+
+static void tune_file_load() {
+    if (g_tune_file_loaded) return;
+    g_tune_file_loaded = true;
+    const char* path = std::getenv("CPGPU_TUNE_FILE");
+    if (!path) return;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return;
+    char key[256];
+    Schedule S;
+    while (std::fscanf(f, "%255s %d %d %d %d", key, &S.parts, &S.first_share, &S.rest_per_sm, &S.big_rows) == 5) g_tuned[key] = S;
+    std::fclose(f);
+}
+
+static void tune_file_save(const std::string& key, const Schedule& S) {
+    const char* path = std::getenv("CPGPU_TUNE_FILE");
+    if (!path) return;
+    FILE* f = std::fopen(path, "a");
+    if (!f) return;
+    std::fprintf(f, "%s %d %d %d %d\n", key.c_str(), S.parts, S.first_share, S.rest_per_sm, S.big_rows);
+    std::fclose(f);
+}
+
+// The batch object: parts built for a schedule
+static std::unique_ptr<cpgpu_batch> make_batch(const std::vector<World*>& ws, const Schedule& S) {
+    const int n = (int)ws.size();
+    auto b = std::make_unique<cpgpu_batch>();
+    b->sched = S;
+    b->part_of.resize(n);
+    b->local_of.resize(n);
+    b->row0.resize(n);
+    for (int i = 0; i < n; i++) {
+        b->row0[i] = (int)b->n_bodies;
+        b->n_bodies += (int64_t)ws[i]->bodies.size();
+    }
+    const auto parts = batch_partition(ws, S);
+    b->sched.parts = (int)parts.size();
+    for (size_t p = 0; p < parts.size(); p++) {
+        std::vector<World*> sub;
+        std::vector<int> rows;
+        for (size_t k = 0; k < parts[p].size(); k++) {
+            const int wi = parts[p][k];
+            b->part_of[wi] = (int)p;
+            b->local_of[wi] = (int)k;
+            sub.push_back(ws[wi]);
+            for (size_t j = 0; j < ws[wi]->bodies.size(); j++) rows.push_back(b->row0[wi] + (int)j);
+        }
+        // the parts' solver-chain kernels run at the same time and share the
+        // SMs' shared memory: the later parts take at most rest_per_sm chain
+        // workers per SM so that the first part's longest chains are not
+        // queued behind them
+        b->parts.push_back(build_batch(sub, p == 0 ? 0 : (parts.size() > 1 ? S.rest_per_sm : 0)));
+        if (S.big_rows != kDefaultBigRows) b->parts.back()->set_schedule(b->parts.back()->pgs_per_sm, S.big_rows);
+        int* d_rows = nullptr;
+        CK(cudaMalloc(&d_rows, sizeof(int) * std::max<size_t>(rows.size(), 1)));
+        CK(cudaMemcpy(d_rows, rows.data(), sizeof(int) * rows.size(), cudaMemcpyHostToDevice));
+        b->rows.push_back(d_rows);
+    }
+    CK(cudaMalloc(&b->stage, sizeof(float4) * 4 * std::max<int64_t>(b->n_bodies, 1)));
+    CK(cudaEventCreate(&b->ev0));
+    CK(cudaEventCreate(&b->ev1));
+    CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->done.resize(b->parts.size());
+    for (auto& e : b->done) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return b;
+}
+
+static std::vector<World*> batch_worlds(cpgpu_world* const* worlds, int n) {
+    if (!worlds || n <= 0) throw ApiFail{CPGPU_ERR_INVALID_ARG, "empty batch"};
+    std::vector<World*> ws;
+    for (int i = 0; i < n; i++) {
+        if (!worlds[i]) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null world"};
+        if (worlds[i]->w.dev && worlds[i]->w.dev_valid) download_state(worlds[i]->w);
+        ws.push_back(&worlds[i]->w);
+    }
+    return ws;
+}
+
 int cpgpu_batch_create(cpgpu_world* const* worlds, int n, cpgpu_batch** out) {
     return guarded([&] {
-        if (!worlds || n <= 0 || !out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "empty batch"};
-        std::vector<World*> ws;
-        for (int i = 0; i < n; i++) {
-            if (!worlds[i]) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null world"};
-            if (worlds[i]->w.dev && worlds[i]->w.dev_valid) download_state(worlds[i]->w);
-            ws.push_back(&worlds[i]->w);
+        if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null output"};
+        const std::vector<World*> ws = batch_worlds(worlds, n);
+        Schedule S = default_schedule(ws);
+        bool tuned = false;
+        // a schedule set through the environment takes precedence over the cache
+        const bool env_set = std::getenv("CPGPU_BATCH_PARTS") || std::getenv("CPGPU_BATCH_FIRST_SHARE") ||
+                             std::getenv("CPGPU_PGS_REST_PER_SM");
+        if (!env_set) {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            tune_file_load();
+            auto it = g_tuned.find(histogram_key(ws));
+            if (it != g_tuned.end()) { S = it->second; tuned = true; }
         }
-        auto b = std::make_unique<cpgpu_batch>();
-        b->part_of.resize(n);
-        b->local_of.resize(n);
-        b->row0.resize(n);
-        for (int i = 0; i < n; i++) {
-            b->row0[i] = (int)b->n_bodies;
-            b->n_bodies += (int64_t)ws[i]->bodies.size();
-        }
-        const auto parts = batch_partition(ws);
-        for (size_t p = 0; p < parts.size(); p++) {
-            std::vector<World*> sub;
-            std::vector<int> rows;
-            for (size_t k = 0; k < parts[p].size(); k++) {
-                const int wi = parts[p][k];
-                b->part_of[wi] = (int)p;
-                b->local_of[wi] = (int)k;
-                sub.push_back(ws[wi]);
-                for (size_t j = 0; j < ws[wi]->bodies.size(); j++) rows.push_back(b->row0[wi] + (int)j);
-            }
-            // the parts' solver-chain kernels run at the same time and share
-            // the SMs' shared memory: the later parts take at most 2 chain
-            // workers per SM so that the first part's longest chains are not
-            // queued behind them (4,096 worlds: 21.5 -> 20.3 ms per step)
-            const int rest_per_sm = parts.size() > 1 ? env_int("CPGPU_PGS_REST_PER_SM", 2) : 0;
-            b->parts.push_back(build_batch(sub, p == 0 ? 0 : rest_per_sm));
-            int* d_rows = nullptr;
-            CK(cudaMalloc(&d_rows, sizeof(int) * std::max<size_t>(rows.size(), 1)));
-            CK(cudaMemcpy(d_rows, rows.data(), sizeof(int) * rows.size(), cudaMemcpyHostToDevice));
-            b->rows.push_back(d_rows);
-        }
-        CK(cudaMalloc(&b->stage, sizeof(float4) * 4 * std::max<int64_t>(b->n_bodies, 1)));
-        CK(cudaEventCreate(&b->ev0));
-        CK(cudaEventCreate(&b->ev1));
-        CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
-        b->done.resize(b->parts.size());
-        for (auto& e : b->done) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        auto b = make_batch(ws, S);
+        b->tuned = tuned;
         *out = b.release();
         return CPGPU_OK;
     });
+}
+
+// Device time of n steps of every part (graph launches, the parts
+// concurrent), the parts' streams joined before and after
+static double time_steps(cpgpu_batch* b, int n) {
+    CK(cudaEventRecord(b->ev0, b->st0()));
+    b->fan_out();
+    for (auto& p : b->parts) p->step(n);
+    b->fan_in();
+    CK(cudaEventRecord(b->ev1, b->st0()));
+    CK(cudaEventSynchronize(b->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    for (auto& p : b->parts) p->check_status();
+    return ms;
+}
+
+// Autotuned batch: candidate schedules (one, two or three parts with
+// several first-part shares; for each, the later parts' chain workers per SM
+// and the big-island threshold) are built and timed on trial steps from the
+// worlds' current state, each trial's state restored afterwards, and the
+// fastest kept (restored to the starting state).  The choice is cached for
+// the world-size histogram, so later batches with the same histogram start
+// with it.
+int cpgpu_batch_create_tuned(cpgpu_world* const* worlds, int n, int trial_steps, cpgpu_batch** out) {
+    return guarded([&] {
+        if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null output"};
+        const std::vector<World*> ws = batch_worlds(worlds, n);
+        const int T = std::max(1, trial_steps);
+        const Schedule dflt = default_schedule(ws);
+        std::vector<Schedule> layouts{dflt};
+        auto add = [&](int parts, int share) {
+            if (parts > (int)ws.size()) return;
+            for (const Schedule& x : layouts) if (x.parts == parts && (parts == 1 || x.first_share == share)) return;
+            Schedule s;
+            s.parts = parts; s.first_share = parts > 1 ? share : 100;
+            layouts.push_back(s);
+        };
+        add(1, 100);
+        for (int share : {10, 20, 30}) add(2, share);
+        add(3, 20);
+        std::unique_ptr<cpgpu_batch> best;
+        double best_ms = 1e300, dflt_ms = -1;
+        for (const Schedule& L : layouts) {
+            std::unique_ptr<cpgpu_batch> cand = make_batch(ws, L);
+            for (auto& p : cand->parts) p->snapshot();
+            const std::vector<int> per_sms = cand->parts.size() > 1 ? std::vector<int>{1, 2, 3} : std::vector<int>{0};
+            Schedule cbest = cand->sched;
+            double cbest_ms = 1e300;
+            for (int per_sm : per_sms)
+                for (int big : {32, 48, 96}) {
+                    for (size_t p = 0; p < cand->parts.size(); p++) cand->parts[p]->set_schedule(p == 0 ? 0 : per_sm, big);
+                    time_steps(cand.get(), 1);   // warm-up
+                    const double ms = time_steps(cand.get(), T) / T;
+                    for (auto& p : cand->parts) p->restore(false);
+                    const bool is_dflt = L.parts == dflt.parts && L.first_share == dflt.first_share &&
+                                         big == dflt.big_rows && (cand->parts.size() == 1 || per_sm == dflt.rest_per_sm);
+                    if (is_dflt) dflt_ms = ms;
+                    if (ms < cbest_ms) {
+                        cbest_ms = ms;
+                        cbest.rest_per_sm = cand->parts.size() > 1 ? per_sm : 0;
+                        cbest.big_rows = big;
+                    }
+                }
+            if (cbest_ms < best_ms) {
+                for (size_t p = 0; p < cand->parts.size(); p++)
+                    cand->parts[p]->set_schedule(p == 0 ? 0 : cbest.rest_per_sm, cbest.big_rows);
+                for (auto& p : cand->parts) p->restore(true);
+                cand->sched = cbest;
+                best_ms = cbest_ms;
+                best = std::move(cand);
+            }
+        }
+        best->tuned = true;
+        best->tuned_ms = best_ms;
+        best->default_ms = dflt_ms;
+        {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            const std::string key = histogram_key(ws);
+            g_tuned[key] = best->sched;
+            tune_file_save(key, best->sched);
+        }
+        *out = best.release();
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_batch_schedule(cpgpu_batch* b, int* sched, double* times) {
+    if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
+    if (sched) {
+        sched[0] = b->sched.parts; sched[1] = b->sched.first_share; sched[2] = b->sched.rest_per_sm;
+        sched[3] = b->sched.big_rows; sched[4] = b->tuned ? 1 : 0;
+    }
+    if (times) { times[0] = b->tuned_ms; times[1] = b->default_ms; }
+    return CPGPU_OK;
 }
 int cpgpu_batch_destroy(cpgpu_batch* b) { delete b; return CPGPU_OK; }
 
@@ -2162,6 +2633,30 @@ int cpgpu_batch_step(cpgpu_batch* b, int n) {
         return batch_check(b);
     });
 }
+int cpgpu_batch_set_audit(cpgpu_batch* b, int enabled) {
+    if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
+    return guarded([&] {
+        for (auto& p : b->parts) p->set_audit(enabled != 0);
+        return CPGPU_OK;
+    });
+}
+
+int cpgpu_batch_read_audit(cpgpu_batch* b, double* out) {
+    if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
+    return guarded([&] {
+        if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null output"};
+        std::vector<std::vector<double>> per(b->parts.size());
+        for (size_t p = 0; p < b->parts.size(); p++) {
+            per[p].resize((size_t)kAuditValues * b->parts[p]->n_worlds);
+            b->parts[p]->read_audit(per[p].data());
+        }
+        for (size_t wi = 0; wi < b->part_of.size(); wi++)
+            for (int k = 0; k < kAuditValues; k++)
+                out[kAuditValues * wi + k] = per[b->part_of[wi]][(size_t)kAuditValues * b->local_of[wi] + k];
+        return CPGPU_OK;
+    });
+}
+
 int cpgpu_batch_get_body_state(cpgpu_batch* b, int wi, double* com, double* quat, double* vel, double* ang) {
     if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
     return guarded([&] {
@@ -2248,34 +2743,59 @@ int cpgpu_batch_write_state(cpgpu_batch* b, const float* in) {
 
 // Stage times of n steps, part by part (each part's stages timed alone and
 // summed over the parts: the work of each stage, not the overlapped step)
+// Stage times of n steps launched stage by stage (no graph) with the parts
+// running concurrently, one step at a time (every part's stream waits for
+// the previous step of all parts): CUDA events on each part's stream mark its
+// stages, every mark is timed against one start event, and a stage's time in
+// a step is its window over the parts, from the first part entering it to the
+// last part leaving it.  The windows lie inside the step, so a stage's time
+// never exceeds the step's.
 int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* counts) {
     if (!b || !stage_ms) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
     return guarded([&] {
         for (int k = 0; k < CPGPU_N_STAGES; k++) stage_ms[k] = 0;
         if (counts) counts[0] = counts[1] = counts[2] = 0;
-        for (auto& part : b->parts) {
-            Batch& B = *part;
-            const int n_marks = 7 + 3 * B.substeps;
-            std::vector<cudaEvent_t> ev(n_marks);
-            for (auto& e : ev) CK(cudaEventCreate(&e));
-            B.marks = &ev;
-            for (int i = 0; i < n_steps; i++) {
+        const size_t np = b->parts.size();
+        std::vector<std::vector<cudaEvent_t>> ev(np);
+        for (size_t p = 0; p < np; p++) {
+            ev[p].resize(7 + 3 * b->parts[p]->substeps);
+            for (auto& e : ev[p]) CK(cudaEventCreate(&e));
+        }
+        for (int i = 0; i < n_steps; i++) {
+            CK(cudaEventRecord(b->ev0, b->st0()));
+            b->fan_out();
+            for (size_t p = 0; p < np; p++) {
+                Batch& B = *b->parts[p];
+                B.marks = &ev[p];
                 B.launch_step(B.d[B.parity]);
+                B.marks = nullptr;
                 CK(cudaGetLastError());   // a launch refused here would leave its stage untimed
                 B.parity ^= 1;
-                CK(cudaEventSynchronize(ev[n_marks - 1]));
-                auto span = [&](int a, int c) { float ms = 0; CK(cudaEventElapsedTime(&ms, ev[a], ev[c])); return (double)ms; };
-                for (int k = 0; k < 5; k++) stage_ms[k] += span(k, k + 1);
-                for (int s = 0; s < B.substeps; s++) {
-                    stage_ms[5] += span(5 + 3 * s, 6 + 3 * s);
-                    stage_ms[6] += span(6 + 3 * s, 7 + 3 * s);
-                    stage_ms[7] += span(7 + 3 * s, 8 + 3 * s);
-                }
-                stage_ms[8] += span(5 + 3 * B.substeps, 6 + 3 * B.substeps);
             }
-            B.marks = nullptr;
-            for (auto& e : ev) cudaEventDestroy(e);
-            if (counts) {
+            b->fan_in();
+            CK(cudaEventRecord(b->ev1, b->st0()));
+            CK(cudaEventSynchronize(b->ev1));
+            auto at = [&](size_t p, int m) { float ms = 0; CK(cudaEventElapsedTime(&ms, b->ev0, ev[p][m])); return (double)ms; };
+            auto window = [&](auto first_mark, auto last_mark) {
+                double lo = 1e300, hi = -1e300;
+                for (size_t p = 0; p < np; p++) { lo = std::min(lo, at(p, first_mark(p))); hi = std::max(hi, at(p, last_mark(p))); }
+                return hi > lo ? hi - lo : 0.0;
+            };
+            for (int k = 0; k < 5; k++) stage_ms[k] += window([&](size_t) { return k; }, [&](size_t) { return k + 1; });
+            // per-substep stages: the parts share the substep count
+            const int S = b->parts[0]->substeps;
+            for (int s2 = 0; s2 < S; s2++) {
+                stage_ms[5] += window([&](size_t) { return 5 + 3 * s2; }, [&](size_t) { return 6 + 3 * s2; });
+                stage_ms[6] += window([&](size_t) { return 6 + 3 * s2; }, [&](size_t) { return 7 + 3 * s2; });
+                stage_ms[7] += window([&](size_t) { return 7 + 3 * s2; }, [&](size_t) { return 8 + 3 * s2; });
+            }
+            stage_ms[8] += window([&](size_t) { return 5 + 3 * S; }, [&](size_t) { return 6 + 3 * S; });
+        }
+        for (auto& v : ev)
+            for (auto& e : v) cudaEventDestroy(e);
+        if (counts)
+            for (auto& part : b->parts) {
+                Batch& B = *part;
                 int c[6];
                 CK(cudaMemcpyAsync(c, B.cur().n_pairs, sizeof(c), cudaMemcpyDeviceToHost, B.st));
                 CK(cudaStreamSynchronize(B.st));
@@ -2283,9 +2803,7 @@ int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* 
                 counts[1] += c[3 + B.parity];
                 counts[2] += c[5];
             }
-            B.check_status();
-        }
-        return CPGPU_OK;
+        return batch_check(b);
     });
 }
 
@@ -2340,26 +2858,48 @@ struct ServerRequest {
     bool finished = false;   // result captured; still in the batch until the next re-form
 };
 
-// One lane of the server: the requests of one world-size class, stepped as a
-// batch on the lane's own stream.
-struct ServerLane {
-    std::deque<ServerRequest> waiting;
+// A cohort: requests admitted together, stepped as one batch on the batch's
+// own stream.  A cohort never takes in running worlds: requests that arrive
+// later form new cohorts, which step beside it; a finished request's state is
+// read back in place while its cohort keeps going; a cohort is freed when its
+// last request finishes.
+struct Cohort {
     std::vector<ServerRequest> running;   // in batch order
     std::unique_ptr<Batch> batch;
-    int since_reform = 0;
     int inflight = 0;                     // steps launched and not yet accounted
+    int stepped = 0;                      // steps completed since it was built
     cudaEvent_t ev = nullptr;             // recorded after the in-flight steps
-    ~ServerLane() { if (ev) cudaEventDestroy(ev); }
+    ~Cohort() { if (ev) cudaEventDestroy(ev); }
+    int64_t live_bodies() const {
+        int64_t n = 0;
+        for (const auto& r : running) if (!r.finished) n += r.bodies;
+        return n;
+    }
+    int64_t all_bodies() const {
+        int64_t n = 0;
+        for (const auto& r : running) n += r.bodies;
+        return n;
+    }
+};
+
+// One lane of the server: the requests of one world-size class
+struct ServerLane {
+    std::deque<ServerRequest> waiting;
+    std::vector<std::unique_ptr<Cohort>> cohorts;   // oldest first
 };
 
 // Requests are worlds with a step count.  They are sorted by size into lanes
 // (fewer than 128 dynamic bodies, fewer than 512, the rest): a step of a batch
 // lasts as long as its largest island's serial solve, so a small world batched
-// with large ones would advance at the large ones' pace.  Each lane steps on
-// its own stream in chunks: advance() launches the next chunk on every idle
-// lane and returns once one lane's chunk has completed, so small requests take
-// more steps per second than large ones.  Admission is in arrival order per
-// lane under one device-memory budget for all lanes.
+// with large ones would advance at the large ones' pace.  Within a lane,
+// waiting requests are admitted in arrival order under one device-memory
+// budget for all lanes, at most once per `epoch_steps` steps of the lane's
+// newest cohort, as a new cohort (a batch built from the new worlds only);
+// running worlds are never copied to admit new ones.  A cohort whose finished
+// requests hold three quarters of its bodies is compacted into the next new
+// cohort of its lane (its live worlds read back and packed with the new
+// ones).  Every cohort steps on its own stream in chunks: advance() launches
+// the next chunk on every idle cohort and returns once one has completed.
 struct Server {
     int64_t budget = 0;
     int epoch_steps = 10;
@@ -2384,12 +2924,15 @@ struct Server {
     size_t used_bytes() const {
         size_t u = 0;
         for (auto& L : lanes)
-            for (auto& r : L->running) u += r.bytes;
+            for (auto& c : L->cohorts)
+                for (auto& r : c->running) u += r.bytes;
         return u;
     }
     int64_t running_count() const {
         int64_t n = 0;
-        for (auto& L : lanes) n += (int64_t)L->running.size();
+        for (auto& L : lanes)
+            for (auto& c : L->cohorts)
+                for (auto& r : c->running) n += !r.finished;
         return n;
     }
     int64_t waiting_count() const {
@@ -2397,114 +2940,141 @@ struct Server {
         for (auto& L : lanes) n += (int64_t)L->waiting.size();
         return n;
     }
+    int64_t device_bytes() const {
+        int64_t n = 0;
+        for (auto& L : lanes)
+            for (auto& c : L->cohorts) n += c->batch ? (int64_t)c->batch->bytes : 0;
+        return n;
+    }
+    int64_t running_bodies() const {
+        int64_t n = 0;
+        for (auto& L : lanes)
+            for (auto& c : L->cohorts) n += c->live_bodies();
+        return n;
+    }
 
     void submit(const ServerRequest& r) { lanes[lane_of(r.bodies)]->waiting.push_back(r); }
 
     // capture the exact state of requests that reached their step count,
-    // without stopping the batch (they keep stepping as dead weight until the
-    // next re-form)
-    void capture_finished(ServerLane& L) {
+    // without stopping the cohort (they keep stepping as dead weight until the
+    // cohort ends or is compacted)
+    void capture_finished(Cohort& C) {
         std::vector<int> idx;
         std::vector<World*> ws;
-        for (size_t i = 0; i < L.running.size(); i++)
-            if (!L.running[i].finished && L.running[i].remaining <= 0) { idx.push_back((int)i); ws.push_back(L.running[i].w); }
+        for (size_t i = 0; i < C.running.size(); i++)
+            if (!C.running[i].finished && C.running[i].remaining <= 0) { idx.push_back((int)i); ws.push_back(C.running[i].w); }
         if (idx.empty()) return;
-        download_subset(*L.batch, idx, ws);
-        for (int i : idx) { L.running[i].finished = true; done.push_back(L.running[i].token); }
+        download_subset(*C.batch, idx, ws);
+        for (int i : idx) { C.running[i].finished = true; done.push_back(C.running[i].token); }
     }
 
-    void reform(ServerLane& L) {
+    // a new cohort for the lane: the live requests of its sparse cohorts
+    // (read back) and the waiting requests that fit the budget
+    void admit(ServerLane& L) {
         auto t0 = std::chrono::steady_clock::now();
-        std::vector<ServerRequest> keep;
-        std::vector<int> idx;
-        std::vector<World*> ws;
-        for (size_t i = 0; i < L.running.size(); i++)
-            if (!L.running[i].finished) { keep.push_back(L.running[i]); idx.push_back((int)i); ws.push_back(L.running[i].w); }
-        if (L.batch) download_subset(*L.batch, idx, ws);
-        L.batch.reset();
-        L.running.swap(keep);
+        std::vector<ServerRequest> take;
+        for (auto it = L.cohorts.begin(); it != L.cohorts.end();) {
+            Cohort& C = **it;
+            const int64_t live = C.live_bodies(), all = C.all_bodies();
+            if (C.inflight == 0 && live > 0 && 4 * (all - live) >= 3 * all) {
+                std::vector<int> idx;
+                std::vector<World*> ws;
+                for (size_t i = 0; i < C.running.size(); i++)
+                    if (!C.running[i].finished) { idx.push_back((int)i); ws.push_back(C.running[i].w); take.push_back(C.running[i]); }
+                download_subset(*C.batch, idx, ws);
+                it = L.cohorts.erase(it);
+            } else {
+                ++it;
+            }
+        }
         size_t used = used_bytes();
+        for (auto& r : take) used += r.bytes;
         while (!L.waiting.empty()) {
             ServerRequest& r = L.waiting.front();
             r.bytes = estimate(*r.w);
-            if (running_count() > 0 && used + r.bytes > (size_t)budget) break;
+            if ((running_count() > 0 || !take.empty()) && used + r.bytes > (size_t)budget) break;
             used += r.bytes;
-            L.running.push_back(r);
+            take.push_back(r);
             L.waiting.pop_front();
         }
-        if (!L.running.empty()) {
-            std::vector<World*> ws2;
-            for (auto& r : L.running) ws2.push_back(r.w);
-            L.batch = build_batch(ws2);
+        if (!take.empty()) {
+            auto C = std::make_unique<Cohort>();
+            C->running = std::move(take);
+            std::vector<World*> ws;
+            for (auto& r : C->running) ws.push_back(r.w);
+            C->batch = build_batch(ws);
             int64_t nb = 0;
-            for (auto& r : L.running) nb += r.bodies;
-            if (nb > 0) bytes_per_body = (double)L.batch->bytes / (double)nb;
-            for (auto& r : L.running) r.bytes = estimate(*r.w);
-            if (!L.ev) CK(cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming));
+            for (auto& r : C->running) nb += r.bodies;
+            if (nb > 0) bytes_per_body = (double)C->batch->bytes / (double)nb;
+            for (auto& r : C->running) r.bytes = estimate(*r.w);
+            CK(cudaEventCreateWithFlags(&C->ev, cudaEventDisableTiming));
+            L.cohorts.push_back(std::move(C));
+            reforms++;
         }
-        L.since_reform = 0;
-        reforms++;
         reform_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
 
-    // account for a lane's completed chunk
-    void complete(ServerLane& L) {
-        if (L.inflight == 0) return;
-        L.batch->check_status();
-        for (auto& r : L.running) {
+    // account for a cohort's completed chunk; a cohort with no live request
+    // left is freed
+    void complete(Cohort& C) {
+        if (C.inflight == 0) return;
+        C.batch->check_status();
+        for (auto& r : C.running) {
             if (r.finished) continue;
-            r.remaining -= L.inflight;
-            body_steps += (int64_t)L.inflight * r.bodies;
+            r.remaining -= C.inflight;
+            body_steps += (int64_t)C.inflight * r.bodies;
         }
-        L.since_reform += L.inflight;
-        L.inflight = 0;
-        capture_finished(L);
+        C.stepped += C.inflight;
+        C.inflight = 0;
+        capture_finished(C);
     }
 
-    // Launch a lane's next chunk (no wait).  Re-form when requests wait and an
-    // epoch has passed since the last re-form, or when finished requests hold
-    // a quarter of the lane's bodies.  A chunk never passes a running
-    // request's remaining count or the end of the epoch.
-    bool launch(ServerLane& L, int max_steps) {
-        int64_t live = 0, dead = 0;
-        for (auto& r : L.running) (r.finished ? dead : live) += r.bodies;
-        const bool want = !L.waiting.empty() && (live == 0 || L.since_reform >= epoch_steps);
-        const bool reclaim = dead > 0 && (live == 0 || 4 * dead >= live + dead);
-        if (want || reclaim) reform(L);
-        if (!L.batch) return false;
-        live = 0;
-        for (auto& r : L.running) if (!r.finished) live += r.bodies;
-        if (live == 0) return false;
+    void launch(Cohort& C, int max_steps) {
         int n = max_steps;
-        for (auto& r : L.running) if (!r.finished) n = std::min(n, r.remaining);
-        if (!L.waiting.empty()) n = std::min(n, std::max(1, epoch_steps - L.since_reform));
-        if (n <= 0) { capture_finished(L); return false; }
-        L.batch->step(n);
-        CK(cudaEventRecord(L.ev, L.batch->st));
-        L.inflight = n;
-        return true;
+        bool live = false;
+        for (auto& r : C.running) if (!r.finished) { n = std::min(n, r.remaining); live = true; }
+        if (!live) return;
+        if (n <= 0) { capture_finished(C); return; }
+        C.batch->step(n);
+        CK(cudaEventRecord(C.ev, C.batch->st));
+        C.inflight = n;
     }
 
-    // Launch on every idle lane, then wait (bounded) until one lane's chunk
-    // completes and account for it.  Returns the steps that lane completed.
+    // Admit where due, launch on every idle cohort, then wait (bounded) until
+    // one cohort's chunk completes and account for it.  Returns the steps that
+    // cohort completed.
     int advance(int max_steps) {
-        for (auto& L : lanes)
-            if (L->inflight == 0) launch(*L, max_steps);
+        for (auto& L : lanes) {
+            // drop finished cohorts
+            L->cohorts.erase(std::remove_if(L->cohorts.begin(), L->cohorts.end(),
+                                            [](const std::unique_ptr<Cohort>& c) { return c->inflight == 0 && c->live_bodies() == 0; }),
+                             L->cohorts.end());
+            const bool due = L->cohorts.empty() || L->cohorts.back()->stepped + L->cohorts.back()->inflight >= epoch_steps;
+            if (!L->waiting.empty() && due) admit(*L);
+            for (auto& c : L->cohorts)
+                if (c->inflight == 0) {
+                    int n = max_steps;
+                    // the newest cohort stops at the epoch so that the next admission is not delayed
+                    if (!L->waiting.empty() && c.get() == L->cohorts.back().get()) n = std::min(n, std::max(1, epoch_steps - c->stepped));
+                    launch(*c, n);
+                }
+        }
         const auto t0 = std::chrono::steady_clock::now();
         while (true) {
             int stepped = 0;
             bool any = false;
-            for (auto& L : lanes) {
-                if (L->inflight == 0) continue;
-                any = true;
-                const cudaError_t q = cudaEventQuery(L->ev);
-                if (q == cudaSuccess) {
-                    stepped = std::max(stepped, L->inflight);
-                    complete(*L);
-                } else if (q != cudaErrorNotReady) {
-                    CK(q);
+            for (auto& L : lanes)
+                for (auto& c : L->cohorts) {
+                    if (c->inflight == 0) continue;
+                    any = true;
+                    const cudaError_t q = cudaEventQuery(c->ev);
+                    if (q == cudaSuccess) {
+                        stepped = std::max(stepped, c->inflight);
+                        complete(*c);
+                    } else if (q != cudaErrorNotReady) {
+                        CK(q);
+                    }
                 }
-            }
             if (!any || stepped > 0) return stepped;
             if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(600))
                 throw ApiFail{CPGPU_ERR_TIMEOUT, "server chunk did not complete within 600 s"};
@@ -2512,10 +3082,11 @@ struct Server {
         }
     }
 
-    // wait for every lane's chunk in flight
+    // wait for every chunk in flight
     void drain() {
         for (auto& L : lanes)
-            if (L->inflight) { CK(cudaEventSynchronize(L->ev)); complete(*L); }
+            for (auto& c : L->cohorts)
+                if (c->inflight) { CK(cudaEventSynchronize(c->ev)); complete(*c); }
     }
 };
 
@@ -2590,13 +3161,8 @@ int cpgpu_server_stats(cpgpu_server* s, int64_t* body_steps, int64_t* reforms, d
     if (body_steps) *body_steps = s->s.body_steps;
     if (reforms) *reforms = s->s.reforms;
     if (reform_ms) *reform_ms = s->s.reform_ms;
-    int64_t bytes = 0, nb = 0;
-    for (auto& L : s->s.lanes) {
-        if (L->batch) bytes += (int64_t)L->batch->bytes;
-        for (auto& r : L->running) nb += r.bodies;
-    }
-    if (device_bytes) *device_bytes = bytes;
-    if (running_bodies) *running_bodies = nb;
+    if (device_bytes) *device_bytes = s->s.device_bytes();
+    if (running_bodies) *running_bodies = s->s.running_bodies();
     return CPGPU_OK;
 }
 

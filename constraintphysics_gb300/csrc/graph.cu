@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
     const int c1 = (e1 < ne) ? d.e_new.cstart[e1] : ncon;
     // joint edges and joints of this world (row slots of the world start after
     // the joints of the worlds before it)
-    const bool joints = d.n_joints > 0;
+    const bool joints = d.n_joint_edges > 0;
     const int je0 = joints ? d.je.world_start[w] : 0, je1 = joints ? d.je.world_start[w + 1] : 0;
     const int jj0 = joints ? d.je.world_jstart[w] : 0;
     const int sys0 = joints ? d.hs_world_start[w] : 0;
@@ -347,8 +347,17 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
                             for (int q = ss; q < sc; q++) seen |= d.isl_sys[q] == sy;
                             if (!seen) d.isl_sys[sc++] = sy;
                         }
-                        for (int q = d.je.jstart[je]; q < d.je.jstart[je] + d.je.jcount[je]; q++) d.row_contact[rc++] = -(q + 1);
-                        has_joint = true;
+                        // the edge's joints in creation order; a cone or
+                        // twist limit only while its last rebuild found the
+                        // limit reached (ConeRotationLimit::addSolverConstraints,
+                        // PersistentConstraint.h:165, 205); a spring-only
+                        // edge emits no rows
+                        for (int q = d.je.jstart[je]; q < d.je.jstart[je] + d.je.jcount[je]; q++) {
+                            const int jj = d.je.jlist[q];
+                            if (jk_limit(d.jt.kind[jj]) && !d.jt.active[jj]) continue;
+                            d.row_contact[rc++] = -(jj + 1);
+                            has_joint = true;
+                        }
                     } else {
                         // the edge's live contacts take the next rows (written below)
                         const int nl = live[k];
@@ -420,7 +429,7 @@ __global__ void k_island_copy(Dev d) {
             d.g_isl_body_start[o + k] = d.isl_body_start[s + k];
             d.g_isl_body_count[o + k] = d.isl_body_count[s + k];
             d.g_isl_world[o + k] = d.isl_world[s + k];
-            if (d.n_joints > 0) {
+            if (d.n_joint_edges > 0) {
                 d.g_isl_flags[o + k] = d.isl_flags[s + k];
                 d.g_isl_sys_start[o + k] = d.isl_sys_start[s + k];
                 d.g_isl_sys_count[o + k] = d.isl_sys_count[s + k];

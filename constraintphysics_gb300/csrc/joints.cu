@@ -1,4 +1,5 @@
-// joints.cu — joint rows (ball-socket, hinge) and the factorisation of the
+// joints.cu — joint rows (ball-socket, hinge, distance, weld, slider, sliding
+// hinge, cone and twist limits), springs, and the factorisation of the
 // holonomic systems on the device.
 //
 // Rows (BallSocket / Hinge ::updateSolverConstraints, PersistentConstraint.cpp:
@@ -83,82 +84,273 @@ __device__ void invert_block(int n, T* m) {
     for (int k = 0; k < n * n; k++) m[k] = out[k];
 }
 
+// crossMat (NMat.cpp:59-67), row-major
+__device__ __forceinline__ void cross_mat(f3 v, float m[3][3]) {
+    m[0][0] = 0.f;  m[0][1] = -v.z; m[0][2] = v.y;
+    m[1][0] = v.z;  m[1][1] = 0.f;  m[1][2] = -v.x;
+    m[2][0] = -v.y; m[2][1] = v.x;  m[2][2] = 0.f;
+}
+// (1x3 row) * (3x3), as NMat<1,3> * NMat<3,3> accumulates it
+__device__ __forceinline__ f3 row_times(f3 v, const float m[3][3]) {
+    return mk(v.x * m[0][0] + v.y * m[1][0] + v.z * m[2][0], v.x * m[0][1] + v.y * m[1][1] + v.z * m[2][1],
+              v.x * m[0][2] + v.y * m[1][2] + v.z * m[2][2]);
+}
+__device__ __forceinline__ void set_row(float* j, f3 lin, f3 ang) {
+    j[0] = lin.x; j[1] = lin.y; j[2] = lin.z; j[3] = ang.x; j[4] = ang.y; j[5] = ang.z;
+}
+
+// angle * axis of q_b * conj(q_a) scaled by c (Quaternion::angleTo and
+// getRotAxis, Math/src/Quaternion.h:35-49): the orientation error of the weld
+// and slider rows.  The reference takes 2 acos(|q_a . q_b|) and calls angles
+// below 2 acos(0.99999999999) zero; in FP32 the arc cosine of a dot product
+// near 1 loses the angle (resolution ~3e-4 rad), so the same angle is taken
+// as 2 atan2(|vec(dq)|, |dq.r|) (dq.r = q_a . q_b), with the same cutoff.
+__device__ __forceinline__ f3 orientation_error(float4 qa, float4 qb, float c) {
+    const float4 dq = qmul(qb, qconj(qa));
+    const f3 v = mk(dq.y, dq.z, dq.w);
+    const float s = mag(v);
+    const float angle = 2.0f * atan2f(s, fabsf(dq.x));
+    if (!(angle >= 8.944272e-6f) || s == 0.f) return mk(0.f, 0.f, 0.f);
+    const f3 axis = (dq.x < 0.f ? -1.0f / s : 1.0f / s) * v;
+    return (angle * c) * axis;
+}
+
+// 1 - cos(f) by its series to the 8th order, as the limit rows' error
+// (ConstraintSolver.cpp:415-421, 447-455)
+__device__ __forceinline__ float limit_error(float f) {
+    const float f2 = f * f, f4 = f2 * f2, f6 = f4 * f2, f8 = f4 * f4;
+    return -f8 / 40320.0f + f6 / 720.0f - f4 / 24.0f + f2 / 2.0f;
+}
+
 __global__ void k_joint_rows(Dev d) {
     const JointStore& J = d.jt;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < d.n_joints; j += gridDim.x * blockDim.x) {
-        const int a = J.b1[j], b = J.b2[j], n = J.n[j];
+        const int a = J.b1[j], b = J.b2[j], n = J.n[j], kind = J.kind[j];
         if (d.movement[a] != 0 && d.movement[b] != 0) continue;
         const WorldParams& P = d.wparams[d.world[a]];
         const float dts = P.dt_sub;
         const float4 qa = d.rot[a], qb = d.rot[b];
         const f3 ca = mk(d.pos[a]), cb = mk(d.pos[b]);
-        const f3 pa = qrot(qa, mk(J.p1[j])) + ca, pb = qrot(qb, mk(J.p2[j])) + cb;
         const float2 hard = J.hard[j];
-        const float pos_c = fminf(hard.x * dts, 1.0f / dts);
         JointRow& R = d.jt.rows[j];
-        R.n = n;
-        float warm[kJMax];
-        for (int i = 0; i < n; i++) warm[i] = P.warm_disabled ? 0.f : J.impulse[kJMax * j + i];
-        for (int i = 0; i < n; i++) { R.impulse[i] = warm[i]; R.pimpulse[i] = 0.f; R.holo[i] = 0.f; }
-        const f3 rA = pa - ca;
-        if (n == 3) {
-            point_rows(R.ja, R.jb, rA, pb - cb);
-            const f3 e = pb - pa;
-            R.ptarget[0] = pos_c * e.x; R.ptarget[1] = pos_c * e.y; R.ptarget[2] = pos_c * e.z;
+        float* jimp = J.impulse + kJMax * (size_t)j;
+        bool rebuilt = true;
+        if (jk_limit(kind)) {
+            // ConeRotationLimit / TwistLimit::updateSolverConstraints
+            // (PersistentConstraint.cpp:233-272): inside the limit the row is
+            // inactive (warm impulse cleared, the old row kept, not listed in
+            // the next islands); at or past it a one-dof row on the axis,
+            // warm-started from the stored impulse unscaled
+            bool inactive;
+            float f;
+            f3 ja_ang, jb_ang;
+            int proj = 1;
+            if (kind == JK_CONE) {
+                const f3 d1 = qrot(qa, mk(J.ax1[j])), d2 = qrot(qb, mk(J.ax2[j]));
+                // the reference's acos(d1 . d2) is taken on the dot product
+                // clamped to [-1, 1] (FP32 rounding can leave it above 1)
+                const float cur = acosf(fminf(1.0f, fmaxf(-1.0f, dot(d1, d2))));
+                const float mx = J.par[j].x;
+                inactive = cur < mx;
+                const f3 h = normalize(cross(d1, d2));
+                ja_ang = h;
+                jb_ang = -h;
+                f = cur - mx;
+            } else {
+                // getCurrentAngle (PersistentConstraint.cpp:115-131): body 1's
+                // w axis carried by body 2, measured in body 1's (w, u) frame,
+                // unwrapped against the previous value with the reference's
+                // truncated pi
+                const M33 r1 = quatRot(qa), r2 = quatRot(qb);
+                const f3 t1 = mul(r1, mk(J.ax1[j])), u1 = mul(r1, mk(J.ul[j])), w1 = mul(r1, mk(J.wl[j]));
+                const f3 t2 = mul(r2, mk(J.ax2[j])), r2w = mul(r2, mk(J.wl[j]));
+                const float kPi = 3.1415926535f;
+                const float prev = J.angle[j];
+                float ang = atan2f(dot(r2w, u1), dot(r2w, w1));
+                while (prev - ang > kPi) ang += 2.0f * kPi;
+                while (prev - ang < -kPi) ang -= 2.0f * kPi;
+                J.angle[j] = ang;
+                const float mn = J.par[j].y, mx = J.par[j].x;
+                inactive = mn <= ang && ang <= mx;
+                const bool above = ang > mx;
+                proj = above ? 2 : 1;
+                ja_ang = -t1;
+                jb_ang = t2;
+                f = above ? ang - mx : mn - ang;
+            }
+            J.active[j] = inactive ? 0 : 1;
+            if (inactive) {
+                jimp[0] = 0.f;
+                R.impulse[0] = 0.f;
+                rebuilt = false;
+            } else {
+                R.n = 1;
+                R.proj = proj;
+                R.impulse[0] = jimp[0];
+                R.pimpulse[0] = 0.f;
+                R.holo[0] = 0.f;
+                set_row(R.ja, mk(0.f, 0.f, 0.f), ja_ang);
+                set_row(R.jb, mk(0.f, 0.f, 0.f), jb_ang);
+                R.ptarget[0] = limit_error(f) * hard.y;
+            }
         } else {
-            // the reference's hinge takes rB from body 1's anchor point
-            point_rows(R.ja, R.jb, rA, pa - cb);
-            const f3 h1 = qrot(qa, mk(J.ax1[j])), nn = qrot(qb, mk(J.ax2[j]));
+            const f3 pa = qrot(qa, mk(J.p1[j])) + ca, pb = qrot(qb, mk(J.p2[j])) + cb;
+            const float pos_c = fminf(hard.x * dts, 1.0f / dts);
             const float rot_c = fminf(hard.y * dts, 1.0f / dts);
-            f3 uu, ww;
-            basis(h1, &uu, &ww);
-            const f3 su = mk(J.u[j]), sw = mk(J.w[j]);
-            R.impulse[3] = dot(uu, su) * warm[3] + dot(uu, sw) * warm[4];
-            R.impulse[4] = dot(ww, su) * warm[3] + dot(ww, sw) * warm[4];
-            // n^T [u]x, u^T [n]x, n^T [w]x, w^T [n]x
-            const f3 a3 = cross(nn, uu), b3 = cross(uu, nn), a4 = cross(nn, ww), b4 = cross(ww, nn);
-            const float ar[2][3] = {{a3.x, a3.y, a3.z}, {a4.x, a4.y, a4.z}};
-            const float br[2][3] = {{b3.x, b3.y, b3.z}, {b4.x, b4.y, b4.z}};
-            for (int i = 0; i < 2; i++)
-                for (int k = 0; k < 3; k++) {
-                    R.ja[6 * (3 + i) + k] = 0.f;
-                    R.jb[6 * (3 + i) + k] = 0.f;
-                    R.ja[6 * (3 + i) + 3 + k] = ar[i][k];
-                    R.jb[6 * (3 + i) + 3 + k] = br[i][k];
+            R.n = n;
+            R.proj = 0;
+            float warm[kJMax];
+            // Weld::updateSolverConstraints passes the previous impulse on
+            // unscaled whatever the warm-start switch says
+            // (PersistentConstraint.cpp:344-353)
+            for (int i = 0; i < n; i++) warm[i] = (P.warm_disabled && kind != JK_WELD) ? 0.f : jimp[i];
+            for (int i = 0; i < n; i++) { R.impulse[i] = warm[i]; R.pimpulse[i] = 0.f; R.holo[i] = 0.f; }
+            const f3 rA = pa - ca;
+            float sa[3][3], sb[3][3];
+            cross_mat(rA, sa);
+            if (kind == JK_BALL || kind == JK_WELD) {
+                // BallSocketConstraint (ConstraintSolver.cpp:382-405), and the
+                // WeldConstraint's three more rows locking the relative
+                // angular velocity (:861-899)
+                point_rows(R.ja, R.jb, rA, pb - cb);
+                const f3 e = (pb - pa) * pos_c;
+                R.ptarget[0] = e.x; R.ptarget[1] = e.y; R.ptarget[2] = e.z;
+                if (kind == JK_WELD) {
+                    for (int i = 0; i < 3; i++) {
+                        const f3 u = mk(i == 0 ? 1.f : 0.f, i == 1 ? 1.f : 0.f, i == 2 ? 1.f : 0.f);
+                        set_row(R.ja + 6 * (3 + i), mk(0.f, 0.f, 0.f), u);
+                        set_row(R.jb + 6 * (3 + i), mk(0.f, 0.f, 0.f), -u);
+                    }
+                    const f3 oe = orientation_error(qa, qb, rot_c);
+                    R.ptarget[3] = oe.x; R.ptarget[4] = oe.y; R.ptarget[5] = oe.z;
                 }
-            const f3 pc = (pb - pa) * pos_c;
-            R.ptarget[0] = pc.x; R.ptarget[1] = pc.y; R.ptarget[2] = pc.z;
-            R.ptarget[3] = dot(uu, nn) * rot_c;
-            R.ptarget[4] = dot(ww, nn) * rot_c;
-            d.jt.u[j] = make_float4(uu.x, uu.y, uu.z, 0.f);
-            d.jt.w[j] = make_float4(ww.x, ww.y, ww.z, 0.f);
-        }
-        // impulse_to_{a,b}_velocity = M^-1 J^T, impulse_to_value, CFM inverse
-        const float ima = d.pos[a].w, imb = d.pos[b].w;
-        const M33 Ia = load9(d.iinv + 9 * a), Ib = load9(d.iinv + 9 * b);
-        for (int i = 0; i < n; i++) {
-            for (int k = 0; k < 3; k++) {
-                R.ita[kJMax * k + i] = ima * R.ja[6 * i + k];
-                R.itb[kJMax * k + i] = imb * R.jb[6 * i + k];
+            } else if (kind == JK_DISTANCE) {
+                // DistanceConstraint (ConstraintSolver.cpp:348-377): one row
+                // along the attachment direction, error target - |pa - pb|
+                cross_mat(pb - cb, sb);
+                const f3 diff = pa - pb;
+                const f3 dd = normalize(diff);
+                set_row(R.ja, dd, row_times(-dd, sa));
+                set_row(R.jb, -dd, row_times(dd, sb));
+                const float target = J.par[j].x;
+                const float error = mag2(diff) < 0.00001f ? target : target - dot(dd, diff);
+                R.ptarget[0] = pos_c * error;
+            } else if (kind == JK_SLIDER) {
+                // SliderConstraint (ConstraintSolver.cpp:611-696): two rows
+                // across body 1's axis (its u, w) and three locking the
+                // relative rotation; the orientation rows are corrected with
+                // the position coefficient, as Slider::updateSolverConstraints
+                // passes it (PersistentConstraint.cpp:287-298)
+                cross_mat(pb - cb, sb);
+                const f3 ax = normalize(qrot(qa, mk(J.ax1[j])));
+                f3 uu, ww;
+                basis(ax, &uu, &ww);
+                const f3 su = mk(J.u[j]), sw = mk(J.w[j]);
+                R.impulse[0] = dot(uu, su) * warm[0] + dot(uu, sw) * warm[1];
+                R.impulse[1] = dot(ww, su) * warm[0] + dot(ww, sw) * warm[1];
+                const f3 pe = pa - pb;
+                float us[3][3], ws[3][3];
+                cross_mat(uu, us);
+                cross_mat(ww, ws);
+                set_row(R.ja, uu, row_times(-uu, sa) - row_times(pe, us));
+                set_row(R.jb, -uu, row_times(uu, sb));
+                set_row(R.ja + 6, ww, row_times(-ww, sa) - row_times(pe, ws));
+                set_row(R.jb + 6, -ww, row_times(ww, sb));
+                for (int i = 0; i < 3; i++) {
+                    const f3 u = mk(i == 0 ? 1.f : 0.f, i == 1 ? 1.f : 0.f, i == 2 ? 1.f : 0.f);
+                    set_row(R.ja + 6 * (2 + i), mk(0.f, 0.f, 0.f), u);
+                    set_row(R.jb + 6 * (2 + i), mk(0.f, 0.f, 0.f), -u);
+                }
+                const f3 oe = orientation_error(qa, qb, pos_c);
+                R.ptarget[0] = -dot(pe, uu) * pos_c;
+                R.ptarget[1] = -dot(pe, ww) * pos_c;
+                R.ptarget[2] = oe.x; R.ptarget[3] = oe.y; R.ptarget[4] = oe.z;
+                d.jt.u[j] = make_float4(uu.x, uu.y, uu.z, 0.f);
+                d.jt.w[j] = make_float4(ww.x, ww.y, ww.z, 0.f);
+            } else if (kind == JK_SLIDING_HINGE) {
+                // SlidingHingeConstraint (ConstraintSolver.cpp:781-852): two
+                // rows across body 2's axis and two keeping body 1's axis
+                // parallel to it
+                cross_mat(pb - cb, sb);
+                const f3 na = qrot(qa, mk(J.ax1[j])), nb = qrot(qb, mk(J.ax2[j]));
+                f3 uu, ww;
+                basis(nb, &uu, &ww);
+                const f3 su = mk(J.u[j]), sw = mk(J.w[j]);
+                R.impulse[2] = dot(uu, su) * warm[2] + dot(uu, sw) * warm[3];
+                R.impulse[3] = dot(ww, su) * warm[2] + dot(ww, sw) * warm[3];
+                const f3 pd = pa - pb;
+                float us[3][3], ws[3][3], ns[3][3];
+                cross_mat(uu, us);
+                cross_mat(ww, ws);
+                cross_mat(na, ns);
+                set_row(R.ja, uu, row_times(-uu, sa));
+                set_row(R.jb, -uu, row_times(uu, sb) - row_times(pd, us));
+                set_row(R.ja + 6, ww, row_times(-ww, sa));
+                set_row(R.jb + 6, -ww, row_times(ww, sb) - row_times(pd, ws));
+                set_row(R.ja + 12, mk(0.f, 0.f, 0.f), row_times(-uu, ns));
+                set_row(R.jb + 12, mk(0.f, 0.f, 0.f), row_times(-na, us));
+                set_row(R.ja + 18, mk(0.f, 0.f, 0.f), row_times(-ww, ns));
+                set_row(R.jb + 18, mk(0.f, 0.f, 0.f), row_times(-na, ws));
+                R.ptarget[0] = -dot(uu, pd) * pos_c;
+                R.ptarget[1] = -dot(ww, pd) * pos_c;
+                R.ptarget[2] = -dot(uu, na) * rot_c;
+                R.ptarget[3] = -dot(ww, na) * rot_c;
+                d.jt.u[j] = make_float4(uu.x, uu.y, uu.z, 0.f);
+                d.jt.w[j] = make_float4(ww.x, ww.y, ww.z, 0.f);
+            } else {
+                // HingeConstraint (ConstraintSolver.cpp:468-550); the
+                // reference's hinge takes rB from body 1's anchor point
+                point_rows(R.ja, R.jb, rA, pa - cb);
+                const f3 h1 = qrot(qa, mk(J.ax1[j])), nn = qrot(qb, mk(J.ax2[j]));
+                f3 uu, ww;
+                basis(h1, &uu, &ww);
+                const f3 su = mk(J.u[j]), sw = mk(J.w[j]);
+                R.impulse[3] = dot(uu, su) * warm[3] + dot(uu, sw) * warm[4];
+                R.impulse[4] = dot(ww, su) * warm[3] + dot(ww, sw) * warm[4];
+                // n^T [u]x, u^T [n]x, n^T [w]x, w^T [n]x
+                set_row(R.ja + 18, mk(0.f, 0.f, 0.f), cross(nn, uu));
+                set_row(R.jb + 18, mk(0.f, 0.f, 0.f), cross(uu, nn));
+                set_row(R.ja + 24, mk(0.f, 0.f, 0.f), cross(nn, ww));
+                set_row(R.jb + 24, mk(0.f, 0.f, 0.f), cross(ww, nn));
+                const f3 pc = (pb - pa) * pos_c;
+                R.ptarget[0] = pc.x; R.ptarget[1] = pc.y; R.ptarget[2] = pc.z;
+                R.ptarget[3] = dot(uu, nn) * rot_c;
+                R.ptarget[4] = dot(ww, nn) * rot_c;
+                d.jt.u[j] = make_float4(uu.x, uu.y, uu.z, 0.f);
+                d.jt.w[j] = make_float4(ww.x, ww.y, ww.z, 0.f);
             }
-            const f3 ta = mul(Ia, mk(R.ja[6 * i + 3], R.ja[6 * i + 4], R.ja[6 * i + 5]));
-            const f3 tb = mul(Ib, mk(R.jb[6 * i + 3], R.jb[6 * i + 4], R.jb[6 * i + 5]));
-            R.ita[kJMax * 3 + i] = ta.x; R.ita[kJMax * 4 + i] = ta.y; R.ita[kJMax * 5 + i] = ta.z;
-            R.itb[kJMax * 3 + i] = tb.x; R.itb[kJMax * 4 + i] = tb.y; R.itb[kJMax * 5 + i] = tb.z;
         }
-        float m[kJMax * kJMax];
-        for (int i = 0; i < n; i++)
-            for (int c = 0; c < n; c++) {
-                float x = 0.f, y = 0.f;
-                for (int k = 0; k < 6; k++) { x += R.ja[6 * i + k] * R.ita[kJMax * k + c]; y += R.jb[6 * i + k] * R.itb[kJMax * k + c]; }
-                R.itv[kJMax * i + c] = x + y;
-                m[n * i + c] = x + y;
+        const int rn = R.n;
+        if (rebuilt) {
+            // impulse_to_{a,b}_velocity = M^-1 J^T, impulse_to_value, CFM inverse
+            const float ima = d.pos[a].w, imb = d.pos[b].w;
+            const M33 Ia = load9(d.iinv + 9 * a), Ib = load9(d.iinv + 9 * b);
+            for (int i = 0; i < rn; i++) {
+                for (int k = 0; k < 3; k++) {
+                    R.ita[kJMax * k + i] = ima * R.ja[6 * i + k];
+                    R.itb[kJMax * k + i] = imb * R.jb[6 * i + k];
+                }
+                const f3 ta = mul(Ia, mk(R.ja[6 * i + 3], R.ja[6 * i + 4], R.ja[6 * i + 5]));
+                const f3 tb = mul(Ib, mk(R.jb[6 * i + 3], R.jb[6 * i + 4], R.jb[6 * i + 5]));
+                R.ita[kJMax * 3 + i] = ta.x; R.ita[kJMax * 4 + i] = ta.y; R.ita[kJMax * 5 + i] = ta.z;
+                R.itb[kJMax * 3 + i] = tb.x; R.itb[kJMax * 4 + i] = tb.y; R.itb[kJMax * 5 + i] = tb.z;
             }
-        for (int i = 0; i < n; i++) m[n * i + i] *= (1.0f + P.cfm);
-        invert_block<float>(n, m);
-        for (int i = 0; i < n; i++)
-            for (int c = 0; c < n; c++) R.minv[kJMax * i + c] = m[n * i + c];
-        // target from the bodies' velocities at the start of the solve
+            float m[kJMax * kJMax];
+            for (int i = 0; i < rn; i++)
+                for (int c = 0; c < rn; c++) {
+                    float x = 0.f, y = 0.f;
+                    for (int k = 0; k < 6; k++) { x += R.ja[6 * i + k] * R.ita[kJMax * k + c]; y += R.jb[6 * i + k] * R.itb[kJMax * k + c]; }
+                    R.itv[kJMax * i + c] = x + y;
+                    m[rn * i + c] = x + y;
+                }
+            for (int i = 0; i < rn; i++) m[rn * i + i] *= (1.0f + P.cfm);
+            invert_block<float>(rn, m);
+            for (int i = 0; i < rn; i++)
+                for (int c = 0; c < rn; c++) R.minv[kJMax * i + c] = m[rn * i + c];
+        }
+        // target from the bodies' velocities at the start of the solve (also
+        // for a limit row kept from an earlier rebuild: it is solved when its
+        // island listed it)
         float va[6] = {0, 0, 0, 0, 0, 0}, vb[6] = {0, 0, 0, 0, 0, 0}, cur[kJMax];
         if (d.movement[a] != 1) {
             float4 v = d.vel[a], w = d.angv[a];
@@ -168,8 +360,62 @@ __global__ void k_joint_rows(Dev d) {
             float4 v = d.vel[b], w = d.angv[b];
             vb[0] = v.x; vb[1] = v.y; vb[2] = v.z; vb[3] = w.x; vb[4] = w.y; vb[5] = w.z;
         }
-        jvalue(R, va, vb, cur);
-        for (int i = 0; i < n; i++) R.target[i] = -cur[i];
+        if (rn > 0) {
+            jvalue(R, va, vb, cur);
+            for (int i = 0; i < rn; i++) R.target[i] = -cur[i];
+        }
+    }
+}
+
+// Springs (maintainConstraintGraphApplyPoweredConstraints,
+// PhysicsEngine.cpp:1309-1356): at the start of every substep, one thread
+// per world applies its springs in the reference's order (they may share
+// bodies, and each reads the velocities the previous one left): a stiffness
+// impulse along the attachment direction, then a damping impulse capped so
+// that it cannot reverse the relative velocity, measured at the reference's
+// crossed attachment points (RigidBody::getVelOfPoint, RigidBody.cpp:153-155)
+__device__ __forceinline__ void impulse_at(const Dev& d, int b, f3 imp, f3 at) {
+    if (d.movement[b] != 0) return;   // RigidBody::applyImpulse on a fixed or kinematic body changes nothing
+    const float4 p = d.pos[b];
+    const f3 torque = cross(at - mk(p), imp);
+    const M33 I = load9(d.iinv + 9 * b);
+    const f3 dw = mul(I, torque);
+    float4 v = d.vel[b], w = d.angv[b];
+    v.x += p.w * imp.x; v.y += p.w * imp.y; v.z += p.w * imp.z;
+    w.x += dw.x; w.y += dw.y; w.z += dw.z;
+    d.vel[b] = v;
+    d.angv[b] = w;
+}
+
+__global__ void k_springs(Dev d) {
+    const SpringStore& S = d.sp;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < d.n_worlds; w += gridDim.x * blockDim.x) {
+        const float dt = d.wparams[w].dt_sub;
+        for (int k = S.world_start[w]; k < S.world_start[w + 1]; k++) {
+            const int a = S.b1[k], b = S.b2[k];
+            const f3 ca = mk(d.pos[a]), cb = mk(d.pos[b]);
+            const f3 pa = qrot(d.rot[a], mk(S.p1[k])) + ca, pb = qrot(d.rot[b], mk(S.p2[k])) + cb;
+            const float4 par = S.par[k];
+            const f3 diff = pb - pa;
+            const float dist = mag(diff);
+            const f3 dir = dist != 0.f ? normalize(diff) : mk(0.f, -1.f, 0.f);
+            const float expand = par.y * (dist - par.z);
+            impulse_at(d, a, dir * (expand * dt), pa);
+            impulse_at(d, b, -dir * (expand * dt), pb);
+            const f3 rA = pa - ca, rB = pb - cb;
+            const float ima = d.pos[a].w, imb = d.pos[b].w;
+            const f3 rdA = mul(load9(d.iinv + 9 * a), cross(dir, rA));
+            const f3 rdB = mul(load9(d.iinv + 9 * b), cross(dir, rB));
+            const float sens = 1.0f / (ima + imb + dot(cross(rA, rdA), dir) + dot(cross(rB, rdB), dir));
+            const f3 va = mk(d.vel[a]), wa = mk(d.angv[a]), vb = mk(d.vel[b]), wb = mk(d.angv[b]);
+            const float velocity = dot(vb + cross(wb, pa - cb), dir) - dot(va + cross(wa, pb - ca), dir);
+            float dampen = par.x * velocity;
+            const float max_dampen = velocity * sens / dt;
+            if (velocity > 0.f && dampen > max_dampen) dampen = max_dampen;
+            else if (velocity < 0.f && dampen < max_dampen) dampen = max_dampen;
+            impulse_at(d, a, dir * (dampen * dt), pa);
+            impulse_at(d, b, -dir * (dampen * dt), pb);
+        }
     }
 }
 
@@ -275,6 +521,13 @@ __global__ void __launch_bounds__(32) k_holo_factor(Dev d) {
 }
 
 }  // namespace
+
+void launch_springs(const Dev& d, const Launch& L) {
+    if (d.sp.n == 0) return;
+    int g = (d.n_worlds + 127) / 128;
+    g = g > L.n_sms * 8 ? L.n_sms * 8 : g;
+    k_springs<<<g, 128, 0, L.st>>>(d);
+}
 
 void launch_joint_rows(const Dev& d, bool first, const Launch& L) {
     if (d.n_joints == 0) return;

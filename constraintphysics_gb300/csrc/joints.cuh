@@ -1,5 +1,6 @@
-// joints.cuh — device helpers for joint rows (ball-socket, hinge) and the
-// holonomic block solve, shared by the row-building kernels (joints.cu) and
+// joints.cuh — device helpers for joint rows (ball-socket, hinge, distance,
+// weld, slider, sliding hinge, cone and twist limits) and the holonomic block
+// solve, shared by the row-building kernels (joints.cu) and
 // the joint-island PGS kernel (solver.cu).
 #pragma once
 #include "devmath.cuh"
@@ -15,18 +16,17 @@ __device__ __forceinline__ bool jzero(const float* x, int n) {
     return true;
 }
 
-// Δv slots of one island: 4 float4 per island body (v lin, v ang, pv lin, pv ang)
+// Δv slots of one island: kDvF4 float4 per island body, 12 floats v xyz,
+// w xyz, pv xyz, pw xyz; `which` 0 = (v, w), 1 = (pv, pw)
 __device__ __forceinline__ void jload(const float4* dv, int slot, int which, float* out) {
     if (slot < 0) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
-    float4 l = dv[4 * slot + 2 * which], a = dv[4 * slot + 2 * which + 1];
-    out[0] = l.x; out[1] = l.y; out[2] = l.z; out[3] = a.x; out[4] = a.y; out[5] = a.z;
+    const float* f = reinterpret_cast<const float*>(dv + kDvF4 * slot) + 6 * which;
+    for (int k = 0; k < 6; k++) out[k] = f[k];
 }
 __device__ __forceinline__ void jadd(float4* dv, int slot, int which, const float* x) {
     if (slot < 0) return;
-    float4& l = dv[4 * slot + 2 * which];
-    float4& a = dv[4 * slot + 2 * which + 1];
-    l.x += x[0]; l.y += x[1]; l.z += x[2];
-    a.x += x[3]; a.y += x[4]; a.z += x[5];
+    float* f = reinterpret_cast<float*>(dv + kDvF4 * slot) + 6 * which;
+    for (int k = 0; k < 6; k++) f[k] += x[k];
 }
 
 // J_a v_a + J_b v_b
@@ -53,9 +53,10 @@ __device__ __forceinline__ void japply(const JointRow& R, const float* imp, floa
     jadd(dv, R.sb, which, xb);
 }
 
-// The same steps for a row of N dofs known at compile time (3: ball-socket,
-// 5: hinge): every loop unrolls, so the row's entries are loaded once into
-// registers instead of through loops over a run-time count (identical sums)
+// The same steps for a row of N dofs known at compile time (1: distance and
+// limits, 3: ball-socket, 4: sliding hinge, 5: hinge and slider, 6: weld):
+// every loop unrolls, so the row's entries are loaded once into registers
+// instead of through loops over a run-time count (identical sums)
 template <int N>
 __device__ __forceinline__ void japply_n(const JointRow& R, const float* imp, float4* dv, int which) {
     float xa[6], xb[6];
@@ -71,6 +72,10 @@ __device__ __forceinline__ void japply_n(const JointRow& R, const float* imp, fl
     jadd(dv, R.sb, which, xb);
 }
 
+// PGSConstraintStep<n> (ConstraintSolver.cpp:12-40): the accumulated impulse
+// plus the row's correction, projected (ConeLimitConstraint /
+// TwistLimitConstraint::projectValidImpulse, ConstraintSolver.cpp:434-436,
+// 463-465: one-sided limits), applied when the change is not zero
 template <int N>
 __device__ __forceinline__ void jstep_n(JointRow& R, float4* dv, bool pseudo) {
     const int which = pseudo ? 1 : 0;
@@ -95,7 +100,10 @@ __device__ __forceinline__ void jstep_n(JointRow& R, float4* dv, bool pseudo) {
         float x = 0.f;
 #pragma unroll
         for (int k = 0; k < N; k++) x += delta[k] * R.minv[kJMax * i + k];
-        diff[i] = (acc[i] + x) - acc[i];
+        float nw = acc[i] + x;
+        if (N == 1 && R.proj == 1) nw = fmaxf(nw, 0.f);
+        else if (N == 1 && R.proj == 2) nw = fminf(nw, 0.f);
+        diff[i] = nw - acc[i];
         zero = zero && !(fabsf(diff[i]) > kJZero);
     }
     if (!zero) {
@@ -108,14 +116,24 @@ __device__ __forceinline__ void jstep_n(JointRow& R, float4* dv, bool pseudo) {
 // warm start (DegreedConstraint::applyWarmStartVelocityChange)
 __device__ __forceinline__ void jwarm(const JointRow& R, float4* dv) {
     if (jzero(R.impulse, R.n)) return;
-    if (R.n == 3) japply_n<3>(R, R.impulse, dv, 0);
-    else japply_n<5>(R, R.impulse, dv, 0);
+    switch (R.n) {
+        case 1: japply_n<1>(R, R.impulse, dv, 0); break;
+        case 3: japply_n<3>(R, R.impulse, dv, 0); break;
+        case 4: japply_n<4>(R, R.impulse, dv, 0); break;
+        case 5: japply_n<5>(R, R.impulse, dv, 0); break;
+        default: japply_n<6>(R, R.impulse, dv, 0); break;
+    }
 }
 
-// PGSConstraintStep<n> (ConstraintSolver.cpp:12-40) of an equality row
+// one Gauss-Seidel step of a joint row
 __device__ __forceinline__ void jstep(JointRow& R, float4* dv, bool pseudo) {
-    if (R.n == 3) jstep_n<3>(R, dv, pseudo);
-    else jstep_n<5>(R, dv, pseudo);
+    switch (R.n) {
+        case 1: jstep_n<1>(R, dv, pseudo); break;
+        case 3: jstep_n<3>(R, dv, pseudo); break;
+        case 4: jstep_n<4>(R, dv, pseudo); break;
+        case 5: jstep_n<5>(R, dv, pseudo); break;
+        default: jstep_n<6>(R, dv, pseudo); break;
+    }
 }
 
 // ---- holonomic systems (HolonomicBlockSolver.cpp) ------------------------------
@@ -161,7 +179,7 @@ __device__ void holo_solve(const HoloStore& hs, int s, const JointRow* rows, con
     }
     for (int col = n - 2; col >= 0; col--) {
         const int bw = rows[cons[col]].n;
-        T e6[kJMax] = {0, 0, 0, 0, 0};
+        T e6[kJMax] = {};
         for (int q = ls[col]; q < ls[col + 1]; q++) {
             const int row = hs.lrow[q], l = hs.lloc[q];
             const int bh = rows[cons[row]].n;

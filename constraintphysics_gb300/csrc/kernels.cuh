@@ -34,6 +34,9 @@ void launch_merge(const Dev& d, const Launch& L);
 // memory any batch uses: the kernels' dynamic shared memory limits are set to
 // these once for all batches
 constexpr int kPgsDvCapMax = 1536;
+// default size threshold between the thread-per-island and the warp-per-island
+// solvers (rows of the island); the autotuner may choose another
+constexpr int kDefaultBigRows = 48;
 constexpr int kIslandsSmemMax = 160 * 1024;
 // k_islands' dynamic shared memory for worlds of up to `max_bodies` bodies
 // (sets the kernel's limit); worlds that need more run from global memory
@@ -54,6 +57,8 @@ void launch_integrate(const Dev& d, int last, const Launch& L);
 // joints: rows every substep, the holonomic systems' factorisation on the
 // first; islands with joint rows solved by their own kernel
 void launch_joint_rows(const Dev& d, bool first, const Launch& L);
+// springs: impulse pairs at the start of every substep (no-op without springs)
+void launch_springs(const Dev& d, const Launch& L);
 void launch_pgs_joint(const Dev& d, bool first, const Launch& L);
 // external state write: apply the staged state (d.stage); bodies whose pose
 // changed get their world inertia tensors and AABBs recomputed
@@ -61,5 +66,7 @@ void launch_apply_state(const Dev& d, const Launch& L);
 // host-layout rows (pos, rot, vel, ang vel: 4 float4 per body) of a split batch
 void launch_gather_state(const Dev& d, const float4* all, const int* rows, const Launch& L);   // all -> d.stage
 void launch_scatter_state(const Dev& d, const int* rows, float4* all, const Launch& L);       // d -> all
+// FP64 momentum / energy audit of every world (no-op when d.audit is null)
+void launch_audit(const Dev& d, const Launch& L);
 
 }  // namespace cpgpu

@@ -8,6 +8,7 @@
 // edges, contacts, islands) are device-side counters so the whole step can be
 // captured once in a CUDA graph and replayed.
 #pragma once
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -142,14 +143,11 @@ struct EdgeStore {
 
 // Solver row block of one contact (normal row + 2-dof friction row), built each
 // substep in island order (ConstraintSolver.cpp:240-343).  384 bytes, 16-byte
-// aligned.  The Jacobian entries are split by component triple (h[0] linear,
-// h[1] angular, each for both bodies), so that a solver lane owning one triple
-// reads one contiguous half.
-struct RowHalf {
-    float nja[3], njb[3], nita[3], nitb[3];          // normal row J and M^-1 J^T
-    float fja0[3], fja1[3], fjb0[3], fjb1[3];        // friction rows (u, w)
-    float fita0[3], fita1[3], fitb0[3], fitb1[3];    // friction M^-1 J^T columns (u, w)
-};
+// aligned.  After a 96-byte header come twelve 6-vectors (linear xyz, angular
+// xyz), 24 bytes apart from byte 96, so that every (x, y), (z, ax), (ay, az)
+// component pair sits in one half of a 16-byte word: the solver loads the
+// row with 16-byte loads and computes on the pairs with packed FP32
+// instructions (fma.rn.f32x2).
 struct alignas(16) RowBlock {
     float4 imp;          // accumulated impulses: normal, pseudo normal, friction u, w
     int sa, sb;          // island body slots (-1 = body with infinite mass)
@@ -162,15 +160,25 @@ struct alignas(16) RowBlock {
     float nminv, nptarget;
     float kf0, kf1;      // J_f M^-1 J_n^T of friction rows u, w: their velocity change per unit normal impulse
     float fminv[4];
-    RowHalf h[2];
+    float nja[6], njb[6], nita[6], nitb[6];          // normal row J and M^-1 J^T (bodies a, b)
+    float fja0[6], fjb0[6], fja1[6], fjb1[6];        // friction rows (u, w)
+    float fita0[6], fitb0[6], fita1[6], fitb1[6];    // friction M^-1 J^T columns (u, w)
 };
 static_assert(sizeof(RowBlock) == 384, "row block size");
-static_assert(sizeof(RowHalf) == 144, "row half size");
+static_assert(offsetof(RowBlock, nja) == 96, "row vectors start at byte 96");
 
-// One joint row per substep: DegreedConstraint<n> of a BallSocketConstraint
-// (n = 3) or HingeConstraint (n = 5) (ConstraintSolver.h:60-144), row-major,
-// sized for n = 5.
-constexpr int kJMax = 5;
+// Velocity deltas of an island body (the solver's accumulator): 12 floats in
+// kDvF4 float4s, v xyz, w xyz, pv xyz, pw xyz (pseudo velocities for the
+// position passes); the (v, w) and (pv, pw) 6-vectors split into the same
+// component pairs as the rows' vectors
+constexpr int kDvF4 = 3;
+
+// One joint row per substep: DegreedConstraint<n> (ConstraintSolver.h:60-144)
+// of a DistanceConstraint (n = 1), BallSocketConstraint (3),
+// SlidingHingeConstraint (4), HingeConstraint or SliderConstraint (5),
+// WeldConstraint (6), ConeLimitConstraint or TwistLimitConstraint (1, with a
+// one-sided projection); row-major, sized for n = 6.
+constexpr int kJMax = 6;
 struct alignas(16) JointRow {
     float ja[kJMax * 6], jb[kJMax * 6];     // [n][6]
     float ita[6 * kJMax], itb[6 * kJMax];   // [6][n]
@@ -178,33 +186,61 @@ struct alignas(16) JointRow {
     float target[kJMax], ptarget[kJMax];
     float impulse[kJMax], pimpulse[kJMax], holo[kJMax];
     int n, sa, sb;                          // island body slots (-1: infinite mass)
-    int pad;
+    int proj;                               // 0 none, 1 impulse >= 0, 2 impulse <= 0 (limits)
 };
 
-// Static joint description (PhysicsEngine::addBallSocketConstraint /
-// addHingeConstraint): anchors are the tracked points relative to each body's
-// centre of mass in its body frame; hinge axes in body space.
+// Joint kinds (PersistentConstraint.h:90-420).  The limits are inequality
+// rows outside the holonomic systems, listed in an island only while active.
+enum JointKind : int {
+    JK_BALL = 0, JK_HINGE = 1, JK_DISTANCE = 2, JK_WELD = 3, JK_SLIDER = 4, JK_SLIDING_HINGE = 5,
+    JK_CONE = 6, JK_TWIST = 7,
+};
+__host__ __device__ inline bool jk_limit(int k) { return k == JK_CONE || k == JK_TWIST; }
+
+// Static joint description (PhysicsEngine::add*Constraint): anchors are the
+// tracked points relative to each body's centre of mass in its body frame;
+// axes in body space.
 struct JointStore {
     const int* b1;          // global body indices
     const int* b2;
-    const int* n;           // 3 or 5
+    const int* n;           // dofs of the row
+    const int* kind;        // JointKind
     const float4* p1;       // xyz anchor on body 1
     const float4* p2;
-    const float4* ax1;      // hinge axis (body 1 space)
+    const float4* ax1;      // hinge / slider axis, cone direction, twist axis (body 1 space)
     const float4* ax2;
     const float2* hard;     // pos / rot correction strength
-    float* impulse;         // [5] per joint: persistent warm-start impulse
-    float4* u;              // hinge basis of the last rebuild (HingeConstraint::u / w)
+    const float4* par;      // x: distance target or limit max angle, y: twist min angle
+    const float4* ul;       // twist: body 1's u axis (body space)
+    const float4* wl;       //        and w axis
+    float* impulse;         // [kJMax] per joint: persistent warm-start impulse
+    float4* u;              // hinge / slider / sliding-hinge basis of the last rebuild
     float4* w;
+    float* angle;           // twist: current angle, unwrapped across rebuilds
+    int* active;            // limits: 1 when the last rebuild found the limit reached
     JointRow* rows;
+};
+
+// Springs (PhysicsEngine::addSpring, PhysicsEngine.cpp:974-998): impulse
+// pairs at the start of every substep, per world in the reference's order
+// (node-map order, each edge once, the edge's springs in creation order).
+struct SpringStore {
+    int n;
+    const int* b1;          // global body indices
+    const int* b2;
+    const float4* p1;       // tracked points (body frame, relative to the centre of mass)
+    const float4* p2;
+    const float4* par;      // damping, stiffness, resting length
+    const int* world_start; // [n_worlds + 1] ranges in that order
 };
 
 // Joint edges (SharedConstraintsEdge with joints) sorted by key, per world;
 // their joints in insertion order; the holonomic system of the edge (or -1).
 struct JointEdgeStore {
     const uint64_t* key;    // (global a) << 32 | global b, a < b
-    const int* jstart;
-    const int* jcount;
+    const int* jstart;      // the edge's joints: jlist[jstart .. jstart + jcount)
+    const int* jcount;      // 0 for an edge that holds only springs
+    const int* jlist;       // joint indices, each edge's in creation order
     const int* sys;
     const int* world_start; // [n_worlds + 1] joint-edge ranges
     const int* world_jstart;// [n_worlds + 1] joint ranges (row-slot offsets)
@@ -320,6 +356,24 @@ struct Dev {
     const int* hs_world_start;     // [n_worlds + 1] holonomic system ranges (island lists)
     float lin_err_threshold;       // excessive_linear_error_torque_threshold
     float4* dv_err;                // 4 float4 per island body: linearisation-error probe
+    SpringStore sp;                // springs (sp.n == 0: none in the batch)
+    // polls of a bounded mbarrier wait before a kernel gives up and reports
+    // ST_TIMEOUT (kDefaultWaitLimit; CPGPU_WAIT_LIMIT lowers it so that a test
+    // can make the waits run out without a fault).  The drain of a giving-up
+    // warp's own copies always uses kDefaultWaitLimit.
+    long long wait_limit;
+    // FP64 audit (audit.cu), null when disabled: kAuditValues doubles per world
+    double* audit;
+    // islands with at least this many rows take the warp-per-island solver,
+    // the others the thread-per-island one (a schedule choice: same results)
+    int big_rows;
 };
+
+// per world: linear momentum xyz, angular momentum about the origin xyz,
+// kinetic energy, potential energy, largest one-step increase of their sum
+// since the audit was enabled, steps audited
+constexpr int kAuditValues = 10;
+
+constexpr long long kDefaultWaitLimit = 1LL << 24;
 
 }  // namespace cpgpu

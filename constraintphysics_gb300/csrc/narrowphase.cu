@@ -28,7 +28,6 @@ constexpr float kSinTol = (float)0.017452406437283512;   // sin(1 deg)
 constexpr int kMaxClip = 40;
 constexpr int kQueue = 64;                       // queued edge-edge axes per warp
 constexpr int kQueueBytes = kQueue * (16 + 4);
-constexpr long long kSpinLimit = 1LL << 24;  // bounded mbarrier wait
 constexpr int kMeshBlocksPerSm = 2;          // mesh-pair kernel grid (its scratch is per warp)
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -50,8 +49,10 @@ __device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (long long it = 0; it < kSpinLimit; it++) {
+// bounded mbarrier wait: `limit` polls (Dev::wait_limit; kDefaultWaitLimit
+// when draining a giving-up warp's own copies)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit) {
+    for (long long it = 0; it < limit; it++) {
         uint32_t done;
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
@@ -353,7 +354,9 @@ __device__ __forceinline__ bool jointed(const Dev& d, int a, int b) {
         int m = (lo + hi) >> 1;
         if (d.je.key[m] < k) lo = m + 1; else hi = m;
     }
-    return lo < d.n_joint_edges && d.je.key[lo] == k;
+    // a pair joined only by springs still collides (addSpring adds no
+    // collision exception, PhysicsEngine.cpp:974-998)
+    return lo < d.n_joint_edges && d.je.key[lo] == k && d.je.jcount[lo] > 0;
 }
 
 // cull_manifold (CollisionDetect.cpp:2795-2830) to at most 4 points and write
@@ -1511,6 +1514,7 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
     if (lane == 0) mbar_init(&bars[wib]);
     __syncthreads();
     uint32_t parity = 0;
+    bool failed = false;
     const int n_pairs = *d.n_pairs;
     for (int p = blockIdx.x * warps_per_block + wib; p < n_pairs; p += gridDim.x * warps_per_block) {
         const int a = d.pair_a[p], b = d.pair_b[p];
@@ -1519,8 +1523,10 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
         // pairs with a sphere or cylinder belong to k_narrow_prim
         if ((reinterpret_cast<const HullHeader*>(ga)->kind | reinterpret_cast<const HullHeader*>(gb)->kind) != SHAPE_HULL) continue;
         // collision filter of PhysicsEngine.cpp:174 (at least one dynamic body)
-        // and collisionAllowed
-        if (!(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
+        // and collisionAllowed; after a timed-out wait the warp writes empty
+        // manifolds for the rest of its pairs, so no later kernel reads a
+        // previous step's
+        if (failed || !(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
             if (lane == 0) { d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f); d.mf_cnt[p] = 0; }
             continue;
         }
@@ -1536,13 +1542,14 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
             bulk_load(sa, ga, hot_a, &bars[wib]);
             bulk_load(sb, gb, hot_b, &bars[wib]);
         }
-        bool ok = mbar_wait(&bars[wib], parity);
+        bool ok = mbar_wait(&bars[wib], parity, d.wait_limit);
         parity ^= 1u;
         if (!__all_sync(0xffffffffu, ok)) {
             if (lane == 0) { atomicOr(d.status, ST_TIMEOUT); d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f); d.mf_cnt[p] = 0; }
-            // give the copies in flight one more bounded wait, then stop using the slot
-            mbar_wait(&bars[wib], parity ^ 1u);
-            return;
+            // let the copies in flight land (bounded), then stop using the slot
+            mbar_wait(&bars[wib], parity ^ 1u, kDefaultWaitLimit);
+            failed = true;
+            continue;
         }
         HullView A, B;
         stage_hull(ga, sa, d.pos[a], d.rot[a], &A, lane);
@@ -1709,6 +1716,7 @@ __global__ void __launch_bounds__(256, 1) k_narrow_prim(Dev d, int slot_bytes) {
     if (lane == 0) mbar_init(&bars[wib]);
     __syncthreads();
     uint32_t parity = 0;
+    bool failed = false;
     Scratch scratch;
     CP clipped[kMaxClip];
     const int n_pairs = *d.n_pairs;
@@ -1720,7 +1728,7 @@ __global__ void __launch_bounds__(256, 1) k_narrow_prim(Dev d, int slot_bytes) {
         const HullHeader* Hb = reinterpret_cast<const HullHeader*>(gb);
         const uint32_t ka = Ha->kind, kb = Hb->kind;
         if ((ka | kb) == SHAPE_HULL || ka == SHAPE_MESH || kb == SHAPE_MESH) continue;
-        if (!(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
+        if (failed || !(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
             if (lane == 0) no_manifold(d, p);
             continue;
         }
@@ -1734,12 +1742,13 @@ __global__ void __launch_bounds__(256, 1) k_narrow_prim(Dev d, int slot_bytes) {
             bulk_load(sa, ga, hot_a, &bars[wib]);
             bulk_load(sb, gb, hot_b, &bars[wib]);
         }
-        bool ok = mbar_wait(&bars[wib], parity);
+        bool ok = mbar_wait(&bars[wib], parity, d.wait_limit);
         parity ^= 1u;
         if (!__all_sync(0xffffffffu, ok)) {
             if (lane == 0) { atomicOr(d.status, ST_TIMEOUT); no_manifold(d, p); }
-            mbar_wait(&bars[wib], parity ^ 1u);
-            return;
+            mbar_wait(&bars[wib], parity ^ 1u, kDefaultWaitLimit);
+            failed = true;
+            continue;
         }
         narrow_prim(d, p, a, b, sa, sb, ga, gb, ka, kb, lane, scratch, clipped);
     }
@@ -1767,6 +1776,7 @@ __global__ void __launch_bounds__(256) k_narrow_mesh(Dev d, int slot_bytes) {
     if (gw >= d.mesh_warps) return;
     MeshScratch& S = d.msc[gw];
     uint32_t parity = 0;
+    bool failed = false;
     Scratch scratch;
     CP clipped[kMaxClip];
     const int n_pairs = *d.n_pairs;
@@ -1777,7 +1787,7 @@ __global__ void __launch_bounds__(256) k_narrow_mesh(Dev d, int slot_bytes) {
         const uint32_t ka = reinterpret_cast<const HullHeader*>(ga)->kind, kb = reinterpret_cast<const HullHeader*>(gb)->kind;
         if (lane == 0) d.mf_ofs[p] = -1;
         if (ka != SHAPE_MESH && kb != SHAPE_MESH) continue;
-        if ((ka == SHAPE_MESH && kb == SHAPE_MESH) || !(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
+        if (failed || (ka == SHAPE_MESH && kb == SHAPE_MESH) || !(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
             if (lane == 0) no_manifold(d, p);
             continue;
         }
@@ -1793,12 +1803,13 @@ __global__ void __launch_bounds__(256) k_narrow_mesh(Dev d, int slot_bytes) {
             mbar_expect(&bars[wib], hot);
             bulk_load(slot, gc, hot, &bars[wib]);
         }
-        bool ok = mbar_wait(&bars[wib], parity);
+        bool ok = mbar_wait(&bars[wib], parity, d.wait_limit);
         parity ^= 1u;
         if (!__all_sync(0xffffffffu, ok)) {
             if (lane == 0) { atomicOr(d.status, ST_TIMEOUT); no_manifold(d, p); }
-            mbar_wait(&bars[wib], parity ^ 1u);
-            return;
+            mbar_wait(&bars[wib], parity ^ 1u, kDefaultWaitLimit);
+            failed = true;
+            continue;
         }
         HullView hv;
         PrimView pv;

@@ -17,6 +17,7 @@
 // order, ids 1-based.
 #include <cstdio>
 #include <mutex>
+#include <vector>
 
 #include "kernels.cuh"
 
@@ -88,29 +89,60 @@ __global__ void k_na_write(const float* aabbs, int n, const int* scratch, uint32
         int o = scratch[i] + scratch[kNoAllocMaxBodies + i / kNoAllocChunk];
         for (int j = i + 1; j < n; j++) {
             if (overlap6(a, aabbs + 6 * j)) {
-                if (o < cap) { pairs[2 * o] = (uint32_t)i + 1; pairs[2 * o + 1] = (uint32_t)j + 1; }
+                if (o < cap) { pairs[2 * (size_t)o] = (uint32_t)i + 1; pairs[2 * (size_t)o + 1] = (uint32_t)j + 1; }
                 o++;
             }
         }
     }
 }
 
-// device address of the scratch array, looked up once per device with that
-// device current (host code must not use the symbol itself as a pointer)
+// Device address of the scratch array, looked up with the device current
+// (host code must not use the symbol itself as a pointer).  The address is
+// cached per CUDA context, identified by the driver's context id, so that a
+// caller who resets the device (a new primary context, the module loaded
+// again) gets the new address instead of a stale one.  If the driver entry
+// points for the context id are unavailable, the address is looked up again
+// on every call.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+struct NaCache { unsigned long long ctx_id; int* ptr; };
 std::mutex g_na_mutex;
-int* g_na_ptr[64] = {nullptr};
+std::vector<NaCache> g_na_cache;
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+bool g_ctx_fns_looked_up = false;
+
+bool current_context_id(unsigned long long* id) {
+    if (!g_ctx_fns_looked_up) {
+        g_ctx_fns_looked_up = true;
+        cudaDriverEntryPointQueryResult q1, q2;
+        void *f1 = nullptr, *f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess && f1 && f2) {
+            g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+            g_ctx_id = reinterpret_cast<CtxGetIdFn>(f2);
+        }
+    }
+    if (!g_ctx_current || !g_ctx_id) return false;
+    void* ctx = nullptr;
+    if (g_ctx_current(&ctx) != 0 || !ctx) return false;
+    return g_ctx_id(ctx, id) == 0;
+}
 
 int scratch_for_current_device(int** out) {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return CPGPU_ERR_NO_DEVICE;
+    if (cudaGetDevice(&dev) != cudaSuccess) return CPGPU_ERR_NO_DEVICE;
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return CPGPU_ERR_CUDA;
-        g_na_ptr[dev] = static_cast<int*>(p);
-    }
-    *out = g_na_ptr[dev];
+    unsigned long long id = 0;
+    if (current_context_id(&id))
+        for (const NaCache& c : g_na_cache)
+            if (c.ctx_id == id) { *out = c.ptr; return CPGPU_OK; }
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return CPGPU_ERR_CUDA;
+    // the lookup made the device's primary context current if it was not
+    if (current_context_id(&id)) g_na_cache.push_back({id, static_cast<int*>(p)});
+    *out = static_cast<int*>(p);
     return CPGPU_OK;
 }
 
@@ -126,6 +158,16 @@ extern "C" int cpgpu_pairs_noalloc(const float* aabbs, int n_bodies, uint32_t* p
     if (n_bodies > kNoAllocMaxBodies) {
         set_last_error("cpgpu_pairs_noalloc: more than 65536 bodies (the fixed scratch holds one count per body)");
         return CPGPU_ERR_INVALID_ARG;
+    }
+    // an error left by earlier work on this thread is not ours to report or
+    // to clear: refuse to run and leave it pending for its owner
+    cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess) {
+        char msg[256];
+        std::snprintf(msg, sizeof msg, "cpgpu_pairs_noalloc: an earlier CUDA error is pending (%s); nothing launched",
+                      cudaGetErrorName(pending));
+        set_last_error(msg);
+        return CPGPU_ERR_CUDA;
     }
     int* scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);

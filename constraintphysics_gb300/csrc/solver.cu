@@ -55,40 +55,6 @@ __device__ __forceinline__ float dot6(const float* a, const float* b) {
     return s;
 }
 
-// row entries by component k (0..5: linear xyz, angular xyz) and friction
-// direction i (0: u, 1: w), over the split RowBlock layout
-__device__ __forceinline__ float& r_nja(RowBlock& R, int k) { return R.h[k / 3].nja[k % 3]; }
-__device__ __forceinline__ float& r_njb(RowBlock& R, int k) { return R.h[k / 3].njb[k % 3]; }
-__device__ __forceinline__ float& r_nita(RowBlock& R, int k) { return R.h[k / 3].nita[k % 3]; }
-__device__ __forceinline__ float& r_nitb(RowBlock& R, int k) { return R.h[k / 3].nitb[k % 3]; }
-__device__ __forceinline__ float& r_fja(RowBlock& R, int i, int k) { return i ? R.h[k / 3].fja1[k % 3] : R.h[k / 3].fja0[k % 3]; }
-__device__ __forceinline__ float& r_fjb(RowBlock& R, int i, int k) { return i ? R.h[k / 3].fjb1[k % 3] : R.h[k / 3].fjb0[k % 3]; }
-__device__ __forceinline__ float& r_fita(RowBlock& R, int i, int k) { return i ? R.h[k / 3].fita1[k % 3] : R.h[k / 3].fita0[k % 3]; }
-__device__ __forceinline__ float& r_fitb(RowBlock& R, int i, int k) { return i ? R.h[k / 3].fitb1[k % 3] : R.h[k / 3].fitb0[k % 3]; }
-__device__ __forceinline__ float c_nita(const RowBlock& R, int k) { return R.h[k / 3].nita[k % 3]; }
-__device__ __forceinline__ float c_nitb(const RowBlock& R, int k) { return R.h[k / 3].nitb[k % 3]; }
-__device__ __forceinline__ float c_fita(const RowBlock& R, int i, int k) { return i ? R.h[k / 3].fita1[k % 3] : R.h[k / 3].fita0[k % 3]; }
-__device__ __forceinline__ float c_fitb(const RowBlock& R, int i, int k) { return i ? R.h[k / 3].fitb1[k % 3] : R.h[k / 3].fitb0[k % 3]; }
-// six-term dot product as a tree of pairs (three levels of dependent
-// operations instead of six: the solver's serial chain runs through these)
-__device__ __forceinline__ float tdot6(float a0, float a1, float a2, float a3, float a4, float a5, const float* v) {
-    return (a0 * v[0] + a1 * v[1]) + (a2 * v[2] + a3 * v[3]) + (a4 * v[4] + a5 * v[5]);
-}
-// J_a v_a + J_b v_b of the normal row / friction row i
-__device__ __forceinline__ float jn_dot(const RowBlock& R, const float* va, const float* vb) {
-    const RowHalf &l = R.h[0], &w = R.h[1];
-    return tdot6(l.nja[0], l.nja[1], l.nja[2], w.nja[0], w.nja[1], w.nja[2], va) +
-           tdot6(l.njb[0], l.njb[1], l.njb[2], w.njb[0], w.njb[1], w.njb[2], vb);
-}
-__device__ __forceinline__ float jf_dot(const RowBlock& R, int i, const float* va, const float* vb) {
-    const RowHalf &l = R.h[0], &w = R.h[1];
-    if (i == 0)
-        return tdot6(l.fja0[0], l.fja0[1], l.fja0[2], w.fja0[0], w.fja0[1], w.fja0[2], va) +
-               tdot6(l.fjb0[0], l.fjb0[1], l.fjb0[2], w.fjb0[0], w.fjb0[1], w.fjb0[2], vb);
-    return tdot6(l.fja1[0], l.fja1[1], l.fja1[2], w.fja1[0], w.fja1[1], w.fja1[2], va) +
-           tdot6(l.fjb1[0], l.fjb1[1], l.fjb1[2], w.fjb1[0], w.fjb1[1], w.fjb1[2], vb);
-}
-
 __device__ __forceinline__ void body_vel(const Dev& d, int g, float* out) {
     if (d.movement[g] == 1) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
     float4 v = d.vel[g], w = d.angv[g];
@@ -139,7 +105,7 @@ __global__ void k_rows(Dev d, int first, int last) {
             it_of(ima, Ia, ja, ia);
             it_of(imb, Ib, jb, ib);
             float itv = dot6(ja, ia) + dot6(jb, ib);
-            for (int k = 0; k < 6; k++) { r_nja(R, k) = ja[k]; r_njb(R, k) = jb[k]; r_nita(R, k) = ia[k]; r_nitb(R, k) = ib[k]; }
+            for (int k = 0; k < 6; k++) { R.nja[k] = ja[k]; R.njb[k] = jb[k]; R.nita[k] = ia[k]; R.nitb[k] = ib[k]; }
             R.nminv = 1.0f / (itv * (1.0f + P.cfm));
             R.nptarget = fmaxf(0.0f, depth - 0.05f) * pcc;
             // friction rows in the tangent basis of n, warm impulse re-projected
@@ -171,14 +137,12 @@ __global__ void k_rows(Dev d, int first, int last) {
             fv[3] *= (1.0f + P.cfm);
             float di = 1.0f / (fv[0] * fv[3] - fv[1] * fv[2]);
             R.fminv[0] = fv[3] * di; R.fminv[1] = -fv[1] * di; R.fminv[2] = -fv[2] * di; R.fminv[3] = fv[0] * di;
-            R.kf0 = tdot6(fja[0], fja[1], fja[2], fja[3], fja[4], fja[5], ia) + tdot6(fjb[0], fjb[1], fjb[2], fjb[3], fjb[4], fjb[5], ib);
-            R.kf1 = tdot6(fja[6], fja[7], fja[8], fja[9], fja[10], fja[11], ia) +
-                    tdot6(fjb[6], fjb[7], fjb[8], fjb[9], fjb[10], fjb[11], ib);
-            for (int i = 0; i < 2; i++)
-                for (int k = 0; k < 6; k++) {
-                    r_fja(R, i, k) = fja[6 * i + k]; r_fjb(R, i, k) = fjb[6 * i + k];
-                    r_fita(R, i, k) = fia[2 * k + i]; r_fitb(R, i, k) = fib[2 * k + i];
-                }
+            R.kf0 = dot6(fja, ia) + dot6(fjb, ib);
+            R.kf1 = dot6(fja + 6, ia) + dot6(fjb + 6, ib);
+            for (int k = 0; k < 6; k++) {
+                R.fja0[k] = fja[k]; R.fjb0[k] = fjb[k]; R.fja1[k] = fja[6 + k]; R.fjb1[k] = fjb[6 + k];
+                R.fita0[k] = fia[2 * k]; R.fitb0[k] = fib[2 * k]; R.fita1[k] = fia[2 * k + 1]; R.fitb1[k] = fib[2 * k + 1];
+            }
             // velocity targets from the bodies' velocities at the start of the
             // solve (ContactConstraint::findTargetConstraintValue,
             // ConstraintSolver.cpp:264-268; DegreedConstraint default, ConstraintSolver.h:78)
@@ -210,15 +174,56 @@ __global__ void k_rows(Dev d, int first, int last) {
     }
 }
 
-__device__ __forceinline__ void load_dv(const float4* dv, int slot, int which, float* out) {
-    if (slot < 0) { for (int k = 0; k < 6; k++) out[k] = 0.f; return; }
-    float4 l = dv[4 * slot + 2 * which], a = dv[4 * slot + 2 * which + 1];
-    out[0] = l.x; out[1] = l.y; out[2] = l.z; out[3] = a.x; out[4] = a.y; out[5] = a.z;
+// ---- packed FP32 pairs: a row's 6-vectors and a body's Δv are handled as
+// the three component pairs (x, y), (z, ax), (ay, az), two lanes of one
+// fma.rn.f32x2 each (half the instructions of scalar FP32 on the chain)
+struct P3 { float2 a, b, c; };
+__device__ __forceinline__ P3 p3(const float* f) {
+    return P3{make_float2(f[0], f[1]), make_float2(f[2], f[3]), make_float2(f[4], f[5])};
 }
-__device__ __forceinline__ void store_dv(float4* dv, int slot, int which, const float* v) {
+__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
+// J_a v_a + J_b v_b
+__device__ __forceinline__ float pdot(const P3& ja, const P3& va, const P3& jb, const P3& vb) {
+    float2 s = __fmul2_rn(ja.a, va.a);
+    s = __ffma2_rn(ja.b, va.b, s);
+    s = __ffma2_rn(ja.c, va.c, s);
+    float2 t = __fmul2_rn(jb.a, vb.a);
+    t = __ffma2_rn(jb.b, vb.b, t);
+    t = __ffma2_rn(jb.c, vb.c, t);
+    const float2 u = __fadd2_rn(s, t);
+    return u.x + u.y;
+}
+// v += x * s
+__device__ __forceinline__ void paxpy(P3& v, const P3& x, float2 s) {
+    v.a = __ffma2_rn(x.a, s, v.a);
+    v.b = __ffma2_rn(x.b, s, v.b);
+    v.c = __ffma2_rn(x.c, s, v.c);
+}
+
+// Δv of island body `slot`: which 0 = (v, w), 1 = (pv, pw); slot < 0 is a
+// body of infinite mass (always zero)
+__device__ __forceinline__ P3 dv_get(const float4* dv, int slot, int which) {
+    if (slot < 0) return P3{make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    const float4* s = dv + kDvF4 * slot;
+    if (which == 0) {
+        const float4 A = s[0];
+        const float2 B = reinterpret_cast<const float2*>(s + 1)[0];
+        return P3{make_float2(A.x, A.y), make_float2(A.z, A.w), B};
+    }
+    const float2 A = reinterpret_cast<const float2*>(s + 1)[1];
+    const float4 C = s[2];
+    return P3{A, make_float2(C.x, C.y), make_float2(C.z, C.w)};
+}
+__device__ __forceinline__ void dv_put(float4* dv, int slot, int which, const P3& v) {
     if (slot < 0) return;
-    dv[4 * slot + 2 * which] = make_float4(v[0], v[1], v[2], 0.f);
-    dv[4 * slot + 2 * which + 1] = make_float4(v[3], v[4], v[5], 0.f);
+    float4* s = dv + kDvF4 * slot;
+    if (which == 0) {
+        s[0] = make_float4(v.a.x, v.a.y, v.b.x, v.b.y);
+        reinterpret_cast<float2*>(s + 1)[0] = v.c;
+    } else {
+        reinterpret_cast<float2*>(s + 1)[1] = v.a;
+        s[2] = make_float4(v.b.x, v.b.y, v.c.x, v.c.y);
+    }
 }
 
 // ---- one row of each PGS pass (PGS_solve, ConstraintSolver.cpp:120-161) ----------
@@ -227,18 +232,19 @@ __device__ __forceinline__ void store_dv(float4* dv, int slot, int which, const 
 __device__ __forceinline__ void row_warm(const RowBlock& R, const float4 imp, float4* dv) {
     const bool wn = fabsf(imp.x) > kZero, wf = fabsf(imp.z) > kZero || fabsf(imp.w) > kZero;
     if (!wn && !wf) return;
-    float va[6], vb[6];
-    load_dv(dv, R.sa, 0, va);
-    load_dv(dv, R.sb, 0, vb);
-    if (wn)
-        for (int k = 0; k < 6; k++) { va[k] += c_nita(R, k) * imp.x; vb[k] += c_nitb(R, k) * imp.x; }
-    if (wf)
-        for (int k = 0; k < 6; k++) {
-            va[k] += imp.z * c_fita(R, 0, k) + imp.w * c_fita(R, 1, k);
-            vb[k] += imp.z * c_fitb(R, 0, k) + imp.w * c_fitb(R, 1, k);
-        }
-    store_dv(dv, R.sa, 0, va);
-    store_dv(dv, R.sb, 0, vb);
+    P3 va = dv_get(dv, R.sa, 0), vb = dv_get(dv, R.sb, 0);
+    if (wn) {
+        paxpy(va, p3(R.nita), bc2(imp.x));
+        paxpy(vb, p3(R.nitb), bc2(imp.x));
+    }
+    if (wf) {
+        paxpy(va, p3(R.fita0), bc2(imp.z));
+        paxpy(va, p3(R.fita1), bc2(imp.w));
+        paxpy(vb, p3(R.fitb0), bc2(imp.z));
+        paxpy(vb, p3(R.fitb1), bc2(imp.w));
+    }
+    dv_put(dv, R.sa, 0, va);
+    dv_put(dv, R.sb, 0, vb);
 }
 
 // velocity pass: normal row clamped at zero, then the friction rows projected on
@@ -251,11 +257,9 @@ __device__ __forceinline__ void row_warm(const RowBlock& R, const float4 imp, fl
 // of after it.  The disc projection compares squared magnitudes and scales by
 // rsqrt.
 __device__ __forceinline__ void row_vel(const RowBlock& R, float4& imp, int& stat, float4* dv) {
-    float va[6], vb[6];
-    load_dv(dv, R.sa, 0, va);
-    load_dv(dv, R.sb, 0, vb);
-    const float cur = jn_dot(R, va, vb);
-    const float b0 = jf_dot(R, 0, va, vb), b1 = jf_dot(R, 1, va, vb);
+    P3 va = dv_get(dv, R.sa, 0), vb = dv_get(dv, R.sb, 0);
+    const float cur = pdot(p3(R.nja), va, p3(R.njb), vb);
+    const float b0 = pdot(p3(R.fja0), va, p3(R.fjb0), vb), b1 = pdot(p3(R.fja1), va, p3(R.fjb1), vb);
     const float nw = imp.x + R.nminv * (R.tgt_n - cur);
     float diff = fmaxf(nw, 0.0f) - imp.x;
     if (!(fabsf(diff) > kZero)) diff = 0.f;
@@ -271,12 +275,15 @@ __device__ __forceinline__ void row_vel(const RowBlock& R, float4& imp, int& sta
     float e0 = n0 - imp.z, e1 = n1 - imp.w;
     if (!(fabsf(e0) > kZero || fabsf(e1) > kZero)) { e0 = 0.f; e1 = 0.f; }
     if (diff != 0.f || e0 != 0.f || e1 != 0.f) {
-        for (int k = 0; k < 6; k++) {
-            va[k] += c_nita(R, k) * diff + (c_fita(R, 0, k) * e0 + c_fita(R, 1, k) * e1);
-            vb[k] += c_nitb(R, k) * diff + (c_fitb(R, 0, k) * e0 + c_fitb(R, 1, k) * e1);
-        }
-        store_dv(dv, R.sa, 0, va);
-        store_dv(dv, R.sb, 0, vb);
+        const float2 sd = bc2(diff), s0 = bc2(e0), s1 = bc2(e1);
+        paxpy(va, p3(R.nita), sd);
+        paxpy(vb, p3(R.nitb), sd);
+        paxpy(va, p3(R.fita0), s0);
+        paxpy(vb, p3(R.fitb0), s0);
+        paxpy(va, p3(R.fita1), s1);
+        paxpy(vb, p3(R.fitb1), s1);
+        dv_put(dv, R.sa, 0, va);
+        dv_put(dv, R.sb, 0, vb);
     }
     imp.x = ix;
     imp.z += e0;
@@ -285,17 +292,16 @@ __device__ __forceinline__ void row_vel(const RowBlock& R, float4& imp, int& sta
 
 // pseudo-velocity (position correction) pass of the normal row
 __device__ __forceinline__ void row_pos(const RowBlock& R, float4& imp, float4* dv) {
-    float va[6], vb[6];
-    load_dv(dv, R.sa, 1, va);
-    load_dv(dv, R.sb, 1, vb);
-    float cur = jn_dot(R, va, vb);
-    float nw = imp.y + R.nminv * (R.nptarget - cur);
-    float diff = fmaxf(nw, 0.0f) - imp.y;
+    P3 va = dv_get(dv, R.sa, 1), vb = dv_get(dv, R.sb, 1);
+    const float cur = pdot(p3(R.nja), va, p3(R.njb), vb);
+    const float nw = imp.y + R.nminv * (R.nptarget - cur);
+    const float diff = fmaxf(nw, 0.0f) - imp.y;
     if (fabsf(diff) > kZero) {
-        for (int k = 0; k < 6; k++) { va[k] += c_nita(R, k) * diff; vb[k] += c_nitb(R, k) * diff; }
+        paxpy(va, p3(R.nita), bc2(diff));
+        paxpy(vb, p3(R.nitb), bc2(diff));
         imp.y += diff;
-        store_dv(dv, R.sa, 1, va);
-        store_dv(dv, R.sb, 1, vb);
+        dv_put(dv, R.sa, 1, va);
+        dv_put(dv, R.sb, 1, vb);
     }
 }
 
@@ -314,17 +320,18 @@ __device__ void island_finish(const Dev& d, int rs, int rc, int bs, int bc, cons
     for (int k = t; k < bc; k += nt) {
         int g = d.isl_bodies[bs + k];
         if (d.movement[g] != 0) continue;
-        float4 a = dv[4 * k], b = dv[4 * k + 1], c = dv[4 * k + 2], e = dv[4 * k + 3];
+        const float4 A = dv[kDvF4 * k], B = dv[kDvF4 * k + 1], C = dv[kDvF4 * k + 2];
         float4 v = d.vel[g], w = d.angv[g], pv = d.pvel[g], pw = d.pangv[g];
-        d.vel[g] = make_float4(v.x + a.x, v.y + a.y, v.z + a.z, 0.f);
-        d.angv[g] = make_float4(w.x + b.x, w.y + b.y, w.z + b.z, 0.f);
-        d.pvel[g] = make_float4(pv.x + c.x, pv.y + c.y, pv.z + c.z, 0.f);
-        d.pangv[g] = make_float4(pw.x + e.x, pw.y + e.y, pw.z + e.z, 0.f);
+        d.vel[g] = make_float4(v.x + A.x, v.y + A.y, v.z + A.z, 0.f);
+        d.angv[g] = make_float4(w.x + A.w, w.y + B.x, w.z + B.y, 0.f);
+        d.pvel[g] = make_float4(pv.x + B.z, pv.y + B.w, pv.z + C.x, 0.f);
+        d.pangv[g] = make_float4(pw.x + C.y, pw.y + C.z, pw.z + C.w, 0.f);
     }
 }
 
-// ---- scheduling: islands with at least kBigRows rows get a warp each, largest first
-constexpr int kBigRows = 48;
+// ---- scheduling: islands with at least d.big_rows rows get a warp each,
+// largest first; the smaller ones a thread each (the two paths give identical
+// results, so the threshold is a pure schedule choice)
 
 __global__ void k_sched_reset(Dev d) {
     if (threadIdx.x < 96) d.sched[threadIdx.x] = 0;
@@ -335,9 +342,9 @@ __device__ __forceinline__ int size_bucket(int rows) { return 31 - __clz(rows); 
 __global__ void k_sched_count(Dev d) {
     const int ni = *d.n_islands;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
-        if (d.n_joints > 0 && d.g_isl_flags[i]) { d.joint_list[atomicAdd(&d.sched[3], 1)] = i; continue; }
+        if (d.n_joint_edges > 0 && d.g_isl_flags[i]) { d.joint_list[atomicAdd(&d.sched[3], 1)] = i; continue; }
         int rc = d.g_isl_row_count[i];
-        if (rc >= kBigRows) atomicAdd(&d.sched[32 + size_bucket(rc)], 1);
+        if (rc >= d.big_rows) atomicAdd(&d.sched[32 + size_bucket(rc)], 1);
         else d.small_list[atomicAdd(&d.sched[1], 1)] = i;
     }
 }
@@ -345,9 +352,9 @@ __global__ void k_sched_count(Dev d) {
 __global__ void k_sched_place(Dev d) {
     const int ni = *d.n_islands;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
-        if (d.n_joints > 0 && d.g_isl_flags[i]) continue;
+        if (d.n_joint_edges > 0 && d.g_isl_flags[i]) continue;
         int rc = d.g_isl_row_count[i];
-        if (rc < kBigRows) continue;
+        if (rc < d.big_rows) continue;
         int b = size_bucket(rc), off = 0;
         for (int k = 31; k > b; k--) off += d.sched[32 + k];   // larger buckets first
         d.big_list[off + atomicAdd(&d.sched[64 + b], 1)] = i;
@@ -367,8 +374,8 @@ __global__ void k_pgs_small(Dev d) {
         const int rs = d.g_isl_row_start[i], rc = d.g_isl_row_count[i];
         const int bs = d.g_isl_body_start[i], bc = d.g_isl_body_count[i];
         const WorldParams& P = d.wparams[d.g_isl_world[i]];
-        float4* dv = d.dv + 4 * (size_t)bs;
-        for (int k = 0; k < 4 * bc; k++) dv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4* dv = d.dv + kDvF4 * (size_t)bs;
+        for (int k = 0; k < kDvF4 * bc; k++) dv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int r = rs; r < rs + rc; r++) row_warm(d.rows[r], d.rows[r].imp, dv);
         for (int it = 0; it < P.pgs_vel; it++)
             for (int r = rs; r < rs + rc; r++) {
@@ -393,7 +400,6 @@ __global__ void k_pgs_small(Dev d) {
 // ---- large islands: one warp per island, rows streamed through shared memory
 constexpr int kRingSlots = 4;
 constexpr int kChunkRows = 16;
-constexpr long long kWaitLimit = 1LL << 24;
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 
@@ -410,8 +416,8 @@ __device__ __forceinline__ void ring_load(RowBlock* dst, const RowBlock* src, in
                  : "memory");
 }
 
-__device__ __forceinline__ bool ring_wait(uint64_t* bar, uint32_t parity) {
-    for (long long it = 0; it < kWaitLimit; it++) {
+__device__ __forceinline__ bool ring_wait(uint64_t* bar, uint32_t parity, long long limit) {
+    for (long long it = 0; it < limit; it++) {
         uint32_t done;
         asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
                      : "=r"(done) : "r"(saddr(bar)), "r"(parity) : "memory");
@@ -455,7 +461,15 @@ __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t
     for (int t = 0; t < ahead && t < total; t++) issue(t, -1);
     for (int t = 0; t < total; t++) {
         const int slot = t % kRingSlots, pass = t / nch, c = t % nch;
-        if (!ring_wait(&bars[slot], (phase >> slot) & 1u)) return false;
+        if (!ring_wait(&bars[slot], (phase >> slot) & 1u, d.wait_limit)) {
+            // gave up on chunk t: let the copies already issued (chunks t to
+            // t + ahead - 1) land before the ring is abandoned (bounded)
+            for (int u = t; u < t + ahead && u < total; u++) {
+                const int su = u % kRingSlots;
+                ring_wait(&bars[su], (phase >> su) & 1u, kDefaultWaitLimit);
+            }
+            return false;
+        }
         phase ^= 1u << slot;
         const int n = min(kChunkRows, rc - c * kChunkRows);
         const float4* rb = reinterpret_cast<const float4*>(ring + slot * kChunkRows);
@@ -530,17 +544,14 @@ __global__ void __launch_bounds__(32) k_pgs_big(Dev d, int dv_cap) {
         const int rs = d.g_isl_row_start[i], rc = d.g_isl_row_count[i];
         const int bs = d.g_isl_body_start[i], bc = d.g_isl_body_count[i];
         const WorldParams& P = d.wparams[d.g_isl_world[i]];
-        float4* dv = (bc <= dv_cap) ? sdv : d.dv + 4 * (size_t)bs;
-        for (int k = lane; k < 4 * bc; k += 32) dv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4* dv = (bc <= dv_cap) ? sdv : d.dv + kDvF4 * (size_t)bs;
+        for (int k = lane; k < kDvF4 * bc; k += 32) dv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         __syncwarp();
         bool ok = true;
         if (lane == 0) {
             ok = (bc <= dv_cap) ? big_chain(d, ring, bars, phase, sdv, rs, rc, P)
-                                : big_chain(d, ring, bars, phase, d.dv + 4 * (size_t)bs, rs, rc, P);
-            if (!ok) {
-                atomicOr(d.status, ST_TIMEOUT);
-                for (int k = 0; k < kRingSlots; k++) ring_wait(&bars[k], (phase >> k) & 1u);
-            }
+                                : big_chain(d, ring, bars, phase, d.dv + kDvF4 * (size_t)bs, rs, rc, P);
+            if (!ok) atomicOr(d.status, ST_TIMEOUT);
         }
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) return;
@@ -615,9 +626,9 @@ __global__ void __launch_bounds__(32) k_pgs_joint(Dev d, int first) {
         const int rs = d.g_isl_row_start[i], rc = d.g_isl_row_count[i];
         const int bs = d.g_isl_body_start[i], bc = d.g_isl_body_count[i];
         const WorldParams& P = d.wparams[d.g_isl_world[i]];
-        float4* dv = d.dv + 4 * (size_t)bs;
-        float4* err = d.dv_err + 4 * (size_t)bs;
-        for (int k = lane; k < 4 * bc; k += 32) { dv[k] = make_float4(0.f, 0.f, 0.f, 0.f); err[k] = dv[k]; }
+        float4* dv = d.dv + kDvF4 * (size_t)bs;
+        float4* err = d.dv_err + kDvF4 * (size_t)bs;
+        for (int k = lane; k < kDvF4 * bc; k += 32) { dv[k] = make_float4(0.f, 0.f, 0.f, 0.f); err[k] = dv[k]; }
         __syncwarp();
         if (lane == 0) {
             for (int r = rs; r < rs + rc; r++) {
@@ -800,7 +811,7 @@ void launch_rows(const Dev& d, int first, int last, const Launch& L) {
 }
 
 int pgs_big_smem_bytes(int dv_cap) {
-    return 64 + kRingSlots * kChunkRows * (int)sizeof(RowBlock) + dv_cap * 64;
+    return 64 + kRingSlots * kChunkRows * (int)sizeof(RowBlock) + dv_cap * 16 * kDvF4;
 }
 
 // blocks of k_pgs_big resident per SM for this Δv capacity (one chain each)
@@ -825,7 +836,7 @@ void launch_pgs_schedule(const Dev& d, const Launch& L) {
 }
 
 void launch_pgs_joint(const Dev& d, bool first, const Launch& L) {
-    if (d.n_joints == 0) return;
+    if (d.n_joint_edges == 0) return;
     k_pgs_joint<<<L.n_sms * 8, 32, 0, L.st>>>(d, first ? 1 : 0);
 }
 

@@ -507,6 +507,18 @@ class HullPool:
         return pts * rng.uniform(0.5, 1.5), faces
 
 
+# Vertical placement of the pyramid boxes: the lowest layer starts PYR_LIFT
+# above the plate and the layers PYR_PITCH apart (box height 1 m).  The values
+# keep every first touch away from a step boundary: a body falling from rest
+# under g = 6 m/s^2 with dt = 1/60 s covers 0.00167, 0.005, 0.01, ... m after
+# 1, 2, 3, ... steps, so a gap of exactly 0.005 m (the earlier 0.005 m lift
+# and 1.01 m pitch) made every layer touch down with zero depth at step 2,
+# and whether the contact exists that step was decided by rounding (in FP64
+# as much as in FP32), shifting whole pyramids by one step of fall.
+PYR_LIFT = 0.0043
+PYR_PITCH = 1.0087
+
+
 def batched_world(rng, pool, nmin=8, nmax=512, gap=0.05):
     """One world of the batched workload (log-uniform body count)."""
     n = int(math.floor(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
@@ -526,7 +538,7 @@ def batched_world(rng, pool, nmin=8, nmax=512, gap=0.05):
                     for z in range(side):
                         if placed >= n:
                             break
-                        corner = (x * pitch - off + shift, layer * 1.01 + 0.005, z * pitch - off)
+                        corner = (x * pitch - off + shift, layer * PYR_PITCH + PYR_LIFT, z * pitch - off)
                         sc.box((0.0, 0.0, 0.0), 1.0, 1.0, 1.0, PILE_MATERIAL, DYNAMIC, corner)
                         placed += 1
             pyr += 1
@@ -555,3 +567,126 @@ def batched_worlds(seed=0, n_worlds=4096, nmin=8, nmax=512):
     rng = np.random.default_rng(seed)
     pool = HullPool(seed)
     return [batched_world(rng, pool, nmin, nmax) for _ in range(n_worlds)]
+
+
+# ---- joint scenes: one kind of joint (or spring) each, engine settings of 4
+# substeps and PGS (10, 1, holo); used by the restatement's pinning tests and
+# the device's parity tests
+JOINT_PARAMS = dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False)
+_TURN_Z10 = (0.9961946980917455, 0.0, 0.0, 0.08715574274765817)   # 10 degrees about z
+
+
+def distance_chain(mixed=False):
+    """A hanging chain of spheres linked by distance joints (or alternating
+    distance and ball-socket joints: one holonomic system), hit by a box."""
+    M = PILE_MATERIAL
+    sc = Scene("distance_chain", JOINT_PARAMS)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, FIXED, (0.0, 8.0, 0.0))
+    for i in range(6):
+        b = sc.sphere((0, 0, 0), 0.25, M, DYNAMIC, (0.9 * (i + 1), 8.0, 0.0))
+        if mixed and i % 2 == 1:
+            sc.ball_socket(prev, b, (0.45, 0, 0), (-0.45, 0, 0))
+        else:
+            sc.distance(prev, b, (0.25, 0, 0), (-0.25, 0, 0))
+        prev = b
+    # dropped from 0.513 m: a free fall covers g dt^2 n (n + 1) / 2 in n
+    # steps, and 0.5 m (n = 24) would touch down exactly at a step boundary
+    sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, M, DYNAMIC, (2.0, 1.013, 0.3))
+    return sc
+
+
+def weld_cantilever(mixed=False):
+    """A cantilever of boxes welded to a fixed post, one link turned so the
+    orientation correction acts (or every other weld a hinge: one holonomic
+    system of 6- and 5-dof blocks), hit by a falling box."""
+    M = PILE_MATERIAL
+    sc = Scene("weld_cantilever", JOINT_PARAMS)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, FIXED, (0.0, 4.0, 0.0))
+    for i in range(5):
+        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, DYNAMIC, (0.6 * (i + 1), 4.0, 0.0))
+        if i == 2:
+            sc.orient(b, _TURN_Z10)
+        if mixed and i % 2 == 1:
+            sc.hinge(prev, b, (0.3, 0, 0), (-0.3, 0, 0), (0, 0, 1), (0, 0, 1))
+        else:
+            sc.weld(prev, b, (0.3, 0, 0), (-0.3, 0, 0))
+        prev = b
+    sc.box((-0.3, -0.3, -0.3), 0.6, 0.6, 0.6, M, DYNAMIC, (2.4, 6.0, 0.1))
+    return sc
+
+
+def slider_chain(kinds=("slider",) * 4):
+    """Boxes hung from a fixed post by slider / sliding-hinge (/ hinge) joints
+    on tilted axes, one link turned, hit by a falling box."""
+    M = PILE_MATERIAL
+    sc = Scene("slider_chain", JOINT_PARAMS)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, FIXED, (0.0, 4.0, 0.0))
+    axes = [(1.0, -0.4, 0.2), (0.3, -1.0, 0.0), (1.0, 0.2, -0.5), (0.0, -1.0, 0.4)]
+    for i, kind in enumerate(kinds):
+        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, DYNAMIC, (0.6 * (i + 1), 4.0, 0.0))
+        if i == 1:
+            sc.orient(b, _TURN_Z10)
+        getattr(sc, kind)(prev, b, (0.3, 0, 0), (-0.3, 0, 0), axes[i], axes[i])
+        prev = b
+    sc.box((-0.3, -0.3, -0.3), 0.6, 0.6, 0.6, M, DYNAMIC, (1.8, 6.0, 0.1))
+    return sc
+
+
+def spring_chain(with_joints=False):
+    """Boxes hung from a fixed post on damped springs (two sharing a body, one
+    at its creation length), bouncing on the ground and off each other, or
+    sharing bodies with a ball-socket joint."""
+    M = PILE_MATERIAL
+    sc = Scene("spring_chain", JOINT_PARAMS)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, FIXED)
+    post = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, FIXED, (0.0, 4.0, 0.0))
+    prev = post
+    for i in range(4):
+        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, DYNAMIC, (0.4 * (i + 1), 3.2 - 0.7 * i, 0.1 * i))
+        if with_joints and i == 2:
+            sc.ball_socket(prev, b, (0.2, -0.35, 0.05), (-0.2, 0.35, -0.05))
+        else:
+            sc.spring(prev, b, (0.1, -0.25, 0.0), (0.0, 0.25, 0.1), 2.0 + i, 300.0 + 100.0 * i, 0.6 if i % 2 else -1.0)
+        prev = b
+    sc.spring(post, prev, (0.25, 0.0, 0.0), (0.0, 0.0, 0.25), 5.0, 80.0, 1.0)
+    return sc
+
+
+def cone_chain(holo=1, rot_strength=15000.0):
+    """A ball-socket chain swung sideways with a 25-degree cone limit on each
+    joint (holo = 0: without the holonomic block solve).  The limit rows'
+    position correction is the raw strength times the error (not scaled by
+    the step), so the default strength corrects violently once a limit is
+    passed; a small strength keeps the motion smooth."""
+    M = PILE_MATERIAL
+    sc = Scene("cone_chain", dict(JOINT_PARAMS, pgs=(10, 1, holo)))
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, FIXED, (0.0, 6.0, 0.0))
+    for i in range(4):
+        b = sc.box((-0.15, -0.4, -0.15), 0.3, 0.8, 0.3, M, DYNAMIC, (0.0, 5.2 - 1.0 * i, 0.0))
+        sc.ball_socket(prev, b, (0.0, -0.5 if i else -0.25, 0.0), (0.0, 0.5, 0.0))
+        sc.cone_limit(prev, b, (0.0, -1.0, 0.0), (0.0, -1.0, 0.0), 25.0 * math.pi / 180.0, rot_strength)
+        prev = b
+    sc.velocity(prev, (6.0, 0.0, 2.0))
+    return sc
+
+
+def twist_chain(rot_strength=15000.0):
+    """Twist limits beside cone limits on a ball-socket chain spun about its
+    axis (strength: as for cone_chain)."""
+    M = PILE_MATERIAL
+    sc = Scene("twist_chain", JOINT_PARAMS)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, FIXED, (0.0, 6.0, 0.0))
+    for i in range(3):
+        b = sc.box((-0.3, -0.4, -0.1), 0.6, 0.8, 0.2, M, DYNAMIC, (0.0, 5.2 - 1.0 * i, 0.0))
+        sc.ball_socket(prev, b, (0.0, -0.5 if i else -0.25, 0.0), (0.0, 0.5, 0.0))
+        sc.cone_limit(prev, b, (0.0, -1.0, 0.0), (0.0, -1.0, 0.0), 20.0 * math.pi / 180.0, rot_strength)
+        sc.twist_limit(prev, b, (0.0, -1.0, 0.0), (0.0, -1.0, 0.0), -0.3, 0.5, rot_strength)
+        prev = b
+    sc.ang_velocity(prev, (0.5, 9.0, 0.0))
+    sc.velocity(prev, (2.0, 0.0, 0.0))
+    return sc

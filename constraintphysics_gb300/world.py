@@ -310,19 +310,22 @@ class World:
         return contacts_to_numpy(arr, n.value)
 
     def joint_state(self):
-        """Warm-start impulses (n x 5) and hinge bases u, w (n x 3) of the
-        joints in creation order."""
+        """Warm-start state of the joints in creation order: impulses (n x 6),
+        tangent bases u, w (n x 3), and aux (n x 2: a twist limit's angle, and
+        1 when a cone or twist limit was reached at the last rebuild)."""
         n = C.c_int()
-        self._check(self.abi.get_joint_state(self.h, None, None, None, C.addressof(n)))
-        imp, u, w = np.zeros((n.value, 5)), np.zeros((n.value, 3)), np.zeros((n.value, 3))
-        self._check(self.abi.get_joint_state(self.h, _ptr(imp), _ptr(u), _ptr(w), C.addressof(n)))
-        return {"impulse": imp, "u": u, "w": w}
+        self._check(self.abi.get_joint_state(self.h, None, None, None, None, C.addressof(n)))
+        imp, u, w = np.zeros((n.value, 6)), np.zeros((n.value, 3)), np.zeros((n.value, 3))
+        aux = np.zeros((n.value, 2))
+        self._check(self.abi.get_joint_state(self.h, _ptr(imp), _ptr(u), _ptr(w), _ptr(aux), C.addressof(n)))
+        return {"impulse": imp, "u": u, "w": w, "aux": aux}
 
     def set_joint_state(self, st):
         imp = np.ascontiguousarray(st["impulse"], dtype=np.float64)
         u = np.ascontiguousarray(st["u"], dtype=np.float64)
         w = np.ascontiguousarray(st["w"], dtype=np.float64)
-        self._check(self.abi.set_joint_state(self.h, _ptr(imp), _ptr(u), _ptr(w), int(imp.shape[0])))
+        aux = np.ascontiguousarray(st["aux"], dtype=np.float64) if "aux" in st else None
+        self._check(self.abi.set_joint_state(self.h, _ptr(imp), _ptr(u), _ptr(w), _ptr(aux), int(imp.shape[0])))
 
     def set_contacts(self, cts):
         arr = numpy_to_contacts(cts)

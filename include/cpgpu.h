@@ -182,52 +182,45 @@ int cpgpu_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2,
                           double pos_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addDistanceConstraint (PhysicsEngine.cpp:623-660): the
  * attachment points stay `target_distance` apart (-1: their distance at
- * creation); DistanceConstraint rows (ConstraintSolver.cpp:348-377).  Not on
- * the device path yet: returns CPGPU_ERR_UNSUPPORTED there. */
+ * creation); DistanceConstraint rows (ConstraintSolver.cpp:348-377). */
 int cpgpu_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2,
                        const double b1_attach_local[3], const double b2_attach_local[3],
                        double target_distance, double pos_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addWeldConstraint (PhysicsEngine.cpp:892-915): the two
  * bodies move as one about the attachment points; WeldConstraint rows
- * (ConstraintSolver.cpp:861-899).  Not on the device path yet: returns
- * CPGPU_ERR_UNSUPPORTED there. */
+ * (ConstraintSolver.cpp:861-899). */
 int cpgpu_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2,
                    const double b1_attach_local[3], const double b2_attach_local[3],
                    double pos_correct_strength, double rot_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addTwistLimitConstraint (PhysicsEngine.cpp:948-972): the
  * twist of body 2 about the axes stays within [min_angle, max_angle];
- * TwistLimitConstraint row (ConstraintSolver.cpp:439-466).  Not on the
- * device path yet: returns CPGPU_ERR_UNSUPPORTED there. */
+ * TwistLimitConstraint row (ConstraintSolver.cpp:439-466). */
 int cpgpu_add_twist_limit(cpgpu_world* w, uint32_t b1, uint32_t b2,
                           const double b1_twist_axis_local[3], const double b2_twist_axis_local[3],
                           double min_angle, double max_angle, double rot_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addConeLimitConstraint (PhysicsEngine.cpp:922-946): the
  * angle between the bodies' direction vectors (body space) stays below
- * max_angle (< pi); ConeLimitConstraint row (ConstraintSolver.cpp:410-436).
- * Not on the device path yet: returns CPGPU_ERR_UNSUPPORTED there. */
+ * max_angle (< pi); ConeLimitConstraint row (ConstraintSolver.cpp:410-436). */
 int cpgpu_add_cone_limit(cpgpu_world* w, uint32_t b1, uint32_t b2,
                          const double b1_cone_direction_local[3], const double b2_cone_direction_local[3],
                          double max_angle, double rot_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addSpring (PhysicsEngine.cpp:974-998): a damped spring
  * between the attachment points (resting_length < 0: their distance at
  * creation), applied as impulses at the start of every substep
- * (PhysicsEngine.cpp:1313-1356).  Not on the device path yet: returns
- * CPGPU_ERR_UNSUPPORTED there. */
+ * (PhysicsEngine.cpp:1313-1356). */
 int cpgpu_add_spring(cpgpu_world* w, uint32_t b1, uint32_t b2,
                      const double b1_attach_local[3], const double b2_attach_local[3],
                      double damping, double stiffness, double resting_length, uint32_t* out_id);
 /* PhysicsEngine::addSliderConstraint (PhysicsEngine.cpp:769-806): body 2
  * slides along body 1's axis without turning; SliderConstraint rows
- * (ConstraintSolver.cpp:611-696).  Not on the device path yet: returns
- * CPGPU_ERR_UNSUPPORTED there. */
+ * (ConstraintSolver.cpp:611-696). */
 int cpgpu_add_slider(cpgpu_world* w, uint32_t b1, uint32_t b2,
                      const double b1_slider_pos_local[3], const double b2_slider_pos_local[3],
                      const double b1_slider_axis_local[3], const double b2_slider_axis_local[3],
                      double pos_correct_strength, double rot_correct_strength, uint32_t* out_id);
 /* PhysicsEngine::addSlidingHingeConstraint (PhysicsEngine.cpp:856-890): body
  * 2 slides along and turns about the shared axis; SlidingHingeConstraint rows
- * (ConstraintSolver.cpp:781-852).  Not on the device path yet: returns
- * CPGPU_ERR_UNSUPPORTED there. */
+ * (ConstraintSolver.cpp:781-852). */
 int cpgpu_add_sliding_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2,
                             const double b1_slider_pos_local[3], const double b2_slider_pos_local[3],
                             const double b1_slider_axis_local[3], const double b2_slider_axis_local[3],
@@ -278,20 +271,44 @@ int cpgpu_set_contacts(cpgpu_world* w, const cpgpu_contact* in, int n);
 int cpgpu_raycast(cpgpu_world* w, const double* origins, const double* dirs, int n_rays,
                   const uint32_t* ignore, int n_ignore, uint32_t* hit_body,
                   double* hit_pos, double* hit_normal, double* hit_dist);
-/* Warm-start state of the joints in creation order (the impulse of each
- * BallSocketConstraint / HingeConstraint, PersistentConstraint.h:118-313, and
- * a hinge's tangent basis u, w of its last rebuild): impulse 5 doubles per
- * joint (3 used by a ball-socket), u and w 3 doubles each.  With the body
- * state and the contacts this completes a checkpoint; no counterpart in the
- * reference, which keeps these inside its constraint objects. */
-int cpgpu_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv, int* n);
-int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u, const double* wv, int n);
+/* Warm-start state of the joints (not the springs) in creation order: the
+ * impulse of each constraint row (PersistentConstraint.h:90-420), 6 doubles
+ * per joint (ball-socket 3 used, sliding hinge 4, hinge and slider 5, weld 6,
+ * distance and limits 1); the tangent basis u, w of its last rebuild (hinge,
+ * slider, sliding hinge; 3 doubles each); and `aux`, 2 doubles per joint: a
+ * twist limit's current angle (unwrapped across rebuilds) and, for a cone or
+ * twist limit, 1 when its last rebuild found the limit reached (the row is
+ * then solved in the next step), else 0.  With the body state and the
+ * contacts this completes a checkpoint; no counterpart in the reference,
+ * which keeps these inside its constraint objects.  Any pointer but `n` may
+ * be NULL. */
+int cpgpu_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv, double* aux, int* n);
+int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u, const double* wv, const double* aux,
+                          int n);
 
 /* ---- batched worlds ----------------------------------------------------- */
 /* Pack independent worlds into one device batch (segmented arrays) that one
  * launch sequence per step advances.  The worlds keep their own state; the
  * batch starts from their current state and the substep count must agree. */
 int cpgpu_batch_create(cpgpu_world* const* worlds, int n_worlds, cpgpu_batch** out);
+/* The same, with the batch's schedule chosen by timing (no counterpart in the
+ * reference): candidate schedules -- one, two or three parts stepped
+ * concurrently with several shares of the bodies in the part of the largest
+ * worlds; for each, the later parts' solver-chain workers per SM and the
+ * island size from which an island takes the warp-per-island solver -- are
+ * built and timed on `trial_steps` steps from the worlds' current state, the
+ * state restored after each trial, and the fastest kept.  The choice is
+ * cached per world-size histogram (log2 bins of the body counts), for the
+ * process and, when the environment variable CPGPU_TUNE_FILE names a file,
+ * there; cpgpu_batch_create uses a cached choice for a matching histogram.
+ * Every world steps exactly as it does alone under any schedule. */
+int cpgpu_batch_create_tuned(cpgpu_world* const* worlds, int n_worlds, int trial_steps, cpgpu_batch** out);
+/* The batch's schedule: sched[5] = parts, first-part share of the bodies (%),
+ * chain workers per SM of the later parts (0 = as many as fit), big-island row
+ * threshold, 1 if chosen by the autotuner; times[2] = the tuned schedule's and
+ * the hand-set schedule's device ms per step measured while tuning (-1 when
+ * not tuned here).  Either pointer may be NULL. */
+int cpgpu_batch_schedule(cpgpu_batch* b, int* sched, double* times);
 int cpgpu_batch_destroy(cpgpu_batch* b);
 int cpgpu_batch_step(cpgpu_batch* b, int n_steps);
 /* Body state of world `world_index` of the batch (same layout as above). */
@@ -311,14 +328,35 @@ int cpgpu_batch_step_timed(cpgpu_batch* b, int n_steps, double* device_ms);
  * write and the contact graph is kept. */
 int cpgpu_batch_read_state(cpgpu_batch* b, float* out);
 int cpgpu_batch_write_state(cpgpu_batch* b, const float* in);
-/* Per-stage device time of n_steps run stage by stage (no graph), for the
- * roofline: stage_ms receives CPGPU_N_STAGES totals in the order gravity,
- * pairs, narrowphase, merge, islands, rows, pgs, integrate, geometry; counts
- * (may be NULL) receives the last step's pairs, contacts and islands. */
+/* Per-stage device time of n_steps run stage by stage (no graph, the parts
+ * of the batch concurrent, one step at a time), for the roofline: stage_ms
+ * receives CPGPU_N_STAGES totals in the order gravity, pairs, narrowphase,
+ * merge, islands, rows, pgs, integrate, geometry, each step's stage time
+ * being the window from the first part entering the stage to the last part
+ * leaving it (so no stage exceeds the step); counts (may be NULL) receives
+ * the last step's pairs, contacts and islands summed over the parts. */
 #define CPGPU_N_STAGES 9
 int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* counts);
 /* Number of kernel launches one step of the batch issues. */
 int cpgpu_batch_launches_per_step(cpgpu_batch* b, int* n);
+
+/* ---- FP64 momentum / energy audit --------------------------------------- */
+/* No counterpart in the reference (which computes in FP64 throughout).  When
+ * enabled, every step ends with a device pass that sums, per world and in
+ * FP64 over the FP32 state, CPGPU_AUDIT_VALUES values:
+ *   [0..2] linear momentum sum(m v)
+ *   [3..5] angular momentum about the origin sum(x × m v + I_world ω)
+ *   [6]    kinetic energy sum(m |v|^2 / 2 + ω·I_world ω / 2)
+ *   [7]    gravitational potential energy -sum(m g·x)
+ *   [8]    largest increase of [6] + [7] over one step since enabled
+ *   [9]    steps audited since enabled
+ * over the dynamic bodies (fixed and kinematic ones are left out).  Enabling
+ * resets the values; the read returns those of the last step. */
+#define CPGPU_AUDIT_VALUES 10
+int cpgpu_world_set_audit(cpgpu_world* w, int enabled);
+int cpgpu_world_read_audit(cpgpu_world* w, double* out);               /* 10 doubles */
+int cpgpu_batch_set_audit(cpgpu_batch* b, int enabled);
+int cpgpu_batch_read_audit(cpgpu_batch* b, double* out);               /* 10 per world, batch order */
 
 /* ---- allocation-free pair generation ------------------------------------ */
 /* No counterpart in the reference (its broadphase is the AABB tree inside
@@ -341,7 +379,12 @@ int cpgpu_batch_launches_per_step(cpgpu_batch* b, int* n);
  * any stream capture.  Every call on a device shares the scratch array, so
  * calls whose executions overlap on the GPU (different streams without
  * ordering) race; calls ordered on one stream are safe.  Each call rewrites
- * all the scratch it reads. */
+ * all the scratch it reads.  The scratch address is cached per CUDA context,
+ * so a device reset by the caller is followed by a fresh lookup.  Errors:
+ * CPGPU_ERR_INVALID_ARG (sizes, NULL buffers), CPGPU_ERR_NO_DEVICE,
+ * CPGPU_ERR_CUDA when a CUDA error from earlier work is already pending on
+ * the thread (left pending, nothing launched) or when one of this call's
+ * launches fails; kernel faults surface at the caller's next synchronisation. */
 int cpgpu_pairs_noalloc(const float* aabbs, int n_bodies, uint32_t* pairs, int cap, int* count, void* stream);
 
 /* ---- serving ------------------------------------------------------------- */

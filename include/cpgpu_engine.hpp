@@ -7,9 +7,10 @@
 //   * bodies are addressed by id (RigidBody handles wrap the id);
 //   * errors that the reference reports with assert() throw cpgpu::Error;
 //   * only the contact path is on the device: convex hulls, boxes, spheres,
-//     cylinders, capsules and fixed static triangle meshes, ball sockets and
-//     hinges are the supported shapes/joints (others throw cpgpu::Error with
-//     CPGPU_ERR_UNSUPPORTED), one primitive per body, sleeping stays disabled.
+//     cylinders, capsules and fixed static triangle meshes; ball-socket,
+//     hinge, distance, weld, slider and sliding-hinge joints, cone and twist
+//     limits and springs; one primitive per body (others throw cpgpu::Error
+//     with CPGPU_ERR_UNSUPPORTED); sleeping stays disabled.
 #pragma once
 #include <array>
 #include <cstdint>
@@ -195,9 +196,7 @@ public:
     }
     // addDistanceConstraint / addWeldConstraint / addSliderConstraint /
     // addSlidingHingeConstraint / addConeLimitConstraint /
-    // addTwistLimitConstraint / addSpring: the
-    // device path reports
-    // CPGPU_ERR_UNSUPPORTED for these joint types for now
+    // addTwistLimitConstraint / addSpring (PhysicsEngine.cpp:623-998)
     ConstraintID addDistanceConstraint(RigidBody* b1, RigidBody* b2, Vec3 p1, Vec3 p2, double target = -1,
                                        double strength = 15000) {
         uint32_t id = 0;

@@ -18,7 +18,6 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = "/root/reference"
 
 if REPO not in sys.path:
     sys.path.insert(0, REPO)
@@ -29,13 +28,16 @@ from constraintphysics_gb300.world import World  # noqa: E402
 _LIBS = {}
 
 
-def build(jobs=None):
-    """Stage the reference sources (when the reference checkout is present)
-    and build both oracle libraries with make."""
+def build(jobs=None, reference_root=None):
+    """Stage the reference sources (from `reference_root`, else from
+    $CONSTRAINTPHYSICS_REFERENCE, when that checkout is present) and build both
+    oracle libraries with make.  Without a checkout the sources staged earlier
+    (baseline/_ref/src, which travels with the working tree) are built."""
+    from oracle import stage_ref
     staged = os.path.join(REPO, "baseline", "_ref", "src")
-    if os.path.isdir(REFERENCE_ROOT):
-        from oracle import stage_ref
-        stage_ref.stage(REFERENCE_ROOT)
+    root = reference_root or stage_ref.reference_root()
+    if root and os.path.isdir(root):
+        stage_ref.stage(root)
     jobs = jobs or max(1, os.cpu_count() or 1)
     targets = ["port"] + (["ref"] if os.path.isdir(staged) else [])
     subprocess.run(["make", "-s", f"-j{jobs}", *targets], cwd=HERE, check=True)

@@ -346,8 +346,8 @@ struct DV { Vec<6> v, pv, lin_err; };   // VelPair (ConstraintSolver.cpp:83-89)
 // with every loop bounded by n, in the reference's accumulation order.
 constexpr int kMaxDof = 6;
 // impulses per joint in the joint-state layout of cpgpu_get/set_joint_state
-// (the device's joints have at most 5 rows; a weld's sixth is not carried)
-constexpr int kStateDof = 5;
+// (the largest row, a weld's, has 6)
+constexpr int kStateDof = 6;
 struct JRow {
     int n = 3;
     Body* a = nullptr; Body* b = nullptr;

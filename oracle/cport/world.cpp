@@ -1497,15 +1497,21 @@ int cport_get_mass_properties(cpgpu_world* w, uint32_t id, double* mass, double*
     for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) tensor[3 * i + j] = b->ref_tensor.m[i][j];
     return CPGPU_OK;
 }
-// Joint warm-start state (same layout as cpgpu_get/set_joint_state)
-int cport_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv, int* n) {
+// Joint warm-start state (same layout as cpgpu_get/set_joint_state): the
+// row impulse (kStateDof per joint), the tangent basis u, w, and for limits
+// the twist angle and whether the limit was reached at the last rebuild
+int cport_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv, double* aux, int* n) {
     World* x = W(w);
     *n = (int)x->joints.size();
     for (size_t j = 0; j < x->joints.size(); j++) {
         const Joint& J = *x->joints[j];
-        for (int k = 0; k < kStateDof; k++) if (impulse) impulse[kStateDof * j + k] = k < J.n ? J.row.impulse[k] : 0.0;
+        for (int k = 0; k < kStateDof; k++) if (impulse) impulse[kStateDof * j + k] = k < J.row.n ? J.row.impulse[k] : 0.0;
         if (u) { u[3 * j] = J.u.x; u[3 * j + 1] = J.u.y; u[3 * j + 2] = J.u.z; }
         if (wv) { wv[3 * j] = J.w.x; wv[3 * j + 1] = J.w.y; wv[3 * j + 2] = J.w.z; }
+        if (aux) {
+            aux[2 * j] = J.cur_angle;
+            aux[2 * j + 1] = ((J.cone || J.twist) && !J.inactive) ? 1.0 : 0.0;
+        }
     }
     return CPGPU_OK;
 }
@@ -1513,16 +1519,37 @@ int cport_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv
 // (the rebuild of the first substep for rows inside a holonomic system, which
 // the restatement otherwise takes from the end of the previous step, is
 // redone here from the current poses with the imported impulses).
-int cport_set_joint_state(cpgpu_world* w, const double* impulse, const double* u, const double* wv, int n) {
+int cport_set_joint_state(cpgpu_world* w, const double* impulse, const double* u, const double* wv, const double* aux,
+                          int n) {
     World* x = W(w);
     if (n != (int)x->joints.size()) return fail("joint count mismatch");
     for (int j = 0; j < n; j++) {
         Joint& J = *x->joints[j];
-        for (int k = 0; k < std::min(J.n, kStateDof); k++) if (impulse) J.row.impulse[k] = impulse[kStateDof * j + k];
+        for (int k = 0; k < std::min(J.row.n, kStateDof); k++) if (impulse) J.row.impulse[k] = impulse[kStateDof * j + k];
         if (u) J.u = V3(u[3 * j], u[3 * j + 1], u[3 * j + 2]);
         if (wv) J.w = V3(wv[3 * j], wv[3 * j + 1], wv[3 * j + 2]);
+        if (aux) {
+            J.cur_angle = aux[2 * j];
+            if (J.cone || J.twist) J.inactive = aux[2 * j + 1] == 0.0;
+        }
     }
-    if (x->p.pgs_holo > 0) x->updateHolonomicInverses();
+    if (x->p.pgs_holo > 0) {
+        // the rows inside holonomic systems are rebuilt (and factorised) from
+        // the current poses, as the end of the exporting world's last step
+        // did; that rebuild re-projects the warm impulses onto the tangent
+        // basis of the same poses, which the exported impulses and bases
+        // already are, so the imported values are put back unchanged.  A world
+        // that has not stepped yet forms its systems first (its first step
+        // would otherwise form them and rebuild their rows once more).
+        x->maintainHolonomicSystems();
+        x->updateHolonomicInverses();
+        for (int j = 0; j < n; j++) {
+            Joint& J = *x->joints[j];
+            for (int k = 0; k < std::min(J.row.n, kStateDof); k++) if (impulse) J.row.impulse[k] = impulse[kStateDof * j + k];
+            if (u) J.u = V3(u[3 * j], u[3 * j + 1], u[3 * j + 2]);
+            if (wv) J.w = V3(wv[3 * j], wv[3 * j + 1], wv[3 * j + 2]);
+        }
+    }
     return CPGPU_OK;
 }
 // Test hook: number of holonomic systems and the largest verifyInverse error

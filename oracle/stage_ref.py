@@ -36,6 +36,8 @@ The shim makes the MSVC-only code compile with g++:
   * a header named `Vector` (RigidBody.h:9 includes <Vector>).
 
 Usage: python oracle/stage_ref.py [reference_root]
+The reference root is the argument, else the environment variable
+CONSTRAINTPHYSICS_REFERENCE; with neither, nothing is staged.
 """
 import os
 import shutil
@@ -119,6 +121,15 @@ def stage(ref_root):
     return out_src
 
 
+def reference_root():
+    """The reference checkout to stage from: $CONSTRAINTPHYSICS_REFERENCE, or
+    None when it is unset or not a directory."""
+    root = os.environ.get("CONSTRAINTPHYSICS_REFERENCE")
+    return root if root and os.path.isdir(root) else None
+
+
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    if not root:
+        raise SystemExit("usage: stage_ref.py REFERENCE_ROOT (or set CONSTRAINTPHYSICS_REFERENCE)")
     print(stage(root))

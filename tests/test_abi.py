@@ -35,9 +35,11 @@ def test_device_library_exports_every_declared_symbol():
 def test_oracle_libraries_export_the_world_api(oracle_mod, which):
     abi = oracle_mod.ref_abi() if which == "ref" else oracle_mod.port_abi()
     prefix = "cpref_" if which == "ref" else "cport_"
-    # batches and the allocation-free pair entry point exist on the device path only
+    # batches, the allocation-free pair entry point and the FP64 audit exist
+    # on the device path only
     batch_only = {n[len("cpgpu_"):] for n in declared()
-                  if n.startswith(("cpgpu_batch_", "cpgpu_server_"))} | {"pairs_noalloc", "world_clone"}
+                  if n.startswith(("cpgpu_batch_", "cpgpu_server_"))} | {"pairs_noalloc", "world_clone",
+                                                                            "world_set_audit", "world_read_audit"}
     state_import = {"set_body_state", "set_contacts", "get_joint_state", "set_joint_state"}
     for n in declared():
         short = n[len("cpgpu_"):]

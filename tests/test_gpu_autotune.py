@@ -1,0 +1,72 @@
+"""The batch schedule and its autotuner (cpgpu_batch_create_tuned), on a GB300.
+
+A schedule (parts stepped concurrently, solver-chain workers per SM, the
+island size that takes the warp-per-island solver) must never change a
+result: every schedule steps every world exactly as it does alone.  The
+autotuner times candidate schedules on trial steps, restores the state after
+each, and keeps the fastest; the batch it returns starts from the worlds'
+state, and a later plain batch with the same world-size histogram reuses the
+choice.
+"""
+import numpy as np
+import pytest
+
+import constraintphysics_gb300 as cg
+from constraintphysics_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _worlds(n, seed=3):
+    rng = np.random.default_rng(seed)
+    pool = scenes.HullPool(seed, size=32)
+    return [scenes.batched_world(rng, pool, 8, 200) for _ in range(n)]
+
+
+def _build(scs):
+    ws = []
+    for sc in scs:
+        w = cg.world()
+        scenes.apply(sc, w)
+        ws.append(w)
+    return ws
+
+
+def test_schedules_give_identical_results(monkeypatch):
+    scs = _worlds(600)
+    ref = None
+    for parts, share, per_sm in ((1, 100, 0), (2, 20, 2), (3, 30, 1)):
+        monkeypatch.setenv("CPGPU_BATCH_PARTS", str(parts))
+        monkeypatch.setenv("CPGPU_BATCH_FIRST_SHARE", str(share))
+        monkeypatch.setenv("CPGPU_PGS_REST_PER_SM", str(per_sm))
+        b = cg.Batch(_build(scs))
+        assert b.schedule()["parts"] == parts
+        b.step(25)
+        st = [b.state(i) for i in range(0, 600, 37)]
+        b.close()
+        if ref is None:
+            ref = st
+        else:
+            for x, y in zip(st, ref):
+                for k in x:
+                    assert np.array_equal(x[k], y[k]), (parts, k)
+
+
+def test_autotuned_batch_starts_from_the_worlds_and_matches_the_default():
+    scs = _worlds(600, seed=4)
+    plain = cg.Batch(_build(scs))
+    tuned = cg.Batch(_build(scs), tune_steps=2)
+    sch = tuned.schedule()
+    assert sch["tuned"] and sch["tuned_ms_per_step"] > 0 and sch["default_ms_per_step"] > 0
+    assert sch["tuned_ms_per_step"] <= sch["default_ms_per_step"] * 1.0001
+    assert sch["big_island_rows"] in (32, 48, 96)
+    plain.step(20)
+    tuned.step(20)
+    for i in range(0, 600, 23):
+        a, b = plain.state(i), tuned.state(i)
+        for k in a:
+            assert np.array_equal(a[k], b[k]), k
+    # a later plain batch with the same histogram takes the cached choice
+    again = cg.Batch(_build(scs))
+    s2 = again.schedule()
+    assert s2["tuned"] and s2["parts"] == sch["parts"] and s2["big_island_rows"] == sch["big_island_rows"]

@@ -545,18 +545,7 @@ def test_restatement_bitwise_with_distance_joints(oracle_mod, mixed):
     spheres linked by distance joints, or by alternating distance and
     ball-socket joints (one holonomic system, solved by the block LDL), hit by
     a box; bit-identical to the reference over 300 steps."""
-    M = scenes.PILE_MATERIAL
-    sc = scenes.Scene("distance_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
-    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
-    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 8.0, 0.0))
-    for i in range(6):
-        b = sc.sphere((0, 0, 0), 0.25, M, scenes.DYNAMIC, (0.9 * (i + 1), 8.0, 0.0))
-        if mixed and i % 2 == 1:
-            sc.ball_socket(prev, b, (0.45, 0, 0), (-0.45, 0, 0))
-        else:
-            sc.distance(prev, b, (0.25, 0, 0), (-0.25, 0, 0))
-        prev = b
-    sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, M, scenes.DYNAMIC, (2.0, 1.0, 0.3))
+    sc = scenes.distance_chain(mixed)
     r, p = oracle_mod.twin_worlds(sc)
     for s in range(300):
         r.step(1)
@@ -574,20 +563,7 @@ def test_restatement_bitwise_with_weld_joints(oracle_mod, mixed):
     fixed post, one link turned so the orientation correction acts, or with
     every other weld a hinge (one holonomic system of 6- and 5-dof blocks),
     hit by a falling box; bit-identical to the reference over 300 steps."""
-    M = scenes.PILE_MATERIAL
-    sc = scenes.Scene("weld_cantilever", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
-    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
-    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 4.0, 0.0))
-    for i in range(5):
-        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.DYNAMIC, (0.6 * (i + 1), 4.0, 0.0))
-        if i == 2:
-            sc.orient(b, (0.9961946980917455, 0.0, 0.0, 0.08715574274765817))   # 10 degrees about z
-        if mixed and i % 2 == 1:
-            sc.hinge(prev, b, (0.3, 0, 0), (-0.3, 0, 0), (0, 0, 1), (0, 0, 1))
-        else:
-            sc.weld(prev, b, (0.3, 0, 0), (-0.3, 0, 0))
-        prev = b
-    sc.box((-0.3, -0.3, -0.3), 0.6, 0.6, 0.6, M, scenes.DYNAMIC, (2.4, 6.0, 0.1))
+    sc = scenes.weld_cantilever(mixed)
     r, p = oracle_mod.twin_worlds(sc)
     for s in range(300):
         r.step(1)
@@ -607,18 +583,7 @@ def test_restatement_bitwise_with_slider_joints(oracle_mod, kinds):
     on tilted slide axes, one link turned, alone or mixed with a hinge in one
     holonomic system, hit by a falling box; bit-identical to the reference over
     300 steps."""
-    M = scenes.PILE_MATERIAL
-    sc = scenes.Scene("slider_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
-    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
-    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 4.0, 0.0))
-    axes = [(1.0, -0.4, 0.2), (0.3, -1.0, 0.0), (1.0, 0.2, -0.5), (0.0, -1.0, 0.4)]
-    for i, kind in enumerate(kinds):
-        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.DYNAMIC, (0.6 * (i + 1), 4.0, 0.0))
-        if i == 1:
-            sc.orient(b, (0.9961946980917455, 0.0, 0.0, 0.08715574274765817))   # 10 degrees about z
-        getattr(sc, kind)(prev, b, (0.3, 0, 0), (-0.3, 0, 0), axes[i], axes[i])
-        prev = b
-    sc.box((-0.3, -0.3, -0.3), 0.6, 0.6, 0.6, M, scenes.DYNAMIC, (1.8, 6.0, 0.1))
+    sc = scenes.slider_chain(kinds)
     r, p = oracle_mod.twin_worlds(sc)
     start = r.state()["com"][2:6].copy()
     for s in range(300):
@@ -637,19 +602,7 @@ def test_restatement_bitwise_with_springs(oracle_mod, with_joints):
     springs (two sharing a body, one at its creation length), bouncing on the
     ground and off each other, or sharing bodies with ball-socket joints;
     bit-identical to the reference over 300 steps."""
-    M = scenes.PILE_MATERIAL
-    sc = scenes.Scene("spring_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
-    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
-    post = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 4.0, 0.0))
-    prev = post
-    for i in range(4):
-        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.DYNAMIC, (0.4 * (i + 1), 3.2 - 0.7 * i, 0.1 * i))
-        if with_joints and i == 2:
-            sc.ball_socket(prev, b, (0.2, -0.35, 0.05), (-0.2, 0.35, -0.05))
-        else:
-            sc.spring(prev, b, (0.1, -0.25, 0.0), (0.0, 0.25, 0.1), 2.0 + i, 300.0 + 100.0 * i, 0.6 if i % 2 else -1.0)
-        prev = b
-    sc.spring(post, prev, (0.25, 0.0, 0.0), (0.0, 0.0, 0.25), 5.0, 80.0, 1.0)
+    sc = scenes.spring_chain(with_joints)
     r, p = oracle_mod.twin_worlds(sc)
     start = r.state()["com"][2:6].copy()
     for s in range(300):
@@ -668,16 +621,7 @@ def test_restatement_bitwise_with_cone_limits(oracle_mod, holo):
     on each joint, with and without the holonomic block solve (the cone rows
     stay out of the holonomic system); bit-identical to the reference over 300
     steps, and the limits do engage."""
-    M = scenes.PILE_MATERIAL
-    sc = scenes.Scene("cone_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, holo), sleeping=False))
-    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
-    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 6.0, 0.0))
-    for i in range(4):
-        b = sc.box((-0.15, -0.4, -0.15), 0.3, 0.8, 0.3, M, scenes.DYNAMIC, (0.0, 5.2 - 1.0 * i, 0.0))
-        sc.ball_socket(prev, b, (0.0, -0.5 if i else -0.25, 0.0), (0.0, 0.5, 0.0))
-        sc.cone_limit(prev, b, (0.0, -1.0, 0.0), (0.0, -1.0, 0.0), 25.0 * np.pi / 180.0)
-        prev = b
-    sc.velocity(prev, (6.0, 0.0, 2.0))
+    sc = scenes.cone_chain(holo)
     r, p = oracle_mod.twin_worlds(sc)
     for s in range(300):
         r.step(1)
@@ -692,18 +636,7 @@ def test_restatement_bitwise_with_twist_limits(oracle_mod):
     TwistLimitConstraint row, ConstraintSolver.cpp:439-466) beside cone limits
     on a ball-socket chain spun about its axis; bit-identical to the
     reference over 300 steps, and the twist limit does engage."""
-    M = scenes.PILE_MATERIAL
-    sc = scenes.Scene("twist_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
-    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
-    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 6.0, 0.0))
-    for i in range(3):
-        b = sc.box((-0.3, -0.4, -0.1), 0.6, 0.8, 0.2, M, scenes.DYNAMIC, (0.0, 5.2 - 1.0 * i, 0.0))
-        sc.ball_socket(prev, b, (0.0, -0.5 if i else -0.25, 0.0), (0.0, 0.5, 0.0))
-        sc.cone_limit(prev, b, (0.0, -1.0, 0.0), (0.0, -1.0, 0.0), 20.0 * np.pi / 180.0)
-        sc.twist_limit(prev, b, (0.0, -1.0, 0.0), (0.0, -1.0, 0.0), -0.3, 0.5)
-        prev = b
-    sc.ang_velocity(prev, (0.5, 9.0, 0.0))
-    sc.velocity(prev, (2.0, 0.0, 0.0))
+    sc = scenes.twist_chain()
     r, p = oracle_mod.twin_worlds(sc)
     for s in range(300):
         r.step(1)
@@ -712,34 +645,69 @@ def test_restatement_bitwise_with_twist_limits(oracle_mod):
             assert _states_equal(r.state(), p.state()), f"state differs at step {s}"
 
 
-def test_restatement_joint_state_layout(oracle_mod):
-    """The restatement's joint-state export and import use the C ABI's layout
-    (5 impulses per joint, as the device's cpgpu_get/set_joint_state): a
-    round trip through a second world reproduces the state, for hinges, ball
-    sockets and a weld (whose sixth impulse the layout does not carry)."""
+def _state_chain():
     M = scenes.PILE_MATERIAL
     sc = scenes.Scene("state_chain", dict(step_time=1.0 / 60.0, substeps=4, pgs=(10, 1, 1), sleeping=False))
     sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, scenes.FIXED)
     prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.FIXED, (0.0, 4.0, 0.0))
-    for i, kind in enumerate(("hinge", "ball", "weld", "hinge")):
+    for i, kind in enumerate(("hinge", "ball", "weld", "hinge", "ball")):
         b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, scenes.DYNAMIC, (0.6 * (i + 1), 4.0, 0.0))
         if kind == "hinge":
             sc.hinge(prev, b, (0.3, 0, 0), (-0.3, 0, 0), (0, 0, 1), (0, 0, 1))
         elif kind == "ball":
             sc.ball_socket(prev, b, (0.3, 0, 0), (-0.3, 0, 0))
+            sc.cone_limit(prev, b, (1.0, 0.0, 0.0), (1.0, 0.0, 0.0), 15.0 * np.pi / 180.0)
+            sc.twist_limit(prev, b, (1.0, 0.0, 0.0), (1.0, 0.0, 0.0), -0.2, 0.2)
         else:
             sc.weld(prev, b, (0.3, 0, 0), (-0.3, 0, 0))
         prev = b
+    sc.ang_velocity(prev, (6.0, 2.0, 0.0))
+    return sc
+
+
+def test_restatement_joint_state_layout(oracle_mod):
+    """The restatement's joint-state export and import use the C ABI's layout
+    (6 impulses per joint, 2 auxiliary values for limits): a round trip
+    through a second world reproduces the state, for hinges, ball sockets, a
+    weld (all 6 impulses), cone and twist limits (angle and reached flag)."""
+    sc = _state_chain()
     a, b = oracle_mod.port_world(), oracle_mod.port_world()
     scenes.apply(sc, a)
     scenes.apply(sc, b)
     a.step(20)
     ja = a.joint_state()
-    assert ja["impulse"].shape == (4, 5)
-    assert np.abs(ja["impulse"][[0, 1, 3]]).max() > 0
-    assert np.all(ja["impulse"][1, 3:] == 0) and np.abs(ja["impulse"][1, :2]).min() > 0   # the ball socket: 3 rows
+    assert ja["impulse"].shape == (9, 6) and ja["aux"].shape == (9, 2)
+    kinds = ["hinge", "ball", "cone", "twist", "weld", "hinge", "ball", "cone", "twist"]
+    weld = kinds.index("weld")
+    assert np.abs(ja["impulse"][weld, 5]) > 0                                  # the weld's sixth row
+    ball = kinds.index("ball")
+    assert np.all(ja["impulse"][ball, 3:] == 0) and np.abs(ja["impulse"][ball, :2]).min() > 0   # 3 rows
+    twist = [i for i, k in enumerate(kinds) if k == "twist"]
+    assert np.abs(ja["aux"][twist, 0]).max() > 0                               # twist angles tracked
     b.set_joint_state(ja)
     jb = b.joint_state()
     for k in ja:
         assert np.array_equal(ja[k], jb[k]), k
 
+
+def test_restatement_checkpoint_restore_steps_like_the_uninterrupted_run(oracle_mod):
+    """A world restored from a checkpoint (bodies, contacts and joint state,
+    limits included) steps exactly like the run that was never interrupted."""
+    sc = _state_chain()
+    a = oracle_mod.port_world()
+    scenes.apply(sc, a)
+    a.step(25)
+    b = oracle_mod.port_world()
+    scenes.apply(sc, b)
+    b.set_state(**a.state())
+    b.set_contacts(a.contacts())
+    b.set_joint_state(a.joint_state())
+    for _ in range(4):
+        a.step(10)
+        b.step(10)
+        sa, sb = a.state(), b.state()
+        for k in sa:
+            assert np.array_equal(sa[k], sb[k]), k
+    ja, jb = a.joint_state(), b.joint_state()
+    for k in ja:
+        assert np.array_equal(ja[k], jb[k]), k
