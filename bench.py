@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--profile-only", action="store_true", help="build the batch, run warmup + steps, no extras")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="duration of each serving run (0: none)")
     ap.add_argument("--serve-rates", default="2000,20", help="Poisson request rates (requests/s) of the serving runs")
+    ap.add_argument("--workload", default=WORKLOAD,
+                    choices=[WORKLOAD, "hull_drop_1000", "terrain_20k", "chains_1024"],
+                    help="the headline batched workload (default) or one of the other configurations")
     ap.add_argument("--tune-steps", type=int, default=3,
                     help="trial steps per candidate schedule of the batch autotuner (0: the hand-set schedule)")
     return ap.parse_args()
@@ -341,8 +344,103 @@ def measure_drift(cg, ws_scenes, n_per_kind=4, steps=300, max_bodies=400):
     return out
 
 
+SECONDARY = {
+    "hull_drop_1000": "1,000 random hulls (8-32 points, scale U[0.5,1.5] m) on a 10x10x10 grid dropped on the plate; "
+                      "one world (the plain single-world path), dt 1/60, 1 substep, PGS (10,1,1)",
+    "terrain_20k": "20,000 mixed bodies (40% boxes, 20% spheres, 20% cylinders, 20% hulls) dropped on a 256x256 "
+                   "value-noise heightfield mesh (131,072 triangles); one world, PGS (20,1,1)",
+    "chains_1024": "1,024 articulated chains of 16-64 unit boxes (link mass log-uniform [0.1,100] kg), ball-socket and "
+                   "hinge joints, 50 fixed spheres each; one batch, 8 substeps, PGS (4,1,1) with the block solve",
+}
+
+
+def run_secondary(a):
+    """One of the other configurations: device body-steps/s (state in HBM),
+    per-stage windows and roofline, the reference engine on the machine's host
+    cores on a bounded sample, and (1,000 hulls) the 600-step drift."""
+    import constraintphysics_gb300 as cg
+    import oracle
+    threads = max(1, os.cpu_count() or 1)
+    if a.workload == "hull_drop_1000":
+        scs = [scenes.hull_drop(seed=a.seed, n_side=10)]
+        params = {"pgs_vel": 10, "pgs_pos": 1, "substeps": 1}
+    elif a.workload == "terrain_20k":
+        scs = [scenes.terrain_drop(seed=a.seed, n_grid=256, n_side=50, n_layers=8)]
+        params = {"pgs_vel": 20, "pgs_pos": 1, "substeps": 1}
+    else:
+        rng = np.random.default_rng(a.seed)
+        scs = [scenes.chain_world(rng) for _ in range(1024)]
+        params = {"pgs_vel": 4, "pgs_pos": 1, "substeps": 8}
+    n_dyn = sum(sum(1 for m in sc.movements() if m == scenes.DYNAMIC) for sc in scs)
+    t0 = time.perf_counter()
+    worlds = build_worlds(scs, cg.world)
+    batch = cg.Batch(worlds)
+    setup_s = time.perf_counter() - t0
+    batch.step(a.warmup)
+    sampler = ClockSampler(0)
+    dev_ms = batch.step_timed(a.steps)
+    stage_ms, counts = batch.profile(a.steps)
+    clocks = sampler.stop()
+    stage_ms = {k: v / a.steps for k, v in stage_ms.items()}
+    value = n_dyn * a.steps / (dev_ms / 1e3)
+    peak, peak_kind = measured_peaks()
+    dominant = max(stage_ms, key=stage_ms.get)
+    has_hulls = any(op[0] in ("hull", "box") for sc in scs for op in sc.ops)
+    vfe = hull_sizes(scs) if has_hulls else (8, 6, 12)
+    roof = None
+    b = algorithmic_bytes(dominant, counts, batch.n_bodies, vfe, params)
+    if b is not None:
+        roof = {"bound": "hbm", "kernel": dominant, "achieved": b / (stage_ms[dominant] / 1e3) / 1e9, "peak": peak,
+                "unit": "GB/s", "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b,
+                "launch_ms": stage_ms[dominant], "traffic": None}
+        roof["frac"] = roof["achieved"] / peak
+    # the reference engine on a bounded sample of the same scenes
+    idx = list(range(len(scs)))[:: max(1, len(scs) // 64)]
+    ref_steps = 3 if a.workload == "terrain_20k" else 10
+    ref = []
+    for i in idx:
+        w = oracle.ref_world()
+        scenes.apply(scs[i], w)
+        ref.append((w, sum(1 for m in scs[i].movements() if m == scenes.DYNAMIC)))
+    import ctypes
+    step_untraced = oracle.ref_abi()._lib.cpref_step_untraced
+    step_untraced.restype = ctypes.c_int
+    step_untraced.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    with concurrent.futures.ThreadPoolExecutor(min(threads, len(ref))) as ex:
+        list(ex.map(lambda it: step_untraced(it[0].h, 1), ref))
+        tc = time.perf_counter()
+        list(ex.map(lambda it: step_untraced(it[0].h, ref_steps), ref))
+        wall = time.perf_counter() - tc
+    cpu = {"value": sum(n for _, n in ref) * ref_steps / wall, "unit": UNIT, "cores": min(threads, len(ref)),
+           "kind": "reference", "sample": f"{len(ref)} of {len(scs)} worlds, {ref_steps} timed steps after 1, "
+                                         f"one single-threaded reference engine per thread"}
+    drift = None
+    if a.workload == "hull_drop_1000":
+        g = cg.world()
+        scenes.apply(scs[0], g)
+        g.step(600)
+        r = oracle.ref_world()
+        scenes.apply(scs[0], r)
+        r.step(600)
+        dyn = np.array([m == scenes.DYNAMIC for m in scs[0].movements()])
+        d = np.linalg.norm(g.state()["com"][dyn] - r.state()["com"][dyn], axis=1)
+        drift = {"steps": 600, "median_m": float(np.median(d)), "p95_m": float(np.percentile(d, 95)),
+                 "frac_within_1e-3_m": float(np.mean(d <= 1e-3)),
+                 "note": "device FP32 vs the reference FP64 from the same scene; a 1,000-hull drop is chaotic"}
+    line = {"metric": "body-steps/s", "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": dev_ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded scenes)",
+            "config": {"workload": a.workload, "description": SECONDARY[a.workload], "dynamic_bodies": n_dyn,
+                       "seed": a.seed},
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "stage_ms": stage_ms, "counts": counts,
+            "setup_s": setup_s, "drift": drift, "gpu_launches": batch.launches_per_step() * a.steps}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
+    if a.workload != WORKLOAD:
+        return run_secondary(a)
     rank, world_size, local_rank = dist_env()
     t_setup = time.perf_counter()
     ws_scenes = scenes.batched_worlds(seed=a.seed + 1000 * rank, n_worlds=a.worlds)
@@ -373,9 +471,7 @@ def main():
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
     worlds = build_worlds(ws_scenes, cg.world)
-    t_tune = time.perf_counter()
-    batch = cg.Batch(worlds, tune_steps=a.tune_steps)
-    schedule = dict(batch.schedule(), batch_build_and_tune_s=time.perf_counter() - t_tune)
+    batch = cg.Batch(worlds)
     setup_s = time.perf_counter() - t_setup
 
     def barrier():
@@ -384,6 +480,12 @@ def main():
             dist.barrier()
 
     batch.step(a.warmup)
+    # the autotuner chooses the schedule from the warmed-up state (its trial
+    # steps are undone: the timed steps continue from the same state)
+    t_tune = time.perf_counter()
+    if a.tune_steps > 0 and not a.profile_only:
+        batch.tune(a.tune_steps)
+    schedule = dict(batch.schedule(), tune_s=time.perf_counter() - t_tune)
     if a.profile_only:
         batch.step(a.steps)
         print(json.dumps({"profile_only": True, "steps": a.steps, "warmup": a.warmup}), flush=True)
@@ -399,14 +501,20 @@ def main():
     # in the graph-launched steps): each stage's window inside the step
     stage_ms, counts = batch.profile(a.steps)
     clocks = sampler.stop()
-    # FP64 momentum / energy audit: a few steps with the audit kernel at the
-    # end of each, its cost against the same steps without it
-    plain_ms = batch.step_timed(a.warmup)
+    # FP64 momentum / energy audit: steps with the audit kernel at the end of
+    # each, interleaved with steps without it for its cost, then --steps
+    # audited steps for the report
+    plain_ms = audit_ms = 0.0
+    for _ in range(5):
+        plain_ms += batch.step_timed(2)
+        batch.set_audit(True)
+        audit_ms += batch.step_timed(2)
+        batch.set_audit(False)
     batch.set_audit(True)
-    audit_ms = batch.step_timed(a.warmup)
+    batch.step(a.steps)
     av = batch.read_audit()
     batch.set_audit(False)
-    audit = {"steps": int(av[0, 9]), "ms_per_step_added": (audit_ms - plain_ms) / a.warmup,
+    audit = {"steps": int(av[0, 9]), "ms_per_step_added": (audit_ms - plain_ms) / 10,
              "total_kinetic_J": float(av[:, 6].sum()), "total_potential_J": float(av[:, 7].sum()),
              "max_step_energy_gain_J": float(av[:, 8].max()),
              "worlds_gaining_energy": int((av[:, 8] > 1e-6 * (np.abs(av[:, 6]) + np.abs(av[:, 7]) + 1.0)).sum()),

@@ -48,6 +48,7 @@ def lib():
             "server_stats": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_void_p],
             "batch_create_tuned": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
+            "batch_tune": [ctypes.c_void_p, ctypes.c_int],
             "batch_schedule": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
             "world_set_audit": [ctypes.c_void_p, ctypes.c_int],
             "world_read_audit": [ctypes.c_void_p, ctypes.c_void_p],
@@ -116,6 +117,11 @@ class Batch:
             self._check(self.abi.batch_create(arr, len(worlds), ctypes.byref(h)))
         self.h = h
         self.sizes = [w.n_bodies for w in worlds]
+
+    def tune(self, trial_steps=3):
+        """Re-choose the schedule by timing from the current state
+        (cpgpu_batch_tune); the state is unchanged."""
+        self._check(self.abi.batch_tune(self.h, int(trial_steps)))
 
     def schedule(self):
         """The batch's schedule (cpgpu_batch_schedule)."""

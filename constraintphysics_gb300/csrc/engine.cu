@@ -1731,13 +1731,31 @@ struct cpgpu_batch {
     Schedule sched;                       // the schedule the batch was built for
     bool tuned = false;                   // chosen by the autotuner (now or from its cache)
     double tuned_ms = -1, default_ms = -1;   // per step, measured when tuned here
-    ~cpgpu_batch() {
+    std::vector<World*> worlds;           // the worlds, in batch order (their host mirrors)
+    void release() {
         for (int* r : rows) if (r) cudaFree(r);
         if (stage) cudaFree(stage);
         for (cudaEvent_t e : done) cudaEventDestroy(e);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (fork) cudaEventDestroy(fork);
+        rows.clear(); done.clear();
+        stage = nullptr; ev0 = ev1 = fork = nullptr;
+        parts.clear();
+    }
+    ~cpgpu_batch() { release(); }
+    // take over another batch object's device resources (this one's are freed)
+    void adopt(cpgpu_batch& o) {
+        release();
+        parts = std::move(o.parts);
+        part_of = std::move(o.part_of); local_of = std::move(o.local_of); row0 = std::move(o.row0);
+        n_bodies = o.n_bodies;
+        stage = o.stage; o.stage = nullptr;
+        rows = std::move(o.rows); o.rows.clear();
+        ev0 = o.ev0; ev1 = o.ev1; fork = o.fork; o.ev0 = o.ev1 = o.fork = nullptr;
+        done = std::move(o.done); o.done.clear();
+        sched = o.sched;
+        worlds = o.worlds;
     }
     Batch& part(int p) { return *parts[p]; }
     cudaStream_t st0() { return parts[0]->st; }
@@ -2453,6 +2471,7 @@ static std::unique_ptr<cpgpu_batch> make_batch(const std::vector<World*>& ws, co
     const int n = (int)ws.size();
     auto b = std::make_unique<cpgpu_batch>();
     b->sched = S;
+    b->worlds = ws;
     b->part_of.resize(n);
     b->local_of.resize(n);
     b->row0.resize(n);
@@ -2540,72 +2559,93 @@ static double time_steps(cpgpu_batch* b, int n) {
     return ms;
 }
 
-// Autotuned batch: candidate schedules (one, two or three parts with
-// several first-part shares; for each, the later parts' chain workers per SM
-// and the big-island threshold) are built and timed on trial steps from the
-// worlds' current state, each trial's state restored afterwards, and the
-// fastest kept (restored to the starting state).  The choice is cached for
-// the world-size histogram, so later batches with the same histogram start
-// with it.
+// Autotuner: candidate schedules (one, two or three parts with several
+// first-part shares; for each, the later parts' chain workers per SM and the
+// big-island threshold) are built from the batch's current state (read back
+// into the worlds' host mirrors), timed on trial steps, each trial's state
+// restored afterwards, and the fastest adopted; the batch then continues from
+// exactly the state it had.  Tune from a representative state (the first
+// steps of a scene, before bodies touch, cost far less than later ones).  The
+// choice is cached for the world-size histogram, so later batches with the
+// same histogram start with it.
+static void tune_batch(cpgpu_batch* b, int trial_steps) {
+    const int T = std::max(1, trial_steps);
+    for (size_t p = 0; p < b->parts.size(); p++) {
+        std::vector<World*> sub;
+        for (size_t wi = 0; wi < b->worlds.size(); wi++)
+            if (b->part_of[wi] == (int)p) sub.push_back(b->worlds[wi]);
+        download_worlds(*b->parts[p], sub);
+    }
+    const std::vector<World*> ws = b->worlds;
+    const Schedule dflt = default_schedule(ws);
+    std::vector<Schedule> layouts{dflt};
+    auto add = [&](int parts, int share) {
+        if (parts > (int)ws.size()) return;
+        for (const Schedule& x : layouts) if (x.parts == parts && (parts == 1 || x.first_share == share)) return;
+        Schedule sch;
+        sch.parts = parts; sch.first_share = parts > 1 ? share : 100;
+        layouts.push_back(sch);
+    };
+    add(1, 100);
+    for (int share : {10, 20, 30}) add(2, share);
+    add(3, 20);
+    std::unique_ptr<cpgpu_batch> best;
+    double best_ms = 1e300, dflt_ms = -1;
+    for (const Schedule& L : layouts) {
+        std::unique_ptr<cpgpu_batch> cand = make_batch(ws, L);
+        for (auto& p : cand->parts) p->snapshot();
+        const std::vector<int> per_sms = cand->parts.size() > 1 ? std::vector<int>{1, 2, 3} : std::vector<int>{0};
+        Schedule cbest = cand->sched;
+        double cbest_ms = 1e300;
+        for (int per_sm : per_sms)
+            for (int big : {32, 48, 96}) {
+                for (size_t p = 0; p < cand->parts.size(); p++) cand->parts[p]->set_schedule(p == 0 ? 0 : per_sm, big);
+                time_steps(cand.get(), 1);   // warm-up
+                const double ms = time_steps(cand.get(), T) / T;
+                for (auto& p : cand->parts) p->restore(false);
+                const bool is_dflt = L.parts == dflt.parts && L.first_share == dflt.first_share && big == dflt.big_rows &&
+                                     (cand->parts.size() == 1 || per_sm == dflt.rest_per_sm);
+                if (is_dflt) dflt_ms = ms;
+                if (ms < cbest_ms) {
+                    cbest_ms = ms;
+                    cbest.rest_per_sm = cand->parts.size() > 1 ? per_sm : 0;
+                    cbest.big_rows = big;
+                }
+            }
+        if (cbest_ms < best_ms) {
+            for (size_t p = 0; p < cand->parts.size(); p++)
+                cand->parts[p]->set_schedule(p == 0 ? 0 : cbest.rest_per_sm, cbest.big_rows);
+            for (auto& p : cand->parts) p->restore(true);
+            cand->sched = cbest;
+            best_ms = cbest_ms;
+            best = std::move(cand);
+        }
+    }
+    b->adopt(*best);
+    b->tuned = true;
+    b->tuned_ms = best_ms;
+    b->default_ms = dflt_ms;
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    const std::string key = histogram_key(ws);
+    g_tuned[key] = b->sched;
+    tune_file_save(key, b->sched);
+}
+
+int cpgpu_batch_tune(cpgpu_batch* b, int trial_steps) {
+    if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
+    return guarded([&] {
+        tune_batch(b, trial_steps);
+        return CPGPU_OK;
+    });
+}
+
 int cpgpu_batch_create_tuned(cpgpu_world* const* worlds, int n, int trial_steps, cpgpu_batch** out) {
     return guarded([&] {
         if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null output"};
         const std::vector<World*> ws = batch_worlds(worlds, n);
-        const int T = std::max(1, trial_steps);
-        const Schedule dflt = default_schedule(ws);
-        std::vector<Schedule> layouts{dflt};
-        auto add = [&](int parts, int share) {
-            if (parts > (int)ws.size()) return;
-            for (const Schedule& x : layouts) if (x.parts == parts && (parts == 1 || x.first_share == share)) return;
-            Schedule s;
-            s.parts = parts; s.first_share = parts > 1 ? share : 100;
-            layouts.push_back(s);
-        };
-        add(1, 100);
-        for (int share : {10, 20, 30}) add(2, share);
-        add(3, 20);
-        std::unique_ptr<cpgpu_batch> best;
-        double best_ms = 1e300, dflt_ms = -1;
-        for (const Schedule& L : layouts) {
-            std::unique_ptr<cpgpu_batch> cand = make_batch(ws, L);
-            for (auto& p : cand->parts) p->snapshot();
-            const std::vector<int> per_sms = cand->parts.size() > 1 ? std::vector<int>{1, 2, 3} : std::vector<int>{0};
-            Schedule cbest = cand->sched;
-            double cbest_ms = 1e300;
-            for (int per_sm : per_sms)
-                for (int big : {32, 48, 96}) {
-                    for (size_t p = 0; p < cand->parts.size(); p++) cand->parts[p]->set_schedule(p == 0 ? 0 : per_sm, big);
-                    time_steps(cand.get(), 1);   // warm-up
-                    const double ms = time_steps(cand.get(), T) / T;
-                    for (auto& p : cand->parts) p->restore(false);
-                    const bool is_dflt = L.parts == dflt.parts && L.first_share == dflt.first_share &&
-                                         big == dflt.big_rows && (cand->parts.size() == 1 || per_sm == dflt.rest_per_sm);
-                    if (is_dflt) dflt_ms = ms;
-                    if (ms < cbest_ms) {
-                        cbest_ms = ms;
-                        cbest.rest_per_sm = cand->parts.size() > 1 ? per_sm : 0;
-                        cbest.big_rows = big;
-                    }
-                }
-            if (cbest_ms < best_ms) {
-                for (size_t p = 0; p < cand->parts.size(); p++)
-                    cand->parts[p]->set_schedule(p == 0 ? 0 : cbest.rest_per_sm, cbest.big_rows);
-                for (auto& p : cand->parts) p->restore(true);
-                cand->sched = cbest;
-                best_ms = cbest_ms;
-                best = std::move(cand);
-            }
-        }
-        best->tuned = true;
-        best->tuned_ms = best_ms;
-        best->default_ms = dflt_ms;
-        {
-            std::lock_guard<std::mutex> lock(g_tune_mutex);
-            const std::string key = histogram_key(ws);
-            g_tuned[key] = best->sched;
-            tune_file_save(key, best->sched);
-        }
-        *out = best.release();
+        auto b = make_batch(ws, default_schedule(ws));
+        tune_batch(b.get(), trial_steps);
+        *out = b.release();
         return CPGPU_OK;
     });
 }

@@ -291,17 +291,23 @@ int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
  * launch sequence per step advances.  The worlds keep their own state; the
  * batch starts from their current state and the substep count must agree. */
 int cpgpu_batch_create(cpgpu_world* const* worlds, int n_worlds, cpgpu_batch** out);
-/* The same, with the batch's schedule chosen by timing (no counterpart in the
- * reference): candidate schedules -- one, two or three parts stepped
- * concurrently with several shares of the bodies in the part of the largest
- * worlds; for each, the later parts' solver-chain workers per SM and the
- * island size from which an island takes the warp-per-island solver -- are
- * built and timed on `trial_steps` steps from the worlds' current state, the
- * state restored after each trial, and the fastest kept.  The choice is
- * cached per world-size histogram (log2 bins of the body counts), for the
- * process and, when the environment variable CPGPU_TUNE_FILE names a file,
- * there; cpgpu_batch_create uses a cached choice for a matching histogram.
- * Every world steps exactly as it does alone under any schedule. */
+/* Autotuner (no counterpart in the reference): re-chooses the batch's
+ * schedule by timing from its current state.  Candidate schedules -- one, two
+ * or three parts stepped concurrently with several shares of the bodies in the
+ * part of the largest worlds; for each, the later parts' solver-chain workers
+ * per SM and the island size from which an island takes the warp-per-island
+ * solver -- are built from the current state, timed on `trial_steps` steps,
+ * the state restored after each trial, and the fastest adopted; the batch
+ * continues from exactly the state it had.  Tune from a representative state
+ * (e.g. after some steps: before bodies touch, a step costs far less).  The
+ * choice is cached per world-size histogram (log2 bins of the body counts),
+ * for the process and, when the environment variable CPGPU_TUNE_FILE names a
+ * file, there; cpgpu_batch_create uses a cached choice for a matching
+ * histogram unless CPGPU_BATCH_PARTS, CPGPU_BATCH_FIRST_SHARE or
+ * CPGPU_PGS_REST_PER_SM is set.  Every world steps exactly as it does alone
+ * under any schedule. */
+int cpgpu_batch_tune(cpgpu_batch* b, int trial_steps);
+/* cpgpu_batch_create followed by cpgpu_batch_tune from the worlds' state. */
 int cpgpu_batch_create_tuned(cpgpu_world* const* worlds, int n_worlds, int trial_steps, cpgpu_batch** out);
 /* The batch's schedule: sched[5] = parts, first-part share of the bodies (%),
  * chain workers per SM of the later parts (0 = as many as fit), big-island row

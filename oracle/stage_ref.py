@@ -37,7 +37,7 @@ The shim makes the MSVC-only code compile with g++:
 
 Usage: python oracle/stage_ref.py [reference_root]
 The reference root is the argument, else the environment variable
-CONSTRAINTPHYSICS_REFERENCE; with neither, nothing is staged.
+CONSTRAINTPHYSICS_REFERENCE, else DEFAULT_REFERENCE_ROOT when it exists.
 """
 import os
 import shutil
@@ -121,11 +121,19 @@ def stage(ref_root):
     return out_src
 
 
+# where this build's read-only reference checkout lives when
+# CONSTRAINTPHYSICS_REFERENCE does not say otherwise
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+
+
 def reference_root():
-    """The reference checkout to stage from: $CONSTRAINTPHYSICS_REFERENCE, or
-    None when it is unset or not a directory."""
-    root = os.environ.get("CONSTRAINTPHYSICS_REFERENCE")
-    return root if root and os.path.isdir(root) else None
+    """The reference checkout to stage from: $CONSTRAINTPHYSICS_REFERENCE, else
+    the default checkout location; None when neither is a directory (a
+    machine that only has the staged copy)."""
+    for root in (os.environ.get("CONSTRAINTPHYSICS_REFERENCE"), DEFAULT_REFERENCE_ROOT):
+        if root and os.path.isdir(root):
+            return root
+    return None
 
 
 if __name__ == "__main__":

@@ -55,7 +55,10 @@ def test_schedules_give_identical_results(monkeypatch):
 def test_autotuned_batch_starts_from_the_worlds_and_matches_the_default():
     scs = _worlds(600, seed=4)
     plain = cg.Batch(_build(scs))
-    tuned = cg.Batch(_build(scs), tune_steps=2)
+    tuned = cg.Batch(_build(scs))
+    plain.step(15)
+    tuned.step(15)
+    tuned.tune(2)   # from the state after 15 steps; the trial steps are undone
     sch = tuned.schedule()
     assert sch["tuned"] and sch["tuned_ms_per_step"] > 0 and sch["default_ms_per_step"] > 0
     assert sch["tuned_ms_per_step"] <= sch["default_ms_per_step"] * 1.0001
