@@ -17,7 +17,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + os.path.join(os.path.dirname(HERE), "include")]
-SOURCES = ["broadphase.cu", "narrowphase.cu", "graph.cu", "solver.cu", "joints.cu", "engine.cu", "noalloc.cu", "audit.cu"]
+SOURCES = ["broadphase.cu", "narrowphase.cu", "graph.cu", "solver.cu", "joints.cu", "engine.cu", "noalloc.cu", "audit.cu", "sleep.cu"]
 
 
 def _headers():

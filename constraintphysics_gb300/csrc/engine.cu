@@ -92,6 +92,13 @@ struct Body {
     double iref[9], iinv_ref[9], iw[9], iinv[9];
     D3 local_origin;             // tracked geometry origin (RigidBody.cpp:32-33)
     double rest = 0.3, kin = 0.6, sta = 1.1;
+    // sleep state (RigidBody.h: asleep, sleep_ready_counter as a count of
+    // sleepy steps, non_sleepy_tick_count, recievedWakingAction, history):
+    // hist holds hist_n (velocity, angular velocity) records, oldest first
+    int asleep = 0, waking = 0, ready_cnt = 0, non_sleepy = 0, hist_n = 0;
+    std::vector<float> hist;
+    // RigidBody::alertWaking (RigidBody.cpp:318-324)
+    void alert_waking() { waking = 1; ready_cnt = 0; non_sleepy = 0; hist_n = 0; hist.clear(); }
 };
 
 struct Params {
@@ -104,6 +111,10 @@ struct Params {
     int angle_ticks = 4;
     bool gyro_disabled = false, warm_disabled = false;
     double cutoff = 0;           // 2|g|dt, set by setStep_time / setGravity
+    bool sleeping = false;       // the device path starts with sleeping disabled
+    // sleep parameters (PhysicsEngine.h:219-224)
+    double sleep_delay = 0.5, vel_sleep_coeff = 0.1, ang_vel_eps = 0.1, accel_sleep_coeff = 0.044;
+    int non_sleepy_threshold = 3;
 };
 
 struct Batch;
@@ -563,7 +574,7 @@ struct Batch {
     void launch_step(const Dev& x) {
         Launch L{n_sms, st};
         mark(0);
-        launch_gravity(x, L);      mark(1);
+        launch_step_begin(x, L);   mark(1);
         launch_pairs(x, L);        mark(2);
         launch_narrowphase(x, slot_bytes, n_sms, prims, st); mark(3);   // + mesh pairs
         launch_merge(x, L);        mark(4);
@@ -901,6 +912,22 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     std::map<std::string, int> dedupe;
     std::vector<int> shape_off(N);
     std::vector<float4> pos(N), rot(N), vel(N), angv(N), zero4(N, make_float4(0.f, 0.f, 0.f, 0.f)), mat(N);
+    // sleep state: kept on the device when a world has sleeping enabled or a
+    // body is asleep; the velocity records as a ring of hist_cap entries
+    bool has_sleep = false;
+    int hist_cap = 1;
+    for (const World* w : worlds) {
+        bool any_asleep = false;
+        for (const Body& b : w->bodies) any_asleep |= b.asleep != 0;
+        has_sleep |= w->p.sleeping || any_asleep;
+        hist_cap = std::max(hist_cap, (int)(w->p.sleep_delay / w->p.dt));
+    }
+    std::vector<int> s_asleep, s_waking, s_ready, s_nons, s_hn;
+    std::vector<float> s_hist;
+    if (has_sleep) {
+        s_asleep.assign(N, 0); s_waking.assign(N, 0); s_ready.assign(N, 0); s_nons.assign(N, 0); s_hn.assign(N, 0);
+        s_hist.assign((size_t)N * hist_cap * 6, 0.f);
+    }
     std::vector<float> iref(9 * (size_t)N), iinv_ref(9 * (size_t)N), iw(9 * (size_t)N), iinv(9 * (size_t)N);
     std::vector<int> world_of(N), map_order(N);
     std::vector<uint8_t> movement(N);
@@ -945,6 +972,15 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
             }
             world_of[g] = (int)wi;
             movement[g] = (uint8_t)b.movement;
+            if (has_sleep) {
+                s_asleep[g] = b.asleep; s_waking[g] = b.waking; s_ready[g] = b.ready_cnt; s_nons[g] = b.non_sleepy;
+                // the newest records that fit this world's history length, oldest first
+                const int len = std::max(1, (int)(w.p.sleep_delay / w.p.dt));
+                const int keep = std::min(b.hist_n, len), skip = b.hist_n - keep;
+                s_hn[g] = keep;
+                for (int q = 0; q < keep; q++)
+                    for (int k = 0; k < 6; k++) s_hist[((size_t)g * hist_cap + q) * 6 + k] = b.hist[6 * (skip + q) + k];
+            }
         }
         std::vector<int> order = map_iteration_order(w);
         for (size_t k = 0; k < order.size(); k++) map_order[base + k] = base + order[k];
@@ -963,6 +999,26 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
         P.pgs_vel = w.p.pgs_vel;
         P.pgs_pos = w.p.pgs_pos;
         P.pgs_holo = w.p.pgs_holo;
+        {
+            // the reference's thresholds (PhysicsEngine.cpp:1221-1258) and its
+            // FP64 step arithmetic turned into step counts
+            const double gm = w.p.g.mag(), span = w.p.sleep_delay / w.p.dt;
+            P.sleeping = w.p.sleeping ? 1 : 0;
+            P.hist_len = std::max(1, (int)span);
+            int hm = 1;
+            while (2.0 * hm < span) hm++;
+            P.hist_min = hm;
+            double acc = 0.0;
+            int rs = 0;
+            while (!(acc >= w.p.sleep_delay) && rs < (1 << 28)) { acc += w.p.dt; rs++; }
+            P.ready_steps = rs;
+            P.non_sleepy_threshold = w.p.non_sleepy_threshold;
+            P.vel_eps = (float)(w.p.vel_sleep_coeff * gm);
+            P.ang_vel_eps = (float)w.p.ang_vel_eps;
+            P.accel_eps = (float)(w.p.accel_sleep_coeff * gm);
+            P.ang_accel_eps = (float)(w.p.accel_sleep_coeff * 2.5);
+            P.wake_vel = (float)(0.25 * w.p.vel_sleep_coeff * gm);
+        }
     }
     B->movement = movement;
     B->slot_bytes = 2 * max_hot;
@@ -1162,6 +1218,13 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
         x.shape = d_shape; x.world = d_world; x.movement = d_mov; x.material = d_mat;
         x.aabb_lo = A.take<float4>(N); x.aabb_hi = A.take<float4>(N);
         x.moved = A.take<int>(N);
+        if (has_sleep) {
+            x.has_sleep = 1;
+            x.hist_cap = hist_cap;
+            x.asleep = A.take<int>(N); x.waking = A.take<int>(N); x.ready_cnt = A.take<int>(N);
+            x.non_sleepy = A.take<int>(N); x.hist_n = A.take<int>(N); x.hist_head = A.take<int>(N);
+            x.hist = A.take<float>((size_t)N * hist_cap * 6);
+        }
         d_pool = A.take<uint8_t>(pool.size());
         x.shapes = d_pool;
         x.pair_count = A.take<int>(N);
@@ -1288,6 +1351,12 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     up(d_mov, movement.data(), N); up(d_mat, mat.data(), N * sizeof(float4));
     up(d_pool, pool.data(), pool.size());
     CK(cudaMemsetAsync(x.moved, 0, N * sizeof(int), B->st));
+    if (has_sleep) {
+        up(x.asleep, s_asleep.data(), N * 4); up(x.waking, s_waking.data(), N * 4); up(x.ready_cnt, s_ready.data(), N * 4);
+        up(x.non_sleepy, s_nons.data(), N * 4); up(x.hist_n, s_hn.data(), N * 4);
+        CK(cudaMemsetAsync(x.hist_head, 0, N * sizeof(int), B->st));
+        up(x.hist, s_hist.data(), s_hist.size() * 4);
+    }
     const int ne = (int)ekey.size(), nc = (int)cmag.size();
     up(es[0].key, ekey.data(), ne * 8); up(es[0].cstart, ecstart.data(), ne * 4); up(es[0].ccount, eccount.data(), ne * 4);
     up(cs[0].magic, cmag.data(), nc * 8);
@@ -1358,6 +1427,34 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
 // velocities, world inertia tensors, joint warm starts, the persistent contact
 // graph (dead contacts dropped, as the next merge would) and the last pair
 // list.  All arrays are read once and split per world.
+// The sleep state of one world's bodies (global range [g0, g0 + nb)) into
+// their host mirrors, the velocity records turned oldest first
+static void download_sleep(const Batch& B, int g0, World& w) {
+    const Dev& x = B.cur();
+    if (!x.has_sleep) return;
+    const int nb = (int)w.bodies.size(), cap = x.hist_cap;
+    std::vector<int> a(nb), wk(nb), rd(nb), ns(nb), hn(nb), hh(nb);
+    std::vector<float> h((size_t)nb * cap * 6);
+    CK(cudaMemcpyAsync(a.data(), x.asleep + g0, nb * 4, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(wk.data(), x.waking + g0, nb * 4, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(rd.data(), x.ready_cnt + g0, nb * 4, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(ns.data(), x.non_sleepy + g0, nb * 4, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(hn.data(), x.hist_n + g0, nb * 4, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(hh.data(), x.hist_head + g0, nb * 4, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaMemcpyAsync(h.data(), x.hist + (size_t)g0 * cap * 6, h.size() * 4, cudaMemcpyDeviceToHost, B.st));
+    CK(cudaStreamSynchronize(B.st));
+    const int len = std::max(1, (int)(w.p.sleep_delay / w.p.dt));
+    for (int i = 0; i < nb; i++) {
+        Body& b = w.bodies[i];
+        b.asleep = a[i]; b.waking = wk[i]; b.ready_cnt = rd[i]; b.non_sleepy = ns[i]; b.hist_n = hn[i];
+        b.hist.assign(6 * (size_t)hn[i], 0.f);
+        for (int q = 0; q < hn[i]; q++) {
+            const int slot = (hh[i] + q) % len;
+            for (int k = 0; k < 6; k++) b.hist[6 * q + k] = h[((size_t)i * cap + slot) * 6 + k];
+        }
+    }
+}
+
 static void download_worlds(Batch& B, const std::vector<World*>& ws) {
     const Dev& x = B.cur();
     const int N = B.n_bodies;
@@ -1463,6 +1560,7 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
                 w.contacts.push_back(c);
             }
         }
+        download_sleep(B, s0, w);
         w.last_pairs.clear();
         for (; p_cursor < np && pa[p_cursor] < s1; p_cursor++) {
             w.last_pairs.push_back((uint32_t)(pa[p_cursor] - s0) + 1);
@@ -1576,6 +1674,7 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
             }
         }
         w.last_pairs.clear();
+        download_sleep(B, s0, w);
     }
 }
 
@@ -1820,8 +1919,8 @@ SETTER(cpgpu_set_substep_count(cpgpu_world* w, int s), {
 SETTER(cpgpu_set_pgs_iterations(cpgpu_world* w, int v, int p, int h), {
     if (v < 0 || p < 0 || h < 0) throw ApiFail{CPGPU_ERR_INVALID_ARG, "negative iteration count"};
     w->w.p.pgs_vel = v; w->w.p.pgs_pos = p; w->w.p.pgs_holo = h; })
-SETTER(cpgpu_set_sleeping_enabled(cpgpu_world* w, int e), {
-    if (e) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "sleeping is not implemented on the device path"}; })
+// (bodies already asleep stay asleep until woken, as in the reference)
+SETTER(cpgpu_set_sleeping_enabled(cpgpu_world* w, int e), { w->w.p.sleeping = e != 0; })
 SETTER(cpgpu_set_warm_start_disabled(cpgpu_world* w, int d), { w->w.p.warm_disabled = d != 0; })
 SETTER(cpgpu_set_global_cfm(cpgpu_world* w, double c), { w->w.p.cfm = c; })
 SETTER(cpgpu_set_angle_vel_update_tick_count(cpgpu_world* w, int n), {
@@ -1955,11 +2054,23 @@ int cpgpu_body_mesh(cpgpu_world* w, const double* points, int n_points, const in
 
 int cpgpu_body_set_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {
     W_OR_FAIL(w);
-    return guarded([&] { begin_mutation(w->w); body_ref(w->w, id).vel = D3(v[0], v[1], v[2]); return CPGPU_OK; });
+    return guarded([&] {
+        begin_mutation(w->w);
+        Body& b = body_ref(w->w, id);
+        b.vel = D3(v[0], v[1], v[2]);
+        b.alert_waking();
+        return CPGPU_OK;
+    });
 }
 int cpgpu_body_set_ang_velocity(cpgpu_world* w, uint32_t id, const double v[3]) {
     W_OR_FAIL(w);
-    return guarded([&] { begin_mutation(w->w); body_ref(w->w, id).angv = D3(v[0], v[1], v[2]); return CPGPU_OK; });
+    return guarded([&] {
+        begin_mutation(w->w);
+        Body& b = body_ref(w->w, id);
+        b.angv = D3(v[0], v[1], v[2]);
+        b.alert_waking();
+        return CPGPU_OK;
+    });
 }
 // RigidBody::setOrientation (RigidBody.cpp:103-107): the orientation is set and
 // normalised by updateGeometry; the world inertia tensor keeps its value until
@@ -1970,6 +2081,7 @@ int cpgpu_body_set_orientation(cpgpu_world* w, uint32_t id, const double q[4]) {
         begin_mutation(w->w);
         Body& b = body_ref(w->w, id);
         b.q = qnorm(Quat{q[0], q[1], q[2], q[3]});
+        b.alert_waking();
         return CPGPU_OK;
     });
 }
@@ -1981,6 +2093,7 @@ int cpgpu_body_set_position(cpgpu_world* w, uint32_t id, const double p[3]) {
         D3 tracked = b.com + qrot(b.q, b.local_origin);
         b.com = b.com + (D3(p[0], p[1], p[2]) - tracked);
         b.q = qnorm(b.q);
+        b.alert_waking();
         return CPGPU_OK;
     });
 }

@@ -317,13 +317,20 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
     }
     __syncthreads();
     if (tid == 0) {
+        // sleeping (sleepOrSolveIslands, PhysicsEngine.cpp:1536-1613): a
+        // sleeping body's edges to sleeping or fixed bodies carry no rows, and
+        // an island whose bodies are all ready to sleep (and touch no
+        // kinematic body) falls asleep instead of being solved
+        const bool sleep_on = d.has_sleep != 0;                 // sleeping bodies may exist
+        const bool may_sleep = sleep_on && d.wparams[w].sleeping;   // islands may fall asleep
+        const int ready_steps = d.wparams[w].ready_steps;
         int rc = c0 + jj0, bc = s, ni = 0, sc = sys0;
         for (int t = s; t < e; t++) {
             const int node = fast ? order[t - s] : d.map_order[t] - s;
             if (mov[node] != 0 || vis[node] >= 0) continue;
             const int rs = rc, bs = bc, ss = sc;
             int sp = 0;
-            bool has_joint = false;
+            bool has_joint = false, all_ready = true;
             stk[sp++] = node;
             while (sp > 0) {
                 const int cur = stk[--sp];
@@ -331,14 +338,19 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
                 vis[cur] = bc - bs;
                 d.isl_bodies[bc++] = cur + s;
                 const int lo = a_ofs[cur], hi = a_cur[cur];
+                const bool cur_asleep = sleep_on && d.asleep[cur + s];
+                bool kinematic_contact = false;
                 // each edge to a not-yet-visited neighbour emits its rows, then
                 // the neighbour (if dynamic) is pushed; visits happen only at
                 // pops, so one pass over the edges gives the rows in edge order
                 // and the pushes in edge order
                 for (int j = lo; j < hi; j++) {
                     const int o = adj[2 * j], k = adj[2 * j + 1];
+                    if (mov[o] == 2) kinematic_contact = true;
                     if (vis[o] >= 0) continue;
-                    if (k < 0) {
+                    if (cur_asleep && (mov[o] == 1 || d.asleep[o + s])) {
+                        // no rows; the neighbour still joins the island
+                    } else if (k < 0) {
                         // joint edge: its holonomic system joins the island's
                         // list at first sight, then its joints' rows
                         const int je = -k - 1, sy = d.je.sys[je];
@@ -368,6 +380,26 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
                         else atomicOr(d.status, ST_STACK_OVERFLOW);
                     }
                 }
+                if (may_sleep && (kinematic_contact || d.ready_cnt[cur + s] < ready_steps)) all_ready = false;
+            }
+            if (may_sleep && all_ready) {
+                // the island falls asleep (RigidBody::sleep): zero velocities,
+                // its rows and systems are dropped, its edges' row slots freed
+                for (int q = bs; q < bc; q++) {
+                    const int g = d.isl_bodies[q];
+                    d.asleep[g] = 1;
+                    d.vel[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    d.angv[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    const int lb = g - s;
+                    for (int j = a_ofs[lb]; j < a_cur[lb]; j++) {
+                        const int k = adj[2 * j + 1];
+                        if (k >= 0 && d.edge_row[e0 + k] >= rs) d.edge_row[e0 + k] = -1;
+                    }
+                }
+                rc = rs;
+                bc = bs;
+                sc = ss;
+                continue;
             }
             if (rc > rs) {
                 d.isl_row_start[s + ni] = rs;

@@ -375,6 +375,16 @@ __global__ void k_joint_rows(Dev d) {
 // that it cannot reverse the relative velocity, measured at the reference's
 // crossed attachment points (RigidBody::getVelOfPoint, RigidBody.cpp:153-155)
 __device__ __forceinline__ void impulse_at(const Dev& d, int b, f3 imp, f3 at) {
+    if (d.has_sleep) {
+        // RigidBody::applyImpulse alerts the body (RigidBody.cpp:60-67,
+        // alertWaking): its island wakes at the next step and its sleep
+        // record restarts
+        d.waking[b] = 1;
+        d.ready_cnt[b] = 0;
+        d.non_sleepy[b] = 0;
+        d.hist_n[b] = 0;
+        d.hist_head[b] = 0;
+    }
     if (d.movement[b] != 0) return;   // RigidBody::applyImpulse on a fixed or kinematic body changes nothing
     const float4 p = d.pos[b];
     const f3 torque = cross(at - mk(p), imp);

@@ -18,6 +18,9 @@ void scan_exclusive(const int* in, int* out, const int* n_dev, int n_host, int c
 void prepare_kernels();   // one-time function attributes (outside graph capture)
 void set_last_error(const char* msg);   // message returned by cpgpu_last_error
 void launch_gravity(const Dev& d, const Launch& L);
+// the start of a step: gravity, or with sleeping enabled in the batch the
+// waking actions, the sleep bookkeeping and gravity (sleep.cu)
+void launch_step_begin(const Dev& d, const Launch& L);
 void launch_pairs(const Dev& d, const Launch& L);
 void launch_geometry(const Dev& d, int force_all, const Launch& L);
 // hull-hull pairs, then (when the batch holds spheres or cylinders) the pairs

@@ -102,7 +102,16 @@ struct WorldParams {
     int warm_disabled;
     int pgs_vel, pgs_pos;
     int pgs_holo;                // holonomic block-solve iterations (first substep)
-    int pad;
+    // sleeping (PhysicsEngine.h:219-224, PhysicsEngine.cpp:1221-1290): the
+    // thresholds as the reference forms them from its coefficients and |g|,
+    // and the step counts the host derives from its FP64 time arithmetic
+    int sleeping;                // 1: enabled
+    int hist_len;                // velocity history kept: (int)(sleep_delay / dt) steps
+    int hist_min;                // fewest recorded steps for bodySleepy: !(2 n < sleep_delay / dt)
+    int ready_steps;             // sleepy steps for readyToSleep: sleep_delay reached summing dt in FP64
+    int non_sleepy_threshold;
+    float vel_eps, ang_vel_eps, accel_eps, ang_accel_eps;
+    float wake_vel;              // a sleeping body faster than this after a solve wakes its island
 };
 
 // ---- status word bits ----------------------------------------------------------
@@ -367,6 +376,18 @@ struct Dev {
     // islands with at least this many rows take the warp-per-island solver,
     // the others the thread-per-island one (a schedule choice: same results)
     int big_rows;
+    // sleeping (has_sleep == 0: no world of the batch has it enabled).  Per
+    // body: asleep, waking (an API action or a spring impulse since the last
+    // step), sleepy-step count, non-sleepy count, and the last hist_cap
+    // (velocity, angular velocity) records as a ring (6 floats each)
+    int has_sleep, hist_cap;
+    int* asleep;
+    int* waking;
+    int* ready_cnt;
+    int* non_sleepy;
+    int* hist_n;
+    int* hist_head;
+    float* hist;
 };
 
 // per world: linear momentum xyz, angular momentum about the origin xyz,

@@ -346,6 +346,11 @@ __device__ __forceinline__ void stage_hull(const uint8_t* g, uint8_t* s, const f
 
 // collisionAllowed (PhysicsEngine.cpp:570-572): bodies joined by a joint do
 // not collide; the joint-edge keys are sorted, so one binary search decides
+// two sleeping bodies are not tested (PhysicsEngine.cpp:174)
+__device__ __forceinline__ bool both_asleep(const Dev& d, int a, int b) {
+    return d.has_sleep && d.asleep[a] && d.asleep[b];
+}
+
 __device__ __forceinline__ bool jointed(const Dev& d, int a, int b) {
     if (d.n_joint_edges == 0) return false;
     const uint64_t k = ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
@@ -1526,7 +1531,7 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
         // and collisionAllowed; after a timed-out wait the warp writes empty
         // manifolds for the rest of its pairs, so no later kernel reads a
         // previous step's
-        if (failed || !(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
+        if (failed || !(d.movement[a] == 0 || d.movement[b] == 0) || both_asleep(d, a, b) || jointed(d, a, b)) {
             if (lane == 0) { d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f); d.mf_cnt[p] = 0; }
             continue;
         }
@@ -1728,7 +1733,7 @@ __global__ void __launch_bounds__(256, 1) k_narrow_prim(Dev d, int slot_bytes) {
         const HullHeader* Hb = reinterpret_cast<const HullHeader*>(gb);
         const uint32_t ka = Ha->kind, kb = Hb->kind;
         if ((ka | kb) == SHAPE_HULL || ka == SHAPE_MESH || kb == SHAPE_MESH) continue;
-        if (failed || !(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
+        if (failed || !(d.movement[a] == 0 || d.movement[b] == 0) || both_asleep(d, a, b) || jointed(d, a, b)) {
             if (lane == 0) no_manifold(d, p);
             continue;
         }

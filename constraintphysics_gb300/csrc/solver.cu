@@ -167,8 +167,14 @@ __global__ void k_rows(Dev d, int first, int last) {
         // lifetime (PhysicsEngine.cpp:1378-1399, expiry :1434-1446)
         int life = cs_life(st);
         bool lv = live;
-        if (last) { life -= 1; lv = false; }
+        if (last) { life = life > -127 ? life - 1 : life; lv = false; }   // the 8-bit store saturates
         bool dead = cs_dead(st) || (first && life < 0);
+        if (dead && !cs_dead(st) && d.has_sleep) {
+            // Contact::isExpired (PersistentConstraint.h:74): a contact of a
+            // sleeping body does not expire
+            const uint64_t key = d.e_new.key[d.c_new.edge[c]];
+            if (d.asleep[(int)(key >> 32)] || d.asleep[(int)(key & 0xffffffffu)]) dead = false;
+        }
         // a rebuilt FrictionConstraint starts with static_ready = false
         d.c_new.state[c] = cs_make(life, lv, live ? false : cs_static(st), dead);
     }
@@ -317,15 +323,44 @@ __device__ void island_finish(const Dev& d, int rs, int rc, int bs, int bc, cons
         int cst = d.c_new.state[R.contact];
         d.c_new.state[R.contact] = R.stat ? (cst | (1 << 9)) : (cst & ~(1 << 9));
     }
+    bool wake = false;
     for (int k = t; k < bc; k += nt) {
         int g = d.isl_bodies[bs + k];
         if (d.movement[g] != 0) continue;
         const float4 A = dv[kDvF4 * k], B = dv[kDvF4 * k + 1], C = dv[kDvF4 * k + 2];
         float4 v = d.vel[g], w = d.angv[g], pv = d.pvel[g], pw = d.pangv[g];
-        d.vel[g] = make_float4(v.x + A.x, v.y + A.y, v.z + A.z, 0.f);
-        d.angv[g] = make_float4(w.x + A.w, w.y + B.x, w.z + B.y, 0.f);
+        v = make_float4(v.x + A.x, v.y + A.y, v.z + A.z, 0.f);
+        w = make_float4(w.x + A.w, w.y + B.x, w.z + B.y, 0.f);
+        d.vel[g] = v;
+        d.angv[g] = w;
         d.pvel[g] = make_float4(pv.x + B.z, pv.y + B.w, pv.z + C.x, 0.f);
         d.pangv[g] = make_float4(pw.x + C.y, pw.y + C.z, pw.z + C.w, 0.f);
+        if (d.has_sleep && d.asleep[g]) {
+            const float wv = d.wparams[d.world[g]].wake_vel;
+            wake = wake || mag(mk(v)) > wv || mag(mk(w)) > wv;
+        }
+    }
+    if (!d.has_sleep) return;
+    // sleeping bodies of a solved island (PhysicsEngine::applyVelocityChange,
+    // PhysicsEngine.cpp:1113-1136): one pushed faster than a quarter of the
+    // sleep velocity wakes the island (the island is the component
+    // wakeupIsland walks); otherwise they keep zero velocity.  The reference
+    // visits the bodies in an unordered_map's order, and a body zeroed before
+    // the waking one stays at rest there; here a wake takes precedence.
+    if (nt == 32) wake = __any_sync(0xffffffffu, wake);
+    for (int k = t; k < bc; k += nt) {
+        const int g = d.isl_bodies[bs + k];
+        if (d.movement[g] != 0 || !d.asleep[g]) continue;
+        if (wake) {
+            d.asleep[g] = 0;
+            d.ready_cnt[g] = 0;
+            d.non_sleepy[g] = 0;
+            d.hist_n[g] = 0;
+            d.hist_head[g] = 0;
+        } else {
+            d.vel[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+            d.angv[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
     }
 }
 
@@ -694,7 +729,7 @@ __device__ M33 crossm(f3 v) {
 __global__ void k_integrate(Dev d, int last) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
         const int mv = d.movement[i];
-        if (mv == 1) continue;
+        if (mv == 1 || (d.has_sleep && d.asleep[i])) continue;   // sleeping bodies stay put
         const WorldParams& P = d.wparams[d.world[i]];
         const float dt = P.dt_sub;
         float4 pos = d.pos[i], q = d.rot[i];

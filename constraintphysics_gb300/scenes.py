@@ -690,3 +690,18 @@ def twist_chain(rot_strength=15000.0):
     sc.ang_velocity(prev, (0.5, 9.0, 0.0))
     sc.velocity(prev, (2.0, 0.0, 0.0))
     return sc
+
+
+def sleep_stacks(seed=0):
+    """Three stacks of three boxes and a ball on the plate with sleeping
+    enabled (dt 1/60, 1 substep, PGS (10,1,1)).  Returns the scene, the ball's
+    id and an x position above the middle stack (for dropping the ball)."""
+    params = dict(step_time=1.0 / 60.0, substeps=1, pgs=(10, 1, 1), sleeping=True)
+    sc = Scene(f"sleepers_{seed}", params)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, PILE_MATERIAL, FIXED)
+    rng = np.random.default_rng(seed)
+    for i in range(3):
+        for j in range(3):
+            sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, PILE_MATERIAL, DYNAMIC, (3.0 * i - 3, 0.6 + 1.05 * j, 0.1 * rng.uniform()))
+    ball = sc.sphere((0, 0, 0), 0.5, PILE_MATERIAL, DYNAMIC, (8.0, 2.0, 0.0))
+    return sc, ball, 3.0 + 0.2 * rng.uniform()

@@ -90,8 +90,13 @@ int cpgpu_set_gravity(cpgpu_world* w, double gx, double gy, double gz);
 int cpgpu_set_substep_count(cpgpu_world* w, int substeps);
 /* PhysicsEngine::setPGSIterations (PhysicsEngine.h:90) */
 int cpgpu_set_pgs_iterations(cpgpu_world* w, int n_vel, int n_pos, int n_holonomic);
-/* PhysicsEngine::setSleepingEnabled (PhysicsEngine.cpp:1138-1140); the device
- * path implements sleeping disabled only and rejects enabling it. */
+/* PhysicsEngine::setSleepingEnabled (PhysicsEngine.cpp:1138-1140).  Worlds
+ * start with sleeping disabled (the reference's default is enabled); bodies
+ * already asleep stay asleep until woken when it is disabled again, as in the
+ * reference.  Sleeping follows PhysicsEngine.cpp:65-87, 174, 1113-1136,
+ * 1221-1290 and 1536-1613; where the reference's outcome depends on an
+ * unordered_map's iteration order (a sleeping island that one body wakes
+ * while another would have been stopped), a wake takes precedence. */
 int cpgpu_set_sleeping_enabled(cpgpu_world* w, int enabled);
 /* PhysicsEngine::setWarmStartDisabled (PhysicsEngine.cpp:1182-1184) */
 int cpgpu_set_warm_start_disabled(cpgpu_world* w, int disabled);

@@ -429,16 +429,7 @@ def test_raycast_restatement_matches_reference(oracle_mod):
 
 
 def _sleep_scene(seed):
-    params = dict(step_time=1.0 / 60.0, substeps=1, pgs=(10, 1, 1), sleeping=True)
-    sc = scenes.Scene(f"sleepers_{seed}", params)
-    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, scenes.PILE_MATERIAL, scenes.FIXED)
-    rng = np.random.default_rng(seed)
-    for i in range(3):
-        for j in range(3):
-            sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, scenes.PILE_MATERIAL, scenes.DYNAMIC,
-                   (3.0 * i - 3, 0.6 + 1.05 * j, 0.1 * rng.uniform()))
-    ball = sc.sphere((0, 0, 0), 0.5, scenes.PILE_MATERIAL, scenes.DYNAMIC, (8.0, 2.0, 0.0))
-    return sc, ball, 3.0 + 0.2 * rng.uniform()
+    return scenes.sleep_stacks(seed)
 
 
 @pytest.mark.parametrize("seed", [0, 2])
