@@ -51,6 +51,7 @@ SIGNATURES = {
     "step": (I, [P, I]),
     "num_bodies": (I, [P, P]),
     "get_body_state": (I, [P, P, P, P, P]),
+    "get_asleep": (I, [P, P]),
     "set_body_state": (I, [P, P, P, P, P]),
     "get_aabbs": (I, [P, P]),
     "get_pairs": (I, [P, P, I, P]),

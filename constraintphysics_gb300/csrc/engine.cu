@@ -158,7 +158,24 @@ struct World {
     std::unique_ptr<Batch> dev;
     bool dev_valid = false;
     bool audit = false;                            // FP64 audit requested (cpgpu_world_set_audit)
+    uint64_t version = 0;                          // API mutations so far (a batch checks it before re-packing)
 };
+
+// A world's description and host state without its device copy: the
+// autotuner's private copies.  The node map is copied, not re-inserted, so
+// its iteration order (island and system order) is the source's.
+static void copy_world(const World& s, World& c) {
+    c.p = s.p;
+    c.shapes = s.shapes;
+    c.bodies = s.bodies;
+    c.joints = s.joints;
+    c.springs = s.springs;
+    c.constraint_seq = s.constraint_seq;
+    c.nodes = s.nodes;
+    c.contacts = s.contacts;
+    c.last_pairs = s.last_pairs;
+    c.audit = s.audit;
+}
 
 // ---------------------------------------------------------------- shape packing ----
 static void put16(std::vector<uint8_t>& b) { while (b.size() % 16) b.push_back(0); }
@@ -1689,6 +1706,7 @@ static void download_state(World& w) {
 static void begin_mutation(World& w) {
     if (w.dev && w.dev_valid) download_state(w);
     w.dev_valid = false;
+    w.version++;
 }
 
 static void update_cutoff(World& w) { w.p.cutoff = 2 * w.p.g.mag() * w.p.dt; }
@@ -1811,7 +1829,14 @@ struct Schedule {
 };
 }  // namespace cpgpu
 
-struct cpgpu_world { World w; };
+// A world handle.  Batches pin the worlds they were made from (the
+// autotuner re-packs from them): cpgpu_world_destroy of a pinned world only
+// marks it, and the last batch holding it frees it.
+struct cpgpu_world {
+    World w;
+    int batch_refs = 0;
+    bool dropped = false;
+};
 // A batch of worlds, split by world size into parts that step concurrently,
 // each on its own streams with its own graphs.  A step is bounded by the
 // longest serial Gauss-Seidel chain of its largest island; with the largest
@@ -1831,6 +1856,15 @@ struct cpgpu_batch {
     bool tuned = false;                   // chosen by the autotuner (now or from its cache)
     double tuned_ms = -1, default_ms = -1;   // per step, measured when tuned here
     std::vector<World*> worlds;           // the worlds, in batch order (their host mirrors)
+    std::vector<cpgpu_world*> pins;       // the handles pinned by this batch (API-made batches)
+    std::vector<uint64_t> versions;       // the worlds' mutation counts when the batch was made
+    void pin(cpgpu_world* const* ws, int n) {
+        for (int i = 0; i < n; i++) {
+            ws[i]->batch_refs++;
+            pins.push_back(ws[i]);
+            versions.push_back(ws[i]->w.version);
+        }
+    }
     void release() {
         for (int* r : rows) if (r) cudaFree(r);
         if (stage) cudaFree(stage);
@@ -1842,7 +1876,11 @@ struct cpgpu_batch {
         stage = nullptr; ev0 = ev1 = fork = nullptr;
         parts.clear();
     }
-    ~cpgpu_batch() { release(); }
+    ~cpgpu_batch() {
+        release();
+        for (cpgpu_world* w : pins)
+            if (--w->batch_refs == 0 && w->dropped) delete w;
+    }
     // take over another batch object's device resources (this one's are freed)
     void adopt(cpgpu_batch& o) {
         release();
@@ -1853,8 +1891,7 @@ struct cpgpu_batch {
         rows = std::move(o.rows); o.rows.clear();
         ev0 = o.ev0; ev1 = o.ev1; fork = o.fork; o.ev0 = o.ev1 = o.fork = nullptr;
         done = std::move(o.done); o.done.clear();
-        sched = o.sched;
-        worlds = o.worlds;
+        sched = o.sched;   // the worlds, pins and versions stay this batch's
     }
     Batch& part(int p) { return *parts[p]; }
     cudaStream_t st0() { return parts[0]->st; }
@@ -1902,7 +1939,14 @@ int cpgpu_world_create(cpgpu_world** out) {
         return CPGPU_OK;
     });
 }
-int cpgpu_world_destroy(cpgpu_world* w) { delete w; return CPGPU_OK; }
+int cpgpu_world_destroy(cpgpu_world* w) {
+    if (w && w->batch_refs > 0) {
+        w->dropped = true;   // freed with the last batch made from it
+        return CPGPU_OK;
+    }
+    delete w;
+    return CPGPU_OK;
+}
 
 #define SETTER(name, ...)                                                           \
     int name {                                                                      \
@@ -2358,6 +2402,19 @@ int cpgpu_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel,
     });
 }
 
+int cpgpu_get_asleep(cpgpu_world* w, int* flags) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!flags) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null output"};
+        if (w->w.dev && w->w.dev_valid) download_state(w->w);
+        for (size_t i = 0; i < w->w.bodies.size(); i++) {
+            const Body& b = w->w.bodies[i];
+            flags[i] = (b.asleep && b.movement == CPGPU_DYNAMIC) ? 1 : 0;
+        }
+        return CPGPU_OK;
+    });
+}
+
 // Checkpoint restore of the dynamic state: poses and velocities are replaced
 // and the world inertia tensors recomputed from the new orientations.
 int cpgpu_set_body_state(cpgpu_world* w, const double* com, const double* quat, const double* vel, const double* ang) {
@@ -2652,6 +2709,7 @@ int cpgpu_batch_create(cpgpu_world* const* worlds, int n, cpgpu_batch** out) {
         }
         auto b = make_batch(ws, S);
         b->tuned = tuned;
+        b->pin(worlds, n);
         *out = b.release();
         return CPGPU_OK;
     });
@@ -2683,13 +2741,24 @@ static double time_steps(cpgpu_batch* b, int n) {
 // same histogram start with it.
 static void tune_batch(cpgpu_batch* b, int trial_steps) {
     const int T = std::max(1, trial_steps);
+    for (size_t i = 0; i < b->worlds.size(); i++)
+        if (i < b->versions.size() && b->worlds[i]->version != b->versions[i])
+            throw ApiFail{CPGPU_ERR_INVALID_ARG, "a world changed after the batch was made from it: make a new batch"};
+    // private copies of the worlds carry the batch's current state; the
+    // worlds' own host mirrors are left as they are
+    std::vector<std::unique_ptr<World>> copies(b->worlds.size());
+    std::vector<World*> ws(b->worlds.size());
+    for (size_t i = 0; i < copies.size(); i++) {
+        copies[i] = std::make_unique<World>();
+        copy_world(*b->worlds[i], *copies[i]);
+        ws[i] = copies[i].get();
+    }
     for (size_t p = 0; p < b->parts.size(); p++) {
         std::vector<World*> sub;
-        for (size_t wi = 0; wi < b->worlds.size(); wi++)
-            if (b->part_of[wi] == (int)p) sub.push_back(b->worlds[wi]);
+        for (size_t wi = 0; wi < ws.size(); wi++)
+            if (b->part_of[wi] == (int)p) sub.push_back(ws[wi]);
         download_worlds(*b->parts[p], sub);
     }
-    const std::vector<World*> ws = b->worlds;
     const Schedule dflt = default_schedule(ws);
     std::vector<Schedule> layouts{dflt};
     auto add = [&](int parts, int share) {
@@ -2757,6 +2826,7 @@ int cpgpu_batch_create_tuned(cpgpu_world* const* worlds, int n, int trial_steps,
         if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null output"};
         const std::vector<World*> ws = batch_worlds(worlds, n);
         auto b = make_batch(ws, default_schedule(ws));
+        b->pin(worlds, n);
         tune_batch(b.get(), trial_steps);
         *out = b.release();
         return CPGPU_OK;
@@ -2985,14 +3055,7 @@ int cpgpu_world_clone(cpgpu_world* src, cpgpu_world** out) {
         if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null out"};
         if (src->w.dev && src->w.dev_valid) download_state(src->w);
         auto c = std::make_unique<cpgpu_world>();
-        c->w.p = src->w.p;
-        c->w.shapes = src->w.shapes;
-        c->w.bodies = src->w.bodies;
-        c->w.joints = src->w.joints;
-        c->w.contacts = src->w.contacts;
-        c->w.last_pairs = src->w.last_pairs;
-        // same insert sequence, so the same iteration order
-        for (size_t i = 0; i < src->w.bodies.size(); i++) c->w.nodes[(unsigned)(i + 1)] = (int)i;
+        copy_world(src->w, c->w);
         *out = c.release();
         return CPGPU_OK;
     });

@@ -167,8 +167,8 @@ struct alignas(16) RowBlock {
     float tgt_n, tgt_f0, tgt_f1;   // velocity targets (findTargetConstraintValue)
     float fcoeff;
     float nminv, nptarget;
-    float kf0, kf1;      // J_f M^-1 J_n^T of friction rows u, w: their velocity change per unit normal impulse
-    float fminv[4];
+    float kd0, kd1;      // friction impulse change per unit normal impulse: Fm^-1 (J_f M^-1 J_n^T)
+    float fmc[4];        // the friction rows' 2x2 effective-mass inverse Fm^-1 by columns: (m00, m10), (m01, m11)
     float nja[6], njb[6], nita[6], nitb[6];          // normal row J and M^-1 J^T (bodies a, b)
     float fja0[6], fjb0[6], fja1[6], fjb1[6];        // friction rows (u, w)
     float fita0[6], fitb0[6], fita1[6], fitb1[6];    // friction M^-1 J^T columns (u, w)

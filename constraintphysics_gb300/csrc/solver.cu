@@ -136,9 +136,14 @@ __global__ void k_rows(Dev d, int first, int last) {
             fv[0] *= (1.0f + P.cfm);
             fv[3] *= (1.0f + P.cfm);
             float di = 1.0f / (fv[0] * fv[3] - fv[1] * fv[2]);
-            R.fminv[0] = fv[3] * di; R.fminv[1] = -fv[1] * di; R.fminv[2] = -fv[2] * di; R.fminv[3] = fv[0] * di;
-            R.kf0 = dot6(fja, ia) + dot6(fjb, ib);
-            R.kf1 = dot6(fja + 6, ia) + dot6(fjb + 6, ib);
+            const float m00 = fv[3] * di, m01 = -fv[1] * di, m10 = -fv[2] * di, m11 = fv[0] * di;
+            R.fmc[0] = m00; R.fmc[1] = m10; R.fmc[2] = m01; R.fmc[3] = m11;
+            // the friction values' change per unit normal impulse (J_f M^-1 J_n^T),
+            // mapped through Fm^-1 to the friction impulses' change
+            const float kf0 = dot6(fja, ia) + dot6(fjb, ib);
+            const float kf1 = dot6(fja + 6, ia) + dot6(fjb + 6, ib);
+            R.kd0 = m00 * kf0 + m01 * kf1;
+            R.kd1 = m10 * kf0 + m11 * kf1;
             for (int k = 0; k < 6; k++) {
                 R.fja0[k] = fja[k]; R.fjb0[k] = fjb[k]; R.fja1[k] = fja[6 + k]; R.fjb1[k] = fjb[6 + k];
                 R.fita0[k] = fia[2 * k]; R.fitb0[k] = fib[2 * k]; R.fita1[k] = fia[2 * k + 1]; R.fitb1[k] = fib[2 * k + 1];
@@ -182,12 +187,20 @@ __global__ void k_rows(Dev d, int first, int last) {
 
 // ---- packed FP32 pairs: a row's 6-vectors and a body's Δv are handled as
 // the three component pairs (x, y), (z, ax), (ay, az), two lanes of one
-// fma.rn.f32x2 each (half the instructions of scalar FP32 on the chain)
+// fma.rn.f32x2 each (half the instructions of scalar FP32 on the chain).
+// Every operation of the rows is written with an explicit round-to-nearest
+// intrinsic: the row functions are inlined into several kernels (warp per
+// island, thread per island, joint islands), and left to the compiler, a
+// sum of two products could be contracted into a different FMA in each;
+// spelled out, every kernel computes the same bits, so the island-size
+// threshold between the kernels never changes a result.
 struct P3 { float2 a, b, c; };
 __device__ __forceinline__ P3 p3(const float* f) {
     return P3{make_float2(f[0], f[1]), make_float2(f[2], f[3]), make_float2(f[4], f[5])};
 }
 __device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
+// x - y, rounded once (y times -1 is exact)
+__device__ __forceinline__ float2 psub(float2 x, float2 y) { return __ffma2_rn(y, make_float2(-1.f, -1.f), x); }
 // J_a v_a + J_b v_b
 __device__ __forceinline__ float pdot(const P3& ja, const P3& va, const P3& jb, const P3& vb) {
     float2 s = __fmul2_rn(ja.a, va.a);
@@ -197,7 +210,7 @@ __device__ __forceinline__ float pdot(const P3& ja, const P3& va, const P3& jb, 
     t = __ffma2_rn(jb.b, vb.b, t);
     t = __ffma2_rn(jb.c, vb.c, t);
     const float2 u = __fadd2_rn(s, t);
-    return u.x + u.y;
+    return __fadd_rn(u.x, u.y);
 }
 // v += x * s
 __device__ __forceinline__ void paxpy(P3& v, const P3& x, float2 s) {
@@ -256,56 +269,60 @@ __device__ __forceinline__ void row_warm(const RowBlock& R, const float4 imp, fl
 // velocity pass: normal row clamped at zero, then the friction rows projected on
 // the friction disc of the current normal impulse (PGSConstraintStep,
 // ConstraintSolver.cpp:12-40; projections :270-272, :331-343).  The friction
-// rows see the velocities after the normal change; that is evaluated as the
-// friction values of the incoming velocities plus the normal change times the
-// row's coupling constants kf0/kf1 (the same quantity, associated
-// differently), so that both dot products run alongside the normal one instead
-// of after it.  The disc projection compares squared magnitudes and scales by
-// rsqrt.
+// rows see the velocities after the normal change; their new impulses are
+// evaluated as (impulses + Fm^-1 (targets - values of the incoming
+// velocities)) minus the normal change times the row's constants
+// kd = Fm^-1 J_f M^-1 J_n^T (the same quantity, associated differently), so
+// that everything but one FMA per friction row runs alongside the normal row
+// instead of after it; the normal row's velocity change is applied while the
+// friction rows are evaluated.  The disc projection compares squared
+// magnitudes and scales by rsqrt.  Δv is written back unconditionally (a zero
+// change writes the same values).
 __device__ __forceinline__ void row_vel(const RowBlock& R, float4& imp, int& stat, float4* dv) {
     P3 va = dv_get(dv, R.sa, 0), vb = dv_get(dv, R.sb, 0);
     const float cur = pdot(p3(R.nja), va, p3(R.njb), vb);
     const float b0 = pdot(p3(R.fja0), va, p3(R.fjb0), vb), b1 = pdot(p3(R.fja1), va, p3(R.fjb1), vb);
-    const float nw = imp.x + R.nminv * (R.tgt_n - cur);
-    float diff = fmaxf(nw, 0.0f) - imp.x;
+    // friction impulses for the incoming velocities: imp.zw + Fm^-1 (tgt_f - b)
+    const float2 g = psub(make_float2(R.tgt_f0, R.tgt_f1), make_float2(b0, b1));
+    const float2 A = __fadd2_rn(make_float2(imp.z, imp.w),
+                                __ffma2_rn(make_float2(R.fmc[2], R.fmc[3]), bc2(g.y),
+                                           __fmul2_rn(make_float2(R.fmc[0], R.fmc[1]), bc2(g.x))));
+    const float nw = __fmaf_rn(R.nminv, __fsub_rn(R.tgt_n, cur), imp.x);
+    float diff = __fsub_rn(fmaxf(nw, 0.0f), imp.x);
     if (!(fabsf(diff) > kZero)) diff = 0.f;
-    const float ix = imp.x + diff;
-    const float c0 = fmaf(diff, R.kf0, b0), c1 = fmaf(diff, R.kf1, b1);
-    const float d0 = R.tgt_f0 - c0, d1 = R.tgt_f1 - c1;
-    float n0 = imp.z + (d0 * R.fminv[0] + d1 * R.fminv[1]);
-    float n1 = imp.w + (d0 * R.fminv[2] + d1 * R.fminv[3]);
-    const float mx = R.fcoeff * ix;
-    const float s2 = n0 * n0 + n1 * n1;
-    if (s2 > mx * mx) { const float sc = mx * rsqrtf(s2); n0 *= sc; n1 *= sc; stat = 0; }
+    const float ix = __fadd_rn(imp.x, diff);
+    const float2 sd = bc2(diff);
+    paxpy(va, p3(R.nita), sd);
+    paxpy(vb, p3(R.nitb), sd);
+    float2 nf = __ffma2_rn(bc2(-diff), make_float2(R.kd0, R.kd1), A);
+    const float mx = __fmul_rn(R.fcoeff, ix);
+    const float s2 = __fmaf_rn(nf.x, nf.x, __fmul_rn(nf.y, nf.y));
+    if (s2 > __fmul_rn(mx, mx)) { nf = __fmul2_rn(nf, bc2(__fmul_rn(mx, rsqrtf(s2)))); stat = 0; }
     else stat = 1;
-    float e0 = n0 - imp.z, e1 = n1 - imp.w;
-    if (!(fabsf(e0) > kZero || fabsf(e1) > kZero)) { e0 = 0.f; e1 = 0.f; }
-    if (diff != 0.f || e0 != 0.f || e1 != 0.f) {
-        const float2 sd = bc2(diff), s0 = bc2(e0), s1 = bc2(e1);
-        paxpy(va, p3(R.nita), sd);
-        paxpy(vb, p3(R.nitb), sd);
-        paxpy(va, p3(R.fita0), s0);
-        paxpy(vb, p3(R.fitb0), s0);
-        paxpy(va, p3(R.fita1), s1);
-        paxpy(vb, p3(R.fitb1), s1);
-        dv_put(dv, R.sa, 0, va);
-        dv_put(dv, R.sb, 0, vb);
-    }
+    float2 e = psub(nf, make_float2(imp.z, imp.w));
+    if (!(fabsf(e.x) > kZero || fabsf(e.y) > kZero)) e = make_float2(0.f, 0.f);
+    const float2 s0 = bc2(e.x), s1 = bc2(e.y);
+    paxpy(va, p3(R.fita0), s0);
+    paxpy(vb, p3(R.fitb0), s0);
+    paxpy(va, p3(R.fita1), s1);
+    paxpy(vb, p3(R.fitb1), s1);
+    dv_put(dv, R.sa, 0, va);
+    dv_put(dv, R.sb, 0, vb);
     imp.x = ix;
-    imp.z += e0;
-    imp.w += e1;
+    imp.z = __fadd_rn(imp.z, e.x);
+    imp.w = __fadd_rn(imp.w, e.y);
 }
 
 // pseudo-velocity (position correction) pass of the normal row
 __device__ __forceinline__ void row_pos(const RowBlock& R, float4& imp, float4* dv) {
     P3 va = dv_get(dv, R.sa, 1), vb = dv_get(dv, R.sb, 1);
     const float cur = pdot(p3(R.nja), va, p3(R.njb), vb);
-    const float nw = imp.y + R.nminv * (R.nptarget - cur);
-    const float diff = fmaxf(nw, 0.0f) - imp.y;
+    const float nw = __fmaf_rn(R.nminv, __fsub_rn(R.nptarget, cur), imp.y);
+    const float diff = __fsub_rn(fmaxf(nw, 0.0f), imp.y);
     if (fabsf(diff) > kZero) {
         paxpy(va, p3(R.nita), bc2(diff));
         paxpy(vb, p3(R.nitb), bc2(diff));
-        imp.y += diff;
+        imp.y = __fadd_rn(imp.y, diff);
         dv_put(dv, R.sa, 1, va);
         dv_put(dv, R.sb, 1, vb);
     }

@@ -286,6 +286,14 @@ class World:
         self._check(self.abi.get_body_state(self.h, _ptr(com), _ptr(quat), _ptr(vel), _ptr(ang)))
         return {"com": com, "quat": quat, "vel": vel, "ang_vel": ang}
 
+    def asleep(self):
+        """Per body, 1 when asleep (RigidBody::getAsleep), as int32."""
+        n = C.c_int()
+        self._check(self.abi.num_bodies(self.h, C.addressof(n)))
+        out = np.zeros(n.value, dtype=np.int32)
+        self._check(self.abi.get_asleep(self.h, _ptr(out)))
+        return out
+
     def set_state(self, com=None, quat=None, vel=None, ang_vel=None):
         arrs = [None if a is None else _f64(a) for a in (com, quat, vel, ang_vel)]
         self._check(self.abi.set_body_state(self.h, *[_ptr(a) for a in arrs]))

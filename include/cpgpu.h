@@ -80,7 +80,9 @@ typedef struct cpgpu_contact {
 /* ---- world lifetime and parameters ------------------------------------- */
 /* PhysicsEngine::PhysicsEngine() with the defaults of PhysicsEngine.h:170-227 */
 int cpgpu_world_create(cpgpu_world** out);
-/* PhysicsEngine::~PhysicsEngine (PhysicsEngine.cpp:31-37) */
+/* PhysicsEngine::~PhysicsEngine (PhysicsEngine.cpp:31-37).  A world that a
+ * live batch was made from is freed when the last such batch is destroyed
+ * (the handle must not be used after this call either way). */
 int cpgpu_world_destroy(cpgpu_world* w);
 /* PhysicsEngine::setStep_time (PhysicsEngine.cpp:1214-1217) */
 int cpgpu_set_step_time(cpgpu_world* w, double dt);
@@ -246,6 +248,9 @@ int cpgpu_num_bodies(cpgpu_world* w, int* n);
  * any output pointer may be NULL.  com/vel/ang_vel: 3 doubles per body,
  * quat: 4 doubles (r,i,j,k) per body. */
 int cpgpu_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel, double* ang_vel);
+/* RigidBody::getAsleep (RigidBody.h:35) for every body in id order:
+ * flags[i] = 1 for a dynamic body that is asleep, else 0. */
+int cpgpu_get_asleep(cpgpu_world* w, int* flags);
 /* Overwrite the dynamic state of every body (a checkpoint restore); any input
  * pointer may be NULL.  The world geometry follows the new poses. */
 int cpgpu_set_body_state(cpgpu_world* w, const double* com, const double* quat,
@@ -294,7 +299,9 @@ int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
 /* ---- batched worlds ----------------------------------------------------- */
 /* Pack independent worlds into one device batch (segmented arrays) that one
  * launch sequence per step advances.  The worlds keep their own state; the
- * batch starts from their current state and the substep count must agree. */
+ * batch starts from their current state and the substep count must agree.
+ * The batch holds on to the worlds (cpgpu_world_destroy frees them only with
+ * the batch): the autotuner re-packs the batch from their descriptions. */
 int cpgpu_batch_create(cpgpu_world* const* worlds, int n_worlds, cpgpu_batch** out);
 /* Autotuner (no counterpart in the reference): re-chooses the batch's
  * schedule by timing from its current state.  Candidate schedules -- one, two
@@ -303,7 +310,9 @@ int cpgpu_batch_create(cpgpu_world* const* worlds, int n_worlds, cpgpu_batch** o
  * per SM and the island size from which an island takes the warp-per-island
  * solver -- are built from the current state, timed on `trial_steps` steps,
  * the state restored after each trial, and the fastest adopted; the batch
- * continues from exactly the state it had.  Tune from a representative state
+ * continues from exactly the state it had, and the worlds' own state is not
+ * touched.  CPGPU_ERR_INVALID_ARG if a world was changed through the API
+ * after the batch was made from it.  Tune from a representative state
  * (e.g. after some steps: before bodies touch, a step costs far less).  The
  * choice is cached per world-size histogram (log2 bins of the body counts),
  * for the process and, when the environment variable CPGPU_TUNE_FILE names a

@@ -1759,6 +1759,11 @@ int cport_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel,
     }
     return CPGPU_OK;
 }
+int cport_get_asleep(cpgpu_world* w, int* flags) {
+    World* x = W(w);
+    for (size_t i = 0; i < x->bodies.size(); i++) flags[i] = x->bodies[i]->getAsleep() ? 1 : 0;
+    return CPGPU_OK;
+}
 // State import: poses and velocities, then the derived tensors and geometry
 // are recomputed from the new poses.
 int cport_set_body_state(cpgpu_world* w, const double* com, const double* quat, const double* vel, const double* ang) {

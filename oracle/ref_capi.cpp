@@ -416,6 +416,11 @@ int cpref_get_body_state(cpgpu_world* w, double* com, double* quat, double* vel,
     return CPGPU_OK;
 }
 
+int cpref_get_asleep(cpgpu_world* w, int* flags) {
+    for (size_t i = 0; i < RW->bodies.size(); i++) flags[i] = RW->bodies[i]->getAsleep() ? 1 : 0;
+    return CPGPU_OK;
+}
+
 int cpref_get_aabbs(cpgpu_world* w, double* out) {
     for (size_t i = 0; i < RW->bodies.size(); i++) {
         phyz::AABB a = RW->bodies[i]->getAABB();

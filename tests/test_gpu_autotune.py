@@ -73,3 +73,26 @@ def test_autotuned_batch_starts_from_the_worlds_and_matches_the_default():
     again = cg.Batch(_build(scs))
     s2 = again.schedule()
     assert s2["tuned"] and s2["parts"] == sch["parts"] and s2["big_island_rows"] == sch["big_island_rows"]
+
+
+def test_tuning_leaves_the_worlds_alone_and_refuses_changed_ones():
+    scs = _worlds(40, seed=5)
+    ws = _build(scs)
+    before = [w.state() for w in ws]
+    b = cg.Batch(ws)
+    b.step(10)
+    b.tune(1)
+    for w, s0 in zip(ws, before):         # the worlds' own state is untouched
+        s1 = w.state()
+        for k in s0:
+            assert np.array_equal(s0[k], s1[k]), k
+    ws[3].set_velocity(ws[3].n_bodies, (0.0, 1.0, 0.0))   # a world changed after the batch was made
+    with pytest.raises(cg.CPGPUError):
+        b.tune(1)
+    b.close()
+    # worlds dropped while a batch made from them lives stay valid for it
+    b2 = cg.Batch(_build(scs))
+    b2.step(5)
+    b2.tune(1)
+    b2.step(2)
+    b2.close()

@@ -192,7 +192,9 @@ def test_single_step_parity_capsule_drop(oracle_mod, terrain, k):
     by_id, by_pos, miss_p, miss_g = _match(cg_, cp_)
     n = len(by_id) + by_pos + len(miss_p)
     assert n > 10
-    assert len(miss_p) + len(miss_g) <= 0.05 * n, (len(by_id), by_pos, len(miss_p), len(miss_g))
+    # a contact at a near-tie (two features or triangles equally deep in FP32
+    # and FP64) is missing on both sides: one such contact, or 5 %
+    assert len(miss_p) + len(miss_g) <= max(2, 0.05 * n), (len(by_id), by_pos, len(miss_p), len(miss_g))
     sg, sp = g.state(), p.state()
     dv = np.linalg.norm(sg["vel"] - sp["vel"], axis=1)
     vm = np.linalg.norm(sp["vel"], axis=1)

@@ -6,8 +6,8 @@ islands fall asleep (zero velocity, no solve, no integration), a velocity set
 on a sleeping box wakes its stack at step 150, the ball dropped onto a stack
 at step 300 wakes it through the contact, and the boxes fall asleep again.
 The device follows the restatement's sleep events step for step (the set of
-sleeping bodies, read as bodies with exactly zero velocity) except where a
-sleep test sits at its threshold, and its settled positions agree within
+sleeping bodies, RigidBody::getAsleep) except where a sleep test sits at its
+threshold, and its settled positions agree within
 FP32 tolerance.
 """
 import numpy as np
@@ -28,10 +28,9 @@ def _run(w, ball, x, steps=500, record=None):
             w.set_position(ball, (x, 4.5, 0.1))
             w.set_velocity(ball, (0.0, -3.0, 0.0))
         w.step(1)
-        st = w.state()
-        asleep.append(tuple((np.linalg.norm(st["vel"], axis=1) == 0).astype(int)))
+        asleep.append(tuple(int(x) for x in w.asleep()))
         if record is not None and s in record:
-            record[s] = st["com"].copy()
+            record[s] = w.state()["com"].copy()
     return asleep
 
 
@@ -46,10 +45,10 @@ def test_sleep_events_follow_the_restatement(oracle_mod, seed):
     ag = _run(g, ball, x, record=rg)
     ap = _run(p, ball, x, record=rp)
     n = len(ag[0])
-    # all bodies asleep before each waking action, on both
-    assert sum(ag[149]) == n and sum(ag[299]) == n, (sum(ag[149]), sum(ag[299]))
+    # every dynamic body (all but the plate) asleep before each waking action
+    assert sum(ag[149]) == n - 1 and sum(ag[299]) == n - 1, (sum(ag[149]), sum(ag[299]))
     # the actions wake bodies on the device too
-    assert sum(ag[151]) < n and min(sum(a) for a in ag[300:330]) < n - 2
+    assert sum(ag[151]) < n - 1 and min(sum(a) for a in ag[300:330]) < n - 3
     # the same sleeping set as the restatement on all but a few steps
     differ = [s for s in range(500) if ag[s] != ap[s]]
     assert len(differ) <= 10, differ
