@@ -40,6 +40,12 @@ SIGNATURES = {
     "body_set_position": (I, [P, U32, P]),
     "body_set_mass": (I, [P, U32, D]),
     "add_ball_socket": (I, [P, U32, U32, P, P, D, P]),
+    "add_motor": (I, [P, U32, D, D, P]),
+    "add_piston": (I, [P, U32, D, D, P]),
+    "set_motor": (I, [P, U32, I, D, D]),
+    "set_piston": (I, [P, U32, I, D, D]),
+    "get_motor_position": (I, [P, U32, P]),
+    "get_piston_position": (I, [P, U32, P]),
     "add_distance": (I, [P, U32, U32, P, P, D, D, P]),
     "add_weld": (I, [P, U32, U32, P, P, D, D, P]),
     "add_spring": (I, [P, U32, U32, P, P, D, D, D, P]),

@@ -120,13 +120,17 @@ __global__ void k_clamp_pairs(Dev d) {
 
 // RigidBody::updateGeometry (RigidBody.cpp:281-312) for moved bodies: the
 // orientation is renormalised and the AABB recomputed from the world geometry
-// (gen_AABB of the body's primitive).
-__global__ void k_geometry(Dev d, int force_all) {
+// (gen_AABB of the body's primitive).  `mode` 2 (a batch's first pass): every
+// body's AABB, the orientations flagged in `moved` (poses set through the
+// API) renormalised.
+__global__ void k_geometry(Dev d, int mode) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
-        if (!force_all && (d.movement[i] == 1 || !d.moved[i])) continue;
+        if (mode == 0 && (d.movement[i] == 1 || !d.moved[i])) continue;
         float4 q = d.rot[i];
-        q = qnormalize(q);
-        d.rot[i] = q;
+        if (mode != 2 || d.moved[i]) {
+            q = qnormalize(q);
+            d.rot[i] = q;
+        }
         M33 R = quatRot(q);
         f3 c = mk(d.pos[i]);
         f3 mn, mx;
@@ -163,8 +167,8 @@ void launch_pairs(const Dev& d, const Launch& L) {
     k_clamp_pairs<<<1, 1, 0, L.st>>>(d);
 }
 
-void launch_geometry(const Dev& d, int force_all, const Launch& L) {
-    k_geometry<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d, force_all);
+void launch_geometry(const Dev& d, int mode, const Launch& L) {
+    k_geometry<<<grid_for(d.n_bodies, 128, L.n_sms), 128, 0, L.st>>>(d, mode);
 }
 
 }  // namespace cpgpu

@@ -97,6 +97,12 @@ struct Body {
     // hist holds hist_n (velocity, angular velocity) records, oldest first
     int asleep = 0, waking = 0, ready_cnt = 0, non_sleepy = 0, hist_n = 0;
     std::vector<float> hist;
+    // pose given through the API since the last read-back from a device: its
+    // orientation is renormalised on upload (a read-back pose was normalised
+    // by the step that produced it, and normalising it again could change
+    // its last bits, so a batch re-packed from read-back state continues
+    // exactly)
+    int fresh = 1;
     // RigidBody::alertWaking (RigidBody.cpp:318-324)
     void alert_waking() { waking = 1; ready_cnt = 0; non_sleepy = 0; hist_n = 0; hist.clear(); }
 };
@@ -133,8 +139,23 @@ struct HJoint {
     D3 ul, wl;                   // twist: body 1's u and w axes (body space)
     float impulse[kJMax] = {};   // warm-start impulse carried between uploads
     float u[3] = {}, w[3] = {};  // hinge / slider basis of the last rebuild
-    float angle = 0;             // twist: current angle (unwrapped)
+    float angle = 0;             // twist: current angle (unwrapped); motor: angular position; slide limit / piston: slide position
     int active = 0;              // limits: reached at the last rebuild
+    // motor (PersistentConstraint.h:253-275) / piston (:217-251): the powered
+    // mode (0 off, 1 constant torque or force, 2 target velocity, 3 target
+    // position) and its settings; limits in min_angle / max_angle (motor
+    // angles, slide positions); a motor's body 1 reference axes in ul / wl and
+    // body 2's comparison axis in ax2
+    int mode = 0;
+    double pmax = 0, tvel = 0, tpos = 0;
+    float aux = 0;               // motor: relative angular velocity of the last rebuild; slide limit / piston: past a limit
+    // listed in the next island (addSolverConstraints)
+    int listed() const {
+        if (kind == JK_MOTOR) return ((mode != 0 && pmax != 0) || angle < min_angle || angle > max_angle) ? 1 : 0;
+        if (kind == JK_SLIDE_LIMIT) return aux != 0.f ? 1 : 0;
+        if (kind == JK_PISTON) return (mode != 0 && pmax != 0) ? 1 : 0;
+        return active;
+    }
 };
 
 // A spring (PhysicsEngine::addSpring, PhysicsEngine.cpp:974-998)
@@ -744,7 +765,7 @@ struct JointGraph {
     std::vector<HSystem> systems;
 };
 
-static bool holonomic_kind(int k) { return !jk_limit(k); }
+static bool holonomic_kind(int k) { return !jk_conditional(k); }
 
 // HolonomicSystem::HolonomicSystem (HolonomicBlockSolver.cpp:11-132): greedy
 // minimum-fill elimination order over constraints that share a body, and the
@@ -948,6 +969,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     std::vector<float> iref(9 * (size_t)N), iinv_ref(9 * (size_t)N), iw(9 * (size_t)N), iinv(9 * (size_t)N);
     std::vector<int> world_of(N), map_order(N);
     std::vector<uint8_t> movement(N);
+    std::vector<int> fresh(N, 1);
     std::vector<WorldParams> wp(worlds.size());
     int max_hot = 16;
     for (size_t wi = 0; wi < worlds.size(); wi++) {
@@ -989,6 +1011,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
             }
             world_of[g] = (int)wi;
             movement[g] = (uint8_t)b.movement;
+            fresh[g] = b.fresh;
             if (has_sleep) {
                 s_asleep[g] = b.asleep; s_waking[g] = b.waking; s_ready[g] = b.ready_cnt; s_nons[g] = b.non_sleepy;
                 // the newest records that fit this world's history length, oldest first
@@ -1074,7 +1097,8 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     std::vector<int> j_b1, j_b2, j_n, j_kind, j_active;
     std::vector<float4> j_p1, j_p2, j_ax1, j_ax2, j_u, j_w, j_par, j_ul, j_wl;
     std::vector<float2> j_hard;
-    std::vector<float> j_imp, j_angle;
+    std::vector<float> j_imp, j_angle, j_aux;
+    std::vector<float4> j_power;
     std::vector<uint64_t> je_key;
     std::vector<int> je_jstart, je_jcount, je_jlist, je_sys, je_wstart{0}, je_wjstart{0}, hs_wstart{0};
     std::vector<int> hs_cstart{0}, hs_cons, hs_vpos, hs_degree, hs_tstart{0}, hs_table, hs_bstart, hs_cap, hs_fp64, hs_wk;
@@ -1097,7 +1121,9 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
             j_par.push_back(make_float4((float)par_x, (float)j.min_angle, 0.f, 0.f));
             j_ul.push_back(f4d(j.ul)); j_wl.push_back(f4d(j.wl));
             j_angle.push_back(j.angle);
-            j_active.push_back(j.active);
+            j_active.push_back(j.listed());
+            j_aux.push_back(j.aux);
+            j_power.push_back(make_float4((float)j.mode, (float)j.pmax, (float)j.tvel, (float)j.tpos));
             for (int k = 0; k < kJMax; k++) j_imp.push_back(j.impulse[k]);
         }
         if (!w.joints.empty() || !w.springs.empty()) {
@@ -1320,6 +1346,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
             J.impulse = A.take<float>(kJMax * (size_t)n_joints);
             J.u = A.take<float4>(n_joints); J.w = A.take<float4>(n_joints);
             J.angle = A.take<float>(n_joints); J.active = A.take<int>(n_joints);
+            J.aux = A.take<float>(n_joints); J.power = A.take<float4>(n_joints);
             J.rows = A.take<JointRow>(n_joints);
             JointEdgeStore& E = x.je;
             E.key = A.take<uint64_t>(n_je); E.jstart = A.take<int>(n_je); E.jcount = A.take<int>(n_je);
@@ -1367,7 +1394,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     up(d_shape, shape_off.data(), N * 4); up(d_world, world_of.data(), N * 4);
     up(d_mov, movement.data(), N); up(d_mat, mat.data(), N * sizeof(float4));
     up(d_pool, pool.data(), pool.size());
-    CK(cudaMemsetAsync(x.moved, 0, N * sizeof(int), B->st));
+    up(x.moved, fresh.data(), N * 4);   // the first geometry pass renormalises these orientations
     if (has_sleep) {
         up(x.asleep, s_asleep.data(), N * 4); up(x.waking, s_waking.data(), N * 4); up(x.ready_cnt, s_ready.data(), N * 4);
         up(x.non_sleepy, s_nons.data(), N * 4); up(x.hist_n, s_hn.data(), N * 4);
@@ -1401,6 +1428,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
         up(J.impulse, j_imp.data(), j_imp.size() * 4);
         up(J.u, j_u.data(), n_joints * 16); up(J.w, j_w.data(), n_joints * 16);
         up(J.angle, j_angle.data(), n_joints * 4); up(J.active, j_active.data(), n_joints * 4);
+        up(J.aux, j_aux.data(), n_joints * 4); up((void*)J.power, j_power.data(), n_joints * 16);
         if (n_joints > 0) CK(cudaMemsetAsync(J.rows, 0, sizeof(JointRow) * (size_t)n_joints, B->st));
         const JointEdgeStore& E = x.je;
         up((void*)E.key, je_key.data(), n_je * 8); up((void*)E.jstart, je_jstart.data(), n_je * 4);
@@ -1428,7 +1456,7 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     }
     B->parity = 0;
     Launch L{B->n_sms, B->st};
-    launch_geometry(B->d[0], 1, L);
+    launch_geometry(B->d[0], 2, L);
     prepare_kernels();
     prepare_pgs(B->dv_cap);
     B->pgs_per_sm = pgs_per_sm;
@@ -1486,7 +1514,7 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
     int counts[6];
     CK(cudaMemcpyAsync(counts, x.n_pairs, sizeof(counts), cudaMemcpyDeviceToHost, B.st));
     const int nj = x.n_joints;
-    std::vector<float> jimp((size_t)kJMax * nj), jang(nj);
+    std::vector<float> jimp((size_t)kJMax * nj), jang(nj), jaux(nj);
     std::vector<float4> ju(nj), jw(nj);
     std::vector<int> jact(nj);
     if (nj > 0) {
@@ -1495,6 +1523,7 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
         CK(cudaMemcpyAsync(jw.data(), x.jt.w, nj * 16, cudaMemcpyDeviceToHost, B.st));
         CK(cudaMemcpyAsync(jang.data(), x.jt.angle, nj * 4, cudaMemcpyDeviceToHost, B.st));
         CK(cudaMemcpyAsync(jact.data(), x.jt.active, nj * 4, cudaMemcpyDeviceToHost, B.st));
+        CK(cudaMemcpyAsync(jaux.data(), x.jt.aux, nj * 4, cudaMemcpyDeviceToHost, B.st));
     }
     CK(cudaStreamSynchronize(B.st));
     // contact graph (current = the old buffers of the next step)
@@ -1535,6 +1564,7 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
             Body& b = w.bodies[i - s0];
             b.com = D3(pos[i].x, pos[i].y, pos[i].z);
             b.q = Quat{rot[i].x, rot[i].y, rot[i].z, rot[i].w};
+            b.fresh = 0;
             if (b.movement != CPGPU_FIXED) {
                 b.vel = D3(vel[i].x, vel[i].y, vel[i].z);
                 b.angv = D3(angv[i].x, angv[i].y, angv[i].z);
@@ -1549,6 +1579,7 @@ static void download_worlds(Batch& B, const std::vector<World*>& ws) {
                 for (int k = 0; k < kJMax; k++) w.joints[j].impulse[k] = jimp[kJMax * g + k];
                 w.joints[j].angle = jang[g];
                 w.joints[j].active = jact[g];
+                w.joints[j].aux = jaux[g];
                 w.joints[j].u[0] = ju[g].x; w.joints[j].u[1] = ju[g].y; w.joints[j].u[2] = ju[g].z;
                 w.joints[j].w[0] = jw[g].x; w.joints[j].w[1] = jw[g].y; w.joints[j].w[2] = jw[g].z;
             }
@@ -1604,7 +1635,7 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
     CK(cudaStreamSynchronize(B.st));
     struct Buf {
         std::vector<float4> pos, rot, vel, angv;
-        std::vector<float> iw, iinv, jimp, jang;
+        std::vector<float> iw, iinv, jimp, jang, jaux;
         std::vector<float4> ju, jw;
         std::vector<int> jact;
         std::vector<uint64_t> key, mag;
@@ -1626,9 +1657,11 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
         if (x.n_joints > 0) {
             const int j0 = B.world_jstart[w], nj = B.world_jstart[w + 1] - j0;
             b.jimp.resize((size_t)kJMax * nj); b.ju.resize(nj); b.jw.resize(nj); b.jang.resize(nj); b.jact.resize(nj);
+            b.jaux.resize(nj);
             get(b.jimp.data(), x.jt.impulse + (size_t)kJMax * j0, (size_t)kJMax * nj * 4);
             get(b.ju.data(), x.jt.u + j0, nj * 16); get(b.jw.data(), x.jt.w + j0, nj * 16);
             get(b.jang.data(), x.jt.angle + j0, nj * 4); get(b.jact.data(), x.jt.active + j0, nj * 4);
+            get(b.jaux.data(), x.jt.aux + j0, nj * 4);
         }
         const int e0 = rg[4 * i], e1 = rg[4 * i + 1], c0 = rg[4 * i + 2], c1 = rg[4 * i + 3];
         const int ne = e1 - e0, nc = c1 - c0;
@@ -1653,6 +1686,7 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
             Body& bd = w.bodies[k];
             bd.com = D3(b.pos[k].x, b.pos[k].y, b.pos[k].z);
             bd.q = Quat{b.rot[k].x, b.rot[k].y, b.rot[k].z, b.rot[k].w};
+            bd.fresh = 0;
             if (bd.movement != CPGPU_FIXED) {
                 bd.vel = D3(b.vel[k].x, b.vel[k].y, b.vel[k].z);
                 bd.angv = D3(b.angv[k].x, b.angv[k].y, b.angv[k].z);
@@ -1664,6 +1698,7 @@ static void download_subset(Batch& B, const std::vector<int>& widx, const std::v
             for (int k = 0; k < kJMax; k++) w.joints[j].impulse[k] = b.jimp[kJMax * j + k];
             w.joints[j].angle = b.jang[j];
             w.joints[j].active = b.jact[j];
+            w.joints[j].aux = b.jaux[j];
             w.joints[j].u[0] = b.ju[j].x; w.joints[j].u[1] = b.ju[j].y; w.joints[j].u[2] = b.ju[j].z;
             w.joints[j].w[0] = b.jw[j].x; w.joints[j].w[1] = b.jw[j].y; w.joints[j].w[2] = b.jw[j].z;
         }
@@ -2125,6 +2160,7 @@ int cpgpu_body_set_orientation(cpgpu_world* w, uint32_t id, const double q[4]) {
         begin_mutation(w->w);
         Body& b = body_ref(w->w, id);
         b.q = qnorm(Quat{q[0], q[1], q[2], q[3]});
+        b.fresh = 1;
         b.alert_waking();
         return CPGPU_OK;
     });
@@ -2137,6 +2173,7 @@ int cpgpu_body_set_position(cpgpu_world* w, uint32_t id, const double p[3]) {
         D3 tracked = b.com + qrot(b.q, b.local_origin);
         b.com = b.com + (D3(p[0], p[1], p[2]) - tracked);
         b.q = qnorm(b.q);
+        b.fresh = 1;
         b.alert_waking();
         return CPGPU_OK;
     });
@@ -2185,7 +2222,9 @@ static HJoint& add_joint(World& w, int kind, int n, uint32_t b1, uint32_t b2, co
     return w.joints.back();
 }
 
-static uint32_t joint_id(const World& w) { return (uint32_t)w.constraint_seq; }
+// the id of the constraint just created: PhysicsEngine::nextConstraintID
+// order over joints and springs, from 0 (PhysicsEngine.h:301)
+static uint32_t joint_id(const World& w) { return (uint32_t)(w.constraint_seq - 1); }
 
 int cpgpu_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3], const double a2[3], double strength,
                           uint32_t* out_id) {
@@ -2293,6 +2332,137 @@ int cpgpu_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3]
         return CPGPU_OK;
     });
 }
+
+// The joint a constraint id names (ids count joints and springs in creation
+// order from 0; a piston's two joints share its id, the powered one last)
+static HJoint* joint_by_id(World& w, uint32_t id) {
+    HJoint* found = nullptr;
+    for (HJoint& j : w.joints)
+        if ((uint32_t)j.seq == id) found = &j;
+    return found;
+}
+
+// PhysicsEngine::addMotorConstraint (PhysicsEngine.cpp:725-763) and the Motor
+// constructor (PersistentConstraint.cpp:5-24): on a hinge's or sliding
+// hinge's axes and rotation strength, in the base's edge; the reference
+// frame (body 1's perpendicular basis of its axis, body 2's first
+// perpendicular axis) fixed at creation, the angle measured from it
+int cpgpu_add_motor(cpgpu_world* w, uint32_t base, double min_angle, double max_angle, uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        HJoint* b = joint_by_id(w->w, base);
+        if (!b || (b->kind != JK_HINGE && b->kind != JK_SLIDING_HINGE))
+            throw ApiFail{CPGPU_ERR_INVALID_ARG, "a motor needs a hinge or a sliding hinge"};
+        const HJoint base_j = *b;
+        begin_mutation(w->w);
+        HJoint j;
+        j.b1 = base_j.b1; j.b2 = base_j.b2; j.kind = JK_MOTOR; j.n = 1;
+        j.seq = w->w.constraint_seq++;
+        j.ax1 = base_j.ax1;
+        j.rh = base_j.rh;
+        j.min_angle = min_angle; j.max_angle = max_angle;
+        D3 u2, tmp;
+        base_j.ax1.basis(&j.ul, &j.wl);
+        base_j.ax2.basis(&u2, &tmp);
+        j.ax2 = u2;
+        // Motor::calculatePosition from zero with no velocity: the angle of
+        // body 2's comparison axis in body 1's frame now
+        const Body &x = w->w.bodies[j.b1], &y = w->w.bodies[j.b2];
+        const D3 axis = qrot(x.q, j.ax1), ref_u = qrot(x.q, j.ul), ref_w = qrot(x.q, j.wl), cmp = qrot(y.q, j.ax2);
+        double pos = 0;
+        if (!(std::fabs(cmp.dot(axis)) > 0.999)) {
+            const D3 cn = (cmp - axis * axis.dot(cmp)).normalize();
+            const double kPi = 3.1415926535;
+            double rel = 2 * kPi - std::acos(std::min(1.0, std::max(-1.0, cn.dot(ref_u))));
+            if (cn.dot(ref_w) < 0) rel = 2 * kPi - rel;
+            double closest = INFINITY;
+            for (double c : {rel - 2 * kPi, rel, rel + 2 * kPi})
+                if (std::fabs(c) < std::fabs(closest)) closest = c;
+            pos = closest;
+        }
+        j.angle = (float)pos;
+        w->w.joints.push_back(j);
+        if (out_id) *out_id = joint_id(w->w);
+        return CPGPU_OK;
+    });
+}
+
+// PhysicsEngine::addPistonConstraint (PhysicsEngine.cpp:808-852) and the
+// Piston constructor (PersistentConstraint.cpp:134-143): on a slider's or
+// sliding hinge's tracked points, body 1 axis and position strength, in the
+// base's edge, as two joints (its slide limit, then the powered row) under
+// one id.  The position before the first step is measured between the two
+// tracked points (the reference's constructor reads body 2's point key on
+// body 1; every rebuild measures it between the bodies)
+int cpgpu_add_piston(cpgpu_world* w, uint32_t base, double min_pos, double max_pos, uint32_t* out_id) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        HJoint* b = joint_by_id(w->w, base);
+        if (!b || (b->kind != JK_SLIDER && b->kind != JK_SLIDING_HINGE))
+            throw ApiFail{CPGPU_ERR_INVALID_ARG, "a piston needs a slider or a sliding hinge"};
+        const HJoint base_j = *b;
+        begin_mutation(w->w);
+        const int seq = w->w.constraint_seq++;
+        const Body &x = w->w.bodies[base_j.b1], &y = w->w.bodies[base_j.b2];
+        const D3 axis = qrot(x.q, base_j.ax1);
+        const double pos = (y.com + qrot(y.q, base_j.p2)).dot(axis) - (x.com + qrot(x.q, base_j.p1)).dot(axis);
+        for (int kind : {JK_SLIDE_LIMIT, JK_PISTON}) {
+            HJoint j;
+            j.b1 = base_j.b1; j.b2 = base_j.b2; j.kind = kind; j.n = 1;
+            j.seq = seq;
+            j.p1 = base_j.p1; j.p2 = base_j.p2;
+            j.ax1 = base_j.ax1;
+            j.ph = base_j.ph;
+            j.min_angle = min_pos; j.max_angle = max_pos;
+            j.angle = (float)pos;
+            w->w.joints.push_back(j);
+        }
+        if (out_id) *out_id = joint_id(w->w);
+        return CPGPU_OK;
+    });
+}
+
+// setMotorOff / setMotorConstantTorque / setMotorTargetVelocity /
+// setMotorTargetPosition (PhysicsEngine.cpp:1857-1912) and the piston's
+// setters (:1800-1855): each sets the fields the reference's setter sets and
+// alerts both bodies
+static int set_powered(cpgpu_world* w, uint32_t id, int kind, int mode, double max, double target) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        HJoint* j = joint_by_id(w->w, id);
+        if (!j || j->kind != kind) throw ApiFail{CPGPU_ERR_INVALID_ARG, kind == JK_MOTOR ? "not a motor" : "not a piston"};
+        if (mode < 0 || mode > 3) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad mode"};
+        begin_mutation(w->w);
+        j = joint_by_id(w->w, id);
+        j->mode = mode;
+        if (mode >= 1) j->pmax = max;
+        if (mode == 2) j->tvel = target;
+        if (mode == 3) j->tpos = target;
+        w->w.bodies[j->b1].alert_waking();
+        w->w.bodies[j->b2].alert_waking();
+        return CPGPU_OK;
+    });
+}
+int cpgpu_set_motor(cpgpu_world* w, uint32_t id, int mode, double max_torque, double target) {
+    return set_powered(w, id, JK_MOTOR, mode, max_torque, target);
+}
+int cpgpu_set_piston(cpgpu_world* w, uint32_t id, int mode, double max_force, double target) {
+    return set_powered(w, id, JK_PISTON, mode, max_force, target);
+}
+// getMotorAngularPosition / getPistonPosition (PhysicsEngine.cpp:1914-1930)
+static int get_powered(cpgpu_world* w, uint32_t id, int kind, double* out) {
+    W_OR_FAIL(w);
+    return guarded([&] {
+        if (!out) throw ApiFail{CPGPU_ERR_INVALID_ARG, "null output"};
+        if (w->w.dev && w->w.dev_valid) download_state(w->w);
+        HJoint* j = joint_by_id(w->w, id);
+        if (!j || j->kind != kind) throw ApiFail{CPGPU_ERR_INVALID_ARG, kind == JK_MOTOR ? "not a motor" : "not a piston"};
+        *out = j->angle;
+        return CPGPU_OK;
+    });
+}
+int cpgpu_get_motor_position(cpgpu_world* w, uint32_t id, double* out) { return get_powered(w, id, JK_MOTOR, out); }
+int cpgpu_get_piston_position(cpgpu_world* w, uint32_t id, double* out) { return get_powered(w, id, JK_PISTON, out); }
 
 int cpgpu_step(cpgpu_world* w, int n_steps) {
     W_OR_FAIL(w);
@@ -2425,6 +2595,7 @@ int cpgpu_set_body_state(cpgpu_world* w, const double* com, const double* quat, 
             Body& b = w->w.bodies[i];
             if (com) b.com = D3(com[3 * i], com[3 * i + 1], com[3 * i + 2]);
             if (quat) b.q = qnorm(Quat{quat[4 * i], quat[4 * i + 1], quat[4 * i + 2], quat[4 * i + 3]});
+            if (com || quat) b.fresh = 1;
             if (vel) b.vel = D3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
             if (ang) b.angv = D3(ang[3 * i], ang[3 * i + 1], ang[3 * i + 2]);
             if (b.movement == CPGPU_DYNAMIC) {
@@ -2513,7 +2684,7 @@ int cpgpu_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv
             const HJoint& x = w->w.joints[j];
             for (int k = 0; k < kJMax; k++) if (impulse) impulse[kJMax * j + k] = x.impulse[k];
             for (int k = 0; k < 3; k++) { if (u) u[3 * j + k] = x.u[k]; if (wv) wv[3 * j + k] = x.w[k]; }
-            if (aux) { aux[2 * j] = x.angle; aux[2 * j + 1] = x.active; }
+            if (aux) { aux[2 * j] = x.angle; aux[2 * j + 1] = jk_powered(x.kind) ? (double)x.aux : (double)x.active; }
         }
         return CPGPU_OK;
     });
@@ -2528,7 +2699,11 @@ int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
             HJoint& x = w->w.joints[j];
             for (int k = 0; k < kJMax; k++) if (impulse) x.impulse[k] = (float)impulse[kJMax * j + k];
             for (int k = 0; k < 3; k++) { if (u) x.u[k] = (float)u[3 * j + k]; if (wv) x.w[k] = (float)wv[3 * j + k]; }
-            if (aux) { x.angle = (float)aux[2 * j]; x.active = aux[2 * j + 1] != 0.0 ? 1 : 0; }
+            if (aux) {
+                x.angle = (float)aux[2 * j];
+                if (jk_powered(x.kind)) x.aux = (float)aux[2 * j + 1];
+                else x.active = aux[2 * j + 1] != 0.0 ? 1 : 0;
+            }
         }
         return CPGPU_OK;
     });

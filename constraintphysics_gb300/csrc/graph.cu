@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
                         // edge emits no rows
                         for (int q = d.je.jstart[je]; q < d.je.jstart[je] + d.je.jcount[je]; q++) {
                             const int jj = d.je.jlist[q];
-                            if (jk_limit(d.jt.kind[jj]) && !d.jt.active[jj]) continue;
+                            if (jk_conditional(d.jt.kind[jj]) && !d.jt.active[jj]) continue;
                             d.row_contact[rc++] = -(jj + 1);
                             has_joint = true;
                         }

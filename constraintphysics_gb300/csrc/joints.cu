@@ -122,6 +122,52 @@ __device__ __forceinline__ float limit_error(float f) {
     return -f8 / 40320.0f + f6 / 720.0f - f4 / 24.0f + f2 / 2.0f;
 }
 
+// Motor::calculatePosition (PersistentConstraint.cpp:30-71): the last angle
+// advanced by the relative angular velocity, snapped to the angle of body 2's
+// comparison axis in body 1's (u, w) plane in the 2 pi window nearest the
+// prediction, unless that axis is within acos(0.999) of the motor axis.  The
+// reference takes that angle as 2 pi - acos(c . u) (or acos(c . u) when
+// c . w < 0); in FP32 the arc cosine of a dot product near 1 has a resolution
+// of ~3.5e-4 rad, so the same angle is taken from the signed
+// atan2(c . w, c . u) instead.
+__device__ float motor_position(float prev, f3 axis, f3 w1, f3 w2, float dts, float4 qa, float4 qb, f3 ul, f3 wl, f3 cl) {
+    const float kTwoPi = 2.0f * 3.1415926535f;
+    const f3 ref_u = qrot(qa, ul), ref_w = qrot(qa, wl), cmp = qrot(qb, cl);
+    const float rel = dot(axis, w1) - dot(axis, w2);
+    const float pred = prev + rel * dts;
+    if (fabsf(dot(cmp, axis)) > 0.999f) return pred;
+    const f3 cn = normalize(cmp - axis * dot(axis, cmp));
+    const float su = dot(cn, ref_u), sw = dot(cn, ref_w);
+    const float th = atan2f(sw, su);                 // acos(c . u) with the sign of c . w
+    const float rel_angle = sw >= 0.f ? kTwoPi - th : -th;
+    const float n2 = pred - fmodf(pred, kTwoPi);
+    const float c[3] = {n2 + rel_angle - kTwoPi, n2 + rel_angle, n2 + rel_angle + kTwoPi};
+    float closest = INFINITY;
+    for (int k = 0; k < 3; k++)
+        if (fabsf(pred - c[k]) < fabsf(pred - closest)) closest = c[k];
+    return closest;
+}
+
+// Motor::getConstraintTargetVelocityValue and
+// Piston::getPistonTargetVelocityValue (PersistentConstraint.cpp:77-109,
+// 153-185): off 0, constant torque / force an infinite target in its
+// direction, target velocity as set, target position the velocity that the
+// max torque / force reaches over the remaining distance, the inertia from
+// the last impulse and velocity change (or from `inv_inertia` when either is
+// below 1e-7; the reference's `abs(impulse < EPS)` holds for every impulse
+// below 1e-7, negative ones included)
+__device__ float powered_target(float4 pw, float position, float rel_vel, float prev_vel, float impulse, float inv_inertia) {
+    const int mode = (int)pw.x;
+    if (mode == 0) return 0.f;
+    if (mode == 1) return pw.y > 0.f ? INFINITY : -INFINITY;
+    if (mode == 2) return pw.z;
+    const float ang_diff = position - pw.w;
+    const float dir = ang_diff > 0.f ? -1.f : 1.f;
+    const float vdt = fabsf(rel_vel - prev_vel);
+    const float inertia = (vdt < 0.0000001f || impulse < 0.0000001f) ? 1.0f / inv_inertia : fabsf(impulse) / vdt;
+    return dir * sqrtf(2.0f * fabsf(ang_diff) * pw.y / inertia);
+}
+
 __global__ void k_joint_rows(Dev d) {
     const JointStore& J = d.jt;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < d.n_joints; j += gridDim.x * blockDim.x) {
@@ -135,7 +181,88 @@ __global__ void k_joint_rows(Dev d) {
         JointRow& R = d.jt.rows[j];
         float* jimp = J.impulse + kJMax * (size_t)j;
         bool rebuilt = true;
-        if (jk_limit(kind)) {
+        if (kind == JK_MOTOR) {
+            // Motor::updateSolverConstraints (PersistentConstraint.cpp:320-328)
+            // with MotorConstraint (ConstraintSolver.cpp:555-585): the angle
+            // advanced first; while powered or past a limit one row on body 1's
+            // axis (target velocity limited to the limit's side and a one-sided
+            // projection past a limit, else bounded by max torque x dt); the old
+            // row kept otherwise
+            const f3 axis = qrot(qa, mk(J.ax1[j]));
+            const f3 w1 = d.movement[a] == 1 ? mk(0.f, 0.f, 0.f) : mk(d.angv[a]);
+            const f3 w2 = d.movement[b] == 1 ? mk(0.f, 0.f, 0.f) : mk(d.angv[b]);
+            const float4 pw = J.power[j];
+            const float mx = J.par[j].x, mn = J.par[j].y;
+            const float pos = motor_position(J.angle[j], axis, w1, w2, dts, qa, qb, mk(J.ul[j]), mk(J.wl[j]), mk(J.ax2[j]));
+            J.angle[j] = pos;
+            const bool listed = ((int)pw.x != 0 && pw.y != 0.f) || pos < mn || pos > mx;
+            J.active[j] = listed ? 1 : 0;
+            const float rel = dot(axis, w1) - dot(axis, w2);
+            if (listed) {
+                const M33 Ia = load9(d.iinv + 9 * a), Ib = load9(d.iinv + 9 * b);
+                const float inv_i = dot(axis, mul(Ia, axis)) + dot(axis, mul(Ib, axis));
+                const float tv = powered_target(pw, pos, rel, J.aux[j], jimp[0], inv_i);
+                const float hc = fminf(hard.y * dts, 1.0f / dts);
+                R.n = 1;
+                R.impulse[0] = P.warm_disabled ? 0.f : jimp[0];
+                R.pimpulse[0] = 0.f;
+                R.holo[0] = 0.f;
+                set_row(R.ja, mk(0.f, 0.f, 0.f), axis);
+                set_row(R.jb, mk(0.f, 0.f, 0.f), -axis);
+                R.has_vt = 1;
+                R.pos = 1;
+                if (pos > mx) { R.ptarget[0] = (mx - pos) * hc; R.vt = fminf(0.f, tv); R.proj = 2; }
+                else if (pos < mn) { R.ptarget[0] = (mn - pos) * hc; R.vt = fmaxf(0.f, tv); R.proj = 1; }
+                else { R.ptarget[0] = 0.f; R.vt = tv; R.proj = 3; R.lim = fabsf(pw.y * dts); R.pos = 0; }
+            } else {
+                rebuilt = false;
+            }
+            J.aux[j] = rel;
+        } else if (kind == JK_SLIDE_LIMIT || kind == JK_PISTON) {
+            // Piston::updateSolverConstraints (PersistentConstraint.cpp:300-318):
+            // the slide position along body 1's axis between the slider's
+            // tracked points; past a limit a SlideLimitConstraint row
+            // (ConstraintSolver.cpp:736-775), while powered a PistonConstraint
+            // row (:701-731), both along the axis (their angular Jacobian,
+            // -s^T [s]x, is zero)
+            const f3 pa = qrot(qa, mk(J.p1[j])) + ca, pb = qrot(qb, mk(J.p2[j])) + cb;
+            const f3 axis = qrot(qa, mk(J.ax1[j]));
+            const float pos = dot(pb, axis) - dot(pa, axis);
+            const float mx = J.par[j].x, mn = J.par[j].y;
+            const bool exceeded = pos < mn || pos > mx;
+            const float4 pw = J.power[j];
+            J.angle[j] = pos;
+            J.aux[j] = exceeded ? 1.f : 0.f;
+            const bool listed = kind == JK_SLIDE_LIMIT ? exceeded : ((int)pw.x != 0 && pw.y != 0.f);
+            J.active[j] = listed ? 1 : 0;
+            if (listed) {
+                R.n = 1;
+                R.impulse[0] = P.warm_disabled ? 0.f : jimp[0];
+                R.pimpulse[0] = 0.f;
+                R.holo[0] = 0.f;
+                set_row(R.ja, -axis, mk(0.f, 0.f, 0.f));
+                set_row(R.jb, axis, mk(0.f, 0.f, 0.f));
+                if (kind == JK_SLIDE_LIMIT) {
+                    const float hc = fminf(hard.x * dts, 1.0f / dts);
+                    R.has_vt = 0;
+                    R.pos = 1;
+                    if (pos > mx) { R.ptarget[0] = (mx - pos) * hc; R.proj = 2; }
+                    else { R.ptarget[0] = (mn - pos) * hc; R.proj = 1; }
+                } else {
+                    const f3 v1 = d.movement[a] == 1 ? mk(0.f, 0.f, 0.f) : mk(d.vel[a]);
+                    const f3 v2 = d.movement[b] == 1 ? mk(0.f, 0.f, 0.f) : mk(d.vel[b]);
+                    // the piston's previous velocity is never written and stays 0
+                    R.vt = powered_target(pw, pos, dot(axis, v1) - dot(axis, v2), 0.f, jimp[0], d.pos[a].w + d.pos[b].w);
+                    R.has_vt = 1;
+                    R.proj = 3;
+                    R.lim = pw.y * dts;
+                    R.pos = 0;
+                    R.ptarget[0] = 0.f;
+                }
+            } else {
+                rebuilt = false;
+            }
+        } else if (jk_limit(kind)) {
             // ConeRotationLimit / TwistLimit::updateSolverConstraints
             // (PersistentConstraint.cpp:233-272): inside the limit the row is
             // inactive (warm impulse cleared, the old row kept, not listed in
@@ -186,6 +313,8 @@ __global__ void k_joint_rows(Dev d) {
             } else {
                 R.n = 1;
                 R.proj = proj;
+                R.has_vt = 0;
+                R.pos = 1;
                 R.impulse[0] = jimp[0];
                 R.pimpulse[0] = 0.f;
                 R.holo[0] = 0.f;
@@ -199,6 +328,8 @@ __global__ void k_joint_rows(Dev d) {
             const float rot_c = fminf(hard.y * dts, 1.0f / dts);
             R.n = n;
             R.proj = 0;
+            R.has_vt = 0;
+            R.pos = 1;
             float warm[kJMax];
             // Weld::updateSolverConstraints passes the previous impulse on
             // unscaled whatever the warm-start switch says
@@ -362,7 +493,10 @@ __global__ void k_joint_rows(Dev d) {
         }
         if (rn > 0) {
             jvalue(R, va, vb, cur);
-            for (int i = 0; i < rn; i++) R.target[i] = -cur[i];
+            // MotorConstraint / PistonConstraint::findTargetConstraintValue
+            // (ConstraintSolver.cpp:586-589, 723-726): the target velocity less the value
+            if (R.has_vt) R.target[0] = R.vt - cur[0];
+            else for (int i = 0; i < rn; i++) R.target[i] = -cur[i];
         }
     }
 }

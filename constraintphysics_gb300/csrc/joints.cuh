@@ -1,5 +1,5 @@
 // joints.cuh — device helpers for joint rows (ball-socket, hinge, distance,
-// weld, slider, sliding hinge, cone and twist limits) and the holonomic block
+// weld, slider, sliding hinge, cone and twist limits, motors, pistons) and the holonomic block
 // solve, shared by the row-building kernels (joints.cu) and
 // the joint-island PGS kernel (solver.cu).
 #pragma once
@@ -103,6 +103,9 @@ __device__ __forceinline__ void jstep_n(JointRow& R, float4* dv, bool pseudo) {
         float nw = acc[i] + x;
         if (N == 1 && R.proj == 1) nw = fmaxf(nw, 0.f);
         else if (N == 1 && R.proj == 2) nw = fminf(nw, 0.f);
+        // MotorConstraint / PistonConstraint::projectValidImpulse
+        // (ConstraintSolver.cpp:591-606, 728-731)
+        else if (N == 1 && R.proj == 3) nw = nw > 0.f ? fminf(nw, R.lim) : fmaxf(nw, -R.lim);
         diff[i] = nw - acc[i];
         zero = zero && !(fabsf(diff[i]) > kJZero);
     }

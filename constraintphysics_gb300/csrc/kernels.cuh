@@ -22,7 +22,7 @@ void launch_gravity(const Dev& d, const Launch& L);
 // waking actions, the sleep bookkeeping and gravity (sleep.cu)
 void launch_step_begin(const Dev& d, const Launch& L);
 void launch_pairs(const Dev& d, const Launch& L);
-void launch_geometry(const Dev& d, int force_all, const Launch& L);
+void launch_geometry(const Dev& d, int mode, const Launch& L);   // mode 0 moved bodies, 2 a batch's first pass
 // hull-hull pairs, then (when the batch holds spheres or cylinders) the pairs
 // that involve one
 void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cudaStream_t st);

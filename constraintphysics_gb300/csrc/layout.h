@@ -185,8 +185,10 @@ constexpr int kDvF4 = 3;
 // One joint row per substep: DegreedConstraint<n> (ConstraintSolver.h:60-144)
 // of a DistanceConstraint (n = 1), BallSocketConstraint (3),
 // SlidingHingeConstraint (4), HingeConstraint or SliderConstraint (5),
-// WeldConstraint (6), ConeLimitConstraint or TwistLimitConstraint (1, with a
-// one-sided projection); row-major, sized for n = 6.
+// WeldConstraint (6), ConeLimitConstraint, TwistLimitConstraint or
+// SlideLimitConstraint (1, with a one-sided projection), MotorConstraint or
+// PistonConstraint (1, bounded by the max torque or force, with a velocity
+// target); row-major, sized for n = 6.
 constexpr int kJMax = 6;
 struct alignas(16) JointRow {
     float ja[kJMax * 6], jb[kJMax * 6];     // [n][6]
@@ -195,7 +197,12 @@ struct alignas(16) JointRow {
     float target[kJMax], ptarget[kJMax];
     float impulse[kJMax], pimpulse[kJMax], holo[kJMax];
     int n, sa, sb;                          // island body slots (-1: infinite mass)
-    int proj;                               // 0 none, 1 impulse >= 0, 2 impulse <= 0 (limits)
+    int proj;                               // 0 none, 1 impulse >= 0, 2 impulse <= 0 (limits),
+                                            // 3 x > 0 ? min(x, lim) : max(x, -lim) (motor, piston)
+    float lim;                              // proj 3 bound
+    float vt;                               // motor / piston: target = vt - value
+    int has_vt;
+    int pos;                                // needsPosCorrect: solved in the position passes
 };
 
 // Joint kinds (PersistentConstraint.h:90-420).  The limits are inequality
@@ -203,8 +210,16 @@ struct alignas(16) JointRow {
 enum JointKind : int {
     JK_BALL = 0, JK_HINGE = 1, JK_DISTANCE = 2, JK_WELD = 3, JK_SLIDER = 4, JK_SLIDING_HINGE = 5,
     JK_CONE = 6, JK_TWIST = 7,
+    // Motor (PersistentConstraint.h:253-275) on a hinge's or sliding hinge's
+    // axis; Piston (:217-251) on a slider's or sliding hinge's axis, held as two
+    // joints: its slide limit, then its powered row
+    JK_MOTOR = 8, JK_SLIDE_LIMIT = 9, JK_PISTON = 10,
 };
 __host__ __device__ inline bool jk_limit(int k) { return k == JK_CONE || k == JK_TWIST; }
+__host__ __device__ inline bool jk_powered(int k) { return k == JK_MOTOR || k == JK_SLIDE_LIMIT || k == JK_PISTON; }
+// rows listed in an island only while their `active` flag is set, outside the
+// holonomic systems
+__host__ __device__ inline bool jk_conditional(int k) { return jk_limit(k) || jk_powered(k); }
 
 // Static joint description (PhysicsEngine::add*Constraint): anchors are the
 // tracked points relative to each body's centre of mass in its body frame;
@@ -219,14 +234,19 @@ struct JointStore {
     const float4* ax1;      // hinge / slider axis, cone direction, twist axis (body 1 space)
     const float4* ax2;
     const float2* hard;     // pos / rot correction strength
-    const float4* par;      // x: distance target or limit max angle, y: twist min angle
-    const float4* ul;       // twist: body 1's u axis (body space)
+    const float4* par;      // x: distance target or limit max angle / max slide, y: twist / motor min angle, min slide
+    const float4* ul;       // twist, motor: body 1's u axis (body space)
     const float4* wl;       //        and w axis
+    const float4* power;    // motor / piston: mode (0 off, 1 constant, 2 target velocity, 3 target
+                            // position), max torque / force, target velocity, target position
     float* impulse;         // [kJMax] per joint: persistent warm-start impulse
     float4* u;              // hinge / slider / sliding-hinge basis of the last rebuild
     float4* w;
-    float* angle;           // twist: current angle, unwrapped across rebuilds
-    int* active;            // limits: 1 when the last rebuild found the limit reached
+    float* angle;           // twist: current angle, unwrapped across rebuilds; motor: angular position;
+                            // slide limit / piston: slide position
+    int* active;            // limits: reached at the last rebuild; motor, piston: listed in the next island
+    float* aux;             // motor: relative angular velocity of the last rebuild; slide limit /
+                            // piston: 1 when past a slide limit at the last rebuild
     JointRow* rows;
 };
 

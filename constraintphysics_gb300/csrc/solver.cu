@@ -702,7 +702,11 @@ __global__ void __launch_bounds__(32) k_pgs_joint(Dev d, int first) {
             for (int it = 0; it < n_pos; it++)
                 for (int r = rs; r < rs + rc; r++) {
                     RowBlock& R = d.rows[r];
-                    if (R.contact < 0) { jstep(d.jt.rows[-R.contact - 1], dv, true); continue; }
+                    if (R.contact < 0) {
+                        JointRow& Jr = d.jt.rows[-R.contact - 1];
+                        if (Jr.pos) jstep(Jr, dv, true);   // needsPosCorrect
+                        continue;
+                    }
                     float4 imp = R.imp;
                     row_pos(R, imp, dv);
                     R.imp = imp;

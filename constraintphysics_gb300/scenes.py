@@ -79,11 +79,19 @@ class Scene:
         self.params = dict(params)
         self.ops = []
         self.n_bodies = 0
+        self.n_constraints = 0
 
     def _body(self, op):
         self.ops.append(op)
         self.n_bodies += 1
         return self.n_bodies  # ids start at 1
+
+    def _constraint(self, op):
+        """Joints and springs: the handle is the scene's constraint index
+        (apply() maps it to the world's constraint id)."""
+        self.ops.append(op)
+        self.n_constraints += 1
+        return self.n_constraints - 1
 
     def hull(self, points, faces, material, movement, pos):
         return self._body(("hull", points, faces, material, movement, tuple(pos)))
@@ -111,36 +119,50 @@ class Scene:
         self.ops.append(("mass", bid, float(m)))
 
     def ball_socket(self, b1, b2, a1, a2, strength=15000.0):
-        self.ops.append(("ball", b1, b2, tuple(a1), tuple(a2), float(strength)))
+        return self._constraint(("ball", b1, b2, tuple(a1), tuple(a2), float(strength)))
 
     def distance(self, b1, b2, a1, a2, target=-1.0, strength=15000.0):
-        self.ops.append(("distance", b1, b2, tuple(a1), tuple(a2), float(target), float(strength)))
+        return self._constraint(("distance", b1, b2, tuple(a1), tuple(a2), float(target), float(strength)))
 
     def weld(self, b1, b2, a1, a2, pos_strength=15000.0, rot_strength=15000.0):
-        self.ops.append(("weld", b1, b2, tuple(a1), tuple(a2), float(pos_strength), float(rot_strength)))
+        return self._constraint(("weld", b1, b2, tuple(a1), tuple(a2), float(pos_strength), float(rot_strength)))
 
     def twist_limit(self, b1, b2, ax1, ax2, min_angle, max_angle, rot_strength=15000.0):
-        self.ops.append(("twist_limit", b1, b2, tuple(ax1), tuple(ax2), float(min_angle), float(max_angle),
+        return self._constraint(("twist_limit", b1, b2, tuple(ax1), tuple(ax2), float(min_angle), float(max_angle),
                          float(rot_strength)))
 
     def cone_limit(self, b1, b2, ax1, ax2, max_angle, rot_strength=15000.0):
-        self.ops.append(("cone_limit", b1, b2, tuple(ax1), tuple(ax2), float(max_angle), float(rot_strength)))
+        return self._constraint(("cone_limit", b1, b2, tuple(ax1), tuple(ax2), float(max_angle), float(rot_strength)))
 
     def spring(self, b1, b2, a1, a2, damping, stiffness, resting_length=-1.0):
-        self.ops.append(("spring", b1, b2, tuple(a1), tuple(a2), float(damping), float(stiffness),
+        return self._constraint(("spring", b1, b2, tuple(a1), tuple(a2), float(damping), float(stiffness),
                          float(resting_length)))
 
     def slider(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
-        self.ops.append(("slider", b1, b2, tuple(a1), tuple(a2), tuple(ax1), tuple(ax2), float(pos_strength),
+        return self._constraint(("slider", b1, b2, tuple(a1), tuple(a2), tuple(ax1), tuple(ax2), float(pos_strength),
                          float(rot_strength)))
 
     def sliding_hinge(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
-        self.ops.append(("sliding_hinge", b1, b2, tuple(a1), tuple(a2), tuple(ax1), tuple(ax2), float(pos_strength),
+        return self._constraint(("sliding_hinge", b1, b2, tuple(a1), tuple(a2), tuple(ax1), tuple(ax2), float(pos_strength),
                          float(rot_strength)))
 
     def hinge(self, b1, b2, a1, a2, ax1, ax2, pos_strength=15000.0, rot_strength=15000.0):
-        self.ops.append(("hinge", b1, b2, tuple(a1), tuple(a2), tuple(ax1), tuple(ax2), float(pos_strength),
+        return self._constraint(("hinge", b1, b2, tuple(a1), tuple(a2), tuple(ax1), tuple(ax2), float(pos_strength),
                          float(rot_strength)))
+
+    def motor(self, base, min_angle=-np.inf, max_angle=np.inf):
+        """A motor on the hinge or sliding hinge with handle `base`."""
+        return self._constraint(("motor", base, float(min_angle), float(max_angle)))
+
+    def piston(self, base, min_pos=-np.inf, max_pos=np.inf):
+        """A piston on the slider or sliding hinge with handle `base`."""
+        return self._constraint(("piston", base, float(min_pos), float(max_pos)))
+
+    def set_motor(self, handle, mode, max_torque=0.0, target=0.0):
+        self.ops.append(("set_motor", handle, int(mode), float(max_torque), float(target)))
+
+    def set_piston(self, handle, mode, max_force=0.0, target=0.0):
+        self.ops.append(("set_piston", handle, int(mode), float(max_force), float(target)))
 
     def orient(self, bid, q):
         self.ops.append(("orient", bid, tuple(q)))
@@ -158,9 +180,12 @@ class Scene:
 
 
 def apply(scene, world):
-    """Replay `scene` on a World; returns the list of created body ids."""
+    """Replay `scene` on a World; returns the list of created body ids.  The
+    world's ids of the scene's joints and springs (in handle order) are left
+    in `world.constraint_ids`."""
     world.set_params(**scene.params)
     ids = []
+    cids = []
     for op in scene.ops:
         kind = op[0]
         if kind == "hull":
@@ -186,17 +211,26 @@ def apply(scene, world):
         elif kind == "mass":
             world.set_mass(op[1], op[2])
         elif kind == "distance":
-            world.add_distance(op[1], op[2], op[3], op[4], op[5], op[6])
+            cids.append(world.add_distance(op[1], op[2], op[3], op[4], op[5], op[6]))
         elif kind in ("slider", "sliding_hinge", "spring", "cone_limit", "twist_limit"):
-            getattr(world, "add_" + kind)(*op[1:])
+            cids.append(getattr(world, "add_" + kind)(*op[1:]))
         elif kind == "weld":
-            world.add_weld(op[1], op[2], op[3], op[4], op[5], op[6])
+            cids.append(world.add_weld(op[1], op[2], op[3], op[4], op[5], op[6]))
         elif kind == "ball":
-            world.add_ball_socket(op[1], op[2], op[3], op[4], op[5])
+            cids.append(world.add_ball_socket(op[1], op[2], op[3], op[4], op[5]))
         elif kind == "hinge":
-            world.add_hinge(op[1], op[2], op[3], op[4], op[5], op[6], op[7], op[8])
+            cids.append(world.add_hinge(op[1], op[2], op[3], op[4], op[5], op[6], op[7], op[8]))
+        elif kind == "motor":
+            cids.append(world.add_motor(cids[op[1]], op[2], op[3]))
+        elif kind == "piston":
+            cids.append(world.add_piston(cids[op[1]], op[2], op[3]))
+        elif kind == "set_motor":
+            world.set_motor(cids[op[1]], op[2], op[3], op[4])
+        elif kind == "set_piston":
+            world.set_piston(cids[op[1]], op[2], op[3], op[4])
         else:
             raise ValueError(kind)
+    world.constraint_ids = cids
     return ids
 
 
@@ -632,6 +666,53 @@ def slider_chain(kinds=("slider",) * 4):
         getattr(sc, kind)(prev, b, (0.3, 0, 0), (-0.3, 0, 0), axes[i], axes[i])
         prev = b
     sc.box((-0.3, -0.3, -0.3), 0.6, 0.6, 0.6, M, DYNAMIC, (1.8, 6.0, 0.1))
+    return sc
+
+
+def motor_chain(mode=1, limits=False):
+    """Boxes hung from a fixed post by hinges on horizontal axes, each hinge
+    driven by a motor: mode 1 constant torque, 2 target velocity, 3 target
+    position (modes of World.set_motor); with `limits` the motors also limit
+    the hinge angle to [-0.6, 0.9] rad."""
+    M = PILE_MATERIAL
+    sc = Scene(f"motor_chain_{mode}{'_lim' if limits else ''}", JOINT_PARAMS)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, FIXED, (0.0, 4.0, 0.0))
+    axes = [(0.0, 0.0, 1.0), (0.0, 0.3, 1.0), (0.2, 0.0, 1.0)]
+    for i in range(3):
+        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, DYNAMIC, (0.7 * (i + 1), 4.0, 0.0))
+        h = sc.hinge(prev, b, (0.35, 0, 0), (-0.35, 0, 0), axes[i], axes[i])
+        m = sc.motor(h, -0.6, 0.9) if limits else sc.motor(h)
+        if mode == 1:
+            sc.set_motor(m, 1, 40.0 - 15.0 * i)
+        elif mode == 2:
+            sc.set_motor(m, 2, 60.0, 1.5 - 1.0 * i)
+        else:
+            sc.set_motor(m, 3, 80.0, 0.5 + 0.3 * i)
+        prev = b
+    return sc
+
+
+def piston_chain(mode=2, limits=True):
+    """Boxes on slider joints along tilted axes from a fixed post, each slider
+    driven by a piston: mode 1 constant force, 2 target velocity, 3 target
+    position; with `limits` the slide is limited to [-0.2, 0.5] m."""
+    M = PILE_MATERIAL
+    sc = Scene(f"piston_chain_{mode}{'_lim' if limits else ''}", JOINT_PARAMS)
+    sc.box((-10.0, -1.0, -10.0), 20.0, 1.0, 20.0, M, FIXED)
+    prev = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, FIXED, (0.0, 4.0, 0.0))
+    axes = [(1.0, -0.4, 0.2), (1.0, 0.3, 0.0), (1.0, 0.0, -0.3)]
+    for i in range(3):
+        b = sc.box((-0.25, -0.25, -0.25), 0.5, 0.5, 0.5, M, DYNAMIC, (0.6 * (i + 1), 4.0, 0.0))
+        s = sc.slider(prev, b, (0.3, 0, 0), (-0.3, 0, 0), axes[i], axes[i])
+        p = sc.piston(s, -0.2, 0.5) if limits else sc.piston(s)
+        if mode == 1:
+            sc.set_piston(p, 1, 30.0 - 25.0 * i)
+        elif mode == 2:
+            sc.set_piston(p, 2, 80.0, 0.6 - 0.5 * i)
+        else:
+            sc.set_piston(p, 3, 80.0, 0.3 - 0.2 * i)
+        prev = b
     return sc
 
 

@@ -274,6 +274,39 @@ class World:
                                        float(pos_strength), float(rot_strength), C.addressof(out)))
         return out.value
 
+    def add_motor(self, base_id, min_angle=-np.inf, max_angle=np.inf):
+        """PhysicsEngine::addMotorConstraint on a hinge or sliding hinge id."""
+        out = C.c_uint32()
+        self._check(self.abi.add_motor(self.h, int(base_id), float(min_angle), float(max_angle), C.addressof(out)))
+        return out.value
+
+    def add_piston(self, base_id, min_pos=-np.inf, max_pos=np.inf):
+        """PhysicsEngine::addPistonConstraint on a slider or sliding hinge id."""
+        out = C.c_uint32()
+        self._check(self.abi.add_piston(self.h, int(base_id), float(min_pos), float(max_pos), C.addressof(out)))
+        return out.value
+
+    # powered modes of set_motor / set_piston
+    OFF, CONSTANT, TARGET_VELOCITY, TARGET_POSITION = 0, 1, 2, 3
+
+    def set_motor(self, cid, mode, max_torque=0.0, target=0.0):
+        """setMotorOff / ConstantTorque / TargetVelocity / TargetPosition."""
+        self._check(self.abi.set_motor(self.h, int(cid), int(mode), float(max_torque), float(target)))
+
+    def set_piston(self, cid, mode, max_force=0.0, target=0.0):
+        """setPistonOff / ConstantForce / TargetVelocity / TargetPosition."""
+        self._check(self.abi.set_piston(self.h, int(cid), int(mode), float(max_force), float(target)))
+
+    def motor_position(self, cid):
+        out = C.c_double()
+        self._check(self.abi.get_motor_position(self.h, int(cid), C.addressof(out)))
+        return out.value
+
+    def piston_position(self, cid):
+        out = C.c_double()
+        self._check(self.abi.get_piston_position(self.h, int(cid), C.addressof(out)))
+        return out.value
+
     # -- stepping and state -------------------------------------------------------
     def step(self, n=1):
         self._check(self.abi.step(self.h, int(n)))

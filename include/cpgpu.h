@@ -238,6 +238,28 @@ int cpgpu_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2,
                     const double b1_axis_local[3], const double b2_axis_local[3],
                     double pos_correct_strength, double rot_correct_strength,
                     uint32_t* out_id);
+/* PhysicsEngine::addMotorConstraint (PhysicsEngine.cpp:725-763): a motor on
+ * the hinge or sliding hinge `base_id` (its axes and rotation strength), with
+ * angle limits (-inf / +inf for none).  Off until set_motor powers it; its
+ * row is solved while powered or past a limit. */
+int cpgpu_add_motor(cpgpu_world* w, uint32_t base_id, double min_angle, double max_angle, uint32_t* out_id);
+/* PhysicsEngine::addPistonConstraint (PhysicsEngine.cpp:808-852): a piston on
+ * the slider or sliding hinge `base_id` (its tracked points, body 1 axis and
+ * position strength), with slide limits.  It occupies two consecutive slots
+ * of the joint state (its slide limit, then its powered row). */
+int cpgpu_add_piston(cpgpu_world* w, uint32_t base_id, double min_pos, double max_pos, uint32_t* out_id);
+/* PhysicsEngine::setMotorOff / setMotorConstantTorque / setMotorTargetVelocity
+ * / setMotorTargetPosition (PhysicsEngine.cpp:1857-1912) as mode 0 / 1 / 2 / 3:
+ * mode 1 sets the torque (max_torque), modes 2 and 3 the max torque and the
+ * target velocity or angle; mode 0 leaves them.  Both bodies are woken. */
+int cpgpu_set_motor(cpgpu_world* w, uint32_t id, int mode, double max_torque, double target);
+/* setPistonOff / setPistonConstantForce / setPistonTargetVelocity /
+ * setPistonTargetPosition (PhysicsEngine.cpp:1800-1855), the same for force. */
+int cpgpu_set_piston(cpgpu_world* w, uint32_t id, int mode, double max_force, double target);
+/* getMotorAngularPosition / getPistonPosition (PhysicsEngine.cpp:1914-1930):
+ * the angle (unwrapped) or slide position of the last rebuild. */
+int cpgpu_get_motor_position(cpgpu_world* w, uint32_t id, double* out);
+int cpgpu_get_piston_position(cpgpu_world* w, uint32_t id, double* out);
 
 /* ---- stepping and state ------------------------------------------------- */
 /* n_steps x PhysicsEngine::timeStep (PhysicsEngine.cpp:50-471) */
@@ -284,11 +306,14 @@ int cpgpu_raycast(cpgpu_world* w, const double* origins, const double* dirs, int
 /* Warm-start state of the joints (not the springs) in creation order: the
  * impulse of each constraint row (PersistentConstraint.h:90-420), 6 doubles
  * per joint (ball-socket 3 used, sliding hinge 4, hinge and slider 5, weld 6,
- * distance and limits 1); the tangent basis u, w of its last rebuild (hinge,
- * slider, sliding hinge; 3 doubles each); and `aux`, 2 doubles per joint: a
- * twist limit's current angle (unwrapped across rebuilds) and, for a cone or
- * twist limit, 1 when its last rebuild found the limit reached (the row is
- * then solved in the next step), else 0.  With the body state and the
+ * distance, limits, motors and pistons 1); the tangent basis u, w of its last
+ * rebuild (hinge, slider, sliding hinge; 3 doubles each); and `aux`, 2
+ * doubles per joint: a twist limit's current angle (unwrapped across
+ * rebuilds), a motor's angle or a piston's slide position, and then for a
+ * cone or twist limit 1 when its last rebuild found the limit reached (the
+ * row is then solved in the next step), for a motor the relative angular
+ * velocity of its last rebuild, for a piston's two slots 1 when past a slide
+ * limit, else 0.  With the body state and the
  * contacts this completes a checkpoint; no counterpart in the reference,
  * which keeps these inside its constraint objects.  Any pointer but `n` may
  * be NULL. */

@@ -6,13 +6,14 @@
 // Differences a caller sees:
 //   * bodies are addressed by id (RigidBody handles wrap the id);
 //   * errors that the reference reports with assert() throw cpgpu::Error;
-//   * only the contact path is on the device: convex hulls, boxes, spheres,
-//     cylinders, capsules and fixed static triangle meshes; ball-socket,
-//     hinge, distance, weld, slider and sliding-hinge joints, cone and twist
-//     limits and springs; one primitive per body (others throw cpgpu::Error
-//     with CPGPU_ERR_UNSUPPORTED); sleeping stays disabled.
+//   * on the device: convex hulls, boxes, spheres, cylinders, capsules and
+//     fixed static triangle meshes; ball-socket, hinge, distance, weld,
+//     slider and sliding-hinge joints, cone and twist limits, motors,
+//     pistons and springs; sleeping; one primitive per body (others throw
+//     cpgpu::Error with CPGPU_ERR_UNSUPPORTED).
 #pragma once
 #include <array>
+#include <cmath>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -249,6 +250,37 @@ public:
         check(cpgpu_add_hinge(w_, b1->getID(), b2->getID(), p1.data(), p2.data(), a1.data(), a2.data(), pos_strength,
                               rot_strength, &id));
         return ConstraintID{id};
+    }
+    // addMotorConstraint / addPistonConstraint (PhysicsEngine.cpp:725-852)
+    // and the powered constraints' setters and getters (:1800-1930)
+    ConstraintID addMotorConstraint(ConstraintID base, double min_angle = -INFINITY, double max_angle = INFINITY) {
+        uint32_t id = 0;
+        check(cpgpu_add_motor(w_, base.id, min_angle, max_angle, &id));
+        return ConstraintID{id};
+    }
+    ConstraintID addPistonConstraint(ConstraintID base, double negative_slide_limit = -INFINITY,
+                                     double positive_slide_limit = INFINITY) {
+        uint32_t id = 0;
+        check(cpgpu_add_piston(w_, base.id, negative_slide_limit, positive_slide_limit, &id));
+        return ConstraintID{id};
+    }
+    void setMotorOff(ConstraintID id) { check(cpgpu_set_motor(w_, id.id, 0, 0, 0)); }
+    void setMotorConstantTorque(ConstraintID id, double torque) { check(cpgpu_set_motor(w_, id.id, 1, torque, 0)); }
+    void setMotorTargetVelocity(ConstraintID id, double max_torque, double v) { check(cpgpu_set_motor(w_, id.id, 2, max_torque, v)); }
+    void setMotorTargetPosition(ConstraintID id, double max_torque, double a) { check(cpgpu_set_motor(w_, id.id, 3, max_torque, a)); }
+    void setPistonOff(ConstraintID id) { check(cpgpu_set_piston(w_, id.id, 0, 0, 0)); }
+    void setPistonConstantForce(ConstraintID id, double force) { check(cpgpu_set_piston(w_, id.id, 1, force, 0)); }
+    void setPistonTargetVelocity(ConstraintID id, double max_force, double v) { check(cpgpu_set_piston(w_, id.id, 2, max_force, v)); }
+    void setPistonTargetPosition(ConstraintID id, double max_force, double x) { check(cpgpu_set_piston(w_, id.id, 3, max_force, x)); }
+    double getMotorAngularPosition(ConstraintID id) {
+        double out = 0;
+        check(cpgpu_get_motor_position(w_, id.id, &out));
+        return out;
+    }
+    double getPistonPosition(ConstraintID id) {
+        double out = 0;
+        check(cpgpu_get_piston_position(w_, id.id, &out));
+        return out;
     }
 
     void setStep_time(double d) { check(cpgpu_set_step_time(w_, d)); }

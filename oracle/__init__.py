@@ -118,7 +118,9 @@ def twin_worlds(scene):
         def set_params(self, **k):
             pass
 
-    sc_mod.apply(scene, _Twin())
+    twin = _Twin()
+    sc_mod.apply(scene, twin)
+    r.constraint_ids = p.constraint_ids = twin.constraint_ids   # the same numbering on both
     return r, p
 
 

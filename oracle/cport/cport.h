@@ -353,7 +353,12 @@ struct JRow {
     Body* a = nullptr; Body* b = nullptr;
     DV* da = nullptr; DV* db = nullptr;
     bool in_holo = false;
-    int proj = 0;                 // 1 / 2: accumulated impulse kept >= 0 / <= 0 (projectValidImpulse)
+    int proj = 0;                 // 1 / 2: accumulated impulse kept >= 0 / <= 0 (projectValidImpulse);
+                                  // 3: powered rows, x > 0 ? min(x, lim) : max(x, -lim)
+    double lim = 0;               // proj 3: the motor's or piston's impulse bound
+    bool has_vt = false;          // motor / piston: target = vt - value (findTargetConstraintValue)
+    double vt = 0;
+    bool pos = true;              // needsPosCorrect: solved in the position passes
     double impulse[kMaxDof] = {}, pimpulse[kMaxDof] = {}, holo[kMaxDof] = {};
     double target[kMaxDof] = {}, ptarget[kMaxDof] = {};
     double ja[kMaxDof][6] = {}, jb[kMaxDof][6] = {};
@@ -378,7 +383,33 @@ struct Joint {
     bool twist = false;
     double min_angle = 0, cur_angle = 0;
     V3 u_local, w_local;          // b1's perpendicular basis (w first, as the reference)
-    bool holonomic() const { return !cone && !twist; }
+    // Motor (PersistentConstraint.h:253-275) on a hinge's or sliding hinge's
+    // axis; Piston (:217-251) on a slider's or sliding hinge's axis, held as two
+    // joints: its slide limit, then its powered row (addSolverConstraints
+    // lists them in that order)
+    bool motor = false, slide_limit = false, piston = false;
+    int seq = -1;                 // constraint id: PhysicsEngine's nextConstraintID order over joints and springs, from 0
+    int mode = 0;                 // PoweredConstraitMode: 0 off, 1 constant torque / force, 2 target velocity, 3 target position
+    double power_max = 0;         // max_torque / max_force
+    double target_vel = 0, target_pos = 0;
+    double lim_min = 0, lim_max = 0;   // motor angles / slide positions
+    double position = 0;          // motor_angular_position / piston_position
+    double prev_vel = 0;          // motor: prev_velocity (never written for a piston)
+    bool exceeded = false;        // piston: slide_limit_exceeded of the last rebuild
+    V3 ref_u, ref_w, cmp;         // motor: body 1's u, w reference axes, body 2's comparison axis (body space)
+    bool powered() const { return motor || slide_limit || piston; }
+    bool holonomic() const { return !cone && !twist && !powered(); }
+    // addSolverConstraints: whether the joint's row is listed in its island
+    bool listed() const {
+        if (cone || twist) return !inactive;
+        if (motor) return (mode != 0 && power_max != 0) || position < lim_min || position > lim_max;
+        if (slide_limit) return exceeded;
+        if (piston) return mode != 0 && power_max != 0;
+        return true;
+    }
+    double motorPosition(const V3& axis, const V3& w1, const V3& w2, double dts) const;
+    double motorTargetVelocity(const V3& axis, const V3& w1, const V3& w2) const;
+    double pistonTargetVelocity(const V3& axis) const;
     double target = 0;            // distance: the attachment points' distance
     Body* b1 = nullptr; Body* b2 = nullptr;
     int k1 = 0, k2 = 0;           // tracked point keys
@@ -441,6 +472,7 @@ struct Contact {
 // Spring (PersistentConstraint.h:411-434): not a solver row; an impulse pair
 // applied at the start of every substep
 struct Spring {
+    int seq = -1;                 // constraint id (creation order among joints and springs, from 0)
     Body* b1; Body* b2;
     int k1, k2;                   // tracked point keys
     double stiffness, damping, rest;
@@ -511,6 +543,16 @@ struct World {
     void maintainHolonomicSystems();
     void applySprings(double dt_sub);
     Joint* addTwist(Body* b1, Body* b2, V3 ax1, V3 ax2, double min_angle, double max_angle, double rot_hard);
+    Joint* addMotor(Joint* base, double min_angle, double max_angle);
+    int constraint_seq = 0;       // PhysicsEngine::nextConstraintID (PhysicsEngine.h:301)
+    // the joint a constraint id names (a piston's two joints share its id:
+    // the powered one, created last)
+    Joint* jointById(uint32_t id) {
+        Joint* out = nullptr;
+        for (auto& j : joints) if (j->seq == (int)id) out = j.get();
+        return out;
+    }
+    Joint* addPiston(Joint* base, double min_pos, double max_pos);
     Joint* addCone(Body* b1, Body* b2, V3 ax1, V3 ax2, double max_angle, double rot_hard);
     Spring* addSpring(Body* b1, Body* b2, V3 p1, V3 p2, double damping, double stiffness, double rest);
     void holonomicScan(Edge* e);

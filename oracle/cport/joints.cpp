@@ -112,7 +112,163 @@ static void finishRow(JRow& r, double cfm) {
 // Hinge::updateSolverConstraints (:274-285) with HingeConstraint
 // (ConstraintSolver.cpp:468-550).  The hinge's rB is taken from body 1's
 // anchor point, as the reference's constructor does.
+// Motor::calculatePosition (PersistentConstraint.cpp:30-71): the last angle
+// advanced by the relative angular velocity, snapped to the angle of body 2's
+// comparison axis in body 1's (u, w) plane (in the 2 pi window nearest the
+// prediction) unless that axis is within acos(0.999) of the motor axis
+double Joint::motorPosition(const V3& axis, const V3& w1, const V3& w2, double dts) const {
+    V3 ref_axis_u = b1->q.rotate(ref_u);
+    V3 ref_axis_w = b1->q.rotate(ref_w);
+    V3 compare_axis = b2->q.rotate(cmp);
+    double rel = axis.dot(w1) - axis.dot(w2);
+    double pred = position + rel * dts;
+    if (std::abs(compare_axis.dot(axis)) > 0.999) return pred;
+    V3 cn = (compare_axis - axis * axis.dot(compare_axis)).normalize();
+    double dv = cn.dot(ref_axis_u);
+    if (dv > 1.0) dv = 1.0;
+    if (dv < -1.0) dv = -1.0;
+    double rel_angle = 2 * PI_TRUNC - std::acos(dv);
+    if (cn.dot(ref_axis_w) < 0) rel_angle = 2 * PI_TRUNC - rel_angle;
+    double r = std::fmod(pred, 2 * PI_TRUNC);
+    double n2 = pred - r;
+    const double cands[3] = {n2 + rel_angle - 2 * PI_TRUNC, n2 + rel_angle, n2 + rel_angle + 2 * PI_TRUNC};
+    double closest = std::numeric_limits<double>::infinity();
+    for (double c : cands)
+        if (std::abs(pred - c) < std::abs(pred - closest)) closest = c;
+    return closest;
+}
+
+// Motor::getConstraintTargetVelocityValue (PersistentConstraint.cpp:77-109):
+// off 0, constant torque an infinite target in the torque's direction, target
+// velocity as set, target position the velocity that a constant max torque
+// reaches over the remaining angle, the inertia estimated from the last
+// impulse and velocity change (or from the inverse tensors when either is
+// below 1e-7; the reference tests `abs(impulse < EPS)`, true for every
+// impulse below 1e-7, negative ones included)
+double Joint::motorTargetVelocity(const V3& axis, const V3& w1, const V3& w2) const {
+    switch (mode) {
+        case 0: return 0;
+        case 1: return power_max > 0 ? std::numeric_limits<double>::infinity() : -std::numeric_limits<double>::infinity();
+        case 2: return target_vel;
+        default: {
+            double ang_diff = position - target_pos;
+            double dir = (ang_diff > 0) ? -1 : 1;
+            double vdt = std::abs((axis.dot(w1) - axis.dot(w2)) - prev_vel);
+            const double EPS = 0.0000001;
+            double inertia;
+            if (vdt < EPS || row.impulse[0] < EPS)
+                inertia = 1.0 / (axis.dot(b1->invTensor() * axis) + axis.dot(b2->invTensor() * axis));
+            else
+                inertia = std::abs(row.impulse[0]) / vdt;
+            return dir * std::sqrt(2 * std::abs(ang_diff) * power_max / inertia);
+        }
+    }
+}
+
+// Piston::getPistonTargetVelocityValue (PersistentConstraint.cpp:153-185), the
+// same with the inverse masses; the piston's previous velocity is never
+// written (writePrevVel has no caller) and stays 0
+double Joint::pistonTargetVelocity(const V3& axis) const {
+    switch (mode) {
+        case 0: return 0;
+        case 1: return power_max > 0 ? std::numeric_limits<double>::infinity() : -std::numeric_limits<double>::infinity();
+        case 2: return target_vel;
+        default: {
+            double ang_diff = position - target_pos;
+            double dir = (ang_diff > 0) ? -1 : 1;
+            double vdt = std::abs((axis.dot(b1->getVel()) - axis.dot(b2->getVel())) - prev_vel);
+            const double EPS = 0.0000001;
+            double inertia;
+            if (vdt < EPS || row.impulse[0] < EPS) inertia = 1.0 / (b1->invMass() + b2->invMass());
+            else inertia = std::abs(row.impulse[0]) / vdt;
+            return dir * std::sqrt(2 * std::abs(ang_diff) * power_max / inertia);
+        }
+    }
+}
+
 void Joint::rebuild(const Params& p, double dts, bool in_holo) {
+    if (motor) {
+        // Motor::updateSolverConstraints (PersistentConstraint.cpp:320-328) with
+        // the MotorConstraint constructor (ConstraintSolver.cpp:555-585): the
+        // angle advanced first; while active one row on body 1's axis, its
+        // target velocity limited to the limit's side and a one-sided
+        // projection past a limit, else bounded by max torque x dt; the old
+        // row is kept while inactive
+        V3 axis = b1->q.rotate(ax1);
+        V3 w1 = b1->getAngVel(), w2 = b2->getAngVel();
+        position = motorPosition(axis, w1, w2, dts);
+        const double start = p.warm_start_disabled ? 0.0 : 1.0 * row.impulse[0];
+        if (listed()) {
+            const double tv = 1.0 * motorTargetVelocity(axis, w1, w2);
+            const double hard = std::min<double>(rot_hard * dts, 1.0 / dts);
+            JRow r;
+            r.n = 1; r.a = b1; r.b = b2;
+            r.impulse[0] = start;
+            const double ad[3] = {axis.x, axis.y, axis.z};
+            for (int k = 0; k < 3; k++) {
+                r.ja[0][k] = 0; r.ja[0][3 + k] = ad[k];
+                r.jb[0][k] = 0; r.jb[0][3 + k] = -ad[k];
+            }
+            r.has_vt = true;
+            if (position > lim_max) {
+                r.ptarget[0] = (lim_max - position) * hard;
+                r.vt = std::min<double>(0, tv);
+                r.proj = 2;
+            } else if (position < lim_min) {
+                r.ptarget[0] = (lim_min - position) * hard;
+                r.vt = std::max<double>(0, tv);
+                r.proj = 1;
+            } else {
+                r.ptarget[0] = 0;
+                r.vt = tv;
+                r.proj = 3;
+                r.lim = std::abs(power_max * dts);
+                r.pos = false;
+            }
+            finishRow(r, p.cfm);
+            row = r;
+        }
+        prev_vel = axis.dot(w1) - axis.dot(w2);
+        return;
+    }
+    if (slide_limit || piston) {
+        // Piston::updateSolverConstraints (PersistentConstraint.cpp:300-318):
+        // the slide position along body 1's axis between the slider's tracked
+        // points; past a limit a SlideLimitConstraint row (ConstraintSolver.cpp:
+        // 736-775), while powered a PistonConstraint row (:701-731), both along
+        // the axis (their angular Jacobian, -s^T [s]x, is zero)
+        V3 pa = b1->trackedP(k1), pb = b2->trackedP(k2);
+        V3 axis = b1->q.rotate(ax1);
+        position = pb.dot(axis) - pa.dot(axis);
+        exceeded = position < lim_min || position > lim_max;
+        if (!listed()) return;
+        const double start = p.warm_start_disabled ? 0.0 : 1.0 * row.impulse[0];
+        JRow r;
+        r.n = 1; r.a = b1; r.b = b2;
+        r.impulse[0] = start;
+        const double sd[3] = {axis.x, axis.y, axis.z}, nsd[3] = {-axis.x, -axis.y, -axis.z};
+        double sx[3][3], ang[3];
+        crossMatInto(axis, sx);
+        rowTimes(nsd, sx, ang);
+        for (int k = 0; k < 3; k++) {
+            r.ja[0][k] = -sd[k]; r.ja[0][3 + k] = ang[k];
+            r.jb[0][k] = sd[k]; r.jb[0][3 + k] = 0;
+        }
+        if (slide_limit) {
+            const double hard = std::min<double>(pos_hard * dts, 1.0 / dts);
+            if (position > lim_max) { r.ptarget[0] = (lim_max - position) * hard; r.proj = 2; }
+            else { r.ptarget[0] = (lim_min - position) * hard; r.proj = 1; }
+        } else {
+            r.has_vt = true;
+            r.vt = pistonTargetVelocity(axis);
+            r.proj = 3;
+            r.lim = power_max * dts;
+            r.pos = false;
+        }
+        finishRow(r, p.cfm);
+        row = r;
+        return;
+    }
     if (cone) {
         // ConeRotationLimit::updateSolverConstraints (PersistentConstraint.cpp:233-247)
         // with ConeLimitConstraint (ConstraintSolver.cpp:410-432): inactive
@@ -400,7 +556,10 @@ void jrowTarget(JRow& r) {
     vb.v[0] = v.x; vb.v[1] = v.y; vb.v[2] = v.z; vb.v[3] = w.x; vb.v[4] = w.y; vb.v[5] = w.z;
     double cur[kMaxDof];
     jrowValue(r, va, vb, cur);
-    for (int i = 0; i < r.n; i++) r.target[i] = -cur[i];
+    // MotorConstraint / PistonConstraint::findTargetConstraintValue
+    // (ConstraintSolver.cpp:586-589, 723-726): the target velocity less the value
+    if (r.has_vt) r.target[0] = r.vt - cur[0];
+    else for (int i = 0; i < r.n; i++) r.target[i] = -cur[i];
 }
 
 void jrowWarm(JRow& r) {
@@ -424,6 +583,8 @@ void jrowStep(JRow& r, bool pseudo) {
         // (ConstraintSolver.cpp:434-436, 463-465)
         if (r.proj == 1) nw = std::max<double>(nw, 0);
         else if (r.proj == 2) nw = std::min<double>(nw, 0);
+        // MotorConstraint / PistonConstraint::projectValidImpulse (ConstraintSolver.cpp:591-606, 728-731)
+        else if (r.proj == 3) nw = nw > 0 ? std::min<double>(nw, r.lim) : std::max<double>(nw, -r.lim);
         diff[i] = nw - acc[i];
     }
     if (!isZero(diff, r.n)) {
@@ -702,6 +863,7 @@ Joint* World::addJoint(int n, Body* b1, Body* b2, V3 p1, V3 p2, V3 ax1, V3 ax2, 
     b2->no_collide.insert(b1);
     auto j = std::make_unique<Joint>();
     j->n = n;
+    j->seq = constraint_seq++;
     j->b1 = b1; j->b2 = b2;
     b1->track_p.push_back(b1->local_origin + p1);
     j->k1 = (int)b1->track_p.size() - 1;
@@ -730,6 +892,7 @@ Joint* World::addCone(Body* b1, Body* b2, V3 ax1, V3 ax2, double max_angle, doub
     b2->no_collide.insert(b1);
     auto j = std::make_unique<Joint>();
     j->n = 1; j->cone = true;
+    j->seq = constraint_seq++;
     j->b1 = b1; j->b2 = b2;
     j->ax1 = ax1; j->ax2 = ax2;
     j->max_angle = max_angle;
@@ -752,6 +915,64 @@ Joint* World::addTwist(Body* b1, Body* b2, V3 ax1, V3 ax2, double min_angle, dou
     j->max_angle = max_angle;
     ax1.perpBasis(&j->w_local, &j->u_local);
     return j;
+}
+
+// PhysicsEngine::addMotorConstraint (PhysicsEngine.cpp:725-763) and the Motor
+// constructor (PersistentConstraint.cpp:5-24): on the base hinge's (or
+// sliding hinge's) axes and rotation strength, appended to the base's edge
+Joint* World::addMotor(Joint* base, double min_angle, double max_angle) {
+    auto j = std::make_unique<Joint>();
+    j->n = 1; j->motor = true;
+    j->seq = constraint_seq++;
+    j->b1 = base->b1; j->b2 = base->b2;
+    j->ax1 = base->ax1; j->ax2 = base->ax2;
+    j->rot_hard = base->rot_hard;
+    j->lim_min = min_angle; j->lim_max = max_angle;
+    V3 tmp;
+    j->ax1.perpBasis(&j->ref_u, &j->ref_w);
+    j->ax2.perpBasis(&j->cmp, &tmp);
+    j->row.n = 1; j->row.a = j->b1; j->row.b = j->b2;
+    j->position = 0;
+    j->position = j->motorPosition(j->b1->q.rotate(j->ax1), V3(), V3(), 0);
+    Edge* e = getOrCreateEdge(j->b1, j->b2);
+    j->edge = e;
+    e->joints.push_back(j.get());
+    joints.push_back(std::move(j));
+    return joints.back().get();
+}
+
+// PhysicsEngine::addPistonConstraint (PhysicsEngine.cpp:808-852) and the
+// Piston constructor (PersistentConstraint.cpp:134-143): on the base slider's
+// (or sliding hinge's) tracked points, body 1 axis and position strength, as
+// two joints (slide limit, powered row) appended to the base's edge.  The
+// constructor's position reads body 2's point key on body 1
+// (getTrackedP's (-1, -1, -1) when body 1 has no such key); every rebuild
+// recomputes it from both bodies.  Returns the powered joint.
+Joint* World::addPiston(Joint* base, double min_pos, double max_pos) {
+    Joint* out = nullptr;
+    const int seq = constraint_seq++;
+    for (int part = 0; part < 2; part++) {
+        auto j = std::make_unique<Joint>();
+        j->n = 1;
+        j->seq = seq;
+        (part == 0 ? j->slide_limit : j->piston) = true;
+        j->b1 = base->b1; j->b2 = base->b2;
+        j->k1 = base->k1; j->k2 = base->k2;
+        j->ax1 = base->ax1;
+        j->pos_hard = base->pos_hard;
+        j->lim_min = min_pos; j->lim_max = max_pos;
+        j->row.n = 1; j->row.a = j->b1; j->row.b = j->b2;
+        V3 pa = j->b1->trackedP(j->k1);
+        V3 pb = j->k2 < (int)j->b1->track_p.size() ? j->b1->trackedP(j->k2) : V3(-1, -1, -1);
+        V3 axis = j->b1->q.rotate(j->ax1);
+        j->position = pb.dot(axis) - pa.dot(axis);
+        Edge* e = getOrCreateEdge(j->b1, j->b2);
+        j->edge = e;
+        e->joints.push_back(j.get());
+        joints.push_back(std::move(j));
+        out = joints.back().get();
+    }
+    return out;
 }
 
 // getAllEdgesConnectedHolonomically (PhysicsEngine.cpp:1745-1777)

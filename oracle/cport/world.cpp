@@ -831,7 +831,7 @@ static void pgsSolve(World& world, std::vector<RowRef>& rows, int n_vel, int n_p
     for (int it = 0; it < n_pos; it++)
         for (RowRef& rr : rows) {
             if (rr.kind == 0) pgsStep(rr.c->normal, true, projN);
-            else if (rr.kind == 2) jrowStep(rr.j->row, true);
+            else if (rr.kind == 2 && rr.j->row.pos) jrowStep(rr.j->row, true);   // needsPosCorrect
         }
     // direct solve of the holonomic systems after the sweeps
     // (ConstraintSolver.cpp:160-190); the holonomic impulse is carried into the
@@ -1000,6 +1000,7 @@ void World::applySprings(double dt) {
 // rest length < 0 means the attachment points' current distance
 Spring* World::addSpring(Body* b1, Body* b2, V3 p1, V3 p2, double damping, double stiffness, double rest) {
     auto sp = std::make_unique<Spring>();
+    sp->seq = constraint_seq++;
     sp->b1 = b1; sp->b2 = b2;
     b1->track_p.push_back(b1->local_origin + p1);
     sp->k1 = (int)b1->track_p.size() - 1;
@@ -1120,9 +1121,10 @@ void World::step() {
                     // a sleeping body's edges to sleeping or fixed bodies carry no rows
                     if ((cur->getAsleep() && (o->getAsleep() || o->movement == FIXED)) || visited.count(o)) continue;
                     if (holo && e->h && std::find(blocks.begin(), blocks.end(), e->h) == blocks.end()) blocks.push_back(e->h);
-                    // ConeRotationLimit::addSolverConstraints: only while active
+                    // addSolverConstraints: limits only while reached, motors and
+                    // pistons only while powered or past a limit
                     for (Joint* j : e->joints)
-                        if (!((j->cone || j->twist) && j->inactive)) rows.push_back({2, nullptr, j});
+                        if (j->listed()) rows.push_back({2, nullptr, j});
                     for (auto& c : e->contacts)
                         if (c->live) { rows.push_back({0, c.get()}); rows.push_back({1, c.get()}); }
                 }
@@ -1404,7 +1406,7 @@ int cport_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2, const double
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addJoint(3, x, y, v3(a1), v3(a2), V3(), V3(), strength, 0);
-    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    if (out_id) *out_id = (uint32_t)(W(w)->constraint_seq - 1);
     return CPGPU_OK;
 }
 // PhysicsEngine::addDistanceConstraint (PhysicsEngine.cpp:623-660)
@@ -1413,7 +1415,7 @@ int cport_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addJoint(1, x, y, v3(a1), v3(a2), V3(), V3(), strength, 0, target);
-    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    if (out_id) *out_id = (uint32_t)(W(w)->constraint_seq - 1);
     return CPGPU_OK;
 }
 // PhysicsEngine::addWeldConstraint (PhysicsEngine.cpp:896-915)
@@ -1422,7 +1424,7 @@ int cport_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3],
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addJoint(6, x, y, v3(a1), v3(a2), V3(), V3(), ps, rs);
-    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    if (out_id) *out_id = (uint32_t)(W(w)->constraint_seq - 1);
     return CPGPU_OK;
 }
 // PhysicsEngine::addTwistLimitConstraint (PhysicsEngine.cpp:952-972)
@@ -1431,7 +1433,7 @@ int cport_add_twist_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addTwist(x, y, v3(ax1), v3(ax2), min_angle, max_angle, rs);
-    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    if (out_id) *out_id = (uint32_t)(W(w)->constraint_seq - 1);
     return CPGPU_OK;
 }
 // PhysicsEngine::addConeLimitConstraint (PhysicsEngine.cpp:926-946)
@@ -1440,7 +1442,7 @@ int cport_add_cone_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double 
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addCone(x, y, v3(ax1), v3(ax2), max_angle, rs);
-    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    if (out_id) *out_id = (uint32_t)(W(w)->constraint_seq - 1);
     return CPGPU_OK;
 }
 // PhysicsEngine::addSpring (PhysicsEngine.cpp:974-998)
@@ -1449,7 +1451,7 @@ int cport_add_spring(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addSpring(x, y, v3(a1), v3(a2), damping, stiffness, rest);
-    if (out_id) *out_id = (uint32_t)(W(w)->joints.size() + W(w)->springs.size());
+    if (out_id) *out_id = (uint32_t)(W(w)->constraint_seq - 1);
     return CPGPU_OK;
 }
 // PhysicsEngine::addSliderConstraint (PhysicsEngine.cpp:773-806)
@@ -1458,7 +1460,7 @@ int cport_add_slider(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addJoint(5, x, y, v3(a1), v3(a2), v3(ax1), v3(ax2), ps, rs)->slider = true;
-    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    if (out_id) *out_id = (uint32_t)(W(w)->constraint_seq - 1);
     return CPGPU_OK;
 }
 // PhysicsEngine::addSlidingHingeConstraint (PhysicsEngine.cpp:860-890)
@@ -1467,7 +1469,7 @@ int cport_add_sliding_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const doub
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addJoint(4, x, y, v3(a1), v3(a2), v3(ax1), v3(ax2), ps, rs);
-    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    if (out_id) *out_id = (uint32_t)(W(w)->constraint_seq - 1);
     return CPGPU_OK;
 }
 // PhysicsEngine::addHingeConstraint (PhysicsEngine.cpp:693-723)
@@ -1476,7 +1478,69 @@ int cport_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3]
     Body* x = B(w, b1); Body* y = B(w, b2);
     if (!x || !y || x == y) return fail("bad body id");
     W(w)->addJoint(5, x, y, v3(a1), v3(a2), v3(ax1), v3(ax2), ps, rs);
-    if (out_id) *out_id = (uint32_t)W(w)->joints.size();
+    if (out_id) *out_id = (uint32_t)(W(w)->constraint_seq - 1);
+    return CPGPU_OK;
+}
+// PhysicsEngine::addMotorConstraint (PhysicsEngine.cpp:725-763): on a hinge or
+// a sliding hinge
+int cport_add_motor(cpgpu_world* w, uint32_t base, double min_angle, double max_angle, uint32_t* out_id) {
+    World* x = W(w);
+    Joint* b = x->jointById(base);
+    if (!b) return fail("bad constraint id");
+    const bool hinge = b->n == 5 && !b->slider && !b->powered() && !b->cone && !b->twist;
+    if (!hinge && b->n != 4) return fail("a motor needs a hinge or a sliding hinge");
+    x->addMotor(b, min_angle, max_angle);
+    if (out_id) *out_id = (uint32_t)(x->constraint_seq - 1);
+    return CPGPU_OK;
+}
+// PhysicsEngine::addPistonConstraint (PhysicsEngine.cpp:808-852): on a slider
+// or a sliding hinge; the id names the powered joint (its slide limit is the
+// joint before it)
+int cport_add_piston(cpgpu_world* w, uint32_t base, double min_pos, double max_pos, uint32_t* out_id) {
+    World* x = W(w);
+    Joint* b = x->jointById(base);
+    if (!b) return fail("bad constraint id");
+    if (!(b->n == 5 && b->slider) && b->n != 4) return fail("a piston needs a slider or a sliding hinge");
+    x->addPiston(b, min_pos, max_pos);
+    if (out_id) *out_id = (uint32_t)(x->constraint_seq - 1);
+    return CPGPU_OK;
+}
+// setMotorOff / setMotorConstantTorque / setMotorTargetVelocity /
+// setMotorTargetPosition (PhysicsEngine.cpp:1857-1912) and the piston's
+// (:1800-1855): mode 0 off, 1 constant torque (force) = max, 2 target velocity,
+// 3 target position; each sets the fields the reference's setter sets and
+// alerts both bodies
+static int setPowered(cpgpu_world* w, uint32_t id, bool motor, int mode, double max, double target) {
+    World* x = W(w);
+    Joint* j = x->jointById(id);
+    if (!j) return fail("bad constraint id");
+    if (motor ? !j->motor : !j->piston) return fail(motor ? "not a motor" : "not a piston");
+    if (mode < 0 || mode > 3) return fail("bad mode");
+    j->mode = mode;
+    if (mode >= 1) j->power_max = max;
+    if (mode == 2) j->target_vel = target;
+    if (mode == 3) j->target_pos = target;
+    j->b1->alertWaking();
+    j->b2->alertWaking();
+    return CPGPU_OK;
+}
+int cport_set_motor(cpgpu_world* w, uint32_t id, int mode, double max_torque, double target) {
+    return setPowered(w, id, true, mode, max_torque, target);
+}
+int cport_set_piston(cpgpu_world* w, uint32_t id, int mode, double max_force, double target) {
+    return setPowered(w, id, false, mode, max_force, target);
+}
+// getMotorAngularPosition / getPistonPosition (PhysicsEngine.cpp:1914-1930)
+int cport_get_motor_position(cpgpu_world* w, uint32_t id, double* out) {
+    Joint* j = W(w)->jointById(id);
+    if (!j || !j->motor) return fail("not a motor");
+    *out = j->position;
+    return CPGPU_OK;
+}
+int cport_get_piston_position(cpgpu_world* w, uint32_t id, double* out) {
+    Joint* j = W(w)->jointById(id);
+    if (!j || !j->piston) return fail("not a piston");
+    *out = j->position;
     return CPGPU_OK;
 }
 // Test hook: replace the mass properties computed at creation by given ones
@@ -1509,8 +1573,10 @@ int cport_get_joint_state(cpgpu_world* w, double* impulse, double* u, double* wv
         if (u) { u[3 * j] = J.u.x; u[3 * j + 1] = J.u.y; u[3 * j + 2] = J.u.z; }
         if (wv) { wv[3 * j] = J.w.x; wv[3 * j + 1] = J.w.y; wv[3 * j + 2] = J.w.z; }
         if (aux) {
-            aux[2 * j] = J.cur_angle;
-            aux[2 * j + 1] = ((J.cone || J.twist) && !J.inactive) ? 1.0 : 0.0;
+            aux[2 * j] = J.powered() ? J.position : J.cur_angle;
+            aux[2 * j + 1] = J.motor ? J.prev_vel
+                             : (J.slide_limit || J.piston) ? (J.exceeded ? 1.0 : 0.0)
+                             : ((J.cone || J.twist) && !J.inactive) ? 1.0 : 0.0;
         }
     }
     return CPGPU_OK;
@@ -1529,8 +1595,11 @@ int cport_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
         if (u) J.u = V3(u[3 * j], u[3 * j + 1], u[3 * j + 2]);
         if (wv) J.w = V3(wv[3 * j], wv[3 * j + 1], wv[3 * j + 2]);
         if (aux) {
-            J.cur_angle = aux[2 * j];
+            if (J.powered()) J.position = aux[2 * j];
+            else J.cur_angle = aux[2 * j];
             if (J.cone || J.twist) J.inactive = aux[2 * j + 1] == 0.0;
+            if (J.motor) J.prev_vel = aux[2 * j + 1];
+            if (J.slide_limit || J.piston) J.exceeded = aux[2 * j + 1] != 0.0;
         }
     }
     if (x->p.pgs_holo > 0) {

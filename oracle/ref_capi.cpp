@@ -50,6 +50,7 @@ struct RefWorld {
     phyz::PhysicsEngine engine;
     std::vector<phyz::RigidBody*> bodies;   // index = id - 1
     std::vector<uint32_t> last_pairs;       // flattened (lo, hi)
+    std::unordered_map<uint32_t, phyz::ConstraintID> cids;   // returned id -> the engine's ConstraintID
 };
 
 thread_local std::string g_err;
@@ -295,6 +296,7 @@ int cpref_add_ball_socket(cpgpu_world* w, uint32_t b1, uint32_t b2, const double
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
     if (!r1 || !r2) return fail("bad body id");
     phyz::ConstraintID id = RW->engine.addBallSocketConstraint(r1, r2, v3(a1), v3(a2), strength);
+    RW->cids[id.getID()] = id;
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
@@ -303,6 +305,7 @@ int cpref_add_distance(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
     if (!r1 || !r2) return fail("bad body id");
     phyz::ConstraintID id = RW->engine.addDistanceConstraint(r1, r2, v3(a1), v3(a2), target, strength);
+    RW->cids[id.getID()] = id;
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
@@ -311,6 +314,7 @@ int cpref_add_weld(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3],
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
     if (!r1 || !r2) return fail("bad body id");
     phyz::ConstraintID id = RW->engine.addWeldConstraint(r1, r2, v3(a1), v3(a2), ps, rs);
+    RW->cids[id.getID()] = id;
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
@@ -319,6 +323,7 @@ int cpref_add_twist_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
     if (!r1 || !r2) return fail("bad body id");
     phyz::ConstraintID id = RW->engine.addTwistLimitConstraint(r1, r2, v3(ax1), v3(ax2), min_angle, max_angle, rs);
+    RW->cids[id.getID()] = id;
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
@@ -327,6 +332,7 @@ int cpref_add_cone_limit(cpgpu_world* w, uint32_t b1, uint32_t b2, const double 
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
     if (!r1 || !r2) return fail("bad body id");
     phyz::ConstraintID id = RW->engine.addConeLimitConstraint(r1, r2, v3(ax1), v3(ax2), max_angle, rs);
+    RW->cids[id.getID()] = id;
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
@@ -335,6 +341,7 @@ int cpref_add_spring(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
     if (!r1 || !r2) return fail("bad body id");
     phyz::ConstraintID id = RW->engine.addSpring(r1, r2, v3(a1), v3(a2), damping, stiffness, rest);
+    RW->cids[id.getID()] = id;
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
@@ -343,6 +350,7 @@ int cpref_add_slider(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
     if (!r1 || !r2) return fail("bad body id");
     phyz::ConstraintID id = RW->engine.addSliderConstraint(r1, r2, v3(a1), v3(a2), v3(ax1), v3(ax2), ps, rs);
+    RW->cids[id.getID()] = id;
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
@@ -351,6 +359,7 @@ int cpref_add_sliding_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const doub
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
     if (!r1 || !r2) return fail("bad body id");
     phyz::ConstraintID id = RW->engine.addSlidingHingeConstraint(r1, r2, v3(a1), v3(a2), v3(ax1), v3(ax2), ps, rs);
+    RW->cids[id.getID()] = id;
     if (out_id) *out_id = id.getID();
     return CPGPU_OK;
 }
@@ -359,7 +368,63 @@ int cpref_add_hinge(cpgpu_world* w, uint32_t b1, uint32_t b2, const double a1[3]
     phyz::RigidBody* r1 = body(RW, b1); phyz::RigidBody* r2 = body(RW, b2);
     if (!r1 || !r2) return fail("bad body id");
     phyz::ConstraintID id = RW->engine.addHingeConstraint(r1, r2, v3(a1), v3(a2), v3(ax1), v3(ax2), ps, rs);
+    RW->cids[id.getID()] = id;
     if (out_id) *out_id = id.getID();
+    return CPGPU_OK;
+}
+
+// PhysicsEngine::addMotorConstraint / addPistonConstraint and the powered
+// constraints' setters and getters
+int cpref_add_motor(cpgpu_world* w, uint32_t base, double min_angle, double max_angle, uint32_t* out_id) {
+    auto it = RW->cids.find(base);
+    if (it == RW->cids.end()) return fail("bad constraint id");
+    phyz::ConstraintID id = RW->engine.addMotorConstraint(it->second, min_angle, max_angle);
+    RW->cids[id.getID()] = id;
+    if (out_id) *out_id = id.getID();
+    return CPGPU_OK;
+}
+int cpref_add_piston(cpgpu_world* w, uint32_t base, double min_pos, double max_pos, uint32_t* out_id) {
+    auto it = RW->cids.find(base);
+    if (it == RW->cids.end()) return fail("bad constraint id");
+    phyz::ConstraintID id = RW->engine.addPistonConstraint(it->second, min_pos, max_pos);
+    RW->cids[id.getID()] = id;
+    if (out_id) *out_id = id.getID();
+    return CPGPU_OK;
+}
+int cpref_set_motor(cpgpu_world* w, uint32_t cid, int mode, double max_torque, double target) {
+    auto it = RW->cids.find(cid);
+    if (it == RW->cids.end()) return fail("bad constraint id");
+    switch (mode) {
+        case 0: RW->engine.setMotorOff(it->second); break;
+        case 1: RW->engine.setMotorConstantTorque(it->second, max_torque); break;
+        case 2: RW->engine.setMotorTargetVelocity(it->second, max_torque, target); break;
+        case 3: RW->engine.setMotorTargetPosition(it->second, max_torque, target); break;
+        default: return fail("bad mode");
+    }
+    return CPGPU_OK;
+}
+int cpref_set_piston(cpgpu_world* w, uint32_t cid, int mode, double max_force, double target) {
+    auto it = RW->cids.find(cid);
+    if (it == RW->cids.end()) return fail("bad constraint id");
+    switch (mode) {
+        case 0: RW->engine.setPistonOff(it->second); break;
+        case 1: RW->engine.setPistonConstantForce(it->second, max_force); break;
+        case 2: RW->engine.setPistonTargetVelocity(it->second, max_force, target); break;
+        case 3: RW->engine.setPistonTargetPosition(it->second, max_force, target); break;
+        default: return fail("bad mode");
+    }
+    return CPGPU_OK;
+}
+int cpref_get_motor_position(cpgpu_world* w, uint32_t cid, double* out) {
+    auto it = RW->cids.find(cid);
+    if (it == RW->cids.end()) return fail("bad constraint id");
+    *out = RW->engine.getMotorAngularPosition(it->second);
+    return CPGPU_OK;
+}
+int cpref_get_piston_position(cpgpu_world* w, uint32_t cid, double* out) {
+    auto it = RW->cids.find(cid);
+    if (it == RW->cids.end()) return fail("bad constraint id");
+    *out = RW->engine.getPistonPosition(it->second);
     return CPGPU_OK;
 }
 

@@ -703,3 +703,64 @@ def test_restatement_checkpoint_restore_steps_like_the_uninterrupted_run(oracle_
     ja, jb = a.joint_state(), b.joint_state()
     for k in ja:
         assert np.array_equal(ja[k], jb[k]), k
+
+POWERED = [("motor", m, lim) for m in (1, 2, 3) for lim in (False, True) if not (m == 1 and lim)] + \
+          [("piston", m, lim) for m in (1, 2, 3) for lim in (False, True)]
+
+
+def _powered_scene(kind, mode, limits):
+    return scenes.motor_chain(mode, limits) if kind == "motor" else scenes.piston_chain(mode, limits)
+
+
+@pytest.mark.parametrize("kind,mode,limits", POWERED)
+def test_restatement_bitwise_with_motors_and_pistons(oracle_mod, kind, mode, limits):
+    """Motors on hinges and pistons on sliders (PhysicsEngine.cpp:725-852;
+    Motor / Piston, PersistentConstraint.cpp:5-200, 300-328; MotorConstraint,
+    PistonConstraint, SlideLimitConstraint, ConstraintSolver.cpp:555-775) in
+    constant, target-velocity and target-position modes, with and without
+    limits, switched off and to another mode mid-run: bit-identical to the
+    reference, angles and slide positions included.  (A constant torque
+    driving a hinge past a limit on the side it pushes from makes the
+    reference's target velocity infinite and its state NaN; that case is
+    left out.)"""
+    sc = _powered_scene(kind, mode, limits)
+    r, p = oracle_mod.twin_worlds(sc)
+    ids = r.constraint_ids[1::2]            # hinge / slider, then its motor / piston
+    getter = "motor_position" if kind == "motor" else "piston_position"
+    setter = "set_motor" if kind == "motor" else "set_piston"
+    for s in range(160):
+        if s == 60:
+            for w in (r, p):
+                getattr(w, setter)(ids[0], 0)                       # off
+                getattr(w, setter)(ids[1], 2, 50.0, -0.4)           # target velocity
+        if s == 110:
+            for w in (r, p):
+                getattr(w, setter)(ids[2], 3, 60.0, 0.2)            # target position
+        r.step(1)
+        p.step(1)
+        sr, sp = r.state(), p.state()
+        assert _states_equal(sr, sp), f"state differs at step {s}"
+        pr = [getattr(r, getter)(c) for c in ids]
+        pp = [getattr(p, getter)(c) for c in ids]
+        assert pr == pp, (s, pr, pp)
+    assert np.abs(np.array(pr)).max() > 1e-3     # the joints moved
+
+
+def test_restatement_checkpoint_restore_with_motors_and_pistons(oracle_mod):
+    """Joint state of motors (angle, previous relative velocity) and pistons
+    (slide position, past-limit flag; two slots each) restores exactly."""
+    for sc in (scenes.motor_chain(3, True), scenes.piston_chain(2, True)):
+        a = oracle_mod.port_world()
+        scenes.apply(sc, a)
+        a.step(30)
+        b = oracle_mod.port_world()
+        scenes.apply(sc, b)
+        b.set_state(**a.state())
+        b.set_contacts(a.contacts())
+        b.set_joint_state(a.joint_state())
+        for _ in range(3):
+            a.step(10)
+            b.step(10)
+            sa, sb = a.state(), b.state()
+            for k in sa:
+                assert np.array_equal(sa[k], sb[k]), (sc.name, k)
