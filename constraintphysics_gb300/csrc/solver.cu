@@ -276,10 +276,8 @@ __device__ __forceinline__ void row_warm(const RowBlock& R, const float4 imp, fl
 // that everything but one FMA per friction row runs alongside the normal row
 // instead of after it; the normal row's velocity change is applied while the
 // friction rows are evaluated.  The disc projection compares squared
-// magnitudes and scales by rsqrt.  Δv is written back unconditionally (a zero
-// change writes the same values).
-__device__ __forceinline__ void row_vel(const RowBlock& R, float4& imp, int& stat, float4* dv) {
-    P3 va = dv_get(dv, R.sa, 0), vb = dv_get(dv, R.sb, 0);
+// magnitudes and scales by rsqrt.  `va`, `vb` are the two bodies' Δv.
+__device__ __forceinline__ void row_vel_r(const RowBlock& R, float4& imp, int& stat, P3& va, P3& vb) {
     const float cur = pdot(p3(R.nja), va, p3(R.njb), vb);
     const float b0 = pdot(p3(R.fja0), va, p3(R.fjb0), vb), b1 = pdot(p3(R.fja1), va, p3(R.fjb1), vb);
     // friction impulses for the incoming velocities: imp.zw + Fm^-1 (tgt_f - b)
@@ -306,11 +304,17 @@ __device__ __forceinline__ void row_vel(const RowBlock& R, float4& imp, int& sta
     paxpy(vb, p3(R.fitb0), s0);
     paxpy(va, p3(R.fita1), s1);
     paxpy(vb, p3(R.fitb1), s1);
-    dv_put(dv, R.sa, 0, va);
-    dv_put(dv, R.sb, 0, vb);
     imp.x = ix;
     imp.z = __fadd_rn(imp.z, e.x);
     imp.w = __fadd_rn(imp.w, e.y);
+}
+// the same on the island's Δv array (written back unconditionally: a zero
+// change writes the same values)
+__device__ __forceinline__ void row_vel(const RowBlock& R, float4& imp, int& stat, float4* dv) {
+    P3 va = dv_get(dv, R.sa, 0), vb = dv_get(dv, R.sb, 0);
+    row_vel_r(R, imp, stat, va, vb);
+    dv_put(dv, R.sa, 0, va);
+    dv_put(dv, R.sb, 0, vb);
 }
 
 // pseudo-velocity (position correction) pass of the normal row
@@ -502,6 +506,9 @@ __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t
     // the first velocity pass on); a fence is needed only if none was issued
     // since: about once per pass on a large island, every chunk on a small one.
     int fenced = -1;
+    // body pair whose Δv the velocity passes hold in registers (-1: none)
+    int cur_a = -1, cur_b = -1;
+    P3 ca{}, cb{};
     auto issue = [&](int t, int now) {
         int c = t % nch, slot = t % kRingSlots;
         int n = min(kChunkRows, rc - c * kChunkRows);
@@ -546,15 +553,33 @@ __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t
                 }
             }
         } else if (pass <= n_vel) {
+            // consecutive rows of one body pair (the points of a manifold)
+            // keep the pair's Δv in registers: the array is read when the
+            // pair changes and written back when it changes again (at the
+            // latest at the end of the pass), so the chain skips the
+            // shared-memory round trip between such rows
             const bool last_vel = pass == n_vel;
             for (int j = 0; j < n; j++) {
                 RowBlock R;
                 load(j, R);
+                if (R.sa != cur_a || R.sb != cur_b) {
+                    dv_put(dv, cur_a, 0, ca);
+                    dv_put(dv, cur_b, 0, cb);
+                    cur_a = R.sa;
+                    cur_b = R.sb;
+                    ca = dv_get(dv, cur_a, 0);
+                    cb = dv_get(dv, cur_b, 0);
+                }
                 float4 imp = R.imp;
                 int st = R.stat;
-                row_vel(R, imp, st, dv);
+                row_vel_r(R, imp, st, ca, cb);
                 g[j].imp = imp;
                 if (last_vel) g[j].stat = st;
+            }
+            if (c == nch - 1) {
+                dv_put(dv, cur_a, 0, ca);
+                dv_put(dv, cur_b, 0, cb);
+                cur_a = cur_b = -1;
             }
         } else {
             for (int j = 0; j < n; j++) {

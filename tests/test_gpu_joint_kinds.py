@@ -66,15 +66,15 @@ def _step_both(sc, k, oracle_mod):
 
 
 def _stick_slip_bodies(cg_, cp_):
-    """Bodies with a contact (matched by MagicID) whose static_ready flag
-    differs between the two engines."""
-    key = lambda c, i: (int(c["b1"][i]), int(c["b2"][i]), int(c["magic_c"][i]), int(c["magic_b"][i]))
-    sp = {key(cp_, i): int(cp_["static_ready"][i]) for i in range(len(cp_["b1"]))}
+    """Bodies with a contact that slips (static_ready false: its friction was
+    clamped to the cone in the last pass) in either engine.  Such a contact
+    switches between the static and the kinetic coefficient from substep to
+    substep; FP32 and FP64 can take the switch in different substeps."""
     out = set()
-    for i in range(len(cg_["b1"])):
-        k = key(cg_, i)
-        if k in sp and sp[k] != int(cg_["static_ready"][i]):
-            out.update(k[:2])
+    for c in (cg_, cp_):
+        for i in range(len(c["b1"])):
+            if not int(c["static_ready"][i]):
+                out.update((int(c["b1"][i]), int(c["b2"][i])))
     return out
 
 
@@ -98,10 +98,10 @@ def test_joint_kind_single_step_parity(oracle_mod, name, k):
     wm = np.linalg.norm(sp["ang_vel"], axis=1)
     dx = np.abs(sg["com"] - sp["com"]).max()
     stats = f"dv max {dv.max():.2e} dw max {dw.max():.2e} dx {dx:.2e}"
-    # a contact at the edge of its friction cone (static_ready, the
-    # stick/slip switch between the static and kinetic coefficients, decided
-    # differently in FP32 and FP64) moves its bodies by up to (mu_s - mu_k)
-    # N / m; those bodies get a looser bound
+    # a contact at the edge of its friction cone (the stick/slip switch
+    # between the static and kinetic coefficients, taken in different
+    # substeps in FP32 and FP64) moves its bodies by up to (mu_s - mu_k) N / m;
+    # bodies with a slipping contact get a looser bound
     slip = _stick_slip_bodies(g.contacts(), p.contacts())
     tight = np.array([i + 1 not in slip for i in range(len(dv))])
     # FP32 rows through 4 substeps of 10 velocity sweeps and the block solve
