@@ -7,7 +7,11 @@
 // tree query AABB_Tree.h:153-224 visits every overlapping leaf pair once).
 // Pairs are emitted as (lower id, higher id) sorted by (a, b): one thread per
 // body counts its overlaps with the later bodies of its world, an exclusive
-// scan gives each body its output offset, and a second pass writes.
+// scan gives each body its output offset, and a second pass writes.  Worlds
+// above kTileWorld bodies (where one thread per body would loop over up to
+// the whole world) run the same test over kTile x kTile blocks instead.
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "devmath.cuh"
 #include "shapes.cuh"
@@ -95,6 +99,7 @@ __global__ void k_gravity(Dev d) {
 
 __global__ void k_pairs(Dev d, int write) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
+        if (d.n_tile_tasks > 0 && d.tile_base[d.world[i]] >= 0) continue;   // a large world: k_pairs_tile
         const int end = d.world_start[d.world[i] + 1];
         const float4 lo = d.aabb_lo[i], hi = d.aabb_hi[i];
         if (!write) {
@@ -110,6 +115,65 @@ __global__ void k_pairs(Dev d, int write) {
                 }
             }
         }
+    }
+}
+
+// Large worlds: a block per (i tile, j tile >= i tile) of the world's bodies;
+// the j tile's AABBs are staged in shared memory and each thread tests its
+// body i against them (j > i).  The count pass stores, per body and j tile,
+// the pairs found there; k_pairs_tile_rows turns a body's cells into their
+// prefix and its total; the write pass writes each body's pairs of a tile at
+// its offset plus the tile's prefix, in increasing j -- the same sorted
+// (a, b) list as the per-body loop, with every thread doing kTile tests.
+__global__ void __launch_bounds__(kTile) k_pairs_tile(Dev d, int write) {
+    __shared__ float4 slo[kTile], shi[kTile];
+    for (int q = blockIdx.x; q < d.n_tile_tasks; q += gridDim.x) {
+        const int4 t = d.tile_task[q];
+        const int s = d.world_start[t.x], e = d.world_start[t.x + 1];
+        const int j0 = s + t.z * kTile, jn = min(kTile, e - j0);
+        __syncthreads();   // the previous task's tile is no longer read
+        if ((int)threadIdx.x < jn) {
+            slo[threadIdx.x] = d.aabb_lo[j0 + threadIdx.x];
+            shi[threadIdx.x] = d.aabb_hi[j0 + threadIdx.x];
+        }
+        __syncthreads();
+        const int i = s + t.y * kTile + (int)threadIdx.x;
+        if (i >= e) continue;
+        const float4 lo = d.aabb_lo[i], hi = d.aabb_hi[i];
+        int* cell = d.tile_cnt + d.tile_base[t.x] + (size_t)(i - s) * t.w + t.z;
+        const int first = max(0, i + 1 - j0);   // j > i
+        if (!write) {
+            int c = 0;
+            for (int k = first; k < jn; k++) c += overlap(lo, hi, slo[k], shi[k]);
+            *cell = c;
+        } else {
+            int o = d.pair_count[i] + *cell;
+            for (int k = first; k < jn; k++) {
+                if (overlap(lo, hi, slo[k], shi[k])) {
+                    if (o < d.cap_pairs) { d.pair_a[o] = i; d.pair_b[o] = j0 + k; }
+                    o++;
+                }
+            }
+        }
+    }
+}
+
+// per large-world body: the prefix of its j-tile cells (from its own tile on)
+// and its pair count
+__global__ void k_pairs_tile_rows(Dev d) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n_bodies; i += gridDim.x * blockDim.x) {
+        const int w = d.world[i], base = d.tile_base[w];
+        if (base < 0) continue;
+        const int s = d.world_start[w], e = d.world_start[w + 1];
+        const int T = (e - s + kTile - 1) / kTile;
+        int* row = d.tile_cnt + base + (size_t)(i - s) * T;
+        int acc = 0;
+        for (int jt = (i - s) / kTile; jt < T; jt++) {
+            const int c = row[jt];
+            row[jt] = acc;
+            acc += c;
+        }
+        d.pair_count[i] = acc;
     }
 }
 
@@ -161,9 +225,15 @@ void launch_gravity(const Dev& d, const Launch& L) {
 
 void launch_pairs(const Dev& d, const Launch& L) {
     int g = grid_for(d.n_bodies, 128, L.n_sms);
+    const int gt = std::min(d.n_tile_tasks, L.n_sms * 16);
     k_pairs<<<g, 128, 0, L.st>>>(d, 0);
+    if (d.n_tile_tasks > 0) {
+        k_pairs_tile<<<gt, kTile, 0, L.st>>>(d, 0);
+        k_pairs_tile_rows<<<g, 128, 0, L.st>>>(d);
+    }
     scan_exclusive(d.pair_count, d.pair_count, nullptr, d.n_bodies, d.n_bodies, d.n_pairs, d.scan_tmp, L);
     k_pairs<<<g, 128, 0, L.st>>>(d, 1);
+    if (d.n_tile_tasks > 0) k_pairs_tile<<<gt, kTile, 0, L.st>>>(d, 1);
     k_clamp_pairs<<<1, 1, 0, L.st>>>(d);
 }
 

@@ -571,6 +571,7 @@ struct Batch {
     bool meshes = false;               // the batch holds static triangle meshes
     bool joints = false;               // the batch holds joints (or springs: joint edges)
     bool springs = false;              // the batch holds springs
+    bool tiles = false;                // the batch holds worlds above kTileWorld bodies (tiled pair pass)
     bool systems = false;              // ... and holonomic systems
     cudaStream_t st = nullptr;
     cudaStream_t side = nullptr;       // concurrent branch (small-island PGS)
@@ -635,7 +636,7 @@ struct Batch {
     // (+2 per substep and 1 factorisation with joints)
     int launches_per_step() const {
         return 1 + 6 + 2 + (prims ? 1 : 0) + (meshes ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 5 * substeps + 1 + (joints ? 2 * substeps : 0) +
-               (systems ? 1 : 0) + (audit ? 1 : 0) + (springs ? substeps : 0);
+               (systems ? 1 : 0) + (audit ? 1 : 0) + (springs ? substeps : 0) + (tiles ? 3 : 0);
     }
 
     // solver schedule: chain workers per SM of k_pgs_big (0 = as many as fit)
@@ -940,6 +941,20 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     }
     B->n_bodies = N;
     B->world_start = wstart;
+    // large worlds' pair pass: tasks over (i tile, j tile >= i tile) blocks
+    std::vector<int4> tile_task;
+    std::vector<int> tile_base(worlds.size(), -1);
+    size_t tile_cells = 0;
+    for (size_t k = 0; k < worlds.size(); k++) {
+        const int n = wstart[k + 1] - wstart[k];
+        if (n <= kTileWorld) continue;
+        const int T = (n + kTile - 1) / kTile;
+        tile_base[k] = (int)tile_cells;
+        tile_cells += (size_t)n * T;
+        for (int it = 0; it < T; it++)
+            for (int jt = it; jt < T; jt++) tile_task.push_back(make_int4((int)k, it, jt, T));
+    }
+    B->tiles = !tile_task.empty();
     {
         int max_world = 0;
         for (size_t k = 0; k + 1 < wstart.size(); k++) max_world = std::max(max_world, wstart[k + 1] - wstart[k]);
@@ -1271,6 +1286,16 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
         d_pool = A.take<uint8_t>(pool.size());
         x.shapes = d_pool;
         x.pair_count = A.take<int>(N);
+        x.n_tile_tasks = (int)tile_task.size();
+        x.tile_task = A.take<int4>(tile_task.size());
+        x.tile_base = A.take<int>(worlds.size());
+        x.tile_cnt = A.take<int>(tile_cells);
+        // CPGPU_ISLANDS_SERIAL=1: large worlds take the serial search too (a
+        // test compares the two)
+        if (!tile_task.empty() && !env_int("CPGPU_ISLANDS_SERIAL", 0)) {
+            x.comp = A.take<int>((size_t)kCompArrays * N);
+            x.sys_mark = A.take<int>(std::max<size_t>(hs_degree.size(), 1));
+        }
         x.pair_a = A.take<int>(cap_pairs); x.pair_b = A.take<int>(cap_pairs);
         x.mf_n = A.take<float4>(cap_pairs); x.mf_cnt = A.take<int>(cap_pairs);
         x.mf_pt = A.take<float4>(4 * (size_t)cap_pairs); x.mf_magic = A.take<uint64_t>(4 * (size_t)cap_pairs);
@@ -1395,6 +1420,8 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     up(d_mov, movement.data(), N); up(d_mat, mat.data(), N * sizeof(float4));
     up(d_pool, pool.data(), pool.size());
     up(x.moved, fresh.data(), N * 4);   // the first geometry pass renormalises these orientations
+    up((void*)x.tile_task, tile_task.data(), tile_task.size() * sizeof(int4));
+    up((void*)x.tile_base, tile_base.data(), tile_base.size() * 4);
     if (has_sleep) {
         up(x.asleep, s_asleep.data(), N * 4); up(x.waking, s_waking.data(), N * 4); up(x.ready_cnt, s_ready.data(), N * 4);
         up(x.non_sleepy, s_nons.data(), N * 4); up(x.hist_n, s_hn.data(), N * 4);

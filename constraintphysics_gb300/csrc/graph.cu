@@ -15,7 +15,8 @@
 // (LIFO stack) starts from every unvisited dynamic body in constraint-graph
 // node-map iteration order (supplied by the host) and emits each live contact
 // of each edge to a not-yet-visited neighbour, in per-edge order.  That is the
-// reference's exact row order.
+// reference's exact row order.  Worlds above kTileWorld bodies search their
+// connected components in parallel (islands_big), with the same result.
 #include "kernels.cuh"
 #include "devmath.cuh"
 
@@ -198,6 +199,278 @@ __device__ __forceinline__ long long islands_need(int nb, int ne_w, int nj) {
     return 4LL * (5LL * nb + 4 * E + ne_w + 2 * E + nb) + nb;   // ints, then the body flags (bytes)
 }
 
+// ---- islands of large worlds: one DFS per connected component ----------------
+// The reference's search starts from each unvisited dynamic body in map order
+// and covers that body's component (dynamic bodies joined by edges; fixed and
+// kinematic bodies end it), so each island is the component of its first body
+// in map order, searched from there; its rows depend on nothing outside it.
+// Components are found by a union-find over the adjacency, listed in the map
+// order of their first bodies, searched once to count their rows, bodies and
+// systems, and once more to write them at the prefix of those counts.  The
+// result is the serial search's, position for position.
+
+// exclusive prefix of one value per thread (blockDim.x == 256) with the
+// block's total in *total; `ws` holds 8 ints
+__device__ int block_excl(int v, int* ws, int* total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) { int t = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += t; }
+    if (lane == 31) ws[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int y = lane < 8 ? ws[lane] : 0;
+        for (int o = 1; o < 8; o <<= 1) { int t = __shfl_up_sync(0xffffffffu, y, o); if (lane >= o) y += t; }
+        if (lane < 8) ws[lane] = y;
+    }
+    __syncthreads();
+    const int incl = x + (wid > 0 ? ws[wid - 1] : 0);
+    *total = ws[7];
+    __syncthreads();
+    return incl - v;
+}
+
+__device__ __forceinline__ int uf_root(int* par, int x) {
+    while (true) {
+        const int p = atomicAdd(&par[x], 0);
+        if (p == x) return x;
+        const int g = atomicAdd(&par[p], 0);
+        if (g != p) atomicCAS(&par[x], p, g);   // path halving
+        x = p;
+    }
+}
+__device__ void uf_link(int* par, int a, int b) {
+    while (true) {
+        a = uf_root(par, a);
+        b = uf_root(par, b);
+        if (a == b) return;
+        if (a > b) { const int t = a; a = b; b = t; }
+        if (atomicCAS(&par[b], b, a) == b) return;   // the larger root under the smaller
+    }
+}
+
+struct IslandCtx {
+    int w, s, e0, ready_steps;
+    bool sleep_on, may_sleep, joints;
+    const int *a_ofs, *a_cur, *adj, *live;
+    const uint8_t* mov;
+    int* vis;
+};
+
+// One component's search from `root` (the serial search's loop body).  COUNT:
+// marks its bodies -2 and returns its rows, bodies, systems and whether all of
+// them are ready to sleep; otherwise writes bodies at bc, rows at rc and
+// systems at sc (or, for a component that falls asleep, puts it to sleep).
+template <bool COUNT>
+__device__ void island_search(const Dev& d, const IslandCtx& x, int root, int* stk, int cap, int rc, int bc, int sc,
+                              bool sleeps, int comp_id, int* o_rows, int* o_bodies, int* o_sys, bool* o_ready,
+                              bool* o_joint) {
+    const int rs = rc, bs = bc, ss = sc;
+    int sp = 0, nbod = 0, nsys = 0;
+    bool all_ready = true, has_joint = false;
+    stk[sp++] = root;
+    while (sp > 0) {
+        const int cur = stk[--sp];
+        if (COUNT ? x.vis[cur] == -2 : x.vis[cur] >= 0) continue;
+        if (COUNT) x.vis[cur] = -2;
+        else {
+            x.vis[cur] = bc - bs;
+            if (sleeps) {
+                const int g = cur + x.s;
+                d.asleep[g] = 1;
+                d.vel[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+                d.angv[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                d.isl_bodies[bc] = cur + x.s;
+            }
+            bc++;
+        }
+        nbod++;
+        const int lo = x.a_ofs[cur], hi = x.a_cur[cur];
+        const bool cur_asleep = x.sleep_on && d.asleep[cur + x.s];
+        bool kinematic_contact = false;
+        for (int j = lo; j < hi; j++) {
+            const int o = x.adj[2 * j], k = x.adj[2 * j + 1];
+            if (x.mov[o] == 2) kinematic_contact = true;
+            if (COUNT ? x.vis[o] == -2 : x.vis[o] >= 0) continue;
+            if (cur_asleep && (x.mov[o] == 1 || d.asleep[o + x.s])) {
+                // no rows; the neighbour still joins the island
+            } else if (k < 0) {
+                const int je = -k - 1, sy = d.je.sys[je];
+                if (sy >= 0) {
+                    if (COUNT) {
+                        if (d.sys_mark[sy] != comp_id) { d.sys_mark[sy] = comp_id; nsys++; }
+                    } else if (!sleeps) {
+                        bool seen = false;
+                        for (int q = ss; q < sc; q++) seen |= d.isl_sys[q] == sy;
+                        if (!seen) d.isl_sys[sc++] = sy;
+                    }
+                }
+                for (int q = d.je.jstart[je]; q < d.je.jstart[je] + d.je.jcount[je]; q++) {
+                    const int jj = d.je.jlist[q];
+                    if (jk_conditional(d.jt.kind[jj]) && !d.jt.active[jj]) continue;
+                    if (!COUNT && !sleeps) d.row_contact[rc] = -(jj + 1);
+                    rc++;
+                    has_joint = true;
+                }
+            } else {
+                const int nl = x.live[k];
+                if (nl > 0) {
+                    if (!COUNT && !sleeps) d.edge_row[x.e0 + k] = rc;
+                    rc += nl;
+                }
+            }
+            if (x.mov[o] == 0) {
+                if (sp < cap) stk[sp++] = o;
+                else atomicOr(d.status, ST_STACK_OVERFLOW);
+            }
+        }
+        if (x.may_sleep && (kinematic_contact || d.ready_cnt[cur + x.s] < x.ready_steps)) all_ready = false;
+    }
+    if (COUNT) {
+        *o_rows = rc - rs;
+        *o_bodies = nbod;
+        *o_sys = nsys;
+        *o_ready = all_ready;
+        *o_joint = has_joint;
+    }
+}
+
+// the component-parallel island pass of one large world (all threads of the block)
+__device__ void islands_big(const Dev& d, const IslandCtx& x, int nb, int row0, int sys0, int* ws, int* sh_rows_end) {
+    const int* map_g = d.map_order + x.s;   // map order, global body indices
+    const int tid = threadIdx.x, nt = blockDim.x;
+    int* C = d.comp + (size_t)kCompArrays * x.s;   // this world's scratch: kCompArrays slices of nb
+    int* par = C;                 // union-find parent
+    int* cmin = C + nb;           // per root: first map position of its component
+    int* deg = C + 2 * nb;        // per root: its component's adjacency entries
+    int* list = C + 3 * nb;       // components in map order of their first bodies (root body)
+    int* stk_off = C + 4 * nb;    // per component: its stack slice
+    int* n_rows = C + 5 * nb;
+    int* n_bod = C + 6 * nb;
+    int* n_sys = C + 7 * nb;
+    int* kind = C + 8 * nb;       // 0 none, 1 island, 2 falls asleep
+    int* o_rows = C + 9 * nb;
+    int* o_bod = C + 10 * nb;
+    int* o_sys = C + 11 * nb;
+    __shared__ int sh_tot, sh_ncomp;
+    for (int i = tid; i < nb; i += nt) { par[i] = i; cmin[i] = INT_MAX; deg[i] = 0; }
+    if (x.joints)   // last step's component ids are no marks for this step
+        for (int q = d.hs_world_start[x.w] + tid; q < d.hs_world_start[x.w + 1]; q += nt) d.sys_mark[q] = -1;
+    __syncthreads();
+    for (int i = tid; i < nb; i += nt) {
+        if (x.mov[i] != 0) continue;
+        for (int j = x.a_ofs[i]; j < x.a_cur[i]; j++) {
+            const int o = x.adj[2 * j];
+            if (x.mov[o] == 0 && o > i) uf_link(par, i, o);
+        }
+    }
+    __syncthreads();
+    for (int t = tid; t < nb; t += nt) {
+        const int node = map_g[t] - x.s;
+        if (x.mov[node] != 0) continue;
+        const int r = uf_root(par, node);
+        atomicMin(&cmin[r], t);
+        atomicAdd(&deg[r], x.a_cur[node] - x.a_ofs[node]);
+    }
+    __syncthreads();
+    // the components' roots listed in map order of their first bodies
+    if (tid == 0) sh_ncomp = 0;
+    __syncthreads();
+    for (int base = 0; base < nb; base += nt) {
+        const int t = base + tid;
+        int node = -1, flag = 0;
+        if (t < nb) {
+            node = map_g[t] - x.s;
+            flag = x.mov[node] == 0 && cmin[uf_root(par, node)] == t;
+        }
+        int tot;
+        const int pos = block_excl(flag, ws, &tot);
+        const int k0 = sh_ncomp;
+        if (flag) list[k0 + pos] = node;
+        __syncthreads();
+        if (tid == 0) sh_ncomp = k0 + tot;
+        __syncthreads();
+    }
+    const int K = sh_ncomp;
+    // stack slices: a component pushes at most its adjacency entries plus its root
+    if (tid == 0) sh_tot = 0;
+    __syncthreads();
+    for (int base = 0; base < K; base += nt) {
+        const int k = base + tid;
+        const int v = k < K ? deg[uf_root(par, list[k])] + 1 : 0;
+        int tot;
+        const int pos = block_excl(v, ws, &tot);
+        const int c0 = sh_tot;
+        if (k < K) stk_off[k] = c0 + pos;
+        __syncthreads();
+        if (tid == 0) sh_tot = c0 + tot;
+        __syncthreads();
+    }
+    int* stack_base = d.stack + 2 * (x.e0 + (x.joints ? d.je.world_start[x.w] : 0)) + x.s;
+    // count
+    for (int k = tid; k < K; k += nt) {
+        int r, b, sy;
+        bool ready, joint;
+        const int cap = deg[uf_root(par, list[k])] + 1;
+        island_search<true>(d, x, list[k], stack_base + stk_off[k], cap, 0, 0, 0, false, x.s + k, &r, &b, &sy, &ready, &joint);
+        const bool sleeps = x.may_sleep && ready;
+        kind[k] = sleeps ? 2 : (r > 0 ? 1 : 0);
+        n_rows[k] = kind[k] == 1 ? r : 0;
+        n_bod[k] = kind[k] == 1 ? b : 0;
+        n_sys[k] = kind[k] == 1 ? sy : 0;
+        o_sys[k] = joint ? 1 : 0;   // island flags until the prefix below
+    }
+    __syncthreads();
+    // prefixes in component order: rows, bodies, systems, island index
+    __shared__ int c_rows, c_bod, c_sys, c_isl;
+    if (tid == 0) { c_rows = row0; c_bod = x.s; c_sys = sys0; c_isl = 0; }
+    __syncthreads();
+    for (int base = 0; base < K; base += nt) {
+        const int k = base + tid;
+        const bool in = k < K;
+        int t1, t2, t3, t4;
+        const int pr = block_excl(in ? n_rows[k] : 0, ws, &t1);
+        const int pb = block_excl(in ? n_bod[k] : 0, ws, &t2);
+        const int psy = block_excl(in ? n_sys[k] : 0, ws, &t3);
+        const int pi = block_excl(in && kind[k] == 1 ? 1 : 0, ws, &t4);
+        if (in) {
+            const int flag = o_sys[k];
+            o_rows[k] = c_rows + pr;
+            o_bod[k] = c_bod + pb;
+            o_sys[k] = c_sys + psy;
+            if (kind[k] == 1) {
+                const int ii = x.s + c_isl + pi;
+                d.isl_row_start[ii] = c_rows + pr;
+                d.isl_row_count[ii] = n_rows[k];
+                d.isl_body_start[ii] = c_bod + pb;
+                d.isl_body_count[ii] = n_bod[k];
+                d.isl_world[ii] = x.w;
+                if (x.joints) {
+                    d.isl_flags[ii] = flag;
+                    d.isl_sys_start[ii] = c_sys + psy;
+                    d.isl_sys_count[ii] = n_sys[k];
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0) { c_rows += t1; c_bod += t2; c_sys += t3; c_isl += t4; }
+        __syncthreads();
+    }
+    // write (the count marked the searched bodies -2, which the write pass
+    // treats as not visited)
+    for (int k = tid; k < K; k += nt) {
+        if (kind[k] == 0) continue;
+        const int cap = deg[uf_root(par, list[k])] + 1;
+        island_search<false>(d, x, list[k], stack_base + stk_off[k], cap, o_rows[k], o_bod[k], o_sys[k], kind[k] == 2, 0,
+                             nullptr, nullptr, nullptr, nullptr, nullptr);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        d.isl_count_w[x.w] = c_isl;
+        *sh_rows_end = c_rows;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
     extern __shared__ int sm_isl[];
     __shared__ int sh_carry, sh_rows_end;
@@ -316,7 +589,15 @@ __global__ void __launch_bounds__(256) k_islands(Dev d, int smem_bytes) {
         }
     }
     __syncthreads();
-    if (tid == 0) {
+    if (d.comp != nullptr && nb > kTileWorld) {
+        IslandCtx x;
+        x.w = w; x.s = s; x.e0 = e0; x.ready_steps = d.wparams[w].ready_steps;
+        x.sleep_on = d.has_sleep != 0;
+        x.may_sleep = x.sleep_on && d.wparams[w].sleeping;
+        x.joints = joints;
+        x.a_ofs = a_ofs; x.a_cur = a_cur; x.adj = adj; x.live = live; x.mov = mov; x.vis = vis;
+        islands_big(d, x, nb, c0 + jj0, sys0, warp_sums, &sh_rows_end);
+    } else if (tid == 0) {
         // sleeping (sleepOrSolveIslands, PhysicsEngine.cpp:1536-1613): a
         // sleeping body's edges to sleeping or fixed bodies carry no rows, and
         // an island whose bodies are all ready to sleep (and touch no

@@ -301,6 +301,9 @@ struct HoloStore {
 };
 
 constexpr int kSchedInts = 1024;
+constexpr int kTile = 128;         // bodies per tile of the large-world pair pass
+constexpr int kTileWorld = 2048;   // worlds above this many bodies take the tiled pair pass and component-parallel islands
+constexpr int kCompArrays = 12;
 
 struct Batch;  // host object, engine.cu
 
@@ -326,6 +329,16 @@ struct Dev {
     int* pair_count;               // per body, then exclusive scan
     int* pair_a; int* pair_b;
     int* n_pairs;
+    // worlds of more than kTileWorld bodies: their pairs come from tasks over
+    // kTile x kTile blocks of the world's (i, j > i) pairs
+    int n_tile_tasks;
+    const int4* tile_task;         // x world, y i tile, z j tile (>= y), w the world's tile count
+    const int* tile_base;          // per world: offset of its (body, j tile) cells in tile_cnt, -1 small world
+    int* tile_cnt;                 // per big-world body and j tile: its pairs there, then their prefix
+    // islands of worlds above kTileWorld bodies: one DFS per connected
+    // component, the components in parallel (kCompArrays ints per body)
+    int* comp;
+    int* sys_mark;                 // per holonomic system: the component that counted it
     // narrowphase output per pair
     float4* mf_n;                  // normal xyz, w max_pen (<= 0: no manifold)
     int* mf_cnt;

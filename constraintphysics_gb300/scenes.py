@@ -716,6 +716,33 @@ def piston_chain(mode=2, limits=True):
     return sc
 
 
+def large_mixed_world(seed=0, n_stacks=600, n_chains=40):
+    """One world of ~2,400 bodies: stacks of three boxes, ball-socket chains of
+    eight boxes hung from fixed posts and spheres dropped between them, all
+    apart from each other (many islands), with sleeping enabled."""
+    M = PILE_MATERIAL
+    sc = Scene(f"large_mixed_{seed}", dict(step_time=1.0 / 60.0, substeps=2, pgs=(10, 1, 1), sleeping=True))
+    rng = np.random.default_rng(seed)
+    sc.box((-200.0, -1.0, -200.0), 400.0, 1.0, 400.0, M, FIXED)
+    side = int(np.ceil(np.sqrt(n_stacks + n_chains)))
+    cells = [(3.0 * (k % side) - 1.5 * side, 3.0 * (k // side) - 1.5 * side) for k in range(n_stacks + n_chains)]
+    rng.shuffle(cells)
+    for k in range(n_stacks):
+        x, z = cells[k]
+        for j in range(3):
+            sc.box((-0.5, -0.5, -0.5), 1.0, 1.0, 1.0, M, DYNAMIC, (x, 0.6 + 1.05 * j, z + 0.1 * rng.uniform()))
+        if k % 3 == 0:
+            sc.sphere((0, 0, 0), 0.3, M, DYNAMIC, (x + 1.2, 0.5 + 2.0 * rng.uniform(), z))
+    for k in range(n_chains):
+        x, z = cells[n_stacks + k]
+        prev = sc.box((-0.2, -0.2, -0.2), 0.4, 0.4, 0.4, M, FIXED, (x, 9.0, z))
+        for i in range(8):
+            b = sc.box((-0.2, -0.2, -0.2), 0.4, 0.4, 0.4, M, DYNAMIC, (x + 0.5 * (i + 1), 9.0, z))
+            sc.ball_socket(prev, b, (0.25, 0, 0), (-0.25, 0, 0))
+            prev = b
+    return sc
+
+
 def spring_chain(with_joints=False):
     """Boxes hung from a fixed post on damped springs (two sharing a body, one
     at its creation length), bouncing on the ground and off each other, or

@@ -308,3 +308,31 @@ def test_default_partition_of_large_worlds_equals_single(monkeypatch):
         st, bs = w.state(), b.state(i)
         for k in ("com", "quat", "vel", "ang_vel"):
             assert np.array_equal(bs[k], st[k]), (i, k)
+
+
+def test_large_world_pair_set_is_the_brute_force_set():
+    """A world above the tiled pair pass's size (3,001 bodies: spheres and
+    boxes scattered so that many AABBs overlap, and a plate under them): the
+    pair list is exactly the sorted set of overlapping AABB pairs
+    of the device's own AABBs, as in small worlds."""
+    rng = np.random.default_rng(11)
+    sc = scenes.Scene("scatter_3001", dict(step_time=1.0 / 60.0, sleeping=False, gravity=(0.0, 0.0, 0.0)))
+    sc.box((-30.0, -1.0, -30.0), 60.0, 1.0, 60.0, scenes.PILE_MATERIAL, scenes.FIXED)
+    for k in range(3000):
+        pos = tuple(rng.uniform(-25.0, 25.0, 3) * np.array([1.0, 0.2, 1.0]) + np.array([0.0, 5.0, 0.0]))
+        if k % 3:
+            sc.sphere((0, 0, 0), float(rng.uniform(0.2, 0.6)), scenes.PILE_MATERIAL, scenes.DYNAMIC, pos)
+        else:
+            sc.box((-0.4, -0.4, -0.4), 0.8, 0.8, 0.8, scenes.PILE_MATERIAL, scenes.DYNAMIC, pos)
+    w = cg.world()
+    scenes.apply(sc, w)
+    w.step(1)
+    aabb = w.aabbs()
+    w.step(1)
+    lo, hi = aabb[:, :3], aabb[:, 3:]
+    ov = ~((hi[:, None, :] < lo[None, :, :]) | (lo[:, None, :] > hi[None, :, :])).any(axis=2)
+    i, j = np.nonzero(np.triu(ov, 1))
+    want = np.stack([i + 1, j + 1], 1).astype(np.uint32)
+    got = w.pairs()
+    assert len(want) > 100
+    assert np.array_equal(got, want)
