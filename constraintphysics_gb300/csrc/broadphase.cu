@@ -179,7 +179,7 @@ __global__ void k_pairs_tile_rows(Dev d) {
 
 __global__ void k_clamp_pairs(Dev d) {
     if (*d.n_pairs > d.cap_pairs) { atomicOr(d.status, ST_PAIR_OVERFLOW); *d.n_pairs = d.cap_pairs; }
-    if (d.has_mesh) *d.mm_count = 0;   // mesh store of this step's narrowphase
+    if (d.has_mesh || d.has_union) *d.mm_count = 0;   // mesh store of this step's narrowphase
 }
 
 // RigidBody::updateGeometry (RigidBody.cpp:281-312) for moved bodies: the
@@ -198,7 +198,24 @@ __global__ void k_geometry(Dev d, int mode) {
         M33 R = quatRot(q);
         f3 c = mk(d.pos[i]);
         f3 mn, mx;
-        shape_aabb(d.shapes + d.shape[i], c, R, &mn, &mx);
+        if (d.has_union && d.prim_start[i] >= 0) {
+            // each primitive's AABB, the body's their combination in order
+            // (ConvexUnionGeometry, RigidBody.cpp:286-294; AABB::combine)
+            const int q0 = d.prim_start[i], nq = d.prim_count[i];
+            for (int q = q0; q < q0 + nq; q++) {
+                f3 pl, ph;
+                shape_aabb(d.shapes + d.prim_shape[q], c, R, &pl, &ph);
+                d.prim_lo[q] = make_float4(pl.x, pl.y, pl.z, 0.f);
+                d.prim_hi[q] = make_float4(ph.x, ph.y, ph.z, 0.f);
+                if (q == q0) { mn = pl; mx = ph; }
+                else {
+                    mn = mk(fminf(mn.x, pl.x), fminf(mn.y, pl.y), fminf(mn.z, pl.z));
+                    mx = mk(fmaxf(mx.x, ph.x), fmaxf(mx.y, ph.y), fmaxf(mx.z, ph.z));
+                }
+            }
+        } else {
+            shape_aabb(d.shapes + d.shape[i], c, R, &mn, &mx);
+        }
         d.aabb_lo[i] = make_float4(mn.x, mn.y, mn.z, 0.f);
         d.aabb_hi[i] = make_float4(mx.x, mx.y, mx.z, 0.f);
     }

@@ -97,6 +97,10 @@ struct Body {
     // hist holds hist_n (velocity, angular velocity) records, oldest first
     int asleep = 0, waking = 0, ready_cnt = 0, non_sleepy = 0, hist_n = 0;
     std::vector<float> hist;
+    // a body of several primitives (ConvexUnionGeometry): their shapes, in
+    // order, and materials (restitution, kinetic, static); empty for a body of one
+    std::vector<int> prims;
+    std::vector<std::array<double, 3>> prim_mat;
     // pose given through the API since the last read-back from a device: its
     // orientation is renormalised on upload (a read-back pose was normalised
     // by the step that produced it, and normalising it again could change
@@ -569,6 +573,7 @@ struct Batch {
     int slot_bytes = 0;
     bool prims = false;                // the batch holds spheres or cylinders
     bool meshes = false;               // the batch holds static triangle meshes
+    bool unions = false;               // the batch holds bodies of several primitives
     bool joints = false;               // the batch holds joints (or springs: joint edges)
     bool springs = false;              // the batch holds springs
     bool tiles = false;                // the batch holds worlds above kTileWorld bodies (tiled pair pass)
@@ -635,7 +640,7 @@ struct Batch {
     // schedule 3, 5 per substep (rows, small + grouped + large PGS, integrate), geometry 1
     // (+2 per substep and 1 factorisation with joints)
     int launches_per_step() const {
-        return 1 + 6 + 2 + (prims ? 1 : 0) + (meshes ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 5 * substeps + 1 + (joints ? 2 * substeps : 0) +
+        return 1 + 6 + 2 + (prims ? 1 : 0) + ((meshes || unions) ? 1 : 0) + (6 + 9) + (2 + 3) + 3 + 5 * substeps + 1 + (joints ? 2 * substeps : 0) +
                (systems ? 1 : 0) + (audit ? 1 : 0) + (springs ? substeps : 0) + (tiles ? 3 : 0);
     }
 
@@ -903,17 +908,26 @@ static bool is_mesh(const World& w, uint32_t id) {
 }
 
 // The cID of a contact's MagicID (CollisionDetect.cpp: the primitives' ids,
-// first body low): body ids for convex pairs; for a mesh pair the convex body's
-// id and the triangle id, which is the only part the device keeps.
+// first body low): a primitive's id is its body's id for a body of one, and
+// (body id << 8 | index) for the primitives of a body of several (the ids are
+// process-global counters in the reference; only their equality matters);
+// for a mesh pair the mesh's half is the triangle id.  The device keeps the
+// part of a contact's cID that the pair does not fix in the contact's
+// triangle field: the triangle id (| the convex body's primitive << 24), or
+// (primitive of body 1 << 8 | of body 2) for a pair with a body of several.
+static bool is_union_body(const World& w, uint32_t id) { return w.bodies[id - 1].prims.size() > 1; }
+static uint32_t prim_id(const World& w, uint32_t id, int k) { return is_union_body(w, id) ? ((id << 8) | (uint32_t)k) : id; }
 static uint64_t contact_cid(const World& w, uint32_t b1, uint32_t b2, int tri) {
-    if (is_mesh(w, b1)) return (uint32_t)tri | ((uint64_t)b2 << 32);
-    if (is_mesh(w, b2)) return b1 | ((uint64_t)(uint32_t)tri << 32);
-    return ((uint64_t)b2 << 32) | b1;
+    if (is_mesh(w, b1)) return (uint32_t)(tri & 0xffffff) | ((uint64_t)prim_id(w, b2, (tri >> 24) & 0xff) << 32);
+    if (is_mesh(w, b2)) return prim_id(w, b1, (tri >> 24) & 0xff) | ((uint64_t)(uint32_t)(tri & 0xffffff) << 32);
+    return ((uint64_t)prim_id(w, b2, tri & 0xff) << 32) | prim_id(w, b1, (tri >> 8) & 0xff);
 }
 static int contact_tri(const World& w, uint32_t b1, uint32_t b2, uint64_t cid) {
-    if (is_mesh(w, b1)) return (int)(uint32_t)(cid & 0xffffffffu);
-    if (is_mesh(w, b2)) return (int)(uint32_t)(cid >> 32);
-    return 0;
+    if (is_mesh(w, b1)) return (int)(uint32_t)(cid & 0xffffff) | (is_union_body(w, b2) ? (int)(((cid >> 32) & 0xff) << 24) : 0);
+    if (is_mesh(w, b2)) return (int)(uint32_t)((cid >> 32) & 0xffffff) | (is_union_body(w, b1) ? (int)((cid & 0xff) << 24) : 0);
+    const int i = is_union_body(w, b1) ? (int)(cid & 0xff) : 0;
+    const int j = is_union_body(w, b2) ? (int)((cid >> 32) & 0xff) : 0;
+    return (i << 8) | j;
 }
 
 static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int pgs_per_sm = 0) {
@@ -985,6 +999,8 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     std::vector<int> world_of(N), map_order(N);
     std::vector<uint8_t> movement(N);
     std::vector<int> fresh(N, 1);
+    std::vector<int> prim_start(N, -1), prim_count(N, 1), prim_shape;
+    std::vector<float4> prim_mat;
     std::vector<WorldParams> wp(worlds.size());
     int max_hot = 16;
     for (size_t wi = 0; wi < worlds.size(); wi++) {
@@ -1012,6 +1028,15 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
             const Body& b = w.bodies[i];
             int g = base + (int)i;
             shape_off[g] = shape_pool_off[b.shape];
+            if (b.prims.size() > 1) {
+                B->unions = true;
+                prim_start[g] = (int)prim_shape.size();
+                prim_count[g] = (int)b.prims.size();
+                for (size_t k = 0; k < b.prims.size(); k++) {
+                    prim_shape.push_back(shape_pool_off[b.prims[k]]);
+                    prim_mat.push_back(make_float4((float)b.prim_mat[k][0], (float)b.prim_mat[k][1], (float)b.prim_mat[k][2], 0.f));
+                }
+            }
             bool dyn = b.movement == CPGPU_DYNAMIC;
             pos[g] = make_float4((float)b.com.x, (float)b.com.y, (float)b.com.z, dyn ? (float)(1.0 / b.mass) : 0.f);
             rot[g] = make_float4((float)b.q.r, (float)b.q.i, (float)b.q.j, (float)b.q.k);
@@ -1242,8 +1267,9 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     const int cap_pairs = std::max(floor_, env_int("CPGPU_PAIRS_PER_BODY", 24) * N);
     const int cap_edges = cap_pairs;
     const int cap_contacts = std::max(std::max(2 * floor_, 2 * (int)cmag.size()), env_int("CPGPU_CONTACTS_PER_BODY", 24) * N);
-    const int cap_mesh = B->meshes ? std::max(4096, env_int("CPGPU_MESH_POINTS_PER_BODY", 32) * N) : 0;
-    const int mesh_warps = B->meshes ? mesh_scratch_warps(B->n_sms) : 0;
+    const bool mstore = B->meshes || B->unions;   // pairs through the mesh store
+    const int cap_mesh = mstore ? std::max(4096, env_int("CPGPU_MESH_POINTS_PER_BODY", 32) * N) : 0;
+    const int mesh_warps = mstore ? mesh_scratch_warps(B->n_sms) : 0;
     const int scan_tmp = std::max(cap_pairs, cap_contacts) / 1024 + 64;
     Dev x;
     EdgeStore es[2];
@@ -1335,8 +1361,8 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
         x.sched = A.take<int>(kSchedInts);
         x.status = counts + 6;
         x.cnt = counts + 16;
-        if (B->meshes) {
-            x.has_mesh = 1;
+        if (mstore) {
+            x.has_mesh = B->meshes ? 1 : 0;
             x.cap_mesh_pts = cap_mesh;
             x.mesh_warps = mesh_warps;
             x.mf_ofs = A.take<int>(cap_pairs);
@@ -1344,6 +1370,15 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
             x.mm_magic = A.take<uint64_t>(cap_mesh); x.mm_tri = A.take<int>(cap_mesh);
             x.mm_count = counts + 8;
             x.msc = A.take<MeshScratch>(mesh_warps);
+        }
+        if (B->unions) {
+            x.has_union = 1;
+            x.prim_start = A.take<int>(N);
+            x.prim_count = A.take<int>(N);
+            x.prim_shape = A.take<int>(prim_shape.size());
+            x.prim_mat = A.take<float4>(prim_mat.size());
+            x.prim_lo = A.take<float4>(prim_shape.size());
+            x.prim_hi = A.take<float4>(prim_shape.size());
         }
         x.n_joints = n_joints;
         x.n_joint_edges = n_je;
@@ -1421,6 +1456,11 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     up(d_pool, pool.data(), pool.size());
     up(x.moved, fresh.data(), N * 4);   // the first geometry pass renormalises these orientations
     up((void*)x.tile_task, tile_task.data(), tile_task.size() * sizeof(int4));
+    if (B->unions) {
+        up((void*)x.prim_start, prim_start.data(), N * 4); up((void*)x.prim_count, prim_count.data(), N * 4);
+        up((void*)x.prim_shape, prim_shape.data(), prim_shape.size() * 4);
+        up((void*)x.prim_mat, prim_mat.data(), prim_mat.size() * 16);
+    }
     up((void*)x.tile_base, tile_base.data(), tile_base.size() * 4);
     if (has_sleep) {
         up(x.asleep, s_asleep.data(), N * 4); up(x.waking, s_waking.data(), N * 4); up(x.ready_cnt, s_ready.data(), N * 4);
@@ -2103,23 +2143,127 @@ int cpgpu_body_capsule(cpgpu_world* w, const double bot[3], double radius, doubl
         return CPGPU_OK;
     });
 }
-// createRigidBody(ConvexUnionGeometry) of one primitive: the single-primitive
-// calls; several primitives per body are not on the device path
+// recenterTensor (RigidBody.cpp:406-425): the parallel-axis shift of an
+// inertia tensor from one reference point to another
+static void recenter_tensor(double m, const double* t, D3 new_c, D3 old_origin, D3 true_com, double* o) {
+    for (int k = 0; k < 9; k++) o[k] = t[k];
+    const D3 d = new_c - old_origin, c = true_com - old_origin;
+    o[0] += m * (d.y * d.y + d.z * d.z - 2 * d.y * c.y - 2 * d.z * c.z);
+    o[1] += m * (d.x * c.y + d.y * c.x - d.x * d.y);
+    o[2] += m * (d.x * c.z + d.z * c.x - d.x * d.z);
+    o[4] += m * (d.x * d.x + d.z * d.z - 2 * d.x * c.x - 2 * d.z * c.z);
+    o[5] += m * (d.y * c.z + d.z * c.y - d.y * d.z);
+    o[8] += m * (d.x * d.x + d.y * d.y - 2 * d.x * c.x - 2 * d.y * c.y);
+    o[3] = o[1];
+    o[6] = o[2];
+    o[7] = o[5];
+}
+
+// createRigidBody(ConvexUnionGeometry) (Geometry.cpp:540-550, RigidBody.cpp:
+// 13-39, 427-640): one primitive is the single-primitive calls; several make
+// a body whose mass, centre of mass and tensor are summed over the
+// primitives in order (each primitive's tensor moved to the origin, the sum
+// to the common centre of mass), each primitive packed about that centre
+// with its own material
 int cpgpu_body_union(cpgpu_world* w, const cpgpu_primitive* prims, int n, int movement, const double pos[3],
                      uint32_t* out_id) {
     W_OR_FAIL(w);
     if (!prims || n < 1) return fail(CPGPU_ERR_INVALID_ARG, "a union needs >= 1 primitive");
-    if (n > 1) return fail(CPGPU_ERR_UNSUPPORTED, "multi-primitive bodies are not implemented on the device path");
-    const cpgpu_primitive& q = prims[0];
-    switch (q.kind) {
-    case CPGPU_PRIM_HULL:
-        return cpgpu_body_hull(w, q.points, q.n_points, q.face_offsets, q.face_indices, q.n_faces, &q.mat, movement, pos, out_id);
-    case CPGPU_PRIM_BOX: return cpgpu_body_box(w, q.p, q.a, q.b, q.c, &q.mat, movement, pos, out_id);
-    case CPGPU_PRIM_SPHERE: return cpgpu_body_sphere(w, q.p, q.a, &q.mat, movement, pos, out_id);
-    case CPGPU_PRIM_CYLINDER: return cpgpu_body_cylinder(w, q.p, q.a, q.b, &q.mat, movement, pos, out_id);
-    case CPGPU_PRIM_CAPSULE: return cpgpu_body_capsule(w, q.p, q.a, q.b, &q.mat, movement, pos, out_id);
-    default: return fail(CPGPU_ERR_INVALID_ARG, "bad primitive kind");
+    if (n == 1) {
+        const cpgpu_primitive& q = prims[0];
+        switch (q.kind) {
+        case CPGPU_PRIM_HULL:
+            return cpgpu_body_hull(w, q.points, q.n_points, q.face_offsets, q.face_indices, q.n_faces, &q.mat, movement, pos, out_id);
+        case CPGPU_PRIM_BOX: return cpgpu_body_box(w, q.p, q.a, q.b, q.c, &q.mat, movement, pos, out_id);
+        case CPGPU_PRIM_SPHERE: return cpgpu_body_sphere(w, q.p, q.a, &q.mat, movement, pos, out_id);
+        case CPGPU_PRIM_CYLINDER: return cpgpu_body_cylinder(w, q.p, q.a, q.b, &q.mat, movement, pos, out_id);
+        case CPGPU_PRIM_CAPSULE: return cpgpu_body_capsule(w, q.p, q.a, q.b, &q.mat, movement, pos, out_id);
+        default: return fail(CPGPU_ERR_INVALID_ARG, "bad primitive kind");
+        }
     }
+    return guarded([&] {
+        if (n > 255) throw ApiFail{CPGPU_ERR_INVALID_ARG, "a union holds at most 255 primitives"};
+        if (movement < 0 || movement > 2) throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad movement type"};
+        struct Part { uint32_t kind; HullPrep h; D3 center; double r = 0, hh = 0, m = 0; D3 c; double t[9]; };
+        std::vector<Part> parts(n);
+        double msum = 0, tsum[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        D3 csum;
+        for (int i = 0; i < n; i++) {
+            const cpgpu_primitive& q = prims[i];
+            Part& P = parts[i];
+            const double density = q.mat.density;
+            if (q.kind == CPGPU_PRIM_HULL || q.kind == CPGPU_PRIM_BOX) {
+                std::vector<D3> pts;
+                std::vector<std::vector<int>> faces;
+                if (q.kind == CPGPU_PRIM_BOX) {
+                    // ConvexUnionGeometry::box (Geometry.cpp:14-37)
+                    const D3 p(q.p[0], q.p[1], q.p[2]);
+                    const double dx = q.a, dy = q.b, dz = q.c;
+                    pts = {D3(p.x, p.y, p.z), D3(p.x + dx, p.y, p.z), D3(p.x + dx, p.y + dy, p.z), D3(p.x, p.y + dy, p.z),
+                           D3(p.x, p.y, p.z + dz), D3(p.x + dx, p.y, p.z + dz), D3(p.x + dx, p.y + dy, p.z + dz), D3(p.x, p.y + dy, p.z + dz)};
+                    faces = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+                } else {
+                    if (!q.points || !q.face_offsets || !q.face_indices || q.n_points < 4 || q.n_faces < 4)
+                        throw ApiFail{CPGPU_ERR_INVALID_ARG, "hull needs >= 4 points and faces"};
+                    for (int k = 0; k < q.n_points; k++) pts.push_back(D3(q.points[3 * k], q.points[3 * k + 1], q.points[3 * k + 2]));
+                    faces.resize(q.n_faces);
+                    for (int f = 0; f < q.n_faces; f++)
+                        for (int k = q.face_offsets[f]; k < q.face_offsets[f + 1]; k++) faces[f].push_back(q.face_indices[k]);
+                }
+                if (!P.h.build(pts, faces)) throw ApiFail{CPGPU_ERR_INVALID_ARG, "invalid hull"};
+                P.kind = SHAPE_HULL;
+                double t[3][3];
+                hullMassProperties(P.h, density, &P.c, t, &P.m);
+                for (int a = 0; a < 3; a++) for (int b = 0; b < 3; b++) P.t[3 * a + b] = t[a][b];
+            } else {
+                P.r = q.a;
+                if (q.kind == CPGPU_PRIM_SPHERE) { P.kind = SHAPE_SPHERE; P.center = D3(q.p[0], q.p[1], q.p[2]); }
+                else if (q.kind == CPGPU_PRIM_CYLINDER) { P.kind = SHAPE_CYLINDER; P.hh = q.b; P.center = D3(q.p[0], q.p[1] + q.b / 2.0, q.p[2]); }
+                else if (q.kind == CPGPU_PRIM_CAPSULE) { P.kind = SHAPE_CAPSULE; P.hh = q.b; P.center = D3(q.p[0], q.p[1] + q.b / 2.0, q.p[2]); }
+                else throw ApiFail{CPGPU_ERR_INVALID_ARG, "bad primitive kind"};
+                if (!(P.r > 0) || (P.kind == SHAPE_CYLINDER && !(P.hh > 0)) || (P.kind == SHAPE_CAPSULE && !(P.hh >= 0)))
+                    throw ApiFail{CPGPU_ERR_INVALID_ARG, "radius must be > 0, cylinder height > 0, capsule drum height >= 0"};
+                prim_mass(P.kind, P.center, P.r, P.hh, density, &P.m, P.t);
+                P.c = P.center;
+            }
+            double t0[9];
+            recenter_tensor(P.m, P.t, D3(), P.c, P.c, t0);
+            for (int k = 0; k < 9; k++) tsum[k] = tsum[k] + t0[k];
+            csum = csum + P.c * P.m;
+            msum = msum + P.m;
+        }
+        const D3 com = csum / msum;
+        Body b;
+        b.mass = msum;
+        recenter_tensor(msum, tsum, com, D3(), com, b.iref);
+        inv3(b.iref, b.iinv_ref);
+        std::memcpy(b.iw, b.iref, sizeof(b.iw));
+        std::memcpy(b.iinv, b.iinv_ref, sizeof(b.iinv));
+        b.com = com;
+        b.local_origin = -b.com;
+        D3 p = pos ? D3(pos[0], pos[1], pos[2]) : D3();
+        D3 tracked = b.com + qrot(b.q, b.local_origin);
+        b.com = b.com + (p - tracked);
+        b.movement = movement;
+        b.rest = prims[0].mat.restitution; b.kin = prims[0].mat.kinetic_friction; b.sta = prims[0].mat.static_friction;
+        begin_mutation(w->w);
+        for (int i = 0; i < n; i++) {
+            const Part& P = parts[i];
+            Shape sh = P.kind == SHAPE_HULL ? pack_hull(P.h, com)
+                       : P.kind == SHAPE_SPHERE ? pack_sphere(P.center - com, P.r)
+                       : P.kind == SHAPE_CAPSULE ? pack_capsule(P.center - com, P.r, P.hh)
+                                                 : pack_cylinder(P.center - com, P.r, P.hh);
+            b.prims.push_back((int)w->w.shapes.size());
+            w->w.shapes.push_back(std::move(sh));
+            b.prim_mat.push_back({prims[i].mat.restitution, prims[i].mat.kinetic_friction, prims[i].mat.static_friction});
+        }
+        b.shape = b.prims[0];
+        w->w.bodies.push_back(b);
+        uint32_t id = (uint32_t)w->w.bodies.size();
+        w->w.nodes[id] = (int)id - 1;
+        if (out_id) *out_id = id;
+        return CPGPU_OK;
+    });
 }
 // createRigidBody(StaticMeshGeometry(MeshInput{tris, points}), fixed)
 // (PhysicsEngine.cpp:498-512, RigidBody.cpp:41-58): a fixed body at the

@@ -128,7 +128,7 @@ __global__ void k_contacts(Dev d, int write) {
         }
         // a mesh pair's points (each with its merged manifold's normal) are in
         // the mesh store; the MagicID's cID then carries the triangle id
-        const int mofs = (p >= 0 && d.has_mesh) ? d.mf_ofs[p] : -1;
+        const int mofs = (p >= 0 && (d.has_mesh || d.has_union)) ? d.mf_ofs[p] : -1;
         int np = (p >= 0) ? d.mf_cnt[p] : 0;
         for (int k = 0; k < np; k++) {
             uint64_t m = mofs >= 0 ? d.mm_magic[mofs + k] : d.mf_magic[4 * p + k];
@@ -150,7 +150,24 @@ __global__ void k_contacts(Dev d, int write) {
         float4 m1 = d.material[b1], m2 = d.material[b2];
         float rest = fmaxf(m1.x, m2.x), kin = (m1.y + m2.y) / 2.0f, sta = (m1.z + m2.z) / 2.0f;
         const WorldParams& wp = d.wparams[d.world[b1]];
+        const bool u1 = d.has_union && d.prim_start[b1] >= 0, u2 = d.has_union && d.prim_start[b2] >= 0;
+        const bool with_mesh = reinterpret_cast<const HullHeader*>(d.shapes + d.shape[b1])->kind == SHAPE_MESH ||
+                               reinterpret_cast<const HullHeader*>(d.shapes + d.shape[b2])->kind == SHAPE_MESH;
         for (int j = 0; j < n; j++) {
+            if (u1 || u2) {
+                // a body of several primitives: the touching primitives'
+                // materials (each primitive carries its own)
+                const int t = tris[j];
+                float4 q1 = m1, q2 = m2;
+                if (with_mesh) {
+                    if (u1) q1 = d.prim_mat[d.prim_start[b1] + ((t >> 24) & 0xff)];
+                    if (u2) q2 = d.prim_mat[d.prim_start[b2] + ((t >> 24) & 0xff)];
+                } else {
+                    if (u1) q1 = d.prim_mat[d.prim_start[b1] + ((t >> 8) & 0xff)];
+                    if (u2) q2 = d.prim_mat[d.prim_start[b2] + (t & 0xff)];
+                }
+                rest = fmaxf(q1.x, q2.x); kin = (q1.y + q2.y) / 2.0f; sta = (q1.z + q2.z) / 2.0f;
+            }
             int dst = base + j;
             const ContactStore& O = d.c_old;
             const ContactStore& N = d.c_new;

@@ -355,6 +355,16 @@ struct Dev {
     int* mm_tri;
     int* mm_count;
     MeshScratch* msc;
+    // bodies of several primitives (has_union == 0: none in the batch); their
+    // pairs go through the mesh store like mesh pairs, each point's triangle
+    // field holding (primitive of the pair's first body << 8 | of its second)
+    // (with a mesh: the triangle id | the convex body's primitive << 24)
+    int has_union;
+    const int* prim_start;         // per body: its first primitive, -1 for a body of one
+    const int* prim_count;
+    const int* prim_shape;         // per primitive: blob offset in the pool
+    const float4* prim_mat;        // per primitive: restitution, kinetic, static friction
+    float4 *prim_lo, *prim_hi;     // per primitive: AABB
     // persistent graph (double-buffered by the host)
     EdgeStore e_old, e_new;
     ContactStore c_old, c_new;

@@ -364,6 +364,19 @@ __device__ __forceinline__ bool jointed(const Dev& d, int a, int b) {
     return lo < d.n_joint_edges && d.je.key[lo] == k && d.je.jcount[lo] > 0;
 }
 
+// bodies of several primitives (ConvexUnionGeometry): their primitives'
+// blobs, AABBs and materials live in the primitive tables; a body of one
+// primitive is its own only primitive
+__device__ __forceinline__ bool is_union(const Dev& d, int g) { return d.has_union && d.prim_start[g] >= 0; }
+__device__ __forceinline__ int prim_n(const Dev& d, int g) { return is_union(d, g) ? d.prim_count[g] : 1; }
+__device__ __forceinline__ const uint8_t* prim_blob(const Dev& d, int g, int k) {
+    return d.shapes + (is_union(d, g) ? d.prim_shape[d.prim_start[g] + k] : d.shape[g]);
+}
+__device__ __forceinline__ void prim_box(const Dev& d, int g, int k, f3* lo, f3* hi) {
+    if (is_union(d, g)) { *lo = mk(d.prim_lo[d.prim_start[g] + k]); *hi = mk(d.prim_hi[d.prim_start[g] + k]); }
+    else { *lo = mk(d.aabb_lo[g]); *hi = mk(d.aabb_hi[g]); }
+}
+
 // cull_manifold (CollisionDetect.cpp:2795-2830) to at most 4 points and write
 // the pair's manifold
 __device__ void emit_manifold(const Dev& d, int p, f3 n, float maxpen, const float4* pts, const unsigned long long* magic, int m) {
@@ -1086,9 +1099,12 @@ __device__ bool capsuleCylinder(const PrimView& A, const PrimView& B, int lane, 
 // detectCollision's primitive dispatch (CollisionDetect.cpp:57-150) for every
 // pair involving a sphere, cylinder or capsule.  Pairs the detectors take the other way
 // round are flipped back: normal negated, both MagicID halves swapped.
-__device__ __forceinline__ void narrow_prim(const Dev& d, int p, int a, int b, uint8_t* sa, uint8_t* sb, const uint8_t* ga,
-                                         const uint8_t* gb, uint32_t ka, uint32_t kb, int lane, Scratch& scratch,
-                                         CP* clipped) {
+// the detector of a pair of primitives of which at least one is a sphere,
+// cylinder or capsule (blobs staged at sa / sb): on lane 0, whether they
+// touch and the manifold before the cull, in the pair's order (a first)
+__device__ __forceinline__ bool narrow_prim_out(const Dev& d, int a, int b, uint8_t* sa, uint8_t* sb, const uint8_t* ga,
+                                             const uint8_t* gb, uint32_t ka, uint32_t kb, int lane, Scratch& scratch,
+                                             CP* clipped, PrimOut& o) {
     HullView hv;
     PrimView pa, pb;
     if (ka == SHAPE_HULL) stage_hull(ga, sa, d.pos[a], d.rot[a], &hv, lane);
@@ -1096,7 +1112,6 @@ __device__ __forceinline__ void narrow_prim(const Dev& d, int p, int a, int b, u
     if (kb == SHAPE_HULL) stage_hull(gb, sb, d.pos[b], d.rot[b], &hv, lane);
     else stage_prim(sb, d.pos[b], d.rot[b], &pb, lane);
     __syncwarp();
-    PrimOut o;
     o.m = 0;
     bool hit, flip = false;
     if (ka == SHAPE_HULL || kb == SHAPE_HULL) {
@@ -1122,8 +1137,8 @@ __device__ __forceinline__ void narrow_prim(const Dev& d, int p, int a, int b, u
     } else {
         hit = cylinderCylinder(pa, pb, lane, scratch, clipped, d.status, &o);
     }
-    if (lane != 0) return;
-    if (!hit || !(o.pen > 0.f) || o.m == 0) { no_manifold(d, p); return; }
+    if (lane != 0) return false;
+    if (!hit || !(o.pen > 0.f) || o.m == 0) return false;
     if (flip) {
         o.n = -1.f * o.n;
         for (int i = 0; i < o.m; i++) {
@@ -1131,7 +1146,17 @@ __device__ __forceinline__ void narrow_prim(const Dev& d, int p, int a, int b, u
             o.magic[i] = (x >> 32) | (x << 32);
         }
     }
-    emit_manifold(d, p, o.n, o.pen, o.pts, o.magic, o.m);
+    return true;
+}
+
+__device__ __forceinline__ void narrow_prim(const Dev& d, int p, int a, int b, uint8_t* sa, uint8_t* sb, const uint8_t* ga,
+                                         const uint8_t* gb, uint32_t ka, uint32_t kb, int lane, Scratch& scratch,
+                                         CP* clipped) {
+    PrimOut o;
+    const bool hit = narrow_prim_out(d, a, b, sa, sb, ga, gb, ka, kb, lane, scratch, clipped, o);
+    if (lane != 0) return;
+    if (!hit) no_manifold(d, p);
+    else emit_manifold(d, p, o.n, o.pen, o.pts, o.magic, o.m);
 }
 
 // ---- static triangle meshes --------------------------------------------------------
@@ -1523,6 +1548,12 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
     const int n_pairs = *d.n_pairs;
     for (int p = blockIdx.x * warps_per_block + wib; p < n_pairs; p += gridDim.x * warps_per_block) {
         const int a = d.pair_a[p], b = d.pair_b[p];
+        // pairs with a body of several primitives belong to k_narrow_mesh
+        // (no manifold here, so that k_clip passes them over)
+        if (is_union(d, a) || is_union(d, b)) {
+            if (lane == 0) { d.mf_n[p] = make_float4(0.f, 0.f, 0.f, -1.f); d.mf_cnt[p] = 0; }
+            continue;
+        }
         const uint8_t* ga = d.shapes + d.shape[a];
         const uint8_t* gb = d.shapes + d.shape[b];
         // pairs with a sphere or cylinder belong to k_narrow_prim
@@ -1675,6 +1706,26 @@ __global__ void __launch_bounds__(256) k_narrowphase(Dev d, int slot_bytes) {
 // CollisionDetect.cpp:237-280), clipping (:394-620) and the 4-direction cull
 // (:2795-2830).  The clip is serial per pair; a thread each keeps all lanes of
 // a warp busy on 32 pairs, where a warp per pair would idle 31.
+// the contact points of two hulls along the axis n (depth bp) between the
+// features `feat`, before the cull; returns their count
+__device__ int clip_hulls(const HullG& A, const HullG& B, f3 n, float bp, int2 feat, Scratch& scratch, CP* clipped, int* status,
+                          float4* pts, unsigned long long* mag) {
+    f3 u, w;
+    basis(n, &u, &w);
+    Area ac, bc;
+    contactArea(A, n, feat.x, u, w, &ac);
+    contactArea(B, -1.f * n, feat.y, u, w, &bc);
+    const int m = clipContacts(ac, bc, scratch, clipped, status);
+    const float a_dot = dot(A.vert(feat.x), n);
+    const f3 off = n * a_dot;
+    for (int i = 0; i < m; i++) {
+        f3 q = u * clipped[i].p.x + w * clipped[i].p.y + off;
+        pts[i] = make_float4(q.x, q.y, q.z, dot(q, n) - a_dot + bp);
+        mag[i] = clipped[i].magic;
+    }
+    return m;
+}
+
 __global__ void __launch_bounds__(128) k_clip(Dev d) {
     const int n_pairs = *d.n_pairs;
     Scratch scratch;
@@ -1683,29 +1734,15 @@ __global__ void __launch_bounds__(128) k_clip(Dev d) {
         const float4 nn = d.mf_n[p];
         if (!(nn.w > 0.f)) continue;
         const int a = d.pair_a[p], b = d.pair_b[p];
+        if (is_union(d, a) || is_union(d, b)) continue;
         const uint8_t* ga = d.shapes + d.shape[a];
         const uint8_t* gb = d.shapes + d.shape[b];
         if ((reinterpret_cast<const HullHeader*>(ga)->kind | reinterpret_cast<const HullHeader*>(gb)->kind) != SHAPE_HULL) continue;
         const HullG A(ga, d.pos[a], d.rot[a]), B(gb, d.pos[b], d.rot[b]);
-        const int2 feat = d.mf_feat[p];
-        const f3 n = mk(nn);
-        const float bp = nn.w;
-        f3 u, w;
-        basis(n, &u, &w);
-        Area ac, bc;
-        contactArea(A, n, feat.x, u, w, &ac);
-        contactArea(B, -1.f * n, feat.y, u, w, &bc);
-        const int m = clipContacts(ac, bc, scratch, clipped, d.status);
-        const float a_dot = dot(A.vert(feat.x), n);
-        const f3 off = n * a_dot;
         float4 pts[kMaxClip];
         unsigned long long mag[kMaxClip];
-        for (int i = 0; i < m; i++) {
-            f3 q = u * clipped[i].p.x + w * clipped[i].p.y + off;
-            pts[i] = make_float4(q.x, q.y, q.z, dot(q, n) - a_dot + bp);
-            mag[i] = clipped[i].magic;
-        }
-        emit_manifold(d, p, n, bp, pts, mag, m);
+        const int m = clip_hulls(A, B, mk(nn), nn.w, d.mf_feat[p], scratch, clipped, d.status, pts, mag);
+        emit_manifold(d, p, mk(nn), nn.w, pts, mag, m);
     }
 }
 
@@ -1732,7 +1769,7 @@ __global__ void __launch_bounds__(256, 1) k_narrow_prim(Dev d, int slot_bytes) {
         const HullHeader* Ha = reinterpret_cast<const HullHeader*>(ga);
         const HullHeader* Hb = reinterpret_cast<const HullHeader*>(gb);
         const uint32_t ka = Ha->kind, kb = Hb->kind;
-        if ((ka | kb) == SHAPE_HULL || ka == SHAPE_MESH || kb == SHAPE_MESH) continue;
+        if ((ka | kb) == SHAPE_HULL || ka == SHAPE_MESH || kb == SHAPE_MESH || is_union(d, a) || is_union(d, b)) continue;
         if (failed || !(d.movement[a] == 0 || d.movement[b] == 0) || both_asleep(d, a, b) || jointed(d, a, b)) {
             if (lane == 0) no_manifold(d, p);
             continue;
@@ -1757,6 +1794,60 @@ __global__ void __launch_bounds__(256, 1) k_narrow_prim(Dev d, int slot_bytes) {
         }
         narrow_prim(d, p, a, b, sa, sb, ga, gb, ka, kb, lane, scratch, clipped);
     }
+}
+
+// SAT_PolyPoly's axis search (CollisionDetect.cpp:717-835) for two staged
+// hulls by the whole warp: face normals of A, of B, then the edge pairs whose
+// Gauss arcs cross, every lane taking strided axes; the minimum over
+// (depth, axis order) is the same whatever lane meets an axis, so this equals
+// k_narrowphase's queued form.  Returns false when an axis separates them.
+__device__ bool sat_hulls(const HullView& A, const HullView& B, int lane, Axis* out) {
+    const int nva = A.h->nv, nvb = B.h->nv, nfa = A.h->nf, nfb = B.h->nf;
+    Axis best{INFINITY, 0x7fffffff, -1, -1, mk(0.f, 0.f, 0.f)};
+    bool sep = false;
+    for (int f = lane; f < nfa; f += 32) {
+        float4 g = A.n[f];
+        if (g.w != 0.f) continue;
+        f3 n = mk(g);
+        float4 c = A.cache[f];
+        float shift = dot(n, A.com);
+        Ext ea{c.y + shift, c.x + shift, __float_as_int(c.w), __float_as_int(c.z)};
+        check(ea, extrema(B.v, nvb, n), n, f, &best, &sep);
+    }
+    for (int f = lane; f < nfb; f += 32) {
+        float4 g = B.n[f];
+        if (g.w != 0.f) continue;
+        f3 n = mk(g);
+        float4 c = B.cache[f];
+        float shift = dot(n, B.com);
+        Ext eb{c.y + shift, c.x + shift, __float_as_int(c.w), __float_as_int(c.z)};
+        check(extrema(A.v, nva, n), eb, n, nfa + f, &best, &sep);
+    }
+    if (__any_sync(0xffffffffu, sep)) return false;
+    const int naa = A.h->na, nab = B.h->na, total = naa * nab;
+    for (int base = 0; base < total; base += 32) {
+        const int t = base + lane;
+        if (t < total) {
+            int ia = t / nab, ib = t - ia * nab;
+            f3 a1 = mk(A.n[A.arc[2 * ia]]), a2 = mk(A.n[A.arc[2 * ia + 1]]);
+            f3 b1 = -mk(B.n[B.arc[2 * ib]]), b2 = -mk(B.n[B.arc[2 * ib + 1]]);
+            f3 avg = a1 + a2;
+            if (dot(avg, b1) + dot(avg, b2) > 0.f) {
+                f3 ap = cross(a1, a2), bp = cross(b1, b2);
+                if (!(dot(ap, b1) * dot(ap, b2) > 0.f || dot(bp, a1) * dot(bp, a2) > 0.f)) {
+                    f3 n = cross(ap, bp);
+                    if (mag2(n) != 0.f) {
+                        n = normalize(n);
+                        if (dot(avg, n) < 0.f) n = n * -1.f;
+                        check(extrema(A.v, nva, n), extrema(B.v, nvb, n), n, nfa + nfb + t, &best, &sep);
+                    }
+                }
+            }
+        }
+        if (__any_sync(0xffffffffu, sep)) return false;
+    }
+    *out = warp_best(best);
+    return out->pen < INFINITY && out->aid >= 0 && out->bid >= 0;
 }
 
 // One warp per candidate pair with a static mesh (the other pairs are
@@ -1790,96 +1881,166 @@ __global__ void __launch_bounds__(256) k_narrow_mesh(Dev d, int slot_bytes) {
         const uint8_t* ga = d.shapes + d.shape[a];
         const uint8_t* gb = d.shapes + d.shape[b];
         const uint32_t ka = reinterpret_cast<const HullHeader*>(ga)->kind, kb = reinterpret_cast<const HullHeader*>(gb)->kind;
+        const bool ua = is_union(d, a), ub = is_union(d, b);
         if (lane == 0) d.mf_ofs[p] = -1;
-        if (ka != SHAPE_MESH && kb != SHAPE_MESH) continue;
-        if (failed || (ka == SHAPE_MESH && kb == SHAPE_MESH) || !(d.movement[a] == 0 || d.movement[b] == 0) || jointed(d, a, b)) {
+        const bool mesh_pair = ka == SHAPE_MESH || kb == SHAPE_MESH;
+        if (!mesh_pair && !ua && !ub) continue;
+        // collision filter of PhysicsEngine.cpp:174 and collisionAllowed (a
+        // static mesh is never asleep)
+        if (failed || (ka == SHAPE_MESH && kb == SHAPE_MESH) || !(d.movement[a] == 0 || d.movement[b] == 0) ||
+            (!mesh_pair && both_asleep(d, a, b)) || jointed(d, a, b)) {
             if (lane == 0) no_manifold(d, p);
             continue;
         }
-        const bool flip = ka == SHAPE_MESH;
-        const int c = flip ? b : a;
-        const uint8_t* gc = flip ? gb : ga;
-        const uint8_t* gm = flip ? ga : gb;
-        const uint32_t kc = flip ? kb : ka;
-        const uint32_t hot = reinterpret_cast<const HullHeader*>(gc)->off_fofs;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncwarp();
-        if (lane == 0) {
-            mbar_expect(&bars[wib], hot);
-            bulk_load(slot, gc, hot, &bars[wib]);
+        int nman = 0, npts = 0;   // lane 0's counts
+        // a manifold (before the cull) into the pair's list, on lane 0
+        auto add_manifold = [&](const PrimOut& o, bool flipped, int tri) {
+            if (nman >= kMeshMans || npts + o.m > kMeshRaw) {
+                atomicOr(d.status, ST_MESH_OVERFLOW);
+                return;
+            }
+            f3 n = flipped ? -1.f * o.n : o.n;
+            S.man_n[nman] = make_float4(n.x, n.y, n.z, o.pen);
+            S.man_first[nman] = npts;
+            S.man_cnt[nman] = o.m;
+            for (int i = 0; i < o.m; i++) {
+                unsigned long long x = o.magic[i];
+                S.pt[npts + i] = o.pts[i];
+                S.magic[npts + i] = flipped ? ((x >> 32) | (x << 32)) : x;
+                S.tri[npts + i] = tri;
+            }
+            npts += o.m;
+            nman++;
+        };
+        bool timed_out = false;
+        // stage blobs into the warp's slot (bounded wait); false on a timeout
+        auto stage = [&](const uint8_t* g1, uint8_t* s1, uint32_t h1, const uint8_t* g2, uint8_t* s2, uint32_t h2) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) {
+                mbar_expect(&bars[wib], h1 + h2);
+                bulk_load(s1, g1, h1, &bars[wib]);
+                if (h2) bulk_load(s2, g2, h2, &bars[wib]);
+            }
+            bool ok = mbar_wait(&bars[wib], parity, d.wait_limit);
+            parity ^= 1u;
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) atomicOr(d.status, ST_TIMEOUT);
+                mbar_wait(&bars[wib], parity ^ 1u, kDefaultWaitLimit);
+                timed_out = true;
+                return false;
+            }
+            return true;
+        };
+        if (mesh_pair) {
+            // SAT_PolyMesh and friends for each primitive of the convex body
+            // (one for a body of one primitive), each behind its own AABB
+            const bool flip = ka == SHAPE_MESH;
+            const int c = flip ? b : a;
+            const uint8_t* gm = flip ? ga : gb;
+            const HullHeader* Hm = reinterpret_cast<const HullHeader*>(gm);
+            const float4* nodes = reinterpret_cast<const float4*>(gm + kMeshOffNodes);
+            const float4* tris = nodes + 2 * (size_t)Hm->pad[1];
+            const int nc = prim_n(d, c);
+            for (int k = 0; k < nc && !timed_out; k++) {
+                const uint8_t* gc = prim_blob(d, c, k);
+                const uint32_t kc = reinterpret_cast<const HullHeader*>(gc)->kind;
+                if (!stage(gc, slot, reinterpret_cast<const HullHeader*>(gc)->off_fofs, nullptr, nullptr, 0)) break;
+                HullView hv;
+                PrimView pv;
+                if (kc == SHAPE_HULL) stage_hull(gc, slot, d.pos[c], d.rot[c], &hv, lane);
+                else stage_prim(slot, d.pos[c], d.rot[c], &pv, lane);
+                f3 blo, bhi;
+                prim_box(d, c, k, &blo, &bhi);
+                int ncand = 0;
+                if (lane == 0) {
+                    int stack[kMeshStack];
+                    int sp = 0;
+                    stack[sp++] = 0;
+                    while (sp > 0) {
+                        const int x = stack[--sp];
+                        const float4 lo = __ldg(nodes + 2 * x), hi = __ldg(nodes + 2 * x + 1);
+                        const int l = __float_as_int(lo.w), r = __float_as_int(hi.w);
+                        if (l < 0) {
+                            const float4* t = tris + (size_t)kMeshTriF4 * r;
+                            if (box_overlap(mk(__ldg(t + 11)), mk(__ldg(t + 12)), blo, bhi)) {
+                                if (ncand < kMeshCand) S.cand[ncand++] = r;
+                                else { atomicOr(d.status, ST_MESH_OVERFLOW); break; }
+                            }
+                        } else if (box_overlap(mk(lo), mk(hi), blo, bhi)) {
+                            if (sp + 2 > kMeshStack) { atomicOr(d.status, ST_MESH_OVERFLOW); break; }
+                            stack[sp++] = l;
+                            stack[sp++] = r;
+                        }
+                    }
+                }
+                ncand = __shfl_sync(0xffffffffu, ncand, 0);
+                __syncwarp();
+                const float pen_scale = kc == SHAPE_HULL ? 0.f : 0.15f;
+                const float body_long = longest(blo, bhi);
+                for (int ci = 0; ci < ncand; ci++) {
+                    TriView T;
+                    load_tri(tris + (size_t)kMeshTriF4 * S.cand[ci], &T);
+                    const float penalty = pen_scale * fminf(body_long, longest(T.lo, T.hi));
+                    PrimOut o;
+                    o.m = 0;
+                    bool hit;
+                    if (kc == SHAPE_HULL) hit = polyTri(hv, T, penalty, lane, scratch, clipped, d.status, &o);
+                    else if (kc == SHAPE_SPHERE) hit = sphereTri(pv, T, penalty, lane, &o);
+                    else if (kc == SHAPE_CAPSULE) hit = capTri(pv, T, penalty, lane, scratch, clipped, d.status, &o);
+                    else hit = cylTri(pv, T, penalty, lane, scratch, clipped, d.status, &o);
+                    // a union primitive's index rides above the triangle id
+                    if (lane == 0 && hit && o.pen > 0.f && o.m > 0) add_manifold(o, flip, T.id | (is_union(d, c) ? k << 24 : 0));
+                }
+                __syncwarp();
+            }
+        } else {
+            // bodies of several primitives (PhysicsEngine.cpp:182-219): every
+            // primitive pair whose AABBs overlap, in order (a's primitives
+            // outer), each detector's manifold before the cull
+            const int na = prim_n(d, a), nb2 = prim_n(d, b);
+            for (int i = 0; i < na && !timed_out; i++)
+                for (int j = 0; j < nb2 && !timed_out; j++) {
+                    f3 alo, ahi, blo, bhi;
+                    prim_box(d, a, i, &alo, &ahi);
+                    prim_box(d, b, j, &blo, &bhi);
+                    if (!box_overlap(alo, ahi, blo, bhi)) continue;
+                    const uint8_t* pa = prim_blob(d, a, i);
+                    const uint8_t* pb = prim_blob(d, b, j);
+                    const HullHeader* Ha = reinterpret_cast<const HullHeader*>(pa);
+                    const HullHeader* Hb = reinterpret_cast<const HullHeader*>(pb);
+                    uint8_t* sa = slot;
+                    uint8_t* sb = slot + ((Ha->off_fofs + 15u) & ~15u);
+                    if (!stage(pa, sa, Ha->off_fofs, pb, sb, Hb->off_fofs)) break;
+                    const int tri = (i << 8) | j;
+                    if (Ha->kind == SHAPE_HULL && Hb->kind == SHAPE_HULL) {
+                        HullView A, B;
+                        stage_hull(pa, sa, d.pos[a], d.rot[a], &A, lane);
+                        stage_hull(pb, sb, d.pos[b], d.rot[b], &B, lane);
+                        __syncwarp();
+                        Axis best;
+                        const bool touch = sat_hulls(A, B, lane, &best);
+                        if (touch && lane == 0) {
+                            const HullG GA(pa, d.pos[a], d.rot[a]), GB(pb, d.pos[b], d.rot[b]);
+                            PrimOut o;
+                            o.n = best.n;
+                            o.pen = best.pen;
+                            o.m = clip_hulls(GA, GB, best.n, best.pen, make_int2(best.aid, best.bid), scratch, clipped, d.status,
+                                             o.pts, o.magic);
+                            if (o.pen > 0.f && o.m > 0) add_manifold(o, false, tri);
+                        }
+                    } else {
+                        PrimOut o;
+                        const bool hit = narrow_prim_out(d, a, b, sa, sb, pa, pb, Ha->kind, Hb->kind, lane, scratch, clipped, o);
+                        if (lane == 0 && hit) add_manifold(o, false, tri);
+                    }
+                    __syncwarp();
+                }
         }
-        bool ok = mbar_wait(&bars[wib], parity, d.wait_limit);
-        parity ^= 1u;
-        if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) { atomicOr(d.status, ST_TIMEOUT); no_manifold(d, p); }
-            mbar_wait(&bars[wib], parity ^ 1u, kDefaultWaitLimit);
+        if (timed_out) {
+            if (lane == 0) no_manifold(d, p);
             failed = true;
             continue;
-        }
-        HullView hv;
-        PrimView pv;
-        if (kc == SHAPE_HULL) stage_hull(gc, slot, d.pos[c], d.rot[c], &hv, lane);
-        else stage_prim(slot, d.pos[c], d.rot[c], &pv, lane);
-        const f3 blo = mk(d.aabb_lo[c]), bhi = mk(d.aabb_hi[c]);
-        const HullHeader* Hm = reinterpret_cast<const HullHeader*>(gm);
-        const float4* nodes = reinterpret_cast<const float4*>(gm + kMeshOffNodes);
-        const float4* tris = nodes + 2 * (size_t)Hm->pad[1];
-        int ncand = 0;
-        if (lane == 0) {
-            int stack[kMeshStack];
-            int sp = 0;
-            stack[sp++] = 0;
-            while (sp > 0) {
-                const int x = stack[--sp];
-                const float4 lo = __ldg(nodes + 2 * x), hi = __ldg(nodes + 2 * x + 1);
-                const int l = __float_as_int(lo.w), r = __float_as_int(hi.w);
-                if (l < 0) {
-                    const float4* t = tris + (size_t)kMeshTriF4 * r;
-                    if (box_overlap(mk(__ldg(t + 11)), mk(__ldg(t + 12)), blo, bhi)) {
-                        if (ncand < kMeshCand) S.cand[ncand++] = r;
-                        else { atomicOr(d.status, ST_MESH_OVERFLOW); break; }
-                    }
-                } else if (box_overlap(mk(lo), mk(hi), blo, bhi)) {
-                    if (sp + 2 > kMeshStack) { atomicOr(d.status, ST_MESH_OVERFLOW); break; }
-                    stack[sp++] = l;
-                    stack[sp++] = r;
-                }
-            }
-        }
-        ncand = __shfl_sync(0xffffffffu, ncand, 0);
-        __syncwarp();
-        const float pen_scale = kc == SHAPE_HULL ? 0.f : 0.15f;
-        const float body_long = longest(blo, bhi);
-        int nman = 0, npts = 0;   // lane 0's counts
-        for (int ci = 0; ci < ncand; ci++) {
-            TriView T;
-            load_tri(tris + (size_t)kMeshTriF4 * S.cand[ci], &T);
-            const float penalty = pen_scale * fminf(body_long, longest(T.lo, T.hi));
-            PrimOut o;
-            o.m = 0;
-            bool hit;
-            if (kc == SHAPE_HULL) hit = polyTri(hv, T, penalty, lane, scratch, clipped, d.status, &o);
-            else if (kc == SHAPE_SPHERE) hit = sphereTri(pv, T, penalty, lane, &o);
-            else if (kc == SHAPE_CAPSULE) hit = capTri(pv, T, penalty, lane, scratch, clipped, d.status, &o);
-            else hit = cylTri(pv, T, penalty, lane, scratch, clipped, d.status, &o);
-            if (lane == 0 && hit && o.pen > 0.f && o.m > 0) {
-                if (nman >= kMeshMans || npts + o.m > kMeshRaw) {
-                    atomicOr(d.status, ST_MESH_OVERFLOW);
-                    continue;
-                }
-                f3 n = flip ? -1.f * o.n : o.n;
-                S.man_n[nman] = make_float4(n.x, n.y, n.z, o.pen);
-                S.man_first[nman] = npts;
-                S.man_cnt[nman] = o.m;
-                for (int i = 0; i < o.m; i++) {
-                    unsigned long long x = o.magic[i];
-                    S.pt[npts + i] = o.pts[i];
-                    S.magic[npts + i] = flip ? ((x >> 32) | (x << 32)) : x;
-                    S.tri[npts + i] = T.id;
-                }
-                npts += o.m;
-                nman++;
-            }
         }
         if (lane == 0) {
             float maxpen;
@@ -2039,31 +2200,44 @@ __global__ void k_raycast(Dev d, int s, int e, const float* rays, int n, const u
             bool skip = false;
             for (int q = 0; q < n_ignore; q++) skip |= ignore[q] == id;
             if (skip || !rayAABB(mk(d.aabb_lo[g]), mk(d.aabb_hi[g]), o, dir)) continue;
-            const uint8_t* blob = d.shapes + d.shape[g];
-            const uint32_t kind = reinterpret_cast<const HullHeader*>(blob)->kind;
+            // RigidBody::checkRayIntersection (RigidBody.cpp:185-200): each
+            // primitive behind its own AABB (a body of one: behind the body's),
+            // the nearest primitive hit
             RayHitD h{false};
-            if (kind == SHAPE_MESH) {
-                h = rayMesh(blob, o, dir);
-            } else if (kind == SHAPE_HULL) {
-                h = rayHull(blob, d.pos[g], d.rot[g], o, dir);
-            } else {
-                const M33 R = quatRot(qnormalize(d.rot[g]));
-                const float4 cr = *reinterpret_cast<const float4*>(blob + sizeof(HullHeader));
-                const f3 c = mul(R, mk(cr)) + mk(d.pos[g]);
-                if (kind == SHAPE_SPHERE) {
-                    h = raySphere(o, dir, c, cr.w);
+            const int nprim = prim_n(d, g);
+            for (int pk = 0; pk < nprim; pk++) {
+                if (nprim > 1) {
+                    f3 plo, phi;
+                    prim_box(d, g, pk, &plo, &phi);
+                    if (!rayAABB(plo, phi, o, dir)) continue;
+                }
+                const uint8_t* blob = prim_blob(d, g, pk);
+                const uint32_t kind = reinterpret_cast<const HullHeader*>(blob)->kind;
+                RayHitD hp{false};
+                if (kind == SHAPE_MESH) {
+                    hp = rayMesh(blob, o, dir);
+                } else if (kind == SHAPE_HULL) {
+                    hp = rayHull(blob, d.pos[g], d.rot[g], o, dir);
                 } else {
-                    const float4 ax4 = *reinterpret_cast<const float4*>(blob + kCylOffAxis);
-                    const f3 ax = mul(R, mk(ax4));
-                    h = rayCylSide(o, dir, c, cr.w, ax4.w, ax);
-                    if (kind == SHAPE_CYLINDER) {   // Cylinder::testRayIntersection (ConvexPrimitive.cpp:308-318)
-                        const float sgn = dot(ax, dir) < 0.f ? 1.f : -1.f;
-                        rayNearer(&h, rayDisk(o, dir, c + sgn * ax * (0.5f * ax4.w), ax, cr.w));
-                    } else {                        // Capsule::testRayIntersection (:403-411)
-                        rayNearer(&h, raySphere(o, dir, c + ax * (0.5f * ax4.w), cr.w));
-                        rayNearer(&h, raySphere(o, dir, c - ax * (0.5f * ax4.w), cr.w));
+                    const M33 R = quatRot(qnormalize(d.rot[g]));
+                    const float4 cr = *reinterpret_cast<const float4*>(blob + sizeof(HullHeader));
+                    const f3 c = mul(R, mk(cr)) + mk(d.pos[g]);
+                    if (kind == SHAPE_SPHERE) {
+                        hp = raySphere(o, dir, c, cr.w);
+                    } else {
+                        const float4 ax4 = *reinterpret_cast<const float4*>(blob + kCylOffAxis);
+                        const f3 ax = mul(R, mk(ax4));
+                        hp = rayCylSide(o, dir, c, cr.w, ax4.w, ax);
+                        if (kind == SHAPE_CYLINDER) {   // Cylinder::testRayIntersection (ConvexPrimitive.cpp:308-318)
+                            const float sgn = dot(ax, dir) < 0.f ? 1.f : -1.f;
+                            rayNearer(&hp, rayDisk(o, dir, c + sgn * ax * (0.5f * ax4.w), ax, cr.w));
+                        } else {                        // Capsule::testRayIntersection (:403-411)
+                            rayNearer(&hp, raySphere(o, dir, c + ax * (0.5f * ax4.w), cr.w));
+                            rayNearer(&hp, raySphere(o, dir, c - ax * (0.5f * ax4.w), cr.w));
+                        }
                     }
                 }
+                if (hp.hit && (!h.hit || hp.t < h.t)) h = hp;
             }
             if (h.hit && (!best.hit || h.t < best.t)) { best = h; best_id = (int)id; }
         }
@@ -2088,7 +2262,7 @@ void launch_narrowphase(const Dev& d, int slot_bytes, int n_sms, bool prims, cud
     k_narrowphase<<<n_sms * 4, warps * 32, smem, st>>>(d, slot_bytes);
     k_clip<<<n_sms * 16, 128, 0, st>>>(d);
     if (prims) k_narrow_prim<<<n_sms * 4, warps * 32, 16 * warps + (size_t)warps * slot_bytes, st>>>(d, slot_bytes);
-    if (d.has_mesh)
+    if (d.has_mesh || d.has_union)
         k_narrow_mesh<<<n_sms * kMeshBlocksPerSm, warps * 32, 16 * warps + (size_t)warps * slot_bytes, st>>>(d, slot_bytes);
 }
 

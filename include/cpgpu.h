@@ -162,8 +162,9 @@ typedef struct cpgpu_primitive {
  * order, movement, pos) (Geometry.cpp:540-550, RigidBody.cpp:13-39): mass
  * properties summed over the primitives, each primitive its own AABB and
  * material, pairs of bodies tested primitive pair by primitive pair
- * (PhysicsEngine.cpp:182-219).  The device path takes n = 1 (the same as the
- * single-primitive calls); n > 1 returns CPGPU_ERR_UNSUPPORTED there. */
+ * (PhysicsEngine.cpp:182-219), their manifolds merged and culled per body
+ * pair (PhysicsEngine.cpp:257-295).  n = 1 is the same as the
+ * single-primitive calls; at most 255 primitives per body. */
 int cpgpu_body_union(cpgpu_world* w, const cpgpu_primitive* prims, int n, int movement, const double pos[3],
                      uint32_t* out_id);
 /* createRigidBody(StaticMeshGeometry(MeshInput{tris, points}), fixed)

@@ -9,8 +9,8 @@
 //   * on the device: convex hulls, boxes, spheres, cylinders, capsules and
 //     fixed static triangle meshes; ball-socket, hinge, distance, weld,
 //     slider and sliding-hinge joints, cone and twist limits, motors,
-//     pistons and springs; sleeping; one primitive per body (others throw
-//     cpgpu::Error with CPGPU_ERR_UNSUPPORTED).
+//     pistons and springs; sleeping; bodies of several primitives
+//     (ConvexUnionGeometry::merge).
 #pragma once
 #include <array>
 #include <cmath>
@@ -54,8 +54,8 @@ struct Material {
     cpgpu_material c() const { return cpgpu_material{density, restitution, kinetic_friction_coeff, static_friction_coeff}; }
 };
 
-// ConvexUnionGeometry restricted to one convex primitive (Geometry.h:9-47)
-struct ConvexUnionGeometry {
+// One convex primitive of a ConvexUnionGeometry (ConvexPrimitive.h:36-60)
+struct ConvexPrimitive {
     enum Kind { HULL, BOX, SPHERE, CYLINDER, CAPSULE } kind = HULL;
     std::vector<Vec3> points;
     std::vector<std::vector<int>> faces;
@@ -63,31 +63,63 @@ struct ConvexUnionGeometry {
     double dx = 0, dy = 0, dz = 0;
     double radius = 0, height = 0;   // sphere / cylinder / capsule (capsule: drum height)
     Material material;
-    static ConvexUnionGeometry sphere(Vec3 center, double radius, Material m = Material::default_material()) {
+};
+
+// ConvexUnionGeometry (Geometry.h:9-47): a list of convex primitives that one
+// rigid body is made of
+struct ConvexUnionGeometry {
+    std::vector<ConvexPrimitive> polyhedra;
+
+    static ConvexUnionGeometry of(const ConvexPrimitive& c) {
         ConvexUnionGeometry g;
-        g.kind = SPHERE; g.corner = center; g.radius = radius; g.material = m;
+        g.polyhedra.push_back(c);
         return g;
     }
+    static ConvexUnionGeometry sphere(Vec3 center, double radius, Material m = Material::default_material()) {
+        ConvexPrimitive c;
+        c.kind = ConvexPrimitive::SPHERE; c.corner = center; c.radius = radius; c.material = m;
+        return of(c);
+    }
     static ConvexUnionGeometry cylinder(Vec3 pos, double radius, double height, Material m = Material::default_material()) {
-        ConvexUnionGeometry g;
-        g.kind = CYLINDER; g.corner = pos; g.radius = radius; g.height = height; g.material = m;
-        return g;
+        ConvexPrimitive c;
+        c.kind = ConvexPrimitive::CYLINDER; c.corner = pos; c.radius = radius; c.height = height; c.material = m;
+        return of(c);
     }
     static ConvexUnionGeometry capsule(Vec3 bot_sphere_center, double radius, double drum_height,
                                        Material m = Material::default_material()) {
-        ConvexUnionGeometry g;
-        g.kind = CAPSULE; g.corner = bot_sphere_center; g.radius = radius; g.height = drum_height; g.material = m;
-        return g;
+        ConvexPrimitive c;
+        c.kind = ConvexPrimitive::CAPSULE; c.corner = bot_sphere_center; c.radius = radius; c.height = drum_height;
+        c.material = m;
+        return of(c);
     }
     static ConvexUnionGeometry box(Vec3 pos, double dx, double dy, double dz, Material m = Material::default_material()) {
-        ConvexUnionGeometry g;
-        g.kind = BOX; g.corner = pos; g.dx = dx; g.dy = dy; g.dz = dz; g.material = m;
-        return g;
+        ConvexPrimitive c;
+        c.kind = ConvexPrimitive::BOX; c.corner = pos; c.dx = dx; c.dy = dy; c.dz = dz; c.material = m;
+        return of(c);
     }
     static ConvexUnionGeometry polyhedron(const std::vector<Vec3>& pts, const std::vector<std::vector<int>>& faces,
                                           Material m = Material::default_material()) {
-        ConvexUnionGeometry g;
-        g.kind = HULL; g.points = pts; g.faces = faces; g.material = m;
+        ConvexPrimitive c;
+        c.kind = ConvexPrimitive::HULL; c.points = pts; c.faces = faces; c.material = m;
+        return of(c);
+    }
+    // ConvexUnionGeometry::merge (Geometry.cpp:540-550): g1's primitives, then g2's
+    static ConvexUnionGeometry merge(const ConvexUnionGeometry& g1, const ConvexUnionGeometry& g2) {
+        ConvexUnionGeometry g = g1;
+        g.polyhedra.insert(g.polyhedra.end(), g2.polyhedra.begin(), g2.polyhedra.end());
+        return g;
+    }
+    ConvexUnionGeometry getNewMaterial(Material m) const {
+        ConvexUnionGeometry g = *this;
+        for (ConvexPrimitive& c : g.polyhedra) c.material = m;
+        return g;
+    }
+    ConvexUnionGeometry getTranslated(Vec3 v) const {
+        ConvexUnionGeometry g = *this;
+        for (ConvexPrimitive& c : g.polyhedra) {
+            c.corner = Vec3(c.corner.x + v.x, c.corner.y + v.y, c.corner.z + v.z);
+            for (Vec3& p : c.points) p = Vec3(p.x + v.x, p.y + v.y, p.z + v.z);
+        }
         return g;
     }
 };
@@ -134,24 +166,37 @@ public:
     void timeSteps(int n) { check(cpgpu_step(w_, n)); }
 
     RigidBody* createRigidBody(const ConvexUnionGeometry& g, MovementType movement = DYNAMIC, Vec3 position = Vec3()) {
-        uint32_t id = 0;
-        cpgpu_material m = g.material.c();
-        if (g.kind == ConvexUnionGeometry::BOX) {
-            check(cpgpu_body_box(w_, g.corner.data(), g.dx, g.dy, g.dz, &m, movement, position.data(), &id));
-        } else if (g.kind == ConvexUnionGeometry::SPHERE) {
-            check(cpgpu_body_sphere(w_, g.corner.data(), g.radius, &m, movement, position.data(), &id));
-        } else if (g.kind == ConvexUnionGeometry::CYLINDER) {
-            check(cpgpu_body_cylinder(w_, g.corner.data(), g.radius, g.height, &m, movement, position.data(), &id));
-        } else if (g.kind == ConvexUnionGeometry::CAPSULE) {
-            check(cpgpu_body_capsule(w_, g.corner.data(), g.radius, g.height, &m, movement, position.data(), &id));
-        } else {
-            std::vector<double> pts;
-            for (const Vec3& p : g.points) { pts.push_back(p.x); pts.push_back(p.y); pts.push_back(p.z); }
-            std::vector<int> offs{0}, idx;
-            for (const auto& f : g.faces) { idx.insert(idx.end(), f.begin(), f.end()); offs.push_back((int)idx.size()); }
-            check(cpgpu_body_hull(w_, pts.data(), (int)g.points.size(), offs.data(), idx.data(), (int)g.faces.size(), &m,
-                                  movement, position.data(), &id));
+        const size_t n = g.polyhedra.size();
+        if (n == 0) throw Error(CPGPU_ERR_INVALID_ARG, "cpgpu: createRigidBody of an empty ConvexUnionGeometry");
+        // storage the primitive descriptors point into, alive until the call returns
+        std::vector<std::vector<double>> pts(n);
+        std::vector<std::vector<int>> offs(n), idx(n);
+        std::vector<cpgpu_primitive> prims(n);
+        for (size_t i = 0; i < n; i++) {
+            const ConvexPrimitive& c = g.polyhedra[i];
+            cpgpu_primitive& q = prims[i];
+            q = cpgpu_primitive{};
+            q.mat = c.material.c();
+            q.p[0] = c.corner.x; q.p[1] = c.corner.y; q.p[2] = c.corner.z;
+            switch (c.kind) {
+            case ConvexPrimitive::BOX: q.kind = CPGPU_PRIM_BOX; q.a = c.dx; q.b = c.dy; q.c = c.dz; break;
+            case ConvexPrimitive::SPHERE: q.kind = CPGPU_PRIM_SPHERE; q.a = c.radius; break;
+            case ConvexPrimitive::CYLINDER: q.kind = CPGPU_PRIM_CYLINDER; q.a = c.radius; q.b = c.height; break;
+            case ConvexPrimitive::CAPSULE: q.kind = CPGPU_PRIM_CAPSULE; q.a = c.radius; q.b = c.height; break;
+            default:
+                for (const Vec3& p : c.points) { pts[i].push_back(p.x); pts[i].push_back(p.y); pts[i].push_back(p.z); }
+                offs[i].push_back(0);
+                for (const auto& f : c.faces) {
+                    idx[i].insert(idx[i].end(), f.begin(), f.end());
+                    offs[i].push_back((int)idx[i].size());
+                }
+                q.kind = CPGPU_PRIM_HULL;
+                q.points = pts[i].data(); q.n_points = (int)c.points.size();
+                q.face_offsets = offs[i].data(); q.face_indices = idx[i].data(); q.n_faces = (int)c.faces.size();
+            }
         }
+        uint32_t id = 0;
+        check(cpgpu_body_union(w_, prims.data(), (int)n, movement, position.data(), &id));
         RigidBody* b = new RigidBody(this, id);
         owned_.push_back(b);
         return b;

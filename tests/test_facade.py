@@ -21,7 +21,7 @@ def _build(tmp_path, name="facade_box_drop"):
     return exe
 
 
-@pytest.mark.parametrize("name", ["facade_box_drop", "facade_primitives_drop"])
+@pytest.mark.parametrize("name", ["facade_box_drop", "facade_primitives_drop", "facade_union_drop"])
 def test_facade_compiles_and_fails_loudly_without_gpu(tmp_path, name):
     exe = _build(tmp_path, name)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
@@ -31,7 +31,7 @@ def test_facade_compiles_and_fails_loudly_without_gpu(tmp_path, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["facade_box_drop", "facade_primitives_drop"])
+@pytest.mark.parametrize("name", ["facade_box_drop", "facade_primitives_drop", "facade_union_drop"])
 def test_facade_box_drop_on_device(tmp_path, name):
     exe = _build(tmp_path, name)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
