@@ -356,7 +356,7 @@ SECONDARY = {
 
 def run_secondary(a):
     """One of the other configurations: device body-steps/s (state in HBM),
-    per-stage windows and roofline, the reference engine on the machine's host
+    per-stage times and roofline, the reference engine on the machine's host
     cores on a bounded sample, and (1,000 hulls) the 600-step drift."""
     import constraintphysics_gb300 as cg
     import oracle
@@ -497,8 +497,9 @@ def main():
     # per-step latency distribution over another `steps` steps
     lat = [batch.step_timed(1) for _ in range(a.steps)]
     # per-stage device times over another `steps` steps launched stage by
-    # stage with CUDA events on every part's stream (the parts concurrent as
-    # in the graph-launched steps): each stage's window inside the step
+    # stage with CUDA events on every part's stream (one step at a time, the
+    # parts concurrent): each stage's time is the union of the parts'
+    # intervals in it
     stage_ms, counts = batch.profile(a.steps)
     clocks = sampler.stop()
     # FP64 momentum / energy audit: steps with the audit kernel at the end of
@@ -561,8 +562,9 @@ def main():
             roof = {"bound": "hbm", "kernel": stage, "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": measured_traffic(stage, a.worlds),
                     "algorithmic_bytes_per_launch": b, "launch_ms": stage_ms[stage],
-                    "note": ("dominant stage (k_pgs_big with k_pgs_small beside it, both parts); launch_ms is its "
-                             "window inside the step, CUDA events on every part's stream over --steps steps")
+                    "note": ("dominant stage (k_pgs_big with k_pgs_small beside it, every part); launch_ms is the "
+                             "time some part spends in it per step (union of the parts' intervals), CUDA events "
+                             "on every part's stream over --steps steps")
                     if stage == dominant else f"dominant stage {dominant} has no byte model"}
             break
 

@@ -38,6 +38,8 @@ def lib():
             "batch_read_state": [ctypes.c_void_p, ctypes.c_void_p],
             "batch_write_state": [ctypes.c_void_p, ctypes.c_void_p],
             "batch_profile": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
+            "batch_timeline": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                               ctypes.c_void_p],
             "batch_launches_per_step": [ctypes.c_void_p, ctypes.c_void_p],
             "world_clone": [ctypes.c_void_p, ctypes.c_void_p],
             "server_create": [ctypes.c_int64, ctypes.c_int, ctypes.c_void_p],
@@ -125,11 +127,11 @@ class Batch:
 
     def schedule(self):
         """The batch's schedule (cpgpu_batch_schedule)."""
-        sched = (ctypes.c_int * 5)()
+        sched = (ctypes.c_int * 6)()
         times = (ctypes.c_double * 2)()
         self._check(self.abi.batch_schedule(self.h, ctypes.addressof(sched), ctypes.addressof(times)))
         return {"parts": sched[0], "first_share_pct": sched[1], "rest_chain_workers_per_sm": sched[2],
-                "big_island_rows": sched[3], "tuned": bool(sched[4]),
+                "big_island_rows": sched[3], "tuned": bool(sched[4]), "second_share_pct": sched[5],
                 "tuned_ms_per_step": times[0] if times[0] >= 0 else None,
                 "default_ms_per_step": times[1] if times[1] >= 0 else None}
 
@@ -176,6 +178,16 @@ class Batch:
         self._check(self.abi.batch_profile(self.h, int(n), ms.ctypes.data, counts.ctypes.data))
         return dict(zip(self.STAGES, ms.tolist())), {"pairs": int(counts[0]), "contacts": int(counts[1]),
                                                       "islands": int(counts[2])}
+
+    def timeline(self, n=1):
+        """Per part, the mean ms from the step's start to each stage mark
+        (cpgpu_batch_timeline): array (parts, 7 + 3 * substeps)."""
+        np_, nm = ctypes.c_int(), ctypes.c_int()
+        self._check(self.abi.batch_timeline(self.h, 0, None, 0, ctypes.addressof(np_), ctypes.addressof(nm)))
+        out = np.zeros((np_.value, nm.value))
+        self._check(self.abi.batch_timeline(self.h, int(n), out.ctypes.data, out.size, ctypes.addressof(np_),
+                                            ctypes.addressof(nm)))
+        return out
 
     def set_audit(self, enabled=True):
         """Per-step FP64 momentum / energy audit of every world (cpgpu_batch_set_audit)."""

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <memory>
@@ -588,15 +589,22 @@ struct Batch {
     size_t bytes = 0;                  // device arena size
     Dev d[2];                  // d[p]: old = buffer p, new = buffer 1-p
     int parity = 0;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    // per parity, the step as two graphs: up to the PGS schedule, and the rest
+    cudaGraphExec_t graph_pre[2] = {nullptr, nullptr}, graph_rest[2] = {nullptr, nullptr};
+    cudaEvent_t pre_done = nullptr;    // recorded after each step's first graph
     std::vector<int> world_start;
     std::vector<int> world_jstart;     // joint ranges of the worlds
     std::vector<uint8_t> movement;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double* audit = nullptr;           // FP64 audit values (kAuditValues per world), null when disabled
 
+    void drop_graphs() {
+        for (auto* gs : {graph_pre, graph_rest})
+            for (int p = 0; p < 2; p++) if (gs[p]) { cudaGraphExecDestroy(gs[p]); gs[p] = nullptr; }
+    }
     ~Batch() {
-        for (auto& g : graph) if (g) cudaGraphExecDestroy(g);
+        drop_graphs();
+        if (pre_done) cudaEventDestroy(pre_done);
         if (audit) cudaFree(audit);
         if (snap) cudaFree(snap);
         if (ev0) cudaEventDestroy(ev0);
@@ -615,7 +623,9 @@ struct Batch {
     void mark(int stage) {
         if (marks) CK(cudaEventRecord((*marks)[stage], st));
     }
-    void launch_step(const Dev& x) {
+    // a step in two halves: gravity to the PGS schedule (the work every
+    // island's solver chain waits for), then the substeps and geometry
+    void launch_pre(const Dev& x) {
         Launch L{n_sms, st};
         mark(0);
         launch_step_begin(x, L);   mark(1);
@@ -624,6 +634,13 @@ struct Batch {
         launch_merge(x, L);        mark(4);
         launch_islands(x, isl_smem, L);
         launch_pgs_schedule(x, L); mark(5);
+    }
+    void launch_step(const Dev& x) {
+        launch_pre(x);
+        launch_rest(x);
+    }
+    void launch_rest(const Dev& x) {
+        Launch L{n_sms, st};
         for (int s = 0; s < substeps; s++) {
             launch_springs(x, L);                          // impulses before the rows read the velocities
             launch_rows(x, s == 0, s == substeps - 1, L);
@@ -653,7 +670,7 @@ struct Batch {
         const int fit = pgs_big_blocks_per_sm(dv_cap);
         pgs_blocks = n_sms * (per_sm > 0 ? std::min(per_sm, fit) : fit);
         d[0].big_rows = d[1].big_rows = big_rows;
-        for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        drop_graphs();
         build_graphs();
     }
     // whole device state (one arena) copied aside and back, so that trial
@@ -686,7 +703,7 @@ struct Batch {
             audit = nullptr;
         }
         d[0].audit = d[1].audit = audit;
-        for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        drop_graphs();
         build_graphs();
     }
     void read_audit(double* out) {
@@ -696,22 +713,30 @@ struct Batch {
     }
 
     void build_graphs() {
-        for (int p = 0; p < 2; p++) {
-            cudaGraph_t g;
-            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            launch_step(d[p]);
-            CK(cudaStreamEndCapture(st, &g));
-            CK(cudaGraphInstantiate(&graph[p], g, 0));
-            cudaGraphDestroy(g);
-        }
+        if (!pre_done) CK(cudaEventCreateWithFlags(&pre_done, cudaEventDisableTiming));
+        for (int p = 0; p < 2; p++)
+            for (int half = 0; half < 2; half++) {
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                if (half == 0) launch_pre(d[p]);
+                else launch_rest(d[p]);
+                CK(cudaStreamEndCapture(st, &g));
+                CK(cudaGraphInstantiate(half == 0 ? &graph_pre[p] : &graph_rest[p], g, 0));
+                cudaGraphDestroy(g);
+            }
     }
 
-    void step(int n, bool use_graph = true) {
-        for (int i = 0; i < n; i++) {
-            if (use_graph) CK(cudaGraphLaunch(graph[parity], st));
-            else launch_step(d[parity]);
-            parity ^= 1;
-        }
+    // one step from the graphs; `after` (may be null): the step's first half
+    // waits for that event (another part's first half of the same step)
+    void step_one(cudaEvent_t after) {
+        if (after) CK(cudaStreamWaitEvent(st, after, 0));
+        CK(cudaGraphLaunch(graph_pre[parity], st));
+        CK(cudaEventRecord(pre_done, st));
+        CK(cudaGraphLaunch(graph_rest[parity], st));
+        parity ^= 1;
+    }
+    void step(int n) {
+        for (int i = 0; i < n; i++) step_one(nullptr);
     }
 
     int check_status() {
@@ -930,15 +955,24 @@ static int contact_tri(const World& w, uint32_t b1, uint32_t b2, uint64_t cid) {
     return (i << 8) | j;
 }
 
-static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int pgs_per_sm = 0) {
+// `rank` >= 0: the batch is part `rank` of a batch cut into parts, and its
+// streams take the device's greatest priority lowered by `rank` (a graph
+// launched into a stream runs at that stream's priority), so the block
+// scheduler serves the part holding the largest worlds first and their
+// serial solver chains start as early as the step allows.  Priorities order
+// the work, never its results.
+static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int pgs_per_sm = 0, int rank = -1) {
     auto B = std::make_unique<Batch>();
     B->n_worlds = (int)worlds.size();
     B->substeps = worlds.empty() ? 1 : worlds[0]->p.substeps;
     int dev = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&B->n_sms, cudaDevAttrMultiProcessorCount, dev));
-    CK(cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&B->side, cudaStreamNonBlocking));
+    int prio_least = 0, prio_greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+    const int prio = rank < 0 ? prio_least : std::min(prio_least, prio_greatest + rank);
+    CK(cudaStreamCreateWithPriority(&B->st, cudaStreamNonBlocking, prio));
+    CK(cudaStreamCreateWithPriority(&B->side, cudaStreamNonBlocking, prio));
     CK(cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&B->join, cudaEventDisableTiming));
     CK(cudaEventCreate(&B->ev0));
@@ -1928,6 +1962,8 @@ struct Schedule {
     int first_share = 100;  // percent of the bodies in the first part (the largest worlds)
     int rest_per_sm = 0;    // chain workers per SM of the later parts (0 = as many as fit)
     int big_rows = kDefaultBigRows;
+    int second_share = 0;   // three or more parts: percent of the bodies in the second part (0: the rest split evenly)
+    int mid_per_sm = -1;    // three or more parts: chain workers per SM of the second part (-1: rest_per_sm)
 };
 }  // namespace cpgpu
 
@@ -1955,6 +1991,7 @@ struct cpgpu_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr;
     std::vector<cudaEvent_t> done;        // per part
     Schedule sched;                       // the schedule the batch was built for
+    bool stagger = true;                  // step_parts: the parts' first halves in order (CPGPU_BATCH_STAGGER=0: concurrent)
     bool tuned = false;                   // chosen by the autotuner (now or from its cache)
     double tuned_ms = -1, default_ms = -1;   // per step, measured when tuned here
     std::vector<World*> worlds;           // the worlds, in batch order (their host mirrors)
@@ -1994,9 +2031,26 @@ struct cpgpu_batch {
         ev0 = o.ev0; ev1 = o.ev1; fork = o.fork; o.ev0 = o.ev1 = o.fork = nullptr;
         done = std::move(o.done); o.done.clear();
         sched = o.sched;   // the worlds, pins and versions stay this batch's
+        stagger = o.stagger;
     }
     Batch& part(int p) { return *parts[p]; }
     cudaStream_t st0() { return parts[0]->st; }
+    // n steps of every part from the graphs.  Over several steps
+    // (staggered, the default) part p's first half of each step (gravity to
+    // the PGS schedule) waits for part p-1's, so the parts holding the
+    // largest worlds reach their serial solver chains without the other
+    // parts' pair, narrowphase and island kernels competing for the SMs; the
+    // chains and second halves overlap freely, and the parts drift apart
+    // over the steps.  A single step, which the caller waits for, runs the
+    // parts fully concurrently: its end is the last part's, which the stagger
+    // would delay.  Worlds never interact: the order changes no result.
+    void step_parts(int n) {
+        if (parts.size() > 1 && stagger && n > 1)
+            for (int i = 0; i < n; i++)
+                for (size_t p = 0; p < parts.size(); p++) parts[p]->step_one(p > 0 ? parts[p - 1]->pre_done : nullptr);
+        else
+            for (auto& p : parts) p->step(n);   // graph launches only: the parts run concurrently
+    }
     // every part's stream waits for what part 0's stream has issued so far
     void fan_out() {
         CK(cudaEventRecord(fork, st0()));
@@ -2888,8 +2942,10 @@ int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
 // most 2 chain workers per SM (the parts' solver kernels share the SMs'
 // shared memory; measured on 4,096 worlds of 8-512 bodies: 23.7 -> 21.3 ms
 // per step with the parts, 21.5 -> 20.3 ms with the cap); otherwise one
-// part.  CPGPU_BATCH_PARTS, CPGPU_BATCH_FIRST_SHARE (percent) and
-// CPGPU_PGS_REST_PER_SM override it.
+// part.  CPGPU_BATCH_PARTS, CPGPU_BATCH_FIRST_SHARE (percent),
+// CPGPU_BATCH_SECOND_SHARE (percent, three or more parts),
+// CPGPU_PGS_REST_PER_SM and CPGPU_PGS_MID_PER_SM (the second part's chain
+// workers per SM, three or more parts) override it.
 static std::vector<int> size_order(const std::vector<World*>& ws) {
     std::vector<int> order(ws.size());
     for (size_t i = 0; i < ws.size(); i++) order[i] = (int)i;
@@ -2906,6 +2962,10 @@ static Schedule default_schedule(const std::vector<World*>& ws) {
     const int first_dflt = (skewed && S.parts == 2) ? 20 : 100 / S.parts;
     S.first_share = S.parts > 1 ? std::max(1, std::min(99, env_int("CPGPU_BATCH_FIRST_SHARE", first_dflt))) : 100;
     S.rest_per_sm = S.parts > 1 ? env_int("CPGPU_PGS_REST_PER_SM", 2) : 0;
+    if (S.parts > 2) {
+        S.second_share = std::max(0, std::min(99 - S.first_share, env_int("CPGPU_BATCH_SECOND_SHARE", 0)));
+        S.mid_per_sm = env_int("CPGPU_PGS_MID_PER_SM", -1);
+    }
     return S;
 }
 
@@ -2919,7 +2979,13 @@ static std::vector<std::vector<int>> batch_partition(const std::vector<World*>& 
     int64_t total = 0;
     for (World* w : ws) total += (int64_t)w->bodies.size();
     const int first = S.first_share;
-    auto bound = [&](int q) { return P > 1 ? total * (first * (P - 1) + (100 - first) * q) / (100 * (P - 1)) : total; };
+    const int second = P > 2 ? S.second_share : 0;
+    auto bound = [&](int q) {
+        if (P == 1) return total;
+        if (second > 0 && q >= 1)   // the first two parts by their shares, the later ones split the rest
+            return total * ((first + second) * (P - 2) + (100 - first - second) * (q - 1)) / (100 * (P - 2));
+        return total * (first * (P - 1) + (100 - first) * q) / (100 * (P - 1));
+    };
     std::vector<std::vector<int>> parts(P);
     int64_t acc = 0;
     int p = 0;
@@ -2969,7 +3035,9 @@ static void tune_file_load() {
     if (!f) return;
     char key[256];
     Schedule S;
-    while (std::fscanf(f, "%255s %d %d %d %d", key, &S.parts, &S.first_share, &S.rest_per_sm, &S.big_rows) == 5) g_tuned[key] = S;
+    while (std::fscanf(f, "%255s %d %d %d %d %d %d", key, &S.parts, &S.first_share, &S.rest_per_sm, &S.big_rows,
+                       &S.second_share, &S.mid_per_sm) == 7)
+        g_tuned[key] = S;
     std::fclose(f);
 }
 
@@ -2978,7 +3046,8 @@ static void tune_file_save(const std::string& key, const Schedule& S) {
     if (!path) return;
     FILE* f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "%s %d %d %d %d\n", key.c_str(), S.parts, S.first_share, S.rest_per_sm, S.big_rows);
+    std::fprintf(f, "%s %d %d %d %d %d %d\n", key.c_str(), S.parts, S.first_share, S.rest_per_sm, S.big_rows, S.second_share,
+                 S.mid_per_sm);
     std::fclose(f);
 }
 
@@ -2987,6 +3056,7 @@ static std::unique_ptr<cpgpu_batch> make_batch(const std::vector<World*>& ws, co
     const int n = (int)ws.size();
     auto b = std::make_unique<cpgpu_batch>();
     b->sched = S;
+    b->stagger = env_int("CPGPU_BATCH_STAGGER", 1) != 0;
     b->worlds = ws;
     b->part_of.resize(n);
     b->local_of.resize(n);
@@ -3011,7 +3081,9 @@ static std::unique_ptr<cpgpu_batch> make_batch(const std::vector<World*>& ws, co
         // SMs' shared memory: the later parts take at most rest_per_sm chain
         // workers per SM so that the first part's longest chains are not
         // queued behind them
-        b->parts.push_back(build_batch(sub, p == 0 ? 0 : (parts.size() > 1 ? S.rest_per_sm : 0)));
+        const int rank = parts.size() > 1 && env_int("CPGPU_BATCH_PRIORITY", 1) ? (int)p : -1;
+        const int per_sm = p == 0 || parts.size() == 1 ? 0 : (p == 1 && S.mid_per_sm >= 0 ? S.mid_per_sm : S.rest_per_sm);
+        b->parts.push_back(build_batch(sub, per_sm, rank));
         if (S.big_rows != kDefaultBigRows) b->parts.back()->set_schedule(b->parts.back()->pgs_per_sm, S.big_rows);
         int* d_rows = nullptr;
         CK(cudaMalloc(&d_rows, sizeof(int) * std::max<size_t>(rows.size(), 1)));
@@ -3046,7 +3118,8 @@ int cpgpu_batch_create(cpgpu_world* const* worlds, int n, cpgpu_batch** out) {
         bool tuned = false;
         // a schedule set through the environment takes precedence over the cache
         const bool env_set = std::getenv("CPGPU_BATCH_PARTS") || std::getenv("CPGPU_BATCH_FIRST_SHARE") ||
-                             std::getenv("CPGPU_PGS_REST_PER_SM");
+                             std::getenv("CPGPU_BATCH_SECOND_SHARE") || std::getenv("CPGPU_PGS_REST_PER_SM") ||
+                             std::getenv("CPGPU_PGS_MID_PER_SM");
         if (!env_set) {
             std::lock_guard<std::mutex> lock(g_tune_mutex);
             tune_file_load();
@@ -3066,7 +3139,7 @@ int cpgpu_batch_create(cpgpu_world* const* worlds, int n, cpgpu_batch** out) {
 static double time_steps(cpgpu_batch* b, int n) {
     CK(cudaEventRecord(b->ev0, b->st0()));
     b->fan_out();
-    for (auto& p : b->parts) p->step(n);
+    b->step_parts(n);
     b->fan_in();
     CK(cudaEventRecord(b->ev1, b->st0()));
     CK(cudaEventSynchronize(b->ev1));
@@ -3074,6 +3147,17 @@ static double time_steps(cpgpu_batch* b, int n) {
     CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     for (auto& p : b->parts) p->check_status();
     return ms;
+}
+
+// The autotuner's score of a schedule, ms per step: the mean of a step inside
+// a run of n steps (the parts drift apart, staggered) and a step run alone and
+// waited for (the parts concurrent; a caller that reads the state back every
+// step sees this one).  A schedule can favour one and cost the other.
+static double tune_score(cpgpu_batch* b, int n) {
+    const double run = time_steps(b, n) / n;
+    double single = 0;
+    for (int i = 0; i < n; i++) single += time_steps(b, 1);
+    return 0.5 * (run + single / n);
 }
 
 // Autotuner: candidate schedules (one, two or three parts with several
@@ -3107,23 +3191,28 @@ static void tune_batch(cpgpu_batch* b, int trial_steps) {
     }
     const Schedule dflt = default_schedule(ws);
     std::vector<Schedule> layouts{dflt};
-    auto add = [&](int parts, int share) {
+    auto add = [&](int parts, int share, int second) {
         if (parts > (int)ws.size()) return;
-        for (const Schedule& x : layouts) if (x.parts == parts && (parts == 1 || x.first_share == share)) return;
+        for (const Schedule& x : layouts)
+            if (x.parts == parts && (parts == 1 || (x.first_share == share && x.second_share == second))) return;
         Schedule sch;
         sch.parts = parts; sch.first_share = parts > 1 ? share : 100;
+        sch.second_share = parts > 2 ? second : 0;
         layouts.push_back(sch);
     };
-    add(1, 100);
-    for (int share : {10, 20, 30}) add(2, share);
-    add(3, 20);
+    add(1, 100, 0);
+    for (int share : {10, 20, 30}) add(2, share, 0);
+    // graduated parts (the largest worlds' few percent first), whose
+    // staggered first halves let the longest chains start soonest
+    add(3, 5, 20);
+    add(4, 3, 12);
     std::unique_ptr<cpgpu_batch> best, dcand;   // dcand: the hand-set default's layout, kept for the final check
     double best_ms = 1e300, dflt_ms = -1;
     Schedule dcfg = dflt;
     for (const Schedule& L : layouts) {
         std::unique_ptr<cpgpu_batch> cand = make_batch(ws, L);
         for (auto& p : cand->parts) p->snapshot();
-        const bool dflt_layout = L.parts == dflt.parts && L.first_share == dflt.first_share;
+        const bool dflt_layout = L.parts == dflt.parts && L.first_share == dflt.first_share && L.second_share == dflt.second_share;
         const std::vector<int> per_sms = cand->parts.size() > 1 ? std::vector<int>{1, 2, 3} : std::vector<int>{0};
         Schedule cbest = cand->sched;
         double cbest_ms = 1e300;
@@ -3131,7 +3220,7 @@ static void tune_batch(cpgpu_batch* b, int trial_steps) {
             for (int big : {32, 48, 96}) {
                 for (size_t p = 0; p < cand->parts.size(); p++) cand->parts[p]->set_schedule(p == 0 ? 0 : per_sm, big);
                 time_steps(cand.get(), 1);   // warm-up
-                const double ms = time_steps(cand.get(), T) / T;
+                const double ms = tune_score(cand.get(), T);
                 for (auto& p : cand->parts) p->restore(false);
                 const bool is_dflt = dflt_layout && big == dflt.big_rows &&
                                      (cand->parts.size() == 1 || per_sm == dflt.rest_per_sm);
@@ -3147,7 +3236,8 @@ static void tune_batch(cpgpu_batch* b, int trial_steps) {
         cand->sched = cbest;
         if (cbest_ms < best_ms) {
             best_ms = cbest_ms;
-            if (best && !dcand && best->sched.parts == dflt.parts && best->sched.first_share == dflt.first_share)
+            if (best && !dcand && best->sched.parts == dflt.parts && best->sched.first_share == dflt.first_share &&
+                best->sched.second_share == dflt.second_share)
                 dcand = std::move(best);
             best = std::move(cand);
         } else if (dflt_layout) {
@@ -3160,13 +3250,13 @@ static void tune_batch(cpgpu_batch* b, int trial_steps) {
     if (dcand && dflt_ms > 0) {
         const int T2 = std::max(2 * T, 8);
         time_steps(best.get(), 1);
-        const double mb = time_steps(best.get(), T2) / T2;
+        const double mb = tune_score(best.get(), T2);
         for (auto& p : best->parts) p->restore(false);
         for (size_t p = 0; p < dcand->parts.size(); p++)
             dcand->parts[p]->set_schedule(p == 0 ? 0 : dcfg.rest_per_sm, dcfg.big_rows);
         dcand->sched = dcfg;
         time_steps(dcand.get(), 1);
-        const double md = time_steps(dcand.get(), T2) / T2;
+        const double md = tune_score(dcand.get(), T2);
         for (auto& p : dcand->parts) p->restore(false);
         if (md <= mb) { best = std::move(dcand); best_ms = md; dflt_ms = md; }
         else { best_ms = mb; dflt_ms = md; }
@@ -3206,7 +3296,7 @@ int cpgpu_batch_schedule(cpgpu_batch* b, int* sched, double* times) {
     if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
     if (sched) {
         sched[0] = b->sched.parts; sched[1] = b->sched.first_share; sched[2] = b->sched.rest_per_sm;
-        sched[3] = b->sched.big_rows; sched[4] = b->tuned ? 1 : 0;
+        sched[3] = b->sched.big_rows; sched[4] = b->tuned ? 1 : 0; sched[5] = b->sched.second_share;
     }
     if (times) { times[0] = b->tuned_ms; times[1] = b->default_ms; }
     return CPGPU_OK;
@@ -3221,7 +3311,7 @@ static int batch_check(cpgpu_batch* b) {
 int cpgpu_batch_step(cpgpu_batch* b, int n) {
     if (!b) return fail(CPGPU_ERR_INVALID_ARG, "null batch");
     return guarded([&] {
-        for (auto& p : b->parts) p->step(n);   // graph launches only: the parts run concurrently
+        b->step_parts(n);
         return batch_check(b);
     });
 }
@@ -3333,58 +3423,75 @@ int cpgpu_batch_write_state(cpgpu_batch* b, const float* in) {
     });
 }
 
-// Stage times of n steps, part by part (each part's stages timed alone and
-// summed over the parts: the work of each stage, not the overlapped step)
-// Stage times of n steps launched stage by stage (no graph) with the parts
-// running concurrently, one step at a time (every part's stream waits for
-// the previous step of all parts): CUDA events on each part's stream mark its
-// stages, every mark is timed against one start event, and a stage's time in
-// a step is its window over the parts, from the first part entering it to the
-// last part leaving it.  The windows lie inside the step, so a stage's time
-// never exceeds the step's.
+// n steps launched stage by stage with an event after every stage on every
+// part's stream, one step at a time (every part's stream waits for the
+// previous step of all parts), the parts concurrent as in a single step;
+// `each(at)` is called after each step with at(p, m) = ms from the step's
+// start to mark m of part p.
+using StageClock = std::function<double(size_t, int)>;
+static void profile_steps(cpgpu_batch* b, int n_steps, const std::function<void(const StageClock&)>& each) {
+    const size_t np = b->parts.size();
+    std::vector<std::vector<cudaEvent_t>> ev(np);
+    for (size_t p = 0; p < np; p++) {
+        ev[p].resize(7 + 3 * b->parts[p]->substeps);
+        for (auto& e : ev[p]) CK(cudaEventCreate(&e));
+    }
+    for (int i = 0; i < n_steps; i++) {
+        CK(cudaEventRecord(b->ev0, b->st0()));
+        b->fan_out();
+        for (size_t p = 0; p < np; p++) {
+            Batch& B = *b->parts[p];
+            B.marks = &ev[p];
+            B.launch_pre(B.d[B.parity]);
+            CK(cudaEventRecord(B.pre_done, B.st));
+            B.launch_rest(B.d[B.parity]);
+            B.marks = nullptr;
+            CK(cudaGetLastError());   // a launch refused here would leave its stage untimed
+            B.parity ^= 1;
+        }
+        b->fan_in();
+        CK(cudaEventRecord(b->ev1, b->st0()));
+        CK(cudaEventSynchronize(b->ev1));
+        const StageClock at = [&](size_t p, int m) {
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, b->ev0, ev[p][m]));
+            return (double)ms;
+        };
+        each(at);
+    }
+    for (auto& v : ev)
+        for (auto& e : v) cudaEventDestroy(e);
+}
+
 int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* counts) {
     if (!b || !stage_ms) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
     return guarded([&] {
         for (int k = 0; k < CPGPU_N_STAGES; k++) stage_ms[k] = 0;
         if (counts) counts[0] = counts[1] = counts[2] = 0;
         const size_t np = b->parts.size();
-        std::vector<std::vector<cudaEvent_t>> ev(np);
-        for (size_t p = 0; p < np; p++) {
-            ev[p].resize(7 + 3 * b->parts[p]->substeps);
-            for (auto& e : ev[p]) CK(cudaEventCreate(&e));
-        }
-        for (int i = 0; i < n_steps; i++) {
-            CK(cudaEventRecord(b->ev0, b->st0()));
-            b->fan_out();
-            for (size_t p = 0; p < np; p++) {
-                Batch& B = *b->parts[p];
-                B.marks = &ev[p];
-                B.launch_step(B.d[B.parity]);
-                B.marks = nullptr;
-                CK(cudaGetLastError());   // a launch refused here would leave its stage untimed
-                B.parity ^= 1;
-            }
-            b->fan_in();
-            CK(cudaEventRecord(b->ev1, b->st0()));
-            CK(cudaEventSynchronize(b->ev1));
-            auto at = [&](size_t p, int m) { float ms = 0; CK(cudaEventElapsedTime(&ms, b->ev0, ev[p][m])); return (double)ms; };
+        const int S = b->parts[0]->substeps;   // the parts share the substep count
+        profile_steps(b, n_steps, [&](const StageClock& at) {
+            // the stage's time in the step: the length of the union of the
+            // parts' intervals in it (a part's stages are in stream order)
             auto window = [&](auto first_mark, auto last_mark) {
-                double lo = 1e300, hi = -1e300;
-                for (size_t p = 0; p < np; p++) { lo = std::min(lo, at(p, first_mark(p))); hi = std::max(hi, at(p, last_mark(p))); }
-                return hi > lo ? hi - lo : 0.0;
+                std::vector<std::pair<double, double>> iv;
+                for (size_t p = 0; p < np; p++) iv.push_back({at(p, first_mark(p)), at(p, last_mark(p))});
+                std::sort(iv.begin(), iv.end());
+                double total = 0, lo = -1e300, hi = -1e300;
+                for (const auto& x : iv) {
+                    if (x.first > hi) { total += std::max(0.0, hi - lo); lo = x.first; hi = x.second; }
+                    else hi = std::max(hi, x.second);
+                }
+                return total + std::max(0.0, hi - lo);
             };
             for (int k = 0; k < 5; k++) stage_ms[k] += window([&](size_t) { return k; }, [&](size_t) { return k + 1; });
-            // per-substep stages: the parts share the substep count
-            const int S = b->parts[0]->substeps;
             for (int s2 = 0; s2 < S; s2++) {
                 stage_ms[5] += window([&](size_t) { return 5 + 3 * s2; }, [&](size_t) { return 6 + 3 * s2; });
                 stage_ms[6] += window([&](size_t) { return 6 + 3 * s2; }, [&](size_t) { return 7 + 3 * s2; });
                 stage_ms[7] += window([&](size_t) { return 7 + 3 * s2; }, [&](size_t) { return 8 + 3 * s2; });
             }
             stage_ms[8] += window([&](size_t) { return 5 + 3 * S; }, [&](size_t) { return 6 + 3 * S; });
-        }
-        for (auto& v : ev)
-            for (auto& e : v) cudaEventDestroy(e);
+        });
         if (counts)
             for (auto& part : b->parts) {
                 Batch& B = *part;
@@ -3399,6 +3506,23 @@ int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* 
     });
 }
 
+int cpgpu_batch_timeline(cpgpu_batch* b, int n_steps, double* out, int cap, int* n_parts, int* n_marks) {
+    if (!b || !n_parts || !n_marks) return fail(CPGPU_ERR_INVALID_ARG, "null argument");
+    return guarded([&] {
+        const int np = (int)b->parts.size(), nm = 7 + 3 * b->parts[0]->substeps;
+        *n_parts = np;
+        *n_marks = nm;
+        if (!out || n_steps < 1) return CPGPU_OK;
+        if (cap < np * nm) throw ApiFail{CPGPU_ERR_INVALID_ARG, "timeline buffer too small"};
+        for (int k = 0; k < np * nm; k++) out[k] = 0;
+        profile_steps(b, n_steps, [&](const StageClock& at) {
+            for (int p = 0; p < np; p++)
+                for (int m = 0; m < nm; m++) out[p * nm + m] += at(p, m) / n_steps;
+        });
+        return batch_check(b);
+    });
+}
+
 // Device time of n steps of the batch: CUDA events on part 0's stream, which
 // the other parts' streams join before the start and after the last step.
 int cpgpu_batch_step_timed(cpgpu_batch* b, int n, double* device_ms) {
@@ -3406,7 +3530,7 @@ int cpgpu_batch_step_timed(cpgpu_batch* b, int n, double* device_ms) {
     return guarded([&] {
         CK(cudaEventRecord(b->ev0, b->st0()));
         b->fan_out();
-        for (auto& p : b->parts) p->step(n);
+        b->step_parts(n);
         b->fan_in();
         CK(cudaEventRecord(b->ev1, b->st0()));
         CK(cudaEventSynchronize(b->ev1));

@@ -454,7 +454,7 @@ __global__ void k_pgs_small(Dev d) {
 }
 
 // ---- large islands: one warp per island, rows streamed through shared memory
-constexpr int kRingSlots = 4;
+constexpr int kRingSlots = 6;
 constexpr int kChunkRows = 16;
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
@@ -595,14 +595,15 @@ __device__ __forceinline__ bool big_chain(const Dev& d, RowBlock* ring, uint64_t
     return true;
 }
 
-// blockDim.x == 32; `dv_cap` island bodies fit in the shared Δv area
-__global__ void __launch_bounds__(32) k_pgs_big(Dev d, int dv_cap) {
-    extern __shared__ __align__(16) uint8_t sm[];
+// One warp's solver-chain worker: takes big-island list entries q0, q0+1, ...
+// (below q1) through `counter` and runs each island's chain.  `sm`: the
+// warp's own shared area (mbarriers, row ring, Δv of up to `dv_cap` bodies).
+// False when a bounded wait gave up (the status is set).
+__device__ bool big_worker(const Dev& d, int dv_cap, uint8_t* sm, int* counter, int q0, int q1) {
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm);
     RowBlock* ring = reinterpret_cast<RowBlock*>(sm + 64);
     float4* sdv = reinterpret_cast<float4*>(sm + 64 + kRingSlots * kChunkRows * sizeof(RowBlock));
-    __shared__ int sh_island;
-    const int lane = threadIdx.x;
+    const int lane = threadIdx.x & 31;
     if (lane == 0)
         for (int k = 0; k < kRingSlots; k++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(&bars[k])), "r"(1) : "memory");
@@ -610,13 +611,11 @@ __global__ void __launch_bounds__(32) k_pgs_big(Dev d, int dv_cap) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     __syncwarp();
     uint32_t phase = 0;   // bit k: parity of slot k
-    const int n_big = d.sched[0];
     while (true) {
-        if (lane == 0) sh_island = atomicAdd(&d.sched[2], 1);
-        __syncwarp();
-        const int q = sh_island;
-        __syncwarp();
-        if (q >= n_big) break;
+        int q = 0;
+        if (lane == 0) q = q0 + atomicAdd(counter, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= q1) break;
         const int i = d.big_list[q];
         const int rs = d.g_isl_row_start[i], rc = d.g_isl_row_count[i];
         const int bs = d.g_isl_body_start[i], bc = d.g_isl_body_count[i];
@@ -631,11 +630,18 @@ __global__ void __launch_bounds__(32) k_pgs_big(Dev d, int dv_cap) {
             if (!ok) atomicOr(d.status, ST_TIMEOUT);
         }
         ok = __shfl_sync(0xffffffffu, ok, 0);
-        if (!ok) return;
+        if (!ok) return false;
         __syncwarp();
         island_finish(d, rs, rc, bs, bc, dv, lane, 32);
         __syncwarp();
     }
+    return true;
+}
+
+// blockDim.x == 32; `dv_cap` island bodies fit in the shared Δv area
+__global__ void __launch_bounds__(32) k_pgs_big(Dev d, int dv_cap) {
+    extern __shared__ __align__(16) uint8_t sm[];
+    big_worker(d, dv_cap, sm, &d.sched[2], 0, d.sched[0]);
 }
 
 // HolonomicSystem::computeAndApplyImpulses (HolonomicBlockSolver.cpp:319-378)

@@ -330,30 +330,39 @@ int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
  * the batch): the autotuner re-packs the batch from their descriptions. */
 int cpgpu_batch_create(cpgpu_world* const* worlds, int n_worlds, cpgpu_batch** out);
 /* Autotuner (no counterpart in the reference): re-chooses the batch's
- * schedule by timing from its current state.  Candidate schedules -- one, two
- * or three parts stepped concurrently with several shares of the bodies in the
- * part of the largest worlds; for each, the later parts' solver-chain workers
- * per SM and the island size from which an island takes the warp-per-island
- * solver -- are built from the current state, timed on `trial_steps` steps,
- * the state restored after each trial, and the fastest adopted; the batch
- * continues from exactly the state it had, and the worlds' own state is not
- * touched.  CPGPU_ERR_INVALID_ARG if a world was changed through the API
- * after the batch was made from it.  Tune from a representative state
- * (e.g. after some steps: before bodies touch, a step costs far less).  The
- * choice is cached per world-size histogram (log2 bins of the body counts),
- * for the process and, when the environment variable CPGPU_TUNE_FILE names a
- * file, there; cpgpu_batch_create uses a cached choice for a matching
- * histogram unless CPGPU_BATCH_PARTS, CPGPU_BATCH_FIRST_SHARE or
- * CPGPU_PGS_REST_PER_SM is set.  Every world steps exactly as it does alone
- * under any schedule. */
+ * schedule by timing from its current state.  Candidate schedules -- one to
+ * four parts with several shares of the bodies in the parts of the largest
+ * worlds; for each, the later parts' solver-chain workers per SM and the
+ * island size from which an island takes the warp-per-island solver -- are
+ * built from the current state, timed on `trial_steps` steps run together
+ * and as many steps run one at a time (the score is the mean of the two
+ * per-step times), the state restored after each trial, and the fastest
+ * adopted; the batch continues from exactly the state it had, and the
+ * worlds' own state is not touched.  In calls of several steps, each part's
+ * pair, narrowphase and island stages follow those of the part before it
+ * (the parts of the largest worlds reach their solver chains first) and the
+ * rest of the parts' steps run concurrently; a single step runs the parts
+ * fully concurrently.  CPGPU_ERR_INVALID_ARG if a world was changed through
+ * the API after the batch was made from it.  Tune from a representative
+ * state (e.g. after some steps: before bodies touch, a step costs far
+ * less).  The choice is cached per world-size histogram (log2 bins of the
+ * body counts), for the process and, when the environment variable
+ * CPGPU_TUNE_FILE names a file, there; cpgpu_batch_create uses a cached
+ * choice for a matching histogram unless CPGPU_BATCH_PARTS,
+ * CPGPU_BATCH_FIRST_SHARE, CPGPU_BATCH_SECOND_SHARE, CPGPU_PGS_REST_PER_SM or
+ * CPGPU_PGS_MID_PER_SM is set (CPGPU_BATCH_STAGGER=0 runs the parts fully
+ * concurrently in calls of several steps too).  Every world steps exactly
+ * as it does alone under any schedule. */
 int cpgpu_batch_tune(cpgpu_batch* b, int trial_steps);
 /* cpgpu_batch_create followed by cpgpu_batch_tune from the worlds' state. */
 int cpgpu_batch_create_tuned(cpgpu_world* const* worlds, int n_worlds, int trial_steps, cpgpu_batch** out);
-/* The batch's schedule: sched[5] = parts, first-part share of the bodies (%),
+/* The batch's schedule: sched[6] = parts, first-part share of the bodies (%),
  * chain workers per SM of the later parts (0 = as many as fit), big-island row
- * threshold, 1 if chosen by the autotuner; times[2] = the tuned schedule's and
- * the hand-set schedule's device ms per step measured while tuning (-1 when
- * not tuned here).  Either pointer may be NULL. */
+ * threshold, 1 if chosen by the autotuner, second-part share (%, 0: the
+ * parts after the first split the rest evenly); times[2] = the tuned schedule's and
+ * the hand-set schedule's scores measured while tuning (device ms per step,
+ * the mean of a step inside a run of steps and a step run alone; -1 when not
+ * tuned here).  Either pointer may be NULL. */
 int cpgpu_batch_schedule(cpgpu_batch* b, int* sched, double* times);
 int cpgpu_batch_destroy(cpgpu_batch* b);
 int cpgpu_batch_step(cpgpu_batch* b, int n_steps);
@@ -378,11 +387,20 @@ int cpgpu_batch_write_state(cpgpu_batch* b, const float* in);
  * of the batch concurrent, one step at a time), for the roofline: stage_ms
  * receives CPGPU_N_STAGES totals in the order gravity, pairs, narrowphase,
  * merge, islands, rows, pgs, integrate, geometry, each step's stage time
- * being the window from the first part entering the stage to the last part
- * leaving it (so no stage exceeds the step); counts (may be NULL) receives
- * the last step's pairs, contacts and islands summed over the parts. */
+ * being the time some part of the batch spends in the stage (the union of
+ * the parts' intervals in it, so no stage exceeds the step); counts (may be
+ * NULL) receives the last step's pairs, contacts and islands summed over the
+ * parts. */
 #define CPGPU_N_STAGES 9
 int cpgpu_batch_profile(cpgpu_batch* b, int n_steps, double* stage_ms, int64_t* counts);
+/* The same stage-by-stage steps (one at a time, the parts concurrent),
+ * reported per batch part: out[p * n_marks + m] receives the mean ms from
+ * the step's start to mark m of part p: mark 0 the part's start, marks 1-5
+ * the ends of gravity, pairs, narrowphase, merge and islands with the PGS
+ * schedule, then per substep the ends of rows, PGS and integration, and last
+ * the end of geometry (n_marks = 7 + 3 * substeps).  With out == NULL only
+ * n_parts and n_marks are written; cap is out's length in doubles. */
+int cpgpu_batch_timeline(cpgpu_batch* b, int n_steps, double* out, int cap, int* n_parts, int* n_marks);
 /* Number of kernel launches one step of the batch issues. */
 int cpgpu_batch_launches_per_step(cpgpu_batch* b, int* n);
 

@@ -32,15 +32,23 @@ def _build(scs):
     return ws
 
 
-def test_schedules_give_identical_results(monkeypatch):
+@pytest.mark.parametrize("stagger", [1, 0])
+def test_schedules_give_identical_results(monkeypatch, stagger):
+    """Parts stepped with staggered first halves (the default) or fully
+    concurrently, graduated shares, per-part chain workers: the same bits."""
     scs = _worlds(600)
     ref = None
-    for parts, share, per_sm in ((1, 100, 0), (2, 20, 2), (3, 30, 1)):
+    monkeypatch.setenv("CPGPU_BATCH_STAGGER", str(stagger))
+    for parts, share, second, per_sm, mid in ((1, 100, 0, 0, -1), (2, 20, 0, 2, -1), (3, 30, 0, 1, -1),
+                                              (3, 5, 20, 3, 0), (4, 3, 12, 2, 4)):
         monkeypatch.setenv("CPGPU_BATCH_PARTS", str(parts))
         monkeypatch.setenv("CPGPU_BATCH_FIRST_SHARE", str(share))
+        monkeypatch.setenv("CPGPU_BATCH_SECOND_SHARE", str(second))
         monkeypatch.setenv("CPGPU_PGS_REST_PER_SM", str(per_sm))
+        monkeypatch.setenv("CPGPU_PGS_MID_PER_SM", str(mid))
         b = cg.Batch(_build(scs))
-        assert b.schedule()["parts"] == parts
+        sch = b.schedule()
+        assert sch["parts"] == parts and sch["second_share_pct"] == (second if parts > 2 else 0)
         b.step(25)
         st = [b.state(i) for i in range(0, 600, 37)]
         b.close()
@@ -96,3 +104,23 @@ def test_tuning_leaves_the_worlds_alone_and_refuses_changed_ones():
     b2.tune(1)
     b2.step(2)
     b2.close()
+
+
+def test_timeline_marks_are_ordered_per_part(monkeypatch):
+    """cpgpu_batch_timeline: per part, the stage marks of a step in order,
+    and the timed steps advance the batch as plain steps do."""
+    monkeypatch.setenv("CPGPU_BATCH_PARTS", "3")
+    monkeypatch.setenv("CPGPU_BATCH_FIRST_SHARE", "10")
+    monkeypatch.setenv("CPGPU_BATCH_SECOND_SHARE", "30")
+    b = cg.Batch(_build(_worlds(300, seed=6)))
+    b.step(10)
+    tl = b.timeline(3)
+    assert tl.shape == (3, 10)   # 7 + 3 marks of one substep
+    assert np.all(np.diff(tl, axis=1) >= -1e-3)
+    # the timed steps advanced the batch like plain steps
+    ref = cg.Batch(_build(_worlds(300, seed=6)))
+    ref.step(13)
+    for i in range(0, 300, 17):
+        a, c = b.state(i), ref.state(i)
+        for k in a:
+            assert np.array_equal(a[k], c[k]), k
