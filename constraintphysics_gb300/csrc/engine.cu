@@ -1006,7 +1006,12 @@ static std::unique_ptr<Batch> build_batch(const std::vector<World*>& worlds, int
     {
         int max_world = 0;
         for (size_t k = 0; k + 1 < wstart.size(); k++) max_world = std::max(max_world, wstart[k + 1] - wstart[k]);
-        B->dv_cap = std::min(kPgsDvCapMax, std::max(64, max_world));
+        // islands of more bodies keep their Δv in global memory (the same
+        // arithmetic); CPGPU_PGS_DV_CAP lowers the cap, so that a batch of a
+        // few very large worlds does not hold every chain worker's shared area
+        // at the largest world's size
+        const int dv_max = std::max(32, std::min(kPgsDvCapMax, env_int("CPGPU_PGS_DV_CAP", kPgsDvCapMax)));
+        B->dv_cap = std::min(dv_max, std::max(64, max_world));
         B->isl_smem = islands_smem_bytes(max_world);
     }
     std::vector<uint8_t> pool;
@@ -2944,8 +2949,9 @@ int cpgpu_set_joint_state(cpgpu_world* w, const double* impulse, const double* u
 // per step with the parts, 21.5 -> 20.3 ms with the cap); otherwise one
 // part.  CPGPU_BATCH_PARTS, CPGPU_BATCH_FIRST_SHARE (percent),
 // CPGPU_BATCH_SECOND_SHARE (percent, three or more parts),
-// CPGPU_PGS_REST_PER_SM and CPGPU_PGS_MID_PER_SM (the second part's chain
-// workers per SM, three or more parts) override it.
+// CPGPU_PGS_REST_PER_SM, CPGPU_PGS_MID_PER_SM (the second part's chain
+// workers per SM, three or more parts) and CPGPU_PGS_BIG_ROWS (the island
+// rows from which an island takes the warp-per-island solver) override it.
 static std::vector<int> size_order(const std::vector<World*>& ws) {
     std::vector<int> order(ws.size());
     for (size_t i = 0; i < ws.size(); i++) order[i] = (int)i;
@@ -2962,6 +2968,7 @@ static Schedule default_schedule(const std::vector<World*>& ws) {
     const int first_dflt = (skewed && S.parts == 2) ? 20 : 100 / S.parts;
     S.first_share = S.parts > 1 ? std::max(1, std::min(99, env_int("CPGPU_BATCH_FIRST_SHARE", first_dflt))) : 100;
     S.rest_per_sm = S.parts > 1 ? env_int("CPGPU_PGS_REST_PER_SM", 2) : 0;
+    S.big_rows = std::max(1, env_int("CPGPU_PGS_BIG_ROWS", kDefaultBigRows));
     if (S.parts > 2) {
         S.second_share = std::max(0, std::min(99 - S.first_share, env_int("CPGPU_BATCH_SECOND_SHARE", 0)));
         S.mid_per_sm = env_int("CPGPU_PGS_MID_PER_SM", -1);
@@ -3119,7 +3126,7 @@ int cpgpu_batch_create(cpgpu_world* const* worlds, int n, cpgpu_batch** out) {
         // a schedule set through the environment takes precedence over the cache
         const bool env_set = std::getenv("CPGPU_BATCH_PARTS") || std::getenv("CPGPU_BATCH_FIRST_SHARE") ||
                              std::getenv("CPGPU_BATCH_SECOND_SHARE") || std::getenv("CPGPU_PGS_REST_PER_SM") ||
-                             std::getenv("CPGPU_PGS_MID_PER_SM");
+                             std::getenv("CPGPU_PGS_MID_PER_SM") || std::getenv("CPGPU_PGS_BIG_ROWS");
         if (!env_set) {
             std::lock_guard<std::mutex> lock(g_tune_mutex);
             tune_file_load();

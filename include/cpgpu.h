@@ -349,9 +349,11 @@ int cpgpu_batch_create(cpgpu_world* const* worlds, int n_worlds, cpgpu_batch** o
  * body counts), for the process and, when the environment variable
  * CPGPU_TUNE_FILE names a file, there; cpgpu_batch_create uses a cached
  * choice for a matching histogram unless CPGPU_BATCH_PARTS,
- * CPGPU_BATCH_FIRST_SHARE, CPGPU_BATCH_SECOND_SHARE, CPGPU_PGS_REST_PER_SM or
- * CPGPU_PGS_MID_PER_SM is set (CPGPU_BATCH_STAGGER=0 runs the parts fully
- * concurrently in calls of several steps too).  Every world steps exactly
+ * CPGPU_BATCH_FIRST_SHARE, CPGPU_BATCH_SECOND_SHARE, CPGPU_PGS_REST_PER_SM,
+ * CPGPU_PGS_MID_PER_SM or CPGPU_PGS_BIG_ROWS is set (CPGPU_BATCH_STAGGER=0
+ * runs the parts fully concurrently in calls of several steps too;
+ * CPGPU_PGS_DV_CAP caps the island bodies whose solver Δv stays in shared
+ * memory, 1536 by default).  Every world steps exactly
  * as it does alone under any schedule. */
 int cpgpu_batch_tune(cpgpu_batch* b, int trial_steps);
 /* cpgpu_batch_create followed by cpgpu_batch_tune from the worlds' state. */
