@@ -2333,6 +2333,8 @@ int cpgpu_body_mesh(cpgpu_world* w, const double* points, int n_points, const in
     return guarded([&] {
         if (!fixed) throw ApiFail{CPGPU_ERR_UNSUPPORTED, "kinematic meshes are not implemented on the device path"};
         if (!points || !tris || n_points < 3 || n_tris < 1) throw ApiFail{CPGPU_ERR_INVALID_ARG, "mesh needs >= 3 points and >= 1 triangle"};
+        // a contact carries the triangle id in 24 bits (a union primitive's index above it)
+        if (n_tris >= (1 << 24)) throw ApiFail{CPGPU_ERR_INVALID_ARG, "a mesh holds fewer than 16,777,216 triangles"};
         std::vector<D3> pts(n_points);
         for (int i = 0; i < n_points; i++) pts[i] = D3(points[3 * i], points[3 * i + 1], points[3 * i + 2]);
         std::vector<std::array<int, 3>> t(n_tris);
@@ -3612,9 +3614,9 @@ struct ServerLane {
 // budget for all lanes, at most once per `epoch_steps` steps of the lane's
 // newest cohort, as a new cohort (a batch built from the new worlds only);
 // running worlds are never copied to admit new ones.  A cohort whose finished
-// requests hold three quarters of its bodies is compacted into the next new
-// cohort of its lane (its live worlds read back and packed with the new
-// ones).  Every cohort steps on its own stream in chunks: advance() launches
+// requests hold three quarters of its bodies (compact_pct) is compacted into
+// the next new cohort of its lane (its live worlds read back and packed with
+// the new ones).  Every cohort steps on its own stream in chunks: advance() launches
 // the next chunk on every idle cohort and returns once one has completed.
 struct Server {
     int64_t budget = 0;
@@ -3626,8 +3628,12 @@ struct Server {
     uint64_t next_token = 1;
     int64_t body_steps = 0, reforms = 0;
     double reform_ms = 0;
+    // a cohort whose finished requests hold this percentage of its bodies is
+    // compacted into the lane's next new cohort (CPGPU_SERVE_COMPACT_PCT)
+    int compact_pct = 75;
 
     Server() {
+        compact_pct = std::max(1, std::min(100, env_int("CPGPU_SERVE_COMPACT_PCT", 75)));
         for (size_t k = 0; k <= bounds.size(); k++) lanes.push_back(std::make_unique<ServerLane>());
     }
 
@@ -3692,7 +3698,7 @@ struct Server {
         for (auto it = L.cohorts.begin(); it != L.cohorts.end();) {
             Cohort& C = **it;
             const int64_t live = C.live_bodies(), all = C.all_bodies();
-            if (C.inflight == 0 && live > 0 && 4 * (all - live) >= 3 * all) {
+            if (C.inflight == 0 && live > 0 && 100 * (all - live) >= (int64_t)compact_pct * all) {
                 std::vector<int> idx;
                 std::vector<World*> ws;
                 for (size_t i = 0; i < C.running.size(); i++)

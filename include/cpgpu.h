@@ -169,8 +169,9 @@ int cpgpu_body_union(cpgpu_world* w, const cpgpu_primitive* prims, int n, int mo
                      uint32_t* out_id);
 /* createRigidBody(StaticMeshGeometry(MeshInput{tris, points}), fixed)
  * (PhysicsEngine.cpp:498-512, Geometry.h:52-55): points (xyz) and triangles
- * (three point indices each) in world coordinates; `fixed` must be nonzero
- * (kinematic meshes: CPGPU_ERR_UNSUPPORTED).  Mesh-mesh pairs never collide. */
+ * (three point indices each) in world coordinates, fewer than 2^24
+ * triangles; `fixed` must be nonzero (kinematic meshes:
+ * CPGPU_ERR_UNSUPPORTED).  Mesh-mesh pairs never collide. */
 int cpgpu_body_mesh(cpgpu_world* w, const double* points, int n_points,
                     const int* tris, int n_tris, const cpgpu_material* mat,
                     int fixed, uint32_t* out_id);
