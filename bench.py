@@ -76,6 +76,29 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def shard_seed(seed, rank):
+    """The seed of a rank's own worlds: every rank steps a different draw of
+    the workload (world-sharded, no data-path collective)."""
+    return seed + 1000 * rank
+
+
+def across_ranks(world_size, maxes=(), sums=()):
+    """(max over the ranks of each of `maxes`, sum over the ranks of each of
+    `sums`); on one rank the values themselves.  The process group's backend
+    chooses the tensors' device (NCCL: the GPU, gloo: the host)."""
+    maxes, sums = [float(x) for x in maxes], [float(x) for x in sums]
+    if world_size == 1:
+        return maxes, sums
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    m = torch.tensor(maxes or [0.0], dtype=torch.float64, device=dev)
+    s = torch.tensor(sums or [0.0], dtype=torch.float64, device=dev)
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    dist.all_reduce(s, op=dist.ReduceOp.SUM)
+    return m.tolist()[:len(maxes)], s.tolist()[:len(sums)]
+
+
 def build_worlds(ws_scenes, make_world):
     worlds = []
     for sc in ws_scenes:
@@ -443,7 +466,7 @@ def main():
         return run_secondary(a)
     rank, world_size, local_rank = dist_env()
     t_setup = time.perf_counter()
-    ws_scenes = scenes.batched_worlds(seed=a.seed + 1000 * rank, n_worlds=a.worlds)
+    ws_scenes = scenes.batched_worlds(seed=shard_seed(a.seed, rank), n_worlds=a.worlds)
     params = {"pgs_vel": 10, "pgs_pos": 1, "substeps": 1}
     n_dyn = dynamic_bodies(ws_scenes)
     config = {"workload": WORKLOAD, "worlds": a.worlds, "bodies_per_world": "log-uniform [8, 512]",
@@ -538,19 +561,15 @@ def main():
              "worlds_gaining_energy": int((av[:, 8] > 1e-6 * (np.abs(av[:, 6]) + np.abs(av[:, 7]) + 1.0)).sum()),
              "note": "per world, FP64 sums over the FP32 state after every step (cpgpu_batch_set_audit); "
                      "max_step_energy_gain_J is the largest one-step increase of kinetic + potential energy"}
-    if world_size > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([dev_ms, e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms, e2e_s = float(t[0].item()), float(t[1].item())
-    value = n_dyn * a.steps * world_size / (dev_ms / 1e3)
+    info = batch.info()
+    # whole job: the units every rank processed over the slowest rank's time
+    (dev_ms, e2e_s), (n_dyn_all, contacts_all) = across_ranks(world_size, [dev_ms, e2e_s], [n_dyn, info["contacts"]])
+    value = n_dyn_all * a.steps / (dev_ms / 1e3)
     state_bytes = batch.n_bodies * 64
-    e2e = {"value": n_dyn * a.steps * world_size / e2e_s, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
+    e2e = {"value": n_dyn_all * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
            "d2h_bytes_per_step": state_bytes, "host_buffers": host_desc,
            "call": "cpgpu_batch_write_state + cpgpu_batch_step + cpgpu_batch_read_state per step",
            "steps": "the --steps steps right after the timed ones"}
-    info = batch.info()
 
 
     stage_ms = {k: v / a.steps for k, v in stage_ms.items()}
@@ -606,7 +625,7 @@ def main():
                 "l2": "state larger than L2 (%.0f MB resident)" % (batch_bodies * 600 / 1e6),
                 "contacts": info["contacts"],
                 "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-                "contacts_per_s": info["contacts"] * world_size / (dev_ms / a.steps / 1e3),
+                "contacts_per_s": contacts_all / (dev_ms / a.steps / 1e3),
                 "plain": {"value": plain, "unit": UNIT, "sample_worlds": a.plain_sample,
                           "vs_plain": (value / world_size / plain) if plain else None},
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "audit": audit,
