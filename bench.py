@@ -571,7 +571,6 @@ def main():
            "call": "cpgpu_batch_write_state + cpgpu_batch_step + cpgpu_batch_read_state per step",
            "steps": "the --steps steps right after the timed ones"}
 
-
     stage_ms = {k: v / a.steps for k, v in stage_ms.items()}
     dominant = max(stage_ms, key=stage_ms.get)
     vfe = hull_sizes(ws_scenes)
