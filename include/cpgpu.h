@@ -474,7 +474,6 @@ int cpgpu_world_clone(cpgpu_world* src, cpgpu_world** out);
  * caller then reads as usual.  Each request's result equals stepping its
  * world alone.  The caller must not touch a submitted world until its token
  * is returned by cpgpu_server_poll. */
-typedef struct cpgpu_server cpgpu_server;
 int cpgpu_server_create(int64_t hbm_budget_bytes, int epoch_steps, cpgpu_server** out);
 int cpgpu_server_destroy(cpgpu_server* s);
 int cpgpu_server_submit(cpgpu_server* s, cpgpu_world* w, int steps, uint64_t* token);
