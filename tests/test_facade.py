@@ -15,7 +15,8 @@ REPO = os.path.dirname(HERE)
 def _build(tmp_path, name="facade_box_drop"):
     exe = str(tmp_path / name)
     lib_dir = os.path.dirname(cg.LIB_PATH)
-    cmd = ["g++", "-std=c++17", "-O1", "-I" + os.path.join(REPO, "include"), os.path.join(HERE, "cxx", name + ".cpp"),
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I" + os.path.join(REPO, "include"),
+           os.path.join(HERE, "cxx", name + ".cpp"),
            "-L" + lib_dir, "-lcpgpu", "-Wl,-rpath," + lib_dir, "-o", exe]
     subprocess.run(cmd, check=True, capture_output=True)
     return exe
