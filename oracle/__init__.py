@@ -161,7 +161,9 @@ def capture_mass_properties(scene):
         if kind != "add_mesh":   # meshes have no mass properties
             assert get(r.h, bid, m.ctypes.data, c.ctypes.data, t.ctypes.data) == 0
         rows.append((m[0], c, t))
-    sc_mod.apply(scene, _Hooked(r, after))
+    hooked = _Hooked(r, after)
+    sc_mod.apply(scene, hooked)
+    r.constraint_ids = getattr(hooked, "constraint_ids", [])   # apply() leaves them on the wrapper
     mass = np.array([x[0] for x in rows])
     return mass, np.array([x[1] for x in rows]), np.array([x[2] for x in rows]), r
 
@@ -182,5 +184,7 @@ def port_world_with_mass(scene, mass, com, tensor):
         c = np.ascontiguousarray(com[i], dtype=np.float64)
         t = np.ascontiguousarray(tensor[i], dtype=np.float64)
         assert put(p.h, bid, float(mass[i]), c.ctypes.data, t.ctypes.data) == 0
-    sc_mod.apply(scene, _Hooked(p, after))
+    hooked = _Hooked(p, after)
+    sc_mod.apply(scene, hooked)
+    p.constraint_ids = getattr(hooked, "constraint_ids", [])
     return p

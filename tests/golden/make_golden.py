@@ -122,11 +122,64 @@ def unions():
                         magic_b=c["magic_b"], b1=c["b1"], b2=c["b2"], normal_impulse=c["normal_impulse"])
 
 
+# joint scenes of the joint-kinds fixture: name -> (scene, steps)
+def joint_scenes():
+    return {
+        "distance": (scenes.distance_chain(True), 200),
+        "weld": (scenes.weld_cantilever(True), 200),
+        "slider": (scenes.slider_chain(("slider", "sliding_hinge", "slider", "sliding_hinge")), 200),
+        "cone": (scenes.cone_chain(), 200),
+        "twist": (scenes.twist_chain(), 200),
+        "spring": (scenes.spring_chain(True), 200),
+        "motor_pos": (scenes.motor_chain(3, True), 200),
+        "motor_vel": (scenes.motor_chain(2, False), 200),
+        "piston_vel": (scenes.piston_chain(2, True), 200),
+        "piston_pos": (scenes.piston_chain(3, True), 200),
+    }
+
+
+def joint_kinds():
+    """Distance, weld, slider / sliding-hinge, cone- and twist-limit chains,
+    springs sharing bodies with ball-sockets, motors and pistons in their
+    powered modes (with and without limits): each scene after 200 reference
+    steps, with creation-time mass properties, states, and the motors'
+    angles / pistons' slide positions."""
+    out = {}
+    for name, (sc, steps) in joint_scenes().items():
+        mass, com, tensor, w = oracle.capture_mass_properties(sc)
+        w.step(steps)
+        st = w.state()
+        out[f"{name}_steps"] = steps
+        for k, v in (("mass", mass), ("com_geom", com), ("tensor", tensor), ("com", st["com"]), ("quat", st["quat"]),
+                     ("vel", st["vel"]), ("ang_vel", st["ang_vel"])):
+            out[f"{name}_{k}"] = v
+        if name.startswith("motor") or name.startswith("piston"):
+            get = w.motor_position if name.startswith("motor") else w.piston_position
+            out[f"{name}_positions"] = np.array([get(cid) for cid in w.constraint_ids[1::2]])
+    np.savez_compressed(os.path.join(HERE, "joint_kinds.npz"), **out)
+
+
+def sleeping():
+    """Three box stacks and a ball with sleeping enabled (scenes.sleep_stacks,
+    seed 0) after 400 reference steps: states and which bodies sleep, with
+    creation-time mass properties."""
+    steps = 400
+    sc, _, _ = scenes.sleep_stacks(0)
+    mass, com, tensor, w = oracle.capture_mass_properties(sc)
+    w.step(steps)
+    st = w.state()
+    np.savez_compressed(os.path.join(HERE, "sleep_stacks_seed0.npz"), steps=steps, mass=mass, com_geom=com,
+                        tensor=tensor, com=st["com"], quat=st["quat"], vel=st["vel"], ang_vel=st["ang_vel"],
+                        asleep=w.asleep())
+
+
 def main(names=()):
     if names:
         for n in names:
             globals()[n]()
         return
+    joint_kinds()
+    sleeping()
     unions()
     kinematic()
     capsules()

@@ -764,3 +764,53 @@ def test_restatement_checkpoint_restore_with_motors_and_pistons(oracle_mod):
             sa, sb = a.state(), b.state()
             for k in sa:
                 assert np.array_equal(sa[k], sb[k]), (sc.name, k)
+
+
+def _golden_scenes():
+    """The joint-kinds fixture's scene table, from the script that made it."""
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "make_golden.py")
+    spec = importlib.util.spec_from_file_location("make_golden", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.joint_scenes()
+
+
+@pytest.mark.parametrize("name", ["distance", "weld", "slider", "cone", "twist", "spring", "motor_pos", "motor_vel",
+                                  "piston_vel", "piston_pos"])
+def test_golden_fixture_joint_kinds(oracle_mod, name):
+    """Distance, weld, slider / sliding-hinge, cone- and twist-limit joints,
+    springs, motors and pistons against the committed reference outputs (no
+    reference library needed): the restatement, started from the reference's
+    mass properties, gives the reference's states after 200 steps bit for
+    bit, and the motors' angles and pistons' slide positions."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "joint_kinds.npz"))
+    sc, steps = _golden_scenes()[name]
+    assert int(g[f"{name}_steps"]) == steps
+    p = oracle_mod.port_world_with_mass(sc, g[f"{name}_mass"], g[f"{name}_com_geom"], g[f"{name}_tensor"])
+    p.step(steps)
+    st = p.state()
+    for k in ("com", "quat", "vel", "ang_vel"):
+        assert np.array_equal(st[k], g[f"{name}_{k}"]), k
+    if f"{name}_positions" in g.files:
+        get = p.motor_position if name.startswith("motor") else p.piston_position
+        got = np.array([get(cid) for cid in p.constraint_ids[1::2]])
+        assert np.array_equal(got, g[f"{name}_positions"])
+
+
+def test_golden_fixture_sleeping(oracle_mod):
+    """Sleeping against the committed reference outputs: three box stacks and
+    a ball settle and fall asleep; after 400 steps the restatement's states
+    and sleeping bodies are the reference's, bit for bit."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "sleep_stacks_seed0.npz"))
+    sc, _, _ = scenes.sleep_stacks(0)
+    p = oracle_mod.port_world_with_mass(sc, g["mass"], g["com_geom"], g["tensor"])
+    p.step(int(g["steps"]))
+    st = p.state()
+    for k in ("com", "quat", "vel", "ang_vel"):
+        assert np.array_equal(st[k], g[k]), k
+    assert g["asleep"].sum() >= 9   # the stacks sleep
+    assert np.array_equal(p.asleep(), g["asleep"])
