@@ -173,11 +173,47 @@ def sleeping():
                         asleep=w.asleep())
 
 
+# ray fixture scenes: name -> (scene, steps, ignore lists)
+def ray_scenes():
+    return {
+        "capsules": (scenes.capsule_drop(seed=3, n_side=4, n_layers=2, terrain=True), 90, ((), (1, 5, 9))),
+        "unions": (scenes.union_drop(seed=0, n=10), 90, ((), (2, 4))),
+    }
+
+
+def ray_batch(seed, n):
+    """n rays from above the scenes towards them (unit directions)."""
+    rng = np.random.default_rng(seed)
+    o = rng.uniform([-8, 2, -8], [8, 12, 8], size=(n, 3))
+    d = rng.uniform([-6, -1, -6], [6, 4, 6], size=(n, 3)) - o
+    return o, d / np.linalg.norm(d, axis=1, keepdims=True)
+
+
+def rays():
+    """raycastFirstIntersection on 2,000 rays through settled scenes (every
+    primitive kind on a terrain; bodies of several primitives), with and
+    without an ignore list, after 90 reference steps, with creation-time mass
+    properties."""
+    out = {}
+    o, d = ray_batch(0, 2000)
+    out["origins"], out["dirs"] = o, d
+    for name, (sc, steps, ignores) in ray_scenes().items():
+        mass, com, tensor, w = oracle.capture_mass_properties(sc)
+        w.step(steps)
+        out[f"{name}_mass"], out[f"{name}_com_geom"], out[f"{name}_tensor"] = mass, com, tensor
+        for i, ig in enumerate(ignores):
+            h = w.raycast(o, d, ig)
+            for k in ("body", "pos", "normal", "dist"):
+                out[f"{name}_{i}_{k}"] = h[k]
+    np.savez_compressed(os.path.join(HERE, "rays.npz"), **out)
+
+
 def main(names=()):
     if names:
         for n in names:
             globals()[n]()
         return
+    rays()
     joint_kinds()
     sleeping()
     unions()

@@ -814,3 +814,27 @@ def test_golden_fixture_sleeping(oracle_mod):
         assert np.array_equal(st[k], g[k]), k
     assert g["asleep"].sum() >= 9   # the stacks sleep
     assert np.array_equal(p.asleep(), g["asleep"])
+
+
+def test_golden_fixture_rays(oracle_mod):
+    """raycastFirstIntersection against the committed reference outputs (no
+    reference library needed): 2,000 rays through a settled scene of every
+    primitive kind on a terrain and through bodies of several primitives,
+    with and without an ignore list; hit body, point, normal and distance
+    bit for bit."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "rays.npz"))
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(__file__), "golden",
+                                                                             "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    o, d = g["origins"], g["dirs"]
+    for name, (sc, steps, ignores) in mod.ray_scenes().items():
+        p = oracle_mod.port_world_with_mass(sc, g[f"{name}_mass"], g[f"{name}_com_geom"], g[f"{name}_tensor"])
+        p.step(steps)
+        for i, ig in enumerate(ignores):
+            h = p.raycast(o, d, ig)
+            for k in ("body", "pos", "normal", "dist"):
+                assert np.array_equal(h[k], g[f"{name}_{i}_{k}"]), (name, i, k)
+            assert (h["body"] > 0).sum() > 100
